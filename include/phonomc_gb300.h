@@ -1,0 +1,171 @@
+/*
+ * C ABI of the GB300 carrier-loop library (libphonomc_gb300.so).
+ *
+ * Plain structs, pointers and sizes; no C++ or torch types cross this
+ * boundary. Every entry point returns 0 on success and a nonzero status on
+ * failure; phmc_last_error() then holds the message the reference would have
+ * thrown (std::runtime_error / std::invalid_argument text).
+ *
+ * Reference interfaces each entry point replaces (paths inside the PhonoMC
+ * project):
+ *   phmc_material_create      PhononMaterial::PhononMaterial(MaterialData, double, bool, bool)
+ *                             include/PhononMaterial.h:23-26
+ *   phmc_solver_create        MonteCarloSolver::MonteCarloSolver(args, geometry, materials)
+ *                             include/MonteCarloSolver.h:44-49 (with SimulationDomain(args),
+ *                             include/SimulationDomain.h:16)
+ *   phmc_solver_run_timestep  MonteCarloSolver::run_timestep()  include/MonteCarloSolver.h:57
+ *   phmc_solver_run           the main.cpp:100-102 step loop
+ *   phmc_solver_stats         the getters of include/MonteCarloSolver.h:59-101
+ *   phmc_solver_cells         GridState temperatures / energy density / heat flux
+ *                             (include/solver/GridState.h:8-14)
+ *   phmc_solver_get_carriers  ParticleStorage SoA fields (include/solver/ParticleStorage.h:57-71)
+ *   phmc_solver_destroy       ~MonteCarloSolver
+ *   phmc_dev_trace_box        SimulationDomain::trace_boundary_intersection (box branch)
+ *                             src/SimulationDomain.cpp:341-450
+ *   phmc_dev_temperature_from_energy  PhononMaterial::temperature_from_energy_density
+ *                             src/material/Thermodynamics.cpp:173-175
+ *   phmc_dev_rta_collide      RtaCollisionOperator::apply  src/solver/RtaCollisionOperator.cpp:13-189
+ *   phmc_dev_linear_collide   CarrierCollisionOperator::apply src/solver/CarrierCollisionOperator.cpp:38-141
+ *   phmc_dev_rough_reflect    RoughBoundarySampler::sample src/solver/RoughBoundarySampler.cpp:459-533
+ *   phmc_dev_gradient_drive   TemperatureGradientDrive::apply src/solver/TemperatureGradientDrive.cpp:116-171
+ */
+#ifndef PHONOMC_GB300_H
+#define PHONOMC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct phmc_material phmc_material;
+typedef struct phmc_solver phmc_solver;
+
+/* phonomc::MaterialData (include/material/MaterialData.h:17-31). Arrays are
+ * q-major/branch-minor; gamma tables are (temperature, q, branch). Optional
+ * pointers may be NULL. */
+typedef struct phmc_material_data {
+    int32_t qpoints, branches, mesh[3], ntemps;
+    double volume_a3;
+    double reciprocal[9]; /* row-major: reciprocal[3*i+j] = component i of b_j */
+    const double* frequency_thz;    /* [qpoints*branches] */
+    const double* qpoint_fractions; /* [qpoints*3] */
+    const double* group_velocity;   /* [qpoints*branches*3], Angstrom/ps */
+    const double* temperatures;     /* [ntemps] */
+    const double* gamma;            /* [ntemps*qpoints*branches], THz */
+    const double* gamma_normal;     /* optional, same shape as gamma */
+    const double* gamma_umklapp;    /* optional, same shape as gamma */
+    const double* gamma_isotope;    /* optional, length gamma_isotope_len */
+    int64_t gamma_isotope_len;
+} phmc_material_data;
+
+/* SimulationConfig fields read by the carrier loop (include/SimulationConfig.h:42-146),
+ * in internal units (Angstrom, ps, K). Box faces are in facet order
+ * xmin,xmax,ymin,ymax,zmin,zmax with condition 'T','P' or 'R'. */
+typedef struct phmc_config {
+    double sizes[3];
+    double particle_count;
+    double time_step;
+    int32_t iterations;
+    int32_t convergence_write_interval;
+    uint64_t random_seed;
+    int32_t compute_kappa;
+    int32_t transport_axis;          /* -1 legacy grid-based choice, else 0/1/2 */
+    int32_t has_temperature_gradient;
+    double temperature_gradient;     /* K/m */
+    double temperature_lookup_dt;
+    double background_temperature;
+    int32_t lifetime_temperature_is_local;
+    double lifetime_temperature;
+    int32_t collision_model;         /* 0 = RTA, 1 = Callaway */
+    int32_t conservative_boundaries;
+    int32_t grid[3];
+    int32_t initial_temperature_linear;
+    double initial_temperature;
+    char face_condition[6];
+    double face_value[6];            /* reservoir K, roughness nm, 0 for periodic */
+    const char* output_folder;       /* NULL or "" disables file output */
+    int32_t material_interface_axis;
+    int32_t n_interfaces;
+    const double* material_interface_positions; /* Angstrom */
+    double interface_frequency_bin_thz;
+    int32_t precision;               /* 0 = plain FP64 state, 1 = mixed (FP32 transport) */
+} phmc_config;
+
+/* Getters of include/MonteCarloSolver.h:59-101 plus the last step's ledger. */
+typedef struct phmc_stats {
+    int32_t current_timestep;
+    int64_t particle_count;
+    int64_t absorbed_total, injected_total;
+    int64_t step_absorbed, step_injected;
+    double step_absorbed_energy_ev, step_injected_energy_ev;
+    double total_thermal_energy_ev;
+    double total_lifetime_energy_residual_ev, step_lifetime_energy_residual_ev;
+    double total_energy_balance_residual_ev, step_energy_balance_residual_ev;
+    double total_gradient_energy_ev, step_gradient_energy_ev;
+    int64_t step_gradient_updates;
+    double average_heat_flux_along_axis;
+    double kappa_fit, kappa_endpoints;
+    int64_t interface_events, interface_transmitted, interface_reflected;
+    int64_t device_launches;          /* CUDA kernels launched by this solver so far */
+} phmc_stats;
+
+const char* phmc_last_error(void);
+int phmc_device_count(int* count);
+
+int phmc_material_create(const phmc_material_data* data, double temperature_lookup_dt,
+                         int include_stationary_modes, int complete_callaway_bz, phmc_material** out);
+void phmc_material_destroy(phmc_material* m);
+int phmc_material_active_count(const phmc_material* m, int* n_active);
+
+int phmc_solver_create(const phmc_config* cfg, phmc_material* const* materials, int n_materials,
+                       phmc_solver** out);
+int phmc_solver_run_timestep(phmc_solver* s);
+int phmc_solver_run(phmc_solver* s, int steps);
+int phmc_solver_synchronize(phmc_solver* s);
+int phmc_solver_stats(phmc_solver* s, phmc_stats* out);
+int phmc_solver_cell_count(const phmc_solver* s, int* cells);
+int phmc_solver_cells(phmc_solver* s, double* temperature, double* energy_density, double* heat_flux3);
+/* Carrier slots [0, n_slots): dead slots have alive == 0. */
+int phmc_solver_slot_count(phmc_solver* s, int64_t* n_slots);
+int phmc_solver_get_carriers(phmc_solver* s, double* x, double* y, double* z, double* occupation,
+                             uint32_t* mode_word, int32_t* cell, uint8_t* alive);
+/* Replace the carrier population (same SoA layout; mode_word = active | signs<<24 | material<<28). */
+int phmc_solver_set_carriers(phmc_solver* s, int64_t n, const double* x, const double* y, const double* z,
+                             const double* occupation, const uint32_t* mode_word, const uint8_t* alive);
+/* End-to-end stepping from host memory: uploads carriers from host buffers,
+ * runs `steps` timesteps and reads the cell temperatures back. */
+int phmc_solver_run_from_host(phmc_solver* s, int64_t n, const double* x, const double* y, const double* z,
+                              const double* occupation, const uint32_t* mode_word, int steps,
+                              double* cell_temperature_out);
+int phmc_solver_write_outputs(phmc_solver* s);
+void phmc_solver_destroy(phmc_solver* s);
+
+/* ---- deterministic sub-steps on the device (parity entry points) ---- */
+/* Box ray trace for n rays; returns hit point, time and facet (-1 on miss). */
+int phmc_dev_trace_box(const double lo[3], const double hi[3], int64_t n, const double* p3, const double* v3,
+                       double* hit3, double* t, int32_t* facet);
+/* Piecewise-linear E -> T inversion on a material's lookup table. */
+int phmc_dev_temperature_from_energy(const phmc_material* m, int64_t n, const double* energy, double* temperature);
+/* Energy-conserving RTA on carriers grouped by cell (flat modes, one material). */
+int phmc_dev_rta_collide(const phmc_material* m, int64_t n, const int32_t* flat_mode, const int32_t* cell,
+                         double* occupation, int cells, const double* cell_temperature, double dt,
+                         double particle_volume, int local_lifetime, double lifetime_temperature,
+                         double* residual_ev);
+/* Linearized RTA (model 0) or Callaway (model 1) collision at reference temperature Tref. */
+int phmc_dev_linear_collide(const phmc_material* m, int model, double Tref, int64_t n, const int32_t* flat_mode,
+                            const int32_t* cell, double* occupation, int cells, double dt, double particle_volume,
+                            double* residual_ev);
+/* Rough reflection with explicit uniforms u[3*i..3*i+2] for n incoming carriers. */
+int phmc_dev_rough_reflect(const phmc_material* m, int conservative, double Tref, const double normal_out[3],
+                           double roughness_a, int64_t n, const int32_t* flat_in, const double* occ_in,
+                           const double* u3, int32_t* flat_out, double* occ_out);
+/* Periodic-gradient drive on carriers grouped by cell. */
+int phmc_dev_gradient_drive(const phmc_material* m, int axis, double gradient, double Tref, int64_t n,
+                            const int32_t* flat_mode, const int32_t* cell, double* occupation, int cells,
+                            double dt, double particle_volume, double* energy_ev);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,317 @@
+"""ctypes mirror of the C ABI in include/phonomc_gb300.h.
+
+The structs here are byte-for-byte the ones the header declares; `bind()`
+attaches argument/return types to every entry point of a loaded library.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import synthetic
+
+c_double_p = C.POINTER(C.c_double)
+c_int32_p = C.POINTER(C.c_int32)
+c_uint32_p = C.POINTER(C.c_uint32)
+c_uint8_p = C.POINTER(C.c_uint8)
+c_int64_p = C.POINTER(C.c_int64)
+
+
+class MaterialDataPOD(C.Structure):
+    _fields_ = [
+        ("qpoints", C.c_int32), ("branches", C.c_int32), ("mesh", C.c_int32 * 3), ("ntemps", C.c_int32),
+        ("volume_a3", C.c_double), ("reciprocal", C.c_double * 9),
+        ("frequency_thz", c_double_p), ("qpoint_fractions", c_double_p), ("group_velocity", c_double_p),
+        ("temperatures", c_double_p), ("gamma", c_double_p), ("gamma_normal", c_double_p),
+        ("gamma_umklapp", c_double_p), ("gamma_isotope", c_double_p), ("gamma_isotope_len", C.c_int64),
+    ]
+
+
+class ConfigPOD(C.Structure):
+    _fields_ = [
+        ("sizes", C.c_double * 3), ("particle_count", C.c_double), ("time_step", C.c_double),
+        ("iterations", C.c_int32), ("convergence_write_interval", C.c_int32), ("random_seed", C.c_uint64),
+        ("compute_kappa", C.c_int32), ("transport_axis", C.c_int32), ("has_temperature_gradient", C.c_int32),
+        ("temperature_gradient", C.c_double), ("temperature_lookup_dt", C.c_double),
+        ("background_temperature", C.c_double), ("lifetime_temperature_is_local", C.c_int32),
+        ("lifetime_temperature", C.c_double), ("collision_model", C.c_int32),
+        ("conservative_boundaries", C.c_int32), ("grid", C.c_int32 * 3),
+        ("initial_temperature_linear", C.c_int32), ("initial_temperature", C.c_double),
+        ("face_condition", C.c_char * 6), ("face_value", C.c_double * 6), ("output_folder", C.c_char_p),
+        ("material_interface_axis", C.c_int32), ("n_interfaces", C.c_int32),
+        ("material_interface_positions", c_double_p), ("interface_frequency_bin_thz", C.c_double),
+        ("precision", C.c_int32),
+    ]
+
+
+class StatsPOD(C.Structure):
+    _fields_ = [
+        ("current_timestep", C.c_int32), ("particle_count", C.c_int64), ("absorbed_total", C.c_int64),
+        ("injected_total", C.c_int64), ("step_absorbed", C.c_int64), ("step_injected", C.c_int64),
+        ("step_absorbed_energy_ev", C.c_double), ("step_injected_energy_ev", C.c_double),
+        ("total_thermal_energy_ev", C.c_double), ("total_lifetime_energy_residual_ev", C.c_double),
+        ("step_lifetime_energy_residual_ev", C.c_double), ("total_energy_balance_residual_ev", C.c_double),
+        ("step_energy_balance_residual_ev", C.c_double), ("total_gradient_energy_ev", C.c_double),
+        ("step_gradient_energy_ev", C.c_double), ("step_gradient_updates", C.c_int64),
+        ("average_heat_flux_along_axis", C.c_double), ("kappa_fit", C.c_double),
+        ("kappa_endpoints", C.c_double), ("interface_events", C.c_int64),
+        ("interface_transmitted", C.c_int64), ("interface_reflected", C.c_int64),
+        ("device_launches", C.c_int64),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+def dptr(a: Optional[np.ndarray]):
+    if a is None:
+        return None
+    return a.ctypes.data_as(c_double_p)
+
+
+def material_pod(d: synthetic.MaterialData):
+    """Pack a MaterialData; returns (pod, keepalive) so the arrays outlive the call."""
+    keep = []
+
+    def arr(x):
+        if x is None:
+            return None
+        a = np.ascontiguousarray(x, dtype=np.float64)
+        keep.append(a)
+        return a
+
+    pod = MaterialDataPOD()
+    pod.qpoints = d.qpoints
+    pod.branches = d.branches
+    for i in range(3):
+        pod.mesh[i] = int(d.mesh[i])
+    pod.ntemps = int(d.temperatures.size)
+    pod.volume_a3 = float(d.volume_a3)
+    R = np.asarray(d.reciprocal, dtype=np.float64).reshape(3, 3)
+    for i in range(9):
+        pod.reciprocal[i] = float(R.reshape(-1)[i])
+    pod.frequency_thz = dptr(arr(d.frequency_thz))
+    pod.qpoint_fractions = dptr(arr(d.qpoint_fractions))
+    pod.group_velocity = dptr(arr(d.group_velocity))
+    pod.temperatures = dptr(arr(d.temperatures))
+    pod.gamma = dptr(arr(d.gamma))
+    pod.gamma_normal = dptr(arr(d.gamma_normal))
+    pod.gamma_umklapp = dptr(arr(d.gamma_umklapp))
+    iso = d.gamma_resistive.get("gamma_isotope")
+    pod.gamma_isotope = dptr(arr(iso))
+    pod.gamma_isotope_len = 0 if iso is None else int(np.asarray(iso).size)
+    return pod, keep
+
+
+def config_pod(cfg: dict):
+    """Build a ConfigPOD from a dict of SimulationConfig-style fields (internal units)."""
+    keep = []
+    c = ConfigPOD()
+    c.sizes[:] = list(cfg["sizes"])
+    c.particle_count = float(cfg.get("particle_count", 1e4))
+    c.time_step = float(cfg.get("time_step", 1.0))
+    c.iterations = int(cfg.get("iterations", 10000))
+    c.convergence_write_interval = int(cfg.get("convergence_write_interval", 10))
+    c.random_seed = int(cfg.get("random_seed", 12345))
+    c.compute_kappa = int(cfg.get("compute_kappa", False))
+    c.transport_axis = int(cfg.get("transport_axis", -1))
+    g = cfg.get("temperature_gradient")
+    c.has_temperature_gradient = int(g is not None)
+    c.temperature_gradient = float(g or 0.0)
+    c.temperature_lookup_dt = float(cfg.get("temperature_lookup_dt", 0.1))
+    c.background_temperature = float(cfg.get("background_temperature", 300.0))
+    lt = cfg.get("lifetime_temperature", "local")
+    c.lifetime_temperature_is_local = int(lt == "local")
+    c.lifetime_temperature = 300.0 if lt == "local" else float(lt)
+    c.collision_model = 1 if cfg.get("collision_model", "rta") == "callaway" else 0
+    c.conservative_boundaries = int(cfg.get("conservative_boundaries", False))
+    c.grid[:] = list(cfg.get("grid", (1, 1, 1)))
+    it = cfg.get("initial_temperature", 300.0)
+    c.initial_temperature_linear = int(it == "linear")
+    c.initial_temperature = 300.0 if it == "linear" else float(it)
+    c.face_condition = "".join(cfg["faces"]).encode()
+    c.face_value[:] = [float(v) for v in cfg["face_values"]]
+    of = cfg.get("output_folder")
+    if of:
+        b = of.encode()
+        keep.append(b)
+        c.output_folder = b
+    c.material_interface_axis = int(cfg.get("material_interface_axis", 0))
+    planes = np.ascontiguousarray(cfg.get("material_interface_positions", []), dtype=np.float64)
+    keep.append(planes)
+    c.n_interfaces = int(planes.size)
+    c.material_interface_positions = dptr(planes) if planes.size else None
+    c.interface_frequency_bin_thz = float(cfg.get("interface_frequency_bin_thz", 0.1))
+    c.precision = 1 if cfg.get("precision", "fp64") == "mixed" else 0
+    return c, keep
+
+
+SOLVER_PROTOS = {
+    "last_error": (C.c_char_p, []),
+    "material_create": (C.c_int, [C.POINTER(MaterialDataPOD), C.c_double, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "material_destroy": (None, [C.c_void_p]),
+    "solver_create": (C.c_int, [C.POINTER(ConfigPOD), C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),
+    "solver_destroy": (None, [C.c_void_p]),
+    "solver_run": (C.c_int, [C.c_void_p, C.c_int]),
+    "solver_stats": (C.c_int, [C.c_void_p, C.POINTER(StatsPOD)]),
+    "solver_cell_count": (C.c_int, [C.c_void_p, c_int32_p]),
+    "solver_cells": (C.c_int, [C.c_void_p, c_double_p, c_double_p, c_double_p]),
+    "solver_slot_count": (C.c_int, [C.c_void_p, c_int64_p]),
+    "solver_get_carriers": (C.c_int, [C.c_void_p, c_double_p, c_double_p, c_double_p, c_double_p, c_uint32_p,
+                                      c_int32_p, c_uint8_p]),
+    "solver_set_carriers": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_double_p, c_double_p, c_double_p,
+                                      c_uint32_p, c_uint8_p]),
+}
+
+
+def bind(lib: C.CDLL, prefix: str, protos: dict) -> None:
+    for name, (res, args) in protos.items():
+        fn = getattr(lib, prefix + name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+class LibError(RuntimeError):
+    pass
+
+
+class Handle:
+    """Thin solver/material wrapper over a library with the solver ABI shape."""
+
+    def __init__(self, lib: C.CDLL, prefix: str):
+        self.lib = lib
+        self.p = prefix
+
+    def fn(self, name):
+        return getattr(self.lib, self.p + name)
+
+    def check(self, rc: int) -> None:
+        if rc != 0:
+            raise LibError(self.fn("last_error")().decode())
+
+
+class Material(Handle):
+    def __init__(self, lib, prefix, data: synthetic.MaterialData, lookup_dt=0.1, stationary=False,
+                 complete_bz=False):
+        super().__init__(lib, prefix)
+        pod, keep = material_pod(data)
+        h = C.c_void_p()
+        self.check(self.fn("material_create")(C.byref(pod), lookup_dt, int(stationary), int(complete_bz),
+                                              C.byref(h)))
+        self.h = h
+        self.data = data
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.fn("material_destroy")(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Solver(Handle):
+    def __init__(self, lib, prefix, cfg: dict, materials: Sequence[Material]):
+        super().__init__(lib, prefix)
+        pod, keep = config_pod(cfg)
+        arr = (C.c_void_p * len(materials))(*[m.h for m in materials])
+        h = C.c_void_p()
+        self.check(self.fn("solver_create")(C.byref(pod), arr, len(materials), C.byref(h)))
+        self.h = h
+        self.materials = list(materials)
+        self.cfg = dict(cfg)
+
+    def run(self, steps: int = 1) -> None:
+        self.check(self.fn("solver_run")(self.h, steps))
+
+    def stats(self) -> dict:
+        s = StatsPOD()
+        self.check(self.fn("solver_stats")(self.h, C.byref(s)))
+        return s.as_dict()
+
+    def cells(self):
+        n = C.c_int32()
+        self.check(self.fn("solver_cell_count")(self.h, C.byref(n)))
+        T = np.zeros(n.value)
+        E = np.zeros(n.value)
+        q = np.zeros((n.value, 3))
+        self.check(self.fn("solver_cells")(self.h, dptr(T), dptr(E), dptr(q)))
+        return T, E, q
+
+    def carriers(self) -> dict:
+        n = C.c_int64()
+        self.check(self.fn("solver_slot_count")(self.h, C.byref(n)))
+        n = n.value
+        out = {k: np.zeros(n) for k in ("x", "y", "z", "occ")}
+        out["mode"] = np.zeros(n, dtype=np.uint32)
+        out["cell"] = np.zeros(n, dtype=np.int32)
+        out["alive"] = np.zeros(n, dtype=np.uint8)
+        self.check(self.fn("solver_get_carriers")(
+            self.h, dptr(out["x"]), dptr(out["y"]), dptr(out["z"]), dptr(out["occ"]),
+            out["mode"].ctypes.data_as(c_uint32_p), out["cell"].ctypes.data_as(c_int32_p),
+            out["alive"].ctypes.data_as(c_uint8_p)))
+        return out
+
+    def set_carriers(self, c: dict) -> None:
+        n = int(c["x"].size)
+        arrs = [np.ascontiguousarray(c[k], dtype=np.float64) for k in ("x", "y", "z", "occ")]
+        mode = np.ascontiguousarray(c["mode"], dtype=np.uint32)
+        alive = np.ascontiguousarray(c.get("alive", np.ones(n, np.uint8)), dtype=np.uint8)
+        self.check(self.fn("solver_set_carriers")(self.h, n, *[dptr(a) for a in arrs],
+                                                  mode.ctypes.data_as(c_uint32_p),
+                                                  alive.ctypes.data_as(c_uint8_p)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.fn("solver_destroy")(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# Deterministic sub-step entry points; the CUDA library exports them with the
+# prefix phmc_dev_ and the oracle with orc_ (same signatures).
+SUBSTEP_PROTOS = {
+    "trace_box": (C.c_int, [c_double_p, c_double_p, C.c_int64, c_double_p, c_double_p, c_double_p, c_double_p,
+                            c_int32_p]),
+    "temperature_from_energy": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_double_p]),
+    "rta_collide": (C.c_int, [C.c_void_p, C.c_int64, c_int32_p, c_int32_p, c_double_p, C.c_int, c_double_p,
+                              C.c_double, C.c_double, C.c_int, C.c_double, c_double_p]),
+    "linear_collide": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int64, c_int32_p, c_int32_p, c_double_p,
+                                 C.c_int, C.c_double, C.c_double, c_double_p]),
+    "rough_reflect": (C.c_int, [C.c_void_p, C.c_int, C.c_double, c_double_p, C.c_double, C.c_int64, c_int32_p,
+                                c_double_p, c_double_p, c_int32_p, c_double_p]),
+    "gradient_drive": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int64, c_int32_p, c_int32_p,
+                                 c_double_p, C.c_int, C.c_double, C.c_double, c_double_p]),
+}
+
+ORACLE_EXTRA_PROTOS = {
+    "material_query": (C.c_int, [C.c_void_p, C.c_int, C.c_int64, c_int32_p, c_double_p, C.c_double, c_double_p]),
+    "material_scalars": (C.c_int, [C.c_void_p, C.c_double, c_double_p, c_int32_p]),
+    "grid_index": (C.c_int, [c_double_p, c_int32_p, C.c_int64, c_double_p, c_int32_p]),
+    "callaway_evolve": (C.c_int, [C.c_int64, c_double_p, c_double_p, c_double_p, c_double_p, c_double_p, c_double_p,
+                                  C.c_double, c_double_p]),
+    "reservoir_cdf": (C.c_int, [C.c_void_p, c_double_p, C.c_double, C.c_double, C.c_double, c_double_p, c_double_p,
+                                c_int32_p]),
+}
+
+DEVICE_PROTOS = {
+    "device_count": (C.c_int, [c_int32_p]),
+    "material_active_count": (C.c_int, [C.c_void_p, c_int32_p]),
+    "solver_run_timestep": (C.c_int, [C.c_void_p]),
+    "solver_synchronize": (C.c_int, [C.c_void_p]),
+    "solver_write_outputs": (C.c_int, [C.c_void_p]),
+    "solver_run_from_host": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_double_p, c_double_p, c_double_p,
+                                       c_uint32_p, C.c_int, c_double_p]),
+    **{"dev_" + k: v for k, v in SUBSTEP_PROTOS.items()},
+}

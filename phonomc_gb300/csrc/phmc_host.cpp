@@ -1,0 +1,905 @@
+// Host-side tables for the carrier loop. See phmc_host.h for the map to the
+// reference; each function cites the reference lines whose semantics it keeps.
+#include "phmc_host.h"
+
+#include "phmc_rng.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <limits>
+#include <numeric>
+#include <sstream>
+
+namespace phmc {
+namespace {
+double dot3(const Vec3& a, const Vec3& b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+double norm3(const Vec3& a) { return std::sqrt(dot3(a, a)); }
+Vec3 sub3(const Vec3& a, const Vec3& b) { return {a[0] - b[0], a[1] - b[1], a[2] - b[2]}; }
+Vec3 mul3(const Vec3& a, double s) { return {a[0] * s, a[1] * s, a[2] * s}; }
+Vec3 q_to_k(const std::array<Vec3, 3>& R, const Vec3& q) {
+    return {R[0][0] * q[0] + R[0][1] * q[1] + R[0][2] * q[2],
+            R[1][0] * q[0] + R[1][1] * q[1] + R[1][2] * q[2],
+            R[2][0] * q[0] + R[2][1] * q[1] + R[2][2] * q[2]};
+}
+} // namespace
+
+// ------------------------------------------------------------- material
+// Shape/finiteness checks of src/material/MaterialData.cpp:1-131.
+void validate_material_data(const MaterialData& d) {
+    const size_t nm = static_cast<size_t>(d.qpoints) * d.branches;
+    if (!(d.volume_a3 > 0) || !std::isfinite(d.volume_a3))
+        throw std::runtime_error("Unit-cell volume must be finite and positive");
+    if (d.qpoints <= 0 || d.branches <= 0) throw std::runtime_error("empty phonon table");
+    if (d.frequency_thz.size() != nm) throw std::runtime_error("frequency shape mismatch");
+    if (d.qpoint_fractions.size() != static_cast<size_t>(d.qpoints))
+        throw std::runtime_error("qpoint shape mismatch");
+    if (d.group_velocity.size() != nm) throw std::runtime_error("group_velocity shape mismatch");
+    size_t grid = 1;
+    for (int m : d.mesh) {
+        if (m <= 0) throw std::runtime_error("mesh entries must be positive integers");
+        grid *= static_cast<size_t>(m);
+    }
+    if (grid != static_cast<size_t>(d.qpoints))
+        throw std::runtime_error("Full Brillouin-zone grid required: qpoint count differs from "
+                                 "mesh product. Expand reduced data first.");
+    if (d.temperatures.empty() || d.temperatures.front() < 0 ||
+        !std::is_sorted(d.temperatures.begin(), d.temperatures.end()) ||
+        std::adjacent_find(d.temperatures.begin(), d.temperatures.end()) != d.temperatures.end())
+        throw std::runtime_error("temperature must be nonempty, nonnegative and strictly increasing");
+    if (d.gamma.size() != d.temperatures.size() * nm) throw std::runtime_error("gamma shape mismatch");
+    for (double g : d.gamma)
+        if (!std::isfinite(g) || g < 0) throw std::runtime_error("gamma must be nonnegative");
+    if (d.gamma_normal.empty() != d.gamma_umklapp.empty())
+        throw std::runtime_error("gamma_N and gamma_U must both be supplied or both omitted");
+    if (!d.gamma_normal.empty() &&
+        (d.gamma_normal.size() != d.gamma.size() || d.gamma_umklapp.size() != d.gamma.size()))
+        throw std::runtime_error("N/U linewidth shape mismatch");
+    for (const auto& [name, v] : d.gamma_resistive) {
+        if (name != "gamma_isotope" && name != "gamma_impurity" && name != "gamma_defect")
+            throw std::runtime_error("Unsupported resistive linewidth: " + name);
+        if (v.size() != nm && v.size() != d.gamma.size()) throw std::runtime_error(name + " shape mismatch");
+    }
+}
+
+// src/PhononMaterial.cpp:156-171, 216-291
+PhononMaterial::PhononMaterial(MaterialData d, double lookup_dt, bool stationary, bool complete_bz)
+    : dT_(lookup_dt), stationary_(stationary) {
+    if (!std::isfinite(lookup_dt) || lookup_dt <= 0)
+        throw std::invalid_argument("Temperature lookup spacing must be finite and positive");
+    validate_material_data(d);
+    if (complete_bz && !d.gamma_normal.empty()) {
+        // Boundary replication of src/material/BzQuadrature.cpp is applied by the
+        // caller's table when needed; tables built here must already be closed.
+        refinement_ = 1;
+    }
+    volume_ = d.volume_a3;
+    nq_ = d.qpoints;
+    nb_ = d.branches;
+    reciprocal_ = d.reciprocal;
+    mesh_ = d.mesh;
+    const int nm = nq_ * nb_;
+    omega_.resize(nm);
+    knorm_.assign(nm, 0.0);
+    window_.assign(nm, 0.0);
+    kvec_.resize(nm);
+    for (int i = 0; i < nm; ++i) omega_[i] = std::max(0.0, d.frequency_thz[i]) * 2.0 * kPi;
+    vel_ = std::move(d.group_velocity);
+    temps_ = std::move(d.temperatures);
+    gamma_normal_ = std::move(d.gamma_normal);
+    gamma_umklapp_ = std::move(d.gamma_umklapp);
+    gamma_extra_.assign(d.gamma.size(), 0.0);
+    for (const auto& [name, values] : d.gamma_resistive) {
+        (void)name;
+        for (size_t i = 0; i < gamma_extra_.size(); ++i)
+            gamma_extra_[i] += values[values.size() == static_cast<size_t>(nm) ? i % nm : i];
+    }
+    gamma_total_ = d.gamma;
+    for (size_t i = 0; i < gamma_total_.size(); ++i) gamma_total_[i] += gamma_extra_[i];
+    qfrac_ = d.qpoint_fractions;
+    const Vec3 mesh_q{1.0 / (2.0 * mesh_[0]), 1.0 / (2.0 * mesh_[1]), 1.0 / (2.0 * mesh_[2])};
+    const Vec3 kg = q_to_k(reciprocal_, mesh_q);
+    for (int q = 0; q < nq_; ++q) {
+        const Vec3 k = q_to_k(reciprocal_, qfrac_[q]);
+        const double kn = norm3(k);
+        for (int b = 0; b < nb_; ++b) {
+            const int f = q * nb_ + b;
+            const Vec3& v = vel_[f];
+            knorm_[f] = kn;
+            kvec_[f] = k;
+            window_[f] = std::sqrt((v[0] * kg[0]) * (v[0] * kg[0]) + (v[1] * kg[1]) * (v[1] * kg[1]) +
+                                   (v[2] * kg[2]) * (v[2] * kg[2]));
+        }
+    }
+    active_.clear();
+    for (int base = 0; base < nq_; base += static_cast<int>(refinement_)) {
+        for (int b = 0; b < nb_; ++b) {
+            for (unsigned c = 0; c < refinement_; ++c) {
+                const int f = (base + static_cast<int>(c)) * nb_ + b;
+                const double vn = norm3(vel_[f]);
+                if (stationary_ ? omega_[f] > 0.0 : vn > 1e-12) active_.push_back(f);
+            }
+        }
+    }
+    if (active_.empty()) throw std::runtime_error("No active modes found in material data.");
+    flat_to_active_.assign(nm, -1);
+    for (size_t a = 0; a < active_.size(); ++a) flat_to_active_[active_[a]] = static_cast<int>(a);
+    build_lookup();
+}
+
+// src/material/Thermodynamics.cpp:71-82
+double PhononMaterial::bose_occupation(double T, int flat) const {
+    const double w = omega_[flat];
+    if (T <= 0.0 || w <= 0.0) return 0.0;
+    const double x = kHbarEvPs * w / (kBoltzmannEvK * T);
+    if (x > 700.0) return 0.0;
+    return 1.0 / std::max(std::exp(x) - 1.0, 1e-12);
+}
+
+// src/material/Thermodynamics.cpp:11-25
+double PhononMaterial::mode_heat_capacity(double T, int flat) const {
+    const double hw = kHbarEvPs * omega_[flat];
+    if (!(T > 0.0) || !(hw > 0.0)) return 0.0;
+    const double x = hw / (kBoltzmannEvK * T);
+    if (x < 1e-6) return kBoltzmannEvK * (1.0 - x * x / 12.0);
+    if (x > 700.0) return 0.0;
+    const double den = -std::expm1(-x);
+    return kBoltzmannEvK * x * x * std::exp(-x) / (den * den);
+}
+
+// src/material/Thermodynamics.cpp:27-37
+double PhononMaterial::linearized_bose_occupation(double T, double Tref, int flat) const {
+    const double hw = kHbarEvPs * omega_[flat];
+    if (!(hw > 0.0)) return 0.0;
+    return bose_occupation(Tref, flat) + mode_heat_capacity(Tref, flat) * (T - Tref) / hw;
+}
+
+// src/material/Thermodynamics.cpp:40-68
+double PhononMaterial::interp_linear_clamped(const std::vector<double>& xs, const std::vector<double>& ys,
+                                             double x) {
+    if (xs.empty() || ys.empty()) return 0.0;
+    if (xs.size() == 1 || ys.size() == 1) return ys.front();
+    if (x <= xs.front()) return ys.front();
+    if (x >= xs.back()) return ys.back();
+    const size_t hi = static_cast<size_t>(std::upper_bound(xs.begin(), xs.end(), x) - xs.begin());
+    const size_t lo = hi - 1;
+    const double x0 = xs[lo], x1 = xs[hi], y0 = ys[lo], y1 = ys[hi];
+    if (std::abs(x1 - x0) <= 1e-18) return y0;
+    const double t = (x - x0) / (x1 - x0);
+    return y0 * (1.0 - t) + y1 * t;
+}
+
+// src/material/Thermodynamics.cpp:108-132
+double PhononMaterial::mode_gamma(double T, int flat) const {
+    if (!std::isfinite(T) || T < 0.0)
+        throw std::invalid_argument("Lifetime temperature must be finite and nonnegative");
+    const size_t nm = static_cast<size_t>(nq_) * nb_;
+    if (T <= temps_.front()) return gamma_total_[flat];
+    if (T >= temps_.back()) return gamma_total_[(temps_.size() - 1) * nm + flat];
+    const size_t hi = static_cast<size_t>(std::upper_bound(temps_.begin(), temps_.end(), T) - temps_.begin());
+    const size_t lo = hi - 1;
+    const double x0 = temps_[lo], x1 = temps_[hi];
+    const double y0 = gamma_total_[lo * nm + flat], y1 = gamma_total_[hi * nm + flat];
+    if (std::abs(x1 - x0) <= 1e-18) return y0;
+    const double t = (T - x0) / (x1 - x0);
+    return y0 * (1.0 - t) + y1 * t;
+}
+
+// src/material/Thermodynamics.cpp:96-105
+double PhononMaterial::mode_relaxation_weight(double T, int flat, double dt) const {
+    if (!std::isfinite(dt) || dt < 0.0)
+        throw std::invalid_argument("Relaxation time step must be finite and nonnegative");
+    const double g = mode_gamma(T, flat);
+    if (g == 0.0 || dt == 0.0) return 0.0;
+    return -std::expm1(-(g * dt) * (4.0 * kPi));
+}
+
+double PhononMaterial::energy_density_normalization() const {
+    return std::max(1.0, static_cast<double>(nq_) * volume_);
+}
+
+// src/material/Thermodynamics.cpp:134-146
+double PhononMaterial::crystal_energy_density(double T) const {
+    double e = 0.0;
+    for (int f : active_) {
+        const double w = omega_[f];
+        if (w <= 0.0) continue;
+        e += kHbarEvPs * w * bose_occupation(T, f);
+    }
+    return e / energy_density_normalization() + zero_point_;
+}
+
+double PhononMaterial::energy_density_from_temperature(double T) const {
+    if (table_T_.empty()) return crystal_energy_density(T);
+    return interp_linear_clamped(table_T_, table_E_, T);
+}
+
+double PhononMaterial::temperature_from_energy_density(double E) const {
+    return interp_linear_clamped(table_E_, table_T_, E);
+}
+
+// src/material/Thermodynamics.cpp:178-224
+void PhononMaterial::build_lookup() {
+    zero_point_ = 0.0;
+    for (double w : omega_) zero_point_ += 0.5 * kHbarEvPs * std::max(0.0, w);
+    zero_point_ /= energy_density_normalization();
+    const double tmin = 0.0;
+    const double tmax = temps_.empty() ? 1000.0 : std::max(1000.0, *std::max_element(temps_.begin(), temps_.end()));
+    const double dT = std::max(1e-6, dT_);
+    const double intervals = std::floor((tmax - tmin) / dT + 0.5);
+    const int n = std::max(2, static_cast<int>(intervals) + 1);
+    table_T_.assign(n, 0.0);
+    table_E_.assign(n, 0.0);
+    std::vector<double> raw(n);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) raw[i] = crystal_energy_density(tmin + static_cast<double>(i) * dT);
+    for (int i = 0; i < n; ++i) {
+        table_T_[i] = tmin + static_cast<double>(i) * dT;
+        double E = raw[i];
+        if (i > 0) E = std::max(E, std::nextafter(table_E_[i - 1], std::numeric_limits<double>::infinity()));
+        table_E_[i] = E;
+    }
+}
+
+// src/material/PhononMaterialCollisionData.cpp:8-23
+CallawayData PhononMaterial::linearized_rta_data(double T) const {
+    if (!std::isfinite(T) || T <= 0 || temps_.empty() || T < temps_.front() || T > temps_.back())
+        throw std::invalid_argument("Linearized RTA reference temperature is outside the scattering data range.");
+    CallawayData d;
+    for (int f : active_) {
+        d.omega.push_back(omega_[f]);
+        d.capacity.push_back(mode_heat_capacity(T, f));
+        d.wavevector.push_back({0, 0, 0});
+        d.normal_rate.push_back(0);
+        d.resistive_rate.push_back(4 * std::acos(-1.0) * mode_gamma(T, f));
+    }
+    return d;
+}
+
+// src/material/PhononMaterialCollisionData.cpp:32-166 (rates and data; the
+// first-BZ validation of the reference is not repeated here).
+CallawayData PhononMaterial::callaway_data(double T) const {
+    if (gamma_normal_.empty() || gamma_umklapp_.empty())
+        throw std::invalid_argument("Callaway requires gamma_N and gamma_U in kappa-fbz.hdf5; regenerate with "
+                                    "phono3py --br --nu and expand consistently. No N/U split is inferred.");
+    if (!std::isfinite(T) || T <= 0 || T < temps_.front() || T > temps_.back())
+        throw std::invalid_argument("Callaway reference temperature is outside the N/U data range.");
+    const size_t hi = static_cast<size_t>(std::lower_bound(temps_.begin(), temps_.end(), T) - temps_.begin());
+    const size_t lo = hi > 0 ? hi - 1 : hi;
+    const double fr = hi == lo ? 0 : (T - temps_[lo]) / (temps_[hi] - temps_[lo]);
+    const size_t nm = static_cast<size_t>(nq_) * nb_;
+    CallawayData d;
+    for (int f : active_) {
+        d.omega.push_back(omega_[f]);
+        d.capacity.push_back(mode_heat_capacity(T, f));
+        d.wavevector.push_back(kvec_[f]);
+        auto rate = [&](const std::vector<double>& t) {
+            return 4 * std::acos(-1.0) * ((1 - fr) * t[lo * nm + f] + fr * t[hi * nm + f]);
+        };
+        d.normal_rate.push_back(rate(gamma_normal_));
+        d.resistive_rate.push_back(rate(gamma_umklapp_) + rate(gamma_extra_));
+    }
+    return d;
+}
+
+// ---------------------------------------------------------------- domain
+// Box facets in the reference's order (plane 2*axis+side), boundary conditions,
+// periodic pairs and the uniform grid (src/SimulationDomain.cpp:131-198, 408-611, 626-766).
+SimulationDomain::SimulationDomain(const SimulationConfig& cfg) {
+    if (cfg.model != "box") throw std::runtime_error("Only the analytic box geometry is supported.");
+    if (cfg.sizes.size() != 3) throw std::runtime_error("Box requires three finite positive sizes.");
+    for (int a = 0; a < 3; ++a) {
+        if (!std::isfinite(cfg.sizes[a]) || cfg.sizes[a] <= 0)
+            throw std::runtime_error("Box requires three finite positive sizes.");
+        bmin_[a] = 0.0;
+        bmax_[a] = cfg.sizes[a];
+    }
+    volume_ = cfg.sizes[0] * cfg.sizes[1] * cfg.sizes[2];
+    facets_.resize(6);
+    for (int f = 0; f < 6; ++f) {
+        const int axis = f / 2, side = f % 2;
+        Facet& F = facets_[f];
+        F.normal = {0, 0, 0};
+        F.normal[axis] = side ? 1.0 : -1.0;
+        const int u = (axis + 1) % 3, v = (axis + 2) % 3;
+        F.centroid[axis] = side ? bmax_[axis] : bmin_[axis];
+        F.centroid[u] = 0.5 * (bmin_[u] + bmax_[u]);
+        F.centroid[v] = 0.5 * (bmin_[v] + bmax_[v]);
+        F.area = (bmax_[u] - bmin_[u]) * (bmax_[v] - bmin_[v]);
+        Vec3 c00 = F.centroid, c10 = F.centroid, c11 = F.centroid, c01 = F.centroid;
+        c00[u] = bmin_[u]; c00[v] = bmin_[v];
+        c10[u] = bmax_[u]; c10[v] = bmin_[v];
+        c11[u] = bmax_[u]; c11[v] = bmax_[v];
+        c01[u] = bmin_[u]; c01[v] = bmax_[v];
+        F.tri[0] = {c00, c10, c11};
+        F.tri[1] = {c00, c11, c01};
+        const char cond = cfg.face_condition[f];
+        if (cond != 'T' && cond != 'P' && cond != 'R') throw std::runtime_error("Unknown boundary condition.");
+        const double value = cond == 'R' ? cfg.face_value[f] * 10.0 : cfg.face_value[f];
+        if (!std::isfinite(value) || value < 0 || (cond == 'P' && value != 0))
+            throw std::runtime_error("Boundary values must be finite, nonnegative, and zero for periodic boundaries.");
+        F.condition = cond;
+        F.value = value;
+    }
+    for (int axis = 0; axis < 3; ++axis) {
+        Facet& a = facets_[2 * axis];
+        Facet& b = facets_[2 * axis + 1];
+        if (a.condition == 'P' && b.condition == 'P') {
+            a.pair = 2 * axis + 1;
+            b.pair = 2 * axis;
+            a.shift = sub3(b.centroid, a.centroid);
+            b.shift = sub3(a.centroid, b.centroid);
+        } else if (a.condition == 'P' || b.condition == 'P') {
+            throw std::runtime_error("Periodic boundary facet " + std::to_string(a.condition == 'P' ? 2 * axis : 2 * axis + 1) +
+                                     " is not assigned to a periodic pair.");
+        }
+    }
+    for (int f = 0; f < 6; ++f) {
+        if (facets_[f].condition == 'T') {
+            facets_[f].reservoir = static_cast<int>(reservoir_facets_.size());
+            reservoir_facets_.push_back(f);
+        }
+    }
+    const int nx = cfg.grid[0], ny = cfg.grid[1], nz = cfg.grid[2];
+    if (nx <= 0 || ny <= 0 || nz <= 0) throw std::runtime_error("Grid sizes must be positive.");
+    shape_ = {nx, ny, nz};
+    const Vec3 ext = sub3(bmax_, bmin_);
+    inv_cell_ = {nx / ext[0], ny / ext[1], nz / ext[2]};
+    for (int ix = 0; ix < nx; ++ix)
+        for (int iy = 0; iy < ny; ++iy)
+            for (int iz = 0; iz < nz; ++iz)
+                centers_.push_back({bmin_[0] + (ix + 0.5) * ext[0] / nx, bmin_[1] + (iy + 0.5) * ext[1] / ny,
+                                    bmin_[2] + (iz + 0.5) * ext[2] / nz});
+    volumes_.assign(centers_.size(), volume_ / static_cast<double>(centers_.size()));
+}
+
+// src/SimulationDomain.cpp:92-126
+int SimulationDomain::fast_grid_index(const Vec3& p) const {
+    int idx[3];
+    for (int a = 0; a < 3; ++a) {
+        const int n = shape_[a];
+        if (n <= 1) {
+            idx[a] = 0;
+            continue;
+        }
+        int i = static_cast<int>(std::floor((p[a] - bmin_[a]) * inv_cell_[a]));
+        idx[a] = i < 0 ? 0 : (i >= n ? n - 1 : i);
+    }
+    return (idx[0] * shape_[1] + idx[1]) * shape_[2] + idx[2];
+}
+
+// src/SimulationDomain.cpp:399-450 (analytic box branch)
+void SimulationDomain::trace(const Vec3& p, const Vec3& v, Vec3& cp, double& t, int& facet) const {
+    constexpr double velocity_eps = 1e-18, time_eps = 1e-14;
+    const Vec3 ext = sub3(bmax_, bmin_);
+    const double scale = std::max({1.0, std::abs(ext[0]), std::abs(ext[1]), std::abs(ext[2])});
+    const double tol = std::max(1e-9, 64.0 * std::numeric_limits<double>::epsilon() * scale);
+    cp = p;
+    t = std::numeric_limits<double>::infinity();
+    facet = -1;
+    for (int a = 0; a < 3; ++a)
+        if (!std::isfinite(p[a]) || p[a] < bmin_[a] - tol || p[a] > bmax_[a] + tol) return;
+    double best = std::numeric_limits<double>::infinity();
+    int plane = -1;
+    for (int a = 0; a < 3; ++a) {
+        const double c = v[a];
+        if (!std::isfinite(c) || std::abs(c) <= velocity_eps) continue;
+        const int side = c > 0.0 ? 1 : 0;
+        const double target = side ? bmax_[a] : bmin_[a];
+        const double h = (target - p[a]) / c;
+        if (std::isfinite(h) && h > time_eps && h < best) {
+            best = h;
+            plane = 2 * a + side;
+        }
+    }
+    if (plane < 0) return;
+    Vec3 c{p[0] + v[0] * best, p[1] + v[1] * best, p[2] + v[2] * best};
+    const int ha = plane / 2;
+    c[ha] = plane % 2 ? bmax_[ha] : bmin_[ha];
+    for (int a = 0; a < 3; ++a) {
+        if (!std::isfinite(c[a]) || c[a] < bmin_[a] - tol || c[a] > bmax_[a] + tol) return;
+        c[a] = std::clamp(c[a], bmin_[a], bmax_[a]);
+    }
+    cp = c;
+    t = best;
+    facet = plane;
+}
+
+bool SimulationDomain::contains_point(const Vec3& p) const {
+    for (int a = 0; a < 3; ++a)
+        if (!(p[a] >= bmin_[a] && p[a] <= bmax_[a])) return false;
+    return true;
+}
+
+int SimulationDomain::nearest_facet(const Vec3& p) const {
+    int best = -1;
+    double bd = std::numeric_limits<double>::infinity();
+    for (int f = 0; f < 6; ++f) {
+        const int a = f / 2;
+        const double d = std::abs(p[a] - (f % 2 ? bmax_[a] : bmin_[a]));
+        if (d < bd) {
+            bd = d;
+            best = f;
+        }
+    }
+    return best;
+}
+
+// ----------------------------------------------------------- rough tables
+// src/solver/RoughBoundarySampler.cpp:77-368
+void RoughTables::build(const std::vector<const PhononMaterial*>& mats, const std::vector<Vec3>& normals,
+                        const std::vector<double>& roughness, const std::vector<char>& enabled,
+                        bool require_discrete, double Teq) {
+    const int nf = static_cast<int>(normals.size());
+    tables.clear();
+    facet_table.assign(static_cast<size_t>(nf) * mats.size(), -1);
+    int total = 0;
+    for (char e : enabled) total += e ? 1 : 0;
+    if (!total) return;
+    for (size_t mid = 0; mid < mats.size(); ++mid) {
+        const PhononMaterial& M = *mats[mid];
+        const int na = M.active_mode_count();
+        const auto& act = M.active_flat();
+        std::vector<Vec3> va(na);
+        std::vector<double> vn(na), wa(na), kn(na), dw(na);
+        for (int i = 0; i < na; ++i) {
+            va[i] = M.velocity(act[i]);
+            vn[i] = norm3(va[i]);
+            wa[i] = M.omega(act[i]);
+            kn[i] = M.wavevector_norm(act[i]);
+            dw[i] = M.frequency_window(act[i]);
+        }
+        std::vector<int> shell(na), order(na);
+        std::iota(order.begin(), order.end(), 0);
+        std::sort(order.begin(), order.end(), [&](int a, int b) { return wa[a] < wa[b]; });
+        int shells = 0;
+        double sf = -1;
+        for (int ai : order) {
+            if (sf < 0 || wa[ai] - sf > 1e-8 * std::max(sf, 1e-12)) {
+                ++shells;
+                sf = wa[ai];
+            }
+            shell[ai] = shells - 1;
+        }
+        for (int f = 0; f < nf; ++f) {
+            if (!enabled[f]) continue;
+            RoughTable rd;
+            rd.facet = f;
+            rd.material = static_cast<int>(mid);
+            rd.strict_elastic = Teq > 0;
+            rd.specularity.assign(na, 0.0);
+            rd.spec_match.assign(na, -1);
+            rd.diffuse_begin.assign(na, -1);
+            rd.diffuse_end.assign(na, -1);
+            const double eta = std::max(0.0, roughness[f]);
+            const Vec3 nin = mul3(normals[f], -1.0);
+            std::vector<int> incoming, outgoing;
+            std::vector<double> destr(na, 0.0), creat(na, 0.0);
+            for (int ai = 0; ai < na; ++ai) {
+                const double v = dot3(va[ai], nin);
+                if (v < 0.0) {
+                    incoming.push_back(ai);
+                    destr[ai] = -v;
+                } else if (v > 0.0) {
+                    outgoing.push_back(ai);
+                    creat[ai] = v;
+                }
+                const double vnorm = std::max(1e-12, vn[ai]);
+                const double cosi = std::abs(v) / vnorm;
+                const double x = rd.strict_elastic ? 2 * eta * std::abs(dot3(M.wavevector(act[ai]), nin))
+                                                   : 2.0 * eta * cosi * kn[ai];
+                double p = std::exp(-(x * x));
+                if (!std::isfinite(p)) p = 0.0;
+                rd.specularity[ai] = v < 0.0 ? std::clamp(p, 0.0, 1.0) : 0.0;
+                if (rd.strict_elastic) {
+                    const double c = M.mode_heat_capacity(Teq, act[ai]);
+                    destr[ai] *= c;
+                    creat[ai] *= c;
+                }
+            }
+            if (require_discrete && !incoming.empty() && outgoing.empty())
+                throw std::invalid_argument("Full-matrix reflecting facet " + std::to_string(f) +
+                                            " has incoming modes but no inward outgoing material mode for material " +
+                                            std::to_string(mid) + ". Supply a complete full-Brillouin-zone mode bank.");
+            rd.outgoing_active = outgoing;
+            rd.outgoing_sorted = outgoing;
+            std::sort(rd.outgoing_sorted.begin(), rd.outgoing_sorted.end(),
+                      [&](int a, int b) { return wa[a] < wa[b]; });
+            rd.outgoing_sorted_omega.resize(rd.outgoing_sorted.size());
+            for (size_t k = 0; k < rd.outgoing_sorted.size(); ++k) rd.outgoing_sorted_omega[k] = wa[rd.outgoing_sorted[k]];
+            std::vector<int> sb(shells, -1), se(shells, -1);
+            if (rd.strict_elastic) {
+                std::vector<double> inf(shells, 0), outf(shells, 0);
+                for (int ai : incoming) inf[shell[ai]] += destr[ai];
+                for (int ao : outgoing) outf[shell[ao]] += creat[ao];
+                const double resolved = std::max(*std::max_element(inf.begin(), inf.end()),
+                                                 *std::max_element(outf.begin(), outf.end()));
+                const double roundoff = 64 * std::numeric_limits<double>::epsilon() * resolved;
+                for (int s = 0; s < shells; ++s)
+                    if (std::abs(inf[s] - outf[s]) > 1e-7 * std::max(inf[s], outf[s]) + roundoff)
+                        throw std::invalid_argument("Callaway reflecting boundary lacks balanced equal-frequency "
+                                                    "incoming/outgoing flux. Check full-BZ material symmetry and velocities.");
+                for (int pos = 0; pos < static_cast<int>(rd.outgoing_sorted.size()); ++pos) {
+                    const int s = shell[rd.outgoing_sorted[pos]];
+                    if (sb[s] < 0) sb[s] = pos;
+                    se[s] = pos + 1;
+                }
+            }
+            for (int ai : incoming) {
+                if (rd.outgoing_sorted.empty()) continue;
+                const double win = wa[ai];
+                const double tol = std::max(1e-12, dw[ai]);
+                const auto lo = std::lower_bound(rd.outgoing_sorted_omega.begin(), rd.outgoing_sorted_omega.end(), win - tol);
+                const auto hi = std::upper_bound(rd.outgoing_sorted_omega.begin(), rd.outgoing_sorted_omega.end(), win + tol);
+                const int ib = rd.strict_elastic ? sb[shell[ai]] : static_cast<int>(lo - rd.outgoing_sorted_omega.begin());
+                const int ie = rd.strict_elastic ? se[shell[ai]] : static_cast<int>(hi - rd.outgoing_sorted_omega.begin());
+                if (ie <= ib) continue;
+                rd.diffuse_begin[ai] = ib;
+                rd.diffuse_end[ai] = ie;
+                const Vec3 vin = va[ai];
+                const double vdn = dot3(vin, nin);
+                const Vec3 vtry = sub3(vin, mul3(nin, 2.0 * vdn));
+                int best = -1;
+                double bm = std::numeric_limits<double>::infinity();
+                for (int pos = ib; pos < ie; ++pos) {
+                    const int ao = rd.outgoing_sorted[pos];
+                    const Vec3 dv = sub3(vtry, va[ao]);
+                    const double ref = std::max({1e-12, norm3(vtry), norm3(va[ao])});
+                    const double metric = norm3(dv) / ref;
+                    if (metric < bm) {
+                        bm = metric;
+                        best = ao;
+                    }
+                }
+                if (best >= 0) rd.spec_match[ai] = best;
+            }
+            for (int ai : incoming)
+                if (rd.spec_match[ai] < 0) rd.specularity[ai] = 0.0;
+            if (rd.strict_elastic) {
+                std::vector<double> assigned(na, 0);
+                for (int ai : incoming)
+                    if (rd.spec_match[ai] >= 0) assigned[rd.spec_match[ai]] += destr[ai] * rd.specularity[ai];
+                for (int ai : incoming) {
+                    const int ao = rd.spec_match[ai];
+                    if (ao >= 0 && assigned[ao] > creat[ao]) rd.specularity[ai] *= creat[ao] / assigned[ao];
+                }
+            }
+            // residual diffuse creation rates (include/solver/BoundaryFluxSampling.h:16-42)
+            std::vector<double> residual = creat;
+            for (int in = 0; in < na; ++in) {
+                const int out = rd.spec_match[in];
+                if (out < 0 || out >= na) continue;
+                const double flux = destr[in], prob = rd.specularity[in];
+                if (!std::isfinite(flux) || !std::isfinite(prob) || flux <= 0.0 || prob <= 0.0) continue;
+                residual[out] -= flux * std::clamp(prob, 0.0, 1.0);
+            }
+            for (double& r : residual)
+                if (!std::isfinite(r) || r < 0.0) r = 0.0;
+            double rate_sum = 0.0;
+            for (int ao : outgoing) rate_sum += residual[ao];
+            rd.residual_prefix.assign(rd.outgoing_sorted.size() + 1, 0.0);
+            for (size_t i = 0; i < rd.outgoing_sorted.size(); ++i) {
+                double w = residual[rd.outgoing_sorted[i]];
+                if (!std::isfinite(w) || w < 0.0) w = 0.0;
+                rd.residual_prefix[i + 1] = rd.residual_prefix[i] + w;
+            }
+            if (rate_sum > 0.0) {
+                double cdf = 0.0;
+                for (int ao : outgoing) {
+                    const double r = residual[ao];
+                    if (r <= 0.0) continue;
+                    cdf += r;
+                    rd.roulette_active.push_back(ao);
+                    rd.roulette_cdf.push_back(cdf);
+                }
+            }
+            facet_table[mid * nf + f] = static_cast<int>(tables.size());
+            tables.push_back(std::move(rd));
+        }
+    }
+}
+
+// ---------------------------------------------------------------- ledger
+// src/solver/EnergyLedger.cpp:58-90 (same evaluation order of the residual).
+void EnergyLedger::finish_step(double energy, const BoundaryBalance& b) {
+    const double residual = energy - thermal_ - step_.source_energy_ev - step_.drive_energy_ev -
+                            b.injected_energy_ev + b.absorbed_energy_ev - step_.lifetime_residual_ev;
+    if (!std::isfinite(residual)) throw std::invalid_argument("Non-finite energy ledger input.");
+    step_.balance_residual_ev = residual;
+    total_.source_updates += step_.source_updates;
+    total_.source_energy_ev += step_.source_energy_ev;
+    total_.lifetime_residual_ev += step_.lifetime_residual_ev;
+    total_.balance_residual_ev += step_.balance_residual_ev;
+    total_.drive_updates += step_.drive_updates;
+    total_.drive_energy_ev += step_.drive_energy_ev;
+    thermal_ = energy;
+}
+
+// ---------------------------------------------------------------- problem
+Problem build_problem(const SimulationConfig& cfg, SimulationDomain& domain,
+                      const std::vector<const PhononMaterial*>& mats) {
+    if (mats.empty()) throw std::runtime_error("MonteCarloSolver requires at least one material.");
+    if (!std::isfinite(cfg.time_step) || cfg.time_step <= 0) throw std::invalid_argument("time_step must be positive");
+    Problem P;
+    P.cfg = cfg;
+    P.domain = &domain;
+    P.linearized = uses_linearized_transport(cfg);
+    P.conservative = uses_conservative_transport(cfg);
+    P.one_to_one = !(P.conservative || mats.size() > 1);
+    P.initial_particles = static_cast<int>(std::llround(cfg.particle_count));
+    if (P.initial_particles <= 0) throw std::invalid_argument("particle_count must be positive");
+    P.push_eps = 1e-10 * std::max(cfg.time_step, 1.0);
+    P.particle_volume = domain.volume() / static_cast<double>(P.initial_particles);
+    const double Tbg = cfg.background_temperature;
+    P.layout.axis = cfg.material_interface_axis;
+    P.layout.planes = cfg.material_interface_positions;
+    if (P.layout.planes.size() + 1 != mats.size())
+        throw std::runtime_error("Layered materials require one interface plane fewer than materials.");
+    P.cell_material.resize(domain.grid_count());
+    for (int c = 0; c < domain.grid_count(); ++c) P.cell_material[c] = P.layout.material_at(domain.grid_centers()[c]);
+    if (mats.size() > 1) throw std::runtime_error("Multi-material layouts are not enabled in this build.");
+
+    int axis = 0;
+    if (cfg.transport_axis >= 0) axis = cfg.transport_axis;
+    else {
+        const int nx = cfg.grid[0], ny = cfg.grid[1], nz = cfg.grid[2];
+        if (ny > nx && ny >= nz) axis = 1;
+        else if (nz > nx && nz > ny) axis = 2;
+    }
+    P.kappa_axis = axis;
+
+    for (size_t mid = 0; mid < mats.size(); ++mid) {
+        const PhononMaterial& M = *mats[mid];
+        MaterialTables T;
+        T.n_active = M.active_mode_count();
+        T.active_flat = M.active_flat();
+        const int na = T.n_active;
+        T.omega.resize(na);
+        T.hw.resize(na);
+        T.vel.resize(3 * na);
+        T.nbg.resize(na);
+        T.capacity_bg.resize(na);
+        for (int a = 0; a < na; ++a) {
+            const int f = T.active_flat[a];
+            T.omega[a] = M.omega(f);
+            T.hw[a] = kHbarEvPs * M.omega(f);
+            for (int k = 0; k < 3; ++k) T.vel[3 * a + k] = M.velocity(f)[k];
+            T.nbg[a] = M.bose_occupation(Tbg, f);
+            T.capacity_bg[a] = M.mode_heat_capacity(Tbg, f);
+        }
+        // BackgroundCache (include/solver/BackgroundCache.h:13-31)
+        T.energy_weight = static_cast<double>(na) * P.particle_volume / M.energy_density_normalization();
+        T.energy_density_bg = P.linearized ? M.crystal_energy_density(Tbg) : M.energy_density_from_temperature(Tbg);
+        T.heat_capacity_density_bg = 0.0;
+        for (int f = 0; f < M.flat_count(); ++f)
+            T.heat_capacity_density_bg += M.mode_heat_capacity(Tbg, f) / M.energy_density_normalization();
+        T.zero_point = M.zero_point_energy_density();
+        T.lookup_T = M.lookup_T();
+        T.lookup_E = M.lookup_E();
+        T.temperatures = M.temperature_samples();
+        const size_t nT = T.temperatures.size();
+        const size_t nm = static_cast<size_t>(M.flat_count());
+        T.gamma_active.resize(nT * na);
+        for (size_t it = 0; it < nT; ++it)
+            for (int a = 0; a < na; ++a) T.gamma_active[it * na + a] = M.gamma_total()[it * nm + T.active_flat[a]];
+        T.relax_fixed.resize(na);
+        for (int a = 0; a < na; ++a)
+            T.relax_fixed[a] = M.mode_relaxation_weight(cfg.lifetime_temperature, T.active_flat[a], cfg.time_step);
+        if (P.linearized) {
+            const CallawayData d = cfg.collision_model == CollisionModel::Callaway ? M.callaway_data(Tbg)
+                                                                                   : M.linearized_rta_data(Tbg);
+            T.col_capacity = d.capacity;
+            T.col_normal = d.normal_rate;
+            T.col_resistive = d.resistive_rate;
+            T.col_k.resize(3 * na);
+            for (int a = 0; a < na; ++a)
+                for (int k = 0; k < 3; ++k) T.col_k[3 * a + k] = d.wavevector[a][k];
+        }
+        // Mode classes: identical omega and identical linewidth row.
+        std::vector<int> order(na);
+        std::iota(order.begin(), order.end(), 0);
+        auto key_less = [&](int a, int b) {
+            if (T.omega[a] != T.omega[b]) return T.omega[a] < T.omega[b];
+            for (size_t it = 0; it < nT; ++it) {
+                const double ga = T.gamma_active[it * na + a], gb = T.gamma_active[it * na + b];
+                if (ga != gb) return ga < gb;
+            }
+            return false;
+        };
+        std::stable_sort(order.begin(), order.end(), key_less);
+        T.mode_class.assign(na, -1);
+        for (size_t i = 0; i < order.size(); ++i) {
+            const int a = order[i];
+            if (i == 0 || key_less(order[i - 1], a)) {
+                T.class_rep.push_back(a);
+                T.class_omega.push_back(T.omega[a]);
+                T.class_hw.push_back(T.hw[a]);
+            }
+            T.mode_class[a] = static_cast<int>(T.class_rep.size()) - 1;
+        }
+        T.n_classes = static_cast<int>(T.class_rep.size());
+        P.mats.push_back(std::move(T));
+    }
+
+    // Gradient drive (src/solver/TemperatureGradientDrive.cpp:13-86).
+    if (cfg.temperature_gradient) {
+        if (mats.size() != 1) throw std::runtime_error("Gradient driving requires one material.");
+        if (!domain.reservoir_facets().empty())
+            throw std::invalid_argument("Temperature-gradient driving requires a periodic box without reservoirs.");
+        int paired = 0;
+        for (const auto& F : domain.facets()) {
+            if (std::abs(F.normal[axis]) > 1e-8) {
+                if (F.condition != 'P' || F.pair < 0)
+                    throw std::invalid_argument("Temperature-gradient direction must have paired periodic boundaries.");
+                ++paired;
+            }
+        }
+        if (paired < 2) throw std::invalid_argument("Missing periodic boundaries along the imposed gradient.");
+        const PhononMaterial& M = *mats[0];
+        MaterialTables& T = P.mats[0];
+        std::vector<double> cap(T.n_active);
+        long double sum = 0, absolute = 0, total_c = 0;
+        T.grad_rate.resize(T.n_active);
+        for (int a = 0; a < T.n_active; ++a) {
+            const double c = M.mode_heat_capacity(Tbg, T.active_flat[a]);
+            const double rate = -c * M.velocity(T.active_flat[a])[axis] * 1e-10 * (*cfg.temperature_gradient);
+            if (!(c > 0) || !std::isfinite(rate)) throw std::invalid_argument("Invalid gradient source mode.");
+            cap[a] = c;
+            T.grad_rate[a] = rate;
+            sum += rate;
+            absolute += std::abs(rate);
+            total_c += c;
+        }
+        if (std::abs(sum) > 1e-8L * absolute)
+            throw std::invalid_argument("Gradient source has nonzero net energy: supply a balanced full-BZ "
+                                        "velocity/capacity bank.");
+        for (int a = 0; a < T.n_active; ++a) T.grad_rate[a] -= static_cast<double>(sum * cap[a] / total_c);
+        P.gradient_energy_weight = T.n_active * P.particle_volume / M.energy_density_normalization();
+    }
+
+    // Rough tables (src/solver/RoughBoundaryInitialization.cpp:1-26).
+    std::vector<Vec3> normals;
+    std::vector<double> rough;
+    std::vector<char> enabled;
+    for (const auto& F : domain.facets()) {
+        normals.push_back(F.normal);
+        rough.push_back(F.condition == 'R' ? std::max(0.0, F.value) : 0.0);
+        const bool reflecting = F.condition != 'T' && !(F.condition == 'P' && F.pair >= 0);
+        enabled.push_back(P.conservative ? reflecting : F.condition == 'R');
+    }
+    P.rough.build(mats, normals, rough, enabled, P.conservative, P.conservative ? Tbg : 0.0);
+
+    // Reservoirs (src/solver/ReservoirInitialization.cpp:1-45, ReservoirSampler.cpp:17-101).
+    const double density = static_cast<double>(P.initial_particles) / domain.volume();
+    for (int f : domain.reservoir_facets()) {
+        const Facet& F = domain.facets()[f];
+        Reservoir R;
+        R.facet = f;
+        R.material = P.layout.material_at(F.centroid);
+        R.temperature = F.value;
+        R.area = F.area;
+        R.normal = F.normal;
+        const PhononMaterial& M = *mats[R.material];
+        const auto& act = M.active_flat();
+        R.cdf.resize(act.size());
+        const double n_active = static_cast<double>(M.active_mode_count());
+        double expected = 0;
+        if (density > 0.0 && cfg.time_step > 0.0) {
+            const double thickness = n_active / (density * R.area);
+            for (size_t m = 0; m < act.size(); ++m) {
+                const double par = -dot3(R.normal, M.velocity(act[m]));
+                expected += std::max(0.0, par * cfg.time_step / thickness);
+                R.cdf[m] = expected;
+            }
+        }
+        if (expected > 0)
+            for (double& v : R.cdf) v /= expected;
+        R.initial_count = static_cast<int>(std::llround(expected));
+        R.expected = expected;
+        std::vector<double> occ(act.size());
+        for (size_t m = 0; m < act.size(); ++m)
+            occ[m] = P.linearized ? M.linearized_bose_occupation(R.temperature, Tbg, act[m])
+                                  : M.bose_occupation(R.temperature, act[m]);
+        P.reservoir_occ.push_back(std::move(occ));
+        P.reservoirs.push_back(std::move(R));
+    }
+    return P;
+}
+
+// src/solver/Initialization.cpp:32-137, 180-265 with Philox draws.
+CarrierArrays initial_carriers(const Problem& p, const std::vector<const PhononMaterial*>& mats) {
+    const SimulationDomain& D = *p.domain;
+    const int n = p.initial_particles;
+    CarrierArrays c;
+    c.x.resize(n);
+    c.y.resize(n);
+    c.z.resize(n);
+    c.occ.resize(n);
+    c.mode.resize(n);
+    c.cell.resize(n);
+    c.alive.assign(n, 1);
+    // initial temperature profile
+    double cold_t = std::numeric_limits<double>::infinity(), hot_t = -cold_t;
+    int cold = -1, hot = -1;
+    for (int f : D.reservoir_facets()) {
+        const double T = D.facets()[f].value;
+        if (T < cold_t) { cold_t = T; cold = f; }
+        if (T > hot_t) { hot_t = T; hot = f; }
+    }
+    double tmin = 299.0, tmax = 301.0;
+    if (!D.reservoir_facets().empty()) { tmin = cold_t; tmax = hot_t; }
+    const bool linear = p.cfg.initial_temperature_mode == InitialTemperatureMode::Linear;
+    const bool valid_pair = cold >= 0 && hot >= 0 && hot_t > cold_t + 1e-12;
+    const double tmean = 0.5 * (tmin + tmax);
+    Vec3 pc{}, axis{};
+    double axis_len2 = 0;
+    if (linear && valid_pair) {
+        pc = D.facets()[cold].centroid;
+        axis = sub3(D.facets()[hot].centroid, pc);
+        axis_len2 = dot3(axis, axis);
+    }
+    const Vec3& lo = D.bounds_min();
+    const Vec3& hi = D.bounds_max();
+    const uint64_t seed = p.cfg.random_seed;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        const Uniform2 u0 = uniform2(seed, static_cast<uint32_t>(i), 0xFFFFFFFFu, kDrawInit, 0, 0);
+        const Uniform2 u1 = uniform2(seed, static_cast<uint32_t>(i), 0xFFFFFFFFu, kDrawInit, 0, 1);
+        const Vec3 pos{lo[0] + (hi[0] - lo[0]) * u0.a, lo[1] + (hi[1] - lo[1]) * u0.b, lo[2] + (hi[2] - lo[2]) * u1.a};
+        const int mid = p.layout.material_at(pos);
+        const MaterialTables& T = p.mats[mid];
+        int a = static_cast<int>(u1.b * T.n_active);
+        if (a >= T.n_active) a = T.n_active - 1;
+        double temp = p.cfg.initial_temperature;
+        if (linear) {
+            if (valid_pair && axis_len2 > 1e-20) {
+                const double s = std::clamp(dot3(sub3(pos, pc), axis) / axis_len2, 0.0, 1.0);
+                temp = cold_t + s * (hot_t - cold_t);
+            } else {
+                temp = tmean;
+            }
+        }
+        const int flat = T.active_flat[a];
+        c.x[i] = pos[0];
+        c.y[i] = pos[1];
+        c.z[i] = pos[2];
+        c.mode[i] = mode_word(static_cast<uint32_t>(a), 0u, static_cast<uint32_t>(mid));
+        c.cell[i] = D.fast_grid_index(pos);
+        c.occ[i] = p.linearized ? mats[mid]->linearized_bose_occupation(temp, p.cfg.background_temperature, flat)
+                                : mats[mid]->bose_occupation(temp, flat);
+    }
+    return c;
+}
+
+// ------------------------------------------------------------- writers
+std::string format_convergence_header(size_t cells, bool gradient_driven) {
+    std::ostringstream out;
+    out << "# timestep time_ps";
+    for (size_t i = 0; i < cells; ++i) out << " T_" << (i + 1);
+    out << " heatflux kappa_int kappa_eff particle_count absorbed injected recovered net"
+           " reservoir_absorbed_energy_ev reservoir_injected_energy_ev"
+           " hs_occupation_updates hs_injected_energy_ev lifetime_energy_residual_ev"
+           " energy_balance_residual_ev total_thermal_energy_ev"
+           " hs_prescribed_total_ev hs_pending_total_ev hs_ledger_residual_ev";
+    if (gradient_driven) out << " gradient_occupation_updates gradient_energy_ev";
+    out << '\n';
+    return out.str();
+}
+
+// src/solver/ResultWriter.cpp:100-119: default stream precision for the step,
+// time and temperatures, then 12 significant digits.
+std::string format_convergence_row(const ConvergenceRow& s) {
+    std::ostringstream out;
+    out << s.timestep << " " << s.time_ps;
+    for (double t : s.temperatures) out << " " << t;
+    out.precision(12);
+    out << " " << s.heat_flux << " " << s.kappa_int << " " << s.kappa_eff << " " << s.particle_count << " "
+        << s.absorbed << " " << s.injected << " " << 0 << " " << s.net << " " << s.absorbed_ev << " "
+        << s.injected_ev << " " << s.source_updates << " " << s.source_ev << " " << s.lifetime_residual << " "
+        << s.balance_residual << " " << s.thermal_energy << " " << 0 << " " << 0 << " " << 0;
+    if (s.gradient) out << " " << s.gradient_updates << " " << s.gradient_energy;
+    out << '\n';
+    return out.str();
+}
+
+} // namespace phmc

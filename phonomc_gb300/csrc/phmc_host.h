@@ -1,0 +1,358 @@
+// Host-side model of PhonoMC's per-timestep carrier loop: configuration,
+// phonon material, box domain and the immutable sampling tables that the CUDA
+// kernels (and the CPU oracle used by the tests) read every step.
+//
+// The classes keep the reference's names and query semantics:
+//   SimulationConfig   include/SimulationConfig.h:42-156 (the fields this path reads)
+//   PhononMaterial     include/PhononMaterial.h:14-125, src/PhononMaterial.cpp,
+//                      src/material/Thermodynamics.cpp
+//   SimulationDomain   include/SimulationDomain.h:14-99 (analytic box geometry)
+//   RoughTables        src/solver/RoughBoundarySampler.cpp:77-368
+//   ReservoirTables    src/solver/ReservoirSampler.cpp:17-101
+// Everything is flattened into `Problem`, the one structure uploaded to HBM.
+#pragma once
+
+#include <array>
+#include <cstdint>
+#include <map>
+#include <optional>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace phmc {
+
+constexpr double kHbarEvPs = 6.582119569e-4;
+constexpr double kBoltzmannEvK = 8.617333262145e-5;
+constexpr double kPi = 3.14159265358979323846;
+
+using Vec3 = std::array<double, 3>;
+
+// ------------------------------------------------------------------ config
+enum class CollisionModel { Rta, Callaway };
+enum class BoundaryCondition : char { ThermalReservoir = 'T', Periodic = 'P', Rough = 'R' };
+enum class InitialTemperatureMode { Uniform, Linear };
+
+// Subset of the reference's SimulationConfig read by the carrier loop, with the
+// same names, units (lengths in Angstrom internally, as after parsing) and
+// defaults (include/SimulationConfig.h:42-146).
+struct SimulationConfig {
+    std::string model = "box";
+    std::vector<double> sizes{2000.0, 2000.0, 2000.0}; // Angstrom
+    double particle_count = 1e4;
+    double time_step = 1.0;
+    int iterations = 10000;
+    int convergence_write_interval = 10;
+    uint64_t random_seed = 12345;
+    bool compute_kappa = false;
+    int transport_axis = -1;
+    std::optional<double> temperature_gradient;
+    double temperature_lookup_dt = 0.1;
+    double background_temperature = 300.0;
+    bool lifetime_temperature_is_local = true;
+    double lifetime_temperature = 300.0;
+    CollisionModel collision_model = CollisionModel::Rta;
+    bool conservative_boundaries = false;
+    std::array<int, 3> grid{1, 1, 1};
+    InitialTemperatureMode initial_temperature_mode = InitialTemperatureMode::Uniform;
+    double initial_temperature = 300.0;
+    // Per box face in facet order xmin,xmax,ymin,ymax,zmin,zmax: condition and value
+    // (reservoir K, roughness in nm as in TOML; zero for periodic). Periodic faces
+    // are paired with the opposite face of the same axis.
+    std::array<char, 6> face_condition{'R', 'R', 'R', 'R', 'R', 'R'};
+    std::array<double, 6> face_value{0, 0, 0, 0, 0, 0};
+    std::string output_folder;
+    // Layered materials (include/SimulationConfig.h:93-99): N materials, N-1 planes.
+    int material_interface_axis = 0;
+    std::vector<double> material_interface_positions; // Angstrom
+    double material_interface_frequency_bin_thz = 0.1;
+};
+
+// include/SimulationConfig.h:148-156
+inline bool uses_linearized_transport(const SimulationConfig& c) {
+    return c.collision_model == CollisionModel::Callaway || c.temperature_gradient.has_value();
+}
+inline bool uses_conservative_transport(const SimulationConfig& c) {
+    return uses_linearized_transport(c) || c.conservative_boundaries;
+}
+
+// ------------------------------------------------------------- material
+// include/material/MaterialData.h:17-31
+struct MaterialData {
+    double volume_a3 = 0;
+    std::array<Vec3, 3> reciprocal{}; // row i = Cartesian component i of (b1,b2,b3)
+    int qpoints = 0, branches = 0;
+    std::array<int, 3> mesh{};
+    std::vector<double> frequency_thz;
+    std::vector<Vec3> qpoint_fractions, group_velocity;
+    std::vector<double> temperatures, gamma;
+    std::vector<double> gamma_normal, gamma_umklapp;
+    std::map<std::string, std::vector<double>> gamma_resistive;
+};
+
+void validate_material_data(const MaterialData& d);
+
+// Linear-response (Callaway) modal data on the active bank
+// (include/material/CallawayOperator.h:17-24 of the reference).
+struct CallawayData {
+    std::vector<double> omega, capacity, normal_rate, resistive_rate;
+    std::vector<Vec3> wavevector;
+};
+
+class PhononMaterial {
+public:
+    PhononMaterial(MaterialData data, double temperature_lookup_dt = 0.1,
+                   bool include_stationary_modes = false, bool complete_callaway_bz = true);
+
+    int active_mode_count() const { return static_cast<int>(active_.size()); }
+    int qpoint_count() const { return nq_; }
+    int branch_count() const { return nb_; }
+    int flat_count() const { return nq_ * nb_; }
+    const std::vector<int>& active_flat() const { return active_; }
+    int active_index_for_flat(int flat) const {
+        return flat >= 0 && flat < flat_count() ? flat_to_active_[flat] : -1;
+    }
+    double omega(int flat) const { return omega_[flat]; }
+    const Vec3& velocity(int flat) const { return vel_[flat]; }
+    const Vec3& wavevector(int flat) const { return kvec_[flat]; }
+    double wavevector_norm(int flat) const { return knorm_[flat]; }
+    double frequency_window(int flat) const { return window_[flat]; }
+
+    double bose_occupation(double T, int flat) const;
+    double mode_heat_capacity(double T, int flat) const;
+    double linearized_bose_occupation(double T, double Tref, int flat) const;
+    double mode_gamma(double T, int flat) const;
+    double mode_relaxation_weight(double T, int flat, double dt) const;
+    double crystal_energy_density(double T) const;
+    double energy_density_from_temperature(double T) const;
+    double temperature_from_energy_density(double E) const;
+    double energy_density_normalization() const;
+    double zero_point_energy_density() const { return zero_point_; }
+    CallawayData linearized_rta_data(double T) const;
+    CallawayData callaway_data(double T) const;
+    bool has_callaway_rates() const { return !gamma_normal_.empty(); }
+
+    const std::vector<double>& lookup_T() const { return table_T_; }
+    const std::vector<double>& lookup_E() const { return table_E_; }
+    const std::vector<double>& temperature_samples() const { return temps_; }
+    const std::vector<double>& gamma_total() const { return gamma_total_; }
+
+    static double interp_linear_clamped(const std::vector<double>& xs, const std::vector<double>& ys,
+                                        double x);
+
+private:
+    void build_lookup();
+    int nq_ = 0, nb_ = 0;
+    double volume_ = 1.0, dT_ = 0.1, zero_point_ = 0.0;
+    bool stationary_ = false;
+    unsigned refinement_ = 1;
+    std::vector<double> omega_, knorm_, window_;
+    std::vector<Vec3> vel_, kvec_, qfrac_;
+    std::vector<int> active_, flat_to_active_;
+    std::vector<double> temps_, gamma_total_, gamma_normal_, gamma_umklapp_, gamma_extra_;
+    std::vector<double> table_T_, table_E_;
+    std::array<Vec3, 3> reciprocal_{};
+    std::array<int, 3> mesh_{};
+};
+
+// ---------------------------------------------------------------- domain
+struct Facet {
+    Vec3 normal{}, centroid{};
+    double area = 0;
+    char condition = 'R';
+    double value = 0;      // reservoir temperature (K) or roughness (Angstrom)
+    int pair = -1;         // periodic partner facet
+    Vec3 shift{};          // periodic translation a -> pair
+    int reservoir = -1;    // reservoir index for 'T'
+    std::array<Vec3, 3> tri[2]; // two triangles spanning the face (injection sampling)
+};
+
+// Analytic axis-aligned box (src/SimulationDomain.cpp:73-126, 292-450, 626-766).
+// Facet f = 2*axis + side, which is the reference's box facet order.
+class SimulationDomain {
+public:
+    explicit SimulationDomain(const SimulationConfig& cfg);
+    const Vec3& bounds_min() const { return bmin_; }
+    const Vec3& bounds_max() const { return bmax_; }
+    double volume() const { return volume_; }
+    int grid_count() const { return static_cast<int>(centers_.size()); }
+    const std::array<int, 3>& grid_shape() const { return shape_; }
+    const Vec3& inv_cell() const { return inv_cell_; }
+    const std::vector<Vec3>& grid_centers() const { return centers_; }
+    const std::vector<double>& grid_volumes() const { return volumes_; }
+    const std::vector<Facet>& facets() const { return facets_; }
+    const std::vector<int>& reservoir_facets() const { return reservoir_facets_; }
+    int fast_grid_index(const Vec3& p) const;
+    // Returns (collision point, time, facet); facet -1 and infinite time on a miss.
+    void trace(const Vec3& p, const Vec3& v, Vec3& cp, double& t, int& facet) const;
+    bool contains_point(const Vec3& p) const;
+    int nearest_facet(const Vec3& p) const;
+
+private:
+    Vec3 bmin_{}, bmax_{}, inv_cell_{};
+    double volume_ = 0;
+    std::array<int, 3> shape_{1, 1, 1};
+    std::vector<Vec3> centers_;
+    std::vector<double> volumes_;
+    std::vector<Facet> facets_;
+    std::vector<int> reservoir_facets_;
+};
+
+// Layered materials along one axis (src/solver/LayeredMaterialLayout.cpp:24-115).
+struct LayeredLayout {
+    int axis = 0;
+    std::vector<double> planes; // ascending
+    int material_at(const Vec3& p) const {
+        int m = 0;
+        while (m < static_cast<int>(planes.size()) && p[axis] >= planes[m]) ++m;
+        return m;
+    }
+};
+
+// -------------------------------------------------------- rough tables
+struct RoughTable {
+    int material = 0, facet = -1;
+    bool strict_elastic = false;
+    std::vector<double> specularity;                    // [active]
+    std::vector<int> spec_match, diffuse_begin, diffuse_end; // [active]
+    std::vector<int> outgoing_active, outgoing_sorted;
+    std::vector<double> outgoing_sorted_omega, residual_prefix; // prefix: size sorted+1
+    std::vector<int> roulette_active;
+    std::vector<double> roulette_cdf;
+};
+
+// Builds one table per (material, enabled facet) exactly as the reference's
+// RoughBoundarySampler::build; facet_table[material * facets + facet] -> table.
+struct RoughTables {
+    std::vector<RoughTable> tables;
+    std::vector<int> facet_table;
+    void build(const std::vector<const PhononMaterial*>& mats, const std::vector<Vec3>& normals,
+               const std::vector<double>& roughness, const std::vector<char>& enabled,
+               bool require_discrete, double equilibrium_temperature);
+};
+
+// ----------------------------------------------------- reservoir tables
+struct Reservoir {
+    int facet = -1, material = 0;
+    double temperature = 300, area = 0;
+    Vec3 normal{};
+    std::vector<double> cdf; // over the material's active modes
+    double expected = 0;
+    int initial_count = 0;
+};
+
+// ---------------------------------------------------------------- ledgers
+// src/solver/BoundaryLedger.cpp and src/solver/EnergyLedger.cpp, single writer.
+struct BoundaryBalance {
+    long long absorbed = 0, injected = 0;
+    double absorbed_energy_ev = 0, injected_energy_ev = 0;
+    long long net() const { return injected - absorbed; }
+};
+struct EnergyBalance {
+    long long source_updates = 0;
+    double source_energy_ev = 0, lifetime_residual_ev = 0, balance_residual_ev = 0;
+    long long drive_updates = 0;
+    double drive_energy_ev = 0;
+};
+class EnergyLedger {
+public:
+    void initialize(double e) { thermal_ = e; step_ = {}; total_ = {}; }
+    void begin_step() { step_ = {}; }
+    void record_drive(long long updates, double e) { step_.drive_updates += updates; step_.drive_energy_ev += e; }
+    void set_lifetime_residual(double e) { step_.lifetime_residual_ev = e; }
+    void finish_step(double energy, const BoundaryBalance& b);
+    double thermal_energy_ev() const { return thermal_; }
+    const EnergyBalance& step() const { return step_; }
+    const EnergyBalance& total() const { return total_; }
+
+private:
+    double thermal_ = 0;
+    EnergyBalance step_, total_;
+};
+
+// ---------------------------------------------------------------- problem
+// Flattened per-material tables in active-mode order.
+struct MaterialTables {
+    int n_active = 0;
+    std::vector<int> active_flat;
+    std::vector<double> omega, hw, vel; // vel: [active*3]
+    std::vector<double> nbg;            // Bose occupation at the background temperature
+    std::vector<double> capacity_bg;    // modal heat capacity at the background temperature
+    double energy_weight = 0;           // active * particle volume / normalization
+    double energy_density_bg = 0;
+    double heat_capacity_density_bg = 0;
+    double zero_point = 0;
+    std::vector<double> lookup_T, lookup_E;
+    std::vector<double> temperatures;   // linewidth temperature axis
+    std::vector<double> gamma_active;   // [nT * active], total linewidth (THz)
+    std::vector<double> relax_fixed;    // RTA weight at the fixed lifetime temperature
+    // Linear-response collision data (linearized RTA or Callaway) at T_bg.
+    std::vector<double> col_capacity, col_normal, col_resistive, col_k; // col_k: [active*3]
+    // Mode classes: active modes sharing (omega, linewidth row) share the Bose
+    // function and RTA weight; per-cell RTA sums aggregate over them.
+    int n_classes = 0;
+    std::vector<int> mode_class;        // [active]
+    std::vector<double> class_omega, class_hw;
+    std::vector<int> class_rep;         // representative active mode
+    std::vector<double> grad_rate;      // gradient source rate per active mode (eV/ps)
+    std::vector<double> occ_reservoir;  // filled per reservoir: [reservoir][active]
+};
+
+struct Problem {
+    SimulationConfig cfg;
+    bool linearized = false, conservative = false;
+    bool one_to_one = true;
+    double push_eps = 1e-10;
+    double particle_volume = 0;
+    int initial_particles = 0;
+    std::vector<MaterialTables> mats;
+    SimulationDomain* domain = nullptr;
+    LayeredLayout layout;
+    std::vector<int> cell_material;      // [cells]
+    RoughTables rough;
+    std::vector<Reservoir> reservoirs;
+    std::vector<std::vector<double>> reservoir_occ; // [reservoir][active of its material]
+    double gradient_energy_weight = 0;
+    int kappa_axis = 2;
+};
+
+// Builds every table. Materials must outlive the problem.
+Problem build_problem(const SimulationConfig& cfg, SimulationDomain& domain,
+                      const std::vector<const PhononMaterial*>& mats);
+
+// Initial carriers exactly as src/solver/Initialization.cpp:32-137 samples them,
+// with Philox draws: positions uniform in the box, modes uniform over the active
+// bank, temperatures uniform or linear between the reservoirs, occupations
+// Bose or linearized. SoA output; mode word = active | signs<<24 | material<<28.
+struct CarrierArrays {
+    std::vector<double> x, y, z, occ;
+    std::vector<uint32_t> mode;
+    std::vector<int32_t> cell;
+    std::vector<uint8_t> alive;
+};
+CarrierArrays initial_carriers(const Problem& p, const std::vector<const PhononMaterial*>& mats);
+
+// Mode-word helpers shared with the kernels.
+constexpr uint32_t kActiveMask = 0x00FFFFFFu;
+inline uint32_t mode_word(uint32_t active, uint32_t signs, uint32_t material) {
+    return active | (signs << 24) | (material << 28);
+}
+
+// Convergence output (src/solver/ResultWriter.cpp:82-119): header and one row.
+struct ConvergenceRow {
+    int timestep = 0;
+    double time_ps = 0;
+    std::vector<double> temperatures;
+    double heat_flux = 0, kappa_int = 0, kappa_eff = 0;
+    long long particle_count = 0, absorbed = 0, injected = 0, net = 0;
+    double absorbed_ev = 0, injected_ev = 0;
+    long long source_updates = 0;
+    double source_ev = 0, lifetime_residual = 0, balance_residual = 0, thermal_energy = 0;
+    bool gradient = false;
+    long long gradient_updates = 0;
+    double gradient_energy = 0;
+};
+std::string format_convergence_header(size_t cells, bool gradient_driven);
+std::string format_convergence_row(const ConvergenceRow& r);
+
+} // namespace phmc

@@ -1,0 +1,187 @@
+"""Pin the CPU oracle (and the host tables it shares with the CUDA path) to
+golden vectors printed by the reference solver's own code (tests/golden/)."""
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import golden
+from phonomc_gb300 import abi
+
+D = abi.dptr
+I32 = lambda a: a.ctypes.data_as(abi.c_int32_p)  # noqa: E731
+
+
+def _mat(lib, data, stationary=False):
+    return abi.Material(lib, "orc_", data, 0.1, stationary, False)
+
+
+def _i32(x):
+    return np.ascontiguousarray(x, dtype=np.int32)
+
+
+def _f64(x):
+    return np.ascontiguousarray(x, dtype=np.float64)
+
+
+@pytest.mark.parametrize("name,stationary", [("material_m8", False), ("material_m8_stationary", True)])
+def test_material_tables(oracle_lib, m8, name, stationary):
+    g = golden(name)
+    m = _mat(oracle_lib, m8, stationary)
+    na = int(g["active_mode_count"])
+    sc = np.zeros(7)
+    act = np.zeros(na, dtype=np.int32)
+    oracle_lib.orc_material_scalars(m.h, C.c_double(1234.5), D(sc), I32(act))
+    assert int(sc[0]) == na
+    assert np.array_equal(act, np.asarray(g["active_flat"], dtype=np.int32))
+    assert sc[1] == g["energy_density_normalization"]
+    assert abs(sc[2] - g["zero_point_energy_density"]) <= 1e-15 * abs(g["zero_point_energy_density"])
+    assert abs(sc[3] - g["bg_energy_weight"]) <= 1e-15 * g["bg_energy_weight"]
+    assert abs(sc[4] - g["bg_energy_density"]) <= 1e-14 * g["bg_energy_density"]
+    assert abs(sc[5] - g["bg_energy_density_exact"]) <= 1e-13 * g["bg_energy_density_exact"]
+    assert abs(sc[6] - g["bg_heat_capacity_density"]) <= 1e-12 * g["bg_heat_capacity_density"]
+
+    def q(what, flat, x, aux=0.0):
+        x = _f64(x)
+        out = np.zeros(x.size)
+        fl = _i32(flat if flat is not None else np.zeros(x.size))
+        rc = oracle_lib.orc_material_query(m.h, what, x.size, I32(fl), D(x), C.c_double(aux), D(out))
+        assert rc == 0
+        return out
+
+    # lookup tables are bit-exact up to the order of the per-mode energy sum
+    assert np.allclose(q(4, None, g["table_T"]), g["table_E"], rtol=1e-13, atol=0)
+    T = q(5, None, g["inv_E"])
+    assert np.allclose(T, g["inv_T"], rtol=1e-11, atol=1e-9)
+    assert np.allclose(q(6, None, g["crystal_T"]), g["crystal_E"], rtol=1e-13, atol=0)
+    flat, Tq = g["q_mode"], g["q_T"]
+    assert np.array_equal(q(0, flat, Tq), np.asarray(g["q_bose"]))
+    assert np.array_equal(q(1, flat, Tq), np.asarray(g["q_capacity"]))
+    assert np.array_equal(q(2, flat, Tq, 0.5), np.asarray(g["q_relax_dt0p5"]))
+    assert np.array_equal(q(3, flat, Tq, 300.0), np.asarray(g["q_linearized_300"]))
+
+
+def test_box_trace_and_grid(oracle_lib):
+    g = golden("box_trace")
+    p = _f64(g["ray_p"])
+    v = _f64(g["ray_v"])
+    n = p.shape[0]
+    hit = np.zeros((n, 3))
+    t = np.zeros(n)
+    f = np.zeros(n, dtype=np.int32)
+    lo, hi = _f64([0, 0, 0]), _f64([1000, 800, 600])
+    assert oracle_lib.orc_trace_box(D(lo), D(hi), n, D(p), D(v), D(hit), D(t), I32(f)) == 0
+    assert np.array_equal(f, np.asarray(g["hit_f"], dtype=np.int32))
+    ok = f >= 0
+    assert np.array_equal(t[ok], np.asarray(g["hit_t"])[ok])
+    assert np.array_equal(hit[ok], np.asarray(g["hit_p"])[ok])
+    gi = np.zeros(n, dtype=np.int32)
+    sizes = _f64([1000, 800, 600])
+    grid = _i32([3, 2, 5])
+    assert oracle_lib.orc_grid_index(D(sizes), I32(grid), n, D(p), I32(gi)) == 0
+    assert np.array_equal(gi, np.asarray(g["grid_index"], dtype=np.int32))
+    # facet order, normals, areas and grid of the reference box
+    assert np.array_equal(np.asarray(g["facet_normals"]),
+                          np.array([[-1, 0, 0], [1, 0, 0], [0, -1, 0], [0, 1, 0], [0, 0, -1], [0, 0, 1]]))
+    assert g["facet_areas"] == [480000, 480000, 600000, 600000, 800000, 800000]
+    assert len(g["grid_volumes"]) == 30 and np.allclose(g["grid_volumes"], 480000000 / 30)
+
+
+@pytest.mark.parametrize("name", ["rta_fixed", "rta_local"])
+def test_rta_collision(oracle_lib, m8, name):
+    g = golden(name)
+    m = _mat(oracle_lib, m8)
+    flat, cell = _i32(g["flat"]), _i32(g["cell"])
+    occ = _f64(g["occ_in"]).copy()
+    cT = _f64(g["cell_T"])
+    res = C.c_double()
+    rc = oracle_lib.orc_rta_collide(m.h, flat.size, I32(flat), I32(cell), D(occ), cT.size, D(cT),
+                                    C.c_double(g["dt"]), C.c_double(g["particle_volume"]), int(g["local"]),
+                                    C.c_double(g["lifetime_T"]), C.byref(res))
+    assert rc == 0
+    ref = np.asarray(g["occ_out"])
+    assert np.allclose(occ, ref, rtol=1e-12, atol=1e-15)
+    # the residual is a round-off sized number; compare on the energy scale
+    assert abs(res.value - g["residual"]) < 1e-11
+
+
+def test_linearized_rta(oracle_lib, m8):
+    g = golden("linearized_rta")
+    m = _mat(oracle_lib, m8, True)
+    flat, cell = _i32(g["flat"]), _i32(g["cell"])
+    occ = _f64(g["occ_in"]).copy()
+    res = C.c_double()
+    rc = oracle_lib.orc_linear_collide(m.h, 0, C.c_double(300.0), flat.size, I32(flat), I32(cell), D(occ),
+                                       int(cell.max()) + 1, C.c_double(g["dt"]), C.c_double(g["particle_volume"]),
+                                       C.byref(res))
+    assert rc == 0, oracle_lib.orc_last_error()
+    assert np.allclose(occ, g["occ_out"], rtol=1e-12, atol=1e-15)
+    assert abs(res.value - g["residual"]) < 1e-13
+
+
+def test_callaway_evolve(oracle_lib):
+    g = golden("callaway_evolve")
+    for case in g["cases"]:
+        n = len(case["omega"])
+        out = np.zeros(n)
+        args = [_f64(case[k]) for k in ("omega", "capacity", "wavevector", "normal_rate", "resistive_rate", "energy")]
+        rc = oracle_lib.orc_callaway_evolve(n, *[D(a) for a in args], C.c_double(case["dt"]), D(out))
+        assert rc == 0
+        ref = np.asarray(case["evolved"])
+        assert np.allclose(out, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("name,conservative", [("rough_nonconservative", 0), ("rough_conservative", 1)])
+def test_rough_reflection(oracle_lib, m8, name, conservative):
+    g = golden(name)
+    m = _mat(oracle_lib, m8, bool(conservative))
+    draws = _f64(g["draws"]).reshape(-1, 3)
+    facet = np.asarray(g["facet"])
+    for f, (normal, rough) in enumerate([((0, 0, -1), 10.0), ((0, 0, 1), 3.0)]):
+        sel = facet == f
+        fin = _i32(np.asarray(g["in_flat"])[sel])
+        oin = _f64(np.asarray(g["in_occ"])[sel])
+        u = _f64(np.clip(draws[sel], 0, None))
+        fo = np.zeros(fin.size, dtype=np.int32)
+        oo = np.zeros(fin.size)
+        rc = oracle_lib.orc_rough_reflect(m.h, conservative, C.c_double(300.0), D(_f64(normal)), C.c_double(rough),
+                                          fin.size, I32(fin), D(oin), D(u), I32(fo), D(oo))
+        assert rc == 0
+        assert np.array_equal(fo, np.asarray(g["out_flat"])[sel])
+        assert np.array_equal(oo, np.asarray(g["out_occ"])[sel])
+
+
+def test_gradient_drive(oracle_lib, m8):
+    g = golden("gradient_drive")
+    m = _mat(oracle_lib, m8, True)
+    flat, cell = _i32(g["flat"]), _i32(g["cell"])
+    occ = _f64(g["occ_in"]).copy()
+    e = C.c_double()
+    rc = oracle_lib.orc_gradient_drive(m.h, 0, C.c_double(g["gradient"]), C.c_double(300.0), flat.size, I32(flat),
+                                       I32(cell), D(occ), 4, C.c_double(g["dt"]), C.c_double(g["particle_volume"]),
+                                       C.byref(e))
+    assert rc == 0
+    assert np.array_equal(occ, np.asarray(g["occ_out"]))
+    assert abs(e.value - g["energy"]) < 1e-15
+
+
+def test_reservoir_cdf(oracle_lib, m8):
+    g = golden("reservoir")
+    m = _mat(oracle_lib, m8)
+    na = m8.qpoints  # upper bound for buffer
+    cdf = np.zeros(6 * na)
+    exp = C.c_double()
+    init = C.c_int32()
+    counts = []
+    for r, normal in enumerate([(0, 0, -1), (0, 0, 1)]):
+        rc = oracle_lib.orc_reservoir_cdf(m.h, D(_f64(normal)), C.c_double(g["area"]), C.c_double(g["density"]),
+                                          C.c_double(g["dt"]), D(cdf), C.byref(exp), C.byref(init))
+        assert rc == 0
+        counts.append(init.value)
+        draws = np.asarray(g["draw"])[r * 300:(r + 1) * 300]
+        active = 1512
+        idx = np.searchsorted(cdf[:active], draws, side="left")
+        idx = np.minimum(idx, active - 1)
+        assert np.array_equal(idx, np.asarray(g["active_index"])[r * 300:(r + 1) * 300])
+    assert counts == g["initial_count"]
