@@ -1,0 +1,261 @@
+"""Throughput of the PhonoMC carrier loop on one GB300: carrier-steps/s.
+
+Default workload: in-plane periodic-gradient film (100 nm thick, rough 1 nm
+walls, G = 1e7 K/m, 100 z-cells, linearized RTA at 300 K, dt = 0.5 ps) with
+5e7 carriers on the seeded synthetic 16^3 x 6 phonon table. A step is one
+MonteCarloSolver timestep over every carrier. Carrier state (>= 2 GB) is far
+larger than the 129 MB L2, so timed steps do not run from cache.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                  [--workload inplane_gradient|cross_plane_film] [--particles P]
+                  [--precision fp64|mixed]
+
+Prints one JSON line. `--impl reference` times the CPU restatement of the
+reference algorithm (oracle/, the reference's own C++ cannot be built on the
+GPU host) on the host cores: independent replicas, one per core.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "carrier-steps/s on 1 GB300: batched mixed-prec vs plain FP64 at equal kappa error"
+UNIT = "carrier-steps/s"
+# Algorithmic bytes per carrier-step of the transport pass: read position,
+# occupation, mode and cell; write position, occupation and cell.
+BYTES_PER_CARRIER = {"fp64": 76, "mixed": 52}
+
+
+def workload_config(name, particles, precision, seed=12345):
+    from phonomc_gb300 import workloads
+    base = getattr(workloads, name)()
+    return workloads.scaled(base, particles, random_seed=seed, precision=precision)
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", "0"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                         text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, name in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def _oracle_replica(args):
+    """One CPU replica of the workload sample (separate process): init, warm-up
+    steps, then `samples` timed windows of `steps` timesteps each."""
+    name, particles, steps, samples, warmup, seed = args
+    import oracle
+    from phonomc_gb300 import abi, synthetic
+    lib = oracle.load()
+    cfg = workload_config(name, particles, "fp64", seed)
+    stationary = name == "inplane_gradient"
+    m = abi.Material(lib, "orc_", synthetic.make_material(mesh=16), 0.1, stationary, False)
+    s = abi.Solver(lib, "orc_", cfg, [m])
+    s.run(max(1, warmup))
+    cs, dt = 0, 0.0
+    for _ in range(samples):
+        n0 = s.stats()["particle_count"]
+        t0 = time.perf_counter()
+        s.run(steps)
+        dt += time.perf_counter() - t0
+        cs += 0.5 * (n0 + s.stats()["particle_count"]) * steps
+    return cs, dt
+
+
+def cpu_baseline(name, particles, steps, samples, warmup, procs):
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs) as pool:
+        res = pool.map(_oracle_replica, [(name, particles, steps, samples, warmup, 1000 + k) for k in range(procs)])
+    cs = sum(r[0] for r in res)
+    busy = max(r[1] for r in res)
+    return cs / busy, {"carrier_steps": cs, "busy_s": busy}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    procs = max(1, os.cpu_count() or 1)
+    particles, steps = 20000, 4
+    name = args.workload
+    value, info = cpu_baseline(name, particles, steps, args.steps, args.warmup, procs)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * info["busy_s"] / (args.steps * steps),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": name, "particles_per_replica": particles, "replicas": procs,
+                   "timesteps_per_step": steps},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
+                         "sample": f"{procs} independent replicas x {particles} carriers, {steps} timesteps per step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    import phonomc_gb300
+    from phonomc_gb300 import abi, synthetic
+    lib = phonomc_gb300.lib()
+    cfg = workload_config(args.workload, args.particles, args.precision, seed=12345 + rank)
+    stationary = args.workload == "inplane_gradient"
+    m = abi.Material(lib, "phmc_", synthetic.make_material(mesh=16), 0.1, stationary, False)
+    s = abi.Solver(lib, "phmc_", cfg, [m])
+    s.run(args.warmup)
+    n_carriers = s.stats()["particle_count"]
+    tot, kern, launches = C.c_double(), C.c_double(), C.c_int64()
+    with ClockSampler() as clk:
+        s.check(lib.phmc_solver_timed_run(s.h, args.steps, C.byref(tot), C.byref(kern), C.byref(launches)))
+    st = s.stats()
+    n_after = st["particle_count"]
+    carrier_steps = 0.5 * (n_carriers + n_after) * args.steps
+    ms = tot.value
+    value_rank = carrier_steps / (ms * 1e-3)
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        dist.init_process_group("gloo")
+        t = torch.tensor([ms, carrier_steps], dtype=torch.float64)
+        mx = t.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        sm = t.clone()
+        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+        ms = float(mx[0])
+        carrier_steps = float(sm[1])
+    value = carrier_steps / (ms * 1e-3)
+    bpc = BYTES_PER_CARRIER[args.precision]
+    kavg = kern.value / args.steps
+    achieved = bpc * n_carriers / (kavg * 1e-3) / 1e9
+    peak, peak_kind = measured_peak()
+
+    # end to end through the C ABI from pinned host buffers
+    c = s.carriers()
+    live = c["alive"] == 1
+    host = {k: np.ascontiguousarray(c[k][live]) for k in ("x", "y", "z", "occ")}
+    host["mode"] = np.ascontiguousarray(c["mode"][live])
+    n = host["x"].size
+    for a in host.values():
+        lib.phmc_host_register(a.ctypes.data, a.nbytes)
+    Tout = np.zeros(s.cells()[0].size)
+    e2e_steps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        s.check(lib.phmc_solver_run_from_host(s.h, n, abi.dptr(host["x"]), abi.dptr(host["y"]), abi.dptr(host["z"]),
+                                              abi.dptr(host["occ"]), host["mode"].ctypes.data_as(abi.c_uint32_p), 1,
+                                              abi.dptr(Tout)))
+    e2e_s = time.perf_counter() - t0
+    for a in host.values():
+        lib.phmc_host_unregister(a.ctypes.data)
+    e2e_value = n * e2e_steps / e2e_s * (world if world > 1 else 1)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
+        "config": {"workload": args.workload, "particles": int(args.particles), "precision": args.precision,
+                   "material": "synthetic 16^3 x 6 modes (seed 0)", "cells": int(Tout.size),
+                   "l2": "carrier state larger than L2 (no flush needed)", "replicas": world},
+        "gpu_launches": int(launches.value),
+        "roofline": {"bound": "hbm", "kernel": "k_transport (pass A)", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                     "bytes_per_carrier": bpc, "kernel_ms_per_launch": kavg, "traffic": None},
+        "e2e": {"value": e2e_value, "unit": UNIT,
+                "h2d_bytes_per_step": int(n * (4 * 8 + 4)), "d2h_bytes_per_step": int(Tout.size * 8)},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        cb, info = cpu_baseline(args.workload, 200000, 10, 3, 1, 1)
+        line["cpu_baseline"] = {"value": cb, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": f"{args.workload}, 200000 carriers x 30 timed steps, serial CPU oracle"}
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="inplane_gradient", choices=["inplane_gradient", "cross_plane_film"])
+    ap.add_argument("--particles", type=float, default=None)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.particles is None:
+        args.particles = 5e7 if args.workload == "inplane_gradient" else 1e6
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -138,6 +138,13 @@ int phmc_solver_set_carriers(phmc_solver* s, int64_t n, const double* x, const d
 int phmc_solver_run_from_host(phmc_solver* s, int64_t n, const double* x, const double* y, const double* z,
                               const double* occupation, const uint32_t* mode_word, int steps,
                               double* cell_temperature_out);
+/* Runs `steps` timesteps bracketed by CUDA events on the solver's stream:
+ * total_ms is the device time of the region, kernel_ms the summed duration of
+ * its transport-pass launches, launches the number of kernels launched. */
+int phmc_solver_timed_run(phmc_solver* s, int steps, double* total_ms, double* kernel_ms, int64_t* launches);
+/* Page-lock / release caller-owned host buffers used for end-to-end stepping. */
+int phmc_host_register(void* ptr, int64_t bytes);
+int phmc_host_unregister(void* ptr);
 int phmc_solver_write_outputs(phmc_solver* s);
 void phmc_solver_destroy(phmc_solver* s);
 

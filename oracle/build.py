@@ -30,7 +30,7 @@ def build(force: bool = False) -> str:
     if force or _stale():
         os.makedirs(os.path.dirname(OUT), exist_ok=True)
         tmp = OUT + f".{os.getpid()}.tmp"
-        subprocess.run(["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared", "-Wno-unknown-pragmas",
+        subprocess.run(["g++", "-O3", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-Wno-unknown-pragmas",
                         *SOURCES, "-o", tmp], check=True)
         os.replace(tmp, OUT)
     return OUT

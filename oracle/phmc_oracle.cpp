@@ -887,6 +887,10 @@ int orc_solver_set_carriers(void* sp, int64_t n, const double* x, const double* 
         s->cell.resize(n);
         for (int64_t i = 0; i < n; ++i) s->cell[i] = s->domain->fast_grid_index({x[i], y[i], z[i]});
         s->refresh();
+        s->energy.initialize(s->total_thermal());
+        for (size_t r = 0; r < s->P.reservoirs.size(); ++r) s->prev_absorbed[r] = s->P.reservoirs[r].initial_count;
+        s->step = 0;
+        s->elapsed = 0;
     });
 }
 

@@ -311,6 +311,9 @@ DEVICE_PROTOS = {
     "solver_run_timestep": (C.c_int, [C.c_void_p]),
     "solver_synchronize": (C.c_int, [C.c_void_p]),
     "solver_write_outputs": (C.c_int, [C.c_void_p]),
+    "solver_timed_run": (C.c_int, [C.c_void_p, C.c_int, c_double_p, c_double_p, c_int64_p]),
+    "host_register": (C.c_int, [C.c_void_p, C.c_int64]),
+    "host_unregister": (C.c_int, [C.c_void_p]),
     "solver_run_from_host": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_double_p, c_double_p, c_double_p,
                                        c_uint32_p, C.c_int, c_double_p]),
     **{"dev_" + k: v for k, v in SUBSTEP_PROTOS.items()},

@@ -1,0 +1,362 @@
+// extern "C" boundary of libphonomc_gb300.so (declared in include/phonomc_gb300.h).
+// Exceptions never cross it: every entry point returns 0 or 1 and stores the
+// message for phmc_last_error().
+#include "phmc_kernels.cuh"
+#include "phmc_pod.h"
+
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+using namespace phmc;
+
+struct phmc_material {
+    std::unique_ptr<PhononMaterial> m;
+};
+
+struct phmc_solver {
+    std::unique_ptr<DeviceSolver> s;
+};
+
+namespace {
+thread_local std::string g_error;
+
+template <class F> int guard(F&& f) {
+    try {
+        f();
+        return 0;
+    } catch (const std::exception& e) {
+        g_error = e.what();
+        return 1;
+    } catch (...) {
+        g_error = "unknown error";
+        return 1;
+    }
+}
+
+void cuda_check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw std::runtime_error(std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));
+}
+
+template <class T> struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    explicit DBuf(size_t count) : n(count) { cuda_check(cudaMalloc(&p, std::max<size_t>(1, n) * sizeof(T)), "cudaMalloc"); }
+    DBuf(const T* host, size_t count) : DBuf(count) {
+        if (count) cuda_check(cudaMemcpy(p, host, count * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy");
+    }
+    explicit DBuf(const std::vector<T>& v) : DBuf(v.data(), v.size()) {}
+    void get(T* host) const {
+        if (n) cuda_check(cudaMemcpy(host, p, n * sizeof(T), cudaMemcpyDeviceToHost), "cudaMemcpy");
+    }
+    ~DBuf() { cudaFree(p); }
+    DBuf(const DBuf&) = delete;
+};
+
+__global__ void k_trace_rays(DevDomain D, int64_t n, const double* p3, const double* v3, double* hit3, double* t,
+                             int32_t* facet) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const double p[3] = {p3[3 * i], p3[3 * i + 1], p3[3 * i + 2]};
+        const double v[3] = {v3[3 * i], v3[3 * i + 1], v3[3 * i + 2]};
+        double cp[3], tt;
+        int f;
+        trace_box(D, p, v, cp, tt, f);
+        for (int a = 0; a < 3; ++a) hit3[3 * i + a] = f >= 0 ? cp[a] : p[a];
+        t[i] = tt;
+        facet[i] = f;
+    }
+}
+
+__global__ void k_inverse_table(const double* E, const double* T, int nt, int64_t n, const double* e, double* out) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        out[i] = table_inverse(E, T, nt, e[i]);
+}
+
+__global__ void k_rough_rays(DevRoughTable R, DevMaterial M, int conservative, int64_t n, const int32_t* ain,
+                             const double* occ, const double* u3, int32_t* aout, double* oout) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        double o;
+        aout[i] = rough_sample_dev(R, M, ain[i], occ[i], conservative != 0, u3[3 * i], u3[3 * i + 1], u3[3 * i + 2], o);
+        oout[i] = o;
+    }
+}
+
+// A one-material periodic column of `cells` cells whose particle volume is `vol`,
+// used to run the solver's own collision/drive kernels on given carriers.
+SimulationConfig column_config(int64_t n, int cells, double vol, double dt, double Tbg) {
+    SimulationConfig c;
+    c.sizes = {1.0, 1.0, vol * static_cast<double>(n)};
+    c.particle_count = static_cast<double>(n);
+    c.time_step = dt;
+    c.grid = {1, 1, cells};
+    c.face_condition = {'P', 'P', 'P', 'P', 'P', 'P'};
+    c.face_value = {0, 0, 0, 0, 0, 0};
+    c.background_temperature = Tbg;
+    c.transport_axis = 0;
+    return c;
+}
+
+void load_column(DeviceSolver& s, const PhononMaterial& M, const SimulationConfig& c, int64_t n, const int32_t* flat,
+                 const int32_t* cell, const double* occ) {
+    std::vector<double> x(n, 0.5), y(n, 0.5), z(n);
+    std::vector<uint32_t> mode(n);
+    std::vector<uint8_t> alive(n, 1);
+    const double dz = c.sizes[2] / c.grid[2];
+    for (int64_t i = 0; i < n; ++i) {
+        if (cell[i] < 0 || cell[i] >= c.grid[2]) throw std::invalid_argument("carrier cell out of range");
+        z[i] = (cell[i] + 0.5) * dz;
+        const int a = M.active_index_for_flat(flat[i]);
+        if (a < 0) throw std::invalid_argument("Invalid existing collision carrier.");
+        mode[i] = static_cast<uint32_t>(a);
+    }
+    s.set_carriers(n, x.data(), y.data(), z.data(), occ, mode.data(), alive.data());
+}
+
+void read_occupations(DeviceSolver& s, int64_t n, double* occ) {
+    std::vector<double> x(n), y(n), z(n);
+    std::vector<uint32_t> mode(n);
+    std::vector<int32_t> cell(n);
+    std::vector<uint8_t> alive(n);
+    s.get_carriers(x.data(), y.data(), z.data(), occ, mode.data(), cell.data(), alive.data());
+}
+} // namespace
+
+extern "C" {
+
+const char* phmc_last_error(void) { return g_error.c_str(); }
+
+int phmc_device_count(int* count) {
+    return guard([&] {
+        int n = 0;
+        if (cudaGetDeviceCount(&n) != cudaSuccess) n = 0;
+        *count = n;
+    });
+}
+
+int phmc_material_create(const phmc_material_data* data, double dt, int stationary, int complete_bz,
+                         phmc_material** out) {
+    return guard([&] {
+        auto m = std::make_unique<phmc_material>();
+        m->m = std::make_unique<PhononMaterial>(material_from_pod(*data), dt, stationary != 0, complete_bz != 0);
+        *out = m.release();
+    });
+}
+
+void phmc_material_destroy(phmc_material* m) { delete m; }
+
+int phmc_material_active_count(const phmc_material* m, int* n) {
+    return guard([&] { *n = m->m->active_mode_count(); });
+}
+
+int phmc_solver_create(const phmc_config* cfg, phmc_material* const* materials, int n_materials, phmc_solver** out) {
+    return guard([&] {
+        if (cfg->precision != 0) throw std::invalid_argument("mixed precision state is built by phmc_solver_create only with precision=0 in this build");
+        SimulationConfig c = config_from_pod(*cfg);
+        std::vector<const PhononMaterial*> ms;
+        for (int i = 0; i < n_materials; ++i) ms.push_back(materials[i]->m.get());
+        auto s = std::make_unique<phmc_solver>();
+        s->s = std::make_unique<DeviceSolver>(c, ms);
+        *out = s.release();
+    });
+}
+
+int phmc_solver_run_timestep(phmc_solver* s) {
+    return guard([&] {
+        s->s->run_timestep();
+        s->s->synchronize();
+    });
+}
+
+int phmc_solver_run(phmc_solver* s, int steps) {
+    return guard([&] {
+        s->s->run(steps);
+        s->s->synchronize();
+    });
+}
+
+int phmc_solver_synchronize(phmc_solver* s) { return guard([&] { s->s->synchronize(); }); }
+
+int phmc_solver_stats(phmc_solver* s, phmc_stats* out) { return guard([&] { s->s->read_stats(*out); }); }
+
+int phmc_solver_cell_count(const phmc_solver* s, int* cells) {
+    return guard([&] { *cells = s->s->cell_count(); });
+}
+
+int phmc_solver_cells(phmc_solver* s, double* T, double* E, double* q3) {
+    return guard([&] { s->s->read_cells(T, E, q3); });
+}
+
+int phmc_solver_slot_count(phmc_solver* s, int64_t* n) { return guard([&] { *n = s->s->slot_count(); }); }
+
+int phmc_solver_get_carriers(phmc_solver* s, double* x, double* y, double* z, double* occ, uint32_t* mode,
+                             int32_t* cell, uint8_t* alive) {
+    return guard([&] { s->s->get_carriers(x, y, z, occ, mode, cell, alive); });
+}
+
+int phmc_solver_set_carriers(phmc_solver* s, int64_t n, const double* x, const double* y, const double* z,
+                             const double* occ, const uint32_t* mode, const uint8_t* alive) {
+    return guard([&] { s->s->set_carriers(n, x, y, z, occ, mode, alive); });
+}
+
+int phmc_solver_run_from_host(phmc_solver* s, int64_t n, const double* x, const double* y, const double* z,
+                              const double* occ, const uint32_t* mode, int steps, double* cell_T) {
+    return guard([&] {
+        s->s->set_carriers(n, x, y, z, occ, mode, nullptr);
+        s->s->run(steps);
+        s->s->read_cells(cell_T, nullptr, nullptr);
+    });
+}
+
+int phmc_solver_timed_run(phmc_solver* s, int steps, double* total_ms, double* kernel_ms, int64_t* launches) {
+    return guard([&] {
+        long long l = 0;
+        s->s->timed_run(steps, *total_ms, *kernel_ms, l);
+        *launches = l;
+    });
+}
+
+int phmc_host_register(void* ptr, int64_t bytes) {
+    return guard([&] { cuda_check(cudaHostRegister(ptr, static_cast<size_t>(bytes), cudaHostRegisterDefault), "cudaHostRegister"); });
+}
+
+int phmc_host_unregister(void* ptr) {
+    return guard([&] { cuda_check(cudaHostUnregister(ptr), "cudaHostUnregister"); });
+}
+
+int phmc_solver_write_outputs(phmc_solver* s) { return guard([&] { s->s->write_outputs(); }); }
+
+void phmc_solver_destroy(phmc_solver* s) { delete s; }
+
+// ------------------------------------------------------------- sub-steps
+int phmc_dev_trace_box(const double lo[3], const double hi[3], int64_t n, const double* p3, const double* v3,
+                       double* hit3, double* t, int32_t* facet) {
+    return guard([&] {
+        DevDomain D{};
+        double scale = 1.0;
+        for (int a = 0; a < 3; ++a) {
+            D.lo[a] = lo[a];
+            D.hi[a] = hi[a];
+            scale = std::max(scale, std::abs(hi[a] - lo[a]));
+        }
+        D.scale = scale;
+        D.tol = std::max(1e-9, 64.0 * std::numeric_limits<double>::epsilon() * scale);
+        DBuf<double> dp(p3, 3 * n), dv(v3, 3 * n), dh(3 * n), dt(n);
+        DBuf<int32_t> df(n);
+        k_trace_rays<<<256, 256>>>(D, n, dp.p, dv.p, dh.p, dt.p, df.p);
+        cuda_check(cudaDeviceSynchronize(), "k_trace_rays");
+        dh.get(hit3);
+        dt.get(t);
+        df.get(facet);
+    });
+}
+
+int phmc_dev_temperature_from_energy(const phmc_material* m, int64_t n, const double* energy, double* temperature) {
+    return guard([&] {
+        DBuf<double> E(m->m->lookup_E()), T(m->m->lookup_T()), e(energy, n), out(n);
+        k_inverse_table<<<256, 256>>>(E.p, T.p, static_cast<int>(E.n), n, e.p, out.p);
+        cuda_check(cudaDeviceSynchronize(), "k_inverse_table");
+        out.get(temperature);
+    });
+}
+
+int phmc_dev_rta_collide(const phmc_material* m, int64_t n, const int32_t* flat, const int32_t* cell, double* occ,
+                         int cells, const double* cell_T, double dt, double vol, int local, double Tlife,
+                         double* residual) {
+    return guard([&] {
+        SimulationConfig c = column_config(n, cells, vol, dt, 300.0);
+        c.lifetime_temperature_is_local = local != 0;
+        c.lifetime_temperature = Tlife;
+        DeviceSolver s(c, {m->m.get()}, false);
+        load_column(s, *m->m, c, n, flat, cell, occ);
+        *residual = s.collide_only(cell_T);
+        read_occupations(s, n, occ);
+    });
+}
+
+int phmc_dev_linear_collide(const phmc_material* m, int model, double Tref, int64_t n, const int32_t* flat,
+                            const int32_t* cell, double* occ, int cells, double dt, double vol, double* residual) {
+    return guard([&] {
+        SimulationConfig c = column_config(n, cells, vol, dt, Tref);
+        c.lifetime_temperature_is_local = false;
+        c.lifetime_temperature = Tref;
+        if (model == 1) c.collision_model = CollisionModel::Callaway;
+        else c.temperature_gradient = 0.0; // linearized RTA, no drive
+        DeviceSolver s(c, {m->m.get()}, false);
+        load_column(s, *m->m, c, n, flat, cell, occ);
+        *residual = s.collide_only(nullptr);
+        read_occupations(s, n, occ);
+    });
+}
+
+int phmc_dev_gradient_drive(const phmc_material* m, int axis, double G, double Tref, int64_t n, const int32_t* flat,
+                            const int32_t* cell, double* occ, int cells, double dt, double vol, double* energy) {
+    return guard([&] {
+        SimulationConfig c = column_config(n, cells, vol, 2.0 * dt, Tref);
+        c.lifetime_temperature_is_local = false;
+        c.lifetime_temperature = Tref;
+        c.temperature_gradient = G;
+        c.transport_axis = axis;
+        DeviceSolver s(c, {m->m.get()}, false);
+        load_column(s, *m->m, c, n, flat, cell, occ);
+        *energy = s.drive_only();
+        read_occupations(s, n, occ);
+    });
+}
+
+int phmc_dev_rough_reflect(const phmc_material* m, int conservative, double Tref, const double nout[3],
+                           double rough_a, int64_t n, const int32_t* flat_in, const double* occ_in, const double* u3,
+                           int32_t* flat_out, double* occ_out) {
+    return guard([&] {
+        const PhononMaterial& M = *m->m;
+        RoughTables rt;
+        rt.build({&M}, {{nout[0], nout[1], nout[2]}}, {rough_a}, {1}, conservative != 0, conservative ? Tref : 0.0);
+        const RoughTable& R = rt.tables.at(0);
+        DBuf<double> spec(R.specularity), prefix(R.residual_prefix), rcdf(R.roulette_cdf);
+        DBuf<int> match(R.spec_match), db(R.diffuse_begin), de(R.diffuse_end), sorted(R.outgoing_sorted),
+            ract(R.roulette_active), oact(R.outgoing_active);
+        DevRoughTable D{};
+        D.strict = R.strict_elastic;
+        D.n_sorted = static_cast<int>(R.outgoing_sorted.size());
+        D.n_roulette = static_cast<int>(R.roulette_active.size());
+        D.n_outgoing = static_cast<int>(R.outgoing_active.size());
+        D.specularity = spec.p;
+        D.spec_match = match.p;
+        D.diffuse_begin = db.p;
+        D.diffuse_end = de.p;
+        D.outgoing_sorted = sorted.p;
+        D.prefix = prefix.p;
+        D.roulette_active = ract.p;
+        D.roulette_cdf = rcdf.p;
+        D.outgoing_active = oact.p;
+        std::vector<double> om(M.active_mode_count()), nb(M.active_mode_count());
+        for (int a = 0; a < M.active_mode_count(); ++a) {
+            om[a] = M.omega(M.active_flat()[a]);
+            nb[a] = M.bose_occupation(Tref, M.active_flat()[a]);
+        }
+        DBuf<double> dom(om), dnb(nb);
+        DevMaterial DM{};
+        DM.n_active = M.active_mode_count();
+        DM.omega = dom.p;
+        DM.nbg = dnb.p;
+        std::vector<int32_t> ain(n);
+        for (int64_t i = 0; i < n; ++i) {
+            ain[i] = M.active_index_for_flat(flat_in[i]);
+            if (ain[i] < 0) throw std::invalid_argument("incoming mode is not active");
+        }
+        DBuf<int32_t> dain(ain), daout(n);
+        DBuf<double> docc(occ_in, n), du(u3, 3 * n), dout(n);
+        k_rough_rays<<<128, 256>>>(D, DM, conservative, n, dain.p, docc.p, du.p, daout.p, dout.p);
+        cuda_check(cudaDeviceSynchronize(), "k_rough_rays");
+        std::vector<int32_t> aout(n);
+        daout.get(aout.data());
+        dout.get(occ_out);
+        for (int64_t i = 0; i < n; ++i) flat_out[i] = M.active_flat()[aout[i]];
+    });
+}
+
+} // extern "C"

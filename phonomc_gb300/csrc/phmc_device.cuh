@@ -1,0 +1,423 @@
+// Device-side data layout and per-carrier functions of the carrier loop.
+//
+// Carriers are structure-of-arrays in HBM, one slot per carrier:
+//   x, y, z  float64 absolute position (plain path) or
+//   ox,oy,oz float32 offset from the cell origin (mixed path)
+//   occ      float64 occupation
+//   mode     uint32  active index | velocity sign bits << 24 | material << 28
+//   cell     int32   grid cell
+//   alive    uint8   0 for an absorbed (free) slot
+// The velocity is never stored: it is the mode's group velocity with the sign
+// bits applied, which reproduces the reference's velocity bit-for-bit on an
+// axis-aligned box (specular reflection and reservoir inversion only flip
+// signs; src/solver/BoundaryInteraction.cpp:146-159,
+// src/solver/ReservoirInjector.cpp:97-102).
+#pragma once
+#include <cstdint>
+
+#include "phmc_rng.h"
+
+namespace phmc {
+
+constexpr int kMaxMaterials = 4;
+constexpr int kMaxRoughTables = 24;
+constexpr int kMaxReservoirs = 6;
+constexpr double kHbar = 6.582119569e-4;
+constexpr double kKb = 8.617333262145e-5;
+
+enum ErrorCode : int {
+    kErrNone = 0,
+    kErrIntersection = 1,
+    kErrModeMapping = 2,
+    kErrTooManyEvents = 3,
+    kErrInvalidStatistics = 4,
+    kErrEscaped = 5,
+    kErrZeroFluxReservoir = 6,
+    kErrCapacity = 7,
+    kErrOutwardReservoirMode = 8,
+    kErrNonFinite = 9,
+    kErrNoRoughTable = 10,
+    kErrCollision = 11,
+};
+
+struct DevMaterial {
+    int n_active;
+    int n_classes;
+    int n_lookup;
+    int n_temps;
+    const double* omega;    // [active]
+    const double* hw;       // [active]
+    const double* inv_hw;   // [active]
+    const double* vel;      // [active*3]
+    const float* vel32;     // [active*4] (x, y, z, |v|) for the mixed path
+    const double* nbg;      // [active]
+    const double* cap_bg;   // [active]
+    const int* mode_class;  // [active]
+    const double* class_omega;
+    const double* class_hw;
+    const int* class_rep;
+    const double* relax_fixed; // [active]
+    const double* temps;       // [n_temps]
+    const double* gamma;       // [n_temps * active]
+    const double* lookup_T;
+    const double* lookup_E;
+    const double* col_cap;     // [active]
+    const double* col_rate;    // total collision rate [active]
+    const double* col_rn;      // normal rate [active]
+    const double* col_rr;      // resistive rate [active]
+    const double* col_k;       // [active*3]
+    const double* grad_rate;   // [active]
+    double energy_weight;
+    double energy_density_bg;
+    double heat_capacity_density_bg;
+    double zero_point;
+};
+
+struct DevRoughTable {
+    int strict;
+    int n_sorted, n_roulette, n_outgoing;
+    const double* specularity;
+    const int* spec_match;
+    const int* diffuse_begin;
+    const int* diffuse_end;
+    const int* outgoing_sorted;
+    const double* prefix;
+    const int* roulette_active;
+    const double* roulette_cdf;
+    const int* outgoing_active;
+};
+
+struct DevReservoir {
+    int facet, material, n_cdf;
+    double expected;
+    double normal[3];
+    double tri[2][3][3];
+    double area0, area1;
+    const double* cdf;
+    const double* occ; // emitted occupation per active mode
+};
+
+struct DevDomain {
+    double lo[3], hi[3], inv_cell[3], cell_size[3];
+    int shape[3];
+    int ncells;
+    double tol;        // analytic-box position tolerance
+    double scale;      // max(1, extents)
+    char cond[6];
+    double shift[6][3];
+    int pair[6];
+    int reservoir[6];
+    int rough_table[kMaxMaterials][6];
+    // layered materials
+    int layout_axis;
+    int n_planes;
+    double planes[kMaxMaterials];
+};
+
+struct DevParams {
+    double dt;
+    double push_eps;
+    uint64_t seed;
+    int conservative;
+    int linearized;
+    int one_to_one;
+    int n_materials;
+    int n_reservoirs;
+    int lifetime_local;
+    double lifetime_T;
+    double background_T;
+    int gradient_axis;
+    double gradient_energy_weight;
+};
+
+// Per-step accumulators and running totals, all on the device so a step needs
+// no host round trip (src/solver/BoundaryLedger.cpp, src/solver/EnergyLedger.cpp).
+struct DevLedger {
+    int error_code;
+    int error_slot;
+    int n_slots;            // slots in use [0, n_slots)
+    int n_holes;            // free slots below n_slots at injection
+    int n_inject;           // carriers injected this step
+    int inject_count[kMaxReservoirs];
+    int inject_offset[kMaxReservoirs + 1];
+    unsigned int absorbed_res[kMaxReservoirs];  // this step
+    unsigned int previous_res[kMaxReservoirs];  // previous step (one-to-one refill)
+    unsigned long long step_absorbed, step_injected;
+    double step_absorbed_ev, step_injected_ev;
+    double step_lifetime_residual, step_drive_ev;
+    unsigned long long step_drive_updates;
+    double step_balance_residual;
+    double thermal_energy;
+    // totals
+    unsigned long long total_absorbed, total_injected;
+    double total_absorbed_ev, total_injected_ev, total_lifetime_residual, total_balance_residual, total_drive_ev;
+    unsigned long long total_drive_updates;
+    long long particle_count;
+};
+
+struct DevTables {
+    DevMaterial mat[kMaxMaterials];
+    DevRoughTable rough[kMaxRoughTables];
+    DevReservoir res[kMaxReservoirs];
+    DevDomain dom;
+    DevParams par;
+};
+
+struct CarrierState {
+    double* x;
+    double* y;
+    double* z;
+    float* ox;
+    float* oy;
+    float* oz;
+    double* occ;
+    uint32_t* mode;
+    int32_t* cell;
+    uint8_t* alive;
+    int capacity;
+};
+
+// ------------------------------------------------------------ helpers
+__device__ __forceinline__ void raise_error(DevLedger* L, int code, int slot) {
+    if (atomicCAS(&L->error_code, 0, code) == 0) L->error_slot = slot;
+}
+
+__device__ __forceinline__ double bose_dev(double T, double w) {
+    if (T <= 0.0 || w <= 0.0) return 0.0;
+    const double x = kHbar * w / (kKb * T);
+    if (x > 700.0) return 0.0;
+    return 1.0 / fmax(exp(x) - 1.0, 1e-12);
+}
+
+__device__ __forceinline__ int grid_index(const DevDomain& D, double px, double py, double pz) {
+    const double p[3] = {px, py, pz};
+    int idx[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int n = D.shape[a];
+        if (n <= 1) {
+            idx[a] = 0;
+        } else {
+            int i = static_cast<int>(floor((p[a] - D.lo[a]) * D.inv_cell[a]));
+            idx[a] = i < 0 ? 0 : (i >= n ? n - 1 : i);
+        }
+    }
+    return (idx[0] * D.shape[1] + idx[1]) * D.shape[2] + idx[2];
+}
+
+__device__ __forceinline__ int material_at(const DevDomain& D, const double p[3]) {
+    int m = 0;
+    while (m < D.n_planes && p[D.layout_axis] >= D.planes[m]) ++m;
+    return m;
+}
+
+// Analytic box trace (src/SimulationDomain.cpp:399-450); facet -1 on a miss.
+__device__ __forceinline__ void trace_box(const DevDomain& D, const double p[3], const double v[3], double cp[3],
+                                          double& t, int& facet) {
+    const double inf = __longlong_as_double(0x7ff0000000000000LL);
+    t = inf;
+    facet = -1;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        cp[a] = p[a];
+        if (!isfinite(p[a]) || p[a] < D.lo[a] - D.tol || p[a] > D.hi[a] + D.tol) return;
+    }
+    double best = inf;
+    int plane = -1;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const double c = v[a];
+        if (!isfinite(c) || fabs(c) <= 1e-18) continue;
+        const int side = c > 0.0 ? 1 : 0;
+        const double target = side ? D.hi[a] : D.lo[a];
+        const double h = (target - p[a]) / c;
+        if (isfinite(h) && h > 1e-14 && h < best) {
+            best = h;
+            plane = 2 * a + side;
+        }
+    }
+    if (plane < 0) return;
+    double c[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) c[a] = __fma_rn(v[a], best, p[a]);
+    const int ha = plane >> 1;
+    c[ha] = (plane & 1) ? D.hi[ha] : D.lo[ha];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (!isfinite(c[a]) || c[a] < D.lo[a] - D.tol || c[a] > D.hi[a] + D.tol) return;
+        c[a] = fmin(fmax(c[a], D.lo[a]), D.hi[a]);
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) cp[a] = c[a];
+    t = best;
+    facet = plane;
+}
+
+__device__ __forceinline__ bool box_contains(const DevDomain& D, const double p[3]) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        if (!(p[a] >= D.lo[a] && p[a] <= D.hi[a])) return false;
+    return true;
+}
+
+// Wall-hit cache with the reference's nudged retries (src/solver/TransportOperator.cpp:186-250).
+__device__ __forceinline__ bool cache_hit(const DevDomain& D, const DevParams& P, double p[3], const double v[3], double cp[3],
+                          double& t, int& f) {
+    const double speed = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    if (isfinite(speed) && speed <= 1e-18) {
+        t = __longlong_as_double(0x7ff0000000000000LL);
+        f = -1;
+        return true;
+    }
+    trace_box(D, p, v, cp, t, f);
+    if (f >= 0 && isfinite(t)) return true;
+    const double eps = fmax(P.push_eps, 1e-10 * D.scale);
+    int nearest = 0;
+    double bd = 1e300;
+    for (int k = 0; k < 6; ++k) {
+        const int a = k >> 1;
+        const double d = fabs(p[a] - ((k & 1) ? D.hi[a] : D.lo[a]));
+        if (d < bd) {
+            bd = d;
+            nearest = k;
+        }
+    }
+    double cand[4][3];
+    for (int c = 0; c < 4; ++c)
+        for (int a = 0; a < 3; ++a) cand[c][a] = p[a];
+    const int na = nearest >> 1;
+    const double nsign = (nearest & 1) ? 1.0 : -1.0;
+    cand[0][na] = p[na] + nsign * eps;
+    cand[1][na] = p[na] - nsign * eps;
+    if (speed > 0.0 && isfinite(speed)) {
+        for (int a = 0; a < 3; ++a) {
+            const double d = v[a] * (1.0 / speed);
+            cand[2][a] = p[a] + d * eps;
+            cand[3][a] = p[a] - d * eps;
+        }
+    }
+    for (int c = 0; c < 4; ++c) {
+        if (!box_contains(D, cand[c])) continue;
+        trace_box(D, cand[c], v, cp, t, f);
+        if (f >= 0 && isfinite(t)) {
+            for (int a = 0; a < 3; ++a) p[a] = cand[c][a];
+            return true;
+        }
+    }
+    return false;
+}
+
+__device__ __forceinline__ void mode_velocity(const DevMaterial& M, uint32_t w, double v[3]) {
+    const int a = static_cast<int>(w & 0x00FFFFFFu);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double c = __ldg(M.vel + 3 * a + k);
+        v[k] = ((w >> (24 + k)) & 1u) ? -c : c;
+    }
+}
+
+// Rough-wall reflection with supplied uniforms (src/solver/RoughBoundarySampler.cpp:373-533).
+__device__ __forceinline__ int rough_sample_dev(const DevRoughTable& R, const DevMaterial& M, int in_ai, double n_in, bool signed_w,
+                                double u0, double u1, double u2, double& n_out) {
+    n_out = n_in;
+    const int na = M.n_active;
+    const double p_spec = fmin(fmax(R.specularity[in_ai], 0.0), 1.0);
+    const double nbg_in = M.nbg[in_ai], w_in = M.omega[in_ai];
+    if (u0 <= p_spec) {
+        const int out = R.spec_match[in_ai];
+        if (out >= 0 && out < na) {
+            const double mapped = M.nbg[out] + w_in * (n_in - nbg_in) / fmax(1e-30, M.omega[out]);
+            if (isfinite(mapped) && (signed_w || mapped >= 0.0)) {
+                n_out = mapped;
+                return out;
+            }
+            return in_ai;
+        }
+    }
+    int out = -1;
+    const int b = R.diffuse_begin[in_ai], e = R.diffuse_end[in_ai];
+    if (b >= 0 && e > b && e <= R.n_sorted) {
+        const double fb = R.prefix[b], fe = R.prefix[e];
+        const double window = fe - fb;
+        if (window > 0.0 && isfinite(window)) {
+            const double u = fmin(fmax(u1, 0.0), 0.99999999999999989);
+            const double target = fb + u * window;
+            // upper_bound over prefix[b+1 .. e]
+            int lo = b + 1, hi = e + 1;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (R.prefix[mid] <= target) lo = mid + 1;
+                else hi = mid;
+            }
+            int pos = lo - 1;
+            pos = pos < b ? b : (pos > e - 1 ? e - 1 : pos);
+            out = R.outgoing_sorted[pos];
+        }
+    }
+    if (out < 0) {
+        if (R.strict) return in_ai;
+        if (R.n_roulette > 0 && R.roulette_cdf[R.n_roulette - 1] > 0.0) {
+            const double r = R.roulette_cdf[R.n_roulette - 1] * u1;
+            int lo = 0, hi = R.n_roulette;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (R.roulette_cdf[mid] < r) lo = mid + 1;
+                else hi = mid;
+            }
+            if (lo >= R.n_roulette) lo = R.n_roulette - 1;
+            out = R.roulette_active[lo];
+        } else if (R.n_outgoing > 0) {
+            int k = static_cast<int>(u2 * R.n_outgoing);
+            out = R.outgoing_active[k < R.n_outgoing ? k : R.n_outgoing - 1];
+        } else {
+            const int k = static_cast<int>(u2 * na);
+            out = k < na ? k : na - 1;
+        }
+    }
+    const double mapped = M.nbg[out] + w_in * (n_in - nbg_in) / fmax(1e-30, M.omega[out]);
+    if (isfinite(mapped) && (signed_w || mapped >= 0.0)) {
+        n_out = mapped;
+        return out;
+    }
+    n_out = n_in;
+    return in_ai;
+}
+
+__device__ __forceinline__ double table_inverse(const double* E, const double* T, int n, double e) {
+    if (n <= 0) return 0.0;
+    if (n == 1 || e <= E[0]) return T[0];
+    if (e >= E[n - 1]) return T[n - 1];
+    int lo = 0, hi = n;
+    while (lo < hi) { // upper_bound
+        const int mid = (lo + hi) >> 1;
+        if (E[mid] <= e) lo = mid + 1;
+        else hi = mid;
+    }
+    const int h = lo, l = h - 1;
+    const double x0 = E[l], x1 = E[h];
+    if (fabs(x1 - x0) <= 1e-18) return T[l];
+    const double t = (e - x0) / (x1 - x0);
+    return T[l] * (1.0 - t) + T[h] * t;
+}
+
+// Linear interpolation of the linewidth table, clamped (src/material/Thermodynamics.cpp:108-132).
+__device__ __forceinline__ double gamma_at(const DevMaterial& M, int a, double T) {
+    const int nT = M.n_temps;
+    if (T <= M.temps[0]) return M.gamma[a];
+    if (T >= M.temps[nT - 1]) return M.gamma[static_cast<size_t>(nT - 1) * M.n_active + a];
+    int lo = 0, hi = nT;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (M.temps[mid] <= T) lo = mid + 1;
+        else hi = mid;
+    }
+    const int h = lo, l = h - 1;
+    const double x0 = M.temps[l], x1 = M.temps[h];
+    const double y0 = M.gamma[static_cast<size_t>(l) * M.n_active + a];
+    const double y1 = M.gamma[static_cast<size_t>(h) * M.n_active + a];
+    if (fabs(x1 - x0) <= 1e-18) return y0;
+    const double t = (T - x0) / (x1 - x0);
+    return y0 * (1.0 - t) + y1 * t;
+}
+
+} // namespace phmc

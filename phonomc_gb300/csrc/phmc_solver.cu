@@ -1,0 +1,622 @@
+// DeviceSolver: table upload, HBM allocation and the per-step kernel sequence.
+#include "phmc_kernels.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <filesystem>
+#include <fstream>
+#include <limits>
+#include <numeric>
+#include <sstream>
+#include <stdexcept>
+
+namespace phmc {
+
+#define PHMC_CUDA(x)                                                                                      \
+    do {                                                                                                  \
+        cudaError_t err_ = (x);                                                                           \
+        if (err_ != cudaSuccess)                                                                          \
+            throw std::runtime_error(std::string("CUDA error: ") + cudaGetErrorString(err_) + " at " #x); \
+    } while (0)
+
+template <class T> T* DeviceSolver::dalloc(size_t n) {
+    void* p = nullptr;
+    const size_t bytes = std::max<size_t>(1, n) * sizeof(T);
+    PHMC_CUDA(cudaMalloc(&p, bytes));
+    PHMC_CUDA(cudaMemsetAsync(p, 0, bytes, stream_));
+    allocations_.push_back(p);
+    return static_cast<T*>(p);
+}
+
+template <class T> T* DeviceSolver::upload(const std::vector<T>& v) {
+    T* p = dalloc<T>(v.size());
+    if (!v.empty()) PHMC_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, stream_));
+    return p;
+}
+
+static const char* error_message(int code) {
+    switch (code) {
+    case kErrIntersection: return "Boundary intersection failed while advancing particles. Check that the STL is closed and manifold.";
+    case kErrModeMapping: return "Full-matrix boundary mode mapping failed while advancing particles. An inward discrete material mode and finite signed energy weight are required; no velocity-only reflection was applied.";
+    case kErrTooManyEvents: return "Particle exceeded 64 transport events in one timestep. Reduce simulation.time_step or inspect narrow STL features; no recovery was applied.";
+    case kErrInvalidStatistics: return "Invalid particle in grid energy statistics.";
+    case kErrEscaped: return "Particle escaped the domain. Refusing to relocate or rethermalize it; inspect the geometry and time step.";
+    case kErrZeroFluxReservoir: return "Cannot sample positive emissions from a zero-flux reservoir.";
+    case kErrCapacity: return "Carrier population exceeds the allocated device capacity.";
+    case kErrOutwardReservoirMode: return "Full-matrix reservoir sampled an outward mode.";
+    case kErrNonFinite: return "Non-finite grid energy reduction.";
+    case kErrNoRoughTable: return "Rough facet without a sampling table.";
+    case kErrCollision: return "Carrier collision occupation overflow.";
+    default: return "Unknown device error.";
+    }
+}
+
+DeviceSolver::DeviceSolver(const SimulationConfig& cfg, const std::vector<const PhononMaterial*>& mats,
+                           bool init_carriers)
+    : cfg_(cfg), mats_(mats) {
+    int dev_count = 0;
+    if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count <= 0)
+        throw std::runtime_error("No CUDA device is available for the GB300 carrier loop.");
+    PHMC_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, 0);
+    domain_ = std::make_unique<SimulationDomain>(cfg_);
+    P_ = build_problem(cfg_, *domain_, mats_);
+    ncells_ = domain_->grid_count();
+    mixed_ = false;
+    const int n0 = P_.initial_particles;
+    const int margin = P_.reservoirs.empty() ? 1024 : std::max(65536, n0 / 4);
+    allocate_state(n0 + margin);
+    upload_tables();
+    if (!init_carriers) return;
+    const CarrierArrays c = initial_carriers(P_, mats_);
+    set_carriers(n0, c.x.data(), c.y.data(), c.z.data(), c.occ.data(), c.mode.data(), c.alive.data());
+    if (!cfg_.output_folder.empty()) {
+        std::filesystem::create_directories(cfg_.output_folder);
+        std::ofstream(std::filesystem::path(cfg_.output_folder) / "convergence.txt")
+            << format_convergence_header(ncells_, cfg_.temperature_gradient.has_value());
+    }
+    flux_pass();
+    append_convergence_row();
+}
+
+DeviceSolver::~DeviceSolver() {
+    if (stream_) cudaStreamSynchronize(stream_);
+    for (void* p : allocations_) cudaFree(p);
+    if (d_tables_) cudaFree(d_tables_);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+void DeviceSolver::allocate_state(int capacity) {
+    state_.capacity = capacity;
+    state_.x = dalloc<double>(capacity);
+    state_.y = dalloc<double>(capacity);
+    state_.z = dalloc<double>(capacity);
+    state_.occ = dalloc<double>(capacity);
+    state_.mode = dalloc<uint32_t>(capacity);
+    state_.cell = dalloc<int32_t>(capacity);
+    state_.alive = dalloc<uint8_t>(capacity);
+    d_holes_ = dalloc<int>(capacity);
+    n_dead_blocks_ = (capacity + 1023) / 1024;
+    d_block_dead_ = dalloc<int>(n_dead_blocks_);
+    d_ledger_ = dalloc<DevLedger>(1);
+}
+
+void DeviceSolver::upload_tables() {
+    DevTables& T = tables_;
+    std::memset(&T, 0, sizeof T);
+    if (P_.mats.size() > static_cast<size_t>(kMaxMaterials)) throw std::runtime_error("too many materials");
+    int hist_modes = 0;
+    double r_max = 0.0;
+    for (size_t mi = 0; mi < P_.mats.size(); ++mi) {
+        const MaterialTables& M = P_.mats[mi];
+        DevMaterial& D = T.mat[mi];
+        D.n_active = M.n_active;
+        hist_modes = std::max(hist_modes, M.n_active);
+        D.n_classes = M.n_classes;
+        D.n_lookup = static_cast<int>(M.lookup_T.size());
+        D.n_temps = static_cast<int>(M.temperatures.size());
+        D.omega = upload(M.omega);
+        D.hw = upload(M.hw);
+        std::vector<double> inv(M.n_active);
+        for (int a = 0; a < M.n_active; ++a) inv[a] = M.hw[a] > 0 ? 1.0 / M.hw[a] : 0.0;
+        D.inv_hw = upload(inv);
+        D.vel = upload(M.vel);
+        std::vector<float> v32(4 * static_cast<size_t>(M.n_active));
+        for (int a = 0; a < M.n_active; ++a) {
+            const double vx = M.vel[3 * a], vy = M.vel[3 * a + 1], vz = M.vel[3 * a + 2];
+            v32[4 * a] = static_cast<float>(vx);
+            v32[4 * a + 1] = static_cast<float>(vy);
+            v32[4 * a + 2] = static_cast<float>(vz);
+            v32[4 * a + 3] = static_cast<float>(std::sqrt(vx * vx + vy * vy + vz * vz));
+        }
+        D.vel32 = upload(v32);
+        D.nbg = upload(M.nbg);
+        D.cap_bg = upload(M.capacity_bg);
+        D.mode_class = upload(M.mode_class);
+        D.class_omega = upload(M.class_omega);
+        D.class_hw = upload(M.class_hw);
+        D.class_rep = upload(M.class_rep);
+        D.relax_fixed = upload(M.relax_fixed);
+        D.temps = upload(M.temperatures);
+        D.gamma = upload(M.gamma_active);
+        D.lookup_T = upload(M.lookup_T);
+        D.lookup_E = upload(M.lookup_E);
+        if (P_.linearized) {
+            std::vector<double> rate(M.n_active);
+            for (int a = 0; a < M.n_active; ++a) {
+                rate[a] = M.col_normal[a] + M.col_resistive[a];
+                r_max = std::max(r_max, rate[a]);
+            }
+            D.col_cap = upload(M.col_capacity);
+            D.col_rate = upload(rate);
+            D.col_rn = upload(M.col_normal);
+            D.col_rr = upload(M.col_resistive);
+            D.col_k = upload(M.col_k);
+        }
+        if (!M.grad_rate.empty()) D.grad_rate = upload(M.grad_rate);
+        D.energy_weight = M.energy_weight;
+        D.energy_density_bg = M.energy_density_bg;
+        D.heat_capacity_density_bg = M.heat_capacity_density_bg;
+        D.zero_point = M.zero_point;
+    }
+    // rough tables
+    if (P_.rough.tables.size() > static_cast<size_t>(kMaxRoughTables)) throw std::runtime_error("too many rough tables");
+    for (size_t t = 0; t < P_.rough.tables.size(); ++t) {
+        const RoughTable& R = P_.rough.tables[t];
+        DevRoughTable& D = T.rough[t];
+        D.strict = R.strict_elastic ? 1 : 0;
+        D.n_sorted = static_cast<int>(R.outgoing_sorted.size());
+        D.n_roulette = static_cast<int>(R.roulette_active.size());
+        D.n_outgoing = static_cast<int>(R.outgoing_active.size());
+        D.specularity = upload(R.specularity);
+        D.spec_match = upload(R.spec_match);
+        D.diffuse_begin = upload(R.diffuse_begin);
+        D.diffuse_end = upload(R.diffuse_end);
+        D.outgoing_sorted = upload(R.outgoing_sorted);
+        D.prefix = upload(R.residual_prefix);
+        D.roulette_active = upload(R.roulette_active);
+        D.roulette_cdf = upload(R.roulette_cdf);
+        D.outgoing_active = upload(R.outgoing_active);
+    }
+    // reservoirs
+    if (P_.reservoirs.size() > static_cast<size_t>(kMaxReservoirs)) throw std::runtime_error("too many reservoirs");
+    for (size_t r = 0; r < P_.reservoirs.size(); ++r) {
+        const Reservoir& R = P_.reservoirs[r];
+        DevReservoir& D = T.res[r];
+        D.facet = R.facet;
+        D.material = R.material;
+        D.n_cdf = static_cast<int>(R.cdf.size());
+        D.expected = R.expected;
+        for (int k = 0; k < 3; ++k) D.normal[k] = R.normal[k];
+        const Facet& F = domain_->facets()[R.facet];
+        for (int tri = 0; tri < 2; ++tri)
+            for (int v = 0; v < 3; ++v)
+                for (int k = 0; k < 3; ++k) D.tri[tri][v][k] = F.tri[tri][v][k];
+        D.area0 = 0.5 * F.area;
+        D.area1 = 0.5 * F.area;
+        D.cdf = upload(R.cdf);
+        D.occ = upload(P_.reservoir_occ[r]);
+    }
+    // domain
+    DevDomain& D = T.dom;
+    const Vec3& lo = domain_->bounds_min();
+    const Vec3& hi = domain_->bounds_max();
+    double scale = 1.0;
+    for (int a = 0; a < 3; ++a) {
+        D.lo[a] = lo[a];
+        D.hi[a] = hi[a];
+        D.inv_cell[a] = domain_->inv_cell()[a];
+        D.shape[a] = domain_->grid_shape()[a];
+        D.cell_size[a] = (hi[a] - lo[a]) / D.shape[a];
+        scale = std::max(scale, std::abs(hi[a] - lo[a]));
+    }
+    D.scale = scale;
+    D.tol = std::max(1e-9, 64.0 * std::numeric_limits<double>::epsilon() * scale);
+    D.ncells = ncells_;
+    for (int f = 0; f < 6; ++f) {
+        const Facet& F = domain_->facets()[f];
+        D.cond[f] = F.condition;
+        D.pair[f] = F.pair;
+        D.reservoir[f] = F.reservoir;
+        for (int k = 0; k < 3; ++k) D.shift[f][k] = F.shift[k];
+        for (size_t m = 0; m < P_.mats.size(); ++m) D.rough_table[m][f] = P_.rough.facet_table[m * 6 + f];
+    }
+    D.layout_axis = P_.layout.axis;
+    D.n_planes = static_cast<int>(P_.layout.planes.size());
+    for (int k = 0; k < D.n_planes; ++k) D.planes[k] = P_.layout.planes[k];
+    // params
+    DevParams& p = T.par;
+    p.dt = cfg_.time_step;
+    p.push_eps = P_.push_eps;
+    p.seed = cfg_.random_seed;
+    p.conservative = P_.conservative;
+    p.linearized = P_.linearized;
+    p.one_to_one = P_.one_to_one;
+    p.n_materials = static_cast<int>(P_.mats.size());
+    p.n_reservoirs = static_cast<int>(P_.reservoirs.size());
+    p.lifetime_local = cfg_.lifetime_temperature_is_local;
+    p.lifetime_T = cfg_.lifetime_temperature;
+    p.background_T = cfg_.background_temperature;
+    p.gradient_axis = P_.kappa_axis;
+    p.gradient_energy_weight = P_.gradient_energy_weight;
+    PHMC_CUDA(cudaMalloc(&d_tables_, sizeof(DevTables)));
+    PHMC_CUDA(cudaMemcpyAsync(d_tables_, &tables_, sizeof(DevTables), cudaMemcpyHostToDevice, stream_));
+
+    // cells
+    CellArrays& C = cells_;
+    C.ncells = ncells_;
+    C.hist_modes = hist_modes;
+    C.cell_material = upload(P_.cell_material);
+    C.volume = upload(domain_->grid_volumes());
+    const size_t hist = static_cast<size_t>(ncells_) * hist_modes;
+    C.hcnt = dalloc<unsigned int>(hist);
+    C.hE = dalloc<double>(hist);
+    const bool rta = !P_.linearized;
+    if (rta) {
+        C.hN = dalloc<double>(hist);
+        C.hM = dalloc<double>(hist);
+        const size_t nc = static_cast<size_t>(ncells_) * P_.mats[0].n_classes;
+        C.rta_a = dalloc<double>(nc);
+        C.rta_B = dalloc<double>(nc);
+    }
+    C.energy = dalloc<double>(ncells_);
+    C.temperature = dalloc<double>(ncells_);
+    C.grad_R = dalloc<double>(ncells_);
+    C.grad_C = dalloc<double>(ncells_);
+    C.acc = dalloc<double>(ncells_);
+    C.flux = dalloc<double>(3 * static_cast<size_t>(ncells_));
+    if (P_.linearized) {
+        if (P_.mats.size() != 1) throw std::runtime_error("Linear-response collisions support one material in this build.");
+        C.lin_A = dalloc<double>(hist);
+        const int S = std::max(1, static_cast<int>(std::ceil(cfg_.time_step * r_max)));
+        const double h = cfg_.time_step / S;
+        const double x = h * r_max;
+        // smallest K with x^(K+1)/(K+1)! <= 1e-17, x = h * max rate <= 1
+        int K = 1;
+        double bound = x;
+        while (K < 40) {
+            bound = bound * x / (K + 1);
+            if (bound <= 1e-17) break;
+            ++K;
+        }
+        C.lin_substeps = S;
+        C.lin_h = h;
+        C.lin_terms = std::max(1, K);
+        std::vector<double> decay(P_.mats[0].n_active);
+        for (int a = 0; a < P_.mats[0].n_active; ++a)
+            decay[a] = std::exp(-(P_.mats[0].col_normal[a] + P_.mats[0].col_resistive[a]) * cfg_.time_step);
+        C.lin_decay = upload(decay);
+    }
+    scratch_ = nullptr;
+    if (P_.linearized) scratch_ = dalloc<double>(hist * 8);
+    else scratch_ = dalloc<double>(static_cast<size_t>(ncells_) * P_.mats[0].n_classes * 3);
+    // class CSR of material 0
+    const MaterialTables& M0 = P_.mats[0];
+    std::vector<int> start(M0.n_classes + 1, 0), modes(M0.n_active);
+    for (int a = 0; a < M0.n_active; ++a) ++start[M0.mode_class[a] + 1];
+    for (int k = 0; k < M0.n_classes; ++k) start[k + 1] += start[k];
+    std::vector<int> cursor(start.begin(), start.end() - 1);
+    for (int a = 0; a < M0.n_active; ++a) modes[cursor[M0.mode_class[a]]++] = a;
+    class_start_ = upload(start);
+    class_modes_ = upload(modes);
+}
+
+LaunchCtx DeviceSolver::ctx() const {
+    LaunchCtx x;
+    x.T = d_tables_;
+    x.S = state_;
+    x.C = cells_;
+    x.L = d_ledger_;
+    x.stream = stream_;
+    x.grid_blocks = sm_count_ * 8;
+    return x;
+}
+
+int DeviceSolver::collision_kind() const {
+    return P_.linearized ? kCollideLinear : kCollideRta;
+}
+
+void DeviceSolver::initial_statistics() {
+    const LaunchCtx x = ctx();
+    launch_histogram(x, !P_.linearized);
+    launch_cell_solve(x, 0, collision_kind(), P_.mats[0].n_classes, class_start_, class_modes_, scratch_);
+    launch_cells_final(x, 1);
+    counters_.launches += 3;
+}
+
+void DeviceSolver::set_carriers(long long n, const double* x, const double* y, const double* z, const double* occ,
+                                const uint32_t* mode, const uint8_t* alive) {
+    if (n < 0 || n > state_.capacity) throw std::invalid_argument("carrier count exceeds device capacity");
+    PHMC_CUDA(cudaMemcpyAsync(state_.x, x, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    PHMC_CUDA(cudaMemcpyAsync(state_.y, y, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    PHMC_CUDA(cudaMemcpyAsync(state_.z, z, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    PHMC_CUDA(cudaMemcpyAsync(state_.occ, occ, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    PHMC_CUDA(cudaMemcpyAsync(state_.mode, mode, n * sizeof(uint32_t), cudaMemcpyHostToDevice, stream_));
+    if (alive) PHMC_CUDA(cudaMemcpyAsync(state_.alive, alive, n * sizeof(uint8_t), cudaMemcpyHostToDevice, stream_));
+    else PHMC_CUDA(cudaMemsetAsync(state_.alive, 1, n * sizeof(uint8_t), stream_));
+    DevLedger L{};
+    L.n_slots = static_cast<int>(n);
+    for (size_t r = 0; r < P_.reservoirs.size(); ++r) L.previous_res[r] = P_.reservoirs[r].initial_count;
+    PHMC_CUDA(cudaMemcpyAsync(d_ledger_, &L, sizeof L, cudaMemcpyHostToDevice, stream_));
+    step_ = 0;
+    elapsed_ = 0;
+    failed_ = false;
+    launch_init_cells(ctx());
+    counters_.launches += 1;
+    initial_statistics();
+    synchronize();
+}
+
+void DeviceSolver::run_timestep() {
+    if (failed_) throw std::runtime_error("Cannot resume a failed timestep; construct a new solver after fixing its cause.");
+    failed_ = true;
+    const LaunchCtx x = ctx();
+    const bool gradient = cfg_.temperature_gradient.has_value();
+    const int coll = collision_kind();
+    launch_step_begin(x);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (profile_pass_a_) {
+        PHMC_CUDA(cudaEventCreate(&e0));
+        PHMC_CUDA(cudaEventCreate(&e1));
+        PHMC_CUDA(cudaEventRecord(e0, stream_));
+    }
+    launch_transport(x, gradient, coll == kCollideRta, static_cast<uint32_t>(step_));
+    if (profile_pass_a_) {
+        PHMC_CUDA(cudaEventRecord(e1, stream_));
+        pass_a_events_.push_back({e0, e1});
+    }
+    counters_.launches += 2;
+    if (!P_.reservoirs.empty()) counters_.launches += launch_inject(x, coll == kCollideRta, d_holes_, d_block_dead_,
+                                                                   state_.capacity, static_cast<uint32_t>(step_));
+    if (step_ % 100 == 0) {
+        launch_containment(x);
+        counters_.launches += 1;
+    }
+    launch_cell_solve(x, 1, coll, P_.mats[0].n_classes, class_start_, class_modes_, scratch_);
+    launch_update(x, coll, gradient);
+    launch_cells_final(x, 0);
+    counters_.launches += 3;
+    ++step_;
+    elapsed_ += cfg_.time_step;
+    if (step_ == 1 || step_ % cfg_.convergence_write_interval == 0) {
+        flux_pass();
+        append_convergence_row();
+    }
+    failed_ = false;
+}
+
+double DeviceSolver::collide_only(const double* cell_temperature) {
+    const LaunchCtx x = ctx();
+    launch_step_begin(x);
+    launch_histogram(x, !P_.linearized);
+    int phase = 1;
+    if (cell_temperature) {
+        PHMC_CUDA(cudaMemcpyAsync(cells_.temperature, cell_temperature, ncells_ * sizeof(double),
+                                  cudaMemcpyHostToDevice, stream_));
+        phase = 2;
+    }
+    launch_cell_solve(x, phase, collision_kind(), P_.mats[0].n_classes, class_start_, class_modes_, scratch_);
+    launch_update(x, collision_kind(), false);
+    counters_.launches += 4;
+    synchronize();
+    PHMC_CUDA(cudaMemsetAsync(cells_.acc, 0, ncells_ * sizeof(double), stream_));
+    double r = 0;
+    PHMC_CUDA(cudaMemcpy(&r, &d_ledger_->step_lifetime_residual, sizeof(double), cudaMemcpyDeviceToHost));
+    return r;
+}
+
+double DeviceSolver::drive_only() {
+    const LaunchCtx x = ctx();
+    launch_step_begin(x);
+    launch_histogram(x, !P_.linearized);
+    launch_cell_solve(x, 0, collision_kind(), P_.mats[0].n_classes, class_start_, class_modes_, scratch_);
+    launch_update(x, kCollideNone, true);
+    counters_.launches += 4;
+    synchronize();
+    PHMC_CUDA(cudaMemsetAsync(cells_.acc, 0, ncells_ * sizeof(double), stream_));
+    double r = 0;
+    PHMC_CUDA(cudaMemcpy(&r, &d_ledger_->step_drive_ev, sizeof(double), cudaMemcpyDeviceToHost));
+    return r;
+}
+
+void DeviceSolver::timed_run(int steps, double& total_ms, double& kernel_ms, long long& launches) {
+    synchronize();
+    cudaEvent_t a, b;
+    PHMC_CUDA(cudaEventCreate(&a));
+    PHMC_CUDA(cudaEventCreate(&b));
+    const long long l0 = counters_.launches;
+    profile_pass_a_ = true;
+    PHMC_CUDA(cudaEventRecord(a, stream_));
+    run(steps);
+    PHMC_CUDA(cudaEventRecord(b, stream_));
+    profile_pass_a_ = false;
+    synchronize();
+    float ms = 0;
+    PHMC_CUDA(cudaEventElapsedTime(&ms, a, b));
+    total_ms = ms;
+    kernel_ms = 0;
+    for (auto& ev : pass_a_events_) {
+        float k = 0;
+        PHMC_CUDA(cudaEventElapsedTime(&k, ev.first, ev.second));
+        kernel_ms += k;
+        cudaEventDestroy(ev.first);
+        cudaEventDestroy(ev.second);
+    }
+    pass_a_events_.clear();
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    launches = counters_.launches - l0;
+}
+
+void DeviceSolver::run(int steps) {
+    for (int k = 0; k < steps; ++k) run_timestep();
+}
+
+void DeviceSolver::synchronize() {
+    PHMC_CUDA(cudaStreamSynchronize(stream_));
+    check_error();
+}
+
+void DeviceSolver::check_error() {
+    int code = 0, slot = 0;
+    PHMC_CUDA(cudaMemcpy(&code, &d_ledger_->error_code, sizeof(int), cudaMemcpyDeviceToHost));
+    if (code) {
+        PHMC_CUDA(cudaMemcpy(&slot, &d_ledger_->error_slot, sizeof(int), cudaMemcpyDeviceToHost));
+        failed_ = true;
+        throw std::runtime_error(std::string(error_message(code)) + " (carrier slot or cell " + std::to_string(slot) + ")");
+    }
+}
+
+void DeviceSolver::flux_pass() {
+    const LaunchCtx x = ctx();
+    PHMC_CUDA(cudaMemsetAsync(cells_.flux, 0, 3 * sizeof(double) * ncells_, stream_));
+    launch_flux(x);
+    counters_.launches += 1;
+    synchronize();
+    host_T_.resize(ncells_);
+    host_E_.resize(ncells_);
+    host_q_.resize(3 * static_cast<size_t>(ncells_));
+    PHMC_CUDA(cudaMemcpy(host_T_.data(), cells_.temperature, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
+    PHMC_CUDA(cudaMemcpy(host_E_.data(), cells_.energy, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
+    PHMC_CUDA(cudaMemcpy(host_q_.data(), cells_.flux, 3 * ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
+    // src/solver/GridStatistics.cpp:334-343 and src/solver/Observables.cpp:38-144
+    const auto& vol = domain_->grid_volumes();
+    const int axis = P_.kappa_axis;
+    double phi = 0, tv = 0;
+    for (int c = 0; c < ncells_; ++c) {
+        for (int k = 0; k < 3; ++k) host_q_[3 * c + k] = host_q_[3 * c + k] * (1.0 / vol[c]) * 1.602176634e13;
+        phi += host_q_[3 * c + axis] * vol[c];
+        tv += vol[c];
+    }
+    avg_flux_ = phi / tv;
+    kappa_fit_ = kappa_end_ = 0;
+    if (!cfg_.compute_kappa) return;
+    if (cfg_.temperature_gradient) {
+        kappa_end_ = -avg_flux_ / *cfg_.temperature_gradient;
+        return;
+    }
+    double Tl = host_T_.front(), Tr = host_T_.back();
+    const auto& rf = domain_->reservoir_facets();
+    if (rf.size() >= 2) {
+        int fl = rf.front(), fr = rf.front();
+        for (int f : rf) {
+            if (domain_->facets()[f].centroid[axis] < domain_->facets()[fl].centroid[axis]) fl = f;
+            if (domain_->facets()[f].centroid[axis] > domain_->facets()[fr].centroid[axis]) fr = f;
+        }
+        Tl = domain_->facets()[fl].value;
+        Tr = domain_->facets()[fr].value;
+    }
+    const double L = std::abs(domain_->bounds_max()[axis] - domain_->bounds_min()[axis]) * 1e-10;
+    const double ge = std::abs(L) > 1e-24 ? (Tr - Tl) / L : 0.0;
+    kappa_end_ = std::abs(ge) > 1e-18 ? -avg_flux_ / ge : 0.0;
+    double sx = 0, st = 0, sxx = 0, sxt = 0;
+    for (int c = 0; c < ncells_; ++c) {
+        const double xx = domain_->grid_centers()[c][axis] * 1e-10;
+        sx += xx;
+        st += host_T_[c];
+        sxx += xx * xx;
+        sxt += xx * host_T_[c];
+    }
+    double gf = 0;
+    if (ncells_ >= 2) {
+        const double den = ncells_ * sxx - sx * sx;
+        if (std::abs(den) > 1e-30 && std::abs(host_T_.back() - host_T_.front()) > 1e-6) gf = (ncells_ * sxt - sx * st) / den;
+    }
+    kappa_fit_ = std::abs(gf) > 1e-18 ? -avg_flux_ / gf : 0.0;
+}
+
+void DeviceSolver::read_stats(phmc_stats& o) {
+    synchronize();
+    DevLedger L;
+    PHMC_CUDA(cudaMemcpy(&L, d_ledger_, sizeof L, cudaMemcpyDeviceToHost));
+    std::memset(&o, 0, sizeof o);
+    o.current_timestep = step_;
+    o.particle_count = L.particle_count;
+    o.absorbed_total = static_cast<int64_t>(L.total_absorbed);
+    o.injected_total = static_cast<int64_t>(L.total_injected);
+    o.step_absorbed = static_cast<int64_t>(L.step_absorbed);
+    o.step_injected = static_cast<int64_t>(L.step_injected);
+    o.step_absorbed_energy_ev = L.step_absorbed_ev;
+    o.step_injected_energy_ev = L.step_injected_ev;
+    o.total_thermal_energy_ev = L.thermal_energy;
+    o.total_lifetime_energy_residual_ev = L.total_lifetime_residual;
+    o.step_lifetime_energy_residual_ev = L.step_lifetime_residual;
+    o.total_energy_balance_residual_ev = L.total_balance_residual;
+    o.step_energy_balance_residual_ev = L.step_balance_residual;
+    o.total_gradient_energy_ev = L.total_drive_ev;
+    o.step_gradient_energy_ev = L.step_drive_ev;
+    o.step_gradient_updates = static_cast<int64_t>(L.step_drive_updates);
+    o.average_heat_flux_along_axis = avg_flux_;
+    o.kappa_fit = kappa_fit_;
+    o.kappa_endpoints = kappa_end_;
+    o.device_launches = counters_.launches;
+}
+
+void DeviceSolver::read_cells(double* T, double* E, double* q3) {
+    synchronize();
+    if (T) PHMC_CUDA(cudaMemcpy(T, cells_.temperature, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
+    if (E) PHMC_CUDA(cudaMemcpy(E, cells_.energy, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
+    if (q3) std::copy(host_q_.begin(), host_q_.end(), q3);
+}
+
+long long DeviceSolver::slot_count() {
+    synchronize();
+    int n = 0;
+    PHMC_CUDA(cudaMemcpy(&n, &d_ledger_->n_slots, sizeof(int), cudaMemcpyDeviceToHost));
+    return n;
+}
+
+void DeviceSolver::get_carriers(double* x, double* y, double* z, double* occ, uint32_t* mode, int32_t* cell,
+                                uint8_t* alive) {
+    const long long n = slot_count();
+    PHMC_CUDA(cudaMemcpy(x, state_.x, n * sizeof(double), cudaMemcpyDeviceToHost));
+    PHMC_CUDA(cudaMemcpy(y, state_.y, n * sizeof(double), cudaMemcpyDeviceToHost));
+    PHMC_CUDA(cudaMemcpy(z, state_.z, n * sizeof(double), cudaMemcpyDeviceToHost));
+    PHMC_CUDA(cudaMemcpy(occ, state_.occ, n * sizeof(double), cudaMemcpyDeviceToHost));
+    PHMC_CUDA(cudaMemcpy(mode, state_.mode, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    PHMC_CUDA(cudaMemcpy(cell, state_.cell, n * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    PHMC_CUDA(cudaMemcpy(alive, state_.alive, n * sizeof(uint8_t), cudaMemcpyDeviceToHost));
+}
+
+void DeviceSolver::append_convergence_row() {
+    if (cfg_.output_folder.empty()) return;
+    phmc_stats s;
+    read_stats(s);
+    ConvergenceRow r;
+    r.timestep = step_;
+    r.time_ps = elapsed_;
+    r.temperatures = host_T_;
+    r.heat_flux = avg_flux_;
+    r.kappa_int = kappa_fit_;
+    r.kappa_eff = kappa_end_;
+    r.particle_count = s.particle_count;
+    r.absorbed = s.step_absorbed;
+    r.injected = s.step_injected;
+    r.net = s.step_injected - s.step_absorbed;
+    r.absorbed_ev = s.step_absorbed_energy_ev;
+    r.injected_ev = s.step_injected_energy_ev;
+    r.lifetime_residual = s.step_lifetime_energy_residual_ev;
+    r.balance_residual = s.step_energy_balance_residual_ev;
+    r.thermal_energy = s.total_thermal_energy_ev;
+    r.gradient = cfg_.temperature_gradient.has_value();
+    r.gradient_updates = s.step_gradient_updates;
+    r.gradient_energy = s.step_gradient_energy_ev;
+    std::ofstream(std::filesystem::path(cfg_.output_folder) / "convergence.txt", std::ios::app)
+        << format_convergence_row(r);
+}
+
+void DeviceSolver::write_outputs() {
+    if (cfg_.output_folder.empty()) return;
+    // grid_centers.csv (src/geometry/DomainOutput.cpp): index,x_nm,y_nm,z_nm,volume_nm3
+    std::ofstream g(std::filesystem::path(cfg_.output_folder) / "grid_centers.csv");
+    g << "index,x_nm,y_nm,z_nm,volume_nm3\n";
+    g.precision(10);
+    for (int c = 0; c < ncells_; ++c) {
+        const auto& p = domain_->grid_centers()[c];
+        g << c << ',' << p[0] / 10.0 << ',' << p[1] / 10.0 << ',' << p[2] / 10.0 << ','
+          << domain_->grid_volumes()[c] / 1000.0 << '\n';
+    }
+}
+
+} // namespace phmc

@@ -1,0 +1,145 @@
+// Device solver: owns the HBM carrier arrays, the uploaded tables and the
+// per-step kernel sequence of MonteCarloSolver::run_timestep
+// (src/MonteCarloSolver.cpp:348-398), mirrored as
+//
+//   pass A  k_transport  gradient half-step, free flight + wall events, new cell,
+//                        (cell x mode) histogram of counts and energies
+//   inject  hole scan + k_inject (reservoir emissions, advanced from emission time)
+//   cells   k_cell_solve per cell: energy density and temperature, gradient
+//           sums, RTA pseudo-temperature Newton / linearized-RTA coefficients
+//   pass B  k_update     collision update, gradient half-step, energy tally
+//   ledger  k_cells_final + k_ledger_finish
+//
+// Every sum that the reference forms over the carriers of one cell is formed
+// here from the (cell, mode) histogram: carriers of one mode in one cell share
+// frequency, velocity magnitude, rates and equilibrium occupation, so the
+// per-cell solves only need the mode multiplicities and summed energies.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/phonomc_gb300.h"
+#include "phmc_device.cuh"
+#include "phmc_host.h"
+
+namespace phmc {
+
+
+// Per-cell scratch produced by k_cell_solve and read by the update pass.
+struct CellArrays {
+    int ncells;
+    int hist_modes;          // modes per cell in the histogram (max active count over materials)
+    const int* cell_material;
+    const double* volume;
+    // histogram (zeroed by the cell solve after use)
+    unsigned int* hcnt;      // [ncells * hist_modes]
+    double* hE;              // [ncells * hist_modes] summed e_i = hw (n - nbg)
+    double* hN;              // [ncells * hist_modes] summed n (RTA only)
+    double* hM;              // [ncells * hist_modes] summed max(1, n) (RTA only)
+    // per cell results
+    double* energy;          // energy density
+    double* temperature;
+    double* grad_R;          // sum of gradient rates
+    double* grad_C;          // sum of capacities
+    double* acc;             // generic per-cell accumulator (final tally)
+    double* flux;            // [ncells*3]
+    // RTA tables [ncells * n_classes]
+    double* rta_a;           // relaxation weight
+    double* rta_B;           // Bose occupation at the pseudo-temperature
+    // linearized collision tables [ncells * hist_modes]: additive term
+    double* lin_A;
+    // linearized collision per-mode data (one material)
+    const double* lin_decay; // exp(-h r) per active mode
+    int lin_substeps;
+    double lin_h;
+    int lin_terms;
+};
+
+struct StepCounters {
+    long long launches = 0;
+};
+
+struct LaunchCtx;
+
+class DeviceSolver {
+public:
+    // init_carriers=false leaves the population empty (set_carriers fills it).
+    DeviceSolver(const SimulationConfig& cfg, const std::vector<const PhononMaterial*>& mats,
+                 bool init_carriers = true);
+    ~DeviceSolver();
+    DeviceSolver(const DeviceSolver&) = delete;
+    DeviceSolver& operator=(const DeviceSolver&) = delete;
+
+    void run_timestep();
+    void run(int steps);
+    void synchronize();
+    void check_error();
+    void read_stats(phmc_stats& out);
+    int cell_count() const { return ncells_; }
+    void read_cells(double* T, double* E, double* q3);
+    long long slot_count();
+    void get_carriers(double* x, double* y, double* z, double* occ, uint32_t* mode, int32_t* cell, uint8_t* alive);
+    void set_carriers(long long n, const double* x, const double* y, const double* z, const double* occ,
+                      const uint32_t* mode, const uint8_t* alive);
+    void write_outputs();
+    // Deterministic sub-steps on the current population (parity entry points):
+    // one collision with the given cell temperatures (or the tallied ones when
+    // null), and one gradient half-step; both return the ledger energy.
+    double collide_only(const double* cell_temperature);
+    // Steps bracketed by CUDA events on the solver stream; kernel_ms sums the
+    // event-timed duration of every transport-pass launch in the region.
+    void timed_run(int steps, double& total_ms, double& kernel_ms, long long& launches);
+    double drive_only();
+    const Problem& problem() const { return P_; }
+    long long launches() const { return counters_.launches; }
+    cudaStream_t stream() const { return stream_; }
+
+private:
+    void upload_tables();
+    void allocate_state(int capacity);
+    void initial_statistics();
+    void flux_pass();
+    void append_convergence_row();
+
+    SimulationConfig cfg_;
+    std::vector<const PhononMaterial*> mats_;
+    std::unique_ptr<SimulationDomain> domain_;
+    Problem P_;
+    int ncells_ = 0;
+    int step_ = 0;
+    double elapsed_ = 0;
+    bool failed_ = false;
+    bool mixed_ = false;
+    cudaStream_t stream_ = nullptr;
+    int sm_count_ = 152;
+    StepCounters counters_;
+
+    DevTables tables_{};
+    DevTables* d_tables_ = nullptr;
+    DevLedger* d_ledger_ = nullptr;
+    CarrierState state_{};
+    CellArrays cells_{};
+    int* d_holes_ = nullptr;
+    int* d_block_dead_ = nullptr;
+    int n_dead_blocks_ = 0;
+    std::vector<void*> allocations_;
+    // host-side observables
+    double avg_flux_ = 0, kappa_fit_ = 0, kappa_end_ = 0;
+    std::vector<double> host_T_, host_E_, host_q_;
+
+    bool profile_pass_a_ = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pass_a_events_;
+    double* scratch_ = nullptr;
+    const int* class_start_ = nullptr;
+    const int* class_modes_ = nullptr;
+    struct LaunchCtx ctx() const;
+    int collision_kind() const;
+
+    template <class T> T* dalloc(size_t n);
+    template <class T> T* upload(const std::vector<T>& v);
+};
+
+} // namespace phmc

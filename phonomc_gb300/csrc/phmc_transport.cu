@@ -1,0 +1,501 @@
+// Pass A of the timestep: gradient half-step, free flight with wall events,
+// cell reassignment and the (cell, mode) histogram; reservoir injection; the
+// heat-flux tally. Plain-FP64 carrier state.
+//
+// Reference: src/solver/TransportOperator.cpp:113-163 (advance loops),
+// 287-361 (boundary collision), 405-466 (event loop);
+// src/solver/BoundaryInteraction.cpp:53-162; src/solver/ReservoirInjector.cpp:62-132;
+// src/solver/TemperatureGradientDrive.cpp:116-171; src/solver/GridStatistics.cpp:269-347.
+#include "phmc_kernels.cuh"
+
+namespace phmc {
+
+// Per-block partial ledger sums, flushed once per block.
+struct BlockLedger {
+    double absorbed_ev;
+    double injected_ev;
+    double drive_ev;
+    unsigned long long drive_updates;
+    unsigned int absorbed;
+    unsigned int absorbed_res[kMaxReservoirs];
+};
+
+__device__ __forceinline__ void block_ledger_init(BlockLedger* b) {
+    if (threadIdx.x == 0) {
+        b->absorbed_ev = 0;
+        b->injected_ev = 0;
+        b->drive_ev = 0;
+        b->drive_updates = 0;
+        b->absorbed = 0;
+        for (int r = 0; r < kMaxReservoirs; ++r) b->absorbed_res[r] = 0;
+    }
+}
+
+__device__ __forceinline__ void block_ledger_flush(BlockLedger* b, DevLedger* L) {
+    if (threadIdx.x == 0) {
+        if (b->absorbed) {
+            atomicAdd(&L->step_absorbed, static_cast<unsigned long long>(b->absorbed));
+            atomicAdd(&L->step_absorbed_ev, b->absorbed_ev);
+            for (int r = 0; r < kMaxReservoirs; ++r)
+                if (b->absorbed_res[r]) atomicAdd(&L->absorbed_res[r], b->absorbed_res[r]);
+        }
+        if (b->drive_updates) {
+            atomicAdd(&L->step_drive_ev, b->drive_ev);
+            atomicAdd(&L->step_drive_updates, b->drive_updates);
+        }
+        if (b->injected_ev != 0.0) atomicAdd(&L->step_injected_ev, b->injected_ev);
+    }
+}
+
+// One carrier's flight for `remaining` ps. Position, mode word and occupation
+// live in registers; returns false when the carrier was absorbed.
+__device__ bool advance_carrier(const DevTables& T, DevLedger* L, BlockLedger* bl, int slot, double p[3],
+                                uint32_t& w, double& occ, double remaining, uint32_t purpose, uint32_t step) {
+    const DevDomain& D = T.dom;
+    const DevParams& P = T.par;
+    const int mid = static_cast<int>(w >> 28);
+    const DevMaterial& M = T.mat[mid];
+    double v[3];
+    mode_velocity(M, w, v);
+    double cp[3], t;
+    int f;
+    if (!cache_hit(D, P, p, v, cp, t, f)) {
+        raise_error(L, kErrIntersection, slot);
+        return true;
+    }
+    int event = 0;
+    for (; remaining > 1e-14 && event < 64; ++event) {
+        if (!isfinite(t) || t > remaining) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], remaining));
+            return true;
+        }
+        remaining -= fmax(0.0, t);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) p[a] = cp[a];
+        const int axis = f >> 1;
+        const char cond = D.cond[f];
+        const int ai = static_cast<int>(w & 0x00FFFFFFu);
+        if (cond == 'T') {
+            const double e = dmul(dmul(M.hw[ai], occ - M.nbg[ai]), M.energy_weight);
+            atomicAdd(&bl->absorbed, 1u);
+            atomicAdd(&bl->absorbed_ev, e);
+            const int r = D.reservoir[f];
+            if (r >= 0) atomicAdd(&bl->absorbed_res[r], 1u);
+            return false;
+        }
+        if (cond == 'P' && D.pair[f] >= 0) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], D.shift[f][a]);
+        } else {
+            const int table = D.rough_table[mid][f];
+            if (P.conservative || (cond == 'R' && table >= 0)) {
+                if (table < 0) {
+                    raise_error(L, kErrModeMapping, slot);
+                    return true;
+                }
+                const Uniform2 d0 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose,
+                                             static_cast<uint32_t>(event), 0);
+                const Uniform2 d1 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose,
+                                             static_cast<uint32_t>(event), 1);
+                double n_out;
+                const int out = rough_sample_dev(T.rough[table], M, ai, occ, P.conservative != 0, d0.a, d0.b, d1.a,
+                                                 n_out);
+                const double nsign = (f & 1) ? 1.0 : -1.0;
+                const double vn = M.vel[3 * out + axis] * nsign;
+                uint32_t signs = 0;
+                if (P.conservative) {
+                    if (!isfinite(n_out) || !(M.omega[out] > 0.0) || !(vn < 0.0)) {
+                        raise_error(L, kErrModeMapping, slot);
+                        return true;
+                    }
+                } else if (vn > 0.0) {
+                    signs = 1u << axis;
+                }
+                w = static_cast<uint32_t>(out) | (signs << 24) | (static_cast<uint32_t>(mid) << 28);
+                occ = n_out;
+            } else if (cond == 'R') {
+                raise_error(L, kErrNoRoughTable, slot);
+                return true;
+            } else {
+                w ^= 1u << (24 + axis);
+            }
+        }
+        mode_velocity(M, w, v);
+        const double speed = sqrt(dadd(dadd(dmul(v[0], v[0]), dmul(v[1], v[1])), dmul(v[2], v[2])));
+        const double s = P.push_eps / fmax(speed, 1e-12);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], s));
+        if (!cache_hit(D, P, p, v, cp, t, f)) {
+            raise_error(L, kErrIntersection, slot);
+            return true;
+        }
+        if (t < 1e-12) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], 1e-12));
+            if (!cache_hit(D, P, p, v, cp, t, f)) {
+                raise_error(L, kErrIntersection, slot);
+                return true;
+            }
+        }
+    }
+    if (remaining > 1e-14) raise_error(L, kErrTooManyEvents, slot);
+    return true;
+}
+
+// Histogram of the post-transport population for the per-cell solves.
+__device__ __forceinline__ void histogram_add(const CellArrays& C, const DevMaterial& M, DevLedger* L, int slot,
+                                              int cell, int mid, int ai, double occ, bool rta) {
+    if (cell < 0 || cell >= C.ncells || C.cell_material[cell] != mid || !isfinite(occ)) {
+        raise_error(L, kErrInvalidStatistics, slot);
+        return;
+    }
+    const size_t h = static_cast<size_t>(cell) * C.hist_modes + ai;
+    atomicAdd(C.hcnt + h, 1u);
+    atomicAdd(C.hE + h, dmul(M.hw[ai], occ - M.nbg[ai]));
+    if (rta) {
+        atomicAdd(C.hN + h, occ);
+        atomicAdd(C.hM + h, fmax(1.0, occ));
+    }
+}
+
+template <bool kGradient, bool kRta>
+__global__ void __launch_bounds__(256) k_transport(const DevTables* __restrict__ Tp, CarrierState S, CellArrays C,
+                                                   DevLedger* L, uint32_t step) {
+    __shared__ BlockLedger bl;
+    block_ledger_init(&bl);
+    __syncthreads();
+    const DevTables& T = *Tp;
+    const int n = L->n_slots;
+    const double dt = T.par.dt;
+    const double half = 0.5 * dt;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (!S.alive[i]) continue;
+        double p[3] = {S.x[i], S.y[i], S.z[i]};
+        uint32_t w = S.mode[i];
+        double occ = S.occ[i];
+        const int mid = static_cast<int>(w >> 28);
+        const DevMaterial& M = T.mat[mid];
+        if (kGradient) {
+            // first gradient half-step, cell sums of the current membership
+            const int c = S.cell[i];
+            const int ai = static_cast<int>(w & 0x00FFFFFFu);
+            const double R = C.grad_R[c], Cs = C.grad_C[c];
+            const double e = half * (M.grad_rate[ai] - R * M.cap_bg[ai] / Cs);
+            const double next = occ + e / M.hw[ai];
+            atomicAdd(&bl.drive_ev, M.hw[ai] * (next - occ));
+            if (e != 0.0) atomicAdd(&bl.drive_updates, 1ull);
+            occ = next;
+        }
+        const bool alive = advance_carrier(T, L, &bl, i, p, w, occ, dt, kDrawTransport, step);
+        S.x[i] = p[0];
+        S.y[i] = p[1];
+        S.z[i] = p[2];
+        S.mode[i] = w;
+        S.occ[i] = occ;
+        if (!alive) {
+            S.alive[i] = 0;
+            continue;
+        }
+        const int c = grid_index(T.dom, p[0], p[1], p[2]);
+        S.cell[i] = c;
+        histogram_add(C, T.mat[w >> 28], L, i, c, static_cast<int>(w >> 28), static_cast<int>(w & 0x00FFFFFFu), occ,
+                      kRta);
+    }
+    __syncthreads();
+    block_ledger_flush(&bl, L);
+}
+
+// Histogram only (initial population or after carriers were replaced).
+template <bool kRta>
+__global__ void k_histogram(const DevTables* __restrict__ Tp, CarrierState S, CellArrays C, DevLedger* L) {
+    const DevTables& T = *Tp;
+    const int n = L->n_slots;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (!S.alive[i]) continue;
+        const uint32_t w = S.mode[i];
+        histogram_add(C, T.mat[w >> 28], L, i, S.cell[i], static_cast<int>(w >> 28),
+                      static_cast<int>(w & 0x00FFFFFFu), S.occ[i], kRta);
+    }
+}
+
+// Cell of every uploaded carrier and the live count (after set_carriers).
+__global__ void k_init_cells(const DevTables* __restrict__ Tp, CarrierState S, DevLedger* L) {
+    const DevDomain& D = Tp->dom;
+    const int n = L->n_slots;
+    unsigned long long live = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        S.cell[i] = grid_index(D, S.x[i], S.y[i], S.z[i]);
+        live += S.alive[i] ? 1 : 0;
+    }
+    for (int o = 16; o > 0; o >>= 1) live += __shfl_xor_sync(0xffffffffu, live, o);
+    if ((threadIdx.x & 31) == 0 && live) atomicAdd(reinterpret_cast<unsigned long long*>(&L->particle_count), live);
+}
+
+// ------------------------------------------------------------ injection
+// Free slots in ascending order: per-block dead counts, one-block scan, write.
+constexpr int kHoleBlock = 1024;
+
+__global__ void __launch_bounds__(kHoleBlock) k_dead_count(CarrierState S, const DevLedger* L, int* block_dead) {
+    const int n = L->n_slots;
+    const int i = blockIdx.x * kHoleBlock + threadIdx.x;
+    const int dead = (i < n && !S.alive[i]) ? 1 : 0;
+    const int c = __syncthreads_count(dead);
+    if (threadIdx.x == 0) block_dead[blockIdx.x] = c;
+}
+
+// Single block: exclusive scan of block counts, emission counts per reservoir
+// (src/solver/ReservoirInjector.cpp:281-284, ReservoirSampler.cpp:117-124).
+__global__ void __launch_bounds__(1024) k_inject_prepare(const DevTables* __restrict__ Tp, DevLedger* L,
+                                                         int* block_dead, int nblocks, int capacity, uint32_t step) {
+    __shared__ int carry;
+    __shared__ int warp_sums[32];
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < nblocks; base += 1024) {
+        const int i = base + threadIdx.x;
+        const int v = i < nblocks ? block_dead[i] : 0;
+        int x = v;
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_sums[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            int s = warp_sums[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, s, o);
+                if (lane >= o) s += y;
+            }
+            warp_sums[lane] = s;
+        }
+        __syncthreads();
+        const int excl = carry + (wid ? warp_sums[wid - 1] : 0) + x - v;
+        if (i < nblocks) block_dead[i] = excl;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = excl + v;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const DevTables& T = *Tp;
+        L->n_holes = carry;
+        int total = 0;
+        for (int r = 0; r < T.par.n_reservoirs; ++r) {
+            const DevReservoir& R = T.res[r];
+            int count;
+            if (T.par.one_to_one) {
+                count = static_cast<int>(L->previous_res[r]);
+            } else {
+                const int base = static_cast<int>(floor(R.expected));
+                const double frac = R.expected - base;
+                const Uniform2 u = uniform2(T.par.seed, static_cast<uint32_t>(r), step, kDrawInjectCount, 0, 0);
+                count = base + ((frac > 0.0 && u.a < frac) ? 1 : 0);
+            }
+            if (count > 0 && !(R.cdf[R.n_cdf - 1] > 0.0)) {
+                raise_error(L, kErrZeroFluxReservoir, r);
+                count = 0;
+            }
+            L->inject_count[r] = count;
+            L->inject_offset[r] = total;
+            total += count;
+        }
+        L->inject_offset[T.par.n_reservoirs] = total;
+        L->n_inject = total;
+        const int extra = total - carry;
+        const long long new_slots = static_cast<long long>(L->n_slots) + (extra > 0 ? extra : 0);
+        if (new_slots > capacity) {
+            raise_error(L, kErrCapacity, static_cast<int>(new_slots > 0x7fffffff ? 0x7fffffff : new_slots));
+            L->n_inject = 0;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kHoleBlock) k_dead_write(CarrierState S, const DevLedger* L, const int* block_off,
+                                                           int* holes) {
+    __shared__ int warp_base[32];
+    const int n = L->n_slots;
+    const int need = L->n_inject;
+    const int i = blockIdx.x * kHoleBlock + threadIdx.x;
+    const bool dead = i < n && !S.alive[i];
+    const unsigned mask = __ballot_sync(0xffffffffu, dead);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) warp_base[wid] = __popc(mask);
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        int x = warp_base[threadIdx.x];
+        const int v = x;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (threadIdx.x >= o) x += y;
+        }
+        warp_base[threadIdx.x] = x - v;
+    }
+    __syncthreads();
+    if (dead) {
+        const int rank = block_off[blockIdx.x] + warp_base[wid] + __popc(mask & ((1u << lane) - 1u));
+        if (rank < need) holes[rank] = i;
+    }
+}
+
+template <bool kRta>
+__global__ void __launch_bounds__(256) k_inject(const DevTables* __restrict__ Tp, CarrierState S, CellArrays C,
+                                                DevLedger* L, const int* holes, uint32_t step) {
+    __shared__ BlockLedger bl;
+    block_ledger_init(&bl);
+    __syncthreads();
+    const DevTables& T = *Tp;
+    const DevParams& P = T.par;
+    const int ni = L->n_inject;
+    const int nh = L->n_holes;
+    const int n_old = L->n_slots;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < ni; j += gridDim.x * blockDim.x) {
+        int r = 0;
+        while (r + 1 < P.n_reservoirs && j >= L->inject_offset[r + 1]) ++r;
+        const int e = j - L->inject_offset[r];
+        const DevReservoir& R = T.res[r];
+        const DevMaterial& M = T.mat[R.material];
+        const Uniform2 d0 = uniform2(P.seed, static_cast<uint32_t>(e), step, kDrawInject, static_cast<uint32_t>(r), 0);
+        const Uniform2 d1 = uniform2(P.seed, static_cast<uint32_t>(e), step, kDrawInject, static_cast<uint32_t>(r), 1);
+        const Uniform2 d2 = uniform2(P.seed, static_cast<uint32_t>(e), step, kDrawInject, static_cast<uint32_t>(r), 2);
+        int lo = 0, hi = R.n_cdf;
+        while (lo < hi) { // lower_bound
+            const int mid = (lo + hi) >> 1;
+            if (R.cdf[mid] < d0.a) lo = mid + 1;
+            else hi = mid;
+        }
+        const int m = lo < R.n_cdf ? lo : R.n_cdf - 1;
+        const double temit = P.dt * d0.b;
+        const int tri = d1.a * (R.area0 + R.area1) < R.area0 ? 0 : 1;
+        const double sr1 = sqrt(d1.b);
+        const double w0 = 1.0 - sr1, w1 = sr1 * (1.0 - d2.a), w2 = sr1 * d2.a;
+        double p[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+            p[a] = dadd(dadd(dmul(w0, R.tri[tri][0][a]), dmul(w1, R.tri[tri][1][a])), dmul(w2, R.tri[tri][2][a]));
+        double v[3] = {M.vel[3 * m], M.vel[3 * m + 1], M.vel[3 * m + 2]};
+        uint32_t signs = 0;
+        if (dadd(dadd(dmul(v[0], R.normal[0]), dmul(v[1], R.normal[1])), dmul(v[2], R.normal[2])) > 0.0) {
+            if (P.conservative) raise_error(L, kErrOutwardReservoirMode, j);
+            for (int a = 0; a < 3; ++a) v[a] = -v[a];
+            signs = 7u;
+        }
+        const double speed = fmax(1e-12, sqrt(dadd(dadd(dmul(v[0], v[0]), dmul(v[1], v[1])), dmul(v[2], v[2]))));
+        const double s = P.push_eps / speed;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], s));
+        double occ = R.occ[m];
+        uint32_t w = static_cast<uint32_t>(m) | (signs << 24) | (static_cast<uint32_t>(R.material) << 28);
+        const int slot = j < nh ? holes[j] : n_old + (j - nh);
+        atomicAdd(&bl.injected_ev, dmul(dmul(M.hw[m], occ - M.nbg[m]), M.energy_weight));
+        const double remain = P.dt - temit;
+        bool alive = true;
+        if (remain > 1e-14) alive = advance_carrier(T, L, &bl, slot, p, w, occ, remain, kDrawInjected, step);
+        S.x[slot] = p[0];
+        S.y[slot] = p[1];
+        S.z[slot] = p[2];
+        S.mode[slot] = w;
+        S.occ[slot] = occ;
+        S.alive[slot] = alive ? 1 : 0;
+        if (alive) {
+            const int c = grid_index(T.dom, p[0], p[1], p[2]);
+            S.cell[slot] = c;
+            histogram_add(C, T.mat[w >> 28], L, slot, c, static_cast<int>(w >> 28), static_cast<int>(w & 0x00FFFFFFu),
+                          occ, kRta);
+        } else {
+            S.cell[slot] = 0;
+        }
+    }
+    __syncthreads();
+    block_ledger_flush(&bl, L);
+}
+
+// Slot count and injected totals after the injection kernel.
+__global__ void k_inject_finish(DevLedger* L) {
+    const int extra = L->n_inject - L->n_holes;
+    if (extra > 0) L->n_slots += extra;
+    L->step_injected += static_cast<unsigned long long>(L->n_inject);
+}
+
+// Escaped-carrier check (src/solver/TransportOperator.cpp:364-402).
+__global__ void k_containment(const DevTables* __restrict__ Tp, CarrierState S, DevLedger* L) {
+    const DevDomain& D = Tp->dom;
+    const int n = L->n_slots;
+    const double tol = 1e-10 * D.scale;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (!S.alive[i]) continue;
+        const double p[3] = {S.x[i], S.y[i], S.z[i]};
+        for (int a = 0; a < 3; ++a)
+            if (!isfinite(p[a]) || p[a] < D.lo[a] - tol || p[a] > D.hi[a] + tol) raise_error(L, kErrEscaped, i);
+    }
+}
+
+// Heat-flux tally q_c = sum v e w (src/solver/GridStatistics.cpp:269-347), into C.flux.
+__global__ void __launch_bounds__(256) k_flux(const DevTables* __restrict__ Tp, CarrierState S, CellArrays C,
+                                              const DevLedger* L, int use_shared) {
+    extern __shared__ double sq[];
+    const DevTables& T = *Tp;
+    if (use_shared)
+        for (int k = threadIdx.x; k < 3 * C.ncells; k += blockDim.x) sq[k] = 0.0;
+    __syncthreads();
+    const int n = L->n_slots;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (!S.alive[i]) continue;
+        const uint32_t w = S.mode[i];
+        const DevMaterial& M = T.mat[w >> 28];
+        const int ai = static_cast<int>(w & 0x00FFFFFFu);
+        const double e = dmul(dmul(M.hw[ai], S.occ[i] - M.nbg[ai]), M.energy_weight);
+        double v[3];
+        mode_velocity(M, w, v);
+        const int c = S.cell[i];
+        double* dst = use_shared ? sq : C.flux;
+        for (int a = 0; a < 3; ++a) atomicAdd(dst + 3 * c + a, dmul(v[a], e));
+    }
+    __syncthreads();
+    if (use_shared)
+        for (int k = threadIdx.x; k < 3 * C.ncells; k += blockDim.x)
+            if (sq[k] != 0.0) atomicAdd(C.flux + k, sq[k]);
+}
+
+// ----------------------------------------------------------- launchers
+void launch_transport(const LaunchCtx& x, bool gradient, bool rta, uint32_t step) {
+    const dim3 grid(x.grid_blocks), block(256);
+    if (gradient) {
+        if (rta) k_transport<true, true><<<grid, block, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
+        else k_transport<true, false><<<grid, block, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
+    } else {
+        if (rta) k_transport<false, true><<<grid, block, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
+        else k_transport<false, false><<<grid, block, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
+    }
+}
+
+void launch_init_cells(const LaunchCtx& x) { k_init_cells<<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.L); }
+
+void launch_histogram(const LaunchCtx& x, bool rta) {
+    if (rta) k_histogram<true><<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.C, x.L);
+    else k_histogram<false><<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.C, x.L);
+}
+
+int launch_inject(const LaunchCtx& x, bool rta, int* holes, int* block_dead, int capacity, uint32_t step) {
+    const int nb = (capacity + kHoleBlock - 1) / kHoleBlock;
+    k_dead_count<<<nb, kHoleBlock, 0, x.stream>>>(x.S, x.L, block_dead);
+    k_inject_prepare<<<1, 1024, 0, x.stream>>>(x.T, x.L, block_dead, nb, capacity, step);
+    k_dead_write<<<nb, kHoleBlock, 0, x.stream>>>(x.S, x.L, block_dead, holes);
+    if (rta) k_inject<true><<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes, step);
+    else k_inject<false><<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes, step);
+    k_inject_finish<<<1, 1, 0, x.stream>>>(x.L);
+    return 5;
+}
+
+void launch_containment(const LaunchCtx& x) {
+    k_containment<<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.L);
+}
+
+void launch_flux(const LaunchCtx& x) {
+    const size_t sh = 3 * sizeof(double) * static_cast<size_t>(x.C.ncells);
+    const int use_shared = sh <= 32768 ? 1 : 0;
+    k_flux<<<x.grid_blocks, 256, use_shared ? sh : 0, x.stream>>>(x.T, x.S, x.C, x.L, use_shared);
+}
+
+} // namespace phmc

@@ -22,8 +22,8 @@ BUILD = os.path.join(HERE, "_build")
 OUT = os.path.join(BUILD, "libphonomc_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CXX_SOURCES = ["phmc_host.cpp"]
-CU_SOURCES = ["phmc_kernels.cu", "phmc_solver.cu", "phmc_capi.cu"]
-HEADERS = ["phmc_host.h", "phmc_pod.h", "phmc_rng.h", "phmc_device.cuh", "phmc_solver.h"]
+CU_SOURCES = ["phmc_transport.cu", "phmc_cells.cu", "phmc_solver.cu", "phmc_capi.cu"]
+HEADERS = ["phmc_host.h", "phmc_pod.h", "phmc_rng.h", "phmc_device.cuh", "phmc_solver.h", "phmc_kernels.cuh"]
 
 _lock = threading.Lock()
 _lib = None
@@ -66,7 +66,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         for src in CXX_SOURCES:
             obj = os.path.join(BUILD, src + ".o")
             objs.append(obj)
-            jobs.append(["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wno-unknown-pragmas", *inc, "-c",
+            jobs.append(["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wno-unknown-pragmas", *inc, "-c",
                          os.path.join(CSRC, src), "-o", obj])
         for src in CU_SOURCES:
             obj = os.path.join(BUILD, src + ".o")

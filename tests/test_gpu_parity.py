@@ -1,0 +1,189 @@
+"""CUDA path against the reference's golden vectors (deterministic sub-steps)
+and against the CPU oracle (whole timesteps), through the C ABI."""
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import golden
+from phonomc_gb300 import abi, synthetic, workloads
+
+pytestmark = pytest.mark.gpu
+
+D = abi.dptr
+I32 = lambda a: a.ctypes.data_as(abi.c_int32_p)  # noqa: E731
+
+
+def _i32(x):
+    return np.ascontiguousarray(x, dtype=np.int32)
+
+
+def _f64(x):
+    return np.ascontiguousarray(x, dtype=np.float64)
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    import phonomc_gb300
+    lib = phonomc_gb300.lib()
+    n = C.c_int32()
+    assert lib.phmc_device_count(C.byref(n)) == 0 and n.value > 0, "no CUDA device"
+    return lib
+
+
+@pytest.fixture(scope="module")
+def orc():
+    import oracle
+    return oracle.load()
+
+
+def test_trace_box_golden(gpu):
+    g = golden("box_trace")
+    p, v = _f64(g["ray_p"]), _f64(g["ray_v"])
+    n = p.shape[0]
+    hit, t, f = np.zeros((n, 3)), np.zeros(n), np.zeros(n, dtype=np.int32)
+    assert gpu.phmc_dev_trace_box(D(_f64([0, 0, 0])), D(_f64([1000, 800, 600])), n, D(p), D(v), D(hit), D(t),
+                                  I32(f)) == 0
+    assert np.array_equal(f, np.asarray(g["hit_f"], dtype=np.int32))  # hit facets bit-exact
+    ok = f >= 0
+    assert np.allclose(t[ok], np.asarray(g["hit_t"])[ok], rtol=1e-12, atol=0)
+    assert np.allclose(hit[ok], np.asarray(g["hit_p"])[ok], rtol=1e-12, atol=1e-12)
+
+
+def test_temperature_from_energy_golden(gpu, m8):
+    g = golden("material_m8")
+    m = abi.Material(gpu, "phmc_", m8, 0.1, False, False)
+    E = _f64(g["inv_E"])
+    T = np.zeros(E.size)
+    assert gpu.phmc_dev_temperature_from_energy(m.h, E.size, D(E), D(T)) == 0
+    assert np.allclose(T, g["inv_T"], rtol=1e-11, atol=1e-9)
+
+
+@pytest.mark.parametrize("name", ["rta_fixed", "rta_local"])
+def test_rta_golden(gpu, m8, name):
+    g = golden(name)
+    m = abi.Material(gpu, "phmc_", m8, 0.1, False, False)
+    flat, cell = _i32(g["flat"]), _i32(g["cell"])
+    occ = _f64(g["occ_in"]).copy()
+    cT = _f64(g["cell_T"])
+    res = C.c_double()
+    rc = gpu.phmc_dev_rta_collide(m.h, flat.size, I32(flat), I32(cell), D(occ), cT.size, D(cT), g["dt"],
+                                  g["particle_volume"], int(g["local"]), g["lifetime_T"], C.byref(res))
+    assert rc == 0, gpu.phmc_last_error()
+    assert np.allclose(occ, g["occ_out"], rtol=1e-12, atol=1e-15)
+    assert abs(res.value - g["residual"]) < 1e-11
+
+
+def test_linearized_rta_golden(gpu, m8):
+    g = golden("linearized_rta")
+    m = abi.Material(gpu, "phmc_", m8, 0.1, True, False)
+    flat, cell = _i32(g["flat"]), _i32(g["cell"])
+    occ = _f64(g["occ_in"]).copy()
+    res = C.c_double()
+    rc = gpu.phmc_dev_linear_collide(m.h, 0, 300.0, flat.size, I32(flat), I32(cell), D(occ), int(cell.max()) + 1,
+                                     g["dt"], g["particle_volume"], C.byref(res))
+    assert rc == 0, gpu.phmc_last_error()
+    assert np.allclose(occ, g["occ_out"], rtol=1e-12, atol=1e-15)
+    assert abs(res.value - g["residual"]) < 1e-13
+
+
+@pytest.mark.parametrize("name,conservative", [("rough_nonconservative", 0), ("rough_conservative", 1)])
+def test_rough_golden(gpu, m8, name, conservative):
+    g = golden(name)
+    m = abi.Material(gpu, "phmc_", m8, 0.1, bool(conservative), False)
+    draws = _f64(g["draws"]).reshape(-1, 3)
+    facet = np.asarray(g["facet"])
+    for f, (normal, rough) in enumerate([((0, 0, -1), 10.0), ((0, 0, 1), 3.0)]):
+        sel = facet == f
+        fin = _i32(np.asarray(g["in_flat"])[sel])
+        oin = _f64(np.asarray(g["in_occ"])[sel])
+        u = _f64(np.clip(draws[sel], 0, None))
+        fo, oo = np.zeros(fin.size, dtype=np.int32), np.zeros(fin.size)
+        rc = gpu.phmc_dev_rough_reflect(m.h, conservative, 300.0, D(_f64(normal)), rough, fin.size, I32(fin), D(oin),
+                                        D(u), I32(fo), D(oo))
+        assert rc == 0, gpu.phmc_last_error()
+        assert np.array_equal(fo, np.asarray(g["out_flat"])[sel])  # outgoing modes bit-exact
+        assert np.allclose(oo, np.asarray(g["out_occ"])[sel], rtol=1e-12, atol=0)
+
+
+def test_gradient_golden(gpu, m8):
+    g = golden("gradient_drive")
+    m = abi.Material(gpu, "phmc_", m8, 0.1, True, False)
+    flat, cell = _i32(g["flat"]), _i32(g["cell"])
+    occ = _f64(g["occ_in"]).copy()
+    e = C.c_double()
+    rc = gpu.phmc_dev_gradient_drive(m.h, 0, g["gradient"], 300.0, flat.size, I32(flat), I32(cell), D(occ), 4,
+                                     g["dt"], g["particle_volume"], C.byref(e))
+    assert rc == 0, gpu.phmc_last_error()
+    assert np.allclose(occ, g["occ_out"], rtol=1e-13, atol=1e-16)
+    assert abs(e.value - g["energy"]) < 1e-15
+
+
+# ------------------------------------------------------------ whole steps
+def _pair(gpu, orc, cfg, stationary, material):
+    mg = abi.Material(gpu, "phmc_", material, 0.1, stationary, False)
+    mo = abi.Material(orc, "orc_", material, 0.1, stationary, False)
+    sg = abi.Solver(gpu, "phmc_", cfg, [mg])
+    so = abi.Solver(orc, "orc_", cfg, [mo])
+    return (sg, mg), (so, mo)
+
+
+def _compare(sg, so, tol=1e-12):
+    cg, co = sg.carriers(), so.carriers()
+    assert cg["alive"].size == co["alive"].size
+    assert np.array_equal(cg["alive"], co["alive"])
+    a = cg["alive"] == 1
+    assert np.array_equal(cg["mode"][a], co["mode"][a])
+    assert np.array_equal(cg["cell"][a], co["cell"][a])
+    for k in ("x", "y", "z"):
+        assert np.allclose(cg[k][a], co[k][a], rtol=tol, atol=1e-9)
+    assert np.allclose(cg["occ"][a], co["occ"][a], rtol=tol, atol=1e-14)
+    Tg, Eg, qg = sg.cells()
+    To, Eo, qo = so.cells()
+    assert np.allclose(Tg, To, rtol=tol, atol=0)
+    assert np.allclose(Eg, Eo, rtol=tol, atol=0)
+    stg, sto = sg.stats(), so.stats()
+    for k in ("particle_count", "absorbed_total", "injected_total", "step_absorbed", "step_injected"):
+        assert stg[k] == sto[k], k
+    for k in ("total_thermal_energy_ev", "step_absorbed_energy_ev", "step_injected_energy_ev"):
+        assert abs(stg[k] - sto[k]) <= 1e-10 * max(1.0, abs(sto[k])), k
+    return stg, sto
+
+
+def test_cross_plane_steps_match_oracle(gpu, orc):
+    mat = synthetic.make_material(mesh=16)
+    cfg = workloads.scaled(workloads.cross_plane_film(), 20000, random_seed=7)
+    (sg, _), (so, _) = _pair(gpu, orc, cfg, False, mat)
+    _compare(sg, so)
+    for _ in range(3):
+        sg.run(2)
+        so.run(2)
+        _compare(sg, so)
+
+
+def test_inplane_gradient_steps_match_oracle(gpu, orc):
+    mat = synthetic.make_material(mesh=16)
+    cfg = workloads.scaled(workloads.inplane_gradient(), 20000, random_seed=9)
+    (sg, _), (so, _) = _pair(gpu, orc, cfg, True, mat)
+    for _ in range(3):
+        sg.run(2)
+        so.run(2)
+        stg, sto = _compare(sg, so)
+        assert abs(stg["total_gradient_energy_ev"] - sto["total_gradient_energy_ev"]) < 1e-12
+        assert stg["step_gradient_updates"] == sto["step_gradient_updates"]
+
+
+def test_energy_ledger_closes_on_device(gpu):
+    """Energy bookkeeping closes to FP64 round-off at a larger size (property)."""
+    mat = synthetic.make_material(mesh=16)
+    cfg = workloads.scaled(workloads.cross_plane_film(), 400000, random_seed=3)
+    m = abi.Material(gpu, "phmc_", mat, 0.1, False, False)
+    s = abi.Solver(gpu, "phmc_", cfg, [m])
+    s.run(20)
+    st = s.stats()
+    scale = abs(st["step_absorbed_energy_ev"]) + abs(st["step_injected_energy_ev"]) + 1e-30
+    assert abs(st["step_energy_balance_residual_ev"]) < 1e-9 * max(scale, abs(st["total_thermal_energy_ev"]))
+    T, _, _ = s.cells()
+    assert np.all(T > 298.0) and np.all(T < 302.0)
+    assert st["particle_count"] > 0.9 * 400000
