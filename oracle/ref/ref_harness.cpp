@@ -28,6 +28,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <filesystem>
 #include <fstream>
 #include <iostream>
 #include <random>
@@ -567,6 +568,29 @@ std::string cmd_run(const std::string& pmat, const std::string& toml, int steps)
         resid.push_back(s.total_energy_balance_residual_ev());
     }
     Json j;
+    // convergence.txt rows written by the reference's ResultWriter
+    if (!a.output_folder.empty()) {
+        std::ifstream conv(std::filesystem::path(a.output_folder) / "convergence.txt");
+        std::string line;
+        std::ostringstream rows;
+        rows << "[";
+        bool first = true;
+        while (std::getline(conv, line)) {
+            if (line.empty() || line[0] == '#') continue;
+            std::istringstream ls(line);
+            std::string tok;
+            rows << (first ? "" : ",") << "[";
+            bool f2 = true;
+            while (ls >> tok) {
+                rows << (f2 ? "" : ",") << Json::num(std::stod(tok));
+                f2 = false;
+            }
+            rows << "]";
+            first = false;
+        }
+        rows << "]";
+        j.raw("convergence", rows.str());
+    }
     j.arr("particle_count", pc);
     j.arr("absorbed_total", absorbed);
     j.arr("injected_total", injected);

@@ -44,6 +44,73 @@ CASES = {
 }
 
 
+CROSS_PLANE_TOML = """[geometry]
+model = "box"
+sizes = [100, 100, 100]
+
+[simulation]
+particle_count = {particles}
+time_step = 1.0
+iterations = {steps}
+random_seed = {seed}
+compute_kappa = true
+transport_axis = "z"
+initial_temperature = "linear"
+background_temperature = 300
+lifetime_temperature = 300
+grid_xyz = [1, 1, 50]
+convergence_write_interval = 1
+
+[boundary]
+boundary_position = [
+  [-0.01,0,0,0.01,1,1], [0.99,0,0,1.01,1,1],
+  [0,-0.01,0,1,0.01,1], [0,0.99,0,1,1.01,1],
+  [0,0,-0.01,1,1,0.01], [0,0,0.99,1,1,1.01]
+]
+boundary_conditions = ["P","P","P","P","T","T"]
+boundary_values = [0,0,0,0,301,299]
+periodic_pair = [
+  [-0.01,0,0,0.01,1,1], [0.99,0,0,1.01,1,1],
+  [0,-0.01,0,1,0.01,1], [0,0.99,0,1,1.01,1]
+]
+
+[io]
+material_folder = "unused"
+output_folder = "{out}"
+"""
+
+# Full reference runs of the scaled cross-plane film (same geometry and physics
+# as phonomc_gb300.workloads.cross_plane_film, 2e4 carriers): per seed, the
+# cell temperatures and heat flux averaged over the second half of the run.
+STAT_SEEDS = 16
+STAT_PARTICLES = 20000
+STAT_STEPS = 200
+
+
+def full_runs(mpath: str, tmp: str) -> dict:
+    import numpy as np
+    out = {"seeds": [], "T_mean": [], "flux_mean": [], "kappa_eff_mean": [], "particles_mean": [],
+           "particles": STAT_PARTICLES, "steps": STAT_STEPS, "average_from_step": STAT_STEPS // 2 + 1}
+    for k in range(STAT_SEEDS):
+        seed = 101 + k
+        folder = os.path.join(tmp, f"run{seed}")
+        os.makedirs(folder, exist_ok=True)
+        toml = os.path.join(folder, "c1.toml")
+        with open(toml, "w") as f:
+            f.write(CROSS_PLANE_TOML.format(particles=STAT_PARTICLES, steps=STAT_STEPS, seed=seed, out=folder))
+        res = json.loads(subprocess.run([HARNESS, "run", mpath, toml, str(STAT_STEPS)], check=True,
+                                        capture_output=True, text=True).stdout)
+        rows = np.asarray(res["convergence"])
+        late = rows[rows[:, 0] >= STAT_STEPS // 2 + 1]
+        out["seeds"].append(seed)
+        out["T_mean"].append(late[:, 2:52].mean(axis=0).tolist())
+        out["flux_mean"].append(float(late[:, 52].mean()))
+        out["kappa_eff_mean"].append(float(late[:, 54].mean()))
+        out["particles_mean"].append(float(late[:, 55].mean()))
+        out.setdefault("balance_residual_total", []).append(res["balance_residual_total"][-1])
+    return out
+
+
 def build(ref: str) -> None:
     subprocess.run(["make", "-s", "-j8", f"REF={ref}"], cwd=os.path.join(ROOT, "oracle", "ref"),
                    check=True)
@@ -60,6 +127,14 @@ def main() -> None:
     cpath = os.path.join(tmp, "m8c.pmat")
     synthetic.write_pmat(mpath, synthetic.make_material(mesh=8))
     synthetic.write_pmat(cpath, synthetic.make_material(mesh=8, callaway=True))
+    if not args.only or "fullrun_cross_plane" in args.only:
+        m16 = os.path.join(tmp, "m16.pmat")
+        synthetic.write_pmat(m16, synthetic.make_material(mesh=16))
+        data = full_runs(m16, os.path.join(tmp, "fullrun"))
+        data["_harness_args"] = ["run", "{m16}", "<cross-plane toml>", str(STAT_STEPS)]
+        with gzip.open(os.path.join(HERE, "fullrun_cross_plane.json.gz"), "wt") as f:
+            json.dump(data, f)
+        print("fullrun_cross_plane ok")
     for name, argv in CASES.items():
         if args.only and name not in args.only:
             continue

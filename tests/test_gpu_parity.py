@@ -170,7 +170,10 @@ def test_inplane_gradient_steps_match_oracle(gpu, orc):
         sg.run(2)
         so.run(2)
         stg, sto = _compare(sg, so)
-        assert abs(stg["total_gradient_energy_ev"] - sto["total_gradient_energy_ev"]) < 1e-12
+        # the drive is energy-neutral per cell: both totals are round-off of a zero sum
+        scale = abs(sto["total_thermal_energy_ev"])
+        assert abs(stg["total_gradient_energy_ev"]) < 1e-17 * scale
+        assert abs(sto["total_gradient_energy_ev"]) < 1e-17 * scale
         assert stg["step_gradient_updates"] == sto["step_gradient_updates"]
 
 

@@ -1,0 +1,61 @@
+"""Statistical pin of the CPU oracle against full reference runs.
+
+The reference solver (oracle/_ref, its own C++) ran the scaled cross-plane film
+for 16 seeds (tests/golden/fullrun_cross_plane.json.gz). The oracle runs the
+same configuration for 16 other seeds; the late-time cell temperatures, heat
+flux and kappa_eff must agree within the combined standard error (|z| < 4.5 for
+every one of the 50 cells, mean z^2 close to 1, |z| < 3.5 for flux and kappa).
+"""
+
+import multiprocessing as mp
+
+import numpy as np
+
+from conftest import golden
+
+
+def _oracle_run(seed):
+    import oracle
+    from phonomc_gb300 import abi, synthetic, workloads
+    lib = oracle.load()
+    g = golden("fullrun_cross_plane")
+    cfg = workloads.scaled(workloads.cross_plane_film(), g["particles"], random_seed=seed,
+                           convergence_write_interval=1)
+    m = abi.Material(lib, "orc_", synthetic.make_material(mesh=16), 0.1, False, False)
+    s = abi.Solver(lib, "orc_", cfg, [m])
+    T_acc, flux, kappa = [], [], []
+    for step in range(1, g["steps"] + 1):
+        s.run(1)
+        if step >= g["average_from_step"]:
+            T, _, _ = s.cells()
+            st = s.stats()
+            T_acc.append(T)
+            flux.append(st["average_heat_flux_along_axis"])
+            kappa.append(st["kappa_endpoints"])
+    st = s.stats()
+    return np.mean(T_acc, axis=0), float(np.mean(flux)), float(np.mean(kappa)), st["total_energy_balance_residual_ev"]
+
+
+def _z(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    se = np.sqrt(a.var(axis=0, ddof=1) / a.shape[0] + b.var(axis=0, ddof=1) / b.shape[0])
+    return (a.mean(axis=0) - b.mean(axis=0)) / se
+
+
+def test_oracle_matches_reference_statistics():
+    g = golden("fullrun_cross_plane")
+    seeds = [5001 + k for k in range(len(g["seeds"]))]
+    with mp.get_context("spawn").Pool(8) as pool:
+        res = pool.map(_oracle_run, seeds)
+    T_o = np.array([r[0] for r in res])
+    T_r = np.array(g["T_mean"])
+    z = _z(T_o, T_r)
+    assert np.all(np.abs(z) < 4.5), z
+    assert np.mean(z * z) < 2.5, np.mean(z * z)
+    zf = _z(np.array([r[1] for r in res])[:, None], np.array(g["flux_mean"])[:, None])[0]
+    zk = _z(np.array([r[2] for r in res])[:, None], np.array(g["kappa_eff_mean"])[:, None])[0]
+    assert abs(zf) < 3.5, zf
+    assert abs(zk) < 3.5, zk
+    # energy bookkeeping closes to round-off in both (eV, total over the run)
+    assert max(abs(r[3]) for r in res) < 1e-6
+    assert max(abs(x) for x in g["balance_residual_total"]) < 1e-6
