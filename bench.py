@@ -36,7 +36,7 @@ METRIC = "carrier-steps/s on 1 GB300: batched mixed-prec vs plain FP64 at equal 
 UNIT = "carrier-steps/s"
 # Algorithmic bytes per carrier-step of the transport pass: read position,
 # occupation, mode and cell; write position, occupation and cell.
-BYTES_PER_CARRIER = {"fp64": 76, "mixed": 52}
+BYTES_PER_CARRIER = {"fp64": 76, "mixed": 52}  # FP64 state / FP32 cell-local offsets
 
 
 def workload_config(name, particles, precision, seed=12345):
@@ -156,46 +156,56 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def _time_arm(lib, abi, cfg, material, steps, warmup, stationary):
+    m = abi.Material(lib, "phmc_", material, 0.1, stationary, False)
+    s = abi.Solver(lib, "phmc_", cfg, [m])
+    s.run(warmup)
+    n0 = s.stats()["particle_count"]
+    tot, kern, launches = C.c_double(), C.c_double(), C.c_int64()
+    with ClockSampler() as clk:
+        s.check(lib.phmc_solver_timed_run(s.h, steps, C.byref(tot), C.byref(kern), C.byref(launches)))
+    n1 = s.stats()["particle_count"]
+    return {"solver": s, "material": m, "ms": tot.value, "kernel_ms": kern.value, "launches": int(launches.value),
+            "carrier_steps": 0.5 * (n0 + n1) * steps, "carriers": n0, "clocks": clk.summary()}
+
+
 def run_ours(args):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
     import phonomc_gb300
     from phonomc_gb300 import abi, synthetic
     lib = phonomc_gb300.lib()
-    cfg = workload_config(args.workload, args.particles, args.precision, seed=12345 + rank)
+    material = synthetic.make_material(mesh=16)
     stationary = args.workload == "inplane_gradient"
-    m = abi.Material(lib, "phmc_", synthetic.make_material(mesh=16), 0.1, stationary, False)
-    s = abi.Solver(lib, "phmc_", cfg, [m])
-    s.run(args.warmup)
-    n_carriers = s.stats()["particle_count"]
-    tot, kern, launches = C.c_double(), C.c_double(), C.c_int64()
-    with ClockSampler() as clk:
-        s.check(lib.phmc_solver_timed_run(s.h, args.steps, C.byref(tot), C.byref(kern), C.byref(launches)))
-    st = s.stats()
-    n_after = st["particle_count"]
-    carrier_steps = 0.5 * (n_carriers + n_after) * args.steps
-    ms = tot.value
-    value_rank = carrier_steps / (ms * 1e-3)
+    seed = 12345 + rank
+    # headline: the requested precision (mixed by default); comparison arm: plain FP64
+    main_arm = _time_arm(lib, abi, workload_config(args.workload, args.particles, args.precision, seed), material,
+                         args.steps, args.warmup, stationary)
+    plain = None
+    if args.precision == "mixed" and not args.no_plain:
+        plain = _time_arm(lib, abi, workload_config(args.workload, args.particles, "fp64", seed), material,
+                          max(3, args.steps // 4), args.warmup, stationary)
+        plain["solver"].close()
+    ms, carrier_steps = main_arm["ms"], main_arm["carrier_steps"]
     if world > 1:
-        import torch.distributed as dist
         import torch
+        import torch.distributed as dist
         dist.init_process_group("gloo")
         t = torch.tensor([ms, carrier_steps], dtype=torch.float64)
-        mx = t.clone()
+        mx, sm = t.clone(), t.clone()
         dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        sm = t.clone()
         dist.all_reduce(sm, op=dist.ReduceOp.SUM)
-        ms = float(mx[0])
-        carrier_steps = float(sm[1])
+        ms, carrier_steps = float(mx[0]), float(sm[1])
     value = carrier_steps / (ms * 1e-3)
     bpc = BYTES_PER_CARRIER[args.precision]
-    kavg = kern.value / args.steps
-    achieved = bpc * n_carriers / (kavg * 1e-3) / 1e9
+    kavg = main_arm["kernel_ms"] / args.steps
+    achieved = bpc * main_arm["carriers"] / (kavg * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
 
-    # end to end through the C ABI from pinned host buffers
+    # end to end through the C ABI from pinned host buffers: every step uploads
+    # the carriers (positions, occupation, mode), runs one timestep and reads
+    # the cell temperatures back
+    s = main_arm["solver"]
     c = s.carriers()
     live = c["alive"] == 1
     host = {k: np.ascontiguousarray(c[k][live]) for k in ("x", "y", "z", "occ")}
@@ -222,14 +232,21 @@ def run_ours(args):
         "config": {"workload": args.workload, "particles": int(args.particles), "precision": args.precision,
                    "material": "synthetic 16^3 x 6 modes (seed 0)", "cells": int(Tout.size),
                    "l2": "carrier state larger than L2 (no flush needed)", "replicas": world},
-        "gpu_launches": int(launches.value),
-        "roofline": {"bound": "hbm", "kernel": "k_transport (pass A)", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+        "gpu_launches": main_arm["launches"],
+        "roofline": {"bound": "hbm", "kernel": "k_transport (the one carrier pass of a step)", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                      "bytes_per_carrier": bpc, "kernel_ms_per_launch": kavg, "traffic": None},
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": int(n * (4 * 8 + 4)), "d2h_bytes_per_step": int(Tout.size * 8)},
-        "clocks": clk.summary(),
+        "clocks": main_arm["clocks"],
     }
+    if plain is not None:
+        pv = plain["carrier_steps"] / (plain["ms"] * 1e-3)
+        pk = plain["kernel_ms"] / max(1, round(plain["carrier_steps"] / max(1, plain["carriers"])))
+        line["plain_fp64"] = {"value": pv, "unit": UNIT, "ms_per_step": plain["ms"] / max(3, args.steps // 4),
+                              "mixed_over_plain": value / pv,
+                              "roofline_frac": 76 * plain["carriers"] / (pk * 1e-3) / 1e9 / peak,
+                              "clocks": plain["clocks"]}
     if rank == 0 and not args.no_cpu_baseline:
         cb, info = cpu_baseline(args.workload, 200000, 10, 3, 1, 1)
         line["cpu_baseline"] = {"value": cb, "unit": UNIT, "cores": 1, "kind": "port",
@@ -246,7 +263,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="inplane_gradient", choices=["inplane_gradient", "cross_plane_film"])
     ap.add_argument("--particles", type=float, default=None)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.particles is None:

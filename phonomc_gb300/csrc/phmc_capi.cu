@@ -155,12 +155,11 @@ int phmc_material_active_count(const phmc_material* m, int* n) {
 
 int phmc_solver_create(const phmc_config* cfg, phmc_material* const* materials, int n_materials, phmc_solver** out) {
     return guard([&] {
-        if (cfg->precision != 0) throw std::invalid_argument("mixed precision state is built by phmc_solver_create only with precision=0 in this build");
         SimulationConfig c = config_from_pod(*cfg);
         std::vector<const PhononMaterial*> ms;
         for (int i = 0; i < n_materials; ++i) ms.push_back(materials[i]->m.get());
         auto s = std::make_unique<phmc_solver>();
-        s->s = std::make_unique<DeviceSolver>(c, ms);
+        s->s = std::make_unique<DeviceSolver>(c, ms, true, cfg->precision == 1);
         *out = s.release();
     });
 }

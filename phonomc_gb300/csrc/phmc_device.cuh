@@ -49,7 +49,10 @@ struct DevMaterial {
     const double* hw;       // [active]
     const double* inv_hw;   // [active]
     const double* vel;      // [active*3]
-    const float* vel32;     // [active*4] (x, y, z, |v|) for the mixed path
+    const float* vel32;     // [active*4] (vx, vy, vz, 0) for the mixed path
+    const float* ivel32;    // [active*4] (1/vx, 1/vy, 1/vz, 0); 0 where v = 0
+    const double* speed;    // [active] |v|
+    const double* push;     // [active] push_eps / max(|v|, 1e-12)
     const double* nbg;      // [active]
     const double* cap_bg;   // [active]
     const int* mode_class;  // [active]
@@ -146,6 +149,8 @@ struct DevLedger {
     double step_absorbed_ev, step_injected_ev;
     double step_lifetime_residual, step_drive_ev;
     unsigned long long step_drive_updates;
+    double next_drive_ev;                  // first gradient half-step of the next step
+    unsigned long long next_drive_updates;
     double step_balance_residual;
     double thermal_energy;
     // totals
@@ -164,10 +169,10 @@ struct DevTables {
 };
 
 struct CarrierState {
-    double* x;
+    double* x;   // plain path positions; staging for uploads/downloads in the mixed path
     double* y;
     double* z;
-    float* ox;
+    float* ox;   // mixed path: offset from the lower corner of the carrier's cell
     float* oy;
     float* oz;
     double* occ;
@@ -261,9 +266,8 @@ __device__ __forceinline__ bool box_contains(const DevDomain& D, const double p[
 }
 
 // Wall-hit cache with the reference's nudged retries (src/solver/TransportOperator.cpp:186-250).
-__device__ __forceinline__ bool cache_hit(const DevDomain& D, const DevParams& P, double p[3], const double v[3], double cp[3],
-                          double& t, int& f) {
-    const double speed = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+__device__ __forceinline__ bool cache_hit(const DevDomain& D, const DevParams& P, double p[3], const double v[3],
+                                          double speed, double cp[3], double& t, int& f) {
     if (isfinite(speed) && speed <= 1e-18) {
         t = __longlong_as_double(0x7ff0000000000000LL);
         f = -1;

@@ -21,20 +21,19 @@ struct LaunchCtx {
     int grid_blocks;
 };
 
-void launch_transport(const LaunchCtx& x, bool gradient, bool rta, uint32_t step);
-void launch_transport_mixed(const LaunchCtx& x, bool gradient, uint32_t step);
+void launch_transport(const LaunchCtx& x, bool mixed, bool rta, uint32_t step);
 void launch_histogram(const LaunchCtx& x, bool rta);
-void launch_init_cells(const LaunchCtx& x);
-int launch_inject(const LaunchCtx& x, bool rta, int* holes, int* block_dead, int capacity, uint32_t step);
-void launch_containment(const LaunchCtx& x);
-void launch_flux(const LaunchCtx& x);
+void launch_init_cells(const LaunchCtx& x, bool mixed);
+void launch_positions_out(const LaunchCtx& x);
+int launch_inject(const LaunchCtx& x, bool mixed, bool rta, int* holes, int* block_dead, int capacity, uint32_t step);
+void launch_containment(const LaunchCtx& x, bool mixed);
+void launch_flux(const LaunchCtx& x, bool mixed);
+void launch_apply_pending(const LaunchCtx& x, bool subtract_drive);
 void launch_step_begin(const LaunchCtx& x);
-void launch_cell_solve(const LaunchCtx& x, int phase, int collision, int n_classes, const int* class_start,
-                       const int* class_modes, double* lin_scratch);
-void launch_update(const LaunchCtx& x, int collision, bool gradient);
+void launch_cell_solve(const LaunchCtx& x, int phase, int collision);
 void launch_cells_final(const LaunchCtx& x, int initial);
 
-// collision kinds for launch_cell_solve / launch_update
+// collision kinds for launch_cell_solve
 enum CollisionKind : int { kCollideNone = 0, kCollideRta = 1, kCollideLinear = 2 };
 
 } // namespace phmc

@@ -53,8 +53,8 @@ static const char* error_message(int code) {
 }
 
 DeviceSolver::DeviceSolver(const SimulationConfig& cfg, const std::vector<const PhononMaterial*>& mats,
-                           bool init_carriers)
-    : cfg_(cfg), mats_(mats) {
+                           bool init_carriers, bool mixed)
+    : cfg_(cfg), mats_(mats), mixed_(mixed) {
     int dev_count = 0;
     if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count <= 0)
         throw std::runtime_error("No CUDA device is available for the GB300 carrier loop.");
@@ -63,7 +63,6 @@ DeviceSolver::DeviceSolver(const SimulationConfig& cfg, const std::vector<const 
     domain_ = std::make_unique<SimulationDomain>(cfg_);
     P_ = build_problem(cfg_, *domain_, mats_);
     ncells_ = domain_->grid_count();
-    mixed_ = false;
     const int n0 = P_.initial_particles;
     const int margin = P_.reservoirs.empty() ? 1024 : std::max(65536, n0 / 4);
     allocate_state(n0 + margin);
@@ -92,6 +91,11 @@ void DeviceSolver::allocate_state(int capacity) {
     state_.x = dalloc<double>(capacity);
     state_.y = dalloc<double>(capacity);
     state_.z = dalloc<double>(capacity);
+    if (mixed_) {
+        state_.ox = dalloc<float>(capacity);
+        state_.oy = dalloc<float>(capacity);
+        state_.oz = dalloc<float>(capacity);
+    }
     state_.occ = dalloc<double>(capacity);
     state_.mode = dalloc<uint32_t>(capacity);
     state_.cell = dalloc<int32_t>(capacity);
@@ -128,9 +132,23 @@ void DeviceSolver::upload_tables() {
             v32[4 * a] = static_cast<float>(vx);
             v32[4 * a + 1] = static_cast<float>(vy);
             v32[4 * a + 2] = static_cast<float>(vz);
-            v32[4 * a + 3] = static_cast<float>(std::sqrt(vx * vx + vy * vy + vz * vz));
+            v32[4 * a + 3] = 0.0f;
         }
         D.vel32 = upload(v32);
+        std::vector<float> iv32(4 * static_cast<size_t>(M.n_active), 0.0f);
+        std::vector<double> speed(M.n_active), push(M.n_active);
+        for (int a = 0; a < M.n_active; ++a) {
+            for (int k = 0; k < 3; ++k) {
+                const float c = v32[4 * a + k];
+                iv32[4 * a + k] = c != 0.0f ? 1.0f / c : 0.0f;
+            }
+            const double vx = M.vel[3 * a], vy = M.vel[3 * a + 1], vz = M.vel[3 * a + 2];
+            speed[a] = std::sqrt(vx * vx + vy * vy + vz * vz);
+            push[a] = P_.push_eps / std::max(speed[a], 1e-12);
+        }
+        D.ivel32 = upload(iv32);
+        D.speed = upload(speed);
+        D.push = upload(push);
         D.nbg = upload(M.nbg);
         D.cap_bg = upload(M.capacity_bg);
         D.mode_class = upload(M.mode_class);
@@ -247,32 +265,40 @@ void DeviceSolver::upload_tables() {
     CellArrays& C = cells_;
     C.ncells = ncells_;
     C.hist_modes = hist_modes;
+    C.mixed = mixed_ ? 1 : 0;
     C.cell_material = upload(P_.cell_material);
     C.volume = upload(domain_->grid_volumes());
     const size_t hist = static_cast<size_t>(ncells_) * hist_modes;
-    C.hcnt = dalloc<unsigned int>(hist);
-    C.hE = dalloc<double>(hist);
     const bool rta = !P_.linearized;
-    if (rta) {
-        C.hN = dalloc<double>(hist);
-        C.hM = dalloc<double>(hist);
-        const size_t nc = static_cast<size_t>(ncells_) * P_.mats[0].n_classes;
-        C.rta_a = dalloc<double>(nc);
-        C.rta_B = dalloc<double>(nc);
-    }
+    C.hcnt = dalloc<unsigned int>(hist);
+    C.hN = dalloc<double>(hist);
+    C.hM = rta ? dalloc<double>(hist) : nullptr;
+    C.ab = dalloc<double2>(hist);
     C.energy = dalloc<double>(ncells_);
     C.temperature = dalloc<double>(ncells_);
-    C.grad_R = dalloc<double>(ncells_);
-    C.grad_C = dalloc<double>(ncells_);
-    C.acc = dalloc<double>(ncells_);
+    C.energy_final = dalloc<double>(ncells_);
+    C.temperature_final = dalloc<double>(ncells_);
+    C.grad_ratio = dalloc<double>(ncells_);
     C.flux = dalloc<double>(3 * static_cast<size_t>(ncells_));
-    if (P_.linearized) {
+    const MaterialTables& M0 = P_.mats[0];
+    if (rta) {
+        // class CSR of material 0 for the RTA solve
+        std::vector<int> start(M0.n_classes + 1, 0), modes(M0.n_active);
+        for (int a = 0; a < M0.n_active; ++a) ++start[M0.mode_class[a] + 1];
+        for (int k = 0; k < M0.n_classes; ++k) start[k + 1] += start[k];
+        std::vector<int> cursor(start.begin(), start.end() - 1);
+        for (int a = 0; a < M0.n_active; ++a) modes[cursor[M0.mode_class[a]]++] = a;
+        C.class_start = upload(start);
+        C.class_modes = upload(modes);
+        C.n_classes = M0.n_classes;
+        C.scratch = dalloc<double>(static_cast<size_t>(ncells_) * (5 * static_cast<size_t>(M0.n_classes) + 2 * hist_modes));
+    } else {
         if (P_.mats.size() != 1) throw std::runtime_error("Linear-response collisions support one material in this build.");
-        C.lin_A = dalloc<double>(hist);
+        C.scratch = dalloc<double>(static_cast<size_t>(ncells_) * hist_modes * (8 + 2));
         const int S = std::max(1, static_cast<int>(std::ceil(cfg_.time_step * r_max)));
         const double h = cfg_.time_step / S;
         const double x = h * r_max;
-        // smallest K with x^(K+1)/(K+1)! <= 1e-17, x = h * max rate <= 1
+        // smallest K with x^(K+1)/(K+1)! <= 1e-17 (x = h * max rate <= 1)
         int K = 1;
         double bound = x;
         while (K < 40) {
@@ -283,23 +309,21 @@ void DeviceSolver::upload_tables() {
         C.lin_substeps = S;
         C.lin_h = h;
         C.lin_terms = std::max(1, K);
-        std::vector<double> decay(P_.mats[0].n_active);
-        for (int a = 0; a < P_.mats[0].n_active; ++a)
-            decay[a] = std::exp(-(P_.mats[0].col_normal[a] + P_.mats[0].col_resistive[a]) * cfg_.time_step);
+        std::vector<double> decay(M0.n_active), sc(M0.n_active), srn(M0.n_active), srr(M0.n_active);
+        bool has_normal = false;
+        for (int a = 0; a < M0.n_active; ++a) {
+            decay[a] = std::exp(-(M0.col_normal[a] + M0.col_resistive[a]) * cfg_.time_step);
+            sc[a] = std::sqrt(M0.col_capacity[a]);
+            srn[a] = std::sqrt(M0.col_normal[a]);
+            srr[a] = std::sqrt(M0.col_resistive[a]);
+            has_normal = has_normal || M0.col_normal[a] > 0.0;
+        }
         C.lin_decay = upload(decay);
+        C.lin_s = upload(sc);
+        C.lin_sqrt_rn = upload(srn);
+        C.lin_sqrt_rr = upload(srr);
+        C.lin_has_normal = has_normal ? 1 : 0;
     }
-    scratch_ = nullptr;
-    if (P_.linearized) scratch_ = dalloc<double>(hist * 8);
-    else scratch_ = dalloc<double>(static_cast<size_t>(ncells_) * P_.mats[0].n_classes * 3);
-    // class CSR of material 0
-    const MaterialTables& M0 = P_.mats[0];
-    std::vector<int> start(M0.n_classes + 1, 0), modes(M0.n_active);
-    for (int a = 0; a < M0.n_active; ++a) ++start[M0.mode_class[a] + 1];
-    for (int k = 0; k < M0.n_classes; ++k) start[k + 1] += start[k];
-    std::vector<int> cursor(start.begin(), start.end() - 1);
-    for (int a = 0; a < M0.n_active; ++a) modes[cursor[M0.mode_class[a]]++] = a;
-    class_start_ = upload(start);
-    class_modes_ = upload(modes);
 }
 
 LaunchCtx DeviceSolver::ctx() const {
@@ -320,9 +344,10 @@ int DeviceSolver::collision_kind() const {
 void DeviceSolver::initial_statistics() {
     const LaunchCtx x = ctx();
     launch_histogram(x, !P_.linearized);
-    launch_cell_solve(x, 0, collision_kind(), P_.mats[0].n_classes, class_start_, class_modes_, scratch_);
+    launch_cell_solve(x, 0, collision_kind());
     launch_cells_final(x, 1);
     counters_.launches += 3;
+    materialized_ = true;
 }
 
 void DeviceSolver::set_carriers(long long n, const double* x, const double* y, const double* z, const double* occ,
@@ -342,7 +367,7 @@ void DeviceSolver::set_carriers(long long n, const double* x, const double* y, c
     step_ = 0;
     elapsed_ = 0;
     failed_ = false;
-    launch_init_cells(ctx());
+    launch_init_cells(ctx(), mixed_);
     counters_.launches += 1;
     initial_statistics();
     synchronize();
@@ -352,7 +377,6 @@ void DeviceSolver::run_timestep() {
     if (failed_) throw std::runtime_error("Cannot resume a failed timestep; construct a new solver after fixing its cause.");
     failed_ = true;
     const LaunchCtx x = ctx();
-    const bool gradient = cfg_.temperature_gradient.has_value();
     const int coll = collision_kind();
     launch_step_begin(x);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -361,22 +385,23 @@ void DeviceSolver::run_timestep() {
         PHMC_CUDA(cudaEventCreate(&e1));
         PHMC_CUDA(cudaEventRecord(e0, stream_));
     }
-    launch_transport(x, gradient, coll == kCollideRta, static_cast<uint32_t>(step_));
+    launch_transport(x, mixed_, coll == kCollideRta, static_cast<uint32_t>(step_));
     if (profile_pass_a_) {
         PHMC_CUDA(cudaEventRecord(e1, stream_));
         pass_a_events_.push_back({e0, e1});
     }
     counters_.launches += 2;
-    if (!P_.reservoirs.empty()) counters_.launches += launch_inject(x, coll == kCollideRta, d_holes_, d_block_dead_,
-                                                                   state_.capacity, static_cast<uint32_t>(step_));
+    if (!P_.reservoirs.empty())
+        counters_.launches += launch_inject(x, mixed_, coll == kCollideRta, d_holes_, d_block_dead_, state_.capacity,
+                                            static_cast<uint32_t>(step_));
     if (step_ % 100 == 0) {
-        launch_containment(x);
+        launch_containment(x, mixed_);
         counters_.launches += 1;
     }
-    launch_cell_solve(x, 1, coll, P_.mats[0].n_classes, class_start_, class_modes_, scratch_);
-    launch_update(x, coll, gradient);
+    launch_cell_solve(x, 1, coll);
     launch_cells_final(x, 0);
-    counters_.launches += 3;
+    counters_.launches += 2;
+    materialized_ = false;
     ++step_;
     elapsed_ += cfg_.time_step;
     if (step_ == 1 || step_ % cfg_.convergence_write_interval == 0) {
@@ -384,6 +409,13 @@ void DeviceSolver::run_timestep() {
         append_convergence_row();
     }
     failed_ = false;
+}
+
+void DeviceSolver::materialize() {
+    if (materialized_) return;
+    launch_apply_pending(ctx(), true);
+    counters_.launches += 2;
+    materialized_ = true;
 }
 
 double DeviceSolver::collide_only(const double* cell_temperature) {
@@ -396,27 +428,25 @@ double DeviceSolver::collide_only(const double* cell_temperature) {
                                   cudaMemcpyHostToDevice, stream_));
         phase = 2;
     }
-    launch_cell_solve(x, phase, collision_kind(), P_.mats[0].n_classes, class_start_, class_modes_, scratch_);
-    launch_update(x, collision_kind(), false);
-    counters_.launches += 4;
+    launch_cell_solve(x, phase, collision_kind());
+    launch_apply_pending(x, false);
+    counters_.launches += 5;
     synchronize();
-    PHMC_CUDA(cudaMemsetAsync(cells_.acc, 0, ncells_ * sizeof(double), stream_));
     double r = 0;
     PHMC_CUDA(cudaMemcpy(&r, &d_ledger_->step_lifetime_residual, sizeof(double), cudaMemcpyDeviceToHost));
+    materialized_ = true;
     return r;
 }
 
 double DeviceSolver::drive_only() {
     const LaunchCtx x = ctx();
-    launch_step_begin(x);
-    launch_histogram(x, !P_.linearized);
-    launch_cell_solve(x, 0, collision_kind(), P_.mats[0].n_classes, class_start_, class_modes_, scratch_);
-    launch_update(x, kCollideNone, true);
-    counters_.launches += 4;
-    synchronize();
-    PHMC_CUDA(cudaMemsetAsync(cells_.acc, 0, ncells_ * sizeof(double), stream_));
     double r = 0;
-    PHMC_CUDA(cudaMemcpy(&r, &d_ledger_->step_drive_ev, sizeof(double), cudaMemcpyDeviceToHost));
+    synchronize();
+    PHMC_CUDA(cudaMemcpy(&r, &d_ledger_->next_drive_ev, sizeof(double), cudaMemcpyDeviceToHost));
+    launch_apply_pending(x, false);
+    counters_.launches += 2;
+    synchronize();
+    materialized_ = true;
     return r;
 }
 
@@ -471,14 +501,14 @@ void DeviceSolver::check_error() {
 void DeviceSolver::flux_pass() {
     const LaunchCtx x = ctx();
     PHMC_CUDA(cudaMemsetAsync(cells_.flux, 0, 3 * sizeof(double) * ncells_, stream_));
-    launch_flux(x);
+    launch_flux(x, mixed_);
     counters_.launches += 1;
     synchronize();
     host_T_.resize(ncells_);
     host_E_.resize(ncells_);
     host_q_.resize(3 * static_cast<size_t>(ncells_));
-    PHMC_CUDA(cudaMemcpy(host_T_.data(), cells_.temperature, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
-    PHMC_CUDA(cudaMemcpy(host_E_.data(), cells_.energy, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
+    PHMC_CUDA(cudaMemcpy(host_T_.data(), cells_.temperature_final, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
+    PHMC_CUDA(cudaMemcpy(host_E_.data(), cells_.energy_final, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
     PHMC_CUDA(cudaMemcpy(host_q_.data(), cells_.flux, 3 * ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
     // src/solver/GridStatistics.cpp:334-343 and src/solver/Observables.cpp:38-144
     const auto& vol = domain_->grid_volumes();
@@ -555,8 +585,8 @@ void DeviceSolver::read_stats(phmc_stats& o) {
 
 void DeviceSolver::read_cells(double* T, double* E, double* q3) {
     synchronize();
-    if (T) PHMC_CUDA(cudaMemcpy(T, cells_.temperature, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
-    if (E) PHMC_CUDA(cudaMemcpy(E, cells_.energy, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
+    if (T) PHMC_CUDA(cudaMemcpy(T, cells_.temperature_final, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
+    if (E) PHMC_CUDA(cudaMemcpy(E, cells_.energy_final, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
     if (q3) std::copy(host_q_.begin(), host_q_.end(), q3);
 }
 
@@ -570,6 +600,12 @@ long long DeviceSolver::slot_count() {
 void DeviceSolver::get_carriers(double* x, double* y, double* z, double* occ, uint32_t* mode, int32_t* cell,
                                 uint8_t* alive) {
     const long long n = slot_count();
+    materialize();
+    if (mixed_) {
+        launch_positions_out(ctx());
+        counters_.launches += 1;
+    }
+    synchronize();
     PHMC_CUDA(cudaMemcpy(x, state_.x, n * sizeof(double), cudaMemcpyDeviceToHost));
     PHMC_CUDA(cudaMemcpy(y, state_.y, n * sizeof(double), cudaMemcpyDeviceToHost));
     PHMC_CUDA(cudaMemcpy(z, state_.z, n * sizeof(double), cudaMemcpyDeviceToHost));

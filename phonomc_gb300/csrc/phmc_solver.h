@@ -28,34 +28,46 @@
 namespace phmc {
 
 
-// Per-cell scratch produced by k_cell_solve and read by the update pass.
+// Per-cell data of the single-pass timestep.
+//
+// The transport pass bins the post-transport population by (cell, mode):
+// multiplicity, summed occupation and summed max(1, n). The cell solve turns
+// the bins into the cell energy and temperature and into a pending affine
+// update n <- alpha n + beta per (cell, mode) that holds this step's collision
+// and both gradient half-steps around the next transport; the next transport
+// pass applies it when it loads the carrier. Every collision and drive update
+// of the reference is affine in the occupation with coefficients that depend
+// only on the carrier's cell and mode, so this reproduces them exactly.
 struct CellArrays {
     int ncells;
-    int hist_modes;          // modes per cell in the histogram (max active count over materials)
+    int hist_modes;          // modes per cell in the bins (max active count over materials)
     const int* cell_material;
     const double* volume;
-    // histogram (zeroed by the cell solve after use)
-    unsigned int* hcnt;      // [ncells * hist_modes]
-    double* hE;              // [ncells * hist_modes] summed e_i = hw (n - nbg)
-    double* hN;              // [ncells * hist_modes] summed n (RTA only)
+    unsigned int* hcnt;      // [ncells * hist_modes] multiplicity
+    double* hN;              // [ncells * hist_modes] summed occupation
     double* hM;              // [ncells * hist_modes] summed max(1, n) (RTA only)
-    // per cell results
-    double* energy;          // energy density
-    double* temperature;
-    double* grad_R;          // sum of gradient rates
-    double* grad_C;          // sum of capacities
-    double* acc;             // generic per-cell accumulator (final tally)
+    double2* ab;             // [ncells * hist_modes] pending (alpha, beta)
+    double* energy;          // energy density after transport
+    double* temperature;     // temperature after transport
+    double* energy_final;    // energy density at the end of the step
+    double* temperature_final;
+    double* grad_ratio;      // sum of gradient rates / sum of capacities, per cell
     double* flux;            // [ncells*3]
-    // RTA tables [ncells * n_classes]
-    double* rta_a;           // relaxation weight
-    double* rta_B;           // Bose occupation at the pseudo-temperature
-    // linearized collision tables [ncells * hist_modes]: additive term
-    double* lin_A;
-    // linearized collision per-mode data (one material)
-    const double* lin_decay; // exp(-h r) per active mode
+    double* scratch;         // per-cell work space of the collision solve
+    int mixed;               // FP32 linear-response exponential with FP64 energy rescale
+    // linear-response collision (one material): per-mode constants
+    const double* lin_decay; // exp(-r dt)
+    const double* lin_s;     // sqrt(capacity)
+    const double* lin_sqrt_rn;
+    const double* lin_sqrt_rr;
+    int lin_has_normal;
     int lin_substeps;
     double lin_h;
     int lin_terms;
+    // RTA classes of material 0
+    const int* class_start;
+    const int* class_modes;
+    int n_classes;
 };
 
 struct StepCounters {
@@ -68,7 +80,7 @@ class DeviceSolver {
 public:
     // init_carriers=false leaves the population empty (set_carriers fills it).
     DeviceSolver(const SimulationConfig& cfg, const std::vector<const PhononMaterial*>& mats,
-                 bool init_carriers = true);
+                 bool init_carriers = true, bool mixed = false);
     ~DeviceSolver();
     DeviceSolver(const DeviceSolver&) = delete;
     DeviceSolver& operator=(const DeviceSolver&) = delete;
@@ -85,6 +97,7 @@ public:
     void set_carriers(long long n, const double* x, const double* y, const double* z, const double* occ,
                       const uint32_t* mode, const uint8_t* alive);
     void write_outputs();
+    bool mixed() const { return mixed_; }
     // Deterministic sub-steps on the current population (parity entry points):
     // one collision with the given cell temperatures (or the tallied ones when
     // null), and one gradient half-step; both return the ledger energy.
@@ -132,9 +145,8 @@ private:
 
     bool profile_pass_a_ = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pass_a_events_;
-    double* scratch_ = nullptr;
-    const int* class_start_ = nullptr;
-    const int* class_modes_ = nullptr;
+    bool materialized_ = true;
+    void materialize();
     struct LaunchCtx ctx() const;
     int collision_kind() const;
 

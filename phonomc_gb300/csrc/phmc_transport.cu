@@ -59,7 +59,7 @@ __device__ bool advance_carrier(const DevTables& T, DevLedger* L, BlockLedger* b
     mode_velocity(M, w, v);
     double cp[3], t;
     int f;
-    if (!cache_hit(D, P, p, v, cp, t, f)) {
+    if (!cache_hit(D, P, p, v, M.speed[w & 0x00FFFFFFu], cp, t, f)) {
         raise_error(L, kErrIntersection, slot);
         return true;
     }
@@ -122,18 +122,17 @@ __device__ bool advance_carrier(const DevTables& T, DevLedger* L, BlockLedger* b
             }
         }
         mode_velocity(M, w, v);
-        const double speed = sqrt(dadd(dadd(dmul(v[0], v[0]), dmul(v[1], v[1])), dmul(v[2], v[2])));
-        const double s = P.push_eps / fmax(speed, 1e-12);
+        const double s = M.push[w & 0x00FFFFFFu];
 #pragma unroll
         for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], s));
-        if (!cache_hit(D, P, p, v, cp, t, f)) {
+        if (!cache_hit(D, P, p, v, M.speed[w & 0x00FFFFFFu], cp, t, f)) {
             raise_error(L, kErrIntersection, slot);
             return true;
         }
         if (t < 1e-12) {
 #pragma unroll
             for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], 1e-12));
-            if (!cache_hit(D, P, p, v, cp, t, f)) {
+            if (!cache_hit(D, P, p, v, M.speed[w & 0x00FFFFFFu], cp, t, f)) {
                 raise_error(L, kErrIntersection, slot);
                 return true;
             }
@@ -143,23 +142,166 @@ __device__ bool advance_carrier(const DevTables& T, DevLedger* L, BlockLedger* b
     return true;
 }
 
-// Histogram of the post-transport population for the per-cell solves.
-__device__ __forceinline__ void histogram_add(const CellArrays& C, const DevMaterial& M, DevLedger* L, int slot,
-                                              int cell, int mid, int ai, double occ, bool rta) {
+// ------------------------------------------------------------------ bins
+__device__ __forceinline__ void bin_carrier(const CellArrays& C, DevLedger* L, int slot, int cell, int mid, int ai,
+                                           double occ, bool rta) {
     if (cell < 0 || cell >= C.ncells || C.cell_material[cell] != mid || !isfinite(occ)) {
         raise_error(L, kErrInvalidStatistics, slot);
         return;
     }
     const size_t h = static_cast<size_t>(cell) * C.hist_modes + ai;
     atomicAdd(C.hcnt + h, 1u);
-    atomicAdd(C.hE + h, dmul(M.hw[ai], occ - M.nbg[ai]));
-    if (rta) {
-        atomicAdd(C.hN + h, occ);
-        atomicAdd(C.hM + h, fmax(1.0, occ));
+    atomicAdd(C.hN + h, occ);
+    if (rta) atomicAdd(C.hM + h, fmax(1.0, occ));
+}
+
+// Pending (alpha, beta) of the carrier's bin: collision of the previous step
+// and the gradient half-steps around this transport.
+__device__ __forceinline__ double apply_pending(const CellArrays& C, int cell, int ai, double occ) {
+    const double2 ab = __ldg(C.ab + static_cast<size_t>(cell) * C.hist_modes + ai);
+    return fma(ab.x, occ, ab.y);
+}
+
+__device__ __forceinline__ double drive_half(const DevTables& T, const CellArrays& C, const DevMaterial& M, int cell,
+                                             int ai) {
+    if (!M.grad_rate) return 0.0;
+    return 0.5 * T.par.dt * (M.grad_rate[ai] - M.cap_bg[ai] * C.grad_ratio[cell]) * M.inv_hw[ai];
+}
+
+// ---------------------------------------------------- FP32 flight (mixed)
+struct Frame {
+    int i[3];       // cell indices per axis
+    float cs[3];    // cell size
+    float lo[3], hi[3]; // box walls in the frame of the starting cell
+};
+
+__device__ __forceinline__ Frame cell_frame(const DevDomain& D, int cell) {
+    Frame F;
+    const int nyz = D.shape[1] * D.shape[2];
+    F.i[0] = cell / nyz;
+    const int r = cell - F.i[0] * nyz;
+    F.i[1] = r / D.shape[2];
+    F.i[2] = r - F.i[1] * D.shape[2];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        F.cs[a] = static_cast<float>(D.cell_size[a]);
+        F.lo[a] = static_cast<float>(-F.i[a] * D.cell_size[a]);
+        F.hi[a] = static_cast<float>((D.shape[a] - F.i[a]) * D.cell_size[a]);
+    }
+    return F;
+}
+
+__device__ __forceinline__ void mode_velocity32(const DevMaterial& M, uint32_t w, float v[3], float iv[3]) {
+    const int a = static_cast<int>(w & 0x00FFFFFFu);
+    const float4 vv = __ldg(reinterpret_cast<const float4*>(M.vel32) + a);
+    const float4 ii = __ldg(reinterpret_cast<const float4*>(M.ivel32) + a);
+    const float c[3] = {vv.x, vv.y, vv.z}, d[3] = {ii.x, ii.y, ii.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const bool flip = (w >> (24 + k)) & 1u;
+        v[k] = flip ? -c[k] : c[k];
+        iv[k] = flip ? -d[k] : d[k];
     }
 }
 
-template <bool kGradient, bool kRta>
+// Free flight in FP32 in the frame of the starting cell. Walls are hit
+// exactly (the coordinate is set to the wall), so no push-off distance is
+// needed; periodic faces map the coordinate to the opposite wall.
+__device__ bool advance_mixed(const DevTables& T, DevLedger* L, BlockLedger* bl, int slot, const Frame& F, float p[3],
+                              uint32_t& w, double& occ, float remaining, uint32_t purpose, uint32_t step) {
+    const DevDomain& D = T.dom;
+    const DevParams& P = T.par;
+    const int mid = static_cast<int>(w >> 28);
+    const DevMaterial& M = T.mat[mid];
+    float v[3], iv[3];
+    mode_velocity32(M, w, v, iv);
+    int event = 0;
+    for (; remaining > 0.0f && event < 64; ++event) {
+        float t = __int_as_float(0x7f800000);
+        int plane = -1;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            if (v[a] == 0.0f) continue;
+            const bool up = v[a] > 0.0f;
+            const float h = fmaxf(((up ? F.hi[a] : F.lo[a]) - p[a]) * iv[a], 0.0f);
+            if (h < t) {
+                t = h;
+                plane = 2 * a + (up ? 1 : 0);
+            }
+        }
+        if (plane < 0 || t > remaining) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) p[a] = fmaf(v[a], remaining, p[a]);
+            return true;
+        }
+        remaining -= t;
+        const int axis = plane >> 1;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) p[a] = fmaf(v[a], t, p[a]);
+        p[axis] = (plane & 1) ? F.hi[axis] : F.lo[axis];
+        const char cond = D.cond[plane];
+        const int ai = static_cast<int>(w & 0x00FFFFFFu);
+        if (cond == 'T') {
+            const double e = M.hw[ai] * (occ - M.nbg[ai]) * M.energy_weight;
+            atomicAdd(&bl->absorbed, 1u);
+            atomicAdd(&bl->absorbed_ev, e);
+            const int r = D.reservoir[plane];
+            if (r >= 0) atomicAdd(&bl->absorbed_res[r], 1u);
+            return false;
+        }
+        if (cond == 'P' && D.pair[plane] >= 0) {
+            p[axis] = (plane & 1) ? F.lo[axis] : F.hi[axis];
+            continue;
+        }
+        const int table = D.rough_table[mid][plane];
+        if (P.conservative || (cond == 'R' && table >= 0)) {
+            if (table < 0) {
+                raise_error(L, kErrModeMapping, slot);
+                return true;
+            }
+            const Uniform2 d0 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose, static_cast<uint32_t>(event), 0);
+            const Uniform2 d1 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose, static_cast<uint32_t>(event), 1);
+            double n_out;
+            const int out = rough_sample_dev(T.rough[table], M, ai, occ, P.conservative != 0, d0.a, d0.b, d1.a, n_out);
+            const double vn = M.vel[3 * out + axis] * ((plane & 1) ? 1.0 : -1.0);
+            uint32_t signs = 0;
+            if (P.conservative) {
+                if (!isfinite(n_out) || !(M.omega[out] > 0.0) || !(vn < 0.0)) {
+                    raise_error(L, kErrModeMapping, slot);
+                    return true;
+                }
+            } else if (vn > 0.0) {
+                signs = 1u << axis;
+            }
+            w = static_cast<uint32_t>(out) | (signs << 24) | (static_cast<uint32_t>(mid) << 28);
+            occ = n_out;
+        } else if (cond == 'R') {
+            raise_error(L, kErrNoRoughTable, slot);
+            return true;
+        } else {
+            w ^= 1u << (24 + axis);
+        }
+        mode_velocity32(M, w, v, iv);
+    }
+    if (remaining > 0.0f) raise_error(L, kErrTooManyEvents, slot);
+    return true;
+}
+
+// New cell and offset after an FP32 flight in the frame of cell F.
+__device__ __forceinline__ int settle_mixed(const DevDomain& D, const Frame& F, float p[3]) {
+    int j[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        int k = F.i[a] + static_cast<int>(floorf(p[a] / F.cs[a]));
+        k = k < 0 ? 0 : (k >= D.shape[a] ? D.shape[a] - 1 : k);
+        p[a] -= static_cast<float>(k - F.i[a]) * F.cs[a];
+        j[a] = k;
+    }
+    return (j[0] * D.shape[1] + j[1]) * D.shape[2] + j[2];
+}
+
+// ------------------------------------------------------ transport pass
+template <bool kMixed, bool kRta>
 __global__ void __launch_bounds__(256) k_transport(const DevTables* __restrict__ Tp, CarrierState S, CellArrays C,
                                                    DevLedger* L, uint32_t step) {
     __shared__ BlockLedger bl;
@@ -167,69 +309,84 @@ __global__ void __launch_bounds__(256) k_transport(const DevTables* __restrict__
     __syncthreads();
     const DevTables& T = *Tp;
     const int n = L->n_slots;
-    const double dt = T.par.dt;
-    const double half = 0.5 * dt;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         if (!S.alive[i]) continue;
-        double p[3] = {S.x[i], S.y[i], S.z[i]};
         uint32_t w = S.mode[i];
-        double occ = S.occ[i];
-        const int mid = static_cast<int>(w >> 28);
-        const DevMaterial& M = T.mat[mid];
-        if (kGradient) {
-            // first gradient half-step, cell sums of the current membership
-            const int c = S.cell[i];
-            const int ai = static_cast<int>(w & 0x00FFFFFFu);
-            const double R = C.grad_R[c], Cs = C.grad_C[c];
-            const double e = half * (M.grad_rate[ai] - R * M.cap_bg[ai] / Cs);
-            const double next = occ + e / M.hw[ai];
-            atomicAdd(&bl.drive_ev, M.hw[ai] * (next - occ));
-            if (e != 0.0) atomicAdd(&bl.drive_updates, 1ull);
-            occ = next;
+        const int c0 = S.cell[i];
+        double occ = apply_pending(C, c0, static_cast<int>(w & 0x00FFFFFFu), S.occ[i]);
+        bool alive;
+        int c;
+        if (kMixed) {
+            const Frame F = cell_frame(T.dom, c0);
+            float p[3] = {S.ox[i], S.oy[i], S.oz[i]};
+            alive = advance_mixed(T, L, &bl, i, F, p, w, occ, static_cast<float>(T.par.dt), kDrawTransport, step);
+            c = settle_mixed(T.dom, F, p);
+            S.ox[i] = p[0];
+            S.oy[i] = p[1];
+            S.oz[i] = p[2];
+        } else {
+            double p[3] = {S.x[i], S.y[i], S.z[i]};
+            alive = advance_carrier(T, L, &bl, i, p, w, occ, T.par.dt, kDrawTransport, step);
+            c = grid_index(T.dom, p[0], p[1], p[2]);
+            S.x[i] = p[0];
+            S.y[i] = p[1];
+            S.z[i] = p[2];
         }
-        const bool alive = advance_carrier(T, L, &bl, i, p, w, occ, dt, kDrawTransport, step);
-        S.x[i] = p[0];
-        S.y[i] = p[1];
-        S.z[i] = p[2];
         S.mode[i] = w;
         S.occ[i] = occ;
         if (!alive) {
             S.alive[i] = 0;
             continue;
         }
-        const int c = grid_index(T.dom, p[0], p[1], p[2]);
         S.cell[i] = c;
-        histogram_add(C, T.mat[w >> 28], L, i, c, static_cast<int>(w >> 28), static_cast<int>(w & 0x00FFFFFFu), occ,
-                      kRta);
+        bin_carrier(C, L, i, c, static_cast<int>(w >> 28), static_cast<int>(w & 0x00FFFFFFu), occ, kRta);
     }
     __syncthreads();
     block_ledger_flush(&bl, L);
 }
 
-// Histogram only (initial population or after carriers were replaced).
+// Bins of the current population (initial state or after carriers were replaced).
 template <bool kRta>
 __global__ void k_histogram(const DevTables* __restrict__ Tp, CarrierState S, CellArrays C, DevLedger* L) {
-    const DevTables& T = *Tp;
     const int n = L->n_slots;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         if (!S.alive[i]) continue;
         const uint32_t w = S.mode[i];
-        histogram_add(C, T.mat[w >> 28], L, i, S.cell[i], static_cast<int>(w >> 28),
-                      static_cast<int>(w & 0x00FFFFFFu), S.occ[i], kRta);
+        bin_carrier(C, L, i, S.cell[i], static_cast<int>(w >> 28), static_cast<int>(w & 0x00FFFFFFu), S.occ[i], kRta);
     }
 }
 
-// Cell of every uploaded carrier and the live count (after set_carriers).
+// Cells (and FP32 offsets) of uploaded carriers, and the live count.
+template <bool kMixed>
 __global__ void k_init_cells(const DevTables* __restrict__ Tp, CarrierState S, DevLedger* L) {
     const DevDomain& D = Tp->dom;
     const int n = L->n_slots;
     unsigned long long live = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        S.cell[i] = grid_index(D, S.x[i], S.y[i], S.z[i]);
+        const int c = grid_index(D, S.x[i], S.y[i], S.z[i]);
+        S.cell[i] = c;
+        if (kMixed) {
+            const Frame F = cell_frame(D, c);
+            S.ox[i] = static_cast<float>(S.x[i] - (D.lo[0] + F.i[0] * D.cell_size[0]));
+            S.oy[i] = static_cast<float>(S.y[i] - (D.lo[1] + F.i[1] * D.cell_size[1]));
+            S.oz[i] = static_cast<float>(S.z[i] - (D.lo[2] + F.i[2] * D.cell_size[2]));
+        }
         live += S.alive[i] ? 1 : 0;
     }
     for (int o = 16; o > 0; o >>= 1) live += __shfl_xor_sync(0xffffffffu, live, o);
     if ((threadIdx.x & 31) == 0 && live) atomicAdd(reinterpret_cast<unsigned long long*>(&L->particle_count), live);
+}
+
+// Absolute FP64 positions of the mixed state into the staging arrays.
+__global__ void k_positions_out(const DevTables* __restrict__ Tp, CarrierState S, const DevLedger* L) {
+    const DevDomain& D = Tp->dom;
+    const int n = L->n_slots;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const Frame F = cell_frame(D, S.cell[i]);
+        S.x[i] = D.lo[0] + F.i[0] * D.cell_size[0] + static_cast<double>(S.ox[i]);
+        S.y[i] = D.lo[1] + F.i[1] * D.cell_size[1] + static_cast<double>(S.oy[i]);
+        S.z[i] = D.lo[2] + F.i[2] * D.cell_size[2] + static_cast<double>(S.oz[i]);
+    }
 }
 
 // ------------------------------------------------------------ injection
@@ -244,8 +401,8 @@ __global__ void __launch_bounds__(kHoleBlock) k_dead_count(CarrierState S, const
     if (threadIdx.x == 0) block_dead[blockIdx.x] = c;
 }
 
-// Single block: exclusive scan of block counts, emission counts per reservoir
-// (src/solver/ReservoirInjector.cpp:281-284, ReservoirSampler.cpp:117-124).
+// Single block: exclusive scan of block counts and emission counts per reservoir
+// (src/solver/ReservoirInjector.cpp:281-284, src/solver/ReservoirSampler.cpp:117-124).
 __global__ void __launch_bounds__(1024) k_inject_prepare(const DevTables* __restrict__ Tp, DevLedger* L,
                                                          int* block_dead, int nblocks, int capacity, uint32_t step) {
     __shared__ int carry;
@@ -339,7 +496,7 @@ __global__ void __launch_bounds__(kHoleBlock) k_dead_write(CarrierState S, const
     }
 }
 
-template <bool kRta>
+template <bool kMixed, bool kRta>
 __global__ void __launch_bounds__(256) k_inject(const DevTables* __restrict__ Tp, CarrierState S, CellArrays C,
                                                 DevLedger* L, const int* holes, uint32_t step) {
     __shared__ BlockLedger bl;
@@ -381,8 +538,7 @@ __global__ void __launch_bounds__(256) k_inject(const DevTables* __restrict__ Tp
             for (int a = 0; a < 3; ++a) v[a] = -v[a];
             signs = 7u;
         }
-        const double speed = fmax(1e-12, sqrt(dadd(dadd(dmul(v[0], v[0]), dmul(v[1], v[1])), dmul(v[2], v[2]))));
-        const double s = P.push_eps / speed;
+        const double s = M.push[m];
 #pragma unroll
         for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], s));
         double occ = R.occ[m];
@@ -391,27 +547,35 @@ __global__ void __launch_bounds__(256) k_inject(const DevTables* __restrict__ Tp
         atomicAdd(&bl.injected_ev, dmul(dmul(M.hw[m], occ - M.nbg[m]), M.energy_weight));
         const double remain = P.dt - temit;
         bool alive = true;
-        if (remain > 1e-14) alive = advance_carrier(T, L, &bl, slot, p, w, occ, remain, kDrawInjected, step);
-        S.x[slot] = p[0];
-        S.y[slot] = p[1];
-        S.z[slot] = p[2];
+        int c;
+        if (kMixed) {
+            c = grid_index(T.dom, p[0], p[1], p[2]);
+            const Frame F = cell_frame(T.dom, c);
+            float q[3];
+            for (int a = 0; a < 3; ++a) q[a] = static_cast<float>(p[a] - (T.dom.lo[a] + F.i[a] * T.dom.cell_size[a]));
+            if (remain > 1e-14)
+                alive = advance_mixed(T, L, &bl, slot, F, q, w, occ, static_cast<float>(remain), kDrawInjected, step);
+            c = settle_mixed(T.dom, F, q);
+            S.ox[slot] = q[0];
+            S.oy[slot] = q[1];
+            S.oz[slot] = q[2];
+        } else {
+            if (remain > 1e-14) alive = advance_carrier(T, L, &bl, slot, p, w, occ, remain, kDrawInjected, step);
+            c = grid_index(T.dom, p[0], p[1], p[2]);
+            S.x[slot] = p[0];
+            S.y[slot] = p[1];
+            S.z[slot] = p[2];
+        }
         S.mode[slot] = w;
         S.occ[slot] = occ;
         S.alive[slot] = alive ? 1 : 0;
-        if (alive) {
-            const int c = grid_index(T.dom, p[0], p[1], p[2]);
-            S.cell[slot] = c;
-            histogram_add(C, T.mat[w >> 28], L, slot, c, static_cast<int>(w >> 28), static_cast<int>(w & 0x00FFFFFFu),
-                          occ, kRta);
-        } else {
-            S.cell[slot] = 0;
-        }
+        S.cell[slot] = alive ? c : 0;
+        if (alive) bin_carrier(C, L, slot, c, static_cast<int>(w >> 28), static_cast<int>(w & 0x00FFFFFFu), occ, kRta);
     }
     __syncthreads();
     block_ledger_flush(&bl, L);
 }
 
-// Slot count and injected totals after the injection kernel.
 __global__ void k_inject_finish(DevLedger* L) {
     const int extra = L->n_inject - L->n_holes;
     if (extra > 0) L->n_slots += extra;
@@ -419,19 +583,33 @@ __global__ void k_inject_finish(DevLedger* L) {
 }
 
 // Escaped-carrier check (src/solver/TransportOperator.cpp:364-402).
+template <bool kMixed>
 __global__ void k_containment(const DevTables* __restrict__ Tp, CarrierState S, DevLedger* L) {
     const DevDomain& D = Tp->dom;
     const int n = L->n_slots;
     const double tol = 1e-10 * D.scale;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         if (!S.alive[i]) continue;
-        const double p[3] = {S.x[i], S.y[i], S.z[i]};
+        double p[3];
+        if (kMixed) {
+            const Frame F = cell_frame(D, S.cell[i]);
+            p[0] = D.lo[0] + F.i[0] * D.cell_size[0] + S.ox[i];
+            p[1] = D.lo[1] + F.i[1] * D.cell_size[1] + S.oy[i];
+            p[2] = D.lo[2] + F.i[2] * D.cell_size[2] + S.oz[i];
+        } else {
+            p[0] = S.x[i];
+            p[1] = S.y[i];
+            p[2] = S.z[i];
+        }
+        // FP32 offsets carry ~1e-7 relative rounding of the cell size
+        const double t = kMixed ? 1e-5 * D.scale : tol;
         for (int a = 0; a < 3; ++a)
-            if (!isfinite(p[a]) || p[a] < D.lo[a] - tol || p[a] > D.hi[a] + tol) raise_error(L, kErrEscaped, i);
+            if (!isfinite(p[a]) || p[a] < D.lo[a] - t || p[a] > D.hi[a] + t) raise_error(L, kErrEscaped, i);
     }
 }
 
-// Heat-flux tally q_c = sum v e w (src/solver/GridStatistics.cpp:269-347), into C.flux.
+// Heat-flux tally q_c = sum v e w (src/solver/GridStatistics.cpp:269-347) with the
+// end-of-step occupation n = alpha n + beta - (second drive half).
 __global__ void __launch_bounds__(256) k_flux(const DevTables* __restrict__ Tp, CarrierState S, CellArrays C,
                                               const DevLedger* L, int use_shared) {
     extern __shared__ double sq[];
@@ -445,10 +623,11 @@ __global__ void __launch_bounds__(256) k_flux(const DevTables* __restrict__ Tp, 
         const uint32_t w = S.mode[i];
         const DevMaterial& M = T.mat[w >> 28];
         const int ai = static_cast<int>(w & 0x00FFFFFFu);
-        const double e = dmul(dmul(M.hw[ai], S.occ[i] - M.nbg[ai]), M.energy_weight);
+        const int c = S.cell[i];
+        const double occ = apply_pending(C, c, ai, S.occ[i]) - drive_half(T, C, M, c, ai);
+        const double e = dmul(dmul(M.hw[ai], occ - M.nbg[ai]), M.energy_weight);
         double v[3];
         mode_velocity(M, w, v);
-        const int c = S.cell[i];
         double* dst = use_shared ? sq : C.flux;
         for (int a = 0; a < 3; ++a) atomicAdd(dst + 3 * c + a, dmul(v[a], e));
     }
@@ -458,44 +637,93 @@ __global__ void __launch_bounds__(256) k_flux(const DevTables* __restrict__ Tp, 
             if (sq[k] != 0.0) atomicAdd(C.flux + k, sq[k]);
 }
 
-// ----------------------------------------------------------- launchers
-void launch_transport(const LaunchCtx& x, bool gradient, bool rta, uint32_t step) {
-    const dim3 grid(x.grid_blocks), block(256);
-    if (gradient) {
-        if (rta) k_transport<true, true><<<grid, block, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
-        else k_transport<true, false><<<grid, block, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
-    } else {
-        if (rta) k_transport<false, true><<<grid, block, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
-        else k_transport<false, false><<<grid, block, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
+// Apply the pending update to the stored occupations, optionally leaving the
+// next step's first drive half pending; then reset the table.
+__global__ void k_apply_pending(const DevTables* __restrict__ Tp, CarrierState S, CellArrays C, const DevLedger* L,
+                                int subtract_drive) {
+    const DevTables& T = *Tp;
+    const int n = L->n_slots;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (!S.alive[i]) continue;
+        const uint32_t w = S.mode[i];
+        const int ai = static_cast<int>(w & 0x00FFFFFFu);
+        const int c = S.cell[i];
+        double occ = apply_pending(C, c, ai, S.occ[i]);
+        if (subtract_drive) occ -= drive_half(T, C, T.mat[w >> 28], c, ai);
+        S.occ[i] = occ;
     }
 }
 
-void launch_init_cells(const LaunchCtx& x) { k_init_cells<<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.L); }
+__global__ void k_reset_pending(const DevTables* __restrict__ Tp, CellArrays C, int keep_drive) {
+    const DevTables& T = *Tp;
+    const size_t total = static_cast<size_t>(C.ncells) * C.hist_modes;
+    for (size_t k = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; k < total;
+         k += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const int c = static_cast<int>(k / C.hist_modes);
+        const int m = static_cast<int>(k % C.hist_modes);
+        const DevMaterial& M = T.mat[C.cell_material[c]];
+        const double D = (keep_drive && m < M.n_active) ? drive_half(T, C, M, c, m) : 0.0;
+        C.ab[k] = make_double2(1.0, D);
+    }
+}
+
+// ----------------------------------------------------------- launchers
+void launch_transport(const LaunchCtx& x, bool mixed, bool rta, uint32_t step) {
+    const dim3 g(x.grid_blocks), b(256);
+    if (mixed) {
+        if (rta) k_transport<true, true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
+        else k_transport<true, false><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
+    } else {
+        if (rta) k_transport<false, true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
+        else k_transport<false, false><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
+    }
+}
 
 void launch_histogram(const LaunchCtx& x, bool rta) {
     if (rta) k_histogram<true><<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.C, x.L);
     else k_histogram<false><<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.C, x.L);
 }
 
-int launch_inject(const LaunchCtx& x, bool rta, int* holes, int* block_dead, int capacity, uint32_t step) {
+void launch_init_cells(const LaunchCtx& x, bool mixed) {
+    if (mixed) k_init_cells<true><<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.L);
+    else k_init_cells<false><<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.L);
+}
+
+void launch_positions_out(const LaunchCtx& x) {
+    k_positions_out<<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.L);
+}
+
+int launch_inject(const LaunchCtx& x, bool mixed, bool rta, int* holes, int* block_dead, int capacity, uint32_t step) {
     const int nb = (capacity + kHoleBlock - 1) / kHoleBlock;
     k_dead_count<<<nb, kHoleBlock, 0, x.stream>>>(x.S, x.L, block_dead);
     k_inject_prepare<<<1, 1024, 0, x.stream>>>(x.T, x.L, block_dead, nb, capacity, step);
     k_dead_write<<<nb, kHoleBlock, 0, x.stream>>>(x.S, x.L, block_dead, holes);
-    if (rta) k_inject<true><<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes, step);
-    else k_inject<false><<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes, step);
+    const dim3 g(x.grid_blocks), b(256);
+    if (mixed) {
+        if (rta) k_inject<true, true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes, step);
+        else k_inject<true, false><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes, step);
+    } else {
+        if (rta) k_inject<false, true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes, step);
+        else k_inject<false, false><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes, step);
+    }
     k_inject_finish<<<1, 1, 0, x.stream>>>(x.L);
     return 5;
 }
 
-void launch_containment(const LaunchCtx& x) {
-    k_containment<<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.L);
+void launch_containment(const LaunchCtx& x, bool mixed) {
+    if (mixed) k_containment<true><<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.L);
+    else k_containment<false><<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.L);
 }
 
-void launch_flux(const LaunchCtx& x) {
+void launch_flux(const LaunchCtx& x, bool /*mixed*/) {
     const size_t sh = 3 * sizeof(double) * static_cast<size_t>(x.C.ncells);
     const int use_shared = sh <= 32768 ? 1 : 0;
     k_flux<<<x.grid_blocks, 256, use_shared ? sh : 0, x.stream>>>(x.T, x.S, x.C, x.L, use_shared);
+}
+
+void launch_apply_pending(const LaunchCtx& x, bool subtract_drive) {
+    k_apply_pending<<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.C, x.L, subtract_drive ? 1 : 0);
+    k_reset_pending<<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.C, subtract_drive ? 1 : 0);
 }
 
 } // namespace phmc

@@ -190,3 +190,50 @@ def test_energy_ledger_closes_on_device(gpu):
     T, _, _ = s.cells()
     assert np.all(T > 298.0) and np.all(T < 302.0)
     assert st["particle_count"] > 0.9 * 400000
+
+
+# ------------------------------------------------------------ mixed precision
+def _mixed_vs_plain(gpu, cfg, stationary, steps):
+    mat = synthetic.make_material(mesh=16)
+    m = abi.Material(gpu, "phmc_", mat, 0.1, stationary, False)
+    sp = abi.Solver(gpu, "phmc_", dict(cfg, precision="fp64"), [m])
+    sm = abi.Solver(gpu, "phmc_", dict(cfg, precision="mixed"), [m])
+    sp.run(steps)
+    sm.run(steps)
+    return sp, sm
+
+
+@pytest.mark.parametrize("name,stationary", [("cross_plane_film", False), ("inplane_gradient", True)])
+def test_mixed_tracks_plain_trajectory(gpu, name, stationary):
+    """Same seed, same draws: the FP32 flight reproduces the FP64 trajectory up to
+    FP32 rounding (positions), and cell temperatures agree to 1e-4 K after 6 steps."""
+    cfg = workloads.scaled(getattr(workloads, name)(), 50000, random_seed=21)
+    sp, sm = _mixed_vs_plain(gpu, cfg, stationary, 6)
+    cp, cm = sp.carriers(), sm.carriers()
+    a = (cp["alive"] == 1) & (cm["alive"] == 1)
+    assert a.mean() > 0.99
+    same_mode = np.mean(cp["mode"][a] == cm["mode"][a])
+    assert same_mode > 0.999, same_mode
+    assert np.mean(cp["cell"][a] == cm["cell"][a]) > 0.999
+    for k in ("x", "y", "z"):
+        d = np.abs(cp[k][a] - cm[k][a])
+        assert np.median(d) < 1e-3, (k, np.median(d))
+    Tp, _, _ = sp.cells()
+    Tm, _, _ = sm.cells()
+    assert np.max(np.abs(Tp - Tm)) < 1e-3
+    st = sm.stats()
+    assert abs(st["step_energy_balance_residual_ev"]) < 1e-12 * abs(st["total_thermal_energy_ev"])
+
+
+def test_mixed_energy_conservation_linearized(gpu):
+    """The FP32 linear-response exponential is rescaled in FP64: the collision
+    changes the carried energy only at round-off (lifetime residual ~ 0)."""
+    cfg = workloads.scaled(workloads.inplane_gradient(), 200000, random_seed=4)
+    mat = synthetic.make_material(mesh=16)
+    m = abi.Material(gpu, "phmc_", mat, 0.1, True, False)
+    s = abi.Solver(gpu, "phmc_", dict(cfg, precision="mixed"), [m])
+    s.run(5)
+    st = s.stats()
+    scale = abs(st["total_thermal_energy_ev"])
+    assert abs(st["step_lifetime_energy_residual_ev"]) < 1e-13 * scale
+    assert abs(st["step_energy_balance_residual_ev"]) < 1e-13 * scale
