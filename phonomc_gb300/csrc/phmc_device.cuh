@@ -102,6 +102,7 @@ struct DevReservoir {
 
 struct DevDomain {
     double lo[3], hi[3], inv_cell[3], cell_size[3];
+    float cell_size32[3];
     int shape[3];
     int ncells;
     double tol;        // analytic-box position tolerance
@@ -119,6 +120,7 @@ struct DevDomain {
 
 struct DevParams {
     double dt;
+    float dt32;
     double push_eps;
     uint64_t seed;
     int conservative;

@@ -227,6 +227,7 @@ void DeviceSolver::upload_tables() {
         D.inv_cell[a] = domain_->inv_cell()[a];
         D.shape[a] = domain_->grid_shape()[a];
         D.cell_size[a] = (hi[a] - lo[a]) / D.shape[a];
+        D.cell_size32[a] = static_cast<float>(D.cell_size[a]);
         scale = std::max(scale, std::abs(hi[a] - lo[a]));
     }
     D.scale = scale;
@@ -246,6 +247,7 @@ void DeviceSolver::upload_tables() {
     // params
     DevParams& p = T.par;
     p.dt = cfg_.time_step;
+    p.dt32 = static_cast<float>(cfg_.time_step);
     p.push_eps = P_.push_eps;
     p.seed = cfg_.random_seed;
     p.conservative = P_.conservative;

@@ -145,7 +145,8 @@ __device__ bool advance_carrier(const DevTables& T, DevLedger* L, BlockLedger* b
 // ------------------------------------------------------------------ bins
 __device__ __forceinline__ void bin_carrier(const CellArrays& C, DevLedger* L, int slot, int cell, int mid, int ai,
                                            double occ, bool rta) {
-    if (cell < 0 || cell >= C.ncells || C.cell_material[cell] != mid || !isfinite(occ)) {
+    const bool finite = (__double2hiint(occ) & 0x7ff00000) != 0x7ff00000;
+    if (cell < 0 || cell >= C.ncells || C.cell_material[cell] != mid || !finite) {
         raise_error(L, kErrInvalidStatistics, slot);
         return;
     }
@@ -184,9 +185,9 @@ __device__ __forceinline__ Frame cell_frame(const DevDomain& D, int cell) {
     F.i[2] = r - F.i[1] * D.shape[2];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        F.cs[a] = static_cast<float>(D.cell_size[a]);
-        F.lo[a] = static_cast<float>(-F.i[a] * D.cell_size[a]);
-        F.hi[a] = static_cast<float>((D.shape[a] - F.i[a]) * D.cell_size[a]);
+        F.cs[a] = D.cell_size32[a];
+        F.lo[a] = -static_cast<float>(F.i[a]) * F.cs[a];
+        F.hi[a] = static_cast<float>(D.shape[a] - F.i[a]) * F.cs[a];
     }
     return F;
 }
@@ -194,13 +195,11 @@ __device__ __forceinline__ Frame cell_frame(const DevDomain& D, int cell) {
 __device__ __forceinline__ void mode_velocity32(const DevMaterial& M, uint32_t w, float v[3], float iv[3]) {
     const int a = static_cast<int>(w & 0x00FFFFFFu);
     const float4 vv = __ldg(reinterpret_cast<const float4*>(M.vel32) + a);
-    const float4 ii = __ldg(reinterpret_cast<const float4*>(M.ivel32) + a);
-    const float c[3] = {vv.x, vv.y, vv.z}, d[3] = {ii.x, ii.y, ii.z};
+    const float c[3] = {vv.x, vv.y, vv.z};
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const bool flip = (w >> (24 + k)) & 1u;
-        v[k] = flip ? -c[k] : c[k];
-        iv[k] = flip ? -d[k] : d[k];
+        v[k] = ((w >> (24 + k)) & 1u) ? -c[k] : c[k];
+        iv[k] = v[k] != 0.0f ? __frcp_rn(v[k]) : 0.0f;
     }
 }
 
@@ -319,7 +318,7 @@ __global__ void __launch_bounds__(256) k_transport(const DevTables* __restrict__
         if (kMixed) {
             const Frame F = cell_frame(T.dom, c0);
             float p[3] = {S.ox[i], S.oy[i], S.oz[i]};
-            alive = advance_mixed(T, L, &bl, i, F, p, w, occ, static_cast<float>(T.par.dt), kDrawTransport, step);
+            alive = advance_mixed(T, L, &bl, i, F, p, w, occ, T.par.dt32, kDrawTransport, step);
             c = settle_mixed(T.dom, F, p);
             S.ox[i] = p[0];
             S.oy[i] = p[1];
