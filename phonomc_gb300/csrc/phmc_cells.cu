@@ -1,25 +1,41 @@
 // Per-cell work of the timestep, from the (cell, mode) bins of the transport pass.
 //
-//  k_cell_solve   one CTA per cell:
-//    * energy density and temperature after transport
-//      (src/solver/GridStatistics.cpp:95-234)
-//    * gradient cell sums (src/solver/TemperatureGradientDrive.cpp:131-150)
-//    * collision as an affine update per (cell, mode):
-//        RTA      pseudo-temperature bracket + Newton over mode classes
-//                 (src/solver/RtaCollisionOperator.cpp:79-184): n' = (1-a) n + a n_eq(T*)
-//        linear   exp(dt L) on the cell's mode-aggregated quadrature
-//                 (src/material/CallawayOperator.cpp:193-370,
-//                 src/solver/CarrierCollisionOperator.cpp:67-126):
-//                 n' = n_bg + e^{-r dt} (n - n_bg) + A_m
-//    * the pending update table, the step's lifetime residual, drive energy
-//      and the cell energy/temperature at the end of the step
-//  k_cells_final  total thermal energy and the energy ledger (src/solver/EnergyLedger.cpp:58-90)
+//  k_cell_stats    grid over (mode chunk, cell): energy after transport and the
+//                  gradient cell sums (src/solver/GridStatistics.cpp:95-181,
+//                  src/solver/TemperatureGradientDrive.cpp:131-150); RTA class sums
+//  k_cell_state    per cell: energy density -> temperature (src/solver/GridStatistics.cpp:213-226)
+//  k_rta_solve     one CTA per cell: pseudo-temperature bracket + Newton over mode
+//                  classes (src/solver/RtaCollisionOperator.cpp:79-184)
+//  k_linear_solve  one thread-block cluster per cell: exp(dt L) on the cell's
+//                  mode-aggregated quadrature (src/material/CallawayOperator.cpp:193-370,
+//                  src/solver/CarrierCollisionOperator.cpp:67-126); the cell's vectors
+//                  live in the cluster's shared memory, reductions go through DSMEM
+//  k_cell_tables   grid over (mode chunk, cell): the pending affine update per
+//                  (cell, mode), the step's lifetime residual, drive energy and the
+//                  energy at the end of the step; clears the bins
+//  k_cells_final   cell temperatures at the end of the step, total thermal energy
+//                  and the energy ledger (src/solver/EnergyLedger.cpp:58-90)
+//
+// Collisions and drive become n' = alpha n + beta per (cell, mode):
+//   RTA     alpha = 1 - a,  beta = a n_eq(T*)
+//   linear  alpha = e^{-r dt}, beta = (1 - alpha) n_bg + A_m, A_m the common
+//           gain of the mode's carriers (exact: within one mode the carriers
+//           differ only in x_i, and the rank-G gain term is shared)
 #include "phmc_kernels.cuh"
+
+#include <cooperative_groups.h>
+
+#include <stdexcept>
+#include <string>
+
+namespace cg = cooperative_groups;
 
 namespace phmc {
 
-constexpr int kCellThreads = 512;
+constexpr int kStatThreads = 256;
+constexpr int kChunk = 1024;     // modes per stats/tables block
 constexpr int kMaxGains = 5;
+constexpr int kLinThreads = 256;
 
 template <int N> __device__ __forceinline__ void block_sum(double (&v)[N], double* red) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -39,15 +55,6 @@ template <int N> __device__ __forceinline__ void block_sum(double (&v)[N], doubl
     __syncthreads();
 }
 
-template <int N> __device__ __forceinline__ void block_sum_f(float (&v)[N], double* red) {
-    double d[N];
-#pragma unroll
-    for (int k = 0; k < N; ++k) d[k] = v[k];
-    block_sum<N>(d, red);
-#pragma unroll
-    for (int k = 0; k < N; ++k) v[k] = static_cast<float>(d[k]);
-}
-
 __global__ void k_step_begin(DevLedger* L) {
     for (int r = 0; r < kMaxReservoirs; ++r) L->absorbed_res[r] = 0;
     L->step_absorbed = L->step_injected = 0;
@@ -60,29 +67,70 @@ __global__ void k_step_begin(DevLedger* L) {
     L->n_inject = 0;
 }
 
-// ------------------------------------------------------------------ RTA
-__device__ void rta_tables(const DevTables& T, const CellArrays& C, const DevMaterial& M, int c, double Tc,
-                           double* red, double* alpha, double* betac) {
-    const int nc = C.n_classes;
-    double* sc = C.scratch + static_cast<size_t>(c) * nc * 5;
-    double* s_cnt = sc;
-    double* s_N = sc + nc;
-    double* s_M = sc + 2 * nc;
-    double* a_tab = sc + 3 * nc;
-    double* B_tab = sc + 4 * nc;
+// ------------------------------------------------------------ statistics
+template <bool kRta>
+__global__ void __launch_bounds__(kStatThreads) k_cell_stats(const DevTables* __restrict__ Tp, CellArrays C,
+                                                              int classes) {
+    __shared__ double red[3 * 32];
+    const DevTables& T = *Tp;
+    const int c = blockIdx.y;
+    const DevMaterial& M = T.mat[C.cell_material[c]];
     const size_t hb = static_cast<size_t>(c) * C.hist_modes;
+    const int m0 = blockIdx.x * kChunk, m1 = min(M.n_active, m0 + kChunk);
+    double v[3] = {0.0, 0.0, 0.0};
+    for (int m = m0 + threadIdx.x; m < m1; m += blockDim.x) {
+        const unsigned k = C.hcnt[hb + m];
+        if (!k) continue;
+        const double N = C.hN[hb + m];
+        v[0] += M.hw[m] * (N - k * M.nbg[m]);
+        if (M.grad_rate) {
+            v[1] += k * M.grad_rate[m];
+            v[2] += k * M.cap_bg[m];
+        }
+        if (kRta && classes) {
+            double* cs = C.cls_sum + (static_cast<size_t>(c) * C.n_classes + M.mode_class[m]) * 3;
+            atomicAdd(cs, static_cast<double>(k));
+            atomicAdd(cs + 1, N);
+            atomicAdd(cs + 2, C.hM[hb + m]);
+        }
+    }
+    block_sum<3>(v, red);
+    if (threadIdx.x == 0 && m0 < M.n_active) {
+        atomicAdd(C.cell_stats + 4 * c, v[0]);
+        atomicAdd(C.cell_stats + 4 * c + 1, v[1]);
+        atomicAdd(C.cell_stats + 4 * c + 2, v[2]);
+    }
+}
+
+// phase 2 keeps the supplied temperatures
+__global__ void k_cell_state(const DevTables* __restrict__ Tp, CellArrays C, DevLedger* L, int phase) {
+    const DevTables& T = *Tp;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C.ncells; c += gridDim.x * blockDim.x) {
+        const DevMaterial& M = T.mat[C.cell_material[c]];
+        const double* s = C.cell_stats + 4 * c;
+        const double E = s[0] * M.energy_weight / C.volume[c] + M.energy_density_bg;
+        if (!isfinite(E)) raise_error(L, kErrNonFinite, c);
+        C.energy[c] = E;
+        if (phase != 2)
+            C.temperature[c] = T.par.linearized
+                                   ? T.par.background_T + (E - M.energy_density_bg) / M.heat_capacity_density_bg
+                                   : table_inverse(M.lookup_E, M.lookup_T, M.n_lookup, E);
+        C.grad_ratio[c] = s[2] > 0.0 ? s[1] / s[2] : 0.0;
+    }
+}
+
+// ------------------------------------------------------------------ RTA
+__global__ void __launch_bounds__(256) k_rta_solve(const DevTables* __restrict__ Tp, CellArrays C) {
+    __shared__ double red[2 * 32];
+    const DevTables& T = *Tp;
+    const int c = blockIdx.x;
+    const DevMaterial& M = T.mat[C.cell_material[c]];
+    const int nc = C.n_classes;
+    double* cs = C.cls_sum + static_cast<size_t>(c) * nc * 3;
+    double2* ab = C.rta_ab + static_cast<size_t>(c) * nc;
+    const double Tc = C.temperature[c];
     const double dt = T.par.dt;
     for (int k = threadIdx.x; k < nc; k += blockDim.x) {
-        double n0 = 0, n1 = 0, n2 = 0;
-        for (int j = C.class_start[k]; j < C.class_start[k + 1]; ++j) {
-            const int m = C.class_modes[j];
-            n0 += C.hcnt[hb + m];
-            n1 += C.hN[hb + m];
-            n2 += C.hM[hb + m];
-        }
-        s_cnt[k] = n0;
-        s_N[k] = n1;
-        s_M[k] = n2;
         const int rep = M.class_rep[k];
         double a;
         if (T.par.lifetime_local) {
@@ -91,7 +139,7 @@ __device__ void rta_tables(const DevTables& T, const CellArrays& C, const DevMat
         } else {
             a = M.relax_fixed[rep];
         }
-        a_tab[k] = a;
+        ab[k].x = a;
     }
     __syncthreads();
     // f(T) = sum_k hw a (N_k - cnt_k n_eq(T)); f' = -sum cnt hw a dn_eq/dT
@@ -99,14 +147,14 @@ __device__ void rta_tables(const DevTables& T, const CellArrays& C, const DevMat
         const double Tt = fmax(0.0, temperature);
         double v[2] = {0.0, 0.0};
         for (int k = threadIdx.x; k < nc; k += blockDim.x) {
-            const double n0 = s_cnt[k];
+            const double n0 = cs[3 * k];
             if (n0 == 0.0) continue;
             const double w = fmax(0.0, M.class_omega[k]);
             const double hw = kHbar * w;
-            const double a = a_tab[k];
+            const double a = ab[k].x;
             if (!(hw > 0.0) || !(a > 0.0)) continue;
             const double neq = bose_dev(Tt, w);
-            v[0] += hw * a * (s_N[k] - n0 * neq);
+            v[0] += hw * a * (cs[3 * k + 1] - n0 * neq);
             if (want_slope && Tt > 0.0) v[1] -= n0 * hw * a * (hw * neq * (neq + 1.0) / (kKb * Tt * Tt));
         }
         block_sum<2>(v, red);
@@ -127,9 +175,9 @@ __device__ void rta_tables(const DevTables& T, const CellArrays& C, const DevMat
     } else if (f_high >= 0.0) {
         Ts = high;
     } else {
-        double sv[1] = {0.0};
-        for (int k = threadIdx.x; k < nc; k += blockDim.x) sv[0] += kHbar * fmax(0.0, M.class_omega[k]) * a_tab[k] * s_M[k];
-        block_sum<1>(sv, red);
+        double sv[2] = {0.0, 0.0};
+        for (int k = threadIdx.x; k < nc; k += blockDim.x) sv[0] += kHbar * fmax(0.0, M.class_omega[k]) * ab[k].x * cs[3 * k + 2];
+        block_sum<2>(sv, red);
         const double tol = 1e-13 * fmax(1.0, sv[0]);
         for (int it = 0; it < 40; ++it) {
             double d;
@@ -145,40 +193,65 @@ __device__ void rta_tables(const DevTables& T, const CellArrays& C, const DevMat
             Ts = cand;
         }
     }
-    for (int k = threadIdx.x; k < nc; k += blockDim.x) B_tab[k] = bose_dev(Ts, fmax(0.0, M.class_omega[k]));
     __syncthreads();
-    for (int m = threadIdx.x; m < M.n_active; m += blockDim.x) {
-        const int k = M.mode_class[m];
-        const double a = a_tab[k];
-        alpha[m] = 1.0 - a;
-        betac[m] = a * B_tab[k];
+    for (int k = threadIdx.x; k < nc; k += blockDim.x) {
+        ab[k].y = bose_dev(Ts, fmax(0.0, M.class_omega[k]));
+        cs[3 * k] = 0.0;
+        cs[3 * k + 1] = 0.0;
+        cs[3 * k + 2] = 0.0;
     }
-    __syncthreads();
 }
 
 // ----------------------------------------------------- linear response
-// exp(dt L) on the aggregated quadrature of cell c. R = double for the plain
-// path; R = float for the mixed path, whose result is rescaled in FP64 so the
-// collision conserves the cell energy exactly.
-template <class R>
-__device__ void linear_tables(const DevTables& T, const CellArrays& C, const DevMaterial& M, int c, double* red,
-                              double* alpha, double* betac) {
-    const int na = M.n_active;
-    const size_t H = static_cast<size_t>(C.hist_modes);
-    const size_t hb = static_cast<size_t>(c) * H;
-    R* base = reinterpret_cast<R*>(C.scratch) + static_cast<size_t>(c) * H * (3 + kMaxGains);
-    R* X0 = base;
-    R* X = base + H;
-    R* term = base + 2 * H;
-    R* u = base + 3 * H;
-    const unsigned* cnt = C.hcnt + hb;
-    for (int m = threadIdx.x; m < na; m += blockDim.x) {
-        const unsigned k = cnt[m];
-        const double e = k ? M.hw[m] * (C.hN[hb + m] - k * M.nbg[m]) : 0.0;
-        const R xm = k ? static_cast<R>(e / C.lin_s[m]) : R(0);
-        X0[m] = xm;
-        X[m] = xm;
+// Cluster-wide sum of N doubles: CTA partials in shared memory, read by every
+// CTA of the cluster through distributed shared memory.
+template <int N>
+__device__ __forceinline__ void cluster_sum(double (&v)[N], double* red, double* part, cg::cluster_group& cl) {
+    block_sum<N>(v, red);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < N; ++k) part[k] = v[k];
+    cl.sync();
+    double t[N];
+    for (int k = 0; k < N; ++k) t[k] = 0.0;
+    const unsigned ranks = cl.num_blocks();
+    for (unsigned r = 0; r < ranks; ++r) {
+        const double* rp = cl.map_shared_rank(part, r);
+        for (int k = 0; k < N; ++k) t[k] += rp[k];
     }
+    for (int k = 0; k < N; ++k) v[k] = t[k];
+    cl.sync();
+}
+
+template <class R>
+__global__ void __launch_bounds__(kLinThreads) k_linear_solve(const DevTables* __restrict__ Tp, CellArrays C, int gmax) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double red[kMaxGains * 32];
+    __shared__ double part[kMaxGains];
+    cg::cluster_group cl = cg::this_cluster();
+    const DevTables& T = *Tp;
+    const int CL = static_cast<int>(cl.num_blocks());
+    const int rank = static_cast<int>(cl.block_rank());
+    const int c = blockIdx.x / CL;
+    const DevMaterial& M = T.mat[C.cell_material[c]];
+    const int na = M.n_active;
+    const int per = (C.hist_modes + CL - 1) / CL;
+    const int m0 = rank * per, m1 = min(na, m0 + per);
+    const int nloc = max(0, m1 - m0);
+    R* X = reinterpret_cast<R*>(smem);
+    R* term = X + per;
+    R* rate = term + per;
+    R* u = rate + per;                                      // gmax vectors
+    unsigned* cnt = reinterpret_cast<unsigned*>(u + static_cast<size_t>(gmax) * per);
+    const size_t hb = static_cast<size_t>(c) * C.hist_modes;
+    for (int j = threadIdx.x; j < nloc; j += blockDim.x) {
+        const int m = m0 + j;
+        const unsigned k = C.hcnt[hb + m];
+        cnt[j] = k;
+        const double e = k ? M.hw[m] * (C.hN[hb + m] - k * M.nbg[m]) : 0.0;
+        X[j] = k ? static_cast<R>(e / C.lin_s[m]) : R(0);
+        rate[j] = static_cast<R>(M.col_rate[m]);
+    }
+    __syncthreads();
     // gain vectors (src/material/CallawayOperator.cpp:193-229), multiplicity-weighted
     int G = 0;
     for (int kind = 0; kind < 2; ++kind) {
@@ -187,223 +260,196 @@ __device__ void linear_tables(const DevTables& T, const CellArrays& C, const Dev
         const int nbasis = kind == 0 ? 4 : 1;
         const int first = G;
         for (int b = 0; b < nbasis; ++b) {
-            R* v = u + static_cast<size_t>(G) * H;
+            R* v = u + static_cast<size_t>(G) * per;
             double nv[1] = {0.0};
-            for (int m = threadIdx.x; m < na; m += blockDim.x) {
+            for (int j = threadIdx.x; j < nloc; j += blockDim.x) {
+                const int m = m0 + j;
                 double val = 0.0;
-                if (cnt[m]) {
+                if (cnt[j]) {
                     const double s = C.lin_s[m];
                     const double bv = b == 0 ? s : s * M.col_k[3 * m + b - 1] / M.omega[m];
                     val = bv * sq[m];
-                    nv[0] += cnt[m] * val * val;
+                    nv[0] += cnt[j] * val * val;
                 }
-                v[m] = static_cast<R>(val);
+                v[j] = static_cast<R>(val);
             }
-            block_sum<1>(nv, red);
+            cluster_sum<1>(nv, red, part, cl);
             const double original = sqrt(nv[0]);
             if (original == 0.0) continue;
             const R inv = static_cast<R>(1.0 / original);
-            for (int m = threadIdx.x; m < na; m += blockDim.x) v[m] *= inv;
+            for (int j = threadIdx.x; j < nloc; j += blockDim.x) v[j] *= inv;
             __syncthreads();
             for (int pass = 0; pass < 2; ++pass) {
                 for (int q = first; q < G; ++q) {
-                    const R* qv = u + static_cast<size_t>(q) * H;
+                    const R* qv = u + static_cast<size_t>(q) * per;
                     double pr[1] = {0.0};
-                    for (int m = threadIdx.x; m < na; m += blockDim.x) pr[0] += cnt[m] * static_cast<double>(qv[m]) * v[m];
-                    block_sum<1>(pr, red);
+                    for (int j = threadIdx.x; j < nloc; j += blockDim.x) pr[0] += cnt[j] * static_cast<double>(qv[j]) * v[j];
+                    cluster_sum<1>(pr, red, part, cl);
                     const R p = static_cast<R>(pr[0]);
-                    for (int m = threadIdx.x; m < na; m += blockDim.x) v[m] -= p * qv[m];
+                    for (int j = threadIdx.x; j < nloc; j += blockDim.x) v[j] -= p * qv[j];
                     __syncthreads();
                 }
             }
             double ln[1] = {0.0};
-            for (int m = threadIdx.x; m < na; m += blockDim.x) ln[0] += cnt[m] * static_cast<double>(v[m]) * v[m];
-            block_sum<1>(ln, red);
+            for (int j = threadIdx.x; j < nloc; j += blockDim.x) ln[0] += cnt[j] * static_cast<double>(v[j]) * v[j];
+            cluster_sum<1>(ln, red, part, cl);
             const double len = sqrt(ln[0]);
             if (len < 1e-12) continue;
             const R il = static_cast<R>(1.0 / len);
-            for (int m = threadIdx.x; m < na; m += blockDim.x) v[m] *= il;
+            for (int j = threadIdx.x; j < nloc; j += blockDim.x) v[j] *= il;
             __syncthreads();
             ++G;
         }
         for (int q = first; q < G; ++q) {
-            R* qv = u + static_cast<size_t>(q) * H;
-            for (int m = threadIdx.x; m < na; m += blockDim.x) qv[m] *= static_cast<R>(sq[m]);
+            R* qv = u + static_cast<size_t>(q) * per;
+            for (int j = threadIdx.x; j < nloc; j += blockDim.x) qv[j] *= static_cast<R>(sq[m0 + j]);
         }
         __syncthreads();
     }
     // Taylor series of exp(h L) per substep on (L T)_m = -r_m T_m + cnt_m sum_g u_gm (u_g . T)
     const R h = static_cast<R>(C.lin_h);
     for (int sstep = 0; sstep < C.lin_substeps; ++sstep) {
-        for (int m = threadIdx.x; m < na; m += blockDim.x) term[m] = X[m];
+        for (int j = threadIdx.x; j < nloc; j += blockDim.x) term[j] = X[j];
         __syncthreads();
         for (int k = 1; k <= C.lin_terms; ++k) {
             double d[kMaxGains] = {0, 0, 0, 0, 0};
-            for (int m = threadIdx.x; m < na; m += blockDim.x) {
-                const R tm = term[m];
-                for (int g = 0; g < G; ++g) d[g] += static_cast<double>(u[static_cast<size_t>(g) * H + m]) * tm;
+            for (int j = threadIdx.x; j < nloc; j += blockDim.x) {
+                const R tm = term[j];
+                for (int g = 0; g < G; ++g) d[g] += static_cast<double>(u[static_cast<size_t>(g) * per + j] * tm);
             }
-            block_sum<kMaxGains>(d, red);
+            cluster_sum<kMaxGains>(d, red, part, cl);
             const R hk = h / static_cast<R>(k);
             R dg[kMaxGains];
             for (int g = 0; g < kMaxGains; ++g) dg[g] = static_cast<R>(d[g]);
-            for (int m = threadIdx.x; m < na; m += blockDim.x) {
+            for (int j = threadIdx.x; j < nloc; j += blockDim.x) {
                 R gain = 0;
-                for (int g = 0; g < G; ++g) gain += u[static_cast<size_t>(g) * H + m] * dg[g];
-                const R t = hk * (-static_cast<R>(M.col_rate[m]) * term[m] + static_cast<R>(cnt[m]) * gain);
-                term[m] = t;
-                X[m] += t;
+                for (int g = 0; g < G; ++g) gain += u[static_cast<size_t>(g) * per + j] * dg[g];
+                const R t = hk * (-rate[j] * term[j] + static_cast<R>(cnt[j]) * gain);
+                term[j] = t;
+                X[j] += t;
             }
             __syncthreads();
         }
     }
-    // A_m: the carriers' common additive occupation change beyond the decay
+    // A_m and, for FP32 exponentials, the FP64 rescale that conserves the cell energy
     double cons[2] = {0.0, 0.0};
-    for (int m = threadIdx.x; m < na; m += blockDim.x) {
-        const unsigned k = cnt[m];
+    double* beta = C.lin_beta + hb;
+    for (int j = threadIdx.x; j < nloc; j += blockDim.x) {
+        const int m = m0 + j;
+        const unsigned k = cnt[j];
         double A = 0.0;
         if (k) {
-            A = C.lin_s[m] * (static_cast<double>(X[m]) - C.lin_decay[m] * static_cast<double>(X0[m])) / (k * M.hw[m]);
-            cons[0] += (1.0 - C.lin_decay[m]) * M.hw[m] * (C.hN[hb + m] - k * M.nbg[m]);
+            const double e = M.hw[m] * (C.hN[hb + m] - k * M.nbg[m]);
+            const double x0 = e / C.lin_s[m];
+            A = C.lin_s[m] * (static_cast<double>(X[j]) - C.lin_decay[m] * x0) / (k * M.hw[m]);
+            cons[0] += (1.0 - C.lin_decay[m]) * e;
             cons[1] += k * M.hw[m] * A;
         }
-        alpha[m] = C.lin_decay[m];
-        betac[m] = A;
+        beta[m] = A;
     }
     double lambda = 1.0;
     if (C.mixed) {
-        // FP64 energy-conservation rescaling of the FP32 gain term
-        block_sum<2>(cons, red);
+        cluster_sum<2>(cons, red, part, cl);
         if (cons[1] != 0.0 && isfinite(cons[0] / cons[1])) lambda = cons[0] / cons[1];
     }
-    for (int m = threadIdx.x; m < na; m += blockDim.x) betac[m] = (1.0 - C.lin_decay[m]) * M.nbg[m] + lambda * betac[m];
     __syncthreads();
+    for (int j = threadIdx.x; j < nloc; j += blockDim.x) {
+        const int m = m0 + j;
+        beta[m] = (1.0 - C.lin_decay[m]) * M.nbg[m] + lambda * beta[m];
+    }
 }
 
-// phase 0: statistics only (initial population; pending table = first drive half);
-// 1: full step; 2: as 1 with the cell temperatures supplied in C.temperature.
-template <bool kMixed>
-__global__ void __launch_bounds__(kCellThreads) k_cell_solve(const DevTables* __restrict__ Tp, CellArrays C,
-                                                             DevLedger* L, int phase, int collision) {
-    __shared__ double red[kMaxGains * 32];
+// ----------------------------------------------- tables and step energies
+template <int kCollision>
+__global__ void __launch_bounds__(kStatThreads) k_cell_tables(const DevTables* __restrict__ Tp, CellArrays C, int phase) {
+    __shared__ double red[4 * 32];
     const DevTables& T = *Tp;
-    const int c = blockIdx.x;
-    const int mid = C.cell_material[c];
-    const DevMaterial& M = T.mat[mid];
-    const int na = M.n_active;
+    const int c = blockIdx.y;
+    const DevMaterial& M = T.mat[C.cell_material[c]];
     const size_t hb = static_cast<size_t>(c) * C.hist_modes;
-    const unsigned* cnt = C.hcnt + hb;
-    // ---- energy after transport and gradient sums
-    double v[3] = {0.0, 0.0, 0.0};
-    for (int m = threadIdx.x; m < na; m += blockDim.x) {
-        const unsigned k = cnt[m];
-        if (!k) continue;
-        v[0] += M.hw[m] * (C.hN[hb + m] - k * M.nbg[m]);
-        if (M.grad_rate) {
-            v[1] += k * M.grad_rate[m];
-            v[2] += k * M.cap_bg[m];
-        }
-    }
-    block_sum<3>(v, red);
-    const double E = v[0] * M.energy_weight / C.volume[c] + M.energy_density_bg;
-    double Tc;
-    if (phase == 2) {
-        Tc = C.temperature[c];
-    } else {
-        Tc = T.par.linearized ? T.par.background_T + (E - M.energy_density_bg) / M.heat_capacity_density_bg
-                              : table_inverse(M.lookup_E, M.lookup_T, M.n_lookup, E);
-    }
-    const double ratio = v[2] > 0.0 ? v[1] / v[2] : 0.0;
-    if (threadIdx.x == 0) {
-        if (!isfinite(E)) raise_error(L, kErrNonFinite, c);
-        C.energy[c] = E;
-        C.temperature[c] = Tc;
-        C.grad_ratio[c] = ratio;
-    }
-    // ---- collision coefficients (alpha, beta) per mode, in a per-cell slice of
-    // the scratch placed after the solver's work vectors
-    double2* ab = C.ab + hb;
-    double* al = nullptr;
-    double* be = nullptr;
-    const bool collide = phase >= 1 && collision != kCollideNone;
-    if (collide) {
-        al = C.scratch + static_cast<size_t>(gridDim.x) * (collision == kCollideRta ? 5 * C.n_classes
-                                                                                      : C.hist_modes * (3 + kMaxGains)) +
-             static_cast<size_t>(c) * 2 * C.hist_modes;
-        be = al + C.hist_modes;
-        if (collision == kCollideRta) rta_tables(T, C, M, c, Tc, red, al, be);
-        else if (kMixed) linear_tables<float>(T, C, M, c, red, al, be);
-        else linear_tables<double>(T, C, M, c, red, al, be);
-    }
-    // ---- pending table, residual, drive energy, end-of-step energy
+    const int m0 = blockIdx.x * kChunk, m1 = min(M.n_active, m0 + kChunk);
     const double half = 0.5 * T.par.dt;
+    const double ratio = C.grad_ratio[c];
+    const bool collide = phase >= 1 && kCollision != kCollideNone;
     double s[4] = {0.0, 0.0, 0.0, 0.0}; // residual, drive, updates, energy deviation at step end
-    for (int m = threadIdx.x; m < na; m += blockDim.x) {
-        const unsigned k = cnt[m];
-        const double a = collide ? al[m] : 1.0;
-        const double bc = collide ? be[m] : 0.0;
+    for (int m = m0 + threadIdx.x; m < m1; m += blockDim.x) {
+        double a = 1.0, bc = 0.0;
+        if (collide) {
+            if (kCollision == kCollideRta) {
+                const double2 r = C.rta_ab[static_cast<size_t>(c) * C.n_classes + M.mode_class[m]];
+                a = 1.0 - r.x;
+                bc = r.x * r.y;
+            } else {
+                a = C.lin_decay[m];
+                bc = C.lin_beta[hb + m];
+            }
+        }
         const double D = M.grad_rate ? half * (M.grad_rate[m] - M.cap_bg[m] * ratio) * M.inv_hw[m] : 0.0;
-        ab[m] = make_double2(a, collide ? bc + 2.0 * D : D);
-        if (!k) continue;
-        const double N = C.hN[hb + m];
-        const double hw = M.hw[m];
-        s[0] += hw * ((a - 1.0) * N + k * bc);
-        if (D != 0.0) {
-            s[1] += k * hw * D;
-            s[2] += k;
+        C.ab[hb + m] = make_double2(a, collide ? bc + 2.0 * D : D);
+        const unsigned k = C.hcnt[hb + m];
+        if (k) {
+            const double N = C.hN[hb + m];
+            const double hw = M.hw[m];
+            s[0] += hw * ((a - 1.0) * N + k * bc);
+            if (D != 0.0) {
+                s[1] += k * hw * D;
+                s[2] += k;
+            }
+            const double N1 = phase >= 1 ? a * N + k * (bc + D) : N;
+            s[3] += hw * (N1 - k * M.nbg[m]);
         }
-        const double N1 = a * N + k * (bc + D);
-        s[3] += hw * (N1 - k * M.nbg[m]);
-    }
-    block_sum<4>(s, red);
-    if (threadIdx.x == 0) {
-        const double w = M.energy_weight;
-        if (phase >= 1) {
-            atomicAdd(&L->step_lifetime_residual, s[0] * w);
-            atomicAdd(&L->step_drive_ev, s[1] * w);
-            atomicAdd(&L->step_drive_updates, static_cast<unsigned long long>(s[2]));
-        }
-        atomicAdd(&L->next_drive_ev, s[1] * w);
-        atomicAdd(&L->next_drive_updates, static_cast<unsigned long long>(s[2]));
-        const double Ef = (phase >= 1 ? s[3] : v[0]) * w / C.volume[c] + M.energy_density_bg;
-        C.energy_final[c] = Ef;
-        C.temperature_final[c] =
-            phase == 2 ? Tc
-                       : (T.par.linearized
-                              ? T.par.background_T + (Ef - M.energy_density_bg) / M.heat_capacity_density_bg
-                              : table_inverse(M.lookup_E, M.lookup_T, M.n_lookup, Ef));
-    }
-    __syncthreads();
-    // ---- clear the bins for the next transport pass
-    for (int m = threadIdx.x; m < na; m += blockDim.x) {
         C.hcnt[hb + m] = 0;
         C.hN[hb + m] = 0.0;
         if (C.hM) C.hM[hb + m] = 0.0;
     }
+    block_sum<4>(s, red);
+    if (threadIdx.x == 0 && m0 < M.n_active) {
+        double* f = C.cell_final + 4 * c;
+        atomicAdd(f, s[0]);
+        atomicAdd(f + 1, s[1]);
+        atomicAdd(f + 2, s[2]);
+        atomicAdd(f + 3, s[3]);
+    }
 }
 
-// End of step: total thermal energy and the energy ledger. One CTA.
+// End of step: cell temperatures, total thermal energy and the energy ledger. One CTA.
 __global__ void __launch_bounds__(1024) k_cells_final(const DevTables* __restrict__ Tp, CellArrays C, DevLedger* L,
-                                                      int initial) {
-    __shared__ double red[32];
+                                                      int phase) {
+    __shared__ double red[4 * 32];
     const DevTables& T = *Tp;
-    double thermal = 0.0;
+    double v[4] = {0.0, 0.0, 0.0, 0.0}; // thermal, residual, drive, updates
     for (int c = threadIdx.x; c < C.ncells; c += blockDim.x) {
         const DevMaterial& M = T.mat[C.cell_material[c]];
-        thermal += (C.energy_final[c] - M.zero_point) * C.volume[c];
+        double* f = C.cell_final + 4 * c;
+        const double w = M.energy_weight;
+        const double Ef = f[3] * w / C.volume[c] + M.energy_density_bg;
+        if (!isfinite(Ef)) raise_error(L, kErrNonFinite, c);
+        C.energy_final[c] = Ef;
+        C.temperature_final[c] =
+            phase == 2 ? C.temperature[c]
+                       : (T.par.linearized ? T.par.background_T + (Ef - M.energy_density_bg) / M.heat_capacity_density_bg
+                                           : table_inverse(M.lookup_E, M.lookup_T, M.n_lookup, Ef));
+        v[0] += (Ef - M.zero_point) * C.volume[c];
+        v[1] += f[0] * w;
+        v[2] += f[1] * w;
+        v[3] += f[2];
+        for (int k = 0; k < 4; ++k) {
+            f[k] = 0.0;
+            C.cell_stats[4 * c + k] = 0.0;
+        }
     }
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int o = 16; o > 0; o >>= 1) thermal += __shfl_xor_sync(0xffffffffu, thermal, o);
-    if (lane == 0) red[wid] = thermal;
-    __syncthreads();
+    block_sum<4>(v, red);
     if (threadIdx.x != 0) return;
-    double total = 0.0;
-    for (int w = 0; w < (blockDim.x >> 5); ++w) total += red[w];
-    if (initial) {
-        L->thermal_energy = total;
+    L->next_drive_ev += v[2];
+    L->next_drive_updates += static_cast<unsigned long long>(v[3]);
+    if (phase == 0) {
+        L->thermal_energy = v[0];
         return;
     }
-    const double residual = total - L->thermal_energy - 0.0 - L->step_drive_ev - L->step_injected_ev +
+    L->step_lifetime_residual += v[1];
+    L->step_drive_ev += v[2];
+    L->step_drive_updates += static_cast<unsigned long long>(v[3]);
+    const double residual = v[0] - L->thermal_energy - 0.0 - L->step_drive_ev - L->step_injected_ev +
                             L->step_absorbed_ev - L->step_lifetime_residual;
     L->step_balance_residual = residual;
     L->total_absorbed += L->step_absorbed;
@@ -414,7 +460,7 @@ __global__ void __launch_bounds__(1024) k_cells_final(const DevTables* __restric
     L->total_balance_residual += residual;
     L->total_drive_ev += L->step_drive_ev;
     L->total_drive_updates += L->step_drive_updates;
-    L->thermal_energy = total;
+    L->thermal_energy = v[0];
     L->particle_count += static_cast<long long>(L->step_injected) - static_cast<long long>(L->step_absorbed);
     for (int r = 0; r < kMaxReservoirs; ++r) L->previous_res[r] = L->absorbed_res[r];
 }
@@ -422,13 +468,75 @@ __global__ void __launch_bounds__(1024) k_cells_final(const DevTables* __restric
 // ----------------------------------------------------------- launchers
 void launch_step_begin(const LaunchCtx& x) { k_step_begin<<<1, 1, 0, x.stream>>>(x.L); }
 
-void launch_cell_solve(const LaunchCtx& x, int phase, int collision) {
-    if (x.C.mixed) k_cell_solve<true><<<x.C.ncells, kCellThreads, 0, x.stream>>>(x.T, x.C, x.L, phase, collision);
-    else k_cell_solve<false><<<x.C.ncells, kCellThreads, 0, x.stream>>>(x.T, x.C, x.L, phase, collision);
+static size_t linear_smem(const CellArrays& C, int cl, int gmax, size_t real) {
+    const size_t per = (static_cast<size_t>(C.hist_modes) + cl - 1) / cl;
+    return per * ((3 + gmax) * real + sizeof(unsigned));
 }
 
-void launch_cells_final(const LaunchCtx& x, int initial) {
-    k_cells_final<<<1, 1024, 0, x.stream>>>(x.T, x.C, x.L, initial);
+// Cluster size for the linear solve: the smallest of 8, 16 whose per-CTA slice fits.
+int linear_cluster_size(const CellArrays& C, bool mixed) {
+    const int gmax = C.lin_has_normal ? kMaxGains : 1;
+    const size_t real = mixed ? sizeof(float) : sizeof(double);
+    for (int cl : {8, 16})
+        if (linear_smem(C, cl, gmax, real) <= 200 * 1024) return cl;
+    return 0;
+}
+
+void prepare_linear_solve(const CellArrays& C) {
+    const int gmax = C.lin_has_normal ? kMaxGains : 1;
+    const size_t sm = linear_smem(C, C.lin_cluster, gmax, C.mixed ? sizeof(float) : sizeof(double));
+    auto set = [&](const void* f) {
+        cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+        if (C.lin_cluster > 8) cudaFuncSetAttribute(f, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    };
+    if (C.mixed) set(reinterpret_cast<const void*>(k_linear_solve<float>));
+    else set(reinterpret_cast<const void*>(k_linear_solve<double>));
+}
+
+int launch_cell_solve(const LaunchCtx& x, int phase, int collision) {
+    const CellArrays& C = x.C;
+    const DevTables* T = x.T;
+    const int chunks = (C.hist_modes + kChunk - 1) / kChunk;
+    const dim3 grid(chunks, C.ncells);
+    const bool rta = collision == kCollideRta;
+    int launches = 3;
+    if (rta) k_cell_stats<true><<<grid, kStatThreads, 0, x.stream>>>(T, C, phase >= 1 ? 1 : 0);
+    else k_cell_stats<false><<<grid, kStatThreads, 0, x.stream>>>(T, C, 0);
+    k_cell_state<<<(C.ncells + 255) / 256, 256, 0, x.stream>>>(T, C, x.L, phase);
+    if (phase >= 1 && rta) {
+        k_rta_solve<<<C.ncells, 256, 0, x.stream>>>(T, C);
+        ++launches;
+    } else if (phase >= 1 && collision == kCollideLinear) {
+        const int gmax = C.lin_has_normal ? kMaxGains : 1;
+        const int cl = C.lin_cluster;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(C.ncells * cl);
+        cfg.blockDim = dim3(kLinThreads);
+        cfg.dynamicSmemBytes = linear_smem(C, cl, gmax, C.mixed ? sizeof(float) : sizeof(double));
+        cfg.stream = x.stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = cl;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        const cudaError_t err = C.mixed ? cudaLaunchKernelEx(&cfg, k_linear_solve<float>, T, C, gmax)
+                                        : cudaLaunchKernelEx(&cfg, k_linear_solve<double>, T, C, gmax);
+        if (err != cudaSuccess)
+            throw std::runtime_error(std::string("cluster launch of the collision exponential failed: ") +
+                                     cudaGetErrorString(err));
+        ++launches;
+    }
+    if (phase >= 1 && rta) k_cell_tables<kCollideRta><<<grid, kStatThreads, 0, x.stream>>>(T, C, phase);
+    else if (phase >= 1 && collision == kCollideLinear)
+        k_cell_tables<kCollideLinear><<<grid, kStatThreads, 0, x.stream>>>(T, C, phase);
+    else k_cell_tables<kCollideNone><<<grid, kStatThreads, 0, x.stream>>>(T, C, phase);
+    return launches;
+}
+
+void launch_cells_final(const LaunchCtx& x, int phase) {
+    k_cells_final<<<1, 1024, 0, x.stream>>>(x.T, x.C, x.L, phase);
 }
 
 } // namespace phmc

@@ -30,8 +30,10 @@ void launch_containment(const LaunchCtx& x, bool mixed);
 void launch_flux(const LaunchCtx& x, bool mixed);
 void launch_apply_pending(const LaunchCtx& x, bool subtract_drive);
 void launch_step_begin(const LaunchCtx& x);
-void launch_cell_solve(const LaunchCtx& x, int phase, int collision);
-void launch_cells_final(const LaunchCtx& x, int initial);
+int launch_cell_solve(const LaunchCtx& x, int phase, int collision);
+int linear_cluster_size(const CellArrays& C, bool mixed);
+void prepare_linear_solve(const CellArrays& C);
+void launch_cells_final(const LaunchCtx& x, int phase);
 
 // collision kinds for launch_cell_solve
 enum CollisionKind : int { kCollideNone = 0, kCollideRta = 1, kCollideLinear = 2 };

@@ -282,21 +282,17 @@ void DeviceSolver::upload_tables() {
     C.temperature_final = dalloc<double>(ncells_);
     C.grad_ratio = dalloc<double>(ncells_);
     C.flux = dalloc<double>(3 * static_cast<size_t>(ncells_));
+    C.cell_stats = dalloc<double>(4 * static_cast<size_t>(ncells_));
+    C.cell_final = dalloc<double>(4 * static_cast<size_t>(ncells_));
     const MaterialTables& M0 = P_.mats[0];
     if (rta) {
         // class CSR of material 0 for the RTA solve
-        std::vector<int> start(M0.n_classes + 1, 0), modes(M0.n_active);
-        for (int a = 0; a < M0.n_active; ++a) ++start[M0.mode_class[a] + 1];
-        for (int k = 0; k < M0.n_classes; ++k) start[k + 1] += start[k];
-        std::vector<int> cursor(start.begin(), start.end() - 1);
-        for (int a = 0; a < M0.n_active; ++a) modes[cursor[M0.mode_class[a]]++] = a;
-        C.class_start = upload(start);
-        C.class_modes = upload(modes);
         C.n_classes = M0.n_classes;
-        C.scratch = dalloc<double>(static_cast<size_t>(ncells_) * (5 * static_cast<size_t>(M0.n_classes) + 2 * hist_modes));
+        C.cls_sum = dalloc<double>(static_cast<size_t>(ncells_) * M0.n_classes * 3);
+        C.rta_ab = dalloc<double2>(static_cast<size_t>(ncells_) * M0.n_classes);
     } else {
         if (P_.mats.size() != 1) throw std::runtime_error("Linear-response collisions support one material in this build.");
-        C.scratch = dalloc<double>(static_cast<size_t>(ncells_) * hist_modes * (8 + 2));
+        C.lin_beta = dalloc<double>(hist);
         const int S = std::max(1, static_cast<int>(std::ceil(cfg_.time_step * r_max)));
         const double h = cfg_.time_step / S;
         const double x = h * r_max;
@@ -325,6 +321,9 @@ void DeviceSolver::upload_tables() {
         C.lin_sqrt_rn = upload(srn);
         C.lin_sqrt_rr = upload(srr);
         C.lin_has_normal = has_normal ? 1 : 0;
+        C.lin_cluster = linear_cluster_size(C, mixed_);
+        if (C.lin_cluster == 0) throw std::runtime_error("Too many modes per cell for the cluster exponential.");
+        prepare_linear_solve(C);
     }
 }
 
@@ -346,9 +345,8 @@ int DeviceSolver::collision_kind() const {
 void DeviceSolver::initial_statistics() {
     const LaunchCtx x = ctx();
     launch_histogram(x, !P_.linearized);
-    launch_cell_solve(x, 0, collision_kind());
-    launch_cells_final(x, 1);
-    counters_.launches += 3;
+    counters_.launches += 2 + launch_cell_solve(x, 0, collision_kind());
+    launch_cells_final(x, 0);
     materialized_ = true;
 }
 
@@ -400,9 +398,8 @@ void DeviceSolver::run_timestep() {
         launch_containment(x, mixed_);
         counters_.launches += 1;
     }
-    launch_cell_solve(x, 1, coll);
-    launch_cells_final(x, 0);
-    counters_.launches += 2;
+    counters_.launches += 1 + launch_cell_solve(x, 1, coll);
+    launch_cells_final(x, 1);
     materialized_ = false;
     ++step_;
     elapsed_ += cfg_.time_step;
@@ -430,9 +427,9 @@ double DeviceSolver::collide_only(const double* cell_temperature) {
                                   cudaMemcpyHostToDevice, stream_));
         phase = 2;
     }
-    launch_cell_solve(x, phase, collision_kind());
+    counters_.launches += 5 + launch_cell_solve(x, phase, collision_kind());
+    launch_cells_final(x, phase);
     launch_apply_pending(x, false);
-    counters_.launches += 5;
     synchronize();
     double r = 0;
     PHMC_CUDA(cudaMemcpy(&r, &d_ledger_->step_lifetime_residual, sizeof(double), cudaMemcpyDeviceToHost));

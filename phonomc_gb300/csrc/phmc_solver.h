@@ -53,8 +53,15 @@ struct CellArrays {
     double* temperature_final;
     double* grad_ratio;      // sum of gradient rates / sum of capacities, per cell
     double* flux;            // [ncells*3]
-    double* scratch;         // per-cell work space of the collision solve
+    double* cell_stats;      // [ncells*4] energy deviation, gradient rate sum, capacity sum
+    double* cell_final;      // [ncells*4] lifetime residual, drive energy, drive updates, final energy deviation
     int mixed;               // FP32 linear-response exponential with FP64 energy rescale
+    // RTA: per (cell, class) multiplicity / occupation / max(1, n) sums and (a, n_eq(T*))
+    double* cls_sum;
+    double2* rta_ab;
+    // linear response: beta of the pending update per (cell, mode)
+    double* lin_beta;
+    int lin_cluster;         // CTAs per cell of the cluster exponential
     // linear-response collision (one material): per-mode constants
     const double* lin_decay; // exp(-r dt)
     const double* lin_s;     // sqrt(capacity)
