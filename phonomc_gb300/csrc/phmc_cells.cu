@@ -222,8 +222,9 @@ __device__ __forceinline__ void cluster_sum(double (&v)[N], double* red, double*
     cl.sync();
 }
 
-template <class R>
-__global__ void __launch_bounds__(kLinThreads) k_linear_solve(const DevTables* __restrict__ Tp, CellArrays C, int gmax) {
+template <class R, int GMAX>
+__global__ void __launch_bounds__(kLinThreads) k_linear_solve(const DevTables* __restrict__ Tp, CellArrays C) {
+    constexpr int gmax = GMAX;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ double red[kMaxGains * 32];
     __shared__ double part[kMaxGains];
@@ -312,18 +313,29 @@ __global__ void __launch_bounds__(kLinThreads) k_linear_solve(const DevTables* _
         for (int j = threadIdx.x; j < nloc; j += blockDim.x) term[j] = X[j];
         __syncthreads();
         for (int k = 1; k <= C.lin_terms; ++k) {
-            double d[kMaxGains] = {0, 0, 0, 0, 0};
+            // per-thread partials in R, one FP64 conversion per gain
+            R dl[GMAX];
+#pragma unroll
+            for (int g = 0; g < GMAX; ++g) dl[g] = R(0);
             for (int j = threadIdx.x; j < nloc; j += blockDim.x) {
                 const R tm = term[j];
-                for (int g = 0; g < G; ++g) d[g] += static_cast<double>(u[static_cast<size_t>(g) * per + j] * tm);
+#pragma unroll
+                for (int g = 0; g < GMAX; ++g)
+                    if (g < G) dl[g] += u[static_cast<size_t>(g) * per + j] * tm;
             }
-            cluster_sum<kMaxGains>(d, red, part, cl);
+            double d[GMAX];
+#pragma unroll
+            for (int g = 0; g < GMAX; ++g) d[g] = static_cast<double>(dl[g]);
+            cluster_sum<GMAX>(d, red, part, cl);
             const R hk = h / static_cast<R>(k);
-            R dg[kMaxGains];
-            for (int g = 0; g < kMaxGains; ++g) dg[g] = static_cast<R>(d[g]);
+            R dg[GMAX];
+#pragma unroll
+            for (int g = 0; g < GMAX; ++g) dg[g] = static_cast<R>(d[g]);
             for (int j = threadIdx.x; j < nloc; j += blockDim.x) {
                 R gain = 0;
-                for (int g = 0; g < G; ++g) gain += u[static_cast<size_t>(g) * per + j] * dg[g];
+#pragma unroll
+                for (int g = 0; g < GMAX; ++g)
+                    if (g < G) gain += u[static_cast<size_t>(g) * per + j] * dg[g];
                 const R t = hk * (-rate[j] * term[j] + static_cast<R>(cnt[j]) * gain);
                 term[j] = t;
                 X[j] += t;
@@ -368,7 +380,6 @@ __global__ void __launch_bounds__(kStatThreads) k_cell_tables(const DevTables* _
     const DevMaterial& M = T.mat[C.cell_material[c]];
     const size_t hb = static_cast<size_t>(c) * C.hist_modes;
     const int m0 = blockIdx.x * kChunk, m1 = min(M.n_active, m0 + kChunk);
-    const double half = 0.5 * T.par.dt;
     const double ratio = C.grad_ratio[c];
     const bool collide = phase >= 1 && kCollision != kCollideNone;
     double s[4] = {0.0, 0.0, 0.0, 0.0}; // residual, drive, updates, energy deviation at step end
@@ -384,7 +395,7 @@ __global__ void __launch_bounds__(kStatThreads) k_cell_tables(const DevTables* _
                 bc = C.lin_beta[hb + m];
             }
         }
-        const double D = M.grad_rate ? half * (M.grad_rate[m] - M.cap_bg[m] * ratio) * M.inv_hw[m] : 0.0;
+        const double D = M.grad_rate ? fma(-M.drive_cap[m], ratio, M.drive_rate[m]) : 0.0;
         C.ab[hb + m] = make_double2(a, collide ? bc + 2.0 * D : D);
         const unsigned k = C.hcnt[hb + m];
         if (k) {
@@ -489,8 +500,13 @@ void prepare_linear_solve(const CellArrays& C) {
         cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
         if (C.lin_cluster > 8) cudaFuncSetAttribute(f, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     };
-    if (C.mixed) set(reinterpret_cast<const void*>(k_linear_solve<float>));
-    else set(reinterpret_cast<const void*>(k_linear_solve<double>));
+    if (C.lin_has_normal) {
+        if (C.mixed) set(reinterpret_cast<const void*>(k_linear_solve<float, kMaxGains>));
+        else set(reinterpret_cast<const void*>(k_linear_solve<double, kMaxGains>));
+    } else {
+        if (C.mixed) set(reinterpret_cast<const void*>(k_linear_solve<float, 1>));
+        else set(reinterpret_cast<const void*>(k_linear_solve<double, 1>));
+    }
 }
 
 int launch_cell_solve(const LaunchCtx& x, int phase, int collision) {
@@ -521,8 +537,13 @@ int launch_cell_solve(const LaunchCtx& x, int phase, int collision) {
         attr[0].val.clusterDim.z = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        const cudaError_t err = C.mixed ? cudaLaunchKernelEx(&cfg, k_linear_solve<float>, T, C, gmax)
-                                        : cudaLaunchKernelEx(&cfg, k_linear_solve<double>, T, C, gmax);
+        cudaError_t err;
+        if (C.lin_has_normal)
+            err = C.mixed ? cudaLaunchKernelEx(&cfg, k_linear_solve<float, kMaxGains>, T, C)
+                          : cudaLaunchKernelEx(&cfg, k_linear_solve<double, kMaxGains>, T, C);
+        else
+            err = C.mixed ? cudaLaunchKernelEx(&cfg, k_linear_solve<float, 1>, T, C)
+                          : cudaLaunchKernelEx(&cfg, k_linear_solve<double, 1>, T, C);
         if (err != cudaSuccess)
             throw std::runtime_error(std::string("cluster launch of the collision exponential failed: ") +
                                      cudaGetErrorString(err));

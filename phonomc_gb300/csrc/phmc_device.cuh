@@ -70,6 +70,8 @@ struct DevMaterial {
     const double* col_rr;      // resistive rate [active]
     const double* col_k;       // [active*3]
     const double* grad_rate;   // [active]
+    const double* drive_rate;  // [active] half dt * rate / hw: drive half-step D = drive_rate - drive_cap * ratio
+    const double* drive_cap;   // [active] half dt * capacity / hw
     double energy_weight;
     double energy_density_bg;
     double heat_capacity_density_bg;

@@ -79,8 +79,35 @@ DeviceSolver::DeviceSolver(const SimulationConfig& cfg, const std::vector<const 
     append_convergence_row();
 }
 
+void DeviceSolver::set_l2_window() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceProp prop{};
+    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess || prop.persistingL2CacheMaxSize <= 0 ||
+        prop.accessPolicyMaxWindowSize <= 0)
+        return;
+    const size_t persist = std::min(hot_bytes_, static_cast<size_t>(prop.persistingL2CacheMaxSize));
+    if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, persist) != cudaSuccess) return;
+    cudaStreamAttrValue attr{};
+    attr.accessPolicyWindow.base_ptr = hot_;
+    attr.accessPolicyWindow.num_bytes = std::min(hot_bytes_, static_cast<size_t>(prop.accessPolicyMaxWindowSize));
+    attr.accessPolicyWindow.hitRatio =
+        static_cast<float>(std::min(1.0, static_cast<double>(persist) / attr.accessPolicyWindow.num_bytes));
+    attr.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    attr.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    if (cudaStreamSetAttribute(stream_, cudaStreamAttributeAccessPolicyWindow, &attr) == cudaSuccess)
+        l2_window_ = true;
+}
+
 DeviceSolver::~DeviceSolver() {
     if (stream_) cudaStreamSynchronize(stream_);
+    if (l2_window_) {
+        cudaStreamAttrValue attr{};
+        attr.accessPolicyWindow.num_bytes = 0;
+        cudaStreamSetAttribute(stream_, cudaStreamAttributeAccessPolicyWindow, &attr);
+        cudaCtxResetPersistingL2Cache();
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
+    }
     for (void* p : allocations_) cudaFree(p);
     if (d_tables_) cudaFree(d_tables_);
     if (stream_) cudaStreamDestroy(stream_);
@@ -172,7 +199,16 @@ void DeviceSolver::upload_tables() {
             D.col_rr = upload(M.col_resistive);
             D.col_k = upload(M.col_k);
         }
-        if (!M.grad_rate.empty()) D.grad_rate = upload(M.grad_rate);
+        if (!M.grad_rate.empty()) {
+            D.grad_rate = upload(M.grad_rate);
+            std::vector<double> dr(M.n_active), dc(M.n_active);
+            for (int a = 0; a < M.n_active; ++a) {
+                dr[a] = 0.5 * cfg_.time_step * M.grad_rate[a] / M.hw[a];
+                dc[a] = 0.5 * cfg_.time_step * M.capacity_bg[a] / M.hw[a];
+            }
+            D.drive_rate = upload(dr);
+            D.drive_cap = upload(dc);
+        }
         D.energy_weight = M.energy_weight;
         D.energy_density_bg = M.energy_density_bg;
         D.heat_capacity_density_bg = M.heat_capacity_density_bg;
@@ -272,10 +308,22 @@ void DeviceSolver::upload_tables() {
     C.volume = upload(domain_->grid_volumes());
     const size_t hist = static_cast<size_t>(ncells_) * hist_modes;
     const bool rta = !P_.linearized;
-    C.hcnt = dalloc<unsigned int>(hist);
-    C.hN = dalloc<double>(hist);
-    C.hM = rta ? dalloc<double>(hist) : nullptr;
-    C.ab = dalloc<double2>(hist);
+    // The bins and the pending table are gathered/atomically updated at random
+    // by the transport pass: keep them in one block that an L2 access-policy
+    // window marks persisting, while carrier arrays stream through.
+    {
+        auto align = [](size_t b) { return (b + 255) & ~size_t(255); };
+        const size_t b_ab = align(hist * sizeof(double2)), b_n = align(hist * sizeof(double)),
+                     b_c = align(hist * sizeof(unsigned)), b_m = rta ? align(hist * sizeof(double)) : 0;
+        hot_bytes_ = b_ab + b_n + b_c + b_m;
+        char* hot = dalloc<char>(hot_bytes_);
+        hot_ = hot;
+        C.ab = reinterpret_cast<double2*>(hot);
+        C.hN = reinterpret_cast<double*>(hot + b_ab);
+        C.hcnt = reinterpret_cast<unsigned int*>(hot + b_ab + b_n);
+        C.hM = rta ? reinterpret_cast<double*>(hot + b_ab + b_n + b_c) : nullptr;
+        set_l2_window();
+    }
     C.energy = dalloc<double>(ncells_);
     C.temperature = dalloc<double>(ncells_);
     C.energy_final = dalloc<double>(ncells_);

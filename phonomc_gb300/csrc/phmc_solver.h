@@ -153,6 +153,10 @@ private:
     bool profile_pass_a_ = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pass_a_events_;
     bool materialized_ = true;
+    void* hot_ = nullptr;
+    size_t hot_bytes_ = 0;
+    bool l2_window_ = false;
+    void set_l2_window();
     void materialize();
     struct LaunchCtx ctx() const;
     int collision_kind() const;

@@ -166,7 +166,7 @@ __device__ __forceinline__ double apply_pending(const CellArrays& C, int cell, i
 __device__ __forceinline__ double drive_half(const DevTables& T, const CellArrays& C, const DevMaterial& M, int cell,
                                              int ai) {
     if (!M.grad_rate) return 0.0;
-    return 0.5 * T.par.dt * (M.grad_rate[ai] - M.cap_bg[ai] * C.grad_ratio[cell]) * M.inv_hw[ai];
+    return fma(-M.drive_cap[ai], C.grad_ratio[cell], M.drive_rate[ai]);
 }
 
 // ---------------------------------------------------- FP32 flight (mixed)
@@ -309,35 +309,35 @@ __global__ void __launch_bounds__(256) k_transport(const DevTables* __restrict__
     const DevTables& T = *Tp;
     const int n = L->n_slots;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        if (!S.alive[i]) continue;
-        uint32_t w = S.mode[i];
-        const int c0 = S.cell[i];
-        double occ = apply_pending(C, c0, static_cast<int>(w & 0x00FFFFFFu), S.occ[i]);
+        if (!__ldcs(S.alive + i)) continue;
+        uint32_t w = __ldcs(S.mode + i);
+        const int c0 = __ldcs(S.cell + i);
+        double occ = apply_pending(C, c0, static_cast<int>(w & 0x00FFFFFFu), __ldcs(S.occ + i));
         bool alive;
         int c;
         if (kMixed) {
             const Frame F = cell_frame(T.dom, c0);
-            float p[3] = {S.ox[i], S.oy[i], S.oz[i]};
+            float p[3] = {__ldcs(S.ox + i), __ldcs(S.oy + i), __ldcs(S.oz + i)};
             alive = advance_mixed(T, L, &bl, i, F, p, w, occ, T.par.dt32, kDrawTransport, step);
             c = settle_mixed(T.dom, F, p);
-            S.ox[i] = p[0];
-            S.oy[i] = p[1];
-            S.oz[i] = p[2];
+            __stcs(S.ox + i, p[0]);
+            __stcs(S.oy + i, p[1]);
+            __stcs(S.oz + i, p[2]);
         } else {
-            double p[3] = {S.x[i], S.y[i], S.z[i]};
+            double p[3] = {__ldcs(S.x + i), __ldcs(S.y + i), __ldcs(S.z + i)};
             alive = advance_carrier(T, L, &bl, i, p, w, occ, T.par.dt, kDrawTransport, step);
             c = grid_index(T.dom, p[0], p[1], p[2]);
-            S.x[i] = p[0];
-            S.y[i] = p[1];
-            S.z[i] = p[2];
+            __stcs(S.x + i, p[0]);
+            __stcs(S.y + i, p[1]);
+            __stcs(S.z + i, p[2]);
         }
-        S.mode[i] = w;
-        S.occ[i] = occ;
+        __stcs(S.mode + i, w);
+        __stcs(S.occ + i, occ);
         if (!alive) {
             S.alive[i] = 0;
             continue;
         }
-        S.cell[i] = c;
+        __stcs(S.cell + i, c);
         bin_carrier(C, L, i, c, static_cast<int>(w >> 28), static_cast<int>(w & 0x00FFFFFFu), occ, kRta);
     }
     __syncthreads();
