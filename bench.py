@@ -56,32 +56,87 @@ def measured_peak():
 
 
 class ClockSampler:
-    """nvidia-smi clock/throttle samples during the timed region."""
+    """SM clock and clock-event reasons sampled DURING the timed region.
+
+    A thread polls NVML (libnvidia-ml through ctypes) every 10 ms, so even a
+    timed region of a few milliseconds gets samples; where NVML cannot be
+    loaded it falls back to `nvidia-smi -lms 200`."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReasons bits
+    BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20, "hw_thermal_slowdown": 0x40,
+            "hw_power_brake_slowdown": 0x80}
 
-    def __init__(self):
-        self.rows = []
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []          # (sm_mhz, max_mhz, reasons bitmask)
         self.proc = None
+        self.nvml = None
+        self.stop = threading.Event()
+
+    def _nvml_open(self):
+        try:
+            nv = C.CDLL("libnvidia-ml.so.1")
+            if nv.nvmlInit_v2() != 0:
+                return False
+            h = C.c_void_p()
+            if nv.nvmlDeviceGetHandleByIndex_v2(C.c_uint(self.index), C.byref(h)) != 0:
+                return False
+            self.nvml, self.handle = nv, h
+            self.reason_fn = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                nv.nvmlDeviceGetCurrentClocksThrottleReasons
+            return True
+        except (OSError, AttributeError):
+            return False
+
+    def _nvml_sample(self):
+        cur, mx, rs = C.c_uint(), C.c_uint(), C.c_ulonglong()
+        if self.nvml.nvmlDeviceGetClockInfo(self.handle, 1, C.byref(cur)) != 0:
+            return
+        self.nvml.nvmlDeviceGetMaxClockInfo(self.handle, 1, C.byref(mx))
+        self.reason_fn(self.handle, C.byref(rs))
+        self.rows.append((float(cur.value), float(mx.value), int(rs.value)))
+
+    def _nvml_loop(self):
+        while not self.stop.is_set():
+            self._nvml_sample()
+            self.stop.wait(0.01)
 
     def __enter__(self):
+        if self._nvml_open():
+            self._nvml_sample()
+            self.t = threading.Thread(target=self._nvml_loop, daemon=True)
+            self.t.start()
+            return self
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
-                                          "-lms", "200", "-i", "0"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
-                                         text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
+                                          "-lms", "200", "-i", str(self.index)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._smi_read, daemon=True)
             self.t.start()
         except Exception:
             self.proc = None
         return self
 
-    def _read(self):
+    def _smi_read(self):
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in self.proc.stdout:
-            self.rows.append([x.strip() for x in line.split(",")])
+            r = [x.strip() for x in line.split(",")]
+            if len(r) < 9 or not r[1].replace(".", "").isdigit():
+                continue
+            bits = 0
+            for k, name in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    bits |= self.BITS[name]
+            self.rows.append((float(r[1]), float(r[2]) if r[2].replace(".", "").isdigit() else 0.0, bits))
 
     def __exit__(self, *a):
+        if self.nvml is not None:
+            self._nvml_sample()
+            self.stop.set()
+            self.t.join(timeout=5)
         if self.proc:
             self.proc.terminate()
             try:
@@ -92,16 +147,9 @@ class ClockSampler:
     def summary(self):
         if not self.rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
-        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = set()
-        for r in self.rows:
-            for k, name in enumerate(names):
-                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
-                    reasons.add(name)
-        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(self.rows)}
+        reasons = sorted({name for _, _, bits in self.rows for name, b in self.BITS.items() if bits & b})
+        return {"sm_mhz": float(np.median([r[0] for r in self.rows])), "sm_max_mhz": max(r[1] for r in self.rows),
+                "reasons": reasons, "samples": len(self.rows), "source": "nvml" if self.nvml else "nvidia-smi"}
 
 
 def _oracle_replica(args):

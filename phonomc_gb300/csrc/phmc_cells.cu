@@ -37,6 +37,9 @@ constexpr int kChunk = 1024;     // modes per stats/tables block
 constexpr int kMaxGains = 5;
 constexpr int kLinThreads = 256;
 
+// Sum over the block, result in every thread: shuffles within each warp, then
+// warp 0 folds the per-warp sums, so only 2 x 5 shuffle-adds per value reach
+// the FP64 pipe in the threads that do them.
 template <int N> __device__ __forceinline__ void block_sum(double (&v)[N], double* red) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
@@ -46,12 +49,17 @@ template <int N> __device__ __forceinline__ void block_sum(double (&v)[N], doubl
         if (lane == 0) red[k * 32 + wid] = x;
     }
     __syncthreads();
+    if (wid == 0) {
 #pragma unroll
-    for (int k = 0; k < N; ++k) {
-        double x = 0.0;
-        for (int w = 0; w < nw; ++w) x += red[k * 32 + w];
-        v[k] = x;
+        for (int k = 0; k < N; ++k) {
+            double x = lane < nw ? red[k * 32 + lane] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            if (lane == 0) red[k * 32] = x;
+        }
     }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < N; ++k) v[k] = red[k * 32];
     __syncthreads();
 }
 
@@ -79,9 +87,9 @@ __global__ void __launch_bounds__(kStatThreads) k_cell_stats(const DevTables* __
     const int m0 = blockIdx.x * kChunk, m1 = min(M.n_active, m0 + kChunk);
     double v[3] = {0.0, 0.0, 0.0};
     for (int m = m0 + threadIdx.x; m < m1; m += blockDim.x) {
-        const unsigned k = C.hcnt[hb + m];
+        const unsigned k = C.bins[hb + m].cnt;
         if (!k) continue;
-        const double N = C.hN[hb + m];
+        const double N = C.bins[hb + m].N;
         v[0] += M.hw[m] * (N - k * M.nbg[m]);
         if (M.grad_rate) {
             v[1] += k * M.grad_rate[m];
@@ -205,29 +213,60 @@ __global__ void __launch_bounds__(256) k_rta_solve(const DevTables* __restrict__
 // ----------------------------------------------------- linear response
 // Cluster-wide sum of N doubles: CTA partials in shared memory, read by every
 // CTA of the cluster through distributed shared memory.
-template <int N>
-__device__ __forceinline__ void cluster_sum(double (&v)[N], double* red, double* part, cg::cluster_group& cl) {
-    block_sum<N>(v, red);
-    if (threadIdx.x == 0)
-        for (int k = 0; k < N; ++k) part[k] = v[k];
-    cl.sync();
-    double t[N];
-    for (int k = 0; k < N; ++k) t[k] = 0.0;
-    const unsigned ranks = cl.num_blocks();
-    for (unsigned r = 0; r < ranks; ++r) {
-        const double* rp = cl.map_shared_rank(part, r);
-        for (int k = 0; k < N; ++k) t[k] += rp[k];
+// Sum over the thread-block cluster, result in every thread. Values are
+// summed in V within each warp; warp 0 of each block folds its warps in FP64
+// into part[parity][], and after the cluster barrier warp 0 of each block
+// folds the blocks' part[parity][] through distributed shared memory into
+// total[]. part[] alternates between two buffers, so one cluster barrier per
+// sum suffices: a block can only write a buffer again after every block has
+// passed the next sum's barrier, i.e. finished reading that buffer.
+template <int N, class V>
+__device__ __forceinline__ void cluster_sum(V (&v)[N], double* red, double (*part)[kMaxGains], double* total,
+                                            int& parity, cg::cluster_group& cl) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        V x = v[k];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) red[k * 32 + wid] = static_cast<double>(x);
     }
-    for (int k = 0; k < N; ++k) v[k] = t[k];
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            double x = lane < nw ? red[k * 32 + lane] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            if (lane == 0) part[parity][k] = x;
+        }
+    }
     cl.sync();
+    if (wid == 0) {
+        const int ranks = static_cast<int>(cl.num_blocks());
+        const double* rp = cl.map_shared_rank(part[parity], lane < ranks ? lane : 0);
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            double x = lane < ranks ? rp[k] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            if (lane == 0) total[k] = x;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < N; ++k) v[k] = static_cast<V>(total[k]);
+    parity ^= 1;
 }
 
 template <class R, int GMAX>
 __global__ void __launch_bounds__(kLinThreads) k_linear_solve(const DevTables* __restrict__ Tp, CellArrays C) {
+    // R = float: FP32 exponential from division-free FP32 per-mode tables; FP64
+    // only for the bin energies, the conservation sums and the final beta.
+    constexpr bool kF32 = sizeof(R) == sizeof(float);
     constexpr int gmax = GMAX;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ double red[kMaxGains * 32];
-    __shared__ double part[kMaxGains];
+    __shared__ double part[2][kMaxGains];
+    __shared__ double total[kMaxGains];
+    int parity = 0;
     cg::cluster_group cl = cg::this_cluster();
     const DevTables& T = *Tp;
     const int CL = static_cast<int>(cl.num_blocks());
@@ -246,11 +285,17 @@ __global__ void __launch_bounds__(kLinThreads) k_linear_solve(const DevTables* _
     const size_t hb = static_cast<size_t>(c) * C.hist_modes;
     for (int j = threadIdx.x; j < nloc; j += blockDim.x) {
         const int m = m0 + j;
-        const unsigned k = C.hcnt[hb + m];
+        const BinSum bin = C.bins[hb + m];
+        const unsigned k = bin.cnt;
         cnt[j] = k;
-        const double e = k ? M.hw[m] * (C.hN[hb + m] - k * M.nbg[m]) : 0.0;
-        X[j] = k ? static_cast<R>(e / C.lin_s[m]) : R(0);
-        rate[j] = static_cast<R>(M.col_rate[m]);
+        const double e = k ? M.hw[m] * (bin.N - k * M.nbg[m]) : 0.0;
+        if constexpr (kF32) {
+            X[j] = static_cast<float>(e) * C.lin32_inv_s[m];
+            rate[j] = C.lin32_rate[m];
+        } else {
+            X[j] = k ? e / C.lin_s[m] : 0.0;
+            rate[j] = M.col_rate[m];
+        }
     }
     __syncthreads();
     // gain vectors (src/material/CallawayOperator.cpp:193-229), multiplicity-weighted
@@ -258,52 +303,61 @@ __global__ void __launch_bounds__(kLinThreads) k_linear_solve(const DevTables* _
     for (int kind = 0; kind < 2; ++kind) {
         if (kind == 0 && !C.lin_has_normal) continue;
         const double* sq = kind == 0 ? C.lin_sqrt_rn : C.lin_sqrt_rr;
+        const float* sq32 = kind == 0 ? C.lin32_sqrt_rn : C.lin32_sqrt_rr;
         const int nbasis = kind == 0 ? 4 : 1;
         const int first = G;
         for (int b = 0; b < nbasis; ++b) {
             R* v = u + static_cast<size_t>(G) * per;
-            double nv[1] = {0.0};
+            R nv[1] = {R(0)};
+            const float* basis32 = C.lin32_basis + static_cast<size_t>(kind == 0 ? 1 + b : 0) * na;
             for (int j = threadIdx.x; j < nloc; j += blockDim.x) {
                 const int m = m0 + j;
-                double val = 0.0;
+                R val = R(0);
                 if (cnt[j]) {
-                    const double s = C.lin_s[m];
-                    const double bv = b == 0 ? s : s * M.col_k[3 * m + b - 1] / M.omega[m];
-                    val = bv * sq[m];
-                    nv[0] += cnt[j] * val * val;
+                    if constexpr (kF32) {
+                        val = basis32[m];
+                    } else {
+                        const double sv = C.lin_s[m];
+                        val = (b == 0 ? sv : sv * M.col_k[3 * m + b - 1] / M.omega[m]) * sq[m];
+                    }
+                    nv[0] += static_cast<R>(cnt[j]) * val * val;
                 }
-                v[j] = static_cast<R>(val);
+                v[j] = val;
             }
-            cluster_sum<1>(nv, red, part, cl);
-            const double original = sqrt(nv[0]);
-            if (original == 0.0) continue;
-            const R inv = static_cast<R>(1.0 / original);
+            cluster_sum<1>(nv, red, part, total, parity, cl);
+            const R original = sqrt(nv[0]);
+            if (original == R(0)) continue;
+            const R inv = R(1) / original;
             for (int j = threadIdx.x; j < nloc; j += blockDim.x) v[j] *= inv;
             __syncthreads();
             for (int pass = 0; pass < 2; ++pass) {
                 for (int q = first; q < G; ++q) {
                     const R* qv = u + static_cast<size_t>(q) * per;
-                    double pr[1] = {0.0};
-                    for (int j = threadIdx.x; j < nloc; j += blockDim.x) pr[0] += cnt[j] * static_cast<double>(qv[j]) * v[j];
-                    cluster_sum<1>(pr, red, part, cl);
-                    const R p = static_cast<R>(pr[0]);
-                    for (int j = threadIdx.x; j < nloc; j += blockDim.x) v[j] -= p * qv[j];
+                    R pr[1] = {R(0)};
+                    for (int j = threadIdx.x; j < nloc; j += blockDim.x) pr[0] += static_cast<R>(cnt[j]) * qv[j] * v[j];
+                    cluster_sum<1>(pr, red, part, total, parity, cl);
+                    const R pq = pr[0];
+                    for (int j = threadIdx.x; j < nloc; j += blockDim.x) v[j] -= pq * qv[j];
                     __syncthreads();
                 }
             }
-            double ln[1] = {0.0};
-            for (int j = threadIdx.x; j < nloc; j += blockDim.x) ln[0] += cnt[j] * static_cast<double>(v[j]) * v[j];
-            cluster_sum<1>(ln, red, part, cl);
-            const double len = sqrt(ln[0]);
-            if (len < 1e-12) continue;
-            const R il = static_cast<R>(1.0 / len);
+            R ln[1] = {R(0)};
+            for (int j = threadIdx.x; j < nloc; j += blockDim.x) ln[0] += static_cast<R>(cnt[j]) * v[j] * v[j];
+            cluster_sum<1>(ln, red, part, total, parity, cl);
+            const R len = sqrt(ln[0]);
+            // dependent direction: dropped below 1e-12 (FP64), or below FP32 round-off
+            if (len < R(kF32 ? 1e-5 : 1e-12)) continue;
+            const R il = R(1) / len;
             for (int j = threadIdx.x; j < nloc; j += blockDim.x) v[j] *= il;
             __syncthreads();
             ++G;
         }
         for (int q = first; q < G; ++q) {
             R* qv = u + static_cast<size_t>(q) * per;
-            for (int j = threadIdx.x; j < nloc; j += blockDim.x) qv[j] *= static_cast<R>(sq[m0 + j]);
+            for (int j = threadIdx.x; j < nloc; j += blockDim.x) {
+                if constexpr (kF32) qv[j] *= sq32[m0 + j];
+                else qv[j] *= sq[m0 + j];
+            }
         }
         __syncthreads();
     }
@@ -313,7 +367,7 @@ __global__ void __launch_bounds__(kLinThreads) k_linear_solve(const DevTables* _
         for (int j = threadIdx.x; j < nloc; j += blockDim.x) term[j] = X[j];
         __syncthreads();
         for (int k = 1; k <= C.lin_terms; ++k) {
-            // per-thread partials in R, one FP64 conversion per gain
+            // per-thread partials and warp sums in R; FP64 only across warps and blocks
             R dl[GMAX];
 #pragma unroll
             for (int g = 0; g < GMAX; ++g) dl[g] = R(0);
@@ -323,19 +377,13 @@ __global__ void __launch_bounds__(kLinThreads) k_linear_solve(const DevTables* _
                 for (int g = 0; g < GMAX; ++g)
                     if (g < G) dl[g] += u[static_cast<size_t>(g) * per + j] * tm;
             }
-            double d[GMAX];
-#pragma unroll
-            for (int g = 0; g < GMAX; ++g) d[g] = static_cast<double>(dl[g]);
-            cluster_sum<GMAX>(d, red, part, cl);
+            cluster_sum<GMAX>(dl, red, part, total, parity, cl);
             const R hk = h / static_cast<R>(k);
-            R dg[GMAX];
-#pragma unroll
-            for (int g = 0; g < GMAX; ++g) dg[g] = static_cast<R>(d[g]);
             for (int j = threadIdx.x; j < nloc; j += blockDim.x) {
                 R gain = 0;
 #pragma unroll
                 for (int g = 0; g < GMAX; ++g)
-                    if (g < G) gain += u[static_cast<size_t>(g) * per + j] * dg[g];
+                    if (g < G) gain += u[static_cast<size_t>(g) * per + j] * dl[g];
                 const R t = hk * (-rate[j] * term[j] + static_cast<R>(cnt[j]) * gain);
                 term[j] = t;
                 X[j] += t;
@@ -351,24 +399,34 @@ __global__ void __launch_bounds__(kLinThreads) k_linear_solve(const DevTables* _
         const unsigned k = cnt[j];
         double A = 0.0;
         if (k) {
-            const double e = M.hw[m] * (C.hN[hb + m] - k * M.nbg[m]);
-            const double x0 = e / C.lin_s[m];
-            A = C.lin_s[m] * (static_cast<double>(X[j]) - C.lin_decay[m] * x0) / (k * M.hw[m]);
-            cons[0] += (1.0 - C.lin_decay[m]) * e;
+            const double e = M.hw[m] * (C.bins[hb + m].N - k * M.nbg[m]);
+            if constexpr (kF32) {
+                const float x0 = static_cast<float>(e) * C.lin32_inv_s[m];
+                A = static_cast<double>(C.lin32_s_over_hw[m] * (X[j] - C.lin32_decay[m] * x0) *
+                                        __frcp_rn(static_cast<float>(k)));
+                cons[0] += C.lin_omd[m] * e;
+            } else {
+                const double x0 = e / C.lin_s[m];
+                A = C.lin_s[m] * (static_cast<double>(X[j]) - C.lin_decay[m] * x0) / (k * M.hw[m]);
+                cons[0] += (1.0 - C.lin_decay[m]) * e;
+            }
             cons[1] += k * M.hw[m] * A;
         }
         beta[m] = A;
     }
     double lambda = 1.0;
     if (C.mixed) {
-        cluster_sum<2>(cons, red, part, cl);
+        cluster_sum<2>(cons, red, part, total, parity, cl);
         if (cons[1] != 0.0 && isfinite(cons[0] / cons[1])) lambda = cons[0] / cons[1];
     }
     __syncthreads();
     for (int j = threadIdx.x; j < nloc; j += blockDim.x) {
         const int m = m0 + j;
-        beta[m] = (1.0 - C.lin_decay[m]) * M.nbg[m] + lambda * beta[m];
+        if constexpr (kF32) beta[m] = fma(lambda, beta[m], C.lin_bg[m]);
+        else beta[m] = (1.0 - C.lin_decay[m]) * M.nbg[m] + lambda * beta[m];
     }
+    // no block leaves while another block of the cluster may still read its part[]
+    cl.sync();
 }
 
 // ----------------------------------------------- tables and step energies
@@ -382,7 +440,7 @@ __global__ void __launch_bounds__(kStatThreads) k_cell_tables(const DevTables* _
     const int m0 = blockIdx.x * kChunk, m1 = min(M.n_active, m0 + kChunk);
     const double ratio = C.grad_ratio[c];
     const bool collide = phase >= 1 && kCollision != kCollideNone;
-    double s[4] = {0.0, 0.0, 0.0, 0.0}; // residual, drive, updates, energy deviation at step end
+    double s[3] = {0.0, 0.0, 0.0}; // residual, drive, updates
     for (int m = m0 + threadIdx.x; m < m1; m += blockDim.x) {
         double a = 1.0, bc = 0.0;
         if (collide) {
@@ -396,30 +454,32 @@ __global__ void __launch_bounds__(kStatThreads) k_cell_tables(const DevTables* _
             }
         }
         const double D = M.grad_rate ? fma(-M.drive_cap[m], ratio, M.drive_rate[m]) : 0.0;
-        C.ab[hb + m] = make_double2(a, collide ? bc + 2.0 * D : D);
-        const unsigned k = C.hcnt[hb + m];
+        const BinSum bin = C.bins[hb + m];
+        const unsigned k = bin.cnt;
         if (k) {
-            const double N = C.hN[hb + m];
             const double hw = M.hw[m];
-            s[0] += hw * ((a - 1.0) * N + k * bc);
+            s[0] += hw * ((a - 1.0) * bin.N + k * bc);
             if (D != 0.0) {
                 s[1] += k * hw * D;
                 s[2] += k;
             }
-            const double N1 = phase >= 1 ? a * N + k * (bc + D) : N;
-            s[3] += hw * (N1 - k * M.nbg[m]);
         }
-        C.hcnt[hb + m] = 0;
-        C.hN[hb + m] = 0.0;
+        C.ab[hb + m] = make_double2(a, collide ? bc + 2.0 * D : D);
+        BinSum zero;
+        zero.N = 0.0;
+        zero.cnt = 0;
+        zero.pad = 0;
+        C.bins[hb + m] = zero;
         if (C.hM) C.hM[hb + m] = 0.0;
     }
-    block_sum<4>(s, red);
+    // the step-end energy deviation of the cell is the step-start one (cell
+    // statistics) plus the collision change s[0] plus the drive change s[1]
+    block_sum<3>(s, red);
     if (threadIdx.x == 0 && m0 < M.n_active) {
         double* f = C.cell_final + 4 * c;
         atomicAdd(f, s[0]);
         atomicAdd(f + 1, s[1]);
         atomicAdd(f + 2, s[2]);
-        atomicAdd(f + 3, s[3]);
     }
 }
 
@@ -433,7 +493,8 @@ __global__ void __launch_bounds__(1024) k_cells_final(const DevTables* __restric
         const DevMaterial& M = T.mat[C.cell_material[c]];
         double* f = C.cell_final + 4 * c;
         const double w = M.energy_weight;
-        const double Ef = f[3] * w / C.volume[c] + M.energy_density_bg;
+        const double dev = C.cell_stats[4 * c] + (phase >= 1 ? f[0] + f[1] : 0.0);
+        const double Ef = dev * w / C.volume[c] + M.energy_density_bg;
         if (!isfinite(Ef)) raise_error(L, kErrNonFinite, c);
         C.energy_final[c] = Ef;
         C.temperature_final[c] =

@@ -79,35 +79,8 @@ DeviceSolver::DeviceSolver(const SimulationConfig& cfg, const std::vector<const 
     append_convergence_row();
 }
 
-void DeviceSolver::set_l2_window() {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceProp prop{};
-    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess || prop.persistingL2CacheMaxSize <= 0 ||
-        prop.accessPolicyMaxWindowSize <= 0)
-        return;
-    const size_t persist = std::min(hot_bytes_, static_cast<size_t>(prop.persistingL2CacheMaxSize));
-    if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, persist) != cudaSuccess) return;
-    cudaStreamAttrValue attr{};
-    attr.accessPolicyWindow.base_ptr = hot_;
-    attr.accessPolicyWindow.num_bytes = std::min(hot_bytes_, static_cast<size_t>(prop.accessPolicyMaxWindowSize));
-    attr.accessPolicyWindow.hitRatio =
-        static_cast<float>(std::min(1.0, static_cast<double>(persist) / attr.accessPolicyWindow.num_bytes));
-    attr.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
-    attr.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
-    if (cudaStreamSetAttribute(stream_, cudaStreamAttributeAccessPolicyWindow, &attr) == cudaSuccess)
-        l2_window_ = true;
-}
-
 DeviceSolver::~DeviceSolver() {
     if (stream_) cudaStreamSynchronize(stream_);
-    if (l2_window_) {
-        cudaStreamAttrValue attr{};
-        attr.accessPolicyWindow.num_bytes = 0;
-        cudaStreamSetAttribute(stream_, cudaStreamAttributeAccessPolicyWindow, &attr);
-        cudaCtxResetPersistingL2Cache();
-        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
-    }
     for (void* p : allocations_) cudaFree(p);
     if (d_tables_) cudaFree(d_tables_);
     if (stream_) cudaStreamDestroy(stream_);
@@ -308,22 +281,9 @@ void DeviceSolver::upload_tables() {
     C.volume = upload(domain_->grid_volumes());
     const size_t hist = static_cast<size_t>(ncells_) * hist_modes;
     const bool rta = !P_.linearized;
-    // The bins and the pending table are gathered/atomically updated at random
-    // by the transport pass: keep them in one block that an L2 access-policy
-    // window marks persisting, while carrier arrays stream through.
-    {
-        auto align = [](size_t b) { return (b + 255) & ~size_t(255); };
-        const size_t b_ab = align(hist * sizeof(double2)), b_n = align(hist * sizeof(double)),
-                     b_c = align(hist * sizeof(unsigned)), b_m = rta ? align(hist * sizeof(double)) : 0;
-        hot_bytes_ = b_ab + b_n + b_c + b_m;
-        char* hot = dalloc<char>(hot_bytes_);
-        hot_ = hot;
-        C.ab = reinterpret_cast<double2*>(hot);
-        C.hN = reinterpret_cast<double*>(hot + b_ab);
-        C.hcnt = reinterpret_cast<unsigned int*>(hot + b_ab + b_n);
-        C.hM = rta ? reinterpret_cast<double*>(hot + b_ab + b_n + b_c) : nullptr;
-        set_l2_window();
-    }
+    C.bins = dalloc<BinSum>(hist);
+    C.ab = dalloc<double2>(hist);
+    C.hM = rta ? dalloc<double>(hist) : nullptr;
     C.energy = dalloc<double>(ncells_);
     C.temperature = dalloc<double>(ncells_);
     C.energy_final = dalloc<double>(ncells_);
@@ -369,6 +329,36 @@ void DeviceSolver::upload_tables() {
         C.lin_sqrt_rn = upload(srn);
         C.lin_sqrt_rr = upload(srr);
         C.lin_has_normal = has_normal ? 1 : 0;
+        {
+            const int na = M0.n_active;
+            std::vector<float> inv_s(na), rate(na), dec(na), soh(na), basis(5 * static_cast<size_t>(na)), rn(na), rr(na);
+            std::vector<double> omd(na), bg(na);
+            for (int a = 0; a < na; ++a) {
+                const double hw = M0.hw[a];
+                inv_s[a] = sc[a] > 0.0 ? static_cast<float>(1.0 / sc[a]) : 0.0f;
+                rate[a] = static_cast<float>(M0.col_normal[a] + M0.col_resistive[a]);
+                dec[a] = static_cast<float>(decay[a]);
+                soh[a] = hw > 0.0 ? static_cast<float>(sc[a] / hw) : 0.0f;
+                basis[a] = static_cast<float>(sc[a] * srr[a]);
+                for (int b = 0; b < 4; ++b) {
+                    const double kb = b == 0 ? 1.0 : (M0.omega[a] != 0.0 ? M0.col_k[3 * a + b - 1] / M0.omega[a] : 0.0);
+                    basis[(1 + b) * static_cast<size_t>(na) + a] = static_cast<float>(sc[a] * kb * srn[a]);
+                }
+                rn[a] = static_cast<float>(srn[a]);
+                rr[a] = static_cast<float>(srr[a]);
+                omd[a] = 1.0 - decay[a];
+                bg[a] = omd[a] * M0.nbg[a];
+            }
+            C.lin32_inv_s = upload(inv_s);
+            C.lin32_rate = upload(rate);
+            C.lin32_decay = upload(dec);
+            C.lin32_s_over_hw = upload(soh);
+            C.lin32_basis = upload(basis);
+            C.lin32_sqrt_rn = upload(rn);
+            C.lin32_sqrt_rr = upload(rr);
+            C.lin_omd = upload(omd);
+            C.lin_bg = upload(bg);
+        }
         C.lin_cluster = linear_cluster_size(C, mixed_);
         if (C.lin_cluster == 0) throw std::runtime_error("Too many modes per cell for the cluster exponential.");
         prepare_linear_solve(C);

@@ -38,15 +38,23 @@ namespace phmc {
 // pass applies it when it loads the carrier. Every collision and drive update
 // of the reference is affine in the occupation with coefficients that depend
 // only on the carrier's cell and mode, so this reproduces them exactly.
+// Population sums of one (cell, mode) bin, accumulated by the transport pass:
+// sum of occupations and multiplicity share one 16-byte record, so the two
+// atomics of a carrier touch one L2 sector.
+struct __align__(16) BinSum {
+    double N;
+    unsigned int cnt;
+    unsigned int pad;
+};
+
 struct CellArrays {
     int ncells;
     int hist_modes;          // modes per cell in the bins (max active count over materials)
     const int* cell_material;
     const double* volume;
-    unsigned int* hcnt;      // [ncells * hist_modes] multiplicity
-    double* hN;              // [ncells * hist_modes] summed occupation
-    double* hM;              // [ncells * hist_modes] summed max(1, n) (RTA only)
+    BinSum* bins;            // [ncells * hist_modes] bin sums (sum of n, multiplicity)
     double2* ab;             // [ncells * hist_modes] pending (alpha, beta)
+    double* hM;              // [ncells * hist_modes] summed max(1, n) (RTA only)
     double* energy;          // energy density after transport
     double* temperature;     // temperature after transport
     double* energy_final;    // energy density at the end of the step
@@ -68,6 +76,16 @@ struct CellArrays {
     const double* lin_sqrt_rn;
     const double* lin_sqrt_rr;
     int lin_has_normal;
+    // FP32 exponential (mixed precision): per-mode constants without divisions
+    const float* lin32_inv_s;     // 1 / sqrt(capacity)
+    const float* lin32_rate;      // total collision rate
+    const float* lin32_decay;     // exp(-r dt)
+    const float* lin32_s_over_hw; // sqrt(capacity) / (hbar omega)
+    const float* lin32_basis;     // [5][modes]: s sqrt(r_R), s k_b/omega sqrt(r_N) (b = 0..3, k_0/omega = 1)
+    const float* lin32_sqrt_rn;
+    const float* lin32_sqrt_rr;
+    const double* lin_omd;        // 1 - exp(-r dt)
+    const double* lin_bg;         // (1 - exp(-r dt)) n_bg
     int lin_substeps;
     double lin_h;
     int lin_terms;
@@ -153,10 +171,6 @@ private:
     bool profile_pass_a_ = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pass_a_events_;
     bool materialized_ = true;
-    void* hot_ = nullptr;
-    size_t hot_bytes_ = 0;
-    bool l2_window_ = false;
-    void set_l2_window();
     void materialize();
     struct LaunchCtx ctx() const;
     int collision_kind() const;

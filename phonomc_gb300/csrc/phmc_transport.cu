@@ -151,8 +151,8 @@ __device__ __forceinline__ void bin_carrier(const CellArrays& C, DevLedger* L, i
         return;
     }
     const size_t h = static_cast<size_t>(cell) * C.hist_modes + ai;
-    atomicAdd(C.hcnt + h, 1u);
-    atomicAdd(C.hN + h, occ);
+    atomicAdd(&C.bins[h].cnt, 1u);
+    atomicAdd(&C.bins[h].N, occ);
     if (rta) atomicAdd(C.hM + h, fmax(1.0, occ));
 }
 
@@ -206,7 +206,7 @@ __device__ __forceinline__ void mode_velocity32(const DevMaterial& M, uint32_t w
 // Free flight in FP32 in the frame of the starting cell. Walls are hit
 // exactly (the coordinate is set to the wall), so no push-off distance is
 // needed; periodic faces map the coordinate to the opposite wall.
-__device__ bool advance_mixed(const DevTables& T, DevLedger* L, BlockLedger* bl, int slot, const Frame& F, float p[3],
+__device__ __forceinline__ bool advance_mixed(const DevTables& T, DevLedger* L, BlockLedger* bl, int slot, const Frame& F, float p[3],
                               uint32_t& w, double& occ, float remaining, uint32_t purpose, uint32_t step) {
     const DevDomain& D = T.dom;
     const DevParams& P = T.par;
@@ -235,9 +235,13 @@ __device__ bool advance_mixed(const DevTables& T, DevLedger* L, BlockLedger* bl,
         }
         remaining -= t;
         const int axis = plane >> 1;
+        const bool hi_side = (plane & 1) != 0;
+        // the hit coordinate lands on the wall (selects keep p and F in registers)
 #pragma unroll
-        for (int a = 0; a < 3; ++a) p[a] = fmaf(v[a], t, p[a]);
-        p[axis] = (plane & 1) ? F.hi[axis] : F.lo[axis];
+        for (int a = 0; a < 3; ++a) {
+            p[a] = fmaf(v[a], t, p[a]);
+            if (a == axis) p[a] = hi_side ? F.hi[a] : F.lo[a];
+        }
         const char cond = D.cond[plane];
         const int ai = static_cast<int>(w & 0x00FFFFFFu);
         if (cond == 'T') {
@@ -249,7 +253,9 @@ __device__ bool advance_mixed(const DevTables& T, DevLedger* L, BlockLedger* bl,
             return false;
         }
         if (cond == 'P' && D.pair[plane] >= 0) {
-            p[axis] = (plane & 1) ? F.lo[axis] : F.hi[axis];
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                if (a == axis) p[a] = hi_side ? F.lo[a] : F.hi[a];
             continue;
         }
         const int table = D.rough_table[mid][plane];

@@ -237,3 +237,44 @@ def test_mixed_energy_conservation_linearized(gpu):
     scale = abs(st["total_thermal_energy_ev"])
     assert abs(st["step_lifetime_energy_residual_ev"]) < 1e-13 * scale
     assert abs(st["step_energy_balance_residual_ev"]) < 1e-13 * scale
+
+
+# ------------------------------------------------------------ Callaway (normal + resistive)
+def _callaway_cfg(particles, seed):
+    return workloads.scaled(workloads.inplane_gradient(), particles, random_seed=seed, collision_model="callaway")
+
+
+def test_callaway_steps_match_oracle(gpu, orc):
+    """Linear-response collisions with momentum-conserving normal processes
+    (four normal gain directions plus the resistive one): whole steps on the
+    device against the oracle."""
+    mat = synthetic.make_material(mesh=16, callaway=True)
+    cfg = _callaway_cfg(20000, 13)
+    mg = abi.Material(gpu, "phmc_", mat, 0.1, True, True)
+    mo = abi.Material(orc, "orc_", mat, 0.1, True, True)
+    sg = abi.Solver(gpu, "phmc_", cfg, [mg])
+    so = abi.Solver(orc, "orc_", cfg, [mo])
+    for _ in range(2):
+        sg.run(2)
+        so.run(2)
+        _compare(sg, so, tol=1e-11)
+
+
+def test_mixed_callaway_conserves_energy_and_tracks_plain(gpu):
+    """FP32 Callaway exponential (five gain directions) with the FP64 rescale:
+    the collision changes the carried energy only at round-off, and cell
+    temperatures follow the FP64 path to 1e-3 K."""
+    mat = synthetic.make_material(mesh=16, callaway=True)
+    cfg = _callaway_cfg(100000, 17)
+    m = abi.Material(gpu, "phmc_", mat, 0.1, True, True)
+    sp = abi.Solver(gpu, "phmc_", dict(cfg, precision="fp64"), [m])
+    sm = abi.Solver(gpu, "phmc_", dict(cfg, precision="mixed"), [m])
+    sp.run(5)
+    sm.run(5)
+    st = sm.stats()
+    scale = abs(st["total_thermal_energy_ev"])
+    assert abs(st["step_lifetime_energy_residual_ev"]) < 1e-13 * scale
+    assert abs(st["step_energy_balance_residual_ev"]) < 1e-13 * scale
+    Tp, _, _ = sp.cells()
+    Tm, _, _ = sm.cells()
+    assert np.max(np.abs(Tp - Tm)) < 1e-3
