@@ -73,6 +73,7 @@ __global__ void k_step_begin(DevLedger* L) {
     L->next_drive_ev = 0;
     L->next_drive_updates = 0;
     L->n_inject = 0;
+    L->n_deferred = 0;
 }
 
 // ------------------------------------------------------------ statistics

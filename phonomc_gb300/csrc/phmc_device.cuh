@@ -145,6 +145,7 @@ struct DevLedger {
     int n_slots;            // slots in use [0, n_slots)
     int n_holes;            // free slots below n_slots at injection
     int n_inject;           // carriers injected this step
+    int n_deferred;         // wall events queued by the mixed transport pass this step
     int inject_count[kMaxReservoirs];
     int inject_offset[kMaxReservoirs + 1];
     unsigned int absorbed_res[kMaxReservoirs];  // this step
@@ -183,6 +184,7 @@ struct CarrierState {
     uint32_t* mode;
     int32_t* cell;
     uint8_t* alive;
+    int4* deferred; // mixed path: queued wall events (slot, time left, event, wall), capacity entries
     int capacity;
 };
 

@@ -21,7 +21,7 @@ struct LaunchCtx {
     int grid_blocks;
 };
 
-void launch_transport(const LaunchCtx& x, bool mixed, bool rta, uint32_t step);
+int launch_transport(const LaunchCtx& x, bool mixed, bool rta, uint32_t step);
 void launch_histogram(const LaunchCtx& x, bool rta);
 void launch_init_cells(const LaunchCtx& x, bool mixed);
 void launch_positions_out(const LaunchCtx& x);

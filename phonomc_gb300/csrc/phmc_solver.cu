@@ -95,6 +95,7 @@ void DeviceSolver::allocate_state(int capacity) {
         state_.ox = dalloc<float>(capacity);
         state_.oy = dalloc<float>(capacity);
         state_.oz = dalloc<float>(capacity);
+        state_.deferred = dalloc<int4>(capacity);
     }
     state_.occ = dalloc<double>(capacity);
     state_.mode = dalloc<uint32_t>(capacity);
@@ -423,12 +424,11 @@ void DeviceSolver::run_timestep() {
         PHMC_CUDA(cudaEventCreate(&e1));
         PHMC_CUDA(cudaEventRecord(e0, stream_));
     }
-    launch_transport(x, mixed_, coll == kCollideRta, static_cast<uint32_t>(step_));
+    counters_.launches += 1 + launch_transport(x, mixed_, coll == kCollideRta, static_cast<uint32_t>(step_));
     if (profile_pass_a_) {
         PHMC_CUDA(cudaEventRecord(e1, stream_));
         pass_a_events_.push_back({e0, e1});
     }
-    counters_.launches += 2;
     if (!P_.reservoirs.empty())
         counters_.launches += launch_inject(x, mixed_, coll == kCollideRta, d_holes_, d_block_dead_, state_.capacity,
                                             static_cast<uint32_t>(step_));

@@ -203,18 +203,62 @@ __device__ __forceinline__ void mode_velocity32(const DevMaterial& M, uint32_t w
     }
 }
 
+// Rough (or, with conservative boundaries, any non-periodic) wall hit
+// (src/solver/BoundaryInteraction.cpp:53-162): sample the outgoing mode and
+// occupation from the wall's table with the draws of (slot, step, purpose,
+// event). False when the event raised an error (the carrier then stays where
+// it is, as the reference stops its flight with the throw).
+__device__ __forceinline__ bool wall_sample_mixed(const DevTables& T, DevLedger* L, int slot, int plane, uint32_t& w,
+                                                  double& occ, int event, uint32_t purpose, uint32_t step) {
+    const DevDomain& D = T.dom;
+    const DevParams& P = T.par;
+    const int mid = static_cast<int>(w >> 28);
+    const DevMaterial& M = T.mat[mid];
+    const int axis = plane >> 1;
+    const int ai = static_cast<int>(w & 0x00FFFFFFu);
+    const int table = D.rough_table[mid][plane];
+    if (table < 0) {
+        raise_error(L, kErrModeMapping, slot);
+        return false;
+    }
+    const Uniform2 d0 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose, static_cast<uint32_t>(event), 0);
+    const Uniform2 d1 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose, static_cast<uint32_t>(event), 1);
+    double n_out;
+    const int out = rough_sample_dev(T.rough[table], M, ai, occ, P.conservative != 0, d0.a, d0.b, d1.a, n_out);
+    const double vn = M.vel[3 * out + axis] * ((plane & 1) ? 1.0 : -1.0);
+    uint32_t signs = 0;
+    if (P.conservative) {
+        if (!isfinite(n_out) || !(M.omega[out] > 0.0) || !(vn < 0.0)) {
+            raise_error(L, kErrModeMapping, slot);
+            return false;
+        }
+    } else if (vn > 0.0) {
+        signs = 1u << axis;
+    }
+    w = static_cast<uint32_t>(out) | (signs << 24) | (static_cast<uint32_t>(mid) << 28);
+    occ = n_out;
+    return true;
+}
+
+enum FlightEnd { kFlightDone = 0, kFlightAbsorbed = 1, kFlightDeferred = 2 };
+
 // Free flight in FP32 in the frame of the starting cell. Walls are hit
 // exactly (the coordinate is set to the wall), so no push-off distance is
-// needed; periodic faces map the coordinate to the opposite wall.
-__device__ __forceinline__ bool advance_mixed(const DevTables& T, DevLedger* L, BlockLedger* bl, int slot, const Frame& F, float p[3],
-                              uint32_t& w, double& occ, float remaining, uint32_t purpose, uint32_t step) {
+// needed; periodic faces map the coordinate to the opposite wall. With kDefer
+// the flight stops at a wall that needs table sampling and reports the wall
+// (plane), the time left and the event index, so that the few carriers that
+// sample a wall are finished together by k_deferred instead of stalling the
+// whole warp on the long sampling path.
+template <bool kDefer>
+__device__ __forceinline__ int advance_mixed(const DevTables& T, DevLedger* L, BlockLedger* bl, int slot,
+                                             const Frame& F, float p[3], uint32_t& w, double& occ, float& remaining,
+                                             int& event, int& plane_out, uint32_t purpose, uint32_t step) {
     const DevDomain& D = T.dom;
     const DevParams& P = T.par;
     const int mid = static_cast<int>(w >> 28);
     const DevMaterial& M = T.mat[mid];
     float v[3], iv[3];
     mode_velocity32(M, w, v, iv);
-    int event = 0;
     for (; remaining > 0.0f && event < 64; ++event) {
         float t = __int_as_float(0x7f800000);
         int plane = -1;
@@ -231,7 +275,7 @@ __device__ __forceinline__ bool advance_mixed(const DevTables& T, DevLedger* L, 
         if (plane < 0 || t > remaining) {
 #pragma unroll
             for (int a = 0; a < 3; ++a) p[a] = fmaf(v[a], remaining, p[a]);
-            return true;
+            return kFlightDone;
         }
         remaining -= t;
         const int axis = plane >> 1;
@@ -243,14 +287,14 @@ __device__ __forceinline__ bool advance_mixed(const DevTables& T, DevLedger* L, 
             if (a == axis) p[a] = hi_side ? F.hi[a] : F.lo[a];
         }
         const char cond = D.cond[plane];
-        const int ai = static_cast<int>(w & 0x00FFFFFFu);
         if (cond == 'T') {
+            const int ai = static_cast<int>(w & 0x00FFFFFFu);
             const double e = M.hw[ai] * (occ - M.nbg[ai]) * M.energy_weight;
             atomicAdd(&bl->absorbed, 1u);
             atomicAdd(&bl->absorbed_ev, e);
             const int r = D.reservoir[plane];
             if (r >= 0) atomicAdd(&bl->absorbed_res[r], 1u);
-            return false;
+            return kFlightAbsorbed;
         }
         if (cond == 'P' && D.pair[plane] >= 0) {
 #pragma unroll
@@ -258,38 +302,22 @@ __device__ __forceinline__ bool advance_mixed(const DevTables& T, DevLedger* L, 
                 if (a == axis) p[a] = hi_side ? F.lo[a] : F.hi[a];
             continue;
         }
-        const int table = D.rough_table[mid][plane];
-        if (P.conservative || (cond == 'R' && table >= 0)) {
-            if (table < 0) {
-                raise_error(L, kErrModeMapping, slot);
-                return true;
+        if (P.conservative || (cond == 'R' && D.rough_table[mid][plane] >= 0)) {
+            if (kDefer) {
+                plane_out = plane;
+                return kFlightDeferred;
             }
-            const Uniform2 d0 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose, static_cast<uint32_t>(event), 0);
-            const Uniform2 d1 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose, static_cast<uint32_t>(event), 1);
-            double n_out;
-            const int out = rough_sample_dev(T.rough[table], M, ai, occ, P.conservative != 0, d0.a, d0.b, d1.a, n_out);
-            const double vn = M.vel[3 * out + axis] * ((plane & 1) ? 1.0 : -1.0);
-            uint32_t signs = 0;
-            if (P.conservative) {
-                if (!isfinite(n_out) || !(M.omega[out] > 0.0) || !(vn < 0.0)) {
-                    raise_error(L, kErrModeMapping, slot);
-                    return true;
-                }
-            } else if (vn > 0.0) {
-                signs = 1u << axis;
-            }
-            w = static_cast<uint32_t>(out) | (signs << 24) | (static_cast<uint32_t>(mid) << 28);
-            occ = n_out;
+            if (!wall_sample_mixed(T, L, slot, plane, w, occ, event, purpose, step)) return kFlightDone;
         } else if (cond == 'R') {
             raise_error(L, kErrNoRoughTable, slot);
-            return true;
+            return kFlightDone;
         } else {
             w ^= 1u << (24 + axis);
         }
         mode_velocity32(M, w, v, iv);
     }
     if (remaining > 0.0f) raise_error(L, kErrTooManyEvents, slot);
-    return true;
+    return kFlightDone;
 }
 
 // New cell and offset after an FP32 flight in the frame of cell F.
@@ -306,45 +334,161 @@ __device__ __forceinline__ int settle_mixed(const DevDomain& D, const Frame& F, 
 }
 
 // ------------------------------------------------------ transport pass
+// Common end of a carrier's step: store the state; a live carrier takes its
+// new cell and enters the bins.
+template <bool kRta>
+__device__ __forceinline__ void finish_mixed(const DevTables& T, const CarrierState& S, const CellArrays& C,
+                                             DevLedger* L, int i, const Frame& F, float p[3], uint32_t w, double occ,
+                                             bool alive) {
+    const int c = settle_mixed(T.dom, F, p);
+    __stcs(S.ox + i, p[0]);
+    __stcs(S.oy + i, p[1]);
+    __stcs(S.oz + i, p[2]);
+    __stcs(S.mode + i, w);
+    __stcs(S.occ + i, occ);
+    if (!alive) {
+        S.alive[i] = 0;
+        return;
+    }
+    __stcs(S.cell + i, c);
+    bin_carrier(C, L, i, c, static_cast<int>(w >> 28), static_cast<int>(w & 0x00FFFFFFu), occ, kRta);
+}
+
+constexpr int kTransportThreads = 256;
+constexpr int kDeferBuffer = 64; // queued wall events per warp before a flush
+
+// The one carrier pass of a timestep: apply the pending update on load, fly,
+// bin. Mixed path: carriers that reach a wall needing table sampling are
+// queued (per-warp shared buffers, one global atomic per 32 entries) and
+// finished by k_deferred.
 template <bool kMixed, bool kRta>
-__global__ void __launch_bounds__(256) k_transport(const DevTables* __restrict__ Tp, CarrierState S, CellArrays C,
-                                                   DevLedger* L, uint32_t step) {
+__global__ void __launch_bounds__(kTransportThreads) k_transport(const DevTables* __restrict__ Tp, CarrierState S,
+                                                                 CellArrays C, DevLedger* L, uint32_t step) {
     __shared__ BlockLedger bl;
+    __shared__ int4 qbuf[kMixed ? kTransportThreads / 32 : 1][kMixed ? kDeferBuffer : 1];
     block_ledger_init(&bl);
     __syncthreads();
     const DevTables& T = *Tp;
     const int n = L->n_slots;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        if (!__ldcs(S.alive + i)) continue;
-        uint32_t w = __ldcs(S.mode + i);
-        const int c0 = __ldcs(S.cell + i);
-        double occ = apply_pending(C, c0, static_cast<int>(w & 0x00FFFFFFu), __ldcs(S.occ + i));
-        bool alive;
-        int c;
-        if (kMixed) {
-            const Frame F = cell_frame(T.dom, c0);
-            float p[3] = {__ldcs(S.ox + i), __ldcs(S.oy + i), __ldcs(S.oz + i)};
-            alive = advance_mixed(T, L, &bl, i, F, p, w, occ, T.par.dt32, kDrawTransport, step);
-            c = settle_mixed(T.dom, F, p);
-            __stcs(S.ox + i, p[0]);
-            __stcs(S.oy + i, p[1]);
-            __stcs(S.oz + i, p[2]);
-        } else {
+    if constexpr (kMixed) {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        int queued = 0; // warp-uniform
+        // block-uniform trip count so that every lane reaches the warp-wide ballot
+        for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+            const int i = base + threadIdx.x;
+            bool defer = false;
+            int4 entry;
+            if (i < n && __ldcs(S.alive + i)) {
+                uint32_t w = __ldcs(S.mode + i);
+                const int c0 = __ldcs(S.cell + i);
+                double occ = apply_pending(C, c0, static_cast<int>(w & 0x00FFFFFFu), __ldcs(S.occ + i));
+                const Frame F = cell_frame(T.dom, c0);
+                float p[3] = {__ldcs(S.ox + i), __ldcs(S.oy + i), __ldcs(S.oz + i)};
+                float remaining = T.par.dt32;
+                int event = 0, plane = -1;
+                const int end =
+                    advance_mixed<true>(T, L, &bl, i, F, p, w, occ, remaining, event, plane, kDrawTransport, step);
+                if (end == kFlightDeferred) {
+                    // state at the wall, cell unchanged (the frame of the flight)
+                    __stcs(S.ox + i, p[0]);
+                    __stcs(S.oy + i, p[1]);
+                    __stcs(S.oz + i, p[2]);
+                    __stcs(S.mode + i, w);
+                    __stcs(S.occ + i, occ);
+                    defer = true;
+                    entry = make_int4(i, __float_as_int(remaining), event, plane);
+                } else {
+                    finish_mixed<kRta>(T, S, C, L, i, F, p, w, occ, end != kFlightAbsorbed);
+                }
+            }
+            const unsigned mask = __ballot_sync(0xffffffffu, defer);
+            if (mask) {
+                if (defer) qbuf[warp][queued + __popc(mask & ((1u << lane) - 1u))] = entry;
+                queued += __popc(mask);
+                __syncwarp();
+                if (queued >= 32) {
+                    int at = 0;
+                    if (lane == 0) at = atomicAdd(&L->n_deferred, 32);
+                    at = __shfl_sync(0xffffffffu, at, 0);
+                    if (at + lane < S.capacity) S.deferred[at + lane] = qbuf[warp][lane];
+                    else raise_error(L, kErrInvalidStatistics, i);
+                    __syncwarp();
+                    const int rest = queued - 32;
+                    int4 t = make_int4(0, 0, 0, 0);
+                    if (lane < rest) t = qbuf[warp][32 + lane];
+                    __syncwarp();
+                    if (lane < rest) qbuf[warp][lane] = t;
+                    __syncwarp();
+                    queued = rest;
+                }
+            }
+        }
+        if (queued > 0) {
+            int at = 0;
+            if (lane == 0) at = atomicAdd(&L->n_deferred, queued);
+            at = __shfl_sync(0xffffffffu, at, 0);
+            if (lane < queued) {
+                if (at + lane < S.capacity) S.deferred[at + lane] = qbuf[warp][lane];
+                else raise_error(L, kErrInvalidStatistics, at + lane);
+            }
+        }
+    } else {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+            if (!__ldcs(S.alive + i)) continue;
+            uint32_t w = __ldcs(S.mode + i);
+            const int c0 = __ldcs(S.cell + i);
+            double occ = apply_pending(C, c0, static_cast<int>(w & 0x00FFFFFFu), __ldcs(S.occ + i));
             double p[3] = {__ldcs(S.x + i), __ldcs(S.y + i), __ldcs(S.z + i)};
-            alive = advance_carrier(T, L, &bl, i, p, w, occ, T.par.dt, kDrawTransport, step);
-            c = grid_index(T.dom, p[0], p[1], p[2]);
+            const bool alive = advance_carrier(T, L, &bl, i, p, w, occ, T.par.dt, kDrawTransport, step);
+            const int c = grid_index(T.dom, p[0], p[1], p[2]);
             __stcs(S.x + i, p[0]);
             __stcs(S.y + i, p[1]);
             __stcs(S.z + i, p[2]);
+            __stcs(S.mode + i, w);
+            __stcs(S.occ + i, occ);
+            if (!alive) {
+                S.alive[i] = 0;
+                continue;
+            }
+            __stcs(S.cell + i, c);
+            bin_carrier(C, L, i, c, static_cast<int>(w >> 28), static_cast<int>(w & 0x00FFFFFFu), occ, kRta);
         }
-        __stcs(S.mode + i, w);
-        __stcs(S.occ + i, occ);
-        if (!alive) {
-            S.alive[i] = 0;
+    }
+    __syncthreads();
+    block_ledger_flush(&bl, L);
+}
+
+// Wall events queued by the mixed transport pass: sample the wall with the
+// draws of the queued event index, finish the flight (further walls inline),
+// then settle and bin exactly as the transport pass would have.
+template <bool kRta>
+__global__ void __launch_bounds__(kTransportThreads) k_deferred(const DevTables* __restrict__ Tp, CarrierState S,
+                                                                CellArrays C, DevLedger* L, uint32_t step) {
+    __shared__ BlockLedger bl;
+    block_ledger_init(&bl);
+    __syncthreads();
+    const DevTables& T = *Tp;
+    const int nq = min(L->n_deferred, S.capacity);
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+        const int4 e = S.deferred[q];
+        const int i = e.x;
+        if (i < 0 || i >= S.capacity) {
+            raise_error(L, kErrInvalidStatistics, i);
             continue;
         }
-        __stcs(S.cell + i, c);
-        bin_carrier(C, L, i, c, static_cast<int>(w >> 28), static_cast<int>(w & 0x00FFFFFFu), occ, kRta);
+        float remaining = __int_as_float(e.y);
+        int event = e.z, plane = e.w;
+        uint32_t w = S.mode[i];
+        double occ = S.occ[i];
+        const Frame F = cell_frame(T.dom, S.cell[i]);
+        float p[3] = {S.ox[i], S.oy[i], S.oz[i]};
+        int end = kFlightDone;
+        if (plane >= 0 && plane < 6 && wall_sample_mixed(T, L, i, plane, w, occ, event, kDrawTransport, step)) {
+            ++event;
+            int unused = -1;
+            end = advance_mixed<false>(T, L, &bl, i, F, p, w, occ, remaining, event, unused, kDrawTransport, step);
+        }
+        finish_mixed<kRta>(T, S, C, L, i, F, p, w, occ, end != kFlightAbsorbed);
     }
     __syncthreads();
     block_ledger_flush(&bl, L);
@@ -558,8 +702,12 @@ __global__ void __launch_bounds__(256) k_inject(const DevTables* __restrict__ Tp
             const Frame F = cell_frame(T.dom, c);
             float q[3];
             for (int a = 0; a < 3; ++a) q[a] = static_cast<float>(p[a] - (T.dom.lo[a] + F.i[a] * T.dom.cell_size[a]));
-            if (remain > 1e-14)
-                alive = advance_mixed(T, L, &bl, slot, F, q, w, occ, static_cast<float>(remain), kDrawInjected, step);
+            if (remain > 1e-14) {
+                float rem = static_cast<float>(remain);
+                int event = 0, plane = -1;
+                alive = advance_mixed<false>(T, L, &bl, slot, F, q, w, occ, rem, event, plane, kDrawInjected, step) !=
+                        kFlightAbsorbed;
+            }
             c = settle_mixed(T.dom, F, q);
             S.ox[slot] = q[0];
             S.oy[slot] = q[1];
@@ -673,15 +821,21 @@ __global__ void k_reset_pending(const DevTables* __restrict__ Tp, CellArrays C, 
 }
 
 // ----------------------------------------------------------- launchers
-void launch_transport(const LaunchCtx& x, bool mixed, bool rta, uint32_t step) {
-    const dim3 g(x.grid_blocks), b(256);
+int launch_transport(const LaunchCtx& x, bool mixed, bool rta, uint32_t step) {
+    const dim3 g(x.grid_blocks), b(kTransportThreads);
     if (mixed) {
-        if (rta) k_transport<true, true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
-        else k_transport<true, false><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
-    } else {
-        if (rta) k_transport<false, true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
-        else k_transport<false, false><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
+        if (rta) {
+            k_transport<true, true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
+            k_deferred<true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
+        } else {
+            k_transport<true, false><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
+            k_deferred<false><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
+        }
+        return 2;
     }
+    if (rta) k_transport<false, true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
+    else k_transport<false, false><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
+    return 1;
 }
 
 void launch_histogram(const LaunchCtx& x, bool rta) {
