@@ -105,6 +105,9 @@ struct DevReservoir {
 struct DevDomain {
     double lo[3], hi[3], inv_cell[3], cell_size[3];
     float cell_size32[3];
+    float inv_cell32[3];
+    // c / (shape[1] shape[2]) and r / shape[2] as __umul64hi(c, magic); 0 means divisor 1
+    unsigned long long div_yz, div_z;
     int shape[3];
     int ncells;
     double tol;        // analytic-box position tolerance

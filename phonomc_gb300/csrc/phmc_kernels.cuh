@@ -13,7 +13,8 @@ __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a,
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
 
 struct LaunchCtx {
-    const DevTables* T;
+    const DevTables* T;  // device copy
+    const DevTables* Th; // host copy, passed by value to the carrier kernels
     CarrierState S;
     CellArrays C;
     DevLedger* L;

@@ -238,11 +238,30 @@ void DeviceSolver::upload_tables() {
         D.shape[a] = domain_->grid_shape()[a];
         D.cell_size[a] = (hi[a] - lo[a]) / D.shape[a];
         D.cell_size32[a] = static_cast<float>(D.cell_size[a]);
+        D.inv_cell32[a] = 1.0f / D.cell_size32[a];
         scale = std::max(scale, std::abs(hi[a] - lo[a]));
     }
     D.scale = scale;
     D.tol = std::max(1e-9, 64.0 * std::numeric_limits<double>::epsilon() * scale);
     D.ncells = ncells_;
+    {
+        // multiply-high division constants, checked for every cell index
+        auto magic = [](int d) -> unsigned long long {
+            if (d <= 1) return 0ull;
+            return static_cast<unsigned long long>((static_cast<unsigned __int128>(1) << 64) / d) + 1ull;
+        };
+        const int dyz = D.shape[1] * D.shape[2], dz = D.shape[2];
+        D.div_yz = magic(dyz);
+        D.div_z = magic(dz);
+        auto q = [](long long n, unsigned long long m) -> long long {
+            return m ? static_cast<long long>((static_cast<unsigned __int128>(n) * m) >> 64) : n;
+        };
+        for (long long c = 0; c < ncells_; ++c) {
+            const long long r = c % dyz;
+            if (q(c, D.div_yz) != c / dyz || q(r, D.div_z) != r / dz)
+                throw std::runtime_error("cell index division constants failed their check");
+        }
+    }
     for (int f = 0; f < 6; ++f) {
         const Facet& F = domain_->facets()[f];
         D.cond[f] = F.condition;
@@ -369,6 +388,7 @@ void DeviceSolver::upload_tables() {
 LaunchCtx DeviceSolver::ctx() const {
     LaunchCtx x;
     x.T = d_tables_;
+    x.Th = &tables_;
     x.S = state_;
     x.C = cells_;
     x.L = d_ledger_;

@@ -176,12 +176,16 @@ struct Frame {
     float lo[3], hi[3]; // box walls in the frame of the starting cell
 };
 
+// Exact quotient of n < 2^31 by d through the host-verified multiplier floor(2^64/d)+1.
+__device__ __forceinline__ int magic_div(int n, unsigned long long magic) {
+    return magic ? static_cast<int>(__umul64hi(static_cast<unsigned long long>(n), magic)) : n;
+}
+
 __device__ __forceinline__ Frame cell_frame(const DevDomain& D, int cell) {
     Frame F;
-    const int nyz = D.shape[1] * D.shape[2];
-    F.i[0] = cell / nyz;
-    const int r = cell - F.i[0] * nyz;
-    F.i[1] = r / D.shape[2];
+    F.i[0] = magic_div(cell, D.div_yz);
+    const int r = cell - F.i[0] * (D.shape[1] * D.shape[2]);
+    F.i[1] = magic_div(r, D.div_z);
     F.i[2] = r - F.i[1] * D.shape[2];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -325,7 +329,7 @@ __device__ __forceinline__ int settle_mixed(const DevDomain& D, const Frame& F, 
     int j[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        int k = F.i[a] + static_cast<int>(floorf(p[a] / F.cs[a]));
+        int k = F.i[a] + static_cast<int>(floorf(p[a] * D.inv_cell32[a]));
         k = k < 0 ? 0 : (k >= D.shape[a] ? D.shape[a] - 1 : k);
         p[a] -= static_cast<float>(k - F.i[a]) * F.cs[a];
         j[a] = k;
@@ -362,13 +366,12 @@ constexpr int kDeferBuffer = 64; // queued wall events per warp before a flush
 // queued (per-warp shared buffers, one global atomic per 32 entries) and
 // finished by k_deferred.
 template <bool kMixed, bool kRta>
-__global__ void __launch_bounds__(kTransportThreads) k_transport(const DevTables* __restrict__ Tp, CarrierState S,
+__global__ void __launch_bounds__(kTransportThreads) k_transport(const __grid_constant__ DevTables T, CarrierState S,
                                                                  CellArrays C, DevLedger* L, uint32_t step) {
     __shared__ BlockLedger bl;
     __shared__ int4 qbuf[kMixed ? kTransportThreads / 32 : 1][kMixed ? kDeferBuffer : 1];
     block_ledger_init(&bl);
     __syncthreads();
-    const DevTables& T = *Tp;
     const int n = L->n_slots;
     if constexpr (kMixed) {
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -462,12 +465,11 @@ __global__ void __launch_bounds__(kTransportThreads) k_transport(const DevTables
 // draws of the queued event index, finish the flight (further walls inline),
 // then settle and bin exactly as the transport pass would have.
 template <bool kRta>
-__global__ void __launch_bounds__(kTransportThreads) k_deferred(const DevTables* __restrict__ Tp, CarrierState S,
+__global__ void __launch_bounds__(kTransportThreads) k_deferred(const __grid_constant__ DevTables T, CarrierState S,
                                                                 CellArrays C, DevLedger* L, uint32_t step) {
     __shared__ BlockLedger bl;
     block_ledger_init(&bl);
     __syncthreads();
-    const DevTables& T = *Tp;
     const int nq = min(L->n_deferred, S.capacity);
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
         const int4 e = S.deferred[q];
@@ -825,16 +827,16 @@ int launch_transport(const LaunchCtx& x, bool mixed, bool rta, uint32_t step) {
     const dim3 g(x.grid_blocks), b(kTransportThreads);
     if (mixed) {
         if (rta) {
-            k_transport<true, true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
-            k_deferred<true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
+            k_transport<true, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L, step);
+            k_deferred<true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L, step);
         } else {
-            k_transport<true, false><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
-            k_deferred<false><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
+            k_transport<true, false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L, step);
+            k_deferred<false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L, step);
         }
         return 2;
     }
-    if (rta) k_transport<false, true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
-    else k_transport<false, false><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, step);
+    if (rta) k_transport<false, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L, step);
+    else k_transport<false, false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L, step);
     return 1;
 }
 
