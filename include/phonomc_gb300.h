@@ -133,8 +133,11 @@ int phmc_solver_get_carriers(phmc_solver* s, double* x, double* y, double* z, do
 /* Replace the carrier population (same SoA layout; mode_word = active | signs<<24 | material<<28). */
 int phmc_solver_set_carriers(phmc_solver* s, int64_t n, const double* x, const double* y, const double* z,
                              const double* occupation, const uint32_t* mode_word, const uint8_t* alive);
-/* End-to-end stepping from host memory: uploads carriers from host buffers,
- * runs `steps` timesteps and reads the cell temperatures back. */
+/* End-to-end stepping from host memory: replaces the carrier population with
+ * the host arrays (all alive), advances `steps` timesteps from the solver's
+ * current time (step counter, elapsed time and ledger totals continue) and
+ * reads the cell temperatures back. Registered host arrays
+ * (phmc_host_register) are read by the device directly over the host link. */
 int phmc_solver_run_from_host(phmc_solver* s, int64_t n, const double* x, const double* y, const double* z,
                               const double* occupation, const uint32_t* mode_word, int steps,
                               double* cell_temperature_out);

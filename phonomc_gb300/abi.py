@@ -262,10 +262,11 @@ class Solver(Handle):
         n = int(c["x"].size)
         arrs = [np.ascontiguousarray(c[k], dtype=np.float64) for k in ("x", "y", "z", "occ")]
         mode = np.ascontiguousarray(c["mode"], dtype=np.uint32)
-        alive = np.ascontiguousarray(c.get("alive", np.ones(n, np.uint8)), dtype=np.uint8)
+        alive = c.get("alive", np.ones(n, np.uint8))
+        alive = None if alive is None else np.ascontiguousarray(alive, dtype=np.uint8)
         self.check(self.fn("solver_set_carriers")(self.h, n, *[dptr(a) for a in arrs],
                                                   mode.ctypes.data_as(c_uint32_p),
-                                                  alive.ctypes.data_as(c_uint8_p)))
+                                                  None if alive is None else alive.ctypes.data_as(c_uint8_p)))
 
     def close(self):
         if getattr(self, "h", None):

@@ -205,7 +205,7 @@ int phmc_solver_set_carriers(phmc_solver* s, int64_t n, const double* x, const d
 int phmc_solver_run_from_host(phmc_solver* s, int64_t n, const double* x, const double* y, const double* z,
                               const double* occ, const uint32_t* mode, int steps, double* cell_T) {
     return guard([&] {
-        s->s->set_carriers(n, x, y, z, occ, mode, nullptr);
+        s->s->set_carriers(n, x, y, z, occ, mode, nullptr, true);
         s->s->run(steps);
         s->s->read_cells(cell_T, nullptr, nullptr);
     });

@@ -25,6 +25,14 @@ struct LaunchCtx {
 int launch_transport(const LaunchCtx& x, bool mixed, bool rta, uint32_t step);
 void launch_histogram(const LaunchCtx& x, bool rta);
 void launch_init_cells(const LaunchCtx& x, bool mixed);
+// Carriers read straight from device-accessible (registered) host arrays.
+struct HostCarriers {
+    const double *x, *y, *z, *occ;
+    const uint32_t* mode;
+    const uint8_t* alive; // null: all alive
+};
+void launch_ingest(const LaunchCtx& x, bool mixed, const HostCarriers& h);
+void launch_ledger_replace(const LaunchCtx& x, int n);
 void launch_positions_out(const LaunchCtx& x);
 int launch_inject(const LaunchCtx& x, bool mixed, bool rta, int* holes, int* block_dead, int capacity, uint32_t step);
 void launch_containment(const LaunchCtx& x, bool mixed);

@@ -409,27 +409,56 @@ void DeviceSolver::initial_statistics() {
     materialized_ = true;
 }
 
+// Device address of registered (pinned or mapped) host memory, or null.
+static const void* mapped_host(const void* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 void DeviceSolver::set_carriers(long long n, const double* x, const double* y, const double* z, const double* occ,
-                                const uint32_t* mode, const uint8_t* alive) {
+                                const uint32_t* mode, const uint8_t* alive, bool keep_clock) {
     if (n < 0 || n > state_.capacity) throw std::invalid_argument("carrier count exceeds device capacity");
-    PHMC_CUDA(cudaMemcpyAsync(state_.x, x, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
-    PHMC_CUDA(cudaMemcpyAsync(state_.y, y, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
-    PHMC_CUDA(cudaMemcpyAsync(state_.z, z, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
-    PHMC_CUDA(cudaMemcpyAsync(state_.occ, occ, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
-    PHMC_CUDA(cudaMemcpyAsync(state_.mode, mode, n * sizeof(uint32_t), cudaMemcpyHostToDevice, stream_));
-    if (alive) PHMC_CUDA(cudaMemcpyAsync(state_.alive, alive, n * sizeof(uint8_t), cudaMemcpyHostToDevice, stream_));
-    else PHMC_CUDA(cudaMemsetAsync(state_.alive, 1, n * sizeof(uint8_t), stream_));
-    DevLedger L{};
-    L.n_slots = static_cast<int>(n);
-    for (size_t r = 0; r < P_.reservoirs.size(); ++r) L.previous_res[r] = P_.reservoirs[r].initial_count;
-    PHMC_CUDA(cudaMemcpyAsync(d_ledger_, &L, sizeof L, cudaMemcpyHostToDevice, stream_));
-    step_ = 0;
-    elapsed_ = 0;
+    const LaunchCtx c = ctx();
+    if (keep_clock) {
+        launch_ledger_replace(c, static_cast<int>(n));
+        counters_.launches += 1;
+    } else {
+        DevLedger L{};
+        L.n_slots = static_cast<int>(n);
+        for (size_t r = 0; r < P_.reservoirs.size(); ++r) L.previous_res[r] = P_.reservoirs[r].initial_count;
+        PHMC_CUDA(cudaMemcpyAsync(d_ledger_, &L, sizeof L, cudaMemcpyHostToDevice, stream_));
+        step_ = 0;
+        elapsed_ = 0;
+    }
     failed_ = false;
-    launch_init_cells(ctx(), mixed_);
+    HostCarriers h{};
+    h.x = static_cast<const double*>(mapped_host(x));
+    h.y = static_cast<const double*>(mapped_host(y));
+    h.z = static_cast<const double*>(mapped_host(z));
+    h.occ = static_cast<const double*>(mapped_host(occ));
+    h.mode = static_cast<const uint32_t*>(mapped_host(mode));
+    h.alive = static_cast<const uint8_t*>(mapped_host(alive));
+    if (h.x && h.y && h.z && h.occ && h.mode && (h.alive || !alive)) {
+        // registered host arrays: one kernel reads them over the link
+        launch_ingest(c, mixed_, h);
+    } else {
+        PHMC_CUDA(cudaMemcpyAsync(state_.x, x, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+        PHMC_CUDA(cudaMemcpyAsync(state_.y, y, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+        PHMC_CUDA(cudaMemcpyAsync(state_.z, z, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+        PHMC_CUDA(cudaMemcpyAsync(state_.occ, occ, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+        PHMC_CUDA(cudaMemcpyAsync(state_.mode, mode, n * sizeof(uint32_t), cudaMemcpyHostToDevice, stream_));
+        if (alive) PHMC_CUDA(cudaMemcpyAsync(state_.alive, alive, n * sizeof(uint8_t), cudaMemcpyHostToDevice, stream_));
+        else PHMC_CUDA(cudaMemsetAsync(state_.alive, 1, n * sizeof(uint8_t), stream_));
+        launch_init_cells(c, mixed_);
+    }
     counters_.launches += 1;
     initial_statistics();
-    synchronize();
+    if (!keep_clock) synchronize();
 }
 
 void DeviceSolver::run_timestep() {

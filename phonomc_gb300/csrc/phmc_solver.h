@@ -120,7 +120,8 @@ public:
     long long slot_count();
     void get_carriers(double* x, double* y, double* z, double* occ, uint32_t* mode, int32_t* cell, uint8_t* alive);
     void set_carriers(long long n, const double* x, const double* y, const double* z, const double* occ,
-                      const uint32_t* mode, const uint8_t* alive);
+                      const uint32_t* mode, const uint8_t* alive,
+                      bool keep_clock = false);
     void write_outputs();
     bool mixed() const { return mixed_; }
     // Deterministic sub-steps on the current population (parity entry points):

@@ -528,6 +528,49 @@ __global__ void k_init_cells(const DevTables* __restrict__ Tp, CarrierState S, D
     if ((threadIdx.x & 31) == 0 && live) atomicAdd(reinterpret_cast<unsigned long long*>(&L->particle_count), live);
 }
 
+// Carriers straight from registered host memory (one pass over the link, no
+// device staging): cell, FP32 offsets or FP64 positions, occupation, mode, alive.
+template <bool kMixed>
+__global__ void k_ingest(const __grid_constant__ DevTables T, CarrierState S, DevLedger* L, HostCarriers H) {
+    const DevDomain& D = T.dom;
+    const int n = L->n_slots;
+    unsigned long long live = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double x = H.x[i], y = H.y[i], z = H.z[i];
+        const int c = grid_index(D, x, y, z);
+        S.cell[i] = c;
+        if (kMixed) {
+            const Frame F = cell_frame(D, c);
+            S.ox[i] = static_cast<float>(x - (D.lo[0] + F.i[0] * D.cell_size[0]));
+            S.oy[i] = static_cast<float>(y - (D.lo[1] + F.i[1] * D.cell_size[1]));
+            S.oz[i] = static_cast<float>(z - (D.lo[2] + F.i[2] * D.cell_size[2]));
+        } else {
+            S.x[i] = x;
+            S.y[i] = y;
+            S.z[i] = z;
+        }
+        S.occ[i] = H.occ[i];
+        S.mode[i] = H.mode[i];
+        const uint8_t a = H.alive ? H.alive[i] : uint8_t(1);
+        S.alive[i] = a;
+        live += a ? 1 : 0;
+    }
+    for (int o = 16; o > 0; o >>= 1) live += __shfl_xor_sync(0xffffffffu, live, o);
+    if ((threadIdx.x & 31) == 0 && live) atomicAdd(reinterpret_cast<unsigned long long*>(&L->particle_count), live);
+}
+
+// A replaced population continuing the run: new slot range and live count;
+// totals, the clock and the previous reservoir counts stay.
+__global__ void k_ledger_replace(DevLedger* L, int n) {
+    L->n_slots = n;
+    L->n_holes = 0;
+    L->n_inject = 0;
+    L->n_deferred = 0;
+    L->particle_count = 0;
+    L->error_code = 0;
+    L->error_slot = 0;
+}
+
 // Absolute FP64 positions of the mixed state into the staging arrays.
 __global__ void k_positions_out(const DevTables* __restrict__ Tp, CarrierState S, const DevLedger* L) {
     const DevDomain& D = Tp->dom;
@@ -849,6 +892,13 @@ void launch_init_cells(const LaunchCtx& x, bool mixed) {
     if (mixed) k_init_cells<true><<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.L);
     else k_init_cells<false><<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.L);
 }
+
+void launch_ingest(const LaunchCtx& x, bool mixed, const HostCarriers& h) {
+    if (mixed) k_ingest<true><<<x.grid_blocks, 256, 0, x.stream>>>(*x.Th, x.S, x.L, h);
+    else k_ingest<false><<<x.grid_blocks, 256, 0, x.stream>>>(*x.Th, x.S, x.L, h);
+}
+
+void launch_ledger_replace(const LaunchCtx& x, int n) { k_ledger_replace<<<1, 1, 0, x.stream>>>(x.L, n); }
 
 void launch_positions_out(const LaunchCtx& x) {
     k_positions_out<<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.L);

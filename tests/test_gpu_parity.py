@@ -278,3 +278,36 @@ def test_mixed_callaway_conserves_energy_and_tracks_plain(gpu):
     Tp, _, _ = sp.cells()
     Tm, _, _ = sm.cells()
     assert np.max(np.abs(Tp - Tm)) < 1e-3
+
+
+# ------------------------------------------------------------ host ingest
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_registered_host_ingest_matches_copy_path(gpu, precision):
+    """Carriers read by the device straight from registered host arrays give
+    the same state and the same steps as the staged copy path."""
+    mat = synthetic.make_material(mesh=16)
+    cfg = workloads.scaled(workloads.inplane_gradient(), 30000, random_seed=5, precision=precision)
+    m = abi.Material(gpu, "phmc_", mat, 0.1, True, False)
+    src = abi.Solver(gpu, "phmc_", cfg, [m])
+    src.run(2)
+    c = src.carriers()
+    live = c["alive"] == 1
+    host = {k: np.ascontiguousarray(c[k][live]) for k in ("x", "y", "z", "occ", "mode")}
+    a = abi.Solver(gpu, "phmc_", cfg, [m])
+    b = abi.Solver(gpu, "phmc_", cfg, [m])
+    a.set_carriers(dict(host, alive=np.ones(host["x"].size, np.uint8)))
+    for arr in host.values():
+        assert gpu.phmc_host_register(arr.ctypes.data, arr.nbytes) == 0
+    try:
+        b.set_carriers(dict(host, alive=None))
+    finally:
+        for arr in host.values():
+            gpu.phmc_host_unregister(arr.ctypes.data)
+    for s in (a, b):
+        s.run(2)
+    ca, cb = a.carriers(), b.carriers()
+    for k in ("alive", "mode", "cell", "x", "y", "z"):
+        assert np.array_equal(ca[k], cb[k]), k
+    # bin sums are FP64 atomics in arrival order: collisions agree to round-off
+    assert np.allclose(ca["occ"], cb["occ"], rtol=1e-12, atol=1e-15)
+    assert np.allclose(a.cells()[0], b.cells()[0], rtol=1e-12, atol=0)
