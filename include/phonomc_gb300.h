@@ -155,6 +155,21 @@ void phmc_solver_destroy(phmc_solver* s);
 /* Box ray trace for n rays; returns hit point, time and facet (-1 on miss). */
 int phmc_dev_trace_box(const double lo[3], const double hi[3], int64_t n, const double* p3, const double* v3,
                        double* hit3, double* t, int32_t* facet);
+/* No counterpart in the reference: phmc_dev_trace_box without any device
+ * allocation, for callers that cannot allocate device memory at call time (a
+ * process whose device memory is held by another allocator or pool, or a
+ * caller that must not hit the device-wide synchronization of cudaFree while
+ * a solver steps on another stream). Rays are staged in one static device
+ * block of PHMC_NOALLOC_MAX_RAYS rays: larger n returns 1 before any device
+ * work. Calls on one device share that block and are serialized by a
+ * process-wide lock. The first call per device resolves the block's address
+ * and creates a non-blocking stream (n = 0 performs only this setup); make it
+ * before any phase in which the device must not allocate, such as a stream
+ * capture. `misses` (may be null) receives the number of rays without a
+ * facet. */
+#define PHMC_NOALLOC_MAX_RAYS 65536
+int phmc_dev_trace_box_noalloc(const double lo[3], const double hi[3], int64_t n, const double* p3, const double* v3,
+                               double* hit3, double* t, int32_t* facet, int64_t* misses);
 /* Piecewise-linear E -> T inversion on a material's lookup table. */
 int phmc_dev_temperature_from_energy(const phmc_material* m, int64_t n, const double* energy, double* temperature);
 /* Energy-conserving RTA on carriers grouped by cell (flat modes, one material). */

@@ -318,4 +318,6 @@ DEVICE_PROTOS = {
     "solver_run_from_host": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_double_p, c_double_p, c_double_p,
                                        c_uint32_p, C.c_int, c_double_p]),
     **{"dev_" + k: v for k, v in SUBSTEP_PROTOS.items()},
+    "dev_trace_box_noalloc": (C.c_int, [c_double_p, c_double_p, C.c_int64, c_double_p, c_double_p, c_double_p,
+                                        c_double_p, c_int32_p, c_int64_p]),
 }

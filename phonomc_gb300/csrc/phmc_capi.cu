@@ -359,3 +359,18 @@ int phmc_dev_rough_reflect(const phmc_material* m, int conservative, double Tref
 }
 
 } // extern "C"
+
+// ------------------------------------------------------ no-allocation variant
+namespace phmc {
+void trace_box_noalloc(const double lo[3], const double hi[3], long long n, const double* p3, const double* v3,
+                       double* hit3, double* t, int32_t* facet, long long* misses);
+}
+
+int phmc_dev_trace_box_noalloc(const double lo[3], const double hi[3], int64_t n, const double* p3, const double* v3,
+                               double* hit3, double* t, int32_t* facet, int64_t* misses) {
+    return guard([&] {
+        long long m = 0;
+        phmc::trace_box_noalloc(lo, hi, n, p3, v3, hit3, t, facet, &m);
+        if (misses) *misses = m;
+    });
+}
