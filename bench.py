@@ -55,6 +55,24 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
+def profiled_traffic(workload, precision, particles):
+    """DRAM bytes (read + write) of one carrier pass from the committed ncu
+    summary of that workload, or None when no capture matches its size."""
+    path = os.path.join(ROOT, "profiles", f"k_transport_{workload}_{precision}.md")
+    try:
+        text = open(path).read()
+    except OSError:
+        return None
+    vals = {}
+    for line in text.splitlines():
+        if "=" in line and line.split("=")[0].strip() in ("pass_traffic_bytes", "carriers"):
+            k, v = line.split("=", 1)
+            vals[k.strip()] = float(v)
+    if "pass_traffic_bytes" not in vals or int(vals.get("carriers", -1)) != int(particles):
+        return None
+    return vals["pass_traffic_bytes"]
+
+
 class ClockSampler:
     """SM clock and clock-event reasons sampled DURING the timed region.
 
@@ -281,9 +299,12 @@ def run_ours(args):
                    "material": "synthetic 16^3 x 6 modes (seed 0)", "cells": int(Tout.size),
                    "l2": "carrier state larger than L2 (no flush needed)", "replicas": world},
         "gpu_launches": main_arm["launches"],
-        "roofline": {"bound": "hbm", "kernel": "k_transport (the one carrier pass of a step)", "achieved": achieved,
+        "roofline": {"bound": "hbm", "kernel": "k_transport + k_deferred (the one carrier pass of a step)", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                     "bytes_per_carrier": bpc, "kernel_ms_per_launch": kavg, "traffic": None},
+                     "bytes_per_carrier": bpc, "kernel_ms_per_launch": kavg,
+                     "traffic": profiled_traffic(args.workload, args.precision, args.particles),
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one carrier pass "
+                                       "(profiles/k_transport_<workload>_<precision>.md)"},
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": int(n * (4 * 8 + 4)), "d2h_bytes_per_step": int(Tout.size * 8)},
         "clocks": main_arm["clocks"],
