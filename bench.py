@@ -7,7 +7,7 @@ MonteCarloSolver timestep over every carrier. Carrier state (>= 2 GB) is far
 larger than the 129 MB L2, so timed steps do not run from cache.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                  [--workload inplane_gradient|cross_plane_film] [--particles P]
+                  [--workload inplane_gradient|cross_plane_film|bilayer_callaway] [--particles P]
                   [--precision fp64|mixed]
 
 Prints one JSON line. `--impl reference` times the CPU restatement of the
@@ -43,6 +43,14 @@ def workload_config(name, particles, precision, seed=12345):
     from phonomc_gb300 import workloads
     base = getattr(workloads, name)()
     return workloads.scaled(base, particles, random_seed=seed, precision=precision)
+
+
+def workload_materials(name):
+    """(material tables, include stationary modes, complete the Callaway BZ) per material."""
+    from phonomc_gb300 import synthetic, workloads
+    if name == "bilayer_callaway":
+        return [(d, True, True) for d in workloads.bilayer_materials(16)]
+    return [(synthetic.make_material(mesh=16), name == "inplane_gradient", False)]
 
 
 def measured_peak():
@@ -175,12 +183,11 @@ def _oracle_replica(args):
     steps, then `samples` timed windows of `steps` timesteps each."""
     name, particles, steps, samples, warmup, seed = args
     import oracle
-    from phonomc_gb300 import abi, synthetic
+    from phonomc_gb300 import abi
     lib = oracle.load()
     cfg = workload_config(name, particles, "fp64", seed)
-    stationary = name == "inplane_gradient"
-    m = abi.Material(lib, "orc_", synthetic.make_material(mesh=16), 0.1, stationary, False)
-    s = abi.Solver(lib, "orc_", cfg, [m])
+    m = [abi.Material(lib, "orc_", d, 0.1, st, bz) for d, st, bz in workload_materials(name)]
+    s = abi.Solver(lib, "orc_", cfg, m)
     s.run(max(1, warmup))
     cs, dt = 0, 0.0
     for _ in range(samples):
@@ -222,9 +229,9 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-def _time_arm(lib, abi, cfg, material, steps, warmup, stationary):
-    m = abi.Material(lib, "phmc_", material, 0.1, stationary, False)
-    s = abi.Solver(lib, "phmc_", cfg, [m])
+def _time_arm(lib, abi, cfg, materials, steps, warmup):
+    m = [abi.Material(lib, "phmc_", d, 0.1, st, bz) for d, st, bz in materials]
+    s = abi.Solver(lib, "phmc_", cfg, m)
     s.run(warmup)
     n0 = s.stats()["particle_count"]
     tot, kern, launches = C.c_double(), C.c_double(), C.c_int64()
@@ -239,18 +246,17 @@ def run_ours(args):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
     import phonomc_gb300
-    from phonomc_gb300 import abi, synthetic
+    from phonomc_gb300 import abi
     lib = phonomc_gb300.lib()
-    material = synthetic.make_material(mesh=16)
-    stationary = args.workload == "inplane_gradient"
+    materials = workload_materials(args.workload)
     seed = 12345 + rank
     # headline: the requested precision (mixed by default); comparison arm: plain FP64
-    main_arm = _time_arm(lib, abi, workload_config(args.workload, args.particles, args.precision, seed), material,
-                         args.steps, args.warmup, stationary)
+    main_arm = _time_arm(lib, abi, workload_config(args.workload, args.particles, args.precision, seed), materials,
+                         args.steps, args.warmup)
     plain = None
     if args.precision == "mixed" and not args.no_plain:
-        plain = _time_arm(lib, abi, workload_config(args.workload, args.particles, "fp64", seed), material,
-                          max(3, args.steps // 4), args.warmup, stationary)
+        plain = _time_arm(lib, abi, workload_config(args.workload, args.particles, "fp64", seed), materials,
+                          max(3, args.steps // 4), args.warmup)
         plain["solver"].close()
     ms, carrier_steps = main_arm["ms"], main_arm["carrier_steps"]
     if world > 1:
@@ -296,7 +302,9 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
         "config": {"workload": args.workload, "particles": int(args.particles), "precision": args.precision,
-                   "material": "synthetic 16^3 x 6 modes (seed 0)", "cells": int(Tout.size),
+                   "material": ("two synthetic 16^3 x 6 tables, second 0.7x frequency 0.75x velocity, Callaway BZ "
+                                "completed" if args.workload == "bilayer_callaway"
+                                else "synthetic 16^3 x 6 modes (seed 0)"), "cells": int(Tout.size),
                    "l2": "carrier state larger than L2 (no flush needed)", "replicas": world},
         "gpu_launches": main_arm["launches"],
         "roofline": {"bound": "hbm", "kernel": "k_transport + k_deferred (the one carrier pass of a step)", "achieved": achieved,
@@ -330,7 +338,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="inplane_gradient", choices=["inplane_gradient", "cross_plane_film"])
+    ap.add_argument("--workload", default="inplane_gradient",
+                    choices=["inplane_gradient", "cross_plane_film", "bilayer_callaway"])
     ap.add_argument("--particles", type=float, default=None)
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison arm")

@@ -170,6 +170,16 @@ int phmc_dev_trace_box(const double lo[3], const double hi[3], int64_t n, const 
 #define PHMC_NOALLOC_MAX_RAYS 65536
 int phmc_dev_trace_box_noalloc(const double lo[3], const double hi[3], int64_t n, const double* p3, const double* v3,
                                double* hit3, double* t, int32_t* facet, int64_t* misses);
+/* Diffuse-mismatch interface events between material a (0) and b (1) with
+ * explicit energy weights and uniforms u[3*i..3*i+2]; the interface is normal to
+ * `axis`, each event goes from src[i] to the other material. Replaces
+ * InterfaceInteraction::interact (src/solver/InterfaceInteraction.cpp:46-153).
+ * action: 3 reflect, 4 transmit, 5 invalid outgoing mode (linearized). */
+int phmc_dev_interface(const phmc_material* a, const phmc_material* b, double weight_a, double weight_b, int axis,
+                       double frequency_bin_thz, double reference_temperature, int linearized, int64_t n,
+                       const int32_t* src, const int32_t* flat_in, const int32_t* signs_in, const double* occ_in,
+                       const double* u3, int32_t* action, int32_t* material_out, int32_t* flat_out,
+                       int32_t* signs_out, double* occ_out);
 /* Piecewise-linear E -> T inversion on a material's lookup table. */
 int phmc_dev_temperature_from_energy(const phmc_material* m, int64_t n, const double* energy, double* temperature);
 /* Energy-conserving RTA on carriers grouped by cell (flat modes, one material). */

@@ -284,6 +284,109 @@ double rta_cell(const std::vector<int>& members, const std::vector<double>& omeg
     return (ea - eb) * cell_weight;
 }
 
+// ------------------------------------------------------ interfaces
+// src/solver/InterfaceModeSampler.cpp:69-108: flux-weighted draw inside the
+// shared band [floor(w/width) width, +width) of one bank; `drew` tells whether
+// the reference consumed a uniform (it does only for a positive band flux).
+int interface_sample_band(const InterfaceBank& B, double omega, double width, double u, bool& drew,
+                          double& flux_sum) {
+    if (!std::isfinite(omega) || omega < 0 || !std::isfinite(width) || width <= 0)
+        throw std::invalid_argument("Invalid shared interface frequency band.");
+    const double bin = std::floor(omega / width);
+    const double lo = bin * width, hi = (bin + 1) * width;
+    const size_t begin = static_cast<size_t>(std::lower_bound(B.omega.begin(), B.omega.end(), lo) - B.omega.begin());
+    const size_t end = static_cast<size_t>(std::lower_bound(B.omega.begin(), B.omega.end(), hi) - B.omega.begin());
+    flux_sum = end > begin ? B.prefix[end] - B.prefix[begin] : 0.0;
+    drew = false;
+    if (!(flux_sum > 0.0)) return -1;
+    drew = true;
+    const double target = B.prefix[begin] + (u * (flux_sum - 0.0) + 0.0);
+    size_t pos = static_cast<size_t>(std::upper_bound(B.prefix.begin() + static_cast<std::ptrdiff_t>(begin + 1),
+                                                      B.prefix.begin() + static_cast<std::ptrdiff_t>(end + 1), target) -
+                                     B.prefix.begin());
+    pos = std::clamp(pos, begin + 1, end) - 1;
+    return B.active[pos];
+}
+
+struct InterfaceOutcome {
+    int action = 0;          // kInterfaceReflect, kInterfaceTransmit or kInterfaceFail
+    int material = 0, active = 0;
+    uint32_t signs = 0;
+    double occ = 0;
+    int events = 0, transmitted = 0, reflected = 0;
+};
+
+// src/solver/InterfaceInteraction.cpp:46-153, diffuse mismatch: reflected draw,
+// transmitted draw, transmission test, occupation remap conserving w ω Δn.
+// Uniforms are consumed in the reference's order from u[0..2].
+InterfaceOutcome interface_interact(const InterfaceTables& I, const std::vector<MaterialTables>& mats, int src, int a,
+                                    uint32_t signs, double occ, int next, const double u[3]) {
+    InterfaceOutcome r;
+    r.material = src;
+    r.active = a;
+    r.signs = signs;
+    r.occ = occ;
+    const MaterialTables& S = mats[src];
+    const int axis = I.axis;
+    const double omega = S.omega[a];
+    const double v_axis = ((signs >> axis) & 1u) ? -S.vel[3 * a + axis] : S.vel[3 * a + axis];
+    const int incident = v_axis > 0.0 ? 1 : 0;
+    int k = 0;
+    bool drew;
+    double source_flux = 0, target_flux = 0;
+    const int reflected = interface_sample_band(I.banks[src][1 - incident], omega, I.band_width, u[k], drew, source_flux);
+    if (drew) ++k;
+    const int transmitted = interface_sample_band(I.banks[next][incident], omega, I.band_width, u[k], drew, target_flux);
+    if (drew) ++k;
+    const double transmission = target_flux > 0 ? target_flux / std::max(1e-300, source_flux + target_flux) : 0;
+    const bool transmit = transmitted >= 0 && u[k] < transmission;
+    const int sel_material = transmit ? next : src;
+    const int sel = transmit ? transmitted : reflected;
+    r.events = 1;
+    if (sel < 0) {
+        if (I.linearized) {
+            r.action = kInterfaceFail;
+            return r;
+        }
+        r.signs ^= 1u << axis;
+        r.reflected = 1;
+        r.action = kInterfaceReflect;
+        return r;
+    }
+    const MaterialTables& D = mats[sel_material];
+    const double new_omega = D.omega[sel];
+    const double old_deviation = occ - S.nbg[a];
+    const double physical = S.energy_weight * omega * old_deviation;
+    const double new_deviation = physical / std::max(1e-300, D.energy_weight * new_omega);
+    const double new_occ = D.nbg[sel] + new_deviation;
+    if (I.linearized) {
+        const double nv = D.vel[3 * sel + axis];
+        const int expected = transmit ? incident : 1 - incident;
+        if (!std::isfinite(new_occ) || !std::isfinite(nv) || (expected ? !(nv > 0.0) : !(nv < 0.0))) {
+            r.action = kInterfaceFail;
+            return r;
+        }
+    }
+    if (!std::isfinite(new_occ) || (!I.linearized && new_occ < 0.0)) {
+        r.signs ^= 1u << axis;
+        r.reflected = 1;
+        r.action = kInterfaceReflect;
+        return r;
+    }
+    r.material = sel_material;
+    r.active = sel;
+    r.signs = 0;
+    r.occ = new_occ;
+    if (transmit) {
+        r.transmitted = 1;
+        r.action = kInterfaceTransmit;
+    } else {
+        r.reflected = 1;
+        r.action = kInterfaceReflect;
+    }
+    return r;
+}
+
 // ---------------------------------------------- linearized collision per cell
 // src/solver/CarrierCollisionOperator.cpp:67-126 for one cell.
 long double linear_cell(const std::vector<int>& members, const MaterialTables& T, const std::vector<int>& active_i,
@@ -336,6 +439,7 @@ struct OracleSolver {
     int step = 0;
     double elapsed = 0;
     double avg_flux = 0, kappa_fit = 0, kappa_end = 0;
+    long long iface_events = 0, iface_transmitted = 0, iface_reflected = 0;
     bool failed = false;
 
     Vec3 velocity(uint32_t w) const {
@@ -459,6 +563,53 @@ struct OracleSolver {
         return true;
     }
 
+    // src/solver/LayeredMaterialLayout.cpp:31-60
+    double next_crossing(const Vec3& p, const Vec3& v, int current, int& destination) const {
+        destination = -1;
+        const int count = static_cast<int>(P.mats.size());
+        if (count <= 1) return std::numeric_limits<double>::infinity();
+        const int ax = P.layout.axis;
+        const double velocity_axis = v[ax];
+        if (std::abs(velocity_axis) <= 1e-18) return std::numeric_limits<double>::infinity();
+        double plane;
+        int dest;
+        if (velocity_axis > 0.0 && current + 1 < count) {
+            plane = P.layout.planes[current];
+            dest = current + 1;
+        } else if (velocity_axis < 0.0 && current > 0) {
+            plane = P.layout.planes[current - 1];
+            dest = current - 1;
+        } else {
+            return std::numeric_limits<double>::infinity();
+        }
+        const double time = (plane - p[ax]) / velocity_axis;
+        if (!std::isfinite(time) || time <= 1e-14) return std::numeric_limits<double>::infinity();
+        destination = dest;
+        return time;
+    }
+
+    // src/solver/TransportOperator.cpp:468-497
+    void material_interface(int i, int destination, uint32_t purpose, int event) {
+        const uint32_t w = mode[i];
+        const Uniform2 d0 = uniform2(P.cfg.random_seed, static_cast<uint32_t>(i), static_cast<uint32_t>(step), purpose,
+                                     static_cast<uint32_t>(event), 0);
+        const Uniform2 d1 = uniform2(P.cfg.random_seed, static_cast<uint32_t>(i), static_cast<uint32_t>(step), purpose,
+                                     static_cast<uint32_t>(event), 1);
+        const double u[3] = {d0.a, d0.b, d1.a};
+        const InterfaceOutcome r = interface_interact(P.iface, P.mats, static_cast<int>(w >> 28),
+                                                      static_cast<int>(w & kActiveMask), (w >> 24) & 7u, occ[i],
+                                                      destination, u);
+        iface_events += r.events;
+        iface_transmitted += r.transmitted;
+        iface_reflected += r.reflected;
+        if (r.action == kInterfaceFail)
+            fail("Full-matrix boundary mode mapping failed while advancing particles for particle " + std::to_string(i) +
+                 ". An inward discrete material mode and finite signed energy weight are required; no velocity-only "
+                 "reflection was applied.");
+        mode[i] = mode_word(static_cast<uint32_t>(r.active), r.signs, static_cast<uint32_t>(r.material));
+        occ[i] = r.occ;
+    }
+
     // src/solver/TransportOperator.cpp:405-466
     void advance(int i, double remaining, uint32_t purpose) {
         if (!alive[i]) return;
@@ -472,20 +623,33 @@ struct OracleSolver {
                  ". Check that the STL is closed and manifold.");
         int event = 0;
         for (; remaining > 1e-14 && event < 64; ++event) {
-            if (!std::isfinite(t) || t > remaining) {
+            int destination = -1;
+            const double t_cross = next_crossing(p, v, static_cast<int>(mode[i] >> 28), destination);
+            const double t_event = std::min(t, t_cross);
+            if (!std::isfinite(t_event) || t_event > remaining) {
                 p = add3(p, mul3(v, remaining));
                 x[i] = p[0]; y[i] = p[1]; z[i] = p[2];
                 return;
             }
-            remaining -= std::max(0.0, t);
-            p = cp;
-            if (!boundary(i, f, p, purpose, event)) {
-                x[i] = p[0]; y[i] = p[1]; z[i] = p[2];
-                return;
+            // the outer wall wins exact ties
+            const bool interface_first = t_cross < t;
+            remaining -= std::max(0.0, t_event);
+            if (interface_first) {
+                p = add3(p, mul3(v, t_cross));
+                material_interface(i, destination, purpose, event);
+                v = velocity(mode[i]);
+                const double speed = std::max(norm3(v), 1e-12);
+                p = add3(p, mul3(v, P.push_eps / speed));
+            } else {
+                p = cp;
+                if (!boundary(i, f, p, purpose, event)) {
+                    x[i] = p[0]; y[i] = p[1]; z[i] = p[2];
+                    return;
+                }
+                v = velocity(mode[i]);
             }
-            v = velocity(mode[i]);
             if (!cache(p, v, cp, t, f)) fail("Boundary intersection failed while advancing particles for particle " + std::to_string(i));
-            if (t < 1e-12) {
+            if (!interface_first && t < 1e-12) {
                 p = add3(p, mul3(v, 1e-12));
                 if (!cache(p, v, cp, t, f)) fail("Boundary intersection failed while advancing particles for particle " + std::to_string(i));
             }
@@ -844,6 +1008,9 @@ int orc_solver_stats(void* sp, phmc_stats* o) {
         o->average_heat_flux_along_axis = s->avg_flux;
         o->kappa_fit = s->kappa_fit;
         o->kappa_endpoints = s->kappa_end;
+        o->interface_events = s->iface_events;
+        o->interface_transmitted = s->iface_transmitted;
+        o->interface_reflected = s->iface_reflected;
     });
 }
 int orc_solver_cell_count(void* sp, int* n) {
@@ -988,6 +1155,47 @@ int orc_rough_reflect(void* m, int conservative, double Tref, const double nout[
                                          RoughDraws{{u3[3 * i], u3[3 * i + 1], u3[3 * i + 2]}}, o);
             flat_out[i] = M->active_flat()[out];
             occ_out[i] = o;
+        }
+    });
+}
+
+// Interface interactions between two materials with explicit weights and draws
+// (src/solver/InterfaceInteraction.cpp:46-153); signs are the carrier's three
+// velocity sign bits relative to the table velocity.
+int orc_interface(void* ma, void* mb, double wa, double wb, int axis, double bin_thz, double Tref, int linearized,
+                  int64_t n, const int32_t* src, const int32_t* flat_in, const int32_t* signs_in, const double* occ_in,
+                  const double* u3, int32_t* action, int32_t* material_out, int32_t* flat_out, int32_t* signs_out,
+                  double* occ_out) {
+    return guard([&] {
+        const PhononMaterial* M[2] = {static_cast<OracleMaterial*>(ma)->m.get(), static_cast<OracleMaterial*>(mb)->m.get()};
+        InterfaceTables I;
+        I.enabled = true;
+        I.linearized = linearized != 0;
+        I.reference_temperature = Tref;
+        I.band_width = 2.0 * std::acos(-1.0) * bin_thz;
+        I.build({M[0], M[1]}, axis);
+        std::vector<MaterialTables> T(2);
+        const double w[2] = {wa, wb};
+        for (int k = 0; k < 2; ++k) {
+            T[k].n_active = M[k]->active_mode_count();
+            T[k].energy_weight = w[k];
+            for (int a = 0; a < T[k].n_active; ++a) {
+                const int f = M[k]->active_flat()[a];
+                T[k].omega.push_back(M[k]->omega(f));
+                T[k].nbg.push_back(M[k]->bose_occupation(Tref, f));
+                for (int c = 0; c < 3; ++c) T[k].vel.push_back(M[k]->velocity(f)[c]);
+            }
+        }
+        for (int64_t i = 0; i < n; ++i) {
+            const int m = src[i];
+            const int a = M[m]->active_index_for_flat(flat_in[i]);
+            const InterfaceOutcome r = interface_interact(I, T, m, a, static_cast<uint32_t>(signs_in[i]), occ_in[i], 1 - m,
+                                                          u3 + 3 * i);
+            action[i] = r.action;
+            material_out[i] = r.material;
+            flat_out[i] = M[r.material]->active_flat()[r.active];
+            signs_out[i] = static_cast<int32_t>(r.signs);
+            occ_out[i] = r.occ;
         }
     });
 }

@@ -19,6 +19,7 @@
 #include "solver/BoundaryInteraction.h"
 #include "solver/CarrierCollisionOperator.h"
 #include "solver/CellParticleIndex.h"
+#include "solver/InterfaceInteraction.h"
 #include "solver/ParticleStorage.h"
 #include "solver/ReservoirSampler.h"
 #include "solver/RoughBoundarySampler.h"
@@ -482,6 +483,100 @@ std::string cmd_rough(const std::string& pmat, bool conservative) {
     return j.str();
 }
 
+// interface <pmat_a> <pmat_b> <linearized>: DMM interactions at a z-normal
+// interface between two materials (InterfaceInteraction::interact), with the
+// engine's draws recorded by replaying a copy of it.
+std::string cmd_interface(const std::string& pa, const std::string& pb, bool linearized) {
+    PhononMaterial ma(read_pmat(pa), 0.1, false, false), mb(read_pmat(pb), 0.1, false, false);
+    const double wa = 1.375e-3, wb = 0.8125e-3;
+    phonomc::InterfaceInteractionConfig cfg;
+    cfg.axis = 2;
+    cfg.enabled = true;
+    cfg.linearized = linearized;
+    cfg.model = InterfaceModel::DiffuseMismatch;
+    cfg.frequency_bin_thz = 0.1;
+    cfg.reference_temperature = 300.0;
+    phonomc::InterfaceInteraction I;
+    I.configure(cfg, {&ma, &mb}, {wa, wb});
+    const PhononMaterial* mats[2] = {&ma, &mb};
+    std::mt19937_64 pick(77);
+    std::uniform_real_distribution<double> U(0, 1);
+    std::vector<int> src, in_flat, in_signs, action, out_material, out_flat, ndraw, events, transmitted, reflected,
+        error;
+    std::vector<double> in_occ, out_occ, draws, out_v;
+    for (int i = 0; i < 1200; ++i) {
+        const int m = i % 2;
+        const int next = 1 - m;
+        const PhononMaterial& M = *mats[m];
+        const int a = static_cast<int>(U(pick) * M.active_mode_count());
+        const auto mode = M.active_mode_at(a);
+        auto v = M.mode_group_velocity(mode);
+        if (std::abs(v[2]) <= 1e-12) continue;
+        // moving toward the other layer (material 0 below, material 1 above)
+        int signs = 0;
+        const bool want_up = m == 0;
+        if ((v[2] > 0) != want_up) {
+            v[2] = -v[2];
+            signs |= 4;
+        }
+        for (int k = 0; k < 2; ++k)
+            if (U(pick) < 0.5) {
+                v[k] = -v[k];
+                signs |= 1 << k;
+            }
+        const double Tn = 300.0 + 8.0 * (U(pick) - 0.5);
+        const double occ = linearized ? M.bose_occupation(300.0, mode) + (U(pick) - 0.5) * 0.02
+                                      : M.bose_occupation(Tn, mode);
+        phonomc::BoundaryState st{mode, m, v, M.mode_angular_frequency(mode), occ};
+        std::mt19937_64 eng(5000 + i), copy = eng;
+        const auto r = I.interact(st, next, eng);
+        int used = 0;
+        std::vector<double> u;
+        while (!(copy == eng) && used < 8) {
+            u.push_back(std::generate_canonical<double, 53>(copy));
+            ++used;
+        }
+        src.push_back(m);
+        in_flat.push_back(mode[0] * M.branch_count() + mode[1]);
+        in_signs.push_back(signs);
+        in_occ.push_back(occ);
+        action.push_back(static_cast<int>(r.action));
+        error.push_back(static_cast<int>(r.error));
+        out_material.push_back(r.state.material);
+        const PhononMaterial& D = *mats[r.state.material];
+        out_flat.push_back(r.state.mode[0] * D.branch_count() + r.state.mode[1]);
+        out_occ.push_back(r.state.occupation);
+        for (int k = 0; k < 3; ++k) out_v.push_back(r.state.velocity[k]);
+        events.push_back(static_cast<int>(r.interface_events));
+        transmitted.push_back(static_cast<int>(r.interface_transmitted));
+        reflected.push_back(static_cast<int>(r.interface_reflected));
+        ndraw.push_back(used);
+        for (int k = 0; k < 3; ++k) draws.push_back(k < used ? u[k] : -1.0);
+    }
+    Json j;
+    j.put("weight_a", wa);
+    j.put("weight_b", wb);
+    j.put("frequency_bin_thz", 0.1);
+    j.put("reference_temperature", 300.0);
+    j.put_i("axis", 2);
+    j.arr("src", src);
+    j.arr("in_flat", in_flat);
+    j.arr("in_signs", in_signs);
+    j.arr("in_occ", in_occ);
+    j.arr("action", action);
+    j.arr("error", error);
+    j.arr("out_material", out_material);
+    j.arr("out_flat", out_flat);
+    j.arr("out_occ", out_occ);
+    j.arr("out_v", out_v);
+    j.arr("events", events);
+    j.arr("transmitted", transmitted);
+    j.arr("reflected", reflected);
+    j.arr("ndraw", ndraw);
+    j.arr("draws", draws);
+    return j.str();
+}
+
 // gradient <pmat>: TemperatureGradientDrive on random carriers in a periodic box.
 std::string cmd_gradient(const std::string& pmat) {
     PhononMaterial m(read_pmat(pmat), 0.1, true, false);
@@ -618,6 +713,7 @@ int main(int argc, char** argv) {
         else if (c == "callaway") out = cmd_callaway();
         else if (c == "rough") out = cmd_rough(argv[2], std::atoi(argv[3]) != 0);
         else if (c == "gradient") out = cmd_gradient(argv[2]);
+        else if (c == "interface") out = cmd_interface(argv[2], argv[3], std::atoi(argv[4]) != 0);
         else if (c == "reservoir") out = cmd_reservoir(argv[2]);
         else if (c == "run") out = cmd_run(argv[2], argv[3], std::atoi(argv[4]));
         else throw std::runtime_error("unknown command " + c);

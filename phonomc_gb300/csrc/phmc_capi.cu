@@ -70,6 +70,21 @@ __global__ void k_trace_rays(DevDomain D, int64_t n, const double* p3, const dou
     }
 }
 
+__global__ void k_interface_rays(const __grid_constant__ DevTables T, int64_t n, const int32_t* src,
+                                 const int32_t* ain, const int32_t* signs, const double* occ, const double* u3,
+                                 int32_t* action, int32_t* mat, int32_t* aout, int32_t* sout, double* oout) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const IfaceOut r = interface_dev(T, src[i], ain[i], static_cast<uint32_t>(signs[i]), occ[i], 1 - src[i],
+                                         u3[3 * i], u3[3 * i + 1], u3[3 * i + 2]);
+        action[i] = r.action;
+        mat[i] = r.material;
+        aout[i] = r.active;
+        sout[i] = static_cast<int32_t>(r.signs);
+        oout[i] = r.occ;
+    }
+}
+
 __global__ void k_inverse_table(const double* E, const double* T, int nt, int64_t n, const double* e, double* out) {
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x)
@@ -251,6 +266,69 @@ int phmc_dev_trace_box(const double lo[3], const double hi[3], int64_t n, const 
         dh.get(hit3);
         dt.get(t);
         df.get(facet);
+    });
+}
+
+int phmc_dev_interface(const phmc_material* ma, const phmc_material* mb, double wa, double wb, int axis,
+                       double bin_thz, double Tref, int linearized, int64_t n, const int32_t* src,
+                       const int32_t* flat_in, const int32_t* signs_in, const double* occ_in, const double* u3,
+                       int32_t* action, int32_t* material_out, int32_t* flat_out, int32_t* signs_out, double* occ_out) {
+    return guard([&] {
+        const PhononMaterial* M[2] = {ma->m.get(), mb->m.get()};
+        InterfaceTables I;
+        I.build({M[0], M[1]}, axis);
+        DevTables T;
+        std::memset(&T, 0, sizeof T);
+        T.iface.enabled = 1;
+        T.iface.linearized = linearized != 0;
+        T.iface.axis = axis;
+        T.iface.band_width = 2.0 * std::acos(-1.0) * bin_thz;
+        std::vector<std::unique_ptr<DBuf<double>>> dbl;
+        std::vector<std::unique_ptr<DBuf<int>>> ints;
+        const double w[2] = {wa, wb};
+        for (int k = 0; k < 2; ++k) {
+            std::vector<double> om, vel, nbg;
+            for (int a = 0; a < M[k]->active_mode_count(); ++a) {
+                const int f = M[k]->active_flat()[a];
+                om.push_back(M[k]->omega(f));
+                nbg.push_back(M[k]->bose_occupation(Tref, f));
+                for (int c = 0; c < 3; ++c) vel.push_back(M[k]->velocity(f)[c]);
+            }
+            dbl.emplace_back(new DBuf<double>(om));
+            T.mat[k].omega = dbl.back()->p;
+            dbl.emplace_back(new DBuf<double>(vel));
+            T.mat[k].vel = dbl.back()->p;
+            dbl.emplace_back(new DBuf<double>(nbg));
+            T.mat[k].nbg = dbl.back()->p;
+            T.mat[k].energy_weight = w[k];
+            T.mat[k].n_active = M[k]->active_mode_count();
+            for (int dir = 0; dir < 2; ++dir) {
+                const InterfaceBank& B = I.banks[k][dir];
+                dbl.emplace_back(new DBuf<double>(B.omega));
+                T.iface.bank[k][dir].omega = dbl.back()->p;
+                dbl.emplace_back(new DBuf<double>(B.prefix));
+                T.iface.bank[k][dir].prefix = dbl.back()->p;
+                ints.emplace_back(new DBuf<int>(B.active));
+                T.iface.bank[k][dir].active = ints.back()->p;
+                T.iface.bank[k][dir].n = static_cast<int>(B.omega.size());
+            }
+        }
+        std::vector<int32_t> ain(n);
+        for (int64_t i = 0; i < n; ++i) ain[i] = M[src[i]]->active_index_for_flat(flat_in[i]);
+        DBuf<int32_t> dsrc(src, n), da(ain), dsg(signs_in, n), dact(n), dmat(n), dao(n), dso(n);
+        DBuf<double> docc(occ_in, n), du(u3, 3 * n), doo(n);
+        k_interface_rays<<<256, 256>>>(T, n, dsrc.p, da.p, dsg.p, docc.p, du.p, dact.p, dmat.p, dao.p, dso.p, doo.p);
+        cuda_check(cudaDeviceSynchronize(), "k_interface_rays");
+        std::vector<int32_t> ao(n), mo(n);
+        dact.get(action);
+        dmat.get(mo.data());
+        dao.get(ao.data());
+        dso.get(signs_out);
+        doo.get(occ_out);
+        for (int64_t i = 0; i < n; ++i) {
+            material_out[i] = mo[i];
+            flat_out[i] = M[mo[i]]->active_flat()[ao[i]];
+        }
     });
 }
 

@@ -134,9 +134,9 @@ __global__ void __launch_bounds__(256) k_rta_solve(const DevTables* __restrict__
     const DevTables& T = *Tp;
     const int c = blockIdx.x;
     const DevMaterial& M = T.mat[C.cell_material[c]];
-    const int nc = C.n_classes;
-    double* cs = C.cls_sum + static_cast<size_t>(c) * nc * 3;
-    double2* ab = C.rta_ab + static_cast<size_t>(c) * nc;
+    const int nc = M.n_classes; // this cell's material; arrays are strided by the largest count
+    double* cs = C.cls_sum + static_cast<size_t>(c) * C.n_classes * 3;
+    double2* ab = C.rta_ab + static_cast<size_t>(c) * C.n_classes;
     const double Tc = C.temperature[c];
     const double dt = T.par.dt;
     for (int k = threadIdx.x; k < nc; k += blockDim.x) {
@@ -273,8 +273,10 @@ __global__ void __launch_bounds__(kLinThreads) k_linear_solve(const DevTables* _
     const int CL = static_cast<int>(cl.num_blocks());
     const int rank = static_cast<int>(cl.block_rank());
     const int c = blockIdx.x / CL;
-    const DevMaterial& M = T.mat[C.cell_material[c]];
+    const int mat = C.cell_material[c];
+    const DevMaterial& M = T.mat[mat];
     const int na = M.n_active;
+    const size_t mo = static_cast<size_t>(mat) * C.hist_modes; // this material's per-mode constants
     const int per = (C.hist_modes + CL - 1) / CL;
     const int m0 = rank * per, m1 = min(na, m0 + per);
     const int nloc = max(0, m1 - m0);
@@ -291,10 +293,10 @@ __global__ void __launch_bounds__(kLinThreads) k_linear_solve(const DevTables* _
         cnt[j] = k;
         const double e = k ? M.hw[m] * (bin.N - k * M.nbg[m]) : 0.0;
         if constexpr (kF32) {
-            X[j] = static_cast<float>(e) * C.lin32_inv_s[m];
-            rate[j] = C.lin32_rate[m];
+            X[j] = static_cast<float>(e) * C.lin32_inv_s[mo + m];
+            rate[j] = C.lin32_rate[mo + m];
         } else {
-            X[j] = k ? e / C.lin_s[m] : 0.0;
+            X[j] = k ? e / C.lin_s[mo + m] : 0.0;
             rate[j] = M.col_rate[m];
         }
     }
@@ -310,7 +312,7 @@ __global__ void __launch_bounds__(kLinThreads) k_linear_solve(const DevTables* _
         for (int b = 0; b < nbasis; ++b) {
             R* v = u + static_cast<size_t>(G) * per;
             R nv[1] = {R(0)};
-            const float* basis32 = C.lin32_basis + static_cast<size_t>(kind == 0 ? 1 + b : 0) * na;
+            const float* basis32 = C.lin32_basis + (static_cast<size_t>(mat) * 5 + (kind == 0 ? 1 + b : 0)) * C.hist_modes;
             for (int j = threadIdx.x; j < nloc; j += blockDim.x) {
                 const int m = m0 + j;
                 R val = R(0);
@@ -318,8 +320,8 @@ __global__ void __launch_bounds__(kLinThreads) k_linear_solve(const DevTables* _
                     if constexpr (kF32) {
                         val = basis32[m];
                     } else {
-                        const double sv = C.lin_s[m];
-                        val = (b == 0 ? sv : sv * M.col_k[3 * m + b - 1] / M.omega[m]) * sq[m];
+                        const double sv = C.lin_s[mo + m];
+                        val = (b == 0 ? sv : sv * M.col_k[3 * m + b - 1] / M.omega[m]) * sq[mo + m];
                     }
                     nv[0] += static_cast<R>(cnt[j]) * val * val;
                 }
@@ -356,8 +358,8 @@ __global__ void __launch_bounds__(kLinThreads) k_linear_solve(const DevTables* _
         for (int q = first; q < G; ++q) {
             R* qv = u + static_cast<size_t>(q) * per;
             for (int j = threadIdx.x; j < nloc; j += blockDim.x) {
-                if constexpr (kF32) qv[j] *= sq32[m0 + j];
-                else qv[j] *= sq[m0 + j];
+                if constexpr (kF32) qv[j] *= sq32[mo + m0 + j];
+                else qv[j] *= sq[mo + m0 + j];
             }
         }
         __syncthreads();
@@ -402,14 +404,14 @@ __global__ void __launch_bounds__(kLinThreads) k_linear_solve(const DevTables* _
         if (k) {
             const double e = M.hw[m] * (C.bins[hb + m].N - k * M.nbg[m]);
             if constexpr (kF32) {
-                const float x0 = static_cast<float>(e) * C.lin32_inv_s[m];
-                A = static_cast<double>(C.lin32_s_over_hw[m] * (X[j] - C.lin32_decay[m] * x0) *
+                const float x0 = static_cast<float>(e) * C.lin32_inv_s[mo + m];
+                A = static_cast<double>(C.lin32_s_over_hw[mo + m] * (X[j] - C.lin32_decay[mo + m] * x0) *
                                         __frcp_rn(static_cast<float>(k)));
-                cons[0] += C.lin_omd[m] * e;
+                cons[0] += C.lin_omd[mo + m] * e;
             } else {
-                const double x0 = e / C.lin_s[m];
-                A = C.lin_s[m] * (static_cast<double>(X[j]) - C.lin_decay[m] * x0) / (k * M.hw[m]);
-                cons[0] += (1.0 - C.lin_decay[m]) * e;
+                const double x0 = e / C.lin_s[mo + m];
+                A = C.lin_s[mo + m] * (static_cast<double>(X[j]) - C.lin_decay[mo + m] * x0) / (k * M.hw[m]);
+                cons[0] += (1.0 - C.lin_decay[mo + m]) * e;
             }
             cons[1] += k * M.hw[m] * A;
         }
@@ -423,8 +425,8 @@ __global__ void __launch_bounds__(kLinThreads) k_linear_solve(const DevTables* _
     __syncthreads();
     for (int j = threadIdx.x; j < nloc; j += blockDim.x) {
         const int m = m0 + j;
-        if constexpr (kF32) beta[m] = fma(lambda, beta[m], C.lin_bg[m]);
-        else beta[m] = (1.0 - C.lin_decay[m]) * M.nbg[m] + lambda * beta[m];
+        if constexpr (kF32) beta[m] = fma(lambda, beta[m], C.lin_bg[mo + m]);
+        else beta[m] = (1.0 - C.lin_decay[mo + m]) * M.nbg[m] + lambda * beta[m];
     }
     // no block leaves while another block of the cluster may still read its part[]
     cl.sync();
@@ -450,7 +452,7 @@ __global__ void __launch_bounds__(kStatThreads) k_cell_tables(const DevTables* _
                 a = 1.0 - r.x;
                 bc = r.x * r.y;
             } else {
-                a = C.lin_decay[m];
+                a = C.lin_decay[static_cast<size_t>(C.cell_material[c]) * C.hist_modes + m];
                 bc = C.lin_beta[hb + m];
             }
         }

@@ -121,6 +121,7 @@ struct DevDomain {
     int layout_axis;
     int n_planes;
     double planes[kMaxMaterials];
+    int plane_cell[kMaxMaterials]; // cell boundary index of each plane along the layout axis
 };
 
 struct DevParams {
@@ -165,11 +166,26 @@ struct DevLedger {
     unsigned long long total_absorbed, total_injected;
     double total_absorbed_ev, total_injected_ev, total_lifetime_residual, total_balance_residual, total_drive_ev;
     unsigned long long total_drive_updates;
+    unsigned long long total_iface_events, total_iface_transmitted, total_iface_reflected;
     long long particle_count;
+};
+
+// Diffuse-mismatch banks (src/solver/InterfaceModeSampler.cpp:11-44).
+struct DevInterfaceBank {
+    const double* omega;  // sorted
+    const int* active;
+    const double* prefix; // n + 1
+    int n;
+};
+struct DevInterface {
+    int enabled, linearized, axis;
+    double band_width;
+    DevInterfaceBank bank[kMaxMaterials][2];
 };
 
 struct DevTables {
     DevMaterial mat[kMaxMaterials];
+    DevInterface iface;
     DevRoughTable rough[kMaxRoughTables];
     DevReservoir res[kMaxReservoirs];
     DevDomain dom;
@@ -431,6 +447,117 @@ __device__ __forceinline__ double gamma_at(const DevMaterial& M, int a, double T
     if (fabs(x1 - x0) <= 1e-18) return y0;
     const double t = (T - x0) / (x1 - x0);
     return y0 * (1.0 - t) + y1 * t;
+}
+
+// ------------------------------------------------------ interfaces
+__device__ __forceinline__ int lower_bound_dev(const double* a, int lo, int hi, double x) {
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (a[mid] < x) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ int upper_bound_dev(const double* a, int lo, int hi, double x) {
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (!(x < a[mid])) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// src/solver/InterfaceModeSampler.cpp:69-108 with the uniform supplied.
+__device__ __forceinline__ int interface_band_dev(const DevInterfaceBank& B, double omega, double width, double u,
+                                                  bool& drew, double& flux) {
+    const double bin = floor(omega / width);
+    const double lo = __dmul_rn(bin, width), hi = __dmul_rn(__dadd_rn(bin, 1.0), width);
+    const int begin = lower_bound_dev(B.omega, 0, B.n, lo);
+    const int end = lower_bound_dev(B.omega, 0, B.n, hi);
+    flux = end > begin ? __dadd_rn(B.prefix[end], -B.prefix[begin]) : 0.0;
+    drew = false;
+    if (!(flux > 0.0)) return -1;
+    drew = true;
+    const double target = __dadd_rn(B.prefix[begin], __dmul_rn(u, flux));
+    int pos = upper_bound_dev(B.prefix, begin + 1, end + 1, target);
+    pos = min(max(pos, begin + 1), end) - 1;
+    return B.active[pos];
+}
+
+struct IfaceOut {
+    int action; // 3 reflect, 4 transmit, 5 fail
+    int material, active;
+    uint32_t signs;
+    double occ;
+    int transmitted;
+};
+
+// src/solver/InterfaceInteraction.cpp:46-153, diffuse mismatch, uniforms
+// consumed in the reference's order from u[0..2].
+__device__ __forceinline__ IfaceOut interface_dev(const DevTables& T, int src, int a, uint32_t signs, double occ,
+                                                  int next, double u0, double u1, double u2) {
+    const DevInterface& I = T.iface;
+    const DevMaterial& S = T.mat[src];
+    IfaceOut r;
+    r.material = src;
+    r.active = a;
+    r.signs = signs;
+    r.occ = occ;
+    r.transmitted = 0;
+    const int axis = I.axis;
+    const double omega = S.omega[a];
+    const double v_axis = ((signs >> axis) & 1u) ? -S.vel[3 * a + axis] : S.vel[3 * a + axis];
+    const int incident = v_axis > 0.0 ? 1 : 0;
+    const double u[3] = {u0, u1, u2};
+    int k = 0;
+    bool drew;
+    double source_flux = 0, target_flux = 0;
+    const int refl = interface_band_dev(I.bank[src][1 - incident], omega, I.band_width, u[k], drew, source_flux);
+    if (drew) ++k;
+    const int trans = interface_band_dev(I.bank[next][incident], omega, I.band_width, k < 3 ? u[k] : 0.0, drew,
+                                         target_flux);
+    if (drew) ++k;
+    const double transmission =
+        target_flux > 0 ? target_flux / fmax(1e-300, __dadd_rn(source_flux, target_flux)) : 0.0;
+    const bool transmit = trans >= 0 && (k < 3 ? u[k] : 1.0) < transmission;
+    const int sel_material = transmit ? next : src;
+    const int sel = transmit ? trans : refl;
+    if (sel < 0) {
+        if (I.linearized) {
+            r.action = 5;
+            return r;
+        }
+        r.signs ^= 1u << axis;
+        r.action = 3;
+        return r;
+    }
+    const DevMaterial& Dm = T.mat[sel_material];
+    const double new_omega = Dm.omega[sel];
+    const double old_deviation = __dadd_rn(occ, -S.nbg[a]);
+    const double physical = __dmul_rn(__dmul_rn(S.energy_weight, omega), old_deviation);
+    const double new_deviation = physical / fmax(1e-300, __dmul_rn(Dm.energy_weight, new_omega));
+    const double new_occ = __dadd_rn(Dm.nbg[sel], new_deviation);
+    if (I.linearized) {
+        const double nv = Dm.vel[3 * sel + axis];
+        const int expected = transmit ? incident : 1 - incident;
+        if (!isfinite(new_occ) || !isfinite(nv) || (expected ? !(nv > 0.0) : !(nv < 0.0))) {
+            r.action = 5;
+            return r;
+        }
+    }
+    if (!isfinite(new_occ) || (!I.linearized && new_occ < 0.0)) {
+        r.signs ^= 1u << axis;
+        r.action = 3;
+        return r;
+    }
+    r.material = sel_material;
+    r.active = sel;
+    r.signs = 0;
+    r.occ = new_occ;
+    r.action = transmit ? 4 : 3;
+    r.transmitted = transmit ? 1 : 0;
+    return r;
 }
 
 } // namespace phmc

@@ -616,6 +616,70 @@ void EnergyLedger::finish_step(double energy, const BoundaryBalance& b) {
 }
 
 // ---------------------------------------------------------------- problem
+// src/solver/InterfaceModeSampler.cpp:11-44
+void InterfaceTables::build(const std::vector<const PhononMaterial*>& mats, int ax) {
+    axis = ax;
+    banks.assign(mats.size(), {});
+    for (size_t mid = 0; mid < mats.size(); ++mid) {
+        const PhononMaterial& M = *mats[mid];
+        const auto& act = M.active_flat();
+        for (int direction = 0; direction < 2; ++direction) {
+            InterfaceBank& B = banks[mid][direction];
+            std::vector<std::pair<double, int>> ordered;
+            for (int a = 0; a < static_cast<int>(act.size()); ++a) {
+                const double c = M.velocity(act[a])[axis];
+                if ((direction == 0 && c < 0.0) || (direction == 1 && c > 0.0)) ordered.push_back({M.omega(act[a]), a});
+            }
+            std::sort(ordered.begin(), ordered.end());
+            B.prefix.assign(ordered.size() + 1, 0.0);
+            for (size_t i = 0; i < ordered.size(); ++i) {
+                B.omega.push_back(ordered[i].first);
+                B.active.push_back(ordered[i].second);
+                const double flux = std::abs(M.velocity(act[ordered[i].second])[axis]) / M.energy_density_normalization();
+                B.prefix[i + 1] = B.prefix[i] + flux;
+            }
+        }
+    }
+}
+
+// src/solver/LayeredMaterialLayout.cpp:62-114: planes inside the box on cell
+// boundaries, every layer with a cell, reservoirs normal to the layout axis,
+// no periodic pair across it.
+static void validate_layout(Problem& P, const SimulationConfig& cfg, const SimulationDomain& domain, int count) {
+    const int axis = P.layout.axis;
+    if (axis < 0 || axis > 2) throw std::invalid_argument("Invalid layered material count, axis or interface count.");
+    for (size_t i = 0; i < P.layout.planes.size(); ++i)
+        if (!std::isfinite(P.layout.planes[i]) || (i && P.layout.planes[i] <= P.layout.planes[i - 1]))
+            throw std::invalid_argument("Material interface positions must be finite and strictly increasing.");
+    const int cells = domain.grid_shape()[axis];
+    const double lo = domain.bounds_min()[axis], hi = domain.bounds_max()[axis];
+    const double width = (hi - lo) / cells;
+    const double tol = std::max(1e-10, 1e-10 * std::abs(hi - lo));
+    P.plane_cell.clear();
+    for (double plane : P.layout.planes) {
+        if (!std::isfinite(plane) || !(plane > lo) || !(plane < hi))
+            throw std::runtime_error("Each material interface must lie strictly inside the loaded geometry bounds.");
+        const double cc = (plane - lo) / width;
+        if (std::abs(cc - std::round(cc)) > tol / width)
+            throw std::runtime_error("Each materials.interface_positions value must coincide with a grid-cell boundary.");
+        P.plane_cell.push_back(static_cast<int>(std::llround(cc)));
+    }
+    std::vector<bool> occupied(count, false);
+    for (int id : P.cell_material) occupied.at(id) = true;
+    for (bool o : occupied)
+        if (!o) throw std::runtime_error("Every material layer must contain at least one active geometry cell.");
+    for (const auto& F : domain.facets()) {
+        if (F.condition == 'P' && std::abs(F.normal[axis]) > 0.99)
+            throw std::runtime_error("Periodic boundaries normal to materials.interface_axis are not supported, "
+                                     "because they would join different end materials.");
+        if (F.condition == 'T' && std::abs(F.normal[axis]) < 0.99)
+            throw std::runtime_error("In the layered-material model, thermal-reservoir facets must be normal to "
+                                     "materials.interface_axis so each reservoir touches one material.");
+    }
+    if (!std::isfinite(cfg.material_interface_frequency_bin_thz) || cfg.material_interface_frequency_bin_thz <= 0)
+        throw std::runtime_error("Interface frequency bin must be finite and positive.");
+}
+
 Problem build_problem(const SimulationConfig& cfg, SimulationDomain& domain,
                       const std::vector<const PhononMaterial*>& mats) {
     if (mats.empty()) throw std::runtime_error("MonteCarloSolver requires at least one material.");
@@ -637,7 +701,7 @@ Problem build_problem(const SimulationConfig& cfg, SimulationDomain& domain,
         throw std::runtime_error("Layered materials require one interface plane fewer than materials.");
     P.cell_material.resize(domain.grid_count());
     for (int c = 0; c < domain.grid_count(); ++c) P.cell_material[c] = P.layout.material_at(domain.grid_centers()[c]);
-    if (mats.size() > 1) throw std::runtime_error("Multi-material layouts are not enabled in this build.");
+    if (mats.size() > 1) validate_layout(P, cfg, domain, static_cast<int>(mats.size()));
 
     int axis = 0;
     if (cfg.transport_axis >= 0) axis = cfg.transport_axis;
@@ -768,6 +832,18 @@ Problem build_problem(const SimulationConfig& cfg, SimulationDomain& domain,
         enabled.push_back(P.conservative ? reflecting : F.condition == 'R');
     }
     P.rough.build(mats, normals, rough, enabled, P.conservative, P.conservative ? Tbg : 0.0);
+
+    // Interface banks (src/solver/InterfaceInitialization.cpp:3-15, InterfaceInteraction.cpp:11-41).
+    P.iface.enabled = mats.size() > 1;
+    P.iface.linearized = P.linearized;
+    P.iface.reference_temperature = Tbg;
+    P.iface.band_width = 2.0 * std::acos(-1.0) * cfg.material_interface_frequency_bin_thz;
+    if (P.iface.enabled) {
+        if (cfg.material_interface_model != 0)
+            throw std::runtime_error("Only the diffuse-mismatch interface model (materials.interface_model = dmm) "
+                                     "is built.");
+        P.iface.build(mats, P.layout.axis);
+    }
 
     // Reservoirs (src/solver/ReservoirInitialization.cpp:1-45, ReservoirSampler.cpp:17-101).
     const double density = static_cast<double>(P.initial_particles) / domain.volume();

@@ -66,6 +66,7 @@ struct SimulationConfig {
     int material_interface_axis = 0;
     std::vector<double> material_interface_positions; // Angstrom
     double material_interface_frequency_bin_thz = 0.1;
+    int material_interface_model = 0; // 0 = diffuse mismatch (dmm)
 };
 
 // include/SimulationConfig.h:148-156
@@ -209,6 +210,30 @@ struct LayeredLayout {
     }
 };
 
+// ---------------------------------------------------- interface banks
+// Diffuse-mismatch mode banks (src/solver/InterfaceModeSampler.cpp:11-44): per
+// material and direction (0: v_axis < 0, 1: v_axis > 0) the active modes sorted
+// by (omega, active index), with the running sum of |v_axis| / energy-density
+// normalization.
+struct InterfaceBank {
+    std::vector<double> omega;
+    std::vector<int> active;
+    std::vector<double> prefix; // size + 1
+};
+
+struct InterfaceTables {
+    bool enabled = false;
+    bool linearized = false;
+    int axis = 0;
+    double band_width = 0;            // 2 pi * frequency bin (rad/ps)
+    double reference_temperature = 300;
+    std::vector<std::array<InterfaceBank, 2>> banks; // [material][direction]
+    void build(const std::vector<const PhononMaterial*>& mats, int axis);
+};
+
+// Outcome of one interface event (src/solver/InterfaceInteraction.cpp:46-153).
+enum InterfaceAction { kInterfaceReflect = 3, kInterfaceTransmit = 4, kInterfaceFail = 5 };
+
 // -------------------------------------------------------- rough tables
 struct RoughTable {
     int material = 0, facet = -1;
@@ -310,6 +335,8 @@ struct Problem {
     LayeredLayout layout;
     std::vector<int> cell_material;      // [cells]
     RoughTables rough;
+    InterfaceTables iface;
+    std::vector<int> plane_cell;         // cell boundary index of each interface plane along the layout axis
     std::vector<Reservoir> reservoirs;
     std::vector<std::vector<double>> reservoir_occ; // [reservoir][active of its material]
     double gradient_energy_weight = 0;

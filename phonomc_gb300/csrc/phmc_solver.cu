@@ -273,6 +273,23 @@ void DeviceSolver::upload_tables() {
     D.layout_axis = P_.layout.axis;
     D.n_planes = static_cast<int>(P_.layout.planes.size());
     for (int k = 0; k < D.n_planes; ++k) D.planes[k] = P_.layout.planes[k];
+    for (size_t k = 0; k < P_.plane_cell.size(); ++k) D.plane_cell[k] = P_.plane_cell[k];
+    // interface banks
+    DevInterface& I = T.iface;
+    I.enabled = P_.iface.enabled ? 1 : 0;
+    I.linearized = P_.iface.linearized ? 1 : 0;
+    I.axis = P_.iface.axis;
+    I.band_width = P_.iface.band_width;
+    for (size_t m = 0; m < P_.iface.banks.size(); ++m)
+        for (int dir = 0; dir < 2; ++dir) {
+            const InterfaceBank& B = P_.iface.banks[m][dir];
+            for (double w : B.omega)
+                if (!std::isfinite(w) || w < 0) throw std::invalid_argument("Invalid shared interface frequency band.");
+            I.bank[m][dir].omega = upload(B.omega);
+            I.bank[m][dir].active = upload(B.active);
+            I.bank[m][dir].prefix = upload(B.prefix);
+            I.bank[m][dir].n = static_cast<int>(B.omega.size());
+        }
     // params
     DevParams& p = T.par;
     p.dt = cfg_.time_step;
@@ -312,14 +329,14 @@ void DeviceSolver::upload_tables() {
     C.flux = dalloc<double>(3 * static_cast<size_t>(ncells_));
     C.cell_stats = dalloc<double>(4 * static_cast<size_t>(ncells_));
     C.cell_final = dalloc<double>(4 * static_cast<size_t>(ncells_));
-    const MaterialTables& M0 = P_.mats[0];
     if (rta) {
-        // class CSR of material 0 for the RTA solve
-        C.n_classes = M0.n_classes;
-        C.cls_sum = dalloc<double>(static_cast<size_t>(ncells_) * M0.n_classes * 3);
-        C.rta_ab = dalloc<double2>(static_cast<size_t>(ncells_) * M0.n_classes);
+        // per-cell class sums; the stride is the largest class count of the materials
+        int max_classes = 0;
+        for (const auto& M : P_.mats) max_classes = std::max(max_classes, M.n_classes);
+        C.n_classes = max_classes;
+        C.cls_sum = dalloc<double>(static_cast<size_t>(ncells_) * max_classes * 3);
+        C.rta_ab = dalloc<double2>(static_cast<size_t>(ncells_) * max_classes);
     } else {
-        if (P_.mats.size() != 1) throw std::runtime_error("Linear-response collisions support one material in this build.");
         C.lin_beta = dalloc<double>(hist);
         const int S = std::max(1, static_cast<int>(std::ceil(cfg_.time_step * r_max)));
         const double h = cfg_.time_step / S;
@@ -335,50 +352,52 @@ void DeviceSolver::upload_tables() {
         C.lin_substeps = S;
         C.lin_h = h;
         C.lin_terms = std::max(1, K);
-        std::vector<double> decay(M0.n_active), sc(M0.n_active), srn(M0.n_active), srr(M0.n_active);
+        // per-mode constants of every material at offset material * hist_modes
+        const size_t nmat = P_.mats.size(), hm = static_cast<size_t>(hist_modes);
+        std::vector<double> decay(nmat * hm, 1.0), sc(nmat * hm, 0.0), srn(nmat * hm, 0.0), srr(nmat * hm, 0.0);
+        std::vector<float> inv_s(nmat * hm, 0.0f), rate(nmat * hm, 0.0f), dec(nmat * hm, 1.0f), soh(nmat * hm, 0.0f),
+            basis(nmat * 5 * hm, 0.0f), rn(nmat * hm, 0.0f), rr(nmat * hm, 0.0f);
+        std::vector<double> omd(nmat * hm, 0.0), bg(nmat * hm, 0.0);
         bool has_normal = false;
-        for (int a = 0; a < M0.n_active; ++a) {
-            decay[a] = std::exp(-(M0.col_normal[a] + M0.col_resistive[a]) * cfg_.time_step);
-            sc[a] = std::sqrt(M0.col_capacity[a]);
-            srn[a] = std::sqrt(M0.col_normal[a]);
-            srr[a] = std::sqrt(M0.col_resistive[a]);
-            has_normal = has_normal || M0.col_normal[a] > 0.0;
+        for (size_t mi = 0; mi < nmat; ++mi) {
+            const MaterialTables& Mt = P_.mats[mi];
+            const size_t o = mi * hm;
+            for (int a = 0; a < Mt.n_active; ++a) {
+                decay[o + a] = std::exp(-(Mt.col_normal[a] + Mt.col_resistive[a]) * cfg_.time_step);
+                sc[o + a] = std::sqrt(Mt.col_capacity[a]);
+                srn[o + a] = std::sqrt(Mt.col_normal[a]);
+                srr[o + a] = std::sqrt(Mt.col_resistive[a]);
+                has_normal = has_normal || Mt.col_normal[a] > 0.0;
+                const double hw = Mt.hw[a];
+                inv_s[o + a] = sc[o + a] > 0.0 ? static_cast<float>(1.0 / sc[o + a]) : 0.0f;
+                rate[o + a] = static_cast<float>(Mt.col_normal[a] + Mt.col_resistive[a]);
+                dec[o + a] = static_cast<float>(decay[o + a]);
+                soh[o + a] = hw > 0.0 ? static_cast<float>(sc[o + a] / hw) : 0.0f;
+                basis[(mi * 5) * hm + a] = static_cast<float>(sc[o + a] * srr[o + a]);
+                for (int b = 0; b < 4; ++b) {
+                    const double kb = b == 0 ? 1.0 : (Mt.omega[a] != 0.0 ? Mt.col_k[3 * a + b - 1] / Mt.omega[a] : 0.0);
+                    basis[(mi * 5 + 1 + b) * hm + a] = static_cast<float>(sc[o + a] * kb * srn[o + a]);
+                }
+                rn[o + a] = static_cast<float>(srn[o + a]);
+                rr[o + a] = static_cast<float>(srr[o + a]);
+                omd[o + a] = 1.0 - decay[o + a];
+                bg[o + a] = omd[o + a] * Mt.nbg[a];
+            }
         }
         C.lin_decay = upload(decay);
         C.lin_s = upload(sc);
         C.lin_sqrt_rn = upload(srn);
         C.lin_sqrt_rr = upload(srr);
         C.lin_has_normal = has_normal ? 1 : 0;
-        {
-            const int na = M0.n_active;
-            std::vector<float> inv_s(na), rate(na), dec(na), soh(na), basis(5 * static_cast<size_t>(na)), rn(na), rr(na);
-            std::vector<double> omd(na), bg(na);
-            for (int a = 0; a < na; ++a) {
-                const double hw = M0.hw[a];
-                inv_s[a] = sc[a] > 0.0 ? static_cast<float>(1.0 / sc[a]) : 0.0f;
-                rate[a] = static_cast<float>(M0.col_normal[a] + M0.col_resistive[a]);
-                dec[a] = static_cast<float>(decay[a]);
-                soh[a] = hw > 0.0 ? static_cast<float>(sc[a] / hw) : 0.0f;
-                basis[a] = static_cast<float>(sc[a] * srr[a]);
-                for (int b = 0; b < 4; ++b) {
-                    const double kb = b == 0 ? 1.0 : (M0.omega[a] != 0.0 ? M0.col_k[3 * a + b - 1] / M0.omega[a] : 0.0);
-                    basis[(1 + b) * static_cast<size_t>(na) + a] = static_cast<float>(sc[a] * kb * srn[a]);
-                }
-                rn[a] = static_cast<float>(srn[a]);
-                rr[a] = static_cast<float>(srr[a]);
-                omd[a] = 1.0 - decay[a];
-                bg[a] = omd[a] * M0.nbg[a];
-            }
-            C.lin32_inv_s = upload(inv_s);
-            C.lin32_rate = upload(rate);
-            C.lin32_decay = upload(dec);
-            C.lin32_s_over_hw = upload(soh);
-            C.lin32_basis = upload(basis);
-            C.lin32_sqrt_rn = upload(rn);
-            C.lin32_sqrt_rr = upload(rr);
-            C.lin_omd = upload(omd);
-            C.lin_bg = upload(bg);
-        }
+        C.lin32_inv_s = upload(inv_s);
+        C.lin32_rate = upload(rate);
+        C.lin32_decay = upload(dec);
+        C.lin32_s_over_hw = upload(soh);
+        C.lin32_basis = upload(basis);
+        C.lin32_sqrt_rn = upload(rn);
+        C.lin32_sqrt_rr = upload(rr);
+        C.lin_omd = upload(omd);
+        C.lin_bg = upload(bg);
         C.lin_cluster = linear_cluster_size(C, mixed_);
         if (C.lin_cluster == 0) throw std::runtime_error("Too many modes per cell for the cluster exponential.");
         prepare_linear_solve(C);
@@ -666,6 +685,9 @@ void DeviceSolver::read_stats(phmc_stats& o) {
     o.average_heat_flux_along_axis = avg_flux_;
     o.kappa_fit = kappa_fit_;
     o.kappa_endpoints = kappa_end_;
+    o.interface_events = static_cast<int64_t>(L.total_iface_events);
+    o.interface_transmitted = static_cast<int64_t>(L.total_iface_transmitted);
+    o.interface_reflected = static_cast<int64_t>(L.total_iface_reflected);
     o.device_launches = counters_.launches;
 }
 

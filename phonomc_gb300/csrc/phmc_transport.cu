@@ -18,6 +18,7 @@ struct BlockLedger {
     unsigned long long drive_updates;
     unsigned int absorbed;
     unsigned int absorbed_res[kMaxReservoirs];
+    unsigned int iface_events, iface_transmitted, iface_reflected;
 };
 
 __device__ __forceinline__ void block_ledger_init(BlockLedger* b) {
@@ -28,6 +29,7 @@ __device__ __forceinline__ void block_ledger_init(BlockLedger* b) {
         b->drive_updates = 0;
         b->absorbed = 0;
         for (int r = 0; r < kMaxReservoirs; ++r) b->absorbed_res[r] = 0;
+        b->iface_events = b->iface_transmitted = b->iface_reflected = 0;
     }
 }
 
@@ -44,40 +46,112 @@ __device__ __forceinline__ void block_ledger_flush(BlockLedger* b, DevLedger* L)
             atomicAdd(&L->step_drive_updates, b->drive_updates);
         }
         if (b->injected_ev != 0.0) atomicAdd(&L->step_injected_ev, b->injected_ev);
+        if (b->iface_events) {
+            atomicAdd(&L->total_iface_events, static_cast<unsigned long long>(b->iface_events));
+            atomicAdd(&L->total_iface_transmitted, static_cast<unsigned long long>(b->iface_transmitted));
+            atomicAdd(&L->total_iface_reflected, static_cast<unsigned long long>(b->iface_reflected));
+        }
     }
 }
 
-// One carrier's flight for `remaining` ps. Position, mode word and occupation
-// live in registers; returns false when the carrier was absorbed.
+__device__ __forceinline__ double axis_of(const double v[3], int axis) {
+    return axis == 0 ? v[0] : (axis == 1 ? v[1] : v[2]);
+}
+
+// src/solver/LayeredMaterialLayout.cpp:31-60: time to the next material plane
+// in the direction of travel (infinite when none or not ahead by > 1e-14 ps).
+__device__ __forceinline__ double next_crossing_dev(const DevDomain& D, int n_materials, const double p[3],
+                                                    const double v[3], int current, int& destination) {
+    destination = -1;
+    const double inf = __longlong_as_double(0x7ff0000000000000LL);
+    if (n_materials <= 1) return inf;
+    const double va = axis_of(v, D.layout_axis);
+    if (fabs(va) <= 1e-18) return inf;
+    double plane;
+    int dest;
+    if (va > 0.0 && current + 1 < n_materials) {
+        plane = D.planes[current];
+        dest = current + 1;
+    } else if (va < 0.0 && current > 0) {
+        plane = D.planes[current - 1];
+        dest = current - 1;
+    } else {
+        return inf;
+    }
+    const double time = __dadd_rn(plane, -axis_of(p, D.layout_axis)) / va;
+    if (!isfinite(time) || time <= 1e-14) return inf;
+    destination = dest;
+    return time;
+}
+
+__device__ __forceinline__ void count_interface(BlockLedger* bl, const IfaceOut& r) {
+    atomicAdd(&bl->iface_events, 1u);
+    if (r.action == 4) atomicAdd(&bl->iface_transmitted, 1u);
+    else if (r.action == 3) atomicAdd(&bl->iface_reflected, 1u);
+}
+
+// One carrier's flight for `remaining` ps (src/solver/TransportOperator.cpp:405-466).
+// Position, mode word and occupation live in registers; returns false when the
+// carrier was absorbed.
 __device__ bool advance_carrier(const DevTables& T, DevLedger* L, BlockLedger* bl, int slot, double p[3],
                                 uint32_t& w, double& occ, double remaining, uint32_t purpose, uint32_t step) {
     const DevDomain& D = T.dom;
     const DevParams& P = T.par;
-    const int mid = static_cast<int>(w >> 28);
-    const DevMaterial& M = T.mat[mid];
+    int mid = static_cast<int>(w >> 28);
+    const DevMaterial* M = &T.mat[mid];
     double v[3];
-    mode_velocity(M, w, v);
+    mode_velocity(*M, w, v);
     double cp[3], t;
     int f;
-    if (!cache_hit(D, P, p, v, M.speed[w & 0x00FFFFFFu], cp, t, f)) {
+    if (!cache_hit(D, P, p, v, M->speed[w & 0x00FFFFFFu], cp, t, f)) {
         raise_error(L, kErrIntersection, slot);
         return true;
     }
     int event = 0;
     for (; remaining > 1e-14 && event < 64; ++event) {
-        if (!isfinite(t) || t > remaining) {
+        int destination = -1;
+        const double t_cross = next_crossing_dev(D, P.n_materials, p, v, mid, destination);
+        const double t_event = t_cross < t ? t_cross : t;
+        if (!isfinite(t_event) || t_event > remaining) {
 #pragma unroll
             for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], remaining));
             return true;
         }
-        remaining -= fmax(0.0, t);
+        // the outer wall wins exact ties
+        const bool interface_first = t_cross < t;
+        remaining -= fmax(0.0, t_event);
+        const int ai = static_cast<int>(w & 0x00FFFFFFu);
+        if (interface_first) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], t_cross));
+            const Uniform2 d0 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose, static_cast<uint32_t>(event), 0);
+            const Uniform2 d1 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose, static_cast<uint32_t>(event), 1);
+            const IfaceOut r = interface_dev(T, mid, ai, (w >> 24) & 7u, occ, destination, d0.a, d0.b, d1.a);
+            count_interface(bl, r);
+            if (r.action == 5) {
+                raise_error(L, kErrModeMapping, slot);
+                return true;
+            }
+            w = static_cast<uint32_t>(r.active) | (r.signs << 24) | (static_cast<uint32_t>(r.material) << 28);
+            occ = r.occ;
+            mid = r.material;
+            M = &T.mat[mid];
+            mode_velocity(*M, w, v);
+            const double s = M->push[r.active];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], s));
+            if (!cache_hit(D, P, p, v, M->speed[w & 0x00FFFFFFu], cp, t, f)) {
+                raise_error(L, kErrIntersection, slot);
+                return true;
+            }
+            continue;
+        }
 #pragma unroll
         for (int a = 0; a < 3; ++a) p[a] = cp[a];
         const int axis = f >> 1;
         const char cond = D.cond[f];
-        const int ai = static_cast<int>(w & 0x00FFFFFFu);
         if (cond == 'T') {
-            const double e = dmul(dmul(M.hw[ai], occ - M.nbg[ai]), M.energy_weight);
+            const double e = dmul(dmul(M->hw[ai], occ - M->nbg[ai]), M->energy_weight);
             atomicAdd(&bl->absorbed, 1u);
             atomicAdd(&bl->absorbed_ev, e);
             const int r = D.reservoir[f];
@@ -99,13 +173,13 @@ __device__ bool advance_carrier(const DevTables& T, DevLedger* L, BlockLedger* b
                 const Uniform2 d1 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose,
                                              static_cast<uint32_t>(event), 1);
                 double n_out;
-                const int out = rough_sample_dev(T.rough[table], M, ai, occ, P.conservative != 0, d0.a, d0.b, d1.a,
+                const int out = rough_sample_dev(T.rough[table], *M, ai, occ, P.conservative != 0, d0.a, d0.b, d1.a,
                                                  n_out);
                 const double nsign = (f & 1) ? 1.0 : -1.0;
-                const double vn = M.vel[3 * out + axis] * nsign;
+                const double vn = M->vel[3 * out + axis] * nsign;
                 uint32_t signs = 0;
                 if (P.conservative) {
-                    if (!isfinite(n_out) || !(M.omega[out] > 0.0) || !(vn < 0.0)) {
+                    if (!isfinite(n_out) || !(M->omega[out] > 0.0) || !(vn < 0.0)) {
                         raise_error(L, kErrModeMapping, slot);
                         return true;
                     }
@@ -121,18 +195,18 @@ __device__ bool advance_carrier(const DevTables& T, DevLedger* L, BlockLedger* b
                 w ^= 1u << (24 + axis);
             }
         }
-        mode_velocity(M, w, v);
-        const double s = M.push[w & 0x00FFFFFFu];
+        mode_velocity(*M, w, v);
+        const double s = M->push[w & 0x00FFFFFFu];
 #pragma unroll
         for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], s));
-        if (!cache_hit(D, P, p, v, M.speed[w & 0x00FFFFFFu], cp, t, f)) {
+        if (!cache_hit(D, P, p, v, M->speed[w & 0x00FFFFFFu], cp, t, f)) {
             raise_error(L, kErrIntersection, slot);
             return true;
         }
         if (t < 1e-12) {
 #pragma unroll
             for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], 1e-12));
-            if (!cache_hit(D, P, p, v, M.speed[w & 0x00FFFFFFu], cp, t, f)) {
+            if (!cache_hit(D, P, p, v, M->speed[w & 0x00FFFFFFu], cp, t, f)) {
                 raise_error(L, kErrIntersection, slot);
                 return true;
             }
@@ -245,24 +319,55 @@ __device__ __forceinline__ bool wall_sample_mixed(const DevTables& T, DevLedger*
 }
 
 enum FlightEnd { kFlightDone = 0, kFlightAbsorbed = 1, kFlightDeferred = 2 };
+constexpr int kDeferInterface = 8; // queued plane code 8 + destination material: an interface event
+
+__device__ __forceinline__ float axis_of(const float v[3], int axis) {
+    return axis == 0 ? v[0] : (axis == 1 ? v[1] : v[2]);
+}
+
+// Diffuse-mismatch interface event of the FP32 flight (same draws as the FP64
+// flight: keyed by slot, step, purpose and event). False on an invalid
+// outgoing mode (error raised).
+__device__ __forceinline__ bool interface_step_mixed(const DevTables& T, DevLedger* L, BlockLedger* bl, int slot,
+                                                     int destination, uint32_t& w, double& occ, int event,
+                                                     uint32_t purpose, uint32_t step) {
+    const DevParams& P = T.par;
+    const Uniform2 d0 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose, static_cast<uint32_t>(event), 0);
+    const Uniform2 d1 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose, static_cast<uint32_t>(event), 1);
+    const IfaceOut r = interface_dev(T, static_cast<int>(w >> 28), static_cast<int>(w & 0x00FFFFFFu), (w >> 24) & 7u,
+                                     occ, destination, d0.a, d0.b, d1.a);
+    count_interface(bl, r);
+    if (r.action == 5) {
+        raise_error(L, kErrModeMapping, slot);
+        return false;
+    }
+    w = static_cast<uint32_t>(r.active) | (r.signs << 24) | (static_cast<uint32_t>(r.material) << 28);
+    occ = r.occ;
+    return true;
+}
 
 // Free flight in FP32 in the frame of the starting cell. Walls are hit
 // exactly (the coordinate is set to the wall), so no push-off distance is
-// needed; periodic faces map the coordinate to the opposite wall. With kDefer
-// the flight stops at a wall that needs table sampling and reports the wall
-// (plane), the time left and the event index, so that the few carriers that
-// sample a wall are finished together by k_deferred instead of stalling the
-// whole warp on the long sampling path.
+// needed; periodic faces map the coordinate to the opposite wall; material
+// planes (cell boundaries) are hit exactly the same way, and the plane ahead
+// is chosen from the carrier's own layer and direction, so a carrier leaving
+// a plane never re-crosses it. With kDefer the flight stops at a wall that
+// needs table sampling, or at a material plane, and reports it (plane), the
+// time left and the event index, so that the few carriers with such events
+// are finished together by k_deferred instead of stalling the whole warp on
+// the long FP64 sampling path.
 template <bool kDefer>
 __device__ __forceinline__ int advance_mixed(const DevTables& T, DevLedger* L, BlockLedger* bl, int slot,
                                              const Frame& F, float p[3], uint32_t& w, double& occ, float& remaining,
                                              int& event, int& plane_out, uint32_t purpose, uint32_t step) {
     const DevDomain& D = T.dom;
     const DevParams& P = T.par;
-    const int mid = static_cast<int>(w >> 28);
-    const DevMaterial& M = T.mat[mid];
+    int mid = static_cast<int>(w >> 28);
+    const DevMaterial* M = &T.mat[mid];
+    const int nmat = P.n_materials;
+    const int lax = D.layout_axis;
     float v[3], iv[3];
-    mode_velocity32(M, w, v, iv);
+    mode_velocity32(*M, w, v, iv);
     for (; remaining > 0.0f && event < 64; ++event) {
         float t = __int_as_float(0x7f800000);
         int plane = -1;
@@ -276,12 +381,50 @@ __device__ __forceinline__ int advance_mixed(const DevTables& T, DevLedger* L, B
                 plane = 2 * a + (up ? 1 : 0);
             }
         }
-        if (plane < 0 || t > remaining) {
+        // material plane ahead (src/solver/LayeredMaterialLayout.cpp:31-60); the wall wins ties
+        float t_if = __int_as_float(0x7f800000);
+        float plane_at = 0.0f;
+        int destination = -1;
+        if (nmat > 1) {
+            const float va = axis_of(v, lax);
+            int k = -1;
+            if (va > 0.0f && mid + 1 < nmat) k = mid;
+            else if (va < 0.0f && mid > 0) k = mid - 1;
+            if (k >= 0) {
+                const int fi = lax == 0 ? F.i[0] : (lax == 1 ? F.i[1] : F.i[2]);
+                const float cs = lax == 0 ? F.cs[0] : (lax == 1 ? F.cs[1] : F.cs[2]);
+                plane_at = static_cast<float>(D.plane_cell[k] - fi) * cs;
+                const float h = (plane_at - axis_of(p, lax)) * axis_of(iv, lax);
+                if (h >= 0.0f) {
+                    t_if = h;
+                    destination = va > 0.0f ? mid + 1 : mid - 1;
+                }
+            }
+        }
+        const bool interface_first = destination >= 0 && t_if < t;
+        const float t_event = interface_first ? t_if : t;
+        if ((plane < 0 && !interface_first) || t_event > remaining) {
 #pragma unroll
             for (int a = 0; a < 3; ++a) p[a] = fmaf(v[a], remaining, p[a]);
             return kFlightDone;
         }
-        remaining -= t;
+        remaining -= t_event;
+        if (interface_first) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                p[a] = fmaf(v[a], t_event, p[a]);
+                if (a == lax) p[a] = plane_at;
+            }
+            if (kDefer) {
+                plane_out = kDeferInterface + destination;
+                return kFlightDeferred;
+            }
+            if (!interface_step_mixed(T, L, bl, slot, destination, w, occ, event, purpose, step)) return kFlightDone;
+            mid = static_cast<int>(w >> 28);
+            M = &T.mat[mid];
+            mode_velocity32(*M, w, v, iv);
+            continue;
+        }
         const int axis = plane >> 1;
         const bool hi_side = (plane & 1) != 0;
         // the hit coordinate lands on the wall (selects keep p and F in registers)
@@ -293,7 +436,7 @@ __device__ __forceinline__ int advance_mixed(const DevTables& T, DevLedger* L, B
         const char cond = D.cond[plane];
         if (cond == 'T') {
             const int ai = static_cast<int>(w & 0x00FFFFFFu);
-            const double e = M.hw[ai] * (occ - M.nbg[ai]) * M.energy_weight;
+            const double e = M->hw[ai] * (occ - M->nbg[ai]) * M->energy_weight;
             atomicAdd(&bl->absorbed, 1u);
             atomicAdd(&bl->absorbed_ev, e);
             const int r = D.reservoir[plane];
@@ -318,7 +461,7 @@ __device__ __forceinline__ int advance_mixed(const DevTables& T, DevLedger* L, B
         } else {
             w ^= 1u << (24 + axis);
         }
-        mode_velocity32(M, w, v, iv);
+        mode_velocity32(*M, w, v, iv);
     }
     if (remaining > 0.0f) raise_error(L, kErrTooManyEvents, slot);
     return kFlightDone;
@@ -338,13 +481,36 @@ __device__ __forceinline__ int settle_mixed(const DevDomain& D, const Frame& F, 
 }
 
 // ------------------------------------------------------ transport pass
+// New cell of an FP32 flight; a carrier that ends exactly on a material plane
+// (a cell boundary) is given the cell of its own layer.
+__device__ __forceinline__ int settle_layer(const DevTables& T, const CellArrays& C, const Frame& F, float p[3],
+                                           int mid) {
+    int c = settle_mixed(T.dom, F, p);
+    if (T.par.n_materials > 1 && C.cell_material[c] != mid) {
+        const DevDomain& D = T.dom;
+        const int lax = D.layout_axis;
+        const int nyz = D.shape[1] * D.shape[2];
+        const int stride = lax == 0 ? nyz : (lax == 1 ? D.shape[2] : 1);
+        const int idx = lax == 0 ? c / nyz : (lax == 1 ? (c / D.shape[2]) % D.shape[1] : c % D.shape[2]);
+        const int n_axis = lax == 0 ? D.shape[0] : (lax == 1 ? D.shape[1] : D.shape[2]);
+        const int dir = mid > C.cell_material[c] ? 1 : -1;
+        if (idx + dir >= 0 && idx + dir < n_axis && C.cell_material[c + dir * stride] == mid) {
+            c += dir * stride;
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                if (a == lax) p[a] -= static_cast<float>(dir) * F.cs[a];
+        }
+    }
+    return c;
+}
+
 // Common end of a carrier's step: store the state; a live carrier takes its
 // new cell and enters the bins.
 template <bool kRta>
 __device__ __forceinline__ void finish_mixed(const DevTables& T, const CarrierState& S, const CellArrays& C,
                                              DevLedger* L, int i, const Frame& F, float p[3], uint32_t w, double occ,
                                              bool alive) {
-    const int c = settle_mixed(T.dom, F, p);
+    const int c = settle_layer(T, C, F, p, static_cast<int>(w >> 28));
     __stcs(S.ox + i, p[0]);
     __stcs(S.oy + i, p[1]);
     __stcs(S.oz + i, p[2]);
@@ -485,7 +651,12 @@ __global__ void __launch_bounds__(kTransportThreads) k_deferred(const __grid_con
         const Frame F = cell_frame(T.dom, S.cell[i]);
         float p[3] = {S.ox[i], S.oy[i], S.oz[i]};
         int end = kFlightDone;
-        if (plane >= 0 && plane < 6 && wall_sample_mixed(T, L, i, plane, w, occ, event, kDrawTransport, step)) {
+        bool resumed = false;
+        if (plane >= kDeferInterface && plane < kDeferInterface + kMaxMaterials)
+            resumed = interface_step_mixed(T, L, &bl, i, plane - kDeferInterface, w, occ, event, kDrawTransport, step);
+        else if (plane >= 0 && plane < 6)
+            resumed = wall_sample_mixed(T, L, i, plane, w, occ, event, kDrawTransport, step);
+        if (resumed) {
             ++event;
             int unused = -1;
             end = advance_mixed<false>(T, L, &bl, i, F, p, w, occ, remaining, event, unused, kDrawTransport, step);
@@ -753,7 +924,7 @@ __global__ void __launch_bounds__(256) k_inject(const DevTables* __restrict__ Tp
                 alive = advance_mixed<false>(T, L, &bl, slot, F, q, w, occ, rem, event, plane, kDrawInjected, step) !=
                         kFlightAbsorbed;
             }
-            c = settle_mixed(T.dom, F, q);
+            c = settle_layer(T, C, F, q, static_cast<int>(w >> 28));
             S.ox[slot] = q[0];
             S.oy[slot] = q[1];
             S.oz[slot] = q[2];

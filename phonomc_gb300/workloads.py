@@ -7,7 +7,13 @@ inplane_gradient   100 nm film, periodic in x/y, rough z walls (1 nm RMS),
                    periodic-gradient drive G = 1e7 K/m along x, 100 z-cells,
                    linearized RTA at 300 K, 5e7 carriers, dt = 0.5 ps.
 
-The lateral repeat cell is 100 nm x 100 nm in both. `scaled()` keeps the
+bilayer_callaway  200 nm stack of two materials (the second with 0.7x
+                   frequencies and 0.75x velocities), interface at 100 nm,
+                   diffuse-mismatch interface, linearized Callaway collisions,
+                   reservoirs 310/290 K on the z faces, 100 z-cells, 1e8
+                   carriers, dt = 0.5 ps.
+
+The lateral repeat cell is 100 nm x 100 nm in all three. `scaled()` keeps the
 geometry and physics and shrinks the carrier count for tests.
 """
 
@@ -58,6 +64,37 @@ def inplane_gradient(particles: float = 5e7, seed: int = 12345, precision: str =
         "face_values": (0, 0, 0, 0, 1.0, 1.0),
         "precision": precision,
     }
+
+
+def bilayer_callaway(particles: float = 1e8, seed: int = 12345, precision: str = "fp64") -> dict:
+    return {
+        "name": "bilayer_callaway",
+        "sizes": (LATERAL_A, LATERAL_A, 2.0 * THICKNESS_A),
+        "particle_count": particles,
+        "time_step": 0.5,
+        "iterations": 3000,
+        "random_seed": seed,
+        "compute_kappa": True,
+        "transport_axis": 2,
+        "background_temperature": 300.0,
+        "lifetime_temperature": 300.0,
+        "initial_temperature": "linear",
+        "grid": (1, 1, 100),
+        "faces": ("P", "P", "P", "P", "T", "T"),
+        "face_values": (0, 0, 0, 0, 310.0, 290.0),
+        "collision_model": "callaway",
+        "material_interface_axis": 2,
+        "material_interface_positions": [THICKNESS_A],
+        "interface_frequency_bin_thz": 0.1,
+        "precision": precision,
+    }
+
+
+def bilayer_materials(mesh: int = 16):
+    """The two synthetic materials of the bilayer (Callaway linewidth split)."""
+    from . import synthetic
+    return [synthetic.make_material(mesh=mesh, callaway=True),
+            synthetic.make_material(mesh=mesh, freq_scale=0.7, vel_scale=0.75, callaway=True)]
 
 
 def scaled(cfg: dict, particles: float, **over) -> dict:

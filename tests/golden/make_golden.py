@@ -41,6 +41,8 @@ CASES = {
     "rough_conservative": ["rough", "{m}", "1"],
     "gradient_drive": ["gradient", "{m}"],
     "reservoir": ["reservoir", "{m}"],
+    "interface_dmm": ["interface", "{m}", "{s}", "0"],
+    "interface_dmm_linearized": ["interface", "{m}", "{s}", "1"],
 }
 
 
@@ -127,6 +129,8 @@ def main() -> None:
     cpath = os.path.join(tmp, "m8c.pmat")
     synthetic.write_pmat(mpath, synthetic.make_material(mesh=8))
     synthetic.write_pmat(cpath, synthetic.make_material(mesh=8, callaway=True))
+    spath = os.path.join(tmp, "m8s.pmat")
+    synthetic.write_pmat(spath, synthetic.make_material(mesh=8, freq_scale=0.7, vel_scale=0.75))
     if not args.only or "fullrun_cross_plane" in args.only:
         m16 = os.path.join(tmp, "m16.pmat")
         synthetic.write_pmat(m16, synthetic.make_material(mesh=16))
@@ -138,7 +142,7 @@ def main() -> None:
     for name, argv in CASES.items():
         if args.only and name not in args.only:
             continue
-        cmd = [HARNESS] + [a.format(m=mpath, c=cpath) for a in argv]
+        cmd = [HARNESS] + [a.format(m=mpath, c=cpath, s=spath) for a in argv]
         out = subprocess.run(cmd, check=True, capture_output=True, text=True).stdout
         data = json.loads(out)
         data["_harness_args"] = argv

@@ -311,3 +311,68 @@ def test_registered_host_ingest_matches_copy_path(gpu, precision):
     # bin sums are FP64 atomics in arrival order: collisions agree to round-off
     assert np.allclose(ca["occ"], cb["occ"], rtol=1e-12, atol=1e-15)
     assert np.allclose(a.cells()[0], b.cells()[0], rtol=1e-12, atol=0)
+
+
+# ------------------------------------------------------------ layered materials
+@pytest.mark.parametrize("name,linearized", [("interface_dmm", 0), ("interface_dmm_linearized", 1)])
+def test_interface_golden(gpu, name, linearized):
+    g = golden(name)
+    ma = abi.Material(gpu, "phmc_", synthetic.make_material(mesh=8), 0.1, False, False)
+    mb = abi.Material(gpu, "phmc_", synthetic.make_material(mesh=8, freq_scale=0.7, vel_scale=0.75), 0.1, False,
+                      False)
+    n = len(g["src"])
+    src, flat, signs = (_i32(g[k]) for k in ("src", "in_flat", "in_signs"))
+    occ, u3 = _f64(g["in_occ"]), _f64(g["draws"])
+    act, mat, fo, so = (np.zeros(n, np.int32) for _ in range(4))
+    oo = np.zeros(n)
+    rc = gpu.phmc_dev_interface(ma.h, mb.h, g["weight_a"], g["weight_b"], g["axis"], g["frequency_bin_thz"],
+                                g["reference_temperature"], linearized, n, I32(src), I32(flat), I32(signs), D(occ),
+                                D(u3), I32(act), I32(mat), I32(fo), I32(so), D(oo))
+    assert rc == 0, gpu.phmc_last_error()
+    assert np.array_equal(act, g["action"])
+    assert np.array_equal(mat, g["out_material"])
+    assert np.array_equal(fo, g["out_flat"])
+    assert np.array_equal(oo, np.asarray(g["out_occ"]))
+
+
+def _bilayer_pair(gpu, orc, particles, seed, precision="fp64"):
+    cfg = workloads.scaled(workloads.bilayer_callaway(), particles, random_seed=seed, precision=precision)
+    data = workloads.bilayer_materials(16)
+    mg = [abi.Material(gpu, "phmc_", d, 0.1, True, True) for d in data]
+    mo = [abi.Material(orc, "orc_", d, 0.1, True, True) for d in data]
+    return (abi.Solver(gpu, "phmc_", cfg, mg), mg), (abi.Solver(orc, "orc_", cfg, mo), mo)
+
+
+def test_bilayer_steps_match_oracle(gpu, orc):
+    """Two materials, diffuse-mismatch interface, linearized Callaway, reservoirs:
+    whole steps on the device against the oracle, interface counters exact."""
+    (sg, _), (so, _) = _bilayer_pair(gpu, orc, 20000, 31)
+    _compare(sg, so, tol=1e-11)
+    for _ in range(3):
+        sg.run(2)
+        so.run(2)
+        stg, sto = _compare(sg, so, tol=1e-11)
+        for k in ("interface_events", "interface_transmitted", "interface_reflected"):
+            assert stg[k] == sto[k], k
+    assert sto["interface_events"] > 0 and sto["interface_transmitted"] > 0
+
+
+def test_mixed_bilayer_conserves_energy_and_tracks_plain(gpu):
+    cfg = workloads.scaled(workloads.bilayer_callaway(), 200000, random_seed=37)
+    data = workloads.bilayer_materials(16)
+    m = [abi.Material(gpu, "phmc_", d, 0.1, True, True) for d in data]
+    sp = abi.Solver(gpu, "phmc_", dict(cfg, precision="fp64"), m)
+    sm = abi.Solver(gpu, "phmc_", dict(cfg, precision="mixed"), m)
+    sp.run(6)
+    sm.run(6)
+    st = sm.stats()
+    scale = abs(st["total_thermal_energy_ev"])
+    assert abs(st["step_lifetime_energy_residual_ev"]) < 1e-13 * scale
+    assert abs(st["step_energy_balance_residual_ev"]) < 1e-12 * scale
+    assert st["interface_events"] > 0
+    Tp, _, _ = sp.cells()
+    Tm, _, _ = sm.cells()
+    assert np.max(np.abs(Tp - Tm)) < 2e-2
+    cp, cm = sp.carriers(), sm.carriers()
+    a = (cp["alive"] == 1) & (cm["alive"] == 1)
+    assert np.mean(cp["mode"][a] == cm["mode"][a]) > 0.99

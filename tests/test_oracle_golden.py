@@ -185,3 +185,38 @@ def test_reservoir_cdf(oracle_lib, m8):
         idx = np.minimum(idx, active - 1)
         assert np.array_equal(idx, np.asarray(g["active_index"])[r * 300:(r + 1) * 300])
     assert counts == g["initial_count"]
+
+
+@pytest.mark.parametrize("name,linearized", [("interface_dmm", 0), ("interface_dmm_linearized", 1)])
+def test_interface_dmm(oracle_lib, name, linearized):
+    """Diffuse-mismatch interface events against InterfaceInteraction::interact,
+    with the reference engine's draws replayed (bit-exact modes and occupations)."""
+    from phonomc_gb300 import synthetic
+    g = golden(name)
+    ma = abi.Material(oracle_lib, "orc_", synthetic.make_material(mesh=8), 0.1, False, False)
+    mb = abi.Material(oracle_lib, "orc_", synthetic.make_material(mesh=8, freq_scale=0.7, vel_scale=0.75), 0.1,
+                      False, False)
+    n = len(g["src"])
+    src, flat, signs = (np.ascontiguousarray(g[k], dtype=np.int32) for k in ("src", "in_flat", "in_signs"))
+    occ = np.ascontiguousarray(g["in_occ"], dtype=np.float64)
+    u3 = np.ascontiguousarray(g["draws"], dtype=np.float64)
+    act, mat, fo, so = (np.zeros(n, np.int32) for _ in range(4))
+    oo = np.zeros(n)
+    I = lambda a: a.ctypes.data_as(abi.c_int32_p)  # noqa: E731
+    rc = oracle_lib.orc_interface(ma.h, mb.h, g["weight_a"], g["weight_b"], g["axis"], g["frequency_bin_thz"],
+                                  g["reference_temperature"], linearized, n, I(src), I(flat), I(signs), D(occ), D(u3),
+                                  I(act), I(mat), I(fo), I(so), D(oo))
+    assert rc == 0, oracle_lib.orc_last_error()
+    assert np.array_equal(act, g["action"])
+    assert np.array_equal(mat, g["out_material"])
+    assert np.array_equal(fo, g["out_flat"])
+    assert np.array_equal(oo, np.asarray(g["out_occ"]))
+    # velocity: table velocity of the outgoing mode with the outgoing sign bits
+    for k, m in enumerate((ma, mb)):
+        sel = mat == k
+        if not sel.any():
+            continue
+        v = np.array(synthetic.make_material(mesh=8, **({} if k == 0 else {"freq_scale": 0.7, "vel_scale": 0.75}))
+                     .group_velocity).reshape(-1, 3)[fo[sel]]
+        sg = np.stack([1 - 2 * ((so[sel] >> b) & 1) for b in range(3)], axis=1)
+        assert np.array_equal(v * sg, np.asarray(g["out_v"]).reshape(-1, 3)[sel])
