@@ -59,6 +59,34 @@ typedef struct phmc_material_data {
     int64_t gamma_isotope_len;
 } phmc_material_data;
 
+/* Prescribed lattice heat source (include/SimulationConfig.h:103-139; the
+ * [heat_source] table of the reference's TOML), lengths in Angstrom. */
+typedef struct phmc_heat_source {
+    int32_t profile;                 /* 0 uniform region, 1 gaussian */
+    int32_t has_box;                 /* min/max given: uniform region or gaussian clip box */
+    double min[3], max[3];
+    int32_t n_centers;               /* gaussian sources; centers[3*n_centers] */
+    const double* centers;
+    double sigma[3];                 /* <= 0: that axis is uniform */
+    double half_width[3];            /* <= 0: none */
+    double power_density;            /* W/m^3 (0 when total_power is used) */
+    int32_t has_total_power;
+    double total_power;              /* W */
+    int32_t n_power_densities;       /* per-source peak values, W/m^3 */
+    const double* power_densities;
+    int32_t spectrum;                /* 0 thermal, 1 weighted, 2 gaussian */
+    int32_t has_frequency_gaussian;
+    double frequency_center, frequency_sigma; /* THz */
+    double frequency_min, frequency_max;      /* THz, < 0: no cut */
+    int32_t n_branches;
+    const int32_t* branches;
+    int32_t n_branch_weights;
+    const double* branch_weights;
+    int32_t time_profile;            /* 0 constant, 1 pulsed */
+    double time_start, time_end;     /* ps; time_end < 0: no end */
+    double period, on_duration, duty_cycle, amplitude;
+} phmc_heat_source;
+
 /* SimulationConfig fields read by the carrier loop (include/SimulationConfig.h:42-146),
  * in internal units (Angstrom, ps, K). Box faces are in facet order
  * xmin,xmax,ymin,ymax,zmin,zmax with condition 'T','P' or 'R'. */
@@ -90,6 +118,7 @@ typedef struct phmc_config {
     const double* material_interface_positions; /* Angstrom */
     double interface_frequency_bin_thz;
     int32_t precision;               /* 0 = plain FP64 state, 1 = mixed (FP32 transport) */
+    const phmc_heat_source* heat_source; /* NULL: no heat source */
 } phmc_config;
 
 /* Getters of include/MonteCarloSolver.h:59-101 plus the last step's ledger. */
@@ -108,6 +137,10 @@ typedef struct phmc_stats {
     double kappa_fit, kappa_endpoints;
     int64_t interface_events, interface_transmitted, interface_reflected;
     int64_t device_launches;          /* CUDA kernels launched by this solver so far */
+    /* heat source: total_/step_ ledger source energy, prescribed and pending budgets (eV) */
+    double total_heat_source_energy_ev, step_heat_source_energy_ev;
+    double prescribed_heat_source_energy_ev, pending_heat_source_energy_ev;
+    int64_t step_heat_source_updates;
 } phmc_stats;
 
 const char* phmc_last_error(void);

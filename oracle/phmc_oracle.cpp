@@ -387,6 +387,135 @@ InterfaceOutcome interface_interact(const InterfaceTables& I, const std::vector<
     return r;
 }
 
+// src/solver/PhononSourceOperator.cpp:119-340 (non-full-matrix branch): the
+// pending energy of every cell with eligible carriers is given to them in the
+// chosen spectrum, the carrier with the largest energy increment absorbs the
+// round-off, and the cell's budget moves to `deposited`.
+void source_apply_cells(const HeatSourceTables& S, const std::vector<const PhononMaterial*>& mats,
+                    const std::vector<MaterialTables>& tables, const std::vector<int>& cell_material, double Tbg,
+                    const std::vector<std::vector<int>>& members, const std::vector<uint32_t>& mode,
+                    std::vector<double>& occ, const std::vector<double>& cell_T, std::vector<double>& src_pending,
+                    std::vector<double>& src_deposited, long long& updates, double& deposited) {
+    double pending_total = 0.0;
+    for (double e : src_pending) pending_total += e;
+    if (pending_total <= 0.0) return;
+    auto fail = [](const std::string& m) { throw std::runtime_error(m); };
+    for (size_t c = 0; c < members.size(); ++c) {
+        if (src_pending[c] <= 0.0) continue;
+        const int mid = cell_material[c];
+        const PhononMaterial& M = *mats[mid];
+        const MaterialTables& T = tables[mid];
+        std::vector<int> idx;
+        for (int i : members[c]) {
+            if (static_cast<int>(mode[i] >> 28) != mid) fail("Source particle and cell material disagree.");
+            const int a = static_cast<int>(mode[i] & kActiveMask);
+            const double hw = kHbarEvPs * M.omega(T.active_flat[a]);
+            if (std::isfinite(hw) && hw > 1e-14 && S.mode_weight(M, T.active_flat[a]) > 0.0) idx.push_back(i);
+        }
+        if (idx.empty()) continue;
+        const double raw_to_physical = T.energy_weight;
+        const double target = src_pending[c] / raw_to_physical;
+        if (!std::isfinite(target)) fail("Non-finite heat-source energy per carrier.");
+        const size_t n = idx.size();
+        std::vector<double> inc(n);
+        auto flat_of = [&](int i) { return T.active_flat[mode[i] & kActiveMask]; };
+        auto hw_of = [&](int i) { return kHbarEvPs * M.omega(flat_of(i)); };
+        if (S.spectrum == HeatSourceSpectrum::Gaussian) {
+            std::vector<long double> w(n);
+            long double peak = -std::numeric_limits<long double>::infinity();
+            for (size_t k = 0; k < n; ++k) {
+                const long double f = M.omega(flat_of(idx[k])) / 6.283185307179586476925286766559L;
+                const long double z = (f - S.gaussian_center) / S.gaussian_sigma;
+                w[k] = -.5L * z * z;
+                peak = std::max(peak, w[k]);
+            }
+            long double sum = 0;
+            for (auto& x : w) {
+                x = std::exp(x - peak);
+                sum += x;
+            }
+            for (size_t k = 0; k < n; ++k) inc[k] = static_cast<double>(target * w[k] / sum) / hw_of(idx[k]);
+        } else if (S.spectrum == HeatSourceSpectrum::Weighted) {
+            double sum = 0.0;
+            for (int i : idx) sum += S.mode_weight(M, flat_of(i));
+            for (size_t k = 0; k < n; ++k)
+                inc[k] = target * (S.mode_weight(M, flat_of(idx[k])) / sum) / hw_of(idx[k]);
+        } else if (S.linearized_thermal) {
+            long double cap = 0;
+            for (int i : idx) cap += M.mode_heat_capacity(Tbg, flat_of(i));
+            if (!(cap > 0)) fail("Source sample has no thermal capacity.");
+            for (size_t k = 0; k < n; ++k)
+                inc[k] = static_cast<double>(target * M.mode_heat_capacity(Tbg, flat_of(idx[k])) / cap) /
+                         (kHbarEvPs * M.omega(flat_of(idx[k])));
+        } else {
+            const double base = std::isfinite(cell_T[c]) && cell_T[c] >= 0.0 ? cell_T[c] : Tbg;
+            auto energy_at = [&](double temperature, double* slope_out) {
+                double e = 0.0, slope = 0.0;
+                for (int i : idx) {
+                    const int f = flat_of(i);
+                    const double hw = kHbarEvPs * std::max(0.0, M.omega(f));
+                    const double n0 = M.bose_occupation(base, f);
+                    const double nn = M.bose_occupation(temperature, f);
+                    e += hw * (nn - n0);
+                    if (slope_out && temperature > 0.0) slope += hw * (hw * nn * (nn + 1.0) / (kBoltzmannEvK * temperature * temperature));
+                }
+                if (slope_out) *slope_out = slope;
+                return e;
+            };
+            double low = std::max(0.0, base);
+            double high = std::max(low + 1.0, 1.05 * low + 1.0);
+            double high_e = energy_at(high, nullptr);
+            for (int k = 0; high_e < target && k < 60; ++k) {
+                high = 2.0 * high + 1.0;
+                high_e = energy_at(high, nullptr);
+            }
+            if (!(high_e >= target) || !std::isfinite(high_e))
+                fail("Could not bracket the occupation-source pseudo-temperature.");
+            double Ts = 0.5 * (low + high);
+            const double tol = 1e-12 * std::max(1e-6, target);
+            for (int it = 0; it < 60; ++it) {
+                double d = 0.0;
+                const double r = energy_at(Ts, &d) - target;
+                if (std::abs(r) <= tol) break;
+                if (r > 0.0) high = Ts;
+                else low = Ts;
+                double cand = 0.5 * (low + high);
+                if (d > 0.0 && std::isfinite(d)) {
+                    const double nt = Ts - r / d;
+                    if (nt > low && nt < high && std::isfinite(nt)) cand = nt;
+                }
+                Ts = cand;
+            }
+            for (size_t k = 0; k < n; ++k)
+                inc[k] = M.bose_occupation(Ts, flat_of(idx[k])) - M.bose_occupation(base, flat_of(idx[k]));
+        }
+        // round-off correction on the carrier with the largest energy increment
+        double applied = 0.0, largest = -1.0;
+        size_t corr = 0;
+        for (size_t k = 0; k < n; ++k) {
+            const double e = hw_of(idx[k]) * inc[k];
+            applied += e;
+            if (e > largest) {
+                largest = e;
+                corr = k;
+            }
+        }
+        inc[corr] += (target - applied) / hw_of(idx[corr]);
+        for (size_t k = 0; k < n; ++k) {
+            const double next = occ[idx[k]] + inc[k];
+            if (!std::isfinite(inc[k]) || !std::isfinite(next) || next < 0.0)
+                fail("Heat source would produce an invalid occupation; cell budget retained.");
+        }
+        for (size_t k = 0; k < n; ++k) occ[idx[k]] += inc[k];
+        const double e = src_pending[c];
+        src_deposited[c] += e;
+        src_pending[c] = 0.0;
+        deposited += e;
+        updates += static_cast<long long>(n);
+    }
+}
+
+
 // ---------------------------------------------- linearized collision per cell
 // src/solver/CarrierCollisionOperator.cpp:67-126 for one cell.
 long double linear_cell(const std::vector<int>& members, const MaterialTables& T, const std::vector<int>& active_i,
@@ -463,6 +592,9 @@ struct OracleSolver {
         const int nc = domain->grid_count();
         cell_T.assign(nc, 300.0);
         cell_E.assign(nc, 0.0);
+        src_pending.assign(nc, 0.0);
+        src_prescribed.assign(nc, 0.0);
+        src_deposited.assign(nc, 0.0);
         cell_q.assign(nc, {0, 0, 0});
         refresh();
         energy.initialize(total_thermal());
@@ -911,15 +1043,53 @@ struct OracleSolver {
     }
 
     // src/MonteCarloSolver.cpp:348-398
+    // ------------------------------------------------------ heat source
+    std::vector<double> src_pending, src_prescribed, src_deposited;
+
+    // src/solver/PrescribedHeatSource.cpp:218-240
+    void source_accrue(double factor) {
+        if (!std::isfinite(factor) || factor < 0.0)
+            throw std::invalid_argument("Integrated heat-source time must be finite and nonnegative.");
+        for (size_t c = 0; c < P.source.rates.size(); ++c) {
+            const double e = P.source.rates[c] * factor;
+            src_prescribed[c] += e;
+            src_pending[c] += e;
+        }
+    }
+
+    void source_apply(long long& updates, double& deposited) {
+        source_apply_cells(P.source, mats, P.mats, P.cell_material, cfg.background_temperature, members_by_cell(),
+                           mode, occ, cell_T, src_pending, src_deposited, updates, deposited);
+    }
+
+    // src/solver/HeatSourceDriving.cpp:46-80
+    void apply_heat_source(double begin, double end) {
+        if (!P.source.enabled) return;
+        const double factor = heat_source_time_factor(cfg, begin, end);
+        double pending_total = 0.0;
+        for (double e : src_pending) pending_total += e;
+        if (factor <= 0.0 && pending_total <= 0.0) return;
+        source_accrue(factor);
+        long long updates = 0;
+        double e = 0.0;
+        source_apply(updates, e);
+        energy.record_source(updates, e);
+    }
+
     void run_timestep() {
         if (failed) throw std::runtime_error("Cannot resume a failed timestep; construct a new solver after fixing its cause.");
         failed = true;
         energy.begin_step();
         step_b = {};
+        const double midpoint = elapsed + 0.5 * cfg.time_step;
+        const double end = elapsed + cfg.time_step;
+        apply_heat_source(elapsed, midpoint);
+        if (energy.step().source_energy_ev > 0.0) refresh();
         gradient_half();
         transport();
         refresh();
         energy.set_lifetime_residual(collide());
+        apply_heat_source(midpoint, end);
         gradient_half();
         refresh();
         energy.finish_step(total_thermal(), step_b);
@@ -1008,6 +1178,11 @@ int orc_solver_stats(void* sp, phmc_stats* o) {
         o->average_heat_flux_along_axis = s->avg_flux;
         o->kappa_fit = s->kappa_fit;
         o->kappa_endpoints = s->kappa_end;
+        o->total_heat_source_energy_ev = s->energy.total().source_energy_ev;
+        o->step_heat_source_energy_ev = s->energy.step().source_energy_ev;
+        o->step_heat_source_updates = s->energy.step().source_updates;
+        for (double e : s->src_prescribed) o->prescribed_heat_source_energy_ev += e;
+        for (double e : s->src_pending) o->pending_heat_source_energy_ev += e;
         o->interface_events = s->iface_events;
         o->interface_transmitted = s->iface_transmitted;
         o->interface_reflected = s->iface_reflected;
@@ -1197,6 +1372,54 @@ int orc_interface(void* ma, void* mb, double wa, double wb, int axis, double bin
             signs_out[i] = static_cast<int32_t>(r.signs);
             occ_out[i] = r.occ;
         }
+    });
+}
+
+// PrescribedHeatSource cell powers (eV/ps) of a configuration
+// (src/solver/PrescribedHeatSource.cpp:22-216); `rates` has one entry per cell.
+int orc_source_rates(const phmc_config* cfg, double* rates, int* cells) {
+    return guard([&] {
+        const SimulationConfig c = config_from_pod(*cfg);
+        SimulationDomain d(c);
+        HeatSourceTables S;
+        S.configure(c, d);
+        *cells = d.grid_count();
+        for (int k = 0; k < d.grid_count(); ++k) rates[k] = S.enabled ? S.rates[k] : 0.0;
+    });
+}
+
+// PhononSourceOperator::apply on explicit carriers and cell budgets
+// (src/solver/PhononSourceOperator.cpp:119-340); pending is updated in place.
+int orc_source_apply(void* m, const phmc_heat_source* h, int linearized, double Tbg, double particle_volume,
+                     int cells, const double* cell_T, double* pending, int64_t n, const int32_t* flat,
+                     const int32_t* cell, double* occ, double* energy, int64_t* updates) {
+    return guard([&] {
+        const PhononMaterial* M = static_cast<OracleMaterial*>(m)->m.get();
+        SimulationConfig c;
+        heat_source_from_pod(*h, c);
+        if (linearized) c.collision_model = CollisionModel::Callaway;
+        validate_heat_source_config(c);
+        HeatSourceTables S;
+        S.set_spectrum(c);
+        S.enabled = true;
+        std::vector<MaterialTables> T(1);
+        T[0].n_active = M->active_mode_count();
+        T[0].active_flat = M->active_flat();
+        T[0].energy_weight = T[0].n_active * particle_volume / M->energy_density_normalization();
+        std::vector<uint32_t> mode(n);
+        std::vector<double> o(occ, occ + n), cT(cell_T, cell_T + cells), pend(pending, pending + cells), dep(cells, 0.0);
+        std::vector<std::vector<int>> members(cells);
+        for (int64_t i = 0; i < n; ++i) {
+            mode[i] = static_cast<uint32_t>(M->active_index_for_flat(flat[i]));
+            members.at(cell[i]).push_back(static_cast<int>(i));
+        }
+        long long up = 0;
+        double e = 0.0;
+        source_apply_cells(S, {M}, T, std::vector<int>(cells, 0), Tbg, members, mode, o, cT, pend, dep, up, e);
+        std::copy(o.begin(), o.end(), occ);
+        std::copy(pend.begin(), pend.end(), pending);
+        *energy = e;
+        *updates = up;
     });
 }
 

@@ -20,6 +20,8 @@
 #include "solver/CarrierCollisionOperator.h"
 #include "solver/CellParticleIndex.h"
 #include "solver/InterfaceInteraction.h"
+#include "solver/PhononSourceOperator.h"
+#include "solver/PrescribedHeatSource.h"
 #include "solver/ParticleStorage.h"
 #include "solver/ReservoirSampler.h"
 #include "solver/RoughBoundarySampler.h"
@@ -577,6 +579,69 @@ std::string cmd_interface(const std::string& pa, const std::string& pb, bool lin
     return j.str();
 }
 
+// source <pmat> <spectrum 0 thermal|1 weighted|2 gaussian> <linearized>:
+// PrescribedHeatSource cell powers of a Gaussian source in a 2x2x3 box, one
+// accrual, then PhononSourceOperator::apply on random carriers.
+std::string cmd_source(const std::string& pmat, int spectrum, bool linearized) {
+    PhononMaterial m(read_pmat(pmat), 0.1, true, false);
+    auto a = box_config(500, 400, 300, 2, 2, 3, {"P", "P", "P", "P", "T", "T"}, {0, 0, 0, 0, 301, 299}, true, false);
+    a.heat_source_enabled = true;
+    a.heat_source_profile = HeatSourceProfile::Gaussian;
+    a.heat_source_center = {180.0, 130.0, 90.0};
+    a.heat_source_sigma = {160.0, 140.0, 70.0};
+    a.heat_source_power_density = 3e19;
+    if (linearized) a.collision_model = CollisionModel::Callaway;
+    if (spectrum == 1) {
+        a.heat_source_spectrum = HeatSourceSpectrum::Weighted;
+        a.heat_source_branch_weights = {1.0, 2.0, 1.5, 0.5, 0.25, 0.0};
+        a.heat_source_branches = {0, 1, 2, 3, 4};
+    } else if (spectrum == 2) {
+        a.heat_source_spectrum = HeatSourceSpectrum::Gaussian;
+        a.heat_source_frequency_center = 6.0;
+        a.heat_source_frequency_sigma = 2.5;
+    }
+    a.heat_source_frequency_max = 14.0;
+    SimulationDomain d(a);
+    phonomc::PrescribedHeatSource hs;
+    hs.configure(a, d);
+    const int cells = static_cast<int>(d.grid_centers().size());
+    const double factor = 0.37;
+    hs.accrue(factor);
+    const std::vector<double> pending_before = hs.cell_pending_ev();
+    phonomc::PhononSourceOperator op;
+    std::vector<const PhononMaterial*> ms{&m};
+    op.configure(a, ms);
+    std::mt19937_64 rng(61);
+    auto c = random_carriers(m, 4000, cells, 2.0, rng, 300.0);
+    for (size_t i = 0; i < c.cell.size(); ++i)
+        if (c.cell[i] == 1) c.cell[i] = 0; // cell 1 keeps its budget
+    phonomc::ParticleStorage p;
+    fill_storage(p, m, c);
+    phonomc::CellParticleIndex idx;
+    idx.ensure(p, cells);
+    std::vector<int> mats(cells, 0);
+    std::vector<double> cellT(cells);
+    for (int k = 0; k < cells; ++k) cellT[k] = 298.5 + 0.4 * k;
+    const double vol = 7.5;
+    const auto r = op.apply(p, ms, {mats, cellT, &idx}, hs, vol, 300.0);
+    Json j;
+    j.arr("rates", hs.cell_rates_evps());
+    j.put("factor", factor);
+    j.arr("pending_before", pending_before);
+    j.arr("pending_after", hs.cell_pending_ev());
+    j.arr("cell_temperature", cellT);
+    j.put("particle_volume", vol);
+    j.arr("flat", c.flat);
+    j.arr("cell", c.cell);
+    j.arr("occ_in", c.occ);
+    j.arr("occ_out", p.occupation);
+    j.put("energy", r.energy_ev);
+    j.put_i("updates", r.occupation_updates);
+    j.arr3("centers", d.grid_centers());
+    j.arr("volumes", d.grid_volumes());
+    return j.str();
+}
+
 // gradient <pmat>: TemperatureGradientDrive on random carriers in a periodic box.
 std::string cmd_gradient(const std::string& pmat) {
     PhononMaterial m(read_pmat(pmat), 0.1, true, false);
@@ -713,6 +778,7 @@ int main(int argc, char** argv) {
         else if (c == "callaway") out = cmd_callaway();
         else if (c == "rough") out = cmd_rough(argv[2], std::atoi(argv[3]) != 0);
         else if (c == "gradient") out = cmd_gradient(argv[2]);
+        else if (c == "source") out = cmd_source(argv[2], std::atoi(argv[3]), std::atoi(argv[4]) != 0);
         else if (c == "interface") out = cmd_interface(argv[2], argv[3], std::atoi(argv[4]) != 0);
         else if (c == "reservoir") out = cmd_reservoir(argv[2]);
         else if (c == "run") out = cmd_run(argv[2], argv[3], std::atoi(argv[4]));

@@ -30,6 +30,72 @@ class MaterialDataPOD(C.Structure):
     ]
 
 
+class HeatSourcePOD(C.Structure):
+    _fields_ = [
+        ("profile", C.c_int32), ("has_box", C.c_int32), ("min", C.c_double * 3), ("max", C.c_double * 3),
+        ("n_centers", C.c_int32), ("centers", c_double_p), ("sigma", C.c_double * 3), ("half_width", C.c_double * 3),
+        ("power_density", C.c_double), ("has_total_power", C.c_int32), ("total_power", C.c_double),
+        ("n_power_densities", C.c_int32), ("power_densities", c_double_p), ("spectrum", C.c_int32),
+        ("has_frequency_gaussian", C.c_int32), ("frequency_center", C.c_double), ("frequency_sigma", C.c_double),
+        ("frequency_min", C.c_double), ("frequency_max", C.c_double), ("n_branches", C.c_int32),
+        ("branches", c_int32_p), ("n_branch_weights", C.c_int32), ("branch_weights", c_double_p),
+        ("time_profile", C.c_int32), ("time_start", C.c_double), ("time_end", C.c_double), ("period", C.c_double),
+        ("on_duration", C.c_double), ("duty_cycle", C.c_double), ("amplitude", C.c_double),
+    ]
+
+
+def heat_source_pod(h: dict, keep: list) -> HeatSourcePOD:
+    """HeatSourcePOD from a dict of [heat_source] fields (lengths in Angstrom, THz, ps)."""
+    p = HeatSourcePOD()
+    p.profile = 1 if h.get("profile", "uniform") == "gaussian" else 0
+    if "min" in h and "max" in h:
+        p.has_box = 1
+        p.min[:] = list(h["min"])
+        p.max[:] = list(h["max"])
+    centers = h.get("centers") or ([h["center"]] if "center" in h else [])
+    if centers:
+        arr = np.ascontiguousarray(np.asarray(centers, dtype=np.float64).reshape(-1))
+        keep.append(arr)
+        p.n_centers = arr.size // 3
+        p.centers = dptr(arr)
+    p.sigma[:] = list(h.get("sigma", (0.0, 0.0, 0.0)))
+    p.half_width[:] = list(h.get("half_width", (0.0, 0.0, 0.0)))
+    p.power_density = float(h.get("power_density", 0.0))
+    if "total_power" in h:
+        p.has_total_power = 1
+        p.total_power = float(h["total_power"])
+    if "power_densities" in h:
+        arr = np.ascontiguousarray(h["power_densities"], dtype=np.float64)
+        keep.append(arr)
+        p.n_power_densities = arr.size
+        p.power_densities = dptr(arr)
+    p.spectrum = {"thermal": 0, "weighted": 1, "gaussian": 2}[h.get("spectrum", "thermal")]
+    if "frequency_center" in h or "frequency_sigma" in h:
+        p.has_frequency_gaussian = 1
+        p.frequency_center = float(h.get("frequency_center", 0.0))
+        p.frequency_sigma = float(h.get("frequency_sigma", 0.0))
+    p.frequency_min = float(h.get("frequency_min", -1.0))
+    p.frequency_max = float(h.get("frequency_max", -1.0))
+    if "branches" in h:
+        arr = np.ascontiguousarray(h["branches"], dtype=np.int32)
+        keep.append(arr)
+        p.n_branches = arr.size
+        p.branches = arr.ctypes.data_as(c_int32_p)
+    if "branch_weights" in h:
+        arr = np.ascontiguousarray(h["branch_weights"], dtype=np.float64)
+        keep.append(arr)
+        p.n_branch_weights = arr.size
+        p.branch_weights = dptr(arr)
+    p.time_profile = 1 if h.get("time_profile", "constant") == "pulsed" else 0
+    p.time_start = float(h.get("time_start", 0.0))
+    p.time_end = float(h.get("time_end", -1.0))
+    p.period = float(h.get("period", 0.0))
+    p.on_duration = float(h.get("on_duration", -1.0))
+    p.duty_cycle = float(h.get("duty_cycle", 0.5))
+    p.amplitude = float(h.get("amplitude", 1.0))
+    return p
+
+
 class ConfigPOD(C.Structure):
     _fields_ = [
         ("sizes", C.c_double * 3), ("particle_count", C.c_double), ("time_step", C.c_double),
@@ -43,7 +109,7 @@ class ConfigPOD(C.Structure):
         ("face_condition", C.c_char * 6), ("face_value", C.c_double * 6), ("output_folder", C.c_char_p),
         ("material_interface_axis", C.c_int32), ("n_interfaces", C.c_int32),
         ("material_interface_positions", c_double_p), ("interface_frequency_bin_thz", C.c_double),
-        ("precision", C.c_int32),
+        ("precision", C.c_int32), ("heat_source", C.POINTER(HeatSourcePOD)),
     ]
 
 
@@ -59,7 +125,9 @@ class StatsPOD(C.Structure):
         ("average_heat_flux_along_axis", C.c_double), ("kappa_fit", C.c_double),
         ("kappa_endpoints", C.c_double), ("interface_events", C.c_int64),
         ("interface_transmitted", C.c_int64), ("interface_reflected", C.c_int64),
-        ("device_launches", C.c_int64),
+        ("device_launches", C.c_int64), ("total_heat_source_energy_ev", C.c_double),
+        ("step_heat_source_energy_ev", C.c_double), ("prescribed_heat_source_energy_ev", C.c_double),
+        ("pending_heat_source_energy_ev", C.c_double), ("step_heat_source_updates", C.c_int64),
     ]
 
     def as_dict(self) -> dict:
@@ -146,6 +214,10 @@ def config_pod(cfg: dict):
     c.material_interface_positions = dptr(planes) if planes.size else None
     c.interface_frequency_bin_thz = float(cfg.get("interface_frequency_bin_thz", 0.1))
     c.precision = 1 if cfg.get("precision", "fp64") == "mixed" else 0
+    if cfg.get("heat_source"):
+        hs = heat_source_pod(cfg["heat_source"], keep)
+        keep.append(hs)
+        c.heat_source = C.pointer(hs)
     return c, keep
 
 
@@ -305,6 +377,9 @@ ORACLE_EXTRA_PROTOS = {
     "grid_index": (C.c_int, [c_double_p, c_int32_p, C.c_int64, c_double_p, c_int32_p]),
     "callaway_evolve": (C.c_int, [C.c_int64, c_double_p, c_double_p, c_double_p, c_double_p, c_double_p, c_double_p,
                                   C.c_double, c_double_p]),
+    "source_rates": (C.c_int, [C.POINTER(ConfigPOD), c_double_p, c_int32_p]),
+    "source_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int, c_double_p,
+                               c_double_p, C.c_int64, c_int32_p, c_int32_p, c_double_p, c_double_p, c_int64_p]),
     "reservoir_cdf": (C.c_int, [C.c_void_p, c_double_p, C.c_double, C.c_double, C.c_double, c_double_p, c_double_p,
                                 c_int32_p]),
 }

@@ -72,9 +72,16 @@ __global__ void k_step_begin(DevLedger* L) {
     L->step_drive_updates = L->next_drive_updates;
     L->next_drive_ev = 0;
     L->next_drive_updates = 0;
+    L->step_source_ev = L->next_source_ev;
+    L->step_source_updates = L->next_source_updates;
+    L->next_source_ev = 0;
+    L->next_source_updates = 0;
     L->n_inject = 0;
     L->n_deferred = 0;
 }
+
+__device__ __forceinline__ double idx_to_double(int a) { return static_cast<double>(a); }
+__device__ __forceinline__ int double_to_idx(double a) { return static_cast<int>(a); }
 
 // ------------------------------------------------------------ statistics
 template <bool kRta>
@@ -474,6 +481,7 @@ __global__ void __launch_bounds__(kStatThreads) k_cell_tables(const DevTables* _
         zero.pad = 0;
         C.bins[hb + m] = zero;
         if (C.hM) C.hM[hb + m] = 0.0;
+        if (C.src_next) C.src_next[hb + m] = 0.0;
     }
     // the step-end energy deviation of the cell is the step-start one (cell
     // statistics) plus the collision change s[0] plus the drive change s[1]
@@ -496,7 +504,8 @@ __global__ void __launch_bounds__(1024) k_cells_final(const DevTables* __restric
         const DevMaterial& M = T.mat[C.cell_material[c]];
         double* f = C.cell_final + 4 * c;
         const double w = M.energy_weight;
-        const double dev = C.cell_stats[4 * c] + (phase >= 1 ? f[0] + f[1] : 0.0);
+        // step-start energy + collision + drive half + heat-source half (f[3])
+        const double dev = C.cell_stats[4 * c] + (phase >= 1 ? f[0] + f[1] + f[3] : 0.0);
         const double Ef = dev * w / C.volume[c] + M.energy_density_bg;
         if (!isfinite(Ef)) raise_error(L, kErrNonFinite, c);
         C.energy_final[c] = Ef;
@@ -524,7 +533,7 @@ __global__ void __launch_bounds__(1024) k_cells_final(const DevTables* __restric
     L->step_lifetime_residual += v[1];
     L->step_drive_ev += v[2];
     L->step_drive_updates += static_cast<unsigned long long>(v[3]);
-    const double residual = v[0] - L->thermal_energy - 0.0 - L->step_drive_ev - L->step_injected_ev +
+    const double residual = v[0] - L->thermal_energy - L->step_source_ev - L->step_drive_ev - L->step_injected_ev +
                             L->step_absorbed_ev - L->step_lifetime_residual;
     L->step_balance_residual = residual;
     L->total_absorbed += L->step_absorbed;
@@ -535,13 +544,228 @@ __global__ void __launch_bounds__(1024) k_cells_final(const DevTables* __restric
     L->total_balance_residual += residual;
     L->total_drive_ev += L->step_drive_ev;
     L->total_drive_updates += L->step_drive_updates;
+    L->total_source_ev += L->step_source_ev;
     L->thermal_energy = v[0];
     L->particle_count += static_cast<long long>(L->step_injected) - static_cast<long long>(L->step_absorbed);
     for (int r = 0; r < kMaxReservoirs; ++r) L->previous_res[r] = L->absorbed_res[r];
 }
 
+// ------------------------------------------------------- heat source
+// One heat-source half for one cell (src/solver/PrescribedHeatSource.cpp:218-243
+// accrual, src/solver/PhononSourceOperator.cpp:119-340 deposit): the cell's
+// budget is shared among its eligible carriers by spectrum, the increments
+// are added to the pending update of each (cell, mode), and the mode with the
+// largest energy increment per carrier takes the round-off correction (spread
+// over that mode's carriers in this cell). `next` = the first half of the next
+// step (energy booked to that step). Base temperature of the thermal Newton:
+// `temperature` (cell temperatures of the current refresh).
+__global__ void __launch_bounds__(kStatThreads) k_source(const DevTables* __restrict__ Tp, CellArrays C, DevLedger* L,
+                                                         double factor, const double* temperature, int next) {
+    __shared__ double red[4 * 32];
+    __shared__ double s_pend;
+    __shared__ int s_arg;
+    const DevTables& T = *Tp;
+    const int c = blockIdx.x;
+    if (threadIdx.x == 0) {
+        if (factor > 0.0) {
+            const double e = C.src_rate[c] * factor;
+            C.src_prescribed[c] += e;
+            C.src_pending[c] += e;
+        }
+        s_pend = C.src_pending[c];
+    }
+    __syncthreads();
+    const double pend = s_pend;
+    if (!(pend > 0.0)) return;
+    const int mat = C.cell_material[c];
+    const DevMaterial& M = T.mat[mat];
+    const int na = M.n_active;
+    const size_t hb = static_cast<size_t>(c) * C.hist_modes;
+    const double target = pend / M.energy_weight;
+    const int spectrum = T.par.source_spectrum;
+    // eligible carriers present, and the spectrum's normalization
+    double v[4] = {0.0, 0.0, -1.0e300, 0.0}; // count, sum of weights (k w, k C), max log-weight
+    for (int m = threadIdx.x; m < na; m += blockDim.x) {
+        const unsigned k = C.bins[hb + m].cnt;
+        if (!k || !(M.src_weight[m] > 0.0)) continue;
+        v[0] += k;
+        if (spectrum == 1) v[1] += k * M.src_weight[m];
+        else if (spectrum == 0 && T.par.source_linearized) v[1] += k * M.cap_bg[m];
+        if (spectrum == 2) v[2] = fmax(v[2], M.src_logw[m]);
+    }
+    {
+        double sums[2] = {v[0], v[1]};
+        block_sum<2>(sums, red);
+        v[0] = sums[0];
+        v[1] = sums[1];
+        // block max of the log-weights
+        double x = v[2];
+        for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double y = red[0];
+            for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) y = fmax(y, red[w]);
+            red[0] = y;
+        }
+        __syncthreads();
+        v[2] = red[0];
+        __syncthreads();
+    }
+    if (!(v[0] > 0.0)) return; // no eligible carrier: the cell keeps its budget
+    const double peak = v[2];
+    if (spectrum == 2) {
+        double g[1] = {0.0};
+        for (int m = threadIdx.x; m < na; m += blockDim.x) {
+            const unsigned k = C.bins[hb + m].cnt;
+            if (k && M.src_weight[m] > 0.0) g[0] += k * exp(M.src_logw[m] - peak);
+        }
+        block_sum<1>(g, red);
+        v[1] = g[0];
+    }
+    // thermal spectrum, nonlinear: pseudo-temperature of the eligible carriers
+    double Ts = 0.0, base = 0.0;
+    const bool newton = spectrum == 0 && !T.par.source_linearized;
+    if (newton) {
+        const double Tc = temperature[c];
+        base = isfinite(Tc) && Tc >= 0.0 ? Tc : T.par.background_T;
+        const int ncls = M.n_src_classes;
+        double* cnt = C.src_scratch + static_cast<size_t>(c) * 2 * C.src_classes;
+        double* n0 = cnt + C.src_classes;
+        for (int k = threadIdx.x; k < ncls; k += blockDim.x) {
+            cnt[k] = 0.0;
+            n0[k] = bose_dev(base, M.src_class_omega[k]);
+        }
+        __syncthreads();
+        for (int m = threadIdx.x; m < na; m += blockDim.x) {
+            const unsigned k = C.bins[hb + m].cnt;
+            const int cls = M.src_class[m];
+            if (k && cls >= 0) atomicAdd(cnt + cls, static_cast<double>(k));
+        }
+        __syncthreads();
+        auto energy_at = [&](double temperature_s, bool slope, double& d) {
+            double e[2] = {0.0, 0.0};
+            for (int k = threadIdx.x; k < ncls; k += blockDim.x) {
+                if (cnt[k] == 0.0) continue;
+                const double hw = kHbar * fmax(0.0, M.src_class_omega[k]);
+                const double nn = bose_dev(temperature_s, M.src_class_omega[k]);
+                e[0] += cnt[k] * hw * (nn - n0[k]);
+                if (slope && temperature_s > 0.0)
+                    e[1] += cnt[k] * hw * (hw * nn * (nn + 1.0) / (kKb * temperature_s * temperature_s));
+            }
+            block_sum<2>(e, red);
+            d = e[1];
+            return e[0];
+        };
+        double d;
+        double low = fmax(0.0, base);
+        double high = fmax(low + 1.0, 1.05 * low + 1.0);
+        double high_e = energy_at(high, false, d);
+        for (int k = 0; high_e < target && k < 60; ++k) {
+            high = 2.0 * high + 1.0;
+            high_e = energy_at(high, false, d);
+        }
+        if (!(high_e >= target) || !isfinite(high_e)) {
+            if (threadIdx.x == 0) raise_error(L, kErrCollision, c);
+            return;
+        }
+        Ts = 0.5 * (low + high);
+        const double tol = 1e-12 * fmax(1e-6, target);
+        for (int it = 0; it < 60; ++it) {
+            const double r = energy_at(Ts, true, d) - target;
+            if (fabs(r) <= tol) break;
+            if (r > 0.0) high = Ts;
+            else low = Ts;
+            double cand = 0.5 * (low + high);
+            if (d > 0.0 && isfinite(d)) {
+                const double nt = Ts - r / d;
+                if (nt > low && nt < high && isfinite(nt)) cand = nt;
+            }
+            Ts = cand;
+        }
+    }
+    auto increment = [&](int m) {
+        const double hw = M.hw[m];
+        if (spectrum == 2) return target * exp(M.src_logw[m] - peak) / v[1] / hw;
+        if (spectrum == 1) return target * (M.src_weight[m] / v[1]) / hw;
+        if (!newton) return target * M.cap_bg[m] / v[1] / hw;
+        return bose_dev(Ts, M.omega[m]) - bose_dev(base, M.omega[m]);
+    };
+    // applied energy and the correction mode (largest energy per carrier, lowest index on ties)
+    double applied[1] = {0.0};
+    double best = -1.0;
+    int arg = 0x7fffffff;
+    for (int m = threadIdx.x; m < na; m += blockDim.x) {
+        const unsigned k = C.bins[hb + m].cnt;
+        if (!k || !(M.src_weight[m] > 0.0)) continue;
+        const double e = M.hw[m] * increment(m);
+        applied[0] += k * e;
+        if (e > best || (e == best && m < arg)) {
+            best = e;
+            arg = m;
+        }
+    }
+    block_sum<1>(applied, red);
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oa = __shfl_xor_sync(0xffffffffu, arg, o);
+        if (ob > best || (ob == best && oa < arg)) {
+            best = ob;
+            arg = oa;
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+        red[threadIdx.x >> 5] = best;
+        red[32 + (threadIdx.x >> 5)] = idx_to_double(arg);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = red[0];
+        int a = double_to_idx(red[32]);
+        for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) {
+            const double ob = red[w];
+            const int oa = double_to_idx(red[32 + w]);
+            if (ob > b || (ob == b && oa < a)) {
+                b = ob;
+                a = oa;
+            }
+        }
+        s_arg = a;
+    }
+    __syncthreads();
+    const int corr_mode = s_arg;
+    const double corr = (target - applied[0]) / (M.hw[corr_mode] * C.bins[hb + corr_mode].cnt);
+    for (int m = threadIdx.x; m < na; m += blockDim.x) {
+        const unsigned k = C.bins[hb + m].cnt;
+        if (!k || !(M.src_weight[m] > 0.0)) continue;
+        double inc = increment(m);
+        if (m == corr_mode) inc += corr;
+        C.ab[hb + m].y += inc;
+        if (next) C.src_next[hb + m] += inc;
+    }
+    if (threadIdx.x == 0) {
+        const double raw = applied[0] + C.bins[hb + corr_mode].cnt * M.hw[corr_mode] * corr;
+        C.src_deposited[c] += pend;
+        C.src_pending[c] = 0.0;
+        if (next) {
+            atomicAdd(&L->next_source_ev, pend);
+            atomicAdd(&L->next_source_updates, static_cast<unsigned long long>(v[0]));
+        } else {
+            C.cell_final[4 * c + 3] = raw;
+            atomicAdd(&L->step_source_ev, pend);
+            atomicAdd(&L->step_source_updates, static_cast<unsigned long long>(v[0]));
+        }
+    }
+}
+
 // ----------------------------------------------------------- launchers
 void launch_step_begin(const LaunchCtx& x) { k_step_begin<<<1, 1, 0, x.stream>>>(x.L); }
+
+void launch_source(const LaunchCtx& x, double factor, bool final_temperature, bool next) {
+    k_source<<<x.C.ncells, kStatThreads, 0, x.stream>>>(x.T, x.C, x.L, factor,
+                                                         final_temperature ? x.C.temperature_final : x.C.temperature,
+                                                         next ? 1 : 0);
+}
 
 static size_t linear_smem(const CellArrays& C, int cl, int gmax, size_t real) {
     const size_t per = (static_cast<size_t>(C.hist_modes) + cl - 1) / cl;

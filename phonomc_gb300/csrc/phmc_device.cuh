@@ -72,6 +72,13 @@ struct DevMaterial {
     const double* grad_rate;   // [active]
     const double* drive_rate;  // [active] half dt * rate / hw: drive half-step D = drive_rate - drive_cap * ratio
     const double* drive_cap;   // [active] half dt * capacity / hw
+    // heat source: spectral weight (0: not eligible), Gaussian log-weight, and
+    // the class of equal frequency among eligible modes for the thermal Newton
+    const double* src_weight;  // [active]
+    const double* src_logw;    // [active]
+    const int* src_class;      // [active], -1 when not eligible
+    const double* src_class_omega;
+    int n_src_classes;
     double energy_weight;
     double energy_density_bg;
     double heat_capacity_density_bg;
@@ -139,6 +146,9 @@ struct DevParams {
     double background_T;
     int gradient_axis;
     double gradient_energy_weight;
+    int source_enabled;
+    int source_spectrum;        // 0 thermal, 1 weighted, 2 gaussian
+    int source_linearized;      // thermal spectrum with linearized transport
 };
 
 // Per-step accumulators and running totals, all on the device so a step needs
@@ -160,6 +170,8 @@ struct DevLedger {
     unsigned long long step_drive_updates;
     double next_drive_ev;                  // first gradient half-step of the next step
     unsigned long long next_drive_updates;
+    double step_source_ev, next_source_ev, total_source_ev;   // heat source deposits
+    unsigned long long step_source_updates, next_source_updates;
     double step_balance_residual;
     double thermal_energy;
     // totals

@@ -616,6 +616,211 @@ void EnergyLedger::finish_step(double energy, const BoundaryBalance& b) {
 }
 
 // ---------------------------------------------------------------- problem
+// ------------------------------------------------------- heat source
+// src/config/ConfigValidation.cpp:196-290 (the rules the carrier loop relies on).
+void validate_heat_source_config(const SimulationConfig& c) {
+    if (!c.heat_source_enabled) return;
+    if (c.heat_source_total_power) {
+        if (!std::isfinite(*c.heat_source_total_power) || !(*c.heat_source_total_power > 0.0))
+            throw std::runtime_error("heat_source.total_power must be finite and positive (W).");
+        if (c.heat_source_power_density != 0.0 || !c.heat_source_power_densities.empty())
+            throw std::runtime_error("heat_source.total_power cannot be combined with power_density or power_densities.");
+    } else if (!(c.heat_source_power_density > 0.0) || !std::isfinite(c.heat_source_power_density)) {
+        throw std::runtime_error("enabled heat_source requires positive total_power or power_density.");
+    }
+    for (const auto* v : {&c.heat_source_min, &c.heat_source_max, &c.heat_source_center, &c.heat_source_centers,
+                          &c.heat_source_sigma, &c.heat_source_half_width})
+        for (double x : *v)
+            if (!std::isfinite(x)) throw std::runtime_error("Heat-source spatial parameters must be finite.");
+    std::vector<int> br = c.heat_source_branches;
+    std::sort(br.begin(), br.end());
+    if ((!br.empty() && br.front() < 0) || std::adjacent_find(br.begin(), br.end()) != br.end())
+        throw std::runtime_error("heat_source.branches must contain unique nonnegative indices.");
+    if (c.heat_source_spectrum == HeatSourceSpectrum::Gaussian) {
+        if (!c.heat_source_frequency_center || !c.heat_source_frequency_sigma ||
+            !std::isfinite(*c.heat_source_frequency_center) || *c.heat_source_frequency_center < 0 ||
+            !std::isfinite(*c.heat_source_frequency_sigma) || *c.heat_source_frequency_sigma <= 0)
+            throw std::runtime_error("Gaussian spectrum requires finite frequency_center >= 0 and frequency_sigma > 0, in THz.");
+    } else if (c.heat_source_frequency_center || c.heat_source_frequency_sigma) {
+        throw std::runtime_error("frequency_center/frequency_sigma require heat_source.spectrum='gaussian'.");
+    }
+    if (c.heat_source_spectrum != HeatSourceSpectrum::Weighted) {
+        if (!c.heat_source_branch_weights.empty())
+            throw std::runtime_error("branch_weights requires heat_source.spectrum='weighted'.");
+    } else {
+        bool positive = false;
+        for (size_t b = 0; b < c.heat_source_branch_weights.size(); ++b) {
+            const double w = c.heat_source_branch_weights[b];
+            if (!std::isfinite(w) || w < 0.0) throw std::runtime_error("heat_source.branch_weights must be finite and nonnegative.");
+            if (br.empty() || std::binary_search(br.begin(), br.end(), static_cast<int>(b))) positive = positive || w > 0.0;
+        }
+        if (!positive) throw std::runtime_error("weighted heat_source needs positive weights on selected branches.");
+    }
+    for (double q : c.heat_source_power_densities)
+        if (!(q > 0.0) || !std::isfinite(q)) throw std::runtime_error("heat_source.power_densities values must be finite and positive.");
+    for (double f : {c.heat_source_frequency_min, c.heat_source_frequency_max})
+        if (!(f < 0.0) && !std::isfinite(f)) throw std::runtime_error("heat_source frequency cutoffs must be finite.");
+    if (c.heat_source_time_profile == HeatSourceTimeProfile::Pulsed &&
+        (!(c.heat_source_period > 0.0) || !std::isfinite(c.heat_source_period)))
+        throw std::runtime_error("Pulsed heat source requires a positive period.");
+    if (!std::isfinite(c.heat_source_amplitude) || c.heat_source_amplitude < 0.0)
+        throw std::runtime_error("heat_source.amplitude must be finite and nonnegative.");
+}
+
+// src/solver/HeatSourceDriving.cpp:12-44
+double heat_source_time_factor(const SimulationConfig& c, double begin_ps, double end_ps) {
+    const double begin = std::max(begin_ps, c.heat_source_time_start);
+    const double end = c.heat_source_time_end >= 0.0 ? std::min(end_ps, c.heat_source_time_end) : end_ps;
+    if (end <= begin) return 0.0;
+    if (c.heat_source_time_profile == HeatSourceTimeProfile::Constant) return c.heat_source_amplitude * (end - begin);
+    const double period = c.heat_source_period;
+    const double on = c.heat_source_on_duration < 0.0 ? c.heat_source_duty_cycle * period : c.heat_source_on_duration;
+    if (on <= 0.0) return 0.0;
+    auto on_time = [&](double rel) {
+        if (!(rel > 0.0)) return 0.0;
+        const double cycles = std::floor(rel / period);
+        return cycles * on + std::min(rel - cycles * period, on);
+    };
+    const double rb = begin - c.heat_source_time_start, re = end - c.heat_source_time_start;
+    return c.heat_source_amplitude * std::max(0.0, on_time(re) - on_time(rb));
+}
+
+// src/solver/PrescribedHeatSource.cpp:22-216: cell weights from the grid
+// centres (uniform box, or Gaussian sources cut at 2 sigma per axis with an
+// optional clip box and top-hat axes), then cell power from the density or the
+// total power.
+void HeatSourceTables::configure(const SimulationConfig& c, const SimulationDomain& domain) {
+    *this = HeatSourceTables{};
+    if (!c.heat_source_enabled) return;
+    validate_heat_source_config(c);
+    const double density = c.heat_source_total_power ? 1.0 : c.heat_source_power_density;
+    const auto& centers = domain.grid_centers();
+    std::vector<double> w(centers.size(), 0.0);
+    int selected = 0;
+    if (c.heat_source_profile == HeatSourceProfile::Uniform) {
+        if (c.heat_source_min.size() != 3 || c.heat_source_max.size() != 3)
+            throw std::runtime_error("uniform heat source requires min/max 3D vectors.");
+        Vec3 lo{c.heat_source_min[0], c.heat_source_min[1], c.heat_source_min[2]};
+        Vec3 hi{c.heat_source_max[0], c.heat_source_max[1], c.heat_source_max[2]};
+        for (int k = 0; k < 3; ++k)
+            if (lo[k] > hi[k]) std::swap(lo[k], hi[k]);
+        for (size_t i = 0; i < centers.size(); ++i) {
+            const Vec3& x = centers[i];
+            if (x[0] >= lo[0] && x[0] <= hi[0] && x[1] >= lo[1] && x[1] <= hi[1] && x[2] >= lo[2] && x[2] <= hi[2]) {
+                w[i] = 1.0;
+                ++selected;
+            }
+        }
+        if (!selected) throw std::runtime_error("uniform heat source region does not include any grid center.");
+    } else {
+        if ((c.heat_source_center.size() != 3 && c.heat_source_centers.empty()) || c.heat_source_sigma.size() != 3 ||
+            (!c.heat_source_centers.empty() && c.heat_source_centers.size() % 3 != 0))
+            throw std::runtime_error("gaussian heat source requires center=[x,y,z] or centers=[[x,y,z],...] and "
+                                     "sigma=[sx,sy,sz].");
+        std::vector<Vec3> src;
+        if (!c.heat_source_centers.empty())
+            for (size_t j = 0; j + 2 < c.heat_source_centers.size(); j += 3)
+                src.push_back({c.heat_source_centers[j], c.heat_source_centers[j + 1], c.heat_source_centers[j + 2]});
+        else
+            src.push_back({c.heat_source_center[0], c.heat_source_center[1], c.heat_source_center[2]});
+        std::vector<double> peak(src.size(), 1.0);
+        if (!c.heat_source_power_densities.empty()) {
+            if (c.heat_source_power_densities.size() != src.size())
+                throw std::runtime_error("heat_source.power_densities size does not match heat_source.centers.");
+            for (size_t j = 0; j < src.size(); ++j) peak[j] = c.heat_source_power_densities[j] / density;
+        }
+        const bool clip = c.heat_source_min.size() == 3 && c.heat_source_max.size() == 3;
+        Vec3 lo{0, 0, 0}, hi{0, 0, 0}, sigma{1, 1, 1}, half{};
+        std::array<bool, 3> gauss{true, true, true};
+        for (int k = 0; k < 3; ++k) {
+            if (clip) {
+                lo[k] = std::min(c.heat_source_min[k], c.heat_source_max[k]);
+                hi[k] = std::max(c.heat_source_min[k], c.heat_source_max[k]);
+            }
+            half[k] = std::numeric_limits<double>::infinity();
+            if (c.heat_source_half_width.size() == 3 && std::isfinite(c.heat_source_half_width[k]) &&
+                c.heat_source_half_width[k] > 0.0)
+                half[k] = c.heat_source_half_width[k];
+            else if (!c.heat_source_half_width.empty() && c.heat_source_half_width.size() != 3)
+                throw std::runtime_error("heat_source.half_width must contain 3 values.");
+            const double sk = c.heat_source_sigma[k];
+            gauss[k] = std::isfinite(sk) && sk > 0.0;
+            sigma[k] = gauss[k] ? std::max(1e-12, sk) : 1.0;
+        }
+        for (size_t i = 0; i < centers.size(); ++i) {
+            const Vec3& x = centers[i];
+            bool cut = false;
+            if (clip)
+                for (int k = 0; k < 3 && !cut; ++k) cut = x[k] < lo[k] || x[k] > hi[k];
+            if (cut) continue;
+            double sum = 0.0;
+            for (size_t j = 0; j < src.size(); ++j) {
+                double r2 = 0.0;
+                bool outside = false;
+                for (int k = 0; k < 3 && !outside; ++k) {
+                    if (gauss[k]) {
+                        const double u = std::abs(x[k] - src[j][k]) / sigma[k];
+                        if (u > 2.0) outside = true;
+                        else r2 += u * u;
+                    } else if (std::isfinite(half[k]) && std::abs(x[k] - src[j][k]) > half[k]) {
+                        outside = true;
+                    }
+                }
+                if (!outside) sum += peak[j] * std::exp(-0.5 * r2);
+            }
+            if (sum > 0.0) {
+                w[i] = sum;
+                ++selected;
+            }
+        }
+        if (!selected) throw std::runtime_error("gaussian heat source cannot be applied because grid is empty.");
+    }
+    const auto& vol = domain.grid_volumes();
+    double weighted = 0.0;
+    for (size_t i = 0; i < w.size(); ++i) weighted += w[i] * vol[i];
+    if (!(weighted > 0.0) || !std::isfinite(weighted))
+        throw std::runtime_error("Heat source has no finite positive sampled volume; refine the grid or source region.");
+    rates.resize(w.size());
+    for (size_t i = 0; i < w.size(); ++i) {
+        rates[i] = c.heat_source_total_power ? *c.heat_source_total_power * 6.241509074e6 * (w[i] * vol[i] / weighted)
+                                             : density * 6.241509074e-24 * w[i] * vol[i];
+        if (!std::isfinite(rates[i]) || rates[i] < 0.0) throw std::runtime_error("Non-finite heat-source cell power.");
+    }
+    double total = 0.0;
+    for (double r : rates) total += r;
+    if (!std::isfinite(total) || !(total > 0.0))
+        throw std::runtime_error("Total heat-source rate must be finite and representably positive.");
+    set_spectrum(c);
+    enabled = true;
+}
+
+// src/solver/PhononSourceOperator.cpp:20-40
+void HeatSourceTables::set_spectrum(const SimulationConfig& c) {
+    spectrum = c.heat_source_spectrum;
+    linearized_thermal = uses_linearized_transport(c);
+    frequency_min = c.heat_source_frequency_min;
+    frequency_max = c.heat_source_frequency_max;
+    branches = c.heat_source_branches;
+    weights = c.heat_source_branch_weights;
+    if (!weights.empty()) {
+        const double top = *std::max_element(weights.begin(), weights.end());
+        for (double& x : weights) x /= top;
+    }
+    gaussian_center = c.heat_source_frequency_center.value_or(0);
+    gaussian_sigma = c.heat_source_frequency_sigma.value_or(1);
+}
+
+// src/solver/PhononSourceOperator.cpp:102-117
+double HeatSourceTables::mode_weight(const PhononMaterial& m, int flat) const {
+    constexpr double two_pi = 6.283185307179586476925286766559;
+    const double f = m.omega(flat) / two_pi;
+    if (!std::isfinite(f) || (frequency_min >= 0.0 && f < frequency_min) || (frequency_max >= 0.0 && f > frequency_max))
+        return 0.0;
+    const int branch = flat % m.branch_count();
+    if (!branches.empty() && std::find(branches.begin(), branches.end(), branch) == branches.end()) return 0.0;
+    return spectrum == HeatSourceSpectrum::Weighted ? weights.at(static_cast<size_t>(branch)) : 1.0;
+}
+
 // src/solver/InterfaceModeSampler.cpp:11-44
 void InterfaceTables::build(const std::vector<const PhononMaterial*>& mats, int ax) {
     axis = ax;
@@ -832,6 +1037,18 @@ Problem build_problem(const SimulationConfig& cfg, SimulationDomain& domain,
         enabled.push_back(P.conservative ? reflecting : F.condition == 'R');
     }
     P.rough.build(mats, normals, rough, enabled, P.conservative, P.conservative ? Tbg : 0.0);
+
+    // Heat source (src/solver/HeatSourceDriving.cpp:8-11).
+    P.source.configure(cfg, domain);
+    if (P.source.enabled)
+        for (const PhononMaterial* m : mats)
+            for (int b : P.source.branches)
+                if (b >= m->branch_count())
+                    throw std::invalid_argument("heat_source.branches index exceeds a material's branch count.");
+    if (P.source.enabled && P.source.spectrum == HeatSourceSpectrum::Weighted)
+        for (const PhononMaterial* m : mats)
+            if (P.source.weights.size() != static_cast<size_t>(m->branch_count()))
+                throw std::invalid_argument("heat_source.branch_weights must match each material's branch count.");
 
     // Interface banks (src/solver/InterfaceInitialization.cpp:3-15, InterfaceInteraction.cpp:11-41).
     P.iface.enabled = mats.size() > 1;

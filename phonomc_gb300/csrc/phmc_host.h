@@ -36,6 +36,10 @@ enum class InitialTemperatureMode { Uniform, Linear };
 // Subset of the reference's SimulationConfig read by the carrier loop, with the
 // same names, units (lengths in Angstrom internally, as after parsing) and
 // defaults (include/SimulationConfig.h:42-146).
+enum class HeatSourceProfile { Uniform, Gaussian };
+enum class HeatSourceSpectrum { Thermal, Weighted, Gaussian };
+enum class HeatSourceTimeProfile { Constant, Pulsed };
+
 struct SimulationConfig {
     std::string model = "box";
     std::vector<double> sizes{2000.0, 2000.0, 2000.0}; // Angstrom
@@ -67,7 +71,28 @@ struct SimulationConfig {
     std::vector<double> material_interface_positions; // Angstrom
     double material_interface_frequency_bin_thz = 0.1;
     int material_interface_model = 0; // 0 = diffuse mismatch (dmm)
+    // Prescribed lattice heat source (include/SimulationConfig.h:103-139), lengths in Angstrom.
+    bool heat_source_enabled = false;
+    std::vector<double> heat_source_min, heat_source_max;
+    double heat_source_power_density = 0.0; // W/m^3
+    std::optional<double> heat_source_total_power; // W
+    HeatSourceSpectrum heat_source_spectrum = HeatSourceSpectrum::Thermal;
+    std::optional<double> heat_source_frequency_center, heat_source_frequency_sigma; // THz
+    std::vector<int> heat_source_branches;
+    std::vector<double> heat_source_branch_weights;
+    double heat_source_frequency_min = -1.0, heat_source_frequency_max = -1.0; // THz, <0: no cut
+    HeatSourceProfile heat_source_profile = HeatSourceProfile::Uniform;
+    std::vector<double> heat_source_center, heat_source_centers, heat_source_sigma, heat_source_half_width;
+    std::vector<double> heat_source_power_densities;
+    HeatSourceTimeProfile heat_source_time_profile = HeatSourceTimeProfile::Constant;
+    double heat_source_time_start = 0.0, heat_source_time_end = -1.0, heat_source_period = 0.0;
+    double heat_source_on_duration = -1.0, heat_source_duty_cycle = 0.5, heat_source_amplitude = 1.0;
 };
+
+void validate_heat_source_config(const SimulationConfig& c);
+// Source energy factor (ps) of [begin, end] under the time profile
+// (src/solver/HeatSourceDriving.cpp:12-44).
+double heat_source_time_factor(const SimulationConfig& c, double begin_ps, double end_ps);
 
 // include/SimulationConfig.h:148-156
 inline bool uses_linearized_transport(const SimulationConfig& c) {
@@ -210,6 +235,24 @@ struct LayeredLayout {
     }
 };
 
+// ------------------------------------------------------- heat source
+// PrescribedHeatSource (src/solver/PrescribedHeatSource.cpp:22-216): per-cell
+// power in eV/ps; PhononSourceOperator's spectral filter
+// (src/solver/PhononSourceOperator.cpp:20-130).
+struct HeatSourceTables {
+    bool enabled = false;
+    bool linearized_thermal = false;
+    HeatSourceSpectrum spectrum = HeatSourceSpectrum::Thermal;
+    std::vector<double> rates;            // [cells] eV/ps
+    double frequency_min = -1, frequency_max = -1;
+    std::vector<int> branches;
+    std::vector<double> weights;          // branch weights scaled by their maximum
+    double gaussian_center = 0, gaussian_sigma = 1;
+    void configure(const SimulationConfig& c, const SimulationDomain& domain);
+    void set_spectrum(const SimulationConfig& c); // the PhononSourceOperator part of configure()
+    double mode_weight(const PhononMaterial& m, int flat) const;
+};
+
 // ---------------------------------------------------- interface banks
 // Diffuse-mismatch mode banks (src/solver/InterfaceModeSampler.cpp:11-44): per
 // material and direction (0: v_axis < 0, 1: v_axis > 0) the active modes sorted
@@ -284,6 +327,7 @@ public:
     void initialize(double e) { thermal_ = e; step_ = {}; total_ = {}; }
     void begin_step() { step_ = {}; }
     void record_drive(long long updates, double e) { step_.drive_updates += updates; step_.drive_energy_ev += e; }
+    void record_source(long long updates, double e) { step_.source_updates += updates; step_.source_energy_ev += e; }
     void set_lifetime_residual(double e) { step_.lifetime_residual_ev = e; }
     void finish_step(double energy, const BoundaryBalance& b);
     double thermal_energy_ev() const { return thermal_; }
@@ -336,6 +380,7 @@ struct Problem {
     std::vector<int> cell_material;      // [cells]
     RoughTables rough;
     InterfaceTables iface;
+    HeatSourceTables source;
     std::vector<int> plane_cell;         // cell boundary index of each interface plane along the layout axis
     std::vector<Reservoir> reservoirs;
     std::vector<std::vector<double>> reservoir_occ; // [reservoir][active of its material]

@@ -39,6 +39,8 @@ void launch_containment(const LaunchCtx& x, bool mixed);
 void launch_flux(const LaunchCtx& x, bool mixed);
 void launch_apply_pending(const LaunchCtx& x, bool subtract_drive);
 void launch_step_begin(const LaunchCtx& x);
+// One heat-source half: accrue `factor` ps of power, deposit into the pending updates.
+void launch_source(const LaunchCtx& x, double factor, bool final_temperature, bool next);
 int launch_cell_solve(const LaunchCtx& x, int phase, int collision);
 int linear_cluster_size(const CellArrays& C, bool mixed);
 void prepare_linear_solve(const CellArrays& C);

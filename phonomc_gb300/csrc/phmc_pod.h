@@ -35,6 +35,46 @@ inline MaterialData material_from_pod(const phmc_material_data& p) {
     return d;
 }
 
+// [heat_source] fields of phmc_config (include/SimulationConfig.h:103-139).
+inline void heat_source_from_pod(const phmc_heat_source& h, SimulationConfig& s) {
+    s.heat_source_enabled = true;
+    s.heat_source_profile = h.profile == 1 ? HeatSourceProfile::Gaussian : HeatSourceProfile::Uniform;
+    if (h.has_box) {
+        s.heat_source_min.assign(h.min, h.min + 3);
+        s.heat_source_max.assign(h.max, h.max + 3);
+    }
+    if (h.profile == 1) {
+        if (h.n_centers == 1 && h.centers) s.heat_source_center.assign(h.centers, h.centers + 3);
+        else if (h.n_centers > 1 && h.centers) s.heat_source_centers.assign(h.centers, h.centers + 3 * h.n_centers);
+        s.heat_source_sigma.assign(h.sigma, h.sigma + 3);
+        if (h.half_width[0] > 0 || h.half_width[1] > 0 || h.half_width[2] > 0)
+            s.heat_source_half_width.assign(h.half_width, h.half_width + 3);
+    }
+    s.heat_source_power_density = h.power_density;
+    if (h.has_total_power) s.heat_source_total_power = h.total_power;
+    if (h.n_power_densities > 0 && h.power_densities)
+        s.heat_source_power_densities.assign(h.power_densities, h.power_densities + h.n_power_densities);
+    s.heat_source_spectrum = h.spectrum == 1 ? HeatSourceSpectrum::Weighted
+                           : h.spectrum == 2 ? HeatSourceSpectrum::Gaussian
+                                             : HeatSourceSpectrum::Thermal;
+    if (h.has_frequency_gaussian) {
+        s.heat_source_frequency_center = h.frequency_center;
+        s.heat_source_frequency_sigma = h.frequency_sigma;
+    }
+    s.heat_source_frequency_min = h.frequency_min;
+    s.heat_source_frequency_max = h.frequency_max;
+    if (h.n_branches > 0 && h.branches) s.heat_source_branches.assign(h.branches, h.branches + h.n_branches);
+    if (h.n_branch_weights > 0 && h.branch_weights)
+        s.heat_source_branch_weights.assign(h.branch_weights, h.branch_weights + h.n_branch_weights);
+    s.heat_source_time_profile = h.time_profile == 1 ? HeatSourceTimeProfile::Pulsed : HeatSourceTimeProfile::Constant;
+    s.heat_source_time_start = h.time_start;
+    s.heat_source_time_end = h.time_end;
+    s.heat_source_period = h.period;
+    s.heat_source_on_duration = h.on_duration;
+    s.heat_source_duty_cycle = h.duty_cycle;
+    s.heat_source_amplitude = h.amplitude;
+    }
+
 inline SimulationConfig config_from_pod(const phmc_config& c) {
     SimulationConfig s;
     s.sizes = {c.sizes[0], c.sizes[1], c.sizes[2]};
@@ -66,6 +106,7 @@ inline SimulationConfig config_from_pod(const phmc_config& c) {
         s.material_interface_positions.assign(c.material_interface_positions,
                                               c.material_interface_positions + c.n_interfaces);
     if (c.interface_frequency_bin_thz > 0) s.material_interface_frequency_bin_thz = c.interface_frequency_bin_thz;
+    if (c.heat_source) heat_source_from_pod(*c.heat_source, s);
     // Validation of src/config/ConfigValidation.cpp:403-408: gradient driving
     // requires fixed lifetimes.
     if (s.temperature_gradient && s.lifetime_temperature_is_local)

@@ -113,6 +113,7 @@ void DeviceSolver::upload_tables() {
     if (P_.mats.size() > static_cast<size_t>(kMaxMaterials)) throw std::runtime_error("too many materials");
     int hist_modes = 0;
     double r_max = 0.0;
+    int max_src_classes = 0;
     for (size_t mi = 0; mi < P_.mats.size(); ++mi) {
         const MaterialTables& M = P_.mats[mi];
         DevMaterial& D = T.mat[mi];
@@ -150,6 +151,33 @@ void DeviceSolver::upload_tables() {
         D.ivel32 = upload(iv32);
         D.speed = upload(speed);
         D.push = upload(push);
+        if (P_.source.enabled) {
+            // spectral weights, Gaussian log-weights and equal-frequency classes of eligible modes
+            const PhononMaterial& Pm = *mats_[mi];
+            std::vector<double> wgt(M.n_active, 0.0), logw(M.n_active, 0.0), cls_omega;
+            std::vector<int> cls(M.n_active, -1);
+            std::vector<std::pair<double, int>> order;
+            for (int a = 0; a < M.n_active; ++a) {
+                const int f = M.active_flat[a];
+                const double hw = kHbarEvPs * Pm.omega(f);
+                if (std::isfinite(hw) && hw > 1e-14) wgt[a] = P_.source.mode_weight(Pm, f);
+                const double fr = Pm.omega(f) / 6.283185307179586476925286766559;
+                const double z = (fr - P_.source.gaussian_center) / P_.source.gaussian_sigma;
+                logw[a] = -0.5 * z * z;
+                if (wgt[a] > 0.0) order.push_back({M.omega[a], a});
+            }
+            std::sort(order.begin(), order.end());
+            for (size_t k = 0; k < order.size(); ++k) {
+                if (k == 0 || order[k].first != order[k - 1].first) cls_omega.push_back(order[k].first);
+                cls[order[k].second] = static_cast<int>(cls_omega.size()) - 1;
+            }
+            D.src_weight = upload(wgt);
+            D.src_logw = upload(logw);
+            D.src_class = upload(cls);
+            D.src_class_omega = upload(cls_omega);
+            D.n_src_classes = static_cast<int>(cls_omega.size());
+            max_src_classes = std::max(max_src_classes, D.n_src_classes);
+        }
         D.nbg = upload(M.nbg);
         D.cap_bg = upload(M.capacity_bg);
         D.mode_class = upload(M.mode_class);
@@ -306,6 +334,10 @@ void DeviceSolver::upload_tables() {
     p.background_T = cfg_.background_temperature;
     p.gradient_axis = P_.kappa_axis;
     p.gradient_energy_weight = P_.gradient_energy_weight;
+    p.source_enabled = P_.source.enabled ? 1 : 0;
+    p.source_spectrum = P_.source.spectrum == HeatSourceSpectrum::Weighted ? 1
+                        : P_.source.spectrum == HeatSourceSpectrum::Gaussian ? 2 : 0;
+    p.source_linearized = P_.source.linearized_thermal ? 1 : 0;
     PHMC_CUDA(cudaMalloc(&d_tables_, sizeof(DevTables)));
     PHMC_CUDA(cudaMemcpyAsync(d_tables_, &tables_, sizeof(DevTables), cudaMemcpyHostToDevice, stream_));
 
@@ -328,6 +360,15 @@ void DeviceSolver::upload_tables() {
     C.grad_ratio = dalloc<double>(ncells_);
     C.flux = dalloc<double>(3 * static_cast<size_t>(ncells_));
     C.cell_stats = dalloc<double>(4 * static_cast<size_t>(ncells_));
+    if (P_.source.enabled) {
+        C.src_rate = upload(P_.source.rates);
+        C.src_pending = dalloc<double>(ncells_);
+        C.src_prescribed = dalloc<double>(ncells_);
+        C.src_deposited = dalloc<double>(ncells_);
+        C.src_classes = std::max(1, max_src_classes);
+        C.src_scratch = dalloc<double>(static_cast<size_t>(ncells_) * 2 * C.src_classes);
+        C.src_next = dalloc<double>(hist);
+    }
     C.cell_final = dalloc<double>(4 * static_cast<size_t>(ncells_));
     if (rta) {
         // per-cell class sums; the stride is the largest class count of the materials
@@ -425,6 +466,11 @@ void DeviceSolver::initial_statistics() {
     launch_histogram(x, !P_.linearized);
     counters_.launches += 2 + launch_cell_solve(x, 0, collision_kind());
     launch_cells_final(x, 0);
+    if (P_.source.enabled) {
+        // first heat-source half of the coming step (src/MonteCarloSolver.cpp:364-370)
+        launch_source(x, heat_source_time_factor(cfg_, elapsed_, elapsed_ + 0.5 * cfg_.time_step), true, true);
+        counters_.launches += 1;
+    }
     materialized_ = true;
 }
 
@@ -505,7 +551,18 @@ void DeviceSolver::run_timestep() {
         counters_.launches += 1;
     }
     counters_.launches += 1 + launch_cell_solve(x, 1, coll);
+    const double mid = elapsed_ + 0.5 * cfg_.time_step, end = elapsed_ + cfg_.time_step;
+    if (P_.source.enabled) {
+        // second heat-source half of this step, after the collision (src/MonteCarloSolver.cpp:376)
+        launch_source(x, heat_source_time_factor(cfg_, mid, end), false, false);
+        counters_.launches += 1;
+    }
     launch_cells_final(x, 1);
+    if (P_.source.enabled) {
+        // first half of the next step, folded into the pending update
+        launch_source(x, heat_source_time_factor(cfg_, end, end + 0.5 * cfg_.time_step), true, true);
+        counters_.launches += 1;
+    }
     materialized_ = false;
     ++step_;
     elapsed_ += cfg_.time_step;
@@ -685,6 +742,18 @@ void DeviceSolver::read_stats(phmc_stats& o) {
     o.average_heat_flux_along_axis = avg_flux_;
     o.kappa_fit = kappa_fit_;
     o.kappa_endpoints = kappa_end_;
+    o.total_heat_source_energy_ev = L.total_source_ev;
+    o.step_heat_source_energy_ev = L.step_source_ev;
+    o.step_heat_source_updates = static_cast<int64_t>(L.step_source_updates);
+    if (P_.source.enabled) {
+        std::vector<double> pr(ncells_), pe(ncells_);
+        PHMC_CUDA(cudaMemcpy(pr.data(), cells_.src_prescribed, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
+        PHMC_CUDA(cudaMemcpy(pe.data(), cells_.src_pending, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
+        for (int c = 0; c < ncells_; ++c) {
+            o.prescribed_heat_source_energy_ev += pr[c];
+            o.pending_heat_source_energy_ev += pe[c];
+        }
+    }
     o.interface_events = static_cast<int64_t>(L.total_iface_events);
     o.interface_transmitted = static_cast<int64_t>(L.total_iface_transmitted);
     o.interface_reflected = static_cast<int64_t>(L.total_iface_reflected);

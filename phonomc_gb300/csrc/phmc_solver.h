@@ -87,6 +87,14 @@ struct CellArrays {
     const double* lin_omd;        // 1 - exp(-r dt)
     const double* lin_bg;         // (1 - exp(-r dt)) n_bg
     int lin_substeps;
+    // heat source per cell: power (eV/ps), budgets (eV), Newton scratch [cells][2 * classes]
+    const double* src_rate;
+    double* src_pending;
+    double* src_prescribed;
+    double* src_deposited;
+    double* src_scratch;
+    double* src_next;        // [ncells * hist_modes] next step's first source half inside ab.y (null: no source)
+    int src_classes;
     double lin_h;
     int lin_terms;
     // RTA classes of material 0

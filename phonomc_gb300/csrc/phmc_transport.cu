@@ -993,7 +993,8 @@ __global__ void __launch_bounds__(256) k_flux(const DevTables* __restrict__ Tp, 
         const DevMaterial& M = T.mat[w >> 28];
         const int ai = static_cast<int>(w & 0x00FFFFFFu);
         const int c = S.cell[i];
-        const double occ = apply_pending(C, c, ai, S.occ[i]) - drive_half(T, C, M, c, ai);
+        double occ = apply_pending(C, c, ai, S.occ[i]) - drive_half(T, C, M, c, ai);
+        if (C.src_next) occ -= C.src_next[static_cast<size_t>(c) * C.hist_modes + ai];
         const double e = dmul(dmul(M.hw[ai], occ - M.nbg[ai]), M.energy_weight);
         double v[3];
         mode_velocity(M, w, v);
@@ -1018,7 +1019,10 @@ __global__ void k_apply_pending(const DevTables* __restrict__ Tp, CarrierState S
         const int ai = static_cast<int>(w & 0x00FFFFFFu);
         const int c = S.cell[i];
         double occ = apply_pending(C, c, ai, S.occ[i]);
-        if (subtract_drive) occ -= drive_half(T, C, T.mat[w >> 28], c, ai);
+        if (subtract_drive) {
+            occ -= drive_half(T, C, T.mat[w >> 28], c, ai);
+            if (C.src_next) occ -= C.src_next[static_cast<size_t>(c) * C.hist_modes + ai];
+        }
         S.occ[i] = occ;
     }
 }
@@ -1031,7 +1035,9 @@ __global__ void k_reset_pending(const DevTables* __restrict__ Tp, CellArrays C, 
         const int c = static_cast<int>(k / C.hist_modes);
         const int m = static_cast<int>(k % C.hist_modes);
         const DevMaterial& M = T.mat[C.cell_material[c]];
-        const double D = (keep_drive && m < M.n_active) ? drive_half(T, C, M, c, m) : 0.0;
+        double D = (keep_drive && m < M.n_active) ? drive_half(T, C, M, c, m) : 0.0;
+        if (keep_drive && C.src_next) D += C.src_next[k];
+        else if (C.src_next) C.src_next[k] = 0.0;
         C.ab[k] = make_double2(1.0, D);
     }
 }

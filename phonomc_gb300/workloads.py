@@ -13,7 +13,13 @@ bilayer_callaway  200 nm stack of two materials (the second with 0.7x
                    reservoirs 310/290 K on the z faces, 100 z-cells, 1e8
                    carriers, dt = 0.5 ps.
 
-The lateral repeat cell is 100 nm x 100 nm in all three. `scaled()` keeps the
+heated_film       the cross-plane film with both reservoirs at 300 K and a
+                   prescribed lattice heat source: Gaussian along z (sigma
+                   10 nm, centred at 50 nm, uniform in x and y), 1e18 W/m^3
+                   peak, thermal spectrum; nonlinear RTA with local
+                   lifetimes, 1e6 carriers, dt = 1 ps.
+
+The lateral repeat cell is 100 nm x 100 nm in all four. `scaled()` keeps the
 geometry and physics and shrinks the carrier count for tests.
 """
 
@@ -88,6 +94,20 @@ def bilayer_callaway(particles: float = 1e8, seed: int = 12345, precision: str =
         "interface_frequency_bin_thz": 0.1,
         "precision": precision,
     }
+
+
+def heated_film(particles: float = 1e6, seed: int = 12345, precision: str = "fp64", spectrum: str = "thermal") -> dict:
+    c = cross_plane_film(particles, seed, precision)
+    c.update(name="heated_film", face_values=(0, 0, 0, 0, 300.0, 300.0), initial_temperature=300.0,
+             lifetime_temperature="local")
+    hs = {"profile": "gaussian", "center": (0.5 * LATERAL_A, 0.5 * LATERAL_A, 0.5 * THICKNESS_A),
+          "sigma": (0.0, 0.0, 100.0), "power_density": 1e18, "spectrum": spectrum}
+    if spectrum == "weighted":
+        hs.update(branch_weights=[1.0, 1.0, 2.0, 0.5, 0.5, 0.5])
+    if spectrum == "gaussian":
+        hs.update(frequency_center=6.0, frequency_sigma=2.0)
+    c["heat_source"] = hs
+    return c
 
 
 def bilayer_materials(mesh: int = 16):

@@ -41,6 +41,10 @@ CASES = {
     "rough_conservative": ["rough", "{m}", "1"],
     "gradient_drive": ["gradient", "{m}"],
     "reservoir": ["reservoir", "{m}"],
+    "source_thermal": ["source", "{m}", "0", "0"],
+    "source_thermal_linearized": ["source", "{m}", "0", "1"],
+    "source_weighted": ["source", "{m}", "1", "0"],
+    "source_gaussian": ["source", "{m}", "2", "0"],
     "interface_dmm": ["interface", "{m}", "{s}", "0"],
     "interface_dmm_linearized": ["interface", "{m}", "{s}", "1"],
 }

@@ -376,3 +376,45 @@ def test_mixed_bilayer_conserves_energy_and_tracks_plain(gpu):
     cp, cm = sp.carriers(), sm.carriers()
     a = (cp["alive"] == 1) & (cm["alive"] == 1)
     assert np.mean(cp["mode"][a] == cm["mode"][a]) > 0.99
+
+
+# ------------------------------------------------------------ heat source
+@pytest.mark.parametrize("spectrum,callaway", [("thermal", False), ("weighted", False), ("gaussian", False),
+                                               ("thermal", True)])
+def test_heat_source_steps_match_oracle(gpu, orc, spectrum, callaway):
+    """Prescribed heat source (both halves per step, budgets kept in cells
+    without eligible carriers): device steps against the oracle. The device
+    spreads the round-off correction over the correction mode's carriers of the
+    cell instead of one carrier, so occupations agree to 1e-11."""
+    cfg = workloads.scaled(workloads.heated_film(spectrum=spectrum), 20000, random_seed=43)
+    if callaway:
+        cfg["collision_model"] = "callaway"
+        cfg["lifetime_temperature"] = 300.0
+    mat = synthetic.make_material(mesh=16, callaway=callaway)
+    stationary = spectrum == "gaussian" or callaway
+    mg = abi.Material(gpu, "phmc_", mat, 0.1, stationary, callaway)
+    mo = abi.Material(orc, "orc_", mat, 0.1, stationary, callaway)
+    sg = abi.Solver(gpu, "phmc_", cfg, [mg])
+    so = abi.Solver(orc, "orc_", cfg, [mo])
+    for _ in range(3):
+        sg.run(1)
+        so.run(1)
+        stg, sto = _compare(sg, so, tol=1e-11)
+        for k in ("step_heat_source_energy_ev", "total_heat_source_energy_ev", "prescribed_heat_source_energy_ev",
+                  "pending_heat_source_energy_ev"):
+            assert abs(stg[k] - sto[k]) <= 1e-12 * max(1.0, abs(sto[k])), k
+        assert stg["step_heat_source_updates"] == sto["step_heat_source_updates"]
+        scale = abs(sto["total_thermal_energy_ev"])
+        assert abs(stg["step_energy_balance_residual_ev"]) < 1e-12 * scale
+    assert sto["total_heat_source_energy_ev"] > 0
+
+
+def test_mixed_heat_source_conserves_energy(gpu):
+    cfg = workloads.scaled(workloads.heated_film(), 200000, random_seed=47, precision="mixed")
+    m = abi.Material(gpu, "phmc_", synthetic.make_material(mesh=16), 0.1, False, False)
+    s = abi.Solver(gpu, "phmc_", cfg, [m])
+    s.run(5)
+    st = s.stats()
+    scale = abs(st["total_thermal_energy_ev"])
+    assert st["total_heat_source_energy_ev"] > 0
+    assert abs(st["step_energy_balance_residual_ev"]) < 1e-12 * scale

@@ -220,3 +220,58 @@ def test_interface_dmm(oracle_lib, name, linearized):
                      .group_velocity).reshape(-1, 3)[fo[sel]]
         sg = np.stack([1 - 2 * ((so[sel] >> b) & 1) for b in range(3)], axis=1)
         assert np.array_equal(v * sg, np.asarray(g["out_v"]).reshape(-1, 3)[sel])
+
+
+SOURCE_CASES = {"source_thermal": ("thermal", 0), "source_thermal_linearized": ("thermal", 1),
+                "source_weighted": ("weighted", 0), "source_gaussian": ("gaussian", 0)}
+
+
+def _source_spec(spectrum):
+    h = {"profile": "gaussian", "center": (180.0, 130.0, 90.0), "sigma": (160.0, 140.0, 70.0),
+         "power_density": 3e19, "spectrum": spectrum, "frequency_max": 14.0}
+    if spectrum == "weighted":
+        h.update(branch_weights=[1.0, 2.0, 1.5, 0.5, 0.25, 0.0], branches=[0, 1, 2, 3, 4])
+    if spectrum == "gaussian":
+        h.update(frequency_center=6.0, frequency_sigma=2.5)
+    return h
+
+
+def test_source_cell_rates(oracle_lib):
+    """PrescribedHeatSource cell powers of a Gaussian source (bit-exact)."""
+    g = golden("source_thermal")
+    cfg = {"sizes": (500.0, 400.0, 300.0), "grid": (2, 2, 3), "faces": ("P", "P", "P", "P", "T", "T"),
+           "face_values": (0, 0, 0, 0, 301.0, 299.0), "heat_source": _source_spec("thermal")}
+    pod, keep = abi.config_pod(cfg)
+    rates = np.zeros(64)
+    n = C.c_int32()
+    assert oracle_lib.orc_source_rates(C.byref(pod), D(rates), C.byref(n)) == 0, oracle_lib.orc_last_error()
+    assert np.array_equal(rates[:n.value], np.asarray(g["rates"]))
+    assert np.array_equal(rates[:n.value] * g["factor"], np.asarray(g["pending_before"]))
+
+
+@pytest.mark.parametrize("name", list(SOURCE_CASES))
+def test_source_apply(oracle_lib, name):
+    """PhononSourceOperator::apply: per-carrier increments in each spectrum, the
+    round-off correction carrier, cells without eligible carriers keep their
+    budget (occupations within 1e-15 relative: the reference sums capacities and
+    Gaussian weights in long double)."""
+    from phonomc_gb300 import synthetic
+    g = golden(name)
+    spectrum, linearized = SOURCE_CASES[name]
+    m = abi.Material(oracle_lib, "orc_", synthetic.make_material(mesh=8), 0.1, True, False)
+    keep = []
+    hs = abi.heat_source_pod(_source_spec(spectrum), keep)
+    flat, cell = (np.ascontiguousarray(g[k], dtype=np.int32) for k in ("flat", "cell"))
+    occ = np.ascontiguousarray(g["occ_in"], dtype=np.float64).copy()
+    pend = np.ascontiguousarray(g["pending_before"], dtype=np.float64).copy()
+    cT = np.ascontiguousarray(g["cell_temperature"], dtype=np.float64)
+    e, up = C.c_double(), C.c_int64()
+    rc = oracle_lib.orc_source_apply(m.h, C.byref(hs), linearized, 300.0, g["particle_volume"], cT.size, D(cT), D(pend),
+                                     flat.size, flat.ctypes.data_as(abi.c_int32_p), cell.ctypes.data_as(abi.c_int32_p),
+                                     D(occ), C.byref(e), C.byref(up))
+    assert rc == 0, oracle_lib.orc_last_error()
+    assert up.value == g["updates"]
+    assert e.value == g["energy"]
+    assert np.array_equal(pend, np.asarray(g["pending_after"]))
+    assert np.allclose(occ, g["occ_out"], rtol=1e-15, atol=1e-18)
+    assert np.array_equal(occ == np.asarray(g["occ_in"]), np.asarray(g["occ_out"]) == np.asarray(g["occ_in"]))
