@@ -475,12 +475,14 @@ __global__ void __launch_bounds__(kStatThreads) k_cell_tables(const DevTables* _
             }
         }
         C.ab[hb + m] = make_double2(a, collide ? bc + 2.0 * D : D);
-        BinSum zero;
-        zero.N = 0.0;
-        zero.cnt = 0;
-        zero.pad = 0;
-        C.bins[hb + m] = zero;
-        if (C.hM) C.hM[hb + m] = 0.0;
+        if (!T.par.source_enabled) { // with a heat source the bins are cleared after its halves
+            BinSum zero;
+            zero.N = 0.0;
+            zero.cnt = 0;
+            zero.pad = 0;
+            C.bins[hb + m] = zero;
+            if (C.hM) C.hM[hb + m] = 0.0;
+        }
         if (C.src_next) C.src_next[hb + m] = 0.0;
     }
     // the step-end energy deviation of the cell is the step-start one (cell
@@ -567,10 +569,15 @@ __global__ void __launch_bounds__(kStatThreads) k_source(const DevTables* __rest
     const DevTables& T = *Tp;
     const int c = blockIdx.x;
     if (threadIdx.x == 0) {
+        if (next) {
+            C.src_step_pending[c] = C.src_pending[c];
+            C.src_next_accrued[c] = 0.0;
+        }
         if (factor > 0.0) {
             const double e = C.src_rate[c] * factor;
             C.src_prescribed[c] += e;
             C.src_pending[c] += e;
+            if (next) C.src_next_accrued[c] = e;
         }
         s_pend = C.src_pending[c];
     }
@@ -765,6 +772,12 @@ void launch_source(const LaunchCtx& x, double factor, bool final_temperature, bo
     k_source<<<x.C.ncells, kStatThreads, 0, x.stream>>>(x.T, x.C, x.L, factor,
                                                          final_temperature ? x.C.temperature_final : x.C.temperature,
                                                          next ? 1 : 0);
+    if (next) {
+        // last reader of this step's bins
+        const size_t hist = static_cast<size_t>(x.C.ncells) * x.C.hist_modes;
+        cudaMemsetAsync(x.C.bins, 0, hist * sizeof(BinSum), x.stream);
+        if (x.C.hM) cudaMemsetAsync(x.C.hM, 0, hist * sizeof(double), x.stream);
+    }
 }
 
 static size_t linear_smem(const CellArrays& C, int cl, int gmax, size_t real) {

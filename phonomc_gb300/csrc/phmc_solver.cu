@@ -365,6 +365,8 @@ void DeviceSolver::upload_tables() {
         C.src_pending = dalloc<double>(ncells_);
         C.src_prescribed = dalloc<double>(ncells_);
         C.src_deposited = dalloc<double>(ncells_);
+        C.src_step_pending = dalloc<double>(ncells_);
+        C.src_next_accrued = dalloc<double>(ncells_);
         C.src_classes = std::max(1, max_src_classes);
         C.src_scratch = dalloc<double>(static_cast<size_t>(ncells_) * 2 * C.src_classes);
         C.src_next = dalloc<double>(hist);
@@ -746,11 +748,13 @@ void DeviceSolver::read_stats(phmc_stats& o) {
     o.step_heat_source_energy_ev = L.step_source_ev;
     o.step_heat_source_updates = static_cast<int64_t>(L.step_source_updates);
     if (P_.source.enabled) {
-        std::vector<double> pr(ncells_), pe(ncells_);
+        // budgets at the step boundary: the next step's first half is already accrued here
+        std::vector<double> pr(ncells_), pe(ncells_), na(ncells_);
         PHMC_CUDA(cudaMemcpy(pr.data(), cells_.src_prescribed, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
-        PHMC_CUDA(cudaMemcpy(pe.data(), cells_.src_pending, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
+        PHMC_CUDA(cudaMemcpy(pe.data(), cells_.src_step_pending, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
+        PHMC_CUDA(cudaMemcpy(na.data(), cells_.src_next_accrued, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
         for (int c = 0; c < ncells_; ++c) {
-            o.prescribed_heat_source_energy_ev += pr[c];
+            o.prescribed_heat_source_energy_ev += pr[c] - na[c];
             o.pending_heat_source_energy_ev += pe[c];
         }
     }

@@ -92,6 +92,8 @@ struct CellArrays {
     double* src_pending;
     double* src_prescribed;
     double* src_deposited;
+    double* src_step_pending;  // budget at the step boundary, before the next step's first accrual
+    double* src_next_accrued;  // the next step's first accrual (already in src_prescribed)
     double* src_scratch;
     double* src_next;        // [ncells * hist_modes] next step's first source half inside ab.y (null: no source)
     int src_classes;
