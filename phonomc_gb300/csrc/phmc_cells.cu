@@ -92,26 +92,21 @@ __global__ void __launch_bounds__(kStatThreads) k_cell_stats(const DevTables* __
     const int c = blockIdx.y;
     const DevMaterial& M = T.mat[C.cell_material[c]];
     const size_t hb = static_cast<size_t>(c) * C.hist_modes;
-    const int m0 = blockIdx.x * kChunk, m1 = min(M.n_active, m0 + kChunk);
+    const int m0 = blockIdx.x * kChunk, m1 = min(M.n_bins, m0 + kChunk);
     double v[3] = {0.0, 0.0, 0.0};
-    for (int m = m0 + threadIdx.x; m < m1; m += blockDim.x) {
-        const unsigned k = C.bins[hb + m].cnt;
+    for (int b = m0 + threadIdx.x; b < m1; b += blockDim.x) {
+        const unsigned k = C.bins[hb + b].cnt;
         if (!k) continue;
-        const double N = C.bins[hb + m].N;
+        const double N = C.bins[hb + b].N;
+        const int m = M.bin_rep ? M.bin_rep[b] : b;
         v[0] += M.hw[m] * (N - k * M.nbg[m]);
         if (M.grad_rate) {
             v[1] += k * M.grad_rate[m];
             v[2] += k * M.cap_bg[m];
         }
-        if (kRta && classes) {
-            double* cs = C.cls_sum + (static_cast<size_t>(c) * C.n_classes + M.mode_class[m]) * 3;
-            atomicAdd(cs, static_cast<double>(k));
-            atomicAdd(cs + 1, N);
-            atomicAdd(cs + 2, C.hM[hb + m]);
-        }
     }
     block_sum<3>(v, red);
-    if (threadIdx.x == 0 && m0 < M.n_active) {
+    if (threadIdx.x == 0 && m0 < M.n_bins) {
         atomicAdd(C.cell_stats + 4 * c, v[0]);
         atomicAdd(C.cell_stats + 4 * c + 1, v[1]);
         atomicAdd(C.cell_stats + 4 * c + 2, v[2]);
@@ -141,8 +136,11 @@ __global__ void __launch_bounds__(256) k_rta_solve(const DevTables* __restrict__
     const DevTables& T = *Tp;
     const int c = blockIdx.x;
     const DevMaterial& M = T.mat[C.cell_material[c]];
-    const int nc = M.n_classes; // this cell's material; arrays are strided by the largest count
-    double* cs = C.cls_sum + static_cast<size_t>(c) * C.n_classes * 3;
+    // the bins of an RTA cell are its mode classes: count, sum of n, sum of max(1, n)
+    const int nc = M.n_classes;
+    const size_t hb = static_cast<size_t>(c) * C.hist_modes;
+    const BinSum* bs = C.bins + hb;
+    const double* hm = C.hM + hb;
     double2* ab = C.rta_ab + static_cast<size_t>(c) * C.n_classes;
     const double Tc = C.temperature[c];
     const double dt = T.par.dt;
@@ -163,14 +161,14 @@ __global__ void __launch_bounds__(256) k_rta_solve(const DevTables* __restrict__
         const double Tt = fmax(0.0, temperature);
         double v[2] = {0.0, 0.0};
         for (int k = threadIdx.x; k < nc; k += blockDim.x) {
-            const double n0 = cs[3 * k];
+            const double n0 = static_cast<double>(bs[k].cnt);
             if (n0 == 0.0) continue;
             const double w = fmax(0.0, M.class_omega[k]);
             const double hw = kHbar * w;
             const double a = ab[k].x;
             if (!(hw > 0.0) || !(a > 0.0)) continue;
             const double neq = bose_dev(Tt, w);
-            v[0] += hw * a * (cs[3 * k + 1] - n0 * neq);
+            v[0] += hw * a * (bs[k].N - n0 * neq);
             if (want_slope && Tt > 0.0) v[1] -= n0 * hw * a * (hw * neq * (neq + 1.0) / (kKb * Tt * Tt));
         }
         block_sum<2>(v, red);
@@ -192,7 +190,7 @@ __global__ void __launch_bounds__(256) k_rta_solve(const DevTables* __restrict__
         Ts = high;
     } else {
         double sv[2] = {0.0, 0.0};
-        for (int k = threadIdx.x; k < nc; k += blockDim.x) sv[0] += kHbar * fmax(0.0, M.class_omega[k]) * ab[k].x * cs[3 * k + 2];
+        for (int k = threadIdx.x; k < nc; k += blockDim.x) sv[0] += kHbar * fmax(0.0, M.class_omega[k]) * ab[k].x * hm[k];
         block_sum<2>(sv, red);
         const double tol = 1e-13 * fmax(1.0, sv[0]);
         for (int it = 0; it < 40; ++it) {
@@ -212,9 +210,6 @@ __global__ void __launch_bounds__(256) k_rta_solve(const DevTables* __restrict__
     __syncthreads();
     for (int k = threadIdx.x; k < nc; k += blockDim.x) {
         ab[k].y = bose_dev(Ts, fmax(0.0, M.class_omega[k]));
-        cs[3 * k] = 0.0;
-        cs[3 * k + 1] = 0.0;
-        cs[3 * k + 2] = 0.0;
     }
 }
 
@@ -447,24 +442,25 @@ __global__ void __launch_bounds__(kStatThreads) k_cell_tables(const DevTables* _
     const int c = blockIdx.y;
     const DevMaterial& M = T.mat[C.cell_material[c]];
     const size_t hb = static_cast<size_t>(c) * C.hist_modes;
-    const int m0 = blockIdx.x * kChunk, m1 = min(M.n_active, m0 + kChunk);
+    const int m0 = blockIdx.x * kChunk, m1 = min(M.n_bins, m0 + kChunk);
     const double ratio = C.grad_ratio[c];
     const bool collide = phase >= 1 && kCollision != kCollideNone;
     double s[3] = {0.0, 0.0, 0.0}; // residual, drive, updates
-    for (int m = m0 + threadIdx.x; m < m1; m += blockDim.x) {
+    for (int b = m0 + threadIdx.x; b < m1; b += blockDim.x) {
+        const int m = M.bin_rep ? M.bin_rep[b] : b; // representative mode of the bin
         double a = 1.0, bc = 0.0;
         if (collide) {
             if (kCollision == kCollideRta) {
-                const double2 r = C.rta_ab[static_cast<size_t>(c) * C.n_classes + M.mode_class[m]];
+                const double2 r = C.rta_ab[static_cast<size_t>(c) * C.n_classes + b];
                 a = 1.0 - r.x;
                 bc = r.x * r.y;
             } else {
-                a = C.lin_decay[static_cast<size_t>(C.cell_material[c]) * C.hist_modes + m];
-                bc = C.lin_beta[hb + m];
+                a = C.lin_decay[static_cast<size_t>(C.cell_material[c]) * C.hist_modes + b];
+                bc = C.lin_beta[hb + b];
             }
         }
         const double D = M.grad_rate ? fma(-M.drive_cap[m], ratio, M.drive_rate[m]) : 0.0;
-        const BinSum bin = C.bins[hb + m];
+        const BinSum bin = C.bins[hb + b];
         const unsigned k = bin.cnt;
         if (k) {
             const double hw = M.hw[m];
@@ -474,21 +470,21 @@ __global__ void __launch_bounds__(kStatThreads) k_cell_tables(const DevTables* _
                 s[2] += k;
             }
         }
-        C.ab[hb + m] = make_double2(a, collide ? bc + 2.0 * D : D);
+        C.ab[hb + b] = make_double2(a, collide ? bc + 2.0 * D : D);
         if (!T.par.source_enabled) { // with a heat source the bins are cleared after its halves
             BinSum zero;
             zero.N = 0.0;
             zero.cnt = 0;
             zero.pad = 0;
-            C.bins[hb + m] = zero;
-            if (C.hM) C.hM[hb + m] = 0.0;
+            C.bins[hb + b] = zero;
+            if (C.hM) C.hM[hb + b] = 0.0;
         }
-        if (C.src_next) C.src_next[hb + m] = 0.0;
+        if (C.src_next) C.src_next[hb + b] = 0.0;
     }
     // the step-end energy deviation of the cell is the step-start one (cell
     // statistics) plus the collision change s[0] plus the drive change s[1]
     block_sum<3>(s, red);
-    if (threadIdx.x == 0 && m0 < M.n_active) {
+    if (threadIdx.x == 0 && m0 < M.n_bins) {
         double* f = C.cell_final + 4 * c;
         atomicAdd(f, s[0]);
         atomicAdd(f + 1, s[1]);
@@ -586,14 +582,16 @@ __global__ void __launch_bounds__(kStatThreads) k_source(const DevTables* __rest
     if (!(pend > 0.0)) return;
     const int mat = C.cell_material[c];
     const DevMaterial& M = T.mat[mat];
-    const int na = M.n_active;
+    const int na = M.n_bins; // bins of this cell (modes or classes); rep(b) stands for all its modes
     const size_t hb = static_cast<size_t>(c) * C.hist_modes;
     const double target = pend / M.energy_weight;
     const int spectrum = T.par.source_spectrum;
     // eligible carriers present, and the spectrum's normalization
     double v[4] = {0.0, 0.0, -1.0e300, 0.0}; // count, sum of weights (k w, k C), max log-weight
-    for (int m = threadIdx.x; m < na; m += blockDim.x) {
-        const unsigned k = C.bins[hb + m].cnt;
+    auto rep = [&](int b) { return M.bin_rep ? M.bin_rep[b] : b; };
+    for (int b = threadIdx.x; b < na; b += blockDim.x) {
+        const unsigned k = C.bins[hb + b].cnt;
+        const int m = rep(b);
         if (!k || !(M.src_weight[m] > 0.0)) continue;
         v[0] += k;
         if (spectrum == 1) v[1] += k * M.src_weight[m];
@@ -623,8 +621,9 @@ __global__ void __launch_bounds__(kStatThreads) k_source(const DevTables* __rest
     const double peak = v[2];
     if (spectrum == 2) {
         double g[1] = {0.0};
-        for (int m = threadIdx.x; m < na; m += blockDim.x) {
-            const unsigned k = C.bins[hb + m].cnt;
+        for (int b = threadIdx.x; b < na; b += blockDim.x) {
+            const unsigned k = C.bins[hb + b].cnt;
+            const int m = rep(b);
             if (k && M.src_weight[m] > 0.0) g[0] += k * exp(M.src_logw[m] - peak);
         }
         block_sum<1>(g, red);
@@ -644,9 +643,9 @@ __global__ void __launch_bounds__(kStatThreads) k_source(const DevTables* __rest
             n0[k] = bose_dev(base, M.src_class_omega[k]);
         }
         __syncthreads();
-        for (int m = threadIdx.x; m < na; m += blockDim.x) {
-            const unsigned k = C.bins[hb + m].cnt;
-            const int cls = M.src_class[m];
+        for (int b = threadIdx.x; b < na; b += blockDim.x) {
+            const unsigned k = C.bins[hb + b].cnt;
+            const int cls = M.src_class[rep(b)];
             if (k && cls >= 0) atomicAdd(cnt + cls, static_cast<double>(k));
         }
         __syncthreads();
@@ -702,14 +701,15 @@ __global__ void __launch_bounds__(kStatThreads) k_source(const DevTables* __rest
     double applied[1] = {0.0};
     double best = -1.0;
     int arg = 0x7fffffff;
-    for (int m = threadIdx.x; m < na; m += blockDim.x) {
-        const unsigned k = C.bins[hb + m].cnt;
+    for (int b = threadIdx.x; b < na; b += blockDim.x) {
+        const unsigned k = C.bins[hb + b].cnt;
+        const int m = rep(b);
         if (!k || !(M.src_weight[m] > 0.0)) continue;
         const double e = M.hw[m] * increment(m);
         applied[0] += k * e;
-        if (e > best || (e == best && m < arg)) {
+        if (e > best || (e == best && b < arg)) {
             best = e;
-            arg = m;
+            arg = b;
         }
     }
     block_sum<1>(applied, red);
@@ -740,18 +740,20 @@ __global__ void __launch_bounds__(kStatThreads) k_source(const DevTables* __rest
         s_arg = a;
     }
     __syncthreads();
-    const int corr_mode = s_arg;
-    const double corr = (target - applied[0]) / (M.hw[corr_mode] * C.bins[hb + corr_mode].cnt);
-    for (int m = threadIdx.x; m < na; m += blockDim.x) {
-        const unsigned k = C.bins[hb + m].cnt;
+    const int corr_bin = s_arg;
+    const int corr_mode = rep(corr_bin);
+    const double corr = (target - applied[0]) / (M.hw[corr_mode] * C.bins[hb + corr_bin].cnt);
+    for (int b = threadIdx.x; b < na; b += blockDim.x) {
+        const unsigned k = C.bins[hb + b].cnt;
+        const int m = rep(b);
         if (!k || !(M.src_weight[m] > 0.0)) continue;
         double inc = increment(m);
-        if (m == corr_mode) inc += corr;
-        C.ab[hb + m].y += inc;
-        if (next) C.src_next[hb + m] += inc;
+        if (b == corr_bin) inc += corr;
+        C.ab[hb + b].y += inc;
+        if (next) C.src_next[hb + b] += inc;
     }
     if (threadIdx.x == 0) {
-        const double raw = applied[0] + C.bins[hb + corr_mode].cnt * M.hw[corr_mode] * corr;
+        const double raw = applied[0] + C.bins[hb + corr_bin].cnt * M.hw[corr_mode] * corr;
         C.src_deposited[c] += pend;
         C.src_pending[c] = 0.0;
         if (next) {

@@ -79,6 +79,11 @@ struct DevMaterial {
     const int* src_class;      // [active], -1 when not eligible
     const double* src_class_omega;
     int n_src_classes;
+    // bins per cell: modes sharing every per-cell update share a bin (RTA:
+    // equal frequency and linewidths, and source weight); null = one bin per mode
+    const int* bin;            // [active] -> bin
+    const int* bin_rep;        // [bins] -> representative active mode
+    int n_bins;
     double energy_weight;
     double energy_density_bg;
     double heat_capacity_density_bg;

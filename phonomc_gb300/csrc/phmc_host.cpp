@@ -917,6 +917,18 @@ Problem build_problem(const SimulationConfig& cfg, SimulationDomain& domain,
     }
     P.kappa_axis = axis;
 
+    // Heat source (src/solver/HeatSourceDriving.cpp:8-11).
+    P.source.configure(cfg, domain);
+    if (P.source.enabled)
+        for (const PhononMaterial* m : mats)
+            for (int b : P.source.branches)
+                if (b >= m->branch_count())
+                    throw std::invalid_argument("heat_source.branches index exceeds a material's branch count.");
+    if (P.source.enabled && P.source.spectrum == HeatSourceSpectrum::Weighted)
+        for (const PhononMaterial* m : mats)
+            if (P.source.weights.size() != static_cast<size_t>(m->branch_count()))
+                throw std::invalid_argument("heat_source.branch_weights must match each material's branch count.");
+
     for (size_t mid = 0; mid < mats.size(); ++mid) {
         const PhononMaterial& M = *mats[mid];
         MaterialTables T;
@@ -967,8 +979,13 @@ Problem build_problem(const SimulationConfig& cfg, SimulationDomain& domain,
         // Mode classes: identical omega and identical linewidth row.
         std::vector<int> order(na);
         std::iota(order.begin(), order.end(), 0);
+        // with a heat source, modes of one class must also share its spectral weight
+        std::vector<double> sw(na, 0.0);
+        if (P.source.enabled)
+            for (int a = 0; a < na; ++a) sw[a] = P.source.mode_weight(M, T.active_flat[a]);
         auto key_less = [&](int a, int b) {
             if (T.omega[a] != T.omega[b]) return T.omega[a] < T.omega[b];
+            if (sw[a] != sw[b]) return sw[a] < sw[b];
             for (size_t it = 0; it < nT; ++it) {
                 const double ga = T.gamma_active[it * na + a], gb = T.gamma_active[it * na + b];
                 if (ga != gb) return ga < gb;
@@ -1037,18 +1054,6 @@ Problem build_problem(const SimulationConfig& cfg, SimulationDomain& domain,
         enabled.push_back(P.conservative ? reflecting : F.condition == 'R');
     }
     P.rough.build(mats, normals, rough, enabled, P.conservative, P.conservative ? Tbg : 0.0);
-
-    // Heat source (src/solver/HeatSourceDriving.cpp:8-11).
-    P.source.configure(cfg, domain);
-    if (P.source.enabled)
-        for (const PhononMaterial* m : mats)
-            for (int b : P.source.branches)
-                if (b >= m->branch_count())
-                    throw std::invalid_argument("heat_source.branches index exceeds a material's branch count.");
-    if (P.source.enabled && P.source.spectrum == HeatSourceSpectrum::Weighted)
-        for (const PhononMaterial* m : mats)
-            if (P.source.weights.size() != static_cast<size_t>(m->branch_count()))
-                throw std::invalid_argument("heat_source.branch_weights must match each material's branch count.");
 
     // Interface banks (src/solver/InterfaceInitialization.cpp:3-15, InterfaceInteraction.cpp:11-41).
     P.iface.enabled = mats.size() > 1;

@@ -118,7 +118,18 @@ void DeviceSolver::upload_tables() {
         const MaterialTables& M = P_.mats[mi];
         DevMaterial& D = T.mat[mi];
         D.n_active = M.n_active;
-        hist_modes = std::max(hist_modes, M.n_active);
+        // RTA bins are the mode classes (every per-cell update is class-uniform);
+        // linear response keeps one bin per mode (gain vectors and drive are per mode)
+        if (!P_.linearized) {
+            D.bin = upload(M.mode_class);
+            D.bin_rep = upload(M.class_rep);
+            D.n_bins = M.n_classes;
+        } else {
+            D.bin = nullptr;
+            D.bin_rep = nullptr;
+            D.n_bins = M.n_active;
+        }
+        hist_modes = std::max(hist_modes, D.n_bins);
         D.n_classes = M.n_classes;
         D.n_lookup = static_cast<int>(M.lookup_T.size());
         D.n_temps = static_cast<int>(M.temperatures.size());
@@ -376,8 +387,7 @@ void DeviceSolver::upload_tables() {
         // per-cell class sums; the stride is the largest class count of the materials
         int max_classes = 0;
         for (const auto& M : P_.mats) max_classes = std::max(max_classes, M.n_classes);
-        C.n_classes = max_classes;
-        C.cls_sum = dalloc<double>(static_cast<size_t>(ncells_) * max_classes * 3);
+        C.n_classes = max_classes; // == bins per cell
         C.rta_ab = dalloc<double2>(static_cast<size_t>(ncells_) * max_classes);
     } else {
         C.lin_beta = dalloc<double>(hist);

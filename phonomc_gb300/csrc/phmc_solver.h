@@ -64,8 +64,7 @@ struct CellArrays {
     double* cell_stats;      // [ncells*4] energy deviation, gradient rate sum, capacity sum
     double* cell_final;      // [ncells*4] lifetime residual, drive energy, drive updates, final energy deviation
     int mixed;               // FP32 linear-response exponential with FP64 energy rescale
-    // RTA: per (cell, class) multiplicity / occupation / max(1, n) sums and (a, n_eq(T*))
-    double* cls_sum;
+    // RTA: per (cell, class) (a, n_eq(T*)); the class sums are the bins
     double2* rta_ab;
     // linear response: beta of the pending update per (cell, mode)
     double* lin_beta;

@@ -217,23 +217,28 @@ __device__ bool advance_carrier(const DevTables& T, DevLedger* L, BlockLedger* b
 }
 
 // ------------------------------------------------------------------ bins
-__device__ __forceinline__ void bin_carrier(const CellArrays& C, DevLedger* L, int slot, int cell, int mid, int ai,
-                                           double occ, bool rta) {
+__device__ __forceinline__ int bin_of(const DevMaterial& M, int ai) { return M.bin ? __ldg(M.bin + ai) : ai; }
+
+__device__ __forceinline__ void bin_carrier(const DevTables& T, const CellArrays& C, DevLedger* L, int slot, int cell,
+                                           uint32_t w, double occ, bool rta) {
+    const int mid = static_cast<int>(w >> 28);
     const bool finite = (__double2hiint(occ) & 0x7ff00000) != 0x7ff00000;
     if (cell < 0 || cell >= C.ncells || C.cell_material[cell] != mid || !finite) {
         raise_error(L, kErrInvalidStatistics, slot);
         return;
     }
-    const size_t h = static_cast<size_t>(cell) * C.hist_modes + ai;
+    const size_t h = static_cast<size_t>(cell) * C.hist_modes + bin_of(T.mat[mid], static_cast<int>(w & 0x00FFFFFFu));
     atomicAdd(&C.bins[h].cnt, 1u);
     atomicAdd(&C.bins[h].N, occ);
     if (rta) atomicAdd(C.hM + h, fmax(1.0, occ));
 }
 
 // Pending (alpha, beta) of the carrier's bin: collision of the previous step
-// and the gradient half-steps around this transport.
-__device__ __forceinline__ double apply_pending(const CellArrays& C, int cell, int ai, double occ) {
-    const double2 ab = __ldg(C.ab + static_cast<size_t>(cell) * C.hist_modes + ai);
+// and the gradient / heat-source halves around this transport.
+__device__ __forceinline__ double apply_pending(const DevTables& T, const CellArrays& C, int cell, uint32_t w,
+                                                double occ) {
+    const int b = bin_of(T.mat[w >> 28], static_cast<int>(w & 0x00FFFFFFu));
+    const double2 ab = __ldg(C.ab + static_cast<size_t>(cell) * C.hist_modes + b);
     return fma(ab.x, occ, ab.y);
 }
 
@@ -521,7 +526,7 @@ __device__ __forceinline__ void finish_mixed(const DevTables& T, const CarrierSt
         return;
     }
     __stcs(S.cell + i, c);
-    bin_carrier(C, L, i, c, static_cast<int>(w >> 28), static_cast<int>(w & 0x00FFFFFFu), occ, kRta);
+    bin_carrier(T, C, L, i, c, w, occ, kRta);
 }
 
 constexpr int kTransportThreads = 256;
@@ -550,7 +555,7 @@ __global__ void __launch_bounds__(kTransportThreads) k_transport(const __grid_co
             if (i < n && __ldcs(S.alive + i)) {
                 uint32_t w = __ldcs(S.mode + i);
                 const int c0 = __ldcs(S.cell + i);
-                double occ = apply_pending(C, c0, static_cast<int>(w & 0x00FFFFFFu), __ldcs(S.occ + i));
+                double occ = apply_pending(T, C, c0, w, __ldcs(S.occ + i));
                 const Frame F = cell_frame(T.dom, c0);
                 float p[3] = {__ldcs(S.ox + i), __ldcs(S.oy + i), __ldcs(S.oz + i)};
                 float remaining = T.par.dt32;
@@ -606,7 +611,7 @@ __global__ void __launch_bounds__(kTransportThreads) k_transport(const __grid_co
             if (!__ldcs(S.alive + i)) continue;
             uint32_t w = __ldcs(S.mode + i);
             const int c0 = __ldcs(S.cell + i);
-            double occ = apply_pending(C, c0, static_cast<int>(w & 0x00FFFFFFu), __ldcs(S.occ + i));
+            double occ = apply_pending(T, C, c0, w, __ldcs(S.occ + i));
             double p[3] = {__ldcs(S.x + i), __ldcs(S.y + i), __ldcs(S.z + i)};
             const bool alive = advance_carrier(T, L, &bl, i, p, w, occ, T.par.dt, kDrawTransport, step);
             const int c = grid_index(T.dom, p[0], p[1], p[2]);
@@ -620,7 +625,7 @@ __global__ void __launch_bounds__(kTransportThreads) k_transport(const __grid_co
                 continue;
             }
             __stcs(S.cell + i, c);
-            bin_carrier(C, L, i, c, static_cast<int>(w >> 28), static_cast<int>(w & 0x00FFFFFFu), occ, kRta);
+            bin_carrier(T, C, L, i, c, w, occ, kRta);
         }
     }
     __syncthreads();
@@ -674,7 +679,7 @@ __global__ void k_histogram(const DevTables* __restrict__ Tp, CarrierState S, Ce
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         if (!S.alive[i]) continue;
         const uint32_t w = S.mode[i];
-        bin_carrier(C, L, i, S.cell[i], static_cast<int>(w >> 28), static_cast<int>(w & 0x00FFFFFFu), S.occ[i], kRta);
+        bin_carrier(*Tp, C, L, i, S.cell[i], w, S.occ[i], kRta);
     }
 }
 
@@ -939,7 +944,7 @@ __global__ void __launch_bounds__(256) k_inject(const DevTables* __restrict__ Tp
         S.occ[slot] = occ;
         S.alive[slot] = alive ? 1 : 0;
         S.cell[slot] = alive ? c : 0;
-        if (alive) bin_carrier(C, L, slot, c, static_cast<int>(w >> 28), static_cast<int>(w & 0x00FFFFFFu), occ, kRta);
+        if (alive) bin_carrier(T, C, L, slot, c, w, occ, kRta);
     }
     __syncthreads();
     block_ledger_flush(&bl, L);
@@ -993,8 +998,8 @@ __global__ void __launch_bounds__(256) k_flux(const DevTables* __restrict__ Tp, 
         const DevMaterial& M = T.mat[w >> 28];
         const int ai = static_cast<int>(w & 0x00FFFFFFu);
         const int c = S.cell[i];
-        double occ = apply_pending(C, c, ai, S.occ[i]) - drive_half(T, C, M, c, ai);
-        if (C.src_next) occ -= C.src_next[static_cast<size_t>(c) * C.hist_modes + ai];
+        double occ = apply_pending(T, C, c, w, S.occ[i]) - drive_half(T, C, M, c, ai);
+        if (C.src_next) occ -= C.src_next[static_cast<size_t>(c) * C.hist_modes + bin_of(M, ai)];
         const double e = dmul(dmul(M.hw[ai], occ - M.nbg[ai]), M.energy_weight);
         double v[3];
         mode_velocity(M, w, v);
@@ -1018,10 +1023,10 @@ __global__ void k_apply_pending(const DevTables* __restrict__ Tp, CarrierState S
         const uint32_t w = S.mode[i];
         const int ai = static_cast<int>(w & 0x00FFFFFFu);
         const int c = S.cell[i];
-        double occ = apply_pending(C, c, ai, S.occ[i]);
+        double occ = apply_pending(T, C, c, w, S.occ[i]);
         if (subtract_drive) {
             occ -= drive_half(T, C, T.mat[w >> 28], c, ai);
-            if (C.src_next) occ -= C.src_next[static_cast<size_t>(c) * C.hist_modes + ai];
+            if (C.src_next) occ -= C.src_next[static_cast<size_t>(c) * C.hist_modes + bin_of(T.mat[w >> 28], ai)];
         }
         S.occ[i] = occ;
     }
