@@ -233,13 +233,14 @@ def _time_arm(lib, abi, cfg, materials, steps, warmup):
     m = [abi.Material(lib, "phmc_", d, 0.1, st, bz) for d, st, bz in materials]
     s = abi.Solver(lib, "phmc_", cfg, m)
     s.run(warmup)
-    n0 = s.stats()["particle_count"]
-    tot, kern, launches = C.c_double(), C.c_double(), C.c_int64()
+    tot, kern, launches, n0, n1 = C.c_double(), C.c_double(), C.c_int64(), C.c_int64(), C.c_int64()
     with ClockSampler() as clk:
-        s.check(lib.phmc_solver_timed_run(s.h, steps, C.byref(tot), C.byref(kern), C.byref(launches)))
-    n1 = s.stats()["particle_count"]
-    return {"solver": s, "material": m, "ms": tot.value, "kernel_ms": kern.value, "launches": int(launches.value),
-            "carrier_steps": 0.5 * (n0 + n1) * steps, "carriers": n0, "clocks": clk.summary()}
+        s.check(lib.phmc_solver_timed_run(s.h, steps, C.byref(tot), C.byref(kern), C.byref(launches), C.byref(n0),
+                                          C.byref(n1)))
+    n0, n1 = n0.value, n1.value
+    return {"solver": s, "material": m, "ms": tot.value, "kernel_ms_per_launch": kern.value,
+            "launches": int(launches.value), "carrier_steps": 0.5 * (n0 + n1) * steps, "carriers": n0,
+            "clocks": clk.summary()}
 
 
 def run_ours(args):
@@ -270,7 +271,7 @@ def run_ours(args):
         ms, carrier_steps = float(mx[0]), float(sm[1])
     value = carrier_steps / (ms * 1e-3)
     bpc = BYTES_PER_CARRIER[args.precision]
-    kavg = main_arm["kernel_ms"] / args.steps
+    kavg = main_arm["kernel_ms_per_launch"]
     achieved = bpc * main_arm["carriers"] / (kavg * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
 
@@ -319,7 +320,7 @@ def run_ours(args):
     }
     if plain is not None:
         pv = plain["carrier_steps"] / (plain["ms"] * 1e-3)
-        pk = plain["kernel_ms"] / max(1, round(plain["carrier_steps"] / max(1, plain["carriers"])))
+        pk = plain["kernel_ms_per_launch"]
         line["plain_fp64"] = {"value": pv, "unit": UNIT, "ms_per_step": plain["ms"] / max(3, args.steps // 4),
                               "mixed_over_plain": value / pv,
                               "roofline_frac": 76 * plain["carriers"] / (pk * 1e-3) / 1e9 / peak,

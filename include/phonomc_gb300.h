@@ -174,10 +174,18 @@ int phmc_solver_set_carriers(phmc_solver* s, int64_t n, const double* x, const d
 int phmc_solver_run_from_host(phmc_solver* s, int64_t n, const double* x, const double* y, const double* z,
                               const double* occupation, const uint32_t* mode_word, int steps,
                               double* cell_temperature_out);
-/* Runs `steps` timesteps bracketed by CUDA events on the solver's stream:
- * total_ms is the device time of the region, kernel_ms the summed duration of
- * its transport-pass launches, launches the number of kernels launched. */
-int phmc_solver_timed_run(phmc_solver* s, int steps, double* total_ms, double* kernel_ms, int64_t* launches);
+/* Measurement helper (no counterpart in the reference): first up to three
+ * steps with CUDA events around the carrier pass (kernel_ms = its mean duration
+ * per launch), then `steps` timesteps bracketed by CUDA events on the solver's
+ * stream (total_ms; replayed from the captured step graph unless disabled);
+ * launches counts the kernels of the timed region, live_before/live_after the
+ * live carriers at its ends (either may be NULL). */
+int phmc_solver_timed_run(phmc_solver* s, int steps, double* total_ms, double* kernel_ms, int64_t* launches,
+                          int64_t* live_before, int64_t* live_after);
+/* Timesteps are captured once into a CUDA graph and replayed (default 1);
+ * 0 launches every kernel of every step from the host. No counterpart in the
+ * reference. */
+int phmc_solver_set_graphs(phmc_solver* s, int on);
 /* Page-lock / release caller-owned host buffers used for end-to-end stepping. */
 int phmc_host_register(void* ptr, int64_t bytes);
 int phmc_host_unregister(void* ptr);

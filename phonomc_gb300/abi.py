@@ -390,7 +390,8 @@ DEVICE_PROTOS = {
     "solver_run_timestep": (C.c_int, [C.c_void_p]),
     "solver_synchronize": (C.c_int, [C.c_void_p]),
     "solver_write_outputs": (C.c_int, [C.c_void_p]),
-    "solver_timed_run": (C.c_int, [C.c_void_p, C.c_int, c_double_p, c_double_p, c_int64_p]),
+    "solver_timed_run": (C.c_int, [C.c_void_p, C.c_int, c_double_p, c_double_p, c_int64_p, c_int64_p, c_int64_p]),
+    "solver_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "host_register": (C.c_int, [C.c_void_p, C.c_int64]),
     "host_unregister": (C.c_int, [C.c_void_p]),
     "solver_run_from_host": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_double_p, c_double_p, c_double_p,

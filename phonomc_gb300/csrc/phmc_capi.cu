@@ -226,12 +226,19 @@ int phmc_solver_run_from_host(phmc_solver* s, int64_t n, const double* x, const 
     });
 }
 
-int phmc_solver_timed_run(phmc_solver* s, int steps, double* total_ms, double* kernel_ms, int64_t* launches) {
+int phmc_solver_timed_run(phmc_solver* s, int steps, double* total_ms, double* kernel_ms, int64_t* launches,
+                          int64_t* live_before, int64_t* live_after) {
     return guard([&] {
-        long long l = 0;
-        s->s->timed_run(steps, *total_ms, *kernel_ms, l);
+        long long l = 0, n0 = 0, n1 = 0;
+        s->s->timed_run(steps, *total_ms, *kernel_ms, l, n0, n1);
         *launches = l;
+        if (live_before) *live_before = n0;
+        if (live_after) *live_after = n1;
     });
+}
+
+int phmc_solver_set_graphs(phmc_solver* s, int on) {
+    return guard([&] { s->s->set_graphs(on != 0); });
 }
 
 int phmc_host_register(void* ptr, int64_t bytes) {

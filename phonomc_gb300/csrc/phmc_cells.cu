@@ -546,6 +546,8 @@ __global__ void __launch_bounds__(1024) k_cells_final(const DevTables* __restric
     L->thermal_energy = v[0];
     L->particle_count += static_cast<long long>(L->step_injected) - static_cast<long long>(L->step_absorbed);
     for (int r = 0; r < kMaxReservoirs; ++r) L->previous_res[r] = L->absorbed_res[r];
+    L->step_index += 1;
+    L->elapsed += T.par.dt;
 }
 
 // ------------------------------------------------------- heat source
@@ -558,12 +560,16 @@ __global__ void __launch_bounds__(1024) k_cells_final(const DevTables* __restric
 // step (energy booked to that step). Base temperature of the thermal Newton:
 // `temperature` (cell temperatures of the current refresh).
 __global__ void __launch_bounds__(kStatThreads) k_source(const DevTables* __restrict__ Tp, CellArrays C, DevLedger* L,
-                                                         double factor, const double* temperature, int next) {
+                                                         const double* temperature, int next) {
     __shared__ double red[4 * 32];
     __shared__ double s_pend;
     __shared__ int s_arg;
     const DevTables& T = *Tp;
     const int c = blockIdx.x;
+    // this half's time window: second half of the running step, or first half of the coming one
+    const double t0 = L->elapsed, half = __dmul_rn(0.5, T.par.dt);
+    const double factor = next ? source_time_factor(T.par, t0, __dadd_rn(t0, half))
+                               : source_time_factor(T.par, __dadd_rn(t0, half), __dadd_rn(t0, T.par.dt));
     if (threadIdx.x == 0) {
         if (next) {
             C.src_step_pending[c] = C.src_pending[c];
@@ -770,8 +776,8 @@ __global__ void __launch_bounds__(kStatThreads) k_source(const DevTables* __rest
 // ----------------------------------------------------------- launchers
 void launch_step_begin(const LaunchCtx& x) { k_step_begin<<<1, 1, 0, x.stream>>>(x.L); }
 
-void launch_source(const LaunchCtx& x, double factor, bool final_temperature, bool next) {
-    k_source<<<x.C.ncells, kStatThreads, 0, x.stream>>>(x.T, x.C, x.L, factor,
+void launch_source(const LaunchCtx& x, bool final_temperature, bool next) {
+    k_source<<<x.C.ncells, kStatThreads, 0, x.stream>>>(x.T, x.C, x.L,
                                                          final_temperature ? x.C.temperature_final : x.C.temperature,
                                                          next ? 1 : 0);
     if (next) {

@@ -154,6 +154,8 @@ struct DevParams {
     int source_enabled;
     int source_spectrum;        // 0 thermal, 1 weighted, 2 gaussian
     int source_linearized;      // thermal spectrum with linearized transport
+    int source_pulsed;          // time profile (src/solver/HeatSourceDriving.cpp:12-44)
+    double source_time_start, source_time_end, source_period, source_on, source_amplitude;
 };
 
 // Per-step accumulators and running totals, all on the device so a step needs
@@ -165,6 +167,8 @@ struct DevLedger {
     int n_holes;            // free slots below n_slots at injection
     int n_inject;           // carriers injected this step
     int n_deferred;         // wall events queued by the mixed transport pass this step
+    uint32_t step_index;    // timesteps completed (the draw counter of the running step)
+    double elapsed;         // ps at the start of the running step
     int inject_count[kMaxReservoirs];
     int inject_offset[kMaxReservoirs + 1];
     unsigned int absorbed_res[kMaxReservoirs];  // this step
@@ -575,6 +579,24 @@ __device__ __forceinline__ IfaceOut interface_dev(const DevTables& T, int src, i
     r.action = transmit ? 4 : 3;
     r.transmitted = transmit ? 1 : 0;
     return r;
+}
+
+// Heat-source energy factor (ps) of [begin, end] under the time profile
+// (src/solver/HeatSourceDriving.cpp:12-44), in the same rounding as the host.
+__device__ __forceinline__ double source_time_factor(const DevParams& P, double begin_ps, double end_ps) {
+    const double begin = fmax(begin_ps, P.source_time_start);
+    const double end = P.source_time_end >= 0.0 ? fmin(end_ps, P.source_time_end) : end_ps;
+    if (end <= begin) return 0.0;
+    if (!P.source_pulsed) return __dmul_rn(P.source_amplitude, __dadd_rn(end, -begin));
+    const double period = P.source_period, on = P.source_on;
+    if (on <= 0.0) return 0.0;
+    auto on_time = [&](double rel) {
+        if (!(rel > 0.0)) return 0.0;
+        const double cycles = floor(rel / period);
+        return __dadd_rn(__dmul_rn(cycles, on), fmin(__dadd_rn(rel, -__dmul_rn(cycles, period)), on));
+    };
+    const double rb = __dadd_rn(begin, -P.source_time_start), re = __dadd_rn(end, -P.source_time_start);
+    return __dmul_rn(P.source_amplitude, fmax(0.0, __dadd_rn(on_time(re), -on_time(rb))));
 }
 
 } // namespace phmc

@@ -22,7 +22,7 @@ struct LaunchCtx {
     int grid_blocks;
 };
 
-int launch_transport(const LaunchCtx& x, bool mixed, bool rta, uint32_t step);
+int launch_transport(const LaunchCtx& x, bool mixed, bool rta);
 void launch_histogram(const LaunchCtx& x, bool rta);
 void launch_init_cells(const LaunchCtx& x, bool mixed);
 // Carriers read straight from device-accessible (registered) host arrays.
@@ -34,13 +34,13 @@ struct HostCarriers {
 void launch_ingest(const LaunchCtx& x, bool mixed, const HostCarriers& h);
 void launch_ledger_replace(const LaunchCtx& x, int n);
 void launch_positions_out(const LaunchCtx& x);
-int launch_inject(const LaunchCtx& x, bool mixed, bool rta, int* holes, int* block_dead, int capacity, uint32_t step);
+int launch_inject(const LaunchCtx& x, bool mixed, bool rta, int* holes, int* block_dead, int capacity);
 void launch_containment(const LaunchCtx& x, bool mixed);
 void launch_flux(const LaunchCtx& x, bool mixed);
 void launch_apply_pending(const LaunchCtx& x, bool subtract_drive);
 void launch_step_begin(const LaunchCtx& x);
-// One heat-source half: accrue `factor` ps of power, deposit into the pending updates.
-void launch_source(const LaunchCtx& x, double factor, bool final_temperature, bool next);
+// One heat-source half (time window from the device clock): accrue, deposit into the pending updates.
+void launch_source(const LaunchCtx& x, bool final_temperature, bool next);
 int launch_cell_solve(const LaunchCtx& x, int phase, int collision);
 int linear_cluster_size(const CellArrays& C, bool mixed);
 void prepare_linear_solve(const CellArrays& C);

@@ -76,11 +76,25 @@ DeviceSolver::DeviceSolver(const SimulationConfig& cfg, const std::vector<const 
             << format_convergence_header(ncells_, cfg_.temperature_gradient.has_value());
     }
     flux_pass();
-    append_convergence_row();
 }
 
 DeviceSolver::~DeviceSolver() {
     if (stream_) cudaStreamSynchronize(stream_);
+    try {
+        drain_observations(true);
+    } catch (...) {
+    }
+    for (Observation* o : obs_pending_) obs_free_.push_back(o);
+    for (Observation* o : obs_free_) {
+        cudaFreeHost(o->T);
+        cudaFreeHost(o->E);
+        cudaFreeHost(o->q);
+        cudaFreeHost(o->L);
+        cudaEventDestroy(o->done);
+        delete o;
+    }
+    if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+    if (graph_) cudaGraphDestroy(graph_);
     for (void* p : allocations_) cudaFree(p);
     if (d_tables_) cudaFree(d_tables_);
     if (stream_) cudaStreamDestroy(stream_);
@@ -349,6 +363,13 @@ void DeviceSolver::upload_tables() {
     p.source_spectrum = P_.source.spectrum == HeatSourceSpectrum::Weighted ? 1
                         : P_.source.spectrum == HeatSourceSpectrum::Gaussian ? 2 : 0;
     p.source_linearized = P_.source.linearized_thermal ? 1 : 0;
+    p.source_pulsed = cfg_.heat_source_time_profile == HeatSourceTimeProfile::Pulsed ? 1 : 0;
+    p.source_time_start = cfg_.heat_source_time_start;
+    p.source_time_end = cfg_.heat_source_time_end;
+    p.source_period = cfg_.heat_source_period;
+    p.source_on = cfg_.heat_source_on_duration < 0.0 ? cfg_.heat_source_duty_cycle * cfg_.heat_source_period
+                                                      : cfg_.heat_source_on_duration;
+    p.source_amplitude = cfg_.heat_source_amplitude;
     PHMC_CUDA(cudaMalloc(&d_tables_, sizeof(DevTables)));
     PHMC_CUDA(cudaMemcpyAsync(d_tables_, &tables_, sizeof(DevTables), cudaMemcpyHostToDevice, stream_));
 
@@ -480,7 +501,7 @@ void DeviceSolver::initial_statistics() {
     launch_cells_final(x, 0);
     if (P_.source.enabled) {
         // first heat-source half of the coming step (src/MonteCarloSolver.cpp:364-370)
-        launch_source(x, heat_source_time_factor(cfg_, elapsed_, elapsed_ + 0.5 * cfg_.time_step), true, true);
+        launch_source(x, true, true);
         counters_.launches += 1;
     }
     materialized_ = true;
@@ -538,50 +559,78 @@ void DeviceSolver::set_carriers(long long n, const double* x, const double* y, c
     if (!keep_clock) synchronize();
 }
 
-void DeviceSolver::run_timestep() {
-    if (failed_) throw std::runtime_error("Cannot resume a failed timestep; construct a new solver after fixing its cause.");
-    failed_ = true;
+// The launches of one timestep (src/MonteCarloSolver.cpp:348-398): transport,
+// injection, cell solve, heat-source halves, ledger. Step-dependent values
+// (draw counter, time windows) are read on the device, so the same sequence is
+// captured once into a graph and replayed.
+void DeviceSolver::enqueue_step(bool profile) {
     const LaunchCtx x = ctx();
     const int coll = collision_kind();
     launch_step_begin(x);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    if (profile_pass_a_) {
+    if (profile) {
         PHMC_CUDA(cudaEventCreate(&e0));
         PHMC_CUDA(cudaEventCreate(&e1));
         PHMC_CUDA(cudaEventRecord(e0, stream_));
     }
-    counters_.launches += 1 + launch_transport(x, mixed_, coll == kCollideRta, static_cast<uint32_t>(step_));
-    if (profile_pass_a_) {
+    counters_.launches += 1 + launch_transport(x, mixed_, coll == kCollideRta);
+    if (profile) {
         PHMC_CUDA(cudaEventRecord(e1, stream_));
         pass_a_events_.push_back({e0, e1});
     }
     if (!P_.reservoirs.empty())
-        counters_.launches += launch_inject(x, mixed_, coll == kCollideRta, d_holes_, d_block_dead_, state_.capacity,
-                                            static_cast<uint32_t>(step_));
-    if (step_ % 100 == 0) {
-        launch_containment(x, mixed_);
-        counters_.launches += 1;
-    }
+        counters_.launches += launch_inject(x, mixed_, coll == kCollideRta, d_holes_, d_block_dead_, state_.capacity);
     counters_.launches += 1 + launch_cell_solve(x, 1, coll);
-    const double mid = elapsed_ + 0.5 * cfg_.time_step, end = elapsed_ + cfg_.time_step;
     if (P_.source.enabled) {
         // second heat-source half of this step, after the collision (src/MonteCarloSolver.cpp:376)
-        launch_source(x, heat_source_time_factor(cfg_, mid, end), false, false);
+        launch_source(x, false, false);
         counters_.launches += 1;
     }
     launch_cells_final(x, 1);
     if (P_.source.enabled) {
         // first half of the next step, folded into the pending update
-        launch_source(x, heat_source_time_factor(cfg_, end, end + 0.5 * cfg_.time_step), true, true);
+        launch_source(x, true, true);
+        counters_.launches += 1;
+    }
+}
+
+void DeviceSolver::capture_step_graph() {
+    const long long l0 = counters_.launches;
+    PHMC_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    try {
+        enqueue_step(false);
+    } catch (...) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(stream_, &g);
+        if (g) cudaGraphDestroy(g);
+        counters_.launches = l0;
+        throw;
+    }
+    PHMC_CUDA(cudaStreamEndCapture(stream_, &graph_));
+    PHMC_CUDA(cudaGraphInstantiate(&graph_exec_, graph_, 0));
+    graph_launches_ = counters_.launches - l0;
+    counters_.launches = l0;
+}
+
+void DeviceSolver::run_timestep() {
+    if (failed_) throw std::runtime_error("Cannot resume a failed timestep; construct a new solver after fixing its cause.");
+    failed_ = true;
+    if (use_graphs_ && !profile_pass_a_) {
+        if (!graph_exec_) capture_step_graph();
+        PHMC_CUDA(cudaGraphLaunch(graph_exec_, stream_));
+        counters_.launches += graph_launches_;
+    } else {
+        enqueue_step(profile_pass_a_);
+    }
+    if (step_ % 100 == 0) {
+        // src/solver/TransportOperator.cpp:364-402, every 100 steps
+        launch_containment(ctx(), mixed_);
         counters_.launches += 1;
     }
     materialized_ = false;
     ++step_;
     elapsed_ += cfg_.time_step;
-    if (step_ == 1 || step_ % cfg_.convergence_write_interval == 0) {
-        flux_pass();
-        append_convergence_row();
-    }
+    if (step_ == 1 || step_ % cfg_.convergence_write_interval == 0) flux_pass();
     failed_ = false;
 }
 
@@ -624,21 +673,14 @@ double DeviceSolver::drive_only() {
     return r;
 }
 
-void DeviceSolver::timed_run(int steps, double& total_ms, double& kernel_ms, long long& launches) {
-    synchronize();
-    cudaEvent_t a, b;
-    PHMC_CUDA(cudaEventCreate(&a));
-    PHMC_CUDA(cudaEventCreate(&b));
-    const long long l0 = counters_.launches;
+void DeviceSolver::timed_run(int steps, double& total_ms, double& kernel_ms, long long& launches,
+                             long long& live_before, long long& live_after) {
+    // carrier-pass duration from a few eager steps with events around it
+    const int profiled = std::max(1, std::min(steps, 3));
     profile_pass_a_ = true;
-    PHMC_CUDA(cudaEventRecord(a, stream_));
-    run(steps);
-    PHMC_CUDA(cudaEventRecord(b, stream_));
+    run(profiled);
     profile_pass_a_ = false;
     synchronize();
-    float ms = 0;
-    PHMC_CUDA(cudaEventElapsedTime(&ms, a, b));
-    total_ms = ms;
     kernel_ms = 0;
     for (auto& ev : pass_a_events_) {
         float k = 0;
@@ -647,10 +689,28 @@ void DeviceSolver::timed_run(int steps, double& total_ms, double& kernel_ms, lon
         cudaEventDestroy(ev.first);
         cudaEventDestroy(ev.second);
     }
+    kernel_ms /= static_cast<double>(pass_a_events_.size() ? pass_a_events_.size() : 1);
     pass_a_events_.clear();
+    // the timed region: `steps` steps (graph replays), events on the solver stream
+    DevLedger L;
+    PHMC_CUDA(cudaMemcpy(&L, d_ledger_, sizeof L, cudaMemcpyDeviceToHost));
+    live_before = L.particle_count;
+    cudaEvent_t a, b;
+    PHMC_CUDA(cudaEventCreate(&a));
+    PHMC_CUDA(cudaEventCreate(&b));
+    const long long l0 = counters_.launches;
+    PHMC_CUDA(cudaEventRecord(a, stream_));
+    run(steps);
+    PHMC_CUDA(cudaEventRecord(b, stream_));
+    synchronize();
+    float ms = 0;
+    PHMC_CUDA(cudaEventElapsedTime(&ms, a, b));
+    total_ms = ms;
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     launches = counters_.launches - l0;
+    PHMC_CUDA(cudaMemcpy(&L, d_ledger_, sizeof L, cudaMemcpyDeviceToHost));
+    live_after = L.particle_count;
 }
 
 void DeviceSolver::run(int steps) {
@@ -659,6 +719,7 @@ void DeviceSolver::run(int steps) {
 
 void DeviceSolver::synchronize() {
     PHMC_CUDA(cudaStreamSynchronize(stream_));
+    drain_observations(true);
     check_error();
 }
 
@@ -672,18 +733,61 @@ void DeviceSolver::check_error() {
     }
 }
 
+// Heat flux tally at step 1 and every convergence_write_interval steps. The
+// device results and the ledger are copied into a pinned slot; the host part
+// (flux average, kappa, convergence.txt row) runs when the slot's event has
+// completed, so stepping never waits on it.
 void DeviceSolver::flux_pass() {
+    drain_observations(false);
+    Observation* o;
+    if (!obs_free_.empty()) {
+        o = obs_free_.back();
+        obs_free_.pop_back();
+    } else if (obs_pending_.size() >= 8) {
+        drain_observations(true);
+        o = obs_free_.back();
+        obs_free_.pop_back();
+    } else {
+        o = new Observation;
+        PHMC_CUDA(cudaMallocHost(&o->T, ncells_ * sizeof(double)));
+        PHMC_CUDA(cudaMallocHost(&o->E, ncells_ * sizeof(double)));
+        PHMC_CUDA(cudaMallocHost(&o->q, 3 * ncells_ * sizeof(double)));
+        PHMC_CUDA(cudaMallocHost(&o->L, sizeof(DevLedger)));
+        PHMC_CUDA(cudaEventCreateWithFlags(&o->done, cudaEventDisableTiming));
+    }
+    o->step = step_;
+    o->elapsed = elapsed_;
     const LaunchCtx x = ctx();
     PHMC_CUDA(cudaMemsetAsync(cells_.flux, 0, 3 * sizeof(double) * ncells_, stream_));
     launch_flux(x, mixed_);
     counters_.launches += 1;
-    synchronize();
-    host_T_.resize(ncells_);
-    host_E_.resize(ncells_);
-    host_q_.resize(3 * static_cast<size_t>(ncells_));
-    PHMC_CUDA(cudaMemcpy(host_T_.data(), cells_.temperature_final, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
-    PHMC_CUDA(cudaMemcpy(host_E_.data(), cells_.energy_final, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
-    PHMC_CUDA(cudaMemcpy(host_q_.data(), cells_.flux, 3 * ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
+    PHMC_CUDA(cudaMemcpyAsync(o->T, cells_.temperature_final, ncells_ * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    PHMC_CUDA(cudaMemcpyAsync(o->E, cells_.energy_final, ncells_ * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    PHMC_CUDA(cudaMemcpyAsync(o->q, cells_.flux, 3 * ncells_ * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    PHMC_CUDA(cudaMemcpyAsync(o->L, d_ledger_, sizeof(DevLedger), cudaMemcpyDeviceToHost, stream_));
+    PHMC_CUDA(cudaEventRecord(o->done, stream_));
+    obs_pending_.push_back(o);
+}
+
+void DeviceSolver::drain_observations(bool wait) {
+    while (!obs_pending_.empty()) {
+        Observation* o = obs_pending_.front();
+        if (wait) PHMC_CUDA(cudaEventSynchronize(o->done));
+        else {
+            const cudaError_t q = cudaEventQuery(o->done);
+            if (q == cudaErrorNotReady) return;
+            PHMC_CUDA(q);
+        }
+        obs_pending_.erase(obs_pending_.begin());
+        process_observation(*o);
+        obs_free_.push_back(o);
+    }
+}
+
+void DeviceSolver::process_observation(Observation& o) {
+    host_T_.assign(o.T, o.T + ncells_);
+    host_E_.assign(o.E, o.E + ncells_);
+    host_q_.assign(o.q, o.q + 3 * static_cast<size_t>(ncells_));
     // src/solver/GridStatistics.cpp:334-343 and src/solver/Observables.cpp:38-144
     const auto& vol = domain_->grid_volumes();
     const int axis = P_.kappa_axis;
@@ -694,6 +798,18 @@ void DeviceSolver::flux_pass() {
         tv += vol[c];
     }
     avg_flux_ = phi / tv;
+    update_kappa();
+    if (!cfg_.output_folder.empty()) {
+        phmc_stats s;
+        stats_from_ledger(*o.L, s);
+        append_convergence_row(o, s);
+    }
+}
+
+// kappa_eff from the reservoir temperatures (or the imposed gradient) and
+// kappa_int from the fitted cell-temperature slope (src/solver/Observables.cpp:38-144).
+void DeviceSolver::update_kappa() {
+    const int axis = P_.kappa_axis;
     kappa_fit_ = kappa_end_ = 0;
     if (!cfg_.compute_kappa) return;
     if (cfg_.temperature_gradient) {
@@ -730,12 +846,9 @@ void DeviceSolver::flux_pass() {
     kappa_fit_ = std::abs(gf) > 1e-18 ? -avg_flux_ / gf : 0.0;
 }
 
-void DeviceSolver::read_stats(phmc_stats& o) {
-    synchronize();
-    DevLedger L;
-    PHMC_CUDA(cudaMemcpy(&L, d_ledger_, sizeof L, cudaMemcpyDeviceToHost));
+// Ledger-derived fields of phmc_stats.
+void stats_from_ledger(const DevLedger& L, phmc_stats& o) {
     std::memset(&o, 0, sizeof o);
-    o.current_timestep = step_;
     o.particle_count = L.particle_count;
     o.absorbed_total = static_cast<int64_t>(L.total_absorbed);
     o.injected_total = static_cast<int64_t>(L.total_injected);
@@ -751,12 +864,23 @@ void DeviceSolver::read_stats(phmc_stats& o) {
     o.total_gradient_energy_ev = L.total_drive_ev;
     o.step_gradient_energy_ev = L.step_drive_ev;
     o.step_gradient_updates = static_cast<int64_t>(L.step_drive_updates);
-    o.average_heat_flux_along_axis = avg_flux_;
-    o.kappa_fit = kappa_fit_;
-    o.kappa_endpoints = kappa_end_;
     o.total_heat_source_energy_ev = L.total_source_ev;
     o.step_heat_source_energy_ev = L.step_source_ev;
     o.step_heat_source_updates = static_cast<int64_t>(L.step_source_updates);
+    o.interface_events = static_cast<int64_t>(L.total_iface_events);
+    o.interface_transmitted = static_cast<int64_t>(L.total_iface_transmitted);
+    o.interface_reflected = static_cast<int64_t>(L.total_iface_reflected);
+}
+
+void DeviceSolver::read_stats(phmc_stats& o) {
+    synchronize();
+    DevLedger L;
+    PHMC_CUDA(cudaMemcpy(&L, d_ledger_, sizeof L, cudaMemcpyDeviceToHost));
+    stats_from_ledger(L, o);
+    o.current_timestep = step_;
+    o.average_heat_flux_along_axis = avg_flux_;
+    o.kappa_fit = kappa_fit_;
+    o.kappa_endpoints = kappa_end_;
     if (P_.source.enabled) {
         // budgets at the step boundary: the next step's first half is already accrued here
         std::vector<double> pr(ncells_), pe(ncells_), na(ncells_);
@@ -768,9 +892,6 @@ void DeviceSolver::read_stats(phmc_stats& o) {
             o.pending_heat_source_energy_ev += pe[c];
         }
     }
-    o.interface_events = static_cast<int64_t>(L.total_iface_events);
-    o.interface_transmitted = static_cast<int64_t>(L.total_iface_transmitted);
-    o.interface_reflected = static_cast<int64_t>(L.total_iface_reflected);
     o.device_launches = counters_.launches;
 }
 
@@ -806,13 +927,11 @@ void DeviceSolver::get_carriers(double* x, double* y, double* z, double* occ, ui
     PHMC_CUDA(cudaMemcpy(alive, state_.alive, n * sizeof(uint8_t), cudaMemcpyDeviceToHost));
 }
 
-void DeviceSolver::append_convergence_row() {
+void DeviceSolver::append_convergence_row(const Observation& o, const phmc_stats& s) {
     if (cfg_.output_folder.empty()) return;
-    phmc_stats s;
-    read_stats(s);
     ConvergenceRow r;
-    r.timestep = step_;
-    r.time_ps = elapsed_;
+    r.timestep = o.step;
+    r.time_ps = o.elapsed;
     r.temperatures = host_T_;
     r.heat_flux = avg_flux_;
     r.kappa_int = kappa_fit_;

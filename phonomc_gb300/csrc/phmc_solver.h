@@ -110,6 +110,20 @@ struct StepCounters {
 
 struct LaunchCtx;
 
+// One flux pass in flight: cell temperatures, energies, fluxes and the ledger
+// copied into pinned host memory at the pass, processed in step order.
+struct Observation {
+    int step = 0;
+    double elapsed = 0;
+    double* T = nullptr;
+    double* E = nullptr;
+    double* q = nullptr;
+    DevLedger* L = nullptr;
+    cudaEvent_t done = nullptr;
+};
+
+void stats_from_ledger(const DevLedger& L, phmc_stats& o);
+
 class DeviceSolver {
 public:
     // init_carriers=false leaves the population empty (set_carriers fills it).
@@ -137,9 +151,14 @@ public:
     // one collision with the given cell temperatures (or the tallied ones when
     // null), and one gradient half-step; both return the ledger energy.
     double collide_only(const double* cell_temperature);
-    // Steps bracketed by CUDA events on the solver stream; kernel_ms sums the
-    // event-timed duration of every transport-pass launch in the region.
-    void timed_run(int steps, double& total_ms, double& kernel_ms, long long& launches);
+    // `steps` steps bracketed by CUDA events on the solver stream (graph
+    // replays when enabled), after a few event-profiled eager steps whose
+    // carrier-pass duration gives kernel_ms (mean per launch). Live carrier
+    // counts before and after the timed region are returned.
+    void timed_run(int steps, double& total_ms, double& kernel_ms, long long& launches, long long& live_before,
+                   long long& live_after);
+    // Steps are replayed from a CUDA graph of one captured timestep (default on).
+    void set_graphs(bool on) { use_graphs_ = on; }
     double drive_only();
     const Problem& problem() const { return P_; }
     long long launches() const { return counters_.launches; }
@@ -149,8 +168,13 @@ private:
     void upload_tables();
     void allocate_state(int capacity);
     void initial_statistics();
+    void enqueue_step(bool profile);
+    void capture_step_graph();
     void flux_pass();
-    void append_convergence_row();
+    void drain_observations(bool wait);
+    void process_observation(Observation& o);
+    void update_kappa();
+    void append_convergence_row(const Observation& o, const phmc_stats& s);
 
     SimulationConfig cfg_;
     std::vector<const PhononMaterial*> mats_;
@@ -177,6 +201,13 @@ private:
     // host-side observables
     double avg_flux_ = 0, kappa_fit_ = 0, kappa_end_ = 0;
     std::vector<double> host_T_, host_E_, host_q_;
+    // flux passes copied into pinned host slots and processed when their event completes
+    std::vector<struct Observation*> obs_free_, obs_pending_;
+    // graph of one timestep
+    bool use_graphs_ = true;
+    cudaGraph_t graph_ = nullptr;
+    cudaGraphExec_t graph_exec_ = nullptr;
+    long long graph_launches_ = 0;
 
     bool profile_pass_a_ = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pass_a_events_;

@@ -538,7 +538,8 @@ constexpr int kDeferBuffer = 64; // queued wall events per warp before a flush
 // finished by k_deferred.
 template <bool kMixed, bool kRta>
 __global__ void __launch_bounds__(kTransportThreads) k_transport(const __grid_constant__ DevTables T, CarrierState S,
-                                                                 CellArrays C, DevLedger* L, uint32_t step) {
+                                                                 CellArrays C, DevLedger* L) {
+    const uint32_t step = L->step_index; // timesteps completed: the draw counter of this step
     __shared__ BlockLedger bl;
     __shared__ int4 qbuf[kMixed ? kTransportThreads / 32 : 1][kMixed ? kDeferBuffer : 1];
     block_ledger_init(&bl);
@@ -637,7 +638,8 @@ __global__ void __launch_bounds__(kTransportThreads) k_transport(const __grid_co
 // then settle and bin exactly as the transport pass would have.
 template <bool kRta>
 __global__ void __launch_bounds__(kTransportThreads) k_deferred(const __grid_constant__ DevTables T, CarrierState S,
-                                                                CellArrays C, DevLedger* L, uint32_t step) {
+                                                                CellArrays C, DevLedger* L) {
+    const uint32_t step = L->step_index;
     __shared__ BlockLedger bl;
     block_ledger_init(&bl);
     __syncthreads();
@@ -774,7 +776,8 @@ __global__ void __launch_bounds__(kHoleBlock) k_dead_count(CarrierState S, const
 // Single block: exclusive scan of block counts and emission counts per reservoir
 // (src/solver/ReservoirInjector.cpp:281-284, src/solver/ReservoirSampler.cpp:117-124).
 __global__ void __launch_bounds__(1024) k_inject_prepare(const DevTables* __restrict__ Tp, DevLedger* L,
-                                                         int* block_dead, int nblocks, int capacity, uint32_t step) {
+                                                         int* block_dead, int nblocks, int capacity) {
+    const uint32_t step = L->step_index;
     __shared__ int carry;
     __shared__ int warp_sums[32];
     if (threadIdx.x == 0) carry = 0;
@@ -868,7 +871,8 @@ __global__ void __launch_bounds__(kHoleBlock) k_dead_write(CarrierState S, const
 
 template <bool kMixed, bool kRta>
 __global__ void __launch_bounds__(256) k_inject(const DevTables* __restrict__ Tp, CarrierState S, CellArrays C,
-                                                DevLedger* L, const int* holes, uint32_t step) {
+                                                DevLedger* L, const int* holes) {
+    const uint32_t step = L->step_index;
     __shared__ BlockLedger bl;
     block_ledger_init(&bl);
     __syncthreads();
@@ -1048,20 +1052,20 @@ __global__ void k_reset_pending(const DevTables* __restrict__ Tp, CellArrays C, 
 }
 
 // ----------------------------------------------------------- launchers
-int launch_transport(const LaunchCtx& x, bool mixed, bool rta, uint32_t step) {
+int launch_transport(const LaunchCtx& x, bool mixed, bool rta) {
     const dim3 g(x.grid_blocks), b(kTransportThreads);
     if (mixed) {
         if (rta) {
-            k_transport<true, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L, step);
-            k_deferred<true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L, step);
+            k_transport<true, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+            k_deferred<true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
         } else {
-            k_transport<true, false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L, step);
-            k_deferred<false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L, step);
+            k_transport<true, false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+            k_deferred<false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
         }
         return 2;
     }
-    if (rta) k_transport<false, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L, step);
-    else k_transport<false, false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L, step);
+    if (rta) k_transport<false, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+    else k_transport<false, false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
     return 1;
 }
 
@@ -1086,18 +1090,18 @@ void launch_positions_out(const LaunchCtx& x) {
     k_positions_out<<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.L);
 }
 
-int launch_inject(const LaunchCtx& x, bool mixed, bool rta, int* holes, int* block_dead, int capacity, uint32_t step) {
+int launch_inject(const LaunchCtx& x, bool mixed, bool rta, int* holes, int* block_dead, int capacity) {
     const int nb = (capacity + kHoleBlock - 1) / kHoleBlock;
     k_dead_count<<<nb, kHoleBlock, 0, x.stream>>>(x.S, x.L, block_dead);
-    k_inject_prepare<<<1, 1024, 0, x.stream>>>(x.T, x.L, block_dead, nb, capacity, step);
+    k_inject_prepare<<<1, 1024, 0, x.stream>>>(x.T, x.L, block_dead, nb, capacity);
     k_dead_write<<<nb, kHoleBlock, 0, x.stream>>>(x.S, x.L, block_dead, holes);
     const dim3 g(x.grid_blocks), b(256);
     if (mixed) {
-        if (rta) k_inject<true, true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes, step);
-        else k_inject<true, false><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes, step);
+        if (rta) k_inject<true, true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes);
+        else k_inject<true, false><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes);
     } else {
-        if (rta) k_inject<false, true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes, step);
-        else k_inject<false, false><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes, step);
+        if (rta) k_inject<false, true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes);
+        else k_inject<false, false><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes);
     }
     k_inject_finish<<<1, 1, 0, x.stream>>>(x.L);
     return 5;

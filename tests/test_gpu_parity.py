@@ -418,3 +418,30 @@ def test_mixed_heat_source_conserves_energy(gpu):
     scale = abs(st["total_thermal_energy_ev"])
     assert st["total_heat_source_energy_ev"] > 0
     assert abs(st["step_energy_balance_residual_ev"]) < 1e-12 * scale
+
+
+# ------------------------------------------------------------ graphs
+@pytest.mark.parametrize("name", ["cross_plane_film", "heated_film", "inplane_gradient"])
+def test_graph_replay_matches_eager_steps(gpu, name):
+    """Steps replayed from the captured timestep graph equal steps launched
+    one kernel at a time (draw counter and source windows live on the device)."""
+    cfg = workloads.scaled(getattr(workloads, name)(), 30000, random_seed=53, precision="mixed")
+    mat = synthetic.make_material(mesh=16)
+    m = abi.Material(gpu, "phmc_", mat, 0.1, name == "inplane_gradient", False)
+    a = abi.Solver(gpu, "phmc_", cfg, [m])
+    b = abi.Solver(gpu, "phmc_", cfg, [m])
+    assert gpu.phmc_solver_set_graphs(b.h, 0) == 0
+    for s in (a, b):
+        s.run(12)
+    ca, cb = a.carriers(), b.carriers()
+    for k in ("alive", "mode", "cell"):
+        assert np.array_equal(ca[k], cb[k]), k
+    live = ca["alive"] == 1
+    for k in ("x", "y", "z", "occ"):
+        assert np.allclose(ca[k][live], cb[k][live], rtol=1e-12, atol=1e-12), k
+    sa, sb = a.stats(), b.stats()
+    assert sa["current_timestep"] == sb["current_timestep"] == 12
+    assert sa["particle_count"] == sb["particle_count"]
+    assert abs(sa["average_heat_flux_along_axis"] - sb["average_heat_flux_along_axis"]) <= 1e-9 * abs(
+        sb["average_heat_flux_along_axis"]) + 1e-9
+    assert sa["device_launches"] == sb["device_launches"]
