@@ -214,7 +214,8 @@ def run_reference(args):
         return
     procs = max(1, os.cpu_count() or 1)
     particles, steps = 20000, 4
-    name = args.workload
+    # the batched sweep's films are cross-plane films: their CPU path is the film's
+    name = "cross_plane_film" if args.workload == "batched_films" else args.workload
     value, info = cpu_baseline(name, particles, steps, args.steps, args.warmup, procs)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
@@ -241,6 +242,45 @@ def _time_arm(lib, abi, cfg, materials, steps, warmup):
     return {"solver": s, "material": m, "ms": tot.value, "kernel_ms_per_launch": kern.value,
             "launches": int(launches.value), "carrier_steps": 0.5 * (n0 + n1) * steps, "carriers": n0,
             "clocks": clk.summary()}
+
+
+def run_batch(args):
+    """512 independent cross-plane films of log-uniform thickness advancing
+    together (phmc_batch_*): whole-batch carrier-steps/s, mixed and plain."""
+    import phonomc_gb300
+    from phonomc_gb300 import abi, synthetic, workloads
+    lib = phonomc_gb300.lib()
+    m = abi.Material(lib, "phmc_", synthetic.make_material(mesh=16), 0.1, False, False)
+    out = {}
+    for prec in ([args.precision] if args.no_plain else [args.precision, "fp64"]):
+        films = workloads.batched_films(precision=prec)
+        b = abi.Batch(lib, films, [m])
+        b.run(args.warmup)
+        steps = args.steps if prec == args.precision else max(3, args.steps // 4)
+        with ClockSampler() as clk:
+            ms, cs, launches = b.timed_run(steps)
+        out[prec] = {"value": cs / (ms * 1e-3), "ms_per_step": ms / steps, "launches": launches,
+                     "clocks": clk.summary(), "carriers": sum(c["particle_count"] for c in films), "steps": steps}
+        b.close()
+    main = out[args.precision]
+    line = {
+        "metric": METRIC, "value": main["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": main["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
+        "config": {"workload": "batched_films", "instances": 512, "carriers": int(main["carriers"]),
+                   "thickness_nm": "log-uniform 10-2000 (seed 0)", "cells": "10-200 per film",
+                   "precision": args.precision, "material": "synthetic 16^3 x 6 modes (seed 0)",
+                   "l2": "carrier state larger than L2 (no flush needed)"},
+        "gpu_launches": main["launches"],
+        "e2e": {"value": None, "unit": UNIT,
+                "note": "batched sweep: the default workload measures the host-buffer end-to-end path"},
+        "clocks": main["clocks"],
+    }
+    if "fp64" in out and args.precision != "fp64":
+        line["plain_fp64"] = {"value": out["fp64"]["value"], "unit": UNIT, "ms_per_step": out["fp64"]["ms_per_step"],
+                              "mixed_over_plain": main["value"] / out["fp64"]["value"],
+                              "clocks": out["fp64"]["clocks"]}
+    print(json.dumps(line))
 
 
 def run_ours(args):
@@ -340,7 +380,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="inplane_gradient",
-                    choices=["inplane_gradient", "cross_plane_film", "bilayer_callaway"])
+                    choices=["inplane_gradient", "cross_plane_film", "bilayer_callaway", "heated_film",
+                             "batched_films"])
     ap.add_argument("--particles", type=float, default=None)
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison arm")
@@ -350,6 +391,8 @@ def main():
         args.particles = 5e7 if args.workload == "inplane_gradient" else 1e6
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched_films":
+        run_batch(args)
     else:
         run_ours(args)
 

@@ -192,6 +192,25 @@ int phmc_host_unregister(void* ptr);
 int phmc_solver_write_outputs(phmc_solver* s);
 void phmc_solver_destroy(phmc_solver* s);
 
+/* ---- batched instances (no counterpart in the reference's API; the
+ * reference runs one instance per process) ----
+ * A batch holds independent solvers, one per configuration (films of
+ * different thickness, grid, carrier count and seed) sharing the materials;
+ * each advances on its own stream by replaying its captured step graph, so
+ * the instances' kernels overlap on the device. */
+typedef struct phmc_batch phmc_batch;
+int phmc_batch_create(const phmc_config* cfgs, int n, phmc_material* const* materials, int n_materials,
+                      phmc_batch** out);
+int phmc_batch_size(const phmc_batch* b, int* n);
+int phmc_batch_run(phmc_batch* b, int steps);
+/* `steps` steps of every instance bracketed by CUDA events: device time of the
+ * whole batch, carrier-steps summed over instances, kernels launched. */
+int phmc_batch_timed_run(phmc_batch* b, int steps, double* total_ms, double* carrier_steps, int64_t* launches);
+int phmc_batch_stats(phmc_batch* b, int i, phmc_stats* out);
+int phmc_batch_cells(phmc_batch* b, int i, double* temperature, double* energy_density, double* heat_flux3);
+int phmc_batch_cell_count(const phmc_batch* b, int i, int* cells);
+void phmc_batch_destroy(phmc_batch* b);
+
 /* ---- deterministic sub-steps on the device (parity entry points) ---- */
 /* Box ray trace for n rays; returns hit point, time and facet (-1 on miss). */
 int phmc_dev_trace_box(const double lo[3], const double hi[3], int64_t n, const double* p3, const double* v3,

@@ -392,6 +392,14 @@ DEVICE_PROTOS = {
     "solver_write_outputs": (C.c_int, [C.c_void_p]),
     "solver_timed_run": (C.c_int, [C.c_void_p, C.c_int, c_double_p, c_double_p, c_int64_p, c_int64_p, c_int64_p]),
     "solver_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
+    "batch_create": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),
+    "batch_size": (C.c_int, [C.c_void_p, c_int32_p]),
+    "batch_run": (C.c_int, [C.c_void_p, C.c_int]),
+    "batch_timed_run": (C.c_int, [C.c_void_p, C.c_int, c_double_p, c_double_p, c_int64_p]),
+    "batch_stats": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(StatsPOD)]),
+    "batch_cells": (C.c_int, [C.c_void_p, C.c_int, c_double_p, c_double_p, c_double_p]),
+    "batch_cell_count": (C.c_int, [C.c_void_p, C.c_int, c_int32_p]),
+    "batch_destroy": (None, [C.c_void_p]),
     "host_register": (C.c_int, [C.c_void_p, C.c_int64]),
     "host_unregister": (C.c_int, [C.c_void_p]),
     "solver_run_from_host": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_double_p, c_double_p, c_double_p,
@@ -400,3 +408,59 @@ DEVICE_PROTOS = {
     "dev_trace_box_noalloc": (C.c_int, [c_double_p, c_double_p, C.c_int64, c_double_p, c_double_p, c_double_p,
                                         c_double_p, c_int32_p, c_int64_p]),
 }
+
+
+class Batch:
+    """Independent instances advancing together through phmc_batch_* (device only)."""
+
+    def __init__(self, lib, cfgs: list, materials: list):
+        self.lib = lib
+        pods, self._keep = [], []
+        for cfg in cfgs:
+            pod, keep = config_pod(cfg)
+            pods.append(pod)
+            self._keep.append(keep)
+        arr = (ConfigPOD * len(pods))(*pods)
+        self._keep.append(arr)
+        mats = (C.c_void_p * len(materials))(*[m.h for m in materials])
+        self._mats = materials
+        h = C.c_void_p()
+        self.check(lib.phmc_batch_create(C.cast(arr, C.c_void_p), len(pods), mats, len(materials), C.byref(h)))
+        self.h = h
+        self.n = len(pods)
+
+    def check(self, rc):
+        if rc != 0:
+            raise LibError(self.lib.phmc_last_error().decode())
+
+    def run(self, steps: int) -> None:
+        self.check(self.lib.phmc_batch_run(self.h, steps))
+
+    def timed_run(self, steps: int):
+        ms, cs, launches = C.c_double(), C.c_double(), C.c_int64()
+        self.check(self.lib.phmc_batch_timed_run(self.h, steps, C.byref(ms), C.byref(cs), C.byref(launches)))
+        return ms.value, cs.value, int(launches.value)
+
+    def stats(self, i: int) -> dict:
+        st = StatsPOD()
+        self.check(self.lib.phmc_batch_stats(self.h, i, C.byref(st)))
+        return st.as_dict()
+
+    def cells(self, i: int):
+        n = C.c_int32()
+        self.check(self.lib.phmc_batch_cell_count(self.h, i, C.byref(n)))
+        T, E, q = np.zeros(n.value), np.zeros(n.value), np.zeros(3 * n.value)
+        self.check(self.lib.phmc_batch_cells(self.h, i, dptr(T), dptr(E), dptr(q)))
+        return T, E, q.reshape(-1, 3)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.phmc_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+

@@ -20,6 +20,19 @@ struct phmc_solver {
     std::unique_ptr<DeviceSolver> s;
 };
 
+// Independent instances (films of different thickness, cells, carriers and
+// seeds) advancing together: each has its own stream and replays its own
+// captured step graph, so the instances' kernels overlap on the device while
+// the host only issues one graph launch per instance and step.
+struct phmc_batch {
+    std::vector<std::unique_ptr<DeviceSolver>> s;
+    cudaStream_t master = nullptr;
+    ~phmc_batch() {
+        s.clear();
+        if (master) cudaStreamDestroy(master);
+    }
+};
+
 namespace {
 thread_local std::string g_error;
 
@@ -240,6 +253,95 @@ int phmc_solver_timed_run(phmc_solver* s, int steps, double* total_ms, double* k
 int phmc_solver_set_graphs(phmc_solver* s, int on) {
     return guard([&] { s->s->set_graphs(on != 0); });
 }
+
+// ---------------------------------------------------------------- batches
+int phmc_batch_create(const phmc_config* cfgs, int n, phmc_material* const* materials, int n_materials,
+                      phmc_batch** out) {
+    return guard([&] {
+        if (n <= 0) throw std::invalid_argument("a batch needs at least one instance");
+        std::vector<const PhononMaterial*> ms;
+        for (int i = 0; i < n_materials; ++i) ms.push_back(materials[i]->m.get());
+        auto b = std::make_unique<phmc_batch>();
+        for (int i = 0; i < n; ++i) {
+            SimulationConfig c = config_from_pod(cfgs[i]);
+            b->s.push_back(std::make_unique<DeviceSolver>(c, ms, true, cfgs[i].precision == 1));
+        }
+        cuda_check(cudaStreamCreateWithFlags(&b->master, cudaStreamNonBlocking), "cudaStreamCreateWithFlags");
+        *out = b.release();
+    });
+}
+
+int phmc_batch_size(const phmc_batch* b, int* n) {
+    *n = static_cast<int>(b->s.size());
+    return 0;
+}
+
+int phmc_batch_run(phmc_batch* b, int steps) {
+    return guard([&] {
+        for (int k = 0; k < steps; ++k)
+            for (auto& s : b->s) s->run_timestep();
+        for (auto& s : b->s) s->synchronize();
+    });
+}
+
+int phmc_batch_timed_run(phmc_batch* b, int steps, double* total_ms, double* carrier_steps, int64_t* launches) {
+    return guard([&] {
+        for (auto& s : b->s) s->synchronize();
+        std::vector<long long> n0(b->s.size()), l0(b->s.size());
+        for (size_t i = 0; i < b->s.size(); ++i) {
+            phmc_stats st;
+            b->s[i]->read_stats(st);
+            n0[i] = st.particle_count;
+            l0[i] = b->s[i]->launches();
+        }
+        cudaEvent_t start, stop;
+        cuda_check(cudaEventCreate(&start), "cudaEventCreate");
+        cuda_check(cudaEventCreate(&stop), "cudaEventCreate");
+        std::vector<cudaEvent_t> done(b->s.size());
+        for (auto& e : done) cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+        // every instance stream starts after `start` and the master waits for all of them
+        cuda_check(cudaEventRecord(start, b->master), "cudaEventRecord");
+        for (auto& s : b->s) cuda_check(cudaStreamWaitEvent(s->stream(), start, 0), "cudaStreamWaitEvent");
+        for (int k = 0; k < steps; ++k)
+            for (auto& s : b->s) s->run_timestep();
+        for (size_t i = 0; i < b->s.size(); ++i) {
+            cuda_check(cudaEventRecord(done[i], b->s[i]->stream()), "cudaEventRecord");
+            cuda_check(cudaStreamWaitEvent(b->master, done[i], 0), "cudaStreamWaitEvent");
+        }
+        cuda_check(cudaEventRecord(stop, b->master), "cudaEventRecord");
+        cuda_check(cudaEventSynchronize(stop), "cudaEventSynchronize");
+        float ms = 0;
+        cuda_check(cudaEventElapsedTime(&ms, start, stop), "cudaEventElapsedTime");
+        *total_ms = ms;
+        double cs = 0;
+        long long l = 0;
+        for (size_t i = 0; i < b->s.size(); ++i) {
+            phmc_stats st;
+            b->s[i]->read_stats(st);
+            cs += 0.5 * static_cast<double>(n0[i] + st.particle_count) * steps;
+            l += b->s[i]->launches() - l0[i];
+        }
+        *carrier_steps = cs;
+        *launches = l;
+        cudaEventDestroy(start);
+        cudaEventDestroy(stop);
+        for (auto& e : done) cudaEventDestroy(e);
+    });
+}
+
+int phmc_batch_stats(phmc_batch* b, int i, phmc_stats* out) {
+    return guard([&] { b->s.at(static_cast<size_t>(i))->read_stats(*out); });
+}
+
+int phmc_batch_cells(phmc_batch* b, int i, double* temperature, double* energy_density, double* heat_flux3) {
+    return guard([&] { b->s.at(static_cast<size_t>(i))->read_cells(temperature, energy_density, heat_flux3); });
+}
+
+int phmc_batch_cell_count(const phmc_batch* b, int i, int* cells) {
+    return guard([&] { *cells = b->s.at(static_cast<size_t>(i))->cell_count(); });
+}
+
+void phmc_batch_destroy(phmc_batch* b) { delete b; }
 
 int phmc_host_register(void* ptr, int64_t bytes) {
     return guard([&] { cuda_check(cudaHostRegister(ptr, static_cast<size_t>(bytes), cudaHostRegisterDefault), "cudaHostRegister"); });

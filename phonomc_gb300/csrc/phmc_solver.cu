@@ -486,7 +486,11 @@ LaunchCtx DeviceSolver::ctx() const {
     x.C = cells_;
     x.L = d_ledger_;
     x.stream = stream_;
-    x.grid_blocks = sm_count_ * 8;
+    // grid-stride carrier kernels: 8 CTAs of 256 per SM, fewer for small
+    // populations (about four carriers per thread), so small instances of a
+    // batch do not launch idle CTAs
+    const long long want = (static_cast<long long>(state_.capacity) + 1023) / 1024;
+    x.grid_blocks = static_cast<int>(std::max<long long>(8, std::min<long long>(sm_count_ * 8, want)));
     return x;
 }
 

@@ -19,7 +19,9 @@ heated_film       the cross-plane film with both reservoirs at 300 K and a
                    peak, thermal spectrum; nonlinear RTA with local
                    lifetimes, 1e6 carriers, dt = 1 ps.
 
-The lateral repeat cell is 100 nm x 100 nm in all four. `scaled()` keeps the
+batched_films     512 independent cross-plane films (see batched_films()).
+
+The lateral repeat cell is 100 nm x 100 nm in all of them. `scaled()` keeps the
 geometry and physics and shrinks the carrier count for tests.
 """
 
@@ -108,6 +110,27 @@ def heated_film(particles: float = 1e6, seed: int = 12345, precision: str = "fp6
         hs.update(frequency_center=6.0, frequency_sigma=2.0)
     c["heat_source"] = hs
     return c
+
+
+def batched_films(n: int = 512, seed: int = 0, precision: str = "mixed", particles_per_10nm: float = 5e3) -> list:
+    """Thickness sweep of independent cross-plane films: thickness log-uniform
+    in 10-2000 nm from `seed`, one cell per 10 nm clamped to 10-200 cells,
+    carriers proportional to thickness clamped to 1e4-1e6 (about 1e8 in all
+    for 512 films), reservoirs 301/299 K, fixed 300 K lifetimes, dt = 1 ps,
+    a distinct random seed per film."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    t_nm = np.exp(rng.uniform(np.log(10.0), np.log(2000.0), size=n))
+    films = []
+    for k, t in enumerate(t_nm):
+        c = cross_plane_film(precision=precision)
+        c["name"] = "batched_films"
+        c["sizes"] = (LATERAL_A, LATERAL_A, float(t) * 10.0)
+        c["grid"] = (1, 1, int(min(200, max(10, round(t / 10.0)))))
+        c["particle_count"] = float(min(1e6, max(1e4, round(particles_per_10nm * t / 10.0))))
+        c["random_seed"] = 1000 + k
+        films.append(c)
+    return films
 
 
 def bilayer_materials(mesh: int = 16):

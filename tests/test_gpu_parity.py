@@ -445,3 +445,23 @@ def test_graph_replay_matches_eager_steps(gpu, name):
     assert abs(sa["average_heat_flux_along_axis"] - sb["average_heat_flux_along_axis"]) <= 1e-9 * abs(
         sb["average_heat_flux_along_axis"]) + 1e-9
     assert sa["device_launches"] == sb["device_launches"]
+
+
+# ------------------------------------------------------------ batches
+def test_batch_matches_single_instances(gpu):
+    """Films advanced together in a batch equal the same films advanced one by one."""
+    films = workloads.batched_films(n=4, seed=3, precision="mixed", particles_per_10nm=200)
+    m = abi.Material(gpu, "phmc_", synthetic.make_material(mesh=16), 0.1, False, False)
+    b = abi.Batch(gpu, films, [m])
+    b.run(8)
+    for i, cfg in enumerate(films):
+        s = abi.Solver(gpu, "phmc_", cfg, [m])
+        s.run(8)
+        st, sb = s.stats(), b.stats(i)
+        for k in ("current_timestep", "particle_count", "absorbed_total", "injected_total"):
+            assert st[k] == sb[k], (i, k)
+        T, _, _ = s.cells()
+        Tb, _, _ = b.cells(i)
+        assert np.allclose(T, Tb, rtol=1e-10, atol=0)
+    ms, cs, launches = b.timed_run(3)
+    assert ms > 0 and cs > 0 and launches > 0
