@@ -230,6 +230,12 @@ int phmc_dev_trace_box(const double lo[3], const double hi[3], int64_t n, const 
 #define PHMC_NOALLOC_MAX_RAYS 65536
 int phmc_dev_trace_box_noalloc(const double lo[3], const double hi[3], int64_t n, const double* p3, const double* v3,
                                double* hit3, double* t, int32_t* facet, int64_t* misses);
+/* Ray traces through a closed triangle surface (faces oriented, facet id per
+ * face) with the face BVH: hit point, time (infinity on a miss) and facet (-1
+ * on a miss). Replaces SurfaceMesh::trace_boundary_intersection
+ * (src/SurfaceMesh.cpp:1164-1269). */
+int phmc_dev_trace_mesh(int nv, const double* vertices, int nf, const int32_t* faces, const int32_t* face_to_facet,
+                        int64_t n, const double* p3, const double* v3, double* hit3, double* t, int32_t* facet);
 /* Diffuse-mismatch interface events between material a (0) and b (1) with
  * explicit energy weights and uniforms u[3*i..3*i+2]; the interface is normal to
  * `axis`, each event goes from src[i] to the other material. Replaces

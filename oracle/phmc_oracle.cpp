@@ -1375,6 +1375,27 @@ int orc_interface(void* ma, void* mb, double wa, double wb, int axis, double bin
     });
 }
 
+// Ray traces through a triangle surface (src/SurfaceMesh.cpp:1164-1269) with the
+// faces as given (oriented) and their facet ids.
+int orc_trace_mesh(int nv, const double* vertices, int nf, const int32_t* faces, const int32_t* face_to_facet, int64_t n,
+                   const double* p3, const double* v3, double* hit3, double* t, int32_t* facet) {
+    return guard([&] {
+        MeshTracer M;
+        std::vector<Vec3> V(nv);
+        for (int i = 0; i < nv; ++i) V[i] = {vertices[3 * i], vertices[3 * i + 1], vertices[3 * i + 2]};
+        std::vector<std::array<int, 3>> F(nf);
+        for (int i = 0; i < nf; ++i) F[i] = {faces[3 * i], faces[3 * i + 1], faces[3 * i + 2]};
+        M.build(std::move(V), std::move(F), std::vector<int>(face_to_facet, face_to_facet + nf));
+        for (int64_t i = 0; i < n; ++i) {
+            Vec3 h;
+            int f;
+            M.trace({p3[3 * i], p3[3 * i + 1], p3[3 * i + 2]}, {v3[3 * i], v3[3 * i + 1], v3[3 * i + 2]}, h, t[i], f);
+            for (int a = 0; a < 3; ++a) hit3[3 * i + a] = h[a];
+            facet[i] = f;
+        }
+    });
+}
+
 // PrescribedHeatSource cell powers (eV/ps) of a configuration
 // (src/solver/PrescribedHeatSource.cpp:22-216); `rates` has one entry per cell.
 int orc_source_rates(const phmc_config* cfg, double* rates, int* cells) {

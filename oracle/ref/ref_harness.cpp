@@ -21,6 +21,8 @@
 #include "solver/CellParticleIndex.h"
 #include "solver/InterfaceInteraction.h"
 #include "solver/PhononSourceOperator.h"
+#include "SurfaceMesh.h"
+#include "geometry/MeshReader.h"
 #include "solver/PrescribedHeatSource.h"
 #include "solver/ParticleStorage.h"
 #include "solver/ReservoirSampler.h"
@@ -642,6 +644,69 @@ std::string cmd_source(const std::string& pmat, int spectrum, bool linearized) {
     return j.str();
 }
 
+// mesh <stl>: a surface mesh as the box-free domain builds it (STL in nm scaled
+// to Angstrom, coplanar facets merged, shifted to the origin), then ray traces
+// through SurfaceMesh::trace_boundary_intersection from random interior
+// points, and containment of random points.
+std::string cmd_mesh(const std::string& stl) {
+    auto loaded = phonomc::read_surface_mesh(stl);
+    for (auto& v : loaded.vertices)
+        for (double& x : v) x *= 10.0;
+    SurfaceMesh mesh;
+    mesh.set_merge_coplanar_facets(true);
+    mesh.set_surface_mesh_data(std::move(loaded.vertices), std::move(loaded.faces));
+    mesh.shift_to_origin();
+    Json j;
+    j.arr3("vertices", mesh.vertices());
+    std::vector<int> faces;
+    for (const auto& f : mesh.faces())
+        for (int k = 0; k < 3; ++k) faces.push_back(f[k]);
+    j.arr("faces", faces);
+    std::vector<int> f2f;
+    for (int i = 0; i < mesh.face_count(); ++i) f2f.push_back(mesh.facet_index_for_face(i));
+    j.arr("face_to_facet", f2f);
+    j.put_i("facet_count", mesh.facet_count());
+    j.arr3("facet_normals", mesh.facet_normals());
+    j.arr("bounds_max", std::vector<double>(mesh.bounds_max().begin(), mesh.bounds_max().end()));
+    std::mt19937_64 rng(91);
+    std::uniform_real_distribution<double> U(0, 1);
+    std::normal_distribution<double> N(0, 1);
+    const auto hi = mesh.bounds_max();
+    std::vector<std::array<double, 3>> P, V, H;
+    std::vector<double> T;
+    std::vector<int> F;
+    while (P.size() < 3000) {
+        std::array<double, 3> p{U(rng) * hi[0], U(rng) * hi[1], U(rng) * hi[2]};
+        if (!mesh.contains_point(p)) continue;
+        std::array<double, 3> v{N(rng), N(rng), N(rng)};
+        const double s = 60.0 / std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        for (double& c : v) c *= s;
+        if (P.size() % 10 == 0) v[P.size() % 3] = 0.0; // axis-parallel in one component
+        const auto [hit, t, facet] = mesh.trace_boundary_intersection(p, v);
+        P.push_back(p);
+        V.push_back(v);
+        H.push_back(hit);
+        T.push_back(t);
+        F.push_back(facet);
+    }
+    j.arr3("origins", P);
+    j.arr3("velocities", V);
+    j.arr3("hits", H);
+    j.arr("t", T);
+    j.arr("facet", F);
+    std::vector<std::array<double, 3>> Q;
+    std::vector<int> inside;
+    for (int i = 0; i < 3000; ++i) {
+        std::array<double, 3> q{U(rng) * hi[0], U(rng) * hi[1], U(rng) * hi[2]};
+        Q.push_back(q);
+        inside.push_back(mesh.contains_point(q) ? 1 : 0);
+    }
+    j.arr3("points", Q);
+    j.arr("inside", inside);
+    j.put("volume", mesh.volume());
+    return j.str();
+}
+
 // gradient <pmat>: TemperatureGradientDrive on random carriers in a periodic box.
 std::string cmd_gradient(const std::string& pmat) {
     PhononMaterial m(read_pmat(pmat), 0.1, true, false);
@@ -778,6 +843,7 @@ int main(int argc, char** argv) {
         else if (c == "callaway") out = cmd_callaway();
         else if (c == "rough") out = cmd_rough(argv[2], std::atoi(argv[3]) != 0);
         else if (c == "gradient") out = cmd_gradient(argv[2]);
+        else if (c == "mesh") out = cmd_mesh(argv[2]);
         else if (c == "source") out = cmd_source(argv[2], std::atoi(argv[3]), std::atoi(argv[4]) != 0);
         else if (c == "interface") out = cmd_interface(argv[2], argv[3], std::atoi(argv[4]) != 0);
         else if (c == "reservoir") out = cmd_reservoir(argv[2]);

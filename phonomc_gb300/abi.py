@@ -366,6 +366,8 @@ SUBSTEP_PROTOS = {
                                 c_double_p, c_double_p, c_int32_p, c_double_p]),
     "gradient_drive": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int64, c_int32_p, c_int32_p,
                                  c_double_p, C.c_int, C.c_double, C.c_double, c_double_p]),
+    "trace_mesh": (C.c_int, [C.c_int, c_double_p, C.c_int, c_int32_p, c_int32_p, C.c_int64, c_double_p, c_double_p,
+                             c_double_p, c_double_p, c_int32_p]),
     "interface": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_double, C.c_double, C.c_int,
                             C.c_int64, c_int32_p, c_int32_p, c_int32_p, c_double_p, c_double_p, c_int32_p, c_int32_p,
                             c_int32_p, c_int32_p, c_double_p]),

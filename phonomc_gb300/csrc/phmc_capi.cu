@@ -83,6 +83,21 @@ __global__ void k_trace_rays(DevDomain D, int64_t n, const double* p3, const dou
     }
 }
 
+__global__ void k_trace_mesh_rays(DevMesh M, int64_t n, const double* p3, const double* v3, double* hit3, double* t,
+                                  int32_t* facet) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const double p[3] = {p3[3 * i], p3[3 * i + 1], p3[3 * i + 2]};
+        const double v[3] = {v3[3 * i], v3[3 * i + 1], v3[3 * i + 2]};
+        double h[3], tt;
+        int f;
+        mesh_trace_dev(M, p, v, h, tt, f);
+        for (int a = 0; a < 3; ++a) hit3[3 * i + a] = h[a];
+        t[i] = tt;
+        facet[i] = f;
+    }
+}
+
 __global__ void k_interface_rays(const __grid_constant__ DevTables T, int64_t n, const int32_t* src,
                                  const int32_t* ain, const int32_t* signs, const double* occ, const double* u3,
                                  int32_t* action, int32_t* mat, int32_t* aout, int32_t* sout, double* oout) {
@@ -375,6 +390,54 @@ int phmc_dev_trace_box(const double lo[3], const double hi[3], int64_t n, const 
         dh.get(hit3);
         dt.get(t);
         df.get(facet);
+    });
+}
+
+int phmc_dev_trace_mesh(int nv, const double* vertices, int nf, const int32_t* faces, const int32_t* face_to_facet,
+                        int64_t n, const double* p3, const double* v3, double* hit3, double* t, int32_t* facet) {
+    return guard([&] {
+        MeshTracer T;
+        std::vector<Vec3> V(nv);
+        for (int i = 0; i < nv; ++i) V[i] = {vertices[3 * i], vertices[3 * i + 1], vertices[3 * i + 2]};
+        std::vector<std::array<int, 3>> F(nf);
+        for (int i = 0; i < nf; ++i) F[i] = {faces[3 * i], faces[3 * i + 1], faces[3 * i + 2]};
+        T.build(std::move(V), std::move(F), std::vector<int>(face_to_facet, face_to_facet + nf));
+        std::vector<double> vv, nrm, bnd, nb;
+        std::vector<int> ff, links;
+        for (const auto& v : T.vertices) vv.insert(vv.end(), v.begin(), v.end());
+        for (const auto& f : T.faces) ff.insert(ff.end(), f.begin(), f.end());
+        for (const auto& x : T.normals) nrm.insert(nrm.end(), x.begin(), x.end());
+        for (const auto& b : T.bounds) {
+            bnd.insert(bnd.end(), b[0].begin(), b[0].end());
+            bnd.insert(bnd.end(), b[1].begin(), b[1].end());
+        }
+        for (const auto& nd : T.nodes) {
+            nb.insert(nb.end(), nd.bmin.begin(), nd.bmin.end());
+            nb.insert(nb.end(), nd.bmax.begin(), nd.bmax.end());
+            links.insert(links.end(), {nd.left, nd.right, nd.begin, nd.end});
+        }
+        DBuf<double> dv(vv), dn(nrm), dk(T.k), db(bnd), dnb(nb.empty() ? std::vector<double>(6, 0.0) : nb);
+        DBuf<int> dfa(ff), df2f(T.face_to_facet), dl(links.empty() ? std::vector<int>(4, -1) : links),
+            dord(T.order.empty() ? std::vector<int>(1, 0) : T.order);
+        DevMesh M;
+        M.vertices = dv.p;
+        M.faces = dfa.p;
+        M.face_to_facet = df2f.p;
+        M.normals = dn.p;
+        M.k = dk.p;
+        M.bounds = db.p;
+        M.node_bounds = dnb.p;
+        M.node_links = dl.p;
+        M.order = dord.p;
+        M.root = T.root;
+        M.nfaces = nf;
+        DBuf<double> dp(p3, 3 * n), dvv(v3, 3 * n), dh(3 * n), dt(n);
+        DBuf<int32_t> dfc(n);
+        k_trace_mesh_rays<<<256, 128>>>(M, n, dp.p, dvv.p, dh.p, dt.p, dfc.p);
+        cuda_check(cudaDeviceSynchronize(), "k_trace_mesh_rays");
+        dh.get(hit3);
+        dt.get(t);
+        dfc.get(facet);
     });
 }
 

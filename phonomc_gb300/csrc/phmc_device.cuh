@@ -581,6 +581,190 @@ __device__ __forceinline__ IfaceOut interface_dev(const DevTables& T, int src, i
     return r;
 }
 
+// ------------------------------------------------------ mesh tracing
+// Device copy of a MeshTracer (face planes, bounds, BVH); all arithmetic of
+// the trace below is rounded step by step as the host restatement of
+// src/SurfaceMesh.cpp:111-223 and :1164-1269 is.
+struct DevMesh {
+    const double* vertices;    // [nv][3]
+    const int* faces;          // [nf][3]
+    const int* face_to_facet;  // [nf]
+    const double* normals;     // [nf][3]
+    const double* k;           // [nf]
+    const double* bounds;      // [nf][6] min xyz, max xyz
+    const double* node_bounds; // [nodes][6]
+    const int* node_links;     // [nodes][4] left, right, begin, end
+    const int* order;          // BVH leaf order of the faces
+    int root;                  // -1: scan all faces
+    int nfaces;
+};
+
+namespace meshmath {
+__device__ __forceinline__ double dot(const double a[3], const double b[3]) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(a[0], b[0]), __dmul_rn(a[1], b[1])), __dmul_rn(a[2], b[2]));
+}
+__device__ __forceinline__ void sub(const double a[3], const double b[3], double o[3]) {
+    for (int i = 0; i < 3; ++i) o[i] = __dadd_rn(a[i], -b[i]);
+}
+__device__ __forceinline__ void axpy(const double a[3], const double d[3], double s, double o[3]) {
+    for (int i = 0; i < 3; ++i) o[i] = __dadd_rn(a[i], __dmul_rn(d[i], s));
+}
+// src/SurfaceMesh.cpp:111-159
+__device__ __forceinline__ void closest(const double p[3], const double a[3], const double b[3], const double c[3],
+                                        double o[3]) {
+    double ab[3], ac[3], ap[3];
+    sub(b, a, ab);
+    sub(c, a, ac);
+    sub(p, a, ap);
+    const double d1 = dot(ab, ap), d2 = dot(ac, ap);
+    if (d1 <= 0.0 && d2 <= 0.0) {
+        for (int i = 0; i < 3; ++i) o[i] = a[i];
+        return;
+    }
+    double bp[3];
+    sub(p, b, bp);
+    const double d3 = dot(ab, bp), d4 = dot(ac, bp);
+    if (d3 >= 0.0 && d4 <= d3) {
+        for (int i = 0; i < 3; ++i) o[i] = b[i];
+        return;
+    }
+    const double vc = __dadd_rn(__dmul_rn(d1, d4), -__dmul_rn(d3, d2));
+    if (vc <= 0.0 && d1 >= 0.0 && d3 <= 0.0) {
+        axpy(a, ab, d1 / __dadd_rn(d1, -d3), o);
+        return;
+    }
+    double cp[3];
+    sub(p, c, cp);
+    const double d5 = dot(ab, cp), d6 = dot(ac, cp);
+    if (d6 >= 0.0 && d5 <= d6) {
+        for (int i = 0; i < 3; ++i) o[i] = c[i];
+        return;
+    }
+    const double vb = __dadd_rn(__dmul_rn(d5, d2), -__dmul_rn(d1, d6));
+    if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) {
+        axpy(a, ac, d2 / __dadd_rn(d2, -d6), o);
+        return;
+    }
+    const double va = __dadd_rn(__dmul_rn(d3, d6), -__dmul_rn(d5, d4));
+    const double e43 = __dadd_rn(d4, -d3), e56 = __dadd_rn(d5, -d6);
+    if (va <= 0.0 && e43 >= 0.0 && e56 >= 0.0) {
+        double bc[3];
+        sub(c, b, bc);
+        axpy(b, bc, e43 / __dadd_rn(e43, e56), o);
+        return;
+    }
+    const double denom = 1.0 / __dadd_rn(__dadd_rn(va, vb), vc);
+    double t[3];
+    axpy(a, ab, __dmul_rn(vb, denom), t);
+    axpy(t, ac, __dmul_rn(vc, denom), o);
+}
+// src/SurfaceMesh.cpp:188-223
+__device__ __forceinline__ bool ray_box(const double o[3], const double d[3], const double* bb, double t_limit,
+                                        double& t_near_out) {
+    double t_near = 0.0, t_far = t_limit;
+    for (int a = 0; a < 3; ++a) {
+        if (fabs(d[a]) <= 1e-14) {
+            if (o[a] < bb[a] - 1e-12 || o[a] > bb[3 + a] + 1e-12) return false;
+            continue;
+        }
+        const double inv = 1.0 / d[a];
+        double t0 = __dmul_rn(__dadd_rn(bb[a], -o[a]), inv), t1 = __dmul_rn(__dadd_rn(bb[3 + a], -o[a]), inv);
+        if (t0 > t1) {
+            const double s = t0;
+            t0 = t1;
+            t1 = s;
+        }
+        t_near = fmax(t_near, t0);
+        t_far = fmin(t_far, t1);
+        if (t_far < t_near) return false;
+    }
+    if (t_far <= 1e-10) return false;
+    t_near_out = fmax(0.0, t_near);
+    return t_near_out <= t_limit;
+}
+} // namespace meshmath
+
+// Nearest surface hit of the ray x + v t (t > 1e-10) with the near-first BVH
+// walk (src/SurfaceMesh.cpp:1164-1269); facet -1 and t = infinity on a miss.
+__device__ inline void mesh_trace_dev(const DevMesh& M, const double x[3], const double v[3], double hit[3], double& t_out,
+                                      int& facet) {
+    using namespace meshmath;
+    double best_t = __longlong_as_double(0x7ff0000000000000LL);
+    int best = -1;
+    double best_p[3] = {0.0, 0.0, 0.0};
+    auto try_face = [&](int i) {
+        const double* n = M.normals + 3 * i;
+        const double nn[3] = {n[0], n[1], n[2]};
+        const double denom = dot(v, nn);
+        if (fabs(denom) < 1e-10) return;
+        const double t = -__dadd_rn(dot(x, nn), M.k[i]) / denom;
+        if (t <= 1e-10 || t >= best_t) return;
+        double p[3];
+        axpy(x, v, t, p);
+        const double* bb = M.bounds + 6 * i;
+        if (p[0] < bb[0] - 1e-9 || p[1] < bb[1] - 1e-9 || p[2] < bb[2] - 1e-9 || p[0] > bb[3] + 1e-9 ||
+            p[1] > bb[4] + 1e-9 || p[2] > bb[5] + 1e-9)
+            return;
+        const int* f = M.faces + 3 * i;
+        const double* va = M.vertices + 3 * f[0];
+        const double* vb = M.vertices + 3 * f[1];
+        const double* vc = M.vertices + 3 * f[2];
+        const double A[3] = {va[0], va[1], va[2]}, B[3] = {vb[0], vb[1], vb[2]}, Cc[3] = {vc[0], vc[1], vc[2]};
+        double cp[3], d[3];
+        closest(p, A, B, Cc, cp);
+        sub(cp, p, d);
+        if (sqrt(dot(d, d)) > 1e-7) return;
+        best_t = t;
+        best = i;
+        for (int a = 0; a < 3; ++a) best_p[a] = p[a];
+    };
+    if (M.root >= 0) {
+        int stack[64];
+        int top = 0;
+        stack[top++] = M.root;
+        while (top > 0) {
+            const int node = stack[--top];
+            double tn = 0.0;
+            if (!ray_box(x, v, M.node_bounds + 6 * node, best_t, tn)) continue;
+            const int* L = M.node_links + 4 * node;
+            if (L[0] < 0 && L[1] < 0) {
+                for (int pos = L[2]; pos < L[3]; ++pos) try_face(M.order[pos]);
+                continue;
+            }
+            int near_child = -1, far_child = -1;
+            double near_t = __longlong_as_double(0x7ff0000000000000LL), far_t = near_t;
+            for (int s = 0; s < 2; ++s) {
+                const int child = L[s];
+                if (child < 0) continue;
+                double tc = 0.0;
+                if (!ray_box(x, v, M.node_bounds + 6 * child, best_t, tc)) continue;
+                if (tc < near_t) {
+                    far_child = near_child;
+                    far_t = near_t;
+                    near_child = child;
+                    near_t = tc;
+                } else if (tc < far_t) {
+                    far_child = child;
+                    far_t = tc;
+                }
+            }
+            if (far_child >= 0 && top < 64) stack[top++] = far_child;
+            if (near_child >= 0 && top < 64) stack[top++] = near_child;
+        }
+    } else {
+        for (int i = 0; i < M.nfaces; ++i) try_face(i);
+    }
+    if (best < 0) {
+        for (int a = 0; a < 3; ++a) hit[a] = x[a];
+        t_out = __longlong_as_double(0x7ff0000000000000LL);
+        facet = -1;
+        return;
+    }
+    for (int a = 0; a < 3; ++a) hit[a] = best_p[a];
+    t_out = best_t;
+    facet = M.face_to_facet[best];
+}
+
 // Heat-source energy factor (ps) of [begin, end] under the time profile
 // (src/solver/HeatSourceDriving.cpp:12-44), in the same rounding as the host.
 __device__ __forceinline__ double source_time_factor(const DevParams& P, double begin_ps, double end_ps) {

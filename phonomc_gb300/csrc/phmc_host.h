@@ -253,6 +253,32 @@ struct HeatSourceTables {
     double mode_weight(const PhononMaterial& m, int flat) const;
 };
 
+// ------------------------------------------------------ mesh tracing
+// Triangle-surface ray trace of the reference's SurfaceMesh: face planes,
+// centroids and bounds (src/SurfaceMesh.cpp:455-477), the face BVH (median
+// split on the largest centroid extent, leaves of <= 8 faces, none below 65
+// faces; :479-553) and the near-first traversal with the plane/closest-point
+// face test (:1164-1269). Faces are taken as oriented and grouped by the
+// caller (face_to_facet).
+struct MeshTracer {
+    struct Node {
+        Vec3 bmin{}, bmax{};
+        int left = -1, right = -1, begin = 0, end = 0;
+    };
+    std::vector<Vec3> vertices;
+    std::vector<std::array<int, 3>> faces;
+    std::vector<int> face_to_facet;
+    std::vector<Vec3> normals, centroids;
+    std::vector<double> k;
+    std::vector<std::array<Vec3, 2>> bounds;
+    std::vector<Node> nodes;
+    std::vector<int> order; // BVH leaf order of the faces
+    int root = -1;
+    void build(std::vector<Vec3> v, std::vector<std::array<int, 3>> f, std::vector<int> f2f);
+    // hit point, time (infinity and the origin on a miss) and facet (-1 on a miss)
+    void trace(const Vec3& x, const Vec3& v, Vec3& hit, double& t, int& facet) const;
+};
+
 // ---------------------------------------------------- interface banks
 // Diffuse-mismatch mode banks (src/solver/InterfaceModeSampler.cpp:11-44): per
 // material and direction (0: v_axis < 0, 1: v_axis > 0) the active modes sorted

@@ -179,3 +179,71 @@ def write_pmat(path: str, data: MaterialData) -> None:
             f.write(name.encode().ljust(16, b"\0")[:16])
             f.write(struct.pack("<q", values.size))
             f.write(np.ascontiguousarray(values, dtype="<f8").tobytes())
+
+
+# ------------------------------------------------------------------ meshes
+def finfet_mesh(voxel_nm: float = 5.0, jitter_nm: float = 0.5, seed: int = 0,
+                slab_nm=(200.0, 100.0, 50.0), fin_nm=(10.0, 100.0, 40.0)):
+    """Procedural FinFET surface: a fin (10 nm wide in x, running the full 100 nm
+    along y, 40 nm tall) on a 200 x 100 x 50 nm slab, as the boundary of a voxel
+    solid (voxel_nm lattice), two triangles per exposed voxel face, outward
+    winding. Vertices off the slab's side and bottom planes (which stay flat so
+    periodic pairing and reservoirs keep exact planes) get a uniform jitter of
+    +-jitter_nm per component from `seed`. Returns (vertices [nm], faces)."""
+    nx, ny, nz = (int(round(s / voxel_nm)) for s in slab_nm)
+    fx, fz = int(round(fin_nm[0] / voxel_nm)), int(round(fin_nm[2] / voxel_nm))
+    solid = np.zeros((nx, ny, nz + fz), dtype=bool)
+    solid[:, :, :nz] = True
+    x0 = (nx - fx) // 2
+    solid[x0:x0 + fx, :, nz:nz + fz] = True
+    index = {}
+    verts = []
+
+    def vid(i, j, k):
+        key = (i, j, k)
+        if key not in index:
+            index[key] = len(verts)
+            verts.append((i * voxel_nm, j * voxel_nm, k * voxel_nm))
+        return index[key]
+
+    faces = []
+    shape = solid.shape
+    # corner offsets of the quad on each of the six faces, counter-clockwise seen from outside
+    quads = {
+        (-1, 0, 0): [(0, 0, 0), (0, 0, 1), (0, 1, 1), (0, 1, 0)],
+        (1, 0, 0): [(1, 0, 0), (1, 1, 0), (1, 1, 1), (1, 0, 1)],
+        (0, -1, 0): [(0, 0, 0), (1, 0, 0), (1, 0, 1), (0, 0, 1)],
+        (0, 1, 0): [(0, 1, 0), (0, 1, 1), (1, 1, 1), (1, 1, 0)],
+        (0, 0, -1): [(0, 0, 0), (0, 1, 0), (1, 1, 0), (1, 0, 0)],
+        (0, 0, 1): [(0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)],
+    }
+    for i, j, k in zip(*np.nonzero(solid)):
+        for d, corners in quads.items():
+            a, b, c = i + d[0], j + d[1], k + d[2]
+            if 0 <= a < shape[0] and 0 <= b < shape[1] and 0 <= c < shape[2] and solid[a, b, c]:
+                continue
+            q = [vid(i + o[0], j + o[1], k + o[2]) for o in corners]
+            faces.append((q[0], q[1], q[2]))
+            faces.append((q[0], q[2], q[3]))
+    v = np.array(verts, dtype=np.float64)
+    rng = np.random.default_rng(seed)
+    keep = ((np.abs(v[:, 0]) < 1e-9) | (np.abs(v[:, 0] - slab_nm[0]) < 1e-9) | (np.abs(v[:, 1]) < 1e-9) |
+            (np.abs(v[:, 1] - slab_nm[1]) < 1e-9) | (np.abs(v[:, 2]) < 1e-9))
+    jitter = rng.uniform(-jitter_nm, jitter_nm, size=v.shape)
+    v[~keep] += jitter[~keep]
+    return v, np.array(faces, dtype=np.int64)
+
+
+def write_stl(path: str, vertices, faces, name: str = "synthetic") -> None:
+    """Binary STL (little-endian: 80-byte header, count, 50-byte records)."""
+    import struct
+    v = np.asarray(vertices, dtype=np.float64)
+    f = np.asarray(faces, dtype=np.int64)
+    with open(path, "wb") as out:
+        out.write(name.encode()[:80].ljust(80, b" "))
+        out.write(struct.pack("<I", len(f)))
+        for a, b, c in f:
+            n = np.cross(v[b] - v[a], v[c] - v[a])
+            ln = np.linalg.norm(n)
+            n = n / ln if ln > 0 else n
+            out.write(struct.pack("<12fH", *n, *v[a], *v[b], *v[c], 0))

@@ -45,6 +45,7 @@ CASES = {
     "source_thermal_linearized": ["source", "{m}", "0", "1"],
     "source_weighted": ["source", "{m}", "1", "0"],
     "source_gaussian": ["source", "{m}", "2", "0"],
+    "mesh_finfet": ["mesh", "{f}"],
     "interface_dmm": ["interface", "{m}", "{s}", "0"],
     "interface_dmm_linearized": ["interface", "{m}", "{s}", "1"],
 }
@@ -133,6 +134,8 @@ def main() -> None:
     cpath = os.path.join(tmp, "m8c.pmat")
     synthetic.write_pmat(mpath, synthetic.make_material(mesh=8))
     synthetic.write_pmat(cpath, synthetic.make_material(mesh=8, callaway=True))
+    fpath = os.path.join(tmp, "finfet.stl")
+    synthetic.write_stl(fpath, *synthetic.finfet_mesh())
     spath = os.path.join(tmp, "m8s.pmat")
     synthetic.write_pmat(spath, synthetic.make_material(mesh=8, freq_scale=0.7, vel_scale=0.75))
     if not args.only or "fullrun_cross_plane" in args.only:
@@ -146,7 +149,7 @@ def main() -> None:
     for name, argv in CASES.items():
         if args.only and name not in args.only:
             continue
-        cmd = [HARNESS] + [a.format(m=mpath, c=cpath, s=spath) for a in argv]
+        cmd = [HARNESS] + [a.format(m=mpath, c=cpath, s=spath, f=fpath) for a in argv]
         out = subprocess.run(cmd, check=True, capture_output=True, text=True).stdout
         data = json.loads(out)
         data["_harness_args"] = argv

@@ -465,3 +465,21 @@ def test_batch_matches_single_instances(gpu):
         assert np.allclose(T, Tb, rtol=1e-10, atol=0)
     ms, cs, launches = b.timed_run(3)
     assert ms > 0 and cs > 0 and launches > 0
+
+
+# ------------------------------------------------------------ meshes
+def test_mesh_trace_golden(gpu):
+    """Device BVH walk through the procedural FinFET surface against the
+    reference's SurfaceMesh::trace_boundary_intersection: facet ids, hit times
+    and hit points bit-exact."""
+    g = golden("mesh_finfet")
+    V, F, f2f = _f64(g["vertices"]), _i32(g["faces"]), _i32(g["face_to_facet"])
+    P, Vel = _f64(g["origins"]), _f64(g["velocities"])
+    n = P.shape[0]
+    hit, t, fac = np.zeros((n, 3)), np.zeros(n), np.zeros(n, np.int32)
+    rc = gpu.phmc_dev_trace_mesh(V.shape[0], D(V), F.size // 3, I32(F), I32(f2f), n, D(P), D(Vel), D(hit), D(t),
+                                 I32(fac))
+    assert rc == 0, gpu.phmc_last_error()
+    assert np.array_equal(fac, g["facet"])
+    assert np.array_equal(t, np.asarray(g["t"]))
+    assert np.array_equal(hit, np.asarray(g["hits"]))

@@ -275,3 +275,22 @@ def test_source_apply(oracle_lib, name):
     assert np.array_equal(pend, np.asarray(g["pending_after"]))
     assert np.allclose(occ, g["occ_out"], rtol=1e-15, atol=1e-18)
     assert np.array_equal(occ == np.asarray(g["occ_in"]), np.asarray(g["occ_out"]) == np.asarray(g["occ_in"]))
+
+
+def test_mesh_trace(oracle_lib):
+    """Ray traces through the procedural FinFET surface against the reference's
+    SurfaceMesh::trace_boundary_intersection: facet ids and hit times bit-exact."""
+    g = golden("mesh_finfet")
+    V = np.ascontiguousarray(g["vertices"], dtype=np.float64)
+    F = np.ascontiguousarray(g["faces"], dtype=np.int32)
+    f2f = np.ascontiguousarray(g["face_to_facet"], dtype=np.int32)
+    P = np.ascontiguousarray(g["origins"], dtype=np.float64)
+    Vel = np.ascontiguousarray(g["velocities"], dtype=np.float64)
+    n = P.shape[0]
+    hit, t, fac = np.zeros((n, 3)), np.zeros(n), np.zeros(n, np.int32)
+    I = lambda a: a.ctypes.data_as(abi.c_int32_p)  # noqa: E731
+    rc = oracle_lib.orc_trace_mesh(V.shape[0], D(V), F.size // 3, I(F), I(f2f), n, D(P), D(Vel), D(hit), D(t), I(fac))
+    assert rc == 0, oracle_lib.orc_last_error()
+    assert np.array_equal(fac, g["facet"])
+    assert np.array_equal(t, np.asarray(g["t"]))
+    assert np.array_equal(hit, np.asarray(g["hits"]))
