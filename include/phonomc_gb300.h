@@ -87,6 +87,26 @@ typedef struct phmc_heat_source {
     double period, on_duration, duty_cycle, amplitude;
 } phmc_heat_source;
 
+/* Surface-mesh domain (include/SimulationConfig.h:43-86): the closed surface
+ * and the boundary regions. Regions are relative boxes
+ * [xmin,ymin,zmin,xmax,ymax,zmax] over the mesh bounding box that select
+ * facets by centroid; later regions override earlier ones and unselected
+ * facets are smooth rough walls. */
+typedef struct phmc_mesh_domain {
+    const char* model;               /* STL (nm) or OBJ path; NULL: the triangles below */
+    int64_t n_vertices;
+    const double* vertices;          /* [n_vertices][3], Angstrom */
+    int64_t n_faces;
+    const int32_t* faces;            /* [n_faces][3] vertex indices */
+    int32_t merge_coplanar_facets;   /* reference default 1 */
+    int32_t n_regions;
+    const double* boundary_position; /* [n_regions][6] */
+    const char* boundary_conditions; /* [n_regions] 'T', 'P' or 'R' */
+    const double* boundary_values;   /* [n_regions] K, roughness nm, 0 for periodic */
+    int32_t n_periodic_regions;      /* even: region 2k pairs with 2k+1 */
+    const double* periodic_pair;     /* [n_periodic_regions][6] */
+} phmc_mesh_domain;
+
 /* SimulationConfig fields read by the carrier loop (include/SimulationConfig.h:42-146),
  * in internal units (Angstrom, ps, K). Box faces are in facet order
  * xmin,xmax,ymin,ymax,zmin,zmax with condition 'T','P' or 'R'. */
@@ -119,6 +139,7 @@ typedef struct phmc_config {
     double interface_frequency_bin_thz;
     int32_t precision;               /* 0 = plain FP64 state, 1 = mixed (FP32 transport) */
     const phmc_heat_source* heat_source; /* NULL: no heat source */
+    const phmc_mesh_domain* mesh;    /* NULL: the analytic box of sizes / face_condition */
 } phmc_config;
 
 /* Getters of include/MonteCarloSolver.h:59-101 plus the last step's ledger. */
@@ -199,6 +220,29 @@ void phmc_solver_destroy(phmc_solver* s);
  * each advances on its own stream by replaying its captured step graph, so
  * the instances' kernels overlap on the device. */
 typedef struct phmc_batch phmc_batch;
+
+/* Host geometry of a configuration (SimulationDomain, include/SimulationDomain.h:14-99):
+ * facets, boundary assignment, cells and the voxel -> cell map, with point
+ * membership and cell lookup. No device work. */
+typedef struct phmc_domain phmc_domain;
+int phmc_domain_create(const phmc_config* cfg, phmc_domain** out);
+void phmc_domain_destroy(phmc_domain* d);
+/* counts; shape3 = voxel grid, bounds6 = min xyz, max xyz; volume in A^3 */
+int phmc_domain_info(const phmc_domain* d, int32_t* n_facets, int32_t* n_cells, int32_t* n_faces, int32_t* shape3,
+                     double* volume, double* bounds6);
+/* per facet: outward normal, centroid, area, condition, value (K or Angstrom),
+ * periodic partner (-1) and shift to it; any pointer may be NULL */
+int phmc_domain_facets(const phmc_domain* d, double* normal3, double* centroid3, double* area, char* condition,
+                       double* value, int32_t* pair, double* shift3);
+/* cell centres and volumes [n_cells], voxel -> cell map [nx*ny*nz]; any may be NULL */
+int phmc_domain_cells(const phmc_domain* d, double* centers3, double* volumes, int32_t* voxel_cell);
+/* mesh domains: oriented faces [n_faces][3], vertices [n_faces*3][3] as a
+ * triangle soup, and the facet of each face; any may be NULL */
+int phmc_domain_faces(const phmc_domain* d, int32_t* face_to_facet, double* triangles9);
+int phmc_domain_contains(const phmc_domain* d, int64_t n, const double* p3, uint8_t* inside);
+int phmc_domain_grid_index(const phmc_domain* d, int64_t n, const double* p3, int32_t* cell);
+/* closest facet of each point (-1 for none), src/SurfaceMesh.cpp:996-1003 */
+int phmc_domain_nearest_facet(const phmc_domain* d, int64_t n, const double* p3, int32_t* facet);
 int phmc_batch_create(const phmc_config* cfgs, int n, phmc_material* const* materials, int n_materials,
                       phmc_batch** out);
 int phmc_batch_size(const phmc_batch* b, int* n);

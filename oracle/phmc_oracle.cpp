@@ -812,7 +812,8 @@ struct OracleSolver {
             if (count > 0 && !(R.cdf.back() > 0.0))
                 fail("Cannot sample positive emissions from a zero-flux reservoir.");
             const Facet& F = domain->facets()[R.facet];
-            const double a0 = 0.5 * F.area, a1 = 0.5 * F.area;
+            std::vector<double> cum; // running triangle area (src/geometry/SurfaceSampling.cpp:45-58)
+            for (double a : F.tri_area) cum.push_back((cum.empty() ? 0.0 : cum.back()) + std::max(a, 0.0));
             for (int e = 0; e < count; ++e) {
                 const Uniform2 d0 = uniform2(cfg.random_seed, static_cast<uint32_t>(e), static_cast<uint32_t>(step), kDrawInject, static_cast<uint32_t>(r), 0);
                 const Uniform2 d1 = uniform2(cfg.random_seed, static_cast<uint32_t>(e), static_cast<uint32_t>(step), kDrawInject, static_cast<uint32_t>(r), 1);
@@ -820,7 +821,9 @@ struct OracleSolver {
                 size_t m = static_cast<size_t>(std::lower_bound(R.cdf.begin(), R.cdf.end(), d0.a) - R.cdf.begin());
                 if (m >= R.cdf.size()) m = R.cdf.size() - 1;
                 const double temit = dt * d0.b;
-                const auto& tri = F.tri[d1.a * (a0 + a1) < a0 ? 0 : 1];
+                size_t k = static_cast<size_t>(std::upper_bound(cum.begin(), cum.end(), d1.a * cum.back()) - cum.begin());
+                if (k >= cum.size()) k = cum.size() - 1;
+                const auto& tri = F.tris[k];
                 const double sr1 = std::sqrt(d1.b);
                 const double w0 = 1.0 - sr1, w1 = sr1 * (1.0 - d2.a), w2 = sr1 * d2.a;
                 Vec3 pos{w0 * tri[0][0] + w1 * tri[1][0] + w2 * tri[2][0], w0 * tri[0][1] + w1 * tri[1][1] + w2 * tri[2][1],

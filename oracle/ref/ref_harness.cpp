@@ -707,6 +707,85 @@ std::string cmd_mesh(const std::string& stl) {
     return j.str();
 }
 
+// domain <toml>: SimulationDomain of a mesh TOML (facets, boundary assignment,
+// periodic pairs, cells and the voxel map), membership / nearest-facet / cell
+// queries at random points, and the domain summary file it writes.
+std::string cmd_domain(const std::string& toml) {
+    SimulationConfig a = load_simulation_config(toml);
+    SimulationDomain d(a);
+    const SurfaceMesh& mesh = d.mesh();
+    Json j;
+    j.arr3("vertices", mesh.vertices());
+    std::vector<int> faces, f2f;
+    for (const auto& f : mesh.faces())
+        for (int k = 0; k < 3; ++k) faces.push_back(f[k]);
+    for (int i = 0; i < mesh.face_count(); ++i) f2f.push_back(mesh.facet_index_for_face(i));
+    j.arr("faces", faces);
+    j.arr("face_to_facet", f2f);
+    j.arr3("facet_normals", mesh.facet_normals());
+    j.arr3("facet_centroids", mesh.facet_centroids());
+    j.arr("facet_areas", mesh.facet_areas());
+    std::string cond;
+    std::vector<double> value;
+    std::vector<int> pair;
+    std::vector<std::array<double, 3>> shift;
+    for (int f = 0; f < mesh.facet_count(); ++f) {
+        const char c = d.facet_boundary_condition(f);
+        cond.push_back(c);
+        value.push_back(c == 'T' ? d.reservoir_value_for_facet(f) : (c == 'R' ? d.roughness_for_facet(f) : 0.0));
+        pair.push_back(d.periodic_pair_facet(f));
+        shift.push_back(d.periodic_shift_for_facet(f));
+    }
+    j.put_s("conditions", cond);
+    j.arr("values", value);
+    j.arr("pair", pair);
+    j.arr3("shift", shift);
+    j.arr3("grid_centers", d.grid_centers());
+    j.arr("grid_volumes", d.grid_volumes());
+    j.put("volume", d.volume());
+    std::vector<double> b(d.bounds_min().begin(), d.bounds_min().end());
+    b.insert(b.end(), d.bounds_max().begin(), d.bounds_max().end());
+    j.arr("bounds", b);
+    const auto lo = d.bounds_min(), hi = d.bounds_max();
+    std::vector<int> voxel;
+    const int nx = a.grid.nx, ny = a.grid.ny, nz = a.grid.nz;
+    for (int ix = 0; ix < nx; ++ix)
+        for (int iy = 0; iy < ny; ++iy)
+            for (int iz = 0; iz < nz; ++iz)
+                voxel.push_back(d.fast_grid_index({lo[0] + (ix + 0.5) * (hi[0] - lo[0]) / nx,
+                                                   lo[1] + (iy + 0.5) * (hi[1] - lo[1]) / ny,
+                                                   lo[2] + (iz + 0.5) * (hi[2] - lo[2]) / nz}));
+    j.arr("voxel_cell", voxel);
+    std::mt19937_64 rng(17);
+    std::uniform_real_distribution<double> U(0, 1);
+    std::vector<std::array<double, 3>> P;
+    std::vector<int> inside, nearest, cell;
+    for (int i = 0; i < 2000; ++i) {
+        std::array<double, 3> p{lo[0] + U(rng) * (hi[0] - lo[0]), lo[1] + U(rng) * (hi[1] - lo[1]),
+                                lo[2] + U(rng) * (hi[2] - lo[2])};
+        P.push_back(p);
+        inside.push_back(d.contains_point(p) ? 1 : 0);
+        nearest.push_back(mesh.nearest_facet(p));
+        cell.push_back(d.fast_grid_index(p));
+    }
+    j.arr3("points", P);
+    j.arr("inside", inside);
+    j.arr("nearest_facet", nearest);
+    j.arr("cell", cell);
+    std::ifstream summary(std::filesystem::path(a.output_folder) / "summary.txt");
+    std::ostringstream text;
+    text << summary.rdbuf();
+    std::string esc;
+    for (char c : text.str()) {
+        if (c == '"' || c == '\\') esc.push_back('\\');
+        if (c == '\n') esc += "\\n";
+        else if (c == '\t') esc += "\\t";
+        else esc.push_back(c);
+    }
+    j.put_s("domain_summary", esc);
+    return j.str();
+}
+
 // gradient <pmat>: TemperatureGradientDrive on random carriers in a periodic box.
 std::string cmd_gradient(const std::string& pmat) {
     PhononMaterial m(read_pmat(pmat), 0.1, true, false);
@@ -844,6 +923,7 @@ int main(int argc, char** argv) {
         else if (c == "rough") out = cmd_rough(argv[2], std::atoi(argv[3]) != 0);
         else if (c == "gradient") out = cmd_gradient(argv[2]);
         else if (c == "mesh") out = cmd_mesh(argv[2]);
+        else if (c == "domain") out = cmd_domain(argv[2]);
         else if (c == "source") out = cmd_source(argv[2], std::atoi(argv[3]), std::atoi(argv[4]) != 0);
         else if (c == "interface") out = cmd_interface(argv[2], argv[3], std::atoi(argv[4]) != 0);
         else if (c == "reservoir") out = cmd_reservoir(argv[2]);

@@ -96,6 +96,47 @@ def heat_source_pod(h: dict, keep: list) -> HeatSourcePOD:
     return p
 
 
+class MeshDomainPOD(C.Structure):
+    _fields_ = [
+        ("model", C.c_char_p), ("n_vertices", C.c_int64), ("vertices", c_double_p), ("n_faces", C.c_int64),
+        ("faces", c_int32_p), ("merge_coplanar_facets", C.c_int32), ("n_regions", C.c_int32),
+        ("boundary_position", c_double_p), ("boundary_conditions", C.c_char_p), ("boundary_values", c_double_p),
+        ("n_periodic_regions", C.c_int32), ("periodic_pair", c_double_p),
+    ]
+
+
+def mesh_domain_pod(m: dict, keep: list) -> MeshDomainPOD:
+    """MeshDomainPOD from {"model": path | None, "vertices": [n,3] Angstrom, "faces": [m,3],
+    "merge_coplanar_facets": bool, "regions": [(box6, cond, value)], "periodic_pair": [box6, ...]}."""
+    p = MeshDomainPOD()
+    if m.get("model"):
+        b = str(m["model"]).encode()
+        keep.append(b)
+        p.model = b
+    else:
+        v = np.ascontiguousarray(m["vertices"], dtype=np.float64).reshape(-1, 3)
+        f = np.ascontiguousarray(m["faces"], dtype=np.int32).reshape(-1, 3)
+        keep.extend([v, f])
+        p.n_vertices, p.vertices = v.shape[0], dptr(v)
+        p.n_faces, p.faces = f.shape[0], f.ctypes.data_as(c_int32_p)
+    p.merge_coplanar_facets = int(m.get("merge_coplanar_facets", True))
+    regions = m.get("regions", [])
+    if regions:
+        pos = np.ascontiguousarray([r[0] for r in regions], dtype=np.float64).reshape(-1)
+        cond = "".join(r[1] for r in regions).encode()
+        val = np.ascontiguousarray([r[2] for r in regions], dtype=np.float64)
+        keep.extend([pos, cond, val])
+        p.n_regions = len(regions)
+        p.boundary_position, p.boundary_conditions, p.boundary_values = dptr(pos), cond, dptr(val)
+    pairs = m.get("periodic_pair", [])
+    if pairs:
+        arr = np.ascontiguousarray(pairs, dtype=np.float64).reshape(-1)
+        keep.append(arr)
+        p.n_periodic_regions = len(pairs)
+        p.periodic_pair = dptr(arr)
+    return p
+
+
 class ConfigPOD(C.Structure):
     _fields_ = [
         ("sizes", C.c_double * 3), ("particle_count", C.c_double), ("time_step", C.c_double),
@@ -110,6 +151,7 @@ class ConfigPOD(C.Structure):
         ("material_interface_axis", C.c_int32), ("n_interfaces", C.c_int32),
         ("material_interface_positions", c_double_p), ("interface_frequency_bin_thz", C.c_double),
         ("precision", C.c_int32), ("heat_source", C.POINTER(HeatSourcePOD)),
+        ("mesh", C.POINTER(MeshDomainPOD)),
     ]
 
 
@@ -178,7 +220,7 @@ def config_pod(cfg: dict):
     """Build a ConfigPOD from a dict of SimulationConfig-style fields (internal units)."""
     keep = []
     c = ConfigPOD()
-    c.sizes[:] = list(cfg["sizes"])
+    c.sizes[:] = list(cfg.get("sizes", (1.0, 1.0, 1.0)))
     c.particle_count = float(cfg.get("particle_count", 1e4))
     c.time_step = float(cfg.get("time_step", 1.0))
     c.iterations = int(cfg.get("iterations", 10000))
@@ -200,8 +242,8 @@ def config_pod(cfg: dict):
     it = cfg.get("initial_temperature", 300.0)
     c.initial_temperature_linear = int(it == "linear")
     c.initial_temperature = 300.0 if it == "linear" else float(it)
-    c.face_condition = "".join(cfg["faces"]).encode()
-    c.face_value[:] = [float(v) for v in cfg["face_values"]]
+    c.face_condition = "".join(cfg.get("faces", "RRRRRR")).encode()
+    c.face_value[:] = [float(v) for v in cfg.get("face_values", (0.0,) * 6)]
     of = cfg.get("output_folder")
     if of:
         b = of.encode()
@@ -218,7 +260,26 @@ def config_pod(cfg: dict):
         hs = heat_source_pod(cfg["heat_source"], keep)
         keep.append(hs)
         c.heat_source = C.pointer(hs)
+    if cfg.get("mesh"):
+        mp = mesh_domain_pod(cfg["mesh"], keep)
+        keep.append(mp)
+        c.mesh = C.pointer(mp)
     return c, keep
+
+
+# Host geometry (phmc_domain_*), product library only.
+DOMAIN_PROTOS = {
+    "domain_create": (C.c_int, [C.POINTER(ConfigPOD), C.POINTER(C.c_void_p)]),
+    "domain_destroy": (None, [C.c_void_p]),
+    "domain_info": (C.c_int, [C.c_void_p, c_int32_p, c_int32_p, c_int32_p, c_int32_p, c_double_p, c_double_p]),
+    "domain_facets": (C.c_int, [C.c_void_p, c_double_p, c_double_p, c_double_p, C.c_char_p, c_double_p, c_int32_p,
+                                c_double_p]),
+    "domain_cells": (C.c_int, [C.c_void_p, c_double_p, c_double_p, c_int32_p]),
+    "domain_faces": (C.c_int, [C.c_void_p, c_int32_p, c_double_p]),
+    "domain_contains": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_uint8_p]),
+    "domain_grid_index": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_int32_p]),
+    "domain_nearest_facet": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_int32_p]),
+}
 
 
 SOLVER_PROTOS = {
@@ -466,3 +527,77 @@ class Batch:
         except Exception:
             pass
 
+
+
+class Domain:
+    """Host geometry of a configuration through phmc_domain_* (no device work)."""
+
+    def __init__(self, lib, cfg: dict):
+        self.lib = lib
+        pod, keep = config_pod(cfg)
+        h = C.c_void_p()
+        if lib.phmc_domain_create(C.byref(pod), C.byref(h)) != 0:
+            raise LibError(lib.phmc_last_error().decode())
+        self.h = h
+        nf, nc, nfa = C.c_int32(), C.c_int32(), C.c_int32()
+        shape = (C.c_int32 * 3)()
+        vol = C.c_double()
+        b = (C.c_double * 6)()
+        self._check(lib.phmc_domain_info(h, C.byref(nf), C.byref(nc), C.byref(nfa), shape, C.byref(vol), b))
+        self.n_facets, self.n_cells, self.n_faces = nf.value, nc.value, nfa.value
+        self.shape = tuple(shape)
+        self.volume = vol.value
+        self.bounds = np.array(list(b)).reshape(2, 3)
+
+    def _check(self, rc):
+        if rc != 0:
+            raise LibError(self.lib.phmc_last_error().decode())
+
+    def facets(self) -> dict:
+        n = self.n_facets
+        normal, centroid, shift = (np.zeros((n, 3)) for _ in range(3))
+        area, value = np.zeros(n), np.zeros(n)
+        cond = C.create_string_buffer(max(n, 1))
+        pair = np.zeros(n, dtype=np.int32)
+        self._check(self.lib.phmc_domain_facets(self.h, dptr(normal), dptr(centroid), dptr(area), cond, dptr(value),
+                                                pair.ctypes.data_as(c_int32_p), dptr(shift)))
+        return {"normal": normal, "centroid": centroid, "area": area, "condition": cond.raw[:n].decode(),
+                "value": value, "pair": pair, "shift": shift}
+
+    def cells(self) -> dict:
+        centers, vols = np.zeros((self.n_cells, 3)), np.zeros(self.n_cells)
+        vc = np.zeros(int(np.prod(self.shape)), dtype=np.int32)
+        self._check(self.lib.phmc_domain_cells(self.h, dptr(centers), dptr(vols), vc.ctypes.data_as(c_int32_p)))
+        return {"centers": centers, "volumes": vols, "voxel_cell": vc}
+
+    def faces(self) -> dict:
+        f2f = np.zeros(self.n_faces, dtype=np.int32)
+        tri = np.zeros((self.n_faces, 3, 3))
+        self._check(self.lib.phmc_domain_faces(self.h, f2f.ctypes.data_as(c_int32_p), dptr(tri)))
+        return {"face_to_facet": f2f, "triangles": tri}
+
+    def contains(self, p) -> np.ndarray:
+        p = np.ascontiguousarray(p, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros(p.shape[0], dtype=np.uint8)
+        self._check(self.lib.phmc_domain_contains(self.h, p.shape[0], dptr(p), out.ctypes.data_as(c_uint8_p)))
+        return out
+
+    def grid_index(self, p) -> np.ndarray:
+        p = np.ascontiguousarray(p, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros(p.shape[0], dtype=np.int32)
+        self._check(self.lib.phmc_domain_grid_index(self.h, p.shape[0], dptr(p), out.ctypes.data_as(c_int32_p)))
+        return out
+
+    def nearest_facet(self, p) -> np.ndarray:
+        p = np.ascontiguousarray(p, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros(p.shape[0], dtype=np.int32)
+        self._check(self.lib.phmc_domain_nearest_facet(self.h, p.shape[0], dptr(p), out.ctypes.data_as(c_int32_p)))
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.phmc_domain_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()

@@ -20,6 +20,11 @@ struct phmc_solver {
     std::unique_ptr<DeviceSolver> s;
 };
 
+struct phmc_domain {
+    SimulationConfig cfg;
+    std::unique_ptr<SimulationDomain> d;
+};
+
 // Independent instances (films of different thickness, cells, carriers and
 // seeds) advancing together: each has its own stream and replays its own
 // captured step graph, so the instances' kernels overlap on the device while
@@ -191,6 +196,104 @@ int phmc_material_create(const phmc_material_data* data, double dt, int stationa
 }
 
 void phmc_material_destroy(phmc_material* m) { delete m; }
+
+int phmc_domain_create(const phmc_config* cfg, phmc_domain** out) {
+    return guard([&] {
+        if (!cfg || !out) throw std::invalid_argument("phmc_domain_create: null argument");
+        auto d = std::make_unique<phmc_domain>();
+        d->cfg = config_from_pod(*cfg);
+        d->d = std::make_unique<SimulationDomain>(d->cfg);
+        *out = d.release();
+    });
+}
+
+void phmc_domain_destroy(phmc_domain* d) { delete d; }
+
+int phmc_domain_info(const phmc_domain* d, int32_t* n_facets, int32_t* n_cells, int32_t* n_faces, int32_t* shape3,
+                     double* volume, double* bounds6) {
+    return guard([&] {
+        const SimulationDomain& D = *d->d;
+        if (n_facets) *n_facets = static_cast<int32_t>(D.facets().size());
+        if (n_cells) *n_cells = D.grid_count();
+        if (n_faces) *n_faces = D.is_mesh() ? static_cast<int32_t>(D.mesh()->faces().size()) : 12;
+        for (int a = 0; a < 3; ++a) {
+            if (shape3) shape3[a] = D.grid_shape()[a];
+            if (bounds6) {
+                bounds6[a] = D.bounds_min()[a];
+                bounds6[3 + a] = D.bounds_max()[a];
+            }
+        }
+        if (volume) *volume = D.volume();
+    });
+}
+
+int phmc_domain_facets(const phmc_domain* d, double* normal3, double* centroid3, double* area, char* condition,
+                       double* value, int32_t* pair, double* shift3) {
+    return guard([&] {
+        const auto& F = d->d->facets();
+        for (size_t f = 0; f < F.size(); ++f) {
+            for (int a = 0; a < 3; ++a) {
+                if (normal3) normal3[3 * f + a] = F[f].normal[a];
+                if (centroid3) centroid3[3 * f + a] = F[f].centroid[a];
+                if (shift3) shift3[3 * f + a] = F[f].shift[a];
+            }
+            if (area) area[f] = F[f].area;
+            if (condition) condition[f] = F[f].condition;
+            if (value) value[f] = F[f].value;
+            if (pair) pair[f] = F[f].pair;
+        }
+    });
+}
+
+int phmc_domain_cells(const phmc_domain* d, double* centers3, double* volumes, int32_t* voxel_cell) {
+    return guard([&] {
+        const SimulationDomain& D = *d->d;
+        for (int c = 0; c < D.grid_count(); ++c) {
+            for (int a = 0; a < 3; ++a)
+                if (centers3) centers3[3 * c + a] = D.grid_centers()[c][a];
+            if (volumes) volumes[c] = D.grid_volumes()[c];
+        }
+        if (voxel_cell) {
+            const auto& s = D.grid_shape();
+            const size_t n = static_cast<size_t>(s[0]) * s[1] * s[2];
+            for (size_t v = 0; v < n; ++v)
+                voxel_cell[v] = D.is_mesh() ? D.voxel_cells()[v] : static_cast<int32_t>(v);
+        }
+    });
+}
+
+int phmc_domain_faces(const phmc_domain* d, int32_t* face_to_facet, double* triangles9) {
+    return guard([&] {
+        const SimulationDomain& D = *d->d;
+        if (!D.is_mesh()) throw std::invalid_argument("phmc_domain_faces: the analytic box has no mesh faces");
+        const SurfaceMesh& M = *D.mesh();
+        for (size_t f = 0; f < M.faces().size(); ++f) {
+            if (face_to_facet) face_to_facet[f] = M.face_to_facet()[f];
+            if (triangles9)
+                for (int k = 0; k < 3; ++k)
+                    for (int a = 0; a < 3; ++a) triangles9[9 * f + 3 * k + a] = M.vertices()[M.faces()[f][k]][a];
+        }
+    });
+}
+
+int phmc_domain_contains(const phmc_domain* d, int64_t n, const double* p3, uint8_t* inside) {
+    return guard([&] {
+        for (int64_t i = 0; i < n; ++i)
+            inside[i] = d->d->contains_point({p3[3 * i], p3[3 * i + 1], p3[3 * i + 2]}) ? 1 : 0;
+    });
+}
+
+int phmc_domain_grid_index(const phmc_domain* d, int64_t n, const double* p3, int32_t* cell) {
+    return guard([&] {
+        for (int64_t i = 0; i < n; ++i) cell[i] = d->d->fast_grid_index({p3[3 * i], p3[3 * i + 1], p3[3 * i + 2]});
+    });
+}
+
+int phmc_domain_nearest_facet(const phmc_domain* d, int64_t n, const double* p3, int32_t* facet) {
+    return guard([&] {
+        for (int64_t i = 0; i < n; ++i) facet[i] = d->d->nearest_facet({p3[3 * i], p3[3 * i + 1], p3[3 * i + 2]});
+    });
+}
 
 int phmc_material_active_count(const phmc_material* m, int* n) {
     return guard([&] { *n = m->m->active_mode_count(); });

@@ -108,8 +108,9 @@ struct DevReservoir {
     int facet, material, n_cdf;
     double expected;
     double normal[3];
-    double tri[2][3][3];
-    double area0, area1;
+    int n_tri;             // triangles of the facet
+    const double* tri;     // [n_tri][3 vertices][3]
+    const double* tri_cum; // running area sum, [n_tri]
     const double* cdf;
     const double* occ; // emitted occupation per active mode
 };

@@ -18,7 +18,6 @@ double dot3(const Vec3& a, const Vec3& b) { return a[0] * b[0] + a[1] * b[1] + a
 double norm3(const Vec3& a) { return std::sqrt(dot3(a, a)); }
 Vec3 sub3(const Vec3& a, const Vec3& b) { return {a[0] - b[0], a[1] - b[1], a[2] - b[2]}; }
 Vec3 mul3(const Vec3& a, double s) { return {a[0] * s, a[1] * s, a[2] * s}; }
-Vec3 add3(const Vec3& a, const Vec3& b) { return {a[0] + b[0], a[1] + b[1], a[2] + b[2]}; }
 Vec3 q_to_k(const std::array<Vec3, 3>& R, const Vec3& q) {
     return {R[0][0] * q[0] + R[0][1] * q[1] + R[0][2] * q[2],
             R[1][0] * q[0] + R[1][1] * q[1] + R[1][2] * q[2],
@@ -287,8 +286,13 @@ CallawayData PhononMaterial::callaway_data(double T) const {
 // ---------------------------------------------------------------- domain
 // Box facets in the reference's order (plane 2*axis+side), boundary conditions,
 // periodic pairs and the uniform grid (src/SimulationDomain.cpp:131-198, 408-611, 626-766).
+SimulationDomain::~SimulationDomain() = default;
+
 SimulationDomain::SimulationDomain(const SimulationConfig& cfg) {
-    if (cfg.model != "box") throw std::runtime_error("Only the analytic box geometry is supported.");
+    if (cfg.model != "box") {
+        build_mesh_domain(cfg);
+        return;
+    }
     if (cfg.sizes.size() != 3) throw std::runtime_error("Box requires three finite positive sizes.");
     for (int a = 0; a < 3; ++a) {
         if (!std::isfinite(cfg.sizes[a]) || cfg.sizes[a] <= 0)
@@ -313,8 +317,8 @@ SimulationDomain::SimulationDomain(const SimulationConfig& cfg) {
         c10[u] = bmax_[u]; c10[v] = bmin_[v];
         c11[u] = bmax_[u]; c11[v] = bmax_[v];
         c01[u] = bmin_[u]; c01[v] = bmax_[v];
-        F.tri[0] = {c00, c10, c11};
-        F.tri[1] = {c00, c11, c01};
+        F.tris = {{c00, c10, c11}, {c00, c11, c01}};
+        F.tri_area = {0.5 * F.area, 0.5 * F.area};
         const char cond = cfg.face_condition[f];
         if (cond != 'T' && cond != 'P' && cond != 'R') throw std::runtime_error("Unknown boundary condition.");
         const double value = cond == 'R' ? cfg.face_value[f] * 10.0 : cfg.face_value[f];
@@ -357,6 +361,11 @@ SimulationDomain::SimulationDomain(const SimulationConfig& cfg) {
 
 // src/SimulationDomain.cpp:92-126
 int SimulationDomain::fast_grid_index(const Vec3& p) const {
+    const int voxel = voxel_index(p);
+    return mesh_ ? voxel_cell_[voxel] : voxel;
+}
+
+int SimulationDomain::voxel_index(const Vec3& p) const {
     int idx[3];
     for (int a = 0; a < 3; ++a) {
         const int n = shape_[a];
@@ -372,6 +381,10 @@ int SimulationDomain::fast_grid_index(const Vec3& p) const {
 
 // src/SimulationDomain.cpp:399-450 (analytic box branch)
 void SimulationDomain::trace(const Vec3& p, const Vec3& v, Vec3& cp, double& t, int& facet) const {
+    if (mesh_) {
+        mesh_->trace(p, v, cp, t, facet);
+        return;
+    }
     constexpr double velocity_eps = 1e-18, time_eps = 1e-14;
     const Vec3 ext = sub3(bmax_, bmin_);
     const double scale = std::max({1.0, std::abs(ext[0]), std::abs(ext[1]), std::abs(ext[2])});
@@ -408,12 +421,14 @@ void SimulationDomain::trace(const Vec3& p, const Vec3& v, Vec3& cp, double& t, 
 }
 
 bool SimulationDomain::contains_point(const Vec3& p) const {
+    if (mesh_) return mesh_->contains_point(p);
     for (int a = 0; a < 3; ++a)
         if (!(p[a] >= bmin_[a] && p[a] <= bmax_[a])) return false;
     return true;
 }
 
 int SimulationDomain::nearest_facet(const Vec3& p) const {
+    if (mesh_) return mesh_->nearest_facet(p);
     int best = -1;
     double bd = std::numeric_limits<double>::infinity();
     for (int f = 0; f < 6; ++f) {
@@ -618,182 +633,6 @@ void EnergyLedger::finish_step(double energy, const BoundaryBalance& b) {
 }
 
 // ---------------------------------------------------------------- problem
-// ------------------------------------------------------ mesh tracing
-namespace {
-Vec3 vmin3(const Vec3& a, const Vec3& b) { return {std::min(a[0], b[0]), std::min(a[1], b[1]), std::min(a[2], b[2])}; }
-Vec3 vmax3(const Vec3& a, const Vec3& b) { return {std::max(a[0], b[0]), std::max(a[1], b[1]), std::max(a[2], b[2])}; }
-Vec3 cross3(const Vec3& a, const Vec3& b) {
-    return {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
-}
-
-// src/SurfaceMesh.cpp:111-159: closest point of a triangle (Ericson's regions)
-Vec3 closest_on_triangle(const Vec3& p, const Vec3& a, const Vec3& b, const Vec3& c) {
-    const Vec3 ab = sub3(b, a), ac = sub3(c, a), ap = sub3(p, a);
-    const double d1 = dot3(ab, ap), d2 = dot3(ac, ap);
-    if (d1 <= 0.0 && d2 <= 0.0) return a;
-    const Vec3 bp = sub3(p, b);
-    const double d3 = dot3(ab, bp), d4 = dot3(ac, bp);
-    if (d3 >= 0.0 && d4 <= d3) return b;
-    const double vc = d1 * d4 - d3 * d2;
-    if (vc <= 0.0 && d1 >= 0.0 && d3 <= 0.0) return add3(a, mul3(ab, d1 / (d1 - d3)));
-    const Vec3 cp = sub3(p, c);
-    const double d5 = dot3(ab, cp), d6 = dot3(ac, cp);
-    if (d6 >= 0.0 && d5 <= d6) return c;
-    const double vb = d5 * d2 - d1 * d6;
-    if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) return add3(a, mul3(ac, d2 / (d2 - d6)));
-    const double va = d3 * d6 - d5 * d4;
-    if (va <= 0.0 && (d4 - d3) >= 0.0 && (d5 - d6) >= 0.0)
-        return add3(b, mul3(sub3(c, b), (d4 - d3) / ((d4 - d3) + (d5 - d6))));
-    const double denom = 1.0 / (va + vb + vc);
-    return add3(add3(a, mul3(ab, vb * denom)), mul3(ac, vc * denom));
-}
-
-// src/SurfaceMesh.cpp:188-223
-bool ray_box(const Vec3& o, const Vec3& d, const Vec3& bmin, const Vec3& bmax, double t_limit, double& t_near_out) {
-    double t_near = 0.0, t_far = t_limit;
-    for (int a = 0; a < 3; ++a) {
-        if (std::abs(d[a]) <= 1e-14) {
-            if (o[a] < bmin[a] - 1e-12 || o[a] > bmax[a] + 1e-12) return false;
-            continue;
-        }
-        const double inv = 1.0 / d[a];
-        double t0 = (bmin[a] - o[a]) * inv, t1 = (bmax[a] - o[a]) * inv;
-        if (t0 > t1) std::swap(t0, t1);
-        t_near = std::max(t_near, t0);
-        t_far = std::min(t_far, t1);
-        if (t_far < t_near) return false;
-    }
-    if (t_far <= 1e-10) return false;
-    t_near_out = std::max(0.0, t_near);
-    return t_near_out <= t_limit;
-}
-} // namespace
-
-void MeshTracer::build(std::vector<Vec3> v, std::vector<std::array<int, 3>> f, std::vector<int> f2f) {
-    vertices = std::move(v);
-    faces = std::move(f);
-    face_to_facet = std::move(f2f);
-    const size_t nf = faces.size();
-    if (face_to_facet.size() != nf) throw std::invalid_argument("face_to_facet must have one entry per face");
-    normals.assign(nf, {0, 0, 0});
-    centroids.assign(nf, {0, 0, 0});
-    k.assign(nf, 0.0);
-    bounds.assign(nf, {Vec3{0, 0, 0}, Vec3{0, 0, 0}});
-    for (size_t i = 0; i < nf; ++i) {
-        const Vec3 &a = vertices.at(faces[i][0]), &b = vertices.at(faces[i][1]), &c = vertices.at(faces[i][2]);
-        const Vec3 n = cross3(sub3(b, a), sub3(c, a));
-        const double area2 = norm3(n);
-        normals[i] = area2 > 0.0 ? mul3(n, 1.0 / area2) : Vec3{0, 0, 0};
-        centroids[i] = {(a[0] + b[0] + c[0]) / 3.0, (a[1] + b[1] + c[1]) / 3.0, (a[2] + b[2] + c[2]) / 3.0};
-        k[i] = -dot3(normals[i], a);
-        bounds[i] = {vmin3(vmin3(a, b), c), vmax3(vmax3(a, b), c)};
-    }
-    nodes.clear();
-    order.clear();
-    root = -1;
-    if (nf <= 64) return; // a face scan is used below 65 faces
-    order.resize(nf);
-    std::iota(order.begin(), order.end(), 0);
-    nodes.reserve(2 * nf);
-    std::function<int(int, int)> split = [&](int begin, int end) -> int {
-        const int id = static_cast<int>(nodes.size());
-        nodes.push_back(Node{});
-        Vec3 bmin = bounds[order[begin]][0], bmax = bounds[order[begin]][1];
-        Vec3 cmin = centroids[order[begin]], cmax = cmin;
-        for (int i = begin + 1; i < end; ++i) {
-            bmin = vmin3(bmin, bounds[order[i]][0]);
-            bmax = vmax3(bmax, bounds[order[i]][1]);
-            cmin = vmin3(cmin, centroids[order[i]]);
-            cmax = vmax3(cmax, centroids[order[i]]);
-        }
-        nodes[id].bmin = bmin;
-        nodes[id].bmax = bmax;
-        nodes[id].begin = begin;
-        nodes[id].end = end;
-        const int count = end - begin;
-        if (count <= 8) return id;
-        const Vec3 ext = sub3(cmax, cmin);
-        int axis = 0;
-        if (ext[1] > ext[axis]) axis = 1;
-        if (ext[2] > ext[axis]) axis = 2;
-        if (ext[axis] <= 1e-18) return id;
-        const int mid = begin + count / 2;
-        std::nth_element(order.begin() + begin, order.begin() + mid, order.begin() + end,
-                         [&](int a, int b) { return centroids[a][axis] < centroids[b][axis]; });
-        const int l = split(begin, mid);
-        const int r = split(mid, end);
-        nodes[id].left = l;
-        nodes[id].right = r;
-        return id;
-    };
-    root = split(0, static_cast<int>(nf));
-}
-
-void MeshTracer::trace(const Vec3& x, const Vec3& v, Vec3& hit, double& t_out, int& facet) const {
-    double best_t = std::numeric_limits<double>::infinity();
-    int best = -1;
-    Vec3 best_p{0, 0, 0};
-    auto try_face = [&](int i) {
-        const double denom = dot3(v, normals[i]);
-        if (std::abs(denom) < 1e-10) return;
-        const double t = -(dot3(x, normals[i]) + k[i]) / denom;
-        if (t <= 1e-10 || t >= best_t) return;
-        const Vec3 p = add3(x, mul3(v, t));
-        const auto& bb = bounds[i];
-        if (p[0] < bb[0][0] - 1e-9 || p[1] < bb[0][1] - 1e-9 || p[2] < bb[0][2] - 1e-9 || p[0] > bb[1][0] + 1e-9 ||
-            p[1] > bb[1][1] + 1e-9 || p[2] > bb[1][2] + 1e-9)
-            return;
-        const Vec3 cp = closest_on_triangle(p, vertices[faces[i][0]], vertices[faces[i][1]], vertices[faces[i][2]]);
-        if (norm3(sub3(cp, p)) > 1e-7) return;
-        best_t = t;
-        best_p = p;
-        best = i;
-    };
-    if (root >= 0) {
-        int stack[64];
-        int top = 0;
-        stack[top++] = root;
-        while (top > 0) {
-            const Node& node = nodes[stack[--top]];
-            double tn = 0.0;
-            if (!ray_box(x, v, node.bmin, node.bmax, best_t, tn)) continue;
-            if (node.left < 0 && node.right < 0) {
-                for (int pos = node.begin; pos < node.end; ++pos) try_face(order[pos]);
-                continue;
-            }
-            int near_child = -1, far_child = -1;
-            double near_t = std::numeric_limits<double>::infinity(), far_t = near_t;
-            for (int child : {node.left, node.right}) {
-                if (child < 0) continue;
-                double tc = 0.0;
-                if (!ray_box(x, v, nodes[child].bmin, nodes[child].bmax, best_t, tc)) continue;
-                if (tc < near_t) {
-                    far_child = near_child;
-                    far_t = near_t;
-                    near_child = child;
-                    near_t = tc;
-                } else if (tc < far_t) {
-                    far_child = child;
-                    far_t = tc;
-                }
-            }
-            if (far_child >= 0 && top < 64) stack[top++] = far_child;
-            if (near_child >= 0 && top < 64) stack[top++] = near_child;
-        }
-    } else {
-        for (size_t i = 0; i < faces.size(); ++i) try_face(static_cast<int>(i));
-    }
-    if (best < 0) {
-        hit = x;
-        t_out = std::numeric_limits<double>::infinity();
-        facet = -1;
-        return;
-    }
-    hit = best_p;
-    t_out = best_t;
-    facet = face_to_facet[best];
-}
-
 // ------------------------------------------------------- heat source
 // src/config/ConfigValidation.cpp:196-290 (the rules the carrier loop relies on).
 void validate_heat_source_config(const SimulationConfig& c) {

@@ -15,6 +15,7 @@
 #include <array>
 #include <cstdint>
 #include <map>
+#include <memory>
 #include <optional>
 #include <stdexcept>
 #include <string>
@@ -65,6 +66,18 @@ struct SimulationConfig {
     // are paired with the opposite face of the same axis.
     std::array<char, 6> face_condition{'R', 'R', 'R', 'R', 'R', 'R'};
     std::array<double, 6> face_value{0, 0, 0, 0, 0, 0};
+    // Surface-mesh domains (include/SimulationConfig.h:43-86): `model` is the
+    // path of an STL (nm, scaled to Angstrom) or OBJ file, or "mesh" with the
+    // triangles given in mesh_vertices (Angstrom) / mesh_faces. Boundary
+    // regions are relative boxes [xmin,ymin,zmin,xmax,ymax,zmax] over the
+    // bounding box that select facets by centroid; later regions override.
+    std::vector<Vec3> mesh_vertices;
+    std::vector<std::array<int, 3>> mesh_faces;
+    bool merge_coplanar_facets = true;
+    std::vector<std::array<double, 6>> boundary_position;
+    std::vector<char> boundary_conditions;
+    std::vector<double> boundary_values;   // K for 'T', roughness in nm for 'R', 0 for 'P'
+    std::vector<std::array<double, 6>> periodic_pair; // region pairs, matched facet by facet
     std::string output_folder;
     // Layered materials (include/SimulationConfig.h:93-99): N materials, N-1 planes.
     int material_interface_axis = 0;
@@ -190,14 +203,130 @@ struct Facet {
     int pair = -1;         // periodic partner facet
     Vec3 shift{};          // periodic translation a -> pair
     int reservoir = -1;    // reservoir index for 'T'
-    std::array<Vec3, 3> tri[2]; // two triangles spanning the face (injection sampling)
+    // Triangles of the facet and their areas (area-weighted injection points,
+    // src/geometry/SurfaceSampling.cpp:20-73); a box face has two.
+    std::vector<std::array<Vec3, 3>> tris;
+    std::vector<double> tri_area;
 };
 
-// Analytic axis-aligned box (src/SimulationDomain.cpp:73-126, 292-450, 626-766).
-// Facet f = 2*axis + side, which is the reference's box facet order.
+// ------------------------------------------------------ mesh tracing
+// Triangle-surface ray trace of the reference's SurfaceMesh: face planes,
+// centroids and bounds (src/SurfaceMesh.cpp:455-477), the face BVH (median
+// split on the largest centroid extent, leaves of <= 8 faces, none below 65
+// faces; :479-553) and the near-first traversal with the plane/closest-point
+// face test (:1164-1269). Faces are taken as oriented and grouped by the
+// caller (face_to_facet).
+struct MeshTracer {
+    struct Node {
+        Vec3 bmin{}, bmax{};
+        int left = -1, right = -1, begin = 0, end = 0;
+    };
+    std::vector<Vec3> vertices;
+    std::vector<std::array<int, 3>> faces;
+    std::vector<int> face_to_facet;
+    std::vector<Vec3> normals, centroids;
+    std::vector<double> k;
+    std::vector<std::array<Vec3, 2>> bounds;
+    std::vector<Node> nodes;
+    std::vector<int> order; // BVH leaf order of the faces
+    int root = -1;
+    void build(std::vector<Vec3> v, std::vector<std::array<int, 3>> f, std::vector<int> f2f);
+    // hit point, time (infinity and the origin on a miss) and facet (-1 on a miss)
+    void trace(const Vec3& x, const Vec3& v, Vec3& hit, double& t, int& facet) const;
+};
+
+// ------------------------------------------------------- surface mesh
+// Closed triangle surface of a mesh domain, restating the reference's
+// SurfaceMesh (src/SurfaceMesh.cpp:227-1160): edge list in first-encounter
+// order, winding made consistent (BFS over shared edges, each shell with a
+// positive signed volume; T-junction surfaces by ray-cast side tests), face
+// metrics, the face BVH, coplanar connected faces merged into facets
+// (plane keys llround(1e6 n), llround(1e6 d)), the enclosed volume, the
+// star tetrahedra used by contains_point and volume sampling (the Delaunay
+// path needs the external qdelaunay program; without it the reference uses
+// this same star fallback), +x ray-cast membership and nearest-facet queries.
+class SurfaceMesh {
+public:
+    struct Simplex {
+        std::array<Vec3, 4> v;
+        double volume = 0;
+        std::array<Vec3, 2> bounds;
+        std::array<std::array<double, 3>, 3> inv;
+    };
+    void set_merge_coplanar_facets(bool on) { merge_coplanar_ = on; }
+    void set_data(std::vector<Vec3> vertices, std::vector<std::array<int, 3>> faces);
+    void shift_to_origin();
+
+    const std::vector<Vec3>& vertices() const { return vertices_; }
+    const std::vector<std::array<int, 3>>& faces() const { return faces_; }
+    const std::vector<Vec3>& face_normals() const { return face_normals_; }
+    const std::vector<double>& face_areas() const { return face_areas_; }
+    const std::vector<int>& face_to_facet() const { return face_to_facet_; }
+    int facet_count() const { return static_cast<int>(facet_faces_.size()); }
+    const std::vector<std::vector<int>>& facet_faces() const { return facet_faces_; }
+    const std::vector<Vec3>& facet_normals() const { return facet_normals_; }
+    const std::vector<Vec3>& facet_centroids() const { return facet_centroids_; }
+    const std::vector<double>& facet_areas() const { return facet_areas_; }
+    // sorted lengths of the edges used by exactly one face of the facet
+    std::vector<double> facet_boundary_edge_lengths(int facet) const;
+    const Vec3& bounds_min() const { return bmin_; }
+    const Vec3& bounds_max() const { return bmax_; }
+    double volume() const { return volume_; }
+    const MeshTracer& tracer() const { return tracer_; }
+    const std::vector<Simplex>& simplices() const; // empty: no valid decomposition
+
+    bool contains_point(const Vec3& p) const;
+    bool contains_point_ray_cast(const Vec3& p) const;
+    int nearest_facet(const Vec3& p) const;
+    void trace(const Vec3& x, const Vec3& v, Vec3& hit, double& t, int& facet) const { tracer_.trace(x, v, hit, t, facet); }
+
+private:
+    void rebuild();
+    void compute_edges();
+    void orient();
+    void compute_face_metrics();
+    void compute_facets();
+    void build_simplices() const;
+
+    bool merge_coplanar_ = true;
+    std::vector<Vec3> vertices_;
+    std::vector<std::array<int, 3>> faces_;
+    Vec3 bmin_{}, bmax_{};
+    double volume_ = 0;
+    std::vector<std::array<int, 2>> edges_;
+    std::vector<std::vector<int>> edge_faces_;
+    std::vector<std::array<int, 3>> face_edges_;
+    std::vector<Vec3> face_normals_, face_centroids_;
+    std::vector<double> face_areas_;
+    std::vector<std::array<int, 2>> face_adjacency_;
+    std::vector<int> face_to_facet_;
+    std::vector<std::vector<int>> facet_faces_;
+    std::vector<std::vector<int>> facet_boundary_edges_;
+    std::vector<Vec3> facet_normals_, facet_centroids_;
+    std::vector<double> facet_areas_;
+    MeshTracer tracer_;
+    mutable bool simplices_ready_ = false;
+    mutable std::vector<Simplex> simplices_;
+};
+
+// STL (binary or ASCII, vertices merged on a 1e-10 lattice) and OBJ readers
+// (src/geometry/MeshReader.cpp:60-243). Coordinates as stored in the file.
+void read_surface_mesh(const std::string& path, std::vector<Vec3>& vertices, std::vector<std::array<int, 3>>& faces);
+
+// Analytic axis-aligned box (src/SimulationDomain.cpp:73-126, 292-450, 626-766),
+// facet f = 2*axis + side, which is the reference's box facet order; or a
+// closed surface mesh (model = file path or "mesh"): facets of the merged
+// mesh with boundary regions and periodic pairs assigned by facet centroid
+// (:452-626), cells at the voxel centres inside the mesh and every voxel
+// mapped to an active cell by a breadth-first fill (:626-766).
 class SimulationDomain {
 public:
     explicit SimulationDomain(const SimulationConfig& cfg);
+    ~SimulationDomain();
+    bool is_mesh() const { return mesh_ != nullptr; }
+    const SurfaceMesh* mesh() const { return mesh_.get(); }
+    // voxel (ix*ny + iy)*nz + iz -> active cell (mesh domains; identity for boxes)
+    const std::vector<int>& voxel_cells() const { return voxel_cell_; }
     const Vec3& bounds_min() const { return bmin_; }
     const Vec3& bounds_max() const { return bmax_; }
     double volume() const { return volume_; }
@@ -215,6 +344,9 @@ public:
     int nearest_facet(const Vec3& p) const;
 
 private:
+    void build_mesh_domain(const SimulationConfig& cfg);
+    int voxel_index(const Vec3& p) const;
+
     Vec3 bmin_{}, bmax_{}, inv_cell_{};
     double volume_ = 0;
     std::array<int, 3> shape_{1, 1, 1};
@@ -222,6 +354,8 @@ private:
     std::vector<double> volumes_;
     std::vector<Facet> facets_;
     std::vector<int> reservoir_facets_;
+    std::unique_ptr<SurfaceMesh> mesh_;
+    std::vector<int> voxel_cell_;
 };
 
 // Layered materials along one axis (src/solver/LayeredMaterialLayout.cpp:24-115).
@@ -251,32 +385,6 @@ struct HeatSourceTables {
     void configure(const SimulationConfig& c, const SimulationDomain& domain);
     void set_spectrum(const SimulationConfig& c); // the PhononSourceOperator part of configure()
     double mode_weight(const PhononMaterial& m, int flat) const;
-};
-
-// ------------------------------------------------------ mesh tracing
-// Triangle-surface ray trace of the reference's SurfaceMesh: face planes,
-// centroids and bounds (src/SurfaceMesh.cpp:455-477), the face BVH (median
-// split on the largest centroid extent, leaves of <= 8 faces, none below 65
-// faces; :479-553) and the near-first traversal with the plane/closest-point
-// face test (:1164-1269). Faces are taken as oriented and grouped by the
-// caller (face_to_facet).
-struct MeshTracer {
-    struct Node {
-        Vec3 bmin{}, bmax{};
-        int left = -1, right = -1, begin = 0, end = 0;
-    };
-    std::vector<Vec3> vertices;
-    std::vector<std::array<int, 3>> faces;
-    std::vector<int> face_to_facet;
-    std::vector<Vec3> normals, centroids;
-    std::vector<double> k;
-    std::vector<std::array<Vec3, 2>> bounds;
-    std::vector<Node> nodes;
-    std::vector<int> order; // BVH leaf order of the faces
-    int root = -1;
-    void build(std::vector<Vec3> v, std::vector<std::array<int, 3>> f, std::vector<int> f2f);
-    // hit point, time (infinity and the origin on a miss) and facet (-1 on a miss)
-    void trace(const Vec3& x, const Vec3& v, Vec3& hit, double& t, int& facet) const;
 };
 
 // ---------------------------------------------------- interface banks

@@ -75,6 +75,40 @@ inline void heat_source_from_pod(const phmc_heat_source& h, SimulationConfig& s)
     s.heat_source_amplitude = h.amplitude;
     }
 
+// [geometry] model and [boundary] regions of a mesh domain.
+inline void mesh_domain_from_pod(const phmc_mesh_domain& m, SimulationConfig& s) {
+    if (m.model && m.model[0]) {
+        s.model = m.model;
+        if (s.model == "box" || s.model == "mesh") throw std::invalid_argument("mesh model must be a file path");
+    } else {
+        if (m.n_vertices <= 0 || m.n_faces <= 0 || !m.vertices || !m.faces)
+            throw std::invalid_argument("mesh domain requires a model path or vertices and faces");
+        s.model = "mesh";
+        s.mesh_vertices.resize(static_cast<size_t>(m.n_vertices));
+        for (int64_t i = 0; i < m.n_vertices; ++i)
+            s.mesh_vertices[i] = {m.vertices[3 * i], m.vertices[3 * i + 1], m.vertices[3 * i + 2]};
+        s.mesh_faces.resize(static_cast<size_t>(m.n_faces));
+        for (int64_t i = 0; i < m.n_faces; ++i) s.mesh_faces[i] = {m.faces[3 * i], m.faces[3 * i + 1], m.faces[3 * i + 2]};
+    }
+    s.merge_coplanar_facets = m.merge_coplanar_facets != 0;
+    if (m.n_regions < 0 || m.n_periodic_regions < 0) throw std::invalid_argument("negative region count");
+    if (m.n_regions > 0 && (!m.boundary_position || !m.boundary_conditions || !m.boundary_values))
+        throw std::invalid_argument("boundary regions require positions, conditions and values");
+    for (int i = 0; i < m.n_regions; ++i) {
+        std::array<double, 6> b;
+        for (int k = 0; k < 6; ++k) b[k] = m.boundary_position[6 * i + k];
+        s.boundary_position.push_back(b);
+        s.boundary_conditions.push_back(m.boundary_conditions[i]);
+        s.boundary_values.push_back(m.boundary_values[i]);
+    }
+    if (m.n_periodic_regions > 0 && !m.periodic_pair) throw std::invalid_argument("periodic_pair regions missing");
+    for (int i = 0; i < m.n_periodic_regions; ++i) {
+        std::array<double, 6> b;
+        for (int k = 0; k < 6; ++k) b[k] = m.periodic_pair[6 * i + k];
+        s.periodic_pair.push_back(b);
+    }
+}
+
 inline SimulationConfig config_from_pod(const phmc_config& c) {
     SimulationConfig s;
     s.sizes = {c.sizes[0], c.sizes[1], c.sizes[2]};
@@ -107,6 +141,7 @@ inline SimulationConfig config_from_pod(const phmc_config& c) {
                                               c.material_interface_positions + c.n_interfaces);
     if (c.interface_frequency_bin_thz > 0) s.material_interface_frequency_bin_thz = c.interface_frequency_bin_thz;
     if (c.heat_source) heat_source_from_pod(*c.heat_source, s);
+    if (c.mesh) mesh_domain_from_pod(*c.mesh, s);
     // Validation of src/config/ConfigValidation.cpp:403-408: gradient driving
     // requires fixed lifetimes.
     if (s.temperature_gradient && s.lifetime_temperature_is_local)

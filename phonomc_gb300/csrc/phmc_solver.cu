@@ -271,11 +271,18 @@ void DeviceSolver::upload_tables() {
         D.expected = R.expected;
         for (int k = 0; k < 3; ++k) D.normal[k] = R.normal[k];
         const Facet& F = domain_->facets()[R.facet];
-        for (int tri = 0; tri < 2; ++tri)
+        std::vector<double> tri, cum;
+        double run = 0.0;
+        for (size_t k = 0; k < F.tris.size(); ++k) {
             for (int v = 0; v < 3; ++v)
-                for (int k = 0; k < 3; ++k) D.tri[tri][v][k] = F.tri[tri][v][k];
-        D.area0 = 0.5 * F.area;
-        D.area1 = 0.5 * F.area;
+                for (int a = 0; a < 3; ++a) tri.push_back(F.tris[k][v][a]);
+            run += std::max(F.tri_area[k], 0.0);
+            cum.push_back(run);
+        }
+        if (cum.empty() || !(run > 0.0)) throw std::runtime_error("No faces available for surface sampling.");
+        D.n_tri = static_cast<int>(cum.size());
+        D.tri = upload(tri);
+        D.tri_cum = upload(cum);
         D.cdf = upload(R.cdf);
         D.occ = upload(P_.reservoir_occ[r]);
     }

@@ -898,13 +898,20 @@ __global__ void __launch_bounds__(256) k_inject(const DevTables* __restrict__ Tp
         }
         const int m = lo < R.n_cdf ? lo : R.n_cdf - 1;
         const double temit = P.dt * d0.b;
-        const int tri = d1.a * (R.area0 + R.area1) < R.area0 ? 0 : 1;
+        // area-weighted triangle of the facet: first running sum above u * total
+        const double target = dmul(d1.a, R.tri_cum[R.n_tri - 1]);
+        int lo_t = 0, hi_t = R.n_tri - 1;
+        while (lo_t < hi_t) {
+            const int mid = (lo_t + hi_t) >> 1;
+            if (R.tri_cum[mid] > target) hi_t = mid;
+            else lo_t = mid + 1;
+        }
+        const double* tv = R.tri + 9 * lo_t;
         const double sr1 = sqrt(d1.b);
         const double w0 = 1.0 - sr1, w1 = sr1 * (1.0 - d2.a), w2 = sr1 * d2.a;
         double p[3];
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
-            p[a] = dadd(dadd(dmul(w0, R.tri[tri][0][a]), dmul(w1, R.tri[tri][1][a])), dmul(w2, R.tri[tri][2][a]));
+        for (int a = 0; a < 3; ++a) p[a] = dadd(dadd(dmul(w0, tv[a]), dmul(w1, tv[3 + a])), dmul(w2, tv[6 + a]));
         double v[3] = {M.vel[3 * m], M.vel[3 * m + 1], M.vel[3 * m + 2]};
         uint32_t signs = 0;
         if (dadd(dadd(dmul(v[0], R.normal[0]), dmul(v[1], R.normal[1])), dmul(v[2], R.normal[2])) > 0.0) {

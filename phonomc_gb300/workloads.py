@@ -145,3 +145,40 @@ def scaled(cfg: dict, particles: float, **over) -> dict:
     c["particle_count"] = particles
     c.update(over)
     return c
+
+
+# FinFET mesh domain (10 nm fin, 40 nm tall, on a 200 x 100 x 50 nm slab):
+# x and y sides periodic, the slab bottom a 300 K heat sink, every other wall
+# rough (1 nm). Regions are relative boxes over the bounding box, in order.
+FINFET_REGIONS = [
+    ((0.0, 0.0, 0.001, 1.0, 1.0, 1.01), "R", 1.0),
+    ((-0.001, 0.0, 0.0, 0.001, 1.0, 1.0), "P", 0.0), ((0.999, 0.0, 0.0, 1.001, 1.0, 1.0), "P", 0.0),
+    ((0.0, -0.001, 0.0, 1.0, 0.001, 1.0), "P", 0.0), ((0.0, 0.999, 0.0, 1.0, 1.001, 1.0), "P", 0.0),
+    ((0.0, 0.0, -0.001, 1.0, 1.0, 0.001), "T", 300.0),
+]
+FINFET_PAIRS = [r[0] for r in FINFET_REGIONS[1:5]]
+# Gaussian heat source at the fin top (lengths in Angstrom)
+FINFET_SOURCE = {"profile": "gaussian", "center": (1000.0, 500.0, 900.0), "sigma": (50.0, 50.0, 50.0),
+                 "min": (900.0, 0.0, 700.0), "max": (1100.0, 1000.0, 910.0), "power_density": 1e20,
+                 "spectrum": "thermal"}
+
+
+def finfet_stl(path: str, seed: int = 0) -> str:
+    """Writes the procedural FinFET surface (about 6,300 triangles) as binary STL."""
+    from . import synthetic
+    synthetic.write_stl(path, *synthetic.finfet_mesh(seed=seed))
+    return path
+
+
+def finfet_mesh(stl_path: str, particles: float = 2e7, seed: int = 12345, precision: str = "fp64",
+                grid=(64, 32, 32), heat_source: bool = True, time_step: float = 0.1) -> dict:
+    """FinFET with localized heating: the mesh domain read from `stl_path`,
+    local RTA lifetimes, 300 K background and start, Gaussian 1e20 W/m^3 source
+    of sigma 5 nm at the fin top with thermal spectrum."""
+    c = {"name": "finfet_mesh", "particle_count": float(particles), "time_step": time_step, "iterations": 3000,
+         "random_seed": seed, "compute_kappa": False, "background_temperature": 300.0,
+         "lifetime_temperature": "local", "initial_temperature": 300.0, "grid": tuple(grid), "precision": precision,
+         "mesh": {"model": stl_path, "regions": FINFET_REGIONS, "periodic_pair": FINFET_PAIRS}}
+    if heat_source:
+        c["heat_source"] = dict(FINFET_SOURCE)
+    return c

@@ -46,6 +46,7 @@ CASES = {
     "source_weighted": ["source", "{m}", "1", "0"],
     "source_gaussian": ["source", "{m}", "2", "0"],
     "mesh_finfet": ["mesh", "{f}"],
+    "domain_finfet": ["domain", "{t}"],
     "interface_dmm": ["interface", "{m}", "{s}", "0"],
     "interface_dmm_linearized": ["interface", "{m}", "{s}", "1"],
 }
@@ -85,6 +86,55 @@ periodic_pair = [
 material_folder = "unused"
 output_folder = "{out}"
 """
+
+# FinFET mesh domain in the reference's TOML form (lengths in nm), the same
+# geometry and regions as phonomc_gb300.workloads.finfet_mesh.
+FINFET_TOML = """[geometry]
+model = "{stl}"
+
+[simulation]
+particle_count = {particles}
+time_step = 0.1
+iterations = {steps}
+random_seed = {seed}
+compute_kappa = false
+initial_temperature = 300
+background_temperature = 300
+lifetime_temperature = "local"
+grid_xyz = [{nx}, {ny}, {nz}]
+convergence_write_interval = 1
+
+[boundary]
+boundary_position = [
+  [0.0, 0.0, 0.001, 1.0, 1.0, 1.01],
+  [-0.001, 0.0, 0.0, 0.001, 1.0, 1.0], [0.999, 0.0, 0.0, 1.001, 1.0, 1.0],
+  [0.0, -0.001, 0.0, 1.0, 0.001, 1.0], [0.0, 0.999, 0.0, 1.0, 1.001, 1.0],
+  [0.0, 0.0, -0.001, 1.0, 1.0, 0.001]
+]
+boundary_conditions = ["R", "P", "P", "P", "P", "T"]
+boundary_values = [1.0, 0.0, 0.0, 0.0, 0.0, 300.0]
+periodic_pair = [
+  [-0.001, 0.0, 0.0, 0.001, 1.0, 1.0], [0.999, 0.0, 0.0, 1.001, 1.0, 1.0],
+  [0.0, -0.001, 0.0, 1.0, 0.001, 1.0], [0.0, 0.999, 0.0, 1.0, 1.001, 1.0]
+]
+{source}
+[io]
+material_folder = "unused"
+output_folder = "{out}"
+"""
+
+FINFET_SOURCE_TOML = """
+[heat_source]
+enabled = true
+profile = "gaussian"
+min = [90.0, 0.0, 70.0]
+max = [110.0, 100.0, 91.0]
+center = [100.0, 50.0, 90.0]
+sigma = [5.0, 5.0, 5.0]
+power_density = 1.0e20
+spectrum = "thermal"
+"""
+
 
 # Full reference runs of the scaled cross-plane film (same geometry and physics
 # as phonomc_gb300.workloads.cross_plane_film, 2e4 carriers): per seed, the
@@ -138,6 +188,10 @@ def main() -> None:
     synthetic.write_stl(fpath, *synthetic.finfet_mesh())
     spath = os.path.join(tmp, "m8s.pmat")
     synthetic.write_pmat(spath, synthetic.make_material(mesh=8, freq_scale=0.7, vel_scale=0.75))
+    tpath = os.path.join(tmp, "finfet_domain.toml")
+    with open(tpath, "w") as f:
+        f.write(FINFET_TOML.format(stl=fpath, particles=2000, steps=1, seed=5, nx=64, ny=32, nz=32,
+                                   source=FINFET_SOURCE_TOML, out=os.path.join(tmp, "finfet_domain_out")))
     if not args.only or "fullrun_cross_plane" in args.only:
         m16 = os.path.join(tmp, "m16.pmat")
         synthetic.write_pmat(m16, synthetic.make_material(mesh=16))
@@ -149,7 +203,7 @@ def main() -> None:
     for name, argv in CASES.items():
         if args.only and name not in args.only:
             continue
-        cmd = [HARNESS] + [a.format(m=mpath, c=cpath, s=spath, f=fpath) for a in argv]
+        cmd = [HARNESS] + [a.format(m=mpath, c=cpath, s=spath, f=fpath, t=tpath) for a in argv]
         out = subprocess.run(cmd, check=True, capture_output=True, text=True).stdout
         data = json.loads(out)
         data["_harness_args"] = argv
