@@ -243,6 +243,10 @@ int phmc_domain_contains(const phmc_domain* d, int64_t n, const double* p3, uint
 int phmc_domain_grid_index(const phmc_domain* d, int64_t n, const double* p3, int32_t* cell);
 /* closest facet of each point (-1 for none), src/SurfaceMesh.cpp:996-1003 */
 int phmc_domain_nearest_facet(const phmc_domain* d, int64_t n, const double* p3, int32_t* facet);
+/* The same membership / nearest-facet / cell queries evaluated by the device
+ * code of the carrier loop on a device copy of a mesh domain (nearest may be NULL). */
+int phmc_dev_domain_query(const phmc_domain* d, int64_t n, const double* p3, uint8_t* inside, int32_t* nearest,
+                          int32_t* cell);
 int phmc_batch_create(const phmc_config* cfgs, int n, phmc_material* const* materials, int n_materials,
                       phmc_batch** out);
 int phmc_batch_size(const phmc_batch* b, int* n);

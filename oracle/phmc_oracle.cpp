@@ -40,6 +40,7 @@ double dot3(const Vec3& a, const Vec3& b) { return a[0] * b[0] + a[1] * b[1] + a
 double norm3(const Vec3& a) { return std::sqrt(dot3(a, a)); }
 Vec3 add3(const Vec3& a, const Vec3& b) { return {a[0] + b[0], a[1] + b[1], a[2] + b[2]}; }
 Vec3 mul3(const Vec3& a, double s) { return {a[0] * s, a[1] * s, a[2] * s}; }
+Vec3 sub3(const Vec3& a, const Vec3& b) { return {a[0] - b[0], a[1] - b[1], a[2] - b[2]}; }
 
 double bose(double T, double w) {
     if (T <= 0.0 || w <= 0.0) return 0.0;
@@ -558,6 +559,8 @@ struct OracleSolver {
     std::vector<uint32_t> mode;
     std::vector<int32_t> cell;
     std::vector<uint8_t> alive;
+    // mesh domains: facet whose specular mirror applies to the mode velocity (-1: none)
+    std::vector<int32_t> mirror;
     // grid
     std::vector<double> cell_T, cell_E;
     std::vector<Vec3> cell_q;
@@ -571,14 +574,19 @@ struct OracleSolver {
     long long iface_events = 0, iface_transmitted = 0, iface_reflected = 0;
     bool failed = false;
 
-    Vec3 velocity(uint32_t w) const {
+    Vec3 velocity(uint32_t w, int32_t mir = -1) const {
         const MaterialTables& T = P.mats[w >> 28];
         const int a = static_cast<int>(w & kActiveMask);
         Vec3 v{T.vel[3 * a], T.vel[3 * a + 1], T.vel[3 * a + 2]};
         for (int k = 0; k < 3; ++k)
             if ((w >> (24 + k)) & 1u) v[k] = -v[k];
+        if (mir >= 0) v = reflect(v, domain->facets()[mir].normal);
         return v;
     }
+    Vec3 velocity_of(size_t i) const { return velocity(mode[i], mirror.empty() ? -1 : mirror[i]); }
+
+    // src/solver/BoundaryInteraction.cpp:121-124: v - 2 (v.n) n
+    static Vec3 reflect(const Vec3& v, const Vec3& n) { return sub3(v, mul3(n, 2.0 * dot3(v, n))); }
 
     void init(const std::vector<const PhononMaterial*>& m) {
         mats = m;
@@ -586,6 +594,10 @@ struct OracleSolver {
         P = build_problem(cfg, *domain, mats);
         const CarrierArrays c = initial_carriers(P, mats);
         x = c.x; y = c.y; z = c.z; occ = c.occ; mode = c.mode; cell = c.cell; alive = c.alive;
+        if (domain->is_mesh()) {
+            if (mats.size() != 1) throw std::runtime_error("Layered materials are built for box domains only.");
+            mirror.assign(alive.size(), -1);
+        }
         prev_absorbed.resize(P.reservoirs.size());
         for (size_t r = 0; r < P.reservoirs.size(); ++r) prev_absorbed[r] = P.reservoirs[r].initial_count;
         cur_absorbed.assign(P.reservoirs.size(), 0);
@@ -663,7 +675,8 @@ struct OracleSolver {
         if (F.condition == 'P' && F.pair >= 0) {
             p = add3(p, F.shift);
         } else {
-            const int table = P.rough.facet_table[mid * 6 + f];
+            const int nfac = static_cast<int>(domain->facets().size());
+            const int table = P.rough.facet_table[static_cast<size_t>(mid) * nfac + f];
             if (P.conservative || (F.condition == 'R' && table >= 0)) {
                 if (table < 0) fail("Full-matrix boundary mode mapping failed while advancing particles for particle " + std::to_string(i));
                 const Uniform2 d0 = uniform2(P.cfg.random_seed, static_cast<uint32_t>(i), static_cast<uint32_t>(step), purpose,
@@ -674,23 +687,29 @@ struct OracleSolver {
                 double n_out;
                 const int out = rough_sample(P.rough.tables[table], T, a, occ[i], P.conservative, dr, n_out);
                 uint32_t signs = 0;
-                const double vn = T.vel[3 * out + axis] * F.normal[axis];
+                const bool mesh = domain->is_mesh();
+                const double vn = mesh ? dot3({T.vel[3 * out], T.vel[3 * out + 1], T.vel[3 * out + 2]}, F.normal)
+                                       : T.vel[3 * out + axis] * F.normal[axis];
+                if (mesh) mirror[i] = -1;
                 if (P.conservative) {
                     if (!std::isfinite(n_out) || !(T.omega[out] > 0.0) || !(vn < 0.0))
                         fail("Full-matrix boundary mode mapping failed while advancing particles for particle " + std::to_string(i));
                 } else if (vn > 0.0) {
-                    signs = 1u << axis;
+                    if (mesh) mirror[i] = f; // outward mode velocity mirrored in the facet plane
+                    else signs = 1u << axis;
                 }
                 w = mode_word(static_cast<uint32_t>(out), signs, static_cast<uint32_t>(mid));
                 occ[i] = n_out;
             } else if (F.condition == 'R') {
                 fail("Rough facet without a sampling table is not supported for box geometry.");
+            } else if (domain->is_mesh()) {
+                fail("Specular reflection without a sampling table is not reachable for mesh facets.");
             } else {
                 w ^= 1u << (24 + axis); // specular: exact sign flip of the normal component
             }
             mode[i] = w;
         }
-        const Vec3 v = velocity(mode[i]);
+        const Vec3 v = velocity_of(i);
         p = add3(p, mul3(v, P.push_eps / std::max(norm3(v), 1e-12)));
         return true;
     }
@@ -749,7 +768,7 @@ struct OracleSolver {
         Vec3 cp;
         double t;
         int f;
-        Vec3 v = velocity(mode[i]);
+        Vec3 v = velocity_of(i);
         if (!cache(p, v, cp, t, f))
             fail("Boundary intersection failed while advancing particles for particle " + std::to_string(i) +
                  ". Check that the STL is closed and manifold.");
@@ -769,7 +788,7 @@ struct OracleSolver {
             if (interface_first) {
                 p = add3(p, mul3(v, t_cross));
                 material_interface(i, destination, purpose, event);
-                v = velocity(mode[i]);
+                v = velocity_of(i);
                 const double speed = std::max(norm3(v), 1e-12);
                 p = add3(p, mul3(v, P.push_eps / speed));
             } else {
@@ -778,7 +797,7 @@ struct OracleSolver {
                     x[i] = p[0]; y[i] = p[1]; z[i] = p[2];
                     return;
                 }
-                v = velocity(mode[i]);
+                v = velocity_of(i);
             }
             if (!cache(p, v, cp, t, f)) fail("Boundary intersection failed while advancing particles for particle " + std::to_string(i));
             if (!interface_first && t < 1e-12) {
@@ -844,7 +863,9 @@ struct OracleSolver {
                     slot = static_cast<int>(alive.size());
                     x.push_back(0); y.push_back(0); z.push_back(0); occ.push_back(0); mode.push_back(0);
                     cell.push_back(0); alive.push_back(0);
+                    if (!mirror.empty() || domain->is_mesh()) mirror.push_back(-1);
                 }
+                if (!mirror.empty()) mirror[slot] = -1;
                 x[slot] = pos[0]; y[slot] = pos[1]; z[slot] = pos[2];
                 occ[slot] = o;
                 mode[slot] = mode_word(static_cast<uint32_t>(m), signs, static_cast<uint32_t>(R.material));
@@ -884,9 +905,10 @@ struct OracleSolver {
         for (size_t i = 0; i < alive.size(); ++i) {
             if (!alive[i]) continue;
             const double p[3] = {x[i], y[i], z[i]};
-            for (int a = 0; a < 3; ++a)
-                if (!std::isfinite(p[a]) || p[a] < lo[a] - tol || p[a] > hi[a] + tol)
-                    fail("Particle " + std::to_string(i) + " escaped the domain");
+            bool outside = false;
+            for (int a = 0; a < 3; ++a) outside = outside || !std::isfinite(p[a]) || p[a] < lo[a] - tol || p[a] > hi[a] + tol;
+            if (!outside && domain->is_mesh()) outside = !domain->contains_point({p[0], p[1], p[2]});
+            if (outside) fail("Particle " + std::to_string(i) + " escaped the domain");
         }
     }
 
@@ -1001,7 +1023,7 @@ struct OracleSolver {
             const MaterialTables& T = P.mats[mode[i] >> 28];
             const int a = static_cast<int>(mode[i] & kActiveMask);
             const double e = T.hw[a] * (occ[i] - T.nbg[a]);
-            q[cell[i]] = add3(q[cell[i]], mul3(velocity(mode[i]), e * T.energy_weight));
+            q[cell[i]] = add3(q[cell[i]], mul3(velocity_of(i), e * T.energy_weight));
         }
         double phi = 0, vol = 0;
         const int axis = P.kappa_axis;
@@ -1229,6 +1251,7 @@ int orc_solver_set_carriers(void* sp, int64_t n, const double* x, const double* 
         auto* s = static_cast<OracleSolver*>(sp);
         s->x.assign(x, x + n); s->y.assign(y, y + n); s->z.assign(z, z + n);
         s->occ.assign(occ, occ + n); s->mode.assign(mode, mode + n); s->alive.assign(alive, alive + n);
+        if (s->domain->is_mesh()) s->mirror.assign(static_cast<size_t>(n), -1);
         s->cell.resize(n);
         for (int64_t i = 0; i < n; ++i) s->cell[i] = s->domain->fast_grid_index({x[i], y[i], z[i]});
         s->refresh();

@@ -279,6 +279,7 @@ DOMAIN_PROTOS = {
     "domain_contains": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_uint8_p]),
     "domain_grid_index": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_int32_p]),
     "domain_nearest_facet": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_int32_p]),
+    "dev_domain_query": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_uint8_p, c_int32_p, c_int32_p]),
 }
 
 
@@ -601,3 +602,15 @@ class Domain:
 
     def __del__(self):
         self.close()
+
+
+def device_domain_query(dom: "Domain", p):
+    """(inside, nearest facet, cell) of points by the device code on a mesh domain."""
+    p = np.ascontiguousarray(p, dtype=np.float64).reshape(-1, 3)
+    n = p.shape[0]
+    inside = np.zeros(n, dtype=np.uint8)
+    near = np.zeros(n, dtype=np.int32)
+    cell = np.zeros(n, dtype=np.int32)
+    dom._check(dom.lib.phmc_dev_domain_query(dom.h, n, dptr(p), inside.ctypes.data_as(c_uint8_p),
+                                              near.ctypes.data_as(c_int32_p), cell.ctypes.data_as(c_int32_p)))
+    return inside, near, cell

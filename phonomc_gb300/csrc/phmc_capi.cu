@@ -58,6 +58,37 @@ void cuda_check(cudaError_t e, const char* what) {
     if (e != cudaSuccess) throw std::runtime_error(std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));
 }
 
+// Device copies that live until the end of one entry point.
+struct DevHold {
+    std::vector<void*> p;
+    DevHold() = default;
+    DevHold(const DevHold&) = delete;
+    DevHold& operator=(const DevHold&) = delete;
+    ~DevHold() {
+        for (void* x : p) cudaFree(x);
+    }
+    template <class T> T* put(const std::vector<T>& v) {
+        void* d = nullptr;
+        cuda_check(cudaMalloc(&d, std::max<size_t>(1, v.size()) * sizeof(T)), "cudaMalloc");
+        p.push_back(d);
+        if (!v.empty()) cuda_check(cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy");
+        return static_cast<T*>(d);
+    }
+};
+
+// Membership, nearest facet and cell of points on the device copy of a mesh domain.
+__global__ void k_domain_query(const __grid_constant__ DevTables T, int n, const double* p3, uint8_t* inside,
+                               int32_t* nearest, int32_t* cell, int* err) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double p[3] = {p3[3 * i], p3[3 * i + 1], p3[3 * i + 2]};
+        const int in = mesh_contains(T.fac, p);
+        if (in < 0) atomicExch(err, 1);
+        inside[i] = in > 0 ? 1 : 0;
+        if (nearest) nearest[i] = mesh_nearest_facet(T.fac, p);
+        cell[i] = cell_at(T, p[0], p[1], p[2]);
+    }
+}
+
 template <class T> struct DBuf {
     T* p = nullptr;
     size_t n = 0;
@@ -541,6 +572,43 @@ int phmc_dev_trace_mesh(int nv, const double* vertices, int nf, const int32_t* f
         dh.get(hit3);
         dt.get(t);
         dfc.get(facet);
+    });
+}
+
+int phmc_dev_domain_query(const phmc_domain* d, int64_t n, const double* p3, uint8_t* inside, int32_t* nearest,
+                          int32_t* cell) {
+    return guard([&] {
+        const SimulationDomain& D = *d->d;
+        if (!D.is_mesh()) throw std::invalid_argument("phmc_dev_domain_query: the analytic box has no mesh");
+        if (n < 0 || n > (int64_t{1} << 31) - 1) throw std::invalid_argument("phmc_dev_domain_query: bad point count");
+        DevHold hold;
+        DevTables T;
+        std::memset(&T, 0, sizeof T);
+        double scale = 1.0;
+        for (int a = 0; a < 3; ++a) {
+            T.dom.lo[a] = D.bounds_min()[a];
+            T.dom.hi[a] = D.bounds_max()[a];
+            T.dom.inv_cell[a] = D.inv_cell()[a];
+            T.dom.shape[a] = D.grid_shape()[a];
+            scale = std::max(scale, std::abs(D.bounds_max()[a] - D.bounds_min()[a]));
+        }
+        T.dom.scale = scale;
+        fill_dev_facets(D, scale, T.fac, [&](const auto& v) { return hold.put(v); });
+        if (n == 0) return;
+        DBuf<double> dp(p3, 3 * n);
+        DBuf<uint8_t> din(n);
+        DBuf<int32_t> dnear(n), dcell(n);
+        DBuf<int> derr(1);
+        cuda_check(cudaMemset(derr.p, 0, sizeof(int)), "cudaMemset");
+        k_domain_query<<<256, 128>>>(T, static_cast<int>(n), dp.p, din.p, nearest ? dnear.p : nullptr, dcell.p,
+                                     derr.p);
+        cuda_check(cudaDeviceSynchronize(), "k_domain_query");
+        int err = 0;
+        derr.get(&err);
+        if (err) throw std::runtime_error("phmc_dev_domain_query: membership ray cast hit-list overflow");
+        din.get(inside);
+        if (nearest) dnear.get(nearest);
+        if (cell) dcell.get(cell);
     });
 }
 

@@ -205,6 +205,37 @@ struct DevInterface {
     DevInterfaceBank bank[kMaxMaterials][2];
 };
 
+struct DevMesh {
+    const double* vertices;    // [nv][3]
+    const int* faces;          // [nf][3]
+    const int* face_to_facet;  // [nf]
+    const double* normals;     // [nf][3]
+    const double* k;           // [nf]
+    const double* bounds;      // [nf][6] min xyz, max xyz
+    const double* node_bounds; // [nodes][6]
+    const int* node_links;     // [nodes][4] left, right, begin, end
+    const int* order;          // BVH leaf order of the faces
+    int root;                  // -1: scan all faces
+    int nfaces;
+};
+
+// Boundary data of a mesh domain, per facet (facet count n = 0: analytic box).
+struct DevFacets {
+    int n;
+    const char* cond;              // 'T', 'P', 'R'
+    const int* pair;               // periodic partner or -1
+    const int* reservoir;          // reservoir index or -1
+    const double* shift;           // [n][3] periodic translation
+    const double* normal;          // [n][3] outward unit normal
+    const int* rough_table;        // [material][n] -> rough table or -1
+    const DevRoughTable* rough;    // every rough table of the domain
+    const int* voxel_cell;         // voxel -> active cell
+    DevMesh mesh;                  // oriented faces and their BVH
+    int n_simplex;                 // star decomposition (0: ray cast only)
+    const double* simplex;         // [n_simplex][18]: apex xyz, inverse 3x3 row-major, bounds min xyz, max xyz
+    double ray_pad;                // padding of the BVH culling in the membership ray cast
+};
+
 struct DevTables {
     DevMaterial mat[kMaxMaterials];
     DevInterface iface;
@@ -212,6 +243,7 @@ struct DevTables {
     DevReservoir res[kMaxReservoirs];
     DevDomain dom;
     DevParams par;
+    DevFacets fac;
 };
 
 struct CarrierState {
@@ -225,6 +257,7 @@ struct CarrierState {
     uint32_t* mode;
     int32_t* cell;
     uint8_t* alive;
+    int32_t* mirror; // mesh domains: facet whose mirror applies to the mode velocity, -1 none (else null)
     int4* deferred; // mixed path: queued wall events (slot, time left, event, wall), capacity entries
     int capacity;
 };
@@ -586,19 +619,6 @@ __device__ __forceinline__ IfaceOut interface_dev(const DevTables& T, int src, i
 // Device copy of a MeshTracer (face planes, bounds, BVH); all arithmetic of
 // the trace below is rounded step by step as the host restatement of
 // src/SurfaceMesh.cpp:111-223 and :1164-1269 is.
-struct DevMesh {
-    const double* vertices;    // [nv][3]
-    const int* faces;          // [nf][3]
-    const int* face_to_facet;  // [nf]
-    const double* normals;     // [nf][3]
-    const double* k;           // [nf]
-    const double* bounds;      // [nf][6] min xyz, max xyz
-    const double* node_bounds; // [nodes][6]
-    const int* node_links;     // [nodes][4] left, right, begin, end
-    const int* order;          // BVH leaf order of the faces
-    int root;                  // -1: scan all faces
-    int nfaces;
-};
 
 namespace meshmath {
 __device__ __forceinline__ double dot(const double a[3], const double b[3]) {
@@ -764,6 +784,221 @@ __device__ inline void mesh_trace_dev(const DevMesh& M, const double x[3], const
     for (int a = 0; a < 3; ++a) hit[a] = best_p[a];
     t_out = best_t;
     facet = M.face_to_facet[best];
+}
+
+// ------------------------------------------------------------ mesh domains
+namespace meshmath {
+__device__ __forceinline__ void cross(const double a[3], const double b[3], double o[3]) {
+    o[0] = __dadd_rn(__dmul_rn(a[1], b[2]), -__dmul_rn(a[2], b[1]));
+    o[1] = __dadd_rn(__dmul_rn(a[2], b[0]), -__dmul_rn(a[0], b[2]));
+    o[2] = __dadd_rn(__dmul_rn(a[0], b[1]), -__dmul_rn(a[1], b[0]));
+}
+__device__ __forceinline__ double norm(const double a[3]) { return sqrt(dot(a, a)); }
+// src/SurfaceMesh.cpp:162-186: Moller-Trumbore, eps 1e-10, hit when t > eps
+__device__ __forceinline__ bool ray_triangle(const double o[3], const double d[3], const double a[3], const double b[3],
+                                             const double c[3], double& t) {
+    constexpr double eps = 1e-10;
+    double e1[3], e2[3], pvec[3], tvec[3], qvec[3];
+    sub(b, a, e1);
+    sub(c, a, e2);
+    cross(d, e2, pvec);
+    const double det = dot(e1, pvec);
+    if (fabs(det) < eps) return false;
+    const double inv_det = 1.0 / det;
+    sub(o, a, tvec);
+    const double u = __dmul_rn(dot(tvec, pvec), inv_det);
+    if (u < -eps || u > 1.0 + eps) return false;
+    cross(tvec, e1, qvec);
+    const double v = __dmul_rn(dot(d, qvec), inv_det);
+    if (v < -eps || __dadd_rn(u, v) > 1.0 + eps) return false;
+    t = __dmul_rn(dot(e2, qvec), inv_det);
+    return t > eps;
+}
+} // namespace meshmath
+
+__device__ __forceinline__ void mesh_face(const DevMesh& M, int i, double a[3], double b[3], double c[3]) {
+    const int* f = M.faces + 3 * i;
+    for (int k = 0; k < 3; ++k) {
+        a[k] = M.vertices[3 * f[0] + k];
+        b[k] = M.vertices[3 * f[1] + k];
+        c[k] = M.vertices[3 * f[2] + k];
+    }
+}
+
+// +x ray-cast membership (src/SurfaceMesh.cpp:1100-1124): the Moller-Trumbore
+// hits of every face, sorted, counted as distinct when more than 1e-9 apart;
+// odd means inside. The BVH only culls nodes the ray misses by more than
+// ray_pad, so the hit set is that of the full face scan. Returns -1 when more
+// hits than the local list holds (the caller reports an error).
+__device__ inline int mesh_ray_cast_inside(const DevFacets& F, const double p[3]) {
+    constexpr int kMaxHits = 64;
+    const DevMesh& M = F.mesh;
+    const double dir[3] = {1.0, 0.0, 0.0};
+    double hits[kMaxHits];
+    int nh = 0;
+    bool overflow = false;
+    auto test_face = [&](int i) {
+        double a[3], b[3], c[3], t;
+        mesh_face(M, i, a, b, c);
+        if (!meshmath::ray_triangle(p, dir, a, b, c, t)) return;
+        if (nh < kMaxHits) hits[nh++] = t;
+        else overflow = true;
+    };
+    if (M.root >= 0) {
+        int stack[64];
+        int top = 0;
+        stack[top++] = M.root;
+        const double pad = F.ray_pad;
+        while (top > 0) {
+            const int node = stack[--top];
+            const double* bb = M.node_bounds + 6 * node;
+            if (p[1] < bb[1] - pad || p[1] > bb[4] + pad || p[2] < bb[2] - pad || p[2] > bb[5] + pad ||
+                p[0] > bb[3] + pad)
+                continue;
+            const int* Lk = M.node_links + 4 * node;
+            if (Lk[0] < 0 && Lk[1] < 0) {
+                for (int pos = Lk[2]; pos < Lk[3]; ++pos) test_face(M.order[pos]);
+                continue;
+            }
+            if (top + 2 > 64) {
+                overflow = true;
+                break;
+            }
+            if (Lk[0] >= 0) stack[top++] = Lk[0];
+            if (Lk[1] >= 0) stack[top++] = Lk[1];
+        }
+    } else {
+        for (int i = 0; i < M.nfaces; ++i) test_face(i);
+    }
+    if (overflow) return -1;
+    if (nh == 0) return 0;
+    for (int i = 1; i < nh; ++i) { // insertion sort, ascending
+        const double key = hits[i];
+        int j = i - 1;
+        while (j >= 0 && hits[j] > key) {
+            hits[j + 1] = hits[j];
+            --j;
+        }
+        hits[j + 1] = key;
+    }
+    int unique = 1;
+    for (int i = 1; i < nh; ++i)
+        if (fabs(__dadd_rn(hits[i], -hits[i - 1])) > 1e-9) ++unique;
+    return unique & 1;
+}
+
+// Star-simplex membership with barycentric tolerance 1e-10 (src/SurfaceMesh.cpp:1126-1149).
+__device__ inline bool mesh_simplex_inside(const DevFacets& F, const double p[3]) {
+    constexpr double tol = 1e-10;
+    for (int s = 0; s < F.n_simplex; ++s) {
+        const double* S = F.simplex + 18 * s;
+        if (p[0] < S[12] - tol || p[1] < S[13] - tol || p[2] < S[14] - tol || p[0] > S[15] + tol ||
+            p[1] > S[16] + tol || p[2] > S[17] + tol)
+            continue;
+        const double d[3] = {__dadd_rn(p[0], -S[0]), __dadd_rn(p[1], -S[1]), __dadd_rn(p[2], -S[2])};
+        const double l1 = __dadd_rn(__dadd_rn(__dmul_rn(S[3], d[0]), __dmul_rn(S[4], d[1])), __dmul_rn(S[5], d[2]));
+        const double l2 = __dadd_rn(__dadd_rn(__dmul_rn(S[6], d[0]), __dmul_rn(S[7], d[1])), __dmul_rn(S[8], d[2]));
+        const double l3 = __dadd_rn(__dadd_rn(__dmul_rn(S[9], d[0]), __dmul_rn(S[10], d[1])), __dmul_rn(S[11], d[2]));
+        const double l0 = __dadd_rn(__dadd_rn(__dadd_rn(1.0, -l1), -l2), -l3);
+        if (l0 >= -tol && l1 >= -tol && l2 >= -tol && l3 >= -tol && l0 <= 1.0 + tol && l1 <= 1.0 + tol &&
+            l2 <= 1.0 + tol && l3 <= 1.0 + tol)
+            return true;
+    }
+    return false;
+}
+
+// SurfaceMesh::contains_point: inside a simplex of the decomposition, else the
+// ray cast. Evaluated ray cast first (the result is their union). -1 on a
+// hit-list overflow.
+__device__ inline int mesh_contains(const DevFacets& F, const double p[3]) {
+    const int r = mesh_ray_cast_inside(F, p);
+    if (r != 0) return r;
+    return mesh_simplex_inside(F, p) ? 1 : 0;
+}
+
+// Facet of the closest face, first minimum (src/SurfaceMesh.cpp:996-1023).
+__device__ inline int mesh_nearest_facet(const DevFacets& F, const double p[3]) {
+    const DevMesh& M = F.mesh;
+    int best = -1;
+    double bd = __longlong_as_double(0x7ff0000000000000LL);
+    for (int i = 0; i < M.nfaces; ++i) {
+        double a[3], b[3], c[3], cp[3], d[3];
+        mesh_face(M, i, a, b, c);
+        meshmath::closest(p, a, b, c, cp);
+        meshmath::sub(p, cp, d);
+        const double dist = meshmath::norm(d);
+        if (dist < bd) {
+            bd = dist;
+            best = i;
+        }
+    }
+    return best < 0 ? -1 : M.face_to_facet[best];
+}
+
+// Velocity of a carrier in a mesh domain: the mode velocity (with sign flips),
+// mirrored in the plane of facet `mir` when set (src/solver/BoundaryInteraction.cpp:121-124).
+__device__ __forceinline__ void mesh_velocity(const DevFacets& F, const DevMaterial& M, uint32_t w, int mir,
+                                              double v[3]) {
+    mode_velocity(M, w, v);
+    if (mir >= 0) {
+        const double* n = F.normal + 3 * mir;
+        const double nn[3] = {n[0], n[1], n[2]};
+        const double s = __dmul_rn(2.0, meshmath::dot(v, nn));
+        for (int k = 0; k < 3; ++k) v[k] = __dadd_rn(v[k], -__dmul_rn(nn[k], s));
+    }
+}
+
+// Wall-hit cache with nudged retries on the mesh (src/solver/TransportOperator.cpp:186-250).
+// Returns 0 on success, 1 when no retry found a wall, 2 on a membership overflow.
+__device__ inline int mesh_cache_hit(const DevFacets& F, const DevDomain& D, const DevParams& P, double p[3],
+                                     const double v[3], double cp[3], double& t, int& f) {
+    const double speed = meshmath::norm(v);
+    if (isfinite(speed) && speed <= 1e-18) {
+        for (int a = 0; a < 3; ++a) cp[a] = p[a];
+        t = __longlong_as_double(0x7ff0000000000000LL);
+        f = -1;
+        return 0;
+    }
+    mesh_trace_dev(F.mesh, p, v, cp, t, f);
+    if (f >= 0 && isfinite(t)) return 0;
+    const double eps = fmax(P.push_eps, 1e-10 * D.scale);
+    double cand[4][3];
+    for (int c = 0; c < 4; ++c)
+        for (int a = 0; a < 3; ++a) cand[c][a] = p[a];
+    const int nearest = mesh_nearest_facet(F, p);
+    if (nearest >= 0) {
+        const double* n = F.normal + 3 * nearest;
+        for (int a = 0; a < 3; ++a) {
+            cand[0][a] = __dadd_rn(p[a], __dmul_rn(n[a], eps));
+            cand[1][a] = __dadd_rn(p[a], __dmul_rn(n[a], -eps));
+        }
+    }
+    if (speed > 0.0 && isfinite(speed)) {
+        const double inv = 1.0 / speed;
+        for (int a = 0; a < 3; ++a) {
+            const double d = __dmul_rn(v[a], inv);
+            cand[2][a] = __dadd_rn(p[a], __dmul_rn(d, eps));
+            cand[3][a] = __dadd_rn(p[a], __dmul_rn(d, -eps));
+        }
+    }
+    for (int c = 0; c < 4; ++c) {
+        const int in = mesh_contains(F, cand[c]);
+        if (in < 0) return 2;
+        if (!in) continue;
+        mesh_trace_dev(F.mesh, cand[c], v, cp, t, f);
+        if (f >= 0 && isfinite(t)) {
+            for (int a = 0; a < 3; ++a) p[a] = cand[c][a];
+            return 0;
+        }
+    }
+    return 1;
+}
+
+// Active cell of a point: the voxel, through the voxel map on mesh domains
+// (src/SimulationDomain.cpp:92-126).
+__device__ __forceinline__ int cell_at(const DevTables& T, double x, double y, double z) {
+    const int v = grid_index(T.dom, x, y, z);
+    return T.fac.voxel_cell ? __ldg(T.fac.voxel_cell + v) : v;
 }
 
 // Heat-source energy factor (ps) of [begin, end] under the time profile

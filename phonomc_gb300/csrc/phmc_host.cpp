@@ -478,8 +478,7 @@ void RoughTables::build(const std::vector<const PhononMaterial*>& mats, const st
             }
             shell[ai] = shells - 1;
         }
-        for (int f = 0; f < nf; ++f) {
-            if (!enabled[f]) continue;
+        auto build_one = [&](int f) {
             RoughTable rd;
             rd.facet = f;
             rd.material = static_cast<int>(mid);
@@ -610,8 +609,26 @@ void RoughTables::build(const std::vector<const PhononMaterial*>& mats, const st
                     rd.roulette_cdf.push_back(cdf);
                 }
             }
-            facet_table[mid * nf + f] = static_cast<int>(tables.size());
-            tables.push_back(std::move(rd));
+            return rd;
+        };
+        // Tables of different facets are independent: built in parallel, stored in facet order.
+        std::vector<int> todo;
+        for (int f = 0; f < nf; ++f)
+            if (enabled[f]) todo.push_back(f);
+        std::vector<RoughTable> built(todo.size());
+        std::vector<std::string> errors(todo.size());
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int k = 0; k < static_cast<int>(todo.size()); ++k) {
+            try {
+                built[k] = build_one(todo[k]);
+            } catch (const std::exception& e) {
+                errors[k] = e.what();
+            }
+        }
+        for (size_t k = 0; k < todo.size(); ++k) {
+            if (!errors[k].empty()) throw std::invalid_argument(errors[k]);
+            facet_table[mid * nf + todo[k]] = static_cast<int>(tables.size());
+            tables.push_back(std::move(built[k]));
         }
     }
 }
@@ -1156,11 +1173,48 @@ CarrierArrays initial_carriers(const Problem& p, const std::vector<const PhononM
     const Vec3& lo = D.bounds_min();
     const Vec3& hi = D.bounds_max();
     const uint64_t seed = p.cfg.random_seed;
+    // Mesh domains (src/geometry/SurfaceSampling.cpp:102-155): a simplex of the
+    // volume decomposition by volume, then Dirichlet(1,1,1,1) weights from four
+    // exponentials; without a valid decomposition, uniform box points kept
+    // when the +x ray cast finds them inside (at most 200 trials per carrier).
+    const SurfaceMesh* mesh = D.is_mesh() ? D.mesh() : nullptr;
+    std::vector<double> simplex_cum;
+    if (mesh) {
+        double run = 0.0;
+        for (const auto& sx : mesh->simplices()) simplex_cum.push_back(run += std::max(sx.volume, 0.0));
+        if (!simplex_cum.empty() && !(run > 0.0)) simplex_cum.clear();
+    }
+    int rejected = -1;
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < n; ++i) {
         const Uniform2 u0 = uniform2(seed, static_cast<uint32_t>(i), 0xFFFFFFFFu, kDrawInit, 0, 0);
         const Uniform2 u1 = uniform2(seed, static_cast<uint32_t>(i), 0xFFFFFFFFu, kDrawInit, 0, 1);
-        const Vec3 pos{lo[0] + (hi[0] - lo[0]) * u0.a, lo[1] + (hi[1] - lo[1]) * u0.b, lo[2] + (hi[2] - lo[2]) * u1.a};
+        Vec3 pos{lo[0] + (hi[0] - lo[0]) * u0.a, lo[1] + (hi[1] - lo[1]) * u0.b, lo[2] + (hi[2] - lo[2]) * u1.a};
+        if (mesh && !simplex_cum.empty()) {
+            size_t k = static_cast<size_t>(std::upper_bound(simplex_cum.begin(), simplex_cum.end(),
+                                                            u0.a * simplex_cum.back()) - simplex_cum.begin());
+            if (k >= simplex_cum.size()) k = simplex_cum.size() - 1;
+            const auto& sx = mesh->simplices()[k];
+            const Uniform2 u2 = uniform2(seed, static_cast<uint32_t>(i), 0xFFFFFFFFu, kDrawInit, 0, 2);
+            double a[4] = {-std::log(std::max(u0.b, 1e-15)), -std::log(std::max(u1.a, 1e-15)),
+                           -std::log(std::max(u2.a, 1e-15)), -std::log(std::max(u2.b, 1e-15))};
+            const double sum = a[0] + a[1] + a[2] + a[3];
+            for (double& w : a) w /= sum;
+            for (int c = 0; c < 3; ++c)
+                pos[c] = a[0] * sx.v[0][c] + a[1] * sx.v[1][c] + a[2] * sx.v[2][c] + a[3] * sx.v[3][c];
+        } else if (mesh) {
+            bool ok = mesh->contains_point_ray_cast(pos);
+            for (uint32_t trial = 1; !ok && trial < 200; ++trial) {
+                const Uniform2 r0 = uniform2(seed, static_cast<uint32_t>(i), 0xFFFFFFFFu, kDrawInit, trial, 0);
+                const Uniform2 r1 = uniform2(seed, static_cast<uint32_t>(i), 0xFFFFFFFFu, kDrawInit, trial, 1);
+                pos = {lo[0] + (hi[0] - lo[0]) * r0.a, lo[1] + (hi[1] - lo[1]) * r0.b, lo[2] + (hi[2] - lo[2]) * r1.a};
+                ok = mesh->contains_point_ray_cast(pos);
+            }
+            if (!ok) {
+#pragma omp critical
+                rejected = i;
+            }
+        }
         const int mid = p.layout.material_at(pos);
         const MaterialTables& T = p.mats[mid];
         int a = static_cast<int>(u1.b * T.n_active);
@@ -1183,6 +1237,7 @@ CarrierArrays initial_carriers(const Problem& p, const std::vector<const PhononM
         c.occ[i] = p.linearized ? mats[mid]->linearized_bose_occupation(temp, p.cfg.background_temperature, flat)
                                 : mats[mid]->bose_occupation(temp, flat);
     }
+    if (rejected >= 0) throw std::runtime_error("sample_volume_points_naive: insufficient accepted samples.");
     return c;
 }
 

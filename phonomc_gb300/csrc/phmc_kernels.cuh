@@ -20,6 +20,7 @@ struct LaunchCtx {
     DevLedger* L;
     cudaStream_t stream;
     int grid_blocks;
+    bool mesh = false;   // surface-mesh domain (plain FP64 carrier state)
 };
 
 int launch_transport(const LaunchCtx& x, bool mixed, bool rta);
@@ -48,5 +49,72 @@ void launch_cells_final(const LaunchCtx& x, int phase);
 
 // collision kinds for launch_cell_solve
 enum CollisionKind : int { kCollideNone = 0, kCollideRta = 1, kCollideLinear = 2 };
+
+
+// Device copy of a mesh domain's geometry: facet conditions, partners, shifts
+// and normals, the voxel -> cell map, the faces with their BVH and the star
+// simplices. `up(std::vector<T>)` returns a device pointer holding the vector.
+template <class Upload>
+void fill_dev_facets(const SimulationDomain& dom, double scale, DevFacets& G, Upload&& up) {
+    const auto& F = dom.facets();
+    const SurfaceMesh& M = *dom.mesh();
+    const MeshTracer& Tr = M.tracer();
+    const int nf = static_cast<int>(F.size());
+    std::vector<char> cond(nf);
+    std::vector<int> pair(nf), res(nf);
+    std::vector<double> shift(3 * static_cast<size_t>(nf)), normal(3 * static_cast<size_t>(nf));
+    for (int f = 0; f < nf; ++f) {
+        cond[f] = F[f].condition;
+        pair[f] = F[f].pair;
+        res[f] = F[f].reservoir;
+        for (int a = 0; a < 3; ++a) {
+            shift[3 * f + a] = F[f].shift[a];
+            normal[3 * f + a] = F[f].normal[a];
+        }
+    }
+    G.n = nf;
+    G.cond = up(cond);
+    G.pair = up(pair);
+    G.reservoir = up(res);
+    G.shift = up(shift);
+    G.normal = up(normal);
+    G.voxel_cell = up(dom.voxel_cells());
+    std::vector<double> vv, nrm, bnd, nb;
+    std::vector<int> ff, links;
+    for (const auto& v : Tr.vertices) vv.insert(vv.end(), v.begin(), v.end());
+    for (const auto& f : Tr.faces) ff.insert(ff.end(), f.begin(), f.end());
+    for (const auto& x : Tr.normals) nrm.insert(nrm.end(), x.begin(), x.end());
+    for (const auto& b : Tr.bounds) {
+        bnd.insert(bnd.end(), b[0].begin(), b[0].end());
+        bnd.insert(bnd.end(), b[1].begin(), b[1].end());
+    }
+    for (const auto& nd : Tr.nodes) {
+        nb.insert(nb.end(), nd.bmin.begin(), nd.bmin.end());
+        nb.insert(nb.end(), nd.bmax.begin(), nd.bmax.end());
+        links.insert(links.end(), {nd.left, nd.right, nd.begin, nd.end});
+    }
+    DevMesh& D = G.mesh;
+    D.vertices = up(vv);
+    D.faces = up(ff);
+    D.face_to_facet = up(Tr.face_to_facet);
+    D.normals = up(nrm);
+    D.k = up(Tr.k);
+    D.bounds = up(bnd);
+    D.node_bounds = up(nb);
+    D.node_links = up(links);
+    D.order = up(Tr.order);
+    D.root = Tr.root;
+    D.nfaces = static_cast<int>(Tr.faces.size());
+    std::vector<double> sx;
+    for (const auto& S : M.simplices()) {
+        sx.insert(sx.end(), S.v[0].begin(), S.v[0].end());
+        for (int r = 0; r < 3; ++r) sx.insert(sx.end(), S.inv[r].begin(), S.inv[r].end());
+        sx.insert(sx.end(), S.bounds[0].begin(), S.bounds[0].end());
+        sx.insert(sx.end(), S.bounds[1].begin(), S.bounds[1].end());
+    }
+    G.n_simplex = static_cast<int>(M.simplices().size());
+    G.simplex = up(sx);
+    G.ray_pad = 1e-9 * scale;
+}
 
 } // namespace phmc

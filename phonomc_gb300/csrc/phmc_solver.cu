@@ -61,6 +61,12 @@ DeviceSolver::DeviceSolver(const SimulationConfig& cfg, const std::vector<const 
     PHMC_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, 0);
     domain_ = std::make_unique<SimulationDomain>(cfg_);
+    if (domain_->is_mesh()) {
+        if (mixed_)
+            throw std::runtime_error("Mesh domains run with plain FP64 carrier state (precision = fp64); the FP32 "
+                                     "cell-frame flight is built for box domains.");
+        if (mats_.size() != 1) throw std::runtime_error("Layered materials are built for box domains only.");
+    }
     P_ = build_problem(cfg_, *domain_, mats_);
     ncells_ = domain_->grid_count();
     const int n0 = P_.initial_particles;
@@ -110,6 +116,10 @@ void DeviceSolver::allocate_state(int capacity) {
         state_.oy = dalloc<float>(capacity);
         state_.oz = dalloc<float>(capacity);
         state_.deferred = dalloc<int4>(capacity);
+    }
+    if (domain_->is_mesh()) {
+        state_.mirror = dalloc<int32_t>(capacity);
+        PHMC_CUDA(cudaMemsetAsync(state_.mirror, 0xFF, static_cast<size_t>(capacity) * sizeof(int32_t), stream_));
     }
     state_.occ = dalloc<double>(capacity);
     state_.mode = dalloc<uint32_t>(capacity);
@@ -241,11 +251,14 @@ void DeviceSolver::upload_tables() {
         D.heat_capacity_density_bg = M.heat_capacity_density_bg;
         D.zero_point = M.zero_point;
     }
-    // rough tables
-    if (P_.rough.tables.size() > static_cast<size_t>(kMaxRoughTables)) throw std::runtime_error("too many rough tables");
+    // rough tables: inline for the box, a device array for mesh domains
+    const bool mesh = domain_->is_mesh();
+    std::vector<DevRoughTable> mesh_rough(mesh ? P_.rough.tables.size() : 0);
+    if (!mesh && P_.rough.tables.size() > static_cast<size_t>(kMaxRoughTables))
+        throw std::runtime_error("too many rough tables");
     for (size_t t = 0; t < P_.rough.tables.size(); ++t) {
         const RoughTable& R = P_.rough.tables[t];
-        DevRoughTable& D = T.rough[t];
+        DevRoughTable& D = mesh ? mesh_rough[t] : T.rough[t];
         D.strict = R.strict_elastic ? 1 : 0;
         D.n_sorted = static_cast<int>(R.outgoing_sorted.size());
         D.n_roulette = static_cast<int>(R.roulette_active.size());
@@ -322,7 +335,8 @@ void DeviceSolver::upload_tables() {
                 throw std::runtime_error("cell index division constants failed their check");
         }
     }
-    for (int f = 0; f < 6; ++f) {
+    if (mesh) upload_mesh(mesh_rough);
+    for (int f = 0; f < 6 && !mesh; ++f) {
         const Facet& F = domain_->facets()[f];
         D.cond[f] = F.condition;
         D.pair[f] = F.pair;
@@ -485,6 +499,14 @@ void DeviceSolver::upload_tables() {
     }
 }
 
+// Facet arrays, rough tables, voxel map, face BVH and star simplices of a mesh domain.
+void DeviceSolver::upload_mesh(const std::vector<DevRoughTable>& rough) {
+    DevFacets& G = tables_.fac;
+    fill_dev_facets(*domain_, tables_.dom.scale, G, [&](const auto& v) { return upload(v); });
+    G.rough_table = upload(P_.rough.facet_table);
+    G.rough = upload(rough);
+}
+
 LaunchCtx DeviceSolver::ctx() const {
     LaunchCtx x;
     x.T = d_tables_;
@@ -498,6 +520,7 @@ LaunchCtx DeviceSolver::ctx() const {
     // batch do not launch idle CTAs
     const long long want = (static_cast<long long>(state_.capacity) + 1023) / 1024;
     x.grid_blocks = static_cast<int>(std::max<long long>(8, std::min<long long>(sm_count_ * 8, want)));
+    x.mesh = domain_->is_mesh();
     return x;
 }
 

@@ -166,6 +166,7 @@ public:
 
 private:
     void upload_tables();
+    void upload_mesh(const std::vector<DevRoughTable>& rough);
     void allocate_state(int capacity);
     void initial_statistics();
     void enqueue_step(bool profile);

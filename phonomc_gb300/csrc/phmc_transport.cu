@@ -216,6 +216,92 @@ __device__ bool advance_carrier(const DevTables& T, DevLedger* L, BlockLedger* b
     return true;
 }
 
+// One carrier's flight in a mesh domain (single material): the wall cache on
+// the face BVH with nudged retries, per-facet conditions, rough reflections
+// whose outward mode velocity is mirrored in the facet plane (`mir`), and the
+// push along the velocity actually carried (src/solver/TransportOperator.cpp:287-361, 405-466).
+__device__ bool advance_carrier_mesh(const DevTables& T, DevLedger* L, BlockLedger* bl, int slot, double p[3],
+                                     uint32_t& w, int& mir, double& occ, double remaining, uint32_t purpose,
+                                     uint32_t step) {
+    const DevFacets& F = T.fac;
+    const DevDomain& D = T.dom;
+    const DevParams& P = T.par;
+    const int mid = static_cast<int>(w >> 28);
+    const DevMaterial& M = T.mat[mid];
+    double v[3];
+    mesh_velocity(F, M, w, mir, v);
+    double cp[3], t;
+    int f;
+    auto cache = [&]() {
+        const int r = mesh_cache_hit(F, D, P, p, v, cp, t, f);
+        if (r != 0) raise_error(L, r == 2 ? kErrInvalidStatistics : kErrIntersection, slot);
+        return r == 0;
+    };
+    if (!cache()) return true;
+    int event = 0;
+    for (; remaining > 1e-14 && event < 64; ++event) {
+        if (!isfinite(t) || t > remaining) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], remaining));
+            return true;
+        }
+        remaining -= fmax(0.0, t);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) p[a] = cp[a];
+        const int ai = static_cast<int>(w & 0x00FFFFFFu);
+        const char cond = F.cond[f];
+        if (cond == 'T') {
+            const double e = dmul(dmul(M.hw[ai], occ - M.nbg[ai]), M.energy_weight);
+            atomicAdd(&bl->absorbed, 1u);
+            atomicAdd(&bl->absorbed_ev, e);
+            const int r = F.reservoir[f];
+            if (r >= 0) atomicAdd(&bl->absorbed_res[r], 1u);
+            return false;
+        }
+        if (cond == 'P' && F.pair[f] >= 0) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], F.shift[3 * f + a]);
+        } else {
+            const int table = F.rough_table[mid * F.n + f];
+            if (!(P.conservative || (cond == 'R' && table >= 0)) || table < 0) {
+                raise_error(L, cond == 'R' && !P.conservative ? kErrNoRoughTable : kErrModeMapping, slot);
+                return true;
+            }
+            const Uniform2 d0 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose, static_cast<uint32_t>(event), 0);
+            const Uniform2 d1 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose, static_cast<uint32_t>(event), 1);
+            double n_out;
+            const int out = rough_sample_dev(F.rough[table], M, ai, occ, P.conservative != 0, d0.a, d0.b, d1.a, n_out);
+            const double* nf = F.normal + 3 * f;
+            const double vo[3] = {M.vel[3 * out], M.vel[3 * out + 1], M.vel[3 * out + 2]};
+            const double nn[3] = {nf[0], nf[1], nf[2]};
+            const double vn = meshmath::dot(vo, nn);
+            mir = -1;
+            if (P.conservative) {
+                if (!isfinite(n_out) || !(M.omega[out] > 0.0) || !(vn < 0.0)) {
+                    raise_error(L, kErrModeMapping, slot);
+                    return true;
+                }
+            } else if (vn > 0.0) {
+                mir = f;
+            }
+            w = static_cast<uint32_t>(out) | (static_cast<uint32_t>(mid) << 28);
+            occ = n_out;
+        }
+        mesh_velocity(F, M, w, mir, v);
+        const double s = P.push_eps / fmax(meshmath::norm(v), 1e-12);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], s));
+        if (!cache()) return true;
+        if (t < 1e-12) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], 1e-12));
+            if (!cache()) return true;
+        }
+    }
+    if (remaining > 1e-14) raise_error(L, kErrTooManyEvents, slot);
+    return true;
+}
+
 // ------------------------------------------------------------------ bins
 __device__ __forceinline__ int bin_of(const DevMaterial& M, int ai) { return M.bin ? __ldg(M.bin + ai) : ai; }
 
@@ -536,7 +622,7 @@ constexpr int kDeferBuffer = 64; // queued wall events per warp before a flush
 // bin. Mixed path: carriers that reach a wall needing table sampling are
 // queued (per-warp shared buffers, one global atomic per 32 entries) and
 // finished by k_deferred.
-template <bool kMixed, bool kRta>
+template <bool kMixed, bool kRta, bool kMesh = false>
 __global__ void __launch_bounds__(kTransportThreads) k_transport(const __grid_constant__ DevTables T, CarrierState S,
                                                                  CellArrays C, DevLedger* L) {
     const uint32_t step = L->step_index; // timesteps completed: the draw counter of this step
@@ -614,8 +700,17 @@ __global__ void __launch_bounds__(kTransportThreads) k_transport(const __grid_co
             const int c0 = __ldcs(S.cell + i);
             double occ = apply_pending(T, C, c0, w, __ldcs(S.occ + i));
             double p[3] = {__ldcs(S.x + i), __ldcs(S.y + i), __ldcs(S.z + i)};
-            const bool alive = advance_carrier(T, L, &bl, i, p, w, occ, T.par.dt, kDrawTransport, step);
-            const int c = grid_index(T.dom, p[0], p[1], p[2]);
+            bool alive;
+            int c;
+            if constexpr (kMesh) {
+                int mir = S.mirror[i];
+                alive = advance_carrier_mesh(T, L, &bl, i, p, w, mir, occ, T.par.dt, kDrawTransport, step);
+                S.mirror[i] = mir;
+                c = cell_at(T, p[0], p[1], p[2]);
+            } else {
+                alive = advance_carrier(T, L, &bl, i, p, w, occ, T.par.dt, kDrawTransport, step);
+                c = grid_index(T.dom, p[0], p[1], p[2]);
+            }
             __stcs(S.x + i, p[0]);
             __stcs(S.y + i, p[1]);
             __stcs(S.z + i, p[2]);
@@ -692,8 +787,9 @@ __global__ void k_init_cells(const DevTables* __restrict__ Tp, CarrierState S, D
     const int n = L->n_slots;
     unsigned long long live = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int c = grid_index(D, S.x[i], S.y[i], S.z[i]);
+        const int c = cell_at(*Tp, S.x[i], S.y[i], S.z[i]);
         S.cell[i] = c;
+        if (S.mirror) S.mirror[i] = -1;
         if (kMixed) {
             const Frame F = cell_frame(D, c);
             S.ox[i] = static_cast<float>(S.x[i] - (D.lo[0] + F.i[0] * D.cell_size[0]));
@@ -715,8 +811,9 @@ __global__ void k_ingest(const __grid_constant__ DevTables T, CarrierState S, De
     unsigned long long live = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const double x = H.x[i], y = H.y[i], z = H.z[i];
-        const int c = grid_index(D, x, y, z);
+        const int c = cell_at(T, x, y, z);
         S.cell[i] = c;
+        if (S.mirror) S.mirror[i] = -1;
         if (kMixed) {
             const Frame F = cell_frame(D, c);
             S.ox[i] = static_cast<float>(x - (D.lo[0] + F.i[0] * D.cell_size[0]));
@@ -869,7 +966,7 @@ __global__ void __launch_bounds__(kHoleBlock) k_dead_write(CarrierState S, const
     }
 }
 
-template <bool kMixed, bool kRta>
+template <bool kMixed, bool kRta, bool kMesh = false>
 __global__ void __launch_bounds__(256) k_inject(const DevTables* __restrict__ Tp, CarrierState S, CellArrays C,
                                                 DevLedger* L, const int* holes) {
     const uint32_t step = L->step_index;
@@ -944,6 +1041,14 @@ __global__ void __launch_bounds__(256) k_inject(const DevTables* __restrict__ Tp
             S.ox[slot] = q[0];
             S.oy[slot] = q[1];
             S.oz[slot] = q[2];
+        } else if (kMesh) {
+            int mir = -1;
+            if (remain > 1e-14) alive = advance_carrier_mesh(T, L, &bl, slot, p, w, mir, occ, remain, kDrawInjected, step);
+            S.mirror[slot] = mir;
+            c = cell_at(T, p[0], p[1], p[2]);
+            S.x[slot] = p[0];
+            S.y[slot] = p[1];
+            S.z[slot] = p[2];
         } else {
             if (remain > 1e-14) alive = advance_carrier(T, L, &bl, slot, p, w, occ, remain, kDrawInjected, step);
             c = grid_index(T.dom, p[0], p[1], p[2]);
@@ -988,8 +1093,14 @@ __global__ void k_containment(const DevTables* __restrict__ Tp, CarrierState S, 
         }
         // FP32 offsets carry ~1e-7 relative rounding of the cell size
         const double t = kMixed ? 1e-5 * D.scale : tol;
-        for (int a = 0; a < 3; ++a)
-            if (!isfinite(p[a]) || p[a] < D.lo[a] - t || p[a] > D.hi[a] + t) raise_error(L, kErrEscaped, i);
+        bool outside = false;
+        for (int a = 0; a < 3; ++a) outside = outside || !isfinite(p[a]) || p[a] < D.lo[a] - t || p[a] > D.hi[a] + t;
+        if (!outside && Tp->fac.n > 0) {
+            const int in = mesh_contains(Tp->fac, p);
+            if (in < 0) raise_error(L, kErrInvalidStatistics, i);
+            outside = in == 0;
+        }
+        if (outside) raise_error(L, kErrEscaped, i);
     }
 }
 
@@ -1013,7 +1124,8 @@ __global__ void __launch_bounds__(256) k_flux(const DevTables* __restrict__ Tp, 
         if (C.src_next) occ -= C.src_next[static_cast<size_t>(c) * C.hist_modes + bin_of(M, ai)];
         const double e = dmul(dmul(M.hw[ai], occ - M.nbg[ai]), M.energy_weight);
         double v[3];
-        mode_velocity(M, w, v);
+        if (S.mirror) mesh_velocity(T.fac, M, w, S.mirror[i], v);
+        else mode_velocity(M, w, v);
         double* dst = use_shared ? sq : C.flux;
         for (int a = 0; a < 3; ++a) atomicAdd(dst + 3 * c + a, dmul(v[a], e));
     }
@@ -1071,6 +1183,11 @@ int launch_transport(const LaunchCtx& x, bool mixed, bool rta) {
         }
         return 2;
     }
+    if (x.mesh) {
+        if (rta) k_transport<false, true, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+        else k_transport<false, false, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+        return 1;
+    }
     if (rta) k_transport<false, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
     else k_transport<false, false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
     return 1;
@@ -1106,6 +1223,9 @@ int launch_inject(const LaunchCtx& x, bool mixed, bool rta, int* holes, int* blo
     if (mixed) {
         if (rta) k_inject<true, true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes);
         else k_inject<true, false><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes);
+    } else if (x.mesh) {
+        if (rta) k_inject<false, true, true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes);
+        else k_inject<false, false, true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes);
     } else {
         if (rta) k_inject<false, true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes);
         else k_inject<false, false><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes);

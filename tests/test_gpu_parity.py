@@ -483,3 +483,43 @@ def test_mesh_trace_golden(gpu):
     assert np.array_equal(fac, g["facet"])
     assert np.array_equal(t, np.asarray(g["t"]))
     assert np.array_equal(hit, np.asarray(g["hits"]))
+
+
+@pytest.fixture(scope="module")
+def finfet_stl(tmp_path_factory):
+    return workloads.finfet_stl(str(tmp_path_factory.mktemp("finfet") / "finfet.stl"))
+
+
+def test_mesh_domain_device_queries_golden(gpu, finfet_stl):
+    """Device membership (BVH ray cast, then star simplices), nearest facet and
+    voxel-map cell of the reference's random points, bit-exact."""
+    g = golden("domain_finfet")
+    dom = abi.Domain(gpu, workloads.finfet_mesh(finfet_stl))
+    inside, near, cell = abi.device_domain_query(dom, g["points"])
+    assert np.array_equal(inside, np.asarray(g["inside"], dtype=np.uint8))
+    assert np.array_equal(near, np.asarray(g["nearest_facet"], dtype=np.int32))
+    assert np.array_equal(cell, np.asarray(g["cell"], dtype=np.int32))
+    # cell centres: inside, and each maps to its own cell
+    C = dom.cells()
+    inside, _, cell = abi.device_domain_query(dom, C["centers"])
+    assert inside.all()
+    assert np.array_equal(cell, np.arange(dom.n_cells, dtype=np.int32))
+
+
+@pytest.mark.parametrize("source", [True, False])
+def test_finfet_steps_match_oracle(gpu, orc, finfet_stl, source):
+    """FinFET mesh domain (BVH walls, rough facets with mirrored outward modes,
+    periodic facet pairs, heat sink, Gaussian heat source): device timesteps
+    against the oracle on the same initial carriers."""
+    cfg = workloads.finfet_mesh(finfet_stl, particles=20000, seed=11, grid=(32, 8, 16), heat_source=source)
+    mat = synthetic.make_material(mesh=8)
+    (sg, _), (so, _) = _pair(gpu, orc, cfg, False, mat)
+    _compare(sg, so, tol=1e-11)
+    for _ in range(3):
+        sg.run(1)
+        so.run(1)
+        stg, sto = _compare(sg, so, tol=1e-11)
+        if source:
+            for k in ("total_heat_source_energy_ev", "prescribed_heat_source_energy_ev"):
+                assert abs(stg[k] - sto[k]) <= 1e-12 * max(1.0, abs(sto[k])), k
+    assert sto["absorbed_total"] > 0 and sto["injected_total"] > 0
