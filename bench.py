@@ -37,10 +37,26 @@ UNIT = "carrier-steps/s"
 # Algorithmic bytes per carrier-step of the transport pass: read position,
 # occupation, mode and cell; write position, occupation and cell.
 BYTES_PER_CARRIER = {"fp64": 76, "mixed": 52}  # FP64 state / FP32 cell-local offsets
+MESH_MIRROR_BYTES = 8  # mesh domains: the mirror facet of each carrier, read and written
+
+
+_STL = {}
+
+
+def finfet_stl_path():
+    """The procedural FinFET surface, written once per process to a temporary file."""
+    if "path" not in _STL:
+        import tempfile
+        from phonomc_gb300 import workloads
+        d = tempfile.mkdtemp(prefix="phmc_finfet_")
+        _STL["path"] = workloads.finfet_stl(os.path.join(d, "finfet.stl"))
+    return _STL["path"]
 
 
 def workload_config(name, particles, precision, seed=12345):
     from phonomc_gb300 import workloads
+    if name == "finfet_mesh":
+        return workloads.finfet_mesh(finfet_stl_path(), particles=particles, seed=seed, precision=precision)
     base = getattr(workloads, name)()
     return workloads.scaled(base, particles, random_seed=seed, precision=precision)
 
@@ -310,7 +326,7 @@ def run_ours(args):
         dist.all_reduce(sm, op=dist.ReduceOp.SUM)
         ms, carrier_steps = float(mx[0]), float(sm[1])
     value = carrier_steps / (ms * 1e-3)
-    bpc = BYTES_PER_CARRIER[args.precision]
+    bpc = BYTES_PER_CARRIER[args.precision] + (MESH_MIRROR_BYTES if args.workload == "finfet_mesh" else 0)
     kavg = main_arm["kernel_ms_per_launch"]
     achieved = bpc * main_arm["carriers"] / (kavg * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
@@ -346,6 +362,9 @@ def run_ours(args):
                    "material": ("two synthetic 16^3 x 6 tables, second 0.7x frequency 0.75x velocity, Callaway BZ "
                                 "completed" if args.workload == "bilayer_callaway"
                                 else "synthetic 16^3 x 6 modes (seed 0)"), "cells": int(Tout.size),
+                   **({"mesh": "procedural FinFET, 6304 triangles, 2245 facets (seed 0)", "voxels": "64x32x32",
+                       "heat_source": "gaussian 1e20 W/m^3, sigma 5 nm, fin top, thermal spectrum"}
+                      if args.workload == "finfet_mesh" else {}),
                    "l2": "carrier state larger than L2 (no flush needed)", "replicas": world},
         "gpu_launches": main_arm["launches"],
         "roofline": {"bound": "hbm", "kernel": "k_transport + k_deferred (the one carrier pass of a step)", "achieved": achieved,
@@ -366,9 +385,10 @@ def run_ours(args):
                               "roofline_frac": 76 * plain["carriers"] / (pk * 1e-3) / 1e9 / peak,
                               "clocks": plain["clocks"]}
     if rank == 0 and not args.no_cpu_baseline:
-        cb, info = cpu_baseline(args.workload, 200000, 10, 3, 1, 1)
+        cp, cstep = (50000, 4) if args.workload == "finfet_mesh" else (200000, 10)
+        cb, info = cpu_baseline(args.workload, cp, cstep, 3, 1, 1)
         line["cpu_baseline"] = {"value": cb, "unit": UNIT, "cores": 1, "kind": "port",
-                                "sample": f"{args.workload}, 200000 carriers x 30 timed steps, serial CPU oracle"}
+                                "sample": f"{args.workload}, {cp} carriers x {3 * cstep} timed steps, serial CPU oracle"}
     if rank == 0:
         print(json.dumps(line))
 
@@ -381,14 +401,17 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="inplane_gradient",
                     choices=["inplane_gradient", "cross_plane_film", "bilayer_callaway", "heated_film",
-                             "batched_films"])
+                             "batched_films", "finfet_mesh"])
     ap.add_argument("--particles", type=float, default=None)
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.particles is None:
-        args.particles = 5e7 if args.workload == "inplane_gradient" else 1e6
+        args.particles = {"inplane_gradient": 5e7, "finfet_mesh": 2e7}.get(args.workload, 1e6)
+    if args.workload == "finfet_mesh" and args.impl == "ours":
+        # mesh domains run the plain FP64 carrier state
+        args.precision, args.no_plain = "fp64", True
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batched_films":

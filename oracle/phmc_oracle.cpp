@@ -559,8 +559,13 @@ struct OracleSolver {
     std::vector<uint32_t> mode;
     std::vector<int32_t> cell;
     std::vector<uint8_t> alive;
-    // mesh domains: facet whose specular mirror applies to the mode velocity (-1: none)
+    // mesh domains: facet whose specular mirror applies to the mode velocity (-1: none),
+    // and the persistent wall cache of src/solver/TransportOperator.cpp:186-250
+    // (time to the wall in units of dt, hit point, facet)
     std::vector<int32_t> mirror;
+    std::vector<double> hit_t;
+    std::vector<Vec3> hit_p;
+    std::vector<int32_t> hit_f;
     // grid
     std::vector<double> cell_T, cell_E;
     std::vector<Vec3> cell_q;
@@ -596,7 +601,7 @@ struct OracleSolver {
         x = c.x; y = c.y; z = c.z; occ = c.occ; mode = c.mode; cell = c.cell; alive = c.alive;
         if (domain->is_mesh()) {
             if (mats.size() != 1) throw std::runtime_error("Layered materials are built for box domains only.");
-            mirror.assign(alive.size(), -1);
+            reset_mesh_state();
         }
         prev_absorbed.resize(P.reservoirs.size());
         for (size_t r = 0; r < P.reservoirs.size(); ++r) prev_absorbed[r] = P.reservoirs[r].initial_count;
@@ -761,9 +766,70 @@ struct OracleSolver {
         occ[i] = r.occ;
     }
 
+    // Mesh domains: fresh carriers carry the mode velocity and get their wall cache
+    // (src/solver/Initialization.cpp:131).
+    void reset_mesh_state() {
+        mirror.assign(alive.size(), -1);
+        hit_t.assign(alive.size(), std::numeric_limits<double>::infinity());
+        hit_p.assign(alive.size(), Vec3{0, 0, 0});
+        hit_f.assign(alive.size(), -1);
+        for (size_t i = 0; i < alive.size(); ++i)
+            if (alive[i]) update_cache(static_cast<int>(i));
+    }
+
+    // src/solver/TransportOperator.cpp:186-250: trace from the current position
+    // (with nudged retries, which may move the carrier), time stored in units of dt.
+    void update_cache(int i) {
+        Vec3 p{x[i], y[i], z[i]}, cp;
+        double t;
+        int f;
+        const Vec3 v = velocity_of(i);
+        if (!cache(p, v, cp, t, f))
+            fail("Boundary intersection failed while updating collision cache for particle " + std::to_string(i) +
+                 ". Check that the STL is closed and manifold.");
+        x[i] = p[0]; y[i] = p[1]; z[i] = p[2];
+        hit_t[i] = t / cfg.time_step;
+        hit_p[i] = cp;
+        hit_f[i] = f;
+    }
+
+    // src/solver/TransportOperator.cpp:405-466 with the persistent wall cache (mesh domains).
+    void advance_mesh(int i, double remaining, uint32_t purpose) {
+        const double dt = cfg.time_step;
+        Vec3 v = velocity_of(i);
+        int event = 0;
+        for (; remaining > 1e-14 && event < 64; ++event) {
+            const double t_wall = hit_t[i] * dt;
+            if (!std::isfinite(t_wall) || t_wall > remaining) {
+                x[i] += v[0] * remaining; y[i] += v[1] * remaining; z[i] += v[2] * remaining;
+                if (std::isfinite(hit_t[i])) hit_t[i] -= remaining / dt;
+                return;
+            }
+            remaining -= std::max(0.0, t_wall);
+            Vec3 p = hit_p[i];
+            if (!boundary(i, hit_f[i], p, purpose, event)) {
+                x[i] = p[0]; y[i] = p[1]; z[i] = p[2];
+                return;
+            }
+            x[i] = p[0]; y[i] = p[1]; z[i] = p[2];
+            v = velocity_of(i);
+            update_cache(i);
+            if (hit_t[i] * dt < 1e-12) {
+                x[i] += v[0] * 1e-12; y[i] += v[1] * 1e-12; z[i] += v[2] * 1e-12;
+                update_cache(i);
+            }
+        }
+        if (remaining > 1e-14)
+            fail("Particle " + std::to_string(i) + " exceeded 64 transport events in one timestep");
+    }
+
     // src/solver/TransportOperator.cpp:405-466
     void advance(int i, double remaining, uint32_t purpose) {
         if (!alive[i]) return;
+        if (domain->is_mesh()) {
+            advance_mesh(i, remaining, purpose);
+            return;
+        }
         Vec3 p{x[i], y[i], z[i]};
         Vec3 cp;
         double t;
@@ -863,9 +929,14 @@ struct OracleSolver {
                     slot = static_cast<int>(alive.size());
                     x.push_back(0); y.push_back(0); z.push_back(0); occ.push_back(0); mode.push_back(0);
                     cell.push_back(0); alive.push_back(0);
-                    if (!mirror.empty() || domain->is_mesh()) mirror.push_back(-1);
+                    if (domain->is_mesh()) {
+                        mirror.push_back(-1);
+                        hit_t.push_back(0);
+                        hit_p.push_back({0, 0, 0});
+                        hit_f.push_back(-1);
+                    }
                 }
-                if (!mirror.empty()) mirror[slot] = -1;
+                if (domain->is_mesh()) mirror[slot] = -1;
                 x[slot] = pos[0]; y[slot] = pos[1]; z[slot] = pos[2];
                 occ[slot] = o;
                 mode[slot] = mode_word(static_cast<uint32_t>(m), signs, static_cast<uint32_t>(R.material));
@@ -887,6 +958,8 @@ struct OracleSolver {
         }
         std::vector<std::pair<int, double>> injected;
         inject(injected);
+        if (domain->is_mesh())
+            for (const auto& inj : injected) update_cache(inj.first); // src/MonteCarloSolver.cpp:318-327
         for (const auto& [slot, temit] : injected) {
             const double remain = cfg.time_step - temit;
             if (remain > 1e-14) advance(slot, remain, kDrawInjected);
@@ -1251,7 +1324,7 @@ int orc_solver_set_carriers(void* sp, int64_t n, const double* x, const double* 
         auto* s = static_cast<OracleSolver*>(sp);
         s->x.assign(x, x + n); s->y.assign(y, y + n); s->z.assign(z, z + n);
         s->occ.assign(occ, occ + n); s->mode.assign(mode, mode + n); s->alive.assign(alive, alive + n);
-        if (s->domain->is_mesh()) s->mirror.assign(static_cast<size_t>(n), -1);
+        if (s->domain->is_mesh()) s->reset_mesh_state();
         s->cell.resize(n);
         for (int64_t i = 0; i < n; ++i) s->cell[i] = s->domain->fast_grid_index({x[i], y[i], z[i]});
         s->refresh();

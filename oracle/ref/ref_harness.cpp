@@ -861,13 +861,14 @@ std::string cmd_run(const std::string& pmat, const std::string& toml, int steps)
                      a.collision_model == CollisionModel::Callaway);
     SimulationDomain d(a);
     MonteCarloSolver s(a, d, m);
-    std::vector<double> pc, absorbed, injected, flux, energy, resid;
+    std::vector<double> pc, absorbed, injected, flux, energy, resid, source;
     while (s.current_timestep() < steps) {
         s.run_timestep();
         pc.push_back(s.particle_count());
         absorbed.push_back(static_cast<double>(s.absorbed_particle_count()));
         injected.push_back(static_cast<double>(s.injected_particle_count()));
         flux.push_back(s.average_heat_flux_along_axis());
+        source.push_back(s.total_heat_source_energy_ev());
         energy.push_back(s.total_thermal_energy_ev());
         resid.push_back(s.total_energy_balance_residual_ev());
     }
@@ -895,12 +896,14 @@ std::string cmd_run(const std::string& pmat, const std::string& toml, int steps)
         rows << "]";
         j.raw("convergence", rows.str());
     }
+    j.arr3("grid_centers", d.grid_centers());
     j.arr("particle_count", pc);
     j.arr("absorbed_total", absorbed);
     j.arr("injected_total", injected);
     j.arr("heat_flux", flux);
     j.arr("thermal_energy", energy);
     j.arr("balance_residual_total", resid);
+    j.arr("heat_source_total", source);
     j.put("lifetime_residual_total", s.total_lifetime_energy_residual_ev());
     j.put("gradient_energy_total", s.total_gradient_energy_ev());
     return j.str();

@@ -258,6 +258,11 @@ struct CarrierState {
     int32_t* cell;
     uint8_t* alive;
     int32_t* mirror; // mesh domains: facet whose mirror applies to the mode velocity, -1 none (else null)
+    double* hit_t;   // mesh domains: wall cache, time to the wall in units of dt
+    double* hit_x;   //   cached hit point
+    double* hit_y;
+    double* hit_z;
+    int32_t* hit_f;  //   cached facet
     int4* deferred; // mixed path: queued wall events (slot, time left, event, wall), capacity entries
     int capacity;
 };

@@ -24,6 +24,7 @@ struct LaunchCtx {
 };
 
 int launch_transport(const LaunchCtx& x, bool mixed, bool rta);
+int launch_mesh_cache_init(const LaunchCtx& x);
 void launch_histogram(const LaunchCtx& x, bool rta);
 void launch_init_cells(const LaunchCtx& x, bool mixed);
 // Carriers read straight from device-accessible (registered) host arrays.

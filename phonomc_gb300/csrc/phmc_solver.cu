@@ -120,6 +120,12 @@ void DeviceSolver::allocate_state(int capacity) {
     if (domain_->is_mesh()) {
         state_.mirror = dalloc<int32_t>(capacity);
         PHMC_CUDA(cudaMemsetAsync(state_.mirror, 0xFF, static_cast<size_t>(capacity) * sizeof(int32_t), stream_));
+        state_.hit_t = dalloc<double>(capacity);
+        state_.hit_x = dalloc<double>(capacity);
+        state_.hit_y = dalloc<double>(capacity);
+        state_.hit_z = dalloc<double>(capacity);
+        state_.hit_f = dalloc<int32_t>(capacity);
+        state_.deferred = dalloc<int4>(capacity); // wall-event queue of the mesh transport
     }
     state_.occ = dalloc<double>(capacity);
     state_.mode = dalloc<uint32_t>(capacity);
@@ -588,7 +594,7 @@ void DeviceSolver::set_carriers(long long n, const double* x, const double* y, c
         else PHMC_CUDA(cudaMemsetAsync(state_.alive, 1, n * sizeof(uint8_t), stream_));
         launch_init_cells(c, mixed_);
     }
-    counters_.launches += 1;
+    counters_.launches += 1 + launch_mesh_cache_init(c);
     initial_statistics();
     if (!keep_clock) synchronize();
 }

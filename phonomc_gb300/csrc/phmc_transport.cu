@@ -216,38 +216,85 @@ __device__ bool advance_carrier(const DevTables& T, DevLedger* L, BlockLedger* b
     return true;
 }
 
-// One carrier's flight in a mesh domain (single material): the wall cache on
-// the face BVH with nudged retries, per-facet conditions, rough reflections
-// whose outward mode velocity is mirrored in the facet plane (`mir`), and the
-// push along the velocity actually carried (src/solver/TransportOperator.cpp:287-361, 405-466).
-__device__ bool advance_carrier_mesh(const DevTables& T, DevLedger* L, BlockLedger* bl, int slot, double p[3],
-                                     uint32_t& w, int& mir, double& occ, double remaining, uint32_t purpose,
-                                     uint32_t step) {
+// Persistent wall cache of a mesh carrier (src/solver/TransportOperator.cpp:186-250):
+// time to the wall in units of dt, hit point and facet. The point and facet
+// are read from HBM only when the carrier reaches its wall.
+struct MeshCache {
+    double t, x, y, z;
+    int f;
+    bool loaded, dirty;
+};
+
+__device__ __forceinline__ void mesh_cache_load(const CarrierState& S, int slot, MeshCache& c) {
+    if (c.loaded) return;
+    c.x = S.hit_x[slot];
+    c.y = S.hit_y[slot];
+    c.z = S.hit_z[slot];
+    c.f = S.hit_f[slot];
+    c.loaded = true;
+}
+
+__device__ __forceinline__ void mesh_cache_store(const CarrierState& S, int slot, const MeshCache& c) {
+    S.hit_t[slot] = c.t;
+    if (c.dirty) {
+        S.hit_x[slot] = c.x;
+        S.hit_y[slot] = c.y;
+        S.hit_z[slot] = c.z;
+        S.hit_f[slot] = c.f;
+    }
+}
+
+// Trace from p (nudged retries may move it) into the cache; false after raising an error.
+__device__ __forceinline__ bool mesh_refresh(const DevTables& T, DevLedger* L, int slot, double p[3], const double v[3],
+                                             MeshCache& c) {
+    double cp[3], t;
+    int f;
+    const int r = mesh_cache_hit(T.fac, T.dom, T.par, p, v, cp, t, f);
+    c.loaded = c.dirty = true;
+    if (r != 0) {
+        raise_error(L, r == 2 ? kErrInvalidStatistics : kErrIntersection, slot);
+        c.t = __longlong_as_double(0x7ff0000000000000LL);
+        c.f = -1;
+        return false;
+    }
+    c.t = t / T.par.dt;
+    c.x = cp[0];
+    c.y = cp[1];
+    c.z = cp[2];
+    c.f = f;
+    return true;
+}
+
+// One carrier's flight in a mesh domain (single material), reference event loop
+// on the persistent wall cache: per-facet conditions, rough reflections whose
+// outward mode velocity is mirrored in the facet plane (`mir`), the push along
+// the velocity actually carried, then a fresh cache
+// (src/solver/TransportOperator.cpp:287-361, 405-466).
+__device__ bool advance_carrier_mesh(const DevTables& T, DevLedger* L, BlockLedger* bl, const CarrierState& S,
+                                     int slot, double p[3], uint32_t& w, int& mir, double& occ, MeshCache& c,
+                                     double remaining, uint32_t purpose, uint32_t step) {
     const DevFacets& F = T.fac;
-    const DevDomain& D = T.dom;
     const DevParams& P = T.par;
+    const double dt = P.dt;
     const int mid = static_cast<int>(w >> 28);
     const DevMaterial& M = T.mat[mid];
     double v[3];
     mesh_velocity(F, M, w, mir, v);
-    double cp[3], t;
-    int f;
-    auto cache = [&]() {
-        const int r = mesh_cache_hit(F, D, P, p, v, cp, t, f);
-        if (r != 0) raise_error(L, r == 2 ? kErrInvalidStatistics : kErrIntersection, slot);
-        return r == 0;
-    };
-    if (!cache()) return true;
     int event = 0;
     for (; remaining > 1e-14 && event < 64; ++event) {
-        if (!isfinite(t) || t > remaining) {
+        const double t_wall = dmul(c.t, dt);
+        if (!isfinite(t_wall) || t_wall > remaining) {
 #pragma unroll
             for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], remaining));
+            if (isfinite(c.t)) c.t = dadd(c.t, -(remaining / dt));
             return true;
         }
-        remaining -= fmax(0.0, t);
-#pragma unroll
-        for (int a = 0; a < 3; ++a) p[a] = cp[a];
+        remaining -= fmax(0.0, t_wall);
+        mesh_cache_load(S, slot, c);
+        p[0] = c.x;
+        p[1] = c.y;
+        p[2] = c.z;
+        const int f = c.f;
         const int ai = static_cast<int>(w & 0x00FFFFFFu);
         const char cond = F.cond[f];
         if (cond == 'T') {
@@ -291,15 +338,33 @@ __device__ bool advance_carrier_mesh(const DevTables& T, DevLedger* L, BlockLedg
         const double s = P.push_eps / fmax(meshmath::norm(v), 1e-12);
 #pragma unroll
         for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], s));
-        if (!cache()) return true;
-        if (t < 1e-12) {
+        if (!mesh_refresh(T, L, slot, p, v, c)) return true;
+        if (dmul(c.t, dt) < 1e-12) {
 #pragma unroll
             for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], 1e-12));
-            if (!cache()) return true;
+            if (!mesh_refresh(T, L, slot, p, v, c)) return true;
         }
     }
     if (remaining > 1e-14) raise_error(L, kErrTooManyEvents, slot);
     return true;
+}
+
+// Wall caches of every live carrier after an upload (src/solver/Initialization.cpp:131).
+__global__ void k_mesh_cache_init(const __grid_constant__ DevTables T, CarrierState S, DevLedger* L) {
+    const int n = L->n_slots;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (!S.alive[i]) continue;
+        const uint32_t w = S.mode[i];
+        double v[3];
+        mesh_velocity(T.fac, T.mat[w >> 28], w, S.mirror[i], v);
+        double p[3] = {S.x[i], S.y[i], S.z[i]};
+        MeshCache c;
+        mesh_refresh(T, L, i, p, v, c);
+        S.x[i] = p[0];
+        S.y[i] = p[1];
+        S.z[i] = p[2];
+        mesh_cache_store(S, i, c);
+    }
 }
 
 // ------------------------------------------------------------------ bins
@@ -622,7 +687,7 @@ constexpr int kDeferBuffer = 64; // queued wall events per warp before a flush
 // bin. Mixed path: carriers that reach a wall needing table sampling are
 // queued (per-warp shared buffers, one global atomic per 32 entries) and
 // finished by k_deferred.
-template <bool kMixed, bool kRta, bool kMesh = false>
+template <bool kMixed, bool kRta>
 __global__ void __launch_bounds__(kTransportThreads) k_transport(const __grid_constant__ DevTables T, CarrierState S,
                                                                  CellArrays C, DevLedger* L) {
     const uint32_t step = L->step_index; // timesteps completed: the draw counter of this step
@@ -700,17 +765,8 @@ __global__ void __launch_bounds__(kTransportThreads) k_transport(const __grid_co
             const int c0 = __ldcs(S.cell + i);
             double occ = apply_pending(T, C, c0, w, __ldcs(S.occ + i));
             double p[3] = {__ldcs(S.x + i), __ldcs(S.y + i), __ldcs(S.z + i)};
-            bool alive;
-            int c;
-            if constexpr (kMesh) {
-                int mir = S.mirror[i];
-                alive = advance_carrier_mesh(T, L, &bl, i, p, w, mir, occ, T.par.dt, kDrawTransport, step);
-                S.mirror[i] = mir;
-                c = cell_at(T, p[0], p[1], p[2]);
-            } else {
-                alive = advance_carrier(T, L, &bl, i, p, w, occ, T.par.dt, kDrawTransport, step);
-                c = grid_index(T.dom, p[0], p[1], p[2]);
-            }
+            const bool alive = advance_carrier(T, L, &bl, i, p, w, occ, T.par.dt, kDrawTransport, step);
+            const int c = grid_index(T.dom, p[0], p[1], p[2]);
             __stcs(S.x + i, p[0]);
             __stcs(S.y + i, p[1]);
             __stcs(S.z + i, p[2]);
@@ -723,6 +779,102 @@ __global__ void __launch_bounds__(kTransportThreads) k_transport(const __grid_co
             __stcs(S.cell + i, c);
             bin_carrier(T, C, L, i, c, w, occ, kRta);
         }
+    }
+    __syncthreads();
+    block_ledger_flush(&bl, L);
+}
+
+// Mesh transport, pass 1 of 2: apply the pending update and drift every
+// carrier that does not reach its cached wall within the step (the cache time
+// drops by one step); carriers that do are queued, with their updated
+// occupation, for k_mesh_events. Warps thus run the FP64 BVH work only on
+// compacted event carriers.
+template <bool kRta>
+__global__ void __launch_bounds__(kTransportThreads) k_transport_mesh(const __grid_constant__ DevTables T, CarrierState S,
+                                                                      CellArrays C, DevLedger* L) {
+    const int n = L->n_slots;
+    const double dt = T.par.dt;
+    const int lane = threadIdx.x & 31;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        bool defer = false;
+        if (i < n && __ldcs(S.alive + i)) {
+            const uint32_t w = __ldcs(S.mode + i);
+            const int c0 = __ldcs(S.cell + i);
+            const double occ = apply_pending(T, C, c0, w, __ldcs(S.occ + i));
+            const double ht = __ldcs(S.hit_t + i);
+            const double t_wall = dmul(ht, dt);
+            if (!isfinite(t_wall) || t_wall > dt) {
+                double v[3];
+                mesh_velocity(T.fac, T.mat[w >> 28], w, __ldcs(S.mirror + i), v);
+                const double p[3] = {dadd(__ldcs(S.x + i), dmul(v[0], dt)), dadd(__ldcs(S.y + i), dmul(v[1], dt)),
+                                     dadd(__ldcs(S.z + i), dmul(v[2], dt))};
+                if (isfinite(ht)) __stcs(S.hit_t + i, dadd(ht, -(dt / dt)));
+                const int c = cell_at(T, p[0], p[1], p[2]);
+                __stcs(S.x + i, p[0]);
+                __stcs(S.y + i, p[1]);
+                __stcs(S.z + i, p[2]);
+                __stcs(S.occ + i, occ);
+                __stcs(S.cell + i, c);
+                bin_carrier(T, C, L, i, c, w, occ, kRta);
+            } else {
+                __stcs(S.occ + i, occ);
+                defer = true;
+            }
+        }
+        const unsigned mask = __ballot_sync(0xffffffffu, defer);
+        if (mask) {
+            int at = 0;
+            if (lane == 0) at = atomicAdd(&L->n_deferred, __popc(mask));
+            at = __shfl_sync(0xffffffffu, at, 0);
+            if (defer) {
+                const int q = at + __popc(mask & ((1u << lane) - 1u));
+                if (q < S.capacity) S.deferred[q] = make_int4(i, 0, 0, 0);
+                else raise_error(L, kErrInvalidStatistics, i);
+            }
+        }
+    }
+}
+
+// Mesh transport, pass 2 of 2: the full flight of every queued carrier from
+// the start of the step (occupation already updated), then its cell and bin.
+template <bool kRta>
+__global__ void __launch_bounds__(kTransportThreads) k_mesh_events(const __grid_constant__ DevTables T, CarrierState S,
+                                                                   CellArrays C, DevLedger* L) {
+    const uint32_t step = L->step_index;
+    __shared__ BlockLedger bl;
+    block_ledger_init(&bl);
+    __syncthreads();
+    const int nq = min(L->n_deferred, S.capacity);
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+        const int i = S.deferred[q].x;
+        if (i < 0 || i >= S.capacity) {
+            raise_error(L, kErrInvalidStatistics, i);
+            continue;
+        }
+        uint32_t w = S.mode[i];
+        double occ = S.occ[i];
+        double p[3] = {S.x[i], S.y[i], S.z[i]};
+        const int mir0 = S.mirror[i];
+        int mir = mir0;
+        MeshCache mc;
+        mc.t = S.hit_t[i];
+        mc.loaded = mc.dirty = false;
+        const bool alive = advance_carrier_mesh(T, L, &bl, S, i, p, w, mir, occ, mc, T.par.dt, kDrawTransport, step);
+        if (mir != mir0) S.mirror[i] = mir;
+        mesh_cache_store(S, i, mc);
+        S.x[i] = p[0];
+        S.y[i] = p[1];
+        S.z[i] = p[2];
+        S.mode[i] = w;
+        S.occ[i] = occ;
+        if (!alive) {
+            S.alive[i] = 0;
+            continue;
+        }
+        const int c = cell_at(T, p[0], p[1], p[2]);
+        S.cell[i] = c;
+        bin_carrier(T, C, L, i, c, w, occ, kRta);
     }
     __syncthreads();
     block_ledger_flush(&bl, L);
@@ -1043,8 +1195,12 @@ __global__ void __launch_bounds__(256) k_inject(const DevTables* __restrict__ Tp
             S.oz[slot] = q[2];
         } else if (kMesh) {
             int mir = -1;
-            if (remain > 1e-14) alive = advance_carrier_mesh(T, L, &bl, slot, p, w, mir, occ, remain, kDrawInjected, step);
+            MeshCache mc;
+            mesh_refresh(T, L, slot, p, v, mc); // src/MonteCarloSolver.cpp:318-327
+            if (remain > 1e-14)
+                alive = advance_carrier_mesh(T, L, &bl, S, slot, p, w, mir, occ, mc, remain, kDrawInjected, step);
             S.mirror[slot] = mir;
+            mesh_cache_store(S, slot, mc);
             c = cell_at(T, p[0], p[1], p[2]);
             S.x[slot] = p[0];
             S.y[slot] = p[1];
@@ -1184,9 +1340,14 @@ int launch_transport(const LaunchCtx& x, bool mixed, bool rta) {
         return 2;
     }
     if (x.mesh) {
-        if (rta) k_transport<false, true, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
-        else k_transport<false, false, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
-        return 1;
+        if (rta) {
+            k_transport_mesh<true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+            k_mesh_events<true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+        } else {
+            k_transport_mesh<false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+            k_mesh_events<false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+        }
+        return 2;
     }
     if (rta) k_transport<false, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
     else k_transport<false, false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
@@ -1209,6 +1370,12 @@ void launch_ingest(const LaunchCtx& x, bool mixed, const HostCarriers& h) {
 }
 
 void launch_ledger_replace(const LaunchCtx& x, int n) { k_ledger_replace<<<1, 1, 0, x.stream>>>(x.L, n); }
+
+int launch_mesh_cache_init(const LaunchCtx& x) {
+    if (!x.mesh) return 0;
+    k_mesh_cache_init<<<x.grid_blocks, 128, 0, x.stream>>>(*x.Th, x.S, x.L);
+    return 1;
+}
 
 void launch_positions_out(const LaunchCtx& x) {
     k_positions_out<<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.L);

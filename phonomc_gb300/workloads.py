@@ -182,3 +182,23 @@ def finfet_mesh(stl_path: str, particles: float = 2e7, seed: int = 12345, precis
     if heat_source:
         c["heat_source"] = dict(FINFET_SOURCE)
     return c
+
+
+def finfet_regions(centers):
+    """Cell masks of the FinFET: the fin above the 50 nm slab, the upper and the
+    lower half of the slab (cell centres in Angstrom)."""
+    import numpy as np
+    z = np.asarray(centers)[:, 2]
+    return {"fin": z > 500.0, "top": (z > 250.0) & (z <= 500.0), "bottom": z <= 250.0}
+
+
+def finfet_aggregates(T_steps, energy, absorbed_total, centers, first_step):
+    """Late-time means from step `first_step` on: region temperatures, thermal
+    energy, and absorbed carriers per step (inputs indexed by step - 1)."""
+    import numpy as np
+    T = np.asarray(T_steps)[first_step - 1:]
+    out = {k: float(T[:, m].mean()) for k, m in finfet_regions(centers).items()}
+    out["energy"] = float(np.mean(np.asarray(energy)[first_step - 1:]))
+    a = np.asarray(absorbed_total, dtype=float)
+    out["absorbed_per_step"] = float((a[-1] - a[first_step - 2]) / (len(a) - first_step + 1))
+    return out

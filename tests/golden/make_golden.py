@@ -24,7 +24,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from phonomc_gb300 import synthetic  # noqa: E402
+from phonomc_gb300 import synthetic, workloads  # noqa: E402
 
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
 
@@ -168,6 +168,44 @@ def full_runs(mpath: str, tmp: str) -> dict:
     return out
 
 
+# Full reference runs of the FinFET mesh domain with its heat source (8^3
+# table, 2e4 carriers, 32 x 8 x 16 voxels, 200 steps of 0.1 ps): per seed, the
+# late-time means (steps 101-200) of the region temperatures (fin above the
+# 50 nm slab, upper and lower slab halves), the thermal energy and the
+# absorbed carriers per step, and the heat-source energy at the end.
+FINFET_SEEDS = 16
+FINFET_PARTICLES = 20000
+FINFET_STEPS = 200
+FINFET_GRID = (32, 8, 16)
+
+
+def full_runs_finfet(mpath: str, fpath: str, tmp: str) -> dict:
+    import numpy as np
+    out = {"seeds": [], "particles": FINFET_PARTICLES, "steps": FINFET_STEPS, "grid": list(FINFET_GRID),
+           "average_from_step": FINFET_STEPS // 2 + 1}
+    for k in range(FINFET_SEEDS):
+        seed = 101 + k
+        folder = os.path.join(tmp, f"ff{seed}")
+        os.makedirs(folder, exist_ok=True)
+        toml = os.path.join(folder, "c3.toml")
+        with open(toml, "w") as f:
+            f.write(FINFET_TOML.format(stl=fpath, particles=FINFET_PARTICLES, steps=FINFET_STEPS, seed=seed,
+                                       nx=FINFET_GRID[0], ny=FINFET_GRID[1], nz=FINFET_GRID[2],
+                                       source=FINFET_SOURCE_TOML, out=folder))
+        res = json.loads(subprocess.run([HARNESS, "run", mpath, toml, str(FINFET_STEPS)], check=True,
+                                        capture_output=True, text=True).stdout)
+        rows = np.asarray(res["convergence"])
+        nc = len(res["grid_centers"])
+        agg = workloads.finfet_aggregates(rows[:, 2:2 + nc], res["thermal_energy"], res["absorbed_total"],
+                                res["grid_centers"], out["average_from_step"])
+        out["seeds"].append(seed)
+        for key, v in agg.items():
+            out.setdefault(key, []).append(v)
+        out.setdefault("source_total_end", []).append(res["heat_source_total"][-1])
+        out.setdefault("balance_residual_total", []).append(res["balance_residual_total"][-1])
+    return out
+
+
 def build(ref: str) -> None:
     subprocess.run(["make", "-s", "-j8", f"REF={ref}"], cwd=os.path.join(ROOT, "oracle", "ref"),
                    check=True)
@@ -200,6 +238,12 @@ def main() -> None:
         with gzip.open(os.path.join(HERE, "fullrun_cross_plane.json.gz"), "wt") as f:
             json.dump(data, f)
         print("fullrun_cross_plane ok")
+    if not args.only or "fullrun_finfet" in args.only:
+        data = full_runs_finfet(mpath, fpath, os.path.join(tmp, "fullrun_finfet"))
+        data["_harness_args"] = ["run", "{m}", "<FinFET toml>", str(FINFET_STEPS)]
+        with gzip.open(os.path.join(HERE, "fullrun_finfet.json.gz"), "wt") as f:
+            json.dump(data, f)
+        print("fullrun_finfet ok")
     for name, argv in CASES.items():
         if args.only and name not in args.only:
             continue

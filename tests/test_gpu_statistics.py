@@ -1,0 +1,98 @@
+"""Device runs against full reference runs over 16 independent seeds.
+
+The reference solver (oracle/_ref, its own C++) ran each configuration for 16
+seeds (tests/golden/fullrun_*.json.gz, made by tests/golden/make_golden.py).
+The device runs the same configuration for 16 other seeds through the C ABI;
+the late-time observables must agree within the combined standard error of the
+two 16-seed means: |z| < 3.5 for the scalar observables, and for the 50 cell
+temperatures of the film |z| < 4.5 with mean z^2 below 2.5. Energy bookkeeping
+closes to round-off on the device.
+"""
+
+import numpy as np
+import pytest
+
+from conftest import golden
+from phonomc_gb300 import abi, synthetic, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _z(a, b):
+    a, b = np.asarray(a, dtype=float), np.asarray(b, dtype=float)
+    se = np.sqrt(a.var(axis=0, ddof=1) / a.shape[0] + b.var(axis=0, ddof=1) / b.shape[0])
+    return (a.mean(axis=0) - b.mean(axis=0)) / se
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    import phonomc_gb300
+    return phonomc_gb300.lib()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cross_plane_film_statistics(gpu, precision):
+    g = golden("fullrun_cross_plane")
+    m = abi.Material(gpu, "phmc_", synthetic.make_material(mesh=16), 0.1, False, False)
+    T_mean, flux, kappa, resid = [], [], [], []
+    for k in range(len(g["seeds"])):
+        cfg = workloads.scaled(workloads.cross_plane_film(precision=precision), g["particles"],
+                               random_seed=9001 + k, convergence_write_interval=1)
+        s = abi.Solver(gpu, "phmc_", cfg, [m])
+        T_acc, f_acc, k_acc = [], [], []
+        for step in range(1, g["steps"] + 1):
+            s.run(1)
+            if step >= g["average_from_step"]:
+                st = s.stats()
+                T_acc.append(s.cells()[0])
+                f_acc.append(st["average_heat_flux_along_axis"])
+                k_acc.append(st["kappa_endpoints"])
+        st = s.stats()
+        T_mean.append(np.mean(T_acc, axis=0))
+        flux.append(np.mean(f_acc))
+        kappa.append(np.mean(k_acc))
+        resid.append(abs(st["total_energy_balance_residual_ev"]))
+        s.close()
+    z = _z(T_mean, g["T_mean"])
+    assert np.all(np.abs(z) < 4.5), z
+    assert np.mean(z * z) < 2.5, np.mean(z * z)
+    assert abs(_z(np.asarray(flux)[:, None], np.asarray(g["flux_mean"])[:, None])[0]) < 3.5
+    assert abs(_z(np.asarray(kappa)[:, None], np.asarray(g["kappa_eff_mean"])[:, None])[0]) < 3.5
+    assert max(resid) < 1e-6
+
+
+def test_finfet_statistics(gpu, tmp_path):
+    """FinFET mesh with the fin-top heat source: region temperatures, thermal
+    energy, absorbed carriers per step and deposited source energy."""
+    g = golden("fullrun_finfet")
+    stl = workloads.finfet_stl(str(tmp_path / "finfet.stl"))
+    m = abi.Material(gpu, "phmc_", synthetic.make_material(mesh=8), 0.1, False, False)
+    runs = {}
+    for k in range(len(g["seeds"])):
+        cfg = workloads.finfet_mesh(stl, particles=g["particles"], seed=7001 + k, grid=tuple(g["grid"]))
+        s = abi.Solver(gpu, "phmc_", cfg, [m])
+        dom = abi.Domain(gpu, cfg)
+        centers = dom.cells()["centers"]
+        dom.close()
+        T, energy, absorbed = [], [], []
+        for _ in range(g["steps"]):
+            s.run(1)
+            st = s.stats()
+            T.append(s.cells()[0])
+            energy.append(st["total_thermal_energy_ev"])
+            absorbed.append(st["absorbed_total"])
+        st = s.stats()
+        res = workloads.finfet_aggregates(T, energy, absorbed, centers, g["average_from_step"])
+        # deposited + still pending = prescribed (a source cell without carriers keeps its budget)
+        res["source_total_end"] = st["total_heat_source_energy_ev"] + st["pending_heat_source_energy_ev"]
+        res["balance_residual_total"] = abs(st["total_energy_balance_residual_ev"])
+        for key, v in res.items():
+            runs.setdefault(key, []).append(v)
+        s.close()
+    for key in ("fin", "top", "bottom", "energy", "absorbed_per_step"):
+        z = _z(np.asarray(runs[key])[:, None], np.asarray(g[key])[:, None])[0]
+        assert abs(z) < 3.5, (key, z, np.mean(runs[key]), np.mean(g[key]))
+    # the prescribed source energy is the same; the reference runs deposited all of it
+    assert np.allclose(runs["source_total_end"], g["source_total_end"], rtol=1e-9), (
+        runs["source_total_end"], g["source_total_end"])
+    assert max(runs["balance_residual_total"]) < 1e-6
