@@ -536,35 +536,9 @@ int phmc_dev_trace_mesh(int nv, const double* vertices, int nf, const int32_t* f
         std::vector<std::array<int, 3>> F(nf);
         for (int i = 0; i < nf; ++i) F[i] = {faces[3 * i], faces[3 * i + 1], faces[3 * i + 2]};
         T.build(std::move(V), std::move(F), std::vector<int>(face_to_facet, face_to_facet + nf));
-        std::vector<double> vv, nrm, bnd, nb;
-        std::vector<int> ff, links;
-        for (const auto& v : T.vertices) vv.insert(vv.end(), v.begin(), v.end());
-        for (const auto& f : T.faces) ff.insert(ff.end(), f.begin(), f.end());
-        for (const auto& x : T.normals) nrm.insert(nrm.end(), x.begin(), x.end());
-        for (const auto& b : T.bounds) {
-            bnd.insert(bnd.end(), b[0].begin(), b[0].end());
-            bnd.insert(bnd.end(), b[1].begin(), b[1].end());
-        }
-        for (const auto& nd : T.nodes) {
-            nb.insert(nb.end(), nd.bmin.begin(), nd.bmin.end());
-            nb.insert(nb.end(), nd.bmax.begin(), nd.bmax.end());
-            links.insert(links.end(), {nd.left, nd.right, nd.begin, nd.end});
-        }
-        DBuf<double> dv(vv), dn(nrm), dk(T.k), db(bnd), dnb(nb.empty() ? std::vector<double>(6, 0.0) : nb);
-        DBuf<int> dfa(ff), df2f(T.face_to_facet), dl(links.empty() ? std::vector<int>(4, -1) : links),
-            dord(T.order.empty() ? std::vector<int>(1, 0) : T.order);
+        DevHold hold;
         DevMesh M;
-        M.vertices = dv.p;
-        M.faces = dfa.p;
-        M.face_to_facet = df2f.p;
-        M.normals = dn.p;
-        M.k = dk.p;
-        M.bounds = db.p;
-        M.node_bounds = dnb.p;
-        M.node_links = dl.p;
-        M.order = dord.p;
-        M.root = T.root;
-        M.nfaces = nf;
+        fill_dev_mesh(T, M, [&](const auto& v) { return hold.put(v); });
         DBuf<double> dp(p3, 3 * n), dvv(v3, 3 * n), dh(3 * n), dt(n);
         DBuf<int32_t> dfc(n);
         k_trace_mesh_rays<<<256, 128>>>(M, n, dp.p, dvv.p, dh.p, dt.p, dfc.p);

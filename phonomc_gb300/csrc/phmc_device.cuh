@@ -205,20 +205,26 @@ struct DevInterface {
     DevInterfaceBank bank[kMaxMaterials][2];
 };
 
-struct DevMesh {
-    const double* vertices;    // [nv][3]
-    const int* faces;          // [nf][3]
-    const int* face_to_facet;  // [nf]
-    const double* normals;     // [nf][3]
-    const double* k;           // [nf]
-    const double* bounds;      // [nf][6] min xyz, max xyz
-    const double* node_bounds; // [nodes][6]
-    const int* node_links;     // [nodes][4] left, right, begin, end
-    const int* order;          // BVH leaf order of the faces
-    int root;                  // -1: scan all faces
-    int nfaces;
+// Face BVH node: bounds, children (-1 for a leaf) and the record range of a leaf.
+struct __align__(16) DevBvhNode {
+    double bmin[3], bmax[3];
+    int left, right, begin, end;
 };
 
+// Device layout of the face BVH: nodes in breadth-first order (root at 0),
+// and one contiguous record per face in leaf order (the order the traversal
+// tests them), so a leaf is a run of records with no index indirection:
+// normal xyz, plane offset k, bounds min xyz / max xyz, vertices a, b, c.
+constexpr int kFaceRecord = 19;
+struct DevMesh {
+    const DevBvhNode* nodes;
+    const double* face;        // [nfaces][kFaceRecord]
+    const int* face_facet;     // facet of each record
+    const int* face_id;        // input face index of each record
+    int root;                  // -1: no BVH, records in input order and scanned in full
+    int nfaces;
+    int nnodes;
+};
 // Boundary data of a mesh domain, per facet (facet count n = 0: analytic box).
 struct DevFacets {
     int n;
@@ -684,17 +690,29 @@ __device__ __forceinline__ void closest(const double p[3], const double a[3], co
     axpy(a, ab, __dmul_rn(vb, denom), t);
     axpy(t, ac, __dmul_rn(vc, denom), o);
 }
-// src/SurfaceMesh.cpp:188-223
-__device__ __forceinline__ bool ray_box(const double o[3], const double d[3], const double* bb, double t_limit,
-                                        double& t_near_out) {
+// src/SurfaceMesh.cpp:188-223. The per-axis reciprocal 1/d of the reference is
+// the same for every box of one ray, so it is computed once (RayInv).
+struct RayInv {
+    double inv[3];
+    bool flat[3]; // |d| <= 1e-14: the slab test on the origin instead
+};
+__device__ __forceinline__ RayInv ray_inv(const double d[3]) {
+    RayInv r;
+    for (int a = 0; a < 3; ++a) {
+        r.flat[a] = fabs(d[a]) <= 1e-14;
+        r.inv[a] = r.flat[a] ? 0.0 : 1.0 / d[a];
+    }
+    return r;
+}
+__device__ __forceinline__ bool ray_box(const double o[3], const RayInv& R, const double bmin[3], const double bmax[3],
+                                        double t_limit, double& t_near_out) {
     double t_near = 0.0, t_far = t_limit;
     for (int a = 0; a < 3; ++a) {
-        if (fabs(d[a]) <= 1e-14) {
-            if (o[a] < bb[a] - 1e-12 || o[a] > bb[3 + a] + 1e-12) return false;
+        if (R.flat[a]) {
+            if (o[a] < bmin[a] - 1e-12 || o[a] > bmax[a] + 1e-12) return false;
             continue;
         }
-        const double inv = 1.0 / d[a];
-        double t0 = __dmul_rn(__dadd_rn(bb[a], -o[a]), inv), t1 = __dmul_rn(__dadd_rn(bb[3 + a], -o[a]), inv);
+        double t0 = __dmul_rn(__dadd_rn(bmin[a], -o[a]), R.inv[a]), t1 = __dmul_rn(__dadd_rn(bmax[a], -o[a]), R.inv[a]);
         if (t0 > t1) {
             const double s = t0;
             t0 = t1;
@@ -719,23 +737,18 @@ __device__ inline void mesh_trace_dev(const DevMesh& M, const double x[3], const
     int best = -1;
     double best_p[3] = {0.0, 0.0, 0.0};
     auto try_face = [&](int i) {
-        const double* n = M.normals + 3 * i;
-        const double nn[3] = {n[0], n[1], n[2]};
+        const double* r = M.face + kFaceRecord * i;
+        const double nn[3] = {r[0], r[1], r[2]};
         const double denom = dot(v, nn);
         if (fabs(denom) < 1e-10) return;
-        const double t = -__dadd_rn(dot(x, nn), M.k[i]) / denom;
+        const double t = -__dadd_rn(dot(x, nn), r[3]) / denom;
         if (t <= 1e-10 || t >= best_t) return;
         double p[3];
         axpy(x, v, t, p);
-        const double* bb = M.bounds + 6 * i;
-        if (p[0] < bb[0] - 1e-9 || p[1] < bb[1] - 1e-9 || p[2] < bb[2] - 1e-9 || p[0] > bb[3] + 1e-9 ||
-            p[1] > bb[4] + 1e-9 || p[2] > bb[5] + 1e-9)
+        if (p[0] < r[4] - 1e-9 || p[1] < r[5] - 1e-9 || p[2] < r[6] - 1e-9 || p[0] > r[7] + 1e-9 ||
+            p[1] > r[8] + 1e-9 || p[2] > r[9] + 1e-9)
             return;
-        const int* f = M.faces + 3 * i;
-        const double* va = M.vertices + 3 * f[0];
-        const double* vb = M.vertices + 3 * f[1];
-        const double* vc = M.vertices + 3 * f[2];
-        const double A[3] = {va[0], va[1], va[2]}, B[3] = {vb[0], vb[1], vb[2]}, Cc[3] = {vc[0], vc[1], vc[2]};
+        const double A[3] = {r[10], r[11], r[12]}, B[3] = {r[13], r[14], r[15]}, Cc[3] = {r[16], r[17], r[18]};
         double cp[3], d[3];
         closest(p, A, B, Cc, cp);
         sub(cp, p, d);
@@ -745,25 +758,26 @@ __device__ inline void mesh_trace_dev(const DevMesh& M, const double x[3], const
         for (int a = 0; a < 3; ++a) best_p[a] = p[a];
     };
     if (M.root >= 0) {
+        const RayInv R = ray_inv(v);
         int stack[64];
         int top = 0;
         stack[top++] = M.root;
         while (top > 0) {
-            const int node = stack[--top];
+            const DevBvhNode& nd = M.nodes[stack[--top]];
             double tn = 0.0;
-            if (!ray_box(x, v, M.node_bounds + 6 * node, best_t, tn)) continue;
-            const int* L = M.node_links + 4 * node;
-            if (L[0] < 0 && L[1] < 0) {
-                for (int pos = L[2]; pos < L[3]; ++pos) try_face(M.order[pos]);
+            if (!ray_box(x, R, nd.bmin, nd.bmax, best_t, tn)) continue;
+            if (nd.left < 0 && nd.right < 0) {
+                for (int pos = nd.begin; pos < nd.end; ++pos) try_face(pos);
                 continue;
             }
             int near_child = -1, far_child = -1;
             double near_t = __longlong_as_double(0x7ff0000000000000LL), far_t = near_t;
+            const int kids[2] = {nd.left, nd.right};
             for (int s = 0; s < 2; ++s) {
-                const int child = L[s];
+                const int child = kids[s];
                 if (child < 0) continue;
                 double tc = 0.0;
-                if (!ray_box(x, v, M.node_bounds + 6 * child, best_t, tc)) continue;
+                if (!ray_box(x, R, M.nodes[child].bmin, M.nodes[child].bmax, best_t, tc)) continue;
                 if (tc < near_t) {
                     far_child = near_child;
                     far_t = near_t;
@@ -788,7 +802,7 @@ __device__ inline void mesh_trace_dev(const DevMesh& M, const double x[3], const
     }
     for (int a = 0; a < 3; ++a) hit[a] = best_p[a];
     t_out = best_t;
-    facet = M.face_to_facet[best];
+    facet = M.face_facet[best];
 }
 
 // ------------------------------------------------------------ mesh domains
@@ -821,12 +835,13 @@ __device__ __forceinline__ bool ray_triangle(const double o[3], const double d[3
 }
 } // namespace meshmath
 
+// Vertices of face record i.
 __device__ __forceinline__ void mesh_face(const DevMesh& M, int i, double a[3], double b[3], double c[3]) {
-    const int* f = M.faces + 3 * i;
+    const double* r = M.face + kFaceRecord * i;
     for (int k = 0; k < 3; ++k) {
-        a[k] = M.vertices[3 * f[0] + k];
-        b[k] = M.vertices[3 * f[1] + k];
-        c[k] = M.vertices[3 * f[2] + k];
+        a[k] = r[10 + k];
+        b[k] = r[13 + k];
+        c[k] = r[16 + k];
     }
 }
 
@@ -855,22 +870,20 @@ __device__ inline int mesh_ray_cast_inside(const DevFacets& F, const double p[3]
         stack[top++] = M.root;
         const double pad = F.ray_pad;
         while (top > 0) {
-            const int node = stack[--top];
-            const double* bb = M.node_bounds + 6 * node;
-            if (p[1] < bb[1] - pad || p[1] > bb[4] + pad || p[2] < bb[2] - pad || p[2] > bb[5] + pad ||
-                p[0] > bb[3] + pad)
+            const DevBvhNode& nd = M.nodes[stack[--top]];
+            if (p[1] < nd.bmin[1] - pad || p[1] > nd.bmax[1] + pad || p[2] < nd.bmin[2] - pad ||
+                p[2] > nd.bmax[2] + pad || p[0] > nd.bmax[0] + pad)
                 continue;
-            const int* Lk = M.node_links + 4 * node;
-            if (Lk[0] < 0 && Lk[1] < 0) {
-                for (int pos = Lk[2]; pos < Lk[3]; ++pos) test_face(M.order[pos]);
+            if (nd.left < 0 && nd.right < 0) {
+                for (int pos = nd.begin; pos < nd.end; ++pos) test_face(pos);
                 continue;
             }
             if (top + 2 > 64) {
                 overflow = true;
                 break;
             }
-            if (Lk[0] >= 0) stack[top++] = Lk[0];
-            if (Lk[1] >= 0) stack[top++] = Lk[1];
+            if (nd.left >= 0) stack[top++] = nd.left;
+            if (nd.right >= 0) stack[top++] = nd.right;
         }
     } else {
         for (int i = 0; i < M.nfaces; ++i) test_face(i);
@@ -932,12 +945,13 @@ __device__ inline int mesh_nearest_facet(const DevFacets& F, const double p[3]) 
         meshmath::closest(p, a, b, c, cp);
         meshmath::sub(p, cp, d);
         const double dist = meshmath::norm(d);
-        if (dist < bd) {
+        // first minimum in input face order (records are in leaf order)
+        if (dist < bd || (dist == bd && best >= 0 && M.face_id[i] < M.face_id[best])) {
             bd = dist;
             best = i;
         }
     }
-    return best < 0 ? -1 : M.face_to_facet[best];
+    return best < 0 ? -1 : M.face_facet[best];
 }
 
 // Velocity of a carrier in a mesh domain: the mode velocity (with sign flips),

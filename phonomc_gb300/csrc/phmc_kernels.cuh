@@ -52,6 +52,64 @@ void launch_cells_final(const LaunchCtx& x, int phase);
 enum CollisionKind : int { kCollideNone = 0, kCollideRta = 1, kCollideLinear = 2 };
 
 
+// Device layout of a face BVH (DevMesh): nodes renumbered breadth-first, face
+// records in the leaf order of the traversal (input order without a BVH).
+template <class Upload>
+void fill_dev_mesh(const MeshTracer& Tr, DevMesh& D, Upload&& up) {
+    const int nf = static_cast<int>(Tr.faces.size());
+    std::vector<int> order(nf);
+    for (int i = 0; i < nf; ++i) order[i] = Tr.root >= 0 ? Tr.order[i] : i;
+    std::vector<double> rec(static_cast<size_t>(nf) * kFaceRecord);
+    std::vector<int> facet(nf), id(nf);
+    for (int pos = 0; pos < nf; ++pos) {
+        const int f = order[pos];
+        double* r = rec.data() + static_cast<size_t>(pos) * kFaceRecord;
+        for (int a = 0; a < 3; ++a) {
+            r[a] = Tr.normals[f][a];
+            r[4 + a] = Tr.bounds[f][0][a];
+            r[7 + a] = Tr.bounds[f][1][a];
+            for (int k = 0; k < 3; ++k) r[10 + 3 * k + a] = Tr.vertices[Tr.faces[f][k]][a];
+        }
+        r[3] = Tr.k[f];
+        facet[pos] = Tr.face_to_facet[f];
+        id[pos] = f;
+    }
+    std::vector<DevBvhNode> nodes;
+    if (Tr.root >= 0) {
+        std::vector<int> renum(Tr.nodes.size(), -1), bfs;
+        bfs.push_back(Tr.root);
+        renum[Tr.root] = 0;
+        for (size_t k = 0; k < bfs.size(); ++k) {
+            const auto& nd = Tr.nodes[bfs[k]];
+            for (int child : {nd.left, nd.right})
+                if (child >= 0) {
+                    renum[child] = static_cast<int>(bfs.size());
+                    bfs.push_back(child);
+                }
+        }
+        nodes.resize(bfs.size());
+        for (size_t k = 0; k < bfs.size(); ++k) {
+            const auto& nd = Tr.nodes[bfs[k]];
+            DevBvhNode& o = nodes[k];
+            for (int a = 0; a < 3; ++a) {
+                o.bmin[a] = nd.bmin[a];
+                o.bmax[a] = nd.bmax[a];
+            }
+            o.left = nd.left >= 0 ? renum[nd.left] : -1;
+            o.right = nd.right >= 0 ? renum[nd.right] : -1;
+            o.begin = nd.begin;
+            o.end = nd.end;
+        }
+    }
+    D.nodes = up(nodes);
+    D.face = up(rec);
+    D.face_facet = up(facet);
+    D.face_id = up(id);
+    D.root = Tr.root >= 0 ? 0 : -1;
+    D.nfaces = nf;
+    D.nnodes = static_cast<int>(nodes.size());
+}
+
 // Device copy of a mesh domain's geometry: facet conditions, partners, shifts
 // and normals, the voxel -> cell map, the faces with their BVH and the star
 // simplices. `up(std::vector<T>)` returns a device pointer holding the vector.
@@ -80,32 +138,7 @@ void fill_dev_facets(const SimulationDomain& dom, double scale, DevFacets& G, Up
     G.shift = up(shift);
     G.normal = up(normal);
     G.voxel_cell = up(dom.voxel_cells());
-    std::vector<double> vv, nrm, bnd, nb;
-    std::vector<int> ff, links;
-    for (const auto& v : Tr.vertices) vv.insert(vv.end(), v.begin(), v.end());
-    for (const auto& f : Tr.faces) ff.insert(ff.end(), f.begin(), f.end());
-    for (const auto& x : Tr.normals) nrm.insert(nrm.end(), x.begin(), x.end());
-    for (const auto& b : Tr.bounds) {
-        bnd.insert(bnd.end(), b[0].begin(), b[0].end());
-        bnd.insert(bnd.end(), b[1].begin(), b[1].end());
-    }
-    for (const auto& nd : Tr.nodes) {
-        nb.insert(nb.end(), nd.bmin.begin(), nd.bmin.end());
-        nb.insert(nb.end(), nd.bmax.begin(), nd.bmax.end());
-        links.insert(links.end(), {nd.left, nd.right, nd.begin, nd.end});
-    }
-    DevMesh& D = G.mesh;
-    D.vertices = up(vv);
-    D.faces = up(ff);
-    D.face_to_facet = up(Tr.face_to_facet);
-    D.normals = up(nrm);
-    D.k = up(Tr.k);
-    D.bounds = up(bnd);
-    D.node_bounds = up(nb);
-    D.node_links = up(links);
-    D.order = up(Tr.order);
-    D.root = Tr.root;
-    D.nfaces = static_cast<int>(Tr.faces.size());
+    fill_dev_mesh(Tr, G.mesh, up);
     std::vector<double> sx;
     for (const auto& S : M.simplices()) {
         sx.insert(sx.end(), S.v[0].begin(), S.v[0].end());
