@@ -213,6 +213,93 @@ __global__ void __launch_bounds__(256) k_rta_solve(const DevTables* __restrict__
     }
 }
 
+// Warp-wide sum with the result of lane 0 broadcast, so every lane continues
+// with the same bits (the iteration decisions below stay warp-uniform).
+__device__ __forceinline__ double warp_sum_uniform(double x) {
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return __shfl_sync(0xffffffffu, x, 0);
+}
+
+// k_rta_solve with one warp per cell: the same bracket and Newton/bisection
+// iteration, with warp reductions instead of block barriers. Used when cells
+// are many (a mesh grid): a cell's class loop is short and the block-wide
+// reductions, not the arithmetic, set the time per iteration.
+__global__ void __launch_bounds__(256) k_rta_solve_warp(const DevTables* __restrict__ Tp, CellArrays C) {
+    const DevTables& T = *Tp;
+    const int lane = threadIdx.x & 31;
+    const int c = static_cast<int>((blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x) >> 5);
+    if (c >= C.ncells) return; // warp-uniform
+    const DevMaterial& M = T.mat[C.cell_material[c]];
+    const int nc = M.n_classes;
+    const size_t hb = static_cast<size_t>(c) * C.hist_modes;
+    const BinSum* bs = C.bins + hb;
+    const double* hm = C.hM + hb;
+    double2* ab = C.rta_ab + static_cast<size_t>(c) * C.n_classes;
+    const double Tc = C.temperature[c];
+    const double dt = T.par.dt;
+    for (int k = lane; k < nc; k += 32) {
+        const int rep = M.class_rep[k];
+        double a;
+        if (T.par.lifetime_local) {
+            const double g = gamma_at(M, rep, Tc);
+            a = (g == 0.0 || dt == 0.0) ? 0.0 : -expm1(-(g * dt) * (4.0 * 3.14159265358979323846));
+        } else {
+            a = M.relax_fixed[rep];
+        }
+        ab[k].x = a;
+    }
+    __syncwarp();
+    auto evaluate = [&](double temperature, bool want_slope, double& slope) {
+        const double Tt = fmax(0.0, temperature);
+        double v0 = 0.0, v1 = 0.0;
+        for (int k = lane; k < nc; k += 32) {
+            const double n0 = static_cast<double>(bs[k].cnt);
+            if (n0 == 0.0) continue;
+            const double w = fmax(0.0, M.class_omega[k]);
+            const double hw = kHbar * w;
+            const double a = ab[k].x;
+            if (!(hw > 0.0) || !(a > 0.0)) continue;
+            const double neq = bose_dev(Tt, w);
+            v0 += hw * a * (bs[k].N - n0 * neq);
+            if (want_slope && Tt > 0.0) v1 -= n0 * hw * a * (hw * neq * (neq + 1.0) / (kKb * Tt * Tt));
+        }
+        slope = want_slope ? warp_sum_uniform(v1) : 0.0;
+        return warp_sum_uniform(v0);
+    };
+    double dummy;
+    double low = 0.0, high = fmax(1000.0, 2.0 * fmax(1.0, Tc));
+    const double f_low = evaluate(low, false, dummy);
+    double f_high = evaluate(high, false, dummy);
+    for (int k = 0; f_high > 0.0 && k < 20; ++k) {
+        high *= 2.0;
+        f_high = evaluate(high, false, dummy);
+    }
+    double Ts = fmin(fmax(Tc, low), high);
+    if (f_low <= 0.0) {
+        Ts = low;
+    } else if (f_high >= 0.0) {
+        Ts = high;
+    } else {
+        double s0 = 0.0;
+        for (int k = lane; k < nc; k += 32) s0 += kHbar * fmax(0.0, M.class_omega[k]) * ab[k].x * hm[k];
+        const double tol = 1e-13 * fmax(1.0, warp_sum_uniform(s0));
+        for (int it = 0; it < 40; ++it) {
+            double d;
+            const double v = evaluate(Ts, true, d);
+            if (fabs(v) <= tol) break;
+            if (v > 0.0) low = Ts;
+            else high = Ts;
+            double cand = 0.5 * (low + high);
+            if (d < 0.0 && isfinite(d)) {
+                const double nt = Ts - v / d;
+                if (nt > low && nt < high && isfinite(nt)) cand = nt;
+            }
+            Ts = cand;
+        }
+    }
+    for (int k = lane; k < nc; k += 32) ab[k].y = bose_dev(Ts, fmax(0.0, M.class_omega[k]));
+}
+
 // ----------------------------------------------------- linear response
 // Cluster-wide sum of N doubles: CTA partials in shared memory, read by every
 // CTA of the cluster through distributed shared memory.
@@ -829,7 +916,10 @@ int launch_cell_solve(const LaunchCtx& x, int phase, int collision) {
     else k_cell_stats<false><<<grid, kStatThreads, 0, x.stream>>>(T, C, 0);
     k_cell_state<<<(C.ncells + 255) / 256, 256, 0, x.stream>>>(T, C, x.L, phase);
     if (phase >= 1 && rta) {
-        k_rta_solve<<<C.ncells, 256, 0, x.stream>>>(T, C);
+        if (C.ncells >= 1024) // many cells: one warp per cell
+            k_rta_solve_warp<<<(C.ncells + 7) / 8, 256, 0, x.stream>>>(T, C);
+        else
+            k_rta_solve<<<C.ncells, 256, 0, x.stream>>>(T, C);
         ++launches;
     } else if (phase >= 1 && collision == kCollideLinear) {
         const int gmax = C.lin_has_normal ? kMaxGains : 1;

@@ -216,11 +216,21 @@ struct __align__(16) DevBvhNode {
 // tests them), so a leaf is a run of records with no index indirection:
 // normal xyz, plane offset k, bounds min xyz / max xyz, vertices a, b, c.
 constexpr int kFaceRecord = 19;
+// FP32 copies for the culling walk: node bounds and face planes / bounds
+// rounded outward; `margin` (Angstrom) covers the FP32 rounding of the walk.
+struct __align__(8) DevBvhNode32 {
+    float bmin[3], bmax[3];
+    int left, right, begin, end;
+};
+constexpr int kFaceRecord32 = 10; // normal xyz, k, bounds min xyz, max xyz
 struct DevMesh {
     const DevBvhNode* nodes;
     const double* face;        // [nfaces][kFaceRecord]
     const int* face_facet;     // facet of each record
     const int* face_id;        // input face index of each record
+    const DevBvhNode32* nodes32;
+    const float* face32;       // [nfaces][kFaceRecord32]
+    float margin;
     int root;                  // -1: no BVH, records in input order and scanned in full
     int nfaces;
     int nnodes;
@@ -730,79 +740,190 @@ __device__ __forceinline__ bool ray_box(const double o[3], const RayInv& R, cons
 
 // Nearest surface hit of the ray x + v t (t > 1e-10) with the near-first BVH
 // walk (src/SurfaceMesh.cpp:1164-1269); facet -1 and t = infinity on a miss.
-__device__ inline void mesh_trace_dev(const DevMesh& M, const double x[3], const double v[3], double hit[3], double& t_out,
-                                      int& facet) {
+// Exact face test of the reference (src/SurfaceMesh.cpp:1164-1269): plane time
+// with eps 1e-10, bounds +-1e-9, closest-point distance <= 1e-7.
+struct MeshHit {
+    double t;
+    int face;
+    double p[3];
+};
+__device__ __forceinline__ void mesh_try_face(const DevMesh& M, int i, const double x[3], const double v[3], MeshHit& h) {
     using namespace meshmath;
-    double best_t = __longlong_as_double(0x7ff0000000000000LL);
-    int best = -1;
-    double best_p[3] = {0.0, 0.0, 0.0};
-    auto try_face = [&](int i) {
-        const double* r = M.face + kFaceRecord * i;
-        const double nn[3] = {r[0], r[1], r[2]};
-        const double denom = dot(v, nn);
-        if (fabs(denom) < 1e-10) return;
-        const double t = -__dadd_rn(dot(x, nn), r[3]) / denom;
-        if (t <= 1e-10 || t >= best_t) return;
-        double p[3];
-        axpy(x, v, t, p);
-        if (p[0] < r[4] - 1e-9 || p[1] < r[5] - 1e-9 || p[2] < r[6] - 1e-9 || p[0] > r[7] + 1e-9 ||
-            p[1] > r[8] + 1e-9 || p[2] > r[9] + 1e-9)
-            return;
-        const double A[3] = {r[10], r[11], r[12]}, B[3] = {r[13], r[14], r[15]}, Cc[3] = {r[16], r[17], r[18]};
-        double cp[3], d[3];
-        closest(p, A, B, Cc, cp);
-        sub(cp, p, d);
-        if (sqrt(dot(d, d)) > 1e-7) return;
-        best_t = t;
-        best = i;
-        for (int a = 0; a < 3; ++a) best_p[a] = p[a];
+    const double* r = M.face + kFaceRecord * i;
+    const double nn[3] = {r[0], r[1], r[2]};
+    const double denom = dot(v, nn);
+    if (fabs(denom) < 1e-10) return;
+    const double t = -__dadd_rn(dot(x, nn), r[3]) / denom;
+    if (t <= 1e-10 || t >= h.t) return;
+    double p[3];
+    axpy(x, v, t, p);
+    if (p[0] < r[4] - 1e-9 || p[1] < r[5] - 1e-9 || p[2] < r[6] - 1e-9 || p[0] > r[7] + 1e-9 || p[1] > r[8] + 1e-9 ||
+        p[2] > r[9] + 1e-9)
+        return;
+    const double A[3] = {r[10], r[11], r[12]}, B[3] = {r[13], r[14], r[15]}, Cc[3] = {r[16], r[17], r[18]};
+    double cp[3], d[3];
+    closest(p, A, B, Cc, cp);
+    sub(cp, p, d);
+    if (sqrt(dot(d, d)) > 1e-7) return;
+    h.t = t;
+    h.face = i;
+    for (int a = 0; a < 3; ++a) h.p[a] = p[a];
+}
+
+// Reference BVH walk in FP64: near-first, boxes pruned by the best time so far.
+static __device__ __noinline__ void mesh_walk_fp64(const DevMesh& M, const double x[3], const double v[3], MeshHit& h) {
+    using namespace meshmath;
+    if (M.root < 0) {
+        for (int i = 0; i < M.nfaces; ++i) mesh_try_face(M, i, x, v, h);
+        return;
+    }
+    const RayInv R = ray_inv(v);
+    int stack[64];
+    int top = 0;
+    stack[top++] = M.root;
+    while (top > 0) {
+        const DevBvhNode& nd = M.nodes[stack[--top]];
+        double tn = 0.0;
+        if (!ray_box(x, R, nd.bmin, nd.bmax, h.t, tn)) continue;
+        if (nd.left < 0 && nd.right < 0) {
+            for (int pos = nd.begin; pos < nd.end; ++pos) mesh_try_face(M, pos, x, v, h);
+            continue;
+        }
+        int near_child = -1, far_child = -1;
+        double near_t = __longlong_as_double(0x7ff0000000000000LL), far_t = near_t;
+        const int kids[2] = {nd.left, nd.right};
+        for (int s = 0; s < 2; ++s) {
+            const int child = kids[s];
+            if (child < 0) continue;
+            double tc = 0.0;
+            if (!ray_box(x, R, M.nodes[child].bmin, M.nodes[child].bmax, h.t, tc)) continue;
+            if (tc < near_t) {
+                far_child = near_child;
+                far_t = near_t;
+                near_child = child;
+                near_t = tc;
+            } else if (tc < far_t) {
+                far_child = child;
+                far_t = tc;
+            }
+        }
+        if (far_child >= 0 && top < 64) stack[top++] = far_child;
+        if (near_child >= 0 && top < 64) stack[top++] = near_child;
+    }
+}
+
+// The same walk with FP32 culling. Boxes are widened by `margin`, face
+// planes are tested in FP32 with an error bound, and only faces FP32 cannot
+// rule out go through the exact FP64 test, so FP32 never drops a face the
+// FP64 walk would accept. The FP64 walk runs instead for rays with a velocity
+// component of magnitude in (0, 1e-10], where FP32 slab times lose meaning.
+__device__ inline void mesh_walk_fp32(const DevMesh& M, const double x[3], const double v[3], MeshHit& h) {
+    float xf[3], vf[3], invf[3];
+    bool flat[3];
+    float vmax = 0.0f;
+    for (int a = 0; a < 3; ++a) {
+        xf[a] = static_cast<float>(x[a]);
+        vf[a] = static_cast<float>(v[a]);
+        flat[a] = v[a] == 0.0;
+        invf[a] = flat[a] ? 0.0f : 1.0f / vf[a];
+        vmax = fmaxf(vmax, fabsf(vf[a]));
+    }
+    const float m = M.margin;
+    auto limit = [&]() {
+        return isinf(h.t) ? __int_as_float(0x7f800000) : static_cast<float>(h.t) * 1.000001f + 1e-6f;
     };
-    if (M.root >= 0) {
-        const RayInv R = ray_inv(v);
-        int stack[64];
-        int top = 0;
-        stack[top++] = M.root;
-        while (top > 0) {
-            const DevBvhNode& nd = M.nodes[stack[--top]];
-            double tn = 0.0;
-            if (!ray_box(x, R, nd.bmin, nd.bmax, best_t, tn)) continue;
-            if (nd.left < 0 && nd.right < 0) {
-                for (int pos = nd.begin; pos < nd.end; ++pos) try_face(pos);
+    auto box = [&](const DevBvhNode32& b, float tlim, float& tnear) {
+        float t0 = 0.0f, t1 = tlim;
+        for (int a = 0; a < 3; ++a) {
+            const float lo = b.bmin[a] - m, hi = b.bmax[a] + m;
+            if (flat[a]) {
+                if (xf[a] < lo || xf[a] > hi) return false;
                 continue;
             }
-            int near_child = -1, far_child = -1;
-            double near_t = __longlong_as_double(0x7ff0000000000000LL), far_t = near_t;
-            const int kids[2] = {nd.left, nd.right};
-            for (int s = 0; s < 2; ++s) {
-                const int child = kids[s];
-                if (child < 0) continue;
-                double tc = 0.0;
-                if (!ray_box(x, R, M.nodes[child].bmin, M.nodes[child].bmax, best_t, tc)) continue;
-                if (tc < near_t) {
-                    far_child = near_child;
-                    far_t = near_t;
-                    near_child = child;
-                    near_t = tc;
-                } else if (tc < far_t) {
-                    far_child = child;
-                    far_t = tc;
-                }
+            float s0 = (lo - xf[a]) * invf[a], s1 = (hi - xf[a]) * invf[a];
+            if (s0 > s1) {
+                const float s = s0;
+                s0 = s1;
+                s1 = s;
             }
-            if (far_child >= 0 && top < 64) stack[top++] = far_child;
-            if (near_child >= 0 && top < 64) stack[top++] = near_child;
+            t0 = fmaxf(t0, s0);
+            t1 = fminf(t1, s1);
+            if (t1 < t0) return false;
         }
-    } else {
-        for (int i = 0; i < M.nfaces; ++i) try_face(i);
+        if (t1 < 0.0f) return false;
+        tnear = t0;
+        return true;
+    };
+    auto face = [&](int pos) {
+        const float* r = M.face32 + kFaceRecord32 * pos;
+        const float den = vf[0] * r[0] + vf[1] * r[1] + vf[2] * r[2];
+        if (fabsf(den) >= 1e-4f * vmax) {
+            const float tf = -(xf[0] * r[0] + xf[1] * r[1] + xf[2] * r[2] + r[3]) / den;
+            // error of tf: numerator within m, denominator within 4e-7 vmax (relative to |den| >= 1e-4 vmax)
+            const float rel = 4e-7f * vmax / fabsf(den) + 1e-6f;
+            const float et = m / fabsf(den) + rel * fabsf(tf) + 1e-6f;
+            if (tf + et <= 0.0f || tf - et > limit()) return;
+            const float ep = vmax * (et + 1e-6f * fabsf(tf)) + m;
+            for (int a = 0; a < 3; ++a) {
+                const float p = xf[a] + vf[a] * tf;
+                if (p < r[4 + a] - ep || p > r[7 + a] + ep) return;
+            }
+        }
+        mesh_try_face(M, pos, x, v, h);
+    };
+    int stack[64];
+    int top = 0;
+    stack[top++] = M.root;
+    while (top > 0) {
+        const DevBvhNode32 nd = M.nodes32[stack[--top]];
+        float tn;
+        if (!box(nd, limit(), tn)) continue;
+        if (nd.left < 0 && nd.right < 0) {
+            for (int pos = nd.begin; pos < nd.end; ++pos) face(pos);
+            continue;
+        }
+        int near_child = -1, far_child = -1;
+        float near_t = __int_as_float(0x7f800000), far_t = near_t;
+        const int kids[2] = {nd.left, nd.right};
+        const float tl = limit();
+        for (int s = 0; s < 2; ++s) {
+            const int child = kids[s];
+            if (child < 0) continue;
+            float tc;
+            if (!box(M.nodes32[child], tl, tc)) continue;
+            if (tc < near_t) {
+                far_child = near_child;
+                far_t = near_t;
+                near_child = child;
+                near_t = tc;
+            } else if (tc < far_t) {
+                far_child = child;
+                far_t = tc;
+            }
+        }
+        if (far_child >= 0 && top < 64) stack[top++] = far_child;
+        if (near_child >= 0 && top < 64) stack[top++] = near_child;
     }
-    if (best < 0) {
+}
+
+__device__ inline void mesh_trace_dev(const DevMesh& M, const double x[3], const double v[3], double hit[3], double& t_out,
+                                      int& facet) {
+    MeshHit h;
+    h.t = __longlong_as_double(0x7ff0000000000000LL);
+    h.face = -1;
+    bool tiny = false;
+    for (int a = 0; a < 3; ++a) tiny = tiny || (v[a] != 0.0 && fabs(v[a]) <= 1e-10);
+    if (M.root >= 0 && M.nodes32 && !tiny) mesh_walk_fp32(M, x, v, h);
+    else mesh_walk_fp64(M, x, v, h);
+    if (h.face < 0) {
         for (int a = 0; a < 3; ++a) hit[a] = x[a];
         t_out = __longlong_as_double(0x7ff0000000000000LL);
         facet = -1;
         return;
     }
-    for (int a = 0; a < 3; ++a) hit[a] = best_p[a];
-    t_out = best_t;
-    facet = M.face_facet[best];
+    for (int a = 0; a < 3; ++a) hit[a] = h.p[a];
+    t_out = h.t;
+    facet = M.face_facet[h.face];
 }
 
 // ------------------------------------------------------------ mesh domains
@@ -969,7 +1090,7 @@ __device__ __forceinline__ void mesh_velocity(const DevFacets& F, const DevMater
 
 // Wall-hit cache with nudged retries on the mesh (src/solver/TransportOperator.cpp:186-250).
 // Returns 0 on success, 1 when no retry found a wall, 2 on a membership overflow.
-__device__ inline int mesh_cache_hit(const DevFacets& F, const DevDomain& D, const DevParams& P, double p[3],
+static __device__ __noinline__ int mesh_cache_hit(const DevFacets& F, const DevDomain& D, const DevParams& P, double p[3],
                                      const double v[3], double cp[3], double& t, int& f) {
     const double speed = meshmath::norm(v);
     if (isfinite(speed) && speed <= 1e-18) {

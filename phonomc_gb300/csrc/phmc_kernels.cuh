@@ -2,6 +2,11 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
+#include <limits>
+#include <vector>
+
 #include "phmc_device.cuh"
 #include "phmc_solver.h"
 
@@ -101,6 +106,41 @@ void fill_dev_mesh(const MeshTracer& Tr, DevMesh& D, Upload&& up) {
             o.end = nd.end;
         }
     }
+    // FP32 culling copies: bounds rounded outward, margin for the walk's rounding
+    auto down = [](double x) {
+        float f = static_cast<float>(x);
+        return static_cast<double>(f) > x ? std::nextafter(f, -std::numeric_limits<float>::infinity()) : f;
+    };
+    auto upf = [](double x) {
+        float f = static_cast<float>(x);
+        return static_cast<double>(f) < x ? std::nextafter(f, std::numeric_limits<float>::infinity()) : f;
+    };
+    std::vector<DevBvhNode32> nodes32(nodes.size());
+    for (size_t k = 0; k < nodes.size(); ++k) {
+        for (int a = 0; a < 3; ++a) {
+            nodes32[k].bmin[a] = down(nodes[k].bmin[a]);
+            nodes32[k].bmax[a] = upf(nodes[k].bmax[a]);
+        }
+        nodes32[k].left = nodes[k].left;
+        nodes32[k].right = nodes[k].right;
+        nodes32[k].begin = nodes[k].begin;
+        nodes32[k].end = nodes[k].end;
+    }
+    std::vector<float> rec32(static_cast<size_t>(nf) * kFaceRecord32);
+    double scale = 1.0;
+    for (int pos = 0; pos < nf; ++pos) {
+        const double* r = rec.data() + static_cast<size_t>(pos) * kFaceRecord;
+        float* o = rec32.data() + static_cast<size_t>(pos) * kFaceRecord32;
+        for (int q = 0; q < 4; ++q) o[q] = static_cast<float>(r[q]);
+        for (int a = 0; a < 3; ++a) {
+            o[4 + a] = down(r[4 + a]);
+            o[7 + a] = upf(r[7 + a]);
+            scale = std::max({scale, std::abs(r[4 + a]), std::abs(r[7 + a])});
+        }
+    }
+    D.nodes32 = nodes32.empty() ? nullptr : up(nodes32);
+    D.face32 = up(rec32);
+    D.margin = static_cast<float>(1e-6 * scale + 1e-4);
     D.nodes = up(nodes);
     D.face = up(rec);
     D.face_facet = up(facet);

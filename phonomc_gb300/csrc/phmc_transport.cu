@@ -839,7 +839,7 @@ __global__ void __launch_bounds__(kTransportThreads) k_transport_mesh(const __gr
 // Mesh transport, pass 2 of 2: the full flight of every queued carrier from
 // the start of the step (occupation already updated), then its cell and bin.
 template <bool kRta>
-__global__ void __launch_bounds__(kTransportThreads) k_mesh_events(const __grid_constant__ DevTables T, CarrierState S,
+__global__ void __launch_bounds__(kTransportThreads, 1) k_mesh_events(const __grid_constant__ DevTables T, CarrierState S,
                                                                    CellArrays C, DevLedger* L) {
     const uint32_t step = L->step_index;
     __shared__ BlockLedger bl;
