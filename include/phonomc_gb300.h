@@ -140,6 +140,7 @@ typedef struct phmc_config {
     int32_t precision;               /* 0 = plain FP64 state, 1 = mixed (FP32 transport) */
     const phmc_heat_source* heat_source; /* NULL: no heat source */
     const phmc_mesh_domain* mesh;    /* NULL: the analytic box of sizes / face_condition */
+    const char* material_folder;     /* NULL or a label reported in summary.txt */
 } phmc_config;
 
 /* Getters of include/MonteCarloSolver.h:59-101 plus the last step's ledger. */
@@ -162,6 +163,11 @@ typedef struct phmc_stats {
     double total_heat_source_energy_ev, step_heat_source_energy_ev;
     double prescribed_heat_source_energy_ev, pending_heat_source_energy_ev;
     int64_t step_heat_source_updates;
+    /* rough reflections since the start (src/solver/RoughBoundarySampler.cpp:371-533):
+     * specular, missing specular partner, residual window, window without flux,
+     * diffuse, outgoing-pool fallback, uniform fallback, then all events */
+    int64_t rough_counts[8];
+    int64_t collision_cache_corrections; /* wall caches found from a nudged position */
 } phmc_stats;
 
 const char* phmc_last_error(void);
@@ -210,7 +216,13 @@ int phmc_solver_set_graphs(phmc_solver* s, int on);
 /* Page-lock / release caller-owned host buffers used for end-to-end stepping. */
 int phmc_host_register(void* ptr, int64_t bytes);
 int phmc_host_unregister(void* ptr);
+/* grid_centers.csv again (summary.txt's domain part and grid_centers.csv are
+ * written when the solver is created with an output folder). */
 int phmc_solver_write_outputs(phmc_solver* s);
+/* Appends the [runtime] block and the run diagnostics to summary.txt, as the
+ * reference's main does after the step loop (src/main.cpp:117-131,
+ * MonteCarloSolver::append_profile_summary). */
+int phmc_solver_append_summary(phmc_solver* s, int64_t total_seconds);
 void phmc_solver_destroy(phmc_solver* s);
 
 /* ---- batched instances (no counterpart in the reference's API; the
@@ -225,6 +237,8 @@ typedef struct phmc_batch phmc_batch;
  * facets, boundary assignment, cells and the voxel -> cell map, with point
  * membership and cell lookup. No device work. */
 typedef struct phmc_domain phmc_domain;
+/* With cfg->output_folder set, writes summary.txt (domain part) and
+ * grid_centers.csv there, as SimulationDomain's constructor does. */
 int phmc_domain_create(const phmc_config* cfg, phmc_domain** out);
 void phmc_domain_destroy(phmc_domain* d);
 /* counts; shape3 = voxel grid, bounds6 = min xyz, max xyz; volume in A^3 */

@@ -54,8 +54,16 @@ struct RoughDraws {
     double u[3];
 };
 // src/solver/RoughBoundarySampler.cpp:373-533 with the draws supplied.
+// Outcome flags as counted by the reference's RoughSampleEvents.
+enum : unsigned {
+    kRoughSpecular = 1u, kRoughMissingSpec = 2u, kRoughWindow = 4u, kRoughWindowFallback = 8u,
+    kRoughDiffuse = 16u, kRoughPool = 32u, kRoughRandom = 64u,
+};
 int rough_sample(const RoughTable& rd, const MaterialTables& T, int in_ai, double n_in, bool signed_weights,
-                 const RoughDraws& d, double& n_out) {
+                 const RoughDraws& d, double& n_out, unsigned* diag_out = nullptr) {
+    unsigned diag_local = 0;
+    unsigned& diag = diag_out ? *diag_out : diag_local;
+    diag = 0;
     n_out = n_in;
     const int na = T.n_active;
     const double p_spec = (in_ai >= 0 && in_ai < na) ? std::clamp(rd.specularity[in_ai], 0.0, 1.0) : 0.0;
@@ -65,6 +73,7 @@ int rough_sample(const RoughTable& rd, const MaterialTables& T, int in_ai, doubl
     };
     if (in_ai >= 0 && d.u[0] <= p_spec) {
         const int out_ai = rd.spec_match[in_ai];
+        diag = (out_ai >= 0 && out_ai < na) ? kRoughSpecular : kRoughMissingSpec;
         if (out_ai >= 0 && out_ai < na) {
             const double mapped = remap(out_ai);
             if (std::isfinite(mapped) && (signed_weights || mapped >= 0.0)) {
@@ -89,6 +98,9 @@ int rough_sample(const RoughTable& rd, const MaterialTables& T, int in_ai, doubl
                                                             rd.residual_prefix.begin()) - 1, b, e - 1);
                 out_ai = rd.outgoing_sorted[pos];
                 done = true;
+                diag |= kRoughWindow;
+            } else {
+                diag |= kRoughWindowFallback;
             }
         }
     }
@@ -104,10 +116,13 @@ int rough_sample(const RoughTable& rd, const MaterialTables& T, int in_ai, doubl
             int k = static_cast<int>(d.u[2] * rd.outgoing_active.size());
             k = std::min(k, static_cast<int>(rd.outgoing_active.size()) - 1);
             out_ai = rd.outgoing_active[k];
+            diag |= kRoughPool;
         } else {
             out_ai = std::min(static_cast<int>(d.u[2] * na), na - 1);
+            diag |= kRoughRandom;
         }
     }
+    diag |= kRoughDiffuse;
     const double mapped = remap(out_ai);
     if (std::isfinite(mapped) && (signed_weights || mapped >= 0.0)) {
         n_out = mapped;
@@ -577,6 +592,8 @@ struct OracleSolver {
     double elapsed = 0;
     double avg_flux = 0, kappa_fit = 0, kappa_end = 0;
     long long iface_events = 0, iface_transmitted = 0, iface_reflected = 0;
+    long long rough_counts[8] = {0, 0, 0, 0, 0, 0, 0, 0}; // outcome flags, then events
+    long long cache_corrections = 0;
     bool failed = false;
 
     Vec3 velocity(uint32_t w, int32_t mir = -1) const {
@@ -648,6 +665,7 @@ struct OracleSolver {
                 domain->trace(c, v, cp, t, f);
                 if (f >= 0 && std::isfinite(t)) {
                     p = c;
+                    ++cache_corrections;
                     break;
                 }
             }
@@ -690,7 +708,11 @@ struct OracleSolver {
                                              static_cast<uint32_t>(event), 1);
                 RoughDraws dr{{d0.a, d0.b, d1.a}};
                 double n_out;
-                const int out = rough_sample(P.rough.tables[table], T, a, occ[i], P.conservative, dr, n_out);
+                unsigned diag = 0;
+                const int out = rough_sample(P.rough.tables[table], T, a, occ[i], P.conservative, dr, n_out, &diag);
+                rough_counts[7] += 1;
+                for (int k = 0; k < 7; ++k)
+                    if (diag & (1u << k)) rough_counts[k] += 1;
                 uint32_t signs = 0;
                 const bool mesh = domain->is_mesh();
                 const double vn = mesh ? dot3({T.vel[3 * out], T.vel[3 * out + 1], T.vel[3 * out + 2]}, F.normal)
@@ -1284,6 +1306,8 @@ int orc_solver_stats(void* sp, phmc_stats* o) {
         o->interface_events = s->iface_events;
         o->interface_transmitted = s->iface_transmitted;
         o->interface_reflected = s->iface_reflected;
+        for (int k = 0; k < 8; ++k) o->rough_counts[k] = s->rough_counts[k];
+        o->collision_cache_corrections = s->cache_corrections;
     });
 }
 int orc_solver_cell_count(void* sp, int* n) {

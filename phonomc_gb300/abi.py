@@ -151,7 +151,7 @@ class ConfigPOD(C.Structure):
         ("material_interface_axis", C.c_int32), ("n_interfaces", C.c_int32),
         ("material_interface_positions", c_double_p), ("interface_frequency_bin_thz", C.c_double),
         ("precision", C.c_int32), ("heat_source", C.POINTER(HeatSourcePOD)),
-        ("mesh", C.POINTER(MeshDomainPOD)),
+        ("mesh", C.POINTER(MeshDomainPOD)), ("material_folder", C.c_char_p),
     ]
 
 
@@ -170,10 +170,13 @@ class StatsPOD(C.Structure):
         ("device_launches", C.c_int64), ("total_heat_source_energy_ev", C.c_double),
         ("step_heat_source_energy_ev", C.c_double), ("prescribed_heat_source_energy_ev", C.c_double),
         ("pending_heat_source_energy_ev", C.c_double), ("step_heat_source_updates", C.c_int64),
+        ("rough_counts", C.c_int64 * 8), ("collision_cache_corrections", C.c_int64),
     ]
 
     def as_dict(self) -> dict:
-        return {name: getattr(self, name) for name, _ in self._fields_}
+        out = {name: getattr(self, name) for name, _ in self._fields_}
+        out["rough_counts"] = list(self.rough_counts)
+        return out
 
 
 def dptr(a: Optional[np.ndarray]):
@@ -220,7 +223,7 @@ def config_pod(cfg: dict):
     """Build a ConfigPOD from a dict of SimulationConfig-style fields (internal units)."""
     keep = []
     c = ConfigPOD()
-    c.sizes[:] = list(cfg.get("sizes", (1.0, 1.0, 1.0)))
+    c.sizes[:] = list(cfg.get("sizes", (200.0, 200.0, 200.0)))
     c.particle_count = float(cfg.get("particle_count", 1e4))
     c.time_step = float(cfg.get("time_step", 1.0))
     c.iterations = int(cfg.get("iterations", 10000))
@@ -260,6 +263,10 @@ def config_pod(cfg: dict):
         hs = heat_source_pod(cfg["heat_source"], keep)
         keep.append(hs)
         c.heat_source = C.pointer(hs)
+    if cfg.get("material_folder"):
+        b = str(cfg["material_folder"]).encode()
+        keep.append(b)
+        c.material_folder = b
     if cfg.get("mesh"):
         mp = mesh_domain_pod(cfg["mesh"], keep)
         keep.append(mp)
@@ -454,6 +461,7 @@ DEVICE_PROTOS = {
     "solver_run_timestep": (C.c_int, [C.c_void_p]),
     "solver_synchronize": (C.c_int, [C.c_void_p]),
     "solver_write_outputs": (C.c_int, [C.c_void_p]),
+    "solver_append_summary": (C.c_int, [C.c_void_p, C.c_int64]),
     "solver_timed_run": (C.c_int, [C.c_void_p, C.c_int, c_double_p, c_double_p, c_int64_p, c_int64_p, c_int64_p]),
     "solver_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "batch_create": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),

@@ -5,6 +5,8 @@
 #include "phmc_pod.h"
 
 #include <cstring>
+#include <filesystem>
+#include <fstream>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -160,7 +162,9 @@ __global__ void k_rough_rays(DevRoughTable R, DevMaterial M, int conservative, i
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         double o;
-        aout[i] = rough_sample_dev(R, M, ain[i], occ[i], conservative != 0, u3[3 * i], u3[3 * i + 1], u3[3 * i + 2], o);
+        unsigned diag;
+        aout[i] = rough_sample_dev(R, M, ain[i], occ[i], conservative != 0, u3[3 * i], u3[3 * i + 1], u3[3 * i + 2], o,
+                                   diag);
         oout[i] = o;
     }
 }
@@ -234,6 +238,13 @@ int phmc_domain_create(const phmc_config* cfg, phmc_domain** out) {
         auto d = std::make_unique<phmc_domain>();
         d->cfg = config_from_pod(*cfg);
         d->d = std::make_unique<SimulationDomain>(d->cfg);
+        if (!d->cfg.output_folder.empty()) { // as the reference's SimulationDomain constructor does
+            std::filesystem::create_directories(d->cfg.output_folder);
+            std::ofstream(std::filesystem::path(d->cfg.output_folder) / "summary.txt")
+                << format_domain_summary(d->cfg, *d->d);
+            std::ofstream(std::filesystem::path(d->cfg.output_folder) / "grid_centers.csv")
+                << format_grid_centers(*d->d);
+        }
         *out = d.release();
     });
 }
@@ -501,6 +512,10 @@ int phmc_host_unregister(void* ptr) {
 }
 
 int phmc_solver_write_outputs(phmc_solver* s) { return guard([&] { s->s->write_outputs(); }); }
+
+int phmc_solver_append_summary(phmc_solver* s, int64_t total_seconds) {
+    return guard([&] { s->s->append_summary(static_cast<long long>(total_seconds)); });
+}
 
 void phmc_solver_destroy(phmc_solver* s) { delete s; }
 

@@ -630,6 +630,7 @@ __global__ void __launch_bounds__(1024) k_cells_final(const DevTables* __restric
     L->total_drive_ev += L->step_drive_ev;
     L->total_drive_updates += L->step_drive_updates;
     L->total_source_ev += L->step_source_ev;
+    L->total_source_updates += L->step_source_updates;
     L->thermal_energy = v[0];
     L->particle_count += static_cast<long long>(L->step_injected) - static_cast<long long>(L->step_absorbed);
     for (int r = 0; r < kMaxReservoirs; ++r) L->previous_res[r] = L->absorbed_res[r];

@@ -22,6 +22,19 @@ namespace phmc {
 constexpr int kMaxMaterials = 4;
 constexpr int kMaxRoughTables = 24;
 constexpr int kMaxReservoirs = 6;
+
+// Outcome flags of one rough reflection, the event classes counted by the
+// reference's RoughSampleEvents (src/solver/RoughBoundarySampler.cpp:371-533).
+enum : unsigned {
+    kRoughSpecular = 1u,        // specular partner taken
+    kRoughMissingSpec = 2u,     // specular draw without a partner
+    kRoughWindow = 4u,          // residual-flux window of the incoming frequency
+    kRoughWindowFallback = 8u,  // window present but without residual flux
+    kRoughDiffuse = 16u,        // a diffuse outgoing mode was drawn
+    kRoughPool = 32u,           // uniform outgoing-pool fallback
+    kRoughRandom = 64u,         // uniform over all modes
+};
+constexpr int kRoughCounters = 8; // the seven flags above, then the event count
 constexpr double kHbar = 6.582119569e-4;
 constexpr double kKb = 8.617333262145e-5;
 
@@ -181,7 +194,7 @@ struct DevLedger {
     double next_drive_ev;                  // first gradient half-step of the next step
     unsigned long long next_drive_updates;
     double step_source_ev, next_source_ev, total_source_ev;   // heat source deposits
-    unsigned long long step_source_updates, next_source_updates;
+    unsigned long long step_source_updates, next_source_updates, total_source_updates;
     double step_balance_residual;
     double thermal_energy;
     // totals
@@ -189,6 +202,8 @@ struct DevLedger {
     double total_absorbed_ev, total_injected_ev, total_lifetime_residual, total_balance_residual, total_drive_ev;
     unsigned long long total_drive_updates;
     unsigned long long total_iface_events, total_iface_transmitted, total_iface_reflected;
+    unsigned long long total_rough[kRoughCounters]; // rough reflection outcomes, then the event count
+    unsigned long long total_cache_corrections;     // wall caches found from a nudged position
     long long particle_count;
 };
 
@@ -367,15 +382,16 @@ __device__ __forceinline__ bool box_contains(const DevDomain& D, const double p[
 }
 
 // Wall-hit cache with the reference's nudged retries (src/solver/TransportOperator.cpp:186-250).
-__device__ __forceinline__ bool cache_hit(const DevDomain& D, const DevParams& P, double p[3], const double v[3],
-                                          double speed, double cp[3], double& t, int& f) {
+// 0: no wall found; 1: found; 2: found from a nudged position (the carrier moved).
+__device__ __forceinline__ int cache_hit(const DevDomain& D, const DevParams& P, double p[3], const double v[3],
+                                         double speed, double cp[3], double& t, int& f) {
     if (isfinite(speed) && speed <= 1e-18) {
         t = __longlong_as_double(0x7ff0000000000000LL);
         f = -1;
-        return true;
+        return 1;
     }
     trace_box(D, p, v, cp, t, f);
-    if (f >= 0 && isfinite(t)) return true;
+    if (f >= 0 && isfinite(t)) return 1;
     const double eps = fmax(P.push_eps, 1e-10 * D.scale);
     int nearest = 0;
     double bd = 1e300;
@@ -406,10 +422,10 @@ __device__ __forceinline__ bool cache_hit(const DevDomain& D, const DevParams& P
         trace_box(D, cand[c], v, cp, t, f);
         if (f >= 0 && isfinite(t)) {
             for (int a = 0; a < 3; ++a) p[a] = cand[c][a];
-            return true;
+            return 2;
         }
     }
-    return false;
+    return 0;
 }
 
 __device__ __forceinline__ void mode_velocity(const DevMaterial& M, uint32_t w, double v[3]) {
@@ -422,14 +438,17 @@ __device__ __forceinline__ void mode_velocity(const DevMaterial& M, uint32_t w, 
 }
 
 // Rough-wall reflection with supplied uniforms (src/solver/RoughBoundarySampler.cpp:373-533).
+
 __device__ __forceinline__ int rough_sample_dev(const DevRoughTable& R, const DevMaterial& M, int in_ai, double n_in, bool signed_w,
-                                double u0, double u1, double u2, double& n_out) {
+                                double u0, double u1, double u2, double& n_out, unsigned& diag) {
     n_out = n_in;
+    diag = 0;
     const int na = M.n_active;
     const double p_spec = fmin(fmax(R.specularity[in_ai], 0.0), 1.0);
     const double nbg_in = M.nbg[in_ai], w_in = M.omega[in_ai];
     if (u0 <= p_spec) {
         const int out = R.spec_match[in_ai];
+        diag = (out >= 0 && out < na) ? kRoughSpecular : kRoughMissingSpec;
         if (out >= 0 && out < na) {
             const double mapped = M.nbg[out] + w_in * (n_in - nbg_in) / fmax(1e-30, M.omega[out]);
             if (isfinite(mapped) && (signed_w || mapped >= 0.0)) {
@@ -457,6 +476,9 @@ __device__ __forceinline__ int rough_sample_dev(const DevRoughTable& R, const De
             int pos = lo - 1;
             pos = pos < b ? b : (pos > e - 1 ? e - 1 : pos);
             out = R.outgoing_sorted[pos];
+            diag |= kRoughWindow;
+        } else {
+            diag |= kRoughWindowFallback;
         }
     }
     if (out < 0) {
@@ -474,11 +496,14 @@ __device__ __forceinline__ int rough_sample_dev(const DevRoughTable& R, const De
         } else if (R.n_outgoing > 0) {
             int k = static_cast<int>(u2 * R.n_outgoing);
             out = R.outgoing_active[k < R.n_outgoing ? k : R.n_outgoing - 1];
+            diag |= kRoughPool;
         } else {
             const int k = static_cast<int>(u2 * na);
             out = k < na ? k : na - 1;
+            diag |= kRoughRandom;
         }
     }
+    diag |= kRoughDiffuse;
     const double mapped = M.nbg[out] + w_in * (n_in - nbg_in) / fmax(1e-30, M.omega[out]);
     if (isfinite(mapped) && (signed_w || mapped >= 0.0)) {
         n_out = mapped;
@@ -1089,7 +1114,8 @@ __device__ __forceinline__ void mesh_velocity(const DevFacets& F, const DevMater
 }
 
 // Wall-hit cache with nudged retries on the mesh (src/solver/TransportOperator.cpp:186-250).
-// Returns 0 on success, 1 when no retry found a wall, 2 on a membership overflow.
+// Returns 0 on success, 3 on success from a nudged position, 1 when no retry
+// found a wall, 2 on a membership overflow.
 static __device__ __noinline__ int mesh_cache_hit(const DevFacets& F, const DevDomain& D, const DevParams& P, double p[3],
                                      const double v[3], double cp[3], double& t, int& f) {
     const double speed = meshmath::norm(v);
@@ -1128,7 +1154,7 @@ static __device__ __noinline__ int mesh_cache_hit(const DevFacets& F, const DevD
         mesh_trace_dev(F.mesh, cand[c], v, cp, t, f);
         if (f >= 0 && isfinite(t)) {
             for (int a = 0; a < 3; ++a) p[a] = cand[c][a];
-            return 0;
+            return 3;
         }
     }
     return 1;

@@ -43,7 +43,7 @@ enum class HeatSourceTimeProfile { Constant, Pulsed };
 
 struct SimulationConfig {
     std::string model = "box";
-    std::vector<double> sizes{2000.0, 2000.0, 2000.0}; // Angstrom
+    std::vector<double> sizes{200.0, 200.0, 200.0}; // Angstrom
     double particle_count = 1e4;
     double time_step = 1.0;
     int iterations = 10000;
@@ -79,6 +79,7 @@ struct SimulationConfig {
     std::vector<double> boundary_values;   // K for 'T', roughness in nm for 'R', 0 for 'P'
     std::vector<std::array<double, 6>> periodic_pair; // region pairs, matched facet by facet
     std::string output_folder;
+    std::string material_folder; // reported in summary.txt; tables enter as arrays
     // Layered materials (include/SimulationConfig.h:93-99): N materials, N-1 planes.
     int material_interface_axis = 0;
     std::vector<double> material_interface_positions; // Angstrom
@@ -507,6 +508,7 @@ struct Problem {
     bool one_to_one = true;
     double push_eps = 1e-10;
     double particle_volume = 0;
+    std::vector<double> material_spatial_volume; // per material, layered domains (common state weight)
     int initial_particles = 0;
     std::vector<MaterialTables> mats;
     SimulationDomain* domain = nullptr;
@@ -560,5 +562,34 @@ struct ConvergenceRow {
 };
 std::string format_convergence_header(size_t cells, bool gradient_driven);
 std::string format_convergence_row(const ConvergenceRow& r);
+
+// summary.txt and grid_centers.csv (phmc_output.cpp).
+struct RunSummary {
+    SimulationConfig cfg;
+    uint64_t random_seed = 0;
+    long long cache_corrections = 0, cell_index_rebuilds = 0, temperature_refreshes = 0;
+    long long rough[8] = {0, 0, 0, 0, 0, 0, 0, 0}; // outcome flags of rough reflections, then events
+    int material_count = 1;
+    double interface_frequency_bin_thz = 0.1;
+    bool conservative = false, fixed_flux_reservoirs = false;
+    std::vector<double> material_carrier_volumes_a3;
+    long long interface_events = 0, interface_transmitted = 0, interface_reflected = 0;
+    long long absorbed_total = 0, injected_total = 0;
+    double absorbed_energy_ev = 0, injected_energy_ev = 0;
+    long long initial_particle_count = 0, particle_count = 0;
+    double particle_spatial_weight_a3 = 0, background_temperature = 300;
+    double total_thermal_energy_ev = 0, lifetime_residual_ev = 0, balance_residual_ev = 0;
+    bool gradient_driven = false;
+    long long gradient_updates = 0;
+    double gradient_energy_ev = 0;
+    std::string empty_cell_policy = "defer_locally";
+    double source_base_power = 0, source_prescribed = 0, source_pending = 0, source_deposited = 0;
+    long long source_updates_total = 0, source_updates_step = 0;
+    double source_energy_total_ev = 0, source_energy_step_ev = 0;
+};
+std::string format_domain_summary(const SimulationConfig& cfg, const SimulationDomain& domain);
+std::string format_grid_centers(const SimulationDomain& domain);
+std::string format_run_summary(const RunSummary& s);
+std::string format_runtime(long long total_seconds);
 
 } // namespace phmc

@@ -135,6 +135,7 @@ inline SimulationConfig config_from_pod(const phmc_config& c) {
         s.face_value[f] = c.face_value[f];
     }
     if (c.output_folder) s.output_folder = c.output_folder;
+    if (c.material_folder) s.material_folder = c.material_folder;
     s.material_interface_axis = c.material_interface_axis;
     if (c.n_interfaces > 0 && c.material_interface_positions)
         s.material_interface_positions.assign(c.material_interface_positions,

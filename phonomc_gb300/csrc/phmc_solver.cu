@@ -61,6 +61,12 @@ DeviceSolver::DeviceSolver(const SimulationConfig& cfg, const std::vector<const 
     PHMC_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, 0);
     domain_ = std::make_unique<SimulationDomain>(cfg_);
+    if (!cfg_.output_folder.empty()) {
+        // written by the reference's SimulationDomain constructor (src/geometry/DomainOutput.cpp:12-241)
+        std::filesystem::create_directories(cfg_.output_folder);
+        std::ofstream(std::filesystem::path(cfg_.output_folder) / "summary.txt") << format_domain_summary(cfg_, *domain_);
+        std::ofstream(std::filesystem::path(cfg_.output_folder) / "grid_centers.csv") << format_grid_centers(*domain_);
+    }
     if (domain_->is_mesh()) {
         if (mixed_)
             throw std::runtime_error("Mesh domains run with plain FP64 carrier state (precision = fp64); the FP32 "
@@ -910,6 +916,8 @@ void stats_from_ledger(const DevLedger& L, phmc_stats& o) {
     o.interface_events = static_cast<int64_t>(L.total_iface_events);
     o.interface_transmitted = static_cast<int64_t>(L.total_iface_transmitted);
     o.interface_reflected = static_cast<int64_t>(L.total_iface_reflected);
+    for (int k = 0; k < kRoughCounters; ++k) o.rough_counts[k] = static_cast<int64_t>(L.total_rough[k]);
+    o.collision_cache_corrections = static_cast<int64_t>(L.total_cache_corrections);
 }
 
 void DeviceSolver::read_stats(phmc_stats& o) {
@@ -994,15 +1002,63 @@ void DeviceSolver::append_convergence_row(const Observation& o, const phmc_stats
 
 void DeviceSolver::write_outputs() {
     if (cfg_.output_folder.empty()) return;
-    // grid_centers.csv (src/geometry/DomainOutput.cpp): index,x_nm,y_nm,z_nm,volume_nm3
-    std::ofstream g(std::filesystem::path(cfg_.output_folder) / "grid_centers.csv");
-    g << "index,x_nm,y_nm,z_nm,volume_nm3\n";
-    g.precision(10);
-    for (int c = 0; c < ncells_; ++c) {
-        const auto& p = domain_->grid_centers()[c];
-        g << c << ',' << p[0] / 10.0 << ',' << p[1] / 10.0 << ',' << p[2] / 10.0 << ','
-          << domain_->grid_volumes()[c] / 1000.0 << '\n';
+    std::ofstream(std::filesystem::path(cfg_.output_folder) / "grid_centers.csv") << format_grid_centers(*domain_);
+}
+
+// The end of summary.txt (src/main.cpp:117-131, src/solver/Diagnostics.cpp:216-224):
+// run time, then the run diagnostics.
+void DeviceSolver::append_summary(long long total_seconds) {
+    if (cfg_.output_folder.empty()) return;
+    phmc_stats st;
+    read_stats(st);
+    RunSummary r;
+    r.cfg = cfg_;
+    r.random_seed = cfg_.random_seed;
+    r.cache_corrections = st.collision_cache_corrections;
+    // per step: one (cell, class) binning pass; cell temperatures at the
+    // start (from the bins) and at the end of the step
+    r.cell_index_rebuilds = step_ + 1;
+    r.temperature_refreshes = 2LL * step_ + 1;
+    for (int k = 0; k < 8; ++k) r.rough[k] = st.rough_counts[k];
+    r.material_count = static_cast<int>(P_.mats.size());
+    r.interface_frequency_bin_thz = cfg_.material_interface_frequency_bin_thz;
+    r.conservative = P_.conservative;
+    r.fixed_flux_reservoirs = !P_.one_to_one;
+    if (P_.mats.size() > 1) r.material_carrier_volumes_a3 = P_.material_spatial_volume;
+    r.interface_events = st.interface_events;
+    r.interface_transmitted = st.interface_transmitted;
+    r.interface_reflected = st.interface_reflected;
+    r.absorbed_total = st.absorbed_total;
+    r.injected_total = st.injected_total;
+    DevLedger L;
+    PHMC_CUDA(cudaMemcpy(&L, d_ledger_, sizeof L, cudaMemcpyDeviceToHost));
+    r.absorbed_energy_ev = L.total_absorbed_ev;
+    r.injected_energy_ev = L.total_injected_ev;
+    r.initial_particle_count = P_.initial_particles;
+    r.particle_count = st.particle_count;
+    r.particle_spatial_weight_a3 = P_.particle_volume;
+    r.background_temperature = cfg_.background_temperature;
+    r.total_thermal_energy_ev = st.total_thermal_energy_ev;
+    r.lifetime_residual_ev = st.total_lifetime_energy_residual_ev;
+    r.balance_residual_ev = st.total_energy_balance_residual_ev;
+    r.gradient_driven = cfg_.temperature_gradient.has_value();
+    r.gradient_updates = static_cast<long long>(L.total_drive_updates);
+    r.gradient_energy_ev = st.total_gradient_energy_ev;
+    if (P_.source.enabled) {
+        double rate = 0.0;
+        for (double x : P_.source.rates) rate += x;
+        r.source_base_power = rate / 6.241509074e6; // eV/ps per W
+        r.source_prescribed = st.prescribed_heat_source_energy_ev;
+        r.source_pending = st.pending_heat_source_energy_ev;
+        r.source_deposited = st.total_heat_source_energy_ev;
     }
+    r.source_updates_total = static_cast<long long>(L.total_source_updates);
+    r.source_energy_total_ev = st.total_heat_source_energy_ev;
+    r.source_updates_step = st.step_heat_source_updates;
+    r.source_energy_step_ev = st.step_heat_source_energy_ev;
+    std::ofstream out(std::filesystem::path(cfg_.output_folder) / "summary.txt", std::ios::app);
+    out << format_runtime(total_seconds) << format_run_summary(r);
+    if (!out) throw std::runtime_error("Cannot append runtime summary.txt.");
 }
 
 } // namespace phmc

@@ -146,6 +146,7 @@ public:
                       const uint32_t* mode, const uint8_t* alive,
                       bool keep_clock = false);
     void write_outputs();
+    void append_summary(long long total_seconds);
     bool mixed() const { return mixed_; }
     // Deterministic sub-steps on the current population (parity entry points):
     // one collision with the given cell temperatures (or the tallied ones when

@@ -19,6 +19,8 @@ struct BlockLedger {
     unsigned int absorbed;
     unsigned int absorbed_res[kMaxReservoirs];
     unsigned int iface_events, iface_transmitted, iface_reflected;
+    unsigned int rough[kRoughCounters];
+    unsigned int cache_corrections;
 };
 
 __device__ __forceinline__ void block_ledger_init(BlockLedger* b) {
@@ -30,7 +32,16 @@ __device__ __forceinline__ void block_ledger_init(BlockLedger* b) {
         b->absorbed = 0;
         for (int r = 0; r < kMaxReservoirs; ++r) b->absorbed_res[r] = 0;
         b->iface_events = b->iface_transmitted = b->iface_reflected = 0;
+        for (int k = 0; k < kRoughCounters; ++k) b->rough[k] = 0;
+        b->cache_corrections = 0;
     }
+}
+
+// One rough reflection into the block's diagnostics (flags of rough_sample_dev).
+__device__ __forceinline__ void count_rough(BlockLedger* b, unsigned diag) {
+    atomicAdd(&b->rough[kRoughCounters - 1], 1u);
+    for (int k = 0; k < kRoughCounters - 1; ++k)
+        if (diag & (1u << k)) atomicAdd(&b->rough[k], 1u);
 }
 
 __device__ __forceinline__ void block_ledger_flush(BlockLedger* b, DevLedger* L) {
@@ -46,6 +57,10 @@ __device__ __forceinline__ void block_ledger_flush(BlockLedger* b, DevLedger* L)
             atomicAdd(&L->step_drive_updates, b->drive_updates);
         }
         if (b->injected_ev != 0.0) atomicAdd(&L->step_injected_ev, b->injected_ev);
+        for (int k = 0; k < kRoughCounters; ++k)
+            if (b->rough[k]) atomicAdd(&L->total_rough[k], static_cast<unsigned long long>(b->rough[k]));
+        if (b->cache_corrections)
+            atomicAdd(&L->total_cache_corrections, static_cast<unsigned long long>(b->cache_corrections));
         if (b->iface_events) {
             atomicAdd(&L->total_iface_events, static_cast<unsigned long long>(b->iface_events));
             atomicAdd(&L->total_iface_transmitted, static_cast<unsigned long long>(b->iface_transmitted));
@@ -95,6 +110,10 @@ __device__ __forceinline__ void count_interface(BlockLedger* bl, const IfaceOut&
 // carrier was absorbed.
 __device__ bool advance_carrier(const DevTables& T, DevLedger* L, BlockLedger* bl, int slot, double p[3],
                                 uint32_t& w, double& occ, double remaining, uint32_t purpose, uint32_t step) {
+    auto counted_cache = [&](int r) {
+        if (r == 2) atomicAdd(&bl->cache_corrections, 1u);
+        return r != 0;
+    };
     const DevDomain& D = T.dom;
     const DevParams& P = T.par;
     int mid = static_cast<int>(w >> 28);
@@ -103,7 +122,7 @@ __device__ bool advance_carrier(const DevTables& T, DevLedger* L, BlockLedger* b
     mode_velocity(*M, w, v);
     double cp[3], t;
     int f;
-    if (!cache_hit(D, P, p, v, M->speed[w & 0x00FFFFFFu], cp, t, f)) {
+    if (!counted_cache(cache_hit(D, P, p, v, M->speed[w & 0x00FFFFFFu], cp, t, f))) {
         raise_error(L, kErrIntersection, slot);
         return true;
     }
@@ -140,7 +159,7 @@ __device__ bool advance_carrier(const DevTables& T, DevLedger* L, BlockLedger* b
             const double s = M->push[r.active];
 #pragma unroll
             for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], s));
-            if (!cache_hit(D, P, p, v, M->speed[w & 0x00FFFFFFu], cp, t, f)) {
+            if (!counted_cache(cache_hit(D, P, p, v, M->speed[w & 0x00FFFFFFu], cp, t, f))) {
                 raise_error(L, kErrIntersection, slot);
                 return true;
             }
@@ -173,8 +192,10 @@ __device__ bool advance_carrier(const DevTables& T, DevLedger* L, BlockLedger* b
                 const Uniform2 d1 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose,
                                              static_cast<uint32_t>(event), 1);
                 double n_out;
+                unsigned diag;
                 const int out = rough_sample_dev(T.rough[table], *M, ai, occ, P.conservative != 0, d0.a, d0.b, d1.a,
-                                                 n_out);
+                                                 n_out, diag);
+                count_rough(bl, diag);
                 const double nsign = (f & 1) ? 1.0 : -1.0;
                 const double vn = M->vel[3 * out + axis] * nsign;
                 uint32_t signs = 0;
@@ -199,14 +220,14 @@ __device__ bool advance_carrier(const DevTables& T, DevLedger* L, BlockLedger* b
         const double s = M->push[w & 0x00FFFFFFu];
 #pragma unroll
         for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], s));
-        if (!cache_hit(D, P, p, v, M->speed[w & 0x00FFFFFFu], cp, t, f)) {
+        if (!counted_cache(cache_hit(D, P, p, v, M->speed[w & 0x00FFFFFFu], cp, t, f))) {
             raise_error(L, kErrIntersection, slot);
             return true;
         }
         if (t < 1e-12) {
 #pragma unroll
             for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], 1e-12));
-            if (!cache_hit(D, P, p, v, M->speed[w & 0x00FFFFFFu], cp, t, f)) {
+            if (!counted_cache(cache_hit(D, P, p, v, M->speed[w & 0x00FFFFFFu], cp, t, f))) {
                 raise_error(L, kErrIntersection, slot);
                 return true;
             }
@@ -245,13 +266,14 @@ __device__ __forceinline__ void mesh_cache_store(const CarrierState& S, int slot
 }
 
 // Trace from p (nudged retries may move it) into the cache; false after raising an error.
-__device__ __forceinline__ bool mesh_refresh(const DevTables& T, DevLedger* L, int slot, double p[3], const double v[3],
-                                             MeshCache& c) {
+__device__ __forceinline__ bool mesh_refresh(const DevTables& T, DevLedger* L, BlockLedger* bl, int slot, double p[3],
+                                             const double v[3], MeshCache& c) {
     double cp[3], t;
     int f;
     const int r = mesh_cache_hit(T.fac, T.dom, T.par, p, v, cp, t, f);
     c.loaded = c.dirty = true;
-    if (r != 0) {
+    if (r == 3 && bl) atomicAdd(&bl->cache_corrections, 1u);
+    if (r != 0 && r != 3) {
         raise_error(L, r == 2 ? kErrInvalidStatistics : kErrIntersection, slot);
         c.t = __longlong_as_double(0x7ff0000000000000LL);
         c.f = -1;
@@ -317,7 +339,9 @@ __device__ bool advance_carrier_mesh(const DevTables& T, DevLedger* L, BlockLedg
             const Uniform2 d0 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose, static_cast<uint32_t>(event), 0);
             const Uniform2 d1 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose, static_cast<uint32_t>(event), 1);
             double n_out;
-            const int out = rough_sample_dev(F.rough[table], M, ai, occ, P.conservative != 0, d0.a, d0.b, d1.a, n_out);
+            unsigned diag;
+            const int out = rough_sample_dev(F.rough[table], M, ai, occ, P.conservative != 0, d0.a, d0.b, d1.a, n_out, diag);
+            count_rough(bl, diag);
             const double* nf = F.normal + 3 * f;
             const double vo[3] = {M.vel[3 * out], M.vel[3 * out + 1], M.vel[3 * out + 2]};
             const double nn[3] = {nf[0], nf[1], nf[2]};
@@ -338,11 +362,11 @@ __device__ bool advance_carrier_mesh(const DevTables& T, DevLedger* L, BlockLedg
         const double s = P.push_eps / fmax(meshmath::norm(v), 1e-12);
 #pragma unroll
         for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], s));
-        if (!mesh_refresh(T, L, slot, p, v, c)) return true;
+        if (!mesh_refresh(T, L, bl, slot, p, v, c)) return true;
         if (dmul(c.t, dt) < 1e-12) {
 #pragma unroll
             for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], 1e-12));
-            if (!mesh_refresh(T, L, slot, p, v, c)) return true;
+            if (!mesh_refresh(T, L, bl, slot, p, v, c)) return true;
         }
     }
     if (remaining > 1e-14) raise_error(L, kErrTooManyEvents, slot);
@@ -359,7 +383,7 @@ __global__ void k_mesh_cache_init(const __grid_constant__ DevTables T, CarrierSt
         mesh_velocity(T.fac, T.mat[w >> 28], w, S.mirror[i], v);
         double p[3] = {S.x[i], S.y[i], S.z[i]};
         MeshCache c;
-        mesh_refresh(T, L, i, p, v, c);
+        mesh_refresh(T, L, nullptr, i, p, v, c);
         S.x[i] = p[0];
         S.y[i] = p[1];
         S.z[i] = p[2];
@@ -442,8 +466,8 @@ __device__ __forceinline__ void mode_velocity32(const DevMaterial& M, uint32_t w
 // occupation from the wall's table with the draws of (slot, step, purpose,
 // event). False when the event raised an error (the carrier then stays where
 // it is, as the reference stops its flight with the throw).
-__device__ __forceinline__ bool wall_sample_mixed(const DevTables& T, DevLedger* L, int slot, int plane, uint32_t& w,
-                                                  double& occ, int event, uint32_t purpose, uint32_t step) {
+__device__ __forceinline__ bool wall_sample_mixed(const DevTables& T, DevLedger* L, BlockLedger* bl, int slot, int plane,
+                                                  uint32_t& w, double& occ, int event, uint32_t purpose, uint32_t step) {
     const DevDomain& D = T.dom;
     const DevParams& P = T.par;
     const int mid = static_cast<int>(w >> 28);
@@ -458,7 +482,9 @@ __device__ __forceinline__ bool wall_sample_mixed(const DevTables& T, DevLedger*
     const Uniform2 d0 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose, static_cast<uint32_t>(event), 0);
     const Uniform2 d1 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose, static_cast<uint32_t>(event), 1);
     double n_out;
-    const int out = rough_sample_dev(T.rough[table], M, ai, occ, P.conservative != 0, d0.a, d0.b, d1.a, n_out);
+    unsigned diag;
+    const int out = rough_sample_dev(T.rough[table], M, ai, occ, P.conservative != 0, d0.a, d0.b, d1.a, n_out, diag);
+    count_rough(bl, diag);
     const double vn = M.vel[3 * out + axis] * ((plane & 1) ? 1.0 : -1.0);
     uint32_t signs = 0;
     if (P.conservative) {
@@ -610,7 +636,7 @@ __device__ __forceinline__ int advance_mixed(const DevTables& T, DevLedger* L, B
                 plane_out = plane;
                 return kFlightDeferred;
             }
-            if (!wall_sample_mixed(T, L, slot, plane, w, occ, event, purpose, step)) return kFlightDone;
+            if (!wall_sample_mixed(T, L, bl, slot, plane, w, occ, event, purpose, step)) return kFlightDone;
         } else if (cond == 'R') {
             raise_error(L, kErrNoRoughTable, slot);
             return kFlightDone;
@@ -909,7 +935,7 @@ __global__ void __launch_bounds__(kTransportThreads) k_deferred(const __grid_con
         if (plane >= kDeferInterface && plane < kDeferInterface + kMaxMaterials)
             resumed = interface_step_mixed(T, L, &bl, i, plane - kDeferInterface, w, occ, event, kDrawTransport, step);
         else if (plane >= 0 && plane < 6)
-            resumed = wall_sample_mixed(T, L, i, plane, w, occ, event, kDrawTransport, step);
+            resumed = wall_sample_mixed(T, L, &bl, i, plane, w, occ, event, kDrawTransport, step);
         if (resumed) {
             ++event;
             int unused = -1;
@@ -1196,7 +1222,7 @@ __global__ void __launch_bounds__(256) k_inject(const DevTables* __restrict__ Tp
         } else if (kMesh) {
             int mir = -1;
             MeshCache mc;
-            mesh_refresh(T, L, slot, p, v, mc); // src/MonteCarloSolver.cpp:318-327
+            mesh_refresh(T, L, &bl, slot, p, v, mc); // src/MonteCarloSolver.cpp:318-327
             if (remain > 1e-14)
                 alive = advance_carrier_mesh(T, L, &bl, S, slot, p, w, mir, occ, mc, remain, kDrawInjected, step);
             S.mirror[slot] = mir;

@@ -73,3 +73,32 @@ def test_region_errors(tmp_path):
     cfg["mesh"] = dict(cfg["mesh"], regions=cfg["mesh"]["regions"] + [((0.5, 0.5, -1.0, 0.5, 0.5, -0.9), "T", 300.0)])
     with pytest.raises(abi.LibError, match="did not match any mesh facet"):
         abi.Domain(native.lib(), cfg)
+
+
+def test_domain_summary_and_grid_centers(tmp_path):
+    """summary.txt (domain part) and grid_centers.csv as the reference's
+    SimulationDomain writes them for the FinFET TOML; only the paths differ."""
+    from phonomc_gb300 import abi, native, workloads
+    g = golden("domain_finfet")
+    stl = workloads.finfet_stl(str(tmp_path / "finfet.stl"))
+    out = tmp_path / "out"
+    cfg = workloads.finfet_mesh(stl, particles=2000, seed=5)
+    cfg.update(iterations=1, convergence_write_interval=1, output_folder=str(out), material_folder="unused")
+    d = abi.Domain(native.lib(), cfg)
+    mine = (out / "summary.txt").read_text().splitlines()
+    ref = g["domain_summary"].splitlines()
+    path_keys = ("model = ", "output_folder = ", "grid_centers_csv = ")
+    assert len(mine) == len(ref)
+    for a, b in zip(mine, ref):
+        if a.startswith(path_keys):
+            assert a.split(" = ")[0] == b.split(" = ")[0]
+        else:
+            assert a == b
+    rows = (out / "grid_centers.csv").read_text().splitlines()
+    assert rows[0] == "index,x_nm,y_nm,z_nm,volume_nm3"
+    C, V = g["grid_centers"], g["grid_volumes"]
+    assert len(rows) == len(C) + 1
+    for i in (0, 1, len(C) // 2, len(C) - 1):
+        c = C[i]
+        assert rows[i + 1] == "%d,%g,%g,%g,%g" % (i, c[0] / 10.0, c[1] / 10.0, c[2] / 10.0, V[i] / 1000.0)
+    d.close()
