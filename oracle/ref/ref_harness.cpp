@@ -11,6 +11,8 @@
 //
 // Output is JSON on stdout (numbers with 17 significant digits).
 #include "MonteCarloSolver.h"
+#include <memory>
+#include <sstream>
 #include "PhononMaterial.h"
 #include "SimulationConfig.h"
 #include "SimulationDomain.h"
@@ -854,13 +856,20 @@ std::string cmd_reservoir(const std::string& pmat) {
 }
 
 // run <pmat> <toml> <steps>: full reference solver; prints per-step observables.
+// <pmat> may list several tables separated by commas (layered materials, in order).
 std::string cmd_run(const std::string& pmat, const std::string& toml, int steps) {
     SimulationConfig a = load_simulation_config(toml);
     const bool stationary = uses_conservative_transport(a);
-    PhononMaterial m(read_pmat(pmat), a.temperature_lookup_dt, stationary,
-                     a.collision_model == CollisionModel::Callaway);
+    std::vector<std::unique_ptr<PhononMaterial>> owned;
+    std::vector<std::reference_wrapper<const PhononMaterial>> mats;
+    std::stringstream list(pmat);
+    for (std::string item; std::getline(list, item, ',');) {
+        owned.push_back(std::make_unique<PhononMaterial>(read_pmat(item), a.temperature_lookup_dt, stationary,
+                                                         a.collision_model == CollisionModel::Callaway));
+        mats.push_back(*owned.back());
+    }
     SimulationDomain d(a);
-    MonteCarloSolver s(a, d, m);
+    MonteCarloSolver s(a, d, mats);
     std::vector<double> pc, absorbed, injected, flux, energy, resid, source;
     while (s.current_timestep() < steps) {
         s.run_timestep();
@@ -906,6 +915,9 @@ std::string cmd_run(const std::string& pmat, const std::string& toml, int steps)
     j.arr("heat_source_total", source);
     j.put("lifetime_residual_total", s.total_lifetime_energy_residual_ev());
     j.put("gradient_energy_total", s.total_gradient_energy_ev());
+    j.put_i("interface_events", s.interface_event_count());
+    j.put_i("interface_transmitted", s.interface_transmitted_count());
+    j.put_i("interface_reflected", s.interface_reflected_count());
     return j.str();
 }
 } // namespace

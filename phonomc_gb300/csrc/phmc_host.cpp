@@ -941,6 +941,24 @@ Problem build_problem(const SimulationConfig& cfg, SimulationDomain& domain,
     P.cell_material.resize(domain.grid_count());
     for (int c = 0; c < domain.grid_count(); ++c) P.cell_material[c] = P.layout.material_at(domain.grid_centers()[c]);
     if (mats.size() > 1) validate_layout(P, cfg, domain, static_cast<int>(mats.size()));
+    // Carrier volumes (src/MonteCarloSolver.cpp:80-100): one volume V/N for a
+    // single material; layered crystals sample carriers in proportion to each
+    // material's active-state density with one common state weight, so a
+    // carrier of material m stands for common / density_m of space.
+    P.material_spatial_volume.assign(mats.size(), P.particle_volume);
+    if (mats.size() > 1) {
+        std::vector<double> density(mats.size());
+        for (size_t m = 0; m < mats.size(); ++m)
+            density[m] = mats[m]->active_mode_count() / mats[m]->energy_density_normalization();
+        double states = 0.0;
+        for (int c = 0; c < domain.grid_count(); ++c) states += domain.grid_volumes()[c] * density[P.cell_material[c]];
+        const double common = states / P.initial_particles;
+        for (size_t m = 0; m < mats.size(); ++m) {
+            if (!(density[m] > 0.0) || !std::isfinite(density[m]))
+                throw std::runtime_error("Invalid material phase-space density.");
+            P.material_spatial_volume[m] = common / density[m];
+        }
+    }
 
     int axis = 0;
     if (cfg.transport_axis >= 0) axis = cfg.transport_axis;
@@ -983,7 +1001,7 @@ Problem build_problem(const SimulationConfig& cfg, SimulationDomain& domain,
             T.capacity_bg[a] = M.mode_heat_capacity(Tbg, f);
         }
         // BackgroundCache (include/solver/BackgroundCache.h:13-31)
-        T.energy_weight = static_cast<double>(na) * P.particle_volume / M.energy_density_normalization();
+        T.energy_weight = static_cast<double>(na) * P.material_spatial_volume[mid] / M.energy_density_normalization();
         T.energy_density_bg = P.linearized ? M.crystal_energy_density(Tbg) : M.energy_density_from_temperature(Tbg);
         T.heat_capacity_density_bg = 0.0;
         for (int f = 0; f < M.flat_count(); ++f)
@@ -1102,12 +1120,14 @@ Problem build_problem(const SimulationConfig& cfg, SimulationDomain& domain,
     }
 
     // Reservoirs (src/solver/ReservoirInitialization.cpp:1-45, ReservoirSampler.cpp:17-101).
-    const double density = static_cast<double>(P.initial_particles) / domain.volume();
     for (int f : domain.reservoir_facets()) {
         const Facet& F = domain.facets()[f];
         Reservoir R;
         R.facet = f;
         R.material = P.layout.material_at(F.centroid);
+        // carriers per unit volume of the reservoir's material (src/solver/ReservoirInitialization.cpp:18-23)
+        const double density = mats.size() > 1 ? 1.0 / P.material_spatial_volume[R.material]
+                                               : static_cast<double>(P.initial_particles) / domain.volume();
         R.temperature = F.value;
         R.area = F.area;
         R.normal = F.normal;
@@ -1185,6 +1205,7 @@ CarrierArrays initial_carriers(const Problem& p, const std::vector<const PhononM
         if (!simplex_cum.empty() && !(run > 0.0)) simplex_cum.clear();
     }
     int rejected = -1;
+    const double smallest_volume = *std::min_element(p.material_spatial_volume.begin(), p.material_spatial_volume.end());
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < n; ++i) {
         const Uniform2 u0 = uniform2(seed, static_cast<uint32_t>(i), 0xFFFFFFFFu, kDrawInit, 0, 0);
@@ -1215,9 +1236,28 @@ CarrierArrays initial_carriers(const Problem& p, const std::vector<const PhononM
                 rejected = i;
             }
         }
+        double mode_u = u1.b;
+        if (p.mats.size() > 1) {
+            // keep a point of material m with probability smallest volume / volume_m
+            // (src/solver/Initialization.cpp:48-65)
+            for (uint32_t trial = 0;; ++trial) {
+                const int m = p.layout.material_at(pos);
+                const Uniform2 acc = uniform2(seed, static_cast<uint32_t>(i), 0xFFFFFFFFu, kDrawInit, trial, 3);
+                if (acc.a < smallest_volume / p.material_spatial_volume[m]) break;
+                if (trial + 1 >= 100000u) {
+#pragma omp critical
+                    rejected = i;
+                    break;
+                }
+                const Uniform2 r0 = uniform2(seed, static_cast<uint32_t>(i), 0xFFFFFFFFu, kDrawInit, trial + 1, 0);
+                const Uniform2 r1 = uniform2(seed, static_cast<uint32_t>(i), 0xFFFFFFFFu, kDrawInit, trial + 1, 1);
+                pos = {lo[0] + (hi[0] - lo[0]) * r0.a, lo[1] + (hi[1] - lo[1]) * r0.b, lo[2] + (hi[2] - lo[2]) * r1.a};
+                mode_u = r1.b;
+            }
+        }
         const int mid = p.layout.material_at(pos);
         const MaterialTables& T = p.mats[mid];
-        int a = static_cast<int>(u1.b * T.n_active);
+        int a = static_cast<int>(mode_u * T.n_active);
         if (a >= T.n_active) a = T.n_active - 1;
         double temp = p.cfg.initial_temperature;
         if (linear) {
@@ -1237,7 +1277,7 @@ CarrierArrays initial_carriers(const Problem& p, const std::vector<const PhononM
         c.occ[i] = p.linearized ? mats[mid]->linearized_bose_occupation(temp, p.cfg.background_temperature, flat)
                                 : mats[mid]->bose_occupation(temp, flat);
     }
-    if (rejected >= 0) throw std::runtime_error("sample_volume_points_naive: insufficient accepted samples.");
+    if (rejected >= 0) throw std::runtime_error("Initial carrier sampling found no accepted position.");
     return c;
 }
 

@@ -206,6 +206,87 @@ def full_runs_finfet(mpath: str, fpath: str, tmp: str) -> dict:
     return out
 
 
+# Full reference runs of a scaled bilayer (phonomc_gb300.workloads.bilayer_callaway
+# at 2e4 carriers, 20 cells; 8^3 Callaway tables, the second material softened):
+# per seed, late-time means (steps 101-200) of the cell temperatures, heat flux,
+# kappa_eff and carrier count, and the interface counts over the run.
+BILAYER_SEEDS = 16
+BILAYER_PARTICLES = 20000
+BILAYER_STEPS = 200
+BILAYER_CELLS = 20
+BILAYER_TOML = """[geometry]
+model = "box"
+sizes = [100, 100, 200]
+
+[simulation]
+particle_count = {particles}
+time_step = 0.5
+iterations = {steps}
+random_seed = {seed}
+compute_kappa = true
+transport_axis = "z"
+initial_temperature = "linear"
+background_temperature = 300
+lifetime_temperature = 300
+grid_xyz = [1, 1, {cells}]
+convergence_write_interval = 1
+
+[scattering]
+model = "callaway"
+
+[boundary]
+boundary_position = [
+  [-0.01,0,0,0.01,1,1], [0.99,0,0,1.01,1,1],
+  [0,-0.01,0,1,0.01,1], [0,0.99,0,1,1.01,1],
+  [0,0,-0.01,1,1,0.01], [0,0,0.99,1,1,1.01]
+]
+boundary_conditions = ["P","P","P","P","T","T"]
+boundary_values = [0,0,0,0,310,290]
+periodic_pair = [
+  [-0.01,0,0,0.01,1,1], [0.99,0,0,1.01,1,1],
+  [0,-0.01,0,1,0.01,1], [0,0.99,0,1,1.01,1]
+]
+
+[materials]
+folders = ["a", "b"]
+interface_axis = "z"
+interface_positions = [100]
+interface_model = "dmm"
+
+[io]
+material_folder = "unused"
+output_folder = "{out}"
+"""
+
+
+def full_runs_bilayer(pmats: str, tmp: str) -> dict:
+    import numpy as np
+    out = {"seeds": [], "particles": BILAYER_PARTICLES, "steps": BILAYER_STEPS, "cells": BILAYER_CELLS,
+           "average_from_step": BILAYER_STEPS // 2 + 1}
+    nc = BILAYER_CELLS
+    for k in range(BILAYER_SEEDS):
+        seed = 101 + k
+        folder = os.path.join(tmp, f"bl{seed}")
+        os.makedirs(folder, exist_ok=True)
+        toml = os.path.join(folder, "c5.toml")
+        with open(toml, "w") as f:
+            f.write(BILAYER_TOML.format(particles=BILAYER_PARTICLES, steps=BILAYER_STEPS, seed=seed, cells=nc,
+                                        out=folder))
+        res = json.loads(subprocess.run([HARNESS, "run", pmats, toml, str(BILAYER_STEPS)], check=True,
+                                        capture_output=True, text=True).stdout)
+        rows = np.asarray(res["convergence"])
+        late = rows[rows[:, 0] >= out["average_from_step"]]
+        out["seeds"].append(seed)
+        out.setdefault("T_mean", []).append(late[:, 2:2 + nc].mean(axis=0).tolist())
+        out.setdefault("flux_mean", []).append(float(late[:, 2 + nc].mean()))
+        out.setdefault("kappa_eff_mean", []).append(float(late[:, 4 + nc].mean()))
+        out.setdefault("particles_mean", []).append(float(late[:, 5 + nc].mean()))
+        out.setdefault("interface_events", []).append(res["interface_events"])
+        out.setdefault("interface_transmitted", []).append(res["interface_transmitted"])
+        out.setdefault("balance_residual_total", []).append(res["balance_residual_total"][-1])
+    return out
+
+
 def build(ref: str) -> None:
     subprocess.run(["make", "-s", "-j8", f"REF={ref}"], cwd=os.path.join(ROOT, "oracle", "ref"),
                    check=True)
@@ -238,6 +319,14 @@ def main() -> None:
         with gzip.open(os.path.join(HERE, "fullrun_cross_plane.json.gz"), "wt") as f:
             json.dump(data, f)
         print("fullrun_cross_plane ok")
+    if not args.only or "fullrun_bilayer" in args.only:
+        cs = os.path.join(tmp, "m8cs.pmat")
+        synthetic.write_pmat(cs, synthetic.make_material(mesh=8, freq_scale=0.7, vel_scale=0.75, callaway=True))
+        data = full_runs_bilayer(cpath + "," + cs, os.path.join(tmp, "fullrun_bilayer"))
+        data["_harness_args"] = ["run", "{c},{cs}", "<bilayer toml>", str(BILAYER_STEPS)]
+        with gzip.open(os.path.join(HERE, "fullrun_bilayer.json.gz"), "wt") as f:
+            json.dump(data, f)
+        print("fullrun_bilayer ok")
     if not args.only or "fullrun_finfet" in args.only:
         data = full_runs_finfet(mpath, fpath, os.path.join(tmp, "fullrun_finfet"))
         data["_harness_args"] = ["run", "{m}", "<FinFET toml>", str(FINFET_STEPS)]

@@ -144,7 +144,8 @@ def _compare(sg, so, tol=1e-12):
     assert np.allclose(Tg, To, rtol=tol, atol=0)
     assert np.allclose(Eg, Eo, rtol=tol, atol=0)
     stg, sto = sg.stats(), so.stats()
-    for k in ("particle_count", "absorbed_total", "injected_total", "step_absorbed", "step_injected"):
+    for k in ("particle_count", "absorbed_total", "injected_total", "step_absorbed", "step_injected",
+              "collision_cache_corrections", "rough_counts"):
         assert stg[k] == sto[k], k
     for k in ("total_thermal_energy_ev", "step_absorbed_energy_ev", "step_injected_energy_ev"):
         assert abs(stg[k] - sto[k]) <= 1e-10 * max(1.0, abs(sto[k])), k

@@ -96,3 +96,34 @@ def test_finfet_statistics(gpu, tmp_path):
     assert np.allclose(runs["source_total_end"], g["source_total_end"], rtol=1e-9), (
         runs["source_total_end"], g["source_total_end"])
     assert max(runs["balance_residual_total"]) < 1e-6
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_bilayer_statistics(gpu, precision):
+    """Callaway bilayer with a DMM interface (tests/golden/fullrun_bilayer)."""
+    g = golden("fullrun_bilayer")
+    mats = [abi.Material(gpu, "phmc_", d, 0.1, True, True) for d in workloads.bilayer_materials(8)]
+    T_mean, flux, trans, resid = [], [], [], []
+    for k in range(len(g["seeds"])):
+        cfg = workloads.scaled(workloads.bilayer_callaway(precision=precision), g["particles"], random_seed=9101 + k,
+                               grid=(1, 1, g["cells"]), convergence_write_interval=1)
+        s = abi.Solver(gpu, "phmc_", cfg, mats)
+        T_acc, f_acc = [], []
+        for step in range(1, g["steps"] + 1):
+            s.run(1)
+            if step >= g["average_from_step"]:
+                T_acc.append(s.cells()[0])
+                f_acc.append(s.stats()["average_heat_flux_along_axis"])
+        st = s.stats()
+        T_mean.append(np.mean(T_acc, axis=0))
+        flux.append(np.mean(f_acc))
+        trans.append(st["interface_transmitted"] / max(1, st["interface_events"]))
+        resid.append(abs(st["total_energy_balance_residual_ev"]))
+        s.close()
+    z = _z(T_mean, g["T_mean"])
+    assert np.all(np.abs(z) < 4.5), z
+    assert np.mean(z * z) < 2.5, np.mean(z * z)
+    assert abs(_z(np.asarray(flux)[:, None], np.asarray(g["flux_mean"])[:, None])[0]) < 3.5
+    tr_ref = np.array(g["interface_transmitted"]) / np.array(g["interface_events"])
+    assert abs(_z(np.asarray(trans)[:, None], tr_ref[:, None])[0]) < 3.5
+    assert max(resid) < 1e-6

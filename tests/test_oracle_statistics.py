@@ -59,3 +59,40 @@ def test_oracle_matches_reference_statistics():
     # energy bookkeeping closes to round-off in both (eV, total over the run)
     assert max(abs(r[3]) for r in res) < 1e-6
     assert max(abs(x) for x in g["balance_residual_total"]) < 1e-6
+
+
+def _oracle_bilayer(seed):
+    import oracle
+    from phonomc_gb300 import abi, synthetic, workloads
+    lib = oracle.load()
+    g = golden("fullrun_bilayer")
+    cfg = workloads.scaled(workloads.bilayer_callaway(), g["particles"], random_seed=seed, grid=(1, 1, g["cells"]),
+                           convergence_write_interval=1)
+    mats = [abi.Material(lib, "orc_", d, 0.1, True, True) for d in workloads.bilayer_materials(8)]
+    s = abi.Solver(lib, "orc_", cfg, mats)
+    T, flux = [], []
+    for step in range(1, g["steps"] + 1):
+        s.run(1)
+        if step >= g["average_from_step"]:
+            T.append(s.cells()[0])
+            flux.append(s.stats()["average_heat_flux_along_axis"])
+    st = s.stats()
+    return (np.mean(T, axis=0), float(np.mean(flux)), st["interface_transmitted"] / max(1, st["interface_events"]),
+            st["total_energy_balance_residual_ev"])
+
+
+def test_oracle_matches_reference_bilayer_statistics():
+    """Two Callaway crystals with a DMM interface (carriers in proportion to each
+    crystal's state density, one common weight): the reference's 16 runs against
+    16 oracle runs -- cell temperatures on both sides of the interface jump, heat
+    flux and the interface transmission ratio."""
+    g = golden("fullrun_bilayer")
+    with mp.get_context("spawn").Pool(8) as pool:
+        res = pool.map(_oracle_bilayer, [5001 + k for k in range(len(g["seeds"]))])
+    z = _z(np.array([r[0] for r in res]), np.array(g["T_mean"]))
+    assert np.all(np.abs(z) < 4.5), z
+    assert np.mean(z * z) < 2.5, np.mean(z * z)
+    assert abs(_z(np.array([r[1] for r in res])[:, None], np.array(g["flux_mean"])[:, None])[0]) < 3.5
+    tr_ref = np.array(g["interface_transmitted"]) / np.array(g["interface_events"])
+    assert abs(_z(np.array([r[2] for r in res])[:, None], tr_ref[:, None])[0]) < 3.5
+    assert max(abs(r[3]) for r in res) < 1e-6
