@@ -265,6 +265,13 @@ struct DevFacets {
     int n_simplex;                 // star decomposition (0: ray cast only)
     const double* simplex;         // [n_simplex][18]: apex xyz, inverse 3x3 row-major, bounds min xyz, max xyz
     double ray_pad;                // padding of the BVH culling in the membership ray cast
+    // per-carrier mesh state (kept here so the carrier-state kernel parameter stays small):
+    int32_t* mirror;               // facet whose mirror applies to the mode velocity, -1 none
+    double* hit_t;                 // wall cache: time to the wall in units of dt
+    double* hit_x;                 //   cached hit point
+    double* hit_y;
+    double* hit_z;
+    int32_t* hit_f;                //   cached facet
 };
 
 struct DevTables {
@@ -288,12 +295,6 @@ struct CarrierState {
     uint32_t* mode;
     int32_t* cell;
     uint8_t* alive;
-    int32_t* mirror; // mesh domains: facet whose mirror applies to the mode velocity, -1 none (else null)
-    double* hit_t;   // mesh domains: wall cache, time to the wall in units of dt
-    double* hit_x;   //   cached hit point
-    double* hit_y;
-    double* hit_z;
-    int32_t* hit_f;  //   cached facet
     int4* deferred; // mixed path: queued wall events (slot, time left, event, wall), capacity entries
     int capacity;
 };

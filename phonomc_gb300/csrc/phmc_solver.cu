@@ -124,13 +124,14 @@ void DeviceSolver::allocate_state(int capacity) {
         state_.deferred = dalloc<int4>(capacity);
     }
     if (domain_->is_mesh()) {
-        state_.mirror = dalloc<int32_t>(capacity);
-        PHMC_CUDA(cudaMemsetAsync(state_.mirror, 0xFF, static_cast<size_t>(capacity) * sizeof(int32_t), stream_));
-        state_.hit_t = dalloc<double>(capacity);
-        state_.hit_x = dalloc<double>(capacity);
-        state_.hit_y = dalloc<double>(capacity);
-        state_.hit_z = dalloc<double>(capacity);
-        state_.hit_f = dalloc<int32_t>(capacity);
+        // per-carrier mesh state lives in the facet tables (tables_.fac), filled by upload_mesh
+        mesh_mirror_ = dalloc<int32_t>(capacity);
+        PHMC_CUDA(cudaMemsetAsync(mesh_mirror_, 0xFF, static_cast<size_t>(capacity) * sizeof(int32_t), stream_));
+        mesh_hit_t_ = dalloc<double>(capacity);
+        mesh_hit_x_ = dalloc<double>(capacity);
+        mesh_hit_y_ = dalloc<double>(capacity);
+        mesh_hit_z_ = dalloc<double>(capacity);
+        mesh_hit_f_ = dalloc<int32_t>(capacity);
         state_.deferred = dalloc<int4>(capacity); // wall-event queue of the mesh transport
     }
     state_.occ = dalloc<double>(capacity);
@@ -517,6 +518,12 @@ void DeviceSolver::upload_mesh(const std::vector<DevRoughTable>& rough) {
     fill_dev_facets(*domain_, tables_.dom.scale, G, [&](const auto& v) { return upload(v); });
     G.rough_table = upload(P_.rough.facet_table);
     G.rough = upload(rough);
+    G.mirror = mesh_mirror_;
+    G.hit_t = mesh_hit_t_;
+    G.hit_x = mesh_hit_x_;
+    G.hit_y = mesh_hit_y_;
+    G.hit_z = mesh_hit_z_;
+    G.hit_f = mesh_hit_f_;
 }
 
 LaunchCtx DeviceSolver::ctx() const {

@@ -168,6 +168,10 @@ public:
 private:
     void upload_tables();
     void upload_mesh(const std::vector<DevRoughTable>& rough);
+    // mesh domains: per-carrier mirror facet and wall cache (device arrays)
+    int32_t* mesh_mirror_ = nullptr;
+    double *mesh_hit_t_ = nullptr, *mesh_hit_x_ = nullptr, *mesh_hit_y_ = nullptr, *mesh_hit_z_ = nullptr;
+    int32_t* mesh_hit_f_ = nullptr;
     void allocate_state(int capacity);
     void initial_statistics();
     void enqueue_step(bool profile);

@@ -246,22 +246,22 @@ struct MeshCache {
     bool loaded, dirty;
 };
 
-__device__ __forceinline__ void mesh_cache_load(const CarrierState& S, int slot, MeshCache& c) {
+__device__ __forceinline__ void mesh_cache_load(const DevFacets& F, int slot, MeshCache& c) {
     if (c.loaded) return;
-    c.x = S.hit_x[slot];
-    c.y = S.hit_y[slot];
-    c.z = S.hit_z[slot];
-    c.f = S.hit_f[slot];
+    c.x = F.hit_x[slot];
+    c.y = F.hit_y[slot];
+    c.z = F.hit_z[slot];
+    c.f = F.hit_f[slot];
     c.loaded = true;
 }
 
-__device__ __forceinline__ void mesh_cache_store(const CarrierState& S, int slot, const MeshCache& c) {
-    S.hit_t[slot] = c.t;
+__device__ __forceinline__ void mesh_cache_store(const DevFacets& F, int slot, const MeshCache& c) {
+    F.hit_t[slot] = c.t;
     if (c.dirty) {
-        S.hit_x[slot] = c.x;
-        S.hit_y[slot] = c.y;
-        S.hit_z[slot] = c.z;
-        S.hit_f[slot] = c.f;
+        F.hit_x[slot] = c.x;
+        F.hit_y[slot] = c.y;
+        F.hit_z[slot] = c.z;
+        F.hit_f[slot] = c.f;
     }
 }
 
@@ -292,8 +292,7 @@ __device__ __forceinline__ bool mesh_refresh(const DevTables& T, DevLedger* L, B
 // outward mode velocity is mirrored in the facet plane (`mir`), the push along
 // the velocity actually carried, then a fresh cache
 // (src/solver/TransportOperator.cpp:287-361, 405-466).
-__device__ bool advance_carrier_mesh(const DevTables& T, DevLedger* L, BlockLedger* bl, const CarrierState& S,
-                                     int slot, double p[3], uint32_t& w, int& mir, double& occ, MeshCache& c,
+__device__ bool advance_carrier_mesh(const DevTables& T, DevLedger* L, BlockLedger* bl, int slot, double p[3], uint32_t& w, int& mir, double& occ, MeshCache& c,
                                      double remaining, uint32_t purpose, uint32_t step) {
     const DevFacets& F = T.fac;
     const DevParams& P = T.par;
@@ -312,7 +311,7 @@ __device__ bool advance_carrier_mesh(const DevTables& T, DevLedger* L, BlockLedg
             return true;
         }
         remaining -= fmax(0.0, t_wall);
-        mesh_cache_load(S, slot, c);
+        mesh_cache_load(F, slot, c);
         p[0] = c.x;
         p[1] = c.y;
         p[2] = c.z;
@@ -380,14 +379,14 @@ __global__ void k_mesh_cache_init(const __grid_constant__ DevTables T, CarrierSt
         if (!S.alive[i]) continue;
         const uint32_t w = S.mode[i];
         double v[3];
-        mesh_velocity(T.fac, T.mat[w >> 28], w, S.mirror[i], v);
+        mesh_velocity(T.fac, T.mat[w >> 28], w, T.fac.mirror[i], v);
         double p[3] = {S.x[i], S.y[i], S.z[i]};
         MeshCache c;
         mesh_refresh(T, L, nullptr, i, p, v, c);
         S.x[i] = p[0];
         S.y[i] = p[1];
         S.z[i] = p[2];
-        mesh_cache_store(S, i, c);
+        mesh_cache_store(T.fac, i, c);
     }
 }
 
@@ -828,14 +827,14 @@ __global__ void __launch_bounds__(kTransportThreads) k_transport_mesh(const __gr
             const uint32_t w = __ldcs(S.mode + i);
             const int c0 = __ldcs(S.cell + i);
             const double occ = apply_pending(T, C, c0, w, __ldcs(S.occ + i));
-            const double ht = __ldcs(S.hit_t + i);
+            const double ht = __ldcs(T.fac.hit_t + i);
             const double t_wall = dmul(ht, dt);
             if (!isfinite(t_wall) || t_wall > dt) {
                 double v[3];
-                mesh_velocity(T.fac, T.mat[w >> 28], w, __ldcs(S.mirror + i), v);
+                mesh_velocity(T.fac, T.mat[w >> 28], w, __ldcs(T.fac.mirror + i), v);
                 const double p[3] = {dadd(__ldcs(S.x + i), dmul(v[0], dt)), dadd(__ldcs(S.y + i), dmul(v[1], dt)),
                                      dadd(__ldcs(S.z + i), dmul(v[2], dt))};
-                if (isfinite(ht)) __stcs(S.hit_t + i, dadd(ht, -(dt / dt)));
+                if (isfinite(ht)) __stcs(T.fac.hit_t + i, dadd(ht, -(dt / dt)));
                 const int c = cell_at(T, p[0], p[1], p[2]);
                 __stcs(S.x + i, p[0]);
                 __stcs(S.y + i, p[1]);
@@ -881,14 +880,14 @@ __global__ void __launch_bounds__(kTransportThreads, 1) k_mesh_events(const __gr
         uint32_t w = S.mode[i];
         double occ = S.occ[i];
         double p[3] = {S.x[i], S.y[i], S.z[i]};
-        const int mir0 = S.mirror[i];
+        const int mir0 = T.fac.mirror[i];
         int mir = mir0;
         MeshCache mc;
-        mc.t = S.hit_t[i];
+        mc.t = T.fac.hit_t[i];
         mc.loaded = mc.dirty = false;
-        const bool alive = advance_carrier_mesh(T, L, &bl, S, i, p, w, mir, occ, mc, T.par.dt, kDrawTransport, step);
-        if (mir != mir0) S.mirror[i] = mir;
-        mesh_cache_store(S, i, mc);
+        const bool alive = advance_carrier_mesh(T, L, &bl, i, p, w, mir, occ, mc, T.par.dt, kDrawTransport, step);
+        if (mir != mir0) T.fac.mirror[i] = mir;
+        mesh_cache_store(T.fac, i, mc);
         S.x[i] = p[0];
         S.y[i] = p[1];
         S.z[i] = p[2];
@@ -967,7 +966,7 @@ __global__ void k_init_cells(const DevTables* __restrict__ Tp, CarrierState S, D
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int c = cell_at(*Tp, S.x[i], S.y[i], S.z[i]);
         S.cell[i] = c;
-        if (S.mirror) S.mirror[i] = -1;
+        if (Tp->fac.mirror) Tp->fac.mirror[i] = -1;
         if (kMixed) {
             const Frame F = cell_frame(D, c);
             S.ox[i] = static_cast<float>(S.x[i] - (D.lo[0] + F.i[0] * D.cell_size[0]));
@@ -991,7 +990,7 @@ __global__ void k_ingest(const __grid_constant__ DevTables T, CarrierState S, De
         const double x = H.x[i], y = H.y[i], z = H.z[i];
         const int c = cell_at(T, x, y, z);
         S.cell[i] = c;
-        if (S.mirror) S.mirror[i] = -1;
+        if (T.fac.mirror) T.fac.mirror[i] = -1;
         if (kMixed) {
             const Frame F = cell_frame(D, c);
             S.ox[i] = static_cast<float>(x - (D.lo[0] + F.i[0] * D.cell_size[0]));
@@ -1224,9 +1223,9 @@ __global__ void __launch_bounds__(256) k_inject(const DevTables* __restrict__ Tp
             MeshCache mc;
             mesh_refresh(T, L, &bl, slot, p, v, mc); // src/MonteCarloSolver.cpp:318-327
             if (remain > 1e-14)
-                alive = advance_carrier_mesh(T, L, &bl, S, slot, p, w, mir, occ, mc, remain, kDrawInjected, step);
-            S.mirror[slot] = mir;
-            mesh_cache_store(S, slot, mc);
+                alive = advance_carrier_mesh(T, L, &bl, slot, p, w, mir, occ, mc, remain, kDrawInjected, step);
+            T.fac.mirror[slot] = mir;
+            mesh_cache_store(T.fac, slot, mc);
             c = cell_at(T, p[0], p[1], p[2]);
             S.x[slot] = p[0];
             S.y[slot] = p[1];
@@ -1306,7 +1305,7 @@ __global__ void __launch_bounds__(256) k_flux(const DevTables* __restrict__ Tp, 
         if (C.src_next) occ -= C.src_next[static_cast<size_t>(c) * C.hist_modes + bin_of(M, ai)];
         const double e = dmul(dmul(M.hw[ai], occ - M.nbg[ai]), M.energy_weight);
         double v[3];
-        if (S.mirror) mesh_velocity(T.fac, M, w, S.mirror[i], v);
+        if (T.fac.mirror) mesh_velocity(T.fac, M, w, T.fac.mirror[i], v);
         else mode_velocity(M, w, v);
         double* dst = use_shared ? sq : C.flux;
         for (int a = 0; a < 3; ++a) atomicAdd(dst + 3 * c + a, dmul(v[a], e));
