@@ -4,6 +4,7 @@
 #include "phmc_kernels.cuh"
 #include "phmc_pod.h"
 
+#include <cstdlib>
 #include <cstring>
 #include <filesystem>
 #include <fstream>
@@ -34,10 +35,40 @@ struct phmc_domain {
 struct phmc_batch {
     std::vector<std::unique_ptr<DeviceSolver>> s;
     cudaStream_t master = nullptr;
+    // Fused mode (every instance a nonlinear-RTA box with reservoirs, one
+    // precision): each kernel of the timestep is one launch over all
+    // instances, captured once into a graph on the master stream.
+    // The instances split into kBranches ranges of about equal carrier count,
+    // each its own chain of fused launches: the graph runs the chains side by
+    // side, so one range's FP64 cell solve overlaps another's carrier pass.
+    static constexpr int kBranches = 4;
+    bool fused = false;
+    std::vector<BatchDesc> desc;
+    std::vector<cudaStream_t> side;
+    std::vector<cudaEvent_t> forks;
+    std::vector<void*> dev;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t done = nullptr;
+    std::vector<cudaEvent_t> joins;
+    long long fused_launches = 0, launches = 0;
     ~phmc_batch() {
+        if (master) cudaStreamSynchronize(master);
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (done) cudaEventDestroy(done);
+        for (cudaEvent_t e : joins) cudaEventDestroy(e);
+        for (cudaEvent_t e : forks) cudaEventDestroy(e);
+        for (cudaStream_t x : side) cudaStreamDestroy(x);
+        for (void* p : dev) cudaFree(p);
         s.clear();
         if (master) cudaStreamDestroy(master);
     }
+    template <class T> const T* put(const std::vector<T>& v);
+    void build_fused();
+    BatchDesc describe(int lo, int hi, int persist);
+    void step();
+    void sync_all();
 };
 
 namespace {
@@ -208,6 +239,169 @@ void read_occupations(DeviceSolver& s, int64_t n, double* occ) {
     s.get_carriers(x.data(), y.data(), z.data(), occ, mode.data(), cell.data(), alive.data());
 }
 } // namespace
+
+template <class T> const T* phmc_batch::put(const std::vector<T>& v) {
+    void* d = nullptr;
+    cuda_check(cudaMalloc(&d, std::max<size_t>(1, v.size()) * sizeof(T)), "cudaMalloc");
+    dev.push_back(d);
+    cuda_check(cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy");
+    return static_cast<const T*>(d);
+}
+
+BatchDesc phmc_batch::describe(int lo, int hi, int persist) {
+    const int n = hi - lo;
+    std::vector<const DevTables*> tables(n);
+    std::vector<CarrierState> states(n);
+    std::vector<CellArrays> cells(n);
+    std::vector<DevLedger*> ledgers(n);
+    std::vector<int*> holes(n), hole_counts(n);
+    std::vector<int> capacity(n), carrier_block(n + 1, 0), hole_block(n + 1, 0), cell_begin(n + 1, 0),
+        cell_block(n + 1, 0), inject_block(n + 1, 0);
+    int chunks = 1;
+    for (int i = 0; i < n; ++i) {
+        const DeviceSolver& x = *s[lo + i];
+        tables[i] = x.device_tables();
+        states[i] = x.carrier_state();
+        cells[i] = x.cell_arrays();
+        ledgers[i] = x.device_ledger();
+        holes[i] = x.hole_list();
+        hole_counts[i] = x.hole_blocks();
+        capacity[i] = x.carrier_state().capacity;
+        // virtual CTAs in proportion to the population (about eight carriers
+        // per thread; the grid-stride bodies are correct for any count)
+        const int n0 = x.initial_particles();
+        carrier_block[i + 1] = carrier_block[i] + std::max(1, (n0 + n0 / 4 + 2047) / 2048);
+        inject_block[i + 1] = inject_block[i] + std::max(1, (n0 + 32767) / 32768);
+        hole_block[i + 1] = hole_block[i] + (capacity[i] + 1023) / 1024;
+        cell_begin[i + 1] = cell_begin[i] + x.cell_arrays().ncells;
+        cell_block[i + 1] = cell_block[i] + (x.cell_arrays().ncells + 255) / 256;
+        chunks = std::max(chunks, (x.cell_arrays().hist_modes + 1023) / 1024);
+    }
+    BatchDesc D{};
+    D.n = n;
+    D.tables = put(tables);
+    D.states = put(states);
+    D.cells = put(cells);
+    D.ledgers = put(ledgers);
+    D.holes = put(holes);
+    D.hole_counts = put(hole_counts);
+    D.capacity = put(capacity);
+    D.carrier_block = put(carrier_block);
+    D.hole_block = put(hole_block);
+    D.cell_begin = put(cell_begin);
+    D.cell_block = put(cell_block);
+    D.inject_block = put(inject_block);
+    D.total_carrier_blocks = carrier_block[n];
+    D.total_inject_blocks = inject_block[n];
+    D.total_hole_blocks = hole_block[n];
+    D.total_cells = cell_begin[n];
+    D.total_cell_blocks = cell_block[n];
+    D.chunks = chunks;
+    D.persist = persist;
+    return D;
+}
+
+// Per-instance device state behind arrays and the CTA ranges of every fused
+// launch; fused when all instances qualify (DeviceSolver::fusable).
+void phmc_batch::build_fused() {
+    fused = false;
+    if (const char* e = std::getenv("PHMC_BATCH_FUSED"))
+        if (e[0] == '0') return; // per-instance step graphs on the instance streams
+    for (auto& x : s)
+        if (!x->fusable() || !x->has_reservoirs() || x->mixed() != s[0]->mixed()) return;
+    const int n = static_cast<int>(s.size());
+    int dev = 0, sms = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+    // contiguous instance ranges of about equal initial carrier count
+    const int nb = std::min(kBranches, n);
+    double total = 0.0;
+    for (auto& x : s) total += x->initial_particles();
+    std::vector<int> cut{0};
+    double acc = 0.0;
+    for (int i = 0; i < n && static_cast<int>(cut.size()) < nb; ++i) {
+        acc += s[i]->initial_particles();
+        if (acc >= total * static_cast<double>(cut.size()) / nb && i + 1 < n) cut.push_back(i + 1);
+    }
+    cut.push_back(n);
+    const int branches = static_cast<int>(cut.size()) - 1;
+    const int persist = std::max(1, sms * 8 / branches);
+    desc.clear();
+    for (int k = 0; k < branches; ++k) desc.push_back(describe(cut[k], cut[k + 1], persist));
+    for (const BatchDesc& D : desc)
+        if (D.total_cells > 65535) return; // the per-cell launches put cells on gridDim.y
+    side.resize(branches);
+    forks.resize(branches);
+    for (int k = 0; k < branches; ++k) {
+        cuda_check(cudaStreamCreateWithFlags(&side[k], cudaStreamNonBlocking), "cudaStreamCreateWithFlags");
+        cuda_check(cudaEventCreateWithFlags(&forks[k], cudaEventDisableTiming), "cudaEventCreate");
+    }
+    // work queued on the instance streams (uploads, first observations) precedes the graph
+    for (auto& x : s) x->synchronize();
+    cuda_check(cudaStreamBeginCapture(master, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    try {
+        fused_launches = 0;
+        cuda_check(cudaEventRecord(forks[0], master), "cudaEventRecord");
+        for (int k = 0; k < branches; ++k) {
+            cuda_check(cudaStreamWaitEvent(side[k], forks[0], 0), "cudaStreamWaitEvent");
+            fused_launches += launch_fused_step(desc[k], side[k], s[0]->mixed());
+        }
+        for (int k = 0; k < branches; ++k) {
+            cuda_check(cudaEventRecord(forks[k], side[k]), "cudaEventRecord");
+            cuda_check(cudaStreamWaitEvent(master, forks[k], 0), "cudaStreamWaitEvent");
+        }
+    } catch (...) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(master, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+    }
+    cuda_check(cudaStreamEndCapture(master, &graph), "cudaStreamEndCapture");
+    cuda_check(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
+    cuda_check(cudaEventCreateWithFlags(&done, cudaEventDisableTiming), "cudaEventCreate");
+    joins.resize(s.size());
+    for (auto& e : joins) cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+    fused = true;
+}
+
+// One timestep of every instance. Fused: one graph launch on the master
+// stream; instances that observe or check containment this step order their
+// own stream after it, and the master after their work.
+void phmc_batch::step() {
+    if (!fused) {
+        for (auto& x : s) {
+            const long long l0 = x->launches();
+            x->run_timestep();
+            launches += x->launches() - l0;
+        }
+        return;
+    }
+    cuda_check(cudaGraphLaunch(exec, master), "cudaGraphLaunch");
+    launches += fused_launches;
+    bool recorded = false;
+    for (size_t i = 0; i < s.size(); ++i) {
+        const bool extras = s[i]->batch_extras_due();
+        if (extras) {
+            if (!recorded) {
+                cuda_check(cudaEventRecord(done, master), "cudaEventRecord");
+                recorded = true;
+            }
+            cuda_check(cudaStreamWaitEvent(s[i]->stream(), done, 0), "cudaStreamWaitEvent");
+        }
+        const long long l0 = s[i]->launches();
+        s[i]->finish_batched_step(0);
+        launches += s[i]->launches() - l0;
+        if (extras) {
+            cuda_check(cudaEventRecord(joins[i], s[i]->stream()), "cudaEventRecord");
+            cuda_check(cudaStreamWaitEvent(master, joins[i], 0), "cudaStreamWaitEvent");
+        }
+    }
+}
+
+void phmc_batch::sync_all() {
+    cuda_check(cudaStreamSynchronize(master), "cudaStreamSynchronize");
+    for (auto& x : s) x->synchronize();
+}
 
 extern "C" {
 
@@ -427,6 +621,7 @@ int phmc_batch_create(const phmc_config* cfgs, int n, phmc_material* const* mate
             b->s.push_back(std::make_unique<DeviceSolver>(c, ms, true, cfgs[i].precision == 1));
         }
         cuda_check(cudaStreamCreateWithFlags(&b->master, cudaStreamNonBlocking), "cudaStreamCreateWithFlags");
+        b->build_fused();
         *out = b.release();
     });
 }
@@ -438,22 +633,21 @@ int phmc_batch_size(const phmc_batch* b, int* n) {
 
 int phmc_batch_run(phmc_batch* b, int steps) {
     return guard([&] {
-        for (int k = 0; k < steps; ++k)
-            for (auto& s : b->s) s->run_timestep();
-        for (auto& s : b->s) s->synchronize();
+        for (int k = 0; k < steps; ++k) b->step();
+        b->sync_all();
     });
 }
 
 int phmc_batch_timed_run(phmc_batch* b, int steps, double* total_ms, double* carrier_steps, int64_t* launches) {
     return guard([&] {
-        for (auto& s : b->s) s->synchronize();
-        std::vector<long long> n0(b->s.size()), l0(b->s.size());
+        b->sync_all();
+        std::vector<long long> n0(b->s.size());
         for (size_t i = 0; i < b->s.size(); ++i) {
             phmc_stats st;
             b->s[i]->read_stats(st);
             n0[i] = st.particle_count;
-            l0[i] = b->s[i]->launches();
         }
+        const long long l0 = b->launches;
         cudaEvent_t start, stop;
         cuda_check(cudaEventCreate(&start), "cudaEventCreate");
         cuda_check(cudaEventCreate(&stop), "cudaEventCreate");
@@ -462,8 +656,7 @@ int phmc_batch_timed_run(phmc_batch* b, int steps, double* total_ms, double* car
         // every instance stream starts after `start` and the master waits for all of them
         cuda_check(cudaEventRecord(start, b->master), "cudaEventRecord");
         for (auto& s : b->s) cuda_check(cudaStreamWaitEvent(s->stream(), start, 0), "cudaStreamWaitEvent");
-        for (int k = 0; k < steps; ++k)
-            for (auto& s : b->s) s->run_timestep();
+        for (int k = 0; k < steps; ++k) b->step();
         for (size_t i = 0; i < b->s.size(); ++i) {
             cuda_check(cudaEventRecord(done[i], b->s[i]->stream()), "cudaEventRecord");
             cuda_check(cudaStreamWaitEvent(b->master, done[i], 0), "cudaStreamWaitEvent");
@@ -474,15 +667,13 @@ int phmc_batch_timed_run(phmc_batch* b, int steps, double* total_ms, double* car
         cuda_check(cudaEventElapsedTime(&ms, start, stop), "cudaEventElapsedTime");
         *total_ms = ms;
         double cs = 0;
-        long long l = 0;
         for (size_t i = 0; i < b->s.size(); ++i) {
             phmc_stats st;
             b->s[i]->read_stats(st);
             cs += 0.5 * static_cast<double>(n0[i] + st.particle_count) * steps;
-            l += b->s[i]->launches() - l0[i];
         }
         *carrier_steps = cs;
-        *launches = l;
+        *launches = b->launches - l0;
         cudaEventDestroy(start);
         cudaEventDestroy(stop);
         for (auto& e : done) cudaEventDestroy(e);
@@ -490,11 +681,17 @@ int phmc_batch_timed_run(phmc_batch* b, int steps, double* total_ms, double* car
 }
 
 int phmc_batch_stats(phmc_batch* b, int i, phmc_stats* out) {
-    return guard([&] { b->s.at(static_cast<size_t>(i))->read_stats(*out); });
+    return guard([&] {
+        b->sync_all();
+        b->s.at(static_cast<size_t>(i))->read_stats(*out);
+    });
 }
 
 int phmc_batch_cells(phmc_batch* b, int i, double* temperature, double* energy_density, double* heat_flux3) {
-    return guard([&] { b->s.at(static_cast<size_t>(i))->read_cells(temperature, energy_density, heat_flux3); });
+    return guard([&] {
+        b->sync_all();
+        b->s.at(static_cast<size_t>(i))->read_cells(temperature, energy_density, heat_flux3);
+    });
 }
 
 int phmc_batch_cell_count(const phmc_batch* b, int i, int* cells) {

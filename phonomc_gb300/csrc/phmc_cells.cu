@@ -63,7 +63,9 @@ template <int N> __device__ __forceinline__ void block_sum(double (&v)[N], doubl
     __syncthreads();
 }
 
-__global__ void k_step_begin(DevLedger* L) {
+__device__ __forceinline__ void k_step_begin_body(DevLedger* L, int vbx, int vgx) {
+    (void)vbx;
+    (void)vgx;
     for (int r = 0; r < kMaxReservoirs; ++r) L->absorbed_res[r] = 0;
     L->step_absorbed = L->step_injected = 0;
     L->step_absorbed_ev = L->step_injected_ev = 0;
@@ -80,19 +82,25 @@ __global__ void k_step_begin(DevLedger* L) {
     L->n_deferred = 0;
 }
 
+__global__ void k_step_begin(DevLedger* L) {
+    k_step_begin_body(L, blockIdx.x, gridDim.x);
+}
+
 __device__ __forceinline__ double idx_to_double(int a) { return static_cast<double>(a); }
 __device__ __forceinline__ int double_to_idx(double a) { return static_cast<int>(a); }
 
 // ------------------------------------------------------------ statistics
 template <bool kRta>
-__global__ void __launch_bounds__(kStatThreads) k_cell_stats(const DevTables* __restrict__ Tp, CellArrays C,
-                                                              int classes) {
+__device__ __forceinline__ void k_cell_stats_body(const DevTables* __restrict__ Tp, CellArrays C, int classes, int vbx, int vgx, int vby) {
+    (void)vbx;
+    (void)vgx;
+    (void)vby;
     __shared__ double red[3 * 32];
     const DevTables& T = *Tp;
-    const int c = blockIdx.y;
+    const int c = vby;
     const DevMaterial& M = T.mat[C.cell_material[c]];
     const size_t hb = static_cast<size_t>(c) * C.hist_modes;
-    const int m0 = blockIdx.x * kChunk, m1 = min(M.n_bins, m0 + kChunk);
+    const int m0 = vbx * kChunk, m1 = min(M.n_bins, m0 + kChunk);
     double v[3] = {0.0, 0.0, 0.0};
     for (int b = m0 + threadIdx.x; b < m1; b += blockDim.x) {
         const unsigned k = C.bins[hb + b].cnt;
@@ -113,10 +121,18 @@ __global__ void __launch_bounds__(kStatThreads) k_cell_stats(const DevTables* __
     }
 }
 
+template <bool kRta>
+__global__ void __launch_bounds__(kStatThreads) k_cell_stats(const DevTables* __restrict__ Tp, CellArrays C,
+                                                              int classes) {
+    k_cell_stats_body<kRta>(Tp, C, classes, blockIdx.x, gridDim.x, blockIdx.y);
+}
+
 // phase 2 keeps the supplied temperatures
-__global__ void k_cell_state(const DevTables* __restrict__ Tp, CellArrays C, DevLedger* L, int phase) {
+__device__ __forceinline__ void k_cell_state_body(const DevTables* __restrict__ Tp, CellArrays C, DevLedger* L, int phase, int vbx, int vgx) {
+    (void)vbx;
+    (void)vgx;
     const DevTables& T = *Tp;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C.ncells; c += gridDim.x * blockDim.x) {
+    for (int c = vbx * blockDim.x + threadIdx.x; c < C.ncells; c += vgx * blockDim.x) {
         const DevMaterial& M = T.mat[C.cell_material[c]];
         const double* s = C.cell_stats + 4 * c;
         const double E = s[0] * M.energy_weight / C.volume[c] + M.energy_density_bg;
@@ -130,11 +146,17 @@ __global__ void k_cell_state(const DevTables* __restrict__ Tp, CellArrays C, Dev
     }
 }
 
+__global__ void k_cell_state(const DevTables* __restrict__ Tp, CellArrays C, DevLedger* L, int phase) {
+    k_cell_state_body(Tp, C, L, phase, blockIdx.x, gridDim.x);
+}
+
 // ------------------------------------------------------------------ RTA
-__global__ void __launch_bounds__(256) k_rta_solve(const DevTables* __restrict__ Tp, CellArrays C) {
+__device__ __forceinline__ void k_rta_solve_body(const DevTables* __restrict__ Tp, CellArrays C, int vbx, int vgx) {
+    (void)vbx;
+    (void)vgx;
     __shared__ double red[2 * 32];
     const DevTables& T = *Tp;
-    const int c = blockIdx.x;
+    const int c = vbx;
     const DevMaterial& M = T.mat[C.cell_material[c]];
     // the bins of an RTA cell are its mode classes: count, sum of n, sum of max(1, n)
     const int nc = M.n_classes;
@@ -211,6 +233,10 @@ __global__ void __launch_bounds__(256) k_rta_solve(const DevTables* __restrict__
     for (int k = threadIdx.x; k < nc; k += blockDim.x) {
         ab[k].y = bose_dev(Ts, fmax(0.0, M.class_omega[k]));
     }
+}
+
+__global__ void __launch_bounds__(256) k_rta_solve(const DevTables* __restrict__ Tp, CellArrays C) {
+    k_rta_solve_body(Tp, C, blockIdx.x, gridDim.x);
 }
 
 // Warp-wide sum with the result of lane 0 broadcast, so every lane continues
@@ -523,13 +549,16 @@ __global__ void __launch_bounds__(kLinThreads) k_linear_solve(const DevTables* _
 
 // ----------------------------------------------- tables and step energies
 template <int kCollision>
-__global__ void __launch_bounds__(kStatThreads) k_cell_tables(const DevTables* __restrict__ Tp, CellArrays C, int phase) {
+__device__ __forceinline__ void k_cell_tables_body(const DevTables* __restrict__ Tp, CellArrays C, int phase, int vbx, int vgx, int vby) {
+    (void)vbx;
+    (void)vgx;
+    (void)vby;
     __shared__ double red[4 * 32];
     const DevTables& T = *Tp;
-    const int c = blockIdx.y;
+    const int c = vby;
     const DevMaterial& M = T.mat[C.cell_material[c]];
     const size_t hb = static_cast<size_t>(c) * C.hist_modes;
-    const int m0 = blockIdx.x * kChunk, m1 = min(M.n_bins, m0 + kChunk);
+    const int m0 = vbx * kChunk, m1 = min(M.n_bins, m0 + kChunk);
     const double ratio = C.grad_ratio[c];
     const bool collide = phase >= 1 && kCollision != kCollideNone;
     double s[3] = {0.0, 0.0, 0.0}; // residual, drive, updates
@@ -579,9 +608,15 @@ __global__ void __launch_bounds__(kStatThreads) k_cell_tables(const DevTables* _
     }
 }
 
+template <int kCollision>
+__global__ void __launch_bounds__(kStatThreads) k_cell_tables(const DevTables* __restrict__ Tp, CellArrays C, int phase) {
+    k_cell_tables_body<kCollision>(Tp, C, phase, blockIdx.x, gridDim.x, blockIdx.y);
+}
+
 // End of step: cell temperatures, total thermal energy and the energy ledger. One CTA.
-__global__ void __launch_bounds__(1024) k_cells_final(const DevTables* __restrict__ Tp, CellArrays C, DevLedger* L,
-                                                      int phase) {
+__device__ __forceinline__ void k_cells_final_body(const DevTables* __restrict__ Tp, CellArrays C, DevLedger* L, int phase, int vbx, int vgx) {
+    (void)vbx;
+    (void)vgx;
     __shared__ double red[4 * 32];
     const DevTables& T = *Tp;
     double v[4] = {0.0, 0.0, 0.0, 0.0}; // thermal, residual, drive, updates
@@ -636,6 +671,11 @@ __global__ void __launch_bounds__(1024) k_cells_final(const DevTables* __restric
     for (int r = 0; r < kMaxReservoirs; ++r) L->previous_res[r] = L->absorbed_res[r];
     L->step_index += 1;
     L->elapsed += T.par.dt;
+}
+
+__global__ void __launch_bounds__(1024) k_cells_final(const DevTables* __restrict__ Tp, CellArrays C, DevLedger* L,
+                                                      int phase) {
+    k_cells_final_body(Tp, C, L, phase, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------------------- heat source
@@ -958,6 +998,55 @@ int launch_cell_solve(const LaunchCtx& x, int phase, int collision) {
 
 void launch_cells_final(const LaunchCtx& x, int phase) {
     k_cells_final<<<1, 1024, 0, x.stream>>>(x.T, x.C, x.L, phase);
+}
+
+} // namespace phmc
+
+// ------------------------------------------------- fused batch launches
+namespace phmc {
+
+__global__ void kf_step_begin(const BatchDesc D) {
+    if (threadIdx.x == 0) k_step_begin_body(D.ledgers[blockIdx.x], 0, 1);
+}
+
+__global__ void __launch_bounds__(kStatThreads) kf_cell_stats(const BatchDesc D) {
+    const int i = batch_find(D.cell_begin, D.n, blockIdx.y);
+    k_cell_stats_body<true>(D.tables[i], D.cells[i], 1, blockIdx.x, gridDim.x, blockIdx.y - D.cell_begin[i]);
+}
+
+__global__ void kf_cell_state(const BatchDesc D, int phase) {
+    const int i = batch_find(D.cell_block, D.n, blockIdx.x);
+    const int b0 = D.cell_block[i];
+    k_cell_state_body(D.tables[i], D.cells[i], D.ledgers[i], phase, blockIdx.x - b0, D.cell_block[i + 1] - b0);
+}
+
+__global__ void __launch_bounds__(256) kf_rta_solve(const BatchDesc D) {
+    const int i = batch_find(D.cell_begin, D.n, blockIdx.x);
+    k_rta_solve_body(D.tables[i], D.cells[i], blockIdx.x - D.cell_begin[i], D.cell_begin[i + 1] - D.cell_begin[i]);
+}
+
+__global__ void __launch_bounds__(kStatThreads) kf_cell_tables(const BatchDesc D, int phase) {
+    const int i = batch_find(D.cell_begin, D.n, blockIdx.y);
+    k_cell_tables_body<kCollideRta>(D.tables[i], D.cells[i], phase, blockIdx.x, gridDim.x, blockIdx.y - D.cell_begin[i]);
+}
+
+__global__ void __launch_bounds__(1024) kf_cells_final(const BatchDesc D, int phase) {
+    const int i = blockIdx.x;
+    k_cells_final_body(D.tables[i], D.cells[i], D.ledgers[i], phase, 0, 1);
+}
+
+int launch_fused_cells(const BatchDesc& D, cudaStream_t s) {
+    kf_cell_stats<<<dim3(D.chunks, D.total_cells), kStatThreads, 0, s>>>(D);
+    kf_cell_state<<<D.total_cell_blocks, 256, 0, s>>>(D, 1);
+    kf_rta_solve<<<D.total_cells, 256, 0, s>>>(D);
+    kf_cell_tables<<<dim3(D.chunks, D.total_cells), kStatThreads, 0, s>>>(D, 1);
+    kf_cells_final<<<D.n, 1024, 0, s>>>(D, 1);
+    return 5;
+}
+
+int launch_fused_step(const BatchDesc& D, cudaStream_t s, bool mixed) {
+    kf_step_begin<<<D.n, 32, 0, s>>>(D);
+    return 1 + launch_fused_transport(D, s, mixed) + launch_fused_cells(D, s);
 }
 
 } // namespace phmc

@@ -28,6 +28,45 @@ struct LaunchCtx {
     bool mesh = false;   // surface-mesh domain (plain FP64 carrier state)
 };
 
+// Independent box instances advanced by one launch per kernel of the step:
+// per-instance device state behind arrays, and prefix sums that assign each
+// CTA of a fused launch to an instance (the instance's own grid of CTAs).
+struct BatchDesc {
+    int n;                            // instances
+    const DevTables* const* tables;   // [n] device copies of each instance's tables
+    const CarrierState* states;       // [n]
+    const CellArrays* cells;          // [n]
+    DevLedger* const* ledgers;        // [n]
+    int* const* holes;                // [n] free-slot lists
+    int* const* hole_counts;          // [n] per-CTA dead counts of the slot scan
+    const int* capacity;              // [n]
+    const int* carrier_block;         // [n+1] CTAs of the carrier kernels
+    const int* hole_block;            // [n+1] CTAs of the slot scan (1024 threads)
+    const int* cell_begin;            // [n+1] cells
+    const int* cell_block;            // [n+1] CTAs of the per-cell thread kernels (256 threads)
+    const int* inject_block;          // [n+1] CTAs of the injection kernel
+    int total_carrier_blocks, total_hole_blocks, total_cells, total_cell_blocks, total_inject_blocks;
+    int chunks;                       // mode chunks of the widest instance
+    int persist;                      // resident CTAs of the persistent carrier kernels
+};
+
+// Instance owning index x of a prefix-sum array: the last i with prefix[i] <= x.
+__device__ __forceinline__ int batch_find(const int* prefix, int n, int x) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(prefix + mid) <= x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// The launches of one fused timestep of `D` (nonlinear RTA box instances with
+// reservoirs): transport, injection, cell solve, ledger. Returns the launch count.
+int launch_fused_step(const BatchDesc& D, cudaStream_t stream, bool mixed);
+int launch_fused_transport(const BatchDesc& D, cudaStream_t stream, bool mixed);
+int launch_fused_cells(const BatchDesc& D, cudaStream_t stream);
+
 int launch_transport(const LaunchCtx& x, bool mixed, bool rta);
 int launch_mesh_cache_init(const LaunchCtx& x);
 void launch_histogram(const LaunchCtx& x, bool rta);

@@ -665,6 +665,31 @@ void DeviceSolver::capture_step_graph() {
     counters_.launches = l0;
 }
 
+bool DeviceSolver::fusable() const {
+    return !domain_->is_mesh() && P_.mats.size() == 1 && !P_.linearized && !P_.source.enabled &&
+           !cfg_.temperature_gradient.has_value() && collision_kind() == kCollideRta;
+}
+
+int DeviceSolver::carrier_blocks() const { return ctx().grid_blocks; }
+
+bool DeviceSolver::batch_extras_due() const {
+    const int next = step_ + 1;
+    return step_ % 100 == 0 || next == 1 || next % cfg_.convergence_write_interval == 0;
+}
+
+void DeviceSolver::finish_batched_step(long long launches) {
+    if (failed_) throw std::runtime_error("Cannot resume a failed timestep; construct a new solver after fixing its cause.");
+    counters_.launches += launches;
+    if (step_ % 100 == 0) {
+        launch_containment(ctx(), mixed_);
+        counters_.launches += 1;
+    }
+    materialized_ = false;
+    ++step_;
+    elapsed_ += cfg_.time_step;
+    if (step_ == 1 || step_ % cfg_.convergence_write_interval == 0) flux_pass();
+}
+
 void DeviceSolver::run_timestep() {
     if (failed_) throw std::runtime_error("Cannot resume a failed timestep; construct a new solver after fixing its cause.");
     failed_ = true;

@@ -164,6 +164,23 @@ public:
     const Problem& problem() const { return P_; }
     long long launches() const { return counters_.launches; }
     cudaStream_t stream() const { return stream_; }
+    // Instances that the fused batch kernels can advance together: box domain,
+    // one material, nonlinear RTA, no heat source and no gradient drive.
+    bool fusable() const;
+    // device state of this instance, read by the fused batch kernels
+    const DevTables* device_tables() const { return d_tables_; }
+    DevLedger* device_ledger() const { return d_ledger_; }
+    const CarrierState& carrier_state() const { return state_; }
+    const CellArrays& cell_arrays() const { return cells_; }
+    int* hole_list() const { return d_holes_; }
+    int* hole_blocks() const { return d_block_dead_; }
+    bool has_reservoirs() const { return !P_.reservoirs.empty(); }
+    int initial_particles() const { return P_.initial_particles; }
+    int carrier_blocks() const;
+    // Bookkeeping after a fused batch step: `extras` when the caller has ordered
+    // this solver's stream after the step (containment, flux observation due).
+    bool batch_extras_due() const;
+    void finish_batched_step(long long launches);
 
 private:
     void upload_tables();

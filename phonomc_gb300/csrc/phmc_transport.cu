@@ -713,8 +713,9 @@ constexpr int kDeferBuffer = 64; // queued wall events per warp before a flush
 // queued (per-warp shared buffers, one global atomic per 32 entries) and
 // finished by k_deferred.
 template <bool kMixed, bool kRta>
-__global__ void __launch_bounds__(kTransportThreads) k_transport(const __grid_constant__ DevTables T, CarrierState S,
-                                                                 CellArrays C, DevLedger* L) {
+__device__ __forceinline__ void k_transport_body(const DevTables& T, CarrierState S, CellArrays C, DevLedger* L, int vbx, int vgx) {
+    (void)vbx;
+    (void)vgx;
     const uint32_t step = L->step_index; // timesteps completed: the draw counter of this step
     __shared__ BlockLedger bl;
     __shared__ int4 qbuf[kMixed ? kTransportThreads / 32 : 1][kMixed ? kDeferBuffer : 1];
@@ -725,7 +726,7 @@ __global__ void __launch_bounds__(kTransportThreads) k_transport(const __grid_co
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         int queued = 0; // warp-uniform
         // block-uniform trip count so that every lane reaches the warp-wide ballot
-        for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        for (int base = vbx * blockDim.x; base < n; base += vgx * blockDim.x) {
             const int i = base + threadIdx.x;
             bool defer = false;
             int4 entry;
@@ -784,7 +785,7 @@ __global__ void __launch_bounds__(kTransportThreads) k_transport(const __grid_co
             }
         }
     } else {
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        for (int i = vbx * blockDim.x + threadIdx.x; i < n; i += vgx * blockDim.x) {
             if (!__ldcs(S.alive + i)) continue;
             uint32_t w = __ldcs(S.mode + i);
             const int c0 = __ldcs(S.cell + i);
@@ -807,6 +808,12 @@ __global__ void __launch_bounds__(kTransportThreads) k_transport(const __grid_co
     }
     __syncthreads();
     block_ledger_flush(&bl, L);
+}
+
+template <bool kMixed, bool kRta>
+__global__ void __launch_bounds__(kTransportThreads) k_transport(const __grid_constant__ DevTables T, CarrierState S,
+                                                                 CellArrays C, DevLedger* L) {
+    k_transport_body<kMixed, kRta>(T, S, C, L, blockIdx.x, gridDim.x);
 }
 
 // Mesh transport, pass 1 of 2: apply the pending update and drift every
@@ -909,14 +916,15 @@ __global__ void __launch_bounds__(kTransportThreads, 1) k_mesh_events(const __gr
 // draws of the queued event index, finish the flight (further walls inline),
 // then settle and bin exactly as the transport pass would have.
 template <bool kRta>
-__global__ void __launch_bounds__(kTransportThreads) k_deferred(const __grid_constant__ DevTables T, CarrierState S,
-                                                                CellArrays C, DevLedger* L) {
+__device__ __forceinline__ void k_deferred_body(const DevTables& T, CarrierState S, CellArrays C, DevLedger* L, int vbx, int vgx) {
+    (void)vbx;
+    (void)vgx;
     const uint32_t step = L->step_index;
     __shared__ BlockLedger bl;
     block_ledger_init(&bl);
     __syncthreads();
     const int nq = min(L->n_deferred, S.capacity);
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+    for (int q = vbx * blockDim.x + threadIdx.x; q < nq; q += vgx * blockDim.x) {
         const int4 e = S.deferred[q];
         const int i = e.x;
         if (i < 0 || i >= S.capacity) {
@@ -944,6 +952,12 @@ __global__ void __launch_bounds__(kTransportThreads) k_deferred(const __grid_con
     }
     __syncthreads();
     block_ledger_flush(&bl, L);
+}
+
+template <bool kRta>
+__global__ void __launch_bounds__(kTransportThreads) k_deferred(const __grid_constant__ DevTables T, CarrierState S,
+                                                                CellArrays C, DevLedger* L) {
+    k_deferred_body<kRta>(T, S, C, L, blockIdx.x, gridDim.x);
 }
 
 // Bins of the current population (initial state or after carriers were replaced).
@@ -1039,18 +1053,25 @@ __global__ void k_positions_out(const DevTables* __restrict__ Tp, CarrierState S
 // Free slots in ascending order: per-block dead counts, one-block scan, write.
 constexpr int kHoleBlock = 1024;
 
-__global__ void __launch_bounds__(kHoleBlock) k_dead_count(CarrierState S, const DevLedger* L, int* block_dead) {
+__device__ __forceinline__ void k_dead_count_body(CarrierState S, const DevLedger* L, int* block_dead, int vbx, int vgx) {
+    (void)vbx;
+    (void)vgx;
     const int n = L->n_slots;
-    const int i = blockIdx.x * kHoleBlock + threadIdx.x;
+    const int i = vbx * kHoleBlock + threadIdx.x;
     const int dead = (i < n && !S.alive[i]) ? 1 : 0;
     const int c = __syncthreads_count(dead);
-    if (threadIdx.x == 0) block_dead[blockIdx.x] = c;
+    if (threadIdx.x == 0) block_dead[vbx] = c;
+}
+
+__global__ void __launch_bounds__(kHoleBlock) k_dead_count(CarrierState S, const DevLedger* L, int* block_dead) {
+    k_dead_count_body(S, L, block_dead, blockIdx.x, gridDim.x);
 }
 
 // Single block: exclusive scan of block counts and emission counts per reservoir
 // (src/solver/ReservoirInjector.cpp:281-284, src/solver/ReservoirSampler.cpp:117-124).
-__global__ void __launch_bounds__(1024) k_inject_prepare(const DevTables* __restrict__ Tp, DevLedger* L,
-                                                         int* block_dead, int nblocks, int capacity) {
+__device__ __forceinline__ void k_inject_prepare_body(const DevTables* __restrict__ Tp, DevLedger* L, int* block_dead, int nblocks, int capacity, int vbx, int vgx) {
+    (void)vbx;
+    (void)vgx;
     const uint32_t step = L->step_index;
     __shared__ int carry;
     __shared__ int warp_sums[32];
@@ -1116,12 +1137,18 @@ __global__ void __launch_bounds__(1024) k_inject_prepare(const DevTables* __rest
     }
 }
 
-__global__ void __launch_bounds__(kHoleBlock) k_dead_write(CarrierState S, const DevLedger* L, const int* block_off,
-                                                           int* holes) {
+__global__ void __launch_bounds__(1024) k_inject_prepare(const DevTables* __restrict__ Tp, DevLedger* L,
+                                                         int* block_dead, int nblocks, int capacity) {
+    k_inject_prepare_body(Tp, L, block_dead, nblocks, capacity, blockIdx.x, gridDim.x);
+}
+
+__device__ __forceinline__ void k_dead_write_body(CarrierState S, const DevLedger* L, const int* block_off, int* holes, int vbx, int vgx) {
+    (void)vbx;
+    (void)vgx;
     __shared__ int warp_base[32];
     const int n = L->n_slots;
     const int need = L->n_inject;
-    const int i = blockIdx.x * kHoleBlock + threadIdx.x;
+    const int i = vbx * kHoleBlock + threadIdx.x;
     const bool dead = i < n && !S.alive[i];
     const unsigned mask = __ballot_sync(0xffffffffu, dead);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -1138,14 +1165,20 @@ __global__ void __launch_bounds__(kHoleBlock) k_dead_write(CarrierState S, const
     }
     __syncthreads();
     if (dead) {
-        const int rank = block_off[blockIdx.x] + warp_base[wid] + __popc(mask & ((1u << lane) - 1u));
+        const int rank = block_off[vbx] + warp_base[wid] + __popc(mask & ((1u << lane) - 1u));
         if (rank < need) holes[rank] = i;
     }
 }
 
+__global__ void __launch_bounds__(kHoleBlock) k_dead_write(CarrierState S, const DevLedger* L, const int* block_off,
+                                                           int* holes) {
+    k_dead_write_body(S, L, block_off, holes, blockIdx.x, gridDim.x);
+}
+
 template <bool kMixed, bool kRta, bool kMesh = false>
-__global__ void __launch_bounds__(256) k_inject(const DevTables* __restrict__ Tp, CarrierState S, CellArrays C,
-                                                DevLedger* L, const int* holes) {
+__device__ __forceinline__ void k_inject_body(const DevTables* __restrict__ Tp, CarrierState S, CellArrays C, DevLedger* L, const int* holes, int vbx, int vgx) {
+    (void)vbx;
+    (void)vgx;
     const uint32_t step = L->step_index;
     __shared__ BlockLedger bl;
     block_ledger_init(&bl);
@@ -1155,7 +1188,7 @@ __global__ void __launch_bounds__(256) k_inject(const DevTables* __restrict__ Tp
     const int ni = L->n_inject;
     const int nh = L->n_holes;
     const int n_old = L->n_slots;
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < ni; j += gridDim.x * blockDim.x) {
+    for (int j = vbx * blockDim.x + threadIdx.x; j < ni; j += vgx * blockDim.x) {
         int r = 0;
         while (r + 1 < P.n_reservoirs && j >= L->inject_offset[r + 1]) ++r;
         const int e = j - L->inject_offset[r];
@@ -1247,10 +1280,22 @@ __global__ void __launch_bounds__(256) k_inject(const DevTables* __restrict__ Tp
     block_ledger_flush(&bl, L);
 }
 
-__global__ void k_inject_finish(DevLedger* L) {
+template <bool kMixed, bool kRta, bool kMesh = false>
+__global__ void __launch_bounds__(256) k_inject(const DevTables* __restrict__ Tp, CarrierState S, CellArrays C,
+                                                DevLedger* L, const int* holes) {
+    k_inject_body<kMixed, kRta, kMesh>(Tp, S, C, L, holes, blockIdx.x, gridDim.x);
+}
+
+__device__ __forceinline__ void k_inject_finish_body(DevLedger* L, int vbx, int vgx) {
+    (void)vbx;
+    (void)vgx;
     const int extra = L->n_inject - L->n_holes;
     if (extra > 0) L->n_slots += extra;
     L->step_injected += static_cast<unsigned long long>(L->n_inject);
+}
+
+__global__ void k_inject_finish(DevLedger* L) {
+    k_inject_finish_body(L, blockIdx.x, gridDim.x);
 }
 
 // Escaped-carrier check (src/solver/TransportOperator.cpp:364-402).
@@ -1440,6 +1485,162 @@ void launch_flux(const LaunchCtx& x, bool /*mixed*/) {
 void launch_apply_pending(const LaunchCtx& x, bool subtract_drive) {
     k_apply_pending<<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.C, x.L, subtract_drive ? 1 : 0);
     k_reset_pending<<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.C, subtract_drive ? 1 : 0);
+}
+
+} // namespace phmc
+
+// ------------------------------------------------- fused batch launches
+// Persistent CTAs walk the virtual CTAs of all instances; each virtual CTA
+// runs the single-instance kernel body for its instance with the instance's
+// CTA index and count. The carrier kernels keep the instance's tables in
+// shared memory (copied when the instance changes).
+namespace phmc {
+
+struct SharedTables {
+    __align__(16) unsigned char raw[sizeof(DevTables)];
+    int owner;
+};
+
+__device__ __forceinline__ const DevTables& stage_tables(SharedTables& st, const BatchDesc& D, int inst) {
+    if (st.owner != inst) { // block-uniform
+        __syncthreads();
+        const unsigned* src = reinterpret_cast<const unsigned*>(D.tables[inst]);
+        unsigned* dst = reinterpret_cast<unsigned*>(st.raw);
+        for (int k = threadIdx.x; k < static_cast<int>(sizeof(DevTables) / 4); k += blockDim.x) dst[k] = src[k];
+        __syncthreads();
+        if (threadIdx.x == 0) st.owner = inst;
+        __syncthreads();
+    }
+    return *reinterpret_cast<const DevTables*>(st.raw);
+}
+
+template <bool kMixed, bool kRta>
+__global__ void __launch_bounds__(kTransportThreads) kf_transport(const BatchDesc D) {
+    __shared__ SharedTables st;
+    if (threadIdx.x == 0) st.owner = -1;
+    __syncthreads();
+    for (int vb = blockIdx.x; vb < D.total_carrier_blocks; vb += gridDim.x) {
+        const int i = batch_find(D.carrier_block, D.n, vb);
+        const int b0 = D.carrier_block[i];
+        const DevTables& T = stage_tables(st, D, i);
+        k_transport_body<kMixed, kRta>(T, D.states[i], D.cells[i], D.ledgers[i], vb - b0, D.carrier_block[i + 1] - b0);
+        __syncthreads();
+    }
+}
+
+template <bool kRta>
+__global__ void __launch_bounds__(kTransportThreads) kf_deferred(const BatchDesc D) {
+    __shared__ SharedTables st;
+    if (threadIdx.x == 0) st.owner = -1;
+    __syncthreads();
+    for (int vb = blockIdx.x; vb < D.total_carrier_blocks; vb += gridDim.x) {
+        const int i = batch_find(D.carrier_block, D.n, vb);
+        const int b0 = D.carrier_block[i];
+        const DevTables& T = stage_tables(st, D, i);
+        k_deferred_body<kRta>(T, D.states[i], D.cells[i], D.ledgers[i], vb - b0, D.carrier_block[i + 1] - b0);
+        __syncthreads();
+    }
+}
+
+// Hole scans of the batch: one warp per 1024-slot hole block, lane l covering
+// slots [32 l, 32 l + 32) of it, so ranks still follow the slot order of
+// k_dead_count / k_dead_write.
+__device__ __forceinline__ unsigned dead_bits(const uint8_t* __restrict__ alive, int k0, int n) {
+    unsigned m = 0;
+    if (k0 + 32 <= n) { // k0 is a multiple of 32: both 16-byte loads are aligned and in bounds
+        const uint4* p = reinterpret_cast<const uint4*>(alive + k0);
+        const uint4 a = p[0], b = p[1];
+        const unsigned w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+                if (((w[q] >> (8 * t)) & 0xFFu) == 0u) m |= 1u << (4 * q + t);
+    } else {
+        for (int t = 0; t < 32 && k0 + t < n; ++t)
+            if (!alive[k0 + t]) m |= 1u << t;
+    }
+    return m;
+}
+
+__global__ void __launch_bounds__(256) kf_dead_count(const BatchDesc D) {
+    const int lane = threadIdx.x & 31;
+    const int nw = static_cast<int>((gridDim.x * blockDim.x) >> 5);
+    for (int vb = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5); vb < D.total_hole_blocks; vb += nw) {
+        const int i = batch_find(D.hole_block, D.n, vb); // warp-uniform
+        const int b = vb - D.hole_block[i];
+        const int n = D.ledgers[i]->n_slots;
+        int c = __popc(dead_bits(D.states[i].alive, b * kHoleBlock + 32 * lane, n));
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+        if (lane == 0) D.hole_counts[i][b] = c;
+    }
+}
+
+__global__ void __launch_bounds__(1024) kf_inject_prepare(const BatchDesc D) {
+    const int i = blockIdx.x;
+    k_inject_prepare_body(D.tables[i], D.ledgers[i], D.hole_counts[i], D.hole_block[i + 1] - D.hole_block[i],
+                          D.capacity[i], 0, 1);
+}
+
+__global__ void __launch_bounds__(256) kf_dead_write(const BatchDesc D) {
+    const int lane = threadIdx.x & 31;
+    const int nw = static_cast<int>((gridDim.x * blockDim.x) >> 5);
+    for (int vb = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5); vb < D.total_hole_blocks; vb += nw) {
+        const int i = batch_find(D.hole_block, D.n, vb); // warp-uniform
+        const int b = vb - D.hole_block[i];
+        const DevLedger* L = D.ledgers[i];
+        const int n = L->n_slots, need = L->n_inject;
+        if (need == 0 || b * kHoleBlock >= n) continue; // warp-uniform
+        const int k0 = b * kHoleBlock + 32 * lane;
+        unsigned m = dead_bits(D.states[i].alive, k0, n);
+        const int c = __popc(m);
+        int x = c;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        int rank = D.hole_counts[i][b] + x - c;
+        int* holes = D.holes[i];
+        while (m && rank < need) {
+            const int t = __ffs(m) - 1;
+            m &= m - 1u;
+            holes[rank++] = k0 + t;
+        }
+    }
+}
+
+template <bool kMixed, bool kRta>
+__global__ void __launch_bounds__(256) kf_inject(const BatchDesc D) {
+    for (int vb = blockIdx.x; vb < D.total_inject_blocks; vb += gridDim.x) {
+        const int i = batch_find(D.inject_block, D.n, vb);
+        const int b0 = D.inject_block[i];
+        k_inject_body<kMixed, kRta, false>(D.tables[i], D.states[i], D.cells[i], D.ledgers[i], D.holes[i], vb - b0,
+                                           D.inject_block[i + 1] - b0);
+        __syncthreads();
+    }
+}
+
+__global__ void kf_inject_finish(const BatchDesc D) {
+    if (threadIdx.x == 0) k_inject_finish_body(D.ledgers[blockIdx.x], 0, 1);
+}
+
+int launch_fused_transport(const BatchDesc& D, cudaStream_t s, bool mixed) {
+    const int g = std::min(D.total_carrier_blocks, D.persist);
+    const int gh = std::min((D.total_hole_blocks + 7) / 8, D.persist);
+    const int gi = std::min(D.total_inject_blocks, D.persist);
+    if (mixed) {
+        kf_transport<true, true><<<g, kTransportThreads, 0, s>>>(D);
+        kf_deferred<true><<<g, kTransportThreads, 0, s>>>(D);
+    } else {
+        kf_transport<false, true><<<g, kTransportThreads, 0, s>>>(D);
+    }
+    kf_dead_count<<<gh, 256, 0, s>>>(D);
+    kf_inject_prepare<<<D.n, 1024, 0, s>>>(D);
+    kf_dead_write<<<gh, 256, 0, s>>>(D);
+    if (mixed) kf_inject<true, true><<<gi, 256, 0, s>>>(D);
+    else kf_inject<false, true><<<gi, 256, 0, s>>>(D);
+    kf_inject_finish<<<D.n, 32, 0, s>>>(D);
+    return mixed ? 7 : 6;
 }
 
 } // namespace phmc

@@ -454,10 +454,10 @@ def test_batch_matches_single_instances(gpu):
     films = workloads.batched_films(n=4, seed=3, precision="mixed", particles_per_10nm=200)
     m = abi.Material(gpu, "phmc_", synthetic.make_material(mesh=16), 0.1, False, False)
     b = abi.Batch(gpu, films, [m])
-    b.run(8)
+    b.run(12)  # past a flux observation (every 10 steps) on the batch's own streams
     for i, cfg in enumerate(films):
         s = abi.Solver(gpu, "phmc_", cfg, [m])
-        s.run(8)
+        s.run(12)
         st, sb = s.stats(), b.stats(i)
         for k in ("current_timestep", "particle_count", "absorbed_total", "injected_total"):
             assert st[k] == sb[k], (i, k)
