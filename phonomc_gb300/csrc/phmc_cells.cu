@@ -250,11 +250,7 @@ __device__ __forceinline__ double warp_sum_uniform(double x) {
 // iteration, with warp reductions instead of block barriers. Used when cells
 // are many (a mesh grid): a cell's class loop is short and the block-wide
 // reductions, not the arithmetic, set the time per iteration.
-__global__ void __launch_bounds__(256) k_rta_solve_warp(const DevTables* __restrict__ Tp, CellArrays C) {
-    const DevTables& T = *Tp;
-    const int lane = threadIdx.x & 31;
-    const int c = static_cast<int>((blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x) >> 5);
-    if (c >= C.ncells) return; // warp-uniform
+__device__ __forceinline__ void rta_solve_warp_cell(const DevTables& T, const CellArrays& C, int c, int lane) {
     const DevMaterial& M = T.mat[C.cell_material[c]];
     const int nc = M.n_classes;
     const size_t hb = static_cast<size_t>(c) * C.hist_modes;
@@ -324,6 +320,12 @@ __global__ void __launch_bounds__(256) k_rta_solve_warp(const DevTables* __restr
         }
     }
     for (int k = lane; k < nc; k += 32) ab[k].y = bose_dev(Ts, fmax(0.0, M.class_omega[k]));
+}
+
+__global__ void __launch_bounds__(256) k_rta_solve_warp(const DevTables* __restrict__ Tp, CellArrays C) {
+    const int c = static_cast<int>((blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x) >> 5);
+    if (c >= C.ncells) return; // warp-uniform
+    rta_solve_warp_cell(*Tp, C, c, threadIdx.x & 31);
 }
 
 // ----------------------------------------------------- linear response
@@ -1020,9 +1022,12 @@ __global__ void kf_cell_state(const BatchDesc D, int phase) {
     k_cell_state_body(D.tables[i], D.cells[i], D.ledgers[i], phase, blockIdx.x - b0, D.cell_block[i + 1] - b0);
 }
 
+// one warp per cell of every instance
 __global__ void __launch_bounds__(256) kf_rta_solve(const BatchDesc D) {
-    const int i = batch_find(D.cell_begin, D.n, blockIdx.x);
-    k_rta_solve_body(D.tables[i], D.cells[i], blockIdx.x - D.cell_begin[i], D.cell_begin[i + 1] - D.cell_begin[i]);
+    const int g = static_cast<int>((blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x) >> 5);
+    if (g >= D.total_cells) return; // warp-uniform
+    const int i = batch_find(D.cell_begin, D.n, g);
+    rta_solve_warp_cell(*D.tables[i], D.cells[i], g - D.cell_begin[i], threadIdx.x & 31);
 }
 
 __global__ void __launch_bounds__(kStatThreads) kf_cell_tables(const BatchDesc D, int phase) {
@@ -1038,7 +1043,7 @@ __global__ void __launch_bounds__(1024) kf_cells_final(const BatchDesc D, int ph
 int launch_fused_cells(const BatchDesc& D, cudaStream_t s) {
     kf_cell_stats<<<dim3(D.chunks, D.total_cells), kStatThreads, 0, s>>>(D);
     kf_cell_state<<<D.total_cell_blocks, 256, 0, s>>>(D, 1);
-    kf_rta_solve<<<D.total_cells, 256, 0, s>>>(D);
+    kf_rta_solve<<<(D.total_cells + 7) / 8, 256, 0, s>>>(D);
     kf_cell_tables<<<dim3(D.chunks, D.total_cells), kStatThreads, 0, s>>>(D, 1);
     kf_cells_final<<<D.n, 1024, 0, s>>>(D, 1);
     return 5;
