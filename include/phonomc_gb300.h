@@ -141,6 +141,7 @@ typedef struct phmc_config {
     const phmc_heat_source* heat_source; /* NULL: no heat source */
     const phmc_mesh_domain* mesh;    /* NULL: the analytic box of sizes / face_condition */
     const char* material_folder;     /* NULL or a label reported in summary.txt */
+    int32_t write_cell_heat_flux;    /* simulation.write_cell_heat_flux: grid_heat_flux.csv rows */
 } phmc_config;
 
 /* Getters of include/MonteCarloSolver.h:59-101 plus the last step's ledger. */

@@ -712,6 +712,21 @@ std::string cmd_mesh(const std::string& stl) {
 // domain <toml>: SimulationDomain of a mesh TOML (facets, boundary assignment,
 // periodic pairs, cells and the voxel map), membership / nearest-facet / cell
 // queries at random points, and the domain summary file it writes.
+// A text file as a JSON string body (quotes, backslashes, newlines, tabs escaped).
+std::string escaped_file(const std::filesystem::path& path) {
+    std::ifstream in(path);
+    std::ostringstream text;
+    text << in.rdbuf();
+    std::string esc;
+    for (char c : text.str()) {
+        if (c == '"' || c == '\\') esc.push_back('\\');
+        if (c == '\n') esc += "\\n";
+        else if (c == '\t') esc += "\\t";
+        else esc.push_back(c);
+    }
+    return esc;
+}
+
 std::string cmd_domain(const std::string& toml) {
     SimulationConfig a = load_simulation_config(toml);
     SimulationDomain d(a);
@@ -774,17 +789,7 @@ std::string cmd_domain(const std::string& toml) {
     j.arr("inside", inside);
     j.arr("nearest_facet", nearest);
     j.arr("cell", cell);
-    std::ifstream summary(std::filesystem::path(a.output_folder) / "summary.txt");
-    std::ostringstream text;
-    text << summary.rdbuf();
-    std::string esc;
-    for (char c : text.str()) {
-        if (c == '"' || c == '\\') esc.push_back('\\');
-        if (c == '\n') esc += "\\n";
-        else if (c == '\t') esc += "\\t";
-        else esc.push_back(c);
-    }
-    j.put_s("domain_summary", esc);
+    j.put_s("domain_summary", escaped_file(std::filesystem::path(a.output_folder) / "summary.txt"));
     return j.str();
 }
 
@@ -904,6 +909,9 @@ std::string cmd_run(const std::string& pmat, const std::string& toml, int steps)
         }
         rows << "]";
         j.raw("convergence", rows.str());
+        const std::filesystem::path dir(a.output_folder);
+        for (const char* f : {"convergence.txt", "grid_heat_flux.csv", "heat_source_ledger.txt"})
+            if (std::filesystem::exists(dir / f)) j.put_s(std::string("file:") + f, escaped_file(dir / f));
     }
     j.arr3("grid_centers", d.grid_centers());
     j.arr("particle_count", pc);

@@ -152,6 +152,7 @@ class ConfigPOD(C.Structure):
         ("material_interface_positions", c_double_p), ("interface_frequency_bin_thz", C.c_double),
         ("precision", C.c_int32), ("heat_source", C.POINTER(HeatSourcePOD)),
         ("mesh", C.POINTER(MeshDomainPOD)), ("material_folder", C.c_char_p),
+        ("write_cell_heat_flux", C.c_int32),
     ]
 
 
@@ -230,6 +231,7 @@ def config_pod(cfg: dict):
     c.convergence_write_interval = int(cfg.get("convergence_write_interval", 10))
     c.random_seed = int(cfg.get("random_seed", 12345))
     c.compute_kappa = int(cfg.get("compute_kappa", False))
+    c.write_cell_heat_flux = int(cfg.get("write_cell_heat_flux", False))
     c.transport_axis = int(cfg.get("transport_axis", -1))
     g = cfg.get("temperature_gradient")
     c.has_temperature_gradient = int(g is not None)

@@ -703,13 +703,13 @@ __global__ void __launch_bounds__(kStatThreads) k_source(const DevTables* __rest
     if (threadIdx.x == 0) {
         if (next) {
             C.src_step_pending[c] = C.src_pending[c];
-            C.src_next_accrued[c] = 0.0;
+            C.src_step_book[c] = C.src_prescribed[c];
+            C.src_step_book[C.ncells + c] = C.src_deposited[c];
         }
         if (factor > 0.0) {
             const double e = C.src_rate[c] * factor;
             C.src_prescribed[c] += e;
             C.src_pending[c] += e;
-            if (next) C.src_next_accrued[c] = e;
         }
         s_pend = C.src_pending[c];
     }

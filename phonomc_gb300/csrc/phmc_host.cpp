@@ -1306,7 +1306,8 @@ std::string format_convergence_row(const ConvergenceRow& s) {
     out << " " << s.heat_flux << " " << s.kappa_int << " " << s.kappa_eff << " " << s.particle_count << " "
         << s.absorbed << " " << s.injected << " " << 0 << " " << s.net << " " << s.absorbed_ev << " "
         << s.injected_ev << " " << s.source_updates << " " << s.source_ev << " " << s.lifetime_residual << " "
-        << s.balance_residual << " " << s.thermal_energy << " " << 0 << " " << 0 << " " << 0;
+        << s.balance_residual << " " << s.thermal_energy << " " << s.source_prescribed << " " << s.source_pending << " "
+        << (s.source_prescribed - s.source_deposited - s.source_pending);
     if (s.gradient) out << " " << s.gradient_updates << " " << s.gradient_energy;
     out << '\n';
     return out.str();

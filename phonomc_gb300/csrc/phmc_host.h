@@ -79,6 +79,7 @@ struct SimulationConfig {
     std::vector<double> boundary_values;   // K for 'T', roughness in nm for 'R', 0 for 'P'
     std::vector<std::array<double, 6>> periodic_pair; // region pairs, matched facet by facet
     std::string output_folder;
+    bool write_cell_heat_flux = false; // grid_heat_flux.csv also without a gradient drive
     std::string material_folder; // reported in summary.txt; tables enter as arrays
     // Layered materials (include/SimulationConfig.h:93-99): N materials, N-1 planes.
     int material_interface_axis = 0;
@@ -556,6 +557,7 @@ struct ConvergenceRow {
     double absorbed_ev = 0, injected_ev = 0;
     long long source_updates = 0;
     double source_ev = 0, lifetime_residual = 0, balance_residual = 0, thermal_energy = 0;
+    double source_prescribed = 0, source_pending = 0, source_deposited = 0;
     bool gradient = false;
     long long gradient_updates = 0;
     double gradient_energy = 0;
@@ -590,6 +592,12 @@ struct RunSummary {
 std::string format_domain_summary(const SimulationConfig& cfg, const SimulationDomain& domain);
 std::string format_grid_centers(const SimulationDomain& domain);
 std::string format_run_summary(const RunSummary& s);
+std::string format_cell_flux_header();
+std::string format_cell_flux_rows(int timestep, double time_ps, const std::vector<double>& temperatures,
+                                  const std::vector<double>& q);
+std::string format_source_ledger(const SimulationConfig& c, const SimulationDomain& d, const std::vector<int>& material,
+                                 const std::vector<double>& rate_evps, const double* prescribed,
+                                 const double* deposited, const double* pending);
 std::string format_runtime(long long total_seconds);
 
 } // namespace phmc

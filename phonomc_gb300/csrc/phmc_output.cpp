@@ -331,6 +331,41 @@ std::string format_run_summary(const RunSummary& s) {
     return out.str();
 }
 
+// grid_heat_flux.csv (src/solver/ResultWriter.cpp:35-42, 52-65): the header
+// when the run starts, then per observation one row per cell at 17 digits.
+std::string format_cell_flux_header() { return "timestep,time_ps,cell_index,temperature_K,qx_W_m2,qy_W_m2,qz_W_m2\n"; }
+
+std::string format_cell_flux_rows(int timestep, double time_ps, const std::vector<double>& temperatures,
+                                  const std::vector<double>& q) {
+    std::ostringstream out;
+    out << std::setprecision(17);
+    for (size_t c = 0; c < temperatures.size(); ++c)
+        out << timestep << ',' << time_ps << ',' << c << ',' << temperatures[c] << ',' << q[3 * c] << ','
+            << q[3 * c + 1] << ',' << q[3 * c + 2] << '\n';
+    return out.str();
+}
+
+// heat_source_ledger.txt (src/solver/ResultWriter.cpp:343-354): per cell its
+// centre (Angstrom), material, base power (W) and prescribed / deposited /
+// pending energies (eV).
+std::string format_source_ledger(const SimulationConfig& c, const SimulationDomain& d, const std::vector<int>& material,
+                                 const std::vector<double>& rate_evps, const double* prescribed,
+                                 const double* deposited, const double* pending) {
+    const char* spectrum = c.heat_source_spectrum == HeatSourceSpectrum::Gaussian  ? "gaussian"
+                           : c.heat_source_spectrum == HeatSourceSpectrum::Weighted ? "weighted"
+                                                                                    : "thermal";
+    std::ostringstream out;
+    out << std::setprecision(17) << "# prescribed_lattice_power; not an electron-phonon calculation\n"
+        << "# spectrum=" << spectrum << "; pending energy is not yet represented by phonons\n"
+        << "# cell x_A y_A z_A material base_power_W prescribed_eV deposited_eV pending_eV\n";
+    const auto& centers = d.grid_centers();
+    for (size_t k = 0; k < rate_evps.size(); ++k)
+        out << k << " " << centers[k][0] << " " << centers[k][1] << " " << centers[k][2] << " " << material[k] << " "
+            << rate_evps[k] / 6.241509074e6 << " " << prescribed[k] << " " << deposited[k] << " " << pending[k]
+            << '\n';
+    return out.str();
+}
+
 std::string format_runtime(long long sec) {
     const long long days = sec / (24 * 3600), hours = (sec % (24 * 3600)) / 3600, minutes = (sec % 3600) / 60,
                     seconds = sec % 60;

@@ -86,6 +86,8 @@ DeviceSolver::DeviceSolver(const SimulationConfig& cfg, const std::vector<const 
         std::filesystem::create_directories(cfg_.output_folder);
         std::ofstream(std::filesystem::path(cfg_.output_folder) / "convergence.txt")
             << format_convergence_header(ncells_, cfg_.temperature_gradient.has_value());
+        if (cfg_.temperature_gradient || cfg_.write_cell_heat_flux)
+            std::ofstream(std::filesystem::path(cfg_.output_folder) / "grid_heat_flux.csv") << format_cell_flux_header();
     }
     flux_pass();
 }
@@ -102,6 +104,7 @@ DeviceSolver::~DeviceSolver() {
         cudaFreeHost(o->E);
         cudaFreeHost(o->q);
         cudaFreeHost(o->L);
+        if (o->src) cudaFreeHost(o->src);
         cudaEventDestroy(o->done);
         delete o;
     }
@@ -432,7 +435,7 @@ void DeviceSolver::upload_tables() {
         C.src_prescribed = dalloc<double>(ncells_);
         C.src_deposited = dalloc<double>(ncells_);
         C.src_step_pending = dalloc<double>(ncells_);
-        C.src_next_accrued = dalloc<double>(ncells_);
+        C.src_step_book = dalloc<double>(2 * static_cast<size_t>(ncells_));
         C.src_classes = std::max(1, max_src_classes);
         C.src_scratch = dalloc<double>(static_cast<size_t>(ncells_) * 2 * C.src_classes);
         C.src_next = dalloc<double>(hist);
@@ -831,6 +834,7 @@ void DeviceSolver::flux_pass() {
         PHMC_CUDA(cudaMallocHost(&o->E, ncells_ * sizeof(double)));
         PHMC_CUDA(cudaMallocHost(&o->q, 3 * ncells_ * sizeof(double)));
         PHMC_CUDA(cudaMallocHost(&o->L, sizeof(DevLedger)));
+        if (P_.source.enabled) PHMC_CUDA(cudaMallocHost(&o->src, 3 * ncells_ * sizeof(double)));
         PHMC_CUDA(cudaEventCreateWithFlags(&o->done, cudaEventDisableTiming));
     }
     o->step = step_;
@@ -843,6 +847,11 @@ void DeviceSolver::flux_pass() {
     PHMC_CUDA(cudaMemcpyAsync(o->E, cells_.energy_final, ncells_ * sizeof(double), cudaMemcpyDeviceToHost, stream_));
     PHMC_CUDA(cudaMemcpyAsync(o->q, cells_.flux, 3 * ncells_ * sizeof(double), cudaMemcpyDeviceToHost, stream_));
     PHMC_CUDA(cudaMemcpyAsync(o->L, d_ledger_, sizeof(DevLedger), cudaMemcpyDeviceToHost, stream_));
+    if (o->src) {
+        const size_t b = ncells_ * sizeof(double);
+        PHMC_CUDA(cudaMemcpyAsync(o->src, cells_.src_step_book, 2 * b, cudaMemcpyDeviceToHost, stream_));
+        PHMC_CUDA(cudaMemcpyAsync(o->src + 2 * ncells_, cells_.src_step_pending, b, cudaMemcpyDeviceToHost, stream_));
+    }
     PHMC_CUDA(cudaEventRecord(o->done, stream_));
     obs_pending_.push_back(o);
 }
@@ -963,13 +972,11 @@ void DeviceSolver::read_stats(phmc_stats& o) {
     o.kappa_endpoints = kappa_end_;
     if (P_.source.enabled) {
         // budgets at the step boundary: the next step's first half is already accrued here
-        std::vector<double> pr(ncells_), pe(ncells_), na(ncells_);
-        PHMC_CUDA(cudaMemcpy(pr.data(), cells_.src_prescribed, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
-        PHMC_CUDA(cudaMemcpy(pe.data(), cells_.src_step_pending, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
-        PHMC_CUDA(cudaMemcpy(na.data(), cells_.src_next_accrued, ncells_ * sizeof(double), cudaMemcpyDeviceToHost));
+        std::vector<double> h(3 * static_cast<size_t>(ncells_));
+        read_source_book(h.data());
         for (int c = 0; c < ncells_; ++c) {
-            o.prescribed_heat_source_energy_ev += pr[c] - na[c];
-            o.pending_heat_source_energy_ev += pe[c];
+            o.prescribed_heat_source_energy_ev += h[c];
+            o.pending_heat_source_energy_ev += h[2 * ncells_ + c];
         }
     }
     o.device_launches = counters_.launches;
@@ -1028,8 +1035,38 @@ void DeviceSolver::append_convergence_row(const Observation& o, const phmc_stats
     r.gradient = cfg_.temperature_gradient.has_value();
     r.gradient_updates = s.step_gradient_updates;
     r.gradient_energy = s.step_gradient_energy_ev;
-    std::ofstream(std::filesystem::path(cfg_.output_folder) / "convergence.txt", std::ios::app)
-        << format_convergence_row(r);
+    r.source_updates = s.step_heat_source_updates;
+    r.source_ev = s.step_heat_source_energy_ev;
+    if (o.src) {
+        // src/solver/PrescribedHeatSource.cpp:265-275: sums in cell order
+        for (int c = 0; c < ncells_; ++c) {
+            r.source_prescribed += o.src[c];
+            r.source_deposited += o.src[ncells_ + c];
+            r.source_pending += o.src[2 * ncells_ + c];
+        }
+    }
+    const std::filesystem::path dir(cfg_.output_folder);
+    std::ofstream(dir / "convergence.txt", std::ios::app) << format_convergence_row(r);
+    if (cfg_.temperature_gradient || cfg_.write_cell_heat_flux)
+        std::ofstream(dir / "grid_heat_flux.csv", std::ios::app) << format_cell_flux_rows(o.step, o.elapsed, host_T_, host_q_);
+    if (o.src) write_source_ledger(o.src, o.src + ncells_, o.src + 2 * ncells_);
+}
+
+// Per-cell prescribed, deposited and pending heat-source energy at the step
+// boundary (the device has already accrued, and maybe deposited, the next
+// step's first half): [3 ncells].
+void DeviceSolver::read_source_book(double* h) {
+    synchronize();
+    const size_t b = ncells_ * sizeof(double);
+    PHMC_CUDA(cudaMemcpy(h, cells_.src_step_book, 2 * b, cudaMemcpyDeviceToHost));
+    PHMC_CUDA(cudaMemcpy(h + 2 * ncells_, cells_.src_step_pending, b, cudaMemcpyDeviceToHost));
+}
+
+// heat_source_ledger.txt, rewritten with every convergence row and at the
+// end of the run (src/solver/Diagnostics.cpp:206-224).
+void DeviceSolver::write_source_ledger(const double* prescribed, const double* deposited, const double* pending) const {
+    std::ofstream(std::filesystem::path(cfg_.output_folder) / "heat_source_ledger.txt")
+        << format_source_ledger(cfg_, *domain_, P_.cell_material, P_.source.rates, prescribed, deposited, pending);
 }
 
 void DeviceSolver::write_outputs() {
@@ -1091,6 +1128,11 @@ void DeviceSolver::append_summary(long long total_seconds) {
     std::ofstream out(std::filesystem::path(cfg_.output_folder) / "summary.txt", std::ios::app);
     out << format_runtime(total_seconds) << format_run_summary(r);
     if (!out) throw std::runtime_error("Cannot append runtime summary.txt.");
+    if (P_.source.enabled) {
+        std::vector<double> h(3 * static_cast<size_t>(ncells_));
+        read_source_book(h.data());
+        write_source_ledger(h.data(), h.data() + ncells_, h.data() + 2 * ncells_);
+    }
 }
 
 } // namespace phmc

@@ -92,7 +92,7 @@ struct CellArrays {
     double* src_prescribed;
     double* src_deposited;
     double* src_step_pending;  // budget at the step boundary, before the next step's first accrual
-    double* src_next_accrued;  // the next step's first accrual (already in src_prescribed)
+    double* src_step_book;     // [2 ncells] prescribed, deposited at the step boundary, before the next step's first accrual
     double* src_scratch;
     double* src_next;        // [ncells * hist_modes] next step's first source half inside ab.y (null: no source)
     int src_classes;
@@ -118,6 +118,7 @@ struct Observation {
     double* T = nullptr;
     double* E = nullptr;
     double* q = nullptr;
+    double* src = nullptr; // heat source: per-cell prescribed, deposited, pending (eV)
     DevLedger* L = nullptr;
     cudaEvent_t done = nullptr;
 };
@@ -146,6 +147,8 @@ public:
                       const uint32_t* mode, const uint8_t* alive,
                       bool keep_clock = false);
     void write_outputs();
+    void write_source_ledger(const double* prescribed, const double* deposited, const double* pending) const;
+    void read_source_book(double* h);
     void append_summary(long long total_seconds);
     bool mixed() const { return mixed_; }
     // Deterministic sub-steps on the current population (parity entry points):

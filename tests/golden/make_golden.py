@@ -287,6 +287,28 @@ def full_runs_bilayer(pmats: str, tmp: str) -> dict:
     return out
 
 
+# Output files of a short FinFET run with its heat source and per-cell heat
+# flux rows (simulation.write_cell_heat_flux): convergence.txt,
+# grid_heat_flux.csv and heat_source_ledger.txt as the reference writes them.
+FILES_STEPS = 2
+
+
+def output_files_finfet(mpath: str, fpath: str, tmp: str) -> dict:
+    folder = os.path.join(tmp, "files_finfet")
+    os.makedirs(folder, exist_ok=True)
+    toml = os.path.join(folder, "c3.toml")
+    text = FINFET_TOML.format(stl=fpath, particles=2000, steps=FILES_STEPS, seed=5, nx=FINFET_GRID[0],
+                              ny=FINFET_GRID[1], nz=FINFET_GRID[2], source=FINFET_SOURCE_TOML, out=folder)
+    text = text.replace("convergence_write_interval = 1\n", "convergence_write_interval = 1\nwrite_cell_heat_flux = true\n", 1)
+    assert "write_cell_heat_flux" in text
+    with open(toml, "w") as f:
+        f.write(text)
+    res = json.loads(subprocess.run([HARNESS, "run", mpath, toml, str(FILES_STEPS)], check=True,
+                                    capture_output=True, text=True).stdout)
+    return {"particles": 2000, "seed": 5, "steps": FILES_STEPS, "grid": list(FINFET_GRID),
+            "files": {k[5:]: v for k, v in res.items() if k.startswith("file:")}}
+
+
 def build(ref: str) -> None:
     subprocess.run(["make", "-s", "-j8", f"REF={ref}"], cwd=os.path.join(ROOT, "oracle", "ref"),
                    check=True)
@@ -333,6 +355,12 @@ def main() -> None:
         with gzip.open(os.path.join(HERE, "fullrun_finfet.json.gz"), "wt") as f:
             json.dump(data, f)
         print("fullrun_finfet ok")
+    if not args.only or "files_finfet" in args.only:
+        data = output_files_finfet(mpath, fpath, tmp)
+        data["_harness_args"] = ["run", "{m}", "<FinFET toml, write_cell_heat_flux>", str(FILES_STEPS)]
+        with gzip.open(os.path.join(HERE, "files_finfet.json.gz"), "wt") as f:
+            json.dump(data, f)
+        print("files_finfet ok")
     for name, argv in CASES.items():
         if args.only and name not in args.only:
             continue

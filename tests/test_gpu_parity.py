@@ -524,3 +524,55 @@ def test_finfet_steps_match_oracle(gpu, orc, finfet_stl, source):
             for k in ("total_heat_source_energy_ev", "prescribed_heat_source_energy_ev"):
                 assert abs(stg[k] - sto[k]) <= 1e-12 * max(1.0, abs(sto[k])), k
     assert sto["absorbed_total"] > 0 and sto["injected_total"] > 0
+
+
+def test_output_files_finfet(gpu, finfet_stl, tmp_path):
+    """convergence.txt, grid_heat_flux.csv and heat_source_ledger.txt of a short
+    FinFET run with its heat source against the reference's files
+    (tests/golden/files_finfet): headers and layouts identical, the
+    deterministic columns (steps, times, cell ids and centres, materials, base
+    powers, prescribed energies) equal, the stochastic ones closing the ledger
+    (prescribed = deposited + pending per cell)."""
+    g = golden("files_finfet")
+    files = g["files"]
+    m = abi.Material(gpu, "phmc_", synthetic.make_material(mesh=8), 0.1, False, False)
+    out = tmp_path / "out"
+    cfg = workloads.finfet_mesh(finfet_stl, particles=g["particles"], seed=g["seed"], grid=tuple(g["grid"]))
+    cfg.update(iterations=g["steps"], convergence_write_interval=1, output_folder=str(out),
+               write_cell_heat_flux=True, material_folder="unused")
+    s = abi.Solver(gpu, "phmc_", cfg, [m])
+    s.run(g["steps"])
+    s.close()
+
+    ref = files["convergence.txt"].splitlines()
+    mine = (out / "convergence.txt").read_text().splitlines()
+    assert mine[0] == ref[0] and len(mine) == len(ref)
+    names = ref[0].split()[1:]
+    col = {n: i for i, n in enumerate(names)}
+    for a, b in zip(mine[1:], ref[1:]):
+        ta, tb = a.split(), b.split()
+        assert len(ta) == len(tb) == len(names)
+        assert ta[:2] == tb[:2]
+        for key in ("hs_prescribed_total_ev",):
+            assert np.isclose(float(ta[col[key]]), float(tb[col[key]]), rtol=1e-12, atol=0)
+        assert abs(float(ta[col["hs_ledger_residual_ev"]])) <= 1e-9 * max(1.0, float(tb[col["hs_prescribed_total_ev"]]))
+
+    ref = files["grid_heat_flux.csv"].splitlines()
+    mine = (out / "grid_heat_flux.csv").read_text().splitlines()
+    assert mine[0] == ref[0] and len(mine) == len(ref)
+    for a, b in zip(mine[1:], ref[1:]):
+        ta, tb = a.split(","), b.split(",")
+        assert len(ta) == 7 and ta[0] == tb[0] and ta[2] == tb[2]
+        assert float(ta[1]) == float(tb[1])
+        assert all(np.isfinite(float(x)) for x in ta[3:])
+
+    ref = files["heat_source_ledger.txt"].splitlines()
+    mine = (out / "heat_source_ledger.txt").read_text().splitlines()
+    assert mine[:3] == ref[:3] and len(mine) == len(ref)
+    for a, b in zip(mine[3:], ref[3:]):
+        ta, tb = a.split(), b.split()
+        assert ta[:5] == tb[:5]  # cell, centre (17 digits), material
+        pa, pb = [float(x) for x in ta[5:]], [float(x) for x in tb[5:]]
+        assert np.isclose(pa[0], pb[0], rtol=1e-12, atol=0)  # base power, W
+        assert np.isclose(pa[1], pb[1], rtol=1e-12, atol=0)  # prescribed, eV
+        assert np.isclose(pa[2] + pa[3], pa[1], rtol=1e-9, atol=1e-12 * max(1.0, pb[1]))
