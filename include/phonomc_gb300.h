@@ -26,6 +26,7 @@
  *                             src/material/Thermodynamics.cpp:173-175
  *   phmc_dev_rta_collide      RtaCollisionOperator::apply  src/solver/RtaCollisionOperator.cpp:13-189
  *   phmc_dev_linear_collide   CarrierCollisionOperator::apply src/solver/CarrierCollisionOperator.cpp:38-141
+ *   phmc_dev_ncallaway_evolve nonlinear_callaway_evolve src/solver/NonlinearCallawayCollision.cpp:216-248
  *   phmc_dev_rough_reflect    RoughBoundarySampler::sample src/solver/RoughBoundarySampler.cpp:459-533
  *   phmc_dev_gradient_drive   TemperatureGradientDrive::apply src/solver/TemperatureGradientDrive.cpp:116-171
  */
@@ -142,6 +143,7 @@ typedef struct phmc_config {
     const phmc_mesh_domain* mesh;    /* NULL: the analytic box of sizes / face_condition */
     const char* material_folder;     /* NULL or a label reported in summary.txt */
     int32_t write_cell_heat_flux;    /* simulation.write_cell_heat_flux: grid_heat_flux.csv rows */
+    int32_t callaway_nonlinear;      /* collision.callaway_formulation: 0 linearized, 1 nonlinear */
 } phmc_config;
 
 /* Getters of include/MonteCarloSolver.h:59-101 plus the last step's ledger. */
@@ -316,6 +318,13 @@ int phmc_dev_rta_collide(const phmc_material* m, int64_t n, const int32_t* flat_
                          double* occupation, int cells, const double* cell_temperature, double dt,
                          double particle_volume, int local_lifetime, double lifetime_temperature,
                          double* residual_ev);
+/* One cell of nonlinear Callaway (N(dt/2), R(dt), N(dt/2) moment-matched Bose BGK
+ * substeps): n_modes modes (omega rad/ps, wavevector[3*n_modes], normal and
+ * resistive rates 1/ps), n carriers with their mode index and occupation
+ * (updated in place) at cell temperature T (K) over dt (ps). */
+int phmc_dev_ncallaway_evolve(int32_t n_modes, const double* omega, const double* wavevector,
+                              const double* normal_rate, const double* resistive_rate, int64_t n,
+                              const int32_t* mode, double* occupation, double temperature, double dt);
 /* Linearized RTA (model 0) or Callaway (model 1) collision at reference temperature Tref. */
 int phmc_dev_linear_collide(const phmc_material* m, int model, double Tref, int64_t n, const int32_t* flat_mode,
                             const int32_t* cell, double* occupation, int cells, double dt, double particle_volume,

@@ -562,6 +562,162 @@ long double linear_cell(const std::vector<int>& members, const MaterialTables& T
     return res * cell_weight;
 }
 
+// ------------------------------------------ nonlinear Callaway per cell
+// src/solver/NonlinearCallawayCollision.cpp:25-248, per carrier and in long
+// double as the reference: three BGK substeps N(dt/2), R(dt), N(dt/2), each
+// n <- (1-a) n + a n_target with a = 1 - exp(-rate dt) and n_target a
+// displaced Bose distribution 1/expm1(phi), phi = sum_j lambda_j b_j. The
+// basis b_j is the a-weighted orthonormalised set {hw/kT, k_x, k_y, k_z}
+// (energy only for resistive substeps); lambda solves the moment equations
+// sum a b_j (n - n_target) = 0 by damped Newton on the convex potential.
+namespace ncl {
+using LD = long double;
+constexpr double kHbarNcl = 6.582119569e-4, kKbNcl = 8.617333262145e-5;
+
+LD bose(LD x) { return x > 700 ? 0 : 1 / std::expm1(x); }
+
+void substep(const std::vector<double>& omega, const std::vector<std::array<double, 3>>& k,
+             const std::vector<double>& rate, double dt, bool normal, double T, std::vector<double>& n) {
+    const size_t N = n.size();
+    std::vector<LD> a(N), w(N), phi0(N);
+    LD activity = 0;
+    for (size_t i = 0; i < N; ++i) {
+        a[i] = -std::expm1(-rate[i] * dt);
+        activity += a[i];
+        phi0[i] = kHbarNcl * omega[i] / (kKbNcl * T);
+        const LD e = bose(phi0[i]);
+        w[i] = a[i] * e * (1 + e);
+    }
+    if (activity == 0) return;
+    auto dot = [&](const std::vector<LD>& u, const std::vector<LD>& v) {
+        LD s = 0;
+        for (size_t i = 0; i < N; ++i) s += w[i] * u[i] * v[i];
+        return s;
+    };
+    std::vector<std::vector<LD>> basis;
+    LD lambda[4] = {0, 0, 0, 0};
+    for (int j = 0; j < (normal ? 4 : 1); ++j) {
+        std::vector<LD> v(N);
+        for (size_t i = 0; i < N; ++i) v[i] = j == 0 ? phi0[i] : static_cast<LD>(k[i][j - 1]);
+        const LD norm0 = std::sqrt(dot(v, v));
+        if (norm0 == 0) continue;
+        for (auto& x : v) x /= norm0;
+        for (int pass = 0; pass < 2; ++pass)
+            for (const auto& b : basis) {
+                const LD d = dot(v, b);
+                for (size_t i = 0; i < N; ++i) v[i] -= d * b[i];
+            }
+        const LD len = std::sqrt(dot(v, v));
+        if (len < 1e-12L) continue;
+        for (auto& x : v) x /= len;
+        if (j == 0) lambda[0] = norm0 * len;
+        basis.push_back(std::move(v));
+    }
+    const int dim = static_cast<int>(basis.size());
+    if (dim == 0) throw std::runtime_error("Nonlinear Callaway has no representable energy constraint");
+    LD scale[4] = {0, 0, 0, 0};
+    for (int j = 0; j < dim; ++j)
+        for (size_t i = 0; i < N; ++i)
+            scale[j] += std::abs(a[i] * basis[j][i]) * std::max(static_cast<LD>(n[i]), bose(phi0[i]));
+    std::vector<LD> target(N);
+    // potential F(lambda) = sum a (-log(1 - e^-phi) + n phi), gradient g, Hessian H
+    auto potential = [&](const LD* x, LD* g, LD (*H)[4], bool keep) {
+        for (int j = 0; j < 4; ++j) {
+            g[j] = 0;
+            if (H)
+                for (int l = 0; l < 4; ++l) H[j][l] = 0;
+        }
+        LD F = 0;
+        for (size_t i = 0; i < N; ++i) {
+            if (a[i] == 0) continue;
+            LD phi = 0;
+            for (int j = 0; j < dim; ++j) phi += x[j] * basis[j][i];
+            if (!(phi > 0) || !std::isfinite(phi)) return std::numeric_limits<LD>::infinity();
+            const LD e = bose(phi);
+            if (keep) target[i] = e;
+            F += a[i] * (-std::log(-std::expm1(-phi)) + n[i] * phi);
+            for (int j = 0; j < dim; ++j) {
+                g[j] += a[i] * basis[j][i] * (n[i] - e);
+                if (H)
+                    for (int l = 0; l < dim; ++l) H[j][l] += a[i] * basis[j][i] * basis[l][i] * e * (1 + e);
+            }
+        }
+        return F;
+    };
+    auto residual = [&](const LD* g) {
+        LD r = 0;
+        for (int j = 0; j < dim; ++j) r = std::max(r, std::abs(g[j]) / std::max(1e-30L, scale[j]));
+        return r;
+    };
+    bool converged = false;
+    for (int it = 0; it < 70; ++it) {
+        LD g[4], H[4][4];
+        const LD F = potential(lambda, g, H, true);
+        const LD err = residual(g);
+        if (err < 2e-13L) {
+            converged = true;
+            break;
+        }
+        LD step_dir[4];
+        for (int j = 0; j < dim; ++j) step_dir[j] = -g[j];
+        for (int j = 0; j < dim; ++j) { // Gaussian elimination, partial pivoting
+            int p = j;
+            for (int r = j + 1; r < dim; ++r)
+                if (std::abs(H[r][j]) > std::abs(H[p][j])) p = r;
+            if (!(std::abs(H[p][j]) > 1e-30L)) throw std::runtime_error("Singular nonlinear Callaway moment Jacobian");
+            for (int l = 0; l < 4; ++l) std::swap(H[j][l], H[p][l]);
+            std::swap(step_dir[j], step_dir[p]);
+            for (int r = j + 1; r < dim; ++r) {
+                const LD f = H[r][j] / H[j][j];
+                for (int l = j; l < dim; ++l) H[r][l] -= f * H[j][l];
+                step_dir[r] -= f * step_dir[j];
+            }
+        }
+        for (int j = dim - 1; j >= 0; --j) {
+            for (int l = j + 1; l < dim; ++l) step_dir[j] -= H[j][l] * step_dir[l];
+            step_dir[j] /= H[j][j];
+        }
+        LD slope = 0;
+        for (int j = 0; j < dim; ++j) slope += g[j] * step_dir[j];
+        bool ok = false;
+        for (LD t = 1; t > 1e-14L; t *= .5L) {
+            LD trial[4] = {lambda[0], lambda[1], lambda[2], lambda[3]}, gt[4];
+            for (int j = 0; j < dim; ++j) trial[j] += t * step_dir[j];
+            const LD Ft = potential(trial, gt, nullptr, false);
+            if (std::isfinite(Ft) && (Ft <= F + 1e-4L * t * slope || residual(gt) < err * .9L)) {
+                for (int j = 0; j < 4; ++j) lambda[j] = trial[j];
+                ok = true;
+                break;
+            }
+        }
+        if (!ok) throw std::runtime_error("Nonlinear Callaway moment line search failed");
+    }
+    if (!converged) throw std::runtime_error("Nonlinear Callaway moment solve did not converge");
+    for (size_t i = 0; i < N; ++i) {
+        if (!(a[i] > 0)) continue;
+        n[i] = static_cast<double>((1 - a[i]) * n[i] + a[i] * target[i]);
+        if (!std::isfinite(n[i]) || n[i] < 0) throw std::runtime_error("Nonlinear Callaway occupation is invalid");
+    }
+}
+
+// src/solver/NonlinearCallawayCollision.cpp:216-248
+std::vector<double> evolve(const std::vector<double>& omega, const std::vector<std::array<double, 3>>& k,
+                           const std::vector<double>& rn, const std::vector<double>& rr, std::vector<double> n, double T,
+                           double dt) {
+    if (n.empty() || !std::isfinite(T) || T <= 0 || !std::isfinite(dt) || dt < 0)
+        throw std::invalid_argument("Invalid nonlinear Callaway state");
+    for (size_t i = 0; i < n.size(); ++i)
+        if (!std::isfinite(n[i]) || n[i] < 0 || !(omega[i] > 0) || !std::isfinite(omega[i]) || !(rn[i] >= 0) ||
+            !(rr[i] >= 0) || !std::isfinite(rn[i]) || !std::isfinite(rr[i]))
+            throw std::invalid_argument("Invalid nonlinear Callaway mode");
+    if (dt == 0) return n;
+    substep(omega, k, rn, 0.5 * dt, true, T, n);
+    substep(omega, k, rr, dt, false, T, n);
+    substep(omega, k, rn, 0.5 * dt, true, T, n);
+    return n;
+}
+} // namespace ncl
+
 // ---------------------------------------------------------------- solver
 struct OracleSolver {
     SimulationConfig cfg;
@@ -1061,6 +1217,36 @@ struct OracleSolver {
             }
             return static_cast<double>(sum);
         }
+        if (cfg.callaway_nonlinear) {
+            // src/solver/NonlinearCallawayCollision.cpp:265-343
+            long double sum = 0;
+            for (size_t c = 0; c < members.size(); ++c) {
+                if (members[c].empty()) continue;
+                const int mid = P.cell_material[c];
+                const MaterialTables& T = P.mats[mid];
+                const double Tc = cell_T[c];
+                const double Tr = cfg.lifetime_temperature_is_local ? Tc : cfg.lifetime_temperature;
+                std::vector<double> om, rn, rr, n;
+                std::vector<std::array<double, 3>> kv;
+                for (int i : members[c]) {
+                    const int act = static_cast<int>(mode[i] & kActiveMask);
+                    const auto r = mats[mid]->mode_callaway_rates(Tr, T.active_flat[act]);
+                    om.push_back(T.omega[act]);
+                    kv.push_back({T.col_k[3 * act], T.col_k[3 * act + 1], T.col_k[3 * act + 2]});
+                    rn.push_back(r[0]);
+                    rr.push_back(r[1]);
+                    n.push_back(occ[i]);
+                }
+                const auto out = ncl::evolve(om, kv, rn, rr, n, Tc, dt);
+                long double r = 0;
+                for (size_t j = 0; j < out.size(); ++j) {
+                    occ[members[c][j]] = out[j];
+                    r += ncl::kHbarNcl * om[j] * (static_cast<long double>(out[j]) - n[j]);
+                }
+                sum += r * T.energy_weight;
+            }
+            return static_cast<double>(sum);
+        }
         std::vector<double> om(alive.size(), 0.0), a(alive.size(), 0.0);
         for (size_t i = 0; i < alive.size(); ++i) {
             if (!alive[i]) continue;
@@ -1402,6 +1588,25 @@ int orc_rta_collide(void* m, int64_t n, const int32_t* flat, const int32_t* cell
         for (int c = 0; c < cells; ++c) r += rta_cell(members[c], om, a, o, cell_T[c], w);
         std::copy(o.begin(), o.end(), occ);
         *residual = r;
+    });
+}
+
+// One cell of nonlinear Callaway: carriers with modes into the per-mode tables.
+int orc_ncallaway_evolve(int32_t n_modes, const double* omega, const double* k3, const double* rn, const double* rr,
+                         int64_t n, const int32_t* mode, double* occ, double T, double dt) {
+    return guard([&] {
+        std::vector<double> om(n), a(n), b(n), o(occ, occ + n);
+        std::vector<std::array<double, 3>> k(n);
+        for (int64_t i = 0; i < n; ++i) {
+            const int m = mode[i];
+            if (m < 0 || m >= n_modes) throw std::invalid_argument("Invalid nonlinear Callaway mode");
+            om[i] = omega[m];
+            k[i] = {k3[3 * m], k3[3 * m + 1], k3[3 * m + 2]};
+            a[i] = rn[m];
+            b[i] = rr[m];
+        }
+        const auto out = ncl::evolve(om, k, a, b, o, T, dt);
+        std::copy(out.begin(), out.end(), occ);
     });
 }
 

@@ -26,6 +26,7 @@
 #include "SurfaceMesh.h"
 #include "geometry/MeshReader.h"
 #include "solver/PrescribedHeatSource.h"
+#include "solver/NonlinearCallawayCollision.h"
 #include "solver/ParticleStorage.h"
 #include "solver/ReservoirSampler.h"
 #include "solver/RoughBoundarySampler.h"
@@ -862,6 +863,47 @@ std::string cmd_reservoir(const std::string& pmat) {
 
 // run <pmat> <toml> <steps>: full reference solver; prints per-step observables.
 // <pmat> may list several tables separated by commas (layered materials, in order).
+// Seeded single-cell cases for nonlinear_callaway_evolve: n_modes modes with
+// frequencies, wavevectors and N/R rates, n_carriers carriers drawn over the
+// modes (unique = one carrier per mode) with occupations around Bose at T.
+std::string cmd_ncallaway(int seed, int n_modes, int n_carriers, int unique) {
+    std::mt19937_64 g(static_cast<uint64_t>(seed));
+    std::uniform_real_distribution<double> u(0.0, 1.0);
+    const double T = 150.0 + 300.0 * u(g), dt = 0.25 + u(g);
+    std::vector<double> omega(n_modes), rn(n_modes), rr(n_modes);
+    std::vector<std::array<double, 3>> k(n_modes);
+    for (int m = 0; m < n_modes; ++m) {
+        omega[m] = 2.0 + 90.0 * u(g);
+        for (int a = 0; a < 3; ++a) k[m][a] = 2.0 * u(g) - 1.0;
+        rn[m] = 1.5 * u(g);
+        rr[m] = u(g) < 0.1 ? 0.0 : 0.8 * u(g);
+    }
+    std::vector<int> mode(n_carriers);
+    std::vector<double> n(n_carriers);
+    phonomc::CallawayData d;
+    for (int i = 0; i < n_carriers; ++i) {
+        mode[i] = unique ? i % n_modes : static_cast<int>(u(g) * n_modes) % n_modes;
+        const double x = 6.582119569e-4 * omega[mode[i]] / (8.617333262145e-5 * T);
+        n[i] = (1.0 / std::expm1(x)) * (0.5 + u(g));
+        d.omega.push_back(omega[mode[i]]);
+        d.wavevector.push_back(k[mode[i]]);
+        d.normal_rate.push_back(rn[mode[i]]);
+        d.resistive_rate.push_back(rr[mode[i]]);
+    }
+    const auto out = phonomc::nonlinear_callaway_evolve(d, n, T, dt);
+    Json j;
+    j.put("T", T);
+    j.put("dt", dt);
+    j.arr("omega", omega);
+    j.arr3("k", k);
+    j.arr("rn", rn);
+    j.arr("rr", rr);
+    j.arr("mode", mode);
+    j.arr("n", n);
+    j.arr("out", out);
+    return j.str();
+}
+
 std::string cmd_run(const std::string& pmat, const std::string& toml, int steps) {
     SimulationConfig a = load_simulation_config(toml);
     const bool stationary = uses_conservative_transport(a);
@@ -951,6 +993,8 @@ int main(int argc, char** argv) {
         else if (c == "interface") out = cmd_interface(argv[2], argv[3], std::atoi(argv[4]) != 0);
         else if (c == "reservoir") out = cmd_reservoir(argv[2]);
         else if (c == "run") out = cmd_run(argv[2], argv[3], std::atoi(argv[4]));
+        else if (c == "ncallaway")
+            out = cmd_ncallaway(std::atoi(argv[2]), std::atoi(argv[3]), std::atoi(argv[4]), std::atoi(argv[5]));
         else throw std::runtime_error("unknown command " + c);
         std::cout.rdbuf(saved);
         std::cout << out << std::endl;

@@ -152,7 +152,7 @@ class ConfigPOD(C.Structure):
         ("material_interface_positions", c_double_p), ("interface_frequency_bin_thz", C.c_double),
         ("precision", C.c_int32), ("heat_source", C.POINTER(HeatSourcePOD)),
         ("mesh", C.POINTER(MeshDomainPOD)), ("material_folder", C.c_char_p),
-        ("write_cell_heat_flux", C.c_int32),
+        ("write_cell_heat_flux", C.c_int32), ("callaway_nonlinear", C.c_int32),
     ]
 
 
@@ -232,6 +232,7 @@ def config_pod(cfg: dict):
     c.random_seed = int(cfg.get("random_seed", 12345))
     c.compute_kappa = int(cfg.get("compute_kappa", False))
     c.write_cell_heat_flux = int(cfg.get("write_cell_heat_flux", False))
+    c.callaway_nonlinear = int(cfg.get("callaway_formulation", "linearized") == "nonlinear")
     c.transport_axis = int(cfg.get("transport_axis", -1))
     g = cfg.get("temperature_gradient")
     c.has_temperature_gradient = int(g is not None)
@@ -426,6 +427,8 @@ class Solver(Handle):
 # Deterministic sub-step entry points; the CUDA library exports them with the
 # prefix phmc_dev_ and the oracle with orc_ (same signatures).
 SUBSTEP_PROTOS = {
+    "ncallaway_evolve": (C.c_int, [C.c_int32, c_double_p, c_double_p, c_double_p, c_double_p, C.c_int64, c_int32_p,
+                                   c_double_p, C.c_double, C.c_double]),
     "trace_box": (C.c_int, [c_double_p, c_double_p, C.c_int64, c_double_p, c_double_p, c_double_p, c_double_p,
                             c_int32_p]),
     "temperature_from_energy": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_double_p]),

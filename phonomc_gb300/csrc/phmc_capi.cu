@@ -107,6 +107,18 @@ struct DevHold {
         if (!v.empty()) cuda_check(cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy");
         return static_cast<T*>(d);
     }
+    template <class T> T* put(const T* v, size_t n) {
+        T* d = alloc<T>(n);
+        if (n) cuda_check(cudaMemcpy(d, v, n * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy");
+        return d;
+    }
+    template <class T> T* alloc(size_t n) {
+        void* d = nullptr;
+        cuda_check(cudaMalloc(&d, std::max<size_t>(1, n) * sizeof(T)), "cudaMalloc");
+        p.push_back(d);
+        cuda_check(cudaMemset(d, 0, std::max<size_t>(1, n) * sizeof(T)), "cudaMemset");
+        return static_cast<T*>(d);
+    }
 };
 
 // Membership, nearest facet and cell of points on the device copy of a mesh domain.
@@ -881,6 +893,42 @@ int phmc_dev_rta_collide(const phmc_material* m, int64_t n, const int32_t* flat,
         load_column(s, *m->m, c, n, flat, cell, occ);
         *residual = s.collide_only(cell_T);
         read_occupations(s, n, occ);
+    });
+}
+
+int phmc_dev_ncallaway_evolve(int32_t n_modes, const double* omega, const double* k3, const double* rn,
+                              const double* rr, int64_t n, const int32_t* mode, double* occ, double T, double dt) {
+    return guard([&] {
+        // src/solver/NonlinearCallawayCollision.cpp:216-239: argument checks
+        if (n <= 0 || n_modes <= 0 || !std::isfinite(T) || T <= 0 || !std::isfinite(dt) || dt < 0)
+            throw std::invalid_argument("Invalid nonlinear Callaway state");
+        for (int64_t i = 0; i < n; ++i) {
+            const int m = mode[i];
+            if (m < 0 || m >= n_modes || !std::isfinite(occ[i]) || occ[i] < 0 || !(omega[m] > 0) ||
+                !std::isfinite(omega[m]) || !(rn[m] >= 0) || !(rr[m] >= 0) || !std::isfinite(rn[m]) ||
+                !std::isfinite(rr[m]))
+                throw std::invalid_argument("Invalid nonlinear Callaway mode");
+            for (int k = 0; k < 3; ++k)
+                if (!std::isfinite(k3[3 * m + k])) throw std::invalid_argument("Invalid nonlinear Callaway wavevector");
+        }
+        const size_t nm = static_cast<size_t>(n_modes), nc = static_cast<size_t>(n);
+        DevHold h;
+        double* d_om = h.put(omega, nm);
+        double* d_k = h.put(k3, 3 * nm);
+        double* d_rn = h.put(rn, nm);
+        double* d_rr = h.put(rr, nm);
+        int32_t* d_mode = h.put(mode, nc);
+        double* d_occ = h.put(occ, nc);
+        double* d_cnt = h.alloc<double>(nm);
+        double2* d_ab = h.alloc<double2>(nm);
+        double2* d_work = h.alloc<double2>(nm);
+        int* d_status = h.alloc<int>(1);
+        launch_ncl_cell(n_modes, d_om, d_k, d_rn, d_rr, d_cnt, d_ab, d_work, n, d_mode, d_occ, T, dt, d_status, nullptr);
+        cuda_check(cudaGetLastError(), "k_ncl_cell launch");
+        int status = 0;
+        cuda_check(cudaMemcpy(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy");
+        if (status != 0) throw std::runtime_error(solver_error_message(status));
+        cuda_check(cudaMemcpy(occ, d_occ, nc * sizeof(double), cudaMemcpyDeviceToHost), "cudaMemcpy");
     });
 }
 

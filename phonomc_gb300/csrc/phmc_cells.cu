@@ -328,6 +328,393 @@ __global__ void __launch_bounds__(256) k_rta_solve_warp(const DevTables* __restr
     rta_solve_warp_cell(*Tp, C, c, threadIdx.x & 31);
 }
 
+// --------------------------------------------------- nonlinear Callaway
+// src/solver/NonlinearCallawayCollision.cpp:25-248. Per cell, three BGK
+// substeps N(dt/2), R(dt), N(dt/2) move every carrier n <- (1 - a) n + a t,
+// a = 1 - exp(-rate dt), t = 1/expm1(phi) a displaced Bose occupation with
+// phi = sum_j lambda_j b_j. The basis b_j orthonormalises {hw/kT, k_x, k_y,
+// k_z} (energy only for the resistive substep) in the inner product
+// sum a n_eq (1 + n_eq) u v; lambda matches the a-weighted moments of n by
+// damped Newton on the convex potential sum a (-log(1 - e^-phi) + n phi).
+// Carriers of one mode share every factor, so the sums run over the cell's
+// mode bins (count c, occupation sum N) and each substep is one affine map
+// per mode: the composition (alpha, beta) becomes the cell's pending update.
+// The basis is kept as coefficients over the four features, orthonormalised
+// through their 4 x 4 Gram matrix. The convergence scale uses
+// max(N, c t_eq) per mode for the per-carrier sum of max(n, t_eq) (equal when
+// a mode holds one carrier; the scale only normalises the stopping test).
+constexpr double kNclHbar = 6.582119569e-4, kNclKb = 8.617333262145e-5;
+constexpr int kNclThreads = 256;
+
+__device__ __forceinline__ double ncl_bose(double x) { return x > 700.0 ? 0.0 : 1.0 / expm1(x); }
+
+struct NclBlock {
+    double red[16 * 32];
+    double B[4][4];   // basis coefficients over (phi0, kx, ky, kz)
+    double y[4];      // phi = sum_k y_k f_k for the point being evaluated
+    double lambda[4], delta[4], scale[4];
+    int dim, status;
+};
+
+// Features of mode m in cell temperature T.
+template <class Modes>
+__device__ __forceinline__ void ncl_features(const Modes& Q, int m, double T, double (&f)[4]) {
+    f[0] = kNclHbar * Q.omega(m) / (kNclKb * T);
+    f[1] = Q.kx(m, 0);
+    f[2] = Q.kx(m, 1);
+    f[3] = Q.kx(m, 2);
+}
+
+// Potential, gradient and (want_h) Hessian at the point y of sh; returns
+// invalid (phi <= 0 or not finite somewhere) as +inf in v[0].
+template <class Modes>
+__device__ __forceinline__ void ncl_evaluate(const Modes& Q, NclBlock& sh, double2* work, double T, bool want_h,
+                                             double (&v)[16]) {
+    for (int k = 0; k < 16; ++k) v[k] = 0.0;
+    const int dim = sh.dim;
+    for (int m = threadIdx.x; m < Q.n; m += blockDim.x) {
+        const double c = Q.count(m);
+        const double a = work[m].y;
+        if (c == 0.0 || a == 0.0) continue;
+        double f[4];
+        ncl_features(Q, m, T, f);
+        const double phi = sh.y[0] * f[0] + sh.y[1] * f[1] + sh.y[2] * f[2] + sh.y[3] * f[3];
+        if (!(phi > 0.0) || !isfinite(phi)) {
+            v[15] = 1.0;
+            continue;
+        }
+        const double e = ncl_bose(phi);
+        const double N = work[m].x;
+        v[0] += a * (c * -log(-expm1(-phi)) + N * phi);
+        double b[4];
+        for (int j = 0; j < 4; ++j)
+            b[j] = j < dim ? sh.B[j][0] * f[0] + sh.B[j][1] * f[1] + sh.B[j][2] * f[2] + sh.B[j][3] * f[3] : 0.0;
+        for (int j = 0; j < 4; ++j) v[1 + j] += a * b[j] * (N - c * e);
+        if (want_h) {
+            const double h = a * c * e * (1.0 + e);
+            int q = 5;
+            for (int j = 0; j < 4; ++j)
+                for (int l = j; l < 4; ++l) v[q++] += h * b[j] * b[l];
+        }
+    }
+    block_sum<16>(v, sh.red);
+    if (v[15] != 0.0) v[0] = INFINITY;
+}
+
+__device__ __forceinline__ void ncl_set_point(NclBlock& sh, const double* x) {
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 4; ++k) {
+            double y = 0.0;
+            for (int j = 0; j < sh.dim; ++j) y += x[j] * sh.B[j][k];
+            sh.y[k] = y;
+        }
+    __syncthreads();
+}
+
+__device__ __forceinline__ double ncl_error(const NclBlock& sh, const double (&v)[16]) {
+    double e = 0.0;
+    for (int j = 0; j < sh.dim; ++j) e = fmax(e, fabs(v[1 + j]) / fmax(1e-30, sh.scale[j]));
+    return e;
+}
+
+// One cell: bins of Q (count, work.x = occupation sum on entry), rates by
+// Q.rate(m, normal). Writes (alpha, beta) per mode through Q.out(m, alpha,
+// beta); returns 0 or an error code (block-uniform).
+template <class Modes>
+__device__ int ncl_solve_cell(const Modes& Q, NclBlock& sh, double2* work, double T, double dt) {
+    if (threadIdx.x == 0) sh.status = 0;
+    for (int m = threadIdx.x; m < Q.n; m += blockDim.x) Q.out(m, 1.0, 0.0);
+    __syncthreads();
+    if (dt == 0.0) return 0;
+    for (int sub = 0; sub < 3; ++sub) {
+        const bool normal = sub != 1;
+        const double h = sub == 1 ? dt : dt * 0.5;
+        // relaxation weights, activity and the Gram matrix of the features
+        double v[16];
+        for (int k = 0; k < 16; ++k) v[k] = 0.0;
+        for (int m = threadIdx.x; m < Q.n; m += blockDim.x) {
+            const double a = -expm1(-Q.rate(m, normal) * h);
+            work[m].y = a;
+            const double c = Q.count(m);
+            if (c == 0.0) continue;
+            double f[4];
+            ncl_features(Q, m, T, f);
+            const double e = ncl_bose(f[0]);
+            const double w = c * a * e * (1.0 + e);
+            v[0] += c * a;
+            int q = 1;
+            for (int k = 0; k < 4; ++k)
+                for (int l = k; l < 4; ++l) v[q++] += w * f[k] * f[l];
+        }
+        block_sum<16>(v, sh.red);
+        if (v[0] == 0.0) continue; // no activity
+        if (threadIdx.x == 0) {
+            double G[4][4];
+            int q = 1;
+            for (int k = 0; k < 4; ++k)
+                for (int l = k; l < 4; ++l) G[k][l] = G[l][k] = v[q++];
+            auto gdot = [&](const double* u, const double* w) {
+                double s = 0.0;
+                for (int k = 0; k < 4; ++k)
+                    for (int l = 0; l < 4; ++l) s += u[k] * G[k][l] * w[l];
+                return s;
+            };
+            int dim = 0;
+            for (int k = 0; k < 4; ++k) sh.lambda[k] = 0.0;
+            for (int j = 0; j < (normal ? 4 : 1); ++j) {
+                double u[4] = {0.0, 0.0, 0.0, 0.0};
+                if (!(G[j][j] != 0.0)) continue;
+                const double norm0 = sqrt(G[j][j]);
+                u[j] = 1.0 / norm0;
+                for (int pass = 0; pass < 2; ++pass)
+                    for (int b = 0; b < dim; ++b) {
+                        const double d = gdot(u, sh.B[b]);
+                        for (int k = 0; k < 4; ++k) u[k] -= d * sh.B[b][k];
+                    }
+                const double len = sqrt(gdot(u, u));
+                if (len < 1e-12) continue;
+                for (int k = 0; k < 4; ++k) sh.B[dim][k] = u[k] / len;
+                if (j == 0) sh.lambda[0] = norm0 * len;
+                ++dim;
+            }
+            sh.dim = dim;
+            if (dim == 0) sh.status = kErrNclNoConstraint;
+        }
+        __syncthreads();
+        if (sh.status) return sh.status;
+        // convergence scales
+        for (int k = 0; k < 16; ++k) v[k] = 0.0;
+        for (int m = threadIdx.x; m < Q.n; m += blockDim.x) {
+            const double c = Q.count(m);
+            if (c == 0.0) continue;
+            double f[4];
+            ncl_features(Q, m, T, f);
+            const double a = work[m].y;
+            const double top = fmax(work[m].x, c * ncl_bose(f[0]));
+            for (int j = 0; j < sh.dim; ++j) {
+                const double b = sh.B[j][0] * f[0] + sh.B[j][1] * f[1] + sh.B[j][2] * f[2] + sh.B[j][3] * f[3];
+                v[j] += fabs(a * b) * top;
+            }
+        }
+        block_sum<16>(v, sh.red);
+        if (threadIdx.x == 0)
+            for (int j = 0; j < 4; ++j) sh.scale[j] = v[j];
+        __syncthreads();
+        // damped Newton
+        bool converged = false;
+        for (int it = 0; it < 70 && !converged; ++it) {
+            ncl_set_point(sh, sh.lambda);
+            double g[16];
+            ncl_evaluate(Q, sh, work, T, true, g);
+            const double F = g[0];
+            const double err = ncl_error(sh, g);
+            if (err < 2e-13) {
+                converged = true;
+                break;
+            }
+            if (threadIdx.x == 0) {
+                const int dim = sh.dim;
+                double H[4][4], r[4];
+                int q = 5;
+                for (int j = 0; j < 4; ++j)
+                    for (int l = j; l < 4; ++l) H[j][l] = H[l][j] = g[q++];
+                for (int j = 0; j < dim; ++j) r[j] = -g[1 + j];
+                for (int j = 0; j < dim && !sh.status; ++j) {
+                    int p = j;
+                    for (int k = j + 1; k < dim; ++k)
+                        if (fabs(H[k][j]) > fabs(H[p][j])) p = k;
+                    if (!(fabs(H[p][j]) > 1e-30)) {
+                        sh.status = kErrNclSingular;
+                        break;
+                    }
+                    for (int l = 0; l < 4; ++l) {
+                        const double t = H[j][l];
+                        H[j][l] = H[p][l];
+                        H[p][l] = t;
+                    }
+                    const double t = r[j];
+                    r[j] = r[p];
+                    r[p] = t;
+                    for (int k = j + 1; k < dim; ++k) {
+                        const double fk = H[k][j] / H[j][j];
+                        for (int l = j; l < dim; ++l) H[k][l] -= fk * H[j][l];
+                        r[k] -= fk * r[j];
+                    }
+                }
+                if (!sh.status)
+                    for (int j = dim - 1; j >= 0; --j) {
+                        for (int l = j + 1; l < dim; ++l) r[j] -= H[j][l] * r[l];
+                        sh.delta[j] = r[j] / H[j][j];
+                    }
+            }
+            __syncthreads();
+            if (sh.status) return sh.status;
+            double slope = 0.0;
+            for (int j = 0; j < sh.dim; ++j) slope += g[1 + j] * sh.delta[j];
+            bool accepted = false;
+            for (double t = 1.0; t > 1e-14; t *= 0.5) {
+                double trial[4];
+                for (int j = 0; j < 4; ++j) trial[j] = sh.lambda[j] + (j < sh.dim ? t * sh.delta[j] : 0.0);
+                __syncthreads();
+                ncl_set_point(sh, trial);
+                double gt[16];
+                ncl_evaluate(Q, sh, work, T, false, gt);
+                if (isfinite(gt[0]) && (gt[0] <= F + 1e-4 * t * slope || ncl_error(sh, gt) < err * 0.9)) {
+                    __syncthreads();
+                    if (threadIdx.x == 0)
+                        for (int j = 0; j < 4; ++j) sh.lambda[j] = trial[j];
+                    __syncthreads();
+                    accepted = true;
+                    break;
+                }
+            }
+            if (!accepted) return kErrNclLineSearch;
+        }
+        if (!converged) return kErrNclNoConverge;
+        // move the modes: occupation sums and the composed affine map
+        ncl_set_point(sh, sh.lambda);
+        int bad = 0;
+        for (int m = threadIdx.x; m < Q.n; m += blockDim.x) {
+            const double a = work[m].y, c = Q.count(m);
+            if (!(a > 0.0) || c == 0.0) continue;
+            double f[4];
+            ncl_features(Q, m, T, f);
+            const double t = ncl_bose(sh.y[0] * f[0] + sh.y[1] * f[1] + sh.y[2] * f[2] + sh.y[3] * f[3]);
+            if (!isfinite(t) || t < 0.0) bad = 1;
+            work[m].x = (1.0 - a) * work[m].x + a * c * t;
+            Q.compose(m, 1.0 - a, a * t);
+        }
+        if (__syncthreads_or(bad)) return kErrNclInvalid;
+    }
+    return 0;
+}
+
+// Cell modes of the simulation: bins, material tables, rates at the cell's
+// rate temperature (interpolated as src/material/PhononMaterialCollisionData.cpp:168-193).
+struct NclSimModes {
+    int n;
+    const DevMaterial* M;
+    const double* kv;
+    const double* gn;
+    const double* gu;
+    const double* gx;
+    const BinSum* bins;
+    double2* ab;
+    int lo, hi;
+    double fr;
+    __device__ double omega(int m) const { return M->omega[m]; }
+    __device__ double kx(int m, int k) const { return kv[3 * m + k]; }
+    __device__ double count(int m) const { return static_cast<double>(bins[m].cnt); }
+    __device__ double lerp(const double* g, int m) const {
+        const size_t na = static_cast<size_t>(M->n_active);
+        return 4.0 * 3.14159265358979311600 * ((1.0 - fr) * g[lo * na + m] + fr * g[hi * na + m]);
+    }
+    __device__ double rate(int m, bool normal) const {
+        return normal ? lerp(gn, m) : lerp(gu, m) + (gx ? lerp(gx, m) : 0.0);
+    }
+    __device__ void out(int m, double alpha, double beta) const { ab[m] = make_double2(alpha, beta); }
+    __device__ void compose(int m, double alpha, double beta) const {
+        const double2 p = ab[m];
+        ab[m] = make_double2(alpha * p.x, alpha * p.y + beta);
+    }
+};
+
+// One CTA per cell: the nonlinear Callaway update of the cell's carriers as
+// the pending (alpha, beta) of each mode bin (in C.rta_ab, stride hist_modes).
+__global__ void __launch_bounds__(kNclThreads) k_ncl_solve(const DevTables* __restrict__ Tp, CellArrays C,
+                                                            DevLedger* L, const DevNcl X) {
+    __shared__ NclBlock sh;
+    const DevTables& T = *Tp;
+    const int c = blockIdx.x;
+    const int mid = C.cell_material[c];
+    const DevMaterial& M = T.mat[mid];
+    const size_t hb = static_cast<size_t>(c) * C.hist_modes;
+    NclSimModes Q;
+    Q.n = M.n_bins;
+    Q.M = &M;
+    Q.kv = X.k[mid];
+    Q.gn = X.gamma_n[mid];
+    Q.gu = X.gamma_u[mid];
+    Q.gx = X.gamma_x[mid];
+    Q.bins = C.bins + hb;
+    Q.ab = C.rta_ab + hb;
+    double2* work = X.work + hb;
+    const double Tc = C.temperature[c];
+    const double Tr = X.local ? Tc : X.lifetime_T;
+    // src/solver/NonlinearCallawayCollision.cpp:309-312 and :218-221
+    unsigned carriers = 0;
+    for (int m = threadIdx.x; m < Q.n; m += blockDim.x) {
+        const BinSum b = Q.bins[m];
+        work[m] = make_double2(b.N, 0.0);
+        carriers += b.cnt;
+    }
+    if (!__syncthreads_or(carriers != 0u)) {
+        for (int m = threadIdx.x; m < Q.n; m += blockDim.x) Q.out(m, 1.0, 0.0);
+        return;
+    }
+    if (!(Tr > 0.0) || !isfinite(Tr) || Tr < M.temps[0] || Tr > M.temps[M.n_temps - 1] || !(Tc > 0.0) ||
+        !isfinite(Tc)) {
+        if (threadIdx.x == 0) raise_error(L, kErrNclTemperature, c);
+        for (int m = threadIdx.x; m < Q.n; m += blockDim.x) Q.out(m, 1.0, 0.0);
+        return;
+    }
+    int hi = 0, n = M.n_temps;
+    while (hi < n && M.temps[hi] < Tr) ++hi; // lower_bound
+    Q.hi = hi;
+    Q.lo = hi > 0 ? hi - 1 : hi;
+    Q.fr = Q.lo == Q.hi ? 0.0 : (Tr - M.temps[Q.lo]) / (M.temps[Q.hi] - M.temps[Q.lo]);
+    const int st = ncl_solve_cell(Q, sh, work, Tc, T.par.dt);
+    if (st != 0) {
+        if (threadIdx.x == 0) raise_error(L, st, c);
+        for (int m = threadIdx.x; m < Q.n; m += blockDim.x) Q.out(m, 1.0, 0.0);
+    }
+}
+
+// Stand-alone cell for phmc_dev_ncallaway_evolve: per-mode arrays.
+struct NclArrayModes {
+    int n;
+    const double* om;
+    const double* kv;
+    const double* rn;
+    const double* rr;
+    const double* cnt;
+    double2* ab;
+    __device__ double omega(int m) const { return om[m]; }
+    __device__ double kx(int m, int k) const { return kv[3 * m + k]; }
+    __device__ double count(int m) const { return cnt[m]; }
+    __device__ double rate(int m, bool normal) const { return normal ? rn[m] : rr[m]; }
+    __device__ void out(int m, double alpha, double beta) const { ab[m] = make_double2(alpha, beta); }
+    __device__ void compose(int m, double alpha, double beta) const {
+        const double2 p = ab[m];
+        ab[m] = make_double2(alpha * p.x, alpha * p.y + beta);
+    }
+};
+
+// One CTA: bins the carriers by mode (in carrier order), solves, moves them.
+__global__ void __launch_bounds__(kNclThreads) k_ncl_cell(NclArrayModes Q, double* cnt, double2* work, int64_t n,
+                                                           const int32_t* mode, double* occ, double T, double dt,
+                                                           int* status) {
+    __shared__ NclBlock sh;
+    for (int m = threadIdx.x; m < Q.n; m += blockDim.x) {
+        double c = 0.0, N = 0.0;
+        for (int64_t i = 0; i < n; ++i)
+            if (mode[i] == m) {
+                c += 1.0;
+                N += occ[i];
+            }
+        cnt[m] = c;
+        work[m] = make_double2(N, 0.0);
+    }
+    __syncthreads();
+    const int st = ncl_solve_cell(Q, sh, work, T, dt);
+    if (threadIdx.x == 0) *status = st;
+    if (st != 0) return;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const double2 ab = Q.ab[mode[i]];
+        occ[i] = ab.x * occ[i] + ab.y;
+    }
+}
+
 // ----------------------------------------------------- linear response
 // Cluster-wide sum of N doubles: CTA partials in shared memory, read by every
 // CTA of the cluster through distributed shared memory.
@@ -572,6 +959,10 @@ __device__ __forceinline__ void k_cell_tables_body(const DevTables* __restrict__
                 const double2 r = C.rta_ab[static_cast<size_t>(c) * C.n_classes + b];
                 a = 1.0 - r.x;
                 bc = r.x * r.y;
+            } else if (kCollision == kCollideNonlinear) {
+                const double2 r = C.rta_ab[hb + b]; // composed (alpha, beta) of the three substeps
+                a = r.x;
+                bc = r.y;
             } else {
                 a = C.lin_decay[static_cast<size_t>(C.cell_material[c]) * C.hist_modes + b];
                 bc = C.lin_beta[hb + b];
@@ -991,7 +1382,13 @@ int launch_cell_solve(const LaunchCtx& x, int phase, int collision) {
                                      cudaGetErrorString(err));
         ++launches;
     }
+    if (phase >= 1 && collision == kCollideNonlinear) {
+        k_ncl_solve<<<C.ncells, kNclThreads, 0, x.stream>>>(T, C, x.L, *x.ncl);
+        ++launches;
+    }
     if (phase >= 1 && rta) k_cell_tables<kCollideRta><<<grid, kStatThreads, 0, x.stream>>>(T, C, phase);
+    else if (phase >= 1 && collision == kCollideNonlinear)
+        k_cell_tables<kCollideNonlinear><<<grid, kStatThreads, 0, x.stream>>>(T, C, phase);
     else if (phase >= 1 && collision == kCollideLinear)
         k_cell_tables<kCollideLinear><<<grid, kStatThreads, 0, x.stream>>>(T, C, phase);
     else k_cell_tables<kCollideNone><<<grid, kStatThreads, 0, x.stream>>>(T, C, phase);
@@ -1052,6 +1449,14 @@ int launch_fused_cells(const BatchDesc& D, cudaStream_t s) {
 int launch_fused_step(const BatchDesc& D, cudaStream_t s, bool mixed) {
     kf_step_begin<<<D.n, 32, 0, s>>>(D);
     return 1 + launch_fused_transport(D, s, mixed) + launch_fused_cells(D, s);
+}
+
+// One stand-alone cell of nonlinear Callaway (phmc_dev_ncallaway_evolve).
+void launch_ncl_cell(int n_modes, const double* omega, const double* k3, const double* rn, const double* rr,
+                     double* cnt, double2* ab, double2* work, int64_t n, const int32_t* mode, double* occ, double T,
+                     double dt, int* status, cudaStream_t s) {
+    NclArrayModes Q{n_modes, omega, k3, rn, rr, cnt, ab};
+    k_ncl_cell<<<1, kNclThreads, 0, s>>>(Q, cnt, work, n, mode, occ, T, dt, status);
 }
 
 } // namespace phmc

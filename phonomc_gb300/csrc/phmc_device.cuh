@@ -51,6 +51,12 @@ enum ErrorCode : int {
     kErrNonFinite = 9,
     kErrNoRoughTable = 10,
     kErrCollision = 11,
+    kErrNclNoConstraint = 12,
+    kErrNclSingular = 13,
+    kErrNclLineSearch = 14,
+    kErrNclNoConverge = 15,
+    kErrNclInvalid = 16,
+    kErrNclTemperature = 17,
 };
 
 struct DevMaterial {

@@ -283,6 +283,23 @@ CallawayData PhononMaterial::callaway_data(double T) const {
     return d;
 }
 
+// src/material/PhononMaterialCollisionData.cpp:168-193: normal and resistive
+// (umklapp + extra) rates of one mode at T, linear in the temperature samples.
+std::array<double, 2> PhononMaterial::mode_callaway_rates(double T, int f) const {
+    if (gamma_normal_.empty() || gamma_umklapp_.empty() || !std::isfinite(T) || T <= 0 || T < temps_.front() ||
+        T > temps_.back())
+        throw std::invalid_argument("Nonlinear Callaway temperature " + std::to_string(T) +
+                                    " K is outside the supplied N/U table");
+    const size_t hi = static_cast<size_t>(std::lower_bound(temps_.begin(), temps_.end(), T) - temps_.begin());
+    const size_t lo = hi ? hi - 1 : hi;
+    const double fr = lo == hi ? 0 : (T - temps_[lo]) / (temps_[hi] - temps_[lo]);
+    const size_t nm = static_cast<size_t>(nq_) * nb_;
+    auto rate = [&](const std::vector<double>& t) {
+        return t.empty() ? 0.0 : 4 * std::acos(-1.) * ((1 - fr) * t[lo * nm + f] + fr * t[hi * nm + f]);
+    };
+    return {rate(gamma_normal_), rate(gamma_umklapp_) + rate(gamma_extra_)};
+}
+
 // ---------------------------------------------------------------- domain
 // Box facets in the reference's order (plane 2*axis+side), boundary conditions,
 // periodic pairs and the uniform grid (src/SimulationDomain.cpp:131-198, 408-611, 626-766).
@@ -926,8 +943,12 @@ Problem build_problem(const SimulationConfig& cfg, SimulationDomain& domain,
     Problem P;
     P.cfg = cfg;
     P.domain = &domain;
+    // src/config/ConfigValidation.cpp:349-354
+    if (cfg.callaway_nonlinear && (cfg.collision_model != CollisionModel::Callaway || cfg.temperature_gradient))
+        throw std::runtime_error("Nonlinear Callaway requires model=callaway and finite-domain thermal driving");
     P.linearized = uses_linearized_transport(cfg);
     P.conservative = uses_conservative_transport(cfg);
+    P.callaway_nonlinear = cfg.callaway_nonlinear;
     P.one_to_one = !(P.conservative || mats.size() > 1);
     P.initial_particles = static_cast<int>(std::llround(cfg.particle_count));
     if (P.initial_particles <= 0) throw std::invalid_argument("particle_count must be positive");
@@ -1018,6 +1039,23 @@ Problem build_problem(const SimulationConfig& cfg, SimulationDomain& domain,
         T.relax_fixed.resize(na);
         for (int a = 0; a < na; ++a)
             T.relax_fixed[a] = M.mode_relaxation_weight(cfg.lifetime_temperature, T.active_flat[a], cfg.time_step);
+        if (P.callaway_nonlinear) {
+            // src/solver/NonlinearCallawayCollision.cpp:250-263: the reference's
+            // configure() validates the N/U data at the background temperature
+            const CallawayData d = M.callaway_data(Tbg);
+            T.col_k.resize(3 * na);
+            for (int a = 0; a < na; ++a)
+                for (int k = 0; k < 3; ++k) T.col_k[3 * a + k] = d.wavevector[a][k];
+            auto active_rows = [&](const std::vector<double>& g) {
+                std::vector<double> out(g.empty() ? 0 : nT * na);
+                for (size_t it = 0; it < nT && !g.empty(); ++it)
+                    for (int a = 0; a < na; ++a) out[it * na + a] = g[it * nm + T.active_flat[a]];
+                return out;
+            };
+            T.ncl_gamma_n = active_rows(M.gamma_normal());
+            T.ncl_gamma_u = active_rows(M.gamma_umklapp());
+            T.ncl_gamma_x = active_rows(M.gamma_extra());
+        }
         if (P.linearized) {
             const CallawayData d = cfg.collision_model == CollisionModel::Callaway ? M.callaway_data(Tbg)
                                                                                    : M.linearized_rta_data(Tbg);

@@ -80,6 +80,7 @@ struct SimulationConfig {
     std::vector<std::array<double, 6>> periodic_pair; // region pairs, matched facet by facet
     std::string output_folder;
     bool write_cell_heat_flux = false; // grid_heat_flux.csv also without a gradient drive
+    bool callaway_nonlinear = false;   // collision.callaway_formulation = "nonlinear"
     std::string material_folder; // reported in summary.txt; tables enter as arrays
     // Layered materials (include/SimulationConfig.h:93-99): N materials, N-1 planes.
     int material_interface_axis = 0;
@@ -111,10 +112,10 @@ double heat_source_time_factor(const SimulationConfig& c, double begin_ps, doubl
 
 // include/SimulationConfig.h:148-156
 inline bool uses_linearized_transport(const SimulationConfig& c) {
-    return c.collision_model == CollisionModel::Callaway || c.temperature_gradient.has_value();
+    return (c.collision_model == CollisionModel::Callaway && !c.callaway_nonlinear) || c.temperature_gradient.has_value();
 }
 inline bool uses_conservative_transport(const SimulationConfig& c) {
-    return uses_linearized_transport(c) || c.conservative_boundaries;
+    return uses_linearized_transport(c) || c.callaway_nonlinear || c.conservative_boundaries;
 }
 
 // ------------------------------------------------------------- material
@@ -172,6 +173,10 @@ public:
     CallawayData linearized_rta_data(double T) const;
     CallawayData callaway_data(double T) const;
     bool has_callaway_rates() const { return !gamma_normal_.empty(); }
+    const std::vector<double>& gamma_normal() const { return gamma_normal_; }
+    const std::vector<double>& gamma_umklapp() const { return gamma_umklapp_; }
+    const std::vector<double>& gamma_extra() const { return gamma_extra_; }
+    std::array<double, 2> mode_callaway_rates(double T, int flat) const;
 
     const std::vector<double>& lookup_T() const { return table_T_; }
     const std::vector<double>& lookup_E() const { return table_E_; }
@@ -493,6 +498,8 @@ struct MaterialTables {
     std::vector<double> relax_fixed;    // RTA weight at the fixed lifetime temperature
     // Linear-response collision data (linearized RTA or Callaway) at T_bg.
     std::vector<double> col_capacity, col_normal, col_resistive, col_k; // col_k: [active*3]
+    // nonlinear Callaway: N, U and extra resistive linewidths [nT * active] (THz HWHM)
+    std::vector<double> ncl_gamma_n, ncl_gamma_u, ncl_gamma_x;
     // Mode classes: active modes sharing (omega, linewidth row) share the Bose
     // function and RTA weight; per-cell RTA sums aggregate over them.
     int n_classes = 0;
@@ -506,6 +513,7 @@ struct MaterialTables {
 struct Problem {
     SimulationConfig cfg;
     bool linearized = false, conservative = false;
+    bool callaway_nonlinear = false;
     bool one_to_one = true;
     double push_eps = 1e-10;
     double particle_volume = 0;

@@ -26,6 +26,7 @@ struct LaunchCtx {
     cudaStream_t stream;
     int grid_blocks;
     bool mesh = false;   // surface-mesh domain (plain FP64 carrier state)
+    const DevNcl* ncl = nullptr; // host copy, nonlinear Callaway only
 };
 
 // Independent box instances advanced by one launch per kernel of the step:
@@ -88,12 +89,16 @@ void launch_step_begin(const LaunchCtx& x);
 // One heat-source half (time window from the device clock): accrue, deposit into the pending updates.
 void launch_source(const LaunchCtx& x, bool final_temperature, bool next);
 int launch_cell_solve(const LaunchCtx& x, int phase, int collision);
+void launch_ncl_cell(int n_modes, const double* omega, const double* k3, const double* rn, const double* rr,
+                     double* cnt, double2* ab, double2* work, int64_t n, const int32_t* mode, double* occ, double T,
+                     double dt, int* status, cudaStream_t s);
 int linear_cluster_size(const CellArrays& C, bool mixed);
 void prepare_linear_solve(const CellArrays& C);
 void launch_cells_final(const LaunchCtx& x, int phase);
 
 // collision kinds for launch_cell_solve
-enum CollisionKind : int { kCollideNone = 0, kCollideRta = 1, kCollideLinear = 2 };
+enum CollisionKind : int { kCollideNone = 0, kCollideRta = 1, kCollideLinear = 2, kCollideNonlinear = 3 };
+
 
 
 // Device layout of a face BVH (DevMesh): nodes renumbered breadth-first, face

@@ -48,9 +48,18 @@ static const char* error_message(int code) {
     case kErrNonFinite: return "Non-finite grid energy reduction.";
     case kErrNoRoughTable: return "Rough facet without a sampling table.";
     case kErrCollision: return "Carrier collision occupation overflow.";
+    // src/solver/NonlinearCallawayCollision.cpp:88-213, src/material/PhononMaterialCollisionData.cpp:172-174
+    case kErrNclNoConstraint: return "Nonlinear Callaway has no representable energy constraint";
+    case kErrNclSingular: return "Singular nonlinear Callaway moment Jacobian";
+    case kErrNclLineSearch: return "Nonlinear Callaway moment line search failed";
+    case kErrNclNoConverge: return "Nonlinear Callaway moment solve did not converge";
+    case kErrNclInvalid: return "Nonlinear Callaway occupation is invalid";
+    case kErrNclTemperature: return "Nonlinear Callaway temperature is outside the supplied N/U table";
     default: return "Unknown device error.";
     }
 }
+
+const char* solver_error_message(int code) { return error_message(code); }
 
 DeviceSolver::DeviceSolver(const SimulationConfig& cfg, const std::vector<const PhononMaterial*>& mats,
                            bool init_carriers, bool mixed)
@@ -160,7 +169,7 @@ void DeviceSolver::upload_tables() {
         D.n_active = M.n_active;
         // RTA bins are the mode classes (every per-cell update is class-uniform);
         // linear response keeps one bin per mode (gain vectors and drive are per mode)
-        if (!P_.linearized) {
+        if (!P_.linearized && !P_.callaway_nonlinear) {
             D.bin = upload(M.mode_class);
             D.bin_rep = upload(M.class_rep);
             D.n_bins = M.n_classes;
@@ -240,6 +249,14 @@ void DeviceSolver::upload_tables() {
         D.gamma = upload(M.gamma_active);
         D.lookup_T = upload(M.lookup_T);
         D.lookup_E = upload(M.lookup_E);
+        if (P_.callaway_nonlinear) {
+            ncl_.gamma_n[mi] = upload(M.ncl_gamma_n);
+            ncl_.gamma_u[mi] = upload(M.ncl_gamma_u);
+            ncl_.gamma_x[mi] = M.ncl_gamma_x.empty() ? nullptr : upload(M.ncl_gamma_x);
+            ncl_.k[mi] = upload(M.col_k);
+            ncl_.lifetime_T = cfg_.lifetime_temperature;
+            ncl_.local = cfg_.lifetime_temperature_is_local ? 1 : 0;
+        }
         if (P_.linearized) {
             std::vector<double> rate(M.n_active);
             for (int a = 0; a < M.n_active; ++a) {
@@ -418,7 +435,7 @@ void DeviceSolver::upload_tables() {
     C.cell_material = upload(P_.cell_material);
     C.volume = upload(domain_->grid_volumes());
     const size_t hist = static_cast<size_t>(ncells_) * hist_modes;
-    const bool rta = !P_.linearized;
+    const bool rta = !P_.linearized && !P_.callaway_nonlinear;
     C.bins = dalloc<BinSum>(hist);
     C.ab = dalloc<double2>(hist);
     C.hM = rta ? dalloc<double>(hist) : nullptr;
@@ -447,6 +464,11 @@ void DeviceSolver::upload_tables() {
         for (const auto& M : P_.mats) max_classes = std::max(max_classes, M.n_classes);
         C.n_classes = max_classes; // == bins per cell
         C.rta_ab = dalloc<double2>(static_cast<size_t>(ncells_) * max_classes);
+    } else if (P_.callaway_nonlinear) {
+        // composed (alpha, beta) per (cell, mode) and the moment-solve work space
+        C.n_classes = hist_modes;
+        C.rta_ab = dalloc<double2>(hist);
+        ncl_.work = dalloc<double2>(hist);
     } else {
         C.lin_beta = dalloc<double>(hist);
         const int S = std::max(1, static_cast<int>(std::ceil(cfg_.time_step * r_max)));
@@ -543,16 +565,17 @@ LaunchCtx DeviceSolver::ctx() const {
     const long long want = (static_cast<long long>(state_.capacity) + 1023) / 1024;
     x.grid_blocks = static_cast<int>(std::max<long long>(8, std::min<long long>(sm_count_ * 8, want)));
     x.mesh = domain_->is_mesh();
+    x.ncl = P_.callaway_nonlinear ? &ncl_ : nullptr;
     return x;
 }
 
 int DeviceSolver::collision_kind() const {
-    return P_.linearized ? kCollideLinear : kCollideRta;
+    return P_.callaway_nonlinear ? kCollideNonlinear : P_.linearized ? kCollideLinear : kCollideRta;
 }
 
 void DeviceSolver::initial_statistics() {
     const LaunchCtx x = ctx();
-    launch_histogram(x, !P_.linearized);
+    launch_histogram(x, collision_kind() == kCollideRta);
     counters_.launches += 2 + launch_cell_solve(x, 0, collision_kind());
     launch_cells_final(x, 0);
     if (P_.source.enabled) {
@@ -725,7 +748,7 @@ void DeviceSolver::materialize() {
 double DeviceSolver::collide_only(const double* cell_temperature) {
     const LaunchCtx x = ctx();
     launch_step_begin(x);
-    launch_histogram(x, !P_.linearized);
+    launch_histogram(x, collision_kind() == kCollideRta);
     int phase = 1;
     if (cell_temperature) {
         PHMC_CUDA(cudaMemcpyAsync(cells_.temperature, cell_temperature, ncells_ * sizeof(double),

@@ -41,6 +41,18 @@ namespace phmc {
 // Population sums of one (cell, mode) bin, accumulated by the transport pass:
 // sum of occupations and multiplicity share one 16-byte record, so the two
 // atomics of a carrier touch one L2 sector.
+// Nonlinear Callaway tables of every material (linewidths in the layout of
+// DevMaterial::gamma) and the per-(cell, mode) work space of the moment solve.
+struct DevNcl {
+    const double* gamma_n[kMaxMaterials]; // [n_temps * active] normal linewidth
+    const double* gamma_u[kMaxMaterials]; // umklapp
+    const double* gamma_x[kMaxMaterials]; // extra resistive (isotope, boundary)
+    const double* k[kMaxMaterials];       // [3 * active] wavevector
+    double2* work;                        // [ncells * hist_modes] (sum of occupations, relaxation weight)
+    double lifetime_T;
+    int local;                            // rates at the cell temperature (else lifetime_T)
+};
+
 struct __align__(16) BinSum {
     double N;
     unsigned int cnt;
@@ -124,6 +136,7 @@ struct Observation {
 };
 
 void stats_from_ledger(const DevLedger& L, phmc_stats& o);
+const char* solver_error_message(int code); // message of a device error code
 
 class DeviceSolver {
 public:
@@ -229,6 +242,7 @@ private:
     std::vector<double> host_T_, host_E_, host_q_;
     // flux passes copied into pinned host slots and processed when their event completes
     std::vector<struct Observation*> obs_free_, obs_pending_;
+    DevNcl ncl_{}; // nonlinear Callaway tables and work space
     // graph of one timestep
     bool use_graphs_ = true;
     cudaGraph_t graph_ = nullptr;

@@ -30,6 +30,9 @@ HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
 
 # name -> harness arguments ("{m}" = plain 8^3 table, "{c}" = Callaway table)
 CASES = {
+    "ncallaway_unique": ["ncallaway", "11", "48", "48", "1"],
+    "ncallaway_shared": ["ncallaway", "12", "40", "200", "0"],
+    "ncallaway_large": ["ncallaway", "13", "600", "900", "0"],
     "material_m8": ["material", "{m}", "0"],
     "material_m8_stationary": ["material", "{m}", "1"],
     "box_trace": ["box"],

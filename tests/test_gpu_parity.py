@@ -576,3 +576,41 @@ def test_output_files_finfet(gpu, finfet_stl, tmp_path):
         assert np.isclose(pa[0], pb[0], rtol=1e-12, atol=0)  # base power, W
         assert np.isclose(pa[1], pb[1], rtol=1e-12, atol=0)  # prescribed, eV
         assert np.isclose(pa[2] + pa[3], pa[1], rtol=1e-9, atol=1e-12 * max(1.0, pb[1]))
+
+
+# ------------------------------------------------------ nonlinear Callaway
+@pytest.mark.parametrize("name,rtol", [("ncallaway_unique", 1e-12), ("ncallaway_shared", 1e-10),
+                                       ("ncallaway_large", 1e-10)])
+def test_nonlinear_callaway_cell_golden(gpu, name, rtol):
+    """One cell of nonlinear Callaway on the device (mode bins, moment Newton
+    per substep) against the reference's nonlinear_callaway_evolve on the same
+    carriers. With one carrier per mode the device arithmetic is the
+    reference's in FP64; with shared modes the convergence scale uses the bin
+    bound, so agreement is to the Newton tolerance."""
+    g = golden(name)
+    mode = _i32(g["mode"])
+    occ = _f64(g["n"]).copy()
+    rc = gpu.phmc_dev_ncallaway_evolve(len(g["omega"]), D(_f64(g["omega"])), D(_f64(g["k"])), D(_f64(g["rn"])),
+                                       D(_f64(g["rr"])), mode.size, I32(mode), D(occ), C.c_double(g["T"]),
+                                       C.c_double(g["dt"]))
+    assert rc == 0, gpu.phmc_last_error()
+    assert np.allclose(occ, g["out"], rtol=rtol, atol=0)
+
+
+def test_nonlinear_callaway_steps_match_oracle(gpu, orc):
+    """Whole steps of a cross-plane film with nonlinear Callaway collisions
+    (absolute occupations, conservative boundaries) on the device against the
+    oracle's per-carrier long-double restatement."""
+    mat = synthetic.make_material(mesh=8, callaway=True)
+    cfg = workloads.scaled(workloads.cross_plane_film(), 20000, random_seed=17, collision_model="callaway",
+                           callaway_formulation="nonlinear")
+    mg = abi.Material(gpu, "phmc_", mat, 0.1, True, True)
+    mo = abi.Material(orc, "orc_", mat, 0.1, True, True)
+    sg = abi.Solver(gpu, "phmc_", cfg, [mg])
+    so = abi.Solver(orc, "orc_", cfg, [mo])
+    for _ in range(3):
+        sg.run(2)
+        so.run(2)
+        stg, sto = _compare(sg, so, tol=1e-9)
+        assert abs(stg["total_lifetime_energy_residual_ev"] - sto["total_lifetime_energy_residual_ev"]) < 1e-8
+    assert abs(stg["total_energy_balance_residual_ev"]) < 1e-6

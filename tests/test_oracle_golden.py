@@ -294,3 +294,37 @@ def test_mesh_trace(oracle_lib):
     assert np.array_equal(fac, g["facet"])
     assert np.array_equal(t, np.asarray(g["t"]))
     assert np.array_equal(hit, np.asarray(g["hits"]))
+
+
+@pytest.mark.parametrize("name", ["ncallaway_unique", "ncallaway_shared", "ncallaway_large"])
+def test_nonlinear_callaway_evolve(oracle_lib, name):
+    """The oracle's per-carrier nonlinear Callaway (long double, as the
+    reference) against src/solver/NonlinearCallawayCollision.cpp's own
+    nonlinear_callaway_evolve on seeded single-cell cases."""
+    g = golden(name)
+    mode = _i32(g["mode"])
+    occ = _f64(g["n"]).copy()
+    rc = oracle_lib.orc_ncallaway_evolve(len(g["omega"]), D(_f64(g["omega"])), D(_f64(g["k"])), D(_f64(g["rn"])),
+                                         D(_f64(g["rr"])), mode.size, I32(mode), D(occ), C.c_double(g["T"]),
+                                         C.c_double(g["dt"]))
+    assert rc == 0, oracle_lib.orc_last_error()
+    assert np.allclose(occ, g["out"], rtol=1e-14, atol=0)
+
+
+def test_nonlinear_callaway_config(oracle_lib):
+    """Nonlinear Callaway needs the Callaway model and no gradient drive
+    (src/config/ConfigValidation.cpp:349-354); a film runs with it and its
+    energy ledger closes."""
+    from phonomc_gb300 import synthetic, workloads
+    mat = synthetic.make_material(mesh=8, callaway=True)
+    m = abi.Material(oracle_lib, "orc_", mat, 0.1, True, True)
+    bad = workloads.scaled(workloads.cross_plane_film(), 2000, callaway_formulation="nonlinear")
+    with pytest.raises(abi.LibError, match="Nonlinear Callaway requires model=callaway"):
+        abi.Solver(oracle_lib, "orc_", bad, [m])
+    cfg = dict(bad, collision_model="callaway")
+    s = abi.Solver(oracle_lib, "orc_", cfg, [m])
+    s.run(3)
+    st = s.stats()
+    assert st["current_timestep"] == 3
+    assert abs(st["total_energy_balance_residual_ev"]) < 1e-6
+    assert st["total_lifetime_energy_residual_ev"] != 0.0
