@@ -65,7 +65,7 @@ def workload_materials(name):
     """(material tables, include stationary modes, complete the Callaway BZ) per material."""
     from phonomc_gb300 import synthetic, workloads
     if name == "bilayer_callaway":
-        return [(d, True, True) for d in workloads.bilayer_materials(16)]
+        return [(d, True, True) for d in workloads.bilayer_materials(8)]
     return [(synthetic.make_material(mesh=16), name == "inplane_gradient", False)]
 
 
@@ -359,8 +359,8 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
         "config": {"workload": args.workload, "particles": int(args.particles), "precision": args.precision,
-                   "material": ("two synthetic 16^3 x 6 tables, second 0.7x frequency 0.75x velocity, Callaway BZ "
-                                "completed" if args.workload == "bilayer_callaway"
+                   "material": ("two synthetic 8^3 x 6 tables, second 0.7x frequency 0.75x velocity, Callaway BZ "
+                                "completed (24552 modes)" if args.workload == "bilayer_callaway"
                                 else "synthetic 16^3 x 6 modes (seed 0)"), "cells": int(Tout.size),
                    **({"mesh": "procedural FinFET, 6304 triangles, 2245 facets (seed 0)", "voxels": "64x32x32",
                        "heat_source": "gaussian 1e20 W/m^3, sigma 5 nm, fin top, thermal spectrum"}

@@ -138,8 +138,8 @@ MaterialData read_pmat(const std::string& path) {
 
 // --------------------------------------------------------------- commands
 // material <pmat> <stationary>: lookup tables and thermodynamic queries.
-std::string cmd_material(const std::string& pmat, bool stationary) {
-    PhononMaterial m(read_pmat(pmat), 0.1, stationary, false);
+std::string cmd_material(const std::string& pmat, bool stationary, bool callaway) {
+    PhononMaterial m(read_pmat(pmat), 0.1, stationary, callaway);
     Json j;
     j.put_i("active_mode_count", m.active_mode_count());
     std::vector<int> act;
@@ -980,7 +980,7 @@ int main(int argc, char** argv) {
         // Reference constructors log progress to stdout; keep stdout for JSON only.
         std::ostringstream sink;
         auto* saved = std::cout.rdbuf(sink.rdbuf());
-        if (c == "material") out = cmd_material(argv[2], std::atoi(argv[3]) != 0);
+        if (c == "material") out = cmd_material(argv[2], std::atoi(argv[3]) != 0, argc > 4 && std::atoi(argv[4]) != 0);
         else if (c == "box") out = cmd_box();
         else if (c == "rta") out = cmd_rta(argv[2], std::atoi(argv[3]) != 0);
         else if (c == "lincoll") out = cmd_lincoll(argv[2]);

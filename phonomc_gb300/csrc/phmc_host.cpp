@@ -5,6 +5,7 @@
 #include "phmc_rng.h"
 
 #include <algorithm>
+#include <set>
 #include <functional>
 #include <cmath>
 #include <cstdio>
@@ -64,16 +65,122 @@ void validate_material_data(const MaterialData& d) {
 }
 
 // src/PhononMaterial.cpp:156-171, 216-291
+// src/material/BzQuadrature.cpp:11-160: Callaway needs every q of the
+// Gamma-centred mesh as its first-Brillouin-zone representative. A q with m
+// equally short images q - G (zone-boundary points) is split into its images,
+// and every q is repeated so all carry the same weight: the table grows by
+// the least common multiple of the image counts (at most 96), q-major with
+// the copies of one mesh point adjacent. Returns that factor.
+unsigned complete_callaway_bz(MaterialData& d) {
+    const auto& b = d.reciprocal;
+    const double det = b[0][0] * (b[1][1] * b[2][2] - b[1][2] * b[2][1]) -
+                       b[0][1] * (b[1][0] * b[2][2] - b[1][2] * b[2][0]) +
+                       b[0][2] * (b[1][0] * b[2][1] - b[1][1] * b[2][0]);
+    if (!std::isfinite(det) || det == 0) throw std::invalid_argument("Callaway reciprocal lattice is singular.");
+    double inv[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            inv[i][j] = (b[(j + 1) % 3][(i + 1) % 3] * b[(j + 2) % 3][(i + 2) % 3] -
+                         b[(j + 1) % 3][(i + 2) % 3] * b[(j + 2) % 3][(i + 1) % 3]) / det;
+    auto len2 = [&](const Vec3& q) {
+        double r = 0;
+        for (int i = 0; i < 3; ++i) {
+            double x = 0;
+            for (int j = 0; j < 3; ++j) x += b[i][j] * q[j];
+            r += x * x;
+        }
+        return r;
+    };
+    std::set<std::array<int, 3>> seen;
+    std::vector<std::vector<Vec3>> images(d.qpoints);
+    unsigned refinement = 1;
+    for (int iq = 0; iq < d.qpoints; ++iq) {
+        const Vec3& q = d.qpoint_fractions[iq];
+        std::array<int, 3> key{};
+        for (int a = 0; a < 3; ++a) {
+            const double x = (q[a] - std::floor(q[a])) * d.mesh[a];
+            const long idx = std::lround(x);
+            if (std::abs(x - idx) > 2e-6 * d.mesh[a])
+                throw std::invalid_argument("Callaway requires a complete Gamma-centred full q mesh.");
+            key[a] = static_cast<int>(idx % d.mesh[a]);
+        }
+        if (!seen.insert(key).second)
+            throw std::invalid_argument(
+                "Callaway input q mesh contains duplicate points modulo reciprocal translations.");
+        const double own = len2(q);
+        int lo[3], hi[3];
+        double count = 1;
+        for (int a = 0; a < 3; ++a) {
+            const double ext = std::sqrt(own * (inv[a][0] * inv[a][0] + inv[a][1] * inv[a][1] + inv[a][2] * inv[a][2]));
+            if (!std::isfinite(ext) || ext > 100 || std::abs(q[a]) > 100)
+                throw std::invalid_argument("Callaway first-BZ validation exceeds supported lattice conditioning.");
+            lo[a] = static_cast<int>(std::ceil(q[a] - ext - 1e-10));
+            hi[a] = static_cast<int>(std::floor(q[a] + ext + 1e-10));
+            count *= hi[a] - lo[a] + 1;
+        }
+        if (count > 100000) throw std::invalid_argument("Callaway first-BZ validation work limit exceeded.");
+        std::vector<std::pair<double, Vec3>> cand;
+        double best = own;
+        for (int i = lo[0]; i <= hi[0]; ++i)
+            for (int j = lo[1]; j <= hi[1]; ++j)
+                for (int k = lo[2]; k <= hi[2]; ++k) {
+                    const Vec3 p{q[0] - i, q[1] - j, q[2] - k};
+                    const double r = len2(p);
+                    best = std::min(best, r);
+                    cand.push_back({r, p});
+                }
+        const double tol = 1e-10 * std::max(best, 1e-20);
+        if (own > best + tol)
+            throw std::invalid_argument("Callaway qpoint is outside the first Brillouin zone; supply first-BZ "
+                                        "representatives.");
+        for (const auto& c : cand)
+            if (std::abs(c.first - best) <= tol) images[iq].push_back(c.second);
+        if (images[iq].empty()) throw std::runtime_error("Empty Callaway BZ representative set.");
+        const unsigned m = static_cast<unsigned>(images[iq].size());
+        const unsigned long long next = static_cast<unsigned long long>(refinement / std::gcd(refinement, m)) * m;
+        if (next > 96 || next * static_cast<unsigned long long>(d.qpoints) * d.branches >
+                             static_cast<unsigned long long>(std::numeric_limits<int>::max()))
+            throw std::length_error("Callaway equal-weight BZ refinement exceeds supported storage; use a smaller mesh.");
+        refinement = static_cast<unsigned>(next);
+    }
+    if (refinement == 1) return 1;
+    const size_t nm0 = d.frequency_thz.size();
+    std::vector<size_t> src;
+    std::vector<Vec3> qs;
+    for (int iq = 0; iq < d.qpoints; ++iq)
+        for (const Vec3& im : images[iq])
+            for (unsigned c = 0; c < refinement / images[iq].size(); ++c) {
+                qs.push_back(im);
+                for (int br = 0; br < d.branches; ++br) src.push_back(static_cast<size_t>(iq) * d.branches + br);
+            }
+    auto expand = [&](const std::vector<double>& v) {
+        if (v.empty()) return v;
+        std::vector<double> out;
+        out.reserve(v.size() * refinement);
+        for (size_t t = 0; t < v.size() / nm0; ++t)
+            for (size_t i : src) out.push_back(v[t * nm0 + i]);
+        return out;
+    };
+    std::vector<Vec3> vel;
+    vel.reserve(src.size());
+    for (size_t i : src) vel.push_back(d.group_velocity[i]);
+    d.frequency_thz = expand(d.frequency_thz);
+    d.gamma = expand(d.gamma);
+    d.gamma_normal = expand(d.gamma_normal);
+    d.gamma_umklapp = expand(d.gamma_umklapp);
+    for (auto& e : d.gamma_resistive) e.second = expand(e.second);
+    d.qpoints *= static_cast<int>(refinement);
+    d.qpoint_fractions = std::move(qs);
+    d.group_velocity = std::move(vel);
+    return refinement;
+}
+
 PhononMaterial::PhononMaterial(MaterialData d, double lookup_dt, bool stationary, bool complete_bz)
     : dT_(lookup_dt), stationary_(stationary) {
     if (!std::isfinite(lookup_dt) || lookup_dt <= 0)
         throw std::invalid_argument("Temperature lookup spacing must be finite and positive");
     validate_material_data(d);
-    if (complete_bz && !d.gamma_normal.empty()) {
-        // Boundary replication of src/material/BzQuadrature.cpp is applied by the
-        // caller's table when needed; tables built here must already be closed.
-        refinement_ = 1;
-    }
+    if (complete_bz && !d.gamma_normal.empty()) refinement_ = complete_callaway_bz(d);
     volume_ = d.volume_a3;
     nq_ = d.qpoints;
     nb_ = d.branches;

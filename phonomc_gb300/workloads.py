@@ -133,8 +133,10 @@ def batched_films(n: int = 512, seed: int = 0, precision: str = "mixed", particl
     return films
 
 
-def bilayer_materials(mesh: int = 16):
-    """The two synthetic materials of the bilayer (Callaway linewidth split)."""
+def bilayer_materials(mesh: int = 8):
+    """The two synthetic materials of the bilayer (Callaway linewidth split).
+    Callaway tables are completed over the first Brillouin zone as the
+    reference does: 8^3 q-points x 6 branches become 24,552 modes."""
     from . import synthetic
     return [synthetic.make_material(mesh=mesh, callaway=True),
             synthetic.make_material(mesh=mesh, freq_scale=0.7, vel_scale=0.75, callaway=True)]

@@ -35,6 +35,7 @@ CASES = {
     "ncallaway_large": ["ncallaway", "13", "600", "900", "0"],
     "material_m8": ["material", "{m}", "0"],
     "material_m8_stationary": ["material", "{m}", "1"],
+    "material_m8c_stationary": ["material", "{c}", "1", "1"],
     "box_trace": ["box"],
     "rta_fixed": ["rta", "{m}", "0"],
     "rta_local": ["rta", "{m}", "1"],
@@ -290,6 +291,40 @@ def full_runs_bilayer(pmats: str, tmp: str) -> dict:
     return out
 
 
+# Full reference runs of the cross-plane film with nonlinear Callaway
+# collisions (8^3 Callaway table, 8000 carriers, 120 steps of 1 ps): per seed
+# the late-time (steps 61-120) cell temperatures, heat flux and kappa_eff.
+NCL_SEEDS = 16
+NCL_PARTICLES = 8000
+NCL_STEPS = 120
+
+
+def full_runs_ncallaway(mpath: str, tmp: str) -> dict:
+    import numpy as np
+    out = {"seeds": [], "particles": NCL_PARTICLES, "steps": NCL_STEPS, "average_from_step": NCL_STEPS // 2 + 1}
+    for k in range(NCL_SEEDS):
+        seed = 101 + k
+        folder = os.path.join(tmp, f"ncl{seed}")
+        os.makedirs(folder, exist_ok=True)
+        toml = os.path.join(folder, "ncl.toml")
+        text = CROSS_PLANE_TOML.format(particles=NCL_PARTICLES, steps=NCL_STEPS, seed=seed, out=folder)
+        text = text.replace("[boundary]", '[scattering]\nmodel = "callaway"\ncallaway_formulation = "nonlinear"\n\n'
+                            "[boundary]", 1)
+        with open(toml, "w") as f:
+            f.write(text)
+        res = json.loads(subprocess.run([HARNESS, "run", mpath, toml, str(NCL_STEPS)], check=True,
+                                        capture_output=True, text=True).stdout)
+        rows = np.asarray(res["convergence"])
+        late = rows[rows[:, 0] >= out["average_from_step"]]
+        out["seeds"].append(seed)
+        out.setdefault("T_mean", []).append(late[:, 2:52].mean(axis=0).tolist())
+        out.setdefault("flux_mean", []).append(float(late[:, 52].mean()))
+        out.setdefault("kappa_eff_mean", []).append(float(late[:, 54].mean()))
+        out.setdefault("lifetime_residual_total", []).append(res["lifetime_residual_total"])
+        out.setdefault("balance_residual_total", []).append(res["balance_residual_total"][-1])
+    return out
+
+
 # Output files of a short FinFET run with its heat source and per-cell heat
 # flux rows (simulation.write_cell_heat_flux): convergence.txt,
 # grid_heat_flux.csv and heat_source_ledger.txt as the reference writes them.
@@ -358,6 +393,12 @@ def main() -> None:
         with gzip.open(os.path.join(HERE, "fullrun_finfet.json.gz"), "wt") as f:
             json.dump(data, f)
         print("fullrun_finfet ok")
+    if not args.only or "fullrun_ncallaway" in args.only:
+        data = full_runs_ncallaway(cpath, os.path.join(tmp, "fullrun_ncallaway"))
+        data["_harness_args"] = ["run", "{c}", "<cross-plane toml, nonlinear Callaway>", str(NCL_STEPS)]
+        with gzip.open(os.path.join(HERE, "fullrun_ncallaway.json.gz"), "wt") as f:
+            json.dump(data, f)
+        print("fullrun_ncallaway ok")
     if not args.only or "files_finfet" in args.only:
         data = output_files_finfet(mpath, fpath, tmp)
         data["_harness_args"] = ["run", "{m}", "<FinFET toml, write_cell_heat_flux>", str(FILES_STEPS)]

@@ -249,7 +249,7 @@ def test_callaway_steps_match_oracle(gpu, orc):
     """Linear-response collisions with momentum-conserving normal processes
     (four normal gain directions plus the resistive one): whole steps on the
     device against the oracle."""
-    mat = synthetic.make_material(mesh=16, callaway=True)
+    mat = synthetic.make_material(mesh=8, callaway=True)
     cfg = _callaway_cfg(20000, 13)
     mg = abi.Material(gpu, "phmc_", mat, 0.1, True, True)
     mo = abi.Material(orc, "orc_", mat, 0.1, True, True)
@@ -265,7 +265,7 @@ def test_mixed_callaway_conserves_energy_and_tracks_plain(gpu):
     """FP32 Callaway exponential (five gain directions) with the FP64 rescale:
     the collision changes the carried energy only at round-off, and cell
     temperatures follow the FP64 path to 1e-3 K."""
-    mat = synthetic.make_material(mesh=16, callaway=True)
+    mat = synthetic.make_material(mesh=8, callaway=True)
     cfg = _callaway_cfg(100000, 17)
     m = abi.Material(gpu, "phmc_", mat, 0.1, True, True)
     sp = abi.Solver(gpu, "phmc_", dict(cfg, precision="fp64"), [m])
@@ -338,7 +338,7 @@ def test_interface_golden(gpu, name, linearized):
 
 def _bilayer_pair(gpu, orc, particles, seed, precision="fp64"):
     cfg = workloads.scaled(workloads.bilayer_callaway(), particles, random_seed=seed, precision=precision)
-    data = workloads.bilayer_materials(16)
+    data = workloads.bilayer_materials(8)
     mg = [abi.Material(gpu, "phmc_", d, 0.1, True, True) for d in data]
     mo = [abi.Material(orc, "orc_", d, 0.1, True, True) for d in data]
     return (abi.Solver(gpu, "phmc_", cfg, mg), mg), (abi.Solver(orc, "orc_", cfg, mo), mo)
@@ -360,7 +360,7 @@ def test_bilayer_steps_match_oracle(gpu, orc):
 
 def test_mixed_bilayer_conserves_energy_and_tracks_plain(gpu):
     cfg = workloads.scaled(workloads.bilayer_callaway(), 200000, random_seed=37)
-    data = workloads.bilayer_materials(16)
+    data = workloads.bilayer_materials(8)
     m = [abi.Material(gpu, "phmc_", d, 0.1, True, True) for d in data]
     sp = abi.Solver(gpu, "phmc_", dict(cfg, precision="fp64"), m)
     sm = abi.Solver(gpu, "phmc_", dict(cfg, precision="mixed"), m)
@@ -391,7 +391,7 @@ def test_heat_source_steps_match_oracle(gpu, orc, spectrum, callaway):
     if callaway:
         cfg["collision_model"] = "callaway"
         cfg["lifetime_temperature"] = 300.0
-    mat = synthetic.make_material(mesh=16, callaway=callaway)
+    mat = synthetic.make_material(mesh=8 if callaway else 16, callaway=callaway)
     stationary = spectrum == "gaussian" or callaway
     mg = abi.Material(gpu, "phmc_", mat, 0.1, stationary, callaway)
     mo = abi.Material(orc, "orc_", mat, 0.1, stationary, callaway)

@@ -127,3 +127,39 @@ def test_bilayer_statistics(gpu, precision):
     tr_ref = np.array(g["interface_transmitted"]) / np.array(g["interface_events"])
     assert abs(_z(np.asarray(trans)[:, None], tr_ref[:, None])[0]) < 3.5
     assert max(resid) < 1e-6
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_nonlinear_callaway_statistics(gpu, precision):
+    """Cross-plane film with nonlinear Callaway collisions
+    (tests/golden/fullrun_ncallaway): cell temperatures, heat flux and
+    kappa_eff against 16 reference runs."""
+    g = golden("fullrun_ncallaway")
+    m = abi.Material(gpu, "phmc_", synthetic.make_material(mesh=8, callaway=True), 0.1, True, True)
+    T_mean, flux, kappa, resid = [], [], [], []
+    for k in range(len(g["seeds"])):
+        cfg = workloads.scaled(workloads.cross_plane_film(precision=precision), g["particles"], random_seed=9201 + k,
+                               convergence_write_interval=1, collision_model="callaway",
+                               callaway_formulation="nonlinear")
+        s = abi.Solver(gpu, "phmc_", cfg, [m])
+        T_acc, f_acc, k_acc = [], [], []
+        for step in range(1, g["steps"] + 1):
+            s.run(1)
+            if step >= g["average_from_step"]:
+                st = s.stats()
+                T_acc.append(s.cells()[0])
+                f_acc.append(st["average_heat_flux_along_axis"])
+                k_acc.append(st["kappa_endpoints"])
+        st = s.stats()
+        T_mean.append(np.mean(T_acc, axis=0))
+        flux.append(np.mean(f_acc))
+        kappa.append(np.mean(k_acc))
+        resid.append(abs(st["total_energy_balance_residual_ev"]))
+        s.close()
+    z = _z(T_mean, g["T_mean"])
+    bad = np.flatnonzero(~(np.abs(z) < 4.5))
+    assert bad.size == 0, (bad, z[bad], np.mean(T_mean, axis=0)[bad], np.mean(g["T_mean"], axis=0)[bad])
+    assert np.mean(z * z) < 2.5, np.mean(z * z)
+    assert abs(_z(np.asarray(flux)[:, None], np.asarray(g["flux_mean"])[:, None])[0]) < 3.5
+    assert abs(_z(np.asarray(kappa)[:, None], np.asarray(g["kappa_eff_mean"])[:, None])[0]) < 3.5
+    assert max(resid) < 1e-6

@@ -13,8 +13,8 @@ D = abi.dptr
 I32 = lambda a: a.ctypes.data_as(abi.c_int32_p)  # noqa: E731
 
 
-def _mat(lib, data, stationary=False):
-    return abi.Material(lib, "orc_", data, 0.1, stationary, False)
+def _mat(lib, data, stationary=False, callaway=False):
+    return abi.Material(lib, "orc_", data, 0.1, stationary, callaway)
 
 
 def _i32(x):
@@ -25,10 +25,16 @@ def _f64(x):
     return np.ascontiguousarray(x, dtype=np.float64)
 
 
-@pytest.mark.parametrize("name,stationary", [("material_m8", False), ("material_m8_stationary", True)])
-def test_material_tables(oracle_lib, m8, name, stationary):
+@pytest.mark.parametrize("name,stationary,callaway", [("material_m8", False, False),
+                                                       ("material_m8_stationary", True, False),
+                                                       ("material_m8c_stationary", True, True)])
+def test_material_tables(oracle_lib, m8, name, stationary, callaway):
     g = golden(name)
-    m = _mat(oracle_lib, m8, stationary)
+    if callaway:
+        from phonomc_gb300 import synthetic
+        m = _mat(oracle_lib, synthetic.make_material(mesh=8, callaway=True), stationary, True)
+    else:
+        m = _mat(oracle_lib, m8, stationary)
     na = int(g["active_mode_count"])
     sc = np.zeros(7)
     act = np.zeros(na, dtype=np.int32)
