@@ -1304,7 +1304,8 @@ Problem build_problem(const SimulationConfig& cfg, SimulationDomain& domain,
 }
 
 // src/solver/Initialization.cpp:32-137, 180-265 with Philox draws.
-CarrierArrays initial_carriers(const Problem& p, const std::vector<const PhononMaterial*>& mats) {
+CarrierArrays initial_carriers(const Problem& p, const std::vector<const PhononMaterial*>& mats,
+                               const double* preset_xyz) {
     const SimulationDomain& D = *p.domain;
     const int n = p.initial_particles;
     CarrierArrays c;
@@ -1368,6 +1369,15 @@ CarrierArrays initial_carriers(const Problem& p, const std::vector<const PhononM
             for (double& w : a) w /= sum;
             for (int c = 0; c < 3; ++c)
                 pos[c] = a[0] * sx.v[0][c] + a[1] * sx.v[1][c] + a[2] * sx.v[2][c] + a[3] * sx.v[3][c];
+        } else if (mesh && preset_xyz && !std::isnan(preset_xyz[3 * static_cast<size_t>(i)])) {
+            // accepted point of the same draws, found by the device ray cast
+            const double* q = preset_xyz + 3 * static_cast<size_t>(i);
+            if (std::isinf(q[0])) {
+#pragma omp critical
+                rejected = i;
+            } else {
+                pos = {q[0], q[1], q[2]};
+            }
         } else if (mesh) {
             bool ok = mesh->contains_point_ray_cast(pos);
             for (uint32_t trial = 1; !ok && trial < 200; ++trial) {

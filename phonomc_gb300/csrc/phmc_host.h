@@ -547,7 +547,11 @@ struct CarrierArrays {
     std::vector<int32_t> cell;
     std::vector<uint8_t> alive;
 };
-CarrierArrays initial_carriers(const Problem& p, const std::vector<const PhononMaterial*>& mats);
+// preset_xyz: accepted ray-cast positions of a mesh domain without a volume
+// decomposition, computed elsewhere from the same draws ([3n]; x NaN: sample
+// that carrier here, x +inf: rejected).
+CarrierArrays initial_carriers(const Problem& p, const std::vector<const PhononMaterial*>& mats,
+                               const double* preset_xyz = nullptr);
 
 // Mode-word helpers shared with the kernels.
 constexpr uint32_t kActiveMask = 0x00FFFFFFu;

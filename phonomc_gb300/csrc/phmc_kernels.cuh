@@ -89,6 +89,8 @@ void launch_step_begin(const LaunchCtx& x);
 // One heat-source half (time window from the device clock): accrue, deposit into the pending updates.
 void launch_source(const LaunchCtx& x, bool final_temperature, bool next);
 int launch_cell_solve(const LaunchCtx& x, int phase, int collision);
+void launch_mesh_initial_positions(const LaunchCtx& x, int n, uint64_t seed, const double lo[3], const double hi[3],
+                                   double* xyz);
 void launch_ncl_cell(int n_modes, const double* omega, const double* k3, const double* rn, const double* rr,
                      double* cnt, double2* ab, double2* work, int64_t n, const int32_t* mode, double* occ, double T,
                      double dt, int* status, cudaStream_t s);

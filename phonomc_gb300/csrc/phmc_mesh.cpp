@@ -875,15 +875,24 @@ void SimulationDomain::build_mesh_domain(const SimulationConfig& cfg) {
     inv_cell_ = {ext[0] > 0.0 ? nx / ext[0] : 0.0, ext[1] > 0.0 ? ny / ext[1] : 0.0, ext[2] > 0.0 ? nz / ext[2] : 0.0};
     const size_t total = static_cast<size_t>(nx) * ny * nz;
     voxel_cell_.assign(total, -1);
-    for (int ix = 0; ix < nx; ++ix)
-        for (int iy = 0; iy < ny; ++iy)
-            for (int iz = 0; iz < nz; ++iz) {
-                const Vec3 p{bmin_[0] + (ix + 0.5) * ext[0] / nx, bmin_[1] + (iy + 0.5) * ext[1] / ny,
-                             bmin_[2] + (iz + 0.5) * ext[2] / nz};
-                if (!M.contains_point(p)) continue;
-                voxel_cell_[(static_cast<size_t>(ix) * ny + iy) * nz + iz] = static_cast<int>(centers_.size());
-                centers_.push_back(p);
-            }
+    auto voxel_centre = [&](size_t v) {
+        const int ix = static_cast<int>(v / (static_cast<size_t>(ny) * nz)), iy = static_cast<int>(v / nz % ny),
+                  iz = static_cast<int>(v % nz);
+        return Vec3{bmin_[0] + (ix + 0.5) * ext[0] / nx, bmin_[1] + (iy + 0.5) * ext[1] / ny,
+                    bmin_[2] + (iz + 0.5) * ext[2] / nz};
+    };
+    // membership in parallel (the lazily built decomposition first), cell
+    // numbers in voxel order
+    (void)M.simplices();
+    std::vector<unsigned char> inside(total, 0);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (long long v = 0; v < static_cast<long long>(total); ++v)
+        inside[v] = M.contains_point(voxel_centre(static_cast<size_t>(v))) ? 1 : 0;
+    for (size_t v = 0; v < total; ++v) {
+        if (!inside[v]) continue;
+        voxel_cell_[v] = static_cast<int>(centers_.size());
+        centers_.push_back(voxel_centre(v));
+    }
     if (centers_.empty()) throw std::runtime_error("No valid grid centers found inside mesh.");
     std::deque<int> queue;
     for (size_t c = 0; c < total; ++c)

@@ -89,7 +89,23 @@ DeviceSolver::DeviceSolver(const SimulationConfig& cfg, const std::vector<const 
     allocate_state(n0 + margin);
     upload_tables();
     if (!init_carriers) return;
-    const CarrierArrays c = initial_carriers(P_, mats_);
+    // A mesh without a volume decomposition samples positions by ray-cast
+    // rejection: that part runs on the device, with the host's draws.
+    std::vector<double> preset;
+    if (domain_->is_mesh() && domain_->mesh()->simplices().empty() && n0 > 0) {
+        double* d_xyz = nullptr;
+        const size_t bytes = 3 * static_cast<size_t>(n0) * sizeof(double);
+        PHMC_CUDA(cudaMalloc(&d_xyz, bytes));
+        launch_mesh_initial_positions(ctx(), n0, cfg_.random_seed, domain_->bounds_min().data(),
+                                      domain_->bounds_max().data(), d_xyz);
+        preset.resize(3 * static_cast<size_t>(n0));
+        const cudaError_t e = cudaMemcpyAsync(preset.data(), d_xyz, bytes, cudaMemcpyDeviceToHost, stream_);
+        const cudaError_t e2 = cudaStreamSynchronize(stream_);
+        cudaFree(d_xyz);
+        PHMC_CUDA(e);
+        PHMC_CUDA(e2);
+    }
+    const CarrierArrays c = initial_carriers(P_, mats_, preset.empty() ? nullptr : preset.data());
     set_carriers(n0, c.x.data(), c.y.data(), c.z.data(), c.occ.data(), c.mode.data(), c.alive.data());
     if (!cfg_.output_folder.empty()) {
         std::filesystem::create_directories(cfg_.output_folder);

@@ -1441,6 +1441,40 @@ void launch_ingest(const LaunchCtx& x, bool mixed, const HostCarriers& h) {
 
 void launch_ledger_replace(const LaunchCtx& x, int n) { k_ledger_replace<<<1, 1, 0, x.stream>>>(x.L, n); }
 
+// Initial positions in a mesh domain without a volume decomposition, the
+// ray-cast branch of initial_carriers (src/geometry/SurfaceSampling.cpp:114-121):
+// uniform points of the bounding box kept when the +x ray cast finds them
+// inside, at most 200 trials, with the host's counter-based draws and FP64
+// operation order. x = NaN: the ray cast overflowed its hit list (the host
+// repeats that carrier); x = +inf: no accepted point.
+__global__ void k_mesh_initial_positions(const __grid_constant__ DevTables T, int n, uint64_t seed, double3 lo,
+                                         double3 hi, double* xyz) {
+    const double ex = dadd(hi.x, -lo.x), ey = dadd(hi.y, -lo.y), ez = dadd(hi.z, -lo.z);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int r = 0;
+        double p[3] = {0.0, 0.0, 0.0};
+        for (uint32_t trial = 0; trial < 200u && r == 0; ++trial) {
+            const Uniform2 a = uniform2(seed, static_cast<uint32_t>(i), 0xFFFFFFFFu, kDrawInit, trial, 0);
+            const Uniform2 b = uniform2(seed, static_cast<uint32_t>(i), 0xFFFFFFFFu, kDrawInit, trial, 1);
+            p[0] = dadd(lo.x, dmul(ex, a.a));
+            p[1] = dadd(lo.y, dmul(ey, a.b));
+            p[2] = dadd(lo.z, dmul(ez, b.a));
+            r = mesh_ray_cast_inside(T.fac, p);
+        }
+        double* o = xyz + 3 * static_cast<size_t>(i);
+        o[0] = r > 0 ? p[0] : (r < 0 ? __longlong_as_double(0x7ff8000000000000LL) : INFINITY);
+        o[1] = p[1];
+        o[2] = p[2];
+    }
+}
+
+void launch_mesh_initial_positions(const LaunchCtx& x, int n, uint64_t seed, const double lo[3], const double hi[3],
+                                   double* xyz) {
+    const int g = std::max(1, std::min(x.grid_blocks, (n + 127) / 128));
+    k_mesh_initial_positions<<<g, 128, 0, x.stream>>>(*x.Th, n, seed, make_double3(lo[0], lo[1], lo[2]),
+                                                       make_double3(hi[0], hi[1], hi[2]), xyz);
+}
+
 int launch_mesh_cache_init(const LaunchCtx& x) {
     if (!x.mesh) return 0;
     k_mesh_cache_init<<<x.grid_blocks, 128, 0, x.stream>>>(*x.Th, x.S, x.L);
