@@ -762,7 +762,8 @@ __device__ __forceinline__ void cluster_sum(V (&v)[N], double* red, double (*par
 }
 
 template <class R, int GMAX>
-__global__ void __launch_bounds__(kLinThreads) k_linear_solve(const DevTables* __restrict__ Tp, CellArrays C) {
+__global__ void __launch_bounds__(kLinThreads) k_linear_solve(const DevTables* __restrict__ Tp, CellArrays C,
+                                                               unsigned char* __restrict__ gslice, size_t slice) {
     // R = float: FP32 exponential from division-free FP32 per-mode tables; FP64
     // only for the bin energies, the conservation sums and the final beta.
     constexpr bool kF32 = sizeof(R) == sizeof(float);
@@ -784,7 +785,10 @@ __global__ void __launch_bounds__(kLinThreads) k_linear_solve(const DevTables* _
     const int per = (C.hist_modes + CL - 1) / CL;
     const int m0 = rank * per, m1 = min(na, m0 + per);
     const int nloc = max(0, m1 - m0);
-    R* X = reinterpret_cast<R*>(smem);
+    // per-mode vectors of this CTA's slice: shared memory, or (tables too
+    // large for a 16-CTA cluster) this CTA's slice of a global work area
+    unsigned char* base = gslice ? gslice + static_cast<size_t>(blockIdx.x) * slice : smem;
+    R* X = reinterpret_cast<R*>(base);
     R* term = X + per;
     R* rate = term + per;
     R* u = rate + per;                                      // gmax vectors
@@ -1323,9 +1327,15 @@ int linear_cluster_size(const CellArrays& C, bool mixed) {
     return 0;
 }
 
-void prepare_linear_solve(const CellArrays& C) {
+// Bytes of one CTA's per-mode slice when it lives in global memory (cluster of 16).
+size_t linear_global_slice(const CellArrays& C, bool mixed) {
     const int gmax = C.lin_has_normal ? kMaxGains : 1;
-    const size_t sm = linear_smem(C, C.lin_cluster, gmax, C.mixed ? sizeof(float) : sizeof(double));
+    return (linear_smem(C, 16, gmax, mixed ? sizeof(float) : sizeof(double)) + 255) / 256 * 256;
+}
+
+void prepare_linear_solve(const CellArrays& C, bool global) {
+    const int gmax = C.lin_has_normal ? kMaxGains : 1;
+    const size_t sm = global ? 0 : linear_smem(C, C.lin_cluster, gmax, C.mixed ? sizeof(float) : sizeof(double));
     auto set = [&](const void* f) {
         cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
         if (C.lin_cluster > 8) cudaFuncSetAttribute(f, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
@@ -1361,7 +1371,7 @@ int launch_cell_solve(const LaunchCtx& x, int phase, int collision) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(C.ncells * cl);
         cfg.blockDim = dim3(kLinThreads);
-        cfg.dynamicSmemBytes = linear_smem(C, cl, gmax, C.mixed ? sizeof(float) : sizeof(double));
+        cfg.dynamicSmemBytes = x.lin_slice ? 0 : linear_smem(C, cl, gmax, C.mixed ? sizeof(float) : sizeof(double));
         cfg.stream = x.stream;
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -1371,12 +1381,14 @@ int launch_cell_solve(const LaunchCtx& x, int phase, int collision) {
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         cudaError_t err;
+        unsigned char* gs = x.lin_work;
+        const size_t sl = x.lin_slice;
         if (C.lin_has_normal)
-            err = C.mixed ? cudaLaunchKernelEx(&cfg, k_linear_solve<float, kMaxGains>, T, C)
-                          : cudaLaunchKernelEx(&cfg, k_linear_solve<double, kMaxGains>, T, C);
+            err = C.mixed ? cudaLaunchKernelEx(&cfg, k_linear_solve<float, kMaxGains>, T, C, gs, sl)
+                          : cudaLaunchKernelEx(&cfg, k_linear_solve<double, kMaxGains>, T, C, gs, sl);
         else
-            err = C.mixed ? cudaLaunchKernelEx(&cfg, k_linear_solve<float, 1>, T, C)
-                          : cudaLaunchKernelEx(&cfg, k_linear_solve<double, 1>, T, C);
+            err = C.mixed ? cudaLaunchKernelEx(&cfg, k_linear_solve<float, 1>, T, C, gs, sl)
+                          : cudaLaunchKernelEx(&cfg, k_linear_solve<double, 1>, T, C, gs, sl);
         if (err != cudaSuccess)
             throw std::runtime_error(std::string("cluster launch of the collision exponential failed: ") +
                                      cudaGetErrorString(err));

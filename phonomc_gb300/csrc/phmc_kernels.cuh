@@ -27,6 +27,8 @@ struct LaunchCtx {
     int grid_blocks;
     bool mesh = false;   // surface-mesh domain (plain FP64 carrier state)
     const DevNcl* ncl = nullptr; // host copy, nonlinear Callaway only
+    unsigned char* lin_work = nullptr; // linear Callaway: per-CTA mode slices in global memory (null: shared)
+    size_t lin_slice = 0;              // bytes per CTA slice of lin_work
 };
 
 // Independent box instances advanced by one launch per kernel of the step:
@@ -95,7 +97,8 @@ void launch_ncl_cell(int n_modes, const double* omega, const double* k3, const d
                      double* cnt, double2* ab, double2* work, int64_t n, const int32_t* mode, double* occ, double T,
                      double dt, int* status, cudaStream_t s);
 int linear_cluster_size(const CellArrays& C, bool mixed);
-void prepare_linear_solve(const CellArrays& C);
+void prepare_linear_solve(const CellArrays& C, bool global);
+size_t linear_global_slice(const CellArrays& C, bool mixed);
 void launch_cells_final(const LaunchCtx& x, int phase);
 
 // collision kinds for launch_cell_solve

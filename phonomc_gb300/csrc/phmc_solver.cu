@@ -548,8 +548,14 @@ void DeviceSolver::upload_tables() {
         C.lin_omd = upload(omd);
         C.lin_bg = upload(bg);
         C.lin_cluster = linear_cluster_size(C, mixed_);
-        if (C.lin_cluster == 0) throw std::runtime_error("Too many modes per cell for the cluster exponential.");
-        prepare_linear_solve(C);
+        if (C.lin_cluster == 0) {
+            // a cell's modes exceed the shared memory of a 16-CTA cluster: the
+            // per-mode vectors live in a global work area, 16 CTAs per cell
+            C.lin_cluster = 16;
+            lin_slice_ = linear_global_slice(C, mixed_);
+            lin_work_ = dalloc<unsigned char>(static_cast<size_t>(ncells_) * 16 * lin_slice_);
+        }
+        prepare_linear_solve(C, lin_work_ != nullptr);
     }
 }
 
@@ -582,6 +588,8 @@ LaunchCtx DeviceSolver::ctx() const {
     x.grid_blocks = static_cast<int>(std::max<long long>(8, std::min<long long>(sm_count_ * 8, want)));
     x.mesh = domain_->is_mesh();
     x.ncl = P_.callaway_nonlinear ? &ncl_ : nullptr;
+    x.lin_work = lin_work_;
+    x.lin_slice = lin_slice_;
     return x;
 }
 

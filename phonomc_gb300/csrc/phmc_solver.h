@@ -243,6 +243,8 @@ private:
     // flux passes copied into pinned host slots and processed when their event completes
     std::vector<struct Observation*> obs_free_, obs_pending_;
     DevNcl ncl_{}; // nonlinear Callaway tables and work space
+    unsigned char* lin_work_ = nullptr; // linear Callaway per-mode slices when a cell's modes exceed shared memory
+    size_t lin_slice_ = 0;
     // graph of one timestep
     bool use_graphs_ = true;
     cudaGraph_t graph_ = nullptr;

@@ -614,3 +614,21 @@ def test_nonlinear_callaway_steps_match_oracle(gpu, orc):
         stg, sto = _compare(sg, so, tol=1e-9)
         assert abs(stg["total_lifetime_energy_residual_ev"] - sto["total_lifetime_energy_residual_ev"]) < 1e-8
     assert abs(stg["total_energy_balance_residual_ev"]) < 1e-6
+
+
+def test_callaway_global_mode_slices_match_oracle(gpu, orc):
+    """A 16^3 Callaway table completes to 196,584 modes, more than the shared
+    memory of a 16-CTA cluster holds per cell: the exponential keeps its
+    per-mode vectors in a global work area instead. Whole steps against the
+    oracle."""
+    mat = synthetic.make_material(mesh=16, callaway=True)
+    cfg = workloads.scaled(workloads.inplane_gradient(), 20000, random_seed=19, collision_model="callaway",
+                           grid=(1, 1, 10))
+    mg = abi.Material(gpu, "phmc_", mat, 0.1, True, True)
+    mo = abi.Material(orc, "orc_", mat, 0.1, True, True)
+    sg = abi.Solver(gpu, "phmc_", cfg, [mg])
+    so = abi.Solver(orc, "orc_", cfg, [mo])
+    for _ in range(2):
+        sg.run(2)
+        so.run(2)
+        _compare(sg, so, tol=1e-11)
