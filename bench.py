@@ -66,6 +66,8 @@ def workload_materials(name):
     from phonomc_gb300 import synthetic, workloads
     if name == "bilayer_callaway":
         return [(d, True, True) for d in workloads.bilayer_materials(8)]
+    if name == "nonlinear_callaway_film":
+        return [(synthetic.make_material(mesh=8, callaway=True), True, True)]
     return [(synthetic.make_material(mesh=16), name == "inplane_gradient", False)]
 
 
@@ -361,6 +363,8 @@ def run_ours(args):
         "config": {"workload": args.workload, "particles": int(args.particles), "precision": args.precision,
                    "material": ("two synthetic 8^3 x 6 tables, second 0.7x frequency 0.75x velocity, Callaway BZ "
                                 "completed (24552 modes)" if args.workload == "bilayer_callaway"
+                                else "synthetic 8^3 x 6 Callaway table, BZ completed (24552 modes)"
+                                if args.workload == "nonlinear_callaway_film"
                                 else "synthetic 16^3 x 6 modes (seed 0)"), "cells": int(Tout.size),
                    **({"mesh": "procedural FinFET, 6304 triangles, 2245 facets (seed 0)", "voxels": "64x32x32",
                        "heat_source": "gaussian 1e20 W/m^3, sigma 5 nm, fin top, thermal spectrum"}
@@ -404,14 +408,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="inplane_gradient",
                     choices=["inplane_gradient", "cross_plane_film", "bilayer_callaway", "heated_film",
-                             "batched_films", "finfet_mesh"])
+                             "batched_films", "finfet_mesh", "nonlinear_callaway_film"])
     ap.add_argument("--particles", type=float, default=None)
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.particles is None:
-        args.particles = {"inplane_gradient": 5e7, "finfet_mesh": 2e7}.get(args.workload, 1e6)
+        args.particles = {"inplane_gradient": 5e7, "finfet_mesh": 2e7, "nonlinear_callaway_film": 1e7}.get(
+            args.workload, 1e6)
     if args.workload == "finfet_mesh" and args.impl == "ours":
         # mesh domains run the plain FP64 carrier state
         args.precision, args.no_plain = "fp64", True

@@ -350,10 +350,57 @@ __device__ __forceinline__ double ncl_bose(double x) { return x > 700.0 ? 0.0 : 
 
 struct NclBlock {
     double red[16 * 32];
+    double part[2][16]; // this CTA's partial sums, read by the cluster (alternating buffers)
+    double total[16];
     double B[4][4];   // basis coefficients over (phi0, kx, ky, kz)
     double y[4];      // phi = sum_k y_k f_k for the point being evaluated
     double lambda[4], delta[4], scale[4];
     int dim, status;
+};
+
+// Sums over the modes of one cell: one CTA (block_sum), or the CTAs of a
+// cluster, each holding the modes m = rank * blockDim + t (mod ranks * blockDim);
+// every CTA gets the same totals, so every decision below is cluster-uniform.
+struct NclOneBlock {
+    __device__ int first() const { return threadIdx.x; }
+    __device__ int stride() const { return blockDim.x; }
+    template <int N> __device__ void sum(double (&v)[N], NclBlock& sh) { block_sum<N>(v, sh.red); }
+};
+
+struct NclCluster {
+    int rank, ranks, parity;
+    __device__ int first() const { return rank * blockDim.x + threadIdx.x; }
+    __device__ int stride() const { return ranks * blockDim.x; }
+    template <int N> __device__ void sum(double (&v)[N], NclBlock& sh) {
+        static_assert(N <= 16, "cluster sums hold 16 values");
+        cg::cluster_group cl = cg::this_cluster();
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        for (int k = 0; k < N; ++k) {
+            double x = v[k];
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            if (lane == 0) sh.red[k * 32 + wid] = x;
+        }
+        __syncthreads();
+        if (wid == 0)
+            for (int k = 0; k < N; ++k) {
+                double x = lane < nw ? sh.red[k * 32 + lane] : 0.0;
+                for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+                if (lane == 0) sh.part[parity][k] = x;
+            }
+        cl.sync();
+        if (wid == 0) {
+            const double* rp = cl.map_shared_rank(&sh.part[parity][0], lane < ranks ? lane : 0);
+            for (int k = 0; k < N; ++k) {
+                double x = lane < ranks ? rp[k] : 0.0;
+                for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+                if (lane == 0) sh.total[k] = x;
+            }
+        }
+        __syncthreads();
+        for (int k = 0; k < N; ++k) v[k] = sh.total[k];
+        __syncthreads();
+        parity ^= 1;
+    }
 };
 
 // Features of mode m in cell temperature T.
@@ -367,12 +414,12 @@ __device__ __forceinline__ void ncl_features(const Modes& Q, int m, double T, do
 
 // Potential, gradient and (want_h) Hessian at the point y of sh; returns
 // invalid (phi <= 0 or not finite somewhere) as +inf in v[0].
-template <class Modes>
-__device__ __forceinline__ void ncl_evaluate(const Modes& Q, NclBlock& sh, double2* work, double T, bool want_h,
-                                             double (&v)[16]) {
+template <class Modes, class Red>
+__device__ __forceinline__ void ncl_evaluate(const Modes& Q, NclBlock& sh, Red& rd, double2* work, double T,
+                                             bool want_h, double (&v)[16]) {
     for (int k = 0; k < 16; ++k) v[k] = 0.0;
     const int dim = sh.dim;
-    for (int m = threadIdx.x; m < Q.n; m += blockDim.x) {
+    for (int m = rd.first(); m < Q.n; m += rd.stride()) {
         const double c = Q.count(m);
         const double a = work[m].y;
         if (c == 0.0 || a == 0.0) continue;
@@ -397,7 +444,7 @@ __device__ __forceinline__ void ncl_evaluate(const Modes& Q, NclBlock& sh, doubl
                 for (int l = j; l < 4; ++l) v[q++] += h * b[j] * b[l];
         }
     }
-    block_sum<16>(v, sh.red);
+    rd.sum(v, sh);
     if (v[15] != 0.0) v[0] = INFINITY;
 }
 
@@ -420,10 +467,10 @@ __device__ __forceinline__ double ncl_error(const NclBlock& sh, const double (&v
 // One cell: bins of Q (count, work.x = occupation sum on entry), rates by
 // Q.rate(m, normal). Writes (alpha, beta) per mode through Q.out(m, alpha,
 // beta); returns 0 or an error code (block-uniform).
-template <class Modes>
-__device__ int ncl_solve_cell(const Modes& Q, NclBlock& sh, double2* work, double T, double dt) {
+template <class Modes, class Red>
+__device__ int ncl_solve_cell(const Modes& Q, NclBlock& sh, Red& rd, double2* work, double T, double dt) {
     if (threadIdx.x == 0) sh.status = 0;
-    for (int m = threadIdx.x; m < Q.n; m += blockDim.x) Q.out(m, 1.0, 0.0);
+    for (int m = rd.first(); m < Q.n; m += rd.stride()) Q.out(m, 1.0, 0.0);
     __syncthreads();
     if (dt == 0.0) return 0;
     for (int sub = 0; sub < 3; ++sub) {
@@ -432,7 +479,7 @@ __device__ int ncl_solve_cell(const Modes& Q, NclBlock& sh, double2* work, doubl
         // relaxation weights, activity and the Gram matrix of the features
         double v[16];
         for (int k = 0; k < 16; ++k) v[k] = 0.0;
-        for (int m = threadIdx.x; m < Q.n; m += blockDim.x) {
+        for (int m = rd.first(); m < Q.n; m += rd.stride()) {
             const double a = -expm1(-Q.rate(m, normal) * h);
             work[m].y = a;
             const double c = Q.count(m);
@@ -446,7 +493,7 @@ __device__ int ncl_solve_cell(const Modes& Q, NclBlock& sh, double2* work, doubl
             for (int k = 0; k < 4; ++k)
                 for (int l = k; l < 4; ++l) v[q++] += w * f[k] * f[l];
         }
-        block_sum<16>(v, sh.red);
+        rd.sum(v, sh);
         if (v[0] == 0.0) continue; // no activity
         if (threadIdx.x == 0) {
             double G[4][4];
@@ -484,7 +531,7 @@ __device__ int ncl_solve_cell(const Modes& Q, NclBlock& sh, double2* work, doubl
         if (sh.status) return sh.status;
         // convergence scales
         for (int k = 0; k < 16; ++k) v[k] = 0.0;
-        for (int m = threadIdx.x; m < Q.n; m += blockDim.x) {
+        for (int m = rd.first(); m < Q.n; m += rd.stride()) {
             const double c = Q.count(m);
             if (c == 0.0) continue;
             double f[4];
@@ -496,7 +543,7 @@ __device__ int ncl_solve_cell(const Modes& Q, NclBlock& sh, double2* work, doubl
                 v[j] += fabs(a * b) * top;
             }
         }
-        block_sum<16>(v, sh.red);
+        rd.sum(v, sh);
         if (threadIdx.x == 0)
             for (int j = 0; j < 4; ++j) sh.scale[j] = v[j];
         __syncthreads();
@@ -505,7 +552,7 @@ __device__ int ncl_solve_cell(const Modes& Q, NclBlock& sh, double2* work, doubl
         for (int it = 0; it < 70 && !converged; ++it) {
             ncl_set_point(sh, sh.lambda);
             double g[16];
-            ncl_evaluate(Q, sh, work, T, true, g);
+            ncl_evaluate(Q, sh, rd, work, T, true, g);
             const double F = g[0];
             const double err = ncl_error(sh, g);
             if (err < 2e-13) {
@@ -558,7 +605,7 @@ __device__ int ncl_solve_cell(const Modes& Q, NclBlock& sh, double2* work, doubl
                 __syncthreads();
                 ncl_set_point(sh, trial);
                 double gt[16];
-                ncl_evaluate(Q, sh, work, T, false, gt);
+                ncl_evaluate(Q, sh, rd, work, T, false, gt);
                 if (isfinite(gt[0]) && (gt[0] <= F + 1e-4 * t * slope || ncl_error(sh, gt) < err * 0.9)) {
                     __syncthreads();
                     if (threadIdx.x == 0)
@@ -574,7 +621,7 @@ __device__ int ncl_solve_cell(const Modes& Q, NclBlock& sh, double2* work, doubl
         // move the modes: occupation sums and the composed affine map
         ncl_set_point(sh, sh.lambda);
         int bad = 0;
-        for (int m = threadIdx.x; m < Q.n; m += blockDim.x) {
+        for (int m = rd.first(); m < Q.n; m += rd.stride()) {
             const double a = work[m].y, c = Q.count(m);
             if (!(a > 0.0) || c == 0.0) continue;
             double f[4];
@@ -584,7 +631,9 @@ __device__ int ncl_solve_cell(const Modes& Q, NclBlock& sh, double2* work, doubl
             work[m].x = (1.0 - a) * work[m].x + a * c * t;
             Q.compose(m, 1.0 - a, a * t);
         }
-        if (__syncthreads_or(bad)) return kErrNclInvalid;
+        double flag[1] = {bad ? 1.0 : 0.0};
+        rd.sum(flag, sh);
+        if (flag[0] != 0.0) return kErrNclInvalid;
     }
     return 0;
 }
@@ -619,13 +668,19 @@ struct NclSimModes {
     }
 };
 
-// One CTA per cell: the nonlinear Callaway update of the cell's carriers as
-// the pending (alpha, beta) of each mode bin (in C.rta_ab, stride hist_modes).
+// One cluster of kNclCluster CTAs per cell: the nonlinear Callaway update of
+// the cell's carriers as the pending (alpha, beta) of each mode bin (in
+// C.rta_ab, stride hist_modes). The CTAs split the cell's modes; every exit
+// passes one cluster barrier so no CTA leaves while another reads its sums.
+constexpr int kNclCluster = 8;
+
 __global__ void __launch_bounds__(kNclThreads) k_ncl_solve(const DevTables* __restrict__ Tp, CellArrays C,
                                                             DevLedger* L, const DevNcl X) {
     __shared__ NclBlock sh;
+    cg::cluster_group cl = cg::this_cluster();
+    NclCluster rd{static_cast<int>(cl.block_rank()), static_cast<int>(cl.num_blocks()), 0};
     const DevTables& T = *Tp;
-    const int c = blockIdx.x;
+    const int c = blockIdx.x / rd.ranks;
     const int mid = C.cell_material[c];
     const DevMaterial& M = T.mat[mid];
     const size_t hb = static_cast<size_t>(c) * C.hist_modes;
@@ -642,32 +697,34 @@ __global__ void __launch_bounds__(kNclThreads) k_ncl_solve(const DevTables* __re
     const double Tc = C.temperature[c];
     const double Tr = X.local ? Tc : X.lifetime_T;
     // src/solver/NonlinearCallawayCollision.cpp:309-312 and :218-221
-    unsigned carriers = 0;
-    for (int m = threadIdx.x; m < Q.n; m += blockDim.x) {
+    double carriers[1] = {0.0};
+    for (int m = rd.first(); m < Q.n; m += rd.stride()) {
         const BinSum b = Q.bins[m];
         work[m] = make_double2(b.N, 0.0);
-        carriers += b.cnt;
+        carriers[0] += b.cnt;
     }
-    if (!__syncthreads_or(carriers != 0u)) {
-        for (int m = threadIdx.x; m < Q.n; m += blockDim.x) Q.out(m, 1.0, 0.0);
-        return;
+    rd.sum(carriers, sh);
+    int st = 0;
+    bool solved = false;
+    if (carriers[0] != 0.0) {
+        if (!(Tr > 0.0) || !isfinite(Tr) || Tr < M.temps[0] || Tr > M.temps[M.n_temps - 1] || !(Tc > 0.0) ||
+            !isfinite(Tc)) {
+            st = kErrNclTemperature;
+        } else {
+            int hi = 0;
+            const int n = M.n_temps;
+            while (hi < n && M.temps[hi] < Tr) ++hi; // lower_bound
+            Q.hi = hi;
+            Q.lo = hi > 0 ? hi - 1 : hi;
+            Q.fr = Q.lo == Q.hi ? 0.0 : (Tr - M.temps[Q.lo]) / (M.temps[Q.hi] - M.temps[Q.lo]);
+            st = ncl_solve_cell(Q, sh, rd, work, Tc, T.par.dt);
+            solved = st == 0;
+        }
     }
-    if (!(Tr > 0.0) || !isfinite(Tr) || Tr < M.temps[0] || Tr > M.temps[M.n_temps - 1] || !(Tc > 0.0) ||
-        !isfinite(Tc)) {
-        if (threadIdx.x == 0) raise_error(L, kErrNclTemperature, c);
-        for (int m = threadIdx.x; m < Q.n; m += blockDim.x) Q.out(m, 1.0, 0.0);
-        return;
-    }
-    int hi = 0, n = M.n_temps;
-    while (hi < n && M.temps[hi] < Tr) ++hi; // lower_bound
-    Q.hi = hi;
-    Q.lo = hi > 0 ? hi - 1 : hi;
-    Q.fr = Q.lo == Q.hi ? 0.0 : (Tr - M.temps[Q.lo]) / (M.temps[Q.hi] - M.temps[Q.lo]);
-    const int st = ncl_solve_cell(Q, sh, work, Tc, T.par.dt);
-    if (st != 0) {
-        if (threadIdx.x == 0) raise_error(L, st, c);
-        for (int m = threadIdx.x; m < Q.n; m += blockDim.x) Q.out(m, 1.0, 0.0);
-    }
+    if (!solved)
+        for (int m = rd.first(); m < Q.n; m += rd.stride()) Q.out(m, 1.0, 0.0);
+    if (st != 0 && rd.rank == 0 && threadIdx.x == 0) raise_error(L, st, c);
+    cl.sync();
 }
 
 // Stand-alone cell for phmc_dev_ncallaway_evolve: per-mode arrays.
@@ -694,8 +751,9 @@ struct NclArrayModes {
 __global__ void __launch_bounds__(kNclThreads) k_ncl_cell(NclArrayModes Q, double* cnt, double2* work, int64_t n,
                                                            const int32_t* mode, double* occ, double T, double dt,
                                                            int* status) {
+    NclOneBlock rd;
     __shared__ NclBlock sh;
-    for (int m = threadIdx.x; m < Q.n; m += blockDim.x) {
+    for (int m = rd.first(); m < Q.n; m += rd.stride()) {
         double c = 0.0, N = 0.0;
         for (int64_t i = 0; i < n; ++i)
             if (mode[i] == m) {
@@ -706,7 +764,7 @@ __global__ void __launch_bounds__(kNclThreads) k_ncl_cell(NclArrayModes Q, doubl
         work[m] = make_double2(N, 0.0);
     }
     __syncthreads();
-    const int st = ncl_solve_cell(Q, sh, work, T, dt);
+    const int st = ncl_solve_cell(Q, sh, rd, work, T, dt);
     if (threadIdx.x == 0) *status = st;
     if (st != 0) return;
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
@@ -1395,7 +1453,21 @@ int launch_cell_solve(const LaunchCtx& x, int phase, int collision) {
         ++launches;
     }
     if (phase >= 1 && collision == kCollideNonlinear) {
-        k_ncl_solve<<<C.ncells, kNclThreads, 0, x.stream>>>(T, C, x.L, *x.ncl);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(C.ncells * kNclCluster);
+        cfg.blockDim = dim3(kNclThreads);
+        cfg.stream = x.stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = kNclCluster;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        const cudaError_t err = cudaLaunchKernelEx(&cfg, k_ncl_solve, T, C, x.L, *x.ncl);
+        if (err != cudaSuccess)
+            throw std::runtime_error(std::string("cluster launch of the nonlinear Callaway solve failed: ") +
+                                     cudaGetErrorString(err));
         ++launches;
     }
     if (phase >= 1 && rta) k_cell_tables<kCollideRta><<<grid, kStatThreads, 0, x.stream>>>(T, C, phase);

@@ -53,6 +53,15 @@ def cross_plane_film(particles: float = 1e6, seed: int = 12345, precision: str =
     }
 
 
+def nonlinear_callaway_film(particles: float = 1e7, seed: int = 12345, precision: str = "fp64") -> dict:
+    """The cross-plane film with nonlinear Callaway collisions
+    (scattering.callaway_formulation = "nonlinear"; absolute occupations,
+    conservative boundaries, fixed 300 K rates); 8^3 Callaway table."""
+    c = cross_plane_film(particles, seed, precision)
+    c.update(name="nonlinear_callaway_film", collision_model="callaway", callaway_formulation="nonlinear")
+    return c
+
+
 def inplane_gradient(particles: float = 5e7, seed: int = 12345, precision: str = "fp64") -> dict:
     return {
         "name": "inplane_gradient",
