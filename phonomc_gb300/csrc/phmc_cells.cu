@@ -674,7 +674,7 @@ struct NclSimModes {
 // passes one cluster barrier so no CTA leaves while another reads its sums.
 constexpr int kNclCluster = 8;
 
-__global__ void __launch_bounds__(kNclThreads) k_ncl_solve(const DevTables* __restrict__ Tp, CellArrays C,
+__global__ void __launch_bounds__(kNclThreads, 3) k_ncl_solve(const DevTables* __restrict__ Tp, CellArrays C,
                                                             DevLedger* L, const DevNcl X) {
     __shared__ NclBlock sh;
     cg::cluster_group cl = cg::this_cluster();
