@@ -597,13 +597,15 @@ def test_nonlinear_callaway_cell_golden(gpu, name, rtol):
     assert np.allclose(occ, g["out"], rtol=rtol, atol=0)
 
 
-def test_nonlinear_callaway_steps_match_oracle(gpu, orc):
+@pytest.mark.parametrize("lifetime", [300.0, "local"])
+def test_nonlinear_callaway_steps_match_oracle(gpu, orc, lifetime):
     """Whole steps of a cross-plane film with nonlinear Callaway collisions
     (absolute occupations, conservative boundaries) on the device against the
-    oracle's per-carrier long-double restatement."""
+    oracle's per-carrier long-double restatement; N/U rates at the fixed 300 K
+    or interpolated at each cell's temperature."""
     mat = synthetic.make_material(mesh=8, callaway=True)
     cfg = workloads.scaled(workloads.cross_plane_film(), 20000, random_seed=17, collision_model="callaway",
-                           callaway_formulation="nonlinear")
+                           callaway_formulation="nonlinear", lifetime_temperature=lifetime)
     mg = abi.Material(gpu, "phmc_", mat, 0.1, True, True)
     mo = abi.Material(orc, "orc_", mat, 0.1, True, True)
     sg = abi.Solver(gpu, "phmc_", cfg, [mg])
