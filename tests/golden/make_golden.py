@@ -2,7 +2,7 @@
 
 Run in a container that has the reference sources (it builds them first):
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <reference checkout>   (or PHONOMC_REFERENCE=<checkout>)
 
 Steps: build ``oracle/_ref`` with ``oracle/ref/Makefile`` (the reference's own
 C++ compiled unchanged, HDF5 readers stubbed), write the seeded synthetic
@@ -167,6 +167,7 @@ def full_runs(mpath: str, tmp: str) -> dict:
         out["T_mean"].append(late[:, 2:52].mean(axis=0).tolist())
         out["flux_mean"].append(float(late[:, 52].mean()))
         out["kappa_eff_mean"].append(float(late[:, 54].mean()))
+        out.setdefault("kappa_fit_mean", []).append(float(late[:, 53].mean()))
         out["particles_mean"].append(float(late[:, 55].mean()))
         out.setdefault("balance_residual_total", []).append(res["balance_residual_total"][-1])
     return out
@@ -284,6 +285,7 @@ def full_runs_bilayer(pmats: str, tmp: str) -> dict:
         out.setdefault("T_mean", []).append(late[:, 2:2 + nc].mean(axis=0).tolist())
         out.setdefault("flux_mean", []).append(float(late[:, 2 + nc].mean()))
         out.setdefault("kappa_eff_mean", []).append(float(late[:, 4 + nc].mean()))
+        out.setdefault("kappa_fit_mean", []).append(float(late[:, 3 + nc].mean()))
         out.setdefault("particles_mean", []).append(float(late[:, 5 + nc].mean()))
         out.setdefault("interface_events", []).append(res["interface_events"])
         out.setdefault("interface_transmitted", []).append(res["interface_transmitted"])
@@ -320,7 +322,88 @@ def full_runs_ncallaway(mpath: str, tmp: str) -> dict:
         out.setdefault("T_mean", []).append(late[:, 2:52].mean(axis=0).tolist())
         out.setdefault("flux_mean", []).append(float(late[:, 52].mean()))
         out.setdefault("kappa_eff_mean", []).append(float(late[:, 54].mean()))
+        out.setdefault("kappa_fit_mean", []).append(float(late[:, 53].mean()))
         out.setdefault("lifetime_residual_total", []).append(res["lifetime_residual_total"])
+        out.setdefault("balance_residual_total", []).append(res["balance_residual_total"][-1])
+    return out
+
+
+# Full reference runs of the in-plane periodic-gradient film
+# (phonomc_gb300.workloads.inplane_gradient at 2e4 carriers: 100 nm film,
+# rough 1 nm z walls, G = 1e7 K/m along x, 100 z-cells, linearized RTA at
+# 300 K, dt = 0.5 ps, 2000 steps): per seed the late-time (steps 1001-2000)
+# cell temperatures, heat flux and kappa = -q/G, kappa over every window of
+# 100 steps (the approach to steady state), and the energy closure.
+GRAD_SEEDS = 16
+GRAD_PARTICLES = 20000
+GRAD_STEPS = 2000
+GRAD_CELLS = 100
+GRAD_WINDOW = 100
+INPLANE_TOML = """[geometry]
+model = "box"
+sizes = [100, 100, 100]
+
+[simulation]
+particle_count = {particles}
+time_step = 0.5
+iterations = {steps}
+random_seed = {seed}
+compute_kappa = true
+transport_axis = "x"
+initial_temperature = 300
+background_temperature = 300
+lifetime_temperature = 300
+grid_xyz = [1, 1, {cells}]
+convergence_write_interval = 1
+
+[driving]
+temperature_gradient = 1.0e7
+
+[boundary]
+boundary_position = [
+  [-0.01,0,0,0.01,1,1], [0.99,0,0,1.01,1,1],
+  [0,-0.01,0,1,0.01,1], [0,0.99,0,1,1.01,1],
+  [0,0,-0.01,1,1,0.01], [0,0,0.99,1,1,1.01]
+]
+boundary_conditions = ["P","P","P","P","R","R"]
+boundary_values = [0,0,0,0,1,1]
+periodic_pair = [
+  [-0.01,0,0,0.01,1,1], [0.99,0,0,1.01,1,1],
+  [0,-0.01,0,1,0.01,1], [0,0.99,0,1,1.01,1]
+]
+
+[io]
+material_folder = "unused"
+output_folder = "{out}"
+"""
+
+
+def full_runs_inplane(mpath: str, tmp: str) -> dict:
+    import numpy as np
+    nc = GRAD_CELLS
+    out = {"seeds": [], "particles": GRAD_PARTICLES, "steps": GRAD_STEPS, "cells": nc, "gradient": 1.0e7,
+           "average_from_step": GRAD_STEPS // 2 + 1, "window": GRAD_WINDOW}
+    for k in range(GRAD_SEEDS):
+        seed = 101 + k
+        folder = os.path.join(tmp, f"grad{seed}")
+        os.makedirs(folder, exist_ok=True)
+        toml = os.path.join(folder, "c2.toml")
+        with open(toml, "w") as f:
+            f.write(INPLANE_TOML.format(particles=GRAD_PARTICLES, steps=GRAD_STEPS, seed=seed, cells=nc, out=folder))
+        res = json.loads(subprocess.run([HARNESS, "run", mpath, toml, str(GRAD_STEPS)], check=True,
+                                        capture_output=True, text=True).stdout)
+        rows = np.asarray(res["convergence"])
+        rows = rows[rows[:, 0] >= 1]
+        assert rows.shape[0] == GRAD_STEPS, rows.shape
+        late = rows[rows[:, 0] >= out["average_from_step"]]
+        kappa = rows[:, 4 + nc]
+        out["seeds"].append(seed)
+        out.setdefault("T_mean", []).append(late[:, 2:2 + nc].mean(axis=0).tolist())
+        out.setdefault("flux_mean", []).append(float(late[:, 2 + nc].mean()))
+        out.setdefault("kappa_eff_mean", []).append(float(late[:, 4 + nc].mean()))
+        out.setdefault("kappa_fit_mean", []).append(float(late[:, 3 + nc].mean()))
+        out.setdefault("kappa_windows", []).append(kappa.reshape(-1, GRAD_WINDOW).mean(axis=1).tolist())
+        out.setdefault("gradient_energy_total", []).append(res["gradient_energy_total"])
         out.setdefault("balance_residual_total", []).append(res["balance_residual_total"][-1])
     return out
 
@@ -354,9 +437,12 @@ def build(ref: str) -> None:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("PHONOMC_REFERENCE"),
+                    help="the reference checkout (default: $PHONOMC_REFERENCE)")
     ap.add_argument("--only", nargs="*")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("give --ref or set PHONOMC_REFERENCE to the reference checkout")
     build(args.ref)
     tmp = os.path.join(ROOT, "oracle", "_ref")
     mpath = os.path.join(tmp, "m8.pmat")
@@ -379,6 +465,14 @@ def main() -> None:
         with gzip.open(os.path.join(HERE, "fullrun_cross_plane.json.gz"), "wt") as f:
             json.dump(data, f)
         print("fullrun_cross_plane ok")
+    if not args.only or "fullrun_inplane_gradient" in args.only:
+        m16s = os.path.join(tmp, "m16.pmat")
+        synthetic.write_pmat(m16s, synthetic.make_material(mesh=16))
+        data = full_runs_inplane(m16s, os.path.join(tmp, "fullrun_inplane"))
+        data["_harness_args"] = ["run", "{m16}", "<in-plane gradient toml>", str(GRAD_STEPS)]
+        with gzip.open(os.path.join(HERE, "fullrun_inplane_gradient.json.gz"), "wt") as f:
+            json.dump(data, f)
+        print("fullrun_inplane_gradient ok")
     if not args.only or "fullrun_bilayer" in args.only:
         cs = os.path.join(tmp, "m8cs.pmat")
         synthetic.write_pmat(cs, synthetic.make_material(mesh=8, freq_scale=0.7, vel_scale=0.75, callaway=True))

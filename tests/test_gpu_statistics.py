@@ -4,9 +4,11 @@ The reference solver (oracle/_ref, its own C++) ran each configuration for 16
 seeds (tests/golden/fullrun_*.json.gz, made by tests/golden/make_golden.py).
 The device runs the same configuration for 16 other seeds through the C ABI;
 the late-time observables must agree within the combined standard error of the
-two 16-seed means: |z| < 3.5 for the scalar observables, and for the 50 cell
-temperatures of the film |z| < 4.5 with mean z^2 below 2.5. Energy bookkeeping
-closes to round-off on the device.
+two 16-seed means: |z| < 3 for the scalar observables (heat flux, kappa_eff,
+kappa_int, interface transmission), and for the cell temperatures |z| < 4.5
+with mean z^2 below 2.5 (over 50 or 100 cells at once one cell in 370 exceeds
+3 sigma under agreement, so the mean of z^2 carries the per-cell test). Energy
+bookkeeping closes to round-off on the device.
 """
 
 import numpy as np
@@ -34,12 +36,12 @@ def gpu():
 def test_cross_plane_film_statistics(gpu, precision):
     g = golden("fullrun_cross_plane")
     m = abi.Material(gpu, "phmc_", synthetic.make_material(mesh=16), 0.1, False, False)
-    T_mean, flux, kappa, resid = [], [], [], []
+    T_mean, flux, kappa, kfit, resid = [], [], [], [], []
     for k in range(len(g["seeds"])):
         cfg = workloads.scaled(workloads.cross_plane_film(precision=precision), g["particles"],
                                random_seed=9001 + k, convergence_write_interval=1)
         s = abi.Solver(gpu, "phmc_", cfg, [m])
-        T_acc, f_acc, k_acc = [], [], []
+        T_acc, f_acc, k_acc, i_acc = [], [], [], []
         for step in range(1, g["steps"] + 1):
             s.run(1)
             if step >= g["average_from_step"]:
@@ -47,17 +49,21 @@ def test_cross_plane_film_statistics(gpu, precision):
                 T_acc.append(s.cells()[0])
                 f_acc.append(st["average_heat_flux_along_axis"])
                 k_acc.append(st["kappa_endpoints"])
+                i_acc.append(st["kappa_fit"])
         st = s.stats()
         T_mean.append(np.mean(T_acc, axis=0))
         flux.append(np.mean(f_acc))
         kappa.append(np.mean(k_acc))
+        kfit.append(np.mean(i_acc))
         resid.append(abs(st["total_energy_balance_residual_ev"]))
         s.close()
     z = _z(T_mean, g["T_mean"])
     assert np.all(np.abs(z) < 4.5), z
     assert np.mean(z * z) < 2.5, np.mean(z * z)
-    assert abs(_z(np.asarray(flux)[:, None], np.asarray(g["flux_mean"])[:, None])[0]) < 3.5
-    assert abs(_z(np.asarray(kappa)[:, None], np.asarray(g["kappa_eff_mean"])[:, None])[0]) < 3.5
+    assert abs(_z(np.asarray(flux)[:, None], np.asarray(g["flux_mean"])[:, None])[0]) < 3.0
+    assert abs(_z(np.asarray(kappa)[:, None], np.asarray(g["kappa_eff_mean"])[:, None])[0]) < 3.0
+    # kappa_int: the linear-fit conductivity (src/solver/Observables.cpp:113-144)
+    assert abs(_z(np.asarray(kfit)[:, None], np.asarray(g["kappa_fit_mean"])[:, None])[0]) < 3.0
     assert max(resid) < 1e-6
 
 
@@ -91,7 +97,7 @@ def test_finfet_statistics(gpu, tmp_path):
         s.close()
     for key in ("fin", "top", "bottom", "energy", "absorbed_per_step"):
         z = _z(np.asarray(runs[key])[:, None], np.asarray(g[key])[:, None])[0]
-        assert abs(z) < 3.5, (key, z, np.mean(runs[key]), np.mean(g[key]))
+        assert abs(z) < 3.0, (key, z, np.mean(runs[key]), np.mean(g[key]))
     # the prescribed source energy is the same; the reference runs deposited all of it
     assert np.allclose(runs["source_total_end"], g["source_total_end"], rtol=1e-9), (
         runs["source_total_end"], g["source_total_end"])
@@ -103,29 +109,36 @@ def test_bilayer_statistics(gpu, precision):
     """Callaway bilayer with a DMM interface (tests/golden/fullrun_bilayer)."""
     g = golden("fullrun_bilayer")
     mats = [abi.Material(gpu, "phmc_", d, 0.1, True, True) for d in workloads.bilayer_materials(8)]
-    T_mean, flux, trans, resid = [], [], [], []
+    T_mean, flux, kappa, kfit, trans, resid = [], [], [], [], [], []
     for k in range(len(g["seeds"])):
         cfg = workloads.scaled(workloads.bilayer_callaway(precision=precision), g["particles"], random_seed=9101 + k,
                                grid=(1, 1, g["cells"]), convergence_write_interval=1)
         s = abi.Solver(gpu, "phmc_", cfg, mats)
-        T_acc, f_acc = [], []
+        T_acc, f_acc, k_acc, i_acc = [], [], [], []
         for step in range(1, g["steps"] + 1):
             s.run(1)
             if step >= g["average_from_step"]:
+                st = s.stats()
                 T_acc.append(s.cells()[0])
-                f_acc.append(s.stats()["average_heat_flux_along_axis"])
+                f_acc.append(st["average_heat_flux_along_axis"])
+                k_acc.append(st["kappa_endpoints"])
+                i_acc.append(st["kappa_fit"])
         st = s.stats()
         T_mean.append(np.mean(T_acc, axis=0))
         flux.append(np.mean(f_acc))
+        kappa.append(np.mean(k_acc))
+        kfit.append(np.mean(i_acc))
         trans.append(st["interface_transmitted"] / max(1, st["interface_events"]))
         resid.append(abs(st["total_energy_balance_residual_ev"]))
         s.close()
     z = _z(T_mean, g["T_mean"])
     assert np.all(np.abs(z) < 4.5), z
     assert np.mean(z * z) < 2.5, np.mean(z * z)
-    assert abs(_z(np.asarray(flux)[:, None], np.asarray(g["flux_mean"])[:, None])[0]) < 3.5
+    assert abs(_z(np.asarray(flux)[:, None], np.asarray(g["flux_mean"])[:, None])[0]) < 3.0
+    assert abs(_z(np.asarray(kappa)[:, None], np.asarray(g["kappa_eff_mean"])[:, None])[0]) < 3.0
+    assert abs(_z(np.asarray(kfit)[:, None], np.asarray(g["kappa_fit_mean"])[:, None])[0]) < 3.0
     tr_ref = np.array(g["interface_transmitted"]) / np.array(g["interface_events"])
-    assert abs(_z(np.asarray(trans)[:, None], tr_ref[:, None])[0]) < 3.5
+    assert abs(_z(np.asarray(trans)[:, None], tr_ref[:, None])[0]) < 3.0
     assert max(resid) < 1e-6
 
 
@@ -136,13 +149,13 @@ def test_nonlinear_callaway_statistics(gpu, precision):
     kappa_eff against 16 reference runs."""
     g = golden("fullrun_ncallaway")
     m = abi.Material(gpu, "phmc_", synthetic.make_material(mesh=8, callaway=True), 0.1, True, True)
-    T_mean, flux, kappa, resid = [], [], [], []
+    T_mean, flux, kappa, kfit, resid = [], [], [], [], []
     for k in range(len(g["seeds"])):
         cfg = workloads.scaled(workloads.cross_plane_film(precision=precision), g["particles"], random_seed=9201 + k,
                                convergence_write_interval=1, collision_model="callaway",
                                callaway_formulation="nonlinear")
         s = abi.Solver(gpu, "phmc_", cfg, [m])
-        T_acc, f_acc, k_acc = [], [], []
+        T_acc, f_acc, k_acc, i_acc = [], [], [], []
         for step in range(1, g["steps"] + 1):
             s.run(1)
             if step >= g["average_from_step"]:
@@ -150,16 +163,87 @@ def test_nonlinear_callaway_statistics(gpu, precision):
                 T_acc.append(s.cells()[0])
                 f_acc.append(st["average_heat_flux_along_axis"])
                 k_acc.append(st["kappa_endpoints"])
+                i_acc.append(st["kappa_fit"])
         st = s.stats()
         T_mean.append(np.mean(T_acc, axis=0))
         flux.append(np.mean(f_acc))
         kappa.append(np.mean(k_acc))
+        kfit.append(np.mean(i_acc))
         resid.append(abs(st["total_energy_balance_residual_ev"]))
         s.close()
     z = _z(T_mean, g["T_mean"])
     bad = np.flatnonzero(~(np.abs(z) < 4.5))
     assert bad.size == 0, (bad, z[bad], np.mean(T_mean, axis=0)[bad], np.mean(g["T_mean"], axis=0)[bad])
     assert np.mean(z * z) < 2.5, np.mean(z * z)
-    assert abs(_z(np.asarray(flux)[:, None], np.asarray(g["flux_mean"])[:, None])[0]) < 3.5
-    assert abs(_z(np.asarray(kappa)[:, None], np.asarray(g["kappa_eff_mean"])[:, None])[0]) < 3.5
+    assert abs(_z(np.asarray(flux)[:, None], np.asarray(g["flux_mean"])[:, None])[0]) < 3.0
+    assert abs(_z(np.asarray(kappa)[:, None], np.asarray(g["kappa_eff_mean"])[:, None])[0]) < 3.0
+    assert abs(_z(np.asarray(kfit)[:, None], np.asarray(g["kappa_fit_mean"])[:, None])[0]) < 3.0
     assert max(resid) < 1e-6
+
+
+def _inplane_runs(gpu, precision, particles, seeds, steps, first, window, cells):
+    """Per seed: late-time (from step `first`) cell temperatures, heat flux,
+    kappa = -q/G and kappa_int, kappa over every `window` steps, energy closure."""
+    m = abi.Material(gpu, "phmc_", synthetic.make_material(mesh=16), 0.1, True, False)
+    out = {"T": [], "flux": [], "kappa": [], "kfit": [], "windows": [], "resid": []}
+    for seed in seeds:
+        cfg = workloads.scaled(workloads.inplane_gradient(precision=precision), particles, random_seed=seed,
+                               grid=(1, 1, cells), convergence_write_interval=1)
+        s = abi.Solver(gpu, "phmc_", cfg, [m])
+        T_acc, f_acc, k_all, i_acc = [], [], [], []
+        for step in range(1, steps + 1):
+            s.run(1)
+            st = s.stats()
+            k_all.append(st["kappa_endpoints"])
+            if step >= first:
+                T_acc.append(s.cells()[0])
+                f_acc.append(st["average_heat_flux_along_axis"])
+                i_acc.append(st["kappa_fit"])
+        st = s.stats()
+        out["T"].append(np.mean(T_acc, axis=0))
+        out["flux"].append(np.mean(f_acc))
+        out["kappa"].append(np.mean(k_all[first - 1:]))
+        out["kfit"].append(np.mean(i_acc))
+        out["windows"].append(np.asarray(k_all).reshape(-1, window).mean(axis=1))
+        out["resid"].append(abs(st["total_energy_balance_residual_ev"]))
+        s.close()
+    return {k: np.asarray(v) for k, v in out.items()}
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_inplane_gradient_statistics(gpu, precision):
+    """The headline film (in-plane periodic gradient G = 1e7 K/m, rough 1 nm
+    walls, linearized RTA, 100 z-cells) at 2e4 carriers over 2,000 steps of
+    0.5 ps, against 16 reference runs (tests/golden/fullrun_inplane_gradient):
+    late-time cell temperatures and heat flux, kappa = -q/G over the late half
+    and over every 100-step window of the approach to steady state
+    (src/solver/Observables.cpp:38-144, kappa_int = 0 under a gradient drive),
+    and energy closure."""
+    g = golden("fullrun_inplane_gradient")
+    r = _inplane_runs(gpu, precision, g["particles"], [9301 + k for k in range(len(g["seeds"]))], g["steps"],
+                      g["average_from_step"], g["window"], g["cells"])
+    z = _z(r["T"], g["T_mean"])
+    assert np.all(np.abs(z) < 4.5), z
+    assert np.mean(z * z) < 2.5, np.mean(z * z)
+    assert abs(_z(r["flux"][:, None], np.asarray(g["flux_mean"])[:, None])[0]) < 3.0
+    zk = _z(r["kappa"][:, None], np.asarray(g["kappa_eff_mean"])[:, None])[0]
+    assert abs(zk) < 3.0, (zk, r["kappa"].mean(), np.mean(g["kappa_eff_mean"]))
+    zw = _z(r["windows"], g["kappa_windows"])
+    assert np.all(np.abs(zw) < 4.0), zw
+    assert np.all(r["kfit"] == 0.0)
+    assert r["resid"].max() < 1e-6
+
+
+def test_inplane_gradient_mixed_kappa_error(gpu):
+    """kappa error of the mixed-precision path against the plain FP64 path on
+    the headline film at 1e6 carriers (4 seeds each, steps 1001-2000 of
+    0.5 ps): the relative difference of the mean kappa = -q/G stays inside
+    0.5 % and inside 3 combined standard errors."""
+    seeds = [9401 + k for k in range(4)]
+    runs = {p: _inplane_runs(gpu, p, 1e6, seeds, 2000, 1001, 100, 100) for p in ("fp64", "mixed")}
+    kf, km = runs["fp64"]["kappa"], runs["mixed"]["kappa"]
+    rel = abs(km.mean() - kf.mean()) / abs(kf.mean())
+    assert rel < 5e-3, (rel, km, kf)
+    assert abs(_z(km[:, None], kf[:, None])[0]) < 3.0, (km, kf)
+    for p in runs:
+        assert runs[p]["resid"].max() < 1e-6

@@ -3,8 +3,13 @@
 The reference solver (oracle/_ref, its own C++) ran the scaled cross-plane film
 for 16 seeds (tests/golden/fullrun_cross_plane.json.gz). The oracle runs the
 same configuration for 16 other seeds; the late-time cell temperatures, heat
-flux and kappa_eff must agree within the combined standard error (|z| < 4.5 for
-every one of the 50 cells, mean z^2 close to 1, |z| < 3.5 for flux and kappa).
+flux, kappa_eff and kappa_int must agree within the combined standard error
+(|z| < 4.5 for every one of the 50 cells with mean z^2 below 2.5, |z| < 3 for
+the film's scalar observables). The per-cell bound is looser because it is
+taken over 50 or 100 cells at once: under agreement one cell in 370 exceeds
+3 sigma, so the mean of z^2 carries the per-cell test. The same holds for the
+in-plane gradient film (tests/golden/fullrun_inplane_gradient.json.gz) and the
+bilayer.
 """
 
 import multiprocessing as mp
@@ -23,7 +28,7 @@ def _oracle_run(seed):
                            convergence_write_interval=1)
     m = abi.Material(lib, "orc_", synthetic.make_material(mesh=16), 0.1, False, False)
     s = abi.Solver(lib, "orc_", cfg, [m])
-    T_acc, flux, kappa = [], [], []
+    T_acc, flux, kappa, kfit = [], [], [], []
     for step in range(1, g["steps"] + 1):
         s.run(1)
         if step >= g["average_from_step"]:
@@ -32,8 +37,10 @@ def _oracle_run(seed):
             T_acc.append(T)
             flux.append(st["average_heat_flux_along_axis"])
             kappa.append(st["kappa_endpoints"])
+            kfit.append(st["kappa_fit"])
     st = s.stats()
-    return np.mean(T_acc, axis=0), float(np.mean(flux)), float(np.mean(kappa)), st["total_energy_balance_residual_ev"]
+    return (np.mean(T_acc, axis=0), float(np.mean(flux)), float(np.mean(kappa)),
+            st["total_energy_balance_residual_ev"], float(np.mean(kfit)))
 
 
 def _z(a, b):
@@ -54,8 +61,11 @@ def test_oracle_matches_reference_statistics():
     assert np.mean(z * z) < 2.5, np.mean(z * z)
     zf = _z(np.array([r[1] for r in res])[:, None], np.array(g["flux_mean"])[:, None])[0]
     zk = _z(np.array([r[2] for r in res])[:, None], np.array(g["kappa_eff_mean"])[:, None])[0]
-    assert abs(zf) < 3.5, zf
-    assert abs(zk) < 3.5, zk
+    # kappa_int: the linear-fit conductivity (src/solver/Observables.cpp:113-144)
+    zi = _z(np.array([r[4] for r in res])[:, None], np.array(g["kappa_fit_mean"])[:, None])[0]
+    assert abs(zf) < 3.0, zf
+    assert abs(zk) < 3.0, zk
+    assert abs(zi) < 3.0, zi
     # energy bookkeeping closes to round-off in both (eV, total over the run)
     assert max(abs(r[3]) for r in res) < 1e-6
     assert max(abs(x) for x in g["balance_residual_total"]) < 1e-6
@@ -96,3 +106,51 @@ def test_oracle_matches_reference_bilayer_statistics():
     tr_ref = np.array(g["interface_transmitted"]) / np.array(g["interface_events"])
     assert abs(_z(np.array([r[2] for r in res])[:, None], tr_ref[:, None])[0]) < 3.5
     assert max(abs(r[3]) for r in res) < 1e-6
+
+
+def _oracle_inplane(seed):
+    import oracle
+    from phonomc_gb300 import abi, synthetic, workloads
+    lib = oracle.load()
+    g = golden("fullrun_inplane_gradient")
+    cfg = workloads.scaled(workloads.inplane_gradient(), g["particles"], random_seed=seed, grid=(1, 1, g["cells"]),
+                           convergence_write_interval=1)
+    m = abi.Material(lib, "orc_", synthetic.make_material(mesh=16), 0.1, True, False)
+    s = abi.Solver(lib, "orc_", cfg, [m])
+    T, flux, kappa = [], [], []
+    for step in range(1, g["steps"] + 1):
+        s.run(1)
+        st = s.stats()
+        kappa.append(st["kappa_endpoints"])
+        if step >= g["average_from_step"]:
+            T.append(s.cells()[0])
+            flux.append(st["average_heat_flux_along_axis"])
+    st = s.stats()
+    return (np.mean(T, axis=0), float(np.mean(flux)), np.asarray(kappa).reshape(-1, g["window"]).mean(axis=1),
+            st["kappa_fit"], st["total_energy_balance_residual_ev"])
+
+
+def test_oracle_matches_reference_inplane_gradient_statistics():
+    """In-plane periodic-gradient film (rough walls, G = 1e7 K/m, linearized
+    RTA): the reference's 16 runs of 2,000 steps against 16 oracle runs --
+    late-time cell temperatures, heat flux, kappa = -q/G over the late half and
+    over every 100-step window of the approach to steady state (|z| < 3 for
+    the late-time scalars), kappa_int = 0 as the reference reports it under a
+    gradient drive, and energy closure."""
+    g = golden("fullrun_inplane_gradient")
+    with mp.get_context("spawn").Pool(8) as pool:
+        res = pool.map(_oracle_inplane, [5001 + k for k in range(len(g["seeds"]))])
+    z = _z(np.array([r[0] for r in res]), np.array(g["T_mean"]))
+    assert np.all(np.abs(z) < 4.5), z
+    assert np.mean(z * z) < 2.5, np.mean(z * z)
+    assert abs(_z(np.array([r[1] for r in res])[:, None], np.array(g["flux_mean"])[:, None])[0]) < 3.0
+    kw = np.array([r[2] for r in res])
+    zk = _z(kw, np.array(g["kappa_windows"]))
+    assert np.all(np.abs(zk) < 4.0), zk
+    late = kw.shape[1] // 2
+    zl = _z(kw[:, late:].mean(axis=1)[:, None], np.array(g["kappa_eff_mean"])[:, None])[0]
+    assert abs(zl) < 3.0, (zl, kw[:, late:].mean(), np.mean(g["kappa_eff_mean"]))
+    assert all(r[3] == 0.0 for r in res) and all(k == 0.0 for k in g["kappa_fit_mean"])
+    assert max(abs(r[4]) for r in res) < 1e-6
+    assert max(abs(x) for x in g["balance_residual_total"]) < 1e-6
+
