@@ -249,9 +249,20 @@ def run_reference(args):
 
 
 def _time_arm(lib, abi, cfg, materials, steps, warmup):
+    """Warm-up, then `steps` timed steps. When the solver sorts its carriers
+    every K steps, the warm-up is extended so that the timed window starts on
+    a sort step: the window holds ceil(steps / K) sorts, at least the share
+    of a long run."""
     m = [abi.Material(lib, "phmc_", d, 0.1, st, bz) for d, st, bz in materials]
     s = abi.Solver(lib, "phmc_", cfg, m)
-    s.run(warmup)
+    k = C.c_int32()
+    s.check(lib.phmc_solver_sort_interval(s.h, C.byref(k)))
+    K = int(k.value)
+    profiled = max(1, min(steps, 3))  # eager steps timed_run spends on the carrier-pass events
+    extra = (K - (warmup + profiled) % K) % K if K > 0 else 0
+    s.run(warmup + extra)
+    first = warmup + extra + profiled
+    sorts = sum(1 for t in range(first, first + steps) if K > 0 and t % K == 0)
     tot, kern, launches, n0, n1 = C.c_double(), C.c_double(), C.c_int64(), C.c_int64(), C.c_int64()
     with ClockSampler() as clk:
         s.check(lib.phmc_solver_timed_run(s.h, steps, C.byref(tot), C.byref(kern), C.byref(launches), C.byref(n0),
@@ -259,27 +270,53 @@ def _time_arm(lib, abi, cfg, materials, steps, warmup):
     n0, n1 = n0.value, n1.value
     return {"solver": s, "material": m, "ms": tot.value, "kernel_ms_per_launch": kern.value,
             "launches": int(launches.value), "carrier_steps": 0.5 * (n0 + n1) * steps, "carriers": n0,
-            "clocks": clk.summary()}
+            "clocks": clk.summary(), "sort_interval": K, "sorts_timed": sorts}
+
+
+def kappa_window(s, first, last, every=10):
+    """Mean of kappa = -q/G over the flux passes of steps first..last (every
+    `every` steps; the solver's convergence interval), continuing the run."""
+    cur = s.stats()["current_timestep"]
+    start = max(cur, first - 1)
+    start += (-start) % every
+    if start > cur:
+        s.run(start - cur)
+    vals = []
+    step = start
+    while step + every <= last:
+        s.run(every)
+        step += every
+        if step >= first:
+            vals.append(s.stats()["kappa_endpoints"])
+    return float(np.mean(vals)), len(vals)
+
+
+def measure_batch(lib, precision, steps, warmup, plain=True):
+    """512 independent cross-plane films of log-uniform thickness advancing
+    together (phmc_batch_*): whole-batch carrier-steps/s, `precision` and,
+    unless plain is False, the plain FP64 arm."""
+    from phonomc_gb300 import abi, synthetic, workloads
+    m = abi.Material(lib, "phmc_", synthetic.make_material(mesh=16), 0.1, False, False)
+    out = {}
+    for prec in ([precision, "fp64"] if plain and precision != "fp64" else [precision]):
+        films = workloads.batched_films(precision=prec)
+        b = abi.Batch(lib, films, [m])
+        b.run(warmup)
+        n = steps if prec == precision else max(3, steps // 2)
+        with ClockSampler() as clk:
+            ms, cs, launches = b.timed_run(n)
+        out[prec] = {"value": cs / (ms * 1e-3), "ms_per_step": ms / n, "launches": launches,
+                     "clocks": clk.summary(), "carriers": sum(c["particle_count"] for c in films), "steps": n}
+        b.close()
+    return out
 
 
 def run_batch(args):
     """512 independent cross-plane films of log-uniform thickness advancing
     together (phmc_batch_*): whole-batch carrier-steps/s, mixed and plain."""
     import phonomc_gb300
-    from phonomc_gb300 import abi, synthetic, workloads
     lib = phonomc_gb300.lib()
-    m = abi.Material(lib, "phmc_", synthetic.make_material(mesh=16), 0.1, False, False)
-    out = {}
-    for prec in ([args.precision] if args.no_plain else [args.precision, "fp64"]):
-        films = workloads.batched_films(precision=prec)
-        b = abi.Batch(lib, films, [m])
-        b.run(args.warmup)
-        steps = args.steps if prec == args.precision else max(3, args.steps // 4)
-        with ClockSampler() as clk:
-            ms, cs, launches = b.timed_run(steps)
-        out[prec] = {"value": cs / (ms * 1e-3), "ms_per_step": ms / steps, "launches": launches,
-                     "clocks": clk.summary(), "carriers": sum(c["particle_count"] for c in films), "steps": steps}
-        b.close()
+    out = measure_batch(lib, args.precision, args.steps, args.warmup, plain=not args.no_plain)
     main = out[args.precision]
     line = {
         "metric": METRIC, "value": main["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
@@ -313,9 +350,20 @@ def run_ours(args):
     main_arm = _time_arm(lib, abi, workload_config(args.workload, args.particles, args.precision, seed), materials,
                          args.steps, args.warmup)
     plain = None
+    kappa = None
     if args.precision == "mixed" and not args.no_plain:
         plain = _time_arm(lib, abi, workload_config(args.workload, args.particles, "fp64", seed), materials,
                           max(3, args.steps // 4), args.warmup)
+        if args.kappa_steps > 0 and args.workload == "inplane_gradient":
+            # kappa = -q/G of both arms (same seed, same draws) over the late half
+            # of a kappa_steps run, outside the timed regions
+            first = args.kappa_steps // 2 + 1
+            km, nm = kappa_window(main_arm["solver"], first, args.kappa_steps)
+            kp, npl = kappa_window(plain["solver"], first, args.kappa_steps)
+            kappa = {"window_steps": [first, args.kappa_steps], "samples": min(nm, npl), "mixed": km, "fp64": kp,
+                     "rel_err": abs(km - kp) / abs(kp), "bar": 0.005,
+                     "unit": "W/(m K)", "note": "kappa = -q/G (src/solver/Observables.cpp:75-80), mean over flux "
+                                                 "passes every 10 steps; both arms from the same seed"}
         plain["solver"].close()
     ms, carrier_steps = main_arm["ms"], main_arm["carrier_steps"]
     if world > 1:
@@ -384,13 +432,29 @@ def run_ours(args):
                 "h2d_bytes_per_step": int(n * (4 * 8 + 4)), "d2h_bytes_per_step": int(Tout.size * 8)},
         "clocks": main_arm["clocks"],
     }
+    line["config"]["carrier_sort"] = {"interval_steps": main_arm["sort_interval"],
+                                      "sorts_in_timed_steps": main_arm["sorts_timed"]}
     if plain is not None:
         pv = plain["carrier_steps"] / (plain["ms"] * 1e-3)
         pk = plain["kernel_ms_per_launch"]
         line["plain_fp64"] = {"value": pv, "unit": UNIT, "ms_per_step": plain["ms"] / max(3, args.steps // 4),
                               "mixed_over_plain": value / pv,
                               "roofline_frac": 76 * plain["carriers"] / (pk * 1e-3) / 1e9 / peak,
+                              "kernel_ms_per_launch": pk, "sorts_in_timed_steps": plain["sorts_timed"],
                               "clocks": plain["clocks"]}
+    if kappa is not None:
+        line["kappa"] = kappa
+    if not args.no_batch and world == 1:
+        b = measure_batch(lib, args.precision, args.steps, args.warmup, plain=not args.no_plain)
+        bm = b[args.precision]
+        line["batched"] = {"workload": "batched_films", "instances": 512, "carriers": int(bm["carriers"]),
+                           "value": bm["value"], "unit": UNIT, "ms_per_step": bm["ms_per_step"],
+                           "steps": bm["steps"], "gpu_launches": bm["launches"], "clocks": bm["clocks"],
+                           "thickness_nm": "log-uniform 10-2000 (seed 0)", "cells": "10-200 per film"}
+        if "fp64" in b and args.precision != "fp64":
+            line["batched"]["plain_fp64"] = {"value": b["fp64"]["value"], "ms_per_step": b["fp64"]["ms_per_step"],
+                                             "steps": b["fp64"]["steps"], "clocks": b["fp64"]["clocks"]}
+            line["batched"]["mixed_over_plain"] = bm["value"] / b["fp64"]["value"]
     if rank == 0 and not args.no_cpu_baseline:
         cp, cstep = (50000, 4) if args.workload == "finfet_mesh" else (200000, 10)
         cb, info = cpu_baseline(args.workload, cp, cstep, 3, 1, 1)
@@ -413,6 +477,9 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-films sub-measurement")
+    ap.add_argument("--kappa-steps", type=int, default=2000,
+                    help="in-plane gradient: steps of the mixed-vs-FP64 kappa comparison (0: skip)")
     args = ap.parse_args()
     if args.particles is None:
         args.particles = {"inplane_gradient": 5e7, "finfet_mesh": 2e7, "nonlinear_callaway_film": 1e7}.get(

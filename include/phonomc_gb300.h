@@ -144,6 +144,16 @@ typedef struct phmc_config {
     const char* material_folder;     /* NULL or a label reported in summary.txt */
     int32_t write_cell_heat_flux;    /* simulation.write_cell_heat_flux: grid_heat_flux.csv rows */
     int32_t callaway_nonlinear;      /* collision.callaway_formulation: 0 linearized, 1 nonlinear */
+    /* Device scheduling (no counterpart in the reference's SimulationConfig;
+     * 0 selects the library's tuned default, phonomc_gb300/csrc/phmc_tuning.h).
+     * The sort permutes carrier slots and so which counter-based draws a
+     * carrier receives (the statistics are unchanged); the others change no
+     * result beyond the order of floating-point tally sums. */
+    int32_t carrier_sort_interval;   /* steps between stable carrier sorts by (mode, cell), (cell, mode)
+                                        for mesh domains; < 0 never */
+    int32_t transport_block;         /* threads per CTA of the carrier pass: 128, 256 or 512 */
+    int32_t transport_blocks_per_sm; /* resident CTAs per SM of the carrier kernels (1..16) */
+    int32_t tally_aggregation;       /* 1: warp-summed bin tallies, < 0: one atomic per carrier */
 } phmc_config;
 
 /* Getters of include/MonteCarloSolver.h:59-101 plus the last step's ledger. */
@@ -216,6 +226,9 @@ int phmc_solver_timed_run(phmc_solver* s, int steps, double* total_ms, double* k
  * 0 launches every kernel of every step from the host. No counterpart in the
  * reference. */
 int phmc_solver_set_graphs(phmc_solver* s, int on);
+/* Steps between the solver's carrier sorts, 0 for never (the configured
+ * carrier_sort_interval or its tuned default). No counterpart in the reference. */
+int phmc_solver_sort_interval(const phmc_solver* s, int* steps);
 /* Page-lock / release caller-owned host buffers used for end-to-end stepping. */
 int phmc_host_register(void* ptr, int64_t bytes);
 int phmc_host_unregister(void* ptr);

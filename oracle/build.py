@@ -14,7 +14,7 @@ SOURCES = [os.path.join(HERE, "phmc_oracle.cpp"),
            os.path.join(ROOT, "phonomc_gb300", "csrc", "phmc_host.cpp"),
            os.path.join(ROOT, "phonomc_gb300", "csrc", "phmc_mesh.cpp")]
 DEPS = SOURCES + [os.path.join(ROOT, "phonomc_gb300", "csrc", f)
-                  for f in ("phmc_host.h", "phmc_pod.h", "phmc_rng.h")] + [
+                  for f in ("phmc_host.h", "phmc_pod.h", "phmc_rng.h", "phmc_tuning.h")] + [
     os.path.join(ROOT, "include", "phonomc_gb300.h")]
 _lock = threading.Lock()
 _lib = None

@@ -1382,9 +1382,38 @@ struct OracleSolver {
         energy.record_source(updates, e);
     }
 
+    // Stable reordering of the carrier slots by (active mode, cell), by (cell,
+    // active mode) in mesh domains, dead slots last -- the device's periodic
+    // carrier sort (resolved_sort_interval). Slots key the counter-based
+    // draws, so the oracle reorders its slots at the same steps.
+    void sort_carriers() {
+        const size_t n = alive.size();
+        const bool cell_major = domain->is_mesh();
+        auto key = [&](size_t i) -> uint64_t {
+            if (!alive[i]) return std::numeric_limits<uint64_t>::max();
+            const uint64_t a = mode[i] & kActiveMask, c = static_cast<uint32_t>(cell[i]);
+            return cell_major ? (c << 32) | a : (a << 32) | c;
+        };
+        std::vector<uint64_t> k(n);
+        for (size_t i = 0; i < n; ++i) k[i] = key(i);
+        std::vector<size_t> perm(n);
+        std::iota(perm.begin(), perm.end(), size_t{0});
+        std::stable_sort(perm.begin(), perm.end(), [&](size_t a, size_t b) { return k[a] < k[b]; });
+        auto apply = [&](auto& v) {
+            if (v.size() != n) return;
+            auto w = v;
+            for (size_t i = 0; i < n; ++i) w[i] = v[perm[i]];
+            v.swap(w);
+        };
+        apply(x), apply(y), apply(z), apply(occ), apply(mode), apply(cell), apply(alive);
+        apply(mirror), apply(hit_t), apply(hit_p), apply(hit_f);
+    }
+
     void run_timestep() {
         if (failed) throw std::runtime_error("Cannot resume a failed timestep; construct a new solver after fixing its cause.");
         failed = true;
+        const int sort_every = resolved_sort_interval(cfg);
+        if (sort_every > 0 && step % sort_every == 0) sort_carriers();
         energy.begin_step();
         step_b = {};
         const double midpoint = elapsed + 0.5 * cfg.time_step;

@@ -153,6 +153,8 @@ class ConfigPOD(C.Structure):
         ("precision", C.c_int32), ("heat_source", C.POINTER(HeatSourcePOD)),
         ("mesh", C.POINTER(MeshDomainPOD)), ("material_folder", C.c_char_p),
         ("write_cell_heat_flux", C.c_int32), ("callaway_nonlinear", C.c_int32),
+        ("carrier_sort_interval", C.c_int32), ("transport_block", C.c_int32),
+        ("transport_blocks_per_sm", C.c_int32), ("tally_aggregation", C.c_int32),
     ]
 
 
@@ -233,6 +235,10 @@ def config_pod(cfg: dict):
     c.compute_kappa = int(cfg.get("compute_kappa", False))
     c.write_cell_heat_flux = int(cfg.get("write_cell_heat_flux", False))
     c.callaway_nonlinear = int(cfg.get("callaway_formulation", "linearized") == "nonlinear")
+    c.carrier_sort_interval = int(cfg.get("carrier_sort_interval", 0))
+    c.transport_block = int(cfg.get("transport_block", 0))
+    c.transport_blocks_per_sm = int(cfg.get("transport_blocks_per_sm", 0))
+    c.tally_aggregation = int(cfg.get("tally_aggregation", 0))
     c.transport_axis = int(cfg.get("transport_axis", -1))
     g = cfg.get("temperature_gradient")
     c.has_temperature_gradient = int(g is not None)
@@ -469,6 +475,7 @@ DEVICE_PROTOS = {
     "solver_append_summary": (C.c_int, [C.c_void_p, C.c_int64]),
     "solver_timed_run": (C.c_int, [C.c_void_p, C.c_int, c_double_p, c_double_p, c_int64_p, c_int64_p, c_int64_p]),
     "solver_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
+    "solver_sort_interval": (C.c_int, [C.c_void_p, c_int32_p]),
     "batch_create": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),
     "batch_size": (C.c_int, [C.c_void_p, c_int32_p]),
     "batch_run": (C.c_int, [C.c_void_p, C.c_int]),

@@ -620,6 +620,10 @@ int phmc_solver_set_graphs(phmc_solver* s, int on) {
     return guard([&] { s->s->set_graphs(on != 0); });
 }
 
+int phmc_solver_sort_interval(const phmc_solver* s, int* steps) {
+    return guard([&] { *steps = s->s->sort_interval(); });
+}
+
 // ---------------------------------------------------------------- batches
 int phmc_batch_create(const phmc_config* cfgs, int n, phmc_material* const* materials, int n_materials,
                       phmc_batch** out) {

@@ -3,6 +3,7 @@
 #include "phmc_host.h"
 
 #include "phmc_rng.h"
+#include "phmc_tuning.h"
 
 #include <algorithm>
 #include <set>
@@ -776,6 +777,12 @@ void EnergyLedger::finish_step(double energy, const BoundaryBalance& b) {
 // ---------------------------------------------------------------- problem
 // ------------------------------------------------------- heat source
 // src/config/ConfigValidation.cpp:196-290 (the rules the carrier loop relies on).
+int resolved_sort_interval(const SimulationConfig& c) {
+    if (c.carrier_sort_interval < 0) return 0;
+    if (c.carrier_sort_interval > 0) return c.carrier_sort_interval;
+    return c.particle_count >= tuning::kSortMinCarriers ? tuning::kSortInterval : 0;
+}
+
 void validate_heat_source_config(const SimulationConfig& c) {
     if (!c.heat_source_enabled) return;
     if (c.heat_source_total_power) {

@@ -81,6 +81,13 @@ struct SimulationConfig {
     std::string output_folder;
     bool write_cell_heat_flux = false; // grid_heat_flux.csv also without a gradient drive
     bool callaway_nonlinear = false;   // collision.callaway_formulation = "nonlinear"
+    // Device scheduling, no counterpart in the reference (0: tuned default,
+    // see phmc_tuning.h): carrier sort interval (< 0 never), threads per CTA
+    // and resident CTAs per SM of the carrier pass, bin-tally aggregation.
+    int carrier_sort_interval = 0;
+    int transport_block = 0;
+    int transport_blocks_per_sm = 0;
+    int tally_aggregation = 0;
     std::string material_folder; // reported in summary.txt; tables enter as arrays
     // Layered materials (include/SimulationConfig.h:93-99): N materials, N-1 planes.
     int material_interface_axis = 0;
@@ -106,6 +113,12 @@ struct SimulationConfig {
 };
 
 void validate_heat_source_config(const SimulationConfig& c);
+// Steps between carrier sorts, 0 for never: the configured interval, else the
+// tuned default for populations of at least tuning::kSortMinCarriers. A sort is
+// a stable reordering of the carrier slots by (active mode, cell) -- by (cell,
+// active mode) in mesh domains -- with dead slots last, at the start of every
+// step whose index (steps completed, 0 included) is a multiple of the interval.
+int resolved_sort_interval(const SimulationConfig& c);
 // Source energy factor (ps) of [begin, end] under the time profile
 // (src/solver/HeatSourceDriving.cpp:12-44).
 double heat_source_time_factor(const SimulationConfig& c, double begin_ps, double end_ps);

@@ -29,6 +29,10 @@ struct LaunchCtx {
     const DevNcl* ncl = nullptr; // host copy, nonlinear Callaway only
     unsigned char* lin_work = nullptr; // linear Callaway: per-CTA mode slices in global memory (null: shared)
     size_t lin_slice = 0;              // bytes per CTA slice of lin_work
+    // carrier pass of box domains (k_transport): threads per CTA, CTAs, warp-summed bin tallies
+    int transport_block = 256;
+    int transport_grid = 1;
+    bool tally_agg = true;
 };
 
 // Independent box instances advanced by one launch per kernel of the step:

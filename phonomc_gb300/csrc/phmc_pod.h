@@ -137,6 +137,10 @@ inline SimulationConfig config_from_pod(const phmc_config& c) {
     if (c.output_folder) s.output_folder = c.output_folder;
     s.write_cell_heat_flux = c.write_cell_heat_flux != 0;
     s.callaway_nonlinear = c.callaway_nonlinear != 0;
+    s.carrier_sort_interval = c.carrier_sort_interval;
+    s.transport_block = c.transport_block;
+    s.transport_blocks_per_sm = c.transport_blocks_per_sm;
+    s.tally_aggregation = c.tally_aggregation;
     if (c.material_folder) s.material_folder = c.material_folder;
     s.material_interface_axis = c.material_interface_axis;
     if (c.n_interfaces > 0 && c.material_interface_positions)

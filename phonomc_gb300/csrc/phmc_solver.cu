@@ -1,5 +1,6 @@
 // DeviceSolver: table upload, HBM allocation and the per-step kernel sequence.
 #include "phmc_kernels.cuh"
+#include "phmc_tuning.h"
 
 #include <algorithm>
 #include <cmath>
@@ -84,6 +85,7 @@ DeviceSolver::DeviceSolver(const SimulationConfig& cfg, const std::vector<const 
     }
     P_ = build_problem(cfg_, *domain_, mats_);
     ncells_ = domain_->grid_count();
+    sort_interval_ = resolved_sort_interval(cfg_);
     const int n0 = P_.initial_particles;
     const int margin = P_.reservoirs.empty() ? 1024 : std::max(65536, n0 / 4);
     allocate_state(n0 + margin);
@@ -586,6 +588,15 @@ LaunchCtx DeviceSolver::ctx() const {
     // batch do not launch idle CTAs
     const long long want = (static_cast<long long>(state_.capacity) + 1023) / 1024;
     x.grid_blocks = static_cast<int>(std::max<long long>(8, std::min<long long>(sm_count_ * 8, want)));
+    // the box carrier pass: tuned threads per CTA and resident CTAs per SM, at
+    // least about four carriers per thread for small populations
+    x.transport_block = cfg_.transport_block > 0 ? cfg_.transport_block : tuning::kTransportBlock;
+    const int per_sm = cfg_.transport_blocks_per_sm > 0 ? std::min(cfg_.transport_blocks_per_sm, 16)
+                                                        : tuning::kTransportBlocksPerSm;
+    const long long want_pass = (static_cast<long long>(state_.capacity) + 4LL * x.transport_block - 1) /
+                                (4LL * x.transport_block);
+    x.transport_grid = static_cast<int>(std::max<long long>(8, std::min<long long>(sm_count_ * per_sm, want_pass)));
+    x.tally_agg = cfg_.tally_aggregation > 0 || (cfg_.tally_aggregation == 0 && tuning::kTallyAggregation > 0);
     x.mesh = domain_->is_mesh();
     x.ncl = P_.callaway_nonlinear ? &ncl_ : nullptr;
     x.lin_work = lin_work_;
@@ -716,8 +727,9 @@ void DeviceSolver::capture_step_graph() {
 }
 
 bool DeviceSolver::fusable() const {
+    // fused batch steps run no carrier sorts: instances that sort step on their own graphs
     return !domain_->is_mesh() && P_.mats.size() == 1 && !P_.linearized && !P_.source.enabled &&
-           !cfg_.temperature_gradient.has_value() && collision_kind() == kCollideRta;
+           !cfg_.temperature_gradient.has_value() && collision_kind() == kCollideRta && sort_interval_ == 0;
 }
 
 int DeviceSolver::carrier_blocks() const { return ctx().grid_blocks; }
@@ -740,9 +752,23 @@ void DeviceSolver::finish_batched_step(long long launches) {
     if (step_ == 1 || step_ % cfg_.convergence_write_interval == 0) flux_pass();
 }
 
+void DeviceSolver::sort_carriers() {
+    if (sort_.capacity != state_.capacity) {
+        void* p = nullptr;
+        PHMC_CUDA(cudaMalloc(&p, SortScratch::bytes_for(state_.capacity)));
+        allocations_.push_back(p);
+        sort_.carve(p, state_.capacity);
+    }
+    int modes = 1;
+    for (const PhononMaterial* m : mats_) modes = std::max(modes, m->active_mode_count());
+    counters_.launches += launch_carrier_sort(ctx(), sort_, ncells_, modes, domain_->is_mesh(), mixed_);
+}
+
 void DeviceSolver::run_timestep() {
     if (failed_) throw std::runtime_error("Cannot resume a failed timestep; construct a new solver after fixing its cause.");
     failed_ = true;
+    // stable carrier sort at the start of every sort_interval_-th step (resolved_sort_interval)
+    if (sort_interval_ > 0 && step_ % sort_interval_ == 0) sort_carriers();
     if (use_graphs_ && !profile_pass_a_) {
         if (!graph_exec_) capture_step_graph();
         PHMC_CUDA(cudaGraphLaunch(graph_exec_, stream_));

@@ -17,6 +17,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <memory>
 #include <string>
 #include <vector>
@@ -24,6 +25,7 @@
 #include "../../include/phonomc_gb300.h"
 #include "phmc_device.cuh"
 #include "phmc_host.h"
+#include "phmc_sort.cuh"
 
 namespace phmc {
 
@@ -176,12 +178,14 @@ public:
                    long long& live_after);
     // Steps are replayed from a CUDA graph of one captured timestep (default on).
     void set_graphs(bool on) { use_graphs_ = on; }
+    // Steps between carrier sorts (0 never).
+    int sort_interval() const { return sort_interval_; }
     double drive_only();
     const Problem& problem() const { return P_; }
     long long launches() const { return counters_.launches; }
     cudaStream_t stream() const { return stream_; }
     // Instances that the fused batch kernels can advance together: box domain,
-    // one material, nonlinear RTA, no heat source and no gradient drive.
+    // one material, nonlinear RTA, no heat source, no gradient drive, no sorts.
     bool fusable() const;
     // device state of this instance, read by the fused batch kernels
     const DevTables* device_tables() const { return d_tables_; }
@@ -210,6 +214,10 @@ private:
     void enqueue_step(bool profile);
     void capture_step_graph();
     void flux_pass();
+    // stable reordering of the carrier slots (phmc_sort.cu), every sort_interval_ steps
+    void sort_carriers();
+    int sort_interval_ = 0;
+    SortScratch sort_{};
     void drain_observations(bool wait);
     void process_observation(Observation& o);
     void update_kappa();

@@ -393,18 +393,66 @@ __global__ void k_mesh_cache_init(const __grid_constant__ DevTables T, CarrierSt
 // ------------------------------------------------------------------ bins
 __device__ __forceinline__ int bin_of(const DevMaterial& M, int ai) { return M.bin ? __ldg(M.bin + ai) : ai; }
 
-__device__ __forceinline__ void bin_carrier(const DevTables& T, const CellArrays& C, DevLedger* L, int slot, int cell,
-                                           uint32_t w, double occ, bool rta) {
+// Bin record of a carrier after the checks of GridStatistics
+// (src/solver/GridStatistics.cpp:95-181): -1, with the error latched, for a cell
+// out of range, of another material, or a non-finite occupation.
+__device__ __forceinline__ long long bin_slot(const DevTables& T, const CellArrays& C, DevLedger* L, int slot, int cell,
+                                              uint32_t w, double occ) {
     const int mid = static_cast<int>(w >> 28);
     const bool finite = (__double2hiint(occ) & 0x7ff00000) != 0x7ff00000;
     if (cell < 0 || cell >= C.ncells || C.cell_material[cell] != mid || !finite) {
         raise_error(L, kErrInvalidStatistics, slot);
-        return;
+        return -1;
     }
-    const size_t h = static_cast<size_t>(cell) * C.hist_modes + bin_of(T.mat[mid], static_cast<int>(w & 0x00FFFFFFu));
-    atomicAdd(&C.bins[h].cnt, 1u);
-    atomicAdd(&C.bins[h].N, occ);
-    if (rta) atomicAdd(C.hM + h, fmax(1.0, occ));
+    return static_cast<long long>(cell) * C.hist_modes + bin_of(T.mat[mid], static_cast<int>(w & 0x00FFFFFFu));
+}
+
+__device__ __forceinline__ void bin_add(const CellArrays& C, long long h, unsigned cnt, double N, double M, bool rta) {
+    atomicAdd(&C.bins[h].cnt, cnt);
+    atomicAdd(&C.bins[h].N, N);
+    if (rta) atomicAdd(C.hM + h, M);
+}
+
+__device__ __forceinline__ void bin_carrier(const DevTables& T, const CellArrays& C, DevLedger* L, int slot, int cell,
+                                           uint32_t w, double occ, bool rta) {
+    const long long h = bin_slot(T, C, L, slot, cell, w, occ);
+    if (h >= 0) bin_add(C, h, 1u, occ, fmax(1.0, occ), rta);
+}
+
+// Bin tallies of one warp (all 32 lanes call; h < 0: nothing from this lane).
+// Runs of equal records in lane order -- the common case once the carriers
+// are sorted by (mode, cell) -- are summed with a segmented shuffle scan and
+// the last lane of each run makes one atomic per field. kAgg false: one
+// atomic per carrier.
+template <bool kAgg, bool kRta>
+__device__ __forceinline__ void bin_warp(const CellArrays& C, long long h, double occ) {
+    if constexpr (!kAgg) {
+        if (h >= 0) bin_add(C, h, 1u, occ, fmax(1.0, occ), kRta);
+    } else {
+        const int lane = threadIdx.x & 31;
+        const long long hp = __shfl_up_sync(0xffffffffu, h, 1);
+        const long long hn = __shfl_down_sync(0xffffffffu, h, 1);
+        const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || hp != h);
+        unsigned cnt = h >= 0 ? 1u : 0u;
+        double N = h >= 0 ? occ : 0.0;
+        double M = h >= 0 ? fmax(1.0, occ) : 0.0;
+        if (heads != 0xffffffffu) { // warp-uniform: some run is longer than one lane
+            const int start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned c2 = __shfl_up_sync(0xffffffffu, cnt, o);
+                const double n2 = __shfl_up_sync(0xffffffffu, N, o);
+                double m2 = 0.0;
+                if (kRta) m2 = __shfl_up_sync(0xffffffffu, M, o);
+                if (lane - o >= start) {
+                    cnt += c2;
+                    N += n2;
+                    if (kRta) M += m2;
+                }
+            }
+        }
+        if (h >= 0 && (lane == 31 || hn != h)) bin_add(C, h, cnt, N, M, kRta);
+    }
 }
 
 // Pending (alpha, beta) of the carrier's bin: collision of the previous step
@@ -687,10 +735,11 @@ __device__ __forceinline__ int settle_layer(const DevTables& T, const CellArrays
 
 // Common end of a carrier's step: store the state; a live carrier takes its
 // new cell and enters the bins.
-template <bool kRta>
-__device__ __forceinline__ void finish_mixed(const DevTables& T, const CarrierState& S, const CellArrays& C,
-                                             DevLedger* L, int i, const Frame& F, float p[3], uint32_t w, double occ,
-                                             bool alive) {
+// Stores the carrier after its flight; returns its bin record (-1: absorbed
+// or invalid) for the caller to tally.
+__device__ __forceinline__ long long finish_mixed(const DevTables& T, const CarrierState& S, const CellArrays& C,
+                                                  DevLedger* L, int i, const Frame& F, float p[3], uint32_t w,
+                                                  double occ, bool alive) {
     const int c = settle_layer(T, C, F, p, static_cast<int>(w >> 28));
     __stcs(S.ox + i, p[0]);
     __stcs(S.oy + i, p[1]);
@@ -699,26 +748,26 @@ __device__ __forceinline__ void finish_mixed(const DevTables& T, const CarrierSt
     __stcs(S.occ + i, occ);
     if (!alive) {
         S.alive[i] = 0;
-        return;
+        return -1;
     }
     __stcs(S.cell + i, c);
-    bin_carrier(T, C, L, i, c, w, occ, kRta);
+    return bin_slot(T, C, L, i, c, w, occ);
 }
 
-constexpr int kTransportThreads = 256;
+constexpr int kTransportThreads = 256; // fused batch kernels and the default of the single-instance pass
+constexpr int kTransportMaxThreads = 512;
 constexpr int kDeferBuffer = 64; // queued wall events per warp before a flush
 
 // The one carrier pass of a timestep: apply the pending update on load, fly,
 // bin. Mixed path: carriers that reach a wall needing table sampling are
 // queued (per-warp shared buffers, one global atomic per 32 entries) and
 // finished by k_deferred.
-template <bool kMixed, bool kRta>
-__device__ __forceinline__ void k_transport_body(const DevTables& T, CarrierState S, CellArrays C, DevLedger* L, int vbx, int vgx) {
-    (void)vbx;
-    (void)vgx;
+// qbuf: kDeferBuffer entries per warp of the block (mixed path).
+template <bool kMixed, bool kRta, bool kAgg>
+__device__ __forceinline__ void k_transport_body(const DevTables& T, CarrierState S, CellArrays C, DevLedger* L, int vbx,
+                                                 int vgx, int4 (*qbuf)[kDeferBuffer]) {
     const uint32_t step = L->step_index; // timesteps completed: the draw counter of this step
     __shared__ BlockLedger bl;
-    __shared__ int4 qbuf[kMixed ? kTransportThreads / 32 : 1][kMixed ? kDeferBuffer : 1];
     block_ledger_init(&bl);
     __syncthreads();
     const int n = L->n_slots;
@@ -730,6 +779,8 @@ __device__ __forceinline__ void k_transport_body(const DevTables& T, CarrierStat
             const int i = base + threadIdx.x;
             bool defer = false;
             int4 entry;
+            long long h = -1;
+            double hocc = 0.0;
             if (i < n && __ldcs(S.alive + i)) {
                 uint32_t w = __ldcs(S.mode + i);
                 const int c0 = __ldcs(S.cell + i);
@@ -750,9 +801,11 @@ __device__ __forceinline__ void k_transport_body(const DevTables& T, CarrierStat
                     defer = true;
                     entry = make_int4(i, __float_as_int(remaining), event, plane);
                 } else {
-                    finish_mixed<kRta>(T, S, C, L, i, F, p, w, occ, end != kFlightAbsorbed);
+                    h = finish_mixed(T, S, C, L, i, F, p, w, occ, end != kFlightAbsorbed);
+                    hocc = occ;
                 }
             }
+            bin_warp<kAgg, kRta>(C, h, hocc);
             const unsigned mask = __ballot_sync(0xffffffffu, defer);
             if (mask) {
                 if (defer) qbuf[warp][queued + __popc(mask & ((1u << lane) - 1u))] = entry;
@@ -785,35 +838,45 @@ __device__ __forceinline__ void k_transport_body(const DevTables& T, CarrierStat
             }
         }
     } else {
-        for (int i = vbx * blockDim.x + threadIdx.x; i < n; i += vgx * blockDim.x) {
-            if (!__ldcs(S.alive + i)) continue;
-            uint32_t w = __ldcs(S.mode + i);
-            const int c0 = __ldcs(S.cell + i);
-            double occ = apply_pending(T, C, c0, w, __ldcs(S.occ + i));
-            double p[3] = {__ldcs(S.x + i), __ldcs(S.y + i), __ldcs(S.z + i)};
-            const bool alive = advance_carrier(T, L, &bl, i, p, w, occ, T.par.dt, kDrawTransport, step);
-            const int c = grid_index(T.dom, p[0], p[1], p[2]);
-            __stcs(S.x + i, p[0]);
-            __stcs(S.y + i, p[1]);
-            __stcs(S.z + i, p[2]);
-            __stcs(S.mode + i, w);
-            __stcs(S.occ + i, occ);
-            if (!alive) {
-                S.alive[i] = 0;
-                continue;
+        // block-uniform trip count so that every lane reaches the warp tally
+        for (int base = vbx * blockDim.x; base < n; base += vgx * blockDim.x) {
+            const int i = base + threadIdx.x;
+            long long h = -1;
+            double occ = 0.0;
+            if (i < n && __ldcs(S.alive + i)) {
+                uint32_t w = __ldcs(S.mode + i);
+                const int c0 = __ldcs(S.cell + i);
+                occ = apply_pending(T, C, c0, w, __ldcs(S.occ + i));
+                double p[3] = {__ldcs(S.x + i), __ldcs(S.y + i), __ldcs(S.z + i)};
+                const bool alive = advance_carrier(T, L, &bl, i, p, w, occ, T.par.dt, kDrawTransport, step);
+                const int c = grid_index(T.dom, p[0], p[1], p[2]);
+                __stcs(S.x + i, p[0]);
+                __stcs(S.y + i, p[1]);
+                __stcs(S.z + i, p[2]);
+                __stcs(S.mode + i, w);
+                __stcs(S.occ + i, occ);
+                if (!alive) {
+                    S.alive[i] = 0;
+                } else {
+                    __stcs(S.cell + i, c);
+                    h = bin_slot(T, C, L, i, c, w, occ);
+                }
             }
-            __stcs(S.cell + i, c);
-            bin_carrier(T, C, L, i, c, w, occ, kRta);
+            bin_warp<kAgg, kRta>(C, h, occ);
         }
     }
     __syncthreads();
     block_ledger_flush(&bl, L);
 }
 
-template <bool kMixed, bool kRta>
-__global__ void __launch_bounds__(kTransportThreads) k_transport(const __grid_constant__ DevTables T, CarrierState S,
-                                                                 CellArrays C, DevLedger* L) {
-    k_transport_body<kMixed, kRta>(T, S, C, L, blockIdx.x, gridDim.x);
+// Block size chosen at launch (128, 256 or 512 threads); the wall-event queue
+// of the mixed path is dynamic shared memory, kDeferBuffer entries per warp.
+template <bool kMixed, bool kRta, bool kAgg>
+__global__ void __launch_bounds__(kTransportMaxThreads) k_transport(const __grid_constant__ DevTables T, CarrierState S,
+                                                                    CellArrays C, DevLedger* L) {
+    extern __shared__ int4 qdyn[];
+    k_transport_body<kMixed, kRta, kAgg>(T, S, C, L, blockIdx.x, gridDim.x,
+                                         reinterpret_cast<int4 (*)[kDeferBuffer]>(qdyn));
 }
 
 // Mesh transport, pass 1 of 2: apply the pending update and drift every
@@ -830,6 +893,8 @@ __global__ void __launch_bounds__(kTransportThreads) k_transport_mesh(const __gr
     for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const int i = base + threadIdx.x;
         bool defer = false;
+        long long h = -1;
+        double hocc = 0.0;
         if (i < n && __ldcs(S.alive + i)) {
             const uint32_t w = __ldcs(S.mode + i);
             const int c0 = __ldcs(S.cell + i);
@@ -848,12 +913,14 @@ __global__ void __launch_bounds__(kTransportThreads) k_transport_mesh(const __gr
                 __stcs(S.z + i, p[2]);
                 __stcs(S.occ + i, occ);
                 __stcs(S.cell + i, c);
-                bin_carrier(T, C, L, i, c, w, occ, kRta);
+                h = bin_slot(T, C, L, i, c, w, occ);
+                hocc = occ;
             } else {
                 __stcs(S.occ + i, occ);
                 defer = true;
             }
         }
+        bin_warp<true, kRta>(C, h, hocc);
         const unsigned mask = __ballot_sync(0xffffffffu, defer);
         if (mask) {
             int at = 0;
@@ -948,7 +1015,8 @@ __device__ __forceinline__ void k_deferred_body(const DevTables& T, CarrierState
             int unused = -1;
             end = advance_mixed<false>(T, L, &bl, i, F, p, w, occ, remaining, event, unused, kDrawTransport, step);
         }
-        finish_mixed<kRta>(T, S, C, L, i, F, p, w, occ, end != kFlightAbsorbed);
+        const long long h = finish_mixed(T, S, C, L, i, F, p, w, occ, end != kFlightAbsorbed);
+        if (h >= 0) bin_add(C, h, 1u, occ, fmax(1.0, occ), kRta);
     }
     __syncthreads();
     block_ledger_flush(&bl, L);
@@ -1397,14 +1465,26 @@ __global__ void k_reset_pending(const DevTables* __restrict__ Tp, CellArrays C, 
 }
 
 // ----------------------------------------------------------- launchers
+template <bool kMixed, bool kRta>
+void launch_transport_pass(const LaunchCtx& x, dim3 g) {
+    const int threads = x.transport_block;
+    const size_t sh = kMixed ? static_cast<size_t>(threads / 32) * kDeferBuffer * sizeof(int4) : 0;
+    if (x.tally_agg) k_transport<kMixed, kRta, true><<<g, threads, sh, x.stream>>>(*x.Th, x.S, x.C, x.L);
+    else k_transport<kMixed, kRta, false><<<g, threads, sh, x.stream>>>(*x.Th, x.S, x.C, x.L);
+}
+
 int launch_transport(const LaunchCtx& x, bool mixed, bool rta) {
+    if (x.transport_block != 128 && x.transport_block != 256 && x.transport_block != 512)
+        throw std::invalid_argument("transport_block must be 128, 256 or 512 threads");
     const dim3 g(x.grid_blocks), b(kTransportThreads);
     if (mixed) {
+        // the carrier pass at the configured block size; the deferred wall events at 256
+        const dim3 gp(x.transport_grid);
         if (rta) {
-            k_transport<true, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+            launch_transport_pass<true, true>(x, gp);
             k_deferred<true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
         } else {
-            k_transport<true, false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+            launch_transport_pass<true, false>(x, gp);
             k_deferred<false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
         }
         return 2;
@@ -1419,8 +1499,8 @@ int launch_transport(const LaunchCtx& x, bool mixed, bool rta) {
         }
         return 2;
     }
-    if (rta) k_transport<false, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
-    else k_transport<false, false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+    if (rta) launch_transport_pass<false, true>(x, dim3(x.transport_grid));
+    else launch_transport_pass<false, false>(x, dim3(x.transport_grid));
     return 1;
 }
 
@@ -1551,13 +1631,15 @@ __device__ __forceinline__ const DevTables& stage_tables(SharedTables& st, const
 template <bool kMixed, bool kRta>
 __global__ void __launch_bounds__(kTransportThreads) kf_transport(const BatchDesc D) {
     __shared__ SharedTables st;
+    __shared__ int4 qbuf[kMixed ? kTransportThreads / 32 : 1][kDeferBuffer];
     if (threadIdx.x == 0) st.owner = -1;
     __syncthreads();
     for (int vb = blockIdx.x; vb < D.total_carrier_blocks; vb += gridDim.x) {
         const int i = batch_find(D.carrier_block, D.n, vb);
         const int b0 = D.carrier_block[i];
         const DevTables& T = stage_tables(st, D, i);
-        k_transport_body<kMixed, kRta>(T, D.states[i], D.cells[i], D.ledgers[i], vb - b0, D.carrier_block[i + 1] - b0);
+        k_transport_body<kMixed, kRta, false>(T, D.states[i], D.cells[i], D.ledgers[i], vb - b0,
+                                              D.carrier_block[i + 1] - b0, qbuf);
         __syncthreads();
     }
 }

@@ -17,6 +17,7 @@ import argparse
 import gzip
 import json
 import os
+import shutil
 import subprocess
 import sys
 
@@ -405,6 +406,7 @@ def full_runs_inplane(mpath: str, tmp: str) -> dict:
         out.setdefault("kappa_windows", []).append(kappa.reshape(-1, GRAD_WINDOW).mean(axis=1).tolist())
         out.setdefault("gradient_energy_total", []).append(res["gradient_energy_total"])
         out.setdefault("balance_residual_total", []).append(res["balance_residual_total"][-1])
+        shutil.rmtree(folder, ignore_errors=True)  # 2,000 rows of 100 cells per seed
     return out
 
 
