@@ -877,14 +877,56 @@ void DeviceSolver::synchronize() {
     check_error();
 }
 
+// Stored position of one carrier slot (FP64 positions, or cell corner plus the
+// FP32 offset in the mixed path) and its cached wall facet (mesh domains, else -1).
+void DeviceSolver::carrier_position(int slot, double p[3], int& facet) {
+    facet = -1;
+    if (mixed_) {
+        int c = 0;
+        float o[3];
+        PHMC_CUDA(cudaMemcpy(&c, state_.cell + slot, sizeof(int), cudaMemcpyDeviceToHost));
+        PHMC_CUDA(cudaMemcpy(&o[0], state_.ox + slot, sizeof(float), cudaMemcpyDeviceToHost));
+        PHMC_CUDA(cudaMemcpy(&o[1], state_.oy + slot, sizeof(float), cudaMemcpyDeviceToHost));
+        PHMC_CUDA(cudaMemcpy(&o[2], state_.oz + slot, sizeof(float), cudaMemcpyDeviceToHost));
+        const DevDomain& D = tables_.dom;
+        const int idx[3] = {c / (D.shape[1] * D.shape[2]), (c / D.shape[2]) % D.shape[1], c % D.shape[2]};
+        for (int a = 0; a < 3; ++a) p[a] = D.lo[a] + idx[a] * D.cell_size[a] + static_cast<double>(o[a]);
+        return;
+    }
+    PHMC_CUDA(cudaMemcpy(&p[0], state_.x + slot, sizeof(double), cudaMemcpyDeviceToHost));
+    PHMC_CUDA(cudaMemcpy(&p[1], state_.y + slot, sizeof(double), cudaMemcpyDeviceToHost));
+    PHMC_CUDA(cudaMemcpy(&p[2], state_.z + slot, sizeof(double), cudaMemcpyDeviceToHost));
+    if (mesh_hit_f_) PHMC_CUDA(cudaMemcpy(&facet, mesh_hit_f_ + slot, sizeof(int), cudaMemcpyDeviceToHost));
+}
+
+// Device errors surface at the next host synchronisation with the text of the
+// reference's exceptions; carrier errors name the slot and its position as
+// src/solver/TransportOperator.cpp:252-284 and :364-402 name the particle.
 void DeviceSolver::check_error() {
     int code = 0, slot = 0;
     PHMC_CUDA(cudaMemcpy(&code, &d_ledger_->error_code, sizeof(int), cudaMemcpyDeviceToHost));
-    if (code) {
-        PHMC_CUDA(cudaMemcpy(&slot, &d_ledger_->error_slot, sizeof(int), cudaMemcpyDeviceToHost));
-        failed_ = true;
-        throw std::runtime_error(std::string(error_message(code)) + " (carrier slot or cell " + std::to_string(slot) + ")");
+    if (!code) return;
+    PHMC_CUDA(cudaMemcpy(&slot, &d_ledger_->error_slot, sizeof(int), cudaMemcpyDeviceToHost));
+    failed_ = true;
+    if ((code == kErrTooManyEvents || code == kErrEscaped || code == kErrIntersection) && slot >= 0 &&
+        slot < state_.capacity) {
+        double p[3];
+        int facet = -1;
+        carrier_position(slot, p, facet);
+        const std::string at = "(" + std::to_string(p[0]) + ", " + std::to_string(p[1]) + ", " +
+                               std::to_string(p[2]) + ")";
+        const std::string cached = facet >= 0 ? ", cached facet=" + std::to_string(facet) : std::string();
+        if (code == kErrTooManyEvents)
+            throw std::runtime_error("Particle " + std::to_string(slot) + " exceeded 64 transport events in one timestep at " +
+                                     at + cached + ". Reduce simulation.time_step or inspect narrow STL features; no "
+                                     "recovery was applied.");
+        if (code == kErrEscaped)
+            throw std::runtime_error("Particle " + std::to_string(slot) + " escaped the domain at " + at + cached +
+                                     ". Refusing to relocate or rethermalize it; inspect the geometry and time step.");
+        throw std::runtime_error("Boundary intersection failed while advancing particles for particle " +
+                                 std::to_string(slot) + " at " + at + ". Check that the STL is closed and manifold.");
     }
+    throw std::runtime_error(std::string(error_message(code)) + " (carrier slot or cell " + std::to_string(slot) + ")");
 }
 
 // Heat flux tally at step 1 and every convergence_write_interval steps. The

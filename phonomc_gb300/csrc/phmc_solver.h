@@ -153,6 +153,7 @@ public:
     void run(int steps);
     void synchronize();
     void check_error();
+    void carrier_position(int slot, double p[3], int& facet);
     void read_stats(phmc_stats& out);
     int cell_count() const { return ncells_; }
     void read_cells(double* T, double* E, double* q3);
