@@ -229,6 +229,12 @@ int phmc_solver_set_graphs(phmc_solver* s, int on);
 /* Steps between the solver's carrier sorts, 0 for never (the configured
  * carrier_sort_interval or its tuned default). No counterpart in the reference. */
 int phmc_solver_sort_interval(const phmc_solver* s, int* steps);
+/* Changes the scheduling fields of the configuration (carrier_sort_interval,
+ * transport_block, transport_blocks_per_sm, tally_aggregation; 0 = tuned
+ * default) between steps, e.g. for a tuning sweep on one population. No
+ * counterpart in the reference. */
+int phmc_solver_set_schedule(phmc_solver* s, int sort_interval, int transport_block, int blocks_per_sm,
+                             int tally_aggregation);
 /* Page-lock / release caller-owned host buffers used for end-to-end stepping. */
 int phmc_host_register(void* ptr, int64_t bytes);
 int phmc_host_unregister(void* ptr);

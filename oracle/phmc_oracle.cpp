@@ -1412,7 +1412,7 @@ struct OracleSolver {
     void run_timestep() {
         if (failed) throw std::runtime_error("Cannot resume a failed timestep; construct a new solver after fixing its cause.");
         failed = true;
-        const int sort_every = resolved_sort_interval(cfg);
+        const int sort_every = resolved_sort_interval(cfg, false); // the plain FP64 state's schedule
         if (sort_every > 0 && step % sort_every == 0) sort_carriers();
         energy.begin_step();
         step_b = {};

@@ -624,6 +624,11 @@ int phmc_solver_sort_interval(const phmc_solver* s, int* steps) {
     return guard([&] { *steps = s->s->sort_interval(); });
 }
 
+int phmc_solver_set_schedule(phmc_solver* s, int sort_interval, int transport_block, int blocks_per_sm,
+                             int tally_aggregation) {
+    return guard([&] { s->s->set_schedule(sort_interval, transport_block, blocks_per_sm, tally_aggregation); });
+}
+
 // ---------------------------------------------------------------- batches
 int phmc_batch_create(const phmc_config* cfgs, int n, phmc_material* const* materials, int n_materials,
                       phmc_batch** out) {

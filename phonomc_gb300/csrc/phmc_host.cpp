@@ -777,10 +777,10 @@ void EnergyLedger::finish_step(double energy, const BoundaryBalance& b) {
 // ---------------------------------------------------------------- problem
 // ------------------------------------------------------- heat source
 // src/config/ConfigValidation.cpp:196-290 (the rules the carrier loop relies on).
-int resolved_sort_interval(const SimulationConfig& c) {
+int resolved_sort_interval(const SimulationConfig& c, bool mixed) {
     if (c.carrier_sort_interval < 0) return 0;
     if (c.carrier_sort_interval > 0) return c.carrier_sort_interval;
-    return c.particle_count >= tuning::kSortMinCarriers ? tuning::kSortInterval : 0;
+    return c.particle_count >= tuning::kSortMinCarriers ? tuning::kSortInterval[mixed ? 1 : 0] : 0;
 }
 
 void validate_heat_source_config(const SimulationConfig& c) {

@@ -114,11 +114,12 @@ struct SimulationConfig {
 
 void validate_heat_source_config(const SimulationConfig& c);
 // Steps between carrier sorts, 0 for never: the configured interval, else the
-// tuned default for populations of at least tuning::kSortMinCarriers. A sort is
+// tuned default of the carrier state (plain FP64 or mixed) for populations of
+// at least tuning::kSortMinCarriers. A sort is
 // a stable reordering of the carrier slots by (active mode, cell) -- by (cell,
 // active mode) in mesh domains -- with dead slots last, at the start of every
 // step whose index (steps completed, 0 included) is a multiple of the interval.
-int resolved_sort_interval(const SimulationConfig& c);
+int resolved_sort_interval(const SimulationConfig& c, bool mixed);
 // Source energy factor (ps) of [begin, end] under the time profile
 // (src/solver/HeatSourceDriving.cpp:12-44).
 double heat_source_time_factor(const SimulationConfig& c, double begin_ps, double end_ps);

@@ -93,6 +93,16 @@ void trace_box_noalloc(const double lo[3], const double hi[3], long long n, cons
     cudaStream_t st = g_stream[dev];
     if (misses) *misses = 0;
     if (n == 0) return;
+    // Once copies are queued, an error must not return while they may still
+    // read or write the caller's (possibly pinned) buffers: drain the stream
+    // first, whatever its status.
+    struct DrainOnThrow {
+        cudaStream_t s;
+        bool armed = true;
+        ~DrainOnThrow() {
+            if (armed) cudaStreamSynchronize(s);
+        }
+    } drain{st};
     DevDomain D{};
     double scale = 1.0;
     for (int a = 0; a < 3; ++a) {
@@ -115,7 +125,9 @@ void trace_box_noalloc(const double lo[3], const double hi[3], long long n, cons
     check(cudaMemcpyAsync(facet, S->facet, static_cast<size_t>(n) * sizeof(int32_t), cudaMemcpyDeviceToHost, st),
           "cudaMemcpyAsync");
     check(cudaMemcpyAsync(&missed, &S->misses, sizeof missed, cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync");
-    check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    const cudaError_t done = cudaStreamSynchronize(st);
+    drain.armed = false;
+    check(done, "cudaStreamSynchronize");
     if (misses) *misses = static_cast<long long>(missed);
 }
 

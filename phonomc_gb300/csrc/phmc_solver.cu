@@ -85,7 +85,7 @@ DeviceSolver::DeviceSolver(const SimulationConfig& cfg, const std::vector<const 
     }
     P_ = build_problem(cfg_, *domain_, mats_);
     ncells_ = domain_->grid_count();
-    sort_interval_ = resolved_sort_interval(cfg_);
+    sort_interval_ = resolved_sort_interval(cfg_, mixed_);
     const int n0 = P_.initial_particles;
     const int margin = P_.reservoirs.empty() ? 1024 : std::max(65536, n0 / 4);
     allocate_state(n0 + margin);
@@ -590,13 +590,14 @@ LaunchCtx DeviceSolver::ctx() const {
     x.grid_blocks = static_cast<int>(std::max<long long>(8, std::min<long long>(sm_count_ * 8, want)));
     // the box carrier pass: tuned threads per CTA and resident CTAs per SM, at
     // least about four carriers per thread for small populations
-    x.transport_block = cfg_.transport_block > 0 ? cfg_.transport_block : tuning::kTransportBlock;
+    const int tk = mixed_ ? 1 : 0;
+    x.transport_block = cfg_.transport_block > 0 ? cfg_.transport_block : tuning::kTransportBlock[tk];
     const int per_sm = cfg_.transport_blocks_per_sm > 0 ? std::min(cfg_.transport_blocks_per_sm, 16)
-                                                        : tuning::kTransportBlocksPerSm;
+                                                        : tuning::kTransportBlocksPerSm[tk];
     const long long want_pass = (static_cast<long long>(state_.capacity) + 4LL * x.transport_block - 1) /
                                 (4LL * x.transport_block);
     x.transport_grid = static_cast<int>(std::max<long long>(8, std::min<long long>(sm_count_ * per_sm, want_pass)));
-    x.tally_agg = cfg_.tally_aggregation > 0 || (cfg_.tally_aggregation == 0 && tuning::kTallyAggregation > 0);
+    x.tally_agg = cfg_.tally_aggregation > 0 || (cfg_.tally_aggregation == 0 && tuning::kTallyAggregation[tk] > 0);
     x.mesh = domain_->is_mesh();
     x.ncl = P_.callaway_nonlinear ? &ncl_ : nullptr;
     x.lin_work = lin_work_;
@@ -750,6 +751,23 @@ void DeviceSolver::finish_batched_step(long long launches) {
     ++step_;
     elapsed_ += cfg_.time_step;
     if (step_ == 1 || step_ % cfg_.convergence_write_interval == 0) flux_pass();
+}
+
+void DeviceSolver::set_schedule(int sort_interval, int transport_block, int blocks_per_sm, int tally_aggregation) {
+    if (transport_block != 0 && transport_block != 128 && transport_block != 256 && transport_block != 512)
+        throw std::invalid_argument("transport_block must be 0 (tuned), 128, 256 or 512 threads");
+    if (blocks_per_sm < 0 || blocks_per_sm > 16) throw std::invalid_argument("transport_blocks_per_sm must be in [0, 16]");
+    synchronize();
+    cfg_.carrier_sort_interval = sort_interval;
+    cfg_.transport_block = transport_block;
+    cfg_.transport_blocks_per_sm = blocks_per_sm;
+    cfg_.tally_aggregation = tally_aggregation;
+    sort_interval_ = resolved_sort_interval(cfg_, mixed_);
+    // the captured step bakes in the launch shapes: capture again at the next step
+    if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+    if (graph_) cudaGraphDestroy(graph_);
+    graph_exec_ = nullptr;
+    graph_ = nullptr;
 }
 
 void DeviceSolver::sort_carriers() {

@@ -181,6 +181,9 @@ public:
     void set_graphs(bool on) { use_graphs_ = on; }
     // Steps between carrier sorts (0 never).
     int sort_interval() const { return sort_interval_; }
+    // Scheduling fields of the configuration (0: tuned default), changed
+    // between steps; the step graph is captured again.
+    void set_schedule(int sort_interval, int transport_block, int blocks_per_sm, int tally_aggregation);
     double drive_only();
     const Problem& problem() const { return P_; }
     long long launches() const { return counters_.launches; }

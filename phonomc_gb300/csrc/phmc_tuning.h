@@ -2,21 +2,22 @@
 // phonomc_gb300/autotune.py from timed sweeps on a GB300 (the sweep record it
 // writes sits beside it, phonomc_gb300/tuning_record.json). A configuration
 // field of 0 selects these values; none of them changes the physics.
+// Index [0] is the plain FP64 carrier state, [1] the mixed-precision one.
 #pragma once
 
 namespace phmc {
 namespace tuning {
 // Threads per CTA of the carrier pass (128, 256 or 512).
-constexpr int kTransportBlock = 256;
-// Resident CTAs per SM of the grid-stride carrier kernels (grid = SMs x this,
-// fewer for small populations): sets the carriers each thread walks.
-constexpr int kTransportBlocksPerSm = 8;
+constexpr int kTransportBlock[2] = {256, 256};
+// Resident CTAs per SM of the carrier pass (grid = SMs x this, fewer for
+// small populations): sets the carriers each thread walks.
+constexpr int kTransportBlocksPerSm[2] = {8, 8};
 // Steps between carrier sorts by (mode, cell), or by (cell, mode) in mesh
-// domains, and the smallest population that is sorted at all.
-constexpr int kSortInterval = 50;
-constexpr double kSortMinCarriers = 2e6;
+// domains (0: never), and the smallest population that is sorted at all.
+constexpr int kSortInterval[2] = {50, 50};
+constexpr double kSortMinCarriers = 2e+06;
 // Bin tallies of the carrier pass: 1 sums runs of equal (cell, bin) across
 // the lanes of a warp before one FP64 atomic per run, 0 one atomic per carrier.
-constexpr int kTallyAggregation = 1;
+constexpr int kTallyAggregation[2] = {1, 1};
 } // namespace tuning
 } // namespace phmc

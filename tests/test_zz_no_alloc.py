@@ -95,3 +95,26 @@ def test_noalloc_rejects_oversized_and_sets_up_with_zero(gpu):
     h1, t1, f1, m1 = _noalloc_call(gpu, lo, hi, p1, v1)
     assert np.array_equal(f0, f1) and np.array_equal(h0, h1)
     assert m1 == int(np.count_nonzero(f0 < 0))
+
+
+def test_noalloc_full_call_takes_no_device_memory(gpu):
+    """After the setup call, a full 65,536-ray call leaves the device's free
+    memory unchanged (cudaMemGetInfo through torch); a first full call may
+    still see the driver size the kernel's launch resources, so the memory is
+    read around a second one."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("torch has no CUDA device")
+    lo, hi = (0.0, 0.0, 0.0), (500.0, 400.0, 300.0)
+    D = abi.dptr
+    misses = C.c_int64(-1)
+    assert gpu.phmc_dev_trace_box_noalloc(D(np.asarray(lo)), D(np.asarray(hi)), 0, None, None, None, None, None,
+                                          C.byref(misses)) == 0
+    p, v = _rays(MAX_RAYS, 21, lo, hi, 0.01)
+    _noalloc_call(gpu, lo, hi, p, v)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    _noalloc_call(gpu, lo, hi, p, v)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
