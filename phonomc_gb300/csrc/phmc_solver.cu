@@ -772,10 +772,11 @@ void DeviceSolver::set_schedule(int sort_interval, int transport_block, int bloc
 
 void DeviceSolver::sort_carriers() {
     if (sort_.capacity != state_.capacity) {
+        const int slot_bytes = carrier_slot_bytes(ctx(), mixed_);
         void* p = nullptr;
-        PHMC_CUDA(cudaMalloc(&p, SortScratch::bytes_for(state_.capacity)));
+        PHMC_CUDA(cudaMalloc(&p, SortScratch::bytes_for(state_.capacity, slot_bytes)));
         allocations_.push_back(p);
-        sort_.carve(p, state_.capacity);
+        sort_.carve(p, state_.capacity, slot_bytes);
     }
     int modes = 1;
     for (const PhononMaterial* m : mats_) modes = std::max(modes, m->active_mode_count());

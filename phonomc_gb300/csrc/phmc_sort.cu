@@ -181,10 +181,35 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint32_t* 
     }
 }
 
-template <class T>
-__global__ void __launch_bounds__(256) k_gather(const uint32_t* __restrict__ perm, const T* __restrict__ src,
-                                                T* __restrict__ dst, int n) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[perm[i]];
+// The per-slot arrays of a carrier population and their sorted copies.
+struct SlotFields {
+    int count;
+    unsigned char* cur[kSortMaxFields];
+    unsigned char* alt[kSortMaxFields];
+    int size[kSortMaxFields]; // bytes per slot: 1, 4 or 8
+};
+
+__device__ __forceinline__ void copy_slot(unsigned char* dst, const unsigned char* src, int size, size_t to,
+                                          size_t from) {
+    if (size == 8) reinterpret_cast<unsigned long long*>(dst)[to] = reinterpret_cast<const unsigned long long*>(src)[from];
+    else if (size == 4) reinterpret_cast<unsigned*>(dst)[to] = reinterpret_cast<const unsigned*>(src)[from];
+    else dst[to] = src[from];
+}
+
+// Every field of slot perm[i] into slot i of the sorted copies (one read of the permutation).
+__global__ void __launch_bounds__(256) k_gather_fields(const uint32_t* __restrict__ perm, const SlotFields F, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const size_t from = perm[i];
+        for (int f = 0; f < F.count; ++f) copy_slot(F.alt[f], F.cur[f], F.size[f], static_cast<size_t>(i), from);
+    }
+}
+
+// The sorted copies back into the carrier arrays (the arrays keep their
+// addresses, so captured step graphs stay valid).
+__global__ void __launch_bounds__(256) k_copy_fields(const SlotFields F, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        for (int f = 0; f < F.count; ++f) copy_slot(F.cur[f], F.alt[f], F.size[f], static_cast<size_t>(i),
+                                                    static_cast<size_t>(i));
 }
 
 int bit_length(uint32_t v) {
@@ -198,15 +223,17 @@ int bit_length(uint32_t v) {
 
 } // namespace
 
-size_t SortScratch::bytes_for(int capacity) {
+size_t SortScratch::bytes_for(int capacity, int slot_bytes) {
     const size_t ntiles = (static_cast<size_t>(capacity) + kSortTile - 1) / kSortTile;
     const size_t m = 256 * ntiles;
     const size_t nb = (m + kScanChunk - 1) / kScanChunk;
-    return 4 * 4 * static_cast<size_t>(capacity) + 4 * (m + nb) + 8 * static_cast<size_t>(capacity) + 8 * 256;
+    return 4 * 4 * static_cast<size_t>(capacity) + 4 * (m + nb) +
+           static_cast<size_t>(slot_bytes) * static_cast<size_t>(capacity) + (8 + kSortMaxFields) * 256;
 }
 
-void SortScratch::carve(void* base, int cap) {
+void SortScratch::carve(void* base, int cap, int slot_bytes_) {
     capacity = cap;
+    slot_bytes = slot_bytes_;
     ntiles = (cap + kSortTile - 1) / kSortTile;
     const size_t m = 256 * static_cast<size_t>(ntiles);
     const size_t nb = (m + kScanChunk - 1) / kScanChunk;
@@ -216,13 +243,42 @@ void SortScratch::carve(void* base, int cap) {
         p += (bytes + 255) & ~size_t{255};
         return q;
     };
-    tmp = take(8 * static_cast<size_t>(cap));
+    alt = static_cast<unsigned char*>(take(static_cast<size_t>(slot_bytes) * static_cast<size_t>(cap) +
+                                          kSortMaxFields * 256));
     k0 = static_cast<uint32_t*>(take(4 * static_cast<size_t>(cap)));
     k1 = static_cast<uint32_t*>(take(4 * static_cast<size_t>(cap)));
     v0 = static_cast<uint32_t*>(take(4 * static_cast<size_t>(cap)));
     v1 = static_cast<uint32_t*>(take(4 * static_cast<size_t>(cap)));
     counts = static_cast<uint32_t*>(take(4 * m));
     partial = static_cast<uint32_t*>(take(4 * nb));
+}
+
+// Visits every per-slot array that a sort moves: positions (FP64) or cell
+// offsets (FP32), occupation, mode, cell, alive, and in mesh domains the mirror
+// facet and the wall cache.
+template <class Visit> void slot_arrays(const LaunchCtx& x, bool mixed, Visit&& visit) {
+    if (mixed) {
+        visit(x.S.ox);
+        visit(x.S.oy);
+        visit(x.S.oz);
+    } else {
+        visit(x.S.x);
+        visit(x.S.y);
+        visit(x.S.z);
+    }
+    visit(x.S.occ);
+    visit(x.S.mode);
+    visit(x.S.cell);
+    visit(x.S.alive);
+    if (x.mesh) {
+        const DevFacets& M = x.Th->fac;
+        visit(M.mirror);
+        visit(M.hit_t);
+        visit(M.hit_x);
+        visit(M.hit_y);
+        visit(M.hit_z);
+        visit(M.hit_f);
+    }
 }
 
 int launch_carrier_sort(const LaunchCtx& x, const SortScratch& s, int ncells, int modes, bool cell_major, bool mixed) {
@@ -255,39 +311,32 @@ int launch_carrier_sort(const LaunchCtx& x, const SortScratch& s, int ncells, in
         std::swap(vin, vout);
     }
     const uint32_t* perm = vin;
-    auto move = [&](auto* arr) {
+    SlotFields F{};
+    size_t offset = 0;
+    auto field = [&](auto* arr) {
         using T = std::remove_pointer_t<decltype(arr)>;
         if (!arr) return;
-        T* tmp = static_cast<T*>(s.tmp);
-        k_gather<T><<<g, 256, 0, x.stream>>>(perm, arr, tmp, cap);
-        if (cudaMemcpyAsync(arr, tmp, sizeof(T) * static_cast<size_t>(cap), cudaMemcpyDeviceToDevice, x.stream) !=
-            cudaSuccess)
-            throw std::runtime_error("cudaMemcpyAsync of a sorted carrier array failed");
-        ++launches;
+        if (F.count >= kSortMaxFields) throw std::runtime_error("too many carrier arrays for the sort");
+        F.cur[F.count] = reinterpret_cast<unsigned char*>(arr);
+        F.alt[F.count] = s.alt + offset;
+        F.size[F.count] = static_cast<int>(sizeof(T));
+        offset += (sizeof(T) * static_cast<size_t>(cap) + 255) & ~size_t{255};
+        ++F.count;
     };
-    if (mixed) {
-        move(x.S.ox);
-        move(x.S.oy);
-        move(x.S.oz);
-    } else {
-        move(x.S.x);
-        move(x.S.y);
-        move(x.S.z);
-    }
-    move(x.S.occ);
-    move(x.S.mode);
-    move(x.S.cell);
-    move(x.S.alive);
-    if (x.mesh) {
-        const DevFacets& F = x.Th->fac;
-        move(F.mirror);
-        move(F.hit_t);
-        move(F.hit_x);
-        move(F.hit_y);
-        move(F.hit_z);
-        move(F.hit_f);
-    }
-    return launches;
+    slot_arrays(x, mixed, field);
+    if (offset > static_cast<size_t>(s.slot_bytes) * static_cast<size_t>(cap) + kSortMaxFields * 256)
+        throw std::runtime_error("carrier sort scratch is smaller than the carrier arrays");
+    k_gather_fields<<<g, 256, 0, x.stream>>>(perm, F, cap);
+    k_copy_fields<<<g, 256, 0, x.stream>>>(F, cap);
+    return launches + 2;
+}
+
+int carrier_slot_bytes(const LaunchCtx& x, bool mixed) {
+    int bytes = 0;
+    slot_arrays(x, mixed, [&](auto* arr) {
+        if (arr) bytes += static_cast<int>(sizeof(*arr));
+    });
+    return bytes;
 }
 
 } // namespace phmc

@@ -105,6 +105,28 @@ __device__ __forceinline__ void count_interface(BlockLedger* bl, const IfaceOut&
     else if (r.action == 3) atomicAdd(&bl->iface_reflected, 1u);
 }
 
+// True when the carrier cannot reach a wall plane within `remaining`: it is
+// inside the box and, on every axis it moves along, the distance to the wall
+// ahead -- the numerator target - p of the plane time that trace_box divides
+// by the velocity -- exceeds its reach |v| remaining by a relative margin of
+// 1e-9, far above the rounding of that quotient. The traced flight of such a
+// carrier finds its wall beyond `remaining` and drifts; this test gets there
+// with multiplications and compares instead of three FP64 divisions.
+__device__ __forceinline__ bool clear_of_walls(const DevDomain& D, const double p[3], const double v[3],
+                                               double remaining) {
+    bool clear = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        clear = clear && p[a] >= D.lo[a] && p[a] <= D.hi[a];
+        const double c = v[a];
+        if (!(fabs(c) <= 1e-18)) { // an axis the trace considers (a NaN velocity fails the test below)
+            const double gap = c > 0.0 ? D.hi[a] - p[a] : D.lo[a] - p[a];
+            clear = clear && fabs(gap) > fabs(c) * remaining * (1.0 + 1e-9);
+        }
+    }
+    return clear;
+}
+
 // One carrier's flight for `remaining` ps (src/solver/TransportOperator.cpp:405-466).
 // Position, mode word and occupation live in registers; returns false when the
 // carrier was absorbed.
@@ -120,6 +142,11 @@ __device__ bool advance_carrier(const DevTables& T, DevLedger* L, BlockLedger* b
     const DevMaterial* M = &T.mat[mid];
     double v[3];
     mode_velocity(*M, w, v);
+    if (P.n_materials <= 1 && clear_of_walls(D, p, v, remaining)) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], remaining));
+        return true;
+    }
     double cp[3], t;
     int f;
     if (!counted_cache(cache_hit(D, P, p, v, M->speed[w & 0x00FFFFFFu], cp, t, f))) {
@@ -781,12 +808,19 @@ __device__ __forceinline__ void k_transport_body(const DevTables& T, CarrierStat
             int4 entry;
             long long h = -1;
             double hocc = 0.0;
-            if (i < n && __ldcs(S.alive + i)) {
-                uint32_t w = __ldcs(S.mode + i);
-                const int c0 = __ldcs(S.cell + i);
-                double occ = apply_pending(T, C, c0, w, __ldcs(S.occ + i));
+            // every streamed field is loaded before alive is looked at, so the
+            // loads of a carrier share one memory round trip (slots below
+            // n_slots are allocated whether alive or not)
+            const bool in = i < n;
+            const int ic = in ? i : 0;
+            const uint8_t alive = __ldcs(S.alive + ic);
+            uint32_t w = __ldcs(S.mode + ic);
+            const int c0 = __ldcs(S.cell + ic);
+            const double occ0 = __ldcs(S.occ + ic);
+            float p[3] = {__ldcs(S.ox + ic), __ldcs(S.oy + ic), __ldcs(S.oz + ic)};
+            if (in && alive) {
+                double occ = apply_pending(T, C, c0, w, occ0);
                 const Frame F = cell_frame(T.dom, c0);
-                float p[3] = {__ldcs(S.ox + i), __ldcs(S.oy + i), __ldcs(S.oz + i)};
                 float remaining = T.par.dt32;
                 int event = 0, plane = -1;
                 const int end =
@@ -843,11 +877,16 @@ __device__ __forceinline__ void k_transport_body(const DevTables& T, CarrierStat
             const int i = base + threadIdx.x;
             long long h = -1;
             double occ = 0.0;
-            if (i < n && __ldcs(S.alive + i)) {
-                uint32_t w = __ldcs(S.mode + i);
-                const int c0 = __ldcs(S.cell + i);
-                occ = apply_pending(T, C, c0, w, __ldcs(S.occ + i));
-                double p[3] = {__ldcs(S.x + i), __ldcs(S.y + i), __ldcs(S.z + i)};
+            // all streamed fields in one memory round trip, alive included
+            const bool in = i < n;
+            const int ic = in ? i : 0;
+            const uint8_t alive0 = __ldcs(S.alive + ic);
+            uint32_t w = __ldcs(S.mode + ic);
+            const int c0 = __ldcs(S.cell + ic);
+            const double occ0 = __ldcs(S.occ + ic);
+            double p[3] = {__ldcs(S.x + ic), __ldcs(S.y + ic), __ldcs(S.z + ic)};
+            if (in && alive0) {
+                occ = apply_pending(T, C, c0, w, occ0);
                 const bool alive = advance_carrier(T, L, &bl, i, p, w, occ, T.par.dt, kDrawTransport, step);
                 const int c = grid_index(T.dom, p[0], p[1], p[2]);
                 __stcs(S.x + i, p[0]);
@@ -1399,7 +1438,11 @@ __global__ void k_containment(const DevTables* __restrict__ Tp, CarrierState S, 
 }
 
 // Heat-flux tally q_c = sum v e w (src/solver/GridStatistics.cpp:269-347) with the
-// end-of-step occupation n = alpha n + beta - (second drive half).
+// end-of-step occupation n = alpha n + beta - (second drive half). Carriers
+// sorted by mode put one mode in most warps: such a warp shares one velocity,
+// so it sums the energies of each run of equal cells with a segmented shuffle
+// scan and adds v * sum once per run (no shared-memory atomic contention on
+// the few cells a warp covers); other warps add per carrier.
 __global__ void __launch_bounds__(256) k_flux(const DevTables* __restrict__ Tp, CarrierState S, CellArrays C,
                                               const DevLedger* L, int use_shared) {
     extern __shared__ double sq[];
@@ -1407,21 +1450,44 @@ __global__ void __launch_bounds__(256) k_flux(const DevTables* __restrict__ Tp, 
     if (use_shared)
         for (int k = threadIdx.x; k < 3 * C.ncells; k += blockDim.x) sq[k] = 0.0;
     __syncthreads();
+    double* dst = use_shared ? sq : C.flux;
     const int n = L->n_slots;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        if (!S.alive[i]) continue;
-        const uint32_t w = S.mode[i];
-        const DevMaterial& M = T.mat[w >> 28];
-        const int ai = static_cast<int>(w & 0x00FFFFFFu);
-        const int c = S.cell[i];
-        double occ = apply_pending(T, C, c, w, S.occ[i]) - drive_half(T, C, M, c, ai);
-        if (C.src_next) occ -= C.src_next[static_cast<size_t>(c) * C.hist_modes + bin_of(M, ai)];
-        const double e = dmul(dmul(M.hw[ai], occ - M.nbg[ai]), M.energy_weight);
-        double v[3];
-        if (T.fac.mirror) mesh_velocity(T.fac, M, w, T.fac.mirror[i], v);
-        else mode_velocity(M, w, v);
-        double* dst = use_shared ? sq : C.flux;
-        for (int a = 0; a < 3; ++a) atomicAdd(dst + 3 * c + a, dmul(v[a], e));
+    const int lane = threadIdx.x & 31;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        const int ic = i < n ? i : 0;
+        const bool live = i < n && S.alive[ic];
+        const uint32_t w = S.mode[ic];
+        const int c = live ? S.cell[ic] : -1;
+        double e = 0.0;
+        double v[3] = {0.0, 0.0, 0.0};
+        if (live) {
+            const DevMaterial& M = T.mat[w >> 28];
+            const int ai = static_cast<int>(w & 0x00FFFFFFu);
+            double occ = apply_pending(T, C, c, w, S.occ[ic]) - drive_half(T, C, M, c, ai);
+            if (C.src_next) occ -= C.src_next[static_cast<size_t>(c) * C.hist_modes + bin_of(M, ai)];
+            e = dmul(dmul(M.hw[ai], occ - M.nbg[ai]), M.energy_weight);
+            if (T.fac.mirror) mesh_velocity(T.fac, M, w, T.fac.mirror[ic], v);
+            else mode_velocity(M, w, v);
+        }
+        const uint32_t w0 = __shfl_sync(0xffffffffu, w, 0);
+        const bool one_mode = !T.fac.mirror && __all_sync(0xffffffffu, !live || w == w0) &&
+                              __any_sync(0xffffffffu, live);
+        if (one_mode) {
+            const int cp = __shfl_up_sync(0xffffffffu, c, 1);
+            const int cn = __shfl_down_sync(0xffffffffu, c, 1);
+            const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || cp != c);
+            const int start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const double e2 = __shfl_up_sync(0xffffffffu, e, o);
+                if (lane - o >= start) e += e2;
+            }
+            if (live && (lane == 31 || cn != c))
+                for (int a = 0; a < 3; ++a) atomicAdd(dst + 3 * c + a, dmul(v[a], e));
+        } else if (live) {
+            for (int a = 0; a < 3; ++a) atomicAdd(dst + 3 * c + a, dmul(v[a], e));
+        }
     }
     __syncthreads();
     if (use_shared)
