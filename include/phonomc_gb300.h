@@ -154,6 +154,8 @@ typedef struct phmc_config {
     int32_t transport_block;         /* threads per CTA of the carrier pass: 128, 256 or 512 */
     int32_t transport_blocks_per_sm; /* resident CTAs per SM of the carrier kernels (1..16) */
     int32_t tally_aggregation;       /* 1: warp-summed bin tallies, < 0: one atomic per carrier */
+    int32_t transport_pipeline;      /* mixed state: 1 carrier tiles staged in shared memory by bulk
+                                        asynchronous copies, < 0 direct loads */
 } phmc_config;
 
 /* Getters of include/MonteCarloSolver.h:59-101 plus the last step's ledger. */
@@ -190,6 +192,21 @@ int phmc_material_create(const phmc_material_data* data, double temperature_look
                          int include_stationary_modes, int complete_callaway_bz, phmc_material** out);
 void phmc_material_destroy(phmc_material* m);
 int phmc_material_active_count(const phmc_material* m, int* n_active);
+/* A material from a folder in the reference's layout: POSCAR plus
+ * kappa-fbz.hdf5, kappa.hdf5 or a single *.hdf5 (read_material_data,
+ * src/material/MaterialDataReader.cpp:150-302, then the PhononMaterial
+ * constructor, include/PhononMaterial.h:23-26). libhdf5 is not required. */
+int phmc_material_load(const char* folder, double temperature_lookup_dt, int include_stationary_modes,
+                       int complete_callaway_bz, phmc_material** out);
+/* Writes `data` as a material folder in the reference's layout (POSCAR and
+ * kappa-fbz.hdf5 with unit weights). No counterpart in the reference, whose
+ * tables come from phono3py. */
+int phmc_material_save(const phmc_material_data* data, const char* folder);
+/* One numeric dataset of an HDF5 file's root group, as doubles: its rank and
+ * dims (up to 8), then its values (row-major). No counterpart in the
+ * reference, which links libhdf5. */
+int phmc_h5_shape(const char* path, const char* name, int32_t* rank, int64_t* dims);
+int phmc_h5_read(const char* path, const char* name, double* values);
 
 int phmc_solver_create(const phmc_config* cfg, phmc_material* const* materials, int n_materials,
                        phmc_solver** out);
@@ -230,11 +247,12 @@ int phmc_solver_set_graphs(phmc_solver* s, int on);
  * carrier_sort_interval or its tuned default). No counterpart in the reference. */
 int phmc_solver_sort_interval(const phmc_solver* s, int* steps);
 /* Changes the scheduling fields of the configuration (carrier_sort_interval,
- * transport_block, transport_blocks_per_sm, tally_aggregation; 0 = tuned
+ * transport_block, transport_blocks_per_sm, tally_aggregation,
+ * transport_pipeline; 0 = tuned
  * default) between steps, e.g. for a tuning sweep on one population. No
  * counterpart in the reference. */
 int phmc_solver_set_schedule(phmc_solver* s, int sort_interval, int transport_block, int blocks_per_sm,
-                             int tally_aggregation);
+                             int tally_aggregation, int transport_pipeline);
 /* Page-lock / release caller-owned host buffers used for end-to-end stepping. */
 int phmc_host_register(void* ptr, int64_t bytes);
 int phmc_host_unregister(void* ptr);

@@ -14,6 +14,7 @@
 #include <memory>
 #include <sstream>
 #include "PhononMaterial.h"
+#include "material/MaterialDataReader.h"
 #include "SimulationConfig.h"
 #include "SimulationDomain.h"
 #include "material/CallawayOperator.h"
@@ -911,7 +912,10 @@ std::string cmd_run(const std::string& pmat, const std::string& toml, int steps)
     std::vector<std::reference_wrapper<const PhononMaterial>> mats;
     std::stringstream list(pmat);
     for (std::string item; std::getline(list, item, ',');) {
-        owned.push_back(std::make_unique<PhononMaterial>(read_pmat(item), a.temperature_lookup_dt, stationary,
+        // a material folder (POSCAR + HDF5) goes through the reference's own
+        // read_material_data; a .pmat file through the flat-table reader above
+        MaterialData md = std::filesystem::is_directory(item) ? phonomc::read_material_data(item) : read_pmat(item);
+        owned.push_back(std::make_unique<PhononMaterial>(std::move(md), a.temperature_lookup_dt, stationary,
                                                          a.collision_model == CollisionModel::Callaway));
         mats.push_back(*owned.back());
     }

@@ -155,6 +155,7 @@ class ConfigPOD(C.Structure):
         ("write_cell_heat_flux", C.c_int32), ("callaway_nonlinear", C.c_int32),
         ("carrier_sort_interval", C.c_int32), ("transport_block", C.c_int32),
         ("transport_blocks_per_sm", C.c_int32), ("tally_aggregation", C.c_int32),
+        ("transport_pipeline", C.c_int32),
     ]
 
 
@@ -239,6 +240,7 @@ def config_pod(cfg: dict):
     c.transport_block = int(cfg.get("transport_block", 0))
     c.transport_blocks_per_sm = int(cfg.get("transport_blocks_per_sm", 0))
     c.tally_aggregation = int(cfg.get("tally_aggregation", 0))
+    c.transport_pipeline = int(cfg.get("transport_pipeline", 0))
     c.transport_axis = int(cfg.get("transport_axis", -1))
     g = cfg.get("temperature_gradient")
     c.has_temperature_gradient = int(g is not None)
@@ -296,6 +298,11 @@ DOMAIN_PROTOS = {
     "domain_grid_index": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_int32_p]),
     "domain_nearest_facet": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_int32_p]),
     "dev_domain_query": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_uint8_p, c_int32_p, c_int32_p]),
+    # material folders in the reference's layout (POSCAR + HDF5) and HDF5 datasets
+    "material_load": (C.c_int, [C.c_char_p, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "material_save": (C.c_int, [C.POINTER(MaterialDataPOD), C.c_char_p]),
+    "h5_shape": (C.c_int, [C.c_char_p, C.c_char_p, c_int32_p, c_int64_p]),
+    "h5_read": (C.c_int, [C.c_char_p, C.c_char_p, c_double_p]),
 }
 
 
@@ -364,6 +371,37 @@ class Material(Handle):
             self.close()
         except Exception:
             pass
+
+
+class FolderMaterial(Material):
+    """A material read from a folder in the reference's layout (phmc_material_load)."""
+
+    def __init__(self, lib, folder: str, lookup_dt=0.1, stationary=False, complete_bz=False):
+        Handle.__init__(self, lib, "phmc_")
+        h = C.c_void_p()
+        self.check(lib.phmc_material_load(str(folder).encode(), lookup_dt, int(stationary), int(complete_bz),
+                                          C.byref(h)))
+        self.h = h
+        self.data = None
+
+
+def save_material(lib, data: synthetic.MaterialData, folder: str) -> None:
+    """POSCAR + kappa-fbz.hdf5 of `data` in the reference's layout (phmc_material_save)."""
+    pod, keep = material_pod(data)
+    if lib.phmc_material_save(C.byref(pod), str(folder).encode()) != 0:
+        raise LibError(lib.phmc_last_error().decode())
+
+
+def h5_read(lib, path: str, name: str) -> np.ndarray:
+    """One numeric HDF5 dataset as float64 (phmc_h5_shape / phmc_h5_read)."""
+    rank, dims = C.c_int32(), (C.c_int64 * 8)()
+    if lib.phmc_h5_shape(str(path).encode(), name.encode(), C.byref(rank), dims) != 0:
+        raise LibError(lib.phmc_last_error().decode())
+    shape = tuple(dims[k] for k in range(rank.value))
+    out = np.zeros(int(np.prod(shape)) if shape else 1)
+    if lib.phmc_h5_read(str(path).encode(), name.encode(), dptr(out)) != 0:
+        raise LibError(lib.phmc_last_error().decode())
+    return out.reshape(shape)
 
 
 class Solver(Handle):
@@ -476,7 +514,7 @@ DEVICE_PROTOS = {
     "solver_timed_run": (C.c_int, [C.c_void_p, C.c_int, c_double_p, c_double_p, c_int64_p, c_int64_p, c_int64_p]),
     "solver_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "solver_sort_interval": (C.c_int, [C.c_void_p, c_int32_p]),
-    "solver_set_schedule": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "solver_set_schedule": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
     "batch_create": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),
     "batch_size": (C.c_int, [C.c_void_p, c_int32_p]),
     "batch_run": (C.c_int, [C.c_void_p, C.c_int]),

@@ -8,6 +8,9 @@ change no physics:
                            how many carriers each thread walks
   carrier_sort_interval    steps between stable (mode, cell) carrier sorts
   tally_aggregation        warp-summed bin tallies (1) or one atomic per carrier (-1)
+  transport_pipeline       mixed state: carrier tiles staged in shared memory by
+                           bulk asynchronous copies (1, 256 threads) or loaded
+                           directly (-1)
 
 for the plain FP64 and the mixed-precision carrier state, then the smallest
 population at which sorting pays. Each point is timed over whole timesteps
@@ -47,10 +50,10 @@ def _solver(lib, abi, precision, particles, seed=777):
     return abi.Solver(lib, "phmc_", cfg, [m]), m
 
 
-def _time_point(lib, s, sort, block, per_sm, agg, min_steps):
+def _time_point(lib, s, sort, block, per_sm, agg, min_steps, pipe=-1):
     """Seconds per step of one schedule: two settling steps after the change
     (graph capture), then whole sort intervals from a sort step."""
-    s.check(lib.phmc_solver_set_schedule(s.h, sort, block, per_sm, agg))
+    s.check(lib.phmc_solver_set_schedule(s.h, sort, block, per_sm, agg, pipe))
     s.run(2)
     if sort > 0:
         cur = s.stats()["current_timestep"]
@@ -73,17 +76,21 @@ def sweep(lib, abi, precision, particles, quick=False, log=print):
     sorts = (25, 100) if quick else SORTS
     points = []
 
-    def rec(sort, b, p, a, min_steps):
-        sec, steps = _time_point(lib, s, sort, b, p, a, min_steps)
+    def rec(sort, b, p, a, min_steps, pipe=-1):
+        sec, steps = _time_point(lib, s, sort, b, p, a, min_steps, pipe)
         pt = {"carrier_sort_interval": sort, "transport_block": b, "transport_blocks_per_sm": p,
-              "tally_aggregation": a, "ms_per_step": 1e3 * sec, "carrier_steps_per_s": n / sec, "steps": steps}
+              "tally_aggregation": a, "transport_pipeline": pipe, "ms_per_step": 1e3 * sec,
+              "carrier_steps_per_s": n / sec, "steps": steps}
         points.append(pt)
         log(json.dumps({"precision": precision, **pt}))
+    pipes = (-1, 1) if precision == "mixed" else (-1,)
     # unsorted population first: every schedule without sorts
-    for b, p, a in itertools.product(blocks, per_sm, AGG):
-        rec(-1, b, p, a, 30)
-    for k, b, p, a in itertools.product(sorts, blocks, per_sm, AGG):
-        rec(k, b, p, a, 60)
+    for pipe in pipes:
+        for b, p, a in itertools.product((256,) if pipe > 0 else blocks, per_sm, AGG):
+            rec(-1, b, p, a, 30, pipe)
+    for pipe in pipes:
+        for k, b, p, a in itertools.product(sorts, (256,) if pipe > 0 else blocks, per_sm, AGG):
+            rec(k, b, p, a, 60, pipe)
     s.close()
     best = min(points, key=lambda q: q["ms_per_step"])
     return {"precision": precision, "particles": n, "workload": "inplane_gradient", "points": points, "best": best}
@@ -95,12 +102,12 @@ def population_threshold(lib, abi, best, precision="mixed", sizes=(2e5, 1e6, 4e6
     for n in sizes:
         s, _m = _solver(lib, abi, precision, n)
         never, _ = _time_point(lib, s, -1, best["transport_block"], best["transport_blocks_per_sm"],
-                               best["tally_aggregation"], 60)
+                               best["tally_aggregation"], 60, best.get("transport_pipeline", -1))
         k = best["carrier_sort_interval"]
         if k <= 0:
             k = 50
         sorted_, _ = _time_point(lib, s, k, best["transport_block"], best["transport_blocks_per_sm"],
-                                 best["tally_aggregation"], 100)
+                                 best["tally_aggregation"], 100, best.get("transport_pipeline", -1))
         rows.append({"particles": n, "ms_never": 1e3 * never, "ms_sorted": 1e3 * sorted_, "interval": k})
         log(json.dumps(rows[-1]))
         s.close()
@@ -128,6 +135,9 @@ constexpr double kSortMinCarriers = {nmin:.6g};
 // Bin tallies of the carrier pass: 1 sums runs of equal (cell, bin) across
 // the lanes of a warp before one FP64 atomic per run, 0 one atomic per carrier.
 constexpr int kTallyAggregation[2] = {{{a0}, {a1}}};
+// Mixed carrier pass: carrier tiles staged in shared memory by bulk
+// asynchronous copies one tile ahead (1), or loaded directly (0).
+constexpr int kTransportPipeline = {pipe};
 }} // namespace tuning
 }} // namespace phmc
 """
@@ -153,7 +163,8 @@ def write_outputs(out, record):
     text = HEADER.format(b0=val("fp64", "transport_block", 256), b1=val("mixed", "transport_block", 256),
                          p0=val("fp64", "transport_blocks_per_sm", 8), p1=val("mixed", "transport_blocks_per_sm", 8),
                          k0=sort_of("fp64"), k1=sort_of("mixed"), nmin=float(nmin),
-                         a0=max(0, val("fp64", "tally_aggregation", 1)), a1=max(0, val("mixed", "tally_aggregation", 1)))
+                         a0=max(0, val("fp64", "tally_aggregation", 1)), a1=max(0, val("mixed", "tally_aggregation", 1)),
+                         pipe=max(0, val("mixed", "transport_pipeline", 1)))
     with open(os.path.join(out, "phmc_tuning.h"), "w") as f:
         f.write(text)
 

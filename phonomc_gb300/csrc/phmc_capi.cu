@@ -3,6 +3,7 @@
 // message for phmc_last_error().
 #include "phmc_kernels.cuh"
 #include "phmc_pod.h"
+#include "phmc_hdf5.h"
 
 #include <cstdlib>
 #include <cstring>
@@ -438,6 +439,70 @@ int phmc_material_create(const phmc_material_data* data, double dt, int stationa
 
 void phmc_material_destroy(phmc_material* m) { delete m; }
 
+int phmc_material_load(const char* folder, double dt, int stationary, int complete_bz, phmc_material** out) {
+    return guard([&] {
+        if (!folder) throw std::invalid_argument("material folder path is null");
+        const MaterialFolder f = read_material_folder(folder);
+        MaterialData d;
+        d.volume_a3 = f.volume_a3;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) d.reciprocal[i][j] = f.reciprocal[i][j];
+        d.qpoints = f.qpoints;
+        d.branches = f.branches;
+        d.mesh = f.mesh;
+        d.frequency_thz = f.frequency_thz;
+        d.qpoint_fractions.assign(f.qpoint_fractions.begin(), f.qpoint_fractions.end());
+        d.group_velocity.assign(f.group_velocity.begin(), f.group_velocity.end());
+        d.temperatures = f.temperatures;
+        d.gamma = f.gamma;
+        d.gamma_normal = f.gamma_normal;
+        d.gamma_umklapp = f.gamma_umklapp;
+        d.gamma_resistive = f.gamma_resistive;
+        auto m = std::make_unique<phmc_material>();
+        m->m = std::make_unique<PhononMaterial>(std::move(d), dt, stationary != 0, complete_bz != 0);
+        *out = m.release();
+    });
+}
+
+int phmc_material_save(const phmc_material_data* p, const char* folder) {
+    return guard([&] {
+        if (!p || !folder) throw std::invalid_argument("material data or folder is null");
+        const MaterialData d = material_from_pod(*p);
+        MaterialFolder f;
+        f.volume_a3 = d.volume_a3;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) f.reciprocal[i][j] = d.reciprocal[i][j];
+        f.qpoints = d.qpoints;
+        f.branches = d.branches;
+        f.mesh = d.mesh;
+        f.frequency_thz = d.frequency_thz;
+        f.qpoint_fractions.assign(d.qpoint_fractions.begin(), d.qpoint_fractions.end());
+        f.group_velocity.assign(d.group_velocity.begin(), d.group_velocity.end());
+        f.temperatures = d.temperatures;
+        f.gamma = d.gamma;
+        f.gamma_normal = d.gamma_normal;
+        f.gamma_umklapp = d.gamma_umklapp;
+        f.gamma_resistive = d.gamma_resistive;
+        write_material_folder(folder, f);
+    });
+}
+
+int phmc_h5_shape(const char* path, const char* name, int32_t* rank, int64_t* dims) {
+    return guard([&] {
+        const h5::Dataset d = h5::Reader(path).read(name);
+        if (d.dims.size() > 8) throw std::runtime_error("dataset rank above 8");
+        *rank = static_cast<int32_t>(d.dims.size());
+        for (size_t k = 0; k < d.dims.size(); ++k) dims[k] = static_cast<int64_t>(d.dims[k]);
+    });
+}
+
+int phmc_h5_read(const char* path, const char* name, double* values) {
+    return guard([&] {
+        const h5::Dataset d = h5::Reader(path).read(name);
+        std::copy(d.values.begin(), d.values.end(), values);
+    });
+}
+
 int phmc_domain_create(const phmc_config* cfg, phmc_domain** out) {
     return guard([&] {
         if (!cfg || !out) throw std::invalid_argument("phmc_domain_create: null argument");
@@ -625,8 +690,10 @@ int phmc_solver_sort_interval(const phmc_solver* s, int* steps) {
 }
 
 int phmc_solver_set_schedule(phmc_solver* s, int sort_interval, int transport_block, int blocks_per_sm,
-                             int tally_aggregation) {
-    return guard([&] { s->s->set_schedule(sort_interval, transport_block, blocks_per_sm, tally_aggregation); });
+                             int tally_aggregation, int transport_pipeline) {
+    return guard([&] {
+        s->s->set_schedule(sort_interval, transport_block, blocks_per_sm, tally_aggregation, transport_pipeline);
+    });
 }
 
 // ---------------------------------------------------------------- batches

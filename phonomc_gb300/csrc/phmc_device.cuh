@@ -57,6 +57,7 @@ enum ErrorCode : int {
     kErrNclNoConverge = 15,
     kErrNclInvalid = 16,
     kErrNclTemperature = 17,
+    kErrPipelineTimeout = 18,
 };
 
 struct DevMaterial {

@@ -83,11 +83,13 @@ struct SimulationConfig {
     bool callaway_nonlinear = false;   // collision.callaway_formulation = "nonlinear"
     // Device scheduling, no counterpart in the reference (0: tuned default,
     // see phmc_tuning.h): carrier sort interval (< 0 never), threads per CTA
-    // and resident CTAs per SM of the carrier pass, bin-tally aggregation.
+    // and resident CTAs per SM of the carrier pass, bin-tally aggregation,
+    // shared-memory staging of the mixed carrier pass.
     int carrier_sort_interval = 0;
     int transport_block = 0;
     int transport_blocks_per_sm = 0;
     int tally_aggregation = 0;
+    int transport_pipeline = 0;
     std::string material_folder; // reported in summary.txt; tables enter as arrays
     // Layered materials (include/SimulationConfig.h:93-99): N materials, N-1 planes.
     int material_interface_axis = 0;

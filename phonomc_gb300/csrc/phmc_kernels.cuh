@@ -33,6 +33,8 @@ struct LaunchCtx {
     int transport_block = 256;
     int transport_grid = 1;
     bool tally_agg = true;
+    bool transport_pipe = false; // mixed state: TMA-staged carrier tiles (k_transport_pipe)
+    int pipe_grid = 1;
 };
 
 // Independent box instances advanced by one launch per kernel of the step:

@@ -141,6 +141,7 @@ inline SimulationConfig config_from_pod(const phmc_config& c) {
     s.transport_block = c.transport_block;
     s.transport_blocks_per_sm = c.transport_blocks_per_sm;
     s.tally_aggregation = c.tally_aggregation;
+    s.transport_pipeline = c.transport_pipeline;
     if (c.material_folder) s.material_folder = c.material_folder;
     s.material_interface_axis = c.material_interface_axis;
     if (c.n_interfaces > 0 && c.material_interface_positions)

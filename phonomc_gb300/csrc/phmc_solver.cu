@@ -56,6 +56,7 @@ static const char* error_message(int code) {
     case kErrNclNoConverge: return "Nonlinear Callaway moment solve did not converge";
     case kErrNclInvalid: return "Nonlinear Callaway occupation is invalid";
     case kErrNclTemperature: return "Nonlinear Callaway temperature is outside the supplied N/U table";
+    case kErrPipelineTimeout: return "Carrier tile copies did not complete within the wait limit.";
     default: return "Unknown device error.";
     }
 }
@@ -144,13 +145,16 @@ DeviceSolver::~DeviceSolver() {
 
 void DeviceSolver::allocate_state(int capacity) {
     state_.capacity = capacity;
+    // streamed per-slot arrays get one tile (256 slots) of padding: the staged
+    // carrier pass copies whole 16-byte units of the last tile
+    const int padded = capacity + 256;
     state_.x = dalloc<double>(capacity);
     state_.y = dalloc<double>(capacity);
     state_.z = dalloc<double>(capacity);
     if (mixed_) {
-        state_.ox = dalloc<float>(capacity);
-        state_.oy = dalloc<float>(capacity);
-        state_.oz = dalloc<float>(capacity);
+        state_.ox = dalloc<float>(padded);
+        state_.oy = dalloc<float>(padded);
+        state_.oz = dalloc<float>(padded);
         state_.deferred = dalloc<int4>(capacity);
     }
     if (domain_->is_mesh()) {
@@ -164,10 +168,10 @@ void DeviceSolver::allocate_state(int capacity) {
         mesh_hit_f_ = dalloc<int32_t>(capacity);
         state_.deferred = dalloc<int4>(capacity); // wall-event queue of the mesh transport
     }
-    state_.occ = dalloc<double>(capacity);
-    state_.mode = dalloc<uint32_t>(capacity);
-    state_.cell = dalloc<int32_t>(capacity);
-    state_.alive = dalloc<uint8_t>(capacity);
+    state_.occ = dalloc<double>(padded);
+    state_.mode = dalloc<uint32_t>(padded);
+    state_.cell = dalloc<int32_t>(padded);
+    state_.alive = dalloc<uint8_t>(padded);
     d_holes_ = dalloc<int>(capacity);
     n_dead_blocks_ = (capacity + 1023) / 1024;
     d_block_dead_ = dalloc<int>(n_dead_blocks_);
@@ -598,6 +602,11 @@ LaunchCtx DeviceSolver::ctx() const {
                                 (4LL * x.transport_block);
     x.transport_grid = static_cast<int>(std::max<long long>(8, std::min<long long>(sm_count_ * per_sm, want_pass)));
     x.tally_agg = cfg_.tally_aggregation > 0 || (cfg_.tally_aggregation == 0 && tuning::kTallyAggregation[tk] > 0);
+    // TMA-staged tiles of 256 carriers (mixed state), one CTA per tile slot
+    x.transport_pipe = mixed_ && (cfg_.transport_pipeline > 0 ||
+                                  (cfg_.transport_pipeline == 0 && tuning::kTransportPipeline > 0));
+    const long long tiles = (static_cast<long long>(state_.capacity) + 255) / 256;
+    x.pipe_grid = static_cast<int>(std::max<long long>(1, std::min<long long>(sm_count_ * per_sm, tiles)));
     x.mesh = domain_->is_mesh();
     x.ncl = P_.callaway_nonlinear ? &ncl_ : nullptr;
     x.lin_work = lin_work_;
@@ -753,7 +762,8 @@ void DeviceSolver::finish_batched_step(long long launches) {
     if (step_ == 1 || step_ % cfg_.convergence_write_interval == 0) flux_pass();
 }
 
-void DeviceSolver::set_schedule(int sort_interval, int transport_block, int blocks_per_sm, int tally_aggregation) {
+void DeviceSolver::set_schedule(int sort_interval, int transport_block, int blocks_per_sm, int tally_aggregation,
+                                int transport_pipeline) {
     if (transport_block != 0 && transport_block != 128 && transport_block != 256 && transport_block != 512)
         throw std::invalid_argument("transport_block must be 0 (tuned), 128, 256 or 512 threads");
     if (blocks_per_sm < 0 || blocks_per_sm > 16) throw std::invalid_argument("transport_blocks_per_sm must be in [0, 16]");
@@ -762,6 +772,7 @@ void DeviceSolver::set_schedule(int sort_interval, int transport_block, int bloc
     cfg_.transport_block = transport_block;
     cfg_.transport_blocks_per_sm = blocks_per_sm;
     cfg_.tally_aggregation = tally_aggregation;
+    cfg_.transport_pipeline = transport_pipeline;
     sort_interval_ = resolved_sort_interval(cfg_, mixed_);
     // the captured step bakes in the launch shapes: capture again at the next step
     if (graph_exec_) cudaGraphExecDestroy(graph_exec_);

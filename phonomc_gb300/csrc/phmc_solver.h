@@ -183,7 +183,8 @@ public:
     int sort_interval() const { return sort_interval_; }
     // Scheduling fields of the configuration (0: tuned default), changed
     // between steps; the step graph is captured again.
-    void set_schedule(int sort_interval, int transport_block, int blocks_per_sm, int tally_aggregation);
+    void set_schedule(int sort_interval, int transport_block, int blocks_per_sm, int tally_aggregation,
+                      int transport_pipeline);
     double drive_only();
     const Problem& problem() const { return P_; }
     long long launches() const { return counters_.launches; }

@@ -789,6 +789,79 @@ constexpr int kDeferBuffer = 64; // queued wall events per warp before a flush
 // bin. Mixed path: carriers that reach a wall needing table sampling are
 // queued (per-warp shared buffers, one global atomic per 32 entries) and
 // finished by k_deferred.
+// One carrier of the mixed pass, called by every thread of the block with its
+// fields (in = slot in range): apply the pending update, fly in FP32, store,
+// tally its bin over the warp, and queue a wall event that needs table
+// sampling (per-warp shared buffer qbuf, one global atomic per 32 entries).
+template <bool kRta, bool kAgg>
+__device__ __forceinline__ void mixed_carrier(const DevTables& T, const CarrierState& S, const CellArrays& C,
+                                              DevLedger* L, BlockLedger& bl, uint32_t step, int i, bool in,
+                                              uint8_t alive, uint32_t w, int c0, double occ0, float p[3],
+                                              int4 (*qbuf)[kDeferBuffer], int& queued) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    bool defer = false;
+    int4 entry;
+    long long h = -1;
+    double hocc = 0.0;
+    if (in && alive) {
+        double occ = apply_pending(T, C, c0, w, occ0);
+        const Frame F = cell_frame(T.dom, c0);
+        float remaining = T.par.dt32;
+        int event = 0, plane = -1;
+        const int end = advance_mixed<true>(T, L, &bl, i, F, p, w, occ, remaining, event, plane, kDrawTransport, step);
+        if (end == kFlightDeferred) {
+            // state at the wall, cell unchanged (the frame of the flight)
+            __stcs(S.ox + i, p[0]);
+            __stcs(S.oy + i, p[1]);
+            __stcs(S.oz + i, p[2]);
+            __stcs(S.mode + i, w);
+            __stcs(S.occ + i, occ);
+            defer = true;
+            entry = make_int4(i, __float_as_int(remaining), event, plane);
+        } else {
+            h = finish_mixed(T, S, C, L, i, F, p, w, occ, end != kFlightAbsorbed);
+            hocc = occ;
+        }
+    }
+    bin_warp<kAgg, kRta>(C, h, hocc);
+    const unsigned mask = __ballot_sync(0xffffffffu, defer);
+    if (mask) {
+        if (defer) qbuf[warp][queued + __popc(mask & ((1u << lane) - 1u))] = entry;
+        queued += __popc(mask);
+        __syncwarp();
+        if (queued >= 32) {
+            int at = 0;
+            if (lane == 0) at = atomicAdd(&L->n_deferred, 32);
+            at = __shfl_sync(0xffffffffu, at, 0);
+            if (at + lane < S.capacity) S.deferred[at + lane] = qbuf[warp][lane];
+            else raise_error(L, kErrInvalidStatistics, i);
+            __syncwarp();
+            const int rest = queued - 32;
+            int4 t = make_int4(0, 0, 0, 0);
+            if (lane < rest) t = qbuf[warp][32 + lane];
+            __syncwarp();
+            if (lane < rest) qbuf[warp][lane] = t;
+            __syncwarp();
+            queued = rest;
+        }
+    }
+}
+
+// The rest of a warp's queued wall events, after its last carrier.
+__device__ __forceinline__ void flush_deferred(const CarrierState& S, DevLedger* L, int4 (*qbuf)[kDeferBuffer],
+                                               int queued) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (queued > 0) {
+        int at = 0;
+        if (lane == 0) at = atomicAdd(&L->n_deferred, queued);
+        at = __shfl_sync(0xffffffffu, at, 0);
+        if (lane < queued) {
+            if (at + lane < S.capacity) S.deferred[at + lane] = qbuf[warp][lane];
+            else raise_error(L, kErrInvalidStatistics, at + lane);
+        }
+    }
+}
+
 // qbuf: kDeferBuffer entries per warp of the block (mixed path).
 template <bool kMixed, bool kRta, bool kAgg>
 __device__ __forceinline__ void k_transport_body(const DevTables& T, CarrierState S, CellArrays C, DevLedger* L, int vbx,
@@ -799,78 +872,23 @@ __device__ __forceinline__ void k_transport_body(const DevTables& T, CarrierStat
     __syncthreads();
     const int n = L->n_slots;
     if constexpr (kMixed) {
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         int queued = 0; // warp-uniform
         // block-uniform trip count so that every lane reaches the warp-wide ballot
         for (int base = vbx * blockDim.x; base < n; base += vgx * blockDim.x) {
             const int i = base + threadIdx.x;
-            bool defer = false;
-            int4 entry;
-            long long h = -1;
-            double hocc = 0.0;
             // every streamed field is loaded before alive is looked at, so the
             // loads of a carrier share one memory round trip (slots below
             // n_slots are allocated whether alive or not)
             const bool in = i < n;
             const int ic = in ? i : 0;
             const uint8_t alive = __ldcs(S.alive + ic);
-            uint32_t w = __ldcs(S.mode + ic);
+            const uint32_t w = __ldcs(S.mode + ic);
             const int c0 = __ldcs(S.cell + ic);
             const double occ0 = __ldcs(S.occ + ic);
             float p[3] = {__ldcs(S.ox + ic), __ldcs(S.oy + ic), __ldcs(S.oz + ic)};
-            if (in && alive) {
-                double occ = apply_pending(T, C, c0, w, occ0);
-                const Frame F = cell_frame(T.dom, c0);
-                float remaining = T.par.dt32;
-                int event = 0, plane = -1;
-                const int end =
-                    advance_mixed<true>(T, L, &bl, i, F, p, w, occ, remaining, event, plane, kDrawTransport, step);
-                if (end == kFlightDeferred) {
-                    // state at the wall, cell unchanged (the frame of the flight)
-                    __stcs(S.ox + i, p[0]);
-                    __stcs(S.oy + i, p[1]);
-                    __stcs(S.oz + i, p[2]);
-                    __stcs(S.mode + i, w);
-                    __stcs(S.occ + i, occ);
-                    defer = true;
-                    entry = make_int4(i, __float_as_int(remaining), event, plane);
-                } else {
-                    h = finish_mixed(T, S, C, L, i, F, p, w, occ, end != kFlightAbsorbed);
-                    hocc = occ;
-                }
-            }
-            bin_warp<kAgg, kRta>(C, h, hocc);
-            const unsigned mask = __ballot_sync(0xffffffffu, defer);
-            if (mask) {
-                if (defer) qbuf[warp][queued + __popc(mask & ((1u << lane) - 1u))] = entry;
-                queued += __popc(mask);
-                __syncwarp();
-                if (queued >= 32) {
-                    int at = 0;
-                    if (lane == 0) at = atomicAdd(&L->n_deferred, 32);
-                    at = __shfl_sync(0xffffffffu, at, 0);
-                    if (at + lane < S.capacity) S.deferred[at + lane] = qbuf[warp][lane];
-                    else raise_error(L, kErrInvalidStatistics, i);
-                    __syncwarp();
-                    const int rest = queued - 32;
-                    int4 t = make_int4(0, 0, 0, 0);
-                    if (lane < rest) t = qbuf[warp][32 + lane];
-                    __syncwarp();
-                    if (lane < rest) qbuf[warp][lane] = t;
-                    __syncwarp();
-                    queued = rest;
-                }
-            }
+            mixed_carrier<kRta, kAgg>(T, S, C, L, bl, step, i, in, alive, w, c0, occ0, p, qbuf, queued);
         }
-        if (queued > 0) {
-            int at = 0;
-            if (lane == 0) at = atomicAdd(&L->n_deferred, queued);
-            at = __shfl_sync(0xffffffffu, at, 0);
-            if (lane < queued) {
-                if (at + lane < S.capacity) S.deferred[at + lane] = qbuf[warp][lane];
-                else raise_error(L, kErrInvalidStatistics, at + lane);
-            }
-        }
+        flush_deferred(S, L, qbuf, queued);
     } else {
         // block-uniform trip count so that every lane reaches the warp tally
         for (int base = vbx * blockDim.x; base < n; base += vgx * blockDim.x) {
@@ -904,6 +922,129 @@ __device__ __forceinline__ void k_transport_body(const DevTables& T, CarrierStat
             bin_warp<kAgg, kRta>(C, h, occ);
         }
     }
+    __syncthreads();
+    block_ledger_flush(&bl, L);
+}
+
+// ------------------------------------------- TMA-staged mixed carrier pass
+// The carrier fields of a tile of kPipeTile slots arrive in shared memory by
+// bulk asynchronous copies (cp.async.bulk, completion counted on an mbarrier)
+// one tile ahead: while a CTA flies the carriers of tile k, the copies of
+// tile k + grid are in flight into the other of two stages, so the streamed
+// loads never sit on the dependent chain of a carrier (load -> pending gather
+// -> flight -> store). One elected thread issues the copies; a bounded wait
+// on the stage's barrier phase gives every thread the tile.
+constexpr int kPipeTile = 256;
+
+struct __align__(16) PipeStage {
+    double occ[kPipeTile];
+    uint32_t mode[kPipeTile];
+    int32_t cell[kPipeTile];
+    float ox[kPipeTile], oy[kPipeTile], oz[kPipeTile];
+    uint8_t alive[kPipeTile];
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void bulk_to_shared(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+// Bytes of a tile's field copy: 16-byte multiples (the arrays are padded by a
+// tile past the capacity, so the rounded tail stays inside the allocation).
+__device__ __forceinline__ uint32_t tile_bytes(int count, int size) {
+    return (static_cast<uint32_t>(count * size) + 15u) & ~15u;
+}
+
+__device__ __forceinline__ void issue_tile(const CarrierState& S, int tile, int n, PipeStage* st, uint64_t* bar) {
+    const int first = tile * kPipeTile;
+    const int count = min(kPipeTile, n - first);
+    const uint32_t b8 = tile_bytes(count, 8), b4 = tile_bytes(count, 4), b1 = tile_bytes(count, 1);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(smem_addr(bar)),
+                 "r"(b8 + 5 * b4 + b1)
+                 : "memory");
+    bulk_to_shared(st->occ, S.occ + first, b8, bar);
+    bulk_to_shared(st->mode, S.mode + first, b4, bar);
+    bulk_to_shared(st->cell, S.cell + first, b4, bar);
+    bulk_to_shared(st->ox, S.ox + first, b4, bar);
+    bulk_to_shared(st->oy, S.oy + first, b4, bar);
+    bulk_to_shared(st->oz, S.oz + first, b4, bar);
+    bulk_to_shared(st->alive, S.alive + first, b1, bar);
+}
+
+// Waits for a barrier phase for at most about 2^31 SM clocks (~1 s); false on timeout.
+__device__ __forceinline__ bool wait_phase(uint64_t* bar, uint32_t parity) {
+    const long long t0 = clock64();
+    for (;;) {
+        uint32_t done;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     " selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done)
+                     : "r"(smem_addr(bar)), "r"(parity)
+                     : "memory");
+        if (done) return true;
+        if (clock64() - t0 > (1LL << 31)) return false;
+    }
+}
+
+template <bool kRta, bool kAgg>
+__global__ void __launch_bounds__(kPipeTile) k_transport_pipe(const __grid_constant__ DevTables T, CarrierState S,
+                                                              CellArrays C, DevLedger* L) {
+    __shared__ PipeStage stage[2];
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ int4 qbuf[kPipeTile / 32][kDeferBuffer];
+    __shared__ BlockLedger bl;
+    const uint32_t step = L->step_index;
+    const int n = L->n_slots;
+    const int ntiles = (n + kPipeTile - 1) / kPipeTile;
+    block_ledger_init(&bl);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(&bar[0])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(&bar[1])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        if (static_cast<int>(blockIdx.x) < ntiles) issue_tile(S, blockIdx.x, n, &stage[0], &bar[0]);
+    }
+    __syncthreads();
+    int queued = 0;
+    int k = 0;
+    uint32_t pending = static_cast<int>(blockIdx.x) < ntiles ? 1u : 0u; // stages with copies in flight (bits)
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++k) { // block-uniform
+        const int s = k & 1;
+        const int next = t + static_cast<int>(gridDim.x);
+        if (next < ntiles) {
+            if (threadIdx.x == 0) {
+                // the other stage was read in the previous iteration (ordered by its closing barrier)
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue_tile(S, next, n, &stage[s ^ 1], &bar[s ^ 1]);
+            }
+            pending |= 1u << (s ^ 1);
+        }
+        const bool ok = wait_phase(&bar[s], static_cast<uint32_t>((k >> 1) & 1));
+        if (!__syncthreads_and(ok)) {
+            raise_error(L, kErrPipelineTimeout, t);
+            break;
+        }
+        pending &= ~(1u << s);
+        const int i = t * kPipeTile + static_cast<int>(threadIdx.x);
+        const PipeStage& st = stage[s];
+        float p[3] = {st.ox[threadIdx.x], st.oy[threadIdx.x], st.oz[threadIdx.x]};
+        mixed_carrier<kRta, kAgg>(T, S, C, L, bl, step, i, i < n, st.alive[threadIdx.x], st.mode[threadIdx.x],
+                                  st.cell[threadIdx.x], st.occ[threadIdx.x], p, qbuf, queued);
+        __syncthreads(); // stage s is free for the copies of iteration k + 1
+    }
+    // after a timeout in iteration k: give copies still in flight a bounded
+    // wait before the CTA leaves (stage k & 1 was awaited for iteration k, the
+    // other stage was filled for iteration k + 1)
+    for (int x = 0; x < 2; ++x) {
+        if (!(pending & (1u << x))) continue;
+        const int kk = x == (k & 1) ? k : k + 1;
+        wait_phase(&bar[x], static_cast<uint32_t>((kk >> 1) & 1));
+    }
+    flush_deferred(S, L, qbuf, queued);
     __syncthreads();
     block_ledger_flush(&bl, L);
 }
@@ -1533,6 +1674,12 @@ __global__ void k_reset_pending(const DevTables* __restrict__ Tp, CellArrays C, 
 // ----------------------------------------------------------- launchers
 template <bool kMixed, bool kRta>
 void launch_transport_pass(const LaunchCtx& x, dim3 g) {
+    if (kMixed && x.transport_pipe) {
+        const dim3 gp(x.pipe_grid);
+        if (x.tally_agg) k_transport_pipe<kRta, true><<<gp, kPipeTile, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+        else k_transport_pipe<kRta, false><<<gp, kPipeTile, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+        return;
+    }
     const int threads = x.transport_block;
     const size_t sh = kMixed ? static_cast<size_t>(threads / 32) * kDeferBuffer * sizeof(int4) : 0;
     if (x.tally_agg) k_transport<kMixed, kRta, true><<<g, threads, sh, x.stream>>>(*x.Th, x.S, x.C, x.L);

@@ -19,5 +19,8 @@ constexpr double kSortMinCarriers = 2e+06;
 // Bin tallies of the carrier pass: 1 sums runs of equal (cell, bin) across
 // the lanes of a warp before one FP64 atomic per run, 0 one atomic per carrier.
 constexpr int kTallyAggregation[2] = {1, 1};
+// Mixed carrier pass: carrier tiles staged in shared memory by bulk
+// asynchronous copies one tile ahead (1), or loaded directly (0).
+constexpr int kTransportPipeline = 1;
 } // namespace tuning
 } // namespace phmc

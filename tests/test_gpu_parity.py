@@ -731,3 +731,31 @@ def test_sorted_mixed_path_conserves_energy(gpu):
     scale = abs(st["total_thermal_energy_ev"])
     assert abs(st["step_lifetime_energy_residual_ev"]) < 1e-13 * scale
     assert abs(st["step_energy_balance_residual_ev"]) < 1e-13 * scale
+
+
+@pytest.mark.parametrize("name,stationary", [("inplane_gradient", True), ("cross_plane_film", False)])
+def test_staged_pass_matches_direct_loads(gpu, name, stationary):
+    """The mixed carrier pass with carrier tiles staged in shared memory by bulk
+    asynchronous copies against the same pass with direct loads, on identical
+    draws and 70,001 carriers (a partial last tile): the same carriers, cells
+    and modes, occupations and cell temperatures to bin-sum rounding."""
+    mat = synthetic.make_material(mesh=16)
+    m = abi.Material(gpu, "phmc_", mat, 0.1, stationary, False)
+    base = workloads.scaled(getattr(workloads, name)(precision="mixed"), 70001, random_seed=29,
+                            carrier_sort_interval=3)
+    runs = []
+    for pipe in (1, -1):
+        s = abi.Solver(gpu, "phmc_", dict(base, transport_pipeline=pipe), [m])
+        s.run(7)
+        runs.append((s.carriers(), s.cells()[0], s.stats()))
+    (ca, Ta, sa), (cb, Tb, sb) = runs
+    assert np.array_equal(ca["alive"], cb["alive"])
+    a = ca["alive"] == 1
+    assert np.array_equal(ca["mode"][a], cb["mode"][a])
+    assert np.array_equal(ca["cell"][a], cb["cell"][a])
+    for k in ("x", "y", "z"):
+        assert np.array_equal(ca[k][a], cb[k][a]), k
+    assert np.allclose(ca["occ"][a], cb["occ"][a], rtol=1e-12, atol=1e-14)
+    assert np.allclose(Ta, Tb, rtol=1e-12, atol=0)
+    for k in ("particle_count", "absorbed_total", "injected_total", "rough_counts"):
+        assert sa[k] == sb[k], k
