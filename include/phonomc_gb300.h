@@ -156,6 +156,13 @@ typedef struct phmc_config {
     int32_t tally_aggregation;       /* 1: warp-summed bin tallies, < 0: one atomic per carrier */
     int32_t transport_pipeline;      /* mixed state: 1 carrier tiles staged in shared memory by bulk
                                         asynchronous copies, < 0 direct loads */
+    /* [materials] interface model (include/SimulationConfig.h:93-99):
+     * 0 diffuse mismatch (dmm), 1 acoustic mismatch (amm), 2 mixed (mmm) */
+    int32_t interface_model;
+    double interface_amm_fraction;        /* mmm: acoustic-model probability per event */
+    double interface_parallel_bin_inv_a;  /* amm search bins in k parallel, 1/Angstrom (0: 0.05) */
+    int32_t n_mass_densities;
+    const double* mass_densities_kg_m3;   /* one per material (amm, mmm) */
 } phmc_config;
 
 /* Getters of include/MonteCarloSolver.h:59-101 plus the last step's ledger. */

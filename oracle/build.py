@@ -12,7 +12,8 @@ ROOT = os.path.dirname(HERE)
 OUT = os.path.join(HERE, "_build", "liboracle.so")
 SOURCES = [os.path.join(HERE, "phmc_oracle.cpp"),
            os.path.join(ROOT, "phonomc_gb300", "csrc", "phmc_host.cpp"),
-           os.path.join(ROOT, "phonomc_gb300", "csrc", "phmc_mesh.cpp")]
+           os.path.join(ROOT, "phonomc_gb300", "csrc", "phmc_mesh.cpp"),
+           os.path.join(ROOT, "phonomc_gb300", "csrc", "phmc_amm.cpp")]
 DEPS = SOURCES + [os.path.join(ROOT, "phonomc_gb300", "csrc", f)
                   for f in ("phmc_host.h", "phmc_pod.h", "phmc_rng.h", "phmc_tuning.h")] + [
     os.path.join(ROOT, "include", "phonomc_gb300.h")]

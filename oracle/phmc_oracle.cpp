@@ -336,7 +336,7 @@ struct InterfaceOutcome {
 // transmitted draw, transmission test, occupation remap conserving w ω Δn.
 // Uniforms are consumed in the reference's order from u[0..2].
 InterfaceOutcome interface_interact(const InterfaceTables& I, const std::vector<MaterialTables>& mats, int src, int a,
-                                    uint32_t signs, double occ, int next, const double u[3]) {
+                                    uint32_t signs, double occ, int next, const double u[4]) {
     InterfaceOutcome r;
     r.material = src;
     r.active = a;
@@ -348,16 +348,49 @@ InterfaceOutcome interface_interact(const InterfaceTables& I, const std::vector<
     const double v_axis = ((signs >> axis) & 1u) ? -S.vel[3 * a + axis] : S.vel[3 * a + axis];
     const int incident = v_axis > 0.0 ? 1 : 0;
     int k = 0;
-    bool drew;
-    double source_flux = 0, target_flux = 0;
-    const int reflected = interface_sample_band(I.banks[src][1 - incident], omega, I.band_width, u[k], drew, source_flux);
-    if (drew) ++k;
-    const int transmitted = interface_sample_band(I.banks[next][incident], omega, I.band_width, u[k], drew, target_flux);
-    if (drew) ++k;
-    const double transmission = target_flux > 0 ? target_flux / std::max(1e-300, source_flux + target_flux) : 0;
-    const bool transmit = transmitted >= 0 && u[k] < transmission;
-    const int sel_material = transmit ? next : src;
-    const int sel = transmit ? transmitted : reflected;
+    // model choice (mixed mismatch), src/solver/InterfaceInteraction.cpp:60-67
+    const double acoustic_p = I.model == 1 ? 1.0 : (I.model == 2 ? I.amm_fraction : 0.0);
+    const bool use_amm = acoustic_p >= 1 || (acoustic_p > 0 && u[k++] < acoustic_p);
+    bool transmit;
+    int sel_material, sel;
+    if (use_amm) {
+        r.events = 1;
+        if (std::abs(v_axis) < 1e-7) { // :68-74
+            r.signs ^= 1u << axis;
+            r.reflected = 1;
+            r.action = kInterfaceReflect;
+            return r;
+        }
+        // AcousticInterfaceSampler::sample, src/solver/AcousticInterfaceSampler.cpp:448-470
+        const AmmRow& row = I.amm.faces.at(std::min(src, next)).rows[src < next ? 0 : 1].at(a);
+        if (row.reflected < 0) {
+            r.action = kInterfaceAmmRow;
+            return r;
+        }
+        double x = u[k++];
+        int chosen = -1;
+        for (const auto& e : row.transmitted) {
+            x -= e.second;
+            if (x < 0) {
+                chosen = e.first;
+                break;
+            }
+        }
+        transmit = chosen >= 0;
+        sel_material = transmit ? next : src;
+        sel = transmit ? chosen : row.reflected;
+    } else {
+        bool drew;
+        double source_flux = 0, target_flux = 0;
+        const int reflected = interface_sample_band(I.banks[src][1 - incident], omega, I.band_width, u[k], drew, source_flux);
+        if (drew) ++k;
+        const int transmitted = interface_sample_band(I.banks[next][incident], omega, I.band_width, u[k], drew, target_flux);
+        if (drew) ++k;
+        const double transmission = target_flux > 0 ? target_flux / std::max(1e-300, source_flux + target_flux) : 0;
+        transmit = transmitted >= 0 && u[k] < transmission;
+        sel_material = transmit ? next : src;
+        sel = transmit ? transmitted : reflected;
+    }
     r.events = 1;
     if (sel < 0) {
         if (I.linearized) {
@@ -929,13 +962,14 @@ struct OracleSolver {
                                      static_cast<uint32_t>(event), 0);
         const Uniform2 d1 = uniform2(P.cfg.random_seed, static_cast<uint32_t>(i), static_cast<uint32_t>(step), purpose,
                                      static_cast<uint32_t>(event), 1);
-        const double u[3] = {d0.a, d0.b, d1.a};
+        const double u[4] = {d0.a, d0.b, d1.a, d1.b};
         const InterfaceOutcome r = interface_interact(P.iface, P.mats, static_cast<int>(w >> 28),
                                                       static_cast<int>(w & kActiveMask), (w >> 24) & 7u, occ[i],
                                                       destination, u);
         iface_events += r.events;
         iface_transmitted += r.transmitted;
         iface_reflected += r.reflected;
+        if (r.action == kInterfaceAmmRow) fail("AMM incoming state is tangent or unsupported.");
         if (r.action == kInterfaceFail)
             fail("Full-matrix boundary mode mapping failed while advancing particles for particle " + std::to_string(i) +
                  ". An inward discrete material mode and finite signed energy weight are required; no velocity-only "
@@ -1721,12 +1755,80 @@ int orc_interface(void* ma, void* mb, double wa, double wb, int axis, double bin
         for (int64_t i = 0; i < n; ++i) {
             const int m = src[i];
             const int a = M[m]->active_index_for_flat(flat_in[i]);
+            const double u[4] = {u3[3 * i], u3[3 * i + 1], u3[3 * i + 2], 0.0};
             const InterfaceOutcome r = interface_interact(I, T, m, a, static_cast<uint32_t>(signs_in[i]), occ_in[i], 1 - m,
-                                                          u3 + 3 * i);
+                                                          u);
             action[i] = r.action;
             material_out[i] = r.material;
             flat_out[i] = M[r.material]->active_flat()[r.active];
             signs_out[i] = static_cast<int32_t>(r.signs);
+            occ_out[i] = r.occ;
+        }
+    });
+}
+
+// Acoustic-mismatch rows of one side of the a|b interface normal to z
+// (AcousticInterfaceSampler::configure / row): reflected partner and the
+// transmitted entries [start[a], start[a+1]) of every active mode; dest / prob
+// may be NULL to read the sizes first (start has n_active + 1 entries).
+int orc_amm_rows(void* ma, void* mb, double rho_a, double rho_b, double bin_thz, double bin_k, int side,
+                 int32_t* reflected, int32_t* start, int32_t* dest, double* prob) {
+    return guard([&] {
+        const PhononMaterial* M[2] = {static_cast<OracleMaterial*>(ma)->m.get(), static_cast<OracleMaterial*>(mb)->m.get()};
+        AmmTables A;
+        A.build({M[0], M[1]}, 2, {rho_a, rho_b}, bin_thz, bin_k);
+        const auto& rows = A.faces.at(0).rows[side];
+        int at = 0;
+        start[0] = 0;
+        for (size_t a = 0; a < rows.size(); ++a) {
+            reflected[a] = rows[a].reflected;
+            for (const auto& e : rows[a].transmitted) {
+                if (dest) dest[at] = e.first;
+                if (prob) prob[at] = e.second;
+                ++at;
+            }
+            start[a + 1] = at;
+        }
+    });
+}
+
+// Interface events with the acoustic (model 1) or mixed (model 2) mismatch
+// model between materials a and b (z axis), uniforms u[4 i .. 4 i + 3] in the
+// order InterfaceInteraction::interact consumes them.
+int orc_interface_model(void* ma, void* mb, double wa, double wb, double bin_thz, double Tref, int linearized,
+                        int model, double fraction, double rho_a, double rho_b, double bin_k, int64_t n,
+                        const int32_t* src, const int32_t* flat_in, const double* occ_in, const double* u4,
+                        int32_t* action, int32_t* material_out, int32_t* flat_out, double* occ_out) {
+    return guard([&] {
+        const PhononMaterial* M[2] = {static_cast<OracleMaterial*>(ma)->m.get(), static_cast<OracleMaterial*>(mb)->m.get()};
+        InterfaceTables I;
+        I.enabled = true;
+        I.linearized = linearized != 0;
+        I.reference_temperature = Tref;
+        I.band_width = 2.0 * std::acos(-1.0) * bin_thz;
+        I.build({M[0], M[1]}, 2);
+        I.model = model;
+        I.amm_fraction = model == 1 ? 1.0 : fraction;
+        I.amm.build({M[0], M[1]}, 2, {rho_a, rho_b}, bin_thz, bin_k);
+        std::vector<MaterialTables> T(2);
+        const double w[2] = {wa, wb};
+        for (int k = 0; k < 2; ++k) {
+            T[k].n_active = M[k]->active_mode_count();
+            T[k].energy_weight = w[k];
+            for (int a = 0; a < T[k].n_active; ++a) {
+                const int f = M[k]->active_flat()[a];
+                T[k].omega.push_back(M[k]->omega(f));
+                T[k].nbg.push_back(M[k]->bose_occupation(Tref, f));
+                for (int c = 0; c < 3; ++c) T[k].vel.push_back(M[k]->velocity(f)[c]);
+            }
+        }
+        for (int64_t i = 0; i < n; ++i) {
+            const int m = src[i];
+            const int a = M[m]->active_index_for_flat(flat_in[i]);
+            const InterfaceOutcome r = interface_interact(I, T, m, a, 0u, occ_in[i], 1 - m, u4 + 4 * i);
+            action[i] = r.action;
+            material_out[i] = r.material;
+            flat_out[i] = M[r.material]->active_flat()[r.active];
             occ_out[i] = r.occ;
         }
     });

@@ -23,6 +23,7 @@
 #include "solver/CarrierCollisionOperator.h"
 #include "solver/CellParticleIndex.h"
 #include "solver/InterfaceInteraction.h"
+#include "solver/AcousticInterfaceSampler.h"
 #include "solver/PhononSourceOperator.h"
 #include "SurfaceMesh.h"
 #include "geometry/MeshReader.h"
@@ -585,6 +586,113 @@ std::string cmd_interface(const std::string& pa, const std::string& pb, bool lin
     return j.str();
 }
 
+// amm <pmat a> <pmat b> <model 1 amm|2 mmm> <amm fraction> <linearized>:
+// acoustic-mismatch rows of both sides of the a|b interface (AcousticInterfaceSampler::row
+// for every active mode) and InterfaceInteraction::interact events with the
+// uniforms each consumed (up to four), densities 2329 / 5323 kg/m^3, axis z.
+std::string cmd_amm(const std::string& pa, const std::string& pb, int model, double fraction, bool linearized) {
+    PhononMaterial ma(read_pmat(pa), 0.1, false, false), mb(read_pmat(pb), 0.1, false, false);
+    const double wa = 1.375e-3, wb = 0.8125e-3;
+    phonomc::InterfaceInteractionConfig cfg;
+    cfg.axis = 2;
+    cfg.enabled = true;
+    cfg.linearized = linearized;
+    cfg.model = model == 1 ? InterfaceModel::AcousticMismatch : InterfaceModel::MixedMismatch;
+    cfg.amm_fraction = fraction;
+    cfg.frequency_bin_thz = 0.1;
+    cfg.parallel_bin_inv_a = 0.05;
+    cfg.mass_densities_kg_m3 = {2329.0, 5323.0};
+    cfg.reference_temperature = 300.0;
+    phonomc::InterfaceInteraction I;
+    I.configure(cfg, {&ma, &mb}, {wa, wb});
+    phonomc::AcousticInterfaceSampler S;
+    S.configure({&ma, &mb}, 2, cfg.mass_densities_kg_m3, cfg.frequency_bin_thz, cfg.parallel_bin_inv_a);
+    Json j;
+    const PhononMaterial* mats[2] = {&ma, &mb};
+    for (int side = 0; side < 2; ++side) {
+        std::vector<int> refl, start{0}, dest;
+        std::vector<double> prob;
+        for (int a = 0; a < mats[side]->active_mode_count(); ++a) {
+            const auto& r = S.row(side, 1 - side, a);
+            refl.push_back(r.reflected);
+            for (const auto& e : r.transmitted) {
+                dest.push_back(e.active);
+                prob.push_back(e.probability);
+            }
+            start.push_back(static_cast<int>(dest.size()));
+        }
+        const std::string k = std::to_string(side);
+        j.arr("reflected_" + k, refl);
+        j.arr("start_" + k, start);
+        j.arr("dest_" + k, dest);
+        j.arr("prob_" + k, prob);
+    }
+    std::mt19937_64 pick(91);
+    std::uniform_real_distribution<double> U(0, 1);
+    std::vector<int> src, in_flat, in_signs, action, out_material, out_flat, ndraw, events, transmitted, reflected;
+    std::vector<double> in_occ, out_occ, draws;
+    for (int i = 0; i < 4000; ++i) {
+        const int m = i % 2;
+        const PhononMaterial& M = *mats[m];
+        const int a = static_cast<int>(U(pick) * M.active_mode_count());
+        const auto mode = M.active_mode_at(a);
+        // the carrier moves with its mode's own velocity, toward the other layer
+        // (acoustic rows exist only for those states)
+        const auto v = M.mode_group_velocity(mode);
+        if (std::abs(v[2]) <= 1e-12 || (v[2] > 0) != (m == 0)) continue;
+        const int signs = 0;
+        const double occ = linearized ? M.bose_occupation(300.0, mode) + (U(pick) - 0.5) * 0.02
+                                      : M.bose_occupation(300.0 + 8.0 * (U(pick) - 0.5), mode);
+        phonomc::BoundaryState st{mode, m, v, M.mode_angular_frequency(mode), occ};
+        std::mt19937_64 eng(7000 + i), copy = eng;
+        const auto r = I.interact(st, 1 - m, eng);
+        int used = 0;
+        std::vector<double> u;
+        while (!(copy == eng) && used < 8) {
+            u.push_back(std::generate_canonical<double, 53>(copy));
+            ++used;
+        }
+        src.push_back(m);
+        in_flat.push_back(mode[0] * M.branch_count() + mode[1]);
+        in_signs.push_back(signs);
+        in_occ.push_back(occ);
+        action.push_back(static_cast<int>(r.action));
+        out_material.push_back(r.state.material);
+        const PhononMaterial& D = *mats[r.state.material];
+        out_flat.push_back(r.state.mode[0] * D.branch_count() + r.state.mode[1]);
+        out_occ.push_back(r.state.occupation);
+        events.push_back(static_cast<int>(r.interface_events));
+        transmitted.push_back(static_cast<int>(r.interface_transmitted));
+        reflected.push_back(static_cast<int>(r.interface_reflected));
+        ndraw.push_back(used);
+        for (int k = 0; k < 4; ++k) draws.push_back(k < used ? u[k] : -1.0);
+    }
+    j.put("weight_a", wa);
+    j.put("weight_b", wb);
+    j.put("frequency_bin_thz", 0.1);
+    j.put("parallel_bin_inv_a", 0.05);
+    j.put("density_a", 2329.0);
+    j.put("density_b", 5323.0);
+    j.put("amm_fraction", fraction);
+    j.put_i("model", model);
+    j.put("reference_temperature", 300.0);
+    j.put_i("axis", 2);
+    j.arr("src", src);
+    j.arr("in_flat", in_flat);
+    j.arr("in_signs", in_signs);
+    j.arr("in_occ", in_occ);
+    j.arr("action", action);
+    j.arr("out_material", out_material);
+    j.arr("out_flat", out_flat);
+    j.arr("out_occ", out_occ);
+    j.arr("events", events);
+    j.arr("transmitted", transmitted);
+    j.arr("reflected", reflected);
+    j.arr("ndraw", ndraw);
+    j.arr("draws", draws);
+    return j.str();
+}
+
 // source <pmat> <spectrum 0 thermal|1 weighted|2 gaussian> <linearized>:
 // PrescribedHeatSource cell powers of a Gaussian source in a 2x2x3 box, one
 // accrual, then PhononSourceOperator::apply on random carriers.
@@ -996,6 +1104,8 @@ int main(int argc, char** argv) {
         else if (c == "source") out = cmd_source(argv[2], std::atoi(argv[3]), std::atoi(argv[4]) != 0);
         else if (c == "interface") out = cmd_interface(argv[2], argv[3], std::atoi(argv[4]) != 0);
         else if (c == "reservoir") out = cmd_reservoir(argv[2]);
+        else if (c == "amm")
+            out = cmd_amm(argv[2], argv[3], std::atoi(argv[4]), std::atof(argv[5]), std::atoi(argv[6]) != 0);
         else if (c == "run") out = cmd_run(argv[2], argv[3], std::atoi(argv[4]));
         else if (c == "ncallaway")
             out = cmd_ncallaway(std::atoi(argv[2]), std::atoi(argv[3]), std::atoi(argv[4]), std::atoi(argv[5]));

@@ -156,6 +156,9 @@ class ConfigPOD(C.Structure):
         ("carrier_sort_interval", C.c_int32), ("transport_block", C.c_int32),
         ("transport_blocks_per_sm", C.c_int32), ("tally_aggregation", C.c_int32),
         ("transport_pipeline", C.c_int32),
+        ("interface_model", C.c_int32), ("interface_amm_fraction", C.c_double),
+        ("interface_parallel_bin_inv_a", C.c_double), ("n_mass_densities", C.c_int32),
+        ("mass_densities_kg_m3", c_double_p),
     ]
 
 
@@ -241,6 +244,13 @@ def config_pod(cfg: dict):
     c.transport_blocks_per_sm = int(cfg.get("transport_blocks_per_sm", 0))
     c.tally_aggregation = int(cfg.get("tally_aggregation", 0))
     c.transport_pipeline = int(cfg.get("transport_pipeline", 0))
+    c.interface_model = {"dmm": 0, "amm": 1, "mmm": 2}[cfg.get("interface_model", "dmm")]
+    c.interface_amm_fraction = float(cfg.get("interface_amm_fraction", 0.0))
+    c.interface_parallel_bin_inv_a = float(cfg.get("interface_parallel_bin_inv_a", 0.0))
+    rho = np.ascontiguousarray(cfg.get("mass_densities_kg_m3", []), dtype=np.float64)
+    keep.append(rho)
+    c.n_mass_densities = int(rho.size)
+    c.mass_densities_kg_m3 = dptr(rho) if rho.size else None
     c.transport_axis = int(cfg.get("transport_axis", -1))
     g = cfg.get("temperature_gradient")
     c.has_temperature_gradient = int(g is not None)
@@ -492,6 +502,11 @@ SUBSTEP_PROTOS = {
 }
 
 ORACLE_EXTRA_PROTOS = {
+    "amm_rows": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
+                           c_int32_p, c_int32_p, c_int32_p, c_double_p]),
+    "interface_model": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
+                                  C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int64, c_int32_p,
+                                  c_int32_p, c_double_p, c_double_p, c_int32_p, c_int32_p, c_int32_p, c_double_p]),
     "material_query": (C.c_int, [C.c_void_p, C.c_int, C.c_int64, c_int32_p, c_double_p, C.c_double, c_double_p]),
     "material_scalars": (C.c_int, [C.c_void_p, C.c_double, c_double_p, c_int32_p]),
     "grid_index": (C.c_int, [c_double_p, c_int32_p, C.c_int64, c_double_p, c_int32_p]),

@@ -186,7 +186,7 @@ __global__ void k_interface_rays(const __grid_constant__ DevTables T, int64_t n,
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         const IfaceOut r = interface_dev(T, src[i], ain[i], static_cast<uint32_t>(signs[i]), occ[i], 1 - src[i],
-                                         u3[3 * i], u3[3 * i + 1], u3[3 * i + 2]);
+                                         u3[3 * i], u3[3 * i + 1], u3[3 * i + 2], 0.0);
         action[i] = r.action;
         mat[i] = r.material;
         aout[i] = r.active;

@@ -58,6 +58,7 @@ enum ErrorCode : int {
     kErrNclInvalid = 16,
     kErrNclTemperature = 17,
     kErrPipelineTimeout = 18,
+    kErrAmmRow = 19,
 };
 
 struct DevMaterial {
@@ -221,10 +222,22 @@ struct DevInterfaceBank {
     const double* prefix; // n + 1
     int n;
 };
+// Acoustic-mismatch rows of one side of one interface (src/solver/AcousticInterfaceSampler.cpp):
+// per incoming active mode its mirror partner (-1: not incoming) and the
+// transmitted entries [start[a], start[a+1]) as (destination active, probability).
+struct DevAmmRows {
+    const int* reflected;
+    const int* start;
+    const int* dest;
+    const double* prob;
+};
 struct DevInterface {
     int enabled, linearized, axis;
     double band_width;
     DevInterfaceBank bank[kMaxMaterials][2];
+    int model;             // 0 dmm, 1 amm, 2 mmm
+    double amm_fraction;   // acoustic-model probability per event
+    DevAmmRows amm[kMaxMaterials - 1][2];
 };
 
 // Face BVH node: bounds, children (-1 for a leaf) and the record range of a leaf.
@@ -595,17 +608,19 @@ __device__ __forceinline__ int interface_band_dev(const DevInterfaceBank& B, dou
 }
 
 struct IfaceOut {
-    int action; // 3 reflect, 4 transmit, 5 fail
+    int action; // 3 reflect, 4 transmit, 5 fail, 6 acoustic row missing (tangent or unsupported state)
     int material, active;
     uint32_t signs;
     double occ;
     int transmitted;
 };
 
-// src/solver/InterfaceInteraction.cpp:46-153, diffuse mismatch, uniforms
-// consumed in the reference's order from u[0..2].
+// src/solver/InterfaceInteraction.cpp:46-153 with uniforms consumed in the
+// reference's order: the model choice (mixed mismatch only), then either the
+// acoustic row (AcousticInterfaceSampler::sample) or the diffuse-mismatch
+// reflected band, transmitted band and transmission draws.
 __device__ __forceinline__ IfaceOut interface_dev(const DevTables& T, int src, int a, uint32_t signs, double occ,
-                                                  int next, double u0, double u1, double u2) {
+                                                  int next, double u0, double u1, double u2, double u3) {
     const DevInterface& I = T.iface;
     const DevMaterial& S = T.mat[src];
     IfaceOut r;
@@ -618,20 +633,49 @@ __device__ __forceinline__ IfaceOut interface_dev(const DevTables& T, int src, i
     const double omega = S.omega[a];
     const double v_axis = ((signs >> axis) & 1u) ? -S.vel[3 * a + axis] : S.vel[3 * a + axis];
     const int incident = v_axis > 0.0 ? 1 : 0;
-    const double u[3] = {u0, u1, u2};
+    const double u[4] = {u0, u1, u2, u3};
     int k = 0;
-    bool drew;
-    double source_flux = 0, target_flux = 0;
-    const int refl = interface_band_dev(I.bank[src][1 - incident], omega, I.band_width, u[k], drew, source_flux);
-    if (drew) ++k;
-    const int trans = interface_band_dev(I.bank[next][incident], omega, I.band_width, k < 3 ? u[k] : 0.0, drew,
-                                         target_flux);
-    if (drew) ++k;
-    const double transmission =
-        target_flux > 0 ? target_flux / fmax(1e-300, __dadd_rn(source_flux, target_flux)) : 0.0;
-    const bool transmit = trans >= 0 && (k < 3 ? u[k] : 1.0) < transmission;
-    const int sel_material = transmit ? next : src;
-    const int sel = transmit ? trans : refl;
+    const double acoustic_p = I.model == 1 ? 1.0 : (I.model == 2 ? I.amm_fraction : 0.0);
+    const bool use_amm = acoustic_p >= 1.0 || (acoustic_p > 0.0 && u[k++] < acoustic_p);
+    bool transmit;
+    int sel_material, sel;
+    if (use_amm) {
+        if (fabs(v_axis) < 1e-7) { // tangent: mirrored in the interface plane
+            r.signs ^= 1u << axis;
+            r.action = 3;
+            return r;
+        }
+        const DevAmmRows& R = I.amm[src < next ? src : next][src < next ? 0 : 1];
+        const int refl = R.reflected[a];
+        if (refl < 0) {
+            r.action = 6;
+            return r;
+        }
+        double x = u[k++];
+        int chosen = -1;
+        for (int e = R.start[a]; e < R.start[a + 1]; ++e) {
+            x = __dadd_rn(x, -R.prob[e]);
+            if (x < 0.0) {
+                chosen = R.dest[e];
+                break;
+            }
+        }
+        transmit = chosen >= 0;
+        sel_material = transmit ? next : src;
+        sel = transmit ? chosen : refl;
+    } else {
+        bool drew;
+        double source_flux = 0, target_flux = 0;
+        const int refl = interface_band_dev(I.bank[src][1 - incident], omega, I.band_width, u[k], drew, source_flux);
+        if (drew) ++k;
+        const int trans = interface_band_dev(I.bank[next][incident], omega, I.band_width, u[k], drew, target_flux);
+        if (drew) ++k;
+        const double transmission =
+            target_flux > 0 ? target_flux / fmax(1e-300, __dadd_rn(source_flux, target_flux)) : 0.0;
+        transmit = trans >= 0 && u[k] < transmission;
+        sel_material = transmit ? next : src;
+        sel = transmit ? trans : refl;
+    }
     if (sel < 0) {
         if (I.linearized) {
             r.action = 5;

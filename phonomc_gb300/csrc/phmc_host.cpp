@@ -1264,11 +1264,31 @@ Problem build_problem(const SimulationConfig& cfg, SimulationDomain& domain,
     P.iface.linearized = P.linearized;
     P.iface.reference_temperature = Tbg;
     P.iface.band_width = 2.0 * std::acos(-1.0) * cfg.material_interface_frequency_bin_thz;
+    // materials.interface_model checks of src/config/ConfigValidation.cpp:109-140
+    const int model = cfg.material_interface_model;
+    const double fraction = model == 1 ? 1.0 : cfg.material_interface_amm_fraction;
+    if (model < 0 || model > 2) throw std::runtime_error("materials.interface_model must be dmm, amm or mmm.");
+    if (!std::isfinite(cfg.material_interface_amm_fraction) || cfg.material_interface_amm_fraction < 0 ||
+        cfg.material_interface_amm_fraction > 1)
+        throw std::runtime_error("materials.interface_amm_fraction must be in [0,1].");
+    if (!std::isfinite(cfg.material_interface_parallel_bin_inv_a) || cfg.material_interface_parallel_bin_inv_a <= 0)
+        throw std::runtime_error("materials.interface_parallel_bin_inv_a must be finite and positive.");
+    if (model == 0 && cfg.material_interface_amm_fraction != 0)
+        throw std::runtime_error("DMM cannot have nonzero AMM fraction.");
+    const bool acoustic = model == 1 || (model == 2 && fraction > 0);
+    if (acoustic) {
+        if (mats.size() < 2 || cfg.material_mass_densities_kg_m3.size() != mats.size())
+            throw std::runtime_error("AMM/MMM requires one mass density per material layer.");
+        for (double rho : cfg.material_mass_densities_kg_m3)
+            if (!std::isfinite(rho) || rho <= 0) throw std::runtime_error("Material mass densities must be finite and positive.");
+    }
     if (P.iface.enabled) {
-        if (cfg.material_interface_model != 0)
-            throw std::runtime_error("Only the diffuse-mismatch interface model (materials.interface_model = dmm) "
-                                     "is built.");
         P.iface.build(mats, P.layout.axis);
+        P.iface.model = model;
+        P.iface.amm_fraction = model == 0 ? 0.0 : fraction;
+        if (acoustic)
+            P.iface.amm.build(mats, P.layout.axis, cfg.material_mass_densities_kg_m3,
+                              cfg.material_interface_frequency_bin_thz, cfg.material_interface_parallel_bin_inv_a);
     }
 
     // Reservoirs (src/solver/ReservoirInitialization.cpp:1-45, ReservoirSampler.cpp:17-101).

@@ -95,7 +95,10 @@ struct SimulationConfig {
     int material_interface_axis = 0;
     std::vector<double> material_interface_positions; // Angstrom
     double material_interface_frequency_bin_thz = 0.1;
-    int material_interface_model = 0; // 0 = diffuse mismatch (dmm)
+    int material_interface_model = 0; // 0 = diffuse mismatch (dmm), 1 = acoustic (amm), 2 = mixed (mmm)
+    double material_interface_amm_fraction = 0.0;      // mmm: acoustic-model probability per event
+    double material_interface_parallel_bin_inv_a = 0.05; // amm search bins in k parallel
+    std::vector<double> material_mass_densities_kg_m3; // one per material (amm / mmm)
     // Prescribed lattice heat source (include/SimulationConfig.h:103-139), lengths in Angstrom.
     bool heat_source_enabled = false;
     std::vector<double> heat_source_min, heat_source_max;
@@ -198,6 +201,8 @@ public:
     const std::vector<double>& lookup_E() const { return table_E_; }
     const std::vector<double>& temperature_samples() const { return temps_; }
     const std::vector<double>& gamma_total() const { return gamma_total_; }
+    const std::array<int, 3>& q_mesh() const { return mesh_; }
+    const std::array<Vec3, 3>& reciprocal_lattice() const { return reciprocal_; }
 
     static double interp_linear_clamped(const std::vector<double>& xs, const std::vector<double>& ys,
                                         double x);
@@ -421,6 +426,27 @@ struct InterfaceBank {
     std::vector<double> prefix; // size + 1
 };
 
+// Acoustic-mismatch rows (src/solver/AcousticInterfaceSampler.cpp:18-472): for
+// each incoming active mode of one side of an interface, its mirror partner
+// (the specular reflection) and the transmitted (destination active mode,
+// probability) entries; rows of modes that do not move into the interface
+// stay empty (reflected = -1).
+struct AmmRow {
+    int reflected = -1;
+    double flux = 0;
+    std::vector<std::pair<int, double>> transmitted;
+};
+struct AmmFace {
+    std::array<std::vector<AmmRow>, 2> rows; // [0]: lower material moving +axis, [1]: upper moving -axis
+};
+struct AmmTables {
+    std::vector<AmmFace> faces; // between material f and f + 1
+    // densities kg/m^3 per material; df in THz, dk in 1/Angstrom (search bins only)
+    void build(const std::vector<const PhononMaterial*>& mats, int axis, const std::vector<double>& densities,
+               double df, double dk);
+    static double transmission(double z1, double z2, double c1, double c2);
+};
+
 struct InterfaceTables {
     bool enabled = false;
     bool linearized = false;
@@ -428,11 +454,15 @@ struct InterfaceTables {
     double band_width = 0;            // 2 pi * frequency bin (rad/ps)
     double reference_temperature = 300;
     std::vector<std::array<InterfaceBank, 2>> banks; // [material][direction]
+    // materials.interface_model: 0 diffuse (dmm), 1 acoustic (amm), 2 mixed (mmm)
+    int model = 0;
+    double amm_fraction = 0;  // probability of the acoustic model per event (1 for amm)
+    AmmTables amm;
     void build(const std::vector<const PhononMaterial*>& mats, int axis);
 };
 
 // Outcome of one interface event (src/solver/InterfaceInteraction.cpp:46-153).
-enum InterfaceAction { kInterfaceReflect = 3, kInterfaceTransmit = 4, kInterfaceFail = 5 };
+enum InterfaceAction { kInterfaceReflect = 3, kInterfaceTransmit = 4, kInterfaceFail = 5, kInterfaceAmmRow = 6 };
 
 // -------------------------------------------------------- rough tables
 struct RoughTable {

@@ -142,6 +142,11 @@ inline SimulationConfig config_from_pod(const phmc_config& c) {
     s.transport_blocks_per_sm = c.transport_blocks_per_sm;
     s.tally_aggregation = c.tally_aggregation;
     s.transport_pipeline = c.transport_pipeline;
+    s.material_interface_model = c.interface_model;
+    s.material_interface_amm_fraction = c.interface_amm_fraction;
+    if (c.interface_parallel_bin_inv_a != 0) s.material_interface_parallel_bin_inv_a = c.interface_parallel_bin_inv_a;
+    if (c.n_mass_densities > 0 && c.mass_densities_kg_m3)
+        s.material_mass_densities_kg_m3.assign(c.mass_densities_kg_m3, c.mass_densities_kg_m3 + c.n_mass_densities);
     if (c.material_folder) s.material_folder = c.material_folder;
     s.material_interface_axis = c.material_interface_axis;
     if (c.n_interfaces > 0 && c.material_interface_positions)

@@ -57,6 +57,8 @@ static const char* error_message(int code) {
     case kErrNclInvalid: return "Nonlinear Callaway occupation is invalid";
     case kErrNclTemperature: return "Nonlinear Callaway temperature is outside the supplied N/U table";
     case kErrPipelineTimeout: return "Carrier tile copies did not complete within the wait limit.";
+    // src/solver/AcousticInterfaceSampler.cpp:459-461
+    case kErrAmmRow: return "AMM incoming state is tangent or unsupported.";
     default: return "Unknown device error.";
     }
 }
@@ -418,6 +420,23 @@ void DeviceSolver::upload_tables() {
             I.bank[m][dir].active = upload(B.active);
             I.bank[m][dir].prefix = upload(B.prefix);
             I.bank[m][dir].n = static_cast<int>(B.omega.size());
+        }
+    I.model = P_.iface.model;
+    I.amm_fraction = P_.iface.amm_fraction;
+    for (size_t f = 0; f < P_.iface.amm.faces.size(); ++f)
+        for (int side = 0; side < 2; ++side) {
+            const auto& rows = P_.iface.amm.faces[f].rows[side];
+            std::vector<int> refl, start{0}, dest;
+            std::vector<double> prob;
+            for (const AmmRow& r : rows) {
+                refl.push_back(r.reflected);
+                for (const auto& e : r.transmitted) {
+                    dest.push_back(e.first);
+                    prob.push_back(e.second);
+                }
+                start.push_back(static_cast<int>(dest.size()));
+            }
+            I.amm[f][side] = {upload(refl), upload(start), upload(dest), upload(prob)};
         }
     // params
     DevParams& p = T.par;

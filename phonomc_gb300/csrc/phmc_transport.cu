@@ -172,10 +172,10 @@ __device__ bool advance_carrier(const DevTables& T, DevLedger* L, BlockLedger* b
             for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], t_cross));
             const Uniform2 d0 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose, static_cast<uint32_t>(event), 0);
             const Uniform2 d1 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose, static_cast<uint32_t>(event), 1);
-            const IfaceOut r = interface_dev(T, mid, ai, (w >> 24) & 7u, occ, destination, d0.a, d0.b, d1.a);
+            const IfaceOut r = interface_dev(T, mid, ai, (w >> 24) & 7u, occ, destination, d0.a, d0.b, d1.a, d1.b);
             count_interface(bl, r);
-            if (r.action == 5) {
-                raise_error(L, kErrModeMapping, slot);
+            if (r.action >= 5) {
+                raise_error(L, r.action == 6 ? kErrAmmRow : kErrModeMapping, slot);
                 return true;
             }
             w = static_cast<uint32_t>(r.active) | (r.signs << 24) | (static_cast<uint32_t>(r.material) << 28);
@@ -446,11 +446,30 @@ __device__ __forceinline__ void bin_carrier(const DevTables& T, const CellArrays
     if (h >= 0) bin_add(C, h, 1u, occ, fmax(1.0, occ), rta);
 }
 
+// Sums of `v` over runs of equal keys in lane order, left at the first lane of
+// each run (all 32 lanes call; `heads` marks the first lane of every run). A
+// tree over each run: in round o a lane at an even multiple of o within its
+// run adds the partial sum of the lane o further on, when that lane is still
+// in the run -- every value is added once, so a run of L lanes costs L - 1
+// FP64 additions (GB300 retires two FP64 lanes per SM per clock).
+template <class T>
+__device__ __forceinline__ T run_sum_to_head(T v, unsigned heads, int lane) {
+    const int start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+    const unsigned later = lane == 31 ? 0u : heads & (0xfffffffeu << lane);
+    const int end = later ? __ffs(later) - 1 : 32; // first lane past the run
+    const int pos = lane - start;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const T w = __shfl_down_sync(0xffffffffu, v, o);
+        if ((pos & (2 * o - 1)) == 0 && lane + o < end) v += w;
+    }
+    return v;
+}
+
 // Bin tallies of one warp (all 32 lanes call; h < 0: nothing from this lane).
 // Runs of equal records in lane order -- the common case once the carriers
-// are sorted by (mode, cell) -- are summed with a segmented shuffle scan and
-// the last lane of each run makes one atomic per field. kAgg false: one
-// atomic per carrier.
+// are sorted by (mode, cell) -- are summed (run_sum_to_head) and the first
+// lane of each run makes one atomic per field. kAgg false: one atomic per carrier.
 template <bool kAgg, bool kRta>
 __device__ __forceinline__ void bin_warp(const CellArrays& C, long long h, double occ) {
     if constexpr (!kAgg) {
@@ -458,27 +477,16 @@ __device__ __forceinline__ void bin_warp(const CellArrays& C, long long h, doubl
     } else {
         const int lane = threadIdx.x & 31;
         const long long hp = __shfl_up_sync(0xffffffffu, h, 1);
-        const long long hn = __shfl_down_sync(0xffffffffu, h, 1);
         const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || hp != h);
         unsigned cnt = h >= 0 ? 1u : 0u;
         double N = h >= 0 ? occ : 0.0;
         double M = h >= 0 ? fmax(1.0, occ) : 0.0;
         if (heads != 0xffffffffu) { // warp-uniform: some run is longer than one lane
-            const int start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const unsigned c2 = __shfl_up_sync(0xffffffffu, cnt, o);
-                const double n2 = __shfl_up_sync(0xffffffffu, N, o);
-                double m2 = 0.0;
-                if (kRta) m2 = __shfl_up_sync(0xffffffffu, M, o);
-                if (lane - o >= start) {
-                    cnt += c2;
-                    N += n2;
-                    if (kRta) M += m2;
-                }
-            }
+            cnt = run_sum_to_head(cnt, heads, lane);
+            N = run_sum_to_head(N, heads, lane);
+            if (kRta) M = run_sum_to_head(M, heads, lane);
         }
-        if (h >= 0 && (lane == 31 || hn != h)) bin_add(C, h, cnt, N, M, kRta);
+        if (h >= 0 && ((heads >> lane) & 1u)) bin_add(C, h, cnt, N, M, kRta);
     }
 }
 
@@ -591,10 +599,10 @@ __device__ __forceinline__ bool interface_step_mixed(const DevTables& T, DevLedg
     const Uniform2 d0 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose, static_cast<uint32_t>(event), 0);
     const Uniform2 d1 = uniform2(P.seed, static_cast<uint32_t>(slot), step, purpose, static_cast<uint32_t>(event), 1);
     const IfaceOut r = interface_dev(T, static_cast<int>(w >> 28), static_cast<int>(w & 0x00FFFFFFu), (w >> 24) & 7u,
-                                     occ, destination, d0.a, d0.b, d1.a);
+                                     occ, destination, d0.a, d0.b, d1.a, d1.b);
     count_interface(bl, r);
-    if (r.action == 5) {
-        raise_error(L, kErrModeMapping, slot);
+    if (r.action >= 5) {
+        raise_error(L, r.action == 6 ? kErrAmmRow : kErrModeMapping, slot);
         return false;
     }
     w = static_cast<uint32_t>(r.active) | (r.signs << 24) | (static_cast<uint32_t>(r.material) << 28);
@@ -1616,15 +1624,9 @@ __global__ void __launch_bounds__(256) k_flux(const DevTables* __restrict__ Tp, 
                               __any_sync(0xffffffffu, live);
         if (one_mode) {
             const int cp = __shfl_up_sync(0xffffffffu, c, 1);
-            const int cn = __shfl_down_sync(0xffffffffu, c, 1);
             const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || cp != c);
-            const int start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const double e2 = __shfl_up_sync(0xffffffffu, e, o);
-                if (lane - o >= start) e += e2;
-            }
-            if (live && (lane == 31 || cn != c))
+            e = run_sum_to_head(e, heads, lane);
+            if (live && ((heads >> lane) & 1u))
                 for (int a = 0; a < 3; ++a) atomicAdd(dst + 3 * c + a, dmul(v[a], e));
         } else if (live) {
             for (int a = 0; a < 3; ++a) atomicAdd(dst + 3 * c + a, dmul(v[a], e));

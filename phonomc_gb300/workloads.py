@@ -13,6 +13,9 @@ bilayer_callaway  200 nm stack of two materials (the second with 0.7x
                    reservoirs 310/290 K on the z faces, 100 z-cells, 1e8
                    carriers, dt = 0.5 ps.
 
+bilayer_amm       the bilayer stack with the acoustic-mismatch interface and
+                   nonlinear RTA (plain 8^3 tables).
+
 heated_film       the cross-plane film with both reservoirs at 300 K and a
                    prescribed lattice heat source: Gaussian along z (sigma
                    10 nm, centred at 50 nm, uniform in x and y), 1e18 W/m^3
@@ -107,6 +110,19 @@ def bilayer_callaway(particles: float = 1e8, seed: int = 12345, precision: str =
     }
 
 
+def bilayer_amm(particles: float = 1e7, seed: int = 12345, precision: str = "fp64", model: str = "amm",
+                amm_fraction: float = 1.0) -> dict:
+    """The bilayer stack with the acoustic-mismatch interface model (or the
+    mixed model with `amm_fraction`): nonlinear RTA with lifetimes fixed at
+    300 K, mass densities 2329 / 5323 kg/m^3, the plain 8^3 synthetic table and
+    its softened copy (bilayer_materials(8, callaway=False))."""
+    c = bilayer_callaway(particles, seed, precision)
+    c.update(name="bilayer_amm", collision_model="rta", interface_model=model, mass_densities_kg_m3=[2329.0, 5323.0])
+    if model == "mmm":
+        c["interface_amm_fraction"] = amm_fraction
+    return c
+
+
 def heated_film(particles: float = 1e6, seed: int = 12345, precision: str = "fp64", spectrum: str = "thermal") -> dict:
     c = cross_plane_film(particles, seed, precision)
     c.update(name="heated_film", face_values=(0, 0, 0, 0, 300.0, 300.0), initial_temperature=300.0,
@@ -142,13 +158,14 @@ def batched_films(n: int = 512, seed: int = 0, precision: str = "mixed", particl
     return films
 
 
-def bilayer_materials(mesh: int = 8):
-    """The two synthetic materials of the bilayer (Callaway linewidth split).
-    Callaway tables are completed over the first Brillouin zone as the
-    reference does: 8^3 q-points x 6 branches become 24,552 modes."""
+def bilayer_materials(mesh: int = 8, callaway: bool = True):
+    """The two synthetic materials of the bilayer (Callaway linewidth split
+    unless callaway is False). Callaway tables are completed over the first
+    Brillouin zone as the reference does: 8^3 q-points x 6 branches become
+    24,552 modes."""
     from . import synthetic
-    return [synthetic.make_material(mesh=mesh, callaway=True),
-            synthetic.make_material(mesh=mesh, freq_scale=0.7, vel_scale=0.75, callaway=True)]
+    return [synthetic.make_material(mesh=mesh, callaway=callaway),
+            synthetic.make_material(mesh=mesh, freq_scale=0.7, vel_scale=0.75, callaway=callaway)]
 
 
 def scaled(cfg: dict, particles: float, **over) -> dict:

@@ -54,6 +54,9 @@ CASES = {
     "domain_finfet": ["domain", "{t}"],
     "interface_dmm": ["interface", "{m}", "{s}", "0"],
     "interface_dmm_linearized": ["interface", "{m}", "{s}", "1"],
+    "interface_amm": ["amm", "{m}", "{s}", "1", "1.0", "0"],
+    "interface_amm_linearized": ["amm", "{m}", "{s}", "1", "1.0", "1"],
+    "interface_mmm": ["amm", "{m}", "{s}", "2", "0.4", "0"],
 }
 
 
@@ -294,6 +297,20 @@ def full_runs_bilayer(pmats: str, tmp: str) -> dict:
     return out
 
 
+# Full reference runs of the bilayer with the acoustic-mismatch interface
+# (phonomc_gb300.workloads.bilayer_amm at 2e4 carriers, 20 cells, nonlinear RTA,
+# plain 8^3 tables): the late-time fields of full_runs_bilayer.
+def full_runs_bilayer_amm(pmats: str, tmp: str) -> dict:
+    global BILAYER_TOML
+    saved = BILAYER_TOML
+    BILAYER_TOML = saved.replace('[scattering]\nmodel = "callaway"\n', '[scattering]\nmodel = "rta"\n').replace(
+        'interface_model = "dmm"', 'interface_model = "amm"\nmass_densities_kg_m3 = [2329.0, 5323.0]')
+    try:
+        return full_runs_bilayer(pmats, tmp)
+    finally:
+        BILAYER_TOML = saved
+
+
 # Full reference runs of the cross-plane film with nonlinear Callaway
 # collisions (8^3 Callaway table, 8000 carriers, 120 steps of 1 ps): per seed
 # the late-time (steps 61-120) cell temperatures, heat flux and kappa_eff.
@@ -483,6 +500,12 @@ def main() -> None:
         with gzip.open(os.path.join(HERE, "fullrun_bilayer.json.gz"), "wt") as f:
             json.dump(data, f)
         print("fullrun_bilayer ok")
+    if not args.only or "fullrun_bilayer_amm" in args.only:
+        data = full_runs_bilayer_amm(mpath + "," + spath, os.path.join(tmp, "fullrun_bilayer_amm"))
+        data["_harness_args"] = ["run", "{m},{s}", "<bilayer toml, rta, amm>", str(BILAYER_STEPS)]
+        with gzip.open(os.path.join(HERE, "fullrun_bilayer_amm.json.gz"), "wt") as f:
+            json.dump(data, f)
+        print("fullrun_bilayer_amm ok")
     if not args.only or "fullrun_finfet" in args.only:
         data = full_runs_finfet(mpath, fpath, os.path.join(tmp, "fullrun_finfet"))
         data["_harness_args"] = ["run", "{m}", "<FinFET toml>", str(FINFET_STEPS)]

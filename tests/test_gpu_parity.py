@@ -759,3 +759,23 @@ def test_staged_pass_matches_direct_loads(gpu, name, stationary):
     assert np.allclose(Ta, Tb, rtol=1e-12, atol=0)
     for k in ("particle_count", "absorbed_total", "injected_total", "rough_counts"):
         assert sa[k] == sb[k], k
+
+
+@pytest.mark.parametrize("model,fraction", [("amm", 1.0), ("mmm", 0.4)])
+def test_bilayer_amm_steps_match_oracle(gpu, orc, model, fraction):
+    """Acoustic (and mixed) mismatch interface events inside whole device steps
+    against the oracle: rows built on the host, sampled on the device with the
+    oracle's draws; carriers, cells and interface counters exact."""
+    data = workloads.bilayer_materials(8, callaway=False)
+    cfg = workloads.scaled(workloads.bilayer_amm(model=model, amm_fraction=fraction), 20000, random_seed=41,
+                           grid=(1, 1, 20))
+    mg = [abi.Material(gpu, "phmc_", d, 0.1, False, False) for d in data]
+    mo = [abi.Material(orc, "orc_", d, 0.1, False, False) for d in data]
+    sg, so = abi.Solver(gpu, "phmc_", cfg, mg), abi.Solver(orc, "orc_", cfg, mo)
+    for _ in range(4):
+        sg.run(2)
+        so.run(2)
+        stg, sto = _compare(sg, so)
+        for k in ("interface_events", "interface_transmitted", "interface_reflected"):
+            assert stg[k] == sto[k], k
+    assert sto["interface_transmitted"] > 0

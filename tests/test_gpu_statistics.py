@@ -247,3 +247,34 @@ def test_inplane_gradient_mixed_kappa_error(gpu):
     assert abs(_z(km[:, None], kf[:, None])[0]) < 3.0, (km, kf)
     for p in runs:
         assert runs[p]["resid"].max() < 1e-6
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_bilayer_amm_statistics(gpu, precision):
+    """Bilayer with the acoustic-mismatch interface (tests/golden/fullrun_bilayer_amm)."""
+    g = golden("fullrun_bilayer_amm")
+    mats = [abi.Material(gpu, "phmc_", d, 0.1, False, False) for d in workloads.bilayer_materials(8, callaway=False)]
+    T_mean, flux, trans, resid = [], [], [], []
+    for k in range(len(g["seeds"])):
+        cfg = workloads.scaled(workloads.bilayer_amm(precision=precision), g["particles"], random_seed=9501 + k,
+                               grid=(1, 1, g["cells"]), convergence_write_interval=1)
+        s = abi.Solver(gpu, "phmc_", cfg, mats)
+        T_acc, f_acc = [], []
+        for step in range(1, g["steps"] + 1):
+            s.run(1)
+            if step >= g["average_from_step"]:
+                T_acc.append(s.cells()[0])
+                f_acc.append(s.stats()["average_heat_flux_along_axis"])
+        st = s.stats()
+        T_mean.append(np.mean(T_acc, axis=0))
+        flux.append(np.mean(f_acc))
+        trans.append(st["interface_transmitted"] / max(1, st["interface_events"]))
+        resid.append(abs(st["total_energy_balance_residual_ev"]))
+        s.close()
+    z = _z(T_mean, g["T_mean"])
+    assert np.all(np.abs(z) < 4.5), z
+    assert np.mean(z * z) < 2.5, np.mean(z * z)
+    assert abs(_z(np.asarray(flux)[:, None], np.asarray(g["flux_mean"])[:, None])[0]) < 3.0
+    tr_ref = np.array(g["interface_transmitted"]) / np.array(g["interface_events"])
+    assert abs(_z(np.asarray(trans)[:, None], tr_ref[:, None])[0]) < 3.0
+    assert max(resid) < 1e-6

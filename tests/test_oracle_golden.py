@@ -228,6 +228,63 @@ def test_interface_dmm(oracle_lib, name, linearized):
         assert np.array_equal(v * sg, np.asarray(g["out_v"]).reshape(-1, 3)[sel])
 
 
+def _amm_materials(lib):
+    from phonomc_gb300 import synthetic
+    return (abi.Material(lib, "orc_", synthetic.make_material(mesh=8), 0.1, False, False),
+            abi.Material(lib, "orc_", synthetic.make_material(mesh=8, freq_scale=0.7, vel_scale=0.75), 0.1, False,
+                         False))
+
+
+def test_amm_rows_match_reference(oracle_lib):
+    """Acoustic-mismatch rows (AcousticInterfaceSampler::configure): mirror
+    partners and transmitted destinations exact, probabilities to 1e-12, for
+    both sides of the interface between the 8^3 table and its softened copy."""
+    g = golden("interface_amm")
+    ma, mb = _amm_materials(oracle_lib)
+    I = lambda a: a.ctypes.data_as(abi.c_int32_p)  # noqa: E731
+    for side in (0, 1):
+        n = len(g[f"reflected_{side}"])
+        refl, start = np.zeros(n, np.int32), np.zeros(n + 1, np.int32)
+        assert oracle_lib.orc_amm_rows(ma.h, mb.h, g["density_a"], g["density_b"], g["frequency_bin_thz"],
+                                       g["parallel_bin_inv_a"], side, I(refl), I(start), None, None) == 0, \
+            oracle_lib.orc_last_error()
+        dest, prob = np.zeros(start[-1], np.int32), np.zeros(start[-1])
+        assert oracle_lib.orc_amm_rows(ma.h, mb.h, g["density_a"], g["density_b"], g["frequency_bin_thz"],
+                                       g["parallel_bin_inv_a"], side, I(refl), I(start), I(dest), D(prob)) == 0
+        assert np.array_equal(refl, g[f"reflected_{side}"])
+        assert np.array_equal(start, g[f"start_{side}"])
+        assert np.array_equal(dest, g[f"dest_{side}"])
+        assert np.allclose(prob, g[f"prob_{side}"], rtol=1e-12, atol=0)
+        assert start[-1] > 0
+
+
+@pytest.mark.parametrize("name,linearized", [("interface_amm", 0), ("interface_amm_linearized", 1),
+                                             ("interface_mmm", 0)])
+def test_interface_amm_events(oracle_lib, name, linearized):
+    """Acoustic and mixed-mismatch interface events against
+    InterfaceInteraction::interact with the reference engine's draws replayed:
+    model choice, row sample or diffuse bands, outgoing mode and occupation."""
+    g = golden(name)
+    ma, mb = _amm_materials(oracle_lib)
+    n = len(g["src"])
+    src, flat = (np.ascontiguousarray(g[k], dtype=np.int32) for k in ("src", "in_flat"))
+    occ = np.ascontiguousarray(g["in_occ"], dtype=np.float64)
+    u4 = np.ascontiguousarray(g["draws"], dtype=np.float64)
+    act, mat, fo = (np.zeros(n, np.int32) for _ in range(3))
+    oo = np.zeros(n)
+    I = lambda a: a.ctypes.data_as(abi.c_int32_p)  # noqa: E731
+    rc = oracle_lib.orc_interface_model(ma.h, mb.h, g["weight_a"], g["weight_b"], g["frequency_bin_thz"],
+                                        g["reference_temperature"], linearized, g["model"], g["amm_fraction"],
+                                        g["density_a"], g["density_b"], g["parallel_bin_inv_a"], n, I(src), I(flat),
+                                        D(occ), D(u4), I(act), I(mat), I(fo), D(oo))
+    assert rc == 0, oracle_lib.orc_last_error()
+    assert np.array_equal(act, g["action"])
+    assert np.array_equal(mat, g["out_material"])
+    assert np.array_equal(fo, g["out_flat"])
+    assert np.array_equal(oo, np.asarray(g["out_occ"]))
+    assert (act == 4).sum() == sum(g["transmitted"]) > 0
+
+
 SOURCE_CASES = {"source_thermal": ("thermal", 0), "source_thermal_linearized": ("thermal", 1),
                 "source_weighted": ("weighted", 0), "source_gaussian": ("gaussian", 0)}
 

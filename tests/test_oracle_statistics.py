@@ -160,3 +160,39 @@ def test_oracle_matches_reference_inplane_gradient_statistics():
     assert max(abs(r[4]) for r in res) < 1e-6
     assert max(abs(x) for x in g["balance_residual_total"]) < 1e-6
 
+
+
+def _oracle_bilayer_amm(seed):
+    import oracle
+    from phonomc_gb300 import abi, workloads
+    lib = oracle.load()
+    g = golden("fullrun_bilayer_amm")
+    cfg = workloads.scaled(workloads.bilayer_amm(), g["particles"], random_seed=seed, grid=(1, 1, g["cells"]),
+                           convergence_write_interval=1)
+    mats = [abi.Material(lib, "orc_", d, 0.1, False, False) for d in workloads.bilayer_materials(8, callaway=False)]
+    s = abi.Solver(lib, "orc_", cfg, mats)
+    T, flux = [], []
+    for step in range(1, g["steps"] + 1):
+        s.run(1)
+        if step >= g["average_from_step"]:
+            T.append(s.cells()[0])
+            flux.append(s.stats()["average_heat_flux_along_axis"])
+    st = s.stats()
+    return (np.mean(T, axis=0), float(np.mean(flux)), st["interface_transmitted"] / max(1, st["interface_events"]),
+            st["total_energy_balance_residual_ev"])
+
+
+def test_oracle_matches_reference_bilayer_amm_statistics():
+    """Two crystals with the acoustic-mismatch interface (nonlinear RTA): the
+    reference's 16 runs against 16 oracle runs -- cell temperatures across the
+    interface, heat flux, transmission ratio, energy closure."""
+    g = golden("fullrun_bilayer_amm")
+    with mp.get_context("spawn").Pool(8) as pool:
+        res = pool.map(_oracle_bilayer_amm, [5301 + k for k in range(len(g["seeds"]))])
+    z = _z(np.array([r[0] for r in res]), np.array(g["T_mean"]))
+    assert np.all(np.abs(z) < 4.5), z
+    assert np.mean(z * z) < 2.5, np.mean(z * z)
+    assert abs(_z(np.array([r[1] for r in res])[:, None], np.array(g["flux_mean"])[:, None])[0]) < 3.0
+    tr_ref = np.array(g["interface_transmitted"]) / np.array(g["interface_events"])
+    assert abs(_z(np.array([r[2] for r in res])[:, None], tr_ref[:, None])[0]) < 3.0
+    assert max(abs(r[3]) for r in res) < 1e-6
