@@ -1115,8 +1115,10 @@ struct OracleSolver {
                 const Uniform2 d0 = uniform2(cfg.random_seed, static_cast<uint32_t>(e), static_cast<uint32_t>(step), kDrawInject, static_cast<uint32_t>(r), 0);
                 const Uniform2 d1 = uniform2(cfg.random_seed, static_cast<uint32_t>(e), static_cast<uint32_t>(step), kDrawInject, static_cast<uint32_t>(r), 1);
                 const Uniform2 d2 = uniform2(cfg.random_seed, static_cast<uint32_t>(e), static_cast<uint32_t>(step), kDrawInject, static_cast<uint32_t>(r), 2);
-                size_t m = static_cast<size_t>(std::lower_bound(R.cdf.begin(), R.cdf.end(), d0.a) - R.cdf.begin());
-                if (m >= R.cdf.size()) m = R.cdf.size() - 1;
+                // the emission distribution of ReservoirSampler::sample (its
+                // lower_bound over the flux roulette, ReservoirSampler.cpp:117-146)
+                // drawn from the same weights' alias table, as the device does
+                const size_t m = static_cast<size_t>(alias_draw(R.alias.data(), static_cast<int>(R.alias.size()), d0.a));
                 const double temit = dt * d0.b;
                 size_t k = static_cast<size_t>(std::upper_bound(cum.begin(), cum.end(), d1.a * cum.back()) - cum.begin());
                 if (k >= cum.size()) k = cum.size() - 1;
@@ -2019,6 +2021,20 @@ int orc_reservoir_cdf(void* m, const double normal[3], double area, double densi
             for (size_t i = 0; i < act.size(); ++i) cdf[i] /= e;
         *expected = e;
         *initial_count = static_cast<int32_t>(std::llround(e));
+    });
+}
+
+// The solver's alias table of weights w (build_alias_table, shared with the
+// device build) and the outcomes it gives for uniforms u (alias_draw).
+int orc_alias_table(const double* w, int32_t n, double* prob, int32_t* alias, int32_t n_draws, const double* u,
+                    int32_t* out) {
+    return guard([&] {
+        const std::vector<AliasCell> t = build_alias_table(std::vector<double>(w, w + n));
+        for (int32_t k = 0; k < n; ++k) {
+            prob[k] = t[k].prob;
+            alias[k] = t[k].alias;
+        }
+        for (int32_t j = 0; j < n_draws; ++j) out[j] = alias_draw(t.data(), n, u[j]);
     });
 }
 } // extern "C"

@@ -517,6 +517,7 @@ ORACLE_EXTRA_PROTOS = {
                                c_double_p, C.c_int64, c_int32_p, c_int32_p, c_double_p, c_double_p, c_int64_p]),
     "reservoir_cdf": (C.c_int, [C.c_void_p, c_double_p, C.c_double, C.c_double, C.c_double, c_double_p, c_double_p,
                                 c_int32_p]),
+    "alias_table": (C.c_int, [c_double_p, C.c_int32, c_double_p, c_int32_p, C.c_int32, c_double_p, c_int32_p]),
 }
 
 DEVICE_PROTOS = {

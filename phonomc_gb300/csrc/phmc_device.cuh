@@ -133,6 +133,7 @@ struct DevReservoir {
     const double* tri;     // [n_tri][3 vertices][3]
     const double* tri_cum; // running area sum, [n_tri]
     const double* cdf;
+    const AliasCell* alias; // the emission distribution as an alias table, [n_cdf]
     const double* occ; // emitted occupation per active mode
 };
 

@@ -1306,18 +1306,22 @@ Problem build_problem(const SimulationConfig& cfg, SimulationDomain& domain,
         const PhononMaterial& M = *mats[R.material];
         const auto& act = M.active_flat();
         R.cdf.resize(act.size());
+        std::vector<double> weight(act.size(), 0.0);
         const double n_active = static_cast<double>(M.active_mode_count());
         double expected = 0;
         if (density > 0.0 && cfg.time_step > 0.0) {
             const double thickness = n_active / (density * R.area);
             for (size_t m = 0; m < act.size(); ++m) {
                 const double par = -dot3(R.normal, M.velocity(act[m]));
-                expected += std::max(0.0, par * cfg.time_step / thickness);
+                weight[m] = std::max(0.0, par * cfg.time_step / thickness);
+                expected += weight[m];
                 R.cdf[m] = expected;
             }
         }
-        if (expected > 0)
+        if (expected > 0) {
             for (double& v : R.cdf) v /= expected;
+            R.alias = build_alias_table(weight);
+        }
         R.initial_count = static_cast<int>(std::llround(expected));
         R.expected = expected;
         std::vector<double> occ(act.size());
@@ -1493,6 +1497,40 @@ std::string format_convergence_row(const ConvergenceRow& s) {
     if (s.gradient) out << " " << s.gradient_updates << " " << s.gradient_energy;
     out << '\n';
     return out.str();
+}
+
+std::vector<AliasCell> build_alias_table(const std::vector<double>& weights) {
+    const size_t n = weights.size();
+    double sum = 0.0;
+    for (double w : weights) {
+        if (!(w >= 0.0) || !std::isfinite(w)) throw std::invalid_argument("alias table: weights must be finite and non-negative");
+        sum += w;
+    }
+    if (n == 0 || !(sum > 0.0)) throw std::invalid_argument("alias table: weights must have a positive sum");
+    std::vector<AliasCell> t(n, AliasCell{1.0, 0, 0});
+    std::vector<double> p(n);
+    std::vector<int32_t> small, large;
+    int32_t heaviest = 0;
+    for (size_t k = 0; k < n; ++k) {
+        p[k] = weights[k] * static_cast<double>(n) / sum; // column mass in units of 1/n
+        (p[k] < 1.0 ? small : large).push_back(static_cast<int32_t>(k));
+        if (weights[k] > weights[heaviest]) heaviest = static_cast<int32_t>(k);
+        t[k].alias = static_cast<int32_t>(k);
+    }
+    while (!small.empty() && !large.empty()) {
+        const int32_t s = small.back(), l = large.back();
+        small.pop_back();
+        large.pop_back();
+        t[s].prob = p[s];
+        t[s].alias = l;
+        p[l] = (p[l] + p[s]) - 1.0; // what is left of l after filling column s
+        (p[l] < 1.0 ? small : large).push_back(l);
+    }
+    // columns left over hold mass 1 up to rounding; a weightless one (possible
+    // only through rounding) hands its column to the heaviest outcome
+    for (int32_t l : large) t[l] = AliasCell{1.0, l, 0};
+    for (int32_t s : small) t[s] = weights[s] > 0.0 ? AliasCell{1.0, s, 0} : AliasCell{0.0, heaviest, 0};
+    return t;
 }
 
 } // namespace phmc

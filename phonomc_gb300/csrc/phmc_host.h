@@ -21,6 +21,8 @@
 #include <string>
 #include <vector>
 
+#include "phmc_rng.h"
+
 namespace phmc {
 
 constexpr double kHbarEvPs = 6.582119569e-4;
@@ -492,9 +494,18 @@ struct Reservoir {
     double temperature = 300, area = 0;
     Vec3 normal{};
     std::vector<double> cdf; // over the material's active modes
+    // the same emission distribution as an alias table over the active modes:
+    // one uniform per draw, O(1), in place of a search of `cdf`
+    std::vector<AliasCell> alias;
     double expected = 0;
     int initial_count = 0;
 };
+
+// Alias table of a discrete distribution with non-negative weights (positive
+// sum), built by Vose's two-worklist method (M. D. Vose, IEEE TSE
+// 17(9):972-975, 1991). Outcome k is drawn with probability w_k / sum(w) up
+// to rounding; an outcome of weight zero is never drawn.
+std::vector<AliasCell> build_alias_table(const std::vector<double>& weights);
 
 // ---------------------------------------------------------------- ledgers
 // src/solver/BoundaryLedger.cpp and src/solver/EnergyLedger.cpp, single writer.

@@ -66,4 +66,33 @@ PHMC_HD Uniform2 uniform2(uint64_t seed, uint32_t slot, uint32_t step, uint32_t 
     return {static_cast<double>(m0) * inv53, static_cast<double>(m1) * inv53};
 }
 
+// One column of a Walker alias table (A. J. Walker, ACM TOMS 3(3):253-256,
+// 1977): the column keeps its own outcome with probability `prob` and gives
+// `alias` otherwise. 16 bytes, read with one vector load.
+struct alignas(16) AliasCell {
+    double prob;
+    int32_t alias;
+    int32_t pad;
+};
+
+// A draw from an n-column alias table with one uniform u in [0, 1): column
+// i = floor(u n), kept when the fraction u n - i is below its probability.
+// The product is rounded once, identically on host and device (no FMA).
+PHMC_HD int alias_draw(const AliasCell* t, int n, double u) {
+#if defined(__CUDA_ARCH__)
+    const double s = __dmul_rn(u, static_cast<double>(n));
+#else
+    const double s = u * static_cast<double>(n);
+#endif
+    int i = static_cast<int>(s);
+    if (i > n - 1) i = n - 1;
+    const AliasCell c = t[i];
+#if defined(__CUDA_ARCH__)
+    const double f = __dsub_rn(s, static_cast<double>(i));
+#else
+    const double f = s - static_cast<double>(i);
+#endif
+    return f < c.prob ? i : c.alias;
+}
+
 } // namespace phmc

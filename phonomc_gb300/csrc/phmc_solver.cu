@@ -354,6 +354,7 @@ void DeviceSolver::upload_tables() {
         D.tri = upload(tri);
         D.tri_cum = upload(cum);
         D.cdf = upload(R.cdf);
+        D.alias = R.alias.empty() ? nullptr : upload(R.alias);
         D.occ = upload(P_.reservoir_occ[r]);
     }
     // domain

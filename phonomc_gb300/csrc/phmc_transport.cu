@@ -1453,13 +1453,7 @@ __device__ __forceinline__ void k_inject_body(const DevTables* __restrict__ Tp, 
         const Uniform2 d0 = uniform2(P.seed, static_cast<uint32_t>(e), step, kDrawInject, static_cast<uint32_t>(r), 0);
         const Uniform2 d1 = uniform2(P.seed, static_cast<uint32_t>(e), step, kDrawInject, static_cast<uint32_t>(r), 1);
         const Uniform2 d2 = uniform2(P.seed, static_cast<uint32_t>(e), step, kDrawInject, static_cast<uint32_t>(r), 2);
-        int lo = 0, hi = R.n_cdf;
-        while (lo < hi) { // lower_bound
-            const int mid = (lo + hi) >> 1;
-            if (R.cdf[mid] < d0.a) lo = mid + 1;
-            else hi = mid;
-        }
-        const int m = lo < R.n_cdf ? lo : R.n_cdf - 1;
+        const int m = alias_draw(R.alias, R.n_cdf, d0.a); // emission mode, O(1)
         const double temit = P.dt * d0.b;
         // area-weighted triangle of the facet: first running sum above u * total
         const double target = dmul(d1.a, R.tri_cum[R.n_tri - 1]);

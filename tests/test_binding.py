@@ -11,7 +11,8 @@ values, active modes). The in-plane gradient film and the cross-plane film
 are read from TOML files with their material in the reference's folder layout
 (POSCAR + kappa-fbz.hdf5 written by phmc_material_save).
 
-Needs the reference sources (PHONOMC_REFERENCE, skipped without them). The
+Needs the reference sources (PHONOMC_REFERENCE, or the checkout oracle/_ref
+was built from; skipped without them). The
 device run of the same program ("run" mode) needs a GPU and the reference
 build, which exist together only where the reference is checked out.
 """
@@ -22,13 +23,15 @@ import subprocess
 
 import pytest
 
+import oracle
+
 from phonomc_gb300 import abi, synthetic
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("PHONOMC_REFERENCE", "/root/reference")
+REF = oracle.reference_root() or ""
 REF_LIB = os.path.join(ROOT, "oracle", "_ref", "libphonomc_ref.a")
 
-pytestmark = pytest.mark.skipif(not (os.path.isdir(os.path.join(REF, "include")) and os.path.exists(REF_LIB)),
+pytestmark = pytest.mark.skipif(not (REF and os.path.isdir(os.path.join(REF, "include")) and os.path.exists(REF_LIB)),
                                 reason="reference sources or oracle/_ref build not present")
 
 TOML = """[geometry]

@@ -20,9 +20,11 @@ import os
 import numpy as np
 import pytest
 
+import oracle
+
 from phonomc_gb300 import abi, synthetic
 
-REF = os.environ.get("PHONOMC_REFERENCE", "/root/reference")
+REF = oracle.reference_root() or ""
 SI = os.path.join(REF, "material", "Si")
 
 
@@ -78,7 +80,7 @@ def test_material_folder_errors(lib, tmp_path):
         abi.FolderMaterial(lib, str(empty))
 
 
-@pytest.mark.skipif(not os.path.isdir(SI), reason="reference material folders not present")
+@pytest.mark.skipif(not (REF and os.path.isdir(SI)), reason="reference material folders not present")
 def test_bundled_si_tables_are_read_consistently(lib):
     full, irr = os.path.join(SI, "kappa-fbz.hdf5"), os.path.join(SI, "kappa.hdf5")
     src = abi.h5_read(lib, full, "_fbz_src_q_index").astype(int)

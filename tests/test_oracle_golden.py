@@ -193,6 +193,74 @@ def test_reservoir_cdf(oracle_lib, m8):
     assert counts == g["initial_count"]
 
 
+def _alias(oracle_lib, w, u):
+    w = _f64(w)
+    u = _f64(u)
+    n = w.size
+    prob, alias, out = np.zeros(n), np.zeros(n, np.int32), np.zeros(u.size, np.int32)
+    assert oracle_lib.orc_alias_table(D(w), n, D(prob), I32(alias), u.size, D(u), I32(out)) == 0
+    return prob, alias, out
+
+
+def _alias_mass(prob, alias):
+    """Probability of each outcome implied by an alias table."""
+    n = prob.size
+    q = np.clip(prob, 0.0, 1.0).copy()
+    np.add.at(q, alias, 1.0 - np.clip(prob, 0.0, 1.0))
+    return q / n
+
+
+def test_reservoir_alias_tables_reproduce_the_emission_cdf(oracle_lib, m8):
+    """The emission mode is drawn through an alias table of the reservoir's
+    flux weights (one uniform, O(1)) in place of the reference's lower_bound
+    over the normalised roulette (ReservoirSampler.cpp:117-146). Same
+    distribution: the table's implied probabilities equal the CDF's steps, a
+    mode of zero inward flux is never drawn, and 4096 stratified uniforms per
+    column reproduce the steps to 1/4096 of a column."""
+    g = golden("reservoir")
+    m = _mat(oracle_lib, m8)
+    cdf = np.zeros(6 * m8.qpoints)
+    exp, init = C.c_double(), C.c_int32()
+    active = 1512
+    for r, normal in enumerate([(0, 0, -1), (0, 0, 1)]):
+        assert oracle_lib.orc_reservoir_cdf(m.h, D(_f64(normal)), C.c_double(g["area"]), C.c_double(g["density"]),
+                                            C.c_double(g["dt"]), D(cdf), C.byref(exp), C.byref(init)) == 0
+        c = cdf[:active]
+        step = np.diff(c, prepend=0.0)
+        per = 4096
+        u = (np.arange(active * per) + 0.5) / (active * per)
+        prob, alias, out = _alias(oracle_lib, step, u)
+        q = _alias_mass(prob, alias)
+        assert np.max(np.abs(q - step / step.sum())) < 1e-15
+        zero = step == 0.0
+        assert zero.any() and not zero.all()
+        assert np.all(prob[zero] == 0.0) and not np.isin(np.flatnonzero(zero), alias[prob < 1.0]).any()
+        counts = np.bincount(out, minlength=active)
+        assert np.all(counts[zero] == 0)
+        targets = np.bincount(alias[prob < 1.0], minlength=active)
+        assert np.all(np.abs(counts / u.size - q) <= (1 + targets) / u.size)
+        # the reference's own draws all fall on modes the table can draw
+        ref_modes = np.asarray(g["active_index"])[r * 300:(r + 1) * 300]
+        assert not np.isin(ref_modes, np.flatnonzero(zero)).any()
+
+
+def test_alias_table_edge_weights(oracle_lib):
+    """Zeros, a dominant weight, subnormal-scale weights and a single outcome."""
+    rng = np.random.default_rng(5)
+    cases = [np.array([0.0, 0.0, 3.0, 0.0]), np.array([1e-300, 1.0, 1e-300, 0.0]), np.array([7.0]),
+             np.r_[np.zeros(50), rng.random(2000) ** 8, [1e6], np.zeros(7)], np.ones(1000)]
+    for w in cases:
+        u = np.r_[rng.random(4096), 0.0, np.nextafter(1.0, 0.0)]
+        prob, alias, out = _alias(oracle_lib, w, u)
+        q = _alias_mass(prob, alias)
+        assert np.max(np.abs(q - w / w.sum())) <= 4e-16 * w.size
+        assert np.all(w[out] > 0.0)
+    for bad in (np.zeros(3), np.array([1.0, -1.0]), np.array([1.0, np.nan])):
+        assert oracle_lib.orc_alias_table(D(_f64(bad)), bad.size, D(np.zeros(bad.size)),
+                                          I32(np.zeros(bad.size, np.int32)), 0, D(np.zeros(1)),
+                                          I32(np.zeros(1, np.int32))) != 0
+
+
 @pytest.mark.parametrize("name,linearized", [("interface_dmm", 0), ("interface_dmm_linearized", 1)])
 def test_interface_dmm(oracle_lib, name, linearized):
     """Diffuse-mismatch interface events against InterfaceInteraction::interact,
