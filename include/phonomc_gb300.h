@@ -28,6 +28,7 @@
  *   phmc_dev_linear_collide   CarrierCollisionOperator::apply src/solver/CarrierCollisionOperator.cpp:38-141
  *   phmc_dev_ncallaway_evolve nonlinear_callaway_evolve src/solver/NonlinearCallawayCollision.cpp:216-248
  *   phmc_dev_rough_reflect    RoughBoundarySampler::sample src/solver/RoughBoundarySampler.cpp:459-533
+ *   phmc_dev_rough_spec_match RoughBoundarySampler::build (specular matches) src/solver/RoughBoundarySampler.cpp:286-310
  *   phmc_dev_gradient_drive   TemperatureGradientDrive::apply src/solver/TemperatureGradientDrive.cpp:116-171
  */
 #ifndef PHONOMC_GB300_H
@@ -377,6 +378,12 @@ int phmc_dev_linear_collide(const phmc_material* m, int model, double Tref, int6
 int phmc_dev_rough_reflect(const phmc_material* m, int conservative, double Tref, const double normal_out[3],
                            double roughness_a, int64_t n, const int32_t* flat_in, const double* occ_in,
                            const double* u3, int32_t* flat_out, double* occ_out);
+/* Specular matches of the rough tables of nf facets (outward normals[3*f..],
+ * roughness in Angstrom) built with the device scan (device = 1) or the host
+ * loop (device = 0): match[f * active + ai] = matched outgoing active mode or -1
+ * (RoughBoundarySampler::build, src/solver/RoughBoundarySampler.cpp:286-310). */
+int phmc_dev_rough_spec_match(const phmc_material* m, int conservative, double Tref, int32_t nf,
+                              const double* normals_out, const double* roughness_a, int device, int32_t* match);
 /* Periodic-gradient drive on carriers grouped by cell. */
 int phmc_dev_gradient_drive(const phmc_material* m, int axis, double gradient, double Tref, int64_t n,
                             const int32_t* flat_mode, const int32_t* cell, double* occupation, int cells,

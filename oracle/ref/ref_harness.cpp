@@ -1,7 +1,7 @@
 // Golden-vector harness around the reference's own C++ solver.
 //
 // Linked against oracle/_ref/libphonomc_ref.a, which is the reference's src/
-// compiled unchanged (only the HDF5 readers are stubbed). Every number this
+// compiled unchanged (only the HDF5 readers are replaced). Every number this
 // program prints comes from reference code: PhononMaterial, SimulationDomain,
 // RtaCollisionOperator, CarrierCollisionOperator, CallawayOperator,
 // RoughBoundarySampler, ReservoirSampler, TemperatureGradientDrive and
@@ -35,6 +35,10 @@
 #include "solver/RtaCollisionOperator.h"
 #include "solver/TemperatureGradientDrive.h"
 
+#include <chrono>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1082,6 +1086,36 @@ std::string cmd_run(const std::string& pmat, const std::string& toml, int steps)
     j.put_i("interface_reflected", s.interface_reflected_count());
     return j.str();
 }
+// Wall time of the reference's own step loop: `warm` steps, then `steps`
+// timed steps of MonteCarloSolver::run_timestep; carrier-steps count the
+// carriers present at the start of each timed step. Threads: OMP_NUM_THREADS.
+std::string cmd_time(const std::string& pmat, const std::string& toml, int warm, int steps) {
+    SimulationConfig a = load_simulation_config(toml);
+    const bool stationary = uses_conservative_transport(a);
+    MaterialData md = std::filesystem::is_directory(pmat) ? phonomc::read_material_data(pmat) : read_pmat(pmat);
+    PhononMaterial m(std::move(md), a.temperature_lookup_dt, stationary, a.collision_model == CollisionModel::Callaway);
+    std::vector<std::reference_wrapper<const PhononMaterial>> mats{m};
+    SimulationDomain d(a);
+    MonteCarloSolver s(a, d, mats);
+    for (int k = 0; k < warm; ++k) s.run_timestep();
+    double carrier_steps = 0.0;
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int k = 0; k < steps; ++k) {
+        carrier_steps += static_cast<double>(s.particle_count());
+        s.run_timestep();
+    }
+    const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    Json j;
+    j.put("carrier_steps", carrier_steps);
+    j.put("seconds", sec);
+    j.put("carrier_steps_per_s", carrier_steps / sec);
+#ifdef _OPENMP
+    j.put_i("threads", omp_get_max_threads());
+#else
+    j.put_i("threads", 1);
+#endif
+    return j.str();
+}
 } // namespace
 
 int main(int argc, char** argv) {
@@ -1107,6 +1141,7 @@ int main(int argc, char** argv) {
         else if (c == "amm")
             out = cmd_amm(argv[2], argv[3], std::atoi(argv[4]), std::atof(argv[5]), std::atoi(argv[6]) != 0);
         else if (c == "run") out = cmd_run(argv[2], argv[3], std::atoi(argv[4]));
+        else if (c == "time") out = cmd_time(argv[2], argv[3], std::atoi(argv[4]), std::atoi(argv[5]));
         else if (c == "ncallaway")
             out = cmd_ncallaway(std::atoi(argv[2]), std::atoi(argv[3]), std::atoi(argv[4]), std::atoi(argv[5]));
         else throw std::runtime_error("unknown command " + c);

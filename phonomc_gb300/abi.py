@@ -546,6 +546,8 @@ DEVICE_PROTOS = {
     **{"dev_" + k: v for k, v in SUBSTEP_PROTOS.items()},
     "dev_trace_box_noalloc": (C.c_int, [c_double_p, c_double_p, C.c_int64, c_double_p, c_double_p, c_double_p,
                                         c_double_p, c_int32_p, c_int64_p]),
+    "dev_rough_spec_match": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int32, c_double_p, c_double_p, C.c_int,
+                                       c_int32_p]),
 }
 
 

@@ -149,7 +149,8 @@ def write_outputs(out, record):
         json.dump(record, f, indent=1)
     b = {r["precision"]: r["best"] for r in record["sweeps"]}
     thr = record.get("threshold", [])
-    wins = [r["particles"] for r in thr if r["ms_sorted"] < r["ms_never"]]
+    # sorting counts as a win only when it is at least 1% faster (timing noise)
+    wins = [r["particles"] for r in thr if r["ms_sorted"] < 0.99 * r["ms_never"]]
     nmin = min(wins) if wins else 2e6
 
     def val(prec, key, default):

@@ -1038,13 +1038,39 @@ int phmc_dev_gradient_drive(const phmc_material* m, int axis, double G, double T
     });
 }
 
+int phmc_dev_rough_spec_match(const phmc_material* m, int conservative, double Tref, int32_t nf,
+                              const double* normals, const double* roughness, int device, int32_t* match) {
+    return guard([&] {
+        const PhononMaterial& M = *m->m;
+        if (nf <= 0) throw std::invalid_argument("phmc_dev_rough_spec_match: no facets");
+        std::vector<Vec3> nrm(nf);
+        std::vector<double> rough(roughness, roughness + nf);
+        for (int f = 0; f < nf; ++f) nrm[f] = {normals[3 * f], normals[3 * f + 1], normals[3 * f + 2]};
+        RoughTables rt;
+        const SpecMatchScan scan = [](const std::vector<Vec3>& va, std::vector<SpecMatchJob>& jobs) {
+            spec_match_device(va, jobs, 0);
+        };
+        rt.build({&M}, nrm, rough, std::vector<char>(nf, 1), conservative != 0, conservative ? Tref : 0.0,
+                 device ? &scan : nullptr);
+        const size_t na = static_cast<size_t>(M.active_mode_count());
+        for (int f = 0; f < nf; ++f) {
+            const RoughTable& R = rt.tables.at(rt.facet_table.at(f));
+            std::copy(R.spec_match.begin(), R.spec_match.end(), match + f * na);
+        }
+    });
+}
+
 int phmc_dev_rough_reflect(const phmc_material* m, int conservative, double Tref, const double nout[3],
                            double rough_a, int64_t n, const int32_t* flat_in, const double* occ_in, const double* u3,
                            int32_t* flat_out, double* occ_out) {
     return guard([&] {
         const PhononMaterial& M = *m->m;
         RoughTables rt;
-        rt.build({&M}, {{nout[0], nout[1], nout[2]}}, {rough_a}, {1}, conservative != 0, conservative ? Tref : 0.0);
+        const SpecMatchScan scan = [](const std::vector<Vec3>& va, std::vector<SpecMatchJob>& jobs) {
+            spec_match_device(va, jobs, 0);
+        };
+        rt.build({&M}, {{nout[0], nout[1], nout[2]}}, {rough_a}, {1}, conservative != 0, conservative ? Tref : 0.0,
+                 &scan);
         const RoughTable& R = rt.tables.at(0);
         DBuf<double> spec(R.specularity), prefix(R.residual_prefix), rcdf(R.roulette_cdf);
         DBuf<int> match(R.spec_match), db(R.diffuse_begin), de(R.diffuse_end), sorted(R.outgoing_sorted),

@@ -258,7 +258,10 @@ struct __align__(8) DevBvhNode32 {
     float bmin[3], bmax[3];
     int left, right, begin, end;
 };
-constexpr int kFaceRecord32 = 10; // normal xyz, k, bounds min xyz, max xyz
+// normal xyz, k, bounds min xyz, max xyz, then per edge (AB, BC, CA) its
+// in-plane inward unit normal m and offset m.(edge start): a point p is at
+// least -(m.p - offset) from the triangle when that is positive
+constexpr int kFaceRecord32 = 22;
 struct DevMesh {
     const DevBvhNode* nodes;
     const double* face;        // [nfaces][kFaceRecord]
@@ -282,6 +285,7 @@ struct DevFacets {
     const int* rough_table;        // [material][n] -> rough table or -1
     const DevRoughTable* rough;    // every rough table of the domain
     const int* voxel_cell;         // voxel -> active cell
+    const int* cell_voxel;         // active cell -> home voxel (origin of its FP32 offsets)
     DevMesh mesh;                  // oriented faces and their BVH
     int n_simplex;                 // star decomposition (0: ray cast only)
     const double* simplex;         // [n_simplex][18]: apex xyz, inverse 3x3 row-major, bounds min xyz, max xyz
@@ -942,9 +946,17 @@ __device__ inline void mesh_walk_fp32(const DevMesh& M, const double x[3], const
             const float et = m / fabsf(den) + rel * fabsf(tf) + 1e-6f;
             if (tf + et <= 0.0f || tf - et > limit()) return;
             const float ep = vmax * (et + 1e-6f * fabsf(tf)) + m;
+            float p[3];
             for (int a = 0; a < 3; ++a) {
-                const float p = xf[a] + vf[a] * tf;
-                if (p < r[4 + a] - ep || p > r[7 + a] + ep) return;
+                p[a] = xf[a] + vf[a] * tf;
+                if (p[a] < r[4 + a] - ep || p[a] > r[7 + a] + ep) return;
+            }
+            // outside an edge by more than the FP64 test's 1e-7 plus the
+            // error of p (ep) and of the FP32 edge functions (4 margins)
+            const float tol = ep + 4.0f * m + 1e-7f;
+            for (int e = 0; e < 3; ++e) {
+                const float* q = r + 10 + 4 * e;
+                if (fmaf(q[0], p[0], fmaf(q[1], p[1], q[2] * p[2])) - q[3] < -tol) return;
             }
         }
         mesh_try_face(M, pos, x, v, h);
@@ -1131,6 +1143,25 @@ __device__ inline int mesh_contains(const DevFacets& F, const double p[3]) {
     const int r = mesh_ray_cast_inside(F, p);
     if (r != 0) return r;
     return mesh_simplex_inside(F, p) ? 1 : 0;
+}
+
+// Distance from p to the surface: the smallest distance to a face, faces
+// culled by their bounds once a closer one is known.
+__device__ inline double mesh_surface_distance(const DevFacets& F, const double p[3]) {
+    const DevMesh& M = F.mesh;
+    double bd = __longlong_as_double(0x7ff0000000000000LL);
+    for (int i = 0; i < M.nfaces; ++i) {
+        const double* r = M.face + kFaceRecord * i;
+        bool far = false;
+        for (int a = 0; a < 3; ++a) far = far || p[a] < r[4 + a] - bd || p[a] > r[7 + a] + bd;
+        if (far) continue;
+        double a[3], b[3], c[3], cp[3], d[3];
+        mesh_face(M, i, a, b, c);
+        meshmath::closest(p, a, b, c, cp);
+        meshmath::sub(p, cp, d);
+        bd = fmin(bd, meshmath::norm(d));
+    }
+    return bd;
 }
 
 // Facet of the closest face, first minimum (src/SurfaceMesh.cpp:996-1023).

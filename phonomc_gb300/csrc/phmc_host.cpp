@@ -490,6 +490,16 @@ int SimulationDomain::fast_grid_index(const Vec3& p) const {
     return mesh_ ? voxel_cell_[voxel] : voxel;
 }
 
+std::vector<int> SimulationDomain::cell_voxels() const {
+    std::vector<int> home(centers_.size());
+    for (size_t c = 0; c < centers_.size(); ++c) {
+        home[c] = voxel_index(centers_[c]);
+        if (mesh_ && voxel_cell_[home[c]] != static_cast<int>(c))
+            throw std::runtime_error("cell centre outside its own voxel");
+    }
+    return home;
+}
+
 int SimulationDomain::voxel_index(const Vec3& p) const {
     int idx[3];
     for (int a = 0; a < 3; ++a) {
@@ -569,9 +579,47 @@ int SimulationDomain::nearest_facet(const Vec3& p) const {
 
 // ----------------------------------------------------------- rough tables
 // src/solver/RoughBoundarySampler.cpp:77-368
+// Specular match of every incoming mode of every job: the first outgoing
+// mode of its window in frequency order that minimises
+// |v_try - v_out| / max(1e-12, |v_try|, |v_out|), v_try the incoming velocity
+// mirrored in the facet plane (src/solver/RoughBoundarySampler.cpp:286-310).
+void spec_match_host(const std::vector<Vec3>& va, std::vector<SpecMatchJob>& jobs) {
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int k = 0; k < static_cast<int>(jobs.size()); ++k) {
+        const SpecMatchJob& J = jobs[k];
+        for (int ai : *J.incoming) {
+            const int ib = (*J.begin)[ai], ie = (*J.end)[ai];
+            if (ib < 0 || ie <= ib) continue;
+            const Vec3 vin = va[ai];
+            const double vdn = dot3(vin, J.n_in);
+            const Vec3 vtry = sub3(vin, mul3(J.n_in, 2.0 * vdn));
+            int best = -1;
+            double bm = std::numeric_limits<double>::infinity();
+            for (int pos = ib; pos < ie; ++pos) {
+                const int ao = (*J.sorted)[pos];
+                const Vec3 dv = sub3(vtry, va[ao]);
+                const double ref = std::max({1e-12, norm3(vtry), norm3(va[ao])});
+                const double metric = norm3(dv) / ref;
+                if (metric < bm) {
+                    bm = metric;
+                    best = ao;
+                }
+            }
+            if (best >= 0) (*J.match)[ai] = best;
+        }
+    }
+}
+
 void RoughTables::build(const std::vector<const PhononMaterial*>& mats, const std::vector<Vec3>& normals,
                         const std::vector<double>& roughness, const std::vector<char>& enabled,
-                        bool require_discrete, double Teq) {
+                        bool require_discrete, double Teq, const SpecMatchScan* scan) {
+    // one facet's table between the preparation and the specular-match scan
+    struct FacetWork {
+        RoughTable rd;
+        std::vector<int> incoming, outgoing;
+        std::vector<double> destr, creat;
+        Vec3 n_in{};
+    };
     const int nf = static_cast<int>(normals.size());
     tables.clear();
     facet_table.assign(static_cast<size_t>(nf) * mats.size(), -1);
@@ -603,7 +651,7 @@ void RoughTables::build(const std::vector<const PhononMaterial*>& mats, const st
             }
             shell[ai] = shells - 1;
         }
-        auto build_one = [&](int f) {
+        auto prepare = [&](int f) {
             RoughTable rd;
             rd.facet = f;
             rd.material = static_cast<int>(mid);
@@ -677,23 +725,17 @@ void RoughTables::build(const std::vector<const PhononMaterial*>& mats, const st
                 if (ie <= ib) continue;
                 rd.diffuse_begin[ai] = ib;
                 rd.diffuse_end[ai] = ie;
-                const Vec3 vin = va[ai];
-                const double vdn = dot3(vin, nin);
-                const Vec3 vtry = sub3(vin, mul3(nin, 2.0 * vdn));
-                int best = -1;
-                double bm = std::numeric_limits<double>::infinity();
-                for (int pos = ib; pos < ie; ++pos) {
-                    const int ao = rd.outgoing_sorted[pos];
-                    const Vec3 dv = sub3(vtry, va[ao]);
-                    const double ref = std::max({1e-12, norm3(vtry), norm3(va[ao])});
-                    const double metric = norm3(dv) / ref;
-                    if (metric < bm) {
-                        bm = metric;
-                        best = ao;
-                    }
-                }
-                if (best >= 0) rd.spec_match[ai] = best;
             }
+            return FacetWork{std::move(rd), std::move(incoming), std::move(outgoing), std::move(destr),
+                             std::move(creat), nin};
+        };
+        // the rest of a table once its specular matches are known
+        auto finish = [&](FacetWork& fw) {
+            RoughTable& rd = fw.rd;
+            const std::vector<int>& incoming = fw.incoming;
+            const std::vector<int>& outgoing = fw.outgoing;
+            const std::vector<double>& destr = fw.destr;
+            const std::vector<double>& creat = fw.creat;
             for (int ai : incoming)
                 if (rd.spec_match[ai] < 0) rd.specularity[ai] = 0.0;
             if (rd.strict_elastic) {
@@ -734,26 +776,36 @@ void RoughTables::build(const std::vector<const PhononMaterial*>& mats, const st
                     rd.roulette_cdf.push_back(cdf);
                 }
             }
-            return rd;
         };
-        // Tables of different facets are independent: built in parallel, stored in facet order.
+        // Tables of different facets are independent: prepared in parallel,
+        // their specular matches scanned (host loop, or the caller's scan),
+        // finished in parallel and stored in facet order.
         std::vector<int> todo;
         for (int f = 0; f < nf; ++f)
             if (enabled[f]) todo.push_back(f);
-        std::vector<RoughTable> built(todo.size());
+        std::vector<FacetWork> work(todo.size());
         std::vector<std::string> errors(todo.size());
 #pragma omp parallel for schedule(dynamic, 1)
         for (int k = 0; k < static_cast<int>(todo.size()); ++k) {
             try {
-                built[k] = build_one(todo[k]);
+                work[k] = prepare(todo[k]);
             } catch (const std::exception& e) {
                 errors[k] = e.what();
             }
         }
-        for (size_t k = 0; k < todo.size(); ++k) {
+        for (size_t k = 0; k < todo.size(); ++k)
             if (!errors[k].empty()) throw std::invalid_argument(errors[k]);
+        std::vector<SpecMatchJob> jobs(work.size());
+        for (size_t k = 0; k < work.size(); ++k)
+            jobs[k] = SpecMatchJob{work[k].n_in, &work[k].incoming, &work[k].rd.diffuse_begin,
+                                   &work[k].rd.diffuse_end, &work[k].rd.outgoing_sorted, &work[k].rd.spec_match};
+        if (scan && *scan) (*scan)(va, jobs);
+        else spec_match_host(va, jobs);
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int k = 0; k < static_cast<int>(work.size()); ++k) finish(work[k]);
+        for (size_t k = 0; k < todo.size(); ++k) {
             facet_table[mid * nf + todo[k]] = static_cast<int>(tables.size());
-            tables.push_back(std::move(built[k]));
+            tables.push_back(std::move(work[k].rd));
         }
     }
 }
@@ -1051,7 +1103,7 @@ static void validate_layout(Problem& P, const SimulationConfig& cfg, const Simul
 }
 
 Problem build_problem(const SimulationConfig& cfg, SimulationDomain& domain,
-                      const std::vector<const PhononMaterial*>& mats) {
+                      const std::vector<const PhononMaterial*>& mats, const SpecMatchScan* scan) {
     if (mats.empty()) throw std::runtime_error("MonteCarloSolver requires at least one material.");
     if (!std::isfinite(cfg.time_step) || cfg.time_step <= 0) throw std::invalid_argument("time_step must be positive");
     Problem P;
@@ -1257,7 +1309,7 @@ Problem build_problem(const SimulationConfig& cfg, SimulationDomain& domain,
         const bool reflecting = F.condition != 'T' && !(F.condition == 'P' && F.pair >= 0);
         enabled.push_back(P.conservative ? reflecting : F.condition == 'R');
     }
-    P.rough.build(mats, normals, rough, enabled, P.conservative, P.conservative ? Tbg : 0.0);
+    P.rough.build(mats, normals, rough, enabled, P.conservative, P.conservative ? Tbg : 0.0, scan);
 
     // Interface banks (src/solver/InterfaceInitialization.cpp:3-15, InterfaceInteraction.cpp:11-41).
     P.iface.enabled = mats.size() > 1;

@@ -14,6 +14,7 @@
 
 #include <array>
 #include <cstdint>
+#include <functional>
 #include <map>
 #include <memory>
 #include <optional>
@@ -357,6 +358,9 @@ public:
     const SurfaceMesh* mesh() const { return mesh_.get(); }
     // voxel (ix*ny + iy)*nz + iz -> active cell (mesh domains; identity for boxes)
     const std::vector<int>& voxel_cells() const { return voxel_cell_; }
+    // active cell -> its home voxel, the voxel whose centre made the cell
+    // (mesh domains; the identity for boxes)
+    std::vector<int> cell_voxels() const;
     const Vec3& bounds_min() const { return bmin_; }
     const Vec3& bounds_max() const { return bmax_; }
     double volume() const { return volume_; }
@@ -478,14 +482,35 @@ struct RoughTable {
     std::vector<double> roulette_cdf;
 };
 
+// The specular-match scan of one facet's table (the O(modes x window) part
+// of RoughBoundarySampler::build, src/solver/RoughBoundarySampler.cpp:286-310):
+// for every incoming active mode ai with a window [begin[ai], end[ai]) of the
+// frequency-sorted outgoing modes `sorted`, match[ai] = the first mode of the
+// window that minimises |v_try - v_out| / max(1e-12, |v_try|, |v_out|), with
+// v_try = v_ai - 2 (v_ai . n_in) n_in; match[ai] stays -1 when none compares.
+struct SpecMatchJob {
+    Vec3 n_in;
+    const std::vector<int>* incoming;
+    const std::vector<int>* begin;
+    const std::vector<int>* end;
+    const std::vector<int>* sorted;
+    std::vector<int>* match;
+};
+// A scan over all jobs of one material (velocities of its active modes).
+using SpecMatchScan = std::function<void(const std::vector<Vec3>& velocities, std::vector<SpecMatchJob>& jobs)>;
+// The host scan (OpenMP over facets), in the reference's operation order.
+void spec_match_host(const std::vector<Vec3>& velocities, std::vector<SpecMatchJob>& jobs);
+
 // Builds one table per (material, enabled facet) exactly as the reference's
 // RoughBoundarySampler::build; facet_table[material * facets + facet] -> table.
+// `scan` replaces the host specular-match scan (the device solver passes the
+// GPU scan; the results are the same modes).
 struct RoughTables {
     std::vector<RoughTable> tables;
     std::vector<int> facet_table;
     void build(const std::vector<const PhononMaterial*>& mats, const std::vector<Vec3>& normals,
                const std::vector<double>& roughness, const std::vector<char>& enabled,
-               bool require_discrete, double equilibrium_temperature);
+               bool require_discrete, double equilibrium_temperature, const SpecMatchScan* scan = nullptr);
 };
 
 // ----------------------------------------------------- reservoir tables
@@ -592,7 +617,7 @@ struct Problem {
 
 // Builds every table. Materials must outlive the problem.
 Problem build_problem(const SimulationConfig& cfg, SimulationDomain& domain,
-                      const std::vector<const PhononMaterial*>& mats);
+                      const std::vector<const PhononMaterial*>& mats, const SpecMatchScan* scan = nullptr);
 
 // Initial carriers exactly as src/solver/Initialization.cpp:32-137 samples them,
 // with Philox draws: positions uniform in the box, modes uniform over the active

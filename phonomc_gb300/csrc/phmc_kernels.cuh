@@ -77,7 +77,9 @@ int launch_fused_transport(const BatchDesc& D, cudaStream_t stream, bool mixed);
 int launch_fused_cells(const BatchDesc& D, cudaStream_t stream);
 
 int launch_transport(const LaunchCtx& x, bool mixed, bool rta);
-int launch_mesh_cache_init(const LaunchCtx& x);
+int launch_mesh_cache_init(const LaunchCtx& x, bool mixed);
+// The specular-match scan of the rough-table build on the device (phmc_rough.cu).
+void spec_match_device(const std::vector<Vec3>& velocities, std::vector<SpecMatchJob>& jobs, cudaStream_t stream);
 void launch_histogram(const LaunchCtx& x, bool rta);
 void launch_init_cells(const LaunchCtx& x, bool mixed);
 // Carriers read straight from device-accessible (registered) host arrays.
@@ -192,6 +194,36 @@ void fill_dev_mesh(const MeshTracer& Tr, DevMesh& D, Upload&& up) {
             o[7 + a] = upf(r[7 + a]);
             scale = std::max({scale, std::abs(r[4 + a]), std::abs(r[7 + a])});
         }
+        // edge functions: inward in-plane unit normals of AB, BC, CA (FP64, then rounded)
+        const double* V = r + 10;
+        auto sub3 = [](const double* a, const double* b, double* o3) {
+            for (int k = 0; k < 3; ++k) o3[k] = a[k] - b[k];
+        };
+        auto cross3 = [](const double* a, const double* b, double* o3) {
+            o3[0] = a[1] * b[2] - a[2] * b[1];
+            o3[1] = a[2] * b[0] - a[0] * b[2];
+            o3[2] = a[0] * b[1] - a[1] * b[0];
+        };
+        double ab[3], ac[3], nrm[3];
+        sub3(V + 3, V, ab);
+        sub3(V + 6, V, ac);
+        cross3(ab, ac, nrm);
+        for (int e = 0; e < 3; ++e) {
+            const double* P0 = V + 3 * e;
+            const double* P1 = V + 3 * ((e + 1) % 3);
+            double d[3], m[3];
+            sub3(P1, P0, d);
+            cross3(nrm, d, m);
+            const double len = std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+            float* q = o + 10 + 4 * e;
+            if (!(len > 0.0) || !std::isfinite(len)) { // no edge test: never rejects
+                q[0] = q[1] = q[2] = 0.0f;
+                q[3] = -1e30f;
+                continue;
+            }
+            for (int k = 0; k < 3; ++k) q[k] = static_cast<float>(m[k] / len);
+            q[3] = static_cast<float>((m[0] * P0[0] + m[1] * P0[1] + m[2] * P0[2]) / len);
+        }
     }
     D.nodes32 = nodes32.empty() ? nullptr : up(nodes32);
     D.face32 = up(rec32);
@@ -233,6 +265,7 @@ void fill_dev_facets(const SimulationDomain& dom, double scale, DevFacets& G, Up
     G.shift = up(shift);
     G.normal = up(normal);
     G.voxel_cell = up(dom.voxel_cells());
+    G.cell_voxel = up(dom.cell_voxels());
     fill_dev_mesh(Tr, G.mesh, up);
     std::vector<double> sx;
     for (const auto& S : M.simplices()) {

@@ -80,13 +80,13 @@ DeviceSolver::DeviceSolver(const SimulationConfig& cfg, const std::vector<const 
         std::ofstream(std::filesystem::path(cfg_.output_folder) / "summary.txt") << format_domain_summary(cfg_, *domain_);
         std::ofstream(std::filesystem::path(cfg_.output_folder) / "grid_centers.csv") << format_grid_centers(*domain_);
     }
-    if (domain_->is_mesh()) {
-        if (mixed_)
-            throw std::runtime_error("Mesh domains run with plain FP64 carrier state (precision = fp64); the FP32 "
-                                     "cell-frame flight is built for box domains.");
-        if (mats_.size() != 1) throw std::runtime_error("Layered materials are built for box domains only.");
-    }
-    P_ = build_problem(cfg_, *domain_, mats_);
+    if (domain_->is_mesh() && mats_.size() != 1)
+        throw std::runtime_error("Layered materials are built for box domains only.");
+    // the specular-match scans of the rough tables run on the device
+    const SpecMatchScan scan = [this](const std::vector<Vec3>& va, std::vector<SpecMatchJob>& jobs) {
+        spec_match_device(va, jobs, stream_);
+    };
+    P_ = build_problem(cfg_, *domain_, mats_, &scan);
     ncells_ = domain_->grid_count();
     sort_interval_ = resolved_sort_interval(cfg_, mixed_);
     const int n0 = P_.initial_particles;
@@ -157,8 +157,8 @@ void DeviceSolver::allocate_state(int capacity) {
         state_.ox = dalloc<float>(padded);
         state_.oy = dalloc<float>(padded);
         state_.oz = dalloc<float>(padded);
-        state_.deferred = dalloc<int4>(capacity);
     }
+    state_.deferred = dalloc<int4>(capacity); // wall-event queue of the carrier pass
     if (domain_->is_mesh()) {
         // per-carrier mesh state lives in the facet tables (tables_.fac), filled by upload_mesh
         mesh_mirror_ = dalloc<int32_t>(capacity);
@@ -168,7 +168,6 @@ void DeviceSolver::allocate_state(int capacity) {
         mesh_hit_y_ = dalloc<double>(capacity);
         mesh_hit_z_ = dalloc<double>(capacity);
         mesh_hit_f_ = dalloc<int32_t>(capacity);
-        state_.deferred = dalloc<int4>(capacity); // wall-event queue of the mesh transport
     }
     state_.occ = dalloc<double>(padded);
     state_.mode = dalloc<uint32_t>(padded);
@@ -387,7 +386,9 @@ void DeviceSolver::upload_tables() {
         auto q = [](long long n, unsigned long long m) -> long long {
             return m ? static_cast<long long>((static_cast<unsigned __int128>(n) * m) >> 64) : n;
         };
-        for (long long c = 0; c < ncells_; ++c) {
+        // cell indices, and voxel indices of a mesh domain's grid
+        const long long n_index = std::max<long long>(ncells_, static_cast<long long>(D.shape[0]) * dyz);
+        for (long long c = 0; c < n_index; ++c) {
             const long long r = c % dyz;
             if (q(c, D.div_yz) != c / dyz || q(r, D.div_z) != r / dz)
                 throw std::runtime_error("cell index division constants failed their check");
@@ -698,7 +699,7 @@ void DeviceSolver::set_carriers(long long n, const double* x, const double* y, c
         else PHMC_CUDA(cudaMemsetAsync(state_.alive, 1, n * sizeof(uint8_t), stream_));
         launch_init_cells(c, mixed_);
     }
-    counters_.launches += 1 + launch_mesh_cache_init(c);
+    counters_.launches += 1 + launch_mesh_cache_init(c, mixed_);
     initial_statistics();
     if (!keep_clock) synchronize();
 }
@@ -939,6 +940,12 @@ void DeviceSolver::carrier_position(int slot, double p[3], int& facet) {
         PHMC_CUDA(cudaMemcpy(&o[1], state_.oy + slot, sizeof(float), cudaMemcpyDeviceToHost));
         PHMC_CUDA(cudaMemcpy(&o[2], state_.oz + slot, sizeof(float), cudaMemcpyDeviceToHost));
         const DevDomain& D = tables_.dom;
+        if (mesh_hit_f_) {
+            // offsets of a mesh carrier are measured from its cell's home voxel
+            if (cell_voxel_host_.empty()) cell_voxel_host_ = domain_->cell_voxels();
+            if (c >= 0 && c < static_cast<int>(cell_voxel_host_.size())) c = cell_voxel_host_[c];
+            PHMC_CUDA(cudaMemcpy(&facet, mesh_hit_f_ + slot, sizeof(int), cudaMemcpyDeviceToHost));
+        }
         const int idx[3] = {c / (D.shape[1] * D.shape[2]), (c / D.shape[2]) % D.shape[1], c % D.shape[2]};
         for (int a = 0; a < 3; ++a) p[a] = D.lo[a] + idx[a] * D.cell_size[a] + static_cast<double>(o[a]);
         return;

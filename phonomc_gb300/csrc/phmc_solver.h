@@ -214,6 +214,7 @@ private:
     int32_t* mesh_mirror_ = nullptr;
     double *mesh_hit_t_ = nullptr, *mesh_hit_x_ = nullptr, *mesh_hit_y_ = nullptr, *mesh_hit_z_ = nullptr;
     int32_t* mesh_hit_f_ = nullptr;
+    std::vector<int> cell_voxel_host_; // home voxels of a mesh domain's cells (error reports of the mixed state)
     void allocate_state(int capacity);
     void initial_statistics();
     void enqueue_step(bool profile);

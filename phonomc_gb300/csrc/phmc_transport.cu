@@ -399,24 +399,6 @@ __device__ bool advance_carrier_mesh(const DevTables& T, DevLedger* L, BlockLedg
     return true;
 }
 
-// Wall caches of every live carrier after an upload (src/solver/Initialization.cpp:131).
-__global__ void k_mesh_cache_init(const __grid_constant__ DevTables T, CarrierState S, DevLedger* L) {
-    const int n = L->n_slots;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        if (!S.alive[i]) continue;
-        const uint32_t w = S.mode[i];
-        double v[3];
-        mesh_velocity(T.fac, T.mat[w >> 28], w, T.fac.mirror[i], v);
-        double p[3] = {S.x[i], S.y[i], S.z[i]};
-        MeshCache c;
-        mesh_refresh(T, L, nullptr, i, p, v, c);
-        S.x[i] = p[0];
-        S.y[i] = p[1];
-        S.z[i] = p[2];
-        mesh_cache_store(T.fac, i, c);
-    }
-}
-
 // ------------------------------------------------------------------ bins
 __device__ __forceinline__ int bin_of(const DevMaterial& M, int ai) { return M.bin ? __ldg(M.bin + ai) : ai; }
 
@@ -452,18 +434,26 @@ __device__ __forceinline__ void bin_carrier(const DevTables& T, const CellArrays
 // run adds the partial sum of the lane o further on, when that lane is still
 // in the run -- every value is added once, so a run of L lanes costs L - 1
 // FP64 additions (GB300 retires two FP64 lanes per SM per clock).
+// Rounds run while o is below the longest run of the warp (`span`, from
+// run_span), so short runs cost one or two rounds instead of five.
 template <class T>
-__device__ __forceinline__ T run_sum_to_head(T v, unsigned heads, int lane) {
+__device__ __forceinline__ T run_sum_to_head(T v, unsigned heads, int lane, int span = 32) {
     const int start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
     const unsigned later = lane == 31 ? 0u : heads & (0xfffffffeu << lane);
     const int end = later ? __ffs(later) - 1 : 32; // first lane past the run
     const int pos = lane - start;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
+    for (int o = 1; o < span; o <<= 1) { // warp-uniform trip count
         const T w = __shfl_down_sync(0xffffffffu, v, o);
         if ((pos & (2 * o - 1)) == 0 && lane + o < end) v += w;
     }
     return v;
+}
+
+// Length of the longest run of the warp (all 32 lanes call).
+__device__ __forceinline__ int run_span(unsigned heads, int lane) {
+    const unsigned later = lane == 31 ? 0u : heads & (0xfffffffeu << lane);
+    const unsigned len = ((heads >> lane) & 1u) ? static_cast<unsigned>((later ? __ffs(later) - 1 : 32) - lane) : 0u;
+    return static_cast<int>(__reduce_max_sync(0xffffffffu, len));
 }
 
 // Bin tallies of one warp (all 32 lanes call; h < 0: nothing from this lane).
@@ -482,9 +472,10 @@ __device__ __forceinline__ void bin_warp(const CellArrays& C, long long h, doubl
         double N = h >= 0 ? occ : 0.0;
         double M = h >= 0 ? fmax(1.0, occ) : 0.0;
         if (heads != 0xffffffffu) { // warp-uniform: some run is longer than one lane
-            cnt = run_sum_to_head(cnt, heads, lane);
-            N = run_sum_to_head(N, heads, lane);
-            if (kRta) M = run_sum_to_head(M, heads, lane);
+            const int span = run_span(heads, lane);
+            cnt = run_sum_to_head(cnt, heads, lane, span);
+            N = run_sum_to_head(N, heads, lane, span);
+            if (kRta) M = run_sum_to_head(M, heads, lane, span);
         }
         if (h >= 0 && ((heads >> lane) & 1u)) bin_add(C, h, cnt, N, M, kRta);
     }
@@ -540,6 +531,101 @@ __device__ __forceinline__ void mode_velocity32(const DevMaterial& M, uint32_t w
     for (int k = 0; k < 3; ++k) {
         v[k] = ((w >> (24 + k)) & 1u) ? -c[k] : c[k];
         iv[k] = v[k] != 0.0f ? __frcp_rn(v[k]) : 0.0f;
+    }
+}
+
+// ------------------------------------- mixed carrier state in mesh domains
+// A mesh carrier keeps FP32 offsets from the corner of its cell's home voxel
+// (the voxel whose centre made the cell). A carrier may sit in a voxel whose
+// centre lies outside the mesh: that voxel belongs to a neighbouring cell
+// through the voxel map, and its offsets reach beyond the home voxel by the
+// voxels in between.
+__device__ __forceinline__ Frame cell_frame_of(const DevTables& T, int cell) {
+    return cell_frame(T.dom, T.fac.cell_voxel ? __ldg(T.fac.cell_voxel + cell) : cell);
+}
+
+// FP64 position of FP32 offsets in frame F.
+__device__ __forceinline__ void frame_point(const DevDomain& D, const Frame& F, const float o[3], double p[3]) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        p[a] = dadd(dadd(D.lo[a], dmul(static_cast<double>(F.i[a]), D.cell_size[a])), static_cast<double>(o[a]));
+}
+
+// FP32 offsets of an FP64 position from the home voxel of its cell; returns the cell.
+__device__ __forceinline__ int frame_offsets(const DevTables& T, const double p[3], float o[3]) {
+    const int c = cell_at(T, p[0], p[1], p[2]);
+    const Frame F = cell_frame_of(T, c);
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        o[a] = static_cast<float>(dadd(p[a], -dadd(T.dom.lo[a], dmul(static_cast<double>(F.i[a]), T.dom.cell_size[a]))));
+    return c;
+}
+
+// FP32 velocity of a mesh carrier: the mode velocity with its sign flips,
+// mirrored in the plane of facet `mir` when set.
+__device__ __forceinline__ void mesh_velocity32(const DevFacets& Fc, const DevMaterial& M, uint32_t w, int mir,
+                                                float v[3]) {
+    float iv[3];
+    mode_velocity32(M, w, v, iv);
+    if (mir >= 0) {
+        const double* n = Fc.normal + 3 * mir;
+        const float nn[3] = {static_cast<float>(n[0]), static_cast<float>(n[1]), static_cast<float>(n[2])};
+        const float s = 2.0f * (v[0] * nn[0] + v[1] * nn[1] + v[2] * nn[2]);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) v[k] -= nn[k] * s;
+    }
+}
+
+// Cell after an FP32 flight in frame F of a mesh domain: the voxel the point
+// ends in (clamped to the grid), its cell through the voxel map, and the
+// offsets moved to that cell's home voxel.
+__device__ __forceinline__ int settle_mesh(const DevTables& T, const Frame& F, float p[3]) {
+    const DevDomain& D = T.dom;
+    int j[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        int k = F.i[a] + static_cast<int>(floorf(p[a] * D.inv_cell32[a]));
+        j[a] = k < 0 ? 0 : (k >= D.shape[a] ? D.shape[a] - 1 : k);
+    }
+    const int c = __ldg(T.fac.voxel_cell + (j[0] * D.shape[1] + j[1]) * D.shape[2] + j[2]);
+    const Frame H = cell_frame_of(T, c);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) p[a] -= static_cast<float>(H.i[a] - F.i[a]) * F.cs[a];
+    return c;
+}
+
+// Wall caches of every live carrier after an upload (src/solver/Initialization.cpp:131).
+template <bool kMixed>
+__global__ void k_mesh_cache_init(const __grid_constant__ DevTables T, CarrierState S, DevLedger* L) {
+    const int n = L->n_slots;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (!S.alive[i]) continue;
+        const uint32_t w = S.mode[i];
+        double v[3];
+        mesh_velocity(T.fac, T.mat[w >> 28], w, T.fac.mirror[i], v);
+        double p[3];
+        if (kMixed) {
+            const float o[3] = {S.ox[i], S.oy[i], S.oz[i]};
+            frame_point(T.dom, cell_frame_of(T, S.cell[i]), o, p);
+        } else {
+            p[0] = S.x[i];
+            p[1] = S.y[i];
+            p[2] = S.z[i];
+        }
+        MeshCache c;
+        mesh_refresh(T, L, nullptr, i, p, v, c);
+        if (kMixed) {
+            float o[3];
+            S.cell[i] = frame_offsets(T, p, o);
+            S.ox[i] = o[0];
+            S.oy[i] = o[1];
+            S.oz[i] = o[2];
+        } else {
+            S.x[i] = p[0];
+            S.y[i] = p[1];
+            S.z[i] = p[2];
+        }
+        mesh_cache_store(T.fac, i, c);
     }
 }
 
@@ -870,8 +956,33 @@ __device__ __forceinline__ void flush_deferred(const CarrierState& S, DevLedger*
     }
 }
 
+// First queue entry of a thread in an event pass over a queue of length n:
+// entry 32 w + lane goes to warp w = (warp in block) x CTAs + CTA, so the
+// first entries spread one warp per CTA over every SM instead of filling the
+// first CTAs' warps (a short queue would otherwise run on a few SMs). Stride:
+// CTAs x block threads.
+__device__ __forceinline__ int queue_first(int vbx, int vgx) {
+    return ((static_cast<int>(threadIdx.x >> 5) * vgx + vbx) << 5) + static_cast<int>(threadIdx.x & 31);
+}
+
+// Queues slot i (lanes with `defer`) for an event pass: one global atomic per
+// warp; every lane of the warp calls it.
+__device__ __forceinline__ void queue_event(const CarrierState& S, DevLedger* L, bool defer, int i) {
+    const unsigned mask = __ballot_sync(0xffffffffu, defer);
+    if (!mask) return;
+    const int lane = threadIdx.x & 31;
+    int at = 0;
+    if (lane == 0) at = atomicAdd(&L->n_deferred, __popc(mask));
+    at = __shfl_sync(0xffffffffu, at, 0);
+    if (defer) {
+        const int q = at + __popc(mask & ((1u << lane) - 1u));
+        if (q < S.capacity) S.deferred[q] = make_int4(i, 0, 0, 0);
+        else raise_error(L, kErrInvalidStatistics, i);
+    }
+}
+
 // qbuf: kDeferBuffer entries per warp of the block (mixed path).
-template <bool kMixed, bool kRta, bool kAgg>
+template <bool kMixed, bool kRta, bool kAgg, bool kQueue = true>
 __device__ __forceinline__ void k_transport_body(const DevTables& T, CarrierState S, CellArrays C, DevLedger* L, int vbx,
                                                  int vgx, int4 (*qbuf)[kDeferBuffer]) {
     const uint32_t step = L->step_index; // timesteps completed: the draw counter of this step
@@ -898,11 +1009,16 @@ __device__ __forceinline__ void k_transport_body(const DevTables& T, CarrierStat
         }
         flush_deferred(S, L, qbuf, queued);
     } else {
-        // block-uniform trip count so that every lane reaches the warp tally
+        // kQueue (one material): carriers that cannot reach a wall within the
+        // step drift here; the others are queued, with their updated
+        // occupation, for k_box_events, so no warp of this pass waits on a few
+        // lanes' FP64 wall events. Layered materials run every flight here.
+        // block-uniform trip count so that every lane reaches the warp tally and ballot
         for (int base = vbx * blockDim.x; base < n; base += vgx * blockDim.x) {
             const int i = base + threadIdx.x;
             long long h = -1;
             double occ = 0.0;
+            bool defer = false;
             // all streamed fields in one memory round trip, alive included
             const bool in = i < n;
             const int ic = in ? i : 0;
@@ -913,25 +1029,90 @@ __device__ __forceinline__ void k_transport_body(const DevTables& T, CarrierStat
             double p[3] = {__ldcs(S.x + ic), __ldcs(S.y + ic), __ldcs(S.z + ic)};
             if (in && alive0) {
                 occ = apply_pending(T, C, c0, w, occ0);
-                const bool alive = advance_carrier(T, L, &bl, i, p, w, occ, T.par.dt, kDrawTransport, step);
-                const int c = grid_index(T.dom, p[0], p[1], p[2]);
-                __stcs(S.x + i, p[0]);
-                __stcs(S.y + i, p[1]);
-                __stcs(S.z + i, p[2]);
-                __stcs(S.mode + i, w);
-                __stcs(S.occ + i, occ);
-                if (!alive) {
-                    S.alive[i] = 0;
+                if constexpr (kQueue) {
+                    double v[3];
+                    mode_velocity(T.mat[w >> 28], w, v);
+                    const double dt = T.par.dt;
+                    if (clear_of_walls(T.dom, p, v, dt)) { // the first branch of advance_carrier
+#pragma unroll
+                        for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], dt));
+                        const int c = grid_index(T.dom, p[0], p[1], p[2]);
+                        __stcs(S.x + i, p[0]);
+                        __stcs(S.y + i, p[1]);
+                        __stcs(S.z + i, p[2]);
+                        __stcs(S.occ + i, occ);
+                        __stcs(S.cell + i, c);
+                        h = bin_slot(T, C, L, i, c, w, occ);
+                    } else {
+                        __stcs(S.occ + i, occ);
+                        defer = true;
+                    }
                 } else {
-                    __stcs(S.cell + i, c);
-                    h = bin_slot(T, C, L, i, c, w, occ);
+                    const bool alive = advance_carrier(T, L, &bl, i, p, w, occ, T.par.dt, kDrawTransport, step);
+                    const int c = grid_index(T.dom, p[0], p[1], p[2]);
+                    __stcs(S.x + i, p[0]);
+                    __stcs(S.y + i, p[1]);
+                    __stcs(S.z + i, p[2]);
+                    __stcs(S.mode + i, w);
+                    __stcs(S.occ + i, occ);
+                    if (!alive) {
+                        S.alive[i] = 0;
+                    } else {
+                        __stcs(S.cell + i, c);
+                        h = bin_slot(T, C, L, i, c, w, occ);
+                    }
                 }
             }
             bin_warp<kAgg, kRta>(C, h, occ);
+            if constexpr (kQueue) queue_event(S, L, defer, i);
         }
     }
     __syncthreads();
     block_ledger_flush(&bl, L);
+}
+
+// Plain FP64 wall events queued by the carrier pass: the whole flight of the
+// step from its start (occupation already updated) through advance_carrier,
+// then the cell and the bin. Every lane of a warp runs an event flight.
+template <bool kRta>
+__device__ __forceinline__ void k_box_events_body(const DevTables& T, CarrierState S, CellArrays C, DevLedger* L,
+                                                  int vbx, int vgx) {
+    const uint32_t step = L->step_index;
+    __shared__ BlockLedger bl;
+    block_ledger_init(&bl);
+    __syncthreads();
+    const int nq = min(L->n_deferred, S.capacity);
+    for (int q = queue_first(vbx, vgx); q < nq; q += vgx * blockDim.x) {
+        const int i = S.deferred[q].x;
+        if (i < 0 || i >= S.capacity) {
+            raise_error(L, kErrInvalidStatistics, i);
+            continue;
+        }
+        uint32_t w = S.mode[i];
+        double occ = S.occ[i];
+        double p[3] = {S.x[i], S.y[i], S.z[i]};
+        const bool alive = advance_carrier(T, L, &bl, i, p, w, occ, T.par.dt, kDrawTransport, step);
+        const int c = grid_index(T.dom, p[0], p[1], p[2]);
+        S.x[i] = p[0];
+        S.y[i] = p[1];
+        S.z[i] = p[2];
+        S.mode[i] = w;
+        S.occ[i] = occ;
+        if (!alive) {
+            S.alive[i] = 0;
+            continue;
+        }
+        S.cell[i] = c;
+        bin_carrier(T, C, L, i, c, w, occ, kRta);
+    }
+    __syncthreads();
+    block_ledger_flush(&bl, L);
+}
+
+template <bool kRta>
+__global__ void __launch_bounds__(256) k_box_events(const __grid_constant__ DevTables T, CarrierState S, CellArrays C,
+                                                    DevLedger* L) {
+    k_box_events_body<kRta>(T, S, C, L, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------- TMA-staged mixed carrier pass
@@ -1059,12 +1240,12 @@ __global__ void __launch_bounds__(kPipeTile) k_transport_pipe(const __grid_const
 
 // Block size chosen at launch (128, 256 or 512 threads); the wall-event queue
 // of the mixed path is dynamic shared memory, kDeferBuffer entries per warp.
-template <bool kMixed, bool kRta, bool kAgg>
+template <bool kMixed, bool kRta, bool kAgg, bool kQueue>
 __global__ void __launch_bounds__(kTransportMaxThreads) k_transport(const __grid_constant__ DevTables T, CarrierState S,
                                                                     CellArrays C, DevLedger* L) {
     extern __shared__ int4 qdyn[];
-    k_transport_body<kMixed, kRta, kAgg>(T, S, C, L, blockIdx.x, gridDim.x,
-                                         reinterpret_cast<int4 (*)[kDeferBuffer]>(qdyn));
+    k_transport_body<kMixed, kRta, kAgg, kQueue>(T, S, C, L, blockIdx.x, gridDim.x,
+                                                 reinterpret_cast<int4 (*)[kDeferBuffer]>(qdyn));
 }
 
 // Mesh transport, pass 1 of 2: apply the pending update and drift every
@@ -1072,9 +1253,10 @@ __global__ void __launch_bounds__(kTransportMaxThreads) k_transport(const __grid
 // drops by one step); carriers that do are queued, with their updated
 // occupation, for k_mesh_events. Warps thus run the FP64 BVH work only on
 // compacted event carriers.
-template <bool kRta>
+template <bool kRta, bool kMixedState>
 __global__ void __launch_bounds__(kTransportThreads) k_transport_mesh(const __grid_constant__ DevTables T, CarrierState S,
                                                                       CellArrays C, DevLedger* L) {
+    constexpr bool kMixed = kMixedState;
     const int n = L->n_slots;
     const double dt = T.par.dt;
     const int lane = threadIdx.x & 31;
@@ -1090,15 +1272,29 @@ __global__ void __launch_bounds__(kTransportThreads) k_transport_mesh(const __gr
             const double ht = __ldcs(T.fac.hit_t + i);
             const double t_wall = dmul(ht, dt);
             if (!isfinite(t_wall) || t_wall > dt) {
-                double v[3];
-                mesh_velocity(T.fac, T.mat[w >> 28], w, __ldcs(T.fac.mirror + i), v);
-                const double p[3] = {dadd(__ldcs(S.x + i), dmul(v[0], dt)), dadd(__ldcs(S.y + i), dmul(v[1], dt)),
-                                     dadd(__ldcs(S.z + i), dmul(v[2], dt))};
+                int c;
+                if (kMixed) {
+                    // FP32 flight in the frame of the home voxel, then the new cell
+                    float v[3];
+                    mesh_velocity32(T.fac, T.mat[w >> 28], w, __ldcs(T.fac.mirror + i), v);
+                    const float dt32 = T.par.dt32;
+                    float q[3] = {fmaf(v[0], dt32, __ldcs(S.ox + i)), fmaf(v[1], dt32, __ldcs(S.oy + i)),
+                                  fmaf(v[2], dt32, __ldcs(S.oz + i))};
+                    c = settle_mesh(T, cell_frame_of(T, c0), q);
+                    __stcs(S.ox + i, q[0]);
+                    __stcs(S.oy + i, q[1]);
+                    __stcs(S.oz + i, q[2]);
+                } else {
+                    double v[3];
+                    mesh_velocity(T.fac, T.mat[w >> 28], w, __ldcs(T.fac.mirror + i), v);
+                    const double p[3] = {dadd(__ldcs(S.x + i), dmul(v[0], dt)), dadd(__ldcs(S.y + i), dmul(v[1], dt)),
+                                         dadd(__ldcs(S.z + i), dmul(v[2], dt))};
+                    c = cell_at(T, p[0], p[1], p[2]);
+                    __stcs(S.x + i, p[0]);
+                    __stcs(S.y + i, p[1]);
+                    __stcs(S.z + i, p[2]);
+                }
                 if (isfinite(ht)) __stcs(T.fac.hit_t + i, dadd(ht, -(dt / dt)));
-                const int c = cell_at(T, p[0], p[1], p[2]);
-                __stcs(S.x + i, p[0]);
-                __stcs(S.y + i, p[1]);
-                __stcs(S.z + i, p[2]);
                 __stcs(S.occ + i, occ);
                 __stcs(S.cell + i, c);
                 h = bin_slot(T, C, L, i, c, w, occ);
@@ -1109,23 +1305,13 @@ __global__ void __launch_bounds__(kTransportThreads) k_transport_mesh(const __gr
             }
         }
         bin_warp<true, kRta>(C, h, hocc);
-        const unsigned mask = __ballot_sync(0xffffffffu, defer);
-        if (mask) {
-            int at = 0;
-            if (lane == 0) at = atomicAdd(&L->n_deferred, __popc(mask));
-            at = __shfl_sync(0xffffffffu, at, 0);
-            if (defer) {
-                const int q = at + __popc(mask & ((1u << lane) - 1u));
-                if (q < S.capacity) S.deferred[q] = make_int4(i, 0, 0, 0);
-                else raise_error(L, kErrInvalidStatistics, i);
-            }
-        }
+        queue_event(S, L, defer, i);
     }
 }
 
 // Mesh transport, pass 2 of 2: the full flight of every queued carrier from
 // the start of the step (occupation already updated), then its cell and bin.
-template <bool kRta>
+template <bool kRta, bool kMixed>
 __global__ void __launch_bounds__(kTransportThreads, 1) k_mesh_events(const __grid_constant__ DevTables T, CarrierState S,
                                                                    CellArrays C, DevLedger* L) {
     const uint32_t step = L->step_index;
@@ -1133,7 +1319,7 @@ __global__ void __launch_bounds__(kTransportThreads, 1) k_mesh_events(const __gr
     block_ledger_init(&bl);
     __syncthreads();
     const int nq = min(L->n_deferred, S.capacity);
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+    for (int q = queue_first(blockIdx.x, gridDim.x); q < nq; q += gridDim.x * blockDim.x) {
         const int i = S.deferred[q].x;
         if (i < 0 || i >= S.capacity) {
             raise_error(L, kErrInvalidStatistics, i);
@@ -1141,7 +1327,16 @@ __global__ void __launch_bounds__(kTransportThreads, 1) k_mesh_events(const __gr
         }
         uint32_t w = S.mode[i];
         double occ = S.occ[i];
-        double p[3] = {S.x[i], S.y[i], S.z[i]};
+        double p[3];
+        if (kMixed) {
+            // FP64 position of the FP32 offsets; the events run in FP64
+            const float o[3] = {S.ox[i], S.oy[i], S.oz[i]};
+            frame_point(T.dom, cell_frame_of(T, S.cell[i]), o, p);
+        } else {
+            p[0] = S.x[i];
+            p[1] = S.y[i];
+            p[2] = S.z[i];
+        }
         const int mir0 = T.fac.mirror[i];
         int mir = mir0;
         MeshCache mc;
@@ -1150,16 +1345,25 @@ __global__ void __launch_bounds__(kTransportThreads, 1) k_mesh_events(const __gr
         const bool alive = advance_carrier_mesh(T, L, &bl, i, p, w, mir, occ, mc, T.par.dt, kDrawTransport, step);
         if (mir != mir0) T.fac.mirror[i] = mir;
         mesh_cache_store(T.fac, i, mc);
-        S.x[i] = p[0];
-        S.y[i] = p[1];
-        S.z[i] = p[2];
+        int c;
+        if (kMixed) {
+            float o[3];
+            c = frame_offsets(T, p, o);
+            S.ox[i] = o[0];
+            S.oy[i] = o[1];
+            S.oz[i] = o[2];
+        } else {
+            S.x[i] = p[0];
+            S.y[i] = p[1];
+            S.z[i] = p[2];
+            c = cell_at(T, p[0], p[1], p[2]);
+        }
         S.mode[i] = w;
         S.occ[i] = occ;
         if (!alive) {
             S.alive[i] = 0;
             continue;
         }
-        const int c = cell_at(T, p[0], p[1], p[2]);
         S.cell[i] = c;
         bin_carrier(T, C, L, i, c, w, occ, kRta);
     }
@@ -1179,7 +1383,7 @@ __device__ __forceinline__ void k_deferred_body(const DevTables& T, CarrierState
     block_ledger_init(&bl);
     __syncthreads();
     const int nq = min(L->n_deferred, S.capacity);
-    for (int q = vbx * blockDim.x + threadIdx.x; q < nq; q += vgx * blockDim.x) {
+    for (int q = queue_first(vbx, vgx); q < nq; q += vgx * blockDim.x) {
         const int4 e = S.deferred[q];
         const int i = e.x;
         if (i < 0 || i >= S.capacity) {
@@ -1238,7 +1442,7 @@ __global__ void k_init_cells(const DevTables* __restrict__ Tp, CarrierState S, D
         S.cell[i] = c;
         if (Tp->fac.mirror) Tp->fac.mirror[i] = -1;
         if (kMixed) {
-            const Frame F = cell_frame(D, c);
+            const Frame F = cell_frame_of(*Tp, c);
             S.ox[i] = static_cast<float>(S.x[i] - (D.lo[0] + F.i[0] * D.cell_size[0]));
             S.oy[i] = static_cast<float>(S.y[i] - (D.lo[1] + F.i[1] * D.cell_size[1]));
             S.oz[i] = static_cast<float>(S.z[i] - (D.lo[2] + F.i[2] * D.cell_size[2]));
@@ -1262,7 +1466,7 @@ __global__ void k_ingest(const __grid_constant__ DevTables T, CarrierState S, De
         S.cell[i] = c;
         if (T.fac.mirror) T.fac.mirror[i] = -1;
         if (kMixed) {
-            const Frame F = cell_frame(D, c);
+            const Frame F = cell_frame_of(T, c);
             S.ox[i] = static_cast<float>(x - (D.lo[0] + F.i[0] * D.cell_size[0]));
             S.oy[i] = static_cast<float>(y - (D.lo[1] + F.i[1] * D.cell_size[1]));
             S.oz[i] = static_cast<float>(z - (D.lo[2] + F.i[2] * D.cell_size[2]));
@@ -1298,7 +1502,7 @@ __global__ void k_positions_out(const DevTables* __restrict__ Tp, CarrierState S
     const DevDomain& D = Tp->dom;
     const int n = L->n_slots;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const Frame F = cell_frame(D, S.cell[i]);
+        const Frame F = cell_frame_of(*Tp, S.cell[i]);
         S.x[i] = D.lo[0] + F.i[0] * D.cell_size[0] + static_cast<double>(S.ox[i]);
         S.y[i] = D.lo[1] + F.i[1] * D.cell_size[1] + static_cast<double>(S.oy[i]);
         S.z[i] = D.lo[2] + F.i[2] * D.cell_size[2] + static_cast<double>(S.oz[i]);
@@ -1486,7 +1690,27 @@ __device__ __forceinline__ void k_inject_body(const DevTables* __restrict__ Tp, 
         const double remain = P.dt - temit;
         bool alive = true;
         int c;
-        if (kMixed) {
+        if (kMesh) {
+            int mir = -1;
+            MeshCache mc;
+            mesh_refresh(T, L, &bl, slot, p, v, mc); // src/MonteCarloSolver.cpp:318-327
+            if (remain > 1e-14)
+                alive = advance_carrier_mesh(T, L, &bl, slot, p, w, mir, occ, mc, remain, kDrawInjected, step);
+            T.fac.mirror[slot] = mir;
+            mesh_cache_store(T.fac, slot, mc);
+            if (kMixed) {
+                float o[3];
+                c = frame_offsets(T, p, o);
+                S.ox[slot] = o[0];
+                S.oy[slot] = o[1];
+                S.oz[slot] = o[2];
+            } else {
+                c = cell_at(T, p[0], p[1], p[2]);
+                S.x[slot] = p[0];
+                S.y[slot] = p[1];
+                S.z[slot] = p[2];
+            }
+        } else if (kMixed) {
             c = grid_index(T.dom, p[0], p[1], p[2]);
             const Frame F = cell_frame(T.dom, c);
             float q[3];
@@ -1501,18 +1725,6 @@ __device__ __forceinline__ void k_inject_body(const DevTables* __restrict__ Tp, 
             S.ox[slot] = q[0];
             S.oy[slot] = q[1];
             S.oz[slot] = q[2];
-        } else if (kMesh) {
-            int mir = -1;
-            MeshCache mc;
-            mesh_refresh(T, L, &bl, slot, p, v, mc); // src/MonteCarloSolver.cpp:318-327
-            if (remain > 1e-14)
-                alive = advance_carrier_mesh(T, L, &bl, slot, p, w, mir, occ, mc, remain, kDrawInjected, step);
-            T.fac.mirror[slot] = mir;
-            mesh_cache_store(T.fac, slot, mc);
-            c = cell_at(T, p[0], p[1], p[2]);
-            S.x[slot] = p[0];
-            S.y[slot] = p[1];
-            S.z[slot] = p[2];
         } else {
             if (remain > 1e-14) alive = advance_carrier(T, L, &bl, slot, p, w, occ, remain, kDrawInjected, step);
             c = grid_index(T.dom, p[0], p[1], p[2]);
@@ -1558,7 +1770,7 @@ __global__ void k_containment(const DevTables* __restrict__ Tp, CarrierState S, 
         if (!S.alive[i]) continue;
         double p[3];
         if (kMixed) {
-            const Frame F = cell_frame(D, S.cell[i]);
+            const Frame F = cell_frame_of(*Tp, S.cell[i]);
             p[0] = D.lo[0] + F.i[0] * D.cell_size[0] + S.ox[i];
             p[1] = D.lo[1] + F.i[1] * D.cell_size[1] + S.oy[i];
             p[2] = D.lo[2] + F.i[2] * D.cell_size[2] + S.oz[i];
@@ -1575,61 +1787,92 @@ __global__ void k_containment(const DevTables* __restrict__ Tp, CarrierState S, 
             const int in = mesh_contains(Tp->fac, p);
             if (in < 0) raise_error(L, kErrInvalidStatistics, i);
             outside = in == 0;
+            // the mixed state may sit outside a wall by its FP32 rounding:
+            // escaped only when farther from the surface than that
+            if (kMixed && outside) outside = !(mesh_surface_distance(Tp->fac, p) <= t);
         }
         if (outside) raise_error(L, kErrEscaped, i);
     }
 }
 
+// Sums of x[0..2] over the lanes of `peers` (the lanes that hold the same
+// key), left in the lowest lane of each group: a tree over every group at
+// once in at most five rounds (reduce-by-key of warp-aggregated atomics).
+__device__ __forceinline__ void reduce_peers3(unsigned peers, double x[3]) {
+    const int lane = threadIdx.x & 31;
+    unsigned rel = __popc(peers & ((1u << lane) - 1u)); // rank in the group
+    unsigned above = peers & (0xfffffffeu << lane);      // group lanes above this one
+    while (__any_sync(0xffffffffu, above != 0u)) {
+        const int next = above ? __ffs(above) - 1 : lane;
+        double t[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) t[a] = __shfl_sync(0xffffffffu, x[a], next);
+        if (above) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) x[a] = dadd(x[a], t[a]);
+        }
+        // odd ranks have been read by their lower neighbour: out of every group
+        above &= ~__ballot_sync(0xffffffffu, rel & 1u);
+        rel >>= 1;
+    }
+}
+
 // Heat-flux tally q_c = sum v e w (src/solver/GridStatistics.cpp:269-347) with the
-// end-of-step occupation n = alpha n + beta - (second drive half). Carriers
-// sorted by mode put one mode in most warps: such a warp shares one velocity,
-// so it sums the energies of each run of equal cells with a segmented shuffle
-// scan and adds v * sum once per run (no shared-memory atomic contention on
-// the few cells a warp covers); other warps add per carrier.
+// end-of-step occupation n = alpha n + beta - (second drive half). The lanes of
+// a warp that share a cell sum their v e first (reduce_peers3), so one lane
+// per cell adds. `target`: 2 one private copy of the cell sums per warp in
+// shared memory (plain adds: within a warp the adding lanes hold distinct
+// cells), 1 one copy per block (shared atomics), 0 the global sums.
 __global__ void __launch_bounds__(256) k_flux(const DevTables* __restrict__ Tp, CarrierState S, CellArrays C,
-                                              const DevLedger* L, int use_shared) {
+                                              const DevLedger* L, int target) {
     extern __shared__ double sq[];
     const DevTables& T = *Tp;
-    if (use_shared)
-        for (int k = threadIdx.x; k < 3 * C.ncells; k += blockDim.x) sq[k] = 0.0;
+    const int nq = 3 * C.ncells;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    if (target > 0)
+        for (int k = threadIdx.x; k < (target == 2 ? nwarps : 1) * nq; k += blockDim.x) sq[k] = 0.0;
     __syncthreads();
-    double* dst = use_shared ? sq : C.flux;
+    double* dst = target == 2 ? sq + warp * nq : (target == 1 ? sq : C.flux);
     const int n = L->n_slots;
-    const int lane = threadIdx.x & 31;
     for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const int i = base + threadIdx.x;
         const int ic = i < n ? i : 0;
         const bool live = i < n && S.alive[ic];
         const uint32_t w = S.mode[ic];
         const int c = live ? S.cell[ic] : -1;
-        double e = 0.0;
-        double v[3] = {0.0, 0.0, 0.0};
+        double f[3] = {0.0, 0.0, 0.0};
         if (live) {
             const DevMaterial& M = T.mat[w >> 28];
             const int ai = static_cast<int>(w & 0x00FFFFFFu);
             double occ = apply_pending(T, C, c, w, S.occ[ic]) - drive_half(T, C, M, c, ai);
             if (C.src_next) occ -= C.src_next[static_cast<size_t>(c) * C.hist_modes + bin_of(M, ai)];
-            e = dmul(dmul(M.hw[ai], occ - M.nbg[ai]), M.energy_weight);
+            const double e = dmul(dmul(M.hw[ai], occ - M.nbg[ai]), M.energy_weight);
+            double v[3];
             if (T.fac.mirror) mesh_velocity(T.fac, M, w, T.fac.mirror[ic], v);
             else mode_velocity(M, w, v);
+#pragma unroll
+            for (int a = 0; a < 3; ++a) f[a] = dmul(v[a], e);
         }
-        const uint32_t w0 = __shfl_sync(0xffffffffu, w, 0);
-        const bool one_mode = !T.fac.mirror && __all_sync(0xffffffffu, !live || w == w0) &&
-                              __any_sync(0xffffffffu, live);
-        if (one_mode) {
-            const int cp = __shfl_up_sync(0xffffffffu, c, 1);
-            const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || cp != c);
-            e = run_sum_to_head(e, heads, lane);
-            if (live && ((heads >> lane) & 1u))
-                for (int a = 0; a < 3; ++a) atomicAdd(dst + 3 * c + a, dmul(v[a], e));
-        } else if (live) {
-            for (int a = 0; a < 3; ++a) atomicAdd(dst + 3 * c + a, dmul(v[a], e));
+        const unsigned peers = __match_any_sync(0xffffffffu, c);
+        reduce_peers3(peers, f);
+        if (live && lane == __ffs(peers) - 1) {
+            if (target == 2) {
+#pragma unroll
+                for (int a = 0; a < 3; ++a) dst[3 * c + a] = dadd(dst[3 * c + a], f[a]);
+            } else {
+#pragma unroll
+                for (int a = 0; a < 3; ++a) atomicAdd(dst + 3 * c + a, f[a]);
+            }
         }
+        if (target == 2) __syncwarp();
     }
     __syncthreads();
-    if (use_shared)
-        for (int k = threadIdx.x; k < 3 * C.ncells; k += blockDim.x)
-            if (sq[k] != 0.0) atomicAdd(C.flux + k, sq[k]);
+    if (target > 0)
+        for (int k = threadIdx.x; k < nq; k += blockDim.x) {
+            double sum = 0.0;
+            for (int q = 0; q < (target == 2 ? nwarps : 1); ++q) sum = dadd(sum, sq[q * nq + k]);
+            if (sum != 0.0) atomicAdd(C.flux + k, sum);
+        }
 }
 
 // Apply the pending update to the stored occupations, optionally leaving the
@@ -1678,15 +1921,20 @@ void launch_transport_pass(const LaunchCtx& x, dim3 g) {
     }
     const int threads = x.transport_block;
     const size_t sh = kMixed ? static_cast<size_t>(threads / 32) * kDeferBuffer * sizeof(int4) : 0;
-    if (x.tally_agg) k_transport<kMixed, kRta, true><<<g, threads, sh, x.stream>>>(*x.Th, x.S, x.C, x.L);
-    else k_transport<kMixed, kRta, false><<<g, threads, sh, x.stream>>>(*x.Th, x.S, x.C, x.L);
+    if (!kMixed && x.Th->par.n_materials > 1) { // layered: every flight in the pass
+        if (x.tally_agg) k_transport<kMixed, kRta, true, false><<<g, threads, sh, x.stream>>>(*x.Th, x.S, x.C, x.L);
+        else k_transport<kMixed, kRta, false, false><<<g, threads, sh, x.stream>>>(*x.Th, x.S, x.C, x.L);
+        return;
+    }
+    if (x.tally_agg) k_transport<kMixed, kRta, true, true><<<g, threads, sh, x.stream>>>(*x.Th, x.S, x.C, x.L);
+    else k_transport<kMixed, kRta, false, true><<<g, threads, sh, x.stream>>>(*x.Th, x.S, x.C, x.L);
 }
 
 int launch_transport(const LaunchCtx& x, bool mixed, bool rta) {
     if (x.transport_block != 128 && x.transport_block != 256 && x.transport_block != 512)
         throw std::invalid_argument("transport_block must be 128, 256 or 512 threads");
     const dim3 g(x.grid_blocks), b(kTransportThreads);
-    if (mixed) {
+    if (mixed && !x.mesh) {
         // the carrier pass at the configured block size; the deferred wall events at 256
         const dim3 gp(x.transport_grid);
         if (rta) {
@@ -1699,18 +1947,28 @@ int launch_transport(const LaunchCtx& x, bool mixed, bool rta) {
         return 2;
     }
     if (x.mesh) {
-        if (rta) {
-            k_transport_mesh<true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
-            k_mesh_events<true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+        if (mixed && rta) {
+            k_transport_mesh<true, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+            k_mesh_events<true, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+        } else if (mixed) {
+            k_transport_mesh<false, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+            k_mesh_events<false, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+        } else if (rta) {
+            k_transport_mesh<true, false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+            k_mesh_events<true, false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
         } else {
-            k_transport_mesh<false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
-            k_mesh_events<false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+            k_transport_mesh<false, false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+            k_mesh_events<false, false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
         }
         return 2;
     }
     if (rta) launch_transport_pass<false, true>(x, dim3(x.transport_grid));
     else launch_transport_pass<false, false>(x, dim3(x.transport_grid));
-    return 1;
+    if (x.Th->par.n_materials > 1) return 1;
+    // wall events queued by the pass
+    if (rta) k_box_events<true><<<g, 256, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+    else k_box_events<false><<<g, 256, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+    return 2;
 }
 
 void launch_histogram(const LaunchCtx& x, bool rta) {
@@ -1764,9 +2022,10 @@ void launch_mesh_initial_positions(const LaunchCtx& x, int n, uint64_t seed, con
                                                        make_double3(hi[0], hi[1], hi[2]), xyz);
 }
 
-int launch_mesh_cache_init(const LaunchCtx& x) {
+int launch_mesh_cache_init(const LaunchCtx& x, bool mixed) {
     if (!x.mesh) return 0;
-    k_mesh_cache_init<<<x.grid_blocks, 128, 0, x.stream>>>(*x.Th, x.S, x.L);
+    if (mixed) k_mesh_cache_init<true><<<x.grid_blocks, 128, 0, x.stream>>>(*x.Th, x.S, x.L);
+    else k_mesh_cache_init<false><<<x.grid_blocks, 128, 0, x.stream>>>(*x.Th, x.S, x.L);
     return 1;
 }
 
@@ -1780,7 +2039,10 @@ int launch_inject(const LaunchCtx& x, bool mixed, bool rta, int* holes, int* blo
     k_inject_prepare<<<1, 1024, 0, x.stream>>>(x.T, x.L, block_dead, nb, capacity);
     k_dead_write<<<nb, kHoleBlock, 0, x.stream>>>(x.S, x.L, block_dead, holes);
     const dim3 g(x.grid_blocks), b(256);
-    if (mixed) {
+    if (mixed && x.mesh) {
+        if (rta) k_inject<true, true, true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes);
+        else k_inject<true, false, true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes);
+    } else if (mixed) {
         if (rta) k_inject<true, true><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes);
         else k_inject<true, false><<<g, b, 0, x.stream>>>(x.T, x.S, x.C, x.L, holes);
     } else if (x.mesh) {
@@ -1800,9 +2062,12 @@ void launch_containment(const LaunchCtx& x, bool mixed) {
 }
 
 void launch_flux(const LaunchCtx& x, bool /*mixed*/) {
-    const size_t sh = 3 * sizeof(double) * static_cast<size_t>(x.C.ncells);
-    const int use_shared = sh <= 32768 ? 1 : 0;
-    k_flux<<<x.grid_blocks, 256, use_shared ? sh : 0, x.stream>>>(x.T, x.S, x.C, x.L, use_shared);
+    const size_t per_copy = 3 * sizeof(double) * static_cast<size_t>(x.C.ncells);
+    // a private copy per warp (8 per CTA) up to 48 KB, else one per CTA up to
+    // 32 KB, else the global sums
+    const int target = 8 * per_copy <= 49152 ? 2 : (per_copy <= 32768 ? 1 : 0);
+    const size_t sh = target == 2 ? 8 * per_copy : (target == 1 ? per_copy : 0);
+    k_flux<<<x.grid_blocks, 256, sh, x.stream>>>(x.T, x.S, x.C, x.L, target);
 }
 
 void launch_apply_pending(const LaunchCtx& x, bool subtract_drive) {
@@ -1853,6 +2118,19 @@ __global__ void __launch_bounds__(kTransportThreads) kf_transport(const BatchDes
     }
 }
 
+template <bool kRta>
+__global__ void __launch_bounds__(kTransportThreads) kf_box_events(const BatchDesc D) {
+    __shared__ SharedTables st;
+    if (threadIdx.x == 0) st.owner = -1;
+    __syncthreads();
+    for (int vb = blockIdx.x; vb < D.total_carrier_blocks; vb += gridDim.x) {
+        const int i = batch_find(D.carrier_block, D.n, vb);
+        const int b0 = D.carrier_block[i];
+        const DevTables& T = stage_tables(st, D, i);
+        k_box_events_body<kRta>(T, D.states[i], D.cells[i], D.ledgers[i], vb - b0, D.carrier_block[i + 1] - b0);
+        __syncthreads();
+    }
+}
 template <bool kRta>
 __global__ void __launch_bounds__(kTransportThreads) kf_deferred(const BatchDesc D) {
     __shared__ SharedTables st;
@@ -1958,6 +2236,7 @@ int launch_fused_transport(const BatchDesc& D, cudaStream_t s, bool mixed) {
         kf_deferred<true><<<g, kTransportThreads, 0, s>>>(D);
     } else {
         kf_transport<false, true><<<g, kTransportThreads, 0, s>>>(D);
+        kf_box_events<true><<<g, kTransportThreads, 0, s>>>(D);
     }
     kf_dead_count<<<gh, 256, 0, s>>>(D);
     kf_inject_prepare<<<D.n, 1024, 0, s>>>(D);
@@ -1965,7 +2244,7 @@ int launch_fused_transport(const BatchDesc& D, cudaStream_t s, bool mixed) {
     if (mixed) kf_inject<true, true><<<gi, 256, 0, s>>>(D);
     else kf_inject<false, true><<<gi, 256, 0, s>>>(D);
     kf_inject_finish<<<D.n, 32, 0, s>>>(D);
-    return mixed ? 7 : 6;
+    return 7;
 }
 
 } // namespace phmc

@@ -8,19 +8,19 @@
 namespace phmc {
 namespace tuning {
 // Threads per CTA of the carrier pass (128, 256 or 512).
-constexpr int kTransportBlock[2] = {256, 256};
+constexpr int kTransportBlock[2] = {128, 512};
 // Resident CTAs per SM of the carrier pass (grid = SMs x this, fewer for
 // small populations): sets the carriers each thread walks.
-constexpr int kTransportBlocksPerSm[2] = {8, 8};
+constexpr int kTransportBlocksPerSm[2] = {16, 2};
 // Steps between carrier sorts by (mode, cell), or by (cell, mode) in mesh
 // domains (0: never), and the smallest population that is sorted at all.
-constexpr int kSortInterval[2] = {50, 50};
+constexpr int kSortInterval[2] = {50, 200};
 constexpr double kSortMinCarriers = 2e+06;
 // Bin tallies of the carrier pass: 1 sums runs of equal (cell, bin) across
 // the lanes of a warp before one FP64 atomic per run, 0 one atomic per carrier.
-constexpr int kTallyAggregation[2] = {1, 1};
+constexpr int kTallyAggregation[2] = {0, 1};
 // Mixed carrier pass: carrier tiles staged in shared memory by bulk
 // asynchronous copies one tile ahead (1), or loaded directly (0).
-constexpr int kTransportPipeline = 1;
+constexpr int kTransportPipeline = 0;
 } // namespace tuning
 } // namespace phmc

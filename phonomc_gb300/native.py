@@ -22,7 +22,7 @@ BUILD = os.path.join(HERE, "_build")
 OUT = os.path.join(BUILD, "libphonomc_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CXX_SOURCES = ["phmc_host.cpp", "phmc_mesh.cpp", "phmc_output.cpp", "phmc_hdf5.cpp", "phmc_amm.cpp"]
-CU_SOURCES = ["phmc_transport.cu", "phmc_cells.cu", "phmc_solver.cu", "phmc_capi.cu", "phmc_noalloc.cu", "phmc_sort.cu"]
+CU_SOURCES = ["phmc_transport.cu", "phmc_cells.cu", "phmc_solver.cu", "phmc_capi.cu", "phmc_noalloc.cu", "phmc_sort.cu", "phmc_rough.cu"]
 HEADERS = ["phmc_host.h", "phmc_pod.h", "phmc_rng.h", "phmc_device.cuh", "phmc_solver.h", "phmc_kernels.cuh", "phmc_tuning.h", "phmc_sort.cuh", "phmc_hdf5.h"]
 
 _lock = threading.Lock()

@@ -226,6 +226,70 @@ def test_mixed_tracks_plain_trajectory(gpu, name, stationary):
     assert abs(st["step_energy_balance_residual_ev"]) < 1e-12 * abs(st["total_thermal_energy_ev"])
 
 
+@pytest.mark.parametrize("conservative", [0, 1])
+def test_rough_table_device_scan_matches_host(gpu, conservative):
+    """Rough-table specular matches from the device scan (FP32 screen, FP64
+    decision) equal the host loop's for 96 facets of random orientation and
+    the synthetic tables: the same outgoing mode for every incoming mode."""
+    # conservative walls need the full-zone Callaway bank (8^3 x 6 completed: 24,552 modes)
+    mat = synthetic.make_material(mesh=8 if conservative else 16, callaway=bool(conservative))
+    m = abi.Material(gpu, "phmc_", mat, 0.1, bool(conservative), bool(conservative))
+    na = C.c_int32()
+    assert gpu.phmc_material_active_count(m.h, C.byref(na)) == 0
+    rng = np.random.default_rng(11)
+    nf = 96
+    nrm = rng.normal(size=(nf, 3))
+    nrm[:6] = [[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1]]  # axis-aligned: many ties
+    nrm /= np.linalg.norm(nrm, axis=1)[:, None]
+    nrm = np.ascontiguousarray(nrm)
+    rough = np.full(nf, 10.0)
+    out = {}
+    for dev in (0, 1):
+        match = np.zeros(nf * na.value, np.int32)
+        rc = gpu.phmc_dev_rough_spec_match(m.h, conservative, 300.0, nf, D(nrm), D(rough), dev, I32(match))
+        assert rc == 0, gpu.phmc_last_error()
+        out[dev] = match
+    assert (out[1] >= 0).sum() > nf * na.value // 4
+    assert np.array_equal(out[0], out[1])
+
+
+def test_mixed_mesh_tracks_plain_trajectory(gpu, tmp_path):
+    """FinFET mesh, same seed and draws: the FP32 offsets (from each cell's
+    home voxel) follow the FP64 positions up to FP32 rounding, wall events and
+    injections pick the same modes, cells agree, and the energy ledger closes."""
+    stl = workloads.finfet_stl(str(tmp_path / "finfet.stl"))
+    mat = synthetic.make_material(mesh=8)
+    m = abi.Material(gpu, "phmc_", mat, 0.1, False, False)
+    base = workloads.finfet_mesh(stl, particles=40000, seed=31, grid=(32, 16, 16))
+    sp = abi.Solver(gpu, "phmc_", dict(base, precision="fp64"), [m])
+    sm = abi.Solver(gpu, "phmc_", dict(base, precision="mixed"), [m])
+    c0p, c0m = sp.carriers(), sm.carriers()
+    live0 = c0p["alive"] == 1
+    for k in ("x", "y", "z"):  # the initial population through the offsets
+        assert np.max(np.abs(c0p[k][live0] - c0m[k][live0])) < 1e-3
+    assert np.array_equal(c0p["cell"][live0], c0m["cell"][live0])
+    sp.run(8)
+    sm.run(8)
+    cp, cm = sp.carriers(), sm.carriers()
+    a = (cp["alive"] == 1) & (cm["alive"] == 1)
+    assert a.mean() > 0.99
+    assert np.mean(cp["mode"][a] == cm["mode"][a]) > 0.999
+    assert np.mean(cp["cell"][a] == cm["cell"][a]) > 0.999
+    for k in ("x", "y", "z"):
+        d = np.abs(cp[k][a] - cm[k][a])
+        assert np.median(d) < 1e-3, (k, np.median(d))
+    Tp, _, _ = sp.cells()
+    Tm, _, _ = sm.cells()
+    # a few carriers per cell: a cell whose one carrier took another event
+    # path differs by a carrier's energy; nearly all cells agree to rounding
+    assert np.mean(np.abs(Tp - Tm) < 1e-4) > 0.99
+    for s in (sp, sm):
+        st = s.stats()
+        assert abs(st["step_energy_balance_residual_ev"]) < 1e-9 * abs(st["total_thermal_energy_ev"])
+    sm.close()
+    sp.close()
+
+
 def test_mixed_energy_conservation_linearized(gpu):
     """The FP32 linear-response exponential is rescaled in FP64: the collision
     changes the carried energy only at round-off (lifetime residual ~ 0)."""

@@ -67,15 +67,19 @@ def test_cross_plane_film_statistics(gpu, precision):
     assert max(resid) < 1e-6
 
 
-def test_finfet_statistics(gpu, tmp_path):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_finfet_statistics(gpu, tmp_path, precision):
     """FinFET mesh with the fin-top heat source: region temperatures, thermal
-    energy, absorbed carriers per step and deposited source energy."""
+    energy, absorbed carriers per step and deposited source energy. The mixed
+    state flies in FP32 offsets from each cell's home voxel; wall events run in
+    FP64 from the cached hit points."""
     g = golden("fullrun_finfet")
     stl = workloads.finfet_stl(str(tmp_path / "finfet.stl"))
     m = abi.Material(gpu, "phmc_", synthetic.make_material(mesh=8), 0.1, False, False)
     runs = {}
     for k in range(len(g["seeds"])):
-        cfg = workloads.finfet_mesh(stl, particles=g["particles"], seed=7001 + k, grid=tuple(g["grid"]))
+        cfg = workloads.finfet_mesh(stl, particles=g["particles"], seed=(7001 if precision == "fp64" else 7101) + k,
+                                    grid=tuple(g["grid"]), precision=precision)
         s = abi.Solver(gpu, "phmc_", cfg, [m])
         dom = abi.Domain(gpu, cfg)
         centers = dom.cells()["centers"]
