@@ -228,6 +228,11 @@ int phmc_solver_cells(phmc_solver* s, double* temperature, double* energy_densit
 int phmc_solver_slot_count(phmc_solver* s, int64_t* n_slots);
 int phmc_solver_get_carriers(phmc_solver* s, double* x, double* y, double* z, double* occupation,
                              uint32_t* mode_word, int32_t* cell, uint8_t* alive);
+/* State of one carrier slot for diagnostics: out[0..2] position, [3]
+ * occupation, [4] mode word, [5] cell, [6] alive, and in mesh domains the
+ * wall cache [7] time to the wall in units of dt, [8..10] hit point, [11]
+ * cached facet, [12] mirror facet (-1 elsewhere). */
+int phmc_solver_carrier_state(phmc_solver* s, int64_t slot, double out[13]);
 /* Replace the carrier population (same SoA layout; mode_word = active | signs<<24 | material<<28). */
 int phmc_solver_set_carriers(phmc_solver* s, int64_t n, const double* x, const double* y, const double* z,
                              const double* occupation, const uint32_t* mode_word, const uint8_t* alive);

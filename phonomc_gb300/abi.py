@@ -530,6 +530,7 @@ DEVICE_PROTOS = {
     "solver_timed_run": (C.c_int, [C.c_void_p, C.c_int, c_double_p, c_double_p, c_int64_p, c_int64_p, c_int64_p]),
     "solver_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "solver_sort_interval": (C.c_int, [C.c_void_p, c_int32_p]),
+    "solver_carrier_state": (C.c_int, [C.c_void_p, C.c_int64, c_double_p]),
     "solver_set_schedule": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
     "batch_create": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),
     "batch_size": (C.c_int, [C.c_void_p, c_int32_p]),

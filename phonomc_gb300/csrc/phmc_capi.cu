@@ -656,6 +656,10 @@ int phmc_solver_get_carriers(phmc_solver* s, double* x, double* y, double* z, do
     return guard([&] { s->s->get_carriers(x, y, z, occ, mode, cell, alive); });
 }
 
+int phmc_solver_carrier_state(phmc_solver* s, int64_t slot, double out[13]) {
+    return guard([&] { s->s->carrier_state(slot, out); });
+}
+
 int phmc_solver_set_carriers(phmc_solver* s, int64_t n, const double* x, const double* y, const double* z,
                              const double* occ, const uint32_t* mode, const uint8_t* alive) {
     return guard([&] { s->s->set_carriers(n, x, y, z, occ, mode, alive); });

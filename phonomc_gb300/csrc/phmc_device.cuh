@@ -70,6 +70,7 @@ struct DevMaterial {
     const double* hw;       // [active]
     const double* inv_hw;   // [active]
     const double* vel;      // [active*3]
+    const double* flux_vel; // [active*3] v * (hbar omega) * energy weight: heat-flux term per unit deviation
     const float* vel32;     // [active*4] (vx, vy, vz, 0) for the mixed path
     const float* ivel32;    // [active*4] (1/vx, 1/vy, 1/vz, 0); 0 where v = 0
     const double* speed;    // [active] |v|
@@ -459,7 +460,8 @@ __device__ __forceinline__ void mode_velocity(const DevMaterial& M, uint32_t w, 
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         const double c = __ldg(M.vel + 3 * a + k);
-        v[k] = ((w >> (24 + k)) & 1u) ? -c : c;
+        // sign flip on the sign bit (integer pipe; the same bits as -c)
+        v[k] = __hiloint2double(__double2hiint(c) ^ static_cast<int>(((w >> (24 + k)) & 1u) << 31), __double2loint(c));
     }
 }
 

@@ -303,6 +303,12 @@ void DeviceSolver::upload_tables() {
             D.drive_cap = upload(dc);
         }
         D.energy_weight = M.energy_weight;
+        {
+            std::vector<double> fv(3 * static_cast<size_t>(M.n_active));
+            for (int a = 0; a < M.n_active; ++a)
+                for (int k = 0; k < 3; ++k) fv[3 * a + k] = M.vel[3 * a + k] * (M.hw[a] * M.energy_weight);
+            D.flux_vel = upload(fv);
+        }
         D.energy_density_bg = M.energy_density_bg;
         D.heat_capacity_density_bg = M.heat_capacity_density_bg;
         D.zero_point = M.zero_point;
@@ -954,6 +960,42 @@ void DeviceSolver::carrier_position(int slot, double p[3], int& facet) {
     PHMC_CUDA(cudaMemcpy(&p[1], state_.y + slot, sizeof(double), cudaMemcpyDeviceToHost));
     PHMC_CUDA(cudaMemcpy(&p[2], state_.z + slot, sizeof(double), cudaMemcpyDeviceToHost));
     if (mesh_hit_f_) PHMC_CUDA(cudaMemcpy(&facet, mesh_hit_f_ + slot, sizeof(int), cudaMemcpyDeviceToHost));
+}
+
+void DeviceSolver::carrier_state(long long slot, double out[13]) {
+    if (slot < 0 || slot >= state_.capacity) throw std::invalid_argument("carrier slot out of range");
+    PHMC_CUDA(cudaStreamSynchronize(stream_));
+    const int i = static_cast<int>(slot);
+    int facet = -1;
+    double p[3];
+    carrier_position(i, p, facet);
+    double occ = 0;
+    uint32_t w = 0;
+    int32_t c = 0;
+    uint8_t a = 0;
+    PHMC_CUDA(cudaMemcpy(&occ, state_.occ + i, sizeof occ, cudaMemcpyDeviceToHost));
+    PHMC_CUDA(cudaMemcpy(&w, state_.mode + i, sizeof w, cudaMemcpyDeviceToHost));
+    PHMC_CUDA(cudaMemcpy(&c, state_.cell + i, sizeof c, cudaMemcpyDeviceToHost));
+    PHMC_CUDA(cudaMemcpy(&a, state_.alive + i, sizeof a, cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 3; ++k) out[k] = p[k];
+    out[3] = occ;
+    out[4] = static_cast<double>(w);
+    out[5] = c;
+    out[6] = a;
+    for (int k = 7; k < 13; ++k) out[k] = k == 11 || k == 12 ? -1.0 : 0.0;
+    if (mesh_hit_t_) {
+        double t = 0, h[3] = {0, 0, 0};
+        int32_t mir = -1;
+        PHMC_CUDA(cudaMemcpy(&t, mesh_hit_t_ + i, sizeof t, cudaMemcpyDeviceToHost));
+        PHMC_CUDA(cudaMemcpy(&h[0], mesh_hit_x_ + i, sizeof(double), cudaMemcpyDeviceToHost));
+        PHMC_CUDA(cudaMemcpy(&h[1], mesh_hit_y_ + i, sizeof(double), cudaMemcpyDeviceToHost));
+        PHMC_CUDA(cudaMemcpy(&h[2], mesh_hit_z_ + i, sizeof(double), cudaMemcpyDeviceToHost));
+        PHMC_CUDA(cudaMemcpy(&mir, mesh_mirror_ + i, sizeof mir, cudaMemcpyDeviceToHost));
+        out[7] = t;
+        for (int k = 0; k < 3; ++k) out[8 + k] = h[k];
+        out[11] = facet;
+        out[12] = mir;
+    }
 }
 
 // Device errors surface at the next host synchronisation with the text of the

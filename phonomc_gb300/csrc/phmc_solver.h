@@ -154,6 +154,7 @@ public:
     void synchronize();
     void check_error();
     void carrier_position(int slot, double p[3], int& facet);
+    void carrier_state(long long slot, double out[13]); // phmc_solver_carrier_state
     void read_stats(phmc_stats& out);
     int cell_count() const { return ncells_; }
     void read_cells(double* T, double* E, double* q3);

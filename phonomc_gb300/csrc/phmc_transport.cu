@@ -130,6 +130,32 @@ __device__ __forceinline__ bool clear_of_walls(const DevDomain& D, const double 
 // One carrier's flight for `remaining` ps (src/solver/TransportOperator.cpp:405-466).
 // Position, mode word and occupation live in registers; returns false when the
 // carrier was absorbed.
+// A conservative form of clear_of_walls with few FP64 operations (GB300
+// retires two FP64 lanes per SM per clock): true only where clear_of_walls is
+// true as well. The gaps to the walls are the FP64 differences of the test,
+// rounded toward zero to FP32; the reach |v| dt (1 + 2e-6) is rounded up in
+// FP32, above the test's |v| dt (1 + 1e-9); signs and the 1e-18 velocity floor
+// are read from the bits. `dt_up`: dt rounded up to FP32.
+__device__ __forceinline__ bool clear_of_walls32(const DevDomain& D, const double p[3], const double v[3],
+                                                 float dt_up) {
+    bool clear = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const double ghi = dadd(D.hi[a], -p[a]), glo = dadd(p[a], -D.lo[a]);
+        const int hh = __double2hiint(ghi), hl = __double2hiint(glo);
+        // p in [lo, hi]: both gaps non-negative and finite (a NaN p fails)
+        clear = clear && hh >= 0 && hl >= 0 && (hh & 0x7ff00000) != 0x7ff00000 && (hl & 0x7ff00000) != 0x7ff00000;
+        const long long cb = __double_as_longlong(v[a]);
+        const long long mag = cb & 0x7fffffffffffffffLL;
+        if (mag > 0x3C32725DD1D243ACLL) { // |v| > 1e-18, or NaN: an axis the trace considers
+            const double g = cb >= 0 ? ghi : glo;
+            const float reach = __fmul_ru(__fmul_ru(__double2float_ru(__longlong_as_double(mag)), dt_up), 1.000002f);
+            clear = clear && __double2float_rz(g) > reach;
+        }
+    }
+    return clear;
+}
+
 __device__ bool advance_carrier(const DevTables& T, DevLedger* L, BlockLedger* bl, int slot, double p[3],
                                 uint32_t& w, double& occ, double remaining, uint32_t purpose, uint32_t step) {
     auto counted_cache = [&](int r) {
@@ -1033,7 +1059,8 @@ __device__ __forceinline__ void k_transport_body(const DevTables& T, CarrierStat
                     double v[3];
                     mode_velocity(T.mat[w >> 28], w, v);
                     const double dt = T.par.dt;
-                    if (clear_of_walls(T.dom, p, v, dt)) { // the first branch of advance_carrier
+                    // clear_of_walls32 implies the first branch of advance_carrier
+                    if (clear_of_walls32(T.dom, p, v, __double2float_ru(dt))) {
 #pragma unroll
                         for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], dt));
                         const int c = grid_index(T.dom, p[0], p[1], p[2]);
@@ -1846,12 +1873,23 @@ __global__ void __launch_bounds__(256) k_flux(const DevTables* __restrict__ Tp, 
             const int ai = static_cast<int>(w & 0x00FFFFFFu);
             double occ = apply_pending(T, C, c, w, S.occ[ic]) - drive_half(T, C, M, c, ai);
             if (C.src_next) occ -= C.src_next[static_cast<size_t>(c) * C.hist_modes + bin_of(M, ai)];
-            const double e = dmul(dmul(M.hw[ai], occ - M.nbg[ai]), M.energy_weight);
-            double v[3];
-            if (T.fac.mirror) mesh_velocity(T.fac, M, w, T.fac.mirror[ic], v);
-            else mode_velocity(M, w, v);
+            const double x = occ - M.nbg[ai];
+            if (T.fac.mirror) {
+                double v[3];
+                mesh_velocity(T.fac, M, w, T.fac.mirror[ic], v);
+                const double e = dmul(dmul(M.hw[ai], x), M.energy_weight);
 #pragma unroll
-            for (int a = 0; a < 3; ++a) f[a] = dmul(v[a], e);
+                for (int a = 0; a < 3; ++a) f[a] = dmul(v[a], e);
+            } else {
+                // v hbar omega w per mode: three FP64 products per carrier (sign flips on the bits)
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    const double c = __ldg(M.flux_vel + 3 * ai + a);
+                    const double cs = __hiloint2double(__double2hiint(c) ^ static_cast<int>(((w >> (24 + a)) & 1u) << 31),
+                                                       __double2loint(c));
+                    f[a] = dmul(cs, x);
+                }
+            }
         }
         const unsigned peers = __match_any_sync(0xffffffffu, c);
         reduce_peers3(peers, f);

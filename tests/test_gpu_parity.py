@@ -249,8 +249,8 @@ def test_rough_table_device_scan_matches_host(gpu, conservative):
         rc = gpu.phmc_dev_rough_spec_match(m.h, conservative, 300.0, nf, D(nrm), D(rough), dev, I32(match))
         assert rc == 0, gpu.phmc_last_error()
         out[dev] = match
-    assert (out[1] >= 0).sum() > nf * na.value // 4
     assert np.array_equal(out[0], out[1])
+    assert (out[1] >= 0).sum() > nf * na.value // 10
 
 
 def test_mixed_mesh_tracks_plain_trajectory(gpu, tmp_path):
