@@ -486,8 +486,8 @@ def main():
                     help="in-plane gradient: steps of the mixed-vs-FP64 kappa comparison (0: skip)")
     args = ap.parse_args()
     if args.particles is None:
-        args.particles = {"inplane_gradient": 5e7, "finfet_mesh": 2e7, "nonlinear_callaway_film": 1e7}.get(
-            args.workload, 1e6)
+        args.particles = {"inplane_gradient": 5e7, "finfet_mesh": 2e7, "nonlinear_callaway_film": 1e7,
+                          "bilayer_callaway": 1e8}.get(args.workload, 1e6)
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batched_films":

@@ -107,6 +107,7 @@ typedef struct phmc_mesh_domain {
     const double* boundary_values;   /* [n_regions] K, roughness nm, 0 for periodic */
     int32_t n_periodic_regions;      /* even: region 2k pairs with 2k+1 */
     const double* periodic_pair;     /* [n_periodic_regions][6] */
+    int32_t extruded_z;              /* geometry.extruded_z: constant-height prism, exact cut cells */
 } phmc_mesh_domain;
 
 /* SimulationConfig fields read by the carrier loop (include/SimulationConfig.h:42-146),
@@ -309,7 +310,16 @@ int phmc_domain_faces(const phmc_domain* d, int32_t* face_to_facet, double* tria
 int phmc_domain_contains(const phmc_domain* d, int64_t n, const double* p3, uint8_t* inside);
 int phmc_domain_grid_index(const phmc_domain* d, int64_t n, const double* p3, int32_t* cell);
 /* closest facet of each point (-1 for none), src/SurfaceMesh.cpp:996-1003 */
+/* Wall trace of rays from p (velocity v): hit point, time, facet (-1 and
+ * infinite time on a miss), by the host domain (SimulationDomain::
+ * trace_boundary_intersection, src/SimulationDomain.cpp:341-450). */
+int phmc_domain_trace(const phmc_domain* d, int64_t n, const double* p3, const double* v3, double* hit3, double* t,
+                      int32_t* facet);
 int phmc_domain_nearest_facet(const phmc_domain* d, int64_t n, const double* p3, int32_t* facet);
+/* The same traces by the device code of a mesh domain (face BVH, or the
+ * facet scan of an extruded prism). */
+int phmc_dev_domain_trace(const phmc_domain* d, int64_t n, const double* p3, const double* v3, double* hit3,
+                          double* t, int32_t* facet);
 /* The same membership / nearest-facet / cell queries evaluated by the device
  * code of the carrier loop on a device copy of a mesh domain (nearest may be NULL). */
 int phmc_dev_domain_query(const phmc_domain* d, int64_t n, const double* p3, uint8_t* inside, int32_t* nearest,

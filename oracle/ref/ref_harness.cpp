@@ -841,7 +841,7 @@ std::string escaped_file(const std::filesystem::path& path) {
     return esc;
 }
 
-std::string cmd_domain(const std::string& toml) {
+std::string cmd_domain(const std::string& toml, int n_traces = 0) {
     SimulationConfig a = load_simulation_config(toml);
     SimulationDomain d(a);
     const SurfaceMesh& mesh = d.mesh();
@@ -904,6 +904,30 @@ std::string cmd_domain(const std::string& toml) {
     j.arr("nearest_facet", nearest);
     j.arr("cell", cell);
     j.put_s("domain_summary", escaped_file(std::filesystem::path(a.output_folder) / "summary.txt"));
+    // traces of the domain from inside points along random directions
+    // (SimulationDomain::trace_boundary_intersection)
+    std::vector<std::array<double, 3>> tp, tv, th;
+    std::vector<double> tt;
+    std::vector<int> tf;
+    for (int i = 0; i < static_cast<int>(P.size()) && static_cast<int>(tp.size()) < n_traces; ++i) {
+        if (!inside[i]) continue;
+        const double c = 2 * U(rng) - 1, ph = 6.283185307179586 * U(rng), s = std::sqrt(1 - c * c);
+        const double speed = 20 + 60 * U(rng);
+        std::array<double, 3> v{speed * s * std::cos(ph), speed * s * std::sin(ph), speed * c};
+        const auto [hit, t, f] = d.trace_boundary_intersection(P[i], v);
+        tp.push_back(P[i]);
+        tv.push_back(v);
+        th.push_back(hit);
+        tt.push_back(t);
+        tf.push_back(f);
+    }
+    if (n_traces > 0) {
+        j.arr3("trace_p", tp);
+        j.arr3("trace_v", tv);
+        j.arr3("trace_hit", th);
+        j.arr("trace_t", tt);
+        j.arr("trace_facet", tf);
+    }
     return j.str();
 }
 
@@ -1134,7 +1158,7 @@ int main(int argc, char** argv) {
         else if (c == "rough") out = cmd_rough(argv[2], std::atoi(argv[3]) != 0);
         else if (c == "gradient") out = cmd_gradient(argv[2]);
         else if (c == "mesh") out = cmd_mesh(argv[2]);
-        else if (c == "domain") out = cmd_domain(argv[2]);
+        else if (c == "domain") out = cmd_domain(argv[2], argc > 3 ? std::atoi(argv[3]) : 0);
         else if (c == "source") out = cmd_source(argv[2], std::atoi(argv[3]), std::atoi(argv[4]) != 0);
         else if (c == "interface") out = cmd_interface(argv[2], argv[3], std::atoi(argv[4]) != 0);
         else if (c == "reservoir") out = cmd_reservoir(argv[2]);

@@ -101,13 +101,14 @@ class MeshDomainPOD(C.Structure):
         ("model", C.c_char_p), ("n_vertices", C.c_int64), ("vertices", c_double_p), ("n_faces", C.c_int64),
         ("faces", c_int32_p), ("merge_coplanar_facets", C.c_int32), ("n_regions", C.c_int32),
         ("boundary_position", c_double_p), ("boundary_conditions", C.c_char_p), ("boundary_values", c_double_p),
-        ("n_periodic_regions", C.c_int32), ("periodic_pair", c_double_p),
+        ("n_periodic_regions", C.c_int32), ("periodic_pair", c_double_p), ("extruded_z", C.c_int32),
     ]
 
 
 def mesh_domain_pod(m: dict, keep: list) -> MeshDomainPOD:
     """MeshDomainPOD from {"model": path | None, "vertices": [n,3] Angstrom, "faces": [m,3],
-    "merge_coplanar_facets": bool, "regions": [(box6, cond, value)], "periodic_pair": [box6, ...]}."""
+    "merge_coplanar_facets": bool, "extruded_z": bool, "regions": [(box6, cond, value)],
+    "periodic_pair": [box6, ...]}."""
     p = MeshDomainPOD()
     if m.get("model"):
         b = str(m["model"]).encode()
@@ -120,6 +121,7 @@ def mesh_domain_pod(m: dict, keep: list) -> MeshDomainPOD:
         p.n_vertices, p.vertices = v.shape[0], dptr(v)
         p.n_faces, p.faces = f.shape[0], f.ctypes.data_as(c_int32_p)
     p.merge_coplanar_facets = int(m.get("merge_coplanar_facets", True))
+    p.extruded_z = int(m.get("extruded_z", False))
     regions = m.get("regions", [])
     if regions:
         pos = np.ascontiguousarray([r[0] for r in regions], dtype=np.float64).reshape(-1)
@@ -307,6 +309,8 @@ DOMAIN_PROTOS = {
     "domain_contains": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_uint8_p]),
     "domain_grid_index": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_int32_p]),
     "domain_nearest_facet": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_int32_p]),
+    "domain_trace": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_double_p, c_double_p, c_double_p, c_int32_p]),
+    "dev_domain_trace": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_double_p, c_double_p, c_double_p, c_int32_p]),
     "dev_domain_query": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_uint8_p, c_int32_p, c_int32_p]),
     # material folders in the reference's layout (POSCAR + HDF5) and HDF5 datasets
     "material_load": (C.c_int, [C.c_char_p, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
@@ -654,6 +658,26 @@ class Domain:
         tri = np.zeros((self.n_faces, 3, 3))
         self._check(self.lib.phmc_domain_faces(self.h, f2f.ctypes.data_as(c_int32_p), dptr(tri)))
         return {"face_to_facet": f2f, "triangles": tri}
+
+    def trace(self, p, v):
+        """(hit points, times, facets) of rays by the host domain."""
+        p = np.ascontiguousarray(p, dtype=np.float64).reshape(-1, 3)
+        v = np.ascontiguousarray(v, dtype=np.float64).reshape(-1, 3)
+        n = p.shape[0]
+        hit, t, f = np.zeros((n, 3)), np.zeros(n), np.zeros(n, dtype=np.int32)
+        self._check(self.lib.phmc_domain_trace(self.h, n, dptr(p), dptr(v), dptr(hit), dptr(t),
+                                               f.ctypes.data_as(c_int32_p)))
+        return hit, t, f
+
+    def device_trace(self, p, v):
+        """The same traces by the device code (GPU)."""
+        p = np.ascontiguousarray(p, dtype=np.float64).reshape(-1, 3)
+        v = np.ascontiguousarray(v, dtype=np.float64).reshape(-1, 3)
+        n = p.shape[0]
+        hit, t, f = np.zeros((n, 3)), np.zeros(n), np.zeros(n, dtype=np.int32)
+        self._check(self.lib.phmc_dev_domain_trace(self.h, n, dptr(p), dptr(v), dptr(hit), dptr(t),
+                                                   f.ctypes.data_as(c_int32_p)))
+        return hit, t, f
 
     def contains(self, p) -> np.ndarray:
         p = np.ascontiguousarray(p, dtype=np.float64).reshape(-1, 3)

@@ -123,6 +123,20 @@ struct DevHold {
 };
 
 // Membership, nearest facet and cell of points on the device copy of a mesh domain.
+__global__ void k_domain_trace(const __grid_constant__ DevTables T, int n, const double* p3, const double* v3,
+                               double* hit3, double* t, int32_t* facet) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double p[3] = {p3[3 * i], p3[3 * i + 1], p3[3 * i + 2]};
+        const double v[3] = {v3[3 * i], v3[3 * i + 1], v3[3 * i + 2]};
+        double h[3], tt;
+        int f;
+        domain_trace_dev(T.fac, p, v, h, tt, f);
+        for (int k = 0; k < 3; ++k) hit3[3 * i + k] = h[k];
+        t[i] = tt;
+        facet[i] = f;
+    }
+}
+
 __global__ void k_domain_query(const __grid_constant__ DevTables T, int n, const double* p3, uint8_t* inside,
                                int32_t* nearest, int32_t* cell, int* err) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -602,6 +616,19 @@ int phmc_domain_grid_index(const phmc_domain* d, int64_t n, const double* p3, in
     });
 }
 
+int phmc_domain_trace(const phmc_domain* d, int64_t n, const double* p3, const double* v3, double* hit3, double* t,
+                      int32_t* facet) {
+    return guard([&] {
+        for (int64_t i = 0; i < n; ++i) {
+            Vec3 cp;
+            int f = -1;
+            d->d->trace({p3[3 * i], p3[3 * i + 1], p3[3 * i + 2]}, {v3[3 * i], v3[3 * i + 1], v3[3 * i + 2]}, cp, t[i], f);
+            facet[i] = f;
+            for (int k = 0; k < 3; ++k) hit3[3 * i + k] = cp[k];
+        }
+    });
+}
+
 int phmc_domain_nearest_facet(const phmc_domain* d, int64_t n, const double* p3, int32_t* facet) {
     return guard([&] {
         for (int64_t i = 0; i < n; ++i) facet[i] = d->d->nearest_facet({p3[3 * i], p3[3 * i + 1], p3[3 * i + 2]});
@@ -850,6 +877,29 @@ int phmc_dev_trace_mesh(int nv, const double* vertices, int nf, const int32_t* f
         dh.get(hit3);
         dt.get(t);
         dfc.get(facet);
+    });
+}
+
+int phmc_dev_domain_trace(const phmc_domain* d, int64_t n, const double* p3, const double* v3, double* hit3,
+                          double* t, int32_t* facet) {
+    return guard([&] {
+        const SimulationDomain& D = *d->d;
+        if (!D.is_mesh()) throw std::invalid_argument("phmc_dev_domain_trace: the analytic box has no mesh");
+        if (n < 0 || n > (int64_t{1} << 31) - 1) throw std::invalid_argument("phmc_dev_domain_trace: bad ray count");
+        DevHold hold;
+        DevTables T;
+        std::memset(&T, 0, sizeof T);
+        double scale = 1.0;
+        for (int a = 0; a < 3; ++a) scale = std::max(scale, std::abs(D.bounds_max()[a] - D.bounds_min()[a]));
+        fill_dev_facets(D, scale, T.fac, [&](const auto& v) { return hold.put(v); });
+        if (n == 0) return;
+        DBuf<double> dp(p3, 3 * n), dv(v3, 3 * n), dh(3 * n), dt(n);
+        DBuf<int32_t> df(n);
+        k_domain_trace<<<256, 128>>>(T, static_cast<int>(n), dp.p, dv.p, dh.p, dt.p, df.p);
+        cuda_check(cudaDeviceSynchronize(), "k_domain_trace");
+        dh.get(hit3);
+        dt.get(t);
+        df.get(facet);
     });
 }
 

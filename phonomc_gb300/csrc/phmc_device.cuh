@@ -288,6 +288,10 @@ struct DevFacets {
     const int* voxel_cell;         // voxel -> active cell
     const int* cell_voxel;         // active cell -> home voxel (origin of its FP32 offsets)
     DevMesh mesh;                  // oriented faces and their BVH
+    int prism;                     // extruded prism: facet-scan trace, ray-cast membership
+    const double* facet_centroid;  // [n][3] (prism trace)
+    const int* facet_face_begin;   // [n + 1] the facet's triangles in facet_tri (prism trace)
+    const double* facet_tri;       // [faces][9] vertices a, b, c of each facet's triangles
     int n_simplex;                 // star decomposition (0: ray cast only)
     const double* simplex;         // [n_simplex][18]: apex xyz, inverse 3x3 row-major, bounds min xyz, max xyz
     double ray_pad;                // padding of the BVH culling in the membership ray cast
@@ -1143,7 +1147,7 @@ __device__ inline bool mesh_simplex_inside(const DevFacets& F, const double p[3]
 // hit-list overflow.
 __device__ inline int mesh_contains(const DevFacets& F, const double p[3]) {
     const int r = mesh_ray_cast_inside(F, p);
-    if (r != 0) return r;
+    if (r != 0 || F.prism) return r; // a prism answers by the ray cast alone
     return mesh_simplex_inside(F, p) ? 1 : 0;
 }
 
@@ -1199,6 +1203,65 @@ __device__ __forceinline__ void mesh_velocity(const DevFacets& F, const DevMater
     }
 }
 
+// Trace of an extruded prism (src/SimulationDomain.cpp:344-396): every
+// facet's plane through its centroid, the nearest positive distance along
+// the unit direction, kept when the point lies in one of the facet's
+// triangles by edge functions in the projection dropping the normal's
+// largest axis, tolerance 1e-12 of the projected area. The reference takes
+// the edge functions in long double; here they are FP64, which decides
+// differently only for points within about 1e-16 of the domain size of an
+// edge.
+__device__ inline void prism_trace_dev(const DevFacets& F, const double p[3], const double vel[3], double hit[3],
+                                       double& t_out, int& facet) {
+    using namespace meshmath;
+    const double speed = norm(vel);
+    for (int a = 0; a < 3; ++a) hit[a] = p[a];
+    t_out = __longlong_as_double(0x7ff0000000000000LL);
+    facet = -1;
+    if (!(speed > 0)) return;
+    const double inv = 1 / speed;
+    const double d[3] = {__dmul_rn(vel[0], inv), __dmul_rn(vel[1], inv), __dmul_rn(vel[2], inv)};
+    double best = __longlong_as_double(0x7ff0000000000000LL);
+    for (int f = 0; f < F.n; ++f) {
+        const double n[3] = {F.normal[3 * f], F.normal[3 * f + 1], F.normal[3 * f + 2]};
+        const double den = dot(d, n);
+        if (den <= 1e-16) continue;
+        const double* c = F.facet_centroid + 3 * f;
+        const double cs[3] = {__dadd_rn(c[0], -p[0]), __dadd_rn(c[1], -p[1]), __dadd_rn(c[2], -p[2])};
+        const double dist = dot(cs, n) / den;
+        if (dist <= 1e-12 || dist >= best) continue;
+        double q[3];
+        axpy(p, d, dist, q);
+        int drop = 0;
+        for (int j = 1; j < 3; ++j)
+            if (fabs(n[j]) > fabs(n[drop])) drop = j;
+        const int u = (drop + 1) % 3, v = (drop + 2) % 3;
+        auto cross2 = [&](const double* a, const double* b, const double* cc) {
+            return __dadd_rn(__dmul_rn(__dadd_rn(b[u], -a[u]), __dadd_rn(cc[v], -a[v])),
+                             -__dmul_rn(__dadd_rn(b[v], -a[v]), __dadd_rn(cc[u], -a[u])));
+        };
+        for (int k = F.facet_face_begin[f]; k < F.facet_face_begin[f + 1]; ++k) {
+            const double* T = F.facet_tri + 9 * static_cast<size_t>(k);
+            const double area = cross2(T, T + 3, T + 6), tol = 1e-12 * fabs(area);
+            const double e0 = cross2(T, T + 3, q), e1 = cross2(T + 3, T + 6, q), e2 = cross2(T + 6, T, q);
+            if ((area > 0 && fmin(fmin(e0, e1), e2) >= -tol) || (area < 0 && fmax(fmax(e0, e1), e2) <= tol)) {
+                best = dist;
+                facet = f;
+                for (int a = 0; a < 3; ++a) hit[a] = q[a];
+                break;
+            }
+        }
+    }
+    t_out = best / speed;
+}
+
+// Wall trace of a mesh domain: the face BVH, or the facet scan of a prism.
+__device__ inline void domain_trace_dev(const DevFacets& F, const double p[3], const double v[3], double hit[3],
+                                        double& t_out, int& facet) {
+    if (F.prism) prism_trace_dev(F, p, v, hit, t_out, facet);
+    else mesh_trace_dev(F.mesh, p, v, hit, t_out, facet);
+}
+
 // Wall-hit cache with nudged retries on the mesh (src/solver/TransportOperator.cpp:186-250).
 // Returns 0 on success, 3 on success from a nudged position, 1 when no retry
 // found a wall, 2 on a membership overflow.
@@ -1211,7 +1274,7 @@ static __device__ __noinline__ int mesh_cache_hit(const DevFacets& F, const DevD
         f = -1;
         return 0;
     }
-    mesh_trace_dev(F.mesh, p, v, cp, t, f);
+    domain_trace_dev(F, p, v, cp, t, f);
     if (f >= 0 && isfinite(t)) return 0;
     const double eps = fmax(P.push_eps, 1e-10 * D.scale);
     double cand[4][3];
@@ -1237,7 +1300,7 @@ static __device__ __noinline__ int mesh_cache_hit(const DevFacets& F, const DevD
         const int in = mesh_contains(F, cand[c]);
         if (in < 0) return 2;
         if (!in) continue;
-        mesh_trace_dev(F.mesh, cand[c], v, cp, t, f);
+        domain_trace_dev(F, cand[c], v, cp, t, f);
         if (f >= 0 && isfinite(t)) {
             for (int a = 0; a < 3; ++a) p[a] = cand[c][a];
             return 3;

@@ -516,6 +516,10 @@ int SimulationDomain::voxel_index(const Vec3& p) const {
 
 // src/SimulationDomain.cpp:399-450 (analytic box branch)
 void SimulationDomain::trace(const Vec3& p, const Vec3& v, Vec3& cp, double& t, int& facet) const {
+    if (prism_) {
+        prism_trace(p, v, cp, t, facet);
+        return;
+    }
     if (mesh_) {
         mesh_->trace(p, v, cp, t, facet);
         return;
@@ -556,7 +560,8 @@ void SimulationDomain::trace(const Vec3& p, const Vec3& v, Vec3& cp, double& t, 
 }
 
 bool SimulationDomain::contains_point(const Vec3& p) const {
-    if (mesh_) return mesh_->contains_point(p);
+    // an extruded prism answers by the ray cast alone (include/SimulationDomain.h:43)
+    if (mesh_) return prism_ ? mesh_->contains_point_ray_cast(p) : mesh_->contains_point(p);
     for (int a = 0; a < 3; ++a)
         if (!(p[a] >= bmin_[a] && p[a] <= bmax_[a])) return false;
     return true;
@@ -1433,6 +1438,13 @@ CarrierArrays initial_carriers(const Problem& p, const std::vector<const PhononM
         for (const auto& sx : mesh->simplices()) simplex_cum.push_back(run += std::max(sx.volume, 0.0));
         if (!simplex_cum.empty() && !(run > 0.0)) simplex_cum.clear();
     }
+    std::vector<double> prism_cum; // running doubled areas of the prism's top triangles
+    if (D.is_prism()) {
+        double run = 0.0;
+        for (const auto& t : D.prism_top())
+            prism_cum.push_back(run += std::abs((t[1][0] - t[0][0]) * (t[2][1] - t[0][1]) -
+                                                (t[1][1] - t[0][1]) * (t[2][0] - t[0][0])));
+    }
     int rejected = -1;
     const double smallest_volume = *std::min_element(p.material_spatial_volume.begin(), p.material_spatial_volume.end());
 #pragma omp parallel for schedule(static)
@@ -1440,7 +1452,18 @@ CarrierArrays initial_carriers(const Problem& p, const std::vector<const PhononM
         const Uniform2 u0 = uniform2(seed, static_cast<uint32_t>(i), 0xFFFFFFFFu, kDrawInit, 0, 0);
         const Uniform2 u1 = uniform2(seed, static_cast<uint32_t>(i), 0xFFFFFFFFu, kDrawInit, 0, 1);
         Vec3 pos{lo[0] + (hi[0] - lo[0]) * u0.a, lo[1] + (hi[1] - lo[1]) * u0.b, lo[2] + (hi[2] - lo[2]) * u1.a};
-        if (mesh && !simplex_cum.empty()) {
+        if (D.is_prism()) {
+            // src/SimulationDomain.cpp:239-260: a top triangle by area, a
+            // uniform point in it, a uniform height
+            size_t k = static_cast<size_t>(std::upper_bound(prism_cum.begin(), prism_cum.end(),
+                                                            u0.a * prism_cum.back()) - prism_cum.begin());
+            if (k >= prism_cum.size()) k = prism_cum.size() - 1;
+            const auto& t = D.prism_top()[k];
+            const Uniform2 u2 = uniform2(seed, static_cast<uint32_t>(i), 0xFFFFFFFFu, kDrawInit, 0, 2);
+            const double a = std::sqrt(u0.b), b = u1.a;
+            for (int j = 0; j < 2; ++j) pos[j] = (1 - a) * t[0][j] + a * (1 - b) * t[1][j] + a * b * t[2][j];
+            pos[2] = lo[2] + u2.a * (hi[2] - lo[2]);
+        } else if (mesh && !simplex_cum.empty()) {
             size_t k = static_cast<size_t>(std::upper_bound(simplex_cum.begin(), simplex_cum.end(),
                                                             u0.a * simplex_cum.back()) - simplex_cum.begin());
             if (k >= simplex_cum.size()) k = simplex_cum.size() - 1;

@@ -77,6 +77,10 @@ struct SimulationConfig {
     std::vector<Vec3> mesh_vertices;
     std::vector<std::array<int, 3>> mesh_faces;
     bool merge_coplanar_facets = true;
+    // geometry.extruded_z: a constant-height prism (vertical side walls, flat
+    // top and bottom), traced by its facets and gridded with exact cut-cell
+    // volumes (src/SimulationDomain.cpp:206-260, 344-396, 650-740)
+    bool extruded_z = false;
     std::vector<std::array<double, 6>> boundary_position;
     std::vector<char> boundary_conditions;
     std::vector<double> boundary_values;   // K for 'T', roughness in nm for 'R', 0 for 'P'
@@ -355,6 +359,9 @@ public:
     explicit SimulationDomain(const SimulationConfig& cfg);
     ~SimulationDomain();
     bool is_mesh() const { return mesh_ != nullptr; }
+    // extruded prism (geometry.extruded_z): its top triangles and the z extent
+    bool is_prism() const { return prism_; }
+    const std::vector<std::array<Vec3, 3>>& prism_top() const { return prism_top_; }
     const SurfaceMesh* mesh() const { return mesh_.get(); }
     // voxel (ix*ny + iy)*nz + iz -> active cell (mesh domains; identity for boxes)
     const std::vector<int>& voxel_cells() const { return voxel_cell_; }
@@ -390,6 +397,10 @@ private:
     std::vector<int> reservoir_facets_;
     std::unique_ptr<SurfaceMesh> mesh_;
     std::vector<int> voxel_cell_;
+    bool prism_ = false;
+    std::vector<std::array<Vec3, 3>> prism_top_;
+    void build_prism_cells(int nx, int ny, int nz);
+    void prism_trace(const Vec3& p, const Vec3& v, Vec3& cp, double& t, int& facet) const;
 };
 
 // Layered materials along one axis (src/solver/LayeredMaterialLayout.cpp:24-115).

@@ -266,6 +266,21 @@ void fill_dev_facets(const SimulationDomain& dom, double scale, DevFacets& G, Up
     G.normal = up(normal);
     G.voxel_cell = up(dom.voxel_cells());
     G.cell_voxel = up(dom.cell_voxels());
+    G.prism = dom.is_prism() ? 1 : 0;
+    if (dom.is_prism()) {
+        std::vector<double> centroid(3 * static_cast<size_t>(nf)), tri;
+        std::vector<int> begin(nf + 1, 0);
+        for (int f = 0; f < nf; ++f) {
+            for (int a = 0; a < 3; ++a) centroid[3 * f + a] = F[f].centroid[a];
+            for (const auto& t : F[f].tris)
+                for (int k = 0; k < 3; ++k)
+                    for (int a = 0; a < 3; ++a) tri.push_back(t[k][a]);
+            begin[f + 1] = static_cast<int>(tri.size() / 9);
+        }
+        G.facet_centroid = up(centroid);
+        G.facet_face_begin = up(begin);
+        G.facet_tri = up(tri);
+    }
     fill_dev_mesh(Tr, G.mesh, up);
     std::vector<double> sx;
     for (const auto& S : M.simplices()) {

@@ -761,6 +761,32 @@ void SimulationDomain::build_mesh_domain(const SimulationConfig& cfg) {
         }
     }
 
+    // extruded prism: vertical sides, flat top and bottom; the top triangles
+    // (src/SimulationDomain.cpp:206-231)
+    prism_ = cfg.extruded_z;
+    if (prism_) {
+        const double tol = 1e-10 * std::max(1.0, bmax_[2] - bmin_[2]);
+        double area = 0.0;
+        for (const auto& f : M.faces()) {
+            const std::array<Vec3, 3> tri{M.vertices()[f[0]], M.vertices()[f[1]], M.vertices()[f[2]]};
+            bool top = true, bottom = true;
+            for (const auto& q : tri) {
+                top = top && std::abs(q[2] - bmax_[2]) < tol;
+                bottom = bottom && std::abs(q[2] - bmin_[2]) < tol;
+            }
+            const double twice = (tri[1][0] - tri[0][0]) * (tri[2][1] - tri[0][1]) -
+                                 (tri[1][1] - tri[0][1]) * (tri[2][0] - tri[0][0]);
+            if (top) {
+                prism_top_.push_back(tri);
+                area += std::abs(twice) * 0.5;
+            } else if (!bottom && std::abs(twice) > tol * tol) {
+                throw std::runtime_error("extruded_z requires vertical sides and planar top/bottom");
+            }
+        }
+        if (prism_top_.empty() || std::abs(area * (bmax_[2] - bmin_[2]) - volume_) > 1e-8 * volume_)
+            throw std::runtime_error("extruded_z top area and mesh volume disagree");
+    }
+
     const Vec3 ext = sub3(bmax_, bmin_);
     auto facets_in_region = [&](const std::array<double, 6>& box) {
         const double tolerance = 1e-12 * std::max({1.0, std::abs(ext[0]), std::abs(ext[1]), std::abs(ext[2])});
@@ -881,17 +907,21 @@ void SimulationDomain::build_mesh_domain(const SimulationConfig& cfg) {
         return Vec3{bmin_[0] + (ix + 0.5) * ext[0] / nx, bmin_[1] + (iy + 0.5) * ext[1] / ny,
                     bmin_[2] + (iz + 0.5) * ext[2] / nz};
     };
-    // membership in parallel (the lazily built decomposition first), cell
-    // numbers in voxel order
-    (void)M.simplices();
-    std::vector<unsigned char> inside(total, 0);
+    if (prism_) {
+        build_prism_cells(nx, ny, nz);
+    } else {
+        // membership in parallel (the lazily built decomposition first), cell
+        // numbers in voxel order
+        (void)M.simplices();
+        std::vector<unsigned char> inside(total, 0);
 #pragma omp parallel for schedule(dynamic, 256)
-    for (long long v = 0; v < static_cast<long long>(total); ++v)
-        inside[v] = M.contains_point(voxel_centre(static_cast<size_t>(v))) ? 1 : 0;
-    for (size_t v = 0; v < total; ++v) {
-        if (!inside[v]) continue;
-        voxel_cell_[v] = static_cast<int>(centers_.size());
-        centers_.push_back(voxel_centre(v));
+        for (long long v = 0; v < static_cast<long long>(total); ++v)
+            inside[v] = M.contains_point(voxel_centre(static_cast<size_t>(v))) ? 1 : 0;
+        for (size_t v = 0; v < total; ++v) {
+            if (!inside[v]) continue;
+            voxel_cell_[v] = static_cast<int>(centers_.size());
+            centers_.push_back(voxel_centre(v));
+        }
     }
     if (centers_.empty()) throw std::runtime_error("No valid grid centers found inside mesh.");
     std::deque<int> queue;
@@ -913,7 +943,125 @@ void SimulationDomain::build_mesh_domain(const SimulationConfig& cfg) {
             queue.push_back(next);
         }
     }
-    volumes_.assign(centers_.size(), volume_ / static_cast<double>(centers_.size()));
+    if (!prism_) {
+        volumes_.assign(centers_.size(), volume_ / static_cast<double>(centers_.size()));
+    } else {
+        long double sum = 0;
+        for (double v : volumes_) sum += v;
+        if (std::abs(sum - volume_) > 1e-8 * volume_) throw std::runtime_error("Prism cut-cell volumes do not close");
+    }
+}
+
+// Cells of an extruded prism (src/SimulationDomain.cpp:650-711): per voxel
+// column the top triangles clipped to the column (Sutherland-Hodgman over its
+// four sides), areas and centroids of the clipped polygons summed in long
+// double; a voxel is a cell when its cut volume exceeds 1e-12 of an average
+// voxel's, at the area centroid in x and y and the voxel centre in z. The
+// column's polygons do not depend on z, so they are clipped once per column.
+void SimulationDomain::build_prism_cells(int nx, int ny, int nz) {
+    const Vec3 ext = sub3(bmax_, bmin_);
+    const size_t total = static_cast<size_t>(nx) * ny * nz;
+    volumes_.clear();
+    for (int ix = 0; ix < nx; ++ix)
+        for (int iy = 0; iy < ny; ++iy) {
+            const double x0 = bmin_[0] + ix * ext[0] / nx, x1 = x0 + ext[0] / nx;
+            const double y0 = bmin_[1] + iy * ext[1] / ny, y1 = y0 + ext[1] / ny;
+            long double area_sum = 0, cx = 0, cy = 0;
+            for (const auto& tri : prism_top_) {
+                std::vector<Vec3> poly(tri.begin(), tri.end());
+                for (int edge = 0; edge < 4; ++edge) {
+                    const int axis = edge / 2;
+                    const bool lower = edge % 2 == 0;
+                    const double bound = axis == 0 ? (lower ? x0 : x1) : (lower ? y0 : y1);
+                    std::vector<Vec3> clipped;
+                    for (size_t i = 0; i < poly.size(); ++i) {
+                        const Vec3& a = poly[i];
+                        const Vec3& b = poly[(i + 1) % poly.size()];
+                        const bool ina = lower ? a[axis] >= bound : a[axis] <= bound;
+                        const bool inb = lower ? b[axis] >= bound : b[axis] <= bound;
+                        if (ina) clipped.push_back(a);
+                        if (ina != inb) {
+                            const double f = (bound - a[axis]) / (b[axis] - a[axis]);
+                            clipped.push_back(add3(a, mul3(sub3(b, a), f)));
+                        }
+                    }
+                    poly = std::move(clipped);
+                }
+                for (size_t i = 1; i + 1 < poly.size(); ++i) {
+                    const Vec3& a = poly[0];
+                    const Vec3& b = poly[i];
+                    const Vec3& c = poly[i + 1];
+                    const long double area =
+                        std::abs((b[0] - a[0]) * (c[1] - a[1]) - (b[1] - a[1]) * (c[0] - a[0])) * .5;
+                    area_sum += area;
+                    cx += area * (a[0] + b[0] + c[0]) / 3;
+                    cy += area * (a[1] + b[1] + c[1]) / 3;
+                }
+            }
+            const double cut_volume = static_cast<double>(area_sum) * ext[2] / nz;
+            for (int iz = 0; iz < nz; ++iz) {
+                Vec3 q{bmin_[0] + (static_cast<double>(ix) + 0.5) * ext[0] / static_cast<double>(nx),
+                       bmin_[1] + (static_cast<double>(iy) + 0.5) * ext[1] / static_cast<double>(ny),
+                       bmin_[2] + (static_cast<double>(iz) + 0.5) * ext[2] / static_cast<double>(nz)};
+                if (area_sum > 0) {
+                    q[0] = static_cast<double>(cx / area_sum);
+                    q[1] = static_cast<double>(cy / area_sum);
+                }
+                if (cut_volume > 1e-12 * volume_ / static_cast<double>(total)) {
+                    voxel_cell_[(static_cast<size_t>(ix) * ny + iy) * nz + iz] = static_cast<int>(centers_.size());
+                    centers_.push_back(q);
+                    volumes_.push_back(cut_volume);
+                }
+            }
+        }
+}
+
+// Trace of an extruded prism (src/SimulationDomain.cpp:344-396): every facet's
+// plane through its centroid, the nearest positive distance along the unit
+// direction, the hit kept when it lies in one of the facet's triangles by
+// long-double edge functions in the projection that drops the normal's
+// largest axis (tolerance 1e-12 of the triangle's projected area).
+void SimulationDomain::prism_trace(const Vec3& position, const Vec3& velocity, Vec3& cp, double& t,
+                                   int& facet) const {
+    const double speed = norm3(velocity);
+    cp = position;
+    t = std::numeric_limits<double>::infinity();
+    facet = -1;
+    if (!(speed > 0)) return;
+    const Vec3 direction = mul3(velocity, 1 / speed);
+    const SurfaceMesh& M = *mesh_;
+    double best = std::numeric_limits<double>::infinity();
+    for (int f = 0; f < M.facet_count(); ++f) {
+        const Vec3& n = M.facet_normals()[f];
+        const double denominator = dot3(direction, n);
+        if (denominator <= 1e-16) continue;
+        const double distance = dot3(sub3(M.facet_centroids()[f], position), n) / denominator;
+        if (distance <= 1e-12 || distance >= best) continue;
+        const Vec3 candidate = add3(position, mul3(direction, distance));
+        int drop = 0;
+        for (int j = 1; j < 3; ++j)
+            if (std::abs(n[j]) > std::abs(n[drop])) drop = j;
+        const int u = (drop + 1) % 3, v = (drop + 2) % 3;
+        auto cross2 = [&](const Vec3& a, const Vec3& b, const Vec3& c) {
+            return (static_cast<long double>(b[u]) - a[u]) * (static_cast<long double>(c[v]) - a[v]) -
+                   (static_cast<long double>(b[v]) - a[v]) * (static_cast<long double>(c[u]) - a[u]);
+        };
+        for (int face : M.facet_faces()[f]) {
+            const auto& id = M.faces()[face];
+            const Vec3& a = M.vertices()[id[0]];
+            const Vec3& b = M.vertices()[id[1]];
+            const Vec3& c = M.vertices()[id[2]];
+            const long double area = cross2(a, b, c), tol = 1e-12L * std::abs(area);
+            const long double e0 = cross2(a, b, candidate), e1 = cross2(b, c, candidate), e2 = cross2(c, a, candidate);
+            if ((area > 0 && std::min({e0, e1, e2}) >= -tol) || (area < 0 && std::max({e0, e1, e2}) <= tol)) {
+                best = distance;
+                facet = f;
+                cp = candidate;
+                break;
+            }
+        }
+    }
+    t = best / speed;
 }
 
 } // namespace phmc

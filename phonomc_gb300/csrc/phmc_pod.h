@@ -91,6 +91,7 @@ inline void mesh_domain_from_pod(const phmc_mesh_domain& m, SimulationConfig& s)
         for (int64_t i = 0; i < m.n_faces; ++i) s.mesh_faces[i] = {m.faces[3 * i], m.faces[3 * i + 1], m.faces[3 * i + 2]};
     }
     s.merge_coplanar_facets = m.merge_coplanar_facets != 0;
+    s.extruded_z = m.extruded_z != 0;
     if (m.n_regions < 0 || m.n_periodic_regions < 0) throw std::invalid_argument("negative region count");
     if (m.n_regions > 0 && (!m.boundary_position || !m.boundary_conditions || !m.boundary_values))
         throw std::invalid_argument("boundary regions require positions, conditions and values");

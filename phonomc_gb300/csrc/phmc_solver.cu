@@ -97,7 +97,7 @@ DeviceSolver::DeviceSolver(const SimulationConfig& cfg, const std::vector<const 
     // A mesh without a volume decomposition samples positions by ray-cast
     // rejection: that part runs on the device, with the host's draws.
     std::vector<double> preset;
-    if (domain_->is_mesh() && domain_->mesh()->simplices().empty() && n0 > 0) {
+    if (domain_->is_mesh() && !domain_->is_prism() && domain_->mesh()->simplices().empty() && n0 > 0) {
         double* d_xyz = nullptr;
         const size_t bytes = 3 * static_cast<size_t>(n0) * sizeof(double);
         PHMC_CUDA(cudaMalloc(&d_xyz, bytes));

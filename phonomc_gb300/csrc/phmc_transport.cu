@@ -156,6 +156,25 @@ __device__ __forceinline__ bool clear_of_walls32(const DevDomain& D, const doubl
     return clear;
 }
 
+// No material-plane crossing within dt (conservative FP32 form of
+// next_crossing_dev > dt): true only where the FP64 crossing time is infinite
+// or beyond dt. A plane behind the carrier (gap and velocity of opposite
+// sign) is never crossed; NaN velocities fail.
+__device__ __forceinline__ bool clear_of_planes32(const DevDomain& D, int n_materials, const double p[3],
+                                                  const double v[3], int current, float dt_up) {
+    const long long cb = __double_as_longlong(axis_of(v, D.layout_axis));
+    const long long mag = cb & 0x7fffffffffffffffLL;
+    if (mag <= 0x3C32725DD1D243ACLL) return true; // |v| <= 1e-18 along the layout axis
+    double plane;
+    if (cb >= 0 && current + 1 < n_materials) plane = D.planes[current];
+    else if (cb < 0 && current > 0) plane = D.planes[current - 1];
+    else return mag <= 0x7ff0000000000000LL; // no plane ahead (a NaN velocity fails)
+    const double gap = dadd(plane, -axis_of(p, D.layout_axis));
+    if ((__double2hiint(gap) ^ static_cast<int>(cb >> 32)) < 0) return true; // the plane lies behind
+    const float reach = __fmul_ru(__fmul_ru(__double2float_ru(__longlong_as_double(mag)), dt_up), 1.000002f);
+    return __double2float_rz(fabs(gap)) > reach;
+}
+
 __device__ bool advance_carrier(const DevTables& T, DevLedger* L, BlockLedger* bl, int slot, double p[3],
                                 uint32_t& w, double& occ, double remaining, uint32_t purpose, uint32_t step) {
     auto counted_cache = [&](int r) {
@@ -549,14 +568,18 @@ __device__ __forceinline__ Frame cell_frame(const DevDomain& D, int cell) {
     return F;
 }
 
+// FP32 velocity and its reciprocal (0 where a component is 0) from the
+// per-mode tables, sign flips on the sign bits.
 __device__ __forceinline__ void mode_velocity32(const DevMaterial& M, uint32_t w, float v[3], float iv[3]) {
     const int a = static_cast<int>(w & 0x00FFFFFFu);
     const float4 vv = __ldg(reinterpret_cast<const float4*>(M.vel32) + a);
-    const float c[3] = {vv.x, vv.y, vv.z};
+    const float4 ii = __ldg(reinterpret_cast<const float4*>(M.ivel32) + a);
+    const float c[3] = {vv.x, vv.y, vv.z}, r[3] = {ii.x, ii.y, ii.z};
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        v[k] = ((w >> (24 + k)) & 1u) ? -c[k] : c[k];
-        iv[k] = v[k] != 0.0f ? __frcp_rn(v[k]) : 0.0f;
+        const unsigned flip = ((w >> (24 + k)) & 1u) << 31;
+        v[k] = __uint_as_float(__float_as_uint(c[k]) ^ flip);
+        iv[k] = __uint_as_float(__float_as_uint(r[k]) ^ flip);
     }
 }
 
@@ -629,15 +652,9 @@ __global__ void k_mesh_cache_init(const __grid_constant__ DevTables T, CarrierSt
         const uint32_t w = S.mode[i];
         double v[3];
         mesh_velocity(T.fac, T.mat[w >> 28], w, T.fac.mirror[i], v);
-        double p[3];
-        if (kMixed) {
-            const float o[3] = {S.ox[i], S.oy[i], S.oz[i]};
-            frame_point(T.dom, cell_frame_of(T, S.cell[i]), o, p);
-        } else {
-            p[0] = S.x[i];
-            p[1] = S.y[i];
-            p[2] = S.z[i];
-        }
+        // the uploaded FP64 position, not its FP32 offsets: a carrier within
+        // the offsets' rounding of a wall could otherwise trace from outside
+        double p[3] = {S.x[i], S.y[i], S.z[i]};
         MeshCache c;
         mesh_refresh(T, L, nullptr, i, p, v, c);
         if (kMixed) {
@@ -884,14 +901,16 @@ __device__ __forceinline__ int settle_layer(const DevTables& T, const CellArrays
 // new cell and enters the bins.
 // Stores the carrier after its flight; returns its bin record (-1: absorbed
 // or invalid) for the caller to tally.
+// The mode word is stored only when the flight changed it (most carriers keep
+// their mode for the step, and unchanged words leave most of its sectors clean).
 __device__ __forceinline__ long long finish_mixed(const DevTables& T, const CarrierState& S, const CellArrays& C,
                                                   DevLedger* L, int i, const Frame& F, float p[3], uint32_t w,
-                                                  double occ, bool alive) {
+                                                  double occ, bool alive, uint32_t w0) {
     const int c = settle_layer(T, C, F, p, static_cast<int>(w >> 28));
     __stcs(S.ox + i, p[0]);
     __stcs(S.oy + i, p[1]);
     __stcs(S.oz + i, p[2]);
-    __stcs(S.mode + i, w);
+    if (w != w0) __stcs(S.mode + i, w);
     __stcs(S.occ + i, occ);
     if (!alive) {
         S.alive[i] = 0;
@@ -924,6 +943,7 @@ __device__ __forceinline__ void mixed_carrier(const DevTables& T, const CarrierS
     long long h = -1;
     double hocc = 0.0;
     if (in && alive) {
+        const uint32_t w0 = w;
         double occ = apply_pending(T, C, c0, w, occ0);
         const Frame F = cell_frame(T.dom, c0);
         float remaining = T.par.dt32;
@@ -939,7 +959,7 @@ __device__ __forceinline__ void mixed_carrier(const DevTables& T, const CarrierS
             defer = true;
             entry = make_int4(i, __float_as_int(remaining), event, plane);
         } else {
-            h = finish_mixed(T, S, C, L, i, F, p, w, occ, end != kFlightAbsorbed);
+            h = finish_mixed(T, S, C, L, i, F, p, w, occ, end != kFlightAbsorbed, w0);
             hocc = occ;
         }
     }
@@ -1008,7 +1028,7 @@ __device__ __forceinline__ void queue_event(const CarrierState& S, DevLedger* L,
 }
 
 // qbuf: kDeferBuffer entries per warp of the block (mixed path).
-template <bool kMixed, bool kRta, bool kAgg, bool kQueue = true>
+template <bool kMixed, bool kRta, bool kAgg>
 __device__ __forceinline__ void k_transport_body(const DevTables& T, CarrierState S, CellArrays C, DevLedger* L, int vbx,
                                                  int vgx, int4 (*qbuf)[kDeferBuffer]) {
     const uint32_t step = L->step_index; // timesteps completed: the draw counter of this step
@@ -1035,10 +1055,10 @@ __device__ __forceinline__ void k_transport_body(const DevTables& T, CarrierStat
         }
         flush_deferred(S, L, qbuf, queued);
     } else {
-        // kQueue (one material): carriers that cannot reach a wall within the
-        // step drift here; the others are queued, with their updated
-        // occupation, for k_box_events, so no warp of this pass waits on a few
-        // lanes' FP64 wall events. Layered materials run every flight here.
+        // Carriers that cannot reach a wall (or, layered, the material plane
+        // ahead) within the step drift here; the others are queued, with their
+        // updated occupation, for k_box_events, so no warp of this pass waits
+        // on a few lanes' FP64 wall events.
         // block-uniform trip count so that every lane reaches the warp tally and ballot
         for (int base = vbx * blockDim.x; base < n; base += vgx * blockDim.x) {
             const int i = base + threadIdx.x;
@@ -1055,43 +1075,32 @@ __device__ __forceinline__ void k_transport_body(const DevTables& T, CarrierStat
             double p[3] = {__ldcs(S.x + ic), __ldcs(S.y + ic), __ldcs(S.z + ic)};
             if (in && alive0) {
                 occ = apply_pending(T, C, c0, w, occ0);
-                if constexpr (kQueue) {
-                    double v[3];
-                    mode_velocity(T.mat[w >> 28], w, v);
-                    const double dt = T.par.dt;
-                    // clear_of_walls32 implies the first branch of advance_carrier
-                    if (clear_of_walls32(T.dom, p, v, __double2float_ru(dt))) {
+                double v[3];
+                mode_velocity(T.mat[w >> 28], w, v);
+                const double dt = T.par.dt;
+                const float dt_up = __double2float_ru(dt);
+                // clear of every wall (and, layered, of the material plane ahead)
+                // implies advance_carrier's direct flight: the same position bits
+                bool clear = clear_of_walls32(T.dom, p, v, dt_up);
+                if (T.par.n_materials > 1)
+                    clear = clear && clear_of_planes32(T.dom, T.par.n_materials, p, v, static_cast<int>(w >> 28), dt_up);
+                if (clear) {
 #pragma unroll
-                        for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], dt));
-                        const int c = grid_index(T.dom, p[0], p[1], p[2]);
-                        __stcs(S.x + i, p[0]);
-                        __stcs(S.y + i, p[1]);
-                        __stcs(S.z + i, p[2]);
-                        __stcs(S.occ + i, occ);
-                        __stcs(S.cell + i, c);
-                        h = bin_slot(T, C, L, i, c, w, occ);
-                    } else {
-                        __stcs(S.occ + i, occ);
-                        defer = true;
-                    }
-                } else {
-                    const bool alive = advance_carrier(T, L, &bl, i, p, w, occ, T.par.dt, kDrawTransport, step);
+                    for (int a = 0; a < 3; ++a) p[a] = dadd(p[a], dmul(v[a], dt));
                     const int c = grid_index(T.dom, p[0], p[1], p[2]);
                     __stcs(S.x + i, p[0]);
                     __stcs(S.y + i, p[1]);
                     __stcs(S.z + i, p[2]);
-                    __stcs(S.mode + i, w);
                     __stcs(S.occ + i, occ);
-                    if (!alive) {
-                        S.alive[i] = 0;
-                    } else {
-                        __stcs(S.cell + i, c);
-                        h = bin_slot(T, C, L, i, c, w, occ);
-                    }
+                    __stcs(S.cell + i, c);
+                    h = bin_slot(T, C, L, i, c, w, occ);
+                } else {
+                    __stcs(S.occ + i, occ);
+                    defer = true;
                 }
             }
             bin_warp<kAgg, kRta>(C, h, occ);
-            if constexpr (kQueue) queue_event(S, L, defer, i);
+            queue_event(S, L, defer, i);
         }
     }
     __syncthreads();
@@ -1267,12 +1276,12 @@ __global__ void __launch_bounds__(kPipeTile) k_transport_pipe(const __grid_const
 
 // Block size chosen at launch (128, 256 or 512 threads); the wall-event queue
 // of the mixed path is dynamic shared memory, kDeferBuffer entries per warp.
-template <bool kMixed, bool kRta, bool kAgg, bool kQueue>
+template <bool kMixed, bool kRta, bool kAgg>
 __global__ void __launch_bounds__(kTransportMaxThreads) k_transport(const __grid_constant__ DevTables T, CarrierState S,
                                                                     CellArrays C, DevLedger* L) {
     extern __shared__ int4 qdyn[];
-    k_transport_body<kMixed, kRta, kAgg, kQueue>(T, S, C, L, blockIdx.x, gridDim.x,
-                                                 reinterpret_cast<int4 (*)[kDeferBuffer]>(qdyn));
+    k_transport_body<kMixed, kRta, kAgg>(T, S, C, L, blockIdx.x, gridDim.x,
+                                         reinterpret_cast<int4 (*)[kDeferBuffer]>(qdyn));
 }
 
 // Mesh transport, pass 1 of 2: apply the pending update and drift every
@@ -1434,7 +1443,7 @@ __device__ __forceinline__ void k_deferred_body(const DevTables& T, CarrierState
             int unused = -1;
             end = advance_mixed<false>(T, L, &bl, i, F, p, w, occ, remaining, event, unused, kDrawTransport, step);
         }
-        const long long h = finish_mixed(T, S, C, L, i, F, p, w, occ, end != kFlightAbsorbed);
+        const long long h = finish_mixed(T, S, C, L, i, F, p, w, occ, end != kFlightAbsorbed, ~w);
         if (h >= 0) bin_add(C, h, 1u, occ, fmax(1.0, occ), kRta);
     }
     __syncthreads();
@@ -1497,11 +1506,11 @@ __global__ void k_ingest(const __grid_constant__ DevTables T, CarrierState S, De
             S.ox[i] = static_cast<float>(x - (D.lo[0] + F.i[0] * D.cell_size[0]));
             S.oy[i] = static_cast<float>(y - (D.lo[1] + F.i[1] * D.cell_size[1]));
             S.oz[i] = static_cast<float>(z - (D.lo[2] + F.i[2] * D.cell_size[2]));
-        } else {
-            S.x[i] = x;
-            S.y[i] = y;
-            S.z[i] = z;
         }
+        // FP64 positions (the mixed state's staging): mesh wall caches are traced from them
+        S.x[i] = x;
+        S.y[i] = y;
+        S.z[i] = z;
         S.occ[i] = H.occ[i];
         S.mode[i] = H.mode[i];
         const uint8_t a = H.alive ? H.alive[i] : uint8_t(1);
@@ -1959,13 +1968,8 @@ void launch_transport_pass(const LaunchCtx& x, dim3 g) {
     }
     const int threads = x.transport_block;
     const size_t sh = kMixed ? static_cast<size_t>(threads / 32) * kDeferBuffer * sizeof(int4) : 0;
-    if (!kMixed && x.Th->par.n_materials > 1) { // layered: every flight in the pass
-        if (x.tally_agg) k_transport<kMixed, kRta, true, false><<<g, threads, sh, x.stream>>>(*x.Th, x.S, x.C, x.L);
-        else k_transport<kMixed, kRta, false, false><<<g, threads, sh, x.stream>>>(*x.Th, x.S, x.C, x.L);
-        return;
-    }
-    if (x.tally_agg) k_transport<kMixed, kRta, true, true><<<g, threads, sh, x.stream>>>(*x.Th, x.S, x.C, x.L);
-    else k_transport<kMixed, kRta, false, true><<<g, threads, sh, x.stream>>>(*x.Th, x.S, x.C, x.L);
+    if (x.tally_agg) k_transport<kMixed, kRta, true><<<g, threads, sh, x.stream>>>(*x.Th, x.S, x.C, x.L);
+    else k_transport<kMixed, kRta, false><<<g, threads, sh, x.stream>>>(*x.Th, x.S, x.C, x.L);
 }
 
 int launch_transport(const LaunchCtx& x, bool mixed, bool rta) {
@@ -2002,8 +2006,7 @@ int launch_transport(const LaunchCtx& x, bool mixed, bool rta) {
     }
     if (rta) launch_transport_pass<false, true>(x, dim3(x.transport_grid));
     else launch_transport_pass<false, false>(x, dim3(x.transport_grid));
-    if (x.Th->par.n_materials > 1) return 1;
-    // wall events queued by the pass
+    // wall events (and, layered, plane crossings) queued by the pass
     if (rta) k_box_events<true><<<g, 256, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
     else k_box_events<false><<<g, 256, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
     return 2;

@@ -234,6 +234,28 @@ def finfet_mesh(voxel_nm: float = 5.0, jitter_nm: float = 0.5, seed: int = 0,
     return v, np.array(faces, dtype=np.int64)
 
 
+def prism_mesh(outline_nm=((0.0, 0.0), (100.0, 0.0), (100.0, 30.0), (37.0, 30.0), (37.0, 80.0), (0.0, 80.0)),
+               height_nm: float = 50.0):
+    """An L-shaped prism: the counter-clockwise outline (nm) extruded from z = 0
+    to `height_nm`, vertical side walls (one quad per outline edge, the x = 0
+    edge split at the inner corner's y so every vertex of the top is a vertex
+    of the walls) and a flat top and bottom triangulated as the two rectangles
+    of the L. Returns (vertices [nm], faces) with outward winding."""
+    o = [tuple(map(float, q)) for q in outline_nm]
+    (x0, y0), (x1, _), (_, y1), (xn, _), (_, y2), _ = o
+    ring = [(x0, y0), (x1, y0), (x1, y1), (xn, y1), (xn, y2), (x0, y2), (x0, y1)]  # counter-clockwise
+    n = len(ring)
+    verts = [(x, y, 0.0) for x, y in ring] + [(x, y, float(height_nm)) for x, y in ring]
+    # top (counter-clockwise seen from +z) as index triangles of the ring
+    top = [(0, 1, 2), (0, 2, 3), (0, 3, 6), (6, 3, 4), (6, 4, 5)]
+    faces = [(a + n, b + n, c + n) for a, b, c in top] + [(a, c, b) for a, b, c in top]
+    for i in range(n):
+        j = (i + 1) % n
+        faces.append((i, j, j + n))
+        faces.append((i, j + n, i + n))
+    return np.array(verts, dtype=np.float64), np.array(faces, dtype=np.int64)
+
+
 def write_stl(path: str, vertices, faces, name: str = "synthetic") -> None:
     """Binary STL (little-endian: 80-byte header, count, 50-byte records)."""
     import struct

@@ -212,6 +212,32 @@ def finfet_mesh(stl_path: str, particles: float = 2e7, seed: int = 12345, precis
     return c
 
 
+# Extruded L-shaped prism (synthetic.prism_mesh): 310 K top, 300 K bottom,
+# rough (1 nm) side walls; a constant-height prism gridded by exact cut cells.
+PRISM_REGIONS = [
+    ((-0.01, -0.01, -0.01, 1.01, 1.01, 1.01), "R", 1.0),
+    ((-0.01, -0.01, -0.001, 1.01, 1.01, 0.001), "T", 300.0),
+    ((-0.01, -0.01, 0.999, 1.01, 1.01, 1.001), "T", 310.0),
+]
+
+
+def prism_stl(path: str) -> str:
+    """Writes the L-shaped prism (14 vertices, 24 triangles) as binary STL."""
+    from . import synthetic
+    synthetic.write_stl(path, *synthetic.prism_mesh())
+    return path
+
+
+def prism_film(stl_path: str, particles: float = 2e4, seed: int = 5, precision: str = "fp64",
+               grid=(8, 6, 5)) -> dict:
+    """Cross-plane heat flow through the extruded L prism (geometry.extruded_z)."""
+    return {"name": "prism_film", "particle_count": float(particles), "time_step": 0.5, "iterations": 2000,
+            "random_seed": seed, "compute_kappa": False, "background_temperature": 305.0,
+            "lifetime_temperature": 305.0, "initial_temperature": 305.0, "grid": tuple(grid),
+            "precision": precision,
+            "mesh": {"model": stl_path, "regions": PRISM_REGIONS, "extruded_z": True}}
+
+
 def finfet_regions(centers):
     """Cell masks of the FinFET: the fin above the 50 nm slab, the upper and the
     lower half of the slab (cell centres in Angstrom)."""

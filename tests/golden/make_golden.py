@@ -52,6 +52,7 @@ CASES = {
     "source_gaussian": ["source", "{m}", "2", "0"],
     "mesh_finfet": ["mesh", "{f}"],
     "domain_finfet": ["domain", "{t}"],
+    "domain_prism": ["domain", "{p}", "600"],
     "interface_dmm": ["interface", "{m}", "{s}", "0"],
     "interface_dmm_linearized": ["interface", "{m}", "{s}", "1"],
     "interface_amm": ["amm", "{m}", "{s}", "1", "1.0", "0"],
@@ -89,6 +90,39 @@ periodic_pair = [
   [-0.01,0,0,0.01,1,1], [0.99,0,0,1.01,1,1],
   [0,-0.01,0,1,0.01,1], [0,0.99,0,1,1.01,1]
 ]
+
+[io]
+material_folder = "unused"
+output_folder = "{out}"
+"""
+
+# Extruded L-shaped prism (phonomc_gb300.synthetic.prism_mesh, lengths in nm):
+# constant-height prism with exact cut-cell volumes, heat flowing from the
+# 310 K top to the 300 K bottom, rough side walls.
+PRISM_TOML = """[geometry]
+model = "{stl}"
+extruded_z = true
+
+[simulation]
+particle_count = {particles}
+time_step = 0.5
+iterations = {steps}
+random_seed = {seed}
+compute_kappa = false
+initial_temperature = 305
+background_temperature = 305
+lifetime_temperature = 305
+grid_xyz = [8, 6, 5]
+convergence_write_interval = 1
+
+[boundary]
+boundary_position = [
+  [-0.01, -0.01, -0.01, 1.01, 1.01, 1.01],
+  [-0.01, -0.01, -0.001, 1.01, 1.01, 0.001],
+  [-0.01, -0.01, 0.999, 1.01, 1.01, 1.001]
+]
+boundary_conditions = ["R", "T", "T"]
+boundary_values = [1.0, 300.0, 310.0]
 
 [io]
 material_folder = "unused"
@@ -472,6 +506,11 @@ def main() -> None:
     synthetic.write_stl(fpath, *synthetic.finfet_mesh())
     spath = os.path.join(tmp, "m8s.pmat")
     synthetic.write_pmat(spath, synthetic.make_material(mesh=8, freq_scale=0.7, vel_scale=0.75))
+    ppath = os.path.join(tmp, "prism.stl")
+    synthetic.write_stl(ppath, *synthetic.prism_mesh())
+    prism_toml = os.path.join(tmp, "prism_domain.toml")
+    with open(prism_toml, "w") as f:
+        f.write(PRISM_TOML.format(stl=ppath, particles=2000, steps=1, seed=5, out=os.path.join(tmp, "prism_out")))
     tpath = os.path.join(tmp, "finfet_domain.toml")
     with open(tpath, "w") as f:
         f.write(FINFET_TOML.format(stl=fpath, particles=2000, steps=1, seed=5, nx=64, ny=32, nz=32,
@@ -527,7 +566,7 @@ def main() -> None:
     for name, argv in CASES.items():
         if args.only and name not in args.only:
             continue
-        cmd = [HARNESS] + [a.format(m=mpath, c=cpath, s=spath, f=fpath, t=tpath) for a in argv]
+        cmd = [HARNESS] + [a.format(m=mpath, c=cpath, s=spath, f=fpath, t=tpath, p=prism_toml) for a in argv]
         out = subprocess.run(cmd, check=True, capture_output=True, text=True).stdout
         data = json.loads(out)
         data["_harness_args"] = argv
