@@ -387,24 +387,26 @@ def run_ours(args):
     # the carriers (positions, occupation, mode), runs one timestep and reads
     # the cell temperatures back
     s = main_arm["solver"]
-    c = s.carriers()
-    live = c["alive"] == 1
-    host = {k: np.ascontiguousarray(c[k][live]) for k in ("x", "y", "z", "occ")}
-    host["mode"] = np.ascontiguousarray(c["mode"][live])
-    n = host["x"].size
-    for a in host.values():
-        lib.phmc_host_register(a.ctypes.data, a.nbytes)
     Tout = np.zeros(s.cells()[0].size)
-    e2e_steps = max(1, min(args.steps, 5))
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        s.check(lib.phmc_solver_run_from_host(s.h, n, abi.dptr(host["x"]), abi.dptr(host["y"]), abi.dptr(host["z"]),
-                                              abi.dptr(host["occ"]), host["mode"].ctypes.data_as(abi.c_uint32_p), 1,
-                                              abi.dptr(Tout)))
-    e2e_s = time.perf_counter() - t0
-    for a in host.values():
-        lib.phmc_host_unregister(a.ctypes.data)
-    e2e_value = n * e2e_steps / e2e_s * (world if world > 1 else 1)
+    n, e2e_value = 0, None
+    if not args.no_e2e:
+        c = s.carriers()
+        live = c["alive"] == 1
+        host = {k: np.ascontiguousarray(c[k][live]) for k in ("x", "y", "z", "occ")}
+        host["mode"] = np.ascontiguousarray(c["mode"][live])
+        n = host["x"].size
+        for a in host.values():
+            lib.phmc_host_register(a.ctypes.data, a.nbytes)
+        e2e_steps = max(1, min(args.steps, 5))
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            s.check(lib.phmc_solver_run_from_host(s.h, n, abi.dptr(host["x"]), abi.dptr(host["y"]),
+                                                  abi.dptr(host["z"]), abi.dptr(host["occ"]),
+                                                  host["mode"].ctypes.data_as(abi.c_uint32_p), 1, abi.dptr(Tout)))
+        e2e_s = time.perf_counter() - t0
+        for a in host.values():
+            lib.phmc_host_unregister(a.ctypes.data)
+        e2e_value = n * e2e_steps / e2e_s * (world if world > 1 else 1)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -482,6 +484,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-films sub-measurement")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--kappa-steps", type=int, default=2000,
                     help="in-plane gradient: steps of the mixed-vs-FP64 kappa comparison (0: skip)")
     args = ap.parse_args()

@@ -1151,23 +1151,43 @@ __device__ inline int mesh_contains(const DevFacets& F, const double p[3]) {
     return mesh_simplex_inside(F, p) ? 1 : 0;
 }
 
-// Distance from p to the surface: the smallest distance to a face, faces
-// culled by their bounds once a closer one is known.
-__device__ inline double mesh_surface_distance(const DevFacets& F, const double p[3]) {
+// True when p lies within `tol` of a face: the face BVH culls every node
+// whose bounds, widened by tol, miss p, so only the faces near p are tested.
+__device__ inline bool mesh_near_surface(const DevFacets& F, const double p[3], double tol) {
     const DevMesh& M = F.mesh;
-    double bd = __longlong_as_double(0x7ff0000000000000LL);
-    for (int i = 0; i < M.nfaces; ++i) {
+    auto near_face = [&](int i) {
         const double* r = M.face + kFaceRecord * i;
-        bool far = false;
-        for (int a = 0; a < 3; ++a) far = far || p[a] < r[4 + a] - bd || p[a] > r[7 + a] + bd;
-        if (far) continue;
+        for (int a = 0; a < 3; ++a)
+            if (p[a] < r[4 + a] - tol || p[a] > r[7 + a] + tol) return false;
         double a[3], b[3], c[3], cp[3], d[3];
         mesh_face(M, i, a, b, c);
         meshmath::closest(p, a, b, c, cp);
         meshmath::sub(p, cp, d);
-        bd = fmin(bd, meshmath::norm(d));
+        return meshmath::norm(d) <= tol;
+    };
+    if (M.root < 0) {
+        for (int i = 0; i < M.nfaces; ++i)
+            if (near_face(i)) return true;
+        return false;
     }
-    return bd;
+    int stack[64];
+    int top = 0;
+    stack[top++] = M.root;
+    while (top > 0) {
+        const DevBvhNode& nd = M.nodes[stack[--top]];
+        bool miss = false;
+        for (int a = 0; a < 3; ++a) miss = miss || p[a] < nd.bmin[a] - tol || p[a] > nd.bmax[a] + tol;
+        if (miss) continue;
+        if (nd.left < 0 && nd.right < 0) {
+            for (int pos = nd.begin; pos < nd.end; ++pos)
+                if (near_face(pos)) return true;
+            continue;
+        }
+        if (top + 2 > 64) return true; // too deep to decide: treat as near (no false escape)
+        if (nd.left >= 0) stack[top++] = nd.left;
+        if (nd.right >= 0) stack[top++] = nd.right;
+    }
+    return false;
 }
 
 // Facet of the closest face, first minimum (src/SurfaceMesh.cpp:996-1023).

@@ -25,6 +25,7 @@ struct LaunchCtx {
     DevLedger* L;
     cudaStream_t stream;
     int grid_blocks;
+    int event_grid = 1; // CTAs per SM x SMs of one resident wave of the event kernels (x1 per SM)
     bool mesh = false;   // surface-mesh domain (plain FP64 carrier state)
     const DevNcl* ncl = nullptr; // host copy, nonlinear Callaway only
     unsigned char* lin_work = nullptr; // linear Callaway: per-CTA mode slices in global memory (null: shared)

@@ -619,6 +619,8 @@ LaunchCtx DeviceSolver::ctx() const {
     // batch do not launch idle CTAs
     const long long want = (static_cast<long long>(state_.capacity) + 1023) / 1024;
     x.grid_blocks = static_cast<int>(std::max<long long>(8, std::min<long long>(sm_count_ * 8, want)));
+    // event kernels: the CTAs resident in one wave (their queues are short)
+    x.event_grid = static_cast<int>(std::max<long long>(1, std::min<long long>(sm_count_, want)));
     // the box carrier pass: tuned threads per CTA and resident CTAs per SM, at
     // least about four carriers per thread for small populations
     const int tk = mixed_ ? 1 : 0;

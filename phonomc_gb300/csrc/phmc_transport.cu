@@ -1348,7 +1348,7 @@ __global__ void __launch_bounds__(kTransportThreads) k_transport_mesh(const __gr
 // Mesh transport, pass 2 of 2: the full flight of every queued carrier from
 // the start of the step (occupation already updated), then its cell and bin.
 template <bool kRta, bool kMixed>
-__global__ void __launch_bounds__(kTransportThreads, 1) k_mesh_events(const __grid_constant__ DevTables T, CarrierState S,
+__global__ void __launch_bounds__(kTransportThreads, 2) k_mesh_events(const __grid_constant__ DevTables T, CarrierState S,
                                                                    CellArrays C, DevLedger* L) {
     const uint32_t step = L->step_index;
     __shared__ BlockLedger bl;
@@ -1825,7 +1825,7 @@ __global__ void k_containment(const DevTables* __restrict__ Tp, CarrierState S, 
             outside = in == 0;
             // the mixed state may sit outside a wall by its FP32 rounding:
             // escaped only when farther from the surface than that
-            if (kMixed && outside) outside = !(mesh_surface_distance(Tp->fac, p) <= t);
+            if (kMixed && outside) outside = !mesh_near_surface(Tp->fac, p, t);
         }
         if (outside) raise_error(L, kErrEscaped, i);
     }
@@ -1979,36 +1979,40 @@ int launch_transport(const LaunchCtx& x, bool mixed, bool rta) {
     if (mixed && !x.mesh) {
         // the carrier pass at the configured block size; the deferred wall events at 256
         const dim3 gp(x.transport_grid);
+        // deferred wall events: two resident CTAs per SM (93 registers), one wave
+        const dim3 ge(2 * x.event_grid);
         if (rta) {
             launch_transport_pass<true, true>(x, gp);
-            k_deferred<true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+            k_deferred<true><<<ge, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
         } else {
             launch_transport_pass<true, false>(x, gp);
-            k_deferred<false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+            k_deferred<false><<<ge, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
         }
         return 2;
     }
     if (x.mesh) {
         if (mixed && rta) {
             k_transport_mesh<true, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
-            k_mesh_events<true, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+            k_mesh_events<true, true><<<dim3(2 * x.event_grid), b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
         } else if (mixed) {
             k_transport_mesh<false, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
-            k_mesh_events<false, true><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+            k_mesh_events<false, true><<<dim3(2 * x.event_grid), b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
         } else if (rta) {
             k_transport_mesh<true, false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
-            k_mesh_events<true, false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+            k_mesh_events<true, false><<<dim3(2 * x.event_grid), b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
         } else {
             k_transport_mesh<false, false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
-            k_mesh_events<false, false><<<g, b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+            k_mesh_events<false, false><<<dim3(2 * x.event_grid), b, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
         }
         return 2;
     }
     if (rta) launch_transport_pass<false, true>(x, dim3(x.transport_grid));
     else launch_transport_pass<false, false>(x, dim3(x.transport_grid));
     // wall events (and, layered, plane crossings) queued by the pass
-    if (rta) k_box_events<true><<<g, 256, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
-    else k_box_events<false><<<g, 256, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+    // two resident CTAs per SM (80 registers), one wave
+    const dim3 ge(2 * x.event_grid);
+    if (rta) k_box_events<true><<<ge, 256, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
+    else k_box_events<false><<<ge, 256, 0, x.stream>>>(*x.Th, x.S, x.C, x.L);
     return 2;
 }
 
