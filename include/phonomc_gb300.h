@@ -165,6 +165,11 @@ typedef struct phmc_config {
     double interface_parallel_bin_inv_a;  /* amm search bins in k parallel, 1/Angstrom (0: 0.05) */
     int32_t n_mass_densities;
     const double* mass_densities_kg_m3;   /* one per material (amm, mmm) */
+    /* RTA cell update: 1 one warp per cell for the bin sums, cell state,
+     * pseudo-temperature and pending update together, < 0 separate kernels,
+     * 0 automatic (fused on grids of 1024 cells or more with at most 512
+     * mode classes per cell). */
+    int32_t rta_cell_update;
 } phmc_config;
 
 /* Getters of include/MonteCarloSolver.h:59-101 plus the last step's ledger. */
@@ -308,6 +313,11 @@ int phmc_domain_cells(const phmc_domain* d, double* centers3, double* volumes, i
  * triangle soup, and the facet of each face; any may be NULL */
 int phmc_domain_faces(const phmc_domain* d, int32_t* face_to_facet, double* triangles9);
 int phmc_domain_contains(const phmc_domain* d, int64_t n, const double* p3, uint8_t* inside);
+/* voxel [nx*ny*nz] -> 1 when every point of its box lies inside the mesh (no
+ * face's bounding box reaches it, its centre inside): the containment check
+ * of the carrier loop skips the ray cast of carriers in such voxels. Mesh
+ * domains other than extruded prisms; 0 elsewhere. */
+int phmc_domain_voxel_interior(const phmc_domain* d, uint8_t* interior);
 int phmc_domain_grid_index(const phmc_domain* d, int64_t n, const double* p3, int32_t* cell);
 /* closest facet of each point (-1 for none), src/SurfaceMesh.cpp:996-1003 */
 /* Wall trace of rays from p (velocity v): hit point, time, facet (-1 and

@@ -160,7 +160,7 @@ class ConfigPOD(C.Structure):
         ("transport_pipeline", C.c_int32),
         ("interface_model", C.c_int32), ("interface_amm_fraction", C.c_double),
         ("interface_parallel_bin_inv_a", C.c_double), ("n_mass_densities", C.c_int32),
-        ("mass_densities_kg_m3", c_double_p),
+        ("mass_densities_kg_m3", c_double_p), ("rta_cell_update", C.c_int32),
     ]
 
 
@@ -246,6 +246,7 @@ def config_pod(cfg: dict):
     c.transport_blocks_per_sm = int(cfg.get("transport_blocks_per_sm", 0))
     c.tally_aggregation = int(cfg.get("tally_aggregation", 0))
     c.transport_pipeline = int(cfg.get("transport_pipeline", 0))
+    c.rta_cell_update = int(cfg.get("rta_cell_update", 0))
     c.interface_model = {"dmm": 0, "amm": 1, "mmm": 2}[cfg.get("interface_model", "dmm")]
     c.interface_amm_fraction = float(cfg.get("interface_amm_fraction", 0.0))
     c.interface_parallel_bin_inv_a = float(cfg.get("interface_parallel_bin_inv_a", 0.0))
@@ -307,6 +308,7 @@ DOMAIN_PROTOS = {
     "domain_cells": (C.c_int, [C.c_void_p, c_double_p, c_double_p, c_int32_p]),
     "domain_faces": (C.c_int, [C.c_void_p, c_int32_p, c_double_p]),
     "domain_contains": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_uint8_p]),
+    "domain_voxel_interior": (C.c_int, [C.c_void_p, c_uint8_p]),
     "domain_grid_index": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_int32_p]),
     "domain_nearest_facet": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_int32_p]),
     "domain_trace": (C.c_int, [C.c_void_p, C.c_int64, c_double_p, c_double_p, c_double_p, c_double_p, c_int32_p]),
@@ -684,6 +686,12 @@ class Domain:
         out = np.zeros(p.shape[0], dtype=np.uint8)
         self._check(self.lib.phmc_domain_contains(self.h, p.shape[0], dptr(p), out.ctypes.data_as(c_uint8_p)))
         return out
+
+    def voxel_interior(self) -> np.ndarray:
+        """Voxels whose whole box lies inside the mesh, shape (nx, ny, nz)."""
+        out = np.zeros(int(np.prod(self.shape)), dtype=np.uint8)
+        self._check(self.lib.phmc_domain_voxel_interior(self.h, out.ctypes.data_as(c_uint8_p)))
+        return out.reshape(tuple(self.shape))
 
     def grid_index(self, p) -> np.ndarray:
         p = np.ascontiguousarray(p, dtype=np.float64).reshape(-1, 3)

@@ -114,6 +114,34 @@ def population_threshold(lib, abi, best, precision="mixed", sizes=(2e5, 1e6, 4e6
     return rows
 
 
+def mesh_sort_sweep(lib, abi, particles=2e7, sorts=(25, 50, 100, 200), steps=100, log=print):
+    """Sort interval of surface-mesh domains: the FinFET with its heat source,
+    a fresh population per point (a long FinFET run can lose a carrier through
+    its top surface, which ends the run), timed over `steps` steps from a sort step."""
+    import tempfile
+    from . import synthetic, workloads
+    stl = workloads.finfet_stl(os.path.join(tempfile.mkdtemp(prefix="phmc_tune_"), "finfet.stl"))
+    rows = []
+    for prec in ("mixed", "fp64"):
+        for k in sorts:
+            m = abi.Material(lib, "phmc_", synthetic.make_material(mesh=16), 0.1, False, False)
+            cfg = workloads.finfet_mesh(stl, particles=particles, precision=prec)
+            cfg["carrier_sort_interval"] = k
+            s = abi.Solver(lib, "phmc_", cfg, [m])
+            s.run(3)
+            s.run((-s.stats()["current_timestep"]) % k + 1)
+            s.check(lib.phmc_solver_synchronize(s.h))
+            t0 = time.perf_counter()
+            s.run(steps)
+            s.check(lib.phmc_solver_synchronize(s.h))
+            rows.append({"precision": prec, "carrier_sort_interval": k,
+                         "ms_per_step": 1e3 * (time.perf_counter() - t0) / steps})
+            log(json.dumps(rows[-1]))
+            s.close()
+            m.close()
+    return rows
+
+
 HEADER = """// Launch and scheduling defaults of the device carrier loop, chosen by
 // phonomc_gb300/autotune.py from timed sweeps on a GB300 (the sweep record it
 // writes sits beside it, phonomc_gb300/tuning_record.json). A configuration
@@ -132,6 +160,8 @@ constexpr int kTransportBlocksPerSm[2] = {{{p0}, {p1}}};
 // domains (0: never), and the smallest population that is sorted at all.
 constexpr int kSortInterval[2] = {{{k0}, {k1}}};
 constexpr double kSortMinCarriers = {nmin:.6g};
+// The same for surface-mesh domains (FinFET sweep of the record's "mesh_sorts").
+constexpr int kSortIntervalMesh[2] = {{{m0}, {m1}}};
 // Bin tallies of the carrier pass: 1 sums runs of equal (cell, bin) across
 // the lanes of a warp before one FP64 atomic per run, 0 one atomic per carrier.
 constexpr int kTallyAggregation[2] = {{{a0}, {a1}}};
@@ -161,9 +191,14 @@ def write_outputs(out, record):
         k = val(prec, "carrier_sort_interval", 50)
         return max(0, k)
 
+    def mesh_sort_of(prec):
+        rows = [r for r in record.get("mesh_sorts", []) if r["precision"] == prec]
+        return min(rows, key=lambda r: r["ms_per_step"])["carrier_sort_interval"] if rows else 25
+
     text = HEADER.format(b0=val("fp64", "transport_block", 256), b1=val("mixed", "transport_block", 256),
                          p0=val("fp64", "transport_blocks_per_sm", 8), p1=val("mixed", "transport_blocks_per_sm", 8),
                          k0=sort_of("fp64"), k1=sort_of("mixed"), nmin=float(nmin),
+                         m0=mesh_sort_of("fp64"), m1=mesh_sort_of("mixed"),
                          a0=max(0, val("fp64", "tally_aggregation", 1)), a1=max(0, val("mixed", "tally_aggregation", 1)),
                          pipe=max(0, val("mixed", "transport_pipeline", 1)))
     with open(os.path.join(out, "phmc_tuning.h"), "w") as f:
@@ -176,6 +211,7 @@ def main():
     ap.add_argument("--particles", type=float, default=5e7)
     ap.add_argument("--precisions", nargs="*", default=["mixed", "fp64"])
     ap.add_argument("--quick", action="store_true", help="a reduced grid (smoke of the tuner itself)")
+    ap.add_argument("--mesh", action="store_true", help="also sweep the sort interval of mesh domains (FinFET)")
     args = ap.parse_args()
     from . import abi
     from . import lib as load
@@ -195,6 +231,8 @@ def main():
         mixed = [r for r in record["sweeps"] if r["precision"] == "mixed"]
         if mixed:
             record["threshold"] = population_threshold(lib, abi, mixed[0]["best"], log=log)
+        if args.mesh:
+            record["mesh_sorts"] = mesh_sort_sweep(lib, abi, log=log)
     try:
         import subprocess
         record["gpu"] = subprocess.run(["nvidia-smi", "--query-gpu=name,clocks.max.sm", "--format=csv,noheader"],

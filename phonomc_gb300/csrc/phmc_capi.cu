@@ -610,6 +610,16 @@ int phmc_domain_contains(const phmc_domain* d, int64_t n, const double* p3, uint
     });
 }
 
+int phmc_domain_voxel_interior(const phmc_domain* d, uint8_t* interior) {
+    return guard([&] {
+        const SimulationDomain& D = *d->d;
+        const auto& s = D.grid_shape();
+        const size_t n = static_cast<size_t>(s[0]) * s[1] * s[2];
+        const auto& f = D.voxel_interior();
+        for (size_t v = 0; v < n; ++v) interior[v] = f.empty() ? 0 : f[v];
+    });
+}
+
 int phmc_domain_grid_index(const phmc_domain* d, int64_t n, const double* p3, int32_t* cell) {
     return guard([&] {
         for (int64_t i = 0; i < n; ++i) cell[i] = d->d->fast_grid_index({p3[3 * i], p3[3 * i + 1], p3[3 * i + 2]});

@@ -328,6 +328,415 @@ __global__ void __launch_bounds__(256) k_rta_solve_warp(const DevTables* __restr
     rta_solve_warp_cell(*Tp, C, c, threadIdx.x & 31);
 }
 
+// ----------------------------------------------- RTA cell update (fused)
+// One warp per cell for grids of many cells whose class count fits the warp's
+// shared-memory list: the bin sums and the cell state (k_cell_stats,
+// k_cell_state), the pseudo-temperature (k_rta_solve) and the pending update
+// with the step energies (k_cell_tables) in one kernel. After the first scan
+// of the bins only the cell's occupied classes are visited: an empty class
+// adds nothing to any sum of the solve, and its pending entry is read by no
+// carrier (a carrier reads the entry of the bin it was counted in, and every
+// reader clears or adds to exactly those entries).
+//
+// The iteration of src/solver/RtaCollisionOperator.cpp:79-184 is kept: the
+// bracket [0, max(1000, 2 max(1, T))] with its doubling, the edge cases, the
+// FP64 Newton/bisection steps and the stopping test |f| <= 1e-13 max(1, sum hw
+// a max(1, n)). What changes is how f is evaluated and where the iteration
+// starts. (1) It starts at an FP32 Newton estimate of the root inside the
+// bracket instead of the cell temperature. (2) f and f' at a point T0 come
+// from the Bose occupations (one exp per class); at points within 1e-5 T0 of
+// T0 they come from the third-order Taylor expansion of each occupation in
+// 1/T about T0, which agrees with the direct formula to about 1e-16 relative
+// there (the expansion error is (x dT/T)^4 / 24 for x = hw/kT), so the usual
+// final Newton step and the test of its result need no further exps.
+// (3) f(high) is evaluated in FP64 only when an FP32 bound does not show it
+// negative (only its sign enters the iteration). The occupations at the
+// accepted T* are the ones the pending update uses.
+constexpr int kRtaCellWarps = 4;
+constexpr int kRtaCellMaxCap = 512;
+
+struct RtaCellList {
+    double* N;   // summed occupation of the class
+    double* n0;  // carriers of the class
+    double* hw;  // hbar omega of the class
+    double* a;   // relaxation probability
+    double* p0;  // n_eq at the expansion point
+    float4* f32; // (hw, hw a, N, carriers) in FP32; hw a = 0 marks a class without relaxation
+    int* cls;    // class (bin) index
+};
+
+__device__ __forceinline__ RtaCellList rta_cell_list(int cap) {
+    extern __shared__ double rta_smem[];
+    const int w = threadIdx.x >> 5;
+    const int stride = kRtaCellWarps * cap;
+    RtaCellList l;
+    l.N = rta_smem + w * cap;
+    l.n0 = rta_smem + stride + w * cap;
+    l.hw = rta_smem + 2 * stride + w * cap;
+    l.a = rta_smem + 3 * stride + w * cap;
+    l.p0 = rta_smem + 4 * stride + w * cap;
+    l.f32 = reinterpret_cast<float4*>(rta_smem + 5 * stride) + w * cap;
+    l.cls = reinterpret_cast<int*>(reinterpret_cast<float4*>(rta_smem + 5 * stride) + stride) + w * cap;
+    return l;
+}
+
+static size_t rta_cell_smem(int cap) {
+    return static_cast<size_t>(kRtaCellWarps) * cap * (5 * sizeof(double) + sizeof(float4) + sizeof(int));
+}
+
+// Interval of the linewidth table at temperature T, found once per cell:
+// gamma_at(M, a, T) == gamma_in(M, s, a) for every mode a.
+struct GammaSpan {
+    int l, h;
+    double t;
+    bool lerp;
+};
+
+__device__ __forceinline__ GammaSpan gamma_span(const DevMaterial& M, double T) {
+    GammaSpan s{0, 0, 0.0, false};
+    const int nT = M.n_temps;
+    if (!(T > M.temps[0])) return s; // also a non-finite T: the first row
+    if (T >= M.temps[nT - 1]) {
+        s.l = nT - 1;
+        return s;
+    }
+    int lo = 0, hi = nT;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (M.temps[mid] <= T) lo = mid + 1;
+        else hi = mid;
+    }
+    const int h = lo, l = h - 1;
+    const double x0 = M.temps[l], x1 = M.temps[h];
+    s.l = l;
+    if (fabs(x1 - x0) <= 1e-18) return s;
+    s.h = h;
+    s.t = (T - x0) / (x1 - x0);
+    s.lerp = true;
+    return s;
+}
+
+__device__ __forceinline__ double gamma_in(const DevMaterial& M, const GammaSpan& s, int a) {
+    const double y0 = M.gamma[static_cast<size_t>(s.l) * M.n_active + a];
+    if (!s.lerp) return y0;
+    const double y1 = M.gamma[static_cast<size_t>(s.h) * M.n_active + a];
+    return y0 * (1.0 - s.t) + y1 * s.t;
+}
+
+__device__ __forceinline__ float warp_sum_uniform_f(float x) {
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return __shfl_sync(0xffffffffu, x, 0);
+}
+
+// n_eq(T) of bose_dev from hbar omega (hw = kHbar w, so x is the same product).
+__device__ __forceinline__ double bose_hw(double T, double hw) {
+    if (T <= 0.0 || hw <= 0.0) return 0.0;
+    const double x = hw / (kKb * T);
+    if (x > 700.0) return 0.0;
+    return 1.0 / fmax(exp(x) - 1.0, 1e-12);
+}
+
+// f(T) = sum hw a (N - cnt n_eq(T)) in FP32, its slope and the sum of the
+// magnitudes of its terms (all lanes get the warp totals).
+__device__ __forceinline__ void rta_eval32(const RtaCellList& Ls, int count, int lane, float t, float& v, float& d,
+                                           float& mag) {
+    float v0 = 0.f, v1 = 0.f, m0 = 0.f;
+    const float ikt = 1.0f / (static_cast<float>(kKb) * t);
+    for (int j = lane; j < count; j += 32) {
+        const float4 e = Ls.f32[j]; // (hw, hw a, N, cnt)
+        if (e.y == 0.f) continue;
+        const float x = e.x * ikt;
+        const float neq = x > 80.f ? 0.f : 1.0f / expm1f(x);
+        v0 += e.y * (e.z - e.w * neq);
+        m0 += e.y * (fabsf(e.z) + e.w * neq);
+        v1 -= e.w * e.y * (e.x * neq * (neq + 1.0f) * ikt / t);
+    }
+    v = warp_sum_uniform_f(v0);
+    d = warp_sum_uniform_f(v1);
+    mag = warp_sum_uniform_f(m0);
+}
+
+// f(T) and f'(T) from the Bose occupations; they become the expansion point.
+__device__ __forceinline__ double rta_eval_exp(const RtaCellList& Ls, int count, int lane, double T, double& slope) {
+    double v0 = 0.0, v1 = 0.0;
+    const double ikt2 = T > 0.0 ? 1.0 / (kKb * T * T) : 0.0;
+    for (int j = lane; j < count; j += 32) {
+        const double hw = Ls.hw[j];
+        const double p = bose_hw(T, hw);
+        Ls.p0[j] = p;
+        const double a = Ls.a[j];
+        if (!(hw > 0.0) || !(a > 0.0)) continue;
+        const double hwa = hw * a, n0 = Ls.n0[j];
+        v0 += hwa * (Ls.N[j] - n0 * p);
+        v1 -= n0 * hwa * (hw * p * (p + 1.0) * ikt2);
+    }
+    slope = warp_sum_uniform(v1);
+    return warp_sum_uniform(v0);
+}
+
+// n_eq at T from its expansion about T0: y = (hw / k)(1/T - 1/T0),
+// n = p0 - q y + r2 y^2 / 2 - r3 y^3 / 6 with q = p0 (p0 + 1),
+// r2 = q (2 p0 + 1), r3 = q (6 q + 1) the derivatives of n in x.
+struct RtaModel {
+    double du; // (1/T - 1/T0) / k
+    double ikt2;
+};
+
+__device__ __forceinline__ RtaModel rta_model(double T0, double T) {
+    RtaModel m;
+    m.du = (T0 - T) / (T * T0 * kKb);
+    m.ikt2 = 1.0 / (kKb * T * T);
+    return m;
+}
+
+__device__ __forceinline__ double rta_model_n(const RtaModel& m, double hw, double p0, double& dn) {
+    const double q = p0 * (p0 + 1.0);
+    const double r2 = q * (2.0 * p0 + 1.0), r3 = q * (6.0 * q + 1.0);
+    const double y = hw * m.du;
+    dn = -q + y * (r2 - 0.5 * y * r3); // dn/dx
+    return p0 + y * (-q + y * (0.5 * r2 - y * (r3 * (1.0 / 6.0))));
+}
+
+__device__ __forceinline__ double rta_eval_model(const RtaCellList& Ls, int count, int lane, double T0, double T,
+                                                 double& slope) {
+    const RtaModel m = rta_model(T0, T);
+    double v0 = 0.0, v1 = 0.0;
+    for (int j = lane; j < count; j += 32) {
+        const double hw = Ls.hw[j];
+        const double a = Ls.a[j];
+        if (!(hw > 0.0) || !(a > 0.0)) continue;
+        double dn;
+        const double p = rta_model_n(m, hw, Ls.p0[j], dn);
+        const double hwa = hw * a, n0 = Ls.n0[j];
+        v0 += hwa * (Ls.N[j] - n0 * p);
+        v1 += n0 * hwa * (hw * dn * m.ikt2); // f' = sum hw a cnt (hw / k T^2) dn/dx
+    }
+    slope = warp_sum_uniform(v1);
+    return warp_sum_uniform(v0);
+}
+
+template <bool kCollide>
+__global__ void __launch_bounds__(32 * kRtaCellWarps) k_rta_cell(const DevTables* __restrict__ Tp, CellArrays C,
+                                                                 DevLedger* L, int phase, int cap) {
+    const int c = static_cast<int>((blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x) >> 5);
+    if (c >= C.ncells) return; // warp-uniform
+    const int lane = threadIdx.x & 31;
+    const DevTables& T = *Tp;
+    const DevMaterial& M = T.mat[C.cell_material[c]];
+    const int nb = M.n_bins;
+    const size_t hb = static_cast<size_t>(c) * C.hist_modes;
+    const RtaCellList Ls = rta_cell_list(cap);
+
+    // bin sums of the cell (src/solver/GridStatistics.cpp:95-181) and its occupied classes
+    double st[3] = {0.0, 0.0, 0.0};
+    int count = 0;
+    for (int b0 = 0; b0 < nb; b0 += 32) {
+        const int b = b0 + lane;
+        unsigned k = 0;
+        double N = 0.0;
+        if (b < nb) {
+            const BinSum bin = C.bins[hb + b];
+            k = bin.cnt;
+            N = bin.N;
+            if (k) {
+                const int m = M.bin_rep ? M.bin_rep[b] : b;
+                st[0] += M.hw[m] * (N - k * M.nbg[m]);
+                if (M.grad_rate) {
+                    st[1] += k * M.grad_rate[m];
+                    st[2] += k * M.cap_bg[m];
+                }
+            }
+        }
+        const unsigned occ = __ballot_sync(0xffffffffu, k != 0);
+        if (k) {
+            const int j = count + __popc(occ & ((1u << lane) - 1u));
+            Ls.cls[j] = b;
+            Ls.n0[j] = static_cast<double>(k);
+            Ls.N[j] = N;
+        }
+        count += __popc(occ);
+    }
+    for (int k = 0; k < 3; ++k) st[k] = warp_sum_uniform(st[k]);
+    __syncwarp();
+
+    // cell state (src/solver/GridStatistics.cpp:213-226)
+    const double E = st[0] * M.energy_weight / C.volume[c] + M.energy_density_bg;
+    double Tc;
+    if (phase != 2)
+        Tc = T.par.linearized ? T.par.background_T + (E - M.energy_density_bg) / M.heat_capacity_density_bg
+                              : table_inverse(M.lookup_E, M.lookup_T, M.n_lookup, E);
+    else
+        Tc = C.temperature[c];
+    const double ratio = st[2] > 0.0 ? st[1] / st[2] : 0.0;
+    if (lane == 0) {
+        for (int k = 0; k < 3; ++k) C.cell_stats[4 * c + k] = st[k];
+        if (!isfinite(E)) raise_error(L, kErrNonFinite, c);
+        C.energy[c] = E;
+        if (phase != 2) C.temperature[c] = Tc;
+        C.grad_ratio[c] = ratio;
+    }
+
+    // pseudo-temperature over the occupied classes
+    double Ts = 0.0;
+    int neq_from = 0; // 0 the Bose formula at Ts, 1 the expansion point (T0 == Ts), 2 the expansion about T0
+    double T0 = 0.0;
+    if (kCollide) {
+        const double dt = T.par.dt;
+        const GammaSpan span = T.par.lifetime_local ? gamma_span(M, Tc) : GammaSpan{0, 0, 0.0, false};
+        double flow = 0.0, scale = 0.0;
+        for (int j = lane; j < count; j += 32) {
+            const int k = Ls.cls[j];
+            const int rep = M.class_rep[k];
+            double a;
+            if (T.par.lifetime_local) {
+                const double g = gamma_in(M, span, rep);
+                a = (g == 0.0 || dt == 0.0) ? 0.0 : -expm1(-(g * dt) * (4.0 * 3.14159265358979323846));
+            } else {
+                a = M.relax_fixed[rep];
+            }
+            Ls.a[j] = a;
+            const double hw = kHbar * fmax(0.0, M.class_omega[k]);
+            Ls.hw[j] = hw;
+            const bool act = hw > 0.0 && a > 0.0;
+            Ls.f32[j] = make_float4(static_cast<float>(hw), act ? static_cast<float>(hw * a) : 0.f,
+                                    static_cast<float>(Ls.N[j]), static_cast<float>(Ls.n0[j]));
+            scale += hw * a * C.hM[hb + k];
+            if (act) flow += hw * a * Ls.N[j]; // f(0): n_eq(0) = 0
+        }
+        flow = warp_sum_uniform(flow);
+        scale = warp_sum_uniform(scale);
+        double low = 0.0, high = fmax(1000.0, 2.0 * fmax(1.0, Tc));
+        if (!(flow <= 0.0)) {
+            // sign of f(high): FP32 value against a bound on its rounding error
+            float v32, d32, m32;
+            rta_eval32(Ls, count, lane, static_cast<float>(high), v32, d32, m32);
+            double f_high = -1.0;
+            if (!(v32 < -1e-3f * m32)) {
+                double dd;
+                f_high = rta_eval_exp(Ls, count, lane, high, dd);
+                for (int k = 0; f_high > 0.0 && k < 20; ++k) {
+                    high *= 2.0;
+                    f_high = rta_eval_exp(Ls, count, lane, high, dd);
+                }
+            }
+            if (f_high >= 0.0) {
+                Ts = high;
+            } else {
+                const double tol = 1e-13 * fmax(1.0, scale);
+                Ts = fmin(fmax(Tc, low), high); // the reference's first iterate
+                // Where f(Tc) may already pass the test (the FP32 residual at
+                // Tc is small against its terms, or the terms themselves are
+                // small), the FP64 iteration starts at Tc as the reference's
+                // does; elsewhere the reference cannot stop at Tc, and the FP64
+                // iteration starts at the FP32 root.
+                rta_eval32(Ls, count, lane, static_cast<float>(Ts), v32, d32, m32);
+                const bool from_tc = !(fabsf(v32) > 1e-4f * m32 && 1e-5 * static_cast<double>(m32) > tol);
+                if (!from_tc) {
+                    // FP32 Newton inside [low, high] from Tc
+                    float lo = static_cast<float>(low), hi = static_cast<float>(high);
+                    float t = static_cast<float>(Ts);
+                    for (int it = 0; it < 8 && t > 0.f; ++it) {
+                        if (it > 0) rta_eval32(Ls, count, lane, t, v32, d32, m32);
+                        if (v32 > 0.f) lo = t;
+                        else hi = t;
+                        float cand = 0.5f * (lo + hi);
+                        const float nt = t - v32 / d32;
+                        if (d32 < 0.f && nt > lo && nt < hi && isfinite(nt)) cand = nt;
+                        const bool done = fabsf(cand - t) <= 1e-6f * t;
+                        t = cand;
+                        if (done) break;
+                    }
+                    Ts = fmin(fmax(static_cast<double>(t), low), high);
+                }
+                // the FP64 iteration of the reference from there
+                bool expanded = false;
+                for (int it = 0; it < 40; ++it) {
+                    double d, v;
+                    const bool near = expanded && Ts > 0.0 && fabs(Ts - T0) <= 1e-5 * T0;
+                    if (near) {
+                        v = rta_eval_model(Ls, count, lane, T0, Ts, d);
+                    } else {
+                        v = rta_eval_exp(Ls, count, lane, Ts, d);
+                        T0 = Ts;
+                        expanded = Ts > 0.0;
+                    }
+                    if (fabs(v) <= tol) {
+                        neq_from = near ? 2 : 1;
+                        break;
+                    }
+                    if (v > 0.0) low = Ts;
+                    else high = Ts;
+                    double cand = 0.5 * (low + high);
+                    if (d < 0.0 && isfinite(d)) {
+                        const double nt = Ts - v / d;
+                        if (nt > low && nt < high && isfinite(nt)) cand = nt;
+                    }
+                    Ts = cand;
+                }
+            }
+        }
+    }
+
+    // pending update and step energies of the occupied bins (k_cell_tables)
+    const RtaModel model = neq_from == 2 ? rta_model(T0, Ts) : RtaModel{0.0, 0.0};
+    double s[3] = {0.0, 0.0, 0.0}; // residual, drive, updates
+    for (int j = lane; j < count; j += 32) {
+        const int b = Ls.cls[j];
+        const int m = M.bin_rep ? M.bin_rep[b] : b;
+        double a = 1.0, bc = 0.0;
+        if (kCollide) {
+            const double r = Ls.a[j];
+            double n;
+            if (neq_from == 1) {
+                n = Ls.p0[j];
+            } else if (neq_from == 2) {
+                double dn;
+                n = Ls.hw[j] > 0.0 ? rta_model_n(model, Ls.hw[j], Ls.p0[j], dn) : 0.0;
+            } else {
+                n = bose_hw(Ts, Ls.hw[j]);
+            }
+            a = 1.0 - r;
+            bc = r * n;
+        }
+        const double D = M.grad_rate ? fma(-M.drive_cap[m], ratio, M.drive_rate[m]) : 0.0;
+        const double k = Ls.n0[j];
+        const double hw = M.hw[m];
+        s[0] += hw * ((a - 1.0) * Ls.N[j] + k * bc);
+        if (D != 0.0) {
+            s[1] += k * hw * D;
+            s[2] += k;
+        }
+        C.ab[hb + b] = make_double2(a, kCollide ? bc + 2.0 * D : D);
+        if (!T.par.source_enabled) { // with a heat source the bins are cleared after its halves
+            BinSum zero;
+            zero.N = 0.0;
+            zero.cnt = 0;
+            zero.pad = 0;
+            C.bins[hb + b] = zero;
+            C.hM[hb + b] = 0.0;
+        }
+        if (C.src_next) C.src_next[hb + b] = 0.0;
+    }
+    for (int k = 0; k < 3; ++k) s[k] = warp_sum_uniform(s[k]);
+    if (lane == 0)
+        for (int k = 0; k < 3; ++k) C.cell_final[4 * c + k] = s[k];
+}
+
+int rta_cell_capacity(const CellArrays& C, int mode) {
+    const int cap = (C.hist_modes + 31) / 32 * 32;
+    if (mode < 0 || cap <= 0 || cap > kRtaCellMaxCap) return 0;
+    return (mode > 0 || C.ncells >= 1024) ? cap : 0;
+}
+
+void prepare_rta_cell(const CellArrays& C) {
+    (void)C;
+    // the largest list any solver of the process may use, so that solvers of
+    // different class counts can coexist
+    const int sm = static_cast<int>(rta_cell_smem(kRtaCellMaxCap));
+    cudaFuncSetAttribute(reinterpret_cast<const void*>(k_rta_cell<true>), cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    cudaFuncSetAttribute(reinterpret_cast<const void*>(k_rta_cell<false>), cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+}
+
 // --------------------------------------------------- nonlinear Callaway
 // src/solver/NonlinearCallawayCollision.cpp:25-248. Per cell, three BGK
 // substeps N(dt/2), R(dt), N(dt/2) move every carrier n <- (1 - a) n + a t,
@@ -1068,37 +1477,35 @@ __global__ void __launch_bounds__(kStatThreads) k_cell_tables(const DevTables* _
     k_cell_tables_body<kCollision>(Tp, C, phase, blockIdx.x, gridDim.x, blockIdx.y);
 }
 
-// End of step: cell temperatures, total thermal energy and the energy ledger. One CTA.
-__device__ __forceinline__ void k_cells_final_body(const DevTables* __restrict__ Tp, CellArrays C, DevLedger* L, int phase, int vbx, int vgx) {
-    (void)vbx;
-    (void)vgx;
-    __shared__ double red[4 * 32];
-    const DevTables& T = *Tp;
-    double v[4] = {0.0, 0.0, 0.0, 0.0}; // thermal, residual, drive, updates
-    for (int c = threadIdx.x; c < C.ncells; c += blockDim.x) {
-        const DevMaterial& M = T.mat[C.cell_material[c]];
-        double* f = C.cell_final + 4 * c;
-        const double w = M.energy_weight;
-        // step-start energy + collision + drive half + heat-source half (f[3])
-        const double dev = C.cell_stats[4 * c] + (phase >= 1 ? f[0] + f[1] + f[3] : 0.0);
-        const double Ef = dev * w / C.volume[c] + M.energy_density_bg;
-        if (!isfinite(Ef)) raise_error(L, kErrNonFinite, c);
-        C.energy_final[c] = Ef;
-        C.temperature_final[c] =
-            phase == 2 ? C.temperature[c]
-                       : (T.par.linearized ? T.par.background_T + (Ef - M.energy_density_bg) / M.heat_capacity_density_bg
-                                           : table_inverse(M.lookup_E, M.lookup_T, M.n_lookup, Ef));
-        v[0] += (Ef - M.zero_point) * C.volume[c];
-        v[1] += f[0] * w;
-        v[2] += f[1] * w;
-        v[3] += f[2];
-        for (int k = 0; k < 4; ++k) {
-            f[k] = 0.0;
-            C.cell_stats[4 * c + k] = 0.0;
-        }
+// End of step: cell temperatures, total thermal energy and the energy ledger.
+// Per cell: the step-end energy and temperature; v gathers the thermal energy,
+// lifetime residual, drive energy and drive updates over the cells.
+__device__ __forceinline__ void cells_final_cell(const DevTables& T, const CellArrays& C, DevLedger* L, int phase,
+                                                 int c, double (&v)[4]) {
+    const DevMaterial& M = T.mat[C.cell_material[c]];
+    double* f = C.cell_final + 4 * c;
+    const double w = M.energy_weight;
+    // step-start energy + collision + drive half + heat-source half (f[3])
+    const double dev = C.cell_stats[4 * c] + (phase >= 1 ? f[0] + f[1] + f[3] : 0.0);
+    const double Ef = dev * w / C.volume[c] + M.energy_density_bg;
+    if (!isfinite(Ef)) raise_error(L, kErrNonFinite, c);
+    C.energy_final[c] = Ef;
+    C.temperature_final[c] =
+        phase == 2 ? C.temperature[c]
+                   : (T.par.linearized ? T.par.background_T + (Ef - M.energy_density_bg) / M.heat_capacity_density_bg
+                                       : table_inverse(M.lookup_E, M.lookup_T, M.n_lookup, Ef));
+    v[0] += (Ef - M.zero_point) * C.volume[c];
+    v[1] += f[0] * w;
+    v[2] += f[1] * w;
+    v[3] += f[2];
+    for (int k = 0; k < 4; ++k) {
+        f[k] = 0.0;
+        C.cell_stats[4 * c + k] = 0.0;
     }
-    block_sum<4>(v, red);
-    if (threadIdx.x != 0) return;
+}
+
+// The ledger update from the grid sums v (one thread).
+__device__ __forceinline__ void cells_final_ledger(const DevTables& T, DevLedger* L, int phase, const double (&v)[4]) {
     L->next_drive_ev += v[2];
     L->next_drive_updates += static_cast<unsigned long long>(v[3]);
     if (phase == 0) {
@@ -1128,9 +1535,46 @@ __device__ __forceinline__ void k_cells_final_body(const DevTables* __restrict__
     L->elapsed += T.par.dt;
 }
 
-__global__ void __launch_bounds__(1024) k_cells_final(const DevTables* __restrict__ Tp, CellArrays C, DevLedger* L,
-                                                      int phase) {
-    k_cells_final_body(Tp, C, L, phase, blockIdx.x, gridDim.x);
+// One CTA over all cells (the batched films: one CTA per film).
+__device__ __forceinline__ void k_cells_final_body(const DevTables* __restrict__ Tp, CellArrays C, DevLedger* L, int phase, int vbx, int vgx) {
+    (void)vbx;
+    (void)vgx;
+    __shared__ double red[4 * 32];
+    const DevTables& T = *Tp;
+    double v[4] = {0.0, 0.0, 0.0, 0.0}; // thermal, residual, drive, updates
+    for (int c = threadIdx.x; c < C.ncells; c += blockDim.x) cells_final_cell(T, C, L, phase, c, v);
+    block_sum<4>(v, red);
+    if (threadIdx.x == 0) cells_final_ledger(T, L, phase, v);
+}
+
+// The grid over the cells: every CTA leaves its partial sums in C.final_part;
+// the CTA that finishes last folds them in CTA order (the same sums for the
+// same grid on every run) and updates the ledger.
+__global__ void __launch_bounds__(256) k_cells_final(const DevTables* __restrict__ Tp, CellArrays C, DevLedger* L,
+                                                     int phase) {
+    __shared__ double red[4 * 32];
+    __shared__ bool last;
+    const DevTables& T = *Tp;
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C.ncells; c += gridDim.x * blockDim.x)
+        cells_final_cell(T, C, L, phase, c, v);
+    block_sum<4>(v, red);
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < 4; ++k) C.final_part[4 * blockIdx.x + k] = v[k];
+        __threadfence();
+        last = atomicAdd(C.final_done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double u[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int b = threadIdx.x; b < static_cast<int>(gridDim.x); b += blockDim.x)
+        for (int k = 0; k < 4; ++k) u[k] += __ldcg(C.final_part + 4 * b + k);
+    block_sum<4>(u, red);
+    if (threadIdx.x == 0) {
+        cells_final_ledger(T, L, phase, u);
+        *C.final_done = 0u;
+    }
 }
 
 // ------------------------------------------------------- heat source
@@ -1413,6 +1857,13 @@ int launch_cell_solve(const LaunchCtx& x, int phase, int collision) {
     const int chunks = (C.hist_modes + kChunk - 1) / kChunk;
     const dim3 grid(chunks, C.ncells);
     const bool rta = collision == kCollideRta;
+    if (rta && C.rta_cell_cap) {
+        const int cap = C.rta_cell_cap;
+        const dim3 g((C.ncells + kRtaCellWarps - 1) / kRtaCellWarps), b(32 * kRtaCellWarps);
+        if (phase >= 1) k_rta_cell<true><<<g, b, rta_cell_smem(cap), x.stream>>>(T, C, x.L, phase, cap);
+        else k_rta_cell<false><<<g, b, rta_cell_smem(cap), x.stream>>>(T, C, x.L, phase, cap);
+        return 1;
+    }
     int launches = 3;
     if (rta) k_cell_stats<true><<<grid, kStatThreads, 0, x.stream>>>(T, C, phase >= 1 ? 1 : 0);
     else k_cell_stats<false><<<grid, kStatThreads, 0, x.stream>>>(T, C, 0);
@@ -1480,7 +1931,7 @@ int launch_cell_solve(const LaunchCtx& x, int phase, int collision) {
 }
 
 void launch_cells_final(const LaunchCtx& x, int phase) {
-    k_cells_final<<<1, 1024, 0, x.stream>>>(x.T, x.C, x.L, phase);
+    k_cells_final<<<x.C.final_blocks, 256, 0, x.stream>>>(x.T, x.C, x.L, phase);
 }
 
 } // namespace phmc

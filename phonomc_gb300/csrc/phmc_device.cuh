@@ -287,6 +287,7 @@ struct DevFacets {
     const DevRoughTable* rough;    // every rough table of the domain
     const int* voxel_cell;         // voxel -> active cell
     const int* cell_voxel;         // active cell -> home voxel (origin of its FP32 offsets)
+    const unsigned char* voxel_interior; // voxel -> 1: every point of its box is inside (null: none)
     DevMesh mesh;                  // oriented faces and their BVH
     int prism;                     // extruded prism: facet-scan trace, ray-cast membership
     const double* facet_centroid;  // [n][3] (prism trace)
@@ -1149,6 +1150,20 @@ __device__ inline int mesh_contains(const DevFacets& F, const double p[3]) {
     const int r = mesh_ray_cast_inside(F, p);
     if (r != 0 || F.prism) return r; // a prism answers by the ray cast alone
     return mesh_simplex_inside(F, p) ? 1 : 0;
+}
+
+// True when p lies in a voxel whose whole box is inside the mesh (mesh_contains
+// answers 1 there; the closed surface does not cross such a box).
+__device__ __forceinline__ bool mesh_voxel_interior(const DevFacets& F, const DevDomain& D, const double p[3]) {
+    if (!F.voxel_interior) return false;
+    int idx[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const double u = floor((p[a] - D.lo[a]) * D.inv_cell[a]);
+        if (!(u >= 0.0 && u < static_cast<double>(D.shape[a]))) return false;
+        idx[a] = static_cast<int>(u);
+    }
+    return F.voxel_interior[(static_cast<size_t>(idx[0]) * D.shape[1] + idx[1]) * D.shape[2] + idx[2]] != 0;
 }
 
 // True when p lies within `tol` of a face: the face BVH culls every node

@@ -837,7 +837,8 @@ void EnergyLedger::finish_step(double energy, const BoundaryBalance& b) {
 int resolved_sort_interval(const SimulationConfig& c, bool mixed) {
     if (c.carrier_sort_interval < 0) return 0;
     if (c.carrier_sort_interval > 0) return c.carrier_sort_interval;
-    return c.particle_count >= tuning::kSortMinCarriers ? tuning::kSortInterval[mixed ? 1 : 0] : 0;
+    if (c.particle_count < tuning::kSortMinCarriers) return 0;
+    return c.model != "box" ? tuning::kSortIntervalMesh[mixed ? 1 : 0] : tuning::kSortInterval[mixed ? 1 : 0];
 }
 
 void validate_heat_source_config(const SimulationConfig& c) {

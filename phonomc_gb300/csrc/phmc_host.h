@@ -97,6 +97,7 @@ struct SimulationConfig {
     int transport_blocks_per_sm = 0;
     int tally_aggregation = 0;
     int transport_pipeline = 0;
+    int rta_cell_update = 0; // 1 fused warp-per-cell RTA cell kernel, < 0 separate kernels, 0 by grid size
     std::string material_folder; // reported in summary.txt; tables enter as arrays
     // Layered materials (include/SimulationConfig.h:93-99): N materials, N-1 planes.
     int material_interface_axis = 0;
@@ -368,6 +369,10 @@ public:
     // active cell -> its home voxel, the voxel whose centre made the cell
     // (mesh domains; the identity for boxes)
     std::vector<int> cell_voxels() const;
+    // voxel -> 1 when every point of its box (widened by 1e-6 of the domain
+    // scale) lies inside the mesh: no face's bounding box reaches the widened
+    // box and the voxel centre is inside (mesh domains other than prisms)
+    const std::vector<unsigned char>& voxel_interior() const { return voxel_interior_; }
     const Vec3& bounds_min() const { return bmin_; }
     const Vec3& bounds_max() const { return bmax_; }
     double volume() const { return volume_; }
@@ -397,6 +402,7 @@ private:
     std::vector<int> reservoir_facets_;
     std::unique_ptr<SurfaceMesh> mesh_;
     std::vector<int> voxel_cell_;
+    std::vector<unsigned char> voxel_interior_;
     bool prism_ = false;
     std::vector<std::array<Vec3, 3>> prism_top_;
     void build_prism_cells(int nx, int ny, int nz);

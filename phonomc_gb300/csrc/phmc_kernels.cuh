@@ -93,7 +93,9 @@ void launch_ingest(const LaunchCtx& x, bool mixed, const HostCarriers& h);
 void launch_ledger_replace(const LaunchCtx& x, int n);
 void launch_positions_out(const LaunchCtx& x);
 int launch_inject(const LaunchCtx& x, bool mixed, bool rta, int* holes, int* block_dead, int capacity);
-void launch_containment(const LaunchCtx& x, bool mixed);
+// Containment check of the live carriers; mesh carriers outside the interior
+// voxels are queued in `queue` (capacity: the slots) for the membership test.
+int launch_containment(const LaunchCtx& x, bool mixed, int* queue, int* count);
 void launch_flux(const LaunchCtx& x, bool mixed);
 void launch_apply_pending(const LaunchCtx& x, bool subtract_drive);
 void launch_step_begin(const LaunchCtx& x);
@@ -109,6 +111,11 @@ int linear_cluster_size(const CellArrays& C, bool mixed);
 void prepare_linear_solve(const CellArrays& C, bool global);
 size_t linear_global_slice(const CellArrays& C, bool mixed);
 void launch_cells_final(const LaunchCtx& x, int phase);
+// Occupied-class list entries per warp of the fused RTA cell kernel for these
+// cell arrays (0: separate kernels). mode 1 forces it where the classes fit,
+// < 0 turns it off, 0 takes it on grids of 1024 cells or more.
+int rta_cell_capacity(const CellArrays& C, int mode);
+void prepare_rta_cell(const CellArrays& C);
 
 // collision kinds for launch_cell_solve
 enum CollisionKind : int { kCollideNone = 0, kCollideRta = 1, kCollideLinear = 2, kCollideNonlinear = 3 };
@@ -267,6 +274,7 @@ void fill_dev_facets(const SimulationDomain& dom, double scale, DevFacets& G, Up
     G.normal = up(normal);
     G.voxel_cell = up(dom.voxel_cells());
     G.cell_voxel = up(dom.cell_voxels());
+    if (!dom.voxel_interior().empty()) G.voxel_interior = up(dom.voxel_interior());
     G.prism = dom.is_prism() ? 1 : 0;
     if (dom.is_prism()) {
         std::vector<double> centroid(3 * static_cast<size_t>(nf)), tri;

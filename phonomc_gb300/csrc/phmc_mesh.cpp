@@ -922,6 +922,27 @@ void SimulationDomain::build_mesh_domain(const SimulationConfig& cfg) {
             voxel_cell_[v] = static_cast<int>(centers_.size());
             centers_.push_back(voxel_centre(v));
         }
+        // interior voxels: the closed surface does not cross a box that no
+        // face's bounding box reaches, so the whole box shares its centre's side
+        const double margin = 1e-6 * std::max({1.0, ext[0], ext[1], ext[2]});
+        std::vector<unsigned char> touched(total, 0);
+        const auto& V = M.vertices();
+        for (const auto& fc : M.faces()) {
+            int lo[3], hi[3];
+            for (int a = 0; a < 3; ++a) {
+                const double fmin = std::min({V[fc[0]][a], V[fc[1]][a], V[fc[2]][a]}) - margin;
+                const double fmax = std::max({V[fc[0]][a], V[fc[1]][a], V[fc[2]][a]}) + margin;
+                const int n = shape_[a];
+                // the margin (1e-6 of the scale) dwarfs the rounding of these indices
+                lo[a] = std::max(0, static_cast<int>(std::floor((fmin - bmin_[a]) * inv_cell_[a])));
+                hi[a] = std::min(n - 1, static_cast<int>(std::floor((fmax - bmin_[a]) * inv_cell_[a])));
+            }
+            for (int ix = lo[0]; ix <= hi[0]; ++ix)
+                for (int iy = lo[1]; iy <= hi[1]; ++iy)
+                    for (int iz = lo[2]; iz <= hi[2]; ++iz) touched[(static_cast<size_t>(ix) * ny + iy) * nz + iz] = 1;
+        }
+        voxel_interior_.assign(total, 0);
+        for (size_t v = 0; v < total; ++v) voxel_interior_[v] = inside[v] && !touched[v] ? 1 : 0;
     }
     if (centers_.empty()) throw std::runtime_error("No valid grid centers found inside mesh.");
     std::deque<int> queue;

@@ -143,6 +143,7 @@ inline SimulationConfig config_from_pod(const phmc_config& c) {
     s.transport_blocks_per_sm = c.transport_blocks_per_sm;
     s.tally_aggregation = c.tally_aggregation;
     s.transport_pipeline = c.transport_pipeline;
+    s.rta_cell_update = c.rta_cell_update;
     s.material_interface_model = c.interface_model;
     s.material_interface_amm_fraction = c.interface_amm_fraction;
     if (c.interface_parallel_bin_inv_a != 0) s.material_interface_parallel_bin_inv_a = c.interface_parallel_bin_inv_a;

@@ -174,6 +174,7 @@ void DeviceSolver::allocate_state(int capacity) {
     state_.cell = dalloc<int32_t>(padded);
     state_.alive = dalloc<uint8_t>(padded);
     d_holes_ = dalloc<int>(capacity);
+    d_contain_count_ = dalloc<int>(1);
     n_dead_blocks_ = (capacity + 1023) / 1024;
     d_block_dead_ = dalloc<int>(n_dead_blocks_);
     d_ledger_ = dalloc<DevLedger>(1);
@@ -507,12 +508,17 @@ void DeviceSolver::upload_tables() {
         C.src_next = dalloc<double>(hist);
     }
     C.cell_final = dalloc<double>(4 * static_cast<size_t>(ncells_));
+    C.final_blocks = std::max(1, std::min(256, (ncells_ + 255) / 256));
+    C.final_part = dalloc<double>(4 * static_cast<size_t>(C.final_blocks));
+    C.final_done = dalloc<unsigned>(1);
     if (rta) {
         // per-cell class sums; the stride is the largest class count of the materials
         int max_classes = 0;
         for (const auto& M : P_.mats) max_classes = std::max(max_classes, M.n_classes);
         C.n_classes = max_classes; // == bins per cell
         C.rta_ab = dalloc<double2>(static_cast<size_t>(ncells_) * max_classes);
+        C.rta_cell_cap = rta_cell_capacity(C, cfg_.rta_cell_update);
+        if (C.rta_cell_cap) prepare_rta_cell(C);
     } else if (P_.callaway_nonlinear) {
         // composed (alpha, beta) per (cell, mode) and the moment-solve work space
         C.n_classes = hist_modes;
@@ -781,10 +787,7 @@ bool DeviceSolver::batch_extras_due() const {
 void DeviceSolver::finish_batched_step(long long launches) {
     if (failed_) throw std::runtime_error("Cannot resume a failed timestep; construct a new solver after fixing its cause.");
     counters_.launches += launches;
-    if (step_ % 100 == 0) {
-        launch_containment(ctx(), mixed_);
-        counters_.launches += 1;
-    }
+    if (step_ % 100 == 0) counters_.launches += launch_containment(ctx(), mixed_, d_holes_, d_contain_count_);
     materialized_ = false;
     ++step_;
     elapsed_ += cfg_.time_step;
@@ -835,11 +838,9 @@ void DeviceSolver::run_timestep() {
     } else {
         enqueue_step(profile_pass_a_);
     }
-    if (step_ % 100 == 0) {
-        // src/solver/TransportOperator.cpp:364-402, every 100 steps
-        launch_containment(ctx(), mixed_);
-        counters_.launches += 1;
-    }
+    // src/solver/TransportOperator.cpp:364-402, every 100 steps (the free-slot
+    // list of the injection is the queue: it is rebuilt before its next use)
+    if (step_ % 100 == 0) counters_.launches += launch_containment(ctx(), mixed_, d_holes_, d_contain_count_);
     materialized_ = false;
     ++step_;
     elapsed_ += cfg_.time_step;

@@ -116,6 +116,13 @@ struct CellArrays {
     const int* class_start;
     const int* class_modes;
     int n_classes;
+    // end-of-step sums: one partial per CTA of k_cells_final, folded by the last CTA
+    double* final_part;      // [final_blocks * 4]
+    unsigned* final_done;    // CTAs finished (reset by the last one)
+    int final_blocks;
+    // RTA on grids of many cells: entries of the warp's occupied-class list in
+    // shared memory (k_rta_cell); 0 runs the separate stats / solve / tables kernels
+    int rta_cell_cap;
 };
 
 struct StepCounters {
@@ -250,6 +257,7 @@ private:
     CellArrays cells_{};
     int* d_holes_ = nullptr;
     int* d_block_dead_ = nullptr;
+    int* d_contain_count_ = nullptr; // carriers queued for the membership test of the containment check
     int n_dead_blocks_ = 0;
     std::vector<void*> allocations_;
     // host-side observables

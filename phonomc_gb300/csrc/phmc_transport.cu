@@ -1797,36 +1797,72 @@ __global__ void k_inject_finish(DevLedger* L) {
 }
 
 // Escaped-carrier check (src/solver/TransportOperator.cpp:364-402).
+// Position of carrier i (the mixed state from its cell frame and FP32 offsets).
 template <bool kMixed>
-__global__ void k_containment(const DevTables* __restrict__ Tp, CarrierState S, DevLedger* L) {
+__device__ __forceinline__ void contain_position(const DevTables& T, const CarrierState& S, int i, double p[3]) {
+    if (kMixed) {
+        const DevDomain& D = T.dom;
+        const Frame F = cell_frame_of(T, S.cell[i]);
+        p[0] = D.lo[0] + F.i[0] * D.cell_size[0] + S.ox[i];
+        p[1] = D.lo[1] + F.i[1] * D.cell_size[1] + S.oy[i];
+        p[2] = D.lo[2] + F.i[2] * D.cell_size[2] + S.oz[i];
+    } else {
+        p[0] = S.x[i];
+        p[1] = S.y[i];
+        p[2] = S.z[i];
+    }
+}
+
+// Containment check (src/solver/TransportOperator.cpp:364-402), first part:
+// the bounds test of every live carrier; mesh carriers outside the interior
+// voxels go to `queue` for the membership test (k_contain_cast), so that the
+// ray casts run in full warps.
+template <bool kMixed>
+__global__ void k_contain_screen(const DevTables* __restrict__ Tp, CarrierState S, DevLedger* L, int* queue,
+                                 int* count) {
     const DevDomain& D = Tp->dom;
     const int n = L->n_slots;
-    const double tol = 1e-10 * D.scale;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        if (!S.alive[i]) continue;
+    const int lane = threadIdx.x & 31;
+    // FP32 offsets carry ~1e-7 relative rounding of the cell size
+    const double t = kMixed ? 1e-5 * D.scale : 1e-10 * D.scale;
+    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        bool cast = false;
+        if (i < n && S.alive[i]) {
+            double p[3];
+            contain_position<kMixed>(*Tp, S, i, p);
+            bool outside = false;
+            for (int a = 0; a < 3; ++a) outside = outside || !isfinite(p[a]) || p[a] < D.lo[a] - t || p[a] > D.hi[a] + t;
+            if (outside) raise_error(L, kErrEscaped, i);
+            else cast = Tp->fac.n > 0 && !mesh_voxel_interior(Tp->fac, D, p);
+        }
+        const unsigned want = __ballot_sync(0xffffffffu, cast);
+        if (want) {
+            int first = 0;
+            if (lane == 0) first = atomicAdd(count, __popc(want));
+            first = __shfl_sync(0xffffffffu, first, 0);
+            if (cast) queue[first + __popc(want & ((1u << lane) - 1u))] = i;
+        }
+    }
+}
+
+// Second part: membership of the queued carriers (SurfaceMesh::contains_point).
+template <bool kMixed>
+__global__ void k_contain_cast(const DevTables* __restrict__ Tp, CarrierState S, DevLedger* L, const int* queue,
+                               const int* count) {
+    const DevDomain& D = Tp->dom;
+    const int n = *count;
+    const double t = kMixed ? 1e-5 * D.scale : 1e-10 * D.scale;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const int i = queue[q];
         double p[3];
-        if (kMixed) {
-            const Frame F = cell_frame_of(*Tp, S.cell[i]);
-            p[0] = D.lo[0] + F.i[0] * D.cell_size[0] + S.ox[i];
-            p[1] = D.lo[1] + F.i[1] * D.cell_size[1] + S.oy[i];
-            p[2] = D.lo[2] + F.i[2] * D.cell_size[2] + S.oz[i];
-        } else {
-            p[0] = S.x[i];
-            p[1] = S.y[i];
-            p[2] = S.z[i];
-        }
-        // FP32 offsets carry ~1e-7 relative rounding of the cell size
-        const double t = kMixed ? 1e-5 * D.scale : tol;
-        bool outside = false;
-        for (int a = 0; a < 3; ++a) outside = outside || !isfinite(p[a]) || p[a] < D.lo[a] - t || p[a] > D.hi[a] + t;
-        if (!outside && Tp->fac.n > 0) {
-            const int in = mesh_contains(Tp->fac, p);
-            if (in < 0) raise_error(L, kErrInvalidStatistics, i);
-            outside = in == 0;
-            // the mixed state may sit outside a wall by its FP32 rounding:
-            // escaped only when farther from the surface than that
-            if (kMixed && outside) outside = !mesh_near_surface(Tp->fac, p, t);
-        }
+        contain_position<kMixed>(*Tp, S, i, p);
+        const int in = mesh_contains(Tp->fac, p);
+        if (in < 0) raise_error(L, kErrInvalidStatistics, i);
+        bool outside = in == 0;
+        // the mixed state may sit outside a wall by its FP32 rounding:
+        // escaped only when farther from the surface than that
+        if (kMixed && outside) outside = !mesh_near_surface(Tp->fac, p, t);
         if (outside) raise_error(L, kErrEscaped, i);
     }
 }
@@ -2101,9 +2137,17 @@ int launch_inject(const LaunchCtx& x, bool mixed, bool rta, int* holes, int* blo
     return 5;
 }
 
-void launch_containment(const LaunchCtx& x, bool mixed) {
-    if (mixed) k_containment<true><<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.L);
-    else k_containment<false><<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.L);
+int launch_containment(const LaunchCtx& x, bool mixed, int* queue, int* count) {
+    cudaMemsetAsync(count, 0, sizeof(int), x.stream);
+    const dim3 ge(2 * x.event_grid);
+    if (mixed) {
+        k_contain_screen<true><<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.L, queue, count);
+        if (x.mesh) k_contain_cast<true><<<ge, kTransportThreads, 0, x.stream>>>(x.T, x.S, x.L, queue, count);
+    } else {
+        k_contain_screen<false><<<x.grid_blocks, 256, 0, x.stream>>>(x.T, x.S, x.L, queue, count);
+        if (x.mesh) k_contain_cast<false><<<ge, kTransportThreads, 0, x.stream>>>(x.T, x.S, x.L, queue, count);
+    }
+    return x.mesh ? 2 : 1;
 }
 
 void launch_flux(const LaunchCtx& x, bool /*mixed*/) {

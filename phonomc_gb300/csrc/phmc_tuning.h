@@ -16,6 +16,8 @@ constexpr int kTransportBlocksPerSm[2] = {16, 2};
 // domains (0: never), and the smallest population that is sorted at all.
 constexpr int kSortInterval[2] = {50, 200};
 constexpr double kSortMinCarriers = 2e+06;
+// The same for surface-mesh domains (FinFET sweep of the record's "mesh_sorts").
+constexpr int kSortIntervalMesh[2] = {25, 25};
 // Bin tallies of the carrier pass: 1 sums runs of equal (cell, bin) across
 // the lanes of a warp before one FP64 atomic per run, 0 one atomic per carrier.
 constexpr int kTallyAggregation[2] = {0, 1};

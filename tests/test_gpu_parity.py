@@ -152,9 +152,11 @@ def _compare(sg, so, tol=1e-12):
     return stg, sto
 
 
-def test_cross_plane_steps_match_oracle(gpu, orc):
+@pytest.mark.parametrize("cell_update", [-1, 1])
+def test_cross_plane_steps_match_oracle(gpu, orc, cell_update):
+    """RTA film: separate cell kernels (-1) and the fused warp-per-cell update (1)."""
     mat = synthetic.make_material(mesh=16)
-    cfg = workloads.scaled(workloads.cross_plane_film(), 20000, random_seed=7)
+    cfg = workloads.scaled(workloads.cross_plane_film(), 20000, random_seed=7, rta_cell_update=cell_update)
     (sg, _), (so, _) = _pair(gpu, orc, cfg, False, mat)
     _compare(sg, so)
     for _ in range(3):
@@ -571,12 +573,15 @@ def test_mesh_domain_device_queries_golden(gpu, finfet_stl):
     assert np.array_equal(cell, np.arange(dom.n_cells, dtype=np.int32))
 
 
+@pytest.mark.parametrize("cell_update", [-1, 1])
 @pytest.mark.parametrize("source", [True, False])
-def test_finfet_steps_match_oracle(gpu, orc, finfet_stl, source):
+def test_finfet_steps_match_oracle(gpu, orc, finfet_stl, source, cell_update):
     """FinFET mesh domain (BVH walls, rough facets with mirrored outward modes,
     periodic facet pairs, heat sink, Gaussian heat source): device timesteps
-    against the oracle on the same initial carriers."""
+    against the oracle on the same initial carriers, with the separate RTA
+    cell kernels (-1) and the fused warp-per-cell update (1)."""
     cfg = workloads.finfet_mesh(finfet_stl, particles=20000, seed=11, grid=(32, 8, 16), heat_source=source)
+    cfg["rta_cell_update"] = cell_update
     mat = synthetic.make_material(mesh=8)
     (sg, _), (so, _) = _pair(gpu, orc, cfg, False, mat)
     _compare(sg, so, tol=1e-11)

@@ -61,6 +61,30 @@ def test_cells_and_queries(finfet):
     assert np.array_equal(np.asarray(g["cell"]), finfet.grid_index(P))
 
 
+def test_interior_voxels_lie_inside(finfet):
+    """Voxels flagged interior (no face's bounding box reaches them, centre
+    inside) hold only inside points -- the containment check of the carrier
+    loop skips the ray cast there. Random points of every interior voxel,
+    including its corners, are inside by the reference's membership test, and
+    the flags cover most of the inside voxels."""
+    I = finfet.voxel_interior()
+    C = finfet.cells()
+    assert I.shape == finfet.shape
+    inside_voxels = C["voxel_cell"].reshape(finfet.shape) >= 0
+    flagged = np.argwhere(I == 1)
+    assert len(flagged) > 0.5 * finfet.n_cells
+    lo, hi = finfet.bounds
+    size = (hi - lo) / np.asarray(finfet.shape)
+    rng = np.random.default_rng(3)
+    pick = flagged[rng.choice(len(flagged), size=min(len(flagged), 4000), replace=False)]
+    u = rng.random((len(pick), 3))
+    u[:200] = np.round(u[:200])  # box corners
+    P = lo + (pick + u) * size
+    assert finfet.contains(P).all()
+    # an interior voxel's centre makes a cell (membership of its centre)
+    assert inside_voxels[I == 1].all()
+
+
 def test_region_errors(tmp_path):
     """Configuration errors surface with the reference's messages."""
     from phonomc_gb300 import abi, native, workloads
