@@ -6,6 +6,8 @@
 // 287-361 (boundary collision), 405-466 (event loop);
 // src/solver/BoundaryInteraction.cpp:53-162; src/solver/ReservoirInjector.cpp:62-132;
 // src/solver/TemperatureGradientDrive.cpp:116-171; src/solver/GridStatistics.cpp:269-347.
+#include <type_traits>
+
 #include "phmc_kernels.cuh"
 
 namespace phmc {
@@ -1027,6 +1029,32 @@ __device__ __forceinline__ void queue_event(const CarrierState& S, DevLedger* L,
     }
 }
 
+// Streamed fields of one slot of the mixed state. Every field is loaded before
+// alive is looked at, so the loads of a carrier share one memory round trip
+// (slots below n_slots are allocated whether alive or not).
+struct MixedSlot {
+    bool in;
+    uint8_t alive;
+    uint32_t w;
+    int c0;
+    double occ0;
+    float p[3];
+};
+
+__device__ __forceinline__ MixedSlot load_mixed_slot(const CarrierState& S, int i, int n) {
+    MixedSlot s;
+    s.in = i < n;
+    const int ic = s.in ? i : 0;
+    s.alive = __ldcs(S.alive + ic);
+    s.w = __ldcs(S.mode + ic);
+    s.c0 = __ldcs(S.cell + ic);
+    s.occ0 = __ldcs(S.occ + ic);
+    s.p[0] = __ldcs(S.ox + ic);
+    s.p[1] = __ldcs(S.oy + ic);
+    s.p[2] = __ldcs(S.oz + ic);
+    return s;
+}
+
 // qbuf: kDeferBuffer entries per warp of the block (mixed path).
 template <bool kMixed, bool kRta, bool kAgg>
 __device__ __forceinline__ void k_transport_body(const DevTables& T, CarrierState S, CellArrays C, DevLedger* L, int vbx,
@@ -1038,20 +1066,19 @@ __device__ __forceinline__ void k_transport_body(const DevTables& T, CarrierStat
     const int n = L->n_slots;
     if constexpr (kMixed) {
         int queued = 0; // warp-uniform
-        // block-uniform trip count so that every lane reaches the warp-wide ballot
-        for (int base = vbx * blockDim.x; base < n; base += vgx * blockDim.x) {
+        // block-uniform trip count so that every lane reaches the warp-wide
+        // ballot; the next slot's streamed fields are in flight while this
+        // one flies (each slot belongs to one thread of the pass)
+        const int stride = vgx * blockDim.x;
+        int base = vbx * blockDim.x;
+        MixedSlot cur = load_mixed_slot(S, base + threadIdx.x, n);
+        for (; base < n; base += stride) {
             const int i = base + threadIdx.x;
-            // every streamed field is loaded before alive is looked at, so the
-            // loads of a carrier share one memory round trip (slots below
-            // n_slots are allocated whether alive or not)
-            const bool in = i < n;
-            const int ic = in ? i : 0;
-            const uint8_t alive = __ldcs(S.alive + ic);
-            const uint32_t w = __ldcs(S.mode + ic);
-            const int c0 = __ldcs(S.cell + ic);
-            const double occ0 = __ldcs(S.occ + ic);
-            float p[3] = {__ldcs(S.ox + ic), __ldcs(S.oy + ic), __ldcs(S.oz + ic)};
-            mixed_carrier<kRta, kAgg>(T, S, C, L, bl, step, i, in, alive, w, c0, occ0, p, qbuf, queued);
+            MixedSlot next;
+            if (base + stride < n) next = load_mixed_slot(S, i + stride, n);
+            mixed_carrier<kRta, kAgg>(T, S, C, L, bl, step, i, cur.in, cur.alive, cur.w, cur.c0, cur.occ0, cur.p,
+                                      qbuf, queued);
+            cur = next;
         }
         flush_deferred(S, L, qbuf, queued);
     } else {
@@ -1295,36 +1322,69 @@ __global__ void __launch_bounds__(kTransportThreads) k_transport_mesh(const __gr
     constexpr bool kMixed = kMixedState;
     const int n = L->n_slots;
     const double dt = T.par.dt;
-    const int lane = threadIdx.x & 31;
-    for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    // every streamed field of a slot in one memory round trip, and the next
+    // slot's fields in flight while this one moves (each slot belongs to one
+    // thread of the pass)
+    struct Slot {
+        bool live;
+        uint32_t w;
+        int c0, mirror;
+        double occ0, ht;
+        typename std::conditional<kMixed, float, double>::type p[3]; // FP32 offsets (mixed) or positions
+    };
+    auto load = [&](int i) {
+        Slot s;
+        const int ic = i < n ? i : 0;
+        s.live = i < n && __ldcs(S.alive + ic);
+        s.w = __ldcs(S.mode + ic);
+        s.c0 = __ldcs(S.cell + ic);
+        s.occ0 = __ldcs(S.occ + ic);
+        s.ht = __ldcs(T.fac.hit_t + ic);
+        s.mirror = __ldcs(T.fac.mirror + ic);
+        if (kMixed) {
+            s.p[0] = __ldcs(S.ox + ic);
+            s.p[1] = __ldcs(S.oy + ic);
+            s.p[2] = __ldcs(S.oz + ic);
+        } else {
+            s.p[0] = __ldcs(S.x + ic);
+            s.p[1] = __ldcs(S.y + ic);
+            s.p[2] = __ldcs(S.z + ic);
+        }
+        return s;
+    };
+    const int stride = gridDim.x * blockDim.x;
+    int base = blockIdx.x * blockDim.x;
+    Slot cur = load(base + threadIdx.x);
+    for (; base < n; base += stride) {
         const int i = base + threadIdx.x;
+        Slot next;
+        if (base + stride < n) next = load(i + stride);
         bool defer = false;
         long long h = -1;
         double hocc = 0.0;
-        if (i < n && __ldcs(S.alive + i)) {
-            const uint32_t w = __ldcs(S.mode + i);
-            const int c0 = __ldcs(S.cell + i);
-            const double occ = apply_pending(T, C, c0, w, __ldcs(S.occ + i));
-            const double ht = __ldcs(T.fac.hit_t + i);
+        if (cur.live) {
+            const uint32_t w = cur.w;
+            const int c0 = cur.c0;
+            const double occ = apply_pending(T, C, c0, w, cur.occ0);
+            const double ht = cur.ht;
             const double t_wall = dmul(ht, dt);
             if (!isfinite(t_wall) || t_wall > dt) {
                 int c;
                 if (kMixed) {
                     // FP32 flight in the frame of the home voxel, then the new cell
                     float v[3];
-                    mesh_velocity32(T.fac, T.mat[w >> 28], w, __ldcs(T.fac.mirror + i), v);
+                    mesh_velocity32(T.fac, T.mat[w >> 28], w, cur.mirror, v);
                     const float dt32 = T.par.dt32;
-                    float q[3] = {fmaf(v[0], dt32, __ldcs(S.ox + i)), fmaf(v[1], dt32, __ldcs(S.oy + i)),
-                                  fmaf(v[2], dt32, __ldcs(S.oz + i))};
+                    float q[3] = {fmaf(v[0], dt32, cur.p[0]), fmaf(v[1], dt32, cur.p[1]), fmaf(v[2], dt32, cur.p[2])};
                     c = settle_mesh(T, cell_frame_of(T, c0), q);
                     __stcs(S.ox + i, q[0]);
                     __stcs(S.oy + i, q[1]);
                     __stcs(S.oz + i, q[2]);
                 } else {
                     double v[3];
-                    mesh_velocity(T.fac, T.mat[w >> 28], w, __ldcs(T.fac.mirror + i), v);
-                    const double p[3] = {dadd(__ldcs(S.x + i), dmul(v[0], dt)), dadd(__ldcs(S.y + i), dmul(v[1], dt)),
-                                         dadd(__ldcs(S.z + i), dmul(v[2], dt))};
+                    mesh_velocity(T.fac, T.mat[w >> 28], w, cur.mirror, v);
+                    const double p[3] = {dadd(cur.p[0], dmul(v[0], dt)), dadd(cur.p[1], dmul(v[1], dt)),
+                                         dadd(cur.p[2], dmul(v[2], dt))};
                     c = cell_at(T, p[0], p[1], p[2]);
                     __stcs(S.x + i, p[0]);
                     __stcs(S.y + i, p[1]);
@@ -1342,6 +1402,7 @@ __global__ void __launch_bounds__(kTransportThreads) k_transport_mesh(const __gr
         }
         bin_warp<true, kRta>(C, h, hocc);
         queue_event(S, L, defer, i);
+        cur = next;
     }
 }
 
