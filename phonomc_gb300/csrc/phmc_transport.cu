@@ -1068,16 +1068,26 @@ __device__ __forceinline__ void k_transport_body(const DevTables& T, CarrierStat
         int queued = 0; // warp-uniform
         // block-uniform trip count so that every lane reaches the warp-wide
         // ballot; the next slot's streamed fields are in flight while this
-        // one flies (each slot belongs to one thread of the pass)
+        // one flies (each slot belongs to one thread of the pass). With one
+        // material the mode word's material bits (always 0 then) are cleared
+        // in the copy the carrier works on, so every table index folds to a
+        // compile-time 0 and the table fields become constant-bank operands.
         const int stride = vgx * blockDim.x;
         int base = vbx * blockDim.x;
+        const bool one_material = T.par.n_materials == 1;
+        auto run = [&](MixedSlot& s, int i) {
+            if (one_material)
+                mixed_carrier<kRta, kAgg>(T, S, C, L, bl, step, i, s.in, s.alive, s.w & 0x0FFFFFFFu, s.c0, s.occ0, s.p,
+                                          qbuf, queued);
+            else
+                mixed_carrier<kRta, kAgg>(T, S, C, L, bl, step, i, s.in, s.alive, s.w, s.c0, s.occ0, s.p, qbuf,
+                                          queued);
+        };
         MixedSlot cur = load_mixed_slot(S, base + threadIdx.x, n);
         for (; base < n; base += stride) {
-            const int i = base + threadIdx.x;
             MixedSlot next;
-            if (base + stride < n) next = load_mixed_slot(S, i + stride, n);
-            mixed_carrier<kRta, kAgg>(T, S, C, L, bl, step, i, cur.in, cur.alive, cur.w, cur.c0, cur.occ0, cur.p,
-                                      qbuf, queued);
+            if (base + stride < n) next = load_mixed_slot(S, base + stride + threadIdx.x, n);
+            run(cur, base + threadIdx.x);
             cur = next;
         }
         flush_deferred(S, L, qbuf, queued);
