@@ -1592,7 +1592,7 @@ __global__ void __launch_bounds__(kStatThreads) k_source(const DevTables* __rest
     __shared__ double s_pend;
     __shared__ int s_arg;
     const DevTables& T = *Tp;
-    const int c = blockIdx.x;
+    const int c = C.src_cells[blockIdx.x];
     // this half's time window: second half of the running step, or first half of the coming one
     const double t0 = L->elapsed, half = __dmul_rn(0.5, T.par.dt);
     const double factor = next ? source_time_factor(T.par, t0, __dadd_rn(t0, half))
@@ -1804,9 +1804,10 @@ __global__ void __launch_bounds__(kStatThreads) k_source(const DevTables* __rest
 void launch_step_begin(const LaunchCtx& x) { k_step_begin<<<1, 1, 0, x.stream>>>(x.L); }
 
 void launch_source(const LaunchCtx& x, bool final_temperature, bool next) {
-    k_source<<<x.C.ncells, kStatThreads, 0, x.stream>>>(x.T, x.C, x.L,
-                                                         final_temperature ? x.C.temperature_final : x.C.temperature,
-                                                         next ? 1 : 0);
+    // one CTA per cell of positive power
+    if (x.C.n_src_cells > 0)
+        k_source<<<x.C.n_src_cells, kStatThreads, 0, x.stream>>>(
+            x.T, x.C, x.L, final_temperature ? x.C.temperature_final : x.C.temperature, next ? 1 : 0);
     if (next) {
         // last reader of this step's bins
         const size_t hist = static_cast<size_t>(x.C.ncells) * x.C.hist_modes;

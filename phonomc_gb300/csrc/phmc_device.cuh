@@ -1066,8 +1066,11 @@ __device__ __forceinline__ void mesh_face(const DevMesh& M, int i, double a[3], 
 // +x ray-cast membership (src/SurfaceMesh.cpp:1100-1124): the Moller-Trumbore
 // hits of every face, sorted, counted as distinct when more than 1e-9 apart;
 // odd means inside. The BVH only culls nodes the ray misses by more than
-// ray_pad, so the hit set is that of the full face scan. Returns -1 when more
-// hits than the local list holds (the caller reports an error).
+// ray_pad, so the hit set is that of the full face scan. With the FP32 node
+// and face records (widened by M.margin, and face planes and edges tested
+// with an error bound as in mesh_walk_fp32) only nodes and faces that FP32
+// cannot rule out reach the FP64 test, so the hit set is the same. Returns -1
+// when more hits than the local list holds (the caller reports an error).
 __device__ inline int mesh_ray_cast_inside(const DevFacets& F, const double p[3]) {
     constexpr int kMaxHits = 64;
     const DevMesh& M = F.mesh;
@@ -1082,7 +1085,50 @@ __device__ inline int mesh_ray_cast_inside(const DevFacets& F, const double p[3]
         if (nh < kMaxHits) hits[nh++] = t;
         else overflow = true;
     };
-    if (M.root >= 0) {
+    if (M.root >= 0 && M.nodes32) {
+        const float m = M.margin;
+        const float xf[3] = {static_cast<float>(p[0]), static_cast<float>(p[1]), static_cast<float>(p[2])};
+        // a face FP32 cannot rule out for the ray x + (1, 0, 0) t, t > 0
+        auto screen = [&](int pos) {
+            const float* r = M.face32 + kFaceRecord32 * pos;
+            const float den = r[0];
+            if (fabsf(den) >= 1e-4f) {
+                const float tf = -(xf[0] * r[0] + xf[1] * r[1] + xf[2] * r[2] + r[3]) / den;
+                const float et = m / fabsf(den) + (4e-7f / fabsf(den) + 1e-6f) * fabsf(tf) + 1e-6f;
+                if (tf + et <= 0.0f) return false;
+                const float ep = et + 1e-6f * fabsf(tf) + m;
+                const float q[3] = {xf[0] + tf, xf[1], xf[2]};
+                for (int a = 0; a < 3; ++a)
+                    if (q[a] < r[4 + a] - ep || q[a] > r[7 + a] + ep) return false;
+                const float tol = ep + 4.0f * m + 1e-7f;
+                for (int e = 0; e < 3; ++e) {
+                    const float* g = r + 10 + 4 * e;
+                    if (fmaf(g[0], q[0], fmaf(g[1], q[1], g[2] * q[2])) - g[3] < -tol) return false;
+                }
+            }
+            return true;
+        };
+        int stack[64];
+        int top = 0;
+        stack[top++] = M.root;
+        while (top > 0) {
+            const DevBvhNode32 nd = M.nodes32[stack[--top]];
+            if (xf[1] < nd.bmin[1] - m || xf[1] > nd.bmax[1] + m || xf[2] < nd.bmin[2] - m ||
+                xf[2] > nd.bmax[2] + m || xf[0] > nd.bmax[0] + m)
+                continue;
+            if (nd.left < 0 && nd.right < 0) {
+                for (int pos = nd.begin; pos < nd.end; ++pos)
+                    if (screen(pos)) test_face(pos);
+                continue;
+            }
+            if (top + 2 > 64) {
+                overflow = true;
+                break;
+            }
+            if (nd.left >= 0) stack[top++] = nd.left;
+            if (nd.right >= 0) stack[top++] = nd.right;
+        }
+    } else if (M.root >= 0) {
         int stack[64];
         int top = 0;
         stack[top++] = M.root;

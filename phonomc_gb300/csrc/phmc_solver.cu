@@ -498,6 +498,12 @@ void DeviceSolver::upload_tables() {
     C.cell_stats = dalloc<double>(4 * static_cast<size_t>(ncells_));
     if (P_.source.enabled) {
         C.src_rate = upload(P_.source.rates);
+        // a cell of zero power never accrues a budget, so its halves only copy zeros
+        std::vector<int> powered;
+        for (int c = 0; c < ncells_; ++c)
+            if (P_.source.rates[c] > 0.0) powered.push_back(c);
+        C.n_src_cells = static_cast<int>(powered.size());
+        C.src_cells = powered.empty() ? nullptr : upload(powered);
         C.src_pending = dalloc<double>(ncells_);
         C.src_prescribed = dalloc<double>(ncells_);
         C.src_deposited = dalloc<double>(ncells_);

@@ -109,6 +109,8 @@ struct CellArrays {
     double* src_step_book;     // [2 ncells] prescribed, deposited at the step boundary, before the next step's first accrual
     double* src_scratch;
     double* src_next;        // [ncells * hist_modes] next step's first source half inside ab.y (null: no source)
+    const int* src_cells;    // the cells of positive source power (the only ones a half changes)
+    int n_src_cells;
     int src_classes;
     double lin_h;
     int lin_terms;
