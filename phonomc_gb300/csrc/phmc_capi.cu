@@ -285,8 +285,15 @@ BatchDesc phmc_batch::describe(int lo, int hi, int persist) {
     std::vector<int> capacity(n), carrier_block(n + 1, 0), hole_block(n + 1, 0), cell_begin(n + 1, 0),
         cell_block(n + 1, 0), inject_block(n + 1, 0);
     int chunks = 1;
+    int rta_cap = 0;
+    bool rta_fused = true;
     for (int i = 0; i < n; ++i) {
         const DeviceSolver& x = *s[lo + i];
+        // the batch holds many cells in all: the fused RTA cell update where
+        // every instance's classes fit it and none turned it off
+        const int cap = x.rta_cell_update() < 0 ? 0 : rta_cell_capacity(x.cell_arrays(), 1);
+        rta_fused = rta_fused && cap > 0;
+        rta_cap = std::max(rta_cap, cap);
         tables[i] = x.device_tables();
         states[i] = x.carrier_state();
         cells[i] = x.cell_arrays();
@@ -325,6 +332,8 @@ BatchDesc phmc_batch::describe(int lo, int hi, int persist) {
     D.total_cell_blocks = cell_block[n];
     D.chunks = chunks;
     D.persist = persist;
+    D.rta_cap = rta_fused ? rta_cap : 0;
+    if (D.rta_cap) prepare_rta_cell(cells[0]);
     return D;
 }
 

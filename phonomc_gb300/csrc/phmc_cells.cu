@@ -515,13 +515,11 @@ __device__ __forceinline__ double rta_eval_model(const RtaCellList& Ls, int coun
     return warp_sum_uniform(v0);
 }
 
+// The RTA cell update of cell c by the calling warp (its list is the warp's
+// slot of the CTA's dynamic shared memory).
 template <bool kCollide>
-__global__ void __launch_bounds__(32 * kRtaCellWarps) k_rta_cell(const DevTables* __restrict__ Tp, CellArrays C,
-                                                                 DevLedger* L, int phase, int cap) {
-    const int c = static_cast<int>((blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x) >> 5);
-    if (c >= C.ncells) return; // warp-uniform
-    const int lane = threadIdx.x & 31;
-    const DevTables& T = *Tp;
+__device__ __forceinline__ void rta_cell_body(const DevTables& T, const CellArrays& C, DevLedger* L, int phase,
+                                              int cap, int c, int lane) {
     const DevMaterial& M = T.mat[C.cell_material[c]];
     const int nb = M.n_bins;
     const size_t hb = static_cast<size_t>(c) * C.hist_modes;
@@ -722,6 +720,23 @@ __global__ void __launch_bounds__(32 * kRtaCellWarps) k_rta_cell(const DevTables
         for (int k = 0; k < 3; ++k) C.cell_final[4 * c + k] = s[k];
 }
 
+template <bool kCollide>
+__global__ void __launch_bounds__(32 * kRtaCellWarps) k_rta_cell(const DevTables* __restrict__ Tp, CellArrays C,
+                                                                 DevLedger* L, int phase, int cap) {
+    const int c = static_cast<int>((blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x) >> 5);
+    if (c >= C.ncells) return; // warp-uniform
+    rta_cell_body<kCollide>(*Tp, C, L, phase, cap, c, threadIdx.x & 31);
+}
+
+// The fused update over every cell of a batch (one warp per cell of every
+// instance; all instances have `cap` or fewer classes).
+__global__ void __launch_bounds__(32 * kRtaCellWarps) kf_rta_cell(const BatchDesc D, int cap) {
+    const int g = static_cast<int>((blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x) >> 5);
+    if (g >= D.total_cells) return; // warp-uniform
+    const int i = batch_find(D.cell_begin, D.n, g);
+    rta_cell_body<true>(*D.tables[i], D.cells[i], D.ledgers[i], 1, cap, g - D.cell_begin[i], threadIdx.x & 31);
+}
+
 int rta_cell_capacity(const CellArrays& C, int mode) {
     const int cap = (C.hist_modes + 31) / 32 * 32;
     if (mode < 0 || cap <= 0 || cap > kRtaCellMaxCap) return 0;
@@ -735,6 +750,7 @@ void prepare_rta_cell(const CellArrays& C) {
     const int sm = static_cast<int>(rta_cell_smem(kRtaCellMaxCap));
     cudaFuncSetAttribute(reinterpret_cast<const void*>(k_rta_cell<true>), cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     cudaFuncSetAttribute(reinterpret_cast<const void*>(k_rta_cell<false>), cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    cudaFuncSetAttribute(reinterpret_cast<const void*>(kf_rta_cell), cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
 }
 
 // --------------------------------------------------- nonlinear Callaway
@@ -1974,6 +1990,12 @@ __global__ void __launch_bounds__(1024) kf_cells_final(const BatchDesc D, int ph
 }
 
 int launch_fused_cells(const BatchDesc& D, cudaStream_t s) {
+    if (D.rta_cap > 0) {
+        kf_rta_cell<<<(D.total_cells + kRtaCellWarps - 1) / kRtaCellWarps, 32 * kRtaCellWarps,
+                      rta_cell_smem(D.rta_cap), s>>>(D, D.rta_cap);
+        kf_cells_final<<<D.n, 1024, 0, s>>>(D, 1);
+        return 2;
+    }
     kf_cell_stats<<<dim3(D.chunks, D.total_cells), kStatThreads, 0, s>>>(D);
     kf_cell_state<<<D.total_cell_blocks, 256, 0, s>>>(D, 1);
     kf_rta_solve<<<(D.total_cells + 7) / 8, 256, 0, s>>>(D);

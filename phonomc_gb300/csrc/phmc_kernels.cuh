@@ -58,6 +58,7 @@ struct BatchDesc {
     int total_carrier_blocks, total_hole_blocks, total_cells, total_cell_blocks, total_inject_blocks;
     int chunks;                       // mode chunks of the widest instance
     int persist;                      // resident CTAs of the persistent carrier kernels
+    int rta_cap;                      // occupied-class list of the fused RTA cell update (0: separate kernels)
 };
 
 // Instance owning index x of a prefix-sum array: the last i with prefix[i] <= x.

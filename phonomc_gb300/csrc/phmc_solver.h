@@ -208,6 +208,7 @@ public:
     const CarrierState& carrier_state() const { return state_; }
     const CellArrays& cell_arrays() const { return cells_; }
     int* hole_list() const { return d_holes_; }
+    int rta_cell_update() const { return cfg_.rta_cell_update; }
     int* hole_blocks() const { return d_block_dead_; }
     bool has_reservoirs() const { return !P_.reservoirs.empty(); }
     int initial_particles() const { return P_.initial_particles; }
