@@ -628,7 +628,7 @@ __device__ __forceinline__ void rta_cell_body(const DevTables& T, const CellArra
                 // does; elsewhere the reference cannot stop at Tc, and the FP64
                 // iteration starts at the FP32 root.
                 rta_eval32(Ls, count, lane, static_cast<float>(Ts), v32, d32, m32);
-                const bool from_tc = !(fabsf(v32) > 1e-4f * m32 && 1e-5 * static_cast<double>(m32) > tol);
+                const bool from_tc = !(fabsf(v32) > 2e-5f * m32 && 1e-5 * static_cast<double>(m32) > tol);
                 if (!from_tc) {
                     // FP32 Newton inside [low, high] from Tc
                     float lo = static_cast<float>(low), hi = static_cast<float>(high);
