@@ -830,14 +830,17 @@ def test_staged_pass_matches_direct_loads(gpu, name, stationary):
         assert sa[k] == sb[k], k
 
 
+@pytest.mark.parametrize("cell_update", [-1, 1])
 @pytest.mark.parametrize("model,fraction", [("amm", 1.0), ("mmm", 0.4)])
-def test_bilayer_amm_steps_match_oracle(gpu, orc, model, fraction):
+def test_bilayer_amm_steps_match_oracle(gpu, orc, model, fraction, cell_update):
     """Acoustic (and mixed) mismatch interface events inside whole device steps
     against the oracle: rows built on the host, sampled on the device with the
-    oracle's draws; carriers, cells and interface counters exact."""
+    oracle's draws; carriers, cells and interface counters exact. Two RTA
+    materials: the separate cell kernels (-1) and the fused warp-per-cell
+    update (1), which takes each cell's material and class list."""
     data = workloads.bilayer_materials(8, callaway=False)
     cfg = workloads.scaled(workloads.bilayer_amm(model=model, amm_fraction=fraction), 20000, random_seed=41,
-                           grid=(1, 1, 20))
+                           grid=(1, 1, 20), rta_cell_update=cell_update)
     mg = [abi.Material(gpu, "phmc_", d, 0.1, False, False) for d in data]
     mo = [abi.Material(orc, "orc_", d, 0.1, False, False) for d in data]
     sg, so = abi.Solver(gpu, "phmc_", cfg, mg), abi.Solver(orc, "orc_", cfg, mo)
