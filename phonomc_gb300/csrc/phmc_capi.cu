@@ -1145,7 +1145,8 @@ int phmc_dev_rough_reflect(const phmc_material* m, int conservative, double Tref
         rt.build({&M}, {{nout[0], nout[1], nout[2]}}, {rough_a}, {1}, conservative != 0, conservative ? Tref : 0.0,
                  &scan);
         const RoughTable& R = rt.tables.at(0);
-        DBuf<double> spec(R.specularity), prefix(R.residual_prefix), rcdf(R.roulette_cdf);
+        DBuf<double> spec(R.specularity), prefix(R.residual_prefix), rcdf(R.roulette_cdf),
+            coarse(coarse_prefix(R.residual_prefix));
         DBuf<int> match(R.spec_match), db(R.diffuse_begin), de(R.diffuse_end), sorted(R.outgoing_sorted),
             ract(R.roulette_active), oact(R.outgoing_active);
         DevRoughTable D{};
@@ -1159,6 +1160,7 @@ int phmc_dev_rough_reflect(const phmc_material* m, int conservative, double Tref
         D.diffuse_end = de.p;
         D.outgoing_sorted = sorted.p;
         D.prefix = prefix.p;
+        D.coarse = coarse.p;
         D.roulette_active = ract.p;
         D.roulette_cdf = rcdf.p;
         D.outgoing_active = oact.p;

@@ -121,6 +121,7 @@ struct DevRoughTable {
     const int* diffuse_end;
     const int* outgoing_sorted;
     const double* prefix;
+    const double* coarse;     // prefix[64 k], k = 0 .. n_sorted / 64 (null: one-level search)
     const int* roulette_active;
     const double* roulette_cdf;
     const int* outgoing_active;
@@ -499,8 +500,21 @@ __device__ __forceinline__ int rough_sample_dev(const DevRoughTable& R, const De
         if (window > 0.0 && isfinite(window)) {
             const double u = fmin(fmax(u1, 0.0), 0.99999999999999989);
             const double target = fb + u * window;
-            // upper_bound over prefix[b+1 .. e]
+            // upper_bound over prefix[b+1 .. e]: the block of 64 that holds it
+            // from the coarse copy (small enough to stay in L2), then the block;
+            // the prefix is non-decreasing, so the bound is the one-level one
             int lo = b + 1, hi = e + 1;
+            if (R.coarse) {
+                const int klo = (lo + 63) >> 6, khi = (hi - 1) >> 6; // block starts inside [lo, hi)
+                int a = klo, z = khi + 1;
+                while (a < z) {
+                    const int mid = (a + z) >> 1;
+                    if (R.coarse[mid] <= target) a = mid + 1;
+                    else z = mid;
+                }
+                if (a > klo) lo = max(lo, ((a - 1) << 6) + 1); // prefix[64 (a - 1)] <= target
+                if (a <= khi) hi = min(hi, a << 6);            // prefix[64 a] > target
+            }
             while (lo < hi) {
                 const int mid = (lo + hi) >> 1;
                 if (R.prefix[mid] <= target) lo = mid + 1;

@@ -112,6 +112,14 @@ int linear_cluster_size(const CellArrays& C, bool mixed);
 void prepare_linear_solve(const CellArrays& C, bool global);
 size_t linear_global_slice(const CellArrays& C, bool mixed);
 void launch_cells_final(const LaunchCtx& x, int phase);
+// Every 64th entry of a rough table's residual prefix (the first level of the
+// device's two-level diffuse search).
+inline std::vector<double> coarse_prefix(const std::vector<double>& prefix) {
+    std::vector<double> c;
+    for (size_t k = 0; k < prefix.size(); k += 64) c.push_back(prefix[k]);
+    return c;
+}
+
 // Occupied-class list entries per warp of the fused RTA cell kernel for these
 // cell arrays (0: separate kernels). mode 1 forces it where the classes fit,
 // < 0 turns it off, 0 takes it on grids of 1024 cells or more.

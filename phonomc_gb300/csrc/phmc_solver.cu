@@ -332,6 +332,7 @@ void DeviceSolver::upload_tables() {
         D.diffuse_end = upload(R.diffuse_end);
         D.outgoing_sorted = upload(R.outgoing_sorted);
         D.prefix = upload(R.residual_prefix);
+        D.coarse = upload(coarse_prefix(R.residual_prefix));
         D.roulette_active = upload(R.roulette_active);
         D.roulette_cdf = upload(R.roulette_cdf);
         D.outgoing_active = upload(R.outgoing_active);
