@@ -80,6 +80,7 @@ __device__ __forceinline__ void k_step_begin_body(DevLedger* L, int vbx, int vgx
     L->next_source_updates = 0;
     L->n_inject = 0;
     L->n_deferred = 0;
+    L->event_head = 0;
 }
 
 __global__ void k_step_begin(DevLedger* L) {

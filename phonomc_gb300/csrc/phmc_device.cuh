@@ -192,6 +192,7 @@ struct DevLedger {
     int n_holes;            // free slots below n_slots at injection
     int n_inject;           // carriers injected this step
     int n_deferred;         // wall events queued by the mixed transport pass this step
+    int event_head;         // queue entries handed out to the warps of the mesh event pass
     uint32_t step_index;    // timesteps completed (the draw counter of the running step)
     double elapsed;         // ps at the start of the running step
     int inject_count[kMaxReservoirs];

@@ -1426,7 +1426,16 @@ __global__ void __launch_bounds__(kTransportThreads, 2) k_mesh_events(const __gr
     block_ledger_init(&bl);
     __syncthreads();
     const int nq = min(L->n_deferred, S.capacity);
-    for (int q = queue_first(blockIdx.x, gridDim.x); q < nq; q += gridDim.x * blockDim.x) {
+    // each warp takes the next 32 queue entries when it is done with its own,
+    // so walks of uneven length do not leave warps idle at the end
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int q0 = 0;
+        if (lane == 0) q0 = atomicAdd(&L->event_head, 32);
+        q0 = __shfl_sync(0xffffffffu, q0, 0);
+        if (q0 >= nq) break;
+        const int q = q0 + lane;
+        if (q >= nq) continue;
         const int i = S.deferred[q].x;
         if (i < 0 || i >= S.capacity) {
             raise_error(L, kErrInvalidStatistics, i);
