@@ -309,7 +309,7 @@ BatchDesc phmc_batch::describe(int lo, int hi, int persist) {
         hole_block[i + 1] = hole_block[i] + (capacity[i] + 1023) / 1024;
         cell_begin[i + 1] = cell_begin[i] + x.cell_arrays().ncells;
         cell_block[i + 1] = cell_block[i] + (x.cell_arrays().ncells + 255) / 256;
-        chunks = std::max(chunks, (x.cell_arrays().hist_modes + 1023) / 1024);
+        chunks = std::max(chunks, (x.cell_arrays().hist_modes + kStatChunk - 1) / kStatChunk);
     }
     BatchDesc D{};
     D.n = n;

@@ -33,7 +33,7 @@ namespace cg = cooperative_groups;
 namespace phmc {
 
 constexpr int kStatThreads = 256;
-constexpr int kChunk = 1024;     // modes per stats/tables block
+constexpr int kChunk = kStatChunk; // modes per stats/tables block
 constexpr int kMaxGains = 5;
 constexpr int kLinThreads = 256;
 

@@ -41,6 +41,9 @@ struct LaunchCtx {
 // Independent box instances advanced by one launch per kernel of the step:
 // per-instance device state behind arrays, and prefix sums that assign each
 // CTA of a fused launch to an instance (the instance's own grid of CTAs).
+// Modes per CTA of the per-(cell, mode) statistics and table kernels.
+constexpr int kStatChunk = 4096;
+
 struct BatchDesc {
     int n;                            // instances
     const DevTables* const* tables;   // [n] device copies of each instance's tables
