@@ -139,9 +139,10 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_down(uint32_t* __restrict
     }
 }
 
-// Stable scatter of one tile: items in slot order (round, warp, lane); a key's
-// destination is its digit's offset for this tile, plus the digit's items in
-// earlier rounds, earlier warps of this round, and earlier lanes of its warp.
+// Stable scatter of one tile: items in slot order (sweep of the CTA over the
+// tile, warp, lane); a key's destination is its digit's offset for this tile,
+// plus the digit's items in earlier sweeps, earlier warps of this sweep, and
+// earlier lanes of its warp.
 __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint32_t* __restrict__ kin,
                                                                 const uint32_t* __restrict__ vin,
                                                                 uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
