@@ -15,7 +15,7 @@
 //
 // Each pass of 8 key bits: per-tile digit histograms (k_radix_hist), one
 // exclusive scan over the digit-major count table (k_scan_*), and a stable
-// scatter (k_radix_scatter) in which a tile ranks its keys round by round with
+// scatter (k_radix_scatter) in which a tile ranks its keys sweep by sweep with
 // warp match masks and per-warp digit counts in shared memory.
 #include "phmc_kernels.cuh"
 #include "phmc_sort.cuh"
