@@ -1947,14 +1947,40 @@ __global__ void k_contain_cast(const DevTables* __restrict__ Tp, CarrierState S,
     }
 }
 
+// Sums of x[0..2] over the lanes of `peers` (the lanes that hold the same
+// key), left in the lowest lane of each group: a tree over every group at
+// once in at most five rounds (reduce-by-key of warp-aggregated adds).
+__device__ __forceinline__ void reduce_peers3(unsigned peers, double x[3]) {
+    const int lane = threadIdx.x & 31;
+    unsigned rel = __popc(peers & ((1u << lane) - 1u)); // rank in the group
+    unsigned above = peers & (0xfffffffeu << lane);      // group lanes above this one
+    while (__any_sync(0xffffffffu, above != 0u)) {
+        const int next = above ? __ffs(above) - 1 : lane;
+        double t[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) t[a] = __shfl_sync(0xffffffffu, x[a], next);
+        if (above) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) x[a] = dadd(x[a], t[a]);
+        }
+        // odd ranks have been read by their lower neighbour: out of every group
+        above &= ~__ballot_sync(0xffffffffu, rel & 1u);
+        rel >>= 1;
+    }
+}
+
 // Heat-flux tally q_c = sum v e w (src/solver/GridStatistics.cpp:269-347) with the
 // end-of-step occupation n = alpha n + beta - (second drive half). Each thread
 // walks kFluxRun consecutive slots and keeps one running sum per component
-// while the cell stays the same -- sorted carriers come in runs of one cell --
-// and adds it to the target when the cell changes or its slots end: `target`
-// 2 one copy of the cell sums per warp in shared memory, 1 one copy per block
-// (shared atomics either way), 0 the global sums. Per carrier that leaves the
-// pending update, the drive half and three fused multiply-adds in FP64.
+// while the cell stays the same -- sorted carriers come in runs of one cell.
+// A run ends when the cell changes or the slots end; on every step in which
+// some lane of the warp ends a run, the ending runs are summed by cell across
+// the warp (reduce_peers3) and one lane per cell adds the sum to the target:
+// `target` 2 one copy of the cell sums per warp in shared memory (plain adds:
+// the adding lanes hold distinct cells), 1 one copy per block (shared
+// atomics), 0 the global sums. Sorted carriers thus cost the pending update,
+// the drive half and three fused multiply-adds per carrier plus a reduction
+// every few slots; unsorted ones (one run per carrier) one reduction per slot.
 constexpr int kFluxRun = 8;
 
 __global__ void __launch_bounds__(256) k_flux(const DevTables* __restrict__ Tp, CarrierState S, CellArrays C,
@@ -1962,38 +1988,51 @@ __global__ void __launch_bounds__(256) k_flux(const DevTables* __restrict__ Tp, 
     extern __shared__ double sq[];
     const DevTables& T = *Tp;
     const int nq = 3 * C.ncells;
-    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     if (target > 0)
         for (int k = threadIdx.x; k < (target == 2 ? nwarps : 1) * nq; k += blockDim.x) sq[k] = 0.0;
     __syncthreads();
     double* dst = target == 2 ? sq + warp * nq : (target == 1 ? sq : C.flux);
-    auto flush = [&](int c, const double (&acc)[3]) {
+    // every lane calls: lanes with `ending` hand in their run (cell `key`, sums acc)
+    auto hand_in = [&](bool ending, int key, double a0, double a1, double a2) {
+        if (!__any_sync(0xffffffffu, ending)) return;
+        const unsigned peers = __match_any_sync(0xffffffffu, ending ? key : -1);
+        double v[3] = {ending ? a0 : 0.0, ending ? a1 : 0.0, ending ? a2 : 0.0};
+        reduce_peers3(peers, v);
+        if (ending && lane == __ffs(peers) - 1) {
+            if (target == 2) {
 #pragma unroll
-        for (int a = 0; a < 3; ++a) atomicAdd(dst + 3 * c + a, acc[a]);
+                for (int a = 0; a < 3; ++a) dst[3 * key + a] = dadd(dst[3 * key + a], v[a]);
+            } else {
+#pragma unroll
+                for (int a = 0; a < 3; ++a) atomicAdd(dst + 3 * key + a, v[a]);
+            }
+        }
+        if (target == 2) __syncwarp();
     };
     const int n = L->n_slots;
     const int per_block = blockDim.x * kFluxRun;
-    for (int base = blockIdx.x * per_block; base < n; base += gridDim.x * per_block) {
+    for (int base = blockIdx.x * per_block; base < n; base += gridDim.x * per_block) { // block-uniform
         const int i0 = base + threadIdx.x * kFluxRun;
         int cur = -1;
         double acc[3] = {0.0, 0.0, 0.0};
-#pragma unroll 2
-        for (int k = 0; k < kFluxRun; ++k) {
+        for (int k = 0; k < kFluxRun; ++k) { // warp-uniform trip count: every lane reaches hand_in
             const int i = i0 + k;
-            if (i >= n) break;
-            if (!S.alive[i]) continue;
-            const uint32_t w = S.mode[i];
-            const int c = S.cell[i];
+            const bool live = i < n && S.alive[i];
+            const uint32_t w = live ? S.mode[i] : 0u;
+            const int c = live ? S.cell[i] : -1;
+            const bool change = live && c != cur;
+            hand_in(change && cur >= 0, cur, acc[0], acc[1], acc[2]);
+            if (change) {
+                cur = c;
+                acc[0] = acc[1] = acc[2] = 0.0;
+            }
+            if (!live) continue;
             const DevMaterial& M = T.mat[w >> 28];
             const int ai = static_cast<int>(w & 0x00FFFFFFu);
             double occ = apply_pending(T, C, c, w, S.occ[i]) - drive_half(T, C, M, c, ai);
             if (C.src_next) occ -= C.src_next[static_cast<size_t>(c) * C.hist_modes + bin_of(M, ai)];
             const double x = occ - M.nbg[ai];
-            if (c != cur) {
-                if (cur >= 0) flush(cur, acc);
-                cur = c;
-                acc[0] = acc[1] = acc[2] = 0.0;
-            }
             if (T.fac.mirror) {
                 double v[3];
                 mesh_velocity(T.fac, M, w, T.fac.mirror[i], v);
@@ -2011,7 +2050,7 @@ __global__ void __launch_bounds__(256) k_flux(const DevTables* __restrict__ Tp, 
                 }
             }
         }
-        if (cur >= 0) flush(cur, acc);
+        hand_in(cur >= 0, cur, acc[0], acc[1], acc[2]);
     }
     __syncthreads();
     if (target > 0)
