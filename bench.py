@@ -471,9 +471,12 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    # default: one whole carrier-sort interval of the mixed state (200 steps),
-    # so a sort weighs in the timed window at its share of a long run
-    ap.add_argument("--steps", type=int, default=200)
+    # default: one whole carrier-sort interval of the mixed state on boxes (200
+    # steps), so a sort weighs in the timed window at its share of a long run;
+    # the FinFET mesh 100 (four of its 25-step sort intervals: the synthetic
+    # FinFET loses a carrier through its jittered top surface every few hundred
+    # steps at 2e7 carriers, which ends a run, as in the reference)
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="inplane_gradient",
@@ -488,6 +491,8 @@ def main():
     ap.add_argument("--kappa-steps", type=int, default=2000,
                     help="in-plane gradient: steps of the mixed-vs-FP64 kappa comparison (0: skip)")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 100 if args.workload == "finfet_mesh" else 200
     if args.particles is None:
         args.particles = {"inplane_gradient": 5e7, "finfet_mesh": 2e7, "nonlinear_callaway_film": 1e7,
                           "bilayer_callaway": 1e8}.get(args.workload, 1e6)
